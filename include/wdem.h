@@ -1,0 +1,259 @@
+/*
+ * wdem.h -- C ABI of the GB300 DEM timestep engine (libwdem.so).
+ *
+ * One handle runs Woo's DEM timestep for one scene on one GPU.  It replaces the engine trio
+ *   Leapfrog(reset=True) -> InsertionSortCollider([Bo1_*_Aabb]) -> ContactLoop([Cg2_*],[Cp2_*],[Law2_*])
+ * that woo.utils.defaultEngines / DemField.minimalEngines return (py/utils.py:94-129 of woodem/woo).
+ *
+ * Conventions
+ *  - Plain C structs of pointers and counts.  The caller owns every host array; the library owns
+ *    all device memory and never keeps a pointer to a caller array after a call returns.
+ *  - Every function returns WDEM_OK (0) or a negative WDEM_ERR_* code; wdem_last_error() gives the
+ *    message.  No C++ exception crosses this boundary.
+ *  - A handle is not thread-safe.  It owns one CUDA stream; calls are serialised on it.
+ *  - Particle ids are indices 0..n-1 (Woo's Particle::id_t, src/dem/ParticleContainer.hpp:43).
+ *  - Vectors are stored xyz-interleaved (3 doubles per item), quaternions as (w,x,y,z).
+ *  - L6Geom.trsf is stored as its three columns (local x, y, z axes in global coordinates),
+ *    9 doubles per contact: col0.xyz, col1.xyz, col2.xyz.
+ */
+#ifndef WDEM_H
+#define WDEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WDEM_ABI_VERSION 1
+
+/* ---- error codes ---------------------------------------------------------------------------- */
+enum {
+  WDEM_OK = 0,
+  WDEM_ERR_ARG = -1,           /* invalid argument (null pointer, bad size, unknown enum) */
+  WDEM_ERR_CUDA = -2,          /* a CUDA runtime call failed */
+  WDEM_ERR_NAN = -3,           /* NaN force in a contact (Woo: IdealElPl.cpp:79-83 throws) */
+  WDEM_ERR_OVERFLOW = -4,      /* a device table ran out of capacity and could not be regrown */
+  WDEM_ERR_UNSUPPORTED = -5,   /* a functor/attribute combination the GPU engine does not implement */
+  WDEM_ERR_NO_PHYS = -6,       /* no Cp2 functor for a material pair (Woo: ContactLoop.cpp:181) */
+  WDEM_ERR_TOO_BIG = -7,       /* particle larger than half the periodic cell (Woo: InsertionSortCollider.cpp:286-290) */
+  WDEM_ERR_TIMEOUT = -8,       /* a bounded device loop hit its iteration limit */
+  WDEM_ERR_STATE = -9,         /* call out of order (e.g. step before particles were uploaded) */
+  WDEM_ERR_NO_ALLOC = -10      /* reserved */
+};
+
+/* ---- enums mirroring Woo class names -------------------------------------------------------- */
+enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1 };
+enum { WDEM_MAT_FRICT = 0, WDEM_MAT_HERTZ = 1 };                 /* FrictMat, HertzMat */
+enum { WDEM_CP2_FRICT = 0, WDEM_CP2_HERTZ = 1 };                 /* Cp2_FrictMat_FrictPhys, Cp2_HertzMat_HertzPhys */
+enum { WDEM_LAW_IDEALELPL = 0, WDEM_LAW_HERTZ_DMT = 1 };         /* Law2_L6Geom_FrictPhys_IdealElPl, Law2_L6Geom_HertzPhys_DMT */
+enum { WDEM_UPDATE_PHYS_NEVER = 0, WDEM_UPDATE_PHYS_ALWAYS = 1, WDEM_UPDATE_PHYS_ONCE = 2 };
+
+/* DemData.flags bits (src/dem/Particle.hpp:197-200) */
+enum {
+  WDEM_DOF_X = 1, WDEM_DOF_Y = 2, WDEM_DOF_Z = 4, WDEM_DOF_RX = 8, WDEM_DOF_RY = 16, WDEM_DOF_RZ = 32,
+  WDEM_CLUMP_CLUMPED = 64, WDEM_CLUMP_CLUMP = 128, WDEM_ENERGY_SKIP = 256, WDEM_GRAVITY_SKIP = 512,
+  WDEM_TRACER_SKIP = 1024, WDEM_DAMPING_SKIP = 2048
+};
+
+/* Energy slots, in this order, returned by wdem_get_energy (names of EnergyTracker, src/core/EnergyTracker.cpp:26). */
+enum {
+  WDEM_E_KINETIC = 0, WDEM_E_GRAV = 1, WDEM_E_NONVISCDAMP = 2, WDEM_E_ELAST = 3, WDEM_E_PLAST = 4,
+  WDEM_E_VISCN = 5, WDEM_E_VISCT = 6, WDEM_E_BROKEN = 7, WDEM_E_COUNT = 8
+};
+
+/* ---- materials: FrictMat / HertzMat attributes (src/dem/FrictMat.hpp:6-28, src/dem/Hertz.hpp:5-14) */
+typedef struct wdem_material {
+  int32_t kind;          /* WDEM_MAT_* */
+  int32_t _pad;
+  double density;        /* Material.density */
+  double young;          /* ElastMat.young */
+  double ktDivKn;        /* FrictMat.ktDivKn */
+  double tanPhi;         /* FrictMat.tanPhi */
+  double surfEnergy;     /* HertzMat.surfEnergy */
+  double alpha;          /* HertzMat.alpha */
+} wdem_material;
+
+/* ---- engine + functor attributes -------------------------------------------------------------- */
+typedef struct wdem_params {
+  double dt;              /* Scene.dt (resolved; Scene.dtSafety*critDt when Woo's dt is NaN) */
+  int64_t step;           /* Scene.step at the start of the next wdem_step */
+  double gravity[3];      /* DemField.gravity */
+  double distFactor;      /* DemField.distFactor (negative = 1) */
+  uint32_t loneMask;      /* DemField.loneMask */
+  int32_t trackEnergy;    /* Scene.trackEnergy */
+  /* Leapfrog (src/dem/Leapfrog.hpp:42-61) */
+  double damping;
+  int32_t reset;          /* must be 1 (ForceResetter folded in) */
+  int32_t kinSplit;
+  /* InsertionSortCollider / AabbCollider */
+  double verletDist;      /* absolute; a negative value means |verletDist| x min sphere radius (Collision.cpp:164-184) */
+  /* Cg2_Any_Any_L6Geom__Base (src/dem/L6Geom.hpp:28-49) */
+  int32_t noRatch;
+  int32_t iniLensTouch;
+  int32_t trsfRenorm;
+  int32_t approxMask;
+  /* ContactLoop (src/dem/ContactLoop.hpp:110-130) */
+  int32_t updatePhys;     /* WDEM_UPDATE_PHYS_* */
+  int32_t applyForces;
+  int32_t dist00;
+  /* Cp2 */
+  int32_t cp2;            /* WDEM_CP2_* */
+  double poisson;         /* Cp2_HertzMat_HertzPhys.poisson */
+  double en;              /* Cp2_HertzMat_HertzPhys.en */
+  /* Law2 */
+  int32_t law;            /* WDEM_LAW_* */
+  int32_t noSlip, noBreak, noFrict, iniEqlb;
+  double relRollStiff, relTwistStiff, rollTanPhi;
+  int32_t noAttraction;   /* Law2_L6Geom_HertzPhys_DMT.noAttraction */
+  int32_t _pad;
+  /* materials table */
+  int32_t nMaterials;
+  int32_t _pad2;
+  const wdem_material* materials;
+} wdem_params;
+
+/* ---- particle state, SoA; all arrays have n (or 3n / 4n) items --------------------------------- */
+typedef struct wdem_particles {
+  int32_t n;
+  int32_t _pad;
+  int32_t* shape;         /* WDEM_SHAPE_* */
+  double* radius;         /* Sphere.radius (unused for walls) */
+  int32_t* wallAxis;      /* Wall.axis (unused for spheres) */
+  int32_t* wallSense;     /* Wall.sense */
+  int32_t* material;      /* index into wdem_params.materials */
+  uint32_t* mask;         /* Particle.mask */
+  uint32_t* flags;        /* DemData.flags */
+  double* mass;           /* DemData.mass */
+  double* inertia;        /* 3n DemData.inertia */
+  double* pos;            /* 3n Node.pos */
+  double* ori;            /* 4n Node.ori (w,x,y,z) */
+  double* vel;            /* 3n DemData.vel */
+  double* angVel;         /* 3n DemData.angVel */
+  double* force;          /* 3n DemData.force */
+  double* torque;         /* 3n DemData.torque */
+} wdem_particles;
+
+/* ---- contact state, SoA; n contacts ---------------------------------------------------------- */
+typedef struct wdem_contacts {
+  int64_t n;
+  int32_t* idA;           /* Contact.pA id */
+  int32_t* idB;           /* Contact.pB id */
+  int32_t* real;          /* Contact.isReal(): geom && phys */
+  int32_t* stepCreated;   /* Contact.stepCreated */
+  double* minDist00Sq;    /* Contact.minDist00Sq */
+  double* trsf;           /* 9n L6Geom.trsf columns */
+  double* contPt;         /* 3n L6Geom.node.pos */
+  double* geomOri;        /* 4n L6Geom.node.ori, download only */
+  double* geomVel;        /* 3n L6Geom.vel, download only */
+  double* geomAngVel;     /* 3n L6Geom.angVel, download only */
+  double* uN;             /* L6Geom.uN, download only */
+  double* force;          /* 3n CPhys.force (local) */
+  double* torque;         /* 3n CPhys.torque (local) */
+  double* kn;             /* FrictPhys.kn */
+  double* kt;             /* FrictPhys.kt */
+  double* tanPhi;         /* FrictPhys.tanPhi */
+} wdem_contacts;
+
+/* ---- status ----------------------------------------------------------------------------------- */
+typedef struct wdem_status {
+  int32_t code;            /* first error seen on the device, or WDEM_OK */
+  int32_t detail;          /* e.g. particle id of a NaN or oversized particle */
+  int64_t step;            /* Scene.step after the last wdem_step */
+  int64_t nContacts;       /* contacts in the container (real + potential) */
+  int64_t nReal;           /* real contacts */
+  int64_t nFullRuns;       /* collider rebuilds since creation (InsertionSortCollider.nFullRuns) */
+  int64_t capacity;        /* current contact capacity */
+  int32_t lastRunFull;     /* 1 if the last step rebuilt the collider */
+  int32_t _pad;
+} wdem_status;
+
+typedef struct wdem_handle wdem_handle;
+
+/* Library ABI version (WDEM_ABI_VERSION). */
+int wdem_abi_version(void);
+
+/* Create a handle for up to maxParticles particles on CUDA device `device`.
+ * Replaces constructing Leapfrog + InsertionSortCollider + ContactLoop and appending them to
+ * Scene.engines (py/utils.py:122-129; engine base src/core/Engine.hpp:19-104). */
+int wdem_create(int device, int32_t maxParticles, wdem_handle** out);
+
+/* Release all device memory and the stream. */
+int wdem_destroy(wdem_handle* h);
+
+/* Set engine/functor attributes (Leapfrog, InsertionSortCollider, ContactLoop, Cg2/Cp2/Law2 attrs,
+ * DemField.gravity/distFactor/loneMask, Scene.dt/step).  Mirrors setting those attributes from
+ * Python (src/dem/ContactLoop.cpp:52-66 functor lists; attrs in the *.hpp CLASS_BASE_DOC_ATTRS). */
+int wdem_set_params(wdem_handle* h, const wdem_params* p);
+
+/* Upload particle state.  Marks the contact container dirty, so the next step rebuilds the
+ * collider from scratch, as after ContactContainer.clear() / prologue_doFullRun
+ * (src/dem/InsertionSortCollider.cpp:360-384). */
+int wdem_upload_particles(wdem_handle* h, const wdem_particles* p);
+
+/* Upload the contact container (real contacts with their L6Geom/FrictPhys history and potential
+ * contacts).  Replaces ContactContainer::add for each contact (src/dem/ContactContainer.cpp:18-38). */
+int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c);
+
+/* Run nSteps steps of Leapfrog -> collider -> ContactLoop; replaces Scene::doOneStep's engine loop
+ * (src/core/Scene.cpp:420-427) for the three engines.  Scene.step advances by nSteps. */
+int wdem_step(wdem_handle* h, int32_t nSteps);
+
+/* Download particle state (pos, ori, vel, angVel, force, torque; the other arrays may be null).
+ * force/torque are DemData.force/torque as Woo has them after ContactLoop: m*g + contact forces. */
+int wdem_download_particles(wdem_handle* h, wdem_particles* p);
+
+/* Number of contacts in the container (real + potential), as len(S.dem.con). */
+int wdem_contact_count(wdem_handle* h, int64_t* n);
+
+/* Download the contact container; c->n must be >= wdem_contact_count.  Contacts come sorted by
+ * (min id, max id).  Null arrays are skipped. */
+int wdem_download_contacts(wdem_handle* h, wdem_contacts* c);
+
+/* Critical timestep of the field, DemFuncs::pWaveDt (src/dem/Funcs.cpp:151-175), via DemField::critDt
+ * (src/dem/Particle.cpp:399-404): min over spheres of r/sqrt(E/rho). */
+int wdem_crit_dt(wdem_handle* h, double* dt);
+
+/* Energies accumulated since the last reset, in WDEM_E_* order (EnergyTracker). */
+int wdem_get_energy(wdem_handle* h, double* e, int32_t n);
+int wdem_reset_energy(wdem_handle* h);
+
+/* Device status: the first error flagged by any kernel, counters.  Like Woo's exceptions surfacing
+ * as RuntimeError after the engine run (src/core/Scene.cpp:91-118). */
+int wdem_get_status(wdem_handle* h, wdem_status* s);
+
+/* Message of the last error on this handle (valid until the next call). */
+const char* wdem_last_error(wdem_handle* h);
+
+/* Collider alone: compute the candidate pair set for the given axis-aligned boxes, as
+ * InsertionSortCollider's initial sort + sweep does (src/dem/InsertionSortCollider.cpp:536-605)
+ * with the closed-interval test spatialOverlap (:67-73) and Collider::mayCollide
+ * (src/dem/Collision.cpp:21-43).  Boxes may hold +-inf (walls).  Pairs are written as
+ * (min id, max id), sorted; *nPairs gets the count; at most maxPairs are written. */
+int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const double* maxs,
+                       const uint32_t* mask, uint32_t loneMask,
+                       int32_t* pairs, int64_t maxPairs, int64_t* nPairs);
+
+/* Per-kernel device time of the last wdem_step call, in milliseconds, summed over its steps.
+ * names[i] (static strings) and ms[i], up to n entries; *count gets the number of entries. */
+int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* launches, int32_t n, int32_t* count);
+
+/* Enable/disable per-kernel CUDA-event timing inside wdem_step (off by default). */
+int wdem_set_timing(wdem_handle* h, int32_t enable);
+
+/* Keep L6Geom.uN, L6Geom.vel and L6Geom.angVel of every real contact so that
+ * wdem_download_contacts can return them (off by default: they are per-step values that Woo keeps
+ * in the contact's CGeom object; storing them costs 56 bytes per contact per step). */
+int wdem_keep_geom(wdem_handle* h, int32_t enable);
+
+/* Seeded random sequential addition of n non-overlapping spheres, radii uniform in [rMin, rMax],
+ * inside the box [lo, hi]: the synthetic-input counterpart of Woo's SpherePack::makeCloud
+ * (src/supp/sphere-pack/SpherePack.cpp:140-).  Host only, no GPU needed.  Returns the number placed
+ * (<= n; largest radii first) or a negative WDEM_ERR_*. */
+int64_t wdem_make_cloud(const double* lo, const double* hi, double rMin, double rMax, int64_t n, uint64_t seed,
+                        int32_t maxAttempts, double* centers, double* radii);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WDEM_H */

@@ -1,0 +1,156 @@
+"""ctypes bridge to the CPU oracle (oracle/woo_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg, as the checker of the GPU engine.  It reuses the wdem.h struct layouts of woo_gb300.abi so that
+both sides receive byte-identical inputs.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from woo_gb300 import abi
+from oracle import build as _build
+
+_lib = {}
+
+
+def load(variant="liborc.so"):
+    if variant in _lib:
+        return _lib[variant]
+    libs = _build.build()
+    lib = C.CDLL(libs[variant])
+    h = C.c_void_p
+    sig = {
+        "orc_create": ([], h),
+        "orc_destroy": ([h], None),
+        "orc_last_error": ([h], C.c_char_p),
+        "orc_set_params": ([h, C.POINTER(abi.Params)], C.c_int),
+        "orc_set_mode": ([h, C.c_int, C.c_int, C.c_int], C.c_int),
+        "orc_upload_particles": ([h, C.POINTER(abi.Particles)], C.c_int),
+        "orc_upload_contacts": ([h, C.POINTER(abi.Contacts)], C.c_int),
+        "orc_step": ([h, C.c_int], C.c_int),
+        "orc_step_timed": ([h, C.c_int], C.c_double),
+        "orc_download_particles": ([h, C.POINTER(abi.Particles)], C.c_int),
+        "orc_contact_count": ([h], C.c_long),
+        "orc_download_contacts": ([h, C.POINTER(abi.Contacts)], C.c_int),
+        "orc_crit_dt": ([h], C.c_double),
+        "orc_get_energy": ([h, C.POINTER(C.c_double), C.c_int], C.c_int),
+        "orc_reset_energy": ([h], C.c_int),
+        "orc_nfullruns": ([h], C.c_long),
+        "orc_verlet_dist": ([h], C.c_double),
+        "orc_step_count": ([h], C.c_long),
+        "orc_set_update_phys": ([h, C.c_int], C.c_int),
+        "orc_set_young": ([h, C.c_int, C.c_double], C.c_int),
+        "orc_collide_boxes": ([C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, C.c_int, abi.I32, C.c_long], C.c_long),
+        "orc_collide_frames": ([C.c_int, C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, abi.I32, C.c_long], C.c_long),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib[variant] = lib
+    return lib
+
+
+class Oracle:
+    """One CPU restatement of Woo's DEM scene (Leapfrog, InsertionSortCollider, ContactLoop)."""
+
+    def __init__(self, params, particles, contacts=None, canonical=True, sort_axis=0, variant="liborc.so"):
+        self.lib = load(variant)
+        self.h = self.lib.orc_create()
+        self._params = params
+        self.lib.orc_set_mode(self.h, 1 if canonical else 0, 1 if canonical else 0, sort_axis)
+        self.check(self.lib.orc_set_params(self.h, C.byref(params)))
+        s = particles.struct()
+        self.check(self.lib.orc_upload_particles(self.h, C.byref(s)))
+        self.check(self.lib.orc_set_params(self.h, C.byref(params)))
+        if contacts is not None:
+            cs = contacts.struct()
+            self.check(self.lib.orc_upload_contacts(self.h, C.byref(cs)))
+        self.n = particles.n
+
+    def check(self, rc):
+        if rc != 0:
+            raise RuntimeError("oracle: " + (self.lib.orc_last_error(self.h) or b"").decode())
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_destroy(self.h)
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        self.check(self.lib.orc_step(self.h, int(n)))
+
+    def step_timed(self, n):
+        t = self.lib.orc_step_timed(self.h, int(n))
+        if t < 0:
+            self.check(-1)
+        return t
+
+    def particles(self):
+        pa = abi.ParticleArrays(self.n)
+        s = pa.struct()
+        self.lib.orc_download_particles(self.h, C.byref(s))
+        return pa
+
+    def contacts(self):
+        ca = abi.ContactArrays(self.lib.orc_contact_count(self.h))
+        s = ca.struct()
+        self.lib.orc_download_contacts(self.h, C.byref(s))
+        return ca
+
+    def crit_dt(self):
+        return self.lib.orc_crit_dt(self.h)
+
+    def energy(self):
+        e = (C.c_double * 8)()
+        self.lib.orc_get_energy(self.h, e, 8)
+        return dict(zip(abi.ENERGY_NAMES, list(e)))
+
+    def reset_energy(self):
+        self.lib.orc_reset_energy(self.h)
+
+    def n_full_runs(self):
+        return self.lib.orc_nfullruns(self.h)
+
+    def verlet_dist(self):
+        return self.lib.orc_verlet_dist(self.h)
+
+    def set_update_phys(self, up):
+        self.lib.orc_set_update_phys(self.h, up)
+
+    def set_young(self, mat, young):
+        self.lib.orc_set_young(self.h, mat, young)
+
+
+def collide_boxes(mins, maxs, mask, lone_mask, sort_axis=0):
+    """InsertionSortCollider initial sort + sweep over the given boxes; returns sorted (min,max) pairs."""
+    lib = load()
+    mins = np.ascontiguousarray(mins, np.float64)
+    maxs = np.ascontiguousarray(maxs, np.float64)
+    mask = np.ascontiguousarray(mask, np.uint32)
+    n = len(mins)
+    cnt = lib.orc_collide_boxes(n, abi.ptr(mins, C.c_double), abi.ptr(maxs, C.c_double), abi.ptr(mask, C.c_uint32),
+                                lone_mask, sort_axis, None, 0)
+    pairs = np.zeros((max(cnt, 1), 2), np.int32)
+    lib.orc_collide_boxes(n, abi.ptr(mins, C.c_double), abi.ptr(maxs, C.c_double), abi.ptr(mask, C.c_uint32),
+                          lone_mask, sort_axis, abi.ptr(pairs, C.c_int32), cnt)
+    return pairs[:cnt]
+
+
+def collide_frames(mins, maxs, mask, lone_mask):
+    """Insertion-sort collider run over successive box sets (frames x n x 3); pairs after the last."""
+    lib = load()
+    mins = np.ascontiguousarray(mins, np.float64)
+    maxs = np.ascontiguousarray(maxs, np.float64)
+    mask = np.ascontiguousarray(mask, np.uint32)
+    nf, n = mins.shape[0], mins.shape[1]
+    cnt = lib.orc_collide_frames(n, nf, abi.ptr(mins, C.c_double), abi.ptr(maxs, C.c_double),
+                                 abi.ptr(mask, C.c_uint32), lone_mask, None, 0)
+    pairs = np.zeros((max(cnt, 1), 2), np.int32)
+    lib.orc_collide_frames(n, nf, abi.ptr(mins, C.c_double), abi.ptr(maxs, C.c_double), abi.ptr(mask, C.c_uint32),
+                           lone_mask, abi.ptr(pairs, C.c_int32), cnt)
+    return pairs[:cnt]

@@ -1,0 +1,1171 @@
+/*
+ * woo_oracle.cpp -- CPU ORACLE for the GB300 DEM engine.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain C++17 restatement of woodem/woo's DEM timestep (Leapfrog -> InsertionSortCollider ->
+ * ContactLoop), written from the reference sources cited at each function.  It is the checker for
+ * the CUDA engine: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
+ * The product library (libwdem.so) never links or calls it.
+ *
+ * Build: oracle/build.sh (g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared [-fopenmp]).
+ * -ffp-contract=off keeps every a*b+c as two IEEE operations, as the reference's x86-64 build does.
+ *
+ * Pinning: Woo cannot be compiled here (Eigen3 and Boost are absent), so this restatement is pinned
+ * by the reference's own known-answer tests re-stated in tests/test_oracle_known_answers.py
+ * (py/tests/test_hertz.py:30-47 collision time, py/tests/test_demfield.py:24-51 updatePhys,
+ * py/tests/test_energy.py gravity/damping skips) and by analytic cases.
+ *
+ * Third-party arithmetic restated here: Eigen3 (unpinned version; Ubuntu 20.04 libeigen3-dev in the
+ * reference CI): cross/dot/norm/normalize, 3x3 matrix-vector, Quaternion(Matrix3) (Shoemake's
+ * trace/largest-diagonal method), quaternion*vector (v + 2w(q x v) + q x (2 q x v)), quaternion
+ * product, AngleAxis -> Quaternion (cos(a/2), sin(a/2) axis).  Each is written from the published
+ * formula; evaluation order follows Eigen's left-to-right expression evaluation.
+ *
+ * Two switches make the oracle reproduce the GPU engine's documented conventions exactly:
+ *   canonicalOrient: a new contact between two particles of the same shape gets pA = lower id
+ *     (the reference takes the order in which the insertion sort met the pair, an artefact of the
+ *     sort; InsertionSortCollider.cpp:102, :579).
+ *   applyOrder: 0 = forces added in container order (ContactLoop.cpp:195-197 / :257-264),
+ *     1 = added per contact sorted by (min id, max id), the GPU's CSR order.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include <chrono>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/wdem.h"
+
+namespace orc {
+
+static const double Inf = std::numeric_limits<double>::infinity();
+static const double NaN = std::numeric_limits<double>::quiet_NaN();
+
+/* ------------------------------------------------------------------ small linear algebra */
+struct V3 {
+  double x = 0, y = 0, z = 0;
+  V3() {}
+  V3(double a, double b, double c) : x(a), y(b), z(c) {}
+  double& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+static inline V3 operator+(const V3& a, const V3& b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline V3 operator-(const V3& a, const V3& b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline V3 operator-(const V3& a) { return V3(-a.x, -a.y, -a.z); }
+static inline V3 operator*(const V3& a, double s) { return V3(a.x * s, a.y * s, a.z * s); }
+static inline V3 operator*(double s, const V3& a) { return V3(s * a.x, s * a.y, s * a.z); }
+static inline V3 operator/(const V3& a, double s) { return V3(a.x / s, a.y / s, a.z / s); }
+static inline bool isZero(const V3& a) { return a.x == 0 && a.y == 0 && a.z == 0; }
+/* Eigen redux on a fixed size-3 vector: (a0*b0 + a1*b1) + a2*b2 */
+static inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline double sqnorm(const V3& a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+static inline double norm(const V3& a) { return std::sqrt(sqnorm(a)); }
+static inline V3 cross(const V3& a, const V3& b) {
+  return V3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+/* Eigen normalize(): divide by sqrt(squaredNorm) when it is positive */
+static inline void normalize(V3& a) {
+  double z = sqnorm(a);
+  if (z > 0) { double n = std::sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
+}
+static inline double absmax(const V3& a) { return std::max(a.x, std::max(a.y, a.z)); }
+
+/* 3x3 matrix stored by columns: c[0], c[1], c[2] */
+struct M3 {
+  V3 c[3];
+  double operator()(int r, int k) const { return c[k][r]; }
+};
+/* M^T v: component i is column i dotted with v */
+static inline V3 mulT(const M3& m, const V3& v) { return V3(dot(m.c[0], v), dot(m.c[1], v), dot(m.c[2], v)); }
+
+struct Quat {
+  double w = 1, x = 0, y = 0, z = 0;
+  Quat() {}
+  Quat(double w_, double x_, double y_, double z_) : w(w_), x(x_), y(y_), z(z_) {}
+};
+/* Hamilton product, written term by term as in Eigen's generic quat_product */
+static inline Quat qmul(const Quat& a, const Quat& b) {
+  return Quat(a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z,
+              a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y,
+              a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z,
+              a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x);
+}
+/* rotate v by unit quaternion q: uv = 2 (q.vec x v); v + w uv + q.vec x uv */
+static inline V3 qrot(const Quat& q, const V3& v) {
+  V3 qv(q.x, q.y, q.z);
+  V3 uv = cross(qv, v);
+  uv = uv + uv;
+  return v + q.w * uv + cross(qv, uv);
+}
+static inline void qnormalize(Quat& q) {
+  /* coefficients stored (x,y,z,w): ((x^2+y^2)+z^2)+w^2 */
+  double z2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+  if (z2 > 0) { double n = std::sqrt(z2); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+}
+static inline Quat qconj(const Quat& q) { return Quat(q.w, -q.x, -q.y, -q.z); }
+/* rotation matrix -> quaternion, Shoemake's method (trace branch, else largest diagonal) */
+static Quat quatFromMatrix(const M3& m) {
+  Quat q;
+  double t = m(0, 0) + m(1, 1) + m(2, 2);
+  if (t > 0) {
+    t = std::sqrt(t + 1.0);
+    q.w = 0.5 * t;
+    t = 0.5 / t;
+    q.x = (m(2, 1) - m(1, 2)) * t;
+    q.y = (m(0, 2) - m(2, 0)) * t;
+    q.z = (m(1, 0) - m(0, 1)) * t;
+  } else {
+    int i = 0;
+    if (m(1, 1) > m(0, 0)) i = 1;
+    if (m(2, 2) > m(i, i)) i = 2;
+    int j = (i + 1) % 3, k = (j + 1) % 3;
+    t = std::sqrt(m(i, i) - m(j, j) - m(k, k) + 1.0);
+    double v[3];
+    v[i] = 0.5 * t;
+    t = 0.5 / t;
+    q.w = (m(k, j) - m(j, k)) * t;
+    v[j] = (m(j, i) + m(i, j)) * t;
+    v[k] = (m(k, i) + m(i, k)) * t;
+    q.x = v[0]; q.y = v[1]; q.z = v[2];
+  }
+  return q;
+}
+static inline double pow2(double x) { return x * x; }
+/* Math::Sign (src/supp/base/Math.hpp:145) */
+static inline double Sign(double f) { if (f < 0) return -1; if (f > 0) return 1; return 0; }
+/* pown (src/supp/base/Math.hpp:166-175): x^n by squaring */
+static double pown(double x, unsigned n) {
+  unsigned d = n >> 1, r = n & 1;
+  double x2d = d == 0 ? 1 : pown(x * x, d);
+  double xr = r == 0 ? 1 : x;
+  return x2d * xr;
+}
+
+/* ------------------------------------------------------------------ model */
+struct Aabb {
+  bool has = false;
+  V3 min, max;
+  V3 nodeLastPos;
+  double maxD2 = 0;
+};
+
+struct Particle {
+  int id = 0;
+  int shape = WDEM_SHAPE_SPHERE;
+  double radius = NaN;
+  int axis = 0, sense = 0;
+  int mat = 0;
+  unsigned mask = 1;
+  unsigned flags = 0;
+  double mass = 0;
+  V3 inertia;
+  V3 pos, vel, angVel, force, torque;
+  Quat ori;
+  Aabb bound;
+  std::map<int, std::shared_ptr<struct Contact>> contacts; /* Particle::contacts (Particle.hpp:36) */
+  bool isBlockedNone() const { return (flags & 63u) == 0; }
+  bool isBlockedAll() const { return (flags & 63u) == 63u; }
+  bool isBlockedAllRot() const { return (flags & 56u) == 56u; }
+  bool isBlockedAxisDOF(int ax, bool rot) const { return flags & (1u << (ax + (rot ? 3 : 0))); }
+  bool isAspherical() const { return !(inertia.x == inertia.y && inertia.y == inertia.z); }
+};
+
+struct Contact {
+  int pA = -1, pB = -1;
+  bool geom = false, phys = false;
+  int stepCreated = -1;
+  double minDist00Sq = -1;
+  size_t linIx = 0;
+  /* L6Geom (src/dem/L6Geom.hpp:14-22) */
+  V3 gvel, gangVel;
+  double uN = NaN;
+  double lens[2] = {0, 0};
+  double contA = NaN;
+  M3 trsf;
+  V3 contPt;
+  Quat gori;
+  /* FrictPhys / HertzPhys (FrictMat.hpp:30-41, Hertz.hpp:16-31) */
+  V3 force, torque;
+  double kn = NaN, kt = NaN, tanPhi = NaN;
+  double kt0 = 0, alpha_sqrtMK = 0, R = 0, K = 0, gamma = 0, alpha = 0, contRad = 0;
+  bool isReal() const { return geom && phys; }
+  bool isColliding() const { return stepCreated >= 0; }
+  Contact() {
+    trsf.c[0] = V3(1, 0, 0); trsf.c[1] = V3(0, 1, 0); trsf.c[2] = V3(0, 0, 1);
+  }
+};
+typedef std::shared_ptr<Contact> CPtr;
+
+struct Energy {
+  double v[WDEM_E_COUNT] = {0};
+  bool resettable[WDEM_E_COUNT] = {true, false, false, true, false, false, false, false};
+  void resetResettables() { for (int i = 0; i < WDEM_E_COUNT; i++) if (resettable[i]) v[i] = 0; }
+};
+
+struct Bounds {
+  double coord = 0;
+  int id = 0;
+  bool hasBB = false, isMin = false;
+  Bounds() {}
+  Bounds(double c, int i, bool mn) : coord(c), id(i), hasBB(false), isMin(mn) {}
+  /* InsertionSortCollider.hpp:132-140 */
+  bool operator<(const Bounds& b) const {
+    if (id == b.id && coord == b.coord) return isMin;
+    return coord < b.coord;
+  }
+  bool operator>(const Bounds& b) const {
+    if (id == b.id && coord == b.coord) return !isMin;
+    return coord > b.coord;
+  }
+};
+
+struct Scene {
+  /* Scene + DemField + engine attributes */
+  wdem_params P;
+  std::vector<wdem_material> mats;
+  long step = 0;
+  double time = 0;
+  std::vector<Particle> par;
+  /* ContactContainer */
+  std::vector<CPtr> linView;
+  std::vector<std::pair<CPtr, bool>> pending;
+  bool dirty = true;
+  /* InsertionSortCollider */
+  std::vector<Bounds> BB[3];
+  std::vector<double> minima, maxima;
+  std::vector<CPtr> makeContacts, removeContacts;
+  double verletDist = -0.05;  /* resolved on first run */
+  long nFullRuns = 0;
+  int sortAxis = 0;
+  /* options */
+  int canonicalOrient = 0;
+  int applyOrder = 0;
+  int updatePhys = 0;
+  Energy E;
+  std::string err;
+  int lastRunFull = 0;
+};
+
+/* ------------------------------------------------------------------ ContactContainer */
+/* ContactContainer::addMaybe_fast (ContactContainer.cpp:51-58) */
+static void addMaybe_fast(Scene& S, const CPtr& c) {
+  Particle& A = S.par[c->pA];
+  Particle& B = S.par[c->pB];
+  if (A.contacts.count(B.id) == 1) return;
+  A.contacts[B.id] = c;
+  B.contacts[A.id] = c;
+  S.linView.push_back(c);
+  c->linIx = S.linView.size() - 1;
+}
+/* ContactContainer::linView_remove (ContactContainer.cpp:69-80) */
+static void linView_remove(Scene& S, size_t ix) {
+  if (ix < S.linView.size() - 1) {
+    S.linView[ix] = S.linView.back();
+    S.linView[ix]->linIx = ix;
+  }
+  S.linView.resize(S.linView.size() - 1);
+}
+/* ContactContainer::removeMaybe_fast (ContactContainer.cpp:60-67) */
+static void removeMaybe_fast(Scene& S, const CPtr& c) {
+  Particle& A = S.par[c->pA];
+  Particle& B = S.par[c->pB];
+  auto iA = A.contacts.find(B.id);
+  if (iA == A.contacts.end()) return;
+  A.contacts.erase(iA);
+  B.contacts.erase(B.contacts.find(A.id));
+  linView_remove(S, c->linIx);
+}
+/* ContactContainer::remove (ContactContainer.cpp:82-137), particles never vanish here */
+static bool removeContact(Scene& S, const CPtr& c) {
+  Particle& A = S.par[c->pA];
+  Particle& B = S.par[c->pB];
+  auto iA = A.contacts.find(B.id);
+  if (iA == A.contacts.end()) return false;
+  A.contacts.erase(iA);
+  auto iB = B.contacts.find(A.id);
+  if (iB != B.contacts.end()) B.contacts.erase(iB);
+  linView_remove(S, c->linIx);
+  return true;
+}
+static CPtr findContact(Scene& S, int a, int b) {
+  auto I = S.par[a].contacts.find(b);
+  if (I == S.par[a].contacts.end()) return CPtr();
+  return I->second;
+}
+/* ContactContainer::requestRemoval (ContactContainer.cpp:164-174) + Contact::reset (Contact.cpp:141-145) */
+static void requestRemoval(Scene& S, const CPtr& c, bool force = false) {
+  c->geom = false; c->phys = false;
+  /* Contact::reset drops the CGeom/CPhys objects: a new contact later starts from default values */
+  Contact fresh;
+  c->gvel = fresh.gvel; c->gangVel = fresh.gangVel; c->uN = fresh.uN; c->lens[0] = c->lens[1] = 0; c->contA = NaN;
+  c->trsf = fresh.trsf; c->contPt = V3(); c->gori = Quat();
+  c->force = V3(); c->torque = V3(); c->kn = c->kt = c->tanPhi = NaN;
+  c->kt0 = c->alpha_sqrtMK = c->R = c->K = c->gamma = c->alpha = c->contRad = 0;
+  S.pending.push_back(std::make_pair(c, force));
+}
+
+/* ------------------------------------------------------------------ collider */
+/* Collider::mayCollide (Collision.cpp:21-43); no shared nodes and no clumps in this model */
+static bool mayCollide(const Scene& S, const Particle& A, const Particle& B) {
+  if (A.id == B.id) return false;
+  if (!(A.mask & B.mask)) return false;
+  if ((A.mask & B.mask & S.P.loneMask) != 0) return false;
+  return true;
+}
+/* InsertionSortCollider::spatialOverlap (InsertionSortCollider.cpp:67-73) */
+static bool spatialOverlap(const Scene& S, int id1, int id2) {
+  const double* mn = S.minima.data();
+  const double* mx = S.maxima.data();
+  return (mn[3 * id1 + 0] <= mx[3 * id2 + 0]) && (mx[3 * id1 + 0] >= mn[3 * id2 + 0]) &&
+         (mn[3 * id1 + 1] <= mx[3 * id2 + 1]) && (mx[3 * id1 + 1] >= mn[3 * id2 + 1]) &&
+         (mn[3 * id1 + 2] <= mx[3 * id2 + 2]) && (mx[3 * id1 + 2] >= mn[3 * id2 + 2]);
+}
+/* makeContactLater (InsertionSortCollider.hpp:106-113) */
+static void makeContactLater(Scene& S, int a, int b) {
+  CPtr C = std::make_shared<Contact>();
+  if (S.canonicalOrient && S.par[a].shape == S.par[b].shape && a > b) std::swap(a, b);
+  C->pA = a; C->pB = b; C->stepCreated = (int)S.step;
+  S.makeContacts.push_back(C);
+}
+/* handleBoundInversion (InsertionSortCollider.cpp:78-113) */
+static void handleBoundInversion(Scene& S, int id1, int id2, bool separating) {
+  bool overlap = separating ? false : spatialOverlap(S, id1, id2);
+  CPtr C = findContact(S, id1, id2);
+  bool hasCon = (bool)C;
+  if (!overlap && !hasCon) return;
+  if (overlap && hasCon) return;
+  if (overlap) {
+    if (!mayCollide(S, S.par[id1], S.par[id2])) return;
+    makeContactLater(S, id1, id2);
+    return;
+  }
+  if (!C->isReal()) S.removeContacts.push_back(C);
+}
+/* insertionSort_part, serial form (InsertionSortCollider.cpp:189-223) */
+static void insertionSort(Scene& S, std::vector<Bounds>& v, bool doCollide) {
+  long n = (long)v.size();
+  for (long i = 1; i < n; i++) {
+    if (!(v[i - 1] > v[i])) continue;
+    const Bounds viInit = v[i];
+    long j = i - 1;
+    const bool viInitBB = viInit.hasBB, viInitIsMin = viInit.isMin;
+    while (j >= 0 && v[j] > viInit) {
+      v[j + 1] = v[j];
+      if (viInitIsMin != v[j].isMin && doCollide && viInitBB && v[j].hasBB && viInit.id != v[j].id)
+        handleBoundInversion(S, viInit.id, v[j].id, !viInitIsMin);
+      j--;
+    }
+    v[j + 1] = viInit;
+  }
+}
+/* Bo1_Sphere_Aabb::go (Sphere.cpp:52-64), Bo1_Wall_Aabb::go (Wall.cpp:25-38), then the verlet
+ * enlargement of AabbCollider::updateAabb (Collision.cpp:125-162) */
+static void updateAabb(Scene& S, Particle& p) {
+  Aabb& a = p.bound;
+  a.has = true;
+  if (p.shape == WDEM_SHAPE_SPHERE) {
+    double df = S.P.distFactor;
+    double h = (df > 0 ? df : 1.) * p.radius;
+    V3 half(h, h, h);
+    a.min = p.pos - half;
+    a.max = p.pos + half;
+  } else {
+    a.min = V3(-Inf, -Inf, -Inf);
+    a.max = V3(Inf, Inf, Inf);
+    a.min[p.axis] = a.max[p.axis] = p.pos[p.axis];
+  }
+  a.nodeLastPos = p.pos;
+  a.maxD2 = pow2(S.verletDist);
+  if (S.verletDist > 0) {
+    V3 vd(S.verletDist, S.verletDist, S.verletDist);
+    a.max = a.max + vd;
+    a.min = a.min - vd;
+  }
+}
+/* AabbCollider::setVerletDist (Collision.cpp:164-184) */
+static void setVerletDist(Scene& S) {
+  if (S.verletDist >= 0) return;
+  double minR = Inf;
+  for (const Particle& p : S.par)
+    if (p.shape == WDEM_SHAPE_SPHERE && !std::isnan(p.radius)) minR = std::min(p.radius, minR);
+  if (!std::isinf(minR)) S.verletDist = std::abs(S.verletDist) * minR;
+  else S.verletDist = 0.0;
+}
+/* AabbCollider::aabbIsDirty (Collision.cpp:80-123), maxRot<0 for spheres and walls */
+static bool aabbIsDirty(const Particle& p) {
+  if (!p.bound.has) return true;
+  if (std::isnan(absmax(p.bound.min)) || std::isnan(absmax(p.bound.max))) return true;
+  double d2 = sqnorm(p.bound.nodeLastPos - p.pos);
+  return d2 > p.bound.maxD2;
+}
+/* InsertionSortCollider::run, aperiodic (InsertionSortCollider.cpp:386-613) */
+static void colliderRun(Scene& S) {
+  bool fullRun = false;
+  if (S.dirty) { fullRun = true; S.dirty = false; }
+  long nPar = (long)S.par.size();
+  if ((long)S.BB[0].size() != 2 * nPar) fullRun = true;
+  /* updateBboxes_doFullRun (:308-358) */
+  setVerletDist(S);
+  bool recompute = false;
+  if (S.verletDist == 0) recompute = true;
+  else for (const Particle& p : S.par) if (aabbIsDirty(p)) { recompute = true; break; }
+  if (recompute) for (Particle& p : S.par) updateAabb(S, p);
+  if (recompute) fullRun = true;
+  S.lastRunFull = fullRun;
+  if (!fullRun) {
+    /* removePending (ContactContainer.hpp:78-93) with shouldBeRemoved (InsertionSortCollider.hpp:213-218) */
+    auto pend = S.pending; S.pending.clear();
+    for (auto& pc : pend) if (pc.second || !spatialOverlap(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
+    return;
+  }
+  S.nFullRuns++;
+  bool doInitSort = false;
+  if ((long)S.BB[0].size() != 2 * nPar) {
+    for (int i = 0; i < 3; i++) S.BB[i].clear();
+    doInitSort = true;
+    for (int i = 0; i < 3; i++)
+      for (long id = 0; id < nPar; id++) {
+        S.BB[i].push_back(Bounds(0, (int)id, true));
+        S.BB[i].push_back(Bounds(0, (int)id, false));
+      }
+  }
+  S.minima.assign(3 * nPar, 0); S.maxima.assign(3 * nPar, 0);
+  /* copy bounds (:457-494) */
+  for (int j = 0; j < 3; j++)
+    for (Bounds& b : S.BB[j]) {
+      const Aabb& bv = S.par[b.id].bound;
+      b.hasBB = bv.has;
+      b.coord = b.hasBB ? (b.isMin ? bv.min[j] : bv.max[j]) : S.par[b.id].pos[j];
+    }
+  /* minima/maxima (:498-506) */
+  for (long id = 0; id < nPar; id++)
+    for (int k = 0; k < 3; k++) {
+      S.minima[3 * id + k] = S.par[id].bound.min[k];
+      S.maxima[3 * id + k] = S.par[id].bound.max[k];
+    }
+  /* removePending (:517) */
+  {
+    auto pend = S.pending; S.pending.clear();
+    for (auto& pc : pend) if (pc.second || !spatialOverlap(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
+  }
+  if (!doInitSort) {
+    for (int i = 0; i < 3; i++) insertionSort(S, S.BB[i], true);
+  } else {
+    for (int i = 0; i < 3; i++) std::sort(S.BB[i].begin(), S.BB[i].end());
+    std::vector<Bounds>& V = S.BB[S.sortAxis];
+    long n2 = 2 * nPar;
+    for (long i = 0; i < n2; i++) {
+      if (!(V[i].isMin && V[i].hasBB)) continue;
+      int iid = V[i].id;
+      for (long j = i + 1; j < n2 && V[j].id != iid; j++) {
+        if (!V[j].isMin) continue;
+        handleBoundInversion(S, iid, V[j].id, false);
+      }
+    }
+  }
+  /* makeRemoveContactLater_process (:35-63): removals first, then additions */
+  for (auto& C : S.removeContacts) removeMaybe_fast(S, C);
+  S.removeContacts.clear();
+  for (auto& C : S.makeContacts) addMaybe_fast(S, C);
+  S.makeContacts.clear();
+}
+
+/* ------------------------------------------------------------------ geometry */
+/* L6Geom::setInitialLocalCoords (L6Geom.cpp:25-36) */
+static void setInitialLocalCoords(Contact& C, const V3& locX) {
+  V3 e = std::abs(locX.y) < std::abs(locX.z) ? V3(0, 1, 0) : V3(0, 0, 1);
+  V3 locY = cross(locX, e);
+  locY = locY - locX * dot(locY, locX);
+  normalize(locY);
+  V3 locZ = cross(locX, locY);
+  C.trsf.c[0] = locX; C.trsf.c[1] = locY; C.trsf.c[2] = locZ;
+}
+/* Cg2_Any_Any_L6Geom__Base::handleSpheresLikeContact (L6Geom.cpp:49-216), L6_TRSF_QUATERNION undefined */
+static void handleSpheresLikeContact(Scene& S, Contact& C, const V3& pos1, const V3& vel1, const V3& angVel1,
+                                     const V3& pos2, const V3& vel2, const V3& angVel2, const V3& normal,
+                                     const V3& contPt, double uN, double r1, double r2) {
+  const wdem_params& P = S.P;
+  if (!C.geom) {
+    C.geom = true;
+    C.gvel = V3(); C.gangVel = V3();
+    setInitialLocalCoords(C, normal);
+    C.uN = uN;
+    if (P.iniLensTouch) { C.lens[0] = std::abs(r1); C.lens[1] = std::abs(r2); }
+    else { C.lens[0] = std::abs(r1) + uN / 2; C.lens[1] = std::abs(r2) + uN / 2; }
+    if (C.lens[0] < 0) C.lens[0] = C.lens[1];
+    if (C.lens[1] < 0) C.lens[1] = C.lens[0];
+    C.contA = M_PI * pow2((r1 > 0 && r2 > 0) ? std::min(r1, r2) : (r1 > 0 ? r1 : r2));
+    C.contPt = contPt;
+    C.gori = quatFromMatrix(C.trsf);
+    return;
+  }
+  const V3 currNormal = normal;
+  const V3 prevNormal = C.trsf.c[0];
+  const V3 prevContPt = C.contPt;
+  const double dt = P.dt;
+  V3 shiftVel2;  /* aperiodic */
+  V3 normRotVec = cross(prevNormal, currNormal);
+  V3 midNormal = (P.approxMask & 1) ? prevNormal : 0.5 * (prevNormal + currNormal);
+  if (norm(midNormal) == 0) midNormal = currNormal;
+  else if (!(P.approxMask & 2) && !(P.approxMask & 1)) normalize(midNormal);
+  V3 normTwistVec = midNormal * dt * 0.5 * dot(midNormal, angVel1 + angVel2);
+  const M3 prevTrsf = C.trsf;
+  M3 midTrsf;
+  if (P.approxMask & 4) { midTrsf.c[0] = prevNormal; midTrsf.c[1] = prevTrsf.c[1]; }
+  else { midTrsf.c[0] = midNormal; midTrsf.c[1] = prevTrsf.c[1] - cross(prevTrsf.c[1], normRotVec + normTwistVec) / 2.; }
+  midTrsf.c[2] = cross(midTrsf.c[0], midTrsf.c[1]);
+  M3 currTrsf;
+  currTrsf.c[0] = currNormal;
+  currTrsf.c[1] = prevTrsf.c[1] - cross(midTrsf.c[1], normRotVec + normTwistVec);
+  currTrsf.c[2] = cross(currTrsf.c[0], currTrsf.c[1]);
+  if (P.trsfRenorm > 0 && (S.step % P.trsfRenorm) == 0) {
+    normalize(currTrsf.c[0]);
+    currTrsf.c[1] = currTrsf.c[1] - currTrsf.c[0] * dot(currTrsf.c[1], currTrsf.c[0]);
+    normalize(currTrsf.c[1]);
+    currTrsf.c[2] = cross(currTrsf.c[0], currTrsf.c[1]);
+  }
+  V3 midContPt, midPos1, midPos2;
+  if (P.approxMask & 8) { midContPt = contPt; midPos1 = pos1; midPos2 = pos2; }
+  else { midContPt = 0.5 * (prevContPt + contPt); midPos1 = pos1 - (dt / 2.) * vel1; midPos2 = pos2 - (dt / 2.) * (vel2 + shiftVel2); }
+  V3 c1x = (P.noRatch && r1 > 0) ? r1 * midNormal : midContPt - midPos1;
+  V3 c2x = (P.noRatch && r2 > 0) ? -r2 * midNormal : midContPt - midPos2;
+  V3 relVel = (vel2 + shiftVel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
+  C.trsf = currTrsf;
+  C.gvel = mulT(midTrsf, relVel);
+  C.gangVel = mulT(midTrsf, angVel2 - angVel1);
+  C.uN = uN;
+  C.contPt = contPt;
+  C.gori = quatFromMatrix(C.trsf);
+}
+/* Cg2_Sphere_Sphere_L6Geom::go (Sphere.cpp:92-117) */
+static bool cg2SphereSphere(Scene& S, Contact& C, Particle& A, Particle& B, const V3& shift2, bool force) {
+  const double r1 = A.radius, r2 = B.radius;
+  const double distFactor = S.P.distFactor;
+  V3 relPos = B.pos + shift2 - A.pos;
+  double unDistSq = sqnorm(relPos) - pow2(std::abs(distFactor) * (r1 + r2));
+  if (unDistSq > 0 && !C.isReal() && !force) return false;
+  double dist = norm(relPos);
+  double uN = dist - (r1 + r2);
+  V3 normal = relPos / dist;
+  V3 contPt = A.pos + (r1 + 0.5 * uN) * normal;
+  handleSpheresLikeContact(S, C, A.pos, A.vel, A.angVel, B.pos + shift2, B.vel, B.angVel, normal, contPt, uN, r1, r2);
+  return true;
+}
+/* Cg2_Wall_Sphere_L6Geom::go (Wall.cpp:50-84) */
+static bool cg2WallSphere(Scene& S, Contact& C, Particle& W, Particle& Sp, const V3& shift2, bool force) {
+  const double radius = Sp.radius;
+  const int ax = W.axis, sense = W.sense;
+  const V3 wallPos = W.pos;
+  V3 spherePos = Sp.pos + shift2;
+  double dist = spherePos[ax] - wallPos[ax];
+  if (!C.isReal() && std::abs(dist) > radius && !force) return false;
+  V3 contPt = spherePos; contPt[ax] = wallPos[ax];
+  V3 normal;
+  if (sense == 0) {
+    if (!C.geom) normal[ax] = dist > 0 ? 1. : -1.;
+    else normal[ax] = C.trsf.c[0][ax];
+  } else normal[ax] = (sense == 1 ? 1. : -1);
+  double uN = normal[ax] * dist - radius;
+  handleSpheresLikeContact(S, C, wallPos, W.vel, W.angVel, spherePos, Sp.vel, Sp.angVel, normal, contPt, uN, -radius, radius);
+  return true;
+}
+
+/* ------------------------------------------------------------------ physics */
+/* Cp2_FrictMat_FrictPhys::updateFrictPhys (FrictMat.cpp:20-44), MatchMaker unset -> min tanPhi */
+static void cp2Frict(Scene& S, Contact& C, const wdem_material& m1, const wdem_material& m2) {
+  C.phys = true;
+  double l0 = C.lens[0], l1 = C.lens[1], A = C.contA;
+  C.kn = 1 / (1 / (m1.young * A / l0) + 1 / (m2.young * A / l1));
+  C.kt = .5 * (m1.ktDivKn + m2.ktDivKn) * C.kn;
+  C.tanPhi = std::min(m1.tanPhi, m2.tanPhi);
+}
+/* Cp2_HertzMat_HertzPhys::go (Hertz.cpp:34-77) */
+static void cp2Hertz(Scene& S, Contact& C, const wdem_material& m1, const wdem_material& m2) {
+  C.phys = true;
+  const double r1 = C.lens[0], r2 = C.lens[1];
+  const double E1 = m1.young, E2 = m2.young;
+  const double nu1 = S.P.poisson, nu2 = S.P.poisson;
+  C.K = (4 / 3.) * 1. / ((1 - nu1 * nu1) / E1 + (1 - nu2 * nu2) / E2);
+  C.R = 1. / (1. / r1 + 1. / r2);
+  double kn0 = C.K * std::sqrt(C.R);
+  C.gamma = std::min(m1.surfEnergy, m2.surfEnergy);
+  C.alpha = .5 * (m1.alpha + m2.alpha);
+  double G1 = E1 / (2 * (1 + nu1)); double G2 = E2 / (2 * (1 + nu2));
+  double G = .5 * (G1 + G2);
+  double nu = .5 * (nu1 + nu2);
+  C.kt0 = 2 * std::sqrt(4 * C.R) * G / (2 - nu);
+  C.tanPhi = std::min(m1.tanPhi, m2.tanPhi);
+  double en = S.P.en;
+  if (en > 0 && en < 1.) {
+    const double ma = S.par[C.pA].mass, mb = S.par[C.pB].mass;
+    double mbar = (ma <= 0 && mb > 0) ? mb : ((ma > 0 && mb <= 0) ? ma : (ma * mb) / (ma + mb));
+    double viscAlpha = -std::sqrt(5) * std::log(en) / (std::sqrt(pow2(std::log(en)) + pow2(M_PI)));
+    C.alpha_sqrtMK = std::max(0., viscAlpha * std::sqrt(mbar * kn0));
+  } else C.alpha_sqrtMK = 0.0;
+}
+/* Law2_L6Geom_FrictPhys_IdealElPl::go (IdealElPl.cpp:15-125), iniEqlb unsupported */
+static bool lawIdealElPl(Scene& S, Contact& C) {
+  const wdem_params& P = S.P;
+  double uN = C.uN;
+  if (uN > 0 && !P.noBreak) {
+    if (P.noSlip && P.trackEnergy) {
+      double Fn = C.kn * uN;
+      double ft0 = C.force.y + P.dt * C.kt * C.gvel.y, ft1 = C.force.z + P.dt * C.kt * C.gvel.z;
+      S.E.v[WDEM_E_BROKEN] += .5 * (pow2(Fn) / C.kn + (ft0 * ft0 + ft1 * ft1) / C.kt);
+    }
+    return false;
+  }
+  C.torque = V3();
+  C.force.x = C.kn * uN;
+  if (P.noFrict || C.tanPhi == 0.) {
+    C.force.y = 0; C.force.z = 0;
+  } else {
+    const double vt0 = C.gvel.y, vt1 = C.gvel.z;
+    /* Ft += dt*kt*velT: the scalar (dt*kt) multiplies the vector */
+    double s = P.dt * C.kt;
+    C.force.y = C.force.y + s * vt0;
+    C.force.z = C.force.z + s * vt1;
+    double maxFt = std::abs(C.force.x) * C.tanPhi;
+    double ftSq = C.force.y * C.force.y + C.force.z * C.force.z;
+    if (ftSq > maxFt * maxFt && !P.noSlip) {
+      double FtNorm = std::sqrt(ftSq);
+      double ratio = maxFt / FtNorm;
+      if (FtNorm == 0.) ratio = 0.;
+      if (P.trackEnergy) {
+        double dissip = (C.kt != 0. ? (maxFt) * (FtNorm - maxFt) / C.kt : 0.);
+        S.E.v[WDEM_E_PLAST] += dissip;
+      }
+      C.force.y *= ratio; C.force.z *= ratio;
+    }
+    if (std::isnan(std::max(C.force.x, std::max(C.force.y, C.force.z)))) {
+      S.err = "NaN force in contact ##" + std::to_string(C.pA) + "+" + std::to_string(C.pB);
+      throw std::runtime_error(S.err);
+    }
+  }
+  if (P.trackEnergy) {
+    double ftSq = C.force.y * C.force.y + C.force.z * C.force.z;
+    double elast = 0.5 * (pow2(C.force.x) / C.kn + (C.kt != 0. ? ftSq / C.kt : 0.));
+    if (std::isnan(elast)) elast = 0.;
+    S.E.v[WDEM_E_ELAST] += elast;
+  }
+  if (P.relRollStiff > 0. && P.rollTanPhi > 0.) {
+    double charLen = C.lens[0] + C.lens[1];
+    if (charLen <= 0) throw std::runtime_error("charLen<=0");
+    double kr = C.kn * charLen;
+    if (P.relTwistStiff > 0) {
+      C.torque.x = C.torque.x + P.dt * P.relTwistStiff * kr * C.gangVel.x;
+      double maxTt = std::abs(C.force.x * P.rollTanPhi * charLen);
+      if (std::abs(C.torque.x) > maxTt) C.torque.x = std::copysign(maxTt, C.torque.x);
+    }
+    double s = P.dt * kr;
+    C.torque.y = C.torque.y + s * C.gangVel.y;
+    C.torque.z = C.torque.z + s * C.gangVel.z;
+    double maxTr = std::max(0., std::abs(C.force.x) * P.rollTanPhi * charLen);
+    double trSq = C.torque.y * C.torque.y + C.torque.z * C.torque.z;
+    if (trSq > maxTr * maxTr) {
+      double TrNorm = std::sqrt(trSq);
+      double ratio = maxTr / TrNorm;
+      if (TrNorm == 0.) ratio = 0.;
+      C.torque.y *= ratio; C.torque.z *= ratio;
+    }
+  } else C.torque = V3();
+  return true;
+}
+/* Law2_L6Geom_HertzPhys_DMT::go, DMT branch (Hertz.cpp:85-114, 170-210) */
+static bool lawHertzDMT(Scene& S, Contact& C) {
+  const wdem_params& P = S.P;
+  C.torque = V3();
+  const double dt = P.dt;
+  const double velN = C.gvel.x;
+  const double vt0 = C.gvel.y, vt1 = C.gvel.z;
+  double kn0 = C.K * std::sqrt(C.R);
+  C.kn = (3 / 2.) * kn0 * std::sqrt(-C.uN);
+  double Fne, Fna = 0.;
+  if (C.alpha == 0. || C.gamma == 0.) {
+    if (C.uN > 0) return false;
+    Fne = -kn0 * pown(std::sqrt(-C.uN), 3);
+    Fna = 4 * M_PI * C.R * C.gamma;
+  } else {
+    S.err = "Schwarz branch of Law2_L6Geom_HertzPhys_DMT (alpha!=0 and gamma!=0) is not restated";
+    throw std::runtime_error(S.err);
+  }
+  double eta = (C.alpha_sqrtMK > 0 ? C.alpha_sqrtMK * std::sqrt(std::sqrt(std::max(-C.uN, 0.))) : 0.);
+  double Fnv = eta * velN;
+  if (C.alpha == 0. && P.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
+  C.force.x = Fne + Fna + Fnv;
+  if (P.trackEnergy) S.E.v[WDEM_E_VISCN] += Fnv * velN * dt;
+  C.kt = C.kt0 * std::sqrt(C.uN < 0 ? -C.uN : 0);
+  double s = dt * C.kt;
+  C.force.y = C.force.y + s * vt0;
+  C.force.z = C.force.z + s * vt1;
+  double maxFt = std::abs(std::min(0., C.force.x) * C.tanPhi);
+  double ftSq = C.force.y * C.force.y + C.force.z * C.force.z;
+  if (ftSq > pow2(maxFt)) {
+    double FtNorm = std::sqrt(ftSq);
+    double ratio = maxFt / FtNorm;
+    if (P.trackEnergy) S.E.v[WDEM_E_PLAST] += (.5 * (FtNorm - maxFt) + maxFt) * (FtNorm - maxFt) / C.kt;
+    C.force.y *= ratio; C.force.z *= ratio;
+  } else {
+    C.force.y = C.force.y + eta * vt0;
+    C.force.z = C.force.z + eta * vt1;
+    if (P.trackEnergy) S.E.v[WDEM_E_VISCT] += eta * (vt0 * vt0 + vt1 * vt1) * dt;
+  }
+  if (P.trackEnergy && C.uN < 0) {
+    double ftSq2 = C.force.y * C.force.y + C.force.z * C.force.z;
+    S.E.v[WDEM_E_ELAST] += kn0 * (2 / 5.) * pown(std::sqrt(-C.uN), 5) + 0.5 * ftSq2 / C.kt;
+  }
+  return true;
+}
+
+/* Contact::getForceTorqueBranch (Contact.cpp:24-34) + DemData::addForceTorque (Particle.hpp:249) */
+static void applyForceUninodal(Scene& S, const Contact& C, Particle& p) {
+  bool isPA = (C.pA == p.id);
+  double sign = isPA ? 1 : -1;
+  V3 F = qrot(C.gori, C.force) * sign;
+  V3 T = (isZero(C.torque) ? V3() : qrot(C.gori, C.torque)) * sign;
+  V3 xc = C.contPt - p.pos;
+  p.force = p.force + F;
+  p.torque = p.torque + (cross(xc, F) + T);
+}
+
+static bool isSphereLike(int shape) { return shape == WDEM_SHAPE_SPHERE; }
+
+/* ContactLoop::run (ContactLoop.cpp:93-268), aperiodic, no hook, no stress */
+static void contactLoopRun(Scene& S) {
+  const wdem_params& P = S.P;
+  /* removeAllPending when no collider ran: pending is empty after the collider */
+  if (!S.pending.empty()) {
+    auto pend = S.pending; S.pending.clear();
+    for (auto& pc : pend) removeContact(S, pc.first);
+  }
+  std::vector<CPtr> removeAfter;
+  size_t size = S.linView.size();
+  for (size_t i = 0; i < size; i++) {
+    const CPtr C = S.linView[i];
+    if (!C->isReal() && !C->isColliding()) { removeAfter.push_back(C); continue; }
+    bool fresh = (S.step == C->stepCreated);
+    if (!C->isReal() && fresh) {
+      /* functor order: Cg2_Wall_Sphere_L6Geom wants (Wall, Sphere) (FUNCTOR2D(Wall,Sphere)) */
+      Particle& a = S.par[C->pA];
+      Particle& b = S.par[C->pB];
+      bool known = (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_SPHERE) ||
+                   (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_SPHERE) ||
+                   (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL);
+      if (!known) continue;
+      if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) std::swap(C->pA, C->pB); /* Contact::swapOrder */
+      /* setMinDist00Sq: Sphere+Sphere only (Sphere.cpp:86-89), else -1 (ContactLoop.hpp:18) */
+      if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
+        C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
+      else C->minDist00Sq = -1;
+    }
+    Particle& pA = S.par[C->pA];
+    Particle& pB = S.par[C->pB];
+    V3 shift2;
+    if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
+    bool geomCreated;
+    if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
+    else if (pA.shape == WDEM_SHAPE_WALL && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2WallSphere(S, *C, pA, pB, shift2, false);
+    else geomCreated = false;
+    if (!geomCreated) continue;
+    if (!C->phys) C->stepCreated = (int)S.step;
+    if (!C->phys || S.updatePhys > WDEM_UPDATE_PHYS_NEVER) {
+      const wdem_material& m1 = S.mats[pA.mat];
+      const wdem_material& m2 = S.mats[pB.mat];
+      if (P.cp2 == WDEM_CP2_FRICT) cp2Frict(S, *C, m1, m2);
+      else {
+        if (m1.kind != WDEM_MAT_HERTZ || m2.kind != WDEM_MAT_HERTZ) {
+          S.err = "ContactLoop: ##" + std::to_string(pA.id) + "+" + std::to_string(pB.id) + ": no Contact.phys created from materials";
+          throw std::runtime_error(S.err);
+        }
+        cp2Hertz(S, *C, m1, m2);
+      }
+    }
+    bool keep = (P.law == WDEM_LAW_IDEALELPL) ? lawIdealElPl(S, *C) : lawHertzDMT(S, *C);
+    if (!keep) requestRemoval(S, C);
+    if (P.applyForces && C->isReal() && S.applyOrder == 0) {
+      applyForceUninodal(S, *C, pA);
+      applyForceUninodal(S, *C, pB);
+    }
+  }
+  for (auto& c : removeAfter) removeContact(S, c);
+  if (P.applyForces && S.applyOrder == 1) {
+    std::vector<CPtr> real;
+    for (auto& c : S.linView) if (c->isReal()) real.push_back(c);
+    std::sort(real.begin(), real.end(), [](const CPtr& a, const CPtr& b) {
+      long ka = ((long)std::min(a->pA, a->pB) << 32) | std::max(a->pA, a->pB);
+      long kb = ((long)std::min(b->pA, b->pB) << 32) | std::max(b->pA, b->pB);
+      return ka < kb;
+    });
+    for (auto& c : real) { applyForceUninodal(S, *c, S.par[c->pA]); applyForceUninodal(S, *c, S.par[c->pB]); }
+  }
+  if (S.updatePhys == WDEM_UPDATE_PHYS_ONCE) S.updatePhys = WDEM_UPDATE_PHYS_NEVER;
+}
+
+/* ------------------------------------------------------------------ integrator */
+/* Leapfrog::run, aperiodic (Leapfrog.cpp:104-255), ForceResetter folded in via reset=True */
+static void leapfrogRun(Scene& S) {
+  const wdem_params& P = S.P;
+  const double dt = P.dt;
+  const double damping = P.damping;
+  V3 gravity(P.gravity[0], P.gravity[1], P.gravity[2]);
+  bool hasGravity = !isZero(gravity);
+  for (Particle& p : S.par) {
+    bool damp = (damping != 0. && !(p.flags & WDEM_DAMPING_SKIP));
+    V3& f = p.force;
+    V3& t = p.torque;
+    if (P.trackEnergy) {
+      if (damp && !(p.flags & WDEM_ENERGY_SKIP)) {
+        /* doDampingDissipation (:53-64) */
+        V3 av(std::abs(p.vel.x), std::abs(p.vel.y), std::abs(p.vel.z));
+        V3 af(std::abs(f.x), std::abs(f.y), std::abs(f.z));
+        V3 aw(std::abs(p.angVel.x), std::abs(p.angVel.y), std::abs(p.angVel.z));
+        V3 at(std::abs(t.x), std::abs(t.y), std::abs(t.z));
+        S.E.v[WDEM_E_NONVISCDAMP] += dot(av, af) * damping * dt + dot(aw, at) * damping * dt;
+      }
+      if (hasGravity && !(p.flags & WDEM_GRAVITY_SKIP)) {
+        /* doGravityWork (:67-74) */
+        double gr = 0;
+        if (p.isBlockedNone()) gr = -dot(gravity, p.vel) * p.mass * dt;
+        else for (int ax = 0; ax < 3; ax++) if (!p.isBlockedAxisDOF(ax, false)) gr -= gravity[ax] * p.vel[ax] * p.mass * dt;
+        S.E.v[WDEM_E_GRAV] += gr;
+      }
+    }
+    V3 pprevFluctVel, pprevFluctAngVel;
+    bool useAspherical = p.isAspherical() && !p.isBlockedAllRot();
+    V3 linAccel, angAccel;
+    if (!p.isBlockedAll()) {
+      /* computeAccel (:37-42) */
+      if (p.isBlockedNone()) linAccel = f / p.mass;
+      else for (int i = 0; i < 3; i++) if (!p.isBlockedAxisDOF(i, false)) linAccel[i] += f[i] / p.mass;
+      pprevFluctVel = p.vel; pprevFluctAngVel = p.angVel;
+      /* nonviscDamp2nd (:33-35) */
+      if (damp) for (int i = 0; i < 3; i++) linAccel[i] *= 1 - damping * Sign(f[i] * (pprevFluctVel[i] + 0.5 * dt * linAccel[i]));
+      p.vel = p.vel + dt * linAccel;
+      if (!isZero(p.inertia)) {
+        if (!useAspherical) {
+          if (p.isBlockedNone()) angAccel = V3(t.x / p.inertia.x, t.y / p.inertia.y, t.z / p.inertia.z);
+          else for (int i = 0; i < 3; i++) if (!p.isBlockedAxisDOF(i, true)) angAccel[i] += t[i] / p.inertia[i];
+          if (damp) for (int i = 0; i < 3; i++) angAccel[i] *= 1 - damping * Sign(t[i] * (pprevFluctAngVel[i] + 0.5 * dt * angAccel[i]));
+          p.angVel = p.angVel + dt * angAccel;
+        } else {
+          throw std::runtime_error("aspherical leapfrog is not restated for this particle model");
+        }
+      }
+    }
+    if (P.trackEnergy && !(p.flags & WDEM_ENERGY_SKIP)) {
+      /* doKineticEnergy (:76-98), spherical */
+      V3 cfv = pprevFluctVel + .5 * dt * linAccel, cfa = pprevFluctAngVel + .5 * dt * angAccel;
+      double Etrans = .5 * p.mass * sqnorm(cfv);
+      double Erot = 0.5 * dot(cfa, V3(p.inertia.x * cfa.x, p.inertia.y * cfa.y, p.inertia.z * cfa.z));
+      if (std::isnan(Erot) || std::isinf(absmax(p.inertia))) Erot = 0;
+      S.E.v[WDEM_E_KINETIC] += Etrans + Erot;
+    }
+    /* leapfrogTranslate (:275-278) */
+    p.pos = p.pos + p.vel * dt;
+    /* leapfrogSphericalRotate (:280-297) */
+    V3 axis = p.angVel;
+    if (!isZero(axis)) {
+      double angle = norm(axis);
+      axis = axis / angle;
+      double ha = 0.5 * (angle * dt);
+      double sh = std::sin(ha);
+      Quat q(std::cos(ha), sh * axis.x, sh * axis.y, sh * axis.z);
+      p.ori = qmul(q, p.ori);
+    }
+    qnormalize(p.ori);
+    if (P.reset) {
+      p.force = (hasGravity && !(p.flags & WDEM_GRAVITY_SKIP)) ? p.mass * gravity : V3();
+      p.torque = V3();
+    }
+  }
+}
+
+/* DemFuncs::pWaveDt (Funcs.cpp:151-175) */
+static double pWaveDt(const Scene& S) {
+  double dt = Inf;
+  for (const Particle& p : S.par) {
+    if (p.shape != WDEM_SHAPE_SPHERE) continue;
+    const wdem_material& m = S.mats[p.mat];
+    dt = std::min(dt, p.radius / (1. * std::sqrt(m.young / m.density)));
+  }
+  return dt;
+}
+
+/* Scene::doOneStep (Scene.cpp:366-467) with engines [Leapfrog, InsertionSortCollider, ContactLoop] */
+static void doOneStep(Scene& S) {
+  if (S.P.trackEnergy) S.E.resetResettables();
+  leapfrogRun(S);
+  colliderRun(S);
+  contactLoopRun(S);
+  S.step++;
+  S.time += S.P.dt;
+  S.P.step = S.step;
+}
+
+}  // namespace orc
+
+/* ====================================================================== C ABI for tests */
+using namespace orc;
+
+struct orc_handle { Scene S; };
+
+extern "C" {
+
+orc_handle* orc_create(void) { return new orc_handle(); }
+void orc_destroy(orc_handle* h) { delete h; }
+const char* orc_last_error(orc_handle* h) { return h->S.err.c_str(); }
+
+int orc_set_params(orc_handle* h, const wdem_params* p) {
+  Scene& S = h->S;
+  S.P = *p;
+  S.mats.assign(p->materials, p->materials + p->nMaterials);
+  S.P.materials = nullptr;
+  S.step = p->step;
+  S.updatePhys = p->updatePhys;
+  if (S.nFullRuns == 0 && S.BB[0].empty()) S.verletDist = p->verletDist;
+  return 0;
+}
+
+int orc_set_mode(orc_handle* h, int canonicalOrient, int applyOrder, int sortAxis) {
+  h->S.canonicalOrient = canonicalOrient; h->S.applyOrder = applyOrder; h->S.sortAxis = sortAxis;
+  return 0;
+}
+
+int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
+  Scene& S = h->S;
+  S.par.assign(p->n, Particle());
+  for (int i = 0; i < p->n; i++) {
+    Particle& q = S.par[i];
+    q.id = i;
+    q.shape = p->shape[i];
+    q.radius = p->radius[i];
+    q.axis = p->wallAxis ? p->wallAxis[i] : 0;
+    q.sense = p->wallSense ? p->wallSense[i] : 0;
+    q.mat = p->material[i];
+    q.mask = p->mask[i];
+    q.flags = p->flags[i];
+    q.mass = p->mass[i];
+    q.inertia = V3(p->inertia[3 * i], p->inertia[3 * i + 1], p->inertia[3 * i + 2]);
+    q.pos = V3(p->pos[3 * i], p->pos[3 * i + 1], p->pos[3 * i + 2]);
+    q.ori = Quat(p->ori[4 * i], p->ori[4 * i + 1], p->ori[4 * i + 2], p->ori[4 * i + 3]);
+    q.vel = V3(p->vel[3 * i], p->vel[3 * i + 1], p->vel[3 * i + 2]);
+    q.angVel = V3(p->angVel[3 * i], p->angVel[3 * i + 1], p->angVel[3 * i + 2]);
+    q.force = V3(p->force[3 * i], p->force[3 * i + 1], p->force[3 * i + 2]);
+    q.torque = V3(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2]);
+  }
+  S.linView.clear(); S.pending.clear();
+  for (int i = 0; i < 3; i++) S.BB[i].clear();
+  S.dirty = true;
+  S.verletDist = S.P.verletDist;
+  return 0;
+}
+
+int orc_upload_contacts(orc_handle* h, const wdem_contacts* c) {
+  Scene& S = h->S;
+  for (Particle& p : S.par) p.contacts.clear();
+  S.linView.clear(); S.pending.clear();
+  for (long i = 0; i < c->n; i++) {
+    CPtr C = std::make_shared<Contact>();
+    C->pA = c->idA[i]; C->pB = c->idB[i];
+    C->stepCreated = c->stepCreated[i];
+    C->minDist00Sq = c->minDist00Sq ? c->minDist00Sq[i] : -1;
+    if (c->real[i]) {
+      C->geom = C->phys = true;
+      for (int k = 0; k < 3; k++) C->trsf.c[k] = V3(c->trsf[9 * i + 3 * k], c->trsf[9 * i + 3 * k + 1], c->trsf[9 * i + 3 * k + 2]);
+      C->contPt = V3(c->contPt[3 * i], c->contPt[3 * i + 1], c->contPt[3 * i + 2]);
+      C->gori = quatFromMatrix(C->trsf);
+      C->force = V3(c->force[3 * i], c->force[3 * i + 1], c->force[3 * i + 2]);
+      C->torque = V3(c->torque[3 * i], c->torque[3 * i + 1], c->torque[3 * i + 2]);
+      C->kn = c->kn[i]; C->kt = c->kt[i]; C->tanPhi = c->tanPhi[i];
+      /* lens/contA for iniLensTouch=true; Hertz constants recomputed from the materials */
+      const Particle& a = S.par[C->pA];
+      const Particle& b = S.par[C->pB];
+      double r1 = a.shape == WDEM_SHAPE_WALL ? -b.radius : a.radius, r2 = b.radius;
+      C->lens[0] = std::abs(r1); C->lens[1] = std::abs(r2);
+      C->contA = M_PI * pow2((r1 > 0 && r2 > 0) ? std::min(r1, r2) : (r1 > 0 ? r1 : r2));
+      if (S.P.cp2 == WDEM_CP2_HERTZ) {
+        double kn = C->kn, kt = C->kt, tp = C->tanPhi;
+        cp2Hertz(S, *C, S.mats[a.mat], S.mats[b.mat]);
+        C->kn = kn; C->kt = kt; C->tanPhi = tp;
+      }
+    }
+    addMaybe_fast(S, C);
+  }
+  return 0;
+}
+
+int orc_step(orc_handle* h, int n) {
+  try {
+    for (int i = 0; i < n; i++) doOneStep(h->S);
+  } catch (std::exception& e) {
+    h->S.err = e.what();
+    return WDEM_ERR_NAN;
+  }
+  return 0;
+}
+
+/* Time nSteps steps on the host, returning wall seconds (CPU baseline leg). */
+double orc_step_timed(orc_handle* h, int n) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = orc_step(h, n);
+  auto t1 = std::chrono::steady_clock::now();
+  if (rc) return -1;
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+int orc_download_particles(orc_handle* h, wdem_particles* p) {
+  Scene& S = h->S;
+  for (int i = 0; i < p->n && i < (int)S.par.size(); i++) {
+    const Particle& q = S.par[i];
+    if (p->pos) { p->pos[3 * i] = q.pos.x; p->pos[3 * i + 1] = q.pos.y; p->pos[3 * i + 2] = q.pos.z; }
+    if (p->ori) { p->ori[4 * i] = q.ori.w; p->ori[4 * i + 1] = q.ori.x; p->ori[4 * i + 2] = q.ori.y; p->ori[4 * i + 3] = q.ori.z; }
+    if (p->vel) { p->vel[3 * i] = q.vel.x; p->vel[3 * i + 1] = q.vel.y; p->vel[3 * i + 2] = q.vel.z; }
+    if (p->angVel) { p->angVel[3 * i] = q.angVel.x; p->angVel[3 * i + 1] = q.angVel.y; p->angVel[3 * i + 2] = q.angVel.z; }
+    if (p->force) { p->force[3 * i] = q.force.x; p->force[3 * i + 1] = q.force.y; p->force[3 * i + 2] = q.force.z; }
+    if (p->torque) { p->torque[3 * i] = q.torque.x; p->torque[3 * i + 1] = q.torque.y; p->torque[3 * i + 2] = q.torque.z; }
+  }
+  return 0;
+}
+
+long orc_contact_count(orc_handle* h) { return (long)h->S.linView.size(); }
+
+/* contacts sorted by (min id, max id) */
+int orc_download_contacts(orc_handle* h, wdem_contacts* c) {
+  Scene& S = h->S;
+  std::vector<CPtr> v = S.linView;
+  std::sort(v.begin(), v.end(), [](const CPtr& a, const CPtr& b) {
+    long ka = ((long)std::min(a->pA, a->pB) << 32) | std::max(a->pA, a->pB);
+    long kb = ((long)std::min(b->pA, b->pB) << 32) | std::max(b->pA, b->pB);
+    return ka < kb;
+  });
+  for (long i = 0; i < (long)v.size() && i < c->n; i++) {
+    const Contact& C = *v[i];
+    if (c->idA) c->idA[i] = C.pA;
+    if (c->idB) c->idB[i] = C.pB;
+    if (c->real) c->real[i] = C.isReal();
+    if (c->stepCreated) c->stepCreated[i] = C.stepCreated;
+    if (c->minDist00Sq) c->minDist00Sq[i] = C.minDist00Sq;
+    if (c->trsf) for (int k = 0; k < 3; k++) { c->trsf[9 * i + 3 * k] = C.trsf.c[k].x; c->trsf[9 * i + 3 * k + 1] = C.trsf.c[k].y; c->trsf[9 * i + 3 * k + 2] = C.trsf.c[k].z; }
+    if (c->contPt) { c->contPt[3 * i] = C.contPt.x; c->contPt[3 * i + 1] = C.contPt.y; c->contPt[3 * i + 2] = C.contPt.z; }
+    if (c->geomOri) { c->geomOri[4 * i] = C.gori.w; c->geomOri[4 * i + 1] = C.gori.x; c->geomOri[4 * i + 2] = C.gori.y; c->geomOri[4 * i + 3] = C.gori.z; }
+    if (c->geomVel) { c->geomVel[3 * i] = C.gvel.x; c->geomVel[3 * i + 1] = C.gvel.y; c->geomVel[3 * i + 2] = C.gvel.z; }
+    if (c->geomAngVel) { c->geomAngVel[3 * i] = C.gangVel.x; c->geomAngVel[3 * i + 1] = C.gangVel.y; c->geomAngVel[3 * i + 2] = C.gangVel.z; }
+    if (c->uN) c->uN[i] = C.uN;
+    if (c->force) { c->force[3 * i] = C.force.x; c->force[3 * i + 1] = C.force.y; c->force[3 * i + 2] = C.force.z; }
+    if (c->torque) { c->torque[3 * i] = C.torque.x; c->torque[3 * i + 1] = C.torque.y; c->torque[3 * i + 2] = C.torque.z; }
+    if (c->kn) c->kn[i] = C.kn;
+    if (c->kt) c->kt[i] = C.kt;
+    if (c->tanPhi) c->tanPhi[i] = C.tanPhi;
+  }
+  return 0;
+}
+
+double orc_crit_dt(orc_handle* h) { return pWaveDt(h->S); }
+
+int orc_get_energy(orc_handle* h, double* e, int n) {
+  for (int i = 0; i < n && i < WDEM_E_COUNT; i++) e[i] = h->S.E.v[i];
+  return 0;
+}
+int orc_reset_energy(orc_handle* h) { for (int i = 0; i < WDEM_E_COUNT; i++) h->S.E.v[i] = 0; return 0; }
+
+long orc_nfullruns(orc_handle* h) { return h->S.nFullRuns; }
+double orc_verlet_dist(orc_handle* h) { return h->S.verletDist; }
+long orc_step_count(orc_handle* h) { return h->S.step; }
+int orc_set_update_phys(orc_handle* h, int up) { h->S.updatePhys = up; return 0; }
+int orc_set_young(orc_handle* h, int mat, double young) { h->S.mats[mat].young = young; return 0; }
+
+/* InsertionSortCollider initial sort + sweep (InsertionSortCollider.cpp:536-605) over given boxes,
+ * with spatialOverlap and mayCollide; writes pairs (min id, max id) sorted. */
+long orc_collide_boxes(int n, const double* mins, const double* maxs, const uint32_t* mask, uint32_t loneMask,
+                       int sortAxis, int32_t* pairs, long maxPairs) {
+  Scene S;
+  S.P.loneMask = loneMask;
+  S.par.assign(n, Particle());
+  for (int i = 0; i < n; i++) {
+    Particle& p = S.par[i];
+    p.id = i; p.mask = mask[i];
+    p.bound.has = true;
+    p.bound.min = V3(mins[3 * i], mins[3 * i + 1], mins[3 * i + 2]);
+    p.bound.max = V3(maxs[3 * i], maxs[3 * i + 1], maxs[3 * i + 2]);
+  }
+  S.minima.assign(3 * n, 0); S.maxima.assign(3 * n, 0);
+  for (int i = 0; i < n; i++) for (int k = 0; k < 3; k++) { S.minima[3 * i + k] = mins[3 * i + k]; S.maxima[3 * i + k] = maxs[3 * i + k]; }
+  for (int j = 0; j < 3; j++) {
+    for (int id = 0; id < n; id++) {
+      Bounds a(mins[3 * id + j], id, true); a.hasBB = true;
+      Bounds b(maxs[3 * id + j], id, false); b.hasBB = true;
+      S.BB[j].push_back(a); S.BB[j].push_back(b);
+    }
+    std::sort(S.BB[j].begin(), S.BB[j].end());
+  }
+  std::vector<Bounds>& V = S.BB[sortAxis];
+  long n2 = 2L * n;
+  for (long i = 0; i < n2; i++) {
+    if (!(V[i].isMin && V[i].hasBB)) continue;
+    int iid = V[i].id;
+    for (long j = i + 1; j < n2 && V[j].id != iid; j++) {
+      if (!V[j].isMin) continue;
+      handleBoundInversion(S, iid, V[j].id, false);
+    }
+  }
+  for (auto& C : S.makeContacts) addMaybe_fast(S, C);
+  std::vector<long> keys;
+  for (auto& c : S.linView) keys.push_back(((long)std::min(c->pA, c->pB) << 32) | std::max(c->pA, c->pB));
+  std::sort(keys.begin(), keys.end());
+  long cnt = (long)keys.size();
+  for (long i = 0; i < cnt && i < maxPairs; i++) { pairs[2 * i] = (int32_t)(keys[i] >> 32); pairs[2 * i + 1] = (int32_t)(keys[i] & 0xffffffffL); }
+  return cnt;
+}
+
+/* Incremental collider check: run the insertion-sort collider over a sequence of box sets
+ * (nFrames x n boxes), as InsertionSortCollider does between steps (:524-531), and return the
+ * pair count after the last frame plus the sorted pairs.  All pairs are potential (non-real). */
+long orc_collide_frames(int n, int nFrames, const double* mins, const double* maxs, const uint32_t* mask,
+                        uint32_t loneMask, int32_t* pairs, long maxPairs) {
+  Scene S;
+  S.P.loneMask = loneMask;
+  S.par.assign(n, Particle());
+  for (int i = 0; i < n; i++) { S.par[i].id = i; S.par[i].mask = mask[i]; S.par[i].bound.has = true; }
+  for (int f = 0; f < nFrames; f++) {
+    const double* mn = mins + (size_t)3 * n * f;
+    const double* mx = maxs + (size_t)3 * n * f;
+    bool init = S.BB[0].empty();
+    if (init)
+      for (int j = 0; j < 3; j++)
+        for (int id = 0; id < n; id++) { S.BB[j].push_back(Bounds(0, id, true)); S.BB[j].push_back(Bounds(0, id, false)); }
+    for (int j = 0; j < 3; j++)
+      for (Bounds& b : S.BB[j]) { b.hasBB = true; b.coord = b.isMin ? mn[3 * b.id + j] : mx[3 * b.id + j]; }
+    S.minima.assign(mn, mn + 3 * n); S.maxima.assign(mx, mx + 3 * n);
+    if (!init) { for (int j = 0; j < 3; j++) insertionSort(S, S.BB[j], true); }
+    else {
+      for (int j = 0; j < 3; j++) std::sort(S.BB[j].begin(), S.BB[j].end());
+      std::vector<Bounds>& V = S.BB[0];
+      long n2 = 2L * n;
+      for (long i = 0; i < n2; i++) {
+        if (!(V[i].isMin && V[i].hasBB)) continue;
+        int iid = V[i].id;
+        for (long j = i + 1; j < n2 && V[j].id != iid; j++) { if (!V[j].isMin) continue; handleBoundInversion(S, iid, V[j].id, false); }
+      }
+    }
+    for (auto& C : S.removeContacts) removeMaybe_fast(S, C);
+    S.removeContacts.clear();
+    for (auto& C : S.makeContacts) addMaybe_fast(S, C);
+    S.makeContacts.clear();
+  }
+  std::vector<long> keys;
+  for (auto& c : S.linView) keys.push_back(((long)std::min(c->pA, c->pB) << 32) | std::max(c->pA, c->pB));
+  std::sort(keys.begin(), keys.end());
+  long cnt = (long)keys.size();
+  for (long i = 0; i < cnt && i < maxPairs; i++) { pairs[2 * i] = (int32_t)(keys[i] >> 32); pairs[2 * i + 1] = (int32_t)(keys[i] & 0xffffffffL); }
+  return cnt;
+}
+
+}  /* extern "C" */

@@ -1,0 +1,7 @@
+"""woo_gb300 -- a GB300-native DEM timestep with Woo's engine/functor surface.
+
+One GPU engine (GpuDemEngine) replaces Woo's Leapfrog + InsertionSortCollider + ContactLoop trio.
+The compute path is libwdem.so (hand-written sm_103a CUDA kernels behind the C ABI of
+include/wdem.h); there is no CPU fallback.
+"""
+__version__ = "0.1.0"

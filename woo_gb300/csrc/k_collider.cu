@@ -1,0 +1,617 @@
+// k_collider.cu -- GPU collider for the DEM engine: the GB300 replacement of Woo's
+// InsertionSortCollider (src/dem/InsertionSortCollider.cpp:386-613) and AabbCollider's verlet
+// boxes (src/dem/Collision.cpp:80-184).
+//
+// A rebuild runs whenever a particle left its verlet box (aabbIsDirty).  It produces the same
+// candidate set as the reference collider on the same boxes: every pair whose closed boxes overlap
+// on all three axes (spatialOverlap, InsertionSortCollider.cpp:67-73) and that mayCollide
+// (Collision.cpp:21-43), plus every real contact carried over from before (the reference never
+// removes real contacts in the collider).  Instead of an incremental insertion sort, the rebuild
+//   1. sorts small particles by (grid column in the two short axes, quantised box minimum along the
+//      longest axis) with an LSD radix sort written here,
+//   2. sweeps each particle forward along the long axis in its own and the 8 neighbouring columns,
+//      testing the exact FP64 closed-interval overlap (grid cell >= widest box, so no pair is missed),
+//   3. tests walls and other unbounded boxes against every particle,
+//   4. writes the pairs in a deterministic order (count pass, exclusive scan, write pass),
+//   5. carries contact history over through an open-addressing hash table keyed by (min id, max id),
+//   6. builds the per-particle contact CSR with rows ordered by the partner id.
+#include "wdem_internal.h"
+#include "../../include/wdem.h"
+#include <cstdio>
+
+namespace wdem {
+
+static const unsigned long long HASH_EMPTY = ~0ull;
+static const int QBITS = 24;
+static const unsigned QMAX = (1u << QBITS) - 1;
+
+// ------------------------------------------------------------------------------------------ boxes
+// Bo1_Sphere_Aabb::go / Bo1_Wall_Aabb::go + AabbCollider::updateAabb: pos +- bboxFactor*r,
+// walls unbounded except along their axis; both enlarged by verletDist; nodeLastPos = pos.
+__global__ void k_bboxes(StepParams P, Particles p, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4_32a pr = p.posr[i];
+  int sh = p.meta[i].x & 15;
+  double4_32a mn, mx;
+  if (sh == WDEM_SHAPE_SPHERE) {
+    double h = P.bboxFactor * pr.w;
+    mn = make_double4_32a(pr.x - h, pr.y - h, pr.z - h, 0);
+    mx = make_double4_32a(pr.x + h, pr.y + h, pr.z + h, 0);
+  } else {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    int ax = (p.meta[i].x >> 4) & 3;
+    mn = make_double4_32a(-inf, -inf, -inf, 0);
+    mx = make_double4_32a(inf, inf, inf, 0);
+    double c = ax == 0 ? pr.x : (ax == 1 ? pr.y : pr.z);
+    if (ax == 0) { mn.x = c; mx.x = c; } else if (ax == 1) { mn.y = c; mx.y = c; } else { mn.z = c; mx.z = c; }
+  }
+  if (P.verletDist > 0) {
+    double vd = P.verletDist;
+    mx.x = mx.x + vd; mx.y = mx.y + vd; mx.z = mx.z + vd;
+    mn.x = mn.x - vd; mn.y = mn.y - vd; mn.z = mn.z - vd;
+  }
+  p.bbmin[i] = mn;
+  p.bbmax[i] = mx;
+  p.lastPos[i] = make_double4_32a(pr.x, pr.y, pr.z, 0);
+}
+
+void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n) {
+  if (n <= 0) return;
+  k_bboxes<<<(n + 255) / 256, 256, 0, s>>>(P, p, n);
+}
+
+// ------------------------------------------------------------------------------------ grid setup
+// Order-preserving map double -> unsigned 64 for atomic min/max.
+__device__ __forceinline__ unsigned long long ordKey(double d) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ordVal(unsigned long long k) {
+  unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// ext layout (ordered keys): [0..2] min centre, [3..5] max centre (stored as ~key for max via min),
+// [6..8] min box lower bound, [9..11] max box upper bound, [12..14] max box width
+struct ExtAcc { unsigned long long v[15]; };
+
+__global__ void k_extents_init(unsigned long long* ext) {
+  int t = threadIdx.x;
+  if (t < 15) ext[t] = ~0ull;  // all stored as "min" accumulators
+}
+
+__global__ void k_extents(Particles p, const int* small, int nSmall, unsigned long long* ext) {
+  __shared__ unsigned long long sh[15];
+  if (threadIdx.x < 15) sh[threadIdx.x] = ~0ull;
+  __syncthreads();
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nSmall) {
+    int i = small[k];
+    double4_32a pr = p.posr[i];
+    double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+    double c[3] = {pr.x, pr.y, pr.z};
+    double lo[3] = {mn.x, mn.y, mn.z};
+    double hi[3] = {mx.x, mx.y, mx.z};
+    for (int a = 0; a < 3; a++) {
+      atomicMin(&sh[a], ordKey(c[a]));
+      atomicMin(&sh[3 + a], ~ordKey(c[a]));
+      atomicMin(&sh[6 + a], ordKey(lo[a]));
+      atomicMin(&sh[9 + a], ~ordKey(hi[a]));
+      atomicMin(&sh[12 + a], ~ordKey(hi[a] - lo[a]));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 15) atomicMin(&ext[threadIdx.x], sh[threadIdx.x]);
+}
+
+__global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxCols, GridParams* g) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  GridParams G;
+  G.nSmall = nSmall;
+  if (nSmall == 0) { G.ok = 0; G.sweepAxis = 0; G.ax1 = 1; G.ax2 = 2; G.ncx = G.ncy = 1; G.lo1 = G.lo2 = 0; G.cell = 1; G.loS = 0; G.invQ = 0; *g = G; return; }
+  double cmin[3], cmax[3], bmin[3], bmax[3], w[3];
+  for (int a = 0; a < 3; a++) {
+    cmin[a] = ordVal(ext[a]);
+    cmax[a] = ordVal(~ext[3 + a]);
+    bmin[a] = ordVal(ext[6 + a]);
+    bmax[a] = ordVal(~ext[9 + a]);
+    w[a] = ordVal(~ext[12 + a]);
+  }
+  int ax = 0;
+  for (int a = 1; a < 3; a++) if (cmax[a] - cmin[a] > cmax[ax] - cmin[ax]) ax = a;
+  int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;
+  double W = fmax(w[a1], w[a2]);
+  double cell = W * (1.0 + 1e-6) + 1e-300;
+  double e1 = cmax[a1] - cmin[a1], e2 = cmax[a2] - cmin[a2];
+  // cap the column count; a larger cell stays correct (only the cell >= W bound matters)
+  for (int it = 0; it < 64; it++) {
+    double n1 = floor(e1 / cell) + 1, n2 = floor(e2 / cell) + 1;
+    if (n1 * n2 <= (double)maxCols) break;
+    cell *= 1.25;
+  }
+  // non-finite extents (NaN or infinite positions) or a grid still too fine: one column
+  if (!(e1 >= 0 && e2 >= 0 && e1 < 1e300 && e2 < 1e300 && cell > 0 && cell < 1e300) ||
+      (floor(e1 / cell) + 1) * (floor(e2 / cell) + 1) > (double)maxCols) {
+    e1 = 0; e2 = 0; cell = 1e300;
+    cmin[a1] = 0; cmin[a2] = 0;
+  }
+  G.sweepAxis = ax; G.ax1 = a1; G.ax2 = a2;
+  G.cell = cell;
+  G.lo1 = cmin[a1]; G.lo2 = cmin[a2];
+  G.ncx = (int)(floor(e1 / cell) + 1);
+  G.ncy = (int)(floor(e2 / cell) + 1);
+  G.loS = bmin[ax];
+  double span = bmax[ax] - bmin[ax];
+  G.invQ = (span > 0 && span < 1e300) ? (double)(QMAX - 1) / span : 0.0;
+  if (!(G.invQ == G.invQ)) G.invQ = 0.0;
+  if (!(G.loS == G.loS)) G.loS = 0.0;
+  G.ok = 1;
+  *g = G;
+}
+
+__device__ __forceinline__ double cmp3(const double4_32a& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+// monotone non-decreasing quantisation along the sweep axis
+__device__ __forceinline__ unsigned quant(double x, const GridParams& G) {
+  double t = (x - G.loS) * G.invQ;
+  if (!(t > 0)) return 0;                 // also NaN
+  if (t >= (double)QMAX) return QMAX;
+  return (unsigned)t;                      // truncation == floor for t >= 0
+}
+
+__device__ __forceinline__ void columnOf(const double4_32a& pr, const GridParams& G, int& cx, int& cy) {
+  double t1 = floor((cmp3(pr, G.ax1) - G.lo1) / G.cell);
+  double t2 = floor((cmp3(pr, G.ax2) - G.lo2) / G.cell);
+  cx = (int)fmin(fmax(t1, 0.0), (double)(G.ncx - 1));
+  cy = (int)fmin(fmax(t2, 0.0), (double)(G.ncy - 1));
+}
+
+__global__ void k_make_keys(Particles p, const int* small, int nSmall, const GridParams* g,
+                            unsigned long long* keys, unsigned* vals) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nSmall) return;
+  GridParams G = *g;
+  int i = small[k];
+  int cx, cy;
+  columnOf(p.posr[i], G, cx, cy);
+  unsigned long long col = (unsigned long long)cx + (unsigned long long)G.ncx * cy;
+  unsigned q = quant(cmp3(p.bbmin[i], G.sweepAxis), G);
+  keys[k] = (col << QBITS) | q;
+  vals[k] = (unsigned)i;
+}
+
+
+// ------------------------------------------------------------------------------------ scan
+// Exclusive scan of a[0..n) in place, a[n] <- total.  Block-wise scan, recursive on block sums.
+static const int SCAN_T = 256, SCAN_I = 4, SCAN_TILE = SCAN_T * SCAN_I;
+
+__global__ void k_scan_tiles(unsigned* a, long long n, unsigned* sums) {
+  __shared__ unsigned s[SCAN_T];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  unsigned v[SCAN_I];
+  unsigned tsum = 0;
+  for (int k = 0; k < SCAN_I; k++) {
+    long long idx = base + threadIdx.x * SCAN_I + k;
+    v[k] = idx < n ? a[idx] : 0;
+    tsum += v[k];
+  }
+  s[threadIdx.x] = tsum;
+  __syncthreads();
+  for (int off = 1; off < SCAN_T; off <<= 1) {
+    unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  unsigned run = s[threadIdx.x] - tsum;  // exclusive prefix of this thread
+  for (int k = 0; k < SCAN_I; k++) {
+    long long idx = base + threadIdx.x * SCAN_I + k;
+    if (idx < n) a[idx] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == SCAN_T - 1) sums[blockIdx.x] = s[SCAN_T - 1];
+}
+
+__global__ void k_scan_add(unsigned* a, long long n, const unsigned* sums) {
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  unsigned add = sums[blockIdx.x];
+  for (int k = 0; k < SCAN_I; k++) {
+    long long idx = base + threadIdx.x * SCAN_I + k;
+    if (idx < n) a[idx] += add;
+  }
+}
+
+
+static void scan_rec(cudaStream_t s, unsigned* a, long long n, unsigned* scratch) {
+  long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb == 0) return;
+  unsigned* sums = scratch;  // nb + 1 entries
+  k_scan_tiles<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums);
+  if (nb > 1) {
+    scan_rec(s, sums, nb, scratch + ((nb + 1 + 63) & ~63ll));
+    k_scan_add<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums);
+  } else {
+    // single tile: sums[0] holds the total; scan of one element is 0
+  }
+}
+
+
+__global__ void k_save_last(const unsigned* a, long long n, unsigned* dst) { *dst = n > 0 ? a[n - 1] : 0; }
+__global__ void k_finish_total(unsigned* a, long long n, const unsigned* lastInput) {
+  a[n] = (n > 0 ? a[n - 1] : 0) + *lastInput;
+}
+
+void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs) {
+  unsigned* last = cs.blockSums;        // 1 entry
+  unsigned* scratch = cs.blockSums + 64;
+  k_save_last<<<1, 1, 0, s>>>(a, n, last);
+  scan_rec(s, a, n, scratch);
+  k_finish_total<<<1, 1, 0, s>>>(a, n, last);
+}
+
+// ------------------------------------------------------------------------------------ radix sort
+// LSD radix sort, 8-bit digits, keys u64 with u32 payload; stable within each pass, so the whole
+// sort is stable.  Per pass: tile histograms -> exclusive scan (digit-major) -> ranked scatter.
+static const int RS_T = 256, RS_R = 8, RS_TILE = RS_T * RS_R;
+
+__global__ void k_rs_hist(const unsigned long long* keys, long long n, int shift, unsigned* hist, long long nTiles) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  long long base = (long long)blockIdx.x * RS_TILE;
+  for (int r = 0; r < RS_R; r++) {
+    long long idx = base + r * RS_T + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255], 1u);
+  }
+  __syncthreads();
+  hist[(long long)threadIdx.x * nTiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_rs_scatter(const unsigned long long* kin, const unsigned* vin, unsigned long long* kout,
+                             unsigned* vout, long long n, int shift, const unsigned* hist, long long nTiles) {
+  __shared__ unsigned wc[RS_T / 32][256];
+  __shared__ unsigned runBase[256];
+  __shared__ unsigned gOff[256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  gOff[threadIdx.x] = hist[(long long)threadIdx.x * nTiles + blockIdx.x];
+  runBase[threadIdx.x] = 0;
+  long long base = (long long)blockIdx.x * RS_TILE;
+  for (int r = 0; r < RS_R; r++) {
+    for (int w = 0; w < RS_T / 32; w++) wc[w][threadIdx.x] = 0;
+    __syncthreads();
+    long long idx = base + r * RS_T + threadIdx.x;
+    bool valid = idx < n;
+    unsigned long long k = valid ? kin[idx] : 0;
+    unsigned v = valid ? vin[idx] : 0;
+    unsigned d = valid ? (unsigned)((k >> shift) & 255) : 256u + lane;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    unsigned rankInWarp = __popc(peers & ((1u << lane) - 1));
+    int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) wc[warp][d] = __popc(peers);
+    __syncthreads();
+    // per digit: exclusive prefix over warps, then advance the running base
+    {
+      unsigned dsum = 0;
+      for (int w = 0; w < RS_T / 32; w++) { unsigned c = wc[w][threadIdx.x]; wc[w][threadIdx.x] = dsum; dsum += c; }
+      // store the round total temporarily in runBase after use below
+      __syncthreads();
+      if (valid) {
+        unsigned pos = gOff[d] + runBase[d] + wc[warp][d] + rankInWarp;
+        kout[pos] = k;
+        vout[pos] = v;
+      }
+      __syncthreads();
+      runBase[threadIdx.x] += dsum;
+    }
+    __syncthreads();
+  }
+}
+
+static void radix_sort(cudaStream_t s, unsigned long long*& keys, unsigned*& vals, unsigned long long*& keysAlt,
+                       unsigned*& valsAlt, long long n, int bits, ColliderScratch& cs) {
+  if (n <= 1) return;
+  long long nTiles = (n + RS_TILE - 1) / RS_TILE;
+  for (int shift = 0; shift < bits; shift += 8) {
+    k_rs_hist<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, n, shift, cs.hist, nTiles);
+    exclusive_scan_u32(s, cs.hist, 256 * nTiles, cs);
+    k_rs_scatter<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, vals, keysAlt, valsAlt, n, shift, cs.hist, nTiles);
+    unsigned long long* tk = keys; keys = keysAlt; keysAlt = tk;
+    unsigned* tv = vals; vals = valsAlt; valsAlt = tv;
+  }
+}
+
+// ------------------------------------------------------------------------------------ sort small
+__global__ void k_cell_start(const unsigned long long* keys, int nSmall, const GridParams* g, int* cellStart) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int ncols = g->ncx * g->ncy;
+  if (nSmall == 0) {
+    for (int k = s; k <= ncols; k += gridDim.x * blockDim.x) cellStart[k] = 0;
+    return;
+  }
+  if (s >= nSmall) return;
+  long long c = (long long)(keys[s] >> QBITS);
+  long long cp = s > 0 ? (long long)(keys[s - 1] >> QBITS) : -1;
+  for (long long k = cp + 1; k <= c; k++) cellStart[k] = s;
+  if (s == nSmall - 1)
+    for (long long k = c + 1; k <= ncols; k++) cellStart[k] = nSmall;
+}
+
+
+// ------------------------------------------------------------------------------------ sweep
+__device__ __forceinline__ bool overlap3(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2, const double4_32a& mx2) {
+  return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+__device__ __forceinline__ bool mayCollide(unsigned m1, unsigned m2, unsigned lone) {
+  return (m1 & m2) != 0 && (m1 & m2 & lone) == 0;
+}
+// contact orientation: same shape -> (lower id, higher id); wall + sphere -> wall first
+__device__ __forceinline__ int2 orient(int i, int j, int shi, int shj) {
+  int a = min(i, j), b = max(i, j);
+  int sa = (a == i) ? shi : shj, sb = (a == i) ? shj : shi;
+  if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) { int t = a; a = b; b = t; }
+  return make_int2(a, b);
+}
+
+struct SweepArgs {
+  const unsigned long long* keys;
+  const unsigned* vals;
+  const int* cellStart;
+  const int* large;
+  int nLarge;
+  int nSmall;
+  unsigned loneMask;
+};
+
+template <bool WRITE>
+__global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned* counts, int2* out, long long cap,
+                        DeviceStatus* st) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > A.nSmall) return;
+  unsigned cnt = 0;
+  unsigned long long base = WRITE ? counts[s] : 0;
+  if (s == A.nSmall) {
+    // large-large pairs
+    for (int a = 0; a < A.nLarge; a++)
+      for (int b = a + 1; b < A.nLarge; b++) {
+        int i = A.large[a], j = A.large[b];
+        int4 mi = p.meta[i], mj = p.meta[j];
+        if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
+        if (!overlap3(p.bbmin[i], p.bbmax[i], p.bbmin[j], p.bbmax[j])) continue;
+        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
+        cnt++;
+      }
+    if (!WRITE) counts[s] = cnt;
+    return;
+  }
+  GridParams G = *g;
+  unsigned long long key = A.keys[s];
+  int i = (int)A.vals[s];
+  int4 mi = p.meta[i];
+  double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+  unsigned qi = (unsigned)(key & QMAX);
+  unsigned qmax = quant(cmp3(mx, G.sweepAxis), G);
+  long long col = (long long)(key >> QBITS);
+  int cx = (int)(col % G.ncx), cy = (int)(col / G.ncx);
+  for (int dy = -1; dy <= 1; dy++) {
+    int y = cy + dy;
+    if (y < 0 || y >= G.ncy) continue;
+    for (int dx = -1; dx <= 1; dx++) {
+      int x = cx + dx;
+      if (x < 0 || x >= G.ncx) continue;
+      long long c2 = (long long)x + (long long)G.ncx * y;
+      int beg = A.cellStart[c2], end = A.cellStart[c2 + 1];
+      int q;
+      if (c2 == col) q = s + 1;
+      else {
+        unsigned long long target = ((unsigned long long)c2 << QBITS) | qi;
+        int lo = beg, hi = end;
+        while (lo < hi) { int mid = (lo + hi) >> 1; if (A.keys[mid] < target) lo = mid + 1; else hi = mid; }
+        q = lo;
+        while (q < end && A.keys[q] == target && (int)A.vals[q] < i) q++;
+      }
+      for (; q < end; q++) {
+        unsigned long long kq = A.keys[q];
+        if ((unsigned)(kq & QMAX) > qmax) break;
+        int j = (int)A.vals[q];
+        int4 mj = p.meta[j];
+        if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
+        if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
+        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
+        cnt++;
+      }
+    }
+  }
+  for (int a = 0; a < A.nLarge; a++) {
+    int j = A.large[a];
+    int4 mj = p.meta[j];
+    if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
+    if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
+    if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
+    cnt++;
+  }
+  if (!WRITE) counts[s] = cnt;
+}
+
+// ------------------------------------------------------------------------------------ retain
+// Real contacts whose new boxes no longer overlap stay in the container (the reference collider
+// removes only non-real contacts on separation, InsertionSortCollider.cpp:107-110).
+__global__ void k_retain_flag(Particles p, Contacts old, long long nOld, unsigned* flag) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nOld) return;
+  unsigned f = 0;
+  if (old.state[c] == CS_REAL) {
+    int2 id = old.ids[c];
+    if (!overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y])) f = 1;
+  }
+  flag[c] = f;
+}
+__global__ void k_retain_write(Contacts old, long long nOld, const unsigned* flagScan, int2* out, long long base, long long cap) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nOld) return;
+  if (flagScan[c + 1] != flagScan[c]) {
+    long long o = base + flagScan[c];
+    if (o < cap) out[o] = old.ids[c];
+  }
+}
+
+// ------------------------------------------------------------------------------------ hash table
+__device__ __forceinline__ unsigned long long pairKey(int a, int b) {
+  unsigned lo = (unsigned)min(a, b), hi = (unsigned)max(a, b);
+  return ((unsigned long long)lo << 32) | hi;
+}
+// 64-bit finaliser of MurmurHash3 (Appleby), a published bit mixer
+__device__ __forceinline__ unsigned long long hmix(unsigned long long k) {
+  k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+  return k;
+}
+__global__ void k_hash_clear(unsigned long long* hk, unsigned long long cap) {
+  unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cap) hk[i] = HASH_EMPTY;
+}
+__global__ void k_hash_insert(const int2* ids, long long n, unsigned long long* hk, unsigned* hv, unsigned long long cap,
+                              DeviceStatus* st) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int2 id = ids[c];
+  unsigned long long key = pairKey(id.x, id.y);
+  unsigned long long pos = hmix(key) & (cap - 1);
+  for (unsigned long long probe = 0; probe < cap; probe++) {
+    unsigned long long prev = atomicCAS(&hk[pos], HASH_EMPTY, key);
+    if (prev == HASH_EMPTY || prev == key) { hv[pos] = (unsigned)c; return; }
+    pos = (pos + 1) & (cap - 1);
+  }
+  atomicCAS(&st->code, 0, WDEM_ERR_OVERFLOW);
+}
+__device__ __forceinline__ long long hashFind(const unsigned long long* hk, const unsigned* hv, unsigned long long cap,
+                                              unsigned long long key) {
+  if (cap == 0) return -1;
+  unsigned long long pos = hmix(key) & (cap - 1);
+  for (unsigned long long probe = 0; probe < cap; probe++) {
+    unsigned long long k = hk[pos];
+    if (k == key) return (long long)hv[pos];
+    if (k == HASH_EMPTY) return -1;
+    pos = (pos + 1) & (cap - 1);
+  }
+  return -1;
+}
+
+void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
+                       unsigned long long cap, DeviceStatus* st) {
+  if (cap == 0) return;
+  k_hash_clear<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(hk, cap);
+  if (n > 0) k_hash_insert<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ids, n, hk, hv, cap, st);
+}
+
+// ------------------------------------------------------------------------------------ carry-over
+// History of pairs already in the container is copied; new pairs start as potential contacts
+// created in this step (InsertionSortCollider.hpp:106-113 stepCreated=scene->step).  A contact that
+// the law broke in the previous step (pending) becomes potential: removePending in a full run keeps
+// it only when its new boxes overlap, which holds for every pair the sweep emitted.
+__global__ void k_carry(Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
+                        unsigned long long cap, long long step, int nHist) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nNew) return;
+  int2 id = neu.ids[c];
+  long long j = hashFind(hk, hv, cap, pairKey(id.x, id.y));
+  uint8_t st = CS_POTENTIAL;
+  if (j >= 0) {
+    uint8_t os = old.state[j];
+    if (os == CS_DEAD) j = -1;
+    else st = (os == CS_REAL) ? CS_REAL : CS_POTENTIAL;
+  }
+  if (j < 0) {
+    neu.state[c] = CS_POTENTIAL;
+    neu.step0[c] = (int)step;
+    return;
+  }
+  neu.ids[c] = old.ids[j];  // keep the stored orientation
+  neu.state[c] = st;
+  neu.step0[c] = old.step0[j];
+  if (st == CS_REAL) {
+    for (int h = 0; h < nHist; h++) neu.hist[h][c] = old.hist[h][j];
+    neu.tanPhi[c] = old.tanPhi[j];
+  }
+}
+
+// ------------------------------------------------------------------------------------ CSR
+__global__ void k_csr_entries(Contacts c, long long nc, int idBits, unsigned long long* keys, unsigned* vals) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nc) return;
+  int2 id = c.ids[e];
+  keys[2 * e] = ((unsigned long long)(unsigned)id.x << idBits) | (unsigned)id.y;
+  vals[2 * e] = (unsigned)e;
+  keys[2 * e + 1] = ((unsigned long long)(unsigned)id.y << idBits) | (unsigned)id.x;
+  vals[2 * e + 1] = (unsigned)e | 0x80000000u;
+}
+__global__ void k_csr_rows(const unsigned long long* keys, long long ne, int idBits, int n, int* rowptr) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) {
+    if (ne == 0 && e <= n) rowptr[e] = 0;
+    return;
+  }
+  long long r = (long long)(keys[e] >> idBits);
+  long long rp = e > 0 ? (long long)(keys[e - 1] >> idBits) : -1;
+  for (long long k = rp + 1; k <= r; k++) rowptr[k] = (int)e;
+  if (e == ne - 1)
+    for (long long k = r + 1; k <= n; k++) rowptr[k] = (int)ne;
+}
+
+}  // namespace wdem
+
+// ============================================================================== host orchestration
+namespace wdem {
+
+
+static int bitsFor(unsigned long long v) { int b = 0; while ((1ull << b) < v) b++; return b < 1 ? 1 : b; }
+
+// The collider sub-steps are called from wdem_api.cu through these thin wrappers.
+void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
+  unsigned long long* ext = (unsigned long long*)cs.temp;
+  k_extents_init<<<1, 32, 0, s>>>(ext);
+  if (nSmall > 0) k_extents<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, ext);
+  k_grid_setup<<<1, 1, 0, s>>>(ext, nSmall, cs.maxCols, cs.grid);
+}
+
+void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
+  if (nSmall > 0) k_make_keys<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, cs.grid, cs.keys, cs.vals);
+  int bits = QBITS + bitsFor((unsigned long long)cs.maxCols + 1);
+  radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bits, cs);
+  int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
+  k_cell_start<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.grid, cs.cellStart);
+}
+
+void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out, long long cap,
+               bool write, DeviceStatus* st) {
+  SweepArgs A;
+  A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
+  A.nSmall = nSmall; A.loneMask = loneMask;
+  int threads = nSmall + 1;
+  if (write) k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st);
+  else k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st);
+}
+
+void col_retain_flags(cudaStream_t s, Particles p, Contacts old, long long nOld, ColliderScratch& cs) {
+  if (nOld > 0) k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(p, old, nOld, cs.retainFlag);
+  exclusive_scan_u32(s, cs.retainFlag, nOld, cs);
+}
+void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base, long long cap) {
+  if (nOld > 0) k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap);
+}
+
+void col_carry(cudaStream_t s, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
+               unsigned long long cap, long long step, int nHist) {
+  if (nNew > 0) k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(neu, nNew, old, hk, hv, cap, step, nHist);
+}
+
+void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs) {
+  int idBits = bitsFor((unsigned long long)n + 1);
+  long long ne = 2 * nc;
+  if (nc > 0) k_csr_entries<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(c, nc, idBits, cs.keys, cs.vals);
+  radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, ne, 2 * idBits, cs);
+  long long threads = ne > 0 ? ne : (long long)n + 1;
+  k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr);
+  if (ne > 0) cudaMemcpyAsync(csr.ent, cs.vals, ne * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace wdem

@@ -1,0 +1,345 @@
+// k_contact.cu -- fused contact kernel: the GB300 replacement of one pass of Woo's ContactLoop
+// (src/dem/ContactLoop.cpp:93-268) with the functors
+//   Cg2_Sphere_Sphere_L6Geom (src/dem/Sphere.cpp:92-117), Cg2_Wall_Sphere_L6Geom (src/dem/Wall.cpp:50-84),
+//   Cg2_Any_Any_L6Geom__Base::handleSpheresLikeContact (src/dem/L6Geom.cpp:49-216),
+//   Cp2_FrictMat_FrictPhys (src/dem/FrictMat.cpp:20-44), Cp2_HertzMat_HertzPhys (src/dem/Hertz.cpp:34-77),
+//   Law2_L6Geom_FrictPhys_IdealElPl (src/dem/IdealElPl.cpp:15-125),
+//   Law2_L6Geom_HertzPhys_DMT, DMT branch (src/dem/Hertz.cpp:85-114,170-210),
+// and the force/torque branch of Contact::getForceTorqueBranch (src/dem/Contact.cpp:24-34).
+//
+// One thread per contact, contacts in SoA so every history load/store is coalesced.  Particle
+// state is gathered as 32-byte double4_32a records (position+radius, velocity+mass, angular velocity).
+// Instead of adding into particles under a mutex (DemData::addForceTorque, Particle.hpp:249) each
+// real contact writes its global force and the torques on both particles; the integrator sums them
+// per particle through the CSR in a fixed order.
+#include "wdem_internal.h"
+#include "wdem_math.cuh"
+#include "../../include/wdem.h"
+
+namespace wdem {
+
+__constant__ DevMaterial c_mats[MAX_MATERIALS];
+
+void upload_materials(const DevMaterial* m, int n) {
+  cudaMemcpyToSymbol(c_mats, m, sizeof(DevMaterial) * (n < MAX_MATERIALS ? n : MAX_MATERIALS));
+}
+
+__device__ __forceinline__ bool overlapBoxes(const double4_32a& mn1, const double4_32a& mx1, const double4_32a& mn2, const double4_32a& mx2) {
+  return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+
+__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }   // std::min
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }   // std::max
+
+// Physical constants of a new (or updated) contact, Cp2_*.  Writes tanPhi and, for FrictPhys,
+// kn/kt; for HertzPhys the constants kn0, kt0, alpha_sqrtMK, Fna used by the DMT law each step.
+template <int CP2>
+__device__ __forceinline__ void cp2(const StepParams& P, int matA, int matB, double r1, double r2, double massA,
+                                    double massB, double& kn, double& kt, double& tanPhi, double* hz) {
+  const DevMaterial m1 = c_mats[matA];
+  const DevMaterial m2 = c_mats[matB];
+  // L6Geom.lens and contA with iniLensTouch (L6Geom.cpp:61-68)
+  double l0 = fabs(r1), l1 = fabs(r2);
+  if (CP2 == WDEM_CP2_FRICT) {
+    const double rr = (r1 > 0 && r2 > 0) ? dmin(r1, r2) : (r1 > 0 ? r1 : r2);
+    const double A = M_PI * (rr * rr);
+    kn = 1 / (1 / (m1.young * A / l0) + 1 / (m2.young * A / l1));
+    kt = .5 * (m1.ktDivKn + m2.ktDivKn) * kn;
+    tanPhi = dmin(m1.tanPhi, m2.tanPhi);
+  } else {
+    const double nu1 = P.poisson, nu2 = P.poisson;
+    double K = (4 / 3.) * 1. / ((1 - nu1 * nu1) / m1.young + (1 - nu2 * nu2) / m2.young);
+    double R = 1. / (1. / l0 + 1. / l1);
+    double kn0 = K * sqrt(R);
+    double gamma = dmin(m1.surfEnergy, m2.surfEnergy);
+    double G1 = m1.young / (2 * (1 + nu1)), G2 = m2.young / (2 * (1 + nu2));
+    double G = .5 * (G1 + G2);
+    double nu = .5 * (nu1 + nu2);
+    double kt0 = 2 * sqrt(4 * R) * G / (2 - nu);
+    tanPhi = dmin(m1.tanPhi, m2.tanPhi);
+    double aSMK = 0.0;
+    if (P.en > 0 && P.en < 1.) {
+      double mbar = (massA <= 0 && massB > 0) ? massB : ((massA > 0 && massB <= 0) ? massA : (massA * massB) / (massA + massB));
+      aSMK = dmax(0., P.viscAlpha * sqrt(mbar * kn0));
+    }
+    hz[0] = kn0;
+    hz[1] = kt0;
+    hz[2] = aSMK;
+    hz[3] = 4 * M_PI * R * gamma;  // DMT adhesion force, constant per contact
+  }
+}
+
+template <int LAW, int CP2>
+__global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  uint8_t s = c.state[i];
+  if (s == CS_DEAD) return;
+  const int2 id = c.ids[i];
+  const int a = id.x, b = id.y;
+  const int4 ma = p.meta[a], mb = p.meta[b];
+  // no Cg2 functor for Wall+Wall: the pair stays a potential contact (ContactLoop.cpp:149-150)
+  if ((ma.x & 15) == WDEM_SHAPE_WALL && (mb.x & 15) == WDEM_SHAPE_WALL) return;
+  if (s == CS_PENDING) {
+    // removePending of this step's collider (no rebuild happened; a rebuild clears PENDING):
+    // drop the broken contact when the boxes of the last rebuild do not overlap.
+    if (!overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b])) { c.state[i] = CS_DEAD; return; }
+    s = CS_POTENTIAL;
+    c.state[i] = s;
+  }
+  const bool real = (s == CS_REAL);
+  const double4_32a A4 = p.posr[a], B4 = p.posr[b];
+  const d3 pos1 = xyz(A4), pos2 = xyz(B4);
+  const int shA = ma.x & 15;
+  double r1, r2, uN;
+  d3 normal, contPt;
+  if (shA == WDEM_SHAPE_SPHERE) {
+    // Cg2_Sphere_Sphere_L6Geom::go
+    r1 = A4.w; r2 = B4.w;
+    d3 relPos = pos2 - pos1;
+    double t = fabs(P.distFactor) * (r1 + r2);
+    double unDistSq = sqnorm(relPos) - t * t;
+    if (unDistSq > 0 && !real) return;
+    double dist = sqrt(sqnorm(relPos));
+    uN = dist - (r1 + r2);
+    normal = relPos / dist;
+    contPt = pos1 + (r1 + 0.5 * uN) * normal;
+  } else {
+    // Cg2_Wall_Sphere_L6Geom::go (pA is the wall)
+    const int ax = (ma.x >> 4) & 3, sense = ((ma.x >> 8) & 3) - 1;
+    const double radius = B4.w;
+    double dist = comp(pos2, ax) - comp(pos1, ax);
+    if (!real && fabs(dist) > radius) return;
+    contPt = pos2;
+    setComp(contPt, ax, comp(pos1, ax));
+    normal = mk(0, 0, 0);
+    double nax;
+    if (sense == 0) {
+      if (!real) nax = dist > 0 ? 1. : -1.;
+      else {
+        d3 prev0 = mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
+        nax = comp(prev0, ax);
+      }
+    } else nax = (sense == 1 ? 1. : -1);
+    setComp(normal, ax, nax);
+    uN = nax * dist - radius;
+    r1 = -radius; r2 = radius;
+  }
+
+  double fx, fy, fz, kn, kt, tanPhi;
+  double hz[4] = {0, 0, 0, 0};
+  d3 cur0, cur1, gvel, gangVel;
+  const double4_32a V1 = p.velm[a], V2 = p.velm[b];
+  const double4_32a W1 = p.angw[a], W2 = p.angw[b];
+  const d3 vel1 = xyz(V1), vel2 = xyz(V2), angVel1 = xyz(W1), angVel2 = xyz(W2);
+  if (!real) {
+    // new L6Geom: setInitialLocalCoords (L6Geom.cpp:25-36), node.pos = contPt
+    d3 locX = normal;
+    d3 e = fabs(locX.y) < fabs(locX.z) ? mk(0, 1, 0) : mk(0, 0, 1);
+    d3 locY = cross(locX, e);
+    locY = locY - locX * dot(locY, locX);
+    locY = normalized(locY);
+    cur0 = locX; cur1 = locY;
+    gvel = mk(0, 0, 0); gangVel = mk(0, 0, 0);
+    // new CPhys (ContactLoop.cpp:179-180)
+    cp2<CP2>(P, ma.y, mb.y, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
+    fx = 0; fy = 0; fz = 0;
+    c.step0[i] = (int)P.step;
+  } else {
+    // update (L6Geom.cpp:79-216)
+    const d3 prevNormal = mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
+    const d3 prevT1 = mk(c.hist[HIST_T1X][i], c.hist[HIST_T1Y][i], c.hist[HIST_T1Z][i]);
+    const d3 prevContPt = mk(c.hist[HIST_CX][i], c.hist[HIST_CY][i], c.hist[HIST_CZ][i]);
+    const double dt = P.dt;
+    const int am = P.approxMask;
+    const d3 currNormal = normal;
+    d3 normRotVec = cross(prevNormal, currNormal);
+    d3 midNormal = (am & 1) ? prevNormal : 0.5 * (prevNormal + currNormal);
+    if (sqnorm(midNormal) == 0) midNormal = currNormal;
+    else if (!(am & 2) && !(am & 1)) midNormal = normalized(midNormal);
+    d3 normTwistVec = midNormal * dt * 0.5 * dot(midNormal, angVel1 + angVel2);
+    d3 rt = normRotVec + normTwistVec;
+    d3 mid0, mid1;
+    if (am & 4) { mid0 = prevNormal; mid1 = prevT1; }
+    else { mid0 = midNormal; mid1 = prevT1 - cross(prevT1, rt) * 0.5; }
+    d3 mid2 = cross(mid0, mid1);
+    cur0 = currNormal;
+    cur1 = prevT1 - cross(mid1, rt);
+    if (P.trsfRenorm > 0 && (P.step % P.trsfRenorm) == 0) {
+      cur0 = normalized(cur0);
+      cur1 = cur1 - cur0 * dot(cur1, cur0);
+      cur1 = normalized(cur1);
+    }
+    d3 midContPt, midPos1, midPos2;
+    if (am & 8) { midContPt = contPt; midPos1 = pos1; midPos2 = pos2; }
+    else {
+      midContPt = 0.5 * (prevContPt + contPt);
+      midPos1 = pos1 - (dt * 0.5) * vel1;
+      midPos2 = pos2 - (dt * 0.5) * vel2;
+    }
+    d3 c1x = (P.noRatch && r1 > 0) ? r1 * midNormal : midContPt - midPos1;
+    d3 c2x = (P.noRatch && r2 > 0) ? (-r2) * midNormal : midContPt - midPos2;
+    d3 relVel = (vel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
+    gvel = mk(dot(mid0, relVel), dot(mid1, relVel), dot(mid2, relVel));
+    d3 dw = angVel2 - angVel1;
+    gangVel = mk(dot(mid0, dw), dot(mid1, dw), dot(mid2, dw));
+    fx = c.hist[HIST_FX][i]; fy = c.hist[HIST_FY][i]; fz = c.hist[HIST_FZ][i];
+    kn = c.hist[HIST_KN][i]; kt = c.hist[HIST_KT][i];
+    tanPhi = c.tanPhi[i];
+    if (CP2 == WDEM_CP2_HERTZ) { hz[0] = c.hist[HIST_E0][i]; hz[1] = c.hist[HIST_E1][i]; hz[2] = c.hist[HIST_E2][i]; hz[3] = c.hist[HIST_E3][i]; }
+    if (P.updatePhysNow) cp2<CP2>(P, ma.y, mb.y, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
+  }
+  const d3 cur2 = cross(cur0, cur1);
+
+  // ---- Law2
+  bool keep = true;
+  double tqx = 0, tqy = 0, tqz = 0;
+  const double dt = P.dt;
+  if (LAW == WDEM_LAW_IDEALELPL) {
+    if (uN > 0 && !P.noBreak) keep = false;
+    else {
+      fx = kn * uN;
+      if (P.noFrict || tanPhi == 0.) { fy = 0; fz = 0; }
+      else {
+        double sc = dt * kt;
+        fy = fy + sc * gvel.y;
+        fz = fz + sc * gvel.z;
+        double maxFt = fabs(fx) * tanPhi;
+        double ftSq = fy * fy + fz * fz;
+        if (ftSq > maxFt * maxFt && !P.noSlip) {
+          double FtNorm = sqrt(ftSq);
+          double ratio = maxFt / FtNorm;
+          if (FtNorm == 0.) ratio = 0.;
+          fy *= ratio; fz *= ratio;
+        }
+        // Eigen maxCoeff = maxi(maxi(f0,f1),f2) with maxi(a,b) = a<b ? b : a
+        double m01 = (fx < fy) ? fy : fx;
+        double mm = (m01 < fz) ? fz : m01;
+        if (isnan(mm)) { atomicCAS(&st->code, 0, WDEM_ERR_NAN); st->detail = a; }
+      }
+      if (P.relRollStiff > 0. && P.rollTanPhi > 0.) {
+        double charLen = fabs(r1) + fabs(r2);
+        double kr = kn * charLen;
+        double tq0 = 0, tq1 = 0, tq2 = 0;  // the law resets CPhys.torque first (IdealElPl.cpp:34)
+        if (P.relTwistStiff > 0) {
+          tq0 = tq0 + dt * P.relTwistStiff * kr * gangVel.x;
+          double maxTt = fabs(fx * P.rollTanPhi * charLen);
+          if (fabs(tq0) > maxTt) tq0 = copysign(maxTt, tq0);
+        }
+        double sr = dt * kr;
+        tq1 = tq1 + sr * gangVel.y;
+        tq2 = tq2 + sr * gangVel.z;
+        double maxTr = dmax(0., fabs(fx) * P.rollTanPhi * charLen);
+        double trSq = tq1 * tq1 + tq2 * tq2;
+        if (trSq > maxTr * maxTr) {
+          double TrNorm = sqrt(trSq);
+          double ratio = maxTr / TrNorm;
+          if (TrNorm == 0.) ratio = 0.;
+          tq1 *= ratio; tq2 *= ratio;
+        }
+        tqx = tq0; tqy = tq1; tqz = tq2;
+      }
+    }
+  } else {
+    const double velN = gvel.x;
+    const double kn0 = hz[0];
+    kn = (3 / 2.) * kn0 * sqrt(-uN);
+    if (uN > 0) keep = false;
+    else {
+      double Fne = -kn0 * pown3(sqrt(-uN));
+      double Fna = hz[3];
+      double eta = (hz[2] > 0 ? hz[2] * sqrt(sqrt(dmax(-uN, 0.))) : 0.);
+      double Fnv = eta * velN;
+      // HertzPhys.alpha = mean of the materials' alpha (Hertz.cpp:52); the clamp applies when it is 0
+      const double alphaC = .5 * (c_mats[ma.y].alpha + c_mats[mb.y].alpha);
+      if (alphaC == 0. && P.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
+      fx = Fne + Fna + Fnv;
+      kt = hz[1] * sqrt(uN < 0 ? -uN : 0);
+      double sc = dt * kt;
+      fy = fy + sc * gvel.y;
+      fz = fz + sc * gvel.z;
+      double maxFt = fabs(dmin(0., fx) * tanPhi);
+      double ftSq = fy * fy + fz * fz;
+      if (ftSq > maxFt * maxFt) {
+        double FtNorm = sqrt(ftSq);
+        double ratio = maxFt / FtNorm;
+        fy *= ratio; fz *= ratio;
+      } else {
+        fy = fy + eta * gvel.y;
+        fz = fz + eta * gvel.z;
+      }
+    }
+  }
+
+  if (!keep) {
+    // ContactContainer::requestRemoval: geom and phys dropped, collider decides in the next step
+    c.state[i] = CS_PENDING;
+    return;
+  }
+  // persistent history
+  c.state[i] = CS_REAL;
+  c.hist[HIST_T0X][i] = cur0.x; c.hist[HIST_T0Y][i] = cur0.y; c.hist[HIST_T0Z][i] = cur0.z;
+  c.hist[HIST_T1X][i] = cur1.x; c.hist[HIST_T1Y][i] = cur1.y; c.hist[HIST_T1Z][i] = cur1.z;
+  c.hist[HIST_CX][i] = contPt.x; c.hist[HIST_CY][i] = contPt.y; c.hist[HIST_CZ][i] = contPt.z;
+  c.hist[HIST_FX][i] = fx; c.hist[HIST_FY][i] = fy; c.hist[HIST_FZ][i] = fz;
+  c.hist[HIST_KN][i] = kn; c.hist[HIST_KT][i] = kt;
+  if (!real || P.updatePhysNow) {
+    c.tanPhi[i] = tanPhi;
+    if (CP2 == WDEM_CP2_HERTZ) { c.hist[HIST_E0][i] = hz[0]; c.hist[HIST_E1][i] = hz[1]; c.hist[HIST_E2][i] = hz[2]; c.hist[HIST_E3][i] = hz[3]; }
+  }
+  if (c.geom[0]) {
+    c.geom[0][i] = uN;
+    c.geom[1][i] = gvel.x; c.geom[2][i] = gvel.y; c.geom[3][i] = gvel.z;
+    c.geom[4][i] = gangVel.x; c.geom[5][i] = gangVel.y; c.geom[6][i] = gangVel.z;
+  }
+  // Contact::getForceTorqueBranch: F = ori*force, T = ori*torque (zero if torque is zero),
+  // branch xc = contPt - node pos; the particle receives F and xc x F + T (sign -1 for pB)
+  const qd ori = quatFromCols(cur0, cur1, cur2);
+  const d3 F = qrot(ori, mk(fx, fy, fz));
+  const d3 tq = mk(tqx, tqy, tqz);
+  const d3 T = isZero(tq) ? mk(0, 0, 0) : qrot(ori, tq);
+  const d3 xcA = contPt - pos1;
+  const d3 xcB = contPt - pos2;
+  const d3 TA = cross(xcA, F) + T;
+  const d3 FB = F * -1.0;
+  const d3 TB = cross(xcB, FB) + T * -1.0;
+  c.out[OUT_FX][i] = F.x; c.out[OUT_FY][i] = F.y; c.out[OUT_FZ][i] = F.z;
+  c.out[OUT_TAX][i] = TA.x; c.out[OUT_TAY][i] = TA.y; c.out[OUT_TAZ][i] = TA.z;
+  c.out[OUT_TBX][i] = TB.x; c.out[OUT_TBY][i] = TB.y; c.out[OUT_TBZ][i] = TB.z;
+}
+
+void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
+  if (nc <= 0) return;
+  unsigned blocks = (unsigned)((nc + 127) / 128);
+  if (P.law == WDEM_LAW_IDEALELPL) {
+    if (P.cp2 == WDEM_CP2_FRICT) k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
+    else k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
+  } else {
+    k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
+  }
+}
+
+}  // namespace wdem
+
+namespace wdem {
+
+// HertzPhys constants (kn0, kt0, alpha_sqrtMK, adhesion) of uploaded real contacts: Woo stores them
+// in HertzPhys (Hertz.hpp:16-31); they are pure functions of the materials, radii and masses.
+__global__ void k_init_uploaded(StepParams P, Particles p, Contacts c, long long nc) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc || c.state[i] != CS_REAL) return;
+  const int2 id = c.ids[i];
+  const int4 ma = p.meta[id.x], mb = p.meta[id.y];
+  const double rb = p.posr[id.y].w;
+  const double r1 = ((ma.x & 15) == WDEM_SHAPE_WALL) ? -rb : p.posr[id.x].w, r2 = rb;
+  double kn, kt, tanPhi, hz[4];
+  cp2<WDEM_CP2_HERTZ>(P, ma.y, mb.y, r1, r2, p.velm[id.x].w, p.velm[id.y].w, kn, kt, tanPhi, hz);
+  c.hist[HIST_E0][i] = hz[0]; c.hist[HIST_E1][i] = hz[1]; c.hist[HIST_E2][i] = hz[2]; c.hist[HIST_E3][i] = hz[3];
+}
+
+void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc) {
+  if (nc <= 0 || P.cp2 != WDEM_CP2_HERTZ) return;
+  k_init_uploaded<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(P, p, c, nc);
+}
+
+}  // namespace wdem

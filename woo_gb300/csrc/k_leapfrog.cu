@@ -1,0 +1,151 @@
+// k_leapfrog.cu -- fused integrator: the GB300 replacement of Woo's Leapfrog(reset=True)
+// (src/dem/Leapfrog.cpp:104-255) with ForceResetter folded in, the per-node force accumulation of
+// DemData::addForceTorque (src/dem/Particle.hpp:249) done as a deterministic CSR gather, and the
+// collider's verlet trigger AabbCollider::aabbIsDirty (src/dem/Collision.cpp:80-123).
+//
+// One thread per particle.  The force on a particle is m*g (reset at the end of the previous step)
+// plus the contributions of its real contacts, added in the order of the contacts' (min id, max id)
+// keys; that fixed order makes the sum deterministic and identical to the CPU oracle's.
+#include "wdem_internal.h"
+#include "wdem_math.cuh"
+#include "../../include/wdem.h"
+
+namespace wdem {
+
+// F = m g (unless gravitySkip) + sum of contact forces; T = sum of contact torques
+__device__ __forceinline__ void gatherForce(const StepParams& P, int i, double mass, unsigned flags, const Contacts& c,
+                                            const Csr& csr, d3& F, d3& T) {
+  const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
+  F = grav ? mk(mass * P.gravity[0], mass * P.gravity[1], mass * P.gravity[2]) : mk(0, 0, 0);
+  T = mk(0, 0, 0);
+  const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
+  for (int e = e0; e < e1; e++) {
+    const unsigned en = csr.ent[e];
+    const unsigned ci = en & 0x7fffffffu;
+    if (c.state[ci] != CS_REAL) continue;
+    const d3 f = mk(c.out[OUT_FX][ci], c.out[OUT_FY][ci], c.out[OUT_FZ][ci]);
+    if (en >> 31) {
+      F = F + f * -1.0;
+      T = T + mk(c.out[OUT_TBX][ci], c.out[OUT_TBY][ci], c.out[OUT_TBZ][ci]);
+    } else {
+      F = F + f;
+      T = T + mk(c.out[OUT_TAX][ci], c.out[OUT_TAY][ci], c.out[OUT_TAZ][ci]);
+    }
+  }
+}
+
+template <bool FROM_ARRAYS>
+__global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 meta = p.meta[i];
+  const unsigned flags = (unsigned)meta.w;
+  const double4_32a vm = p.velm[i];
+  const double mass = vm.w;
+  const bool blockedAll = (flags & 63u) == 63u;
+  const bool blockedNone = (flags & 63u) == 0u;
+  d3 F, T;
+  if (FROM_ARRAYS) {
+    F = xyz(p.force[i]);
+    T = xyz(p.torque[i]);
+  } else if (!blockedAll) {
+    gatherForce(P, i, mass, flags, c, csr, F, T);
+  } else {
+    // the force on a fully blocked node changes nothing in its motion; it is materialised only
+    // when downloaded (k_reduce_forces)
+    F = mk(0, 0, 0); T = mk(0, 0, 0);
+  }
+  const double dt = P.dt;
+  const double damping = P.damping;
+  const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
+  d3 vel = xyz(vm);
+  const double4_32a w4 = p.angw[i];
+  d3 angVel = xyz(w4);
+  const double4_32a pr = p.posr[i];
+  d3 pos = xyz(pr);
+  const d3 inertia = xyz(p.inert[i]);
+  if (!blockedAll) {
+    d3 linAccel;
+    if (blockedNone) linAccel = F / mass;
+    else {
+      linAccel = mk(0, 0, 0);
+      if (!(flags & 1u)) linAccel.x = linAccel.x + F.x / mass;
+      if (!(flags & 2u)) linAccel.y = linAccel.y + F.y / mass;
+      if (!(flags & 4u)) linAccel.z = linAccel.z + F.z / mass;
+    }
+    // nonviscDamp2nd (Leapfrog.cpp:33-35)
+    if (damp) {
+      const double hd = 0.5 * dt;
+      linAccel.x = linAccel.x * (1 - damping * signum(F.x * (vel.x + hd * linAccel.x)));
+      linAccel.y = linAccel.y * (1 - damping * signum(F.y * (vel.y + hd * linAccel.y)));
+      linAccel.z = linAccel.z * (1 - damping * signum(F.z * (vel.z + hd * linAccel.z)));
+    }
+    vel = vel + dt * linAccel;
+    if (!isZero(inertia)) {
+      d3 angAccel;
+      if (blockedNone) angAccel = mk(T.x / inertia.x, T.y / inertia.y, T.z / inertia.z);
+      else {
+        angAccel = mk(0, 0, 0);
+        if (!(flags & 8u)) angAccel.x = angAccel.x + T.x / inertia.x;
+        if (!(flags & 16u)) angAccel.y = angAccel.y + T.y / inertia.y;
+        if (!(flags & 32u)) angAccel.z = angAccel.z + T.z / inertia.z;
+      }
+      if (damp) {
+        const double hd = 0.5 * dt;
+        angAccel.x = angAccel.x * (1 - damping * signum(T.x * (angVel.x + hd * angAccel.x)));
+        angAccel.y = angAccel.y * (1 - damping * signum(T.y * (angVel.y + hd * angAccel.y)));
+        angAccel.z = angAccel.z * (1 - damping * signum(T.z * (angVel.z + hd * angAccel.z)));
+      }
+      angVel = angVel + dt * angAccel;
+    }
+  }
+  // leapfrogTranslate (:275-278)
+  pos = pos + vel * dt;
+  // leapfrogSphericalRotate (:280-297): q = AngleAxis(|w| dt, w/|w|) * q, normalised
+  double4_32a o4 = p.ori[i];
+  qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+  if (!isZero(angVel)) {
+    double angle = sqrt(sqnorm(angVel));
+    d3 axis = angVel / angle;
+    double ha = 0.5 * (angle * dt);
+    double sh, ch;
+    sincos(ha, &sh, &ch);
+    qd q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
+    ori = qmul(q, ori);
+  }
+  ori = qnormalized(ori);
+  p.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
+  p.velm[i] = make_double4_32a(vel.x, vel.y, vel.z, mass);
+  p.angw[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, w4.w);
+  p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+  // aabbIsDirty, run by the collider right after Leapfrog: moved^2 > verletDist^2
+  const double4_32a lp = p.lastPos[i];
+  const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
+  if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+}
+
+void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays, Contacts c, Csr csr,
+                     DeviceStatus* st) {
+  if (n <= 0) return;
+  unsigned blocks = (n + 255) / 256;
+  if (fromArrays) k_leapfrog<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  else k_leapfrog<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+}
+
+// DemData.force/torque as Woo holds them after ContactLoop (reset to m*g by Leapfrog, then contacts)
+__global__ void k_reduce_forces(StepParams P, Particles p, int n, Contacts c, Csr csr) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 meta = p.meta[i];
+  d3 F, T;
+  gatherForce(P, i, p.velm[i].w, (unsigned)meta.w, c, csr, F, T);
+  p.force[i] = make_double4_32a(F.x, F.y, F.z, 0);
+  p.torque[i] = make_double4_32a(T.x, T.y, T.z, 0);
+}
+
+void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr) {
+  if (n <= 0) return;
+  k_reduce_forces<<<(n + 127) / 128, 128, 0, s>>>(P, p, n, c, csr);
+}
+
+}  // namespace wdem

@@ -1,0 +1,904 @@
+// wdem_api.cu -- host runtime of the GB300 DEM engine and its C ABI (include/wdem.h).
+//
+// The handle owns all device memory and one CUDA stream.  One wdem_step runs, per step, the same
+// engine order as Woo's Scene::doOneStep with [Leapfrog, InsertionSortCollider, ContactLoop]
+// (src/core/Scene.cpp:420-427):
+//   1. k_leapfrog      forces gathered through the contact CSR, integration, verlet trigger
+//   2. collider        only when a particle left its verlet box (or after an upload): boxes, grid,
+//                      radix sort, sweep, hash-table carry-over of contact history, CSR
+//   3. k_contacts      fused Cg2 + Cp2 + Law2 over the contact list
+#include "wdem_internal.h"
+#include "../../include/wdem.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+using namespace wdem;
+
+namespace {
+
+const char* kPhaseNames[] = {"leapfrog", "collider", "contacts"};
+enum { PH_LEAPFROG = 0, PH_COLLIDER = 1, PH_CONTACTS = 2, PH_COUNT = 3 };
+
+struct ContactBuf {
+  Contacts c;
+  long long cap = 0;
+  bool hertz = false;
+  bool geom = false;
+};
+
+}  // namespace
+
+struct wdem_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int N = 0;   // capacity
+  int n = 0;   // particles
+  Particles d{};
+  // host copies of static per-particle data (radius, shape, material) for pWaveDt and checks
+  std::vector<int> shape, mat;
+  std::vector<double> radius;
+  std::vector<int> smallIds, largeIds;
+  int* dSmall = nullptr;
+  ContactBuf buf[2];
+  int cur = 0;
+  long long nContacts = 0;
+  Csr csr{};
+  long long csrCap = 0;
+  unsigned long long* hk[2] = {nullptr, nullptr};
+  unsigned* hv[2] = {nullptr, nullptr};
+  unsigned long long hcap[2] = {0, 0};
+  unsigned long long hallo[2] = {0, 0};
+  ColliderScratch cs{};
+  DeviceStatus* dst = nullptr;
+  DeviceStatus* hst = nullptr;  // pinned
+  unsigned* hcounts = nullptr;  // pinned, 4 entries
+  wdem_params raw{};
+  std::vector<wdem_material> mats;
+  StepParams P{};
+  bool paramsSet = false;
+  bool particlesSet = false;
+  bool forcesInArrays = true;
+  bool needRebuild = true;
+  bool keepGeom = false;
+  long long step = 0;
+  long long nFullRuns = 0;
+  int lastRunFull = 0;
+  int updatePhys = 0;
+  double verletDistResolved = 0;
+  bool verletResolved = false;
+  // timing
+  bool timing = false;
+  std::vector<cudaEvent_t> evPool;
+  size_t evUsed = 0;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> evMarks;  // phase, (start, stop) indices
+  double phaseMs[PH_COUNT] = {0, 0, 0};
+  int phaseLaunches[PH_COUNT] = {0, 0, 0};
+  std::string err;
+};
+
+namespace {
+
+int fail(wdem_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(h, WDEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T*& p, size_t count) {
+  if (p) { cudaFree(p); p = nullptr; }
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)&p, align256(count * sizeof(T)));
+}
+
+void freeContacts(ContactBuf& b) {
+  Contacts& c = b.c;
+  cudaFree(c.ids); cudaFree(c.state); cudaFree(c.step0); cudaFree(c.tanPhi);
+  for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
+  for (int k = 0; k < OUT_COUNT; k++) cudaFree(c.out[k]);
+  for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
+  memset(&c, 0, sizeof(c));
+  b.cap = 0;
+}
+
+// (Re)allocate one contact buffer for `cap` contacts, keeping nothing.
+cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom) {
+  freeContacts(b);
+  Contacts& c = b.c;
+  cudaError_t e;
+  if ((e = dalloc(c.ids, cap))) return e;
+  if ((e = dalloc(c.state, cap))) return e;
+  if ((e = dalloc(c.step0, cap))) return e;
+  if ((e = dalloc(c.tanPhi, cap))) return e;
+  int nh = hertz ? HIST_COUNT : HIST_FRICT;
+  for (int k = 0; k < nh; k++) if ((e = dalloc(c.hist[k], cap))) return e;
+  for (int k = 0; k < OUT_COUNT; k++) if ((e = dalloc(c.out[k], cap))) return e;
+  if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
+  b.cap = cap;
+  b.hertz = hertz;
+  b.geom = geom;
+  return cudaSuccess;
+}
+
+// Copy the first n contacts of src into dst (both device), used when a buffer grows in place.
+void copyContacts(cudaStream_t s, ContactBuf& dst, const ContactBuf& src, long long n) {
+  if (n <= 0) return;
+  cudaMemcpyAsync(dst.c.ids, src.c.ids, n * sizeof(int2), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst.c.state, src.c.state, n, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst.c.step0, src.c.step0, n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst.c.tanPhi, src.c.tanPhi, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  for (int k = 0; k < HIST_COUNT; k++)
+    if (dst.c.hist[k] && src.c.hist[k]) cudaMemcpyAsync(dst.c.hist[k], src.c.hist[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  for (int k = 0; k < OUT_COUNT; k++) cudaMemcpyAsync(dst.c.out[k], src.c.out[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+}
+
+unsigned long long nextPow2(unsigned long long v) {
+  unsigned long long p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+size_t evNext(wdem_handle* h) {
+  if (h->evUsed >= h->evPool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    h->evPool.push_back(e);
+  }
+  return h->evUsed++;
+}
+
+struct PhaseTimer {
+  wdem_handle* h;
+  int ph;
+  size_t a = 0;
+  PhaseTimer(wdem_handle* h_, int ph_) : h(h_), ph(ph_) {
+    if (h->timing) { a = evNext(h); cudaEventRecord(h->evPool[a], h->stream); }
+  }
+  ~PhaseTimer() {
+    if (h->timing) {
+      size_t b = evNext(h);
+      cudaEventRecord(h->evPool[b], h->stream);
+      h->evMarks.push_back(std::make_pair(ph, std::make_pair(a, b)));
+    }
+  }
+};
+
+void collectTimes(wdem_handle* h) {
+  if (!h->timing || h->evMarks.empty()) return;
+  cudaStreamSynchronize(h->stream);
+  for (auto& m : h->evMarks) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->evPool[m.second.first], h->evPool[m.second.second]);
+    h->phaseMs[m.first] += ms;
+    h->phaseLaunches[m.first] += 1;
+  }
+  h->evMarks.clear();
+  h->evUsed = 0;
+}
+
+// Scratch for the collider sized for nSmall particles and up to nc contacts.
+int ensureScratch(wdem_handle* h, long long nc) {
+  ColliderScratch& cs = h->cs;
+  long long needSort = std::max<long long>((long long)h->smallIds.size(), 2 * nc) + 16;
+  if (needSort > cs.sortCap) {
+    long long cap = std::max<long long>(needSort, cs.sortCap * 3 / 2);
+    CK(dalloc(cs.keys, cap)); CK(dalloc(cs.keysAlt, cap));
+    CK(dalloc(cs.vals, cap)); CK(dalloc(cs.valsAlt, cap));
+    cs.sortCap = cap;
+    long long tiles = (cap + 2047) / 2048;
+    cs.histCap = 256 * tiles + 1;
+    CK(dalloc(cs.hist, cs.histCap));
+  }
+  long long needRetain = std::max<long long>(h->nContacts, nc) + 2;
+  if (needRetain > cs.retainCap) {
+    long long cap = std::max<long long>(needRetain, cs.retainCap * 3 / 2);
+    CK(dalloc(cs.retainFlag, cap));
+    cs.retainCap = cap;
+  }
+  // scan scratch: level sums of the longest scan (histograms, pair counts, retain flags)
+  long long longest = std::max<long long>(std::max<long long>(cs.histCap, (long long)h->N + 2), cs.retainCap);
+  long long needSums = 64 + 2 * (longest / 1024 + 64) + 4096;
+  if (needSums > cs.blockSumsCap) {
+    CK(dalloc(cs.blockSums, needSums));
+    cs.blockSumsCap = needSums;
+  }
+  return WDEM_OK;
+}
+
+int ensureHash(wdem_handle* h, int side, long long n) {
+  unsigned long long cap = nextPow2(std::max<unsigned long long>(1024, 2ull * (unsigned long long)n));
+  if (cap > h->hallo[side]) {
+    CK(dalloc(h->hk[side], cap));
+    CK(dalloc(h->hv[side], cap));
+    h->hallo[side] = cap;
+  }
+  h->hcap[side] = cap;
+  return WDEM_OK;
+}
+
+int ensureCsr(wdem_handle* h, long long nc) {
+  if (2 * nc + 1 > h->csrCap) {
+    long long cap = std::max<long long>(2 * nc + 1, h->csrCap * 3 / 2);
+    CK(dalloc(h->csr.ent, cap));
+    h->csrCap = cap;
+  }
+  return WDEM_OK;
+}
+
+int checkDeviceStatus(wdem_handle* h) {
+  if (h->hst->code != 0) {
+    int code = h->hst->code;
+    std::string m;
+    if (code == WDEM_ERR_NAN) m = "NaN force in contact (particle #" + std::to_string(h->hst->detail) + ")";
+    else if (code == WDEM_ERR_OVERFLOW) m = "contact hash table overflow";
+    else m = "device error " + std::to_string(code);
+    return fail(h, code, m);
+  }
+  return WDEM_OK;
+}
+
+// Collider rebuild: InsertionSortCollider full run (InsertionSortCollider.cpp:407-612).
+int rebuild(wdem_handle* h) {
+  cudaStream_t s = h->stream;
+  const int n = h->n;
+  const int nSmall = (int)h->smallIds.size();
+  ColliderScratch& cs = h->cs;
+  int rc;
+  if ((rc = ensureScratch(h, h->nContacts))) return rc;
+  launch_bboxes(s, h->P, h->d, n);
+  col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
+  col_sort(s, h->d, h->dSmall, nSmall, cs);
+  col_sweep(s, h->d, nSmall, h->P.loneMask, cs, nullptr, 0, false, h->dst);
+  exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
+  ContactBuf& old = h->buf[h->cur];
+  ContactBuf& neu = h->buf[1 - h->cur];
+  const long long nOld = h->nContacts;
+  col_retain_flags(s, h->d, old.c, nOld, cs);
+  CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&h->hcounts[1], cs.retainFlag + nOld, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const long long total = h->hcounts[0];
+  const long long retained = h->hcounts[1];
+  const long long nNew = total + retained;
+  const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
+  if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom) {
+    long long cap = std::max<long long>(nNew + nNew / 4 + 1024, neu.cap);
+    CK(allocContacts(neu, cap, hertz, h->keepGeom));
+  }
+  col_sweep(s, h->d, nSmall, h->P.loneMask, cs, neu.c.ids, neu.cap, true, h->dst);
+  col_retain_write(s, old.c, nOld, cs, neu.c.ids, total, neu.cap);
+  const int side = 1 - h->cur;
+  if ((rc = ensureHash(h, side, nNew))) return rc;
+  launch_hash_build(s, neu.c.ids, nNew, h->hk[side], h->hv[side], h->hcap[side], h->dst);
+  col_carry(s, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
+            hertz ? HIST_COUNT : HIST_FRICT);
+  if ((rc = ensureScratch(h, nNew))) return rc;
+  if ((rc = ensureCsr(h, nNew))) return rc;
+  col_csr(s, neu.c, nNew, n, h->csr, cs);
+  h->cur = side;
+  h->nContacts = nNew;
+  h->nFullRuns++;
+  h->needRebuild = false;
+  return WDEM_OK;
+}
+
+void fillStepParams(wdem_handle* h) {
+  const wdem_params& r = h->raw;
+  StepParams& P = h->P;
+  P.dt = r.dt;
+  P.step = h->step;
+  for (int k = 0; k < 3; k++) P.gravity[k] = r.gravity[k];
+  P.hasGravity = !(r.gravity[0] == 0 && r.gravity[1] == 0 && r.gravity[2] == 0);
+  P.distFactor = r.distFactor;
+  P.bboxFactor = r.distFactor > 0 ? r.distFactor : 1.;
+  P.loneMask = r.loneMask;
+  P.damping = r.damping;
+  P.verletDist = h->verletDistResolved;
+  P.maxD2 = h->verletDistResolved * h->verletDistResolved;
+  P.noRatch = r.noRatch; P.iniLensTouch = r.iniLensTouch; P.trsfRenorm = r.trsfRenorm; P.approxMask = r.approxMask;
+  P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
+  P.cp2 = r.cp2; P.law = r.law;
+  P.noSlip = r.noSlip; P.noBreak = r.noBreak; P.noFrict = r.noFrict;
+  P.relRollStiff = r.relRollStiff; P.relTwistStiff = r.relTwistStiff; P.rollTanPhi = r.rollTanPhi;
+  P.noAttraction = r.noAttraction;
+  P.poisson = r.poisson; P.en = r.en;
+  // Cp2_HertzMat_HertzPhys (Hertz.cpp:70): the same for every contact, so evaluated once here
+  double en = r.en;
+  P.viscAlpha = (en > 0 && en < 1.) ? -std::sqrt(5) * std::log(en) / (std::sqrt(std::log(en) * std::log(en) + M_PI * M_PI)) : 0.;
+  P.trackEnergy = r.trackEnergy;
+  P.nMaterials = (int)h->mats.size();
+}
+
+// AabbCollider::setVerletDist (Collision.cpp:164-184): negative -> |verletDist| * min sphere radius
+void resolveVerlet(wdem_handle* h) {
+  double vd = h->raw.verletDist;
+  if (vd >= 0) { h->verletDistResolved = vd; return; }
+  double minR = std::numeric_limits<double>::infinity();
+  for (int i = 0; i < h->n; i++)
+    if (h->shape[i] == WDEM_SHAPE_SPHERE && !std::isnan(h->radius[i])) minR = std::min(h->radius[i], minR);
+  h->verletDistResolved = std::isinf(minR) ? 0.0 : std::abs(vd) * minR;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wdem_abi_version(void) { return WDEM_ABI_VERSION; }
+
+int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
+  if (!out || maxParticles <= 0) return WDEM_ERR_ARG;
+  *out = nullptr;
+  wdem_handle* h = new wdem_handle();
+  h->device = device;
+  h->N = maxParticles;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete h; return WDEM_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return WDEM_ERR_CUDA; }
+  int N = maxParticles;
+  Particles& d = h->d;
+  bool ok = true;
+  ok &= dalloc(d.posr, N) == cudaSuccess;
+  ok &= dalloc(d.velm, N) == cudaSuccess;
+  ok &= dalloc(d.angw, N) == cudaSuccess;
+  ok &= dalloc(d.inert, N) == cudaSuccess;
+  ok &= dalloc(d.ori, N) == cudaSuccess;
+  ok &= dalloc(d.lastPos, N) == cudaSuccess;
+  ok &= dalloc(d.bbmin, N) == cudaSuccess;
+  ok &= dalloc(d.bbmax, N) == cudaSuccess;
+  ok &= dalloc(d.force, N) == cudaSuccess;
+  ok &= dalloc(d.torque, N) == cudaSuccess;
+  ok &= dalloc(d.meta, N) == cudaSuccess;
+  ok &= dalloc(h->dSmall, N) == cudaSuccess;
+  ok &= dalloc(h->cs.large, N) == cudaSuccess;
+  ok &= dalloc(h->cs.counts, (size_t)N + 2) == cudaSuccess;
+  ok &= dalloc(h->cs.grid, 1) == cudaSuccess;
+  ok &= dalloc(h->csr.rowptr, (size_t)N + 1) == cudaSuccess;
+  ok &= dalloc(h->csr.cursor, (size_t)N) == cudaSuccess;
+  unsigned long long* tmp = nullptr;
+  ok &= dalloc(tmp, 64) == cudaSuccess;
+  h->cs.temp = tmp;
+  // column budget: enough for a fine grid without letting cellStart dominate memory
+  h->cs.maxCols = std::max(1024, std::min(1 << 24, 2 * N));
+  ok &= dalloc(h->cs.cellStart, (size_t)h->cs.maxCols + 2) == cudaSuccess;
+  ok &= dalloc(h->dst, 1) == cudaSuccess;
+  ok &= cudaMallocHost((void**)&h->hst, sizeof(DeviceStatus)) == cudaSuccess;
+  ok &= cudaMallocHost((void**)&h->hcounts, 4 * sizeof(unsigned)) == cudaSuccess;
+  if (!ok) { wdem_destroy(h); return WDEM_ERR_CUDA; }
+  cudaMemset(h->dst, 0, sizeof(DeviceStatus));
+  cudaMemset(h->csr.rowptr, 0, sizeof(int) * ((size_t)N + 1));
+  memset(h->hst, 0, sizeof(DeviceStatus));
+  // an empty contact buffer on the current side
+  if (allocContacts(h->buf[0], 1024, false, false) != cudaSuccess) { wdem_destroy(h); return WDEM_ERR_CUDA; }
+  if (ensureScratch(h, 0)) { wdem_destroy(h); return WDEM_ERR_CUDA; }
+  *out = h;
+  return WDEM_OK;
+}
+
+int wdem_destroy(wdem_handle* h) {
+  if (!h) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  Particles& d = h->d;
+  cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta);
+  cudaFree(h->dSmall);
+  freeContacts(h->buf[0]); freeContacts(h->buf[1]);
+  cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor);
+  for (int k = 0; k < 2; k++) { cudaFree(h->hk[k]); cudaFree(h->hv[k]); }
+  ColliderScratch& cs = h->cs;
+  cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
+  cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid);
+  cudaFree(cs.retainFlag); cudaFree(cs.temp);
+  cudaFree(h->dst);
+  if (h->hst) cudaFreeHost(h->hst);
+  if (h->hcounts) cudaFreeHost(h->hcounts);
+  for (auto e : h->evPool) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return WDEM_OK;
+}
+
+const char* wdem_last_error(wdem_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int wdem_set_params(wdem_handle* h, const wdem_params* p) {
+  if (!h || !p) return WDEM_ERR_ARG;
+  if (!p->reset) return fail(h, WDEM_ERR_UNSUPPORTED, "Leapfrog.reset=False is not supported (ForceResetter is folded into the GPU engine)");
+  if (p->iniEqlb) return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl.iniEqlb is not supported");
+  if (!p->iniLensTouch) return fail(h, WDEM_ERR_UNSUPPORTED, "Cg2_*_L6Geom.iniLensTouch=False is not supported");
+  if (!p->applyForces) return fail(h, WDEM_ERR_UNSUPPORTED, "ContactLoop.applyForces=False is not supported");
+  if (p->nMaterials <= 0 || !p->materials || p->nMaterials > MAX_MATERIALS) return fail(h, WDEM_ERR_ARG, "materials table missing or larger than 64");
+  if (p->law == WDEM_LAW_HERTZ_DMT && p->cp2 != WDEM_CP2_HERTZ)
+    return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT needs Cp2_HertzMat_HertzPhys");
+  if (p->law == WDEM_LAW_IDEALELPL && p->cp2 != WDEM_CP2_FRICT)
+    return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl is supported with Cp2_FrictMat_FrictPhys only");
+  if (p->cp2 == WDEM_CP2_HERTZ) {
+    for (int a = 0; a < p->nMaterials; a++)
+      for (int b = 0; b < p->nMaterials; b++) {
+        const wdem_material &m1 = p->materials[a], &m2 = p->materials[b];
+        double alpha = .5 * (m1.alpha + m2.alpha), gamma = std::min(m1.surfEnergy, m2.surfEnergy);
+        if (alpha != 0. && gamma != 0.)
+          return fail(h, WDEM_ERR_UNSUPPORTED, "Schwarz model of Law2_L6Geom_HertzPhys_DMT (alpha!=0 and surfEnergy!=0) is not supported");
+      }
+  }
+  if (h->paramsSet && h->nContacts > 0 && (p->cp2 != h->raw.cp2 || p->law != h->raw.law))
+    return fail(h, WDEM_ERR_STATE, "Cp2/Law2 functors cannot change while contacts exist; re-upload the particles");
+  bool updatePhysChanged = (h->raw.updatePhys != p->updatePhys) || !h->paramsSet;
+  h->raw = *p;
+  h->raw.materials = nullptr;
+  h->mats.assign(p->materials, p->materials + p->nMaterials);
+  h->step = p->step;
+  if (updatePhysChanged) h->updatePhys = p->updatePhys;
+  std::vector<DevMaterial> dm(h->mats.size());
+  for (size_t k = 0; k < h->mats.size(); k++) {
+    const wdem_material& m = h->mats[k];
+    dm[k].kind = m.kind; dm[k].density = m.density; dm[k].young = m.young; dm[k].ktDivKn = m.ktDivKn;
+    dm[k].tanPhi = m.tanPhi; dm[k].surfEnergy = m.surfEnergy; dm[k].alpha = m.alpha;
+  }
+  cudaSetDevice(h->device);
+  upload_materials(dm.data(), (int)dm.size());
+  if (h->particlesSet) resolveVerlet(h);
+  fillStepParams(h);
+  h->paramsSet = true;
+  return WDEM_OK;
+}
+
+int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
+  if (!h || !p) return WDEM_ERR_ARG;
+  if (p->n < 0 || p->n > h->N) return fail(h, WDEM_ERR_ARG, "particle count exceeds the handle capacity");
+  if (!p->shape || !p->radius || !p->material || !p->mask || !p->flags || !p->mass || !p->inertia || !p->pos || !p->ori ||
+      !p->vel || !p->angVel || !p->force || !p->torque)
+    return fail(h, WDEM_ERR_ARG, "null particle array");
+  const int n = p->n;
+  h->n = n;
+  h->shape.assign(p->shape, p->shape + n);
+  h->mat.assign(p->material, p->material + n);
+  h->radius.assign(p->radius, p->radius + n);
+  h->smallIds.clear(); h->largeIds.clear();
+  std::vector<double4_32a> posr(n), velm(n), angw(n), inert(n), ori(n), force(n), torque(n);
+  std::vector<int4> meta(n);
+  for (int i = 0; i < n; i++) {
+    int sh = p->shape[i];
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL) return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (p->material[i] < 0 || (h->paramsSet && p->material[i] >= (int)h->mats.size()))
+      return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
+    const double* in = p->inertia + 3 * i;
+    unsigned fl = p->flags[i];
+    if (fl & (WDEM_CLUMP_CLUMP | WDEM_CLUMP_CLUMPED)) return fail(h, WDEM_ERR_UNSUPPORTED, "clumps are not supported");
+    bool asph = !(in[0] == in[1] && in[1] == in[2]);
+    if (asph && (fl & 56u) != 56u) return fail(h, WDEM_ERR_UNSUPPORTED, "aspherical integration (unequal inertia) is not supported");
+    int ax = p->wallAxis ? p->wallAxis[i] : 0, sense = p->wallSense ? p->wallSense[i] : 0;
+    if (sh == WDEM_SHAPE_WALL && (ax < 0 || ax > 2 || sense < -1 || sense > 1)) return fail(h, WDEM_ERR_ARG, "bad wall axis/sense");
+    double r = sh == WDEM_SHAPE_SPHERE ? p->radius[i] : 0.0;
+    posr[i] = make_double4_32a(p->pos[3 * i], p->pos[3 * i + 1], p->pos[3 * i + 2], r);
+    velm[i] = make_double4_32a(p->vel[3 * i], p->vel[3 * i + 1], p->vel[3 * i + 2], p->mass[i]);
+    angw[i] = make_double4_32a(p->angVel[3 * i], p->angVel[3 * i + 1], p->angVel[3 * i + 2], 0);
+    inert[i] = make_double4_32a(in[0], in[1], in[2], 0);
+    ori[i] = make_double4_32a(p->ori[4 * i], p->ori[4 * i + 1], p->ori[4 * i + 2], p->ori[4 * i + 3]);
+    force[i] = make_double4_32a(p->force[3 * i], p->force[3 * i + 1], p->force[3 * i + 2], 0);
+    torque[i] = make_double4_32a(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2], 0);
+    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8), p->material[i], (int)p->mask[i], (int)fl);
+    if (sh == WDEM_SHAPE_SPHERE) h->smallIds.push_back(i); else h->largeIds.push_back(i);
+  }
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(h->d.posr, posr.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.velm, velm.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.angw, angw.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.inert, inert.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.ori, ori.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.force, force.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.torque, torque.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.meta, meta.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s));
+  }
+  if (!h->smallIds.empty())
+    CK(cudaMemcpyAsync(h->dSmall, h->smallIds.data(), h->smallIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (!h->largeIds.empty())
+    CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  h->cs.nLarge = (int)h->largeIds.size();
+  CK(cudaStreamSynchronize(s));
+  h->nContacts = 0;
+  h->forcesInArrays = true;
+  h->needRebuild = true;
+  h->particlesSet = true;
+  resolveVerlet(h);
+  fillStepParams(h);
+  return WDEM_OK;
+}
+
+int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
+  if (!h || !c) return WDEM_ERR_ARG;
+  if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "upload particles and params before contacts");
+  const long long nc = c->n;
+  if (nc < 0) return WDEM_ERR_ARG;
+  if (nc > 0 && (!c->idA || !c->idB || !c->real || !c->stepCreated)) return fail(h, WDEM_ERR_ARG, "null contact id/state array");
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
+  ContactBuf& b = h->buf[h->cur];
+  if (nc > b.cap || b.hertz != hertz || b.geom != h->keepGeom) CK(allocContacts(b, std::max<long long>(nc + 1024, 1024), hertz, h->keepGeom));
+  std::vector<int2> ids(nc);
+  std::vector<uint8_t> state(nc);
+  std::vector<int> step0(nc);
+  std::vector<double> hist[HIST_FRICT], tanPhi(nc, 0.0);
+  for (int k = 0; k < HIST_FRICT; k++) hist[k].assign(nc, 0.0);
+  for (long long i = 0; i < nc; i++) {
+    int a = c->idA[i], bb = c->idB[i];
+    if (a < 0 || a >= h->n || bb < 0 || bb >= h->n || a == bb) return fail(h, WDEM_ERR_ARG, "bad contact ids");
+    if (h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[bb] == WDEM_SHAPE_WALL) std::swap(a, bb);
+    ids[i] = make_int2(a, bb);
+    bool real = c->real[i] != 0;
+    state[i] = real ? CS_REAL : CS_POTENTIAL;
+    step0[i] = c->stepCreated[i];
+    if (real) {
+      if (!c->trsf || !c->contPt || !c->force || !c->kn || !c->kt || !c->tanPhi) return fail(h, WDEM_ERR_ARG, "real contact without history arrays");
+      for (int k = 0; k < 3; k++) { hist[HIST_T0X + k][i] = c->trsf[9 * i + k]; hist[HIST_T1X + k][i] = c->trsf[9 * i + 3 + k]; }
+      for (int k = 0; k < 3; k++) { hist[HIST_CX + k][i] = c->contPt[3 * i + k]; hist[HIST_FX + k][i] = c->force[3 * i + k]; }
+      hist[HIST_KN][i] = c->kn[i]; hist[HIST_KT][i] = c->kt[i];
+      tanPhi[i] = c->tanPhi[i];
+    }
+  }
+  if (nc > 0) {
+    CK(cudaMemcpyAsync(b.c.ids, ids.data(), nc * sizeof(int2), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.c.state, state.data(), nc, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.c.step0, step0.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.c.tanPhi, tanPhi.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < HIST_FRICT; k++) CK(cudaMemcpyAsync(b.c.hist[k], hist[k].data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  launch_init_uploaded(s, h->P, h->d, b.c, nc);
+  int rc;
+  if ((rc = ensureHash(h, h->cur, nc))) return rc;
+  launch_hash_build(s, b.c.ids, nc, h->hk[h->cur], h->hv[h->cur], h->hcap[h->cur], h->dst);
+  CK(cudaStreamSynchronize(s));
+  h->nContacts = nc;
+  h->needRebuild = true;
+  return WDEM_OK;
+}
+
+int wdem_step(wdem_handle* h, int32_t nSteps) {
+  if (!h || nSteps < 0) return WDEM_ERR_ARG;
+  if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "wdem_step before particles and params were set");
+  for (int i = 0; i < h->n; i++)
+    if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size())
+      return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  for (int k = 0; k < 3; k++) { h->phaseMs[k] = 0; h->phaseLaunches[k] = 0; }
+  h->evMarks.clear(); h->evUsed = 0;
+  for (int it = 0; it < nSteps; it++) {
+    h->P.step = h->step;
+    h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
+    {
+      PhaseTimer t(h, PH_LEAPFROG);
+      launch_leapfrog(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
+    }
+    h->forcesInArrays = false;
+    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int rc;
+    if ((rc = checkDeviceStatus(h))) return rc;
+    bool full = h->needRebuild || h->hst->dirty || h->verletDistResolved == 0;
+    h->lastRunFull = full;
+    if (full) {
+      CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
+      PhaseTimer t(h, PH_COLLIDER);
+      if ((rc = rebuild(h))) return rc;
+    }
+    {
+      PhaseTimer t(h, PH_CONTACTS);
+      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst);
+    }
+    if (h->updatePhys == WDEM_UPDATE_PHYS_ONCE) { h->updatePhys = WDEM_UPDATE_PHYS_NEVER; h->raw.updatePhys = WDEM_UPDATE_PHYS_NEVER; }
+    h->step++;
+    h->P.step = h->step;
+    h->raw.step = h->step;
+  }
+  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  collectTimes(h);
+  CK(cudaGetLastError());
+  return checkDeviceStatus(h);
+}
+
+int wdem_download_particles(wdem_handle* h, wdem_particles* p) {
+  if (!h || !p) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  const int n = std::min(h->n, p->n);
+  if (!h->forcesInArrays) {
+    launch_reduce_forces(s, h->P, h->d, h->n, h->buf[h->cur].c, h->csr);
+  }
+  std::vector<double4_32a> posr(n), velm(n), angw(n), ori(n), force(n), torque(n);
+  if (n > 0) {
+    CK(cudaMemcpyAsync(posr.data(), h->d.posr, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(velm.data(), h->d.velm, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(angw.data(), h->d.angw, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ori.data(), h->d.ori, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(force.data(), h->d.force, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(torque.data(), h->d.torque, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; i++) {
+    if (p->pos) { p->pos[3 * i] = posr[i].x; p->pos[3 * i + 1] = posr[i].y; p->pos[3 * i + 2] = posr[i].z; }
+    if (p->vel) { p->vel[3 * i] = velm[i].x; p->vel[3 * i + 1] = velm[i].y; p->vel[3 * i + 2] = velm[i].z; }
+    if (p->angVel) { p->angVel[3 * i] = angw[i].x; p->angVel[3 * i + 1] = angw[i].y; p->angVel[3 * i + 2] = angw[i].z; }
+    if (p->ori) { p->ori[4 * i] = ori[i].x; p->ori[4 * i + 1] = ori[i].y; p->ori[4 * i + 2] = ori[i].z; p->ori[4 * i + 3] = ori[i].w; }
+    if (p->force) { p->force[3 * i] = force[i].x; p->force[3 * i + 1] = force[i].y; p->force[3 * i + 2] = force[i].z; }
+    if (p->torque) { p->torque[3 * i] = torque[i].x; p->torque[3 * i + 1] = torque[i].y; p->torque[3 * i + 2] = torque[i].z; }
+  }
+  return WDEM_OK;
+}
+
+namespace {
+struct HostContacts {
+  std::vector<int2> ids;
+  std::vector<uint8_t> state;
+  std::vector<int> step0;
+  std::vector<double> hist[HIST_COUNT], tanPhi, geom[7];
+};
+int fetchContacts(wdem_handle* h, HostContacts& hc) {
+  cudaStream_t s = h->stream;
+  const long long nc = h->nContacts;
+  const ContactBuf& b = h->buf[h->cur];
+  hc.ids.resize(nc); hc.state.resize(nc); hc.step0.resize(nc); hc.tanPhi.resize(nc);
+  if (nc > 0) {
+    CK(cudaMemcpyAsync(hc.ids.data(), b.c.ids, nc * sizeof(int2), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hc.state.data(), b.c.state, nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hc.step0.data(), b.c.step0, nc * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hc.tanPhi.data(), b.c.tanPhi, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int nh = b.hertz ? HIST_COUNT : HIST_FRICT;
+    for (int k = 0; k < nh; k++) {
+      hc.hist[k].resize(nc);
+      CK(cudaMemcpyAsync(hc.hist[k].data(), b.c.hist[k], nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    if (b.geom)
+      for (int k = 0; k < 7; k++) {
+        hc.geom[k].resize(nc);
+        CK(cudaMemcpyAsync(hc.geom[k].data(), b.c.geom[k], nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+      }
+  }
+  CK(cudaStreamSynchronize(s));
+  return WDEM_OK;
+}
+// rotation matrix columns -> quaternion (same method as the device code)
+void quatFromColsHost(const double* c0, const double* c1, const double* c2, double* q) {
+  double m[3][3] = {{c0[0], c1[0], c2[0]}, {c0[1], c1[1], c2[1]}, {c0[2], c1[2], c2[2]}};
+  double t = m[0][0] + m[1][1] + m[2][2];
+  double w, v[3];
+  if (t > 0) {
+    t = std::sqrt(t + 1.0);
+    w = 0.5 * t;
+    t = 0.5 / t;
+    v[0] = (m[2][1] - m[1][2]) * t;
+    v[1] = (m[0][2] - m[2][0]) * t;
+    v[2] = (m[1][0] - m[0][1]) * t;
+  } else {
+    int i = 0;
+    if (m[1][1] > m[0][0]) i = 1;
+    if (m[2][2] > m[i][i]) i = 2;
+    int j = (i + 1) % 3, k = (j + 1) % 3;
+    t = std::sqrt(m[i][i] - m[j][j] - m[k][k] + 1.0);
+    v[i] = 0.5 * t;
+    t = 0.5 / t;
+    w = (m[k][j] - m[j][k]) * t;
+    v[j] = (m[j][i] + m[i][j]) * t;
+    v[k] = (m[k][i] + m[i][k]) * t;
+  }
+  q[0] = w; q[1] = v[0]; q[2] = v[1]; q[3] = v[2];
+}
+}  // namespace
+
+int wdem_contact_count(wdem_handle* h, int64_t* n) {
+  if (!h || !n) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  std::vector<uint8_t> st(h->nContacts);
+  if (h->nContacts > 0) {
+    CK(cudaMemcpy(st.data(), h->buf[h->cur].c.state, h->nContacts, cudaMemcpyDeviceToHost));
+  }
+  long long k = 0;
+  for (auto v : st) if (v != CS_DEAD) k++;
+  *n = k;
+  return WDEM_OK;
+}
+
+int wdem_download_contacts(wdem_handle* h, wdem_contacts* c) {
+  if (!h || !c) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  HostContacts hc;
+  int rc;
+  if ((rc = fetchContacts(h, hc))) return rc;
+  std::vector<long long> order;
+  for (long long i = 0; i < (long long)hc.ids.size(); i++) if (hc.state[i] != CS_DEAD) order.push_back(i);
+  auto key = [&](long long i) {
+    unsigned a = (unsigned)std::min(hc.ids[i].x, hc.ids[i].y), b = (unsigned)std::max(hc.ids[i].x, hc.ids[i].y);
+    return ((unsigned long long)a << 32) | b;
+  };
+  std::sort(order.begin(), order.end(), [&](long long x, long long y) { return key(x) < key(y); });
+  const bool hertz = h->buf[h->cur].hertz;
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (long long o = 0; o < (long long)order.size() && o < c->n; o++) {
+    long long i = order[o];
+    bool real = hc.state[i] == CS_REAL;
+    int a = hc.ids[i].x, b = hc.ids[i].y;
+    if (c->idA) c->idA[o] = a;
+    if (c->idB) c->idB[o] = b;
+    if (c->real) c->real[o] = real ? 1 : 0;
+    if (c->stepCreated) c->stepCreated[o] = hc.step0[i];
+    if (c->minDist00Sq) {
+      bool ss = h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[b] == WDEM_SHAPE_SPHERE;
+      double t = std::abs(h->raw.distFactor * (h->radius[a] + h->radius[b]));
+      c->minDist00Sq[o] = ss ? t * t : -1;
+    }
+    double c0[3], c1[3], c2[3];
+    if (real) {
+      for (int k = 0; k < 3; k++) { c0[k] = hc.hist[HIST_T0X + k][i]; c1[k] = hc.hist[HIST_T1X + k][i]; }
+      c2[0] = c0[1] * c1[2] - c0[2] * c1[1];
+      c2[1] = c0[2] * c1[0] - c0[0] * c1[2];
+      c2[2] = c0[0] * c1[1] - c0[1] * c1[0];
+    } else {
+      c0[0] = 1; c0[1] = 0; c0[2] = 0; c1[0] = 0; c1[1] = 1; c1[2] = 0; c2[0] = 0; c2[1] = 0; c2[2] = 1;
+    }
+    if (c->trsf) for (int k = 0; k < 3; k++) { c->trsf[9 * o + k] = c0[k]; c->trsf[9 * o + 3 + k] = c1[k]; c->trsf[9 * o + 6 + k] = c2[k]; }
+    if (c->geomOri) {
+      if (real) quatFromColsHost(c0, c1, c2, c->geomOri + 4 * o);
+      else { c->geomOri[4 * o] = 1; c->geomOri[4 * o + 1] = 0; c->geomOri[4 * o + 2] = 0; c->geomOri[4 * o + 3] = 0; }
+    }
+    if (c->contPt) for (int k = 0; k < 3; k++) c->contPt[3 * o + k] = real ? hc.hist[HIST_CX + k][i] : 0.0;
+    if (c->force) for (int k = 0; k < 3; k++) c->force[3 * o + k] = real ? hc.hist[HIST_FX + k][i] : 0.0;
+    if (c->torque) for (int k = 0; k < 3; k++) c->torque[3 * o + k] = 0.0;
+    if (c->kn) c->kn[o] = real ? hc.hist[HIST_KN][i] : nan;
+    if (c->kt) c->kt[o] = real ? hc.hist[HIST_KT][i] : nan;
+    if (c->tanPhi) c->tanPhi[o] = real ? hc.tanPhi[i] : nan;
+    bool g = !hc.geom[0].empty();
+    if (c->uN) c->uN[o] = (real && g) ? hc.geom[0][i] : nan;
+    if (c->geomVel) for (int k = 0; k < 3; k++) c->geomVel[3 * o + k] = (real && g) ? hc.geom[1 + k][i] : (real ? nan : 0.0);
+    if (c->geomAngVel) for (int k = 0; k < 3; k++) c->geomAngVel[3 * o + k] = (real && g) ? hc.geom[4 + k][i] : (real ? nan : 0.0);
+    (void)hertz;
+  }
+  return WDEM_OK;
+}
+
+int wdem_crit_dt(wdem_handle* h, double* dt) {
+  if (!h || !dt) return WDEM_ERR_ARG;
+  double r = std::numeric_limits<double>::infinity();
+  for (int i = 0; i < h->n; i++) {
+    if (h->shape[i] != WDEM_SHAPE_SPHERE) continue;
+    if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size()) return fail(h, WDEM_ERR_STATE, "materials not set");
+    const wdem_material& m = h->mats[h->mat[i]];
+    r = std::min(r, h->radius[i] / (1. * std::sqrt(m.young / m.density)));
+  }
+  *dt = r;
+  return WDEM_OK;
+}
+
+int wdem_get_energy(wdem_handle* h, double* e, int32_t n) {
+  if (!h || !e) return WDEM_ERR_ARG;
+  for (int k = 0; k < n; k++) e[k] = 0;
+  return fail(h, WDEM_ERR_UNSUPPORTED, "energy tracking is not implemented on the GPU engine");
+}
+int wdem_reset_energy(wdem_handle* h) { return h ? WDEM_OK : WDEM_ERR_ARG; }
+
+int wdem_get_status(wdem_handle* h, wdem_status* st) {
+  if (!h || !st) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  memset(st, 0, sizeof(*st));
+  st->code = h->hst->code;
+  st->detail = h->hst->detail;
+  st->step = h->step;
+  std::vector<uint8_t> s(h->nContacts);
+  if (h->nContacts > 0) CK(cudaMemcpy(s.data(), h->buf[h->cur].c.state, h->nContacts, cudaMemcpyDeviceToHost));
+  long long live = 0, real = 0;
+  for (auto v : s) { if (v != CS_DEAD) live++; if (v == CS_REAL) real++; }
+  st->nContacts = live;
+  st->nReal = real;
+  st->nFullRuns = h->nFullRuns;
+  st->capacity = h->buf[h->cur].cap;
+  st->lastRunFull = h->lastRunFull;
+  return WDEM_OK;
+}
+
+int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const double* maxs, const uint32_t* mask,
+                       uint32_t loneMask, int32_t* pairs, int64_t maxPairs, int64_t* nPairs) {
+  if (!h || !mins || !maxs || !mask || !nPairs || n < 0 || n > h->N) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  // Boxes go straight into the handle's box arrays; finite boxes are "small", others "large".
+  std::vector<double4_32a> mn(n), mx(n), posr(n);
+  std::vector<int4> meta(n);
+  h->smallIds.clear(); h->largeIds.clear();
+  h->shape.assign(n, WDEM_SHAPE_SPHERE);
+  h->radius.assign(n, 0.0);
+  h->mat.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    mn[i] = make_double4_32a(mins[3 * i], mins[3 * i + 1], mins[3 * i + 2], 0);
+    mx[i] = make_double4_32a(maxs[3 * i], maxs[3 * i + 1], maxs[3 * i + 2], 0);
+    bool finite = true;
+    for (int k = 0; k < 3; k++) finite &= std::isfinite(mins[3 * i + k]) && std::isfinite(maxs[3 * i + k]);
+    posr[i] = finite ? make_double4_32a(.5 * (mn[i].x + mx[i].x), .5 * (mn[i].y + mx[i].y), .5 * (mn[i].z + mx[i].z), 0)
+                     : make_double4_32a(0, 0, 0, 0);
+    meta[i] = make_int4(finite ? WDEM_SHAPE_SPHERE : WDEM_SHAPE_WALL, 0, (int)mask[i], 63);
+    if (finite) h->smallIds.push_back(i); else { h->largeIds.push_back(i); h->shape[i] = WDEM_SHAPE_WALL; }
+  }
+  h->n = n;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(h->d.bbmin, mn.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.bbmax, mx.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.posr, posr.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.meta, meta.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s));
+  }
+  if (!h->smallIds.empty()) CK(cudaMemcpyAsync(h->dSmall, h->smallIds.data(), h->smallIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (!h->largeIds.empty()) CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  h->cs.nLarge = (int)h->largeIds.size();
+  h->nContacts = 0;
+  int rc;
+  if ((rc = ensureScratch(h, 0))) return rc;
+  const int nSmall = (int)h->smallIds.size();
+  ColliderScratch& cs = h->cs;
+  col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
+  col_sort(s, h->d, h->dSmall, nSmall, cs);
+  col_sweep(s, h->d, nSmall, loneMask, cs, nullptr, 0, false, h->dst);
+  exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
+  CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  long long total = h->hcounts[0];
+  int2* dpairs = nullptr;
+  CK(dalloc(dpairs, (size_t)total + 1));
+  col_sweep(s, h->d, nSmall, loneMask, cs, dpairs, total, true, h->dst);
+  std::vector<int2> hp(total);
+  if (total > 0) CK(cudaMemcpyAsync(hp.data(), dpairs, total * sizeof(int2), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  cudaFree(dpairs);
+  std::vector<unsigned long long> keys(total);
+  for (long long i = 0; i < total; i++) {
+    unsigned a = (unsigned)std::min(hp[i].x, hp[i].y), b = (unsigned)std::max(hp[i].x, hp[i].y);
+    keys[i] = ((unsigned long long)a << 32) | b;
+  }
+  std::sort(keys.begin(), keys.end());
+  for (long long i = 0; i < total && i < maxPairs; i++) {
+    pairs[2 * i] = (int32_t)(keys[i] >> 32);
+    pairs[2 * i + 1] = (int32_t)(keys[i] & 0xffffffffu);
+  }
+  *nPairs = total;
+  h->particlesSet = false;  // the particle arrays no longer hold a scene
+  return WDEM_OK;
+}
+
+int wdem_set_timing(wdem_handle* h, int32_t enable) {
+  if (!h) return WDEM_ERR_ARG;
+  h->timing = enable != 0;
+  return WDEM_OK;
+}
+
+int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* launches, int32_t n, int32_t* count) {
+  if (!h || !count) return WDEM_ERR_ARG;
+  for (int k = 0; k < PH_COUNT && k < n; k++) {
+    if (names) names[k] = kPhaseNames[k];
+    if (ms) ms[k] = h->phaseMs[k];
+    if (launches) launches[k] = h->phaseLaunches[k];
+  }
+  *count = PH_COUNT;
+  return WDEM_OK;
+}
+
+/* Keep L6Geom.uN/vel/angVel of every real contact for download (off by default; tests turn it on). */
+int wdem_keep_geom(wdem_handle* h, int32_t enable) {
+  if (!h) return WDEM_ERR_ARG;
+  h->keepGeom = enable != 0;
+  return WDEM_OK;
+}
+
+}  // extern "C"

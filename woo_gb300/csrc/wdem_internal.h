@@ -1,0 +1,154 @@
+// wdem_internal.h -- device-side layout of the GB300 DEM engine and the launchers that the host
+// runtime (wdem_api.cu) calls.  Shared by the kernel translation units; not part of the C ABI.
+//
+// HBM layout (all arrays 256-byte aligned, structure-of-arrays):
+//   particles, capacity N:
+//     posr    double4_32a  (x, y, z, radius)            radius = 0 for walls
+//     velm    double4_32a  (vx, vy, vz, mass)
+//     angw    double4_32a  (wx, wy, wz, unused)
+//     inert   double4_32a  (ix, iy, iz, unused)
+//     ori     double4_32a  (w, x, y, z)
+//     meta    int4     (shape | wallAxis<<4 | (wallSense+1)<<8, material, mask, flags)
+//     lastPos double4_32a  position at the last collider rebuild (Aabb.nodeLastPos)
+//     bbmin, bbmax double4_32a  verlet-enlarged boxes of the last rebuild (minima/maxima)
+//     force, torque double4_32a  DemData.force/torque when materialised (upload, download)
+//   contacts, capacity C, double-buffered across collider rebuilds:
+//     ids     int2     (pA, pB)
+//     state   uint8    CS_POTENTIAL / CS_REAL / CS_PENDING / CS_DEAD
+//     step0   int32    Contact.stepCreated
+//     hist    double x 14 SoA: trsf col0 (3), trsf col1 (3), contPt (3), force (3, local), kn, kt
+//             (+4 for HertzPhys: kn0, kt0, alpha_sqrtMK, adhesion force)
+//     tanPhi  double
+//     out     double x 9 SoA: global force on pA (3), torque on pA (3), torque on pB (3)
+//   CSR over particles: rowptr[N+1], entries[2C] = contact index | (isB << 31), rows sorted
+//   by the partner's id key so that sums run in the order of the sorted contact keys.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wdem {
+
+enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
+enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
+       HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
+       HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
+       HIST_COUNT };
+enum { HIST_FRICT = HIST_E0 };  // FrictPhys contacts carry the first 14 history arrays
+enum { OUT_FX = 0, OUT_FY, OUT_FZ, OUT_TAX, OUT_TAY, OUT_TAZ, OUT_TBX, OUT_TBY, OUT_TBZ, OUT_COUNT };
+enum { MAX_MATERIALS = 64 };
+
+struct DevMaterial {
+  int kind;
+  double density, young, ktDivKn, tanPhi, surfEnergy, alpha;
+};
+
+// Engine + functor attributes as the kernels see them.
+struct StepParams {
+  double dt;
+  long long step;
+  double gravity[3];
+  int hasGravity;
+  double distFactor;        // DemField.distFactor
+  double bboxFactor;        // distFactor > 0 ? distFactor : 1  (Bo1_Sphere_Aabb)
+  unsigned loneMask;
+  double damping;
+  double verletDist;        // resolved, >= 0
+  double maxD2;             // verletDist^2
+  int noRatch, iniLensTouch, trsfRenorm, approxMask;
+  int updatePhysNow;        // Cp2 runs on existing contacts this step (updatePhys always/once)
+  int cp2, law;
+  int noSlip, noBreak, noFrict;
+  double relRollStiff, relTwistStiff, rollTanPhi;
+  int noAttraction;
+  double poisson, en, viscAlpha;  // viscAlpha from en, computed once on the host
+  int trackEnergy;
+  int nMaterials;
+};
+
+struct Particles {
+  double4_32a *posr, *velm, *angw, *inert, *ori, *lastPos, *bbmin, *bbmax, *force, *torque;
+  int4* meta;
+};
+
+struct Contacts {
+  int2* ids;
+  uint8_t* state;
+  int* step0;
+  double* hist[HIST_COUNT];
+  double* tanPhi;
+  double* out[OUT_COUNT];
+  double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
+};
+
+struct Csr {
+  int* rowptr;    // N+1
+  unsigned* ent;  // 2C
+  int* cursor;    // N (scratch for filling)
+};
+
+// Uniform-grid / sweep parameters computed on the device at each rebuild.
+struct GridParams {
+  int sweepAxis, ax1, ax2;
+  int ncx, ncy;
+  double lo1, lo2, cell;
+  double loS, invQ;  // quantisation along the sweep axis
+  int nSmall;        // spheres in the sort
+  int ok;
+};
+
+struct DeviceStatus {
+  int code;
+  int detail;
+  int dirty;          // set by the integrator when a particle left its verlet box
+  int overflow;
+  unsigned long long pairTotal;
+  double ext[12];     // box extents reduction scratch (as ordered ints)
+};
+
+// ---- launchers (k_leapfrog.cu) ----
+void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays,
+                     Contacts c, Csr csr, DeviceStatus* st);
+void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr);
+// ---- launchers (k_contact.cu) ----
+void upload_materials(const DevMaterial* m, int n);
+void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st);
+void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc);
+// ---- collider (k_collider.cu) ----
+struct ColliderScratch {
+  unsigned long long *keys, *keysAlt;   // sort keys (particles, then CSR entries)
+  unsigned *vals, *valsAlt;             // sort payloads
+  long long sortCap;                    // capacity of the four sort arrays
+  unsigned* hist;                       // radix histograms (+1 for the scan total)
+  long long histCap;
+  unsigned* blockSums;                  // scan scratch
+  long long blockSumsCap;
+  int* cellStart;                       // maxCols + 1
+  int maxCols;
+  unsigned* counts;                     // nSmall+2 pair counts per sorted particle, scanned in place
+  int* large;                           // ids of walls (unbounded boxes)
+  int nLarge;
+  GridParams* grid;
+  unsigned* retainFlag;                 // old contacts retained (scanned in place)
+  long long retainCap;
+  void* temp;                           // small scratch (extent reduction)
+};
+void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n);
+void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
+void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
+void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out,
+               long long cap, bool write, DeviceStatus* st);
+void col_retain_flags(cudaStream_t s, Particles p, Contacts old, long long nOld, ColliderScratch& cs);
+void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base,
+                      long long cap);
+void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
+                       unsigned long long cap, DeviceStatus* st);
+void col_carry(cudaStream_t s, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
+               const unsigned* hv, unsigned long long cap, long long step, int nHist);
+void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs);
+// exclusive scan of a[0..n) in place; a[n] receives the total (the array holds n+1 entries)
+void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs);
+int sort_passes_for(int nSmallBits);
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace wdem

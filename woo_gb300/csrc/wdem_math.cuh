@@ -1,0 +1,114 @@
+// wdem_math.cuh -- FP64 vector/quaternion helpers for the DEM kernels.
+//
+// Every helper performs the IEEE operations in the same order as Woo's Eigen expressions
+// (left-to-right; dot = (a0 b0 + a1 b1) + a2 b2), and the kernels are compiled with
+// --fmad=false, so per-contact results reproduce the CPU restatement bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace wdem {
+
+struct d3 { double x, y, z; };
+
+__device__ __forceinline__ d3 mk(double x, double y, double z) { d3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ d3 xyz(const double4_32a& v) { return mk(v.x, v.y, v.z); }
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ d3 operator-(d3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ d3 operator*(d3 a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ d3 operator*(double s, d3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ d3 operator/(d3 a, double s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double sqnorm(d3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ bool isZero(d3 a) { return a.x == 0 && a.y == 0 && a.z == 0; }
+__device__ __forceinline__ d3 normalized(d3 a) {
+  double z = sqnorm(a);
+  if (z > 0) { double n = sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
+  return a;
+}
+__device__ __forceinline__ double comp(d3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ void setComp(d3& a, int i, double v) { if (i == 0) a.x = v; else if (i == 1) a.y = v; else a.z = v; }
+
+struct qd { double w, x, y, z; };
+
+// Rotation matrix given by columns c0, c1, c2 -> unit quaternion (Shoemake: trace branch, else the
+// largest diagonal element).  m(r,k) = column k, row r.
+__device__ __forceinline__ qd quatFromCols(d3 c0, d3 c1, d3 c2) {
+  const double m00 = c0.x, m10 = c0.y, m20 = c0.z;
+  const double m01 = c1.x, m11 = c1.y, m21 = c1.z;
+  const double m02 = c2.x, m12 = c2.y, m22 = c2.z;
+  qd q;
+  double t = m00 + m11 + m22;
+  if (t > 0) {
+    t = sqrt(t + 1.0);
+    q.w = 0.5 * t;
+    t = 0.5 / t;
+    q.x = (m21 - m12) * t;
+    q.y = (m02 - m20) * t;
+    q.z = (m10 - m01) * t;
+  } else {
+    // largest diagonal element i, j = i+1, k = j+1 (mod 3), written out per case
+    int i = 0;
+    if (m11 > m00) i = 1;
+    if (m22 > (i == 0 ? m00 : m11)) i = 2;
+    if (i == 0) {         // j=1, k=2
+      t = sqrt(m00 - m11 - m22 + 1.0);
+      q.x = 0.5 * t; t = 0.5 / t;
+      q.w = (m21 - m12) * t; q.y = (m10 + m01) * t; q.z = (m20 + m02) * t;
+    } else if (i == 1) {  // j=2, k=0
+      t = sqrt(m11 - m22 - m00 + 1.0);
+      q.y = 0.5 * t; t = 0.5 / t;
+      q.w = (m02 - m20) * t; q.z = (m21 + m12) * t; q.x = (m01 + m10) * t;
+    } else {              // j=0, k=1
+      t = sqrt(m22 - m00 - m11 + 1.0);
+      q.z = 0.5 * t; t = 0.5 / t;
+      q.w = (m10 - m01) * t; q.x = (m02 + m20) * t; q.y = (m12 + m21) * t;
+    }
+  }
+  return q;
+}
+
+// v rotated by unit quaternion q: uv = q.vec x v; uv += uv; v + w uv + q.vec x uv
+__device__ __forceinline__ d3 qrot(qd q, d3 v) {
+  d3 qv = mk(q.x, q.y, q.z);
+  d3 uv = cross(qv, v);
+  uv = uv + uv;
+  return v + q.w * uv + cross(qv, uv);
+}
+
+__device__ __forceinline__ qd qmul(qd a, qd b) {
+  qd r;
+  r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+  r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+  r.y = a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z;
+  r.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
+  return r;
+}
+
+__device__ __forceinline__ qd qnormalized(qd q) {
+  double z2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+  if (z2 > 0) { double n = sqrt(z2); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+  return q;
+}
+
+__device__ __forceinline__ double signum(double f) { return f < 0 ? -1.0 : (f > 0 ? 1.0 : 0.0); }
+
+// x^n by squaring, n small and fixed (pown of Woo's Math.hpp)
+__device__ __forceinline__ double pown3(double x) {
+  // n=3: d=1, r=1 -> pown(x*x,1) * x ; pown(y,1): d=0,r=1 -> 1*y
+  double y = x * x;
+  double x2d = 1.0 * y;
+  return x2d * x;
+}
+__device__ __forceinline__ double pown5(double x) {
+  // n=5: d=2, r=1 -> pown(x*x,2)*x ; pown(y,2): d=1,r=0 -> pown(y*y,1)*1 = (1*(y*y))*1
+  double y = x * x;
+  double z = y * y;
+  double p2 = (1.0 * z) * 1.0;
+  return p2 * x;
+}
+
+}  // namespace wdem

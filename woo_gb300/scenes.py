@@ -1,0 +1,216 @@
+"""Seeded synthetic DEM scenes in the engine's SoA format.
+
+Each builder returns a SceneSpec: engine/functor attributes (abi.Params), the materials table and
+the particle arrays.  The benchmark scenes follow the configurations the engine is measured on:
+
+* spheres10k   -- 10,000 spheres r=5 mm, FrictMat (rho 3000, E 1e7, ktDivKn .2, tanPhi .5), random
+                  sequential addition in a 0.5 x 0.5 x 1.0 m box of 6 walls, gravity -9.81 z,
+                  Law2_L6Geom_FrictPhys_IdealElPl, Leapfrog damping .2, dt = 0.4 * p-wave dt.
+* hertz1M      -- 1,000,000 spheres r ~ U[2,6] mm, HertzMat E 5e7, tanPhi .3 / .6 (two materials),
+                  surfEnergy .01, Cp2_HertzMat_HertzPhys(en=.8), Law2_L6Geom_HertzPhys_DMT, a loose
+                  cloud falling into a 1 x 1 x 2 m walled box, dt = 0.3 * p-wave dt,
+                  verletDist = 0.1 * rmin.
+
+Masses and inertias follow Sphere::lumpMassInertia (src/dem/Sphere.cpp:26-33).
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+# DemField defaults (src/dem/Particle.hpp:334-361)
+DEFAULT_MOVABLE_MASK = 0b0101
+DEFAULT_BOUNDARY_MASK = 0b0011
+DEFAULT_LONE_MASK = 0b0010
+
+
+class SceneSpec:
+    def __init__(self, params, materials, particles, name="", info=None):
+        self.params = params
+        self.materials = materials      # ctypes array kept alive for params.materials
+        self.particles = particles
+        self.name = name
+        self.info = info or {}
+
+    def set_dt(self, dt):
+        self.params.dt = dt
+
+
+def materials_array(mats):
+    arr = (abi.Material * len(mats))()
+    for i, m in enumerate(mats):
+        arr[i].kind = m.get("kind", abi.MAT_FRICT)
+        arr[i].density = m.get("density", 1000.0)
+        arr[i].young = m.get("young", 1e9)
+        arr[i].ktDivKn = m.get("ktDivKn", 0.2)
+        arr[i].tanPhi = m.get("tanPhi", 0.5)
+        arr[i].surfEnergy = m.get("surfEnergy", 0.0)
+        arr[i].alpha = m.get("alpha", 0.0)
+    return arr
+
+
+def default_params(materials, **kw):
+    """abi.Params with the defaults of Woo's classes (Leapfrog, InsertionSortCollider, ContactLoop,
+    Cg2_Any_Any_L6Geom__Base, Cp2/Law2 functors, DemField)."""
+    p = abi.Params()
+    p.dt = kw.get("dt", float("nan"))
+    p.step = kw.get("step", 0)
+    g = kw.get("gravity", (0.0, 0.0, 0.0))
+    for k in range(3):
+        p.gravity[k] = g[k]
+    p.distFactor = kw.get("distFactor", -1.0)
+    p.loneMask = kw.get("loneMask", DEFAULT_LONE_MASK)
+    p.trackEnergy = kw.get("trackEnergy", 0)
+    p.damping = kw.get("damping", 0.2)
+    p.reset = 1
+    p.kinSplit = 0
+    p.verletDist = kw.get("verletDist", -0.05)
+    p.noRatch = kw.get("noRatch", 0)
+    p.iniLensTouch = 1
+    p.trsfRenorm = kw.get("trsfRenorm", 100)
+    p.approxMask = kw.get("approxMask", 0)
+    p.updatePhys = kw.get("updatePhys", abi.UPDATE_PHYS_NEVER)
+    p.applyForces = 1
+    p.dist00 = 1
+    p.cp2 = kw.get("cp2", abi.CP2_FRICT)
+    p.poisson = kw.get("poisson", 0.2)
+    p.en = kw.get("en", float("nan"))
+    p.law = kw.get("law", abi.LAW_IDEALELPL)
+    p.noSlip = kw.get("noSlip", 0)
+    p.noBreak = kw.get("noBreak", 0)
+    p.noFrict = kw.get("noFrict", 0)
+    p.iniEqlb = 0
+    p.relRollStiff = kw.get("relRollStiff", 0.0)
+    p.relTwistStiff = kw.get("relTwistStiff", 0.0)
+    p.rollTanPhi = kw.get("rollTanPhi", 0.0)
+    p.noAttraction = kw.get("noAttraction", 1)
+    p.nMaterials = len(materials)
+    p.materials = materials
+    return p
+
+
+def sphere_mass_inertia(radius, density):
+    """Sphere::lumpMassInertia: m = (4/3) pi r^3 rho, I = (2/5) m r^2 (elementwise, same op order)."""
+    r = np.asarray(radius, np.float64)
+    rho = np.asarray(density, np.float64)
+    m = ((4 / 3.0) * math.pi) * (r * r * r) * rho
+    inertia = 0.0 + ((2.0 / 5.0) * m) * (r * r)
+    return m, inertia
+
+
+def assemble(centers, radii, sphere_mat, walls, mats_py, vel=None):
+    """ParticleArrays with walls first (ids 0..nw-1), then spheres.
+
+    walls: list of (axis, sense, position, material index)."""
+    nw = len(walls)
+    ns = len(radii)
+    n = nw + ns
+    pa = abi.ParticleArrays(n)
+    for i, (ax, sense, pos, mi) in enumerate(walls):
+        pa.shape[i] = abi.SHAPE_WALL
+        pa.wallAxis[i] = ax
+        pa.wallSense[i] = sense
+        pa.pos[i, ax] = pos
+        pa.material[i] = mi
+        pa.mask[i] = DEFAULT_BOUNDARY_MASK
+        pa.flags[i] = abi.DOF_ALL
+        pa.radius[i] = np.nan
+    s = slice(nw, n)
+    pa.shape[s] = abi.SHAPE_SPHERE
+    pa.radius[s] = radii
+    pa.pos[s] = centers
+    sm = np.broadcast_to(np.asarray(sphere_mat, np.int32), (ns,))
+    pa.material[s] = sm
+    pa.mask[s] = DEFAULT_MOVABLE_MASK
+    dens = np.array([mats_py[k].get("density", 1000.0) for k in range(len(mats_py))])[sm]
+    m, inert = sphere_mass_inertia(radii, dens)
+    pa.mass[s] = m
+    pa.inertia[s] = inert[:, None]
+    if vel is not None:
+        pa.vel[s] = vel
+    return pa
+
+
+def box_walls(lo, hi, mat=0):
+    """Six axis-aligned walls of a box, each interacting towards the inside (Wall.sense)."""
+    w = []
+    for ax in range(3):
+        w.append((ax, 1, lo[ax], mat))
+        w.append((ax, -1, hi[ax], mat))
+    return w
+
+
+def pwave_dt(radii, mat_idx, mats_py):
+    """DemFuncs::pWaveDt (src/dem/Funcs.cpp:151-175): min r / sqrt(E/rho) over spheres."""
+    E = np.array([m.get("young", 1e9) for m in mats_py])[mat_idx]
+    rho = np.array([m.get("density", 1000.0) for m in mats_py])[mat_idx]
+    return float(np.min(radii / (1.0 * np.sqrt(E / rho))))
+
+
+def spheres10k(n=10000, seed=1):
+    """10k monodisperse FrictMat spheres in a walled 0.5 x 0.5 x 1.0 m box (IdealElPl)."""
+    mats_py = [dict(kind=abi.MAT_FRICT, density=3000.0, young=1e7, ktDivKn=0.2, tanPhi=0.5)]
+    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([0.5, 0.5, 1.0])
+    centers, radii = abi.make_cloud(lo, hi, 0.005, 0.005, n, seed)
+    mats = materials_array(mats_py)
+    pa = assemble(centers, radii, 0, box_walls(lo, hi), mats_py)
+    dt = 0.4 * pwave_dt(radii, np.zeros(len(radii), int), mats_py)
+    p = default_params(mats, dt=dt, gravity=(0, 0, -9.81), damping=0.2, verletDist=-0.05)
+    return SceneSpec(p, mats, pa, "spheres10k", dict(n_spheres=len(radii), seed=seed, dt=dt))
+
+
+def hertz1M(n=1_000_000, seed=2, height=1.12, prefall=0.0):
+    """1M polydisperse HertzMat spheres (DMT, en=.8) as a loose cloud in a 1 x 1 x 2 m walled box.
+
+    The cloud fills z in [0, height] (height 1.12 m gives a solid fraction of about 0.3); prefall>0
+    gives every sphere an initial downward velocity sqrt(2 g prefall), as after falling that far."""
+    mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.3, surfEnergy=0.01),
+               dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.01)]
+    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 2.0])
+    centers, radii = abi.make_cloud(lo, np.array([1.0, 1.0, height]), 0.002, 0.006, n, seed, max_attempts=400)
+    k = len(radii)
+    mat_idx = (np.arange(k) % 2).astype(np.int32)
+    mats = materials_array(mats_py)
+    vel = None
+    if prefall > 0:
+        vel = np.zeros((k, 3)); vel[:, 2] = -math.sqrt(2 * 9.81 * prefall)
+    pa = assemble(centers, radii, mat_idx, box_walls(lo, hi), mats_py, vel=vel)
+    dt = 0.3 * pwave_dt(radii, mat_idx, mats_py)
+    p = default_params(mats, dt=dt, gravity=(0, 0, -9.81), damping=0.0, verletDist=0.1 * 0.002,
+                       cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.8)
+    return SceneSpec(p, mats, pa, "hertz1M", dict(n_spheres=k, seed=seed, dt=dt, height=height))
+
+
+def random_cloud(n, seed, box=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="frict", walls=True, vel_scale=0.5,
+                 angvel_scale=5.0, gravity=(0, 0, -9.81), damping=0.2, dense=1.0, **kw):
+    """Small randomised test scene: a sphere cloud squeezed by `dense` (<1 creates overlaps) with random
+    velocities, optional box walls, FrictMat/IdealElPl or HertzMat/DMT."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.zeros(3), np.asarray(box, np.float64)
+    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed)
+    if dense != 1.0:
+        c = hi / 2
+        centers = c + (centers - c) * dense
+    k = len(radii)
+    vel = rng.normal(0, vel_scale, (k, 3))
+    if law == "frict":
+        mats_py = [dict(kind=abi.MAT_FRICT, density=2500.0, young=1e7, ktDivKn=0.2, tanPhi=0.5),
+                   dict(kind=abi.MAT_FRICT, density=2000.0, young=3e7, ktDivKn=0.3, tanPhi=0.3)]
+        extra = dict(cp2=abi.CP2_FRICT, law=abi.LAW_IDEALELPL)
+    else:
+        mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.3, surfEnergy=0.01),
+                   dict(kind=abi.MAT_HERTZ, density=1200.0, young=8e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.02)]
+        extra = dict(cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.8)
+    extra.update(kw)
+    mat_idx = rng.integers(0, 2, k).astype(np.int32)
+    mats = materials_array(mats_py)
+    pa = assemble(centers, radii, mat_idx, box_walls(lo, hi) if walls else [], mats_py, vel=vel)
+    nw = 6 if walls else 0
+    pa.angVel[nw:] = rng.normal(0, angvel_scale, (k, 3))
+    dt = 0.3 * pwave_dt(radii, mat_idx, mats_py)
+    p = default_params(mats, dt=dt, gravity=gravity, damping=damping, **extra)
+    # initial forces as Woo has them before the first step: m*g (ForceResetter / Leapfrog reset)
+    g = np.asarray(gravity, np.float64)
+    pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
+    return SceneSpec(p, mats, pa, f"cloud{n}", dict(seed=seed, dt=dt))
