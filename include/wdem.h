@@ -246,6 +246,20 @@ int wdem_set_timing(wdem_handle* h, int32_t enable);
  * in the contact's CGeom object; storing them costs 56 bytes per contact per step). */
 int wdem_keep_geom(wdem_handle* h, int32_t enable);
 
+/* The CUDA stream (cudaStream_t) every kernel of this handle is launched on, for callers that
+ * record CUDA events around wdem_step. */
+int wdem_get_stream(wdem_handle* h, void** stream);
+
+/* Overwrite / read the kinematic state of the first n particles in place, without touching the
+ * contact container (as editing S.dem.par[i].pos/vel between steps in Woo).  Caller host buffers
+ * (pinned memory gives full copy bandwidth); null arrays are skipped; pos/vel/angVel are 3n, ori 4n. */
+int wdem_write_state(wdem_handle* h, int32_t n, const double* pos, const double* vel, const double* angVel,
+                     const double* ori);
+int wdem_read_state(wdem_handle* h, int32_t n, double* pos, double* vel, double* angVel, double* ori);
+
+/* Number of CUDA kernels this handle has launched since it was created. */
+int wdem_launch_count(wdem_handle* h, int64_t* count);
+
 /* Seeded random sequential addition of n non-overlapping spheres, radii uniform in [rMin, rMax],
  * inside the box [lo, hi]: the synthetic-input counterpart of Woo's SpherePack::makeCloud
  * (src/supp/sphere-pack/SpherePack.cpp:140-).  Host only, no GPU needed.  Returns the number placed

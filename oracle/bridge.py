@@ -27,6 +27,8 @@ def load(variant="liborc.so"):
         "orc_last_error": ([h], C.c_char_p),
         "orc_set_params": ([h, C.POINTER(abi.Params)], C.c_int),
         "orc_set_mode": ([h, C.c_int, C.c_int, C.c_int], C.c_int),
+        "orc_set_parallel": ([h, C.c_int], C.c_int),
+        "orc_threads": ([], C.c_int),
         "orc_upload_particles": ([h, C.POINTER(abi.Particles)], C.c_int),
         "orc_upload_contacts": ([h, C.POINTER(abi.Contacts)], C.c_int),
         "orc_step": ([h, C.c_int], C.c_int),
@@ -80,6 +82,14 @@ class Oracle:
                 self.lib.orc_destroy(self.h)
         except Exception:
             pass
+
+    def set_parallel(self, on=True):
+        """OpenMP contact/node loops (liborc_omp.so only): the reference's parallel scheme, for timing."""
+        if self.lib.orc_set_parallel(self.h, 1 if on else 0) != 0:
+            raise RuntimeError("this oracle build has no OpenMP")
+
+    def threads(self):
+        return self.lib.orc_threads()
 
     def step(self, n=1):
         self.check(self.lib.orc_step(self.h, int(n)))

@@ -16,7 +16,7 @@ SRC = os.path.join(HERE, "woo_oracle.cpp")
 def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
     out = {}
-    for name, extra in (("liborc.so", ["-O2"]), ("liborc_o3.so", ["-O3"])):
+    for name, extra in (("liborc.so", ["-O2"]), ("liborc_omp.so", ["-O3", "-fopenmp"])):
         lib = os.path.join(BUILD, name)
         deps = [SRC, os.path.join(os.path.dirname(HERE), "include", "wdem.h"), __file__]
         if force or not os.path.exists(lib) or any(os.path.getmtime(d) > os.path.getmtime(lib) for d in deps):

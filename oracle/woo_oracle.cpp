@@ -252,6 +252,11 @@ struct Scene {
   Energy E;
   std::string err;
   int lastRunFull = 0;
+  int parallel = 0;   /* OpenMP contact/node loops with a per-particle lock (reference's OpenMP build) */
+#ifdef _OPENMP
+  std::vector<omp_lock_t> locks;
+  ~Scene() { for (auto& l : locks) omp_destroy_lock(&l); }
+#endif
 };
 
 /* ------------------------------------------------------------------ ContactContainer */
@@ -416,8 +421,22 @@ static void colliderRun(Scene& S) {
   setVerletDist(S);
   bool recompute = false;
   if (S.verletDist == 0) recompute = true;
-  else for (const Particle& p : S.par) if (aabbIsDirty(p)) { recompute = true; break; }
-  if (recompute) for (Particle& p : S.par) updateAabb(S, p);
+  else {
+    const long np = (long)S.par.size();
+    int dirtyAny = 0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(| : dirtyAny) if (S.parallel)
+#endif
+    for (long i = 0; i < np; i++) if (aabbIsDirty(S.par[i])) dirtyAny |= 1;
+    recompute = dirtyAny != 0;
+  }
+  if (recompute) {
+    const long np = (long)S.par.size();
+#ifdef _OPENMP
+#pragma omp parallel for if (S.parallel)
+#endif
+    for (long i = 0; i < np; i++) updateAabb(S, S.par[i]);
+  }
   if (recompute) fullRun = true;
   S.lastRunFull = fullRun;
   if (!fullRun) {
@@ -738,6 +757,79 @@ static void applyForceUninodal(Scene& S, const Contact& C, Particle& p) {
 
 static bool isSphereLike(int shape) { return shape == WDEM_SHAPE_SPHERE; }
 
+#ifdef _OPENMP
+/* ContactLoop::run as the reference's OpenMP build runs it: guided parallel loop over the
+ * contacts (ContactLoop.cpp:134-137), forces added under a per-node lock (DemData::addForceTorque,
+ * Particle.hpp:249), removal requests collected per thread.  Used for the timed CPU baseline only. */
+static void contactLoopParallel(Scene& S) {
+  const wdem_params& P = S.P;
+  const long size = (long)S.linView.size();
+  std::vector<CPtr> removeAfter, removals;
+  bool nanSeen = false;
+  std::string nanMsg;
+#pragma omp parallel
+  {
+    std::vector<CPtr> myRemoveAfter, myRemovals;
+#pragma omp for schedule(guided)
+    for (long i = 0; i < size; i++) {
+      const CPtr C = S.linView[i];
+      if (!C->isReal() && !C->isColliding()) { myRemoveAfter.push_back(C); continue; }
+      bool fresh = (S.step == C->stepCreated);
+      if (!C->isReal() && fresh) {
+        Particle& a = S.par[C->pA];
+        Particle& b = S.par[C->pB];
+        if (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_WALL) continue;
+        if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) std::swap(C->pA, C->pB);
+        if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
+          C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
+        else C->minDist00Sq = -1;
+      }
+      Particle& pA = S.par[C->pA];
+      Particle& pB = S.par[C->pB];
+      V3 shift2;
+      if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
+      bool geomCreated;
+      if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
+      else if (pA.shape == WDEM_SHAPE_WALL && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2WallSphere(S, *C, pA, pB, shift2, false);
+      else geomCreated = false;
+      if (!geomCreated) continue;
+      if (!C->phys) C->stepCreated = (int)S.step;
+      if (!C->phys || S.updatePhys > WDEM_UPDATE_PHYS_NEVER) {
+        const wdem_material& m1 = S.mats[pA.mat];
+        const wdem_material& m2 = S.mats[pB.mat];
+        if (P.cp2 == WDEM_CP2_FRICT) cp2Frict(S, *C, m1, m2); else cp2Hertz(S, *C, m1, m2);
+      }
+      bool keep = true;
+      try {
+        keep = (P.law == WDEM_LAW_IDEALELPL) ? lawIdealElPl(S, *C) : lawHertzDMT(S, *C);
+      } catch (std::exception& e) {
+#pragma omp critical
+        { nanSeen = true; nanMsg = e.what(); }
+      }
+      if (!keep) {
+        C->geom = false; C->phys = false;
+        myRemovals.push_back(C);
+        continue;
+      }
+      for (Particle* pp : {&pA, &pB}) {
+        omp_set_lock(&S.locks[pp->id]);
+        applyForceUninodal(S, *C, *pp);
+        omp_unset_lock(&S.locks[pp->id]);
+      }
+    }
+#pragma omp critical
+    {
+      removeAfter.insert(removeAfter.end(), myRemoveAfter.begin(), myRemoveAfter.end());
+      removals.insert(removals.end(), myRemovals.begin(), myRemovals.end());
+    }
+  }
+  if (nanSeen) throw std::runtime_error(nanMsg);
+  for (auto& c : removals) requestRemoval(S, c);
+  for (auto& c : removeAfter) removeContact(S, c);
+  if (S.updatePhys == WDEM_UPDATE_PHYS_ONCE) S.updatePhys = WDEM_UPDATE_PHYS_NEVER;
+}
+#endif
+
 /* ContactLoop::run (ContactLoop.cpp:93-268), aperiodic, no hook, no stress */
 static void contactLoopRun(Scene& S) {
   const wdem_params& P = S.P;
@@ -748,6 +840,9 @@ static void contactLoopRun(Scene& S) {
   }
   std::vector<CPtr> removeAfter;
   size_t size = S.linView.size();
+#ifdef _OPENMP
+  if (S.parallel && S.applyOrder == 0) { contactLoopParallel(S); return; }
+#endif
   for (size_t i = 0; i < size; i++) {
     const CPtr C = S.linView[i];
     if (!C->isReal() && !C->isColliding()) { removeAfter.push_back(C); continue; }
@@ -817,7 +912,12 @@ static void leapfrogRun(Scene& S) {
   const double damping = P.damping;
   V3 gravity(P.gravity[0], P.gravity[1], P.gravity[2]);
   bool hasGravity = !isZero(gravity);
-  for (Particle& p : S.par) {
+  const long np = (long)S.par.size();
+#ifdef _OPENMP
+#pragma omp parallel for schedule(guided) if (S.parallel && !P.trackEnergy)
+#endif
+  for (long ip = 0; ip < np; ip++) {
+    Particle& p = S.par[ip];
     bool damp = (damping != 0. && !(p.flags & WDEM_DAMPING_SKIP));
     V3& f = p.force;
     V3& t = p.torque;
@@ -932,6 +1032,30 @@ int orc_set_params(orc_handle* h, const wdem_params* p) {
   S.updatePhys = p->updatePhys;
   if (S.nFullRuns == 0 && S.BB[0].empty()) S.verletDist = p->verletDist;
   return 0;
+}
+
+/* OpenMP loops (only in the liborc_omp.so build); forces are then added in thread order. */
+int orc_set_parallel(orc_handle* h, int on) {
+#ifdef _OPENMP
+  Scene& S = h->S;
+  for (auto& l : S.locks) omp_destroy_lock(&l);
+  S.locks.assign(S.par.size(), omp_lock_t());
+  for (auto& l : S.locks) omp_init_lock(&l);
+  S.parallel = on;
+  if (on) S.applyOrder = 0;
+  return 0;
+#else
+  (void)h; (void)on;
+  return -1;
+#endif
+}
+
+int orc_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
 }
 
 int orc_set_mode(orc_handle* h, int canonicalOrient, int applyOrder, int sortAxis) {

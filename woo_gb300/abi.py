@@ -88,7 +88,7 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_upload_contacts", "wdem_step", "wdem_download_particles", "wdem_contact_count",
            "wdem_download_contacts", "wdem_crit_dt", "wdem_get_energy", "wdem_reset_energy", "wdem_get_status",
            "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
-           "wdem_make_cloud"]
+           "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count"]
 
 
 def ptr(a, ctype):
@@ -221,6 +221,10 @@ def load(path=None):
         "wdem_set_timing": ([h, C.c_int32], C.c_int),
         "wdem_keep_geom": ([h, C.c_int32], C.c_int),
         "wdem_make_cloud": ([D, D, C.c_double, C.c_double, C.c_int64, C.c_uint64, C.c_int32, D, D], C.c_int64),
+        "wdem_get_stream": ([h, C.POINTER(C.c_void_p)], C.c_int),
+        "wdem_write_state": ([h, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "wdem_read_state": ([h, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "wdem_launch_count": ([h, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -313,6 +317,23 @@ class Handle:
         cnt = C.c_int32()
         self.check(self.lib.wdem_kernel_times(self.h, names, ms, launches, 8, C.byref(cnt)))
         return {names[i].decode(): (ms[i], launches[i]) for i in range(cnt.value)}
+
+    def stream(self):
+        v = C.c_void_p()
+        self.check(self.lib.wdem_get_stream(self.h, C.byref(v)))
+        return v.value
+
+    def write_state(self, n, pos=None, vel=None, angVel=None, ori=None):
+        """Addresses (ints) of host buffers, e.g. tensor.data_ptr() of pinned tensors, or None."""
+        self.check(self.lib.wdem_write_state(self.h, int(n), pos, vel, angVel, ori))
+
+    def read_state(self, n, pos=None, vel=None, angVel=None, ori=None):
+        self.check(self.lib.wdem_read_state(self.h, int(n), pos, vel, angVel, ori))
+
+    def launch_count(self):
+        v = C.c_int64()
+        self.check(self.lib.wdem_launch_count(self.h, C.byref(v)))
+        return v.value
 
     def collide_boxes(self, mins, maxs, mask, lone_mask):
         mins = np.ascontiguousarray(mins, np.float64)

@@ -58,7 +58,7 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
 
 void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n) {
   if (n <= 0) return;
-  k_bboxes<<<(n + 255) / 256, 256, 0, s>>>(P, p, n);
+  (k_bboxes<<<(n + 255) / 256, 256, 0, s>>>(P, p, n), ++::wdem::g_kernel_launches);
 }
 
 // ------------------------------------------------------------------------------------ grid setup
@@ -227,10 +227,10 @@ static void scan_rec(cudaStream_t s, unsigned* a, long long n, unsigned* scratch
   long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (nb == 0) return;
   unsigned* sums = scratch;  // nb + 1 entries
-  k_scan_tiles<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums);
+  (k_scan_tiles<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums), ++::wdem::g_kernel_launches);
   if (nb > 1) {
     scan_rec(s, sums, nb, scratch + ((nb + 1 + 63) & ~63ll));
-    k_scan_add<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums);
+    (k_scan_add<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums), ++::wdem::g_kernel_launches);
   } else {
     // single tile: sums[0] holds the total; scan of one element is 0
   }
@@ -245,9 +245,9 @@ __global__ void k_finish_total(unsigned* a, long long n, const unsigned* lastInp
 void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs) {
   unsigned* last = cs.blockSums;        // 1 entry
   unsigned* scratch = cs.blockSums + 64;
-  k_save_last<<<1, 1, 0, s>>>(a, n, last);
+  (k_save_last<<<1, 1, 0, s>>>(a, n, last), ++::wdem::g_kernel_launches);
   scan_rec(s, a, n, scratch);
-  k_finish_total<<<1, 1, 0, s>>>(a, n, last);
+  (k_finish_total<<<1, 1, 0, s>>>(a, n, last), ++::wdem::g_kernel_launches);
 }
 
 // ------------------------------------------------------------------------------------ radix sort
@@ -313,9 +313,9 @@ static void radix_sort(cudaStream_t s, unsigned long long*& keys, unsigned*& val
   if (n <= 1) return;
   long long nTiles = (n + RS_TILE - 1) / RS_TILE;
   for (int shift = 0; shift < bits; shift += 8) {
-    k_rs_hist<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, n, shift, cs.hist, nTiles);
+    (k_rs_hist<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, n, shift, cs.hist, nTiles), ++::wdem::g_kernel_launches);
     exclusive_scan_u32(s, cs.hist, 256 * nTiles, cs);
-    k_rs_scatter<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, vals, keysAlt, valsAlt, n, shift, cs.hist, nTiles);
+    (k_rs_scatter<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, vals, keysAlt, valsAlt, n, shift, cs.hist, nTiles), ++::wdem::g_kernel_launches);
     unsigned long long* tk = keys; keys = keysAlt; keysAlt = tk;
     unsigned* tv = vals; vals = valsAlt; valsAlt = tv;
   }
@@ -499,8 +499,8 @@ __device__ __forceinline__ long long hashFind(const unsigned long long* hk, cons
 void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
                        unsigned long long cap, DeviceStatus* st) {
   if (cap == 0) return;
-  k_hash_clear<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(hk, cap);
-  if (n > 0) k_hash_insert<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ids, n, hk, hv, cap, st);
+  (k_hash_clear<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(hk, cap), ++::wdem::g_kernel_launches);
+  if (n > 0) (k_hash_insert<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ids, n, hk, hv, cap, st), ++::wdem::g_kernel_launches);
 }
 
 // ------------------------------------------------------------------------------------ carry-over
@@ -568,17 +568,17 @@ static int bitsFor(unsigned long long v) { int b = 0; while ((1ull << b) < v) b+
 // The collider sub-steps are called from wdem_api.cu through these thin wrappers.
 void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
   unsigned long long* ext = (unsigned long long*)cs.temp;
-  k_extents_init<<<1, 32, 0, s>>>(ext);
-  if (nSmall > 0) k_extents<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, ext);
-  k_grid_setup<<<1, 1, 0, s>>>(ext, nSmall, cs.maxCols, cs.grid);
+  (k_extents_init<<<1, 32, 0, s>>>(ext), ++::wdem::g_kernel_launches);
+  if (nSmall > 0) (k_extents<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, ext), ++::wdem::g_kernel_launches);
+  (k_grid_setup<<<1, 1, 0, s>>>(ext, nSmall, cs.maxCols, cs.grid), ++::wdem::g_kernel_launches);
 }
 
 void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
-  if (nSmall > 0) k_make_keys<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, cs.grid, cs.keys, cs.vals);
+  if (nSmall > 0) (k_make_keys<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, cs.grid, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
   int bits = QBITS + bitsFor((unsigned long long)cs.maxCols + 1);
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bits, cs);
   int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
-  k_cell_start<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.grid, cs.cellStart);
+  (k_cell_start<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.grid, cs.cellStart), ++::wdem::g_kernel_launches);
 }
 
 void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out, long long cap,
@@ -587,30 +587,30 @@ void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, Colli
   A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
   A.nSmall = nSmall; A.loneMask = loneMask;
   int threads = nSmall + 1;
-  if (write) k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st);
-  else k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st);
+  if (write) (k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
+  else (k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
 }
 
 void col_retain_flags(cudaStream_t s, Particles p, Contacts old, long long nOld, ColliderScratch& cs) {
-  if (nOld > 0) k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(p, old, nOld, cs.retainFlag);
+  if (nOld > 0) (k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(p, old, nOld, cs.retainFlag), ++::wdem::g_kernel_launches);
   exclusive_scan_u32(s, cs.retainFlag, nOld, cs);
 }
 void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base, long long cap) {
-  if (nOld > 0) k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap);
+  if (nOld > 0) (k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap), ++::wdem::g_kernel_launches);
 }
 
 void col_carry(cudaStream_t s, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
                unsigned long long cap, long long step, int nHist) {
-  if (nNew > 0) k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(neu, nNew, old, hk, hv, cap, step, nHist);
+  if (nNew > 0) (k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(neu, nNew, old, hk, hv, cap, step, nHist), ++::wdem::g_kernel_launches);
 }
 
 void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs) {
   int idBits = bitsFor((unsigned long long)n + 1);
   long long ne = 2 * nc;
-  if (nc > 0) k_csr_entries<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(c, nc, idBits, cs.keys, cs.vals);
+  if (nc > 0) (k_csr_entries<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(c, nc, idBits, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, ne, 2 * idBits, cs);
   long long threads = ne > 0 ? ne : (long long)n + 1;
-  k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr);
+  (k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr), ++::wdem::g_kernel_launches);
   if (ne > 0) cudaMemcpyAsync(csr.ent, cs.vals, ne * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
 }
 

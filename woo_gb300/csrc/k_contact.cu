@@ -312,10 +312,10 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   if (nc <= 0) return;
   unsigned blocks = (unsigned)((nc + 127) / 128);
   if (P.law == WDEM_LAW_IDEALELPL) {
-    if (P.cp2 == WDEM_CP2_FRICT) k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
-    else k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
+    if (P.cp2 == WDEM_CP2_FRICT) (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    else (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   } else {
-    k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st);
+    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   }
 }
 
@@ -339,7 +339,7 @@ __global__ void k_init_uploaded(StepParams P, Particles p, Contacts c, long long
 
 void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc) {
   if (nc <= 0 || P.cp2 != WDEM_CP2_HERTZ) return;
-  k_init_uploaded<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(P, p, c, nc);
+  (k_init_uploaded<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(P, p, c, nc), ++::wdem::g_kernel_launches);
 }
 
 }  // namespace wdem

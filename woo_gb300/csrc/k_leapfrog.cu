@@ -128,8 +128,8 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
-  if (fromArrays) k_leapfrog<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
-  else k_leapfrog<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  if (fromArrays) (k_leapfrog<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  else (k_leapfrog<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
 }
 
 // DemData.force/torque as Woo holds them after ContactLoop (reset to m*g by Leapfrog, then contacts)
@@ -145,7 +145,38 @@ __global__ void k_reduce_forces(StepParams P, Particles p, int n, Contacts c, Cs
 
 void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr) {
   if (n <= 0) return;
-  k_reduce_forces<<<(n + 127) / 128, 128, 0, s>>>(P, p, n, c, csr);
+  (k_reduce_forces<<<(n + 127) / 128, 128, 0, s>>>(P, p, n, c, csr), ++::wdem::g_kernel_launches);
+}
+
+}  // namespace wdem
+
+namespace wdem {
+
+// Kinematic state exchange with caller buffers (xyz-interleaved / wxyz) through a device staging
+// area: scatter into the double4 records, or gather out of them.
+__global__ void k_state_in(Particles p, int n, const double* pos, const double* vel, const double* angVel,
+                           const double* ori) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (pos) { double4_32a v = p.posr[i]; v.x = pos[3 * i]; v.y = pos[3 * i + 1]; v.z = pos[3 * i + 2]; p.posr[i] = v; }
+  if (vel) { double4_32a v = p.velm[i]; v.x = vel[3 * i]; v.y = vel[3 * i + 1]; v.z = vel[3 * i + 2]; p.velm[i] = v; }
+  if (angVel) { double4_32a v = p.angw[i]; v.x = angVel[3 * i]; v.y = angVel[3 * i + 1]; v.z = angVel[3 * i + 2]; p.angw[i] = v; }
+  if (ori) p.ori[i] = make_double4_32a(ori[4 * i], ori[4 * i + 1], ori[4 * i + 2], ori[4 * i + 3]);
+}
+__global__ void k_state_out(Particles p, int n, double* pos, double* vel, double* angVel, double* ori) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (pos) { double4_32a v = p.posr[i]; pos[3 * i] = v.x; pos[3 * i + 1] = v.y; pos[3 * i + 2] = v.z; }
+  if (vel) { double4_32a v = p.velm[i]; vel[3 * i] = v.x; vel[3 * i + 1] = v.y; vel[3 * i + 2] = v.z; }
+  if (angVel) { double4_32a v = p.angw[i]; angVel[3 * i] = v.x; angVel[3 * i + 1] = v.y; angVel[3 * i + 2] = v.z; }
+  if (ori) { double4_32a v = p.ori[i]; ori[4 * i] = v.x; ori[4 * i + 1] = v.y; ori[4 * i + 2] = v.z; ori[4 * i + 3] = v.w; }
+}
+void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, const double* vel, const double* angVel,
+                     const double* ori) {
+  if (n > 0) (k_state_in<<<(n + 255) / 256, 256, 0, s>>>(p, n, pos, vel, angVel, ori), ++::wdem::g_kernel_launches);
+}
+void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori) {
+  if (n > 0) (k_state_out<<<(n + 255) / 256, 256, 0, s>>>(p, n, pos, vel, angVel, ori), ++::wdem::g_kernel_launches);
 }
 
 }  // namespace wdem

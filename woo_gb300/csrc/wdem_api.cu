@@ -20,6 +20,10 @@
 
 using namespace wdem;
 
+namespace wdem {
+long long g_kernel_launches = 0;
+}
+
 namespace {
 
 const char* kPhaseNames[] = {"leapfrog", "collider", "contacts"};
@@ -80,6 +84,8 @@ struct wdem_handle {
   double phaseMs[PH_COUNT] = {0, 0, 0};
   int phaseLaunches[PH_COUNT] = {0, 0, 0};
   std::string err;
+  double* staging = nullptr;    // 13 n doubles for wdem_write_state / wdem_read_state
+  long long stagingCap = 0;
 };
 
 namespace {
@@ -402,6 +408,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid);
   cudaFree(cs.retainFlag); cudaFree(cs.temp);
   cudaFree(h->dst);
+  cudaFree(h->staging);
   if (h->hst) cudaFreeHost(h->hst);
   if (h->hcounts) cudaFreeHost(h->hcounts);
   for (auto e : h->evPool) cudaEventDestroy(e);
@@ -891,6 +898,62 @@ int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* l
     if (launches) launches[k] = h->phaseLaunches[k];
   }
   *count = PH_COUNT;
+  return WDEM_OK;
+}
+
+int wdem_get_stream(wdem_handle* h, void** stream) {
+  if (!h || !stream) return WDEM_ERR_ARG;
+  *stream = (void*)h->stream;
+  return WDEM_OK;
+}
+
+static int ensureStaging(wdem_handle* h, long long n) {
+  if (13 * n > h->stagingCap) {
+    CK(dalloc(h->staging, (size_t)(13 * n)));
+    h->stagingCap = 13 * n;
+  }
+  return WDEM_OK;
+}
+
+int wdem_write_state(wdem_handle* h, int32_t n, const double* pos, const double* vel, const double* angVel,
+                     const double* ori) {
+  if (!h || n < 0 || n > h->n) return WDEM_ERR_ARG;
+  if (n == 0) return WDEM_OK;
+  cudaSetDevice(h->device);
+  int rc;
+  if ((rc = ensureStaging(h, n))) return rc;
+  cudaStream_t s = h->stream;
+  double *dp = nullptr, *dv = nullptr, *dw = nullptr, *dq = nullptr;
+  double* st = h->staging;
+  if (pos) { dp = st; CK(cudaMemcpyAsync(dp, pos, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, s)); }
+  if (vel) { dv = st + 3 * (size_t)n; CK(cudaMemcpyAsync(dv, vel, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, s)); }
+  if (angVel) { dw = st + 6 * (size_t)n; CK(cudaMemcpyAsync(dw, angVel, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, s)); }
+  if (ori) { dq = st + 9 * (size_t)n; CK(cudaMemcpyAsync(dq, ori, 4 * sizeof(double) * n, cudaMemcpyHostToDevice, s)); }
+  launch_state_in(s, h->d, n, dp, dv, dw, dq);
+  return WDEM_OK;
+}
+
+int wdem_read_state(wdem_handle* h, int32_t n, double* pos, double* vel, double* angVel, double* ori) {
+  if (!h || n < 0 || n > h->n) return WDEM_ERR_ARG;
+  if (n == 0) return WDEM_OK;
+  cudaSetDevice(h->device);
+  int rc;
+  if ((rc = ensureStaging(h, n))) return rc;
+  cudaStream_t s = h->stream;
+  double* st = h->staging;
+  launch_state_out(s, h->d, n, pos ? st : nullptr, vel ? st + 3 * (size_t)n : nullptr, angVel ? st + 6 * (size_t)n : nullptr,
+                   ori ? st + 9 * (size_t)n : nullptr);
+  if (pos) CK(cudaMemcpyAsync(pos, st, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (vel) CK(cudaMemcpyAsync(vel, st + 3 * (size_t)n, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (angVel) CK(cudaMemcpyAsync(angVel, st + 6 * (size_t)n, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (ori) CK(cudaMemcpyAsync(ori, st + 9 * (size_t)n, 4 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return WDEM_OK;
+}
+
+int wdem_launch_count(wdem_handle* h, int64_t* count) {
+  if (!h || !count) return WDEM_ERR_ARG;
+  *count = ::wdem::g_kernel_launches;
   return WDEM_OK;
 }
 

@@ -28,6 +28,9 @@
 
 namespace wdem {
 
+// kernels launched by the library in this process (incremented at every launch site)
+extern long long g_kernel_launches;
+
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
@@ -109,6 +112,9 @@ struct DeviceStatus {
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays,
                      Contacts c, Csr csr, DeviceStatus* st);
 void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr);
+void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, const double* vel, const double* angVel,
+                     const double* ori);
+void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori);
 // ---- launchers (k_contact.cu) ----
 void upload_materials(const DevMaterial* m, int n);
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st);
@@ -131,6 +137,7 @@ struct ColliderScratch {
   unsigned* retainFlag;                 // old contacts retained (scanned in place)
   long long retainCap;
   void* temp;                           // small scratch (extent reduction)
+  long long launches;                   // kernels launched by the collider (counted on the host)
 };
 void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n);
 void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);

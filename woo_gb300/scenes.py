@@ -164,11 +164,14 @@ def hertz1M(n=1_000_000, seed=2, height=1.12, prefall=0.0):
     """1M polydisperse HertzMat spheres (DMT, en=.8) as a loose cloud in a 1 x 1 x 2 m walled box.
 
     The cloud fills z in [0, height] (height 1.12 m gives a solid fraction of about 0.3); prefall>0
-    gives every sphere an initial downward velocity sqrt(2 g prefall), as after falling that far."""
+    gives every sphere an initial downward velocity sqrt(2 g prefall), as after falling that far.
+    For n below 1M the box and the cloud shrink by (n/1e6)^(1/3), keeping the same solid fraction
+    (the "cut" of the same workload used for the CPU baseline)."""
     mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.3, surfEnergy=0.01),
                dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.01)]
-    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 2.0])
-    centers, radii = abi.make_cloud(lo, np.array([1.0, 1.0, height]), 0.002, 0.006, n, seed, max_attempts=400)
+    sc = (n / 1e6) ** (1.0 / 3.0)
+    lo, hi = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 2.0]) * sc
+    centers, radii = abi.make_cloud(lo, np.array([1.0, 1.0, height]) * sc, 0.002, 0.006, n, seed, max_attempts=400)
     k = len(radii)
     mat_idx = (np.arange(k) % 2).astype(np.int32)
     mats = materials_array(mats_py)
@@ -179,7 +182,8 @@ def hertz1M(n=1_000_000, seed=2, height=1.12, prefall=0.0):
     dt = 0.3 * pwave_dt(radii, mat_idx, mats_py)
     p = default_params(mats, dt=dt, gravity=(0, 0, -9.81), damping=0.0, verletDist=0.1 * 0.002,
                        cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.8)
-    return SceneSpec(p, mats, pa, "hertz1M", dict(n_spheres=k, seed=seed, dt=dt, height=height))
+    return SceneSpec(p, mats, pa, "hertz1M" if n == 1_000_000 else f"hertz{n}", dict(n_spheres=k, seed=seed, dt=dt, height=height * sc,
+                                                                                     box=hi.tolist()))
 
 
 def random_cloud(n, seed, box=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="frict", walls=True, vel_scale=0.5,
