@@ -180,21 +180,34 @@ def run_gpu(args, rank, world, local):
     ms_max = float(t.item())
     value = world * n * args.steps / (ms_max / 1e3)
 
-    # roofline of the dominant kernel (fused contact kernel): algorithmic bytes per launch (counts at the
-    # end of the timed region) over the CUDA-event average launch duration inside the timed region
+    # roofline of the dominant kernel: algorithmic bytes per launch (contact counts at the end of the
+    # timed region) over the CUDA-event average launch duration inside the timed region
     cg = h.download_contacts()
     hertz = spec.params.cp2 == abi.CP2_HERTZ
-    abytes, counts = contact_kernel_bytes(cg, spec.particles.shape, hertz)
-    c_ms, c_n = kt.get("contacts", (0.0, 0))
-    lf_ms, lf_n = kt.get("leapfrog", (0.0, 0))
-    co_ms, co_n = kt.get("collider", (0.0, 0))
-    c_avg = c_ms / max(c_n, 1)
-    achieved = abytes / (c_avg / 1e3) / 1e9 if c_avg > 0 else 0.0
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", f"contact_kernel_{args.workload}.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    cbytes, counts = contact_kernel_bytes(cg, spec.particles.shape, hertz)
+    lbytes = 256 * n + 80 * counts["real"]   # fused CSR reduction + Leapfrog: 300+52-96 B/particle, 80 B/real contact
+    fp64_peak = h.fp64_peak()
+    rl = {}
+    for kname, label, abytes in (("contacts", "k_contacts (fused Cg2+Cp2+Law2)", cbytes),
+                                 ("leapfrog", "k_leapfrog (CSR force gather + Leapfrog + verlet check)", lbytes)):
+        k_ms, k_n = kt.get(kname, (0.0, 0))
+        avg = k_ms / max(k_n, 1)
+        ach = abytes / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+        prof = os.path.join(ROOT, "profiles", f"{kname}_{args.workload}.json")
+        traffic = dp_ops = None
+        if os.path.exists(prof):
+            with open(prof) as f:
+                pj = json.load(f)
+            traffic = pj.get("dram_bytes_per_launch")
+            dp_ops = pj.get("fp64_flops_per_launch")
+        rl[kname] = {"kernel": label, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach / hbm_peak, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": abytes, "traffic": traffic, "ms_avg": avg,
+                     "fp64": {"peak_gflops_measured": fp64_peak,
+                              "flops_per_launch_ncu": dp_ops,
+                              "achieved_gflops": (dp_ops / (avg / 1e3) / 1e9) if (dp_ops and avg > 0) else None,
+                              "frac": (dp_ops / (avg / 1e3) / 1e9 / fp64_peak) if (dp_ops and avg > 0) else None}}
+    dominant = max(rl, key=lambda k: rl[k]["ms_avg"])
 
     # end-to-end through the public C ABI with host buffers: per step, the kinematic state goes in from
     # pinned host memory (wdem_write_state), one step runs, and the state comes back (wdem_read_state)
@@ -235,10 +248,8 @@ def run_gpu(args, rank, world, local):
         "gpu_launches": int(launches),
         "kernels": {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / max(v[1], 1)} for k, v in kt.items()},
         "contacts": dict(counts, collider_rebuilds_timed=int(st1.nFullRuns - st0.nFullRuns)),
-        "roofline": {"kernel": "k_contacts (fused Cg2+Cp2+Law2)", "bound": "hbm", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                     "algorithmic_bytes_per_launch": abytes, "traffic": traffic},
+        "roofline": rl[dominant],
+        "roofline_other": {k: v for k, v in rl.items() if k != dominant},
         "clocks": clk,
         "e2e": e2e,
     }

@@ -257,7 +257,11 @@ int wdem_write_state(wdem_handle* h, int32_t n, const double* pos, const double*
                      const double* ori);
 int wdem_read_state(wdem_handle* h, int32_t n, double* pos, double* vel, double* angVel, double* ori);
 
-/* Number of CUDA kernels this handle has launched since it was created. */
+/* Measured FP64 fused-multiply-add throughput of the device in GFLOP/s (2 flops per FMA): the
+ * ceiling of the FP64-issue-bound kernels, reported beside the HBM roofline. */
+int wdem_fp64_peak(wdem_handle* h, double* gflops);
+
+/* Number of CUDA kernels launched by the library in this process (every launch site counts). */
 int wdem_launch_count(wdem_handle* h, int64_t* count);
 
 /* Seeded random sequential addition of n non-overlapping spheres, radii uniform in [rMin, rMax],

@@ -88,7 +88,8 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_upload_contacts", "wdem_step", "wdem_download_particles", "wdem_contact_count",
            "wdem_download_contacts", "wdem_crit_dt", "wdem_get_energy", "wdem_reset_energy", "wdem_get_status",
            "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
-           "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count"]
+           "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
+           "wdem_fp64_peak"]
 
 
 def ptr(a, ctype):
@@ -225,6 +226,7 @@ def load(path=None):
         "wdem_write_state": ([h, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "wdem_read_state": ([h, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "wdem_launch_count": ([h, C.POINTER(C.c_int64)], C.c_int),
+        "wdem_fp64_peak": ([h, C.POINTER(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -329,6 +331,11 @@ class Handle:
 
     def read_state(self, n, pos=None, vel=None, angVel=None, ori=None):
         self.check(self.lib.wdem_read_state(self.h, int(n), pos, vel, angVel, ori))
+
+    def fp64_peak(self):
+        v = C.c_double()
+        self.check(self.lib.wdem_fp64_peak(self.h, C.byref(v)))
+        return v.value
 
     def launch_count(self):
         v = C.c_int64()

@@ -440,7 +440,7 @@ __global__ void k_retain_flag(Particles p, Contacts old, long long nOld, unsigne
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nOld) return;
   unsigned f = 0;
-  if (old.state[c] == CS_REAL) {
+  if ((old.state[c] & CS_MASK) == CS_REAL) {
     int2 id = old.ids[c];
     if (!overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y])) f = 1;
   }
@@ -508,25 +508,27 @@ void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned lo
 // created in this step (InsertionSortCollider.hpp:106-113 stepCreated=scene->step).  A contact that
 // the law broke in the previous step (pending) becomes potential: removePending in a full run keeps
 // it only when its new boxes overlap, which holds for every pair the sweep emitted.
-__global__ void k_carry(Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
-                        unsigned long long cap, long long step, int nHist) {
+__global__ void k_carry(Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
+                        const unsigned* hv, unsigned long long cap, long long step, int nHist) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nNew) return;
   int2 id = neu.ids[c];
   long long j = hashFind(hk, hv, cap, pairKey(id.x, id.y));
   uint8_t st = CS_POTENTIAL;
   if (j >= 0) {
-    uint8_t os = old.state[j];
+    uint8_t os = old.state[j] & CS_MASK;
     if (os == CS_DEAD) j = -1;
     else st = (os == CS_REAL) ? CS_REAL : CS_POTENTIAL;
   }
   if (j < 0) {
-    neu.state[c] = CS_POTENTIAL;
+    const uint8_t sb = (uint8_t)((((p.meta[id.x].x & 15) == WDEM_SHAPE_WALL) ? CS_WALL_A : 0) |
+                                 (((p.meta[id.y].x & 15) == WDEM_SHAPE_WALL) ? CS_WALL_B : 0));
+    neu.state[c] = CS_POTENTIAL | sb;
     neu.step0[c] = (int)step;
     return;
   }
   neu.ids[c] = old.ids[j];  // keep the stored orientation
-  neu.state[c] = st;
+  neu.state[c] = st | (old.state[j] & CS_SHAPES);
   neu.step0[c] = old.step0[j];
   if (st == CS_REAL) {
     for (int h = 0; h < nHist; h++) neu.hist[h][c] = old.hist[h][j];
@@ -599,9 +601,9 @@ void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScra
   if (nOld > 0) (k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap), ++::wdem::g_kernel_launches);
 }
 
-void col_carry(cudaStream_t s, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
-               unsigned long long cap, long long step, int nHist) {
-  if (nNew > 0) (k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(neu, nNew, old, hk, hv, cap, step, nHist), ++::wdem::g_kernel_launches);
+void col_carry(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
+               const unsigned* hv, unsigned long long cap, long long step, int nHist) {
+  if (nNew > 0) (k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(p, neu, nNew, old, hk, hv, cap, step, nHist), ++::wdem::g_kernel_launches);
 }
 
 void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs) {

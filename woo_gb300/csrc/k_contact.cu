@@ -73,27 +73,40 @@ template <int LAW, int CP2>
 __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
-  uint8_t s = c.state[i];
+  const uint8_t s0 = c.state[i];
+  const uint8_t sb = s0 & CS_SHAPES;
+  uint8_t s = s0 & CS_MASK;
   if (s == CS_DEAD) return;
+  // no Cg2 functor for Wall+Wall: the pair stays a potential contact (ContactLoop.cpp:149-150)
+  if (sb == (CS_WALL_A | CS_WALL_B)) return;
   const int2 id = c.ids[i];
   const int a = id.x, b = id.y;
-  const int4 ma = p.meta[a], mb = p.meta[b];
-  // no Cg2 functor for Wall+Wall: the pair stays a potential contact (ContactLoop.cpp:149-150)
-  if ((ma.x & 15) == WDEM_SHAPE_WALL && (mb.x & 15) == WDEM_SHAPE_WALL) return;
   if (s == CS_PENDING) {
     // removePending of this step's collider (no rebuild happened; a rebuild clears PENDING):
     // drop the broken contact when the boxes of the last rebuild do not overlap.
-    if (!overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b])) { c.state[i] = CS_DEAD; return; }
+    if (!overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b])) { c.state[i] = CS_DEAD | sb; return; }
     s = CS_POTENTIAL;
-    c.state[i] = s;
+    c.state[i] = s | sb;
   }
   const bool real = (s == CS_REAL);
+  if (!real && !(sb & CS_WALL_A)) {
+    // Conservative FP32 cull of sphere pairs that cannot touch.  The FP32 copies carry a relative
+    // error <= 2^-24 per coordinate and radius; the margin below (1e-5 relative on the contact
+    // distance plus 1e-6 x the sum of |coordinates|) exceeds the accumulated FP32 error, so every
+    // pair rejected here also fails the exact FP64 test of Cg2_Sphere_Sphere_L6Geom.  Pairs close to
+    // touching, NaN and overflow fall through to the FP64 test.
+    const float4 fa = p.posf[a], fb = p.posf[b];
+    const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z);
+    const float R = (float)fabs(P.distFactor) * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
+    if (d2 > R * R) return;
+  }
   const double4_32a A4 = p.posr[a], B4 = p.posr[b];
   const d3 pos1 = xyz(A4), pos2 = xyz(B4);
-  const int shA = ma.x & 15;
   double r1, r2, uN;
   d3 normal, contPt;
-  if (shA == WDEM_SHAPE_SPHERE) {
+  if (!(sb & CS_WALL_A)) {
     // Cg2_Sphere_Sphere_L6Geom::go
     r1 = A4.w; r2 = B4.w;
     d3 relPos = pos2 - pos1;
@@ -106,7 +119,8 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
     contPt = pos1 + (r1 + 0.5 * uN) * normal;
   } else {
     // Cg2_Wall_Sphere_L6Geom::go (pA is the wall)
-    const int ax = (ma.x >> 4) & 3, sense = ((ma.x >> 8) & 3) - 1;
+    const int wa = p.meta[a].x;
+    const int ax = (wa >> 4) & 3, sense = ((wa >> 8) & 3) - 1;
     const double radius = B4.w;
     double dist = comp(pos2, ax) - comp(pos1, ax);
     if (!real && fabs(dist) > radius) return;
@@ -125,6 +139,9 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
     uN = nax * dist - radius;
     r1 = -radius; r2 = radius;
   }
+  // materials are needed only when Cp2 runs
+  int matA = 0, matB = 0;
+  if (!real || P.updatePhysNow) { matA = p.meta[a].y; matB = p.meta[b].y; }
 
   double fx, fy, fz, kn, kt, tanPhi;
   double hz[4] = {0, 0, 0, 0};
@@ -142,7 +159,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
     cur0 = locX; cur1 = locY;
     gvel = mk(0, 0, 0); gangVel = mk(0, 0, 0);
     // new CPhys (ContactLoop.cpp:179-180)
-    cp2<CP2>(P, ma.y, mb.y, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
+    cp2<CP2>(P, matA, matB, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
     fx = 0; fy = 0; fz = 0;
     c.step0[i] = (int)P.step;
   } else {
@@ -187,7 +204,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
     kn = c.hist[HIST_KN][i]; kt = c.hist[HIST_KT][i];
     tanPhi = c.tanPhi[i];
     if (CP2 == WDEM_CP2_HERTZ) { hz[0] = c.hist[HIST_E0][i]; hz[1] = c.hist[HIST_E1][i]; hz[2] = c.hist[HIST_E2][i]; hz[3] = c.hist[HIST_E3][i]; }
-    if (P.updatePhysNow) cp2<CP2>(P, ma.y, mb.y, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
+    if (P.updatePhysNow) cp2<CP2>(P, matA, matB, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
   }
   const d3 cur2 = cross(cur0, cur1);
 
@@ -215,7 +232,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
         // Eigen maxCoeff = maxi(maxi(f0,f1),f2) with maxi(a,b) = a<b ? b : a
         double m01 = (fx < fy) ? fy : fx;
         double mm = (m01 < fz) ? fz : m01;
-        if (isnan(mm)) { atomicCAS(&st->code, 0, WDEM_ERR_NAN); st->detail = a; }
+        if (isnan(mm)) { if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = a; }
       }
       if (P.relRollStiff > 0. && P.rollTanPhi > 0.) {
         double charLen = fabs(r1) + fabs(r2);
@@ -251,7 +268,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
       double eta = (hz[2] > 0 ? hz[2] * sqrt(sqrt(dmax(-uN, 0.))) : 0.);
       double Fnv = eta * velN;
       // HertzPhys.alpha = mean of the materials' alpha (Hertz.cpp:52); the clamp applies when it is 0
-      const double alphaC = .5 * (c_mats[ma.y].alpha + c_mats[mb.y].alpha);
+      const double alphaC = .5 * (c_mats[p.meta[a].y].alpha + c_mats[p.meta[b].y].alpha);
       if (alphaC == 0. && P.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
       fx = Fne + Fna + Fnv;
       kt = hz[1] * sqrt(uN < 0 ? -uN : 0);
@@ -273,11 +290,11 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
 
   if (!keep) {
     // ContactContainer::requestRemoval: geom and phys dropped, collider decides in the next step
-    c.state[i] = CS_PENDING;
+    c.state[i] = CS_PENDING | sb;
     return;
   }
   // persistent history
-  c.state[i] = CS_REAL;
+  c.state[i] = CS_REAL | sb;
   c.hist[HIST_T0X][i] = cur0.x; c.hist[HIST_T0Y][i] = cur0.y; c.hist[HIST_T0Z][i] = cur0.z;
   c.hist[HIST_T1X][i] = cur1.x; c.hist[HIST_T1Y][i] = cur1.y; c.hist[HIST_T1Z][i] = cur1.z;
   c.hist[HIST_CX][i] = contPt.x; c.hist[HIST_CY][i] = contPt.y; c.hist[HIST_CZ][i] = contPt.z;
@@ -327,7 +344,7 @@ namespace wdem {
 // in HertzPhys (Hertz.hpp:16-31); they are pure functions of the materials, radii and masses.
 __global__ void k_init_uploaded(StepParams P, Particles p, Contacts c, long long nc) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc || c.state[i] != CS_REAL) return;
+  if (i >= nc || (c.state[i] & CS_MASK) != CS_REAL) return;
   const int2 id = c.ids[i];
   const int4 ma = p.meta[id.x], mb = p.meta[id.y];
   const double rb = p.posr[id.y].w;

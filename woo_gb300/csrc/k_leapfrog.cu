@@ -16,13 +16,20 @@ namespace wdem {
 __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double mass, unsigned flags, const Contacts& c,
                                             const Csr& csr, d3& F, d3& T) {
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
-  F = grav ? mk(mass * P.gravity[0], mass * P.gravity[1], mass * P.gravity[2]) : mk(0, 0, 0);
+  if (grav) {
+    // mass * g; a component of g that is exactly zero gives a zero of the sign of the (finite) mass,
+    // set without the multiply (g is uniform over the scene, so the branch does not diverge)
+    const bool mf = finiteBits(mass);
+    F.x = (zeroBits(P.gravity[0]) && mf) ? signedZero(mass, P.gravity[0]) : mass * P.gravity[0];
+    F.y = (zeroBits(P.gravity[1]) && mf) ? signedZero(mass, P.gravity[1]) : mass * P.gravity[1];
+    F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
+  } else F = mk(0, 0, 0);
   T = mk(0, 0, 0);
   const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
   for (int e = e0; e < e1; e++) {
     const unsigned en = csr.ent[e];
     const unsigned ci = en & 0x7fffffffu;
-    if (c.state[ci] != CS_REAL) continue;
+    if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
     const d3 f = mk(c.out[OUT_FX][ci], c.out[OUT_FY][ci], c.out[OUT_FZ][ci]);
     if (en >> 31) {
       F = F + f * -1.0;
@@ -66,12 +73,12 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const d3 inertia = xyz(p.inert[i]);
   if (!blockedAll) {
     d3 linAccel;
-    if (blockedNone) linAccel = F / mass;
+    if (blockedNone) linAccel = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
     else {
       linAccel = mk(0, 0, 0);
-      if (!(flags & 1u)) linAccel.x = linAccel.x + F.x / mass;
-      if (!(flags & 2u)) linAccel.y = linAccel.y + F.y / mass;
-      if (!(flags & 4u)) linAccel.z = linAccel.z + F.z / mass;
+      if (!(flags & 1u)) linAccel.x = linAccel.x + qdiv(F.x, mass);
+      if (!(flags & 2u)) linAccel.y = linAccel.y + qdiv(F.y, mass);
+      if (!(flags & 4u)) linAccel.z = linAccel.z + qdiv(F.z, mass);
     }
     // nonviscDamp2nd (Leapfrog.cpp:33-35)
     if (damp) {
@@ -81,14 +88,17 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       linAccel.z = linAccel.z * (1 - damping * signum(F.z * (vel.z + hd * linAccel.z)));
     }
     vel = vel + dt * linAccel;
-    if (!isZero(inertia)) {
+    // a zero torque adds zeros to angVel, which changes no bit unless angVel holds a -0 (then the
+    // reference's addition may turn it into +0): skip only when that cannot happen
+    const bool inertiaPositive = positiveBits(inertia.x) && positiveBits(inertia.y) && positiveBits(inertia.z);
+    if (!isZeroBits(inertia) && !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel))) {
       d3 angAccel;
-      if (blockedNone) angAccel = mk(T.x / inertia.x, T.y / inertia.y, T.z / inertia.z);
+      if (blockedNone) angAccel = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
       else {
         angAccel = mk(0, 0, 0);
-        if (!(flags & 8u)) angAccel.x = angAccel.x + T.x / inertia.x;
-        if (!(flags & 16u)) angAccel.y = angAccel.y + T.y / inertia.y;
-        if (!(flags & 32u)) angAccel.z = angAccel.z + T.z / inertia.z;
+        if (!(flags & 8u)) angAccel.x = angAccel.x + qdiv(T.x, inertia.x);
+        if (!(flags & 16u)) angAccel.y = angAccel.y + qdiv(T.y, inertia.y);
+        if (!(flags & 32u)) angAccel.z = angAccel.z + qdiv(T.z, inertia.z);
       }
       if (damp) {
         const double hd = 0.5 * dt;
@@ -104,7 +114,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   // leapfrogSphericalRotate (:280-297): q = AngleAxis(|w| dt, w/|w|) * q, normalised
   double4_32a o4 = p.ori[i];
   qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
-  if (!isZero(angVel)) {
+  if (!isZeroBits(angVel)) {
     double angle = sqrt(sqnorm(angVel));
     d3 axis = angVel / angle;
     double ha = 0.5 * (angle * dt);
@@ -115,9 +125,15 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   }
   ori = qnormalized(ori);
   p.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
+  p.posf[i] = make_float4((float)pos.x, (float)pos.y, (float)pos.z, (float)pr.w);
   p.velm[i] = make_double4_32a(vel.x, vel.y, vel.z, mass);
   p.angw[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, w4.w);
   p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+  // a non-finite position can never be collided again (NaN boxes overlap nothing): stop with an error,
+  // as Woo stops on a NaN force
+  if (!finiteBits(pos.x) || !finiteBits(pos.y) || !finiteBits(pos.z)) {
+    if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = i;
+  }
   // aabbIsDirty, run by the collider right after Leapfrog: moved^2 > verletDist^2
   const double4_32a lp = p.lastPos[i];
   const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
@@ -158,7 +174,10 @@ __global__ void k_state_in(Particles p, int n, const double* pos, const double* 
                            const double* ori) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (pos) { double4_32a v = p.posr[i]; v.x = pos[3 * i]; v.y = pos[3 * i + 1]; v.z = pos[3 * i + 2]; p.posr[i] = v; }
+  if (pos) {
+    double4_32a v = p.posr[i]; v.x = pos[3 * i]; v.y = pos[3 * i + 1]; v.z = pos[3 * i + 2]; p.posr[i] = v;
+    p.posf[i] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+  }
   if (vel) { double4_32a v = p.velm[i]; v.x = vel[3 * i]; v.y = vel[3 * i + 1]; v.z = vel[3 * i + 2]; p.velm[i] = v; }
   if (angVel) { double4_32a v = p.angw[i]; v.x = angVel[3 * i]; v.y = angVel[3 * i + 1]; v.z = angVel[3 * i + 2]; p.angw[i] = v; }
   if (ori) p.ori[i] = make_double4_32a(ori[4 * i], ori[4 * i + 1], ori[4 * i + 2], ori[4 * i + 3]);
@@ -179,4 +198,50 @@ void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* v
   if (n > 0) (k_state_out<<<(n + 255) / 256, 256, 0, s>>>(p, n, pos, vel, angVel, ori), ++::wdem::g_kernel_launches);
 }
 
+}  // namespace wdem
+
+namespace wdem {
+
+// FP64 issue-rate probe: independent chains of fused multiply-adds (explicit __fma_rn, so the
+// no-contraction build flag does not split them).  2 flops per FMA.
+__global__ void k_fp64_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-3, x2 = x0 + 2e-3, x3 = x0 + 3e-3;
+  double x4 = x0 + 4e-3, x5 = x0 + 5e-3, x6 = x0 + 6e-3, x7 = x0 + 7e-3;
+  for (int k = 0; k < iters; k++) {
+    x0 = __fma_rn(x0, a, b); x1 = __fma_rn(x1, a, b); x2 = __fma_rn(x2, a, b); x3 = __fma_rn(x3, a, b);
+    x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b); x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
+  }
+  double r = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (r == 1234.5678) out[blockIdx.x] = r;  // keeps the chains alive
+}
+
+double fp64_probe(cudaStream_t s, double* scratch, int sms, float* msOut) {
+  const int iters = 4096, threads = 256, blocks = sms * 8;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0); cudaEventCreate(&e1);
+  (k_fp64_probe<<<blocks, threads, 0, s>>>(scratch, iters, 0.999999, 1e-7), ++::wdem::g_kernel_launches);  // warm-up
+  cudaEventRecord(e0, s);
+  (k_fp64_probe<<<blocks, threads, 0, s>>>(scratch, iters, 0.999999, 1e-7), ++::wdem::g_kernel_launches);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  if (msOut) *msOut = ms;
+  double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e9 : 0.0;
+}
+
+}  // namespace wdem
+
+namespace wdem {
+__global__ void k_refresh_posf(Particles p, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4_32a v = p.posr[i];
+  p.posf[i] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+}
+void launch_refresh_posf(cudaStream_t s, Particles p, int n) {
+  if (n > 0) (k_refresh_posf<<<(n + 255) / 256, 256, 0, s>>>(p, n), ++::wdem::g_kernel_launches);
+}
 }  // namespace wdem

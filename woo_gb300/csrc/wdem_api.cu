@@ -247,7 +247,7 @@ int checkDeviceStatus(wdem_handle* h) {
   if (h->hst->code != 0) {
     int code = h->hst->code;
     std::string m;
-    if (code == WDEM_ERR_NAN) m = "NaN force in contact (particle #" + std::to_string(h->hst->detail) + ")";
+    if (code == WDEM_ERR_NAN) m = "NaN in the state or in a contact force (particle #" + std::to_string(h->hst->detail) + ")";
     else if (code == WDEM_ERR_OVERFLOW) m = "contact hash table overflow";
     else m = "device error " + std::to_string(code);
     return fail(h, code, m);
@@ -288,8 +288,8 @@ int rebuild(wdem_handle* h) {
   const int side = 1 - h->cur;
   if ((rc = ensureHash(h, side, nNew))) return rc;
   launch_hash_build(s, neu.c.ids, nNew, h->hk[side], h->hv[side], h->hcap[side], h->dst);
-  col_carry(s, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
-            hertz ? HIST_COUNT : HIST_FRICT);
+  col_carry(s, h->d, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
+            (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT);
   if ((rc = ensureScratch(h, nNew))) return rc;
   if ((rc = ensureCsr(h, nNew))) return rc;
   col_csr(s, neu.c, nNew, n, h->csr, cs);
@@ -366,6 +366,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.force, N) == cudaSuccess;
   ok &= dalloc(d.torque, N) == cudaSuccess;
   ok &= dalloc(d.meta, N) == cudaSuccess;
+  ok &= dalloc(d.posf, N) == cudaSuccess;
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
   ok &= dalloc(h->cs.large, N) == cudaSuccess;
   ok &= dalloc(h->cs.counts, (size_t)N + 2) == cudaSuccess;
@@ -398,7 +399,7 @@ int wdem_destroy(wdem_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   Particles& d = h->d;
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
-  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
   cudaFree(h->dSmall);
   freeContacts(h->buf[0]); freeContacts(h->buf[1]);
   cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor);
@@ -515,6 +516,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   if (!h->largeIds.empty())
     CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   h->cs.nLarge = (int)h->largeIds.size();
+  launch_refresh_posf(s, h->d, n);
   CK(cudaStreamSynchronize(s));
   h->nContacts = 0;
   h->forcesInArrays = true;
@@ -547,7 +549,8 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     if (h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[bb] == WDEM_SHAPE_WALL) std::swap(a, bb);
     ids[i] = make_int2(a, bb);
     bool real = c->real[i] != 0;
-    state[i] = real ? CS_REAL : CS_POTENTIAL;
+    state[i] = (uint8_t)((real ? CS_REAL : CS_POTENTIAL) | (h->shape[a] == WDEM_SHAPE_WALL ? CS_WALL_A : 0) |
+                         (h->shape[bb] == WDEM_SHAPE_WALL ? CS_WALL_B : 0));
     step0[i] = c->stepCreated[i];
     if (real) {
       if (!c->trsf || !c->contPt || !c->force || !c->kn || !c->kt || !c->tanPhi) return fail(h, WDEM_ERR_ARG, "real contact without history arrays");
@@ -715,7 +718,7 @@ int wdem_contact_count(wdem_handle* h, int64_t* n) {
     CK(cudaMemcpy(st.data(), h->buf[h->cur].c.state, h->nContacts, cudaMemcpyDeviceToHost));
   }
   long long k = 0;
-  for (auto v : st) if (v != CS_DEAD) k++;
+  for (auto v : st) if ((v & CS_MASK) != CS_DEAD) k++;
   *n = k;
   return WDEM_OK;
 }
@@ -727,7 +730,7 @@ int wdem_download_contacts(wdem_handle* h, wdem_contacts* c) {
   int rc;
   if ((rc = fetchContacts(h, hc))) return rc;
   std::vector<long long> order;
-  for (long long i = 0; i < (long long)hc.ids.size(); i++) if (hc.state[i] != CS_DEAD) order.push_back(i);
+  for (long long i = 0; i < (long long)hc.ids.size(); i++) if ((hc.state[i] & CS_MASK) != CS_DEAD) order.push_back(i);
   auto key = [&](long long i) {
     unsigned a = (unsigned)std::min(hc.ids[i].x, hc.ids[i].y), b = (unsigned)std::max(hc.ids[i].x, hc.ids[i].y);
     return ((unsigned long long)a << 32) | b;
@@ -737,7 +740,7 @@ int wdem_download_contacts(wdem_handle* h, wdem_contacts* c) {
   const double nan = std::numeric_limits<double>::quiet_NaN();
   for (long long o = 0; o < (long long)order.size() && o < c->n; o++) {
     long long i = order[o];
-    bool real = hc.state[i] == CS_REAL;
+    bool real = (hc.state[i] & CS_MASK) == CS_REAL;
     int a = hc.ids[i].x, b = hc.ids[i].y;
     if (c->idA) c->idA[o] = a;
     if (c->idB) c->idB[o] = b;
@@ -809,7 +812,7 @@ int wdem_get_status(wdem_handle* h, wdem_status* st) {
   std::vector<uint8_t> s(h->nContacts);
   if (h->nContacts > 0) CK(cudaMemcpy(s.data(), h->buf[h->cur].c.state, h->nContacts, cudaMemcpyDeviceToHost));
   long long live = 0, real = 0;
-  for (auto v : s) { if (v != CS_DEAD) live++; if (v == CS_REAL) real++; }
+  for (auto v : s) { if ((v & CS_MASK) != CS_DEAD) live++; if ((v & CS_MASK) == CS_REAL) real++; }
   st->nContacts = live;
   st->nReal = real;
   st->nFullRuns = h->nFullRuns;
@@ -948,6 +951,18 @@ int wdem_read_state(wdem_handle* h, int32_t n, double* pos, double* vel, double*
   if (angVel) CK(cudaMemcpyAsync(angVel, st + 6 * (size_t)n, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   if (ori) CK(cudaMemcpyAsync(ori, st + 9 * (size_t)n, 4 * sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  return WDEM_OK;
+}
+
+int wdem_fp64_peak(wdem_handle* h, double* gflops) {
+  if (!h || !gflops) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  int rc;
+  if ((rc = ensureStaging(h, std::max(64, sms * 8)))) return rc;
+  *gflops = fp64_probe(h->stream, h->staging, sms, nullptr);
+  CK(cudaGetLastError());
   return WDEM_OK;
 }
 

@@ -9,6 +9,7 @@
 //     inert   double4_32a  (ix, iy, iz, unused)
 //     ori     double4_32a  (w, x, y, z)
 //     meta    int4     (shape | wallAxis<<4 | (wallSense+1)<<8, material, mask, flags)
+//     posf    float4   FP32 copy of posr, read by the contact kernel's conservative distance cull
 //     lastPos double4_32a  position at the last collider rebuild (Aabb.nodeLastPos)
 //     bbmin, bbmax double4_32a  verlet-enlarged boxes of the last rebuild (minima/maxima)
 //     force, torque double4_32a  DemData.force/torque when materialised (upload, download)
@@ -31,7 +32,9 @@ namespace wdem {
 // kernels launched by the library in this process (incremented at every launch site)
 extern long long g_kernel_launches;
 
+// contact state byte: bits 0-1 the lifecycle state, bit 2 "pA is a wall", bit 3 "pB is a wall"
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
+enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_SHAPES = 12 };
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
@@ -71,6 +74,7 @@ struct StepParams {
 struct Particles {
   double4_32a *posr, *velm, *angw, *inert, *ori, *lastPos, *bbmin, *bbmax, *force, *torque;
   int4* meta;
+  float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
 };
 
 struct Contacts {
@@ -115,6 +119,8 @@ void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int 
 void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, const double* vel, const double* angVel,
                      const double* ori);
 void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori);
+double fp64_probe(cudaStream_t s, double* scratch, int sms, float* msOut);
+void launch_refresh_posf(cudaStream_t s, Particles p, int n);
 // ---- launchers (k_contact.cu) ----
 void upload_materials(const DevMaterial* m, int n);
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st);
@@ -149,7 +155,7 @@ void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScra
                       long long cap);
 void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
                        unsigned long long cap, DeviceStatus* st);
-void col_carry(cudaStream_t s, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
+void col_carry(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
                const unsigned* hv, unsigned long long cap, long long step, int nHist);
 void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs);
 // exclusive scan of a[0..n) in place; a[n] receives the total (the array holds n+1 entries)

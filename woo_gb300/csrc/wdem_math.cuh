@@ -6,6 +6,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+// Keeps the compiler from if-converting a skipped branch (which would issue the FP64 division
+// sequence anyway under a predicate): the empty volatile asm marks the block as having effects.
+#define WDEM_REAL_BRANCH() asm volatile("")
+
 namespace wdem {
 
 struct d3 { double x, y, z; };
@@ -24,10 +28,38 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
   return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 __device__ __forceinline__ bool isZero(d3 a) { return a.x == 0 && a.y == 0 && a.z == 0; }
+
+// Predicates on the bit patterns, evaluated on the integer pipe instead of FP64 compares (the FP64
+// pipe is the binding unit of these kernels on GB300).  Each equals its FP64 counterpart exactly.
+__device__ __forceinline__ unsigned long long bitsOf(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ bool zeroBits(double x) { return (bitsOf(x) << 1) == 0; }                     // x == 0
+__device__ __forceinline__ bool isZeroBits(d3 a) { return ((bitsOf(a.x) | bitsOf(a.y) | bitsOf(a.z)) << 1) == 0; }
+__device__ __forceinline__ bool negZero(double x) { return bitsOf(x) == 0x8000000000000000ull; }
+__device__ __forceinline__ bool hasNegZero(d3 a) { return negZero(a.x) || negZero(a.y) || negZero(a.z); }
+// y > 0 (positive, nonzero, not NaN; +inf included)
+__device__ __forceinline__ bool positiveBits(double y) {
+  long long b = __double_as_longlong(y);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool isOneBits(double x) { return bitsOf(x) == 0x3ff0000000000000ull; }       // x == 1.0
+__device__ __forceinline__ bool finiteBits(double x) { return ((bitsOf(x) >> 52) & 0x7ff) != 0x7ff; }
+// a * b for finite a and b == +-0: the zero with the product's sign
+__device__ __forceinline__ double signedZero(double a, double b) {
+  return __longlong_as_double((long long)((bitsOf(a) ^ bitsOf(b)) & 0x8000000000000000ull));
+}
+// Eigen normalize().  When the squared norm is exactly 1, sqrt gives exactly 1 and the divisions
+// are identities: skipping them changes no bit and saves FP64 issue slots.
 __device__ __forceinline__ d3 normalized(d3 a) {
   double z = sqnorm(a);
-  if (z > 0) { double n = sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
+  if (z > 0 && z != 1.0) { WDEM_REAL_BRANCH(); double n = sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
   return a;
+}
+// x / y for y > 0 finite or +inf: a zero numerator is its own quotient (keeping the sign of zero),
+// so the software FP64 division is skipped bit-exactly.
+__device__ __forceinline__ double qdiv(double x, double y) {
+  double r = x;
+  if (!(zeroBits(x) && positiveBits(y))) { WDEM_REAL_BRANCH(); r = x / y; }
+  return r;
 }
 __device__ __forceinline__ double comp(d3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 __device__ __forceinline__ void setComp(d3& a, int i, double v) { if (i == 0) a.x = v; else if (i == 1) a.y = v; else a.z = v; }
@@ -90,7 +122,7 @@ __device__ __forceinline__ qd qmul(qd a, qd b) {
 
 __device__ __forceinline__ qd qnormalized(qd q) {
   double z2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
-  if (z2 > 0) { double n = sqrt(z2); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+  if (!isOneBits(z2) && z2 > 0) { WDEM_REAL_BRANCH(); double n = sqrt(z2); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
   return q;
 }
 
