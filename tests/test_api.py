@@ -1,0 +1,84 @@
+"""The Woo-compatible Python surface (no GPU needed): scene construction, engine lists, labels,
+attribute mapping into the engine parameters, critical dt, and loud failure without a CUDA device."""
+import math
+
+import numpy as np
+import pytest
+
+import woo_gb300 as woo
+from woo_gb300 import abi, dem, utils
+from woo_gb300.core import Scene
+
+
+def small_scene(**kw):
+    m = dem.FrictMat(density=2500, young=1e7, ktDivKn=0.2, tanPhi=0.5)
+    par = [dem.Wall.make(0, axis=2, sense=1, mat=m)] + [dem.Sphere.make((0, 0, 0.011 + 0.021 * k), 0.01, mat=m) for k in range(5)]
+    return Scene(fields=[dem.DemField(gravity=(0, 0, -9.81), par=par)],
+                 engines=dem.DemField.minimalEngines(damping=0.2, dynDtPeriod=0), **kw)
+
+
+def test_minimal_engines_structure():
+    ee = utils.defaultEngines(dynDtPeriod=0)
+    assert [type(e).__name__ for e in ee] == ["Leapfrog", "InsertionSortCollider", "ContactLoop"]
+    assert ee[0].reset is True and ee[1].verletDist == -0.05
+    assert isinstance(ee[2].phyFunctors[0], dem.Cp2_FrictMat_FrictPhys)
+    assert isinstance(ee[2].lawFunctors[0], dem.Law2_L6Geom_FrictPhys_IdealElPl)
+    assert type(utils.defaultEngines()[-1]).__name__ == "DynDt"
+
+
+def test_labels_and_attributes():
+    S = small_scene()
+    assert isinstance(S.lab.contactLoop, dem.ContactLoop)
+    assert isinstance(S.lab.contactLaw, dem.Law2_L6Geom_FrictPhys_IdealElPl)
+    S.lab.contactLoop.updatePhys = "always"
+    g = dem.GpuDemEngine.fromEngines(S.engines)
+    assert g.updatePhys == "always" and g.damping == 0.2 and g.verletDist == -0.05
+    with pytest.raises(AttributeError):
+        dem.FrictMat(yuong=1)
+
+
+def test_particle_construction_matches_woo_formulas():
+    m = dem.FrictMat(density=3000)
+    p = dem.Sphere.make((1, 2, 3), 0.005, mat=m)
+    mass = ((4 / 3.0) * math.pi) * (0.005 ** 3) * 3000
+    assert p.mass == pytest.approx(mass, rel=1e-15)
+    assert np.allclose(p.inertia, 0.4 * mass * 0.005 ** 2)
+    w = dem.Wall.make(0.5, axis=1, sense=-1)
+    assert w.blocked == "xyzXYZ" and w.mask == dem.DemField.defaultBoundaryMask
+    assert np.array_equal(w.pos, [0, 0.5, 0])
+
+
+def test_crit_dt_and_auto_dt():
+    S = small_scene(dtSafety=0.4)
+    pw = 0.01 / math.sqrt(1e7 / 2500)
+    assert S.dem.critDt() == pytest.approx(pw)
+    S._prepare_dt()
+    assert S.dt == pytest.approx(0.4 * pw)
+
+
+def test_params_packing():
+    S = small_scene()
+    S._prepare_dt()
+    g = S._engine()
+    p = g._build_params(S, S.dem)
+    pa = g._pack(S.dem)
+    assert p.law == abi.LAW_IDEALELPL and p.cp2 == abi.CP2_FRICT and p.reset == 1
+    assert p.loneMask == 2 and list(p.gravity) == [0, 0, -9.81]
+    assert pa.n == 6 and pa.shape[0] == abi.SHAPE_WALL and pa.flags[0] == 63
+    assert pa.mask[1] == 5 and pa.wallAxis[0] == 2 and pa.wallSense[0] == 1
+
+
+def test_unsupported_engine_rejected():
+    S = small_scene()
+    S.engines = utils.defaultEngines(dynDtPeriod=100)
+    with pytest.raises(RuntimeError, match="DynDt"):
+        S.run(1)
+
+
+def test_fails_loudly_without_gpu():
+    from conftest import HAS_GPU
+    if HAS_GPU:
+        pytest.skip("a GPU is present")
+    S = small_scene()
+    with pytest.raises(RuntimeError):
+        S.run(1)

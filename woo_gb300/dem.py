@@ -1,0 +1,774 @@
+"""Woo's DEM surface (woo.dem): materials, shapes, particles, contacts, DemField, the functor and
+engine classes of the hot path, and GpuDemEngine, the one engine that runs them on the GPU.
+
+Names and attribute defaults follow the reference classes (cited per class).  The objects hold
+attributes only; the computation is libwdem.so (no CPU path).  Once a scene has run, particle state
+lives on the GPU: reading an attribute downloads the field's state once (bulk), writing one marks the
+field so the next run uploads the kinematic state again.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+nan = float("nan")
+
+
+def _vec3(v):
+    a = np.asarray(v, dtype=np.float64).reshape(3)
+    return a.copy()
+
+
+def _quat(q):
+    a = np.asarray(q, dtype=np.float64).reshape(4)
+    return a.copy()
+
+
+class _Attrs:
+    """Keyword constructor with defaults from a class table (like Woo's attribute macros)."""
+    _defaults = {}
+
+    def __init__(self, **kw):
+        for cls in reversed(type(self).__mro__):
+            for k, v in getattr(cls, "_defaults", {}).items():
+                setattr(self, k, v)
+        for k, v in kw.items():
+            if not any(k in getattr(c, "_defaults", {}) for c in type(self).__mro__) and k != "label":
+                raise AttributeError(f"{type(self).__name__} has no attribute {k!r}")
+            setattr(self, k, v)
+        if "label" not in kw:
+            self.label = ""
+
+    def __repr__(self):
+        return f"<{type(self).__name__}>"
+
+
+# ---------------------------------------------------------------------------------------- materials
+class Material(_Attrs):
+    """Material (src/dem/Particle.hpp:483): density 1000."""
+    _defaults = dict(density=1000.0, id=-1)
+
+
+class ElastMat(Material):
+    """ElastMat (src/dem/FrictMat.hpp:6-16): young 1e9."""
+    _defaults = dict(young=1e9)
+
+
+class FrictMat(ElastMat):
+    """FrictMat (src/dem/FrictMat.hpp:18-28): tanPhi .5, ktDivKn .2."""
+    _defaults = dict(tanPhi=0.5, ktDivKn=0.2)
+    _kind = abi.MAT_FRICT
+
+
+class HertzMat(FrictMat):
+    """HertzMat (src/dem/Hertz.hpp:5-14): surfEnergy 0, alpha 0."""
+    _defaults = dict(surfEnergy=0.0, alpha=0.0)
+    _kind = abi.MAT_HERTZ
+
+
+# ---------------------------------------------------------------------------------------- nodes
+class DemData:
+    """DemData (src/dem/Particle.hpp:189-306): per-node dynamic state and flags."""
+    DOF_X, DOF_Y, DOF_Z, DOF_RX, DOF_RY, DOF_RZ = 1, 2, 4, 8, 16, 32
+    CLUMP_CLUMPED, CLUMP_CLUMP, ENERGY_SKIP, GRAVITY_SKIP, TRACER_SKIP, DAMPING_SKIP = 64, 128, 256, 512, 1024, 2048
+
+    def __init__(self, node):
+        self._node = node
+
+    def _get(self, name):
+        return self._node._get(name)
+
+    def _set(self, name, v):
+        self._node._set(name, v)
+
+    vel = property(lambda s: s._get("vel"), lambda s, v: s._set("vel", _vec3(v)))
+    angVel = property(lambda s: s._get("angVel"), lambda s, v: s._set("angVel", _vec3(v)))
+    force = property(lambda s: s._get("force"), lambda s, v: s._set("force", _vec3(v)))
+    torque = property(lambda s: s._get("torque"), lambda s, v: s._set("torque", _vec3(v)))
+    mass = property(lambda s: float(s._get("mass")), lambda s, v: s._set("mass", float(v)))
+    inertia = property(lambda s: s._get("inertia"), lambda s, v: s._set("inertia", _vec3(v)))
+    flags = property(lambda s: int(s._get("flags")), lambda s, v: s._set("flags", int(v)))
+
+    @property
+    def blocked(self):
+        f = self.flags
+        return "".join(c for i, c in enumerate("xyzXYZ") if f & (1 << i))
+
+    @blocked.setter
+    def blocked(self, dofs):
+        f = self.flags & ~63
+        for c in dofs:
+            f |= 1 << "xyzXYZ".index(c)
+        self.flags = f
+
+    def _flag(bit):
+        return property(lambda s: bool(s.flags & bit),
+                        lambda s, v: setattr(s, "flags", (s.flags | bit) if v else (s.flags & ~bit)))
+
+    gravitySkip = _flag(512)
+    dampingSkip = _flag(2048)
+    energySkip = _flag(256)
+    del _flag
+
+    def isBlockedAll(self):
+        return (self.flags & 63) == 63
+
+
+class Node:
+    """Node (src/core/Field.hpp) with DemData; pos and ori (w, x, y, z)."""
+
+    def __init__(self, pos=(0, 0, 0), ori=(1, 0, 0, 0)):
+        self._local = dict(pos=_vec3(pos), ori=_quat(ori), vel=np.zeros(3), angVel=np.zeros(3),
+                           force=np.zeros(3), torque=np.zeros(3), mass=0.0, inertia=np.zeros(3), flags=0)
+        self._field = None
+        self._idx = -1
+        self.dem = DemData(self)
+
+    def _get(self, name):
+        if self._field is None:
+            return self._local[name].copy() if isinstance(self._local[name], np.ndarray) else self._local[name]
+        return self._field._get(self._idx, name)
+
+    def _set(self, name, v):
+        if self._field is None:
+            self._local[name] = v
+        else:
+            self._field._set(self._idx, name, v)
+
+    pos = property(lambda s: s._get("pos"), lambda s, v: s._set("pos", _vec3(v)))
+    ori = property(lambda s: s._get("ori"), lambda s, v: s._set("ori", _quat(v)))
+
+
+# ---------------------------------------------------------------------------------------- shapes
+DEFAULT_MOVABLE_MASK = 0b0101
+DEFAULT_BOUNDARY_MASK = 0b0011
+DEFAULT_LONE_MASK = 0b0010
+
+
+class Shape:
+    def __init__(self):
+        self.nodes = []
+
+
+class Sphere(Shape):
+    """Sphere (src/dem/Sphere.hpp:10-30); mass/inertia from Sphere::lumpMassInertia (Sphere.cpp:26-33)."""
+    _shape = abi.SHAPE_SPHERE
+
+    def __init__(self, radius=nan):
+        super().__init__()
+        self.radius = float(radius)
+
+    @staticmethod
+    def make(center, radius, mat=None, fixed=False, mask=DEFAULT_MOVABLE_MASK, vel=None, wire=False, color=None):
+        """woo.utils.sphere / Sphere.make (py/utils.py:153-199)."""
+        mat = mat if mat is not None else defaultMaterial()
+        sh = Sphere(radius)
+        n = Node(pos=center)
+        sh.nodes.append(n)
+        p = Particle(shape=sh, material=mat, mask=mask)
+        r = float(radius)
+        m = ((4 / 3.0) * math.pi) * (r * r * r) * mat.density
+        n.dem.mass = m
+        n.dem.inertia = np.full(3, 0.0 + ((2.0 / 5.0) * m) * (r * r))
+        if fixed:
+            n.dem.blocked = "xyzXYZ"
+        if vel is not None:
+            n.dem.vel = vel
+        return p
+
+
+class Wall(Shape):
+    """Wall (src/dem/Wall.hpp:13-37): axis-aligned plane; sense -1/0/+1."""
+    _shape = abi.SHAPE_WALL
+
+    def __init__(self, axis=0, sense=0):
+        super().__init__()
+        self.axis = int(axis)
+        self.sense = int(sense)
+
+    @staticmethod
+    def make(position, axis, sense=0, mat=None, fixed=True, mass=0, mask=DEFAULT_BOUNDARY_MASK, glAB=None, color=None):
+        """woo.utils.wall (py/utils.py:245-267)."""
+        if not fixed and mass <= 0:
+            raise ValueError("Non-fixed wall must have positive mass")
+        mat = mat if mat is not None else defaultMaterial()
+        sh = Wall(axis, sense)
+        pos = np.zeros(3)
+        if np.ndim(position) == 0:
+            pos[axis] = position
+        else:
+            pos = _vec3(position)
+        n = Node(pos=pos)
+        sh.nodes.append(n)
+        p = Particle(shape=sh, material=mat, mask=mask)
+        n.dem.mass = float(mass)
+        if fixed:
+            n.dem.blocked = "xyzXYZ"
+        return p
+
+
+def defaultMaterial():
+    """woo.utils.defaultMaterial (py/utils.py:86-92)."""
+    return FrictMat(density=1e3, young=1e7, ktDivKn=0.2, tanPhi=math.tan(0.5))
+
+
+# ---------------------------------------------------------------------------------------- particles
+class Particle:
+    """Particle (src/dem/Particle.hpp:60-130) with the uninodal shorthands pos/ori/vel/angVel/f/t."""
+
+    def __init__(self, shape=None, material=None, mask=1):
+        self.shape = shape
+        self.material = material
+        self.mask = int(mask)
+        self.id = -1
+
+    def _node(self):
+        if not self.shape or len(self.shape.nodes) != 1:
+            raise RuntimeError("uninodal particles only")
+        return self.shape.nodes[0]
+
+    pos = property(lambda s: s._node().pos, lambda s, v: setattr(s._node(), "pos", v))
+    ori = property(lambda s: s._node().ori, lambda s, v: setattr(s._node(), "ori", v))
+    vel = property(lambda s: s._node().dem.vel, lambda s, v: setattr(s._node().dem, "vel", v))
+    angVel = property(lambda s: s._node().dem.angVel, lambda s, v: setattr(s._node().dem, "angVel", v))
+    f = property(lambda s: s._node().dem.force)
+    t = property(lambda s: s._node().dem.torque)
+    mass = property(lambda s: s._node().dem.mass)
+    inertia = property(lambda s: s._node().dem.inertia)
+    blocked = property(lambda s: s._node().dem.blocked, lambda s, v: setattr(s._node().dem, "blocked", v))
+
+    @property
+    def nodes(self):
+        return self.shape.nodes
+
+    @property
+    def Ekt(self):
+        v = self.vel
+        return 0.5 * self.mass * float(v @ v)
+
+
+class ParticleContainer:
+    """S.dem.par (src/dem/ParticleContainer.hpp)."""
+
+    def __init__(self, field):
+        self._field = field
+        self._list = []
+
+    def add(self, par, nodes=-1):
+        if isinstance(par, (list, tuple)):
+            return [self.add(p) for p in par]
+        if self._field._engine_bound():
+            raise RuntimeError("adding particles after the GPU engine has started is not supported")
+        par.id = len(self._list)
+        self._list.append(par)
+        return par.id
+
+    def __getitem__(self, i):
+        return self._list[i]
+
+    def __len__(self):
+        return len(self._list)
+
+    def __iter__(self):
+        return iter(self._list)
+
+
+# ---------------------------------------------------------------------------------------- contacts
+class L6Geom:
+    """L6Geom (src/dem/L6Geom.hpp:10-24): trsf rows are... columns are the local axes."""
+
+    def __init__(self, uN, vel, angVel, trsf_cols, contPt, ori, lens, contA):
+        self.uN = uN
+        self.vel = vel
+        self.angVel = angVel
+        self.trsf = np.stack([trsf_cols[0:3], trsf_cols[3:6], trsf_cols[6:9]], axis=1)
+        self.node = Node(pos=contPt, ori=ori)
+        self.lens = lens
+        self.contA = contA
+
+
+class FrictPhys:
+    """FrictPhys (src/dem/FrictMat.hpp:30-41); HertzPhys adds kn/kt as current stiffnesses."""
+
+    def __init__(self, force, torque, kn, kt, tanPhi):
+        self.force = force
+        self.torque = torque
+        self.kn = kn
+        self.kt = kt
+        self.tanPhi = tanPhi
+
+
+class HertzPhys(FrictPhys):
+    pass
+
+
+class Contact:
+    """Contact (src/dem/Contact.hpp:47-121)."""
+
+    def __init__(self, arrays, i, field):
+        ca = arrays
+        self.id1 = int(ca.idA[i])
+        self.id2 = int(ca.idB[i])
+        self.real = bool(ca.real[i])
+        self.stepCreated = int(ca.stepCreated[i])
+        self.minDist00Sq = float(ca.minDist00Sq[i])
+        if self.real:
+            pa, pb = field.par[self.id1], field.par[self.id2]
+            r1 = -pb.shape.radius if isinstance(pa.shape, Wall) else pa.shape.radius
+            r2 = pb.shape.radius
+            lens = np.array([abs(r1), abs(r2)])
+            rr = min(r1, r2) if (r1 > 0 and r2 > 0) else (r1 if r1 > 0 else r2)
+            self.geom = L6Geom(float(ca.uN[i]), ca.geomVel[i].copy(), ca.geomAngVel[i].copy(), ca.trsf[i],
+                               ca.contPt[i], ca.geomOri[i], lens, math.pi * rr * rr)
+            cls = HertzPhys if isinstance(pa.material, HertzMat) and isinstance(pb.material, HertzMat) and \
+                field._engine_cp2() == abi.CP2_HERTZ else FrictPhys
+            self.phys = cls(ca.force[i].copy(), ca.torque[i].copy(), float(ca.kn[i]), float(ca.kt[i]), float(ca.tanPhi[i]))
+        else:
+            self.geom = None
+            self.phys = None
+
+    @property
+    def ids(self):
+        return (min(self.id1, self.id2), max(self.id1, self.id2))
+
+    def forceSign(self, p):
+        pid = p if isinstance(p, int) else p.id
+        if pid not in (self.id1, self.id2):
+            raise RuntimeError(f"Contact.forceSign: particle #{pid} does not participate in ##{self.id1}+{self.id2}.")
+        return 1 if pid == self.id1 else -1
+
+    def isFresh(self, scene):
+        return scene.step == self.stepCreated
+
+    def __repr__(self):
+        return f"<Contact ##{self.id1}+{self.id2}>"
+
+
+class ContactContainer:
+    """S.dem.con (src/dem/ContactContainer.hpp:16-140): all contacts by linear index or id pair;
+    iteration yields real contacts only."""
+
+    def __init__(self, field):
+        self._field = field
+
+    def _arrays(self):
+        return self._field._contacts()
+
+    def __len__(self):
+        return self._arrays().n
+
+    def __getitem__(self, key):
+        ca = self._arrays()
+        if isinstance(key, (tuple, list)):
+            a, b = min(key), max(key)
+            k = (a << 32) | b
+            idx = np.nonzero(ca.keys() == k)[0]
+            return Contact(ca, int(idx[0]), self._field) if len(idx) else None
+        n = ca.n
+        if key < -n or key >= n:
+            raise IndexError(f"Linear index out of range ({-n}..{n - 1})")
+        return Contact(ca, key % n, self._field)
+
+    def __iter__(self):
+        ca = self._arrays()
+        for i in np.nonzero(ca.real)[0]:
+            yield Contact(ca, int(i), self._field)
+
+    def countReal(self):
+        return int(self._arrays().real.sum())
+
+    def realRatio(self):
+        n = len(self)
+        return self.countReal() / n if n else float("nan")
+
+    def exists(self, a, b):
+        return self[(a, b)] is not None
+
+    def existsReal(self, a, b):
+        c = self[(a, b)]
+        return c is not None and c.real
+
+
+# ---------------------------------------------------------------------------------------- field
+_FIELD_ARRAY_NAMES = ("pos", "ori", "vel", "angVel", "force", "torque", "mass", "inertia", "flags")
+
+
+class DemField:
+    """DemField (src/dem/Particle.hpp:310-391)."""
+    defaultMovableBit, defaultBoundaryBit, defaultOutletBit, defaultStaticBit = 1, 2, 4, 8
+    defaultLoneMask, defaultMovableMask, defaultBoundaryMask = 2, 5, 3
+    defaultStaticMask, defaultInletMask, defaultOutletMask, defaultHighestBit = 11, 5, 4, 8
+
+    def __init__(self, gravity=(0, 0, 0), distFactor=-1.0, loneMask=DEFAULT_LONE_MASK, par=None):
+        self.gravity = _vec3(gravity)
+        self.distFactor = float(distFactor)
+        self.loneMask = int(loneMask)
+        self.par = ParticleContainer(self)
+        self.con = ContactContainer(self)
+        self.scene = None
+        self._engine = None
+        self._arrays = None      # abi.ParticleArrays once bound to an engine
+        self._stale = False      # device state newer than _arrays
+        self._dirty = set()      # host edits not yet uploaded
+        self._con_cache = None
+        if par:
+            self.par.add(list(par))
+
+    # --- binding to the engine
+    def _engine_bound(self):
+        return self._engine is not None
+
+    def _engine_cp2(self):
+        return self._engine._cp2_kind if self._engine else abi.CP2_FRICT
+
+    def _bind(self, engine, arrays):
+        self._engine = engine
+        self._arrays = arrays
+        for p in self.par:
+            for n in p.shape.nodes:
+                n._field, n._idx = self, p.id
+
+    def _get(self, idx, name):
+        if self._stale:
+            self._engine._download_particles(self)
+        v = getattr(self._arrays, name)[idx]
+        return v.copy() if isinstance(v, np.ndarray) else (float(v) if name == "mass" else int(v))
+
+    def _set(self, idx, name, v):
+        if self._stale:
+            self._engine._download_particles(self)
+        getattr(self._arrays, name)[idx] = v
+        self._dirty.add(name)
+
+    def _contacts(self):
+        if self._engine is None:
+            return abi.ContactArrays(0)
+        if self._con_cache is None:
+            self._con_cache = self._engine._download_contacts()
+        return self._con_cache
+
+    # --- Woo API
+    @property
+    def nodes(self):
+        return [p.shape.nodes[0] for p in self.par]
+
+    def critDt(self):
+        """DemField::critDt -> DemFuncs::pWaveDt (src/dem/Particle.cpp:399-404, src/dem/Funcs.cpp:151-175)."""
+        dt = math.inf
+        for p in self.par:
+            if isinstance(p.shape, Sphere) and isinstance(p.material, ElastMat):
+                dt = min(dt, p.shape.radius / (1.0 * math.sqrt(p.material.young / p.material.density)))
+        return dt
+
+    @staticmethod
+    def minimalEngines(**kw):
+        from . import utils
+        return utils.defaultEngines(**kw)
+
+    @staticmethod
+    def sceneHasField(scene):
+        return any(isinstance(f, DemField) for f in scene.fields)
+
+
+# ---------------------------------------------------------------------------------------- functors
+class Functor(_Attrs):
+    pass
+
+
+class BoundFunctor(Functor):
+    pass
+
+
+class Bo1_Sphere_Aabb(BoundFunctor):
+    """Bo1_Sphere_Aabb (src/dem/Sphere.hpp:33-42)."""
+
+
+class Bo1_Wall_Aabb(BoundFunctor):
+    """Bo1_Wall_Aabb (src/dem/Wall.cpp:25-38)."""
+
+
+class CGeomFunctor(Functor):
+    pass
+
+
+class Cg2_Any_Any_L6Geom__Base(CGeomFunctor):
+    """Cg2_Any_Any_L6Geom__Base (src/dem/L6Geom.hpp:28-49)."""
+    _defaults = dict(noRatch=False, iniLensTouch=True, trsfRenorm=100, approxMask=0)
+
+
+class Cg2_Sphere_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Sphere_Sphere_L6Geom (src/dem/Sphere.cpp:86-117)."""
+
+
+class Cg2_Wall_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Wall_Sphere_L6Geom (src/dem/Wall.cpp:50-84)."""
+
+
+class CPhysFunctor(Functor):
+    pass
+
+
+class Cp2_FrictMat_FrictPhys(CPhysFunctor):
+    """Cp2_FrictMat_FrictPhys (src/dem/FrictMat.cpp:20-44); tanPhi MatchMaker unset -> min."""
+    _defaults = dict(tanPhi=None)
+
+
+class Cp2_HertzMat_HertzPhys(Cp2_FrictMat_FrictPhys):
+    """Cp2_HertzMat_HertzPhys (src/dem/Hertz.hpp:52-62)."""
+    _defaults = dict(poisson=0.2, en=nan)
+
+
+class LawFunctor(Functor):
+    pass
+
+
+class Law2_L6Geom_FrictPhys_IdealElPl(LawFunctor):
+    """Law2_L6Geom_FrictPhys_IdealElPl (src/dem/IdealElPl.hpp:6-28)."""
+    _defaults = dict(iniEqlb=False, relRollStiff=0.0, relTwistStiff=0.0, rollTanPhi=0.0, noSlip=False,
+                     noBreak=False, noFrict=False)
+
+
+class Law2_L6Geom_HertzPhys_DMT(LawFunctor):
+    """Law2_L6Geom_HertzPhys_DMT (src/dem/Hertz.hpp:67-101)."""
+    _defaults = dict(noAttraction=True)
+
+
+# ---------------------------------------------------------------------------------------- engines
+class Engine(_Attrs):
+    _defaults = dict(dead=False)
+
+    def critDt(self):
+        return math.inf
+
+
+class Leapfrog(Engine):
+    """Leapfrog (src/dem/Leapfrog.hpp:17-61)."""
+    _defaults = dict(damping=0.2, reset=False, kinSplit=False, dontCollect=False)
+
+
+class InsertionSortCollider(Engine):
+    """InsertionSortCollider (src/dem/InsertionSortCollider.hpp:264-296) + AabbCollider.verletDist."""
+    _defaults = dict(verletDist=-0.05, sortAxis=0, forceInitSort=False, sortThenCollide=False)
+
+    def __init__(self, boundFunctors=None, **kw):
+        super().__init__(**kw)
+        self.boundFunctors = list(boundFunctors or [])
+
+
+class ContactLoop(Engine):
+    """ContactLoop (src/dem/ContactLoop.hpp:110-130); constructed from 3 functor lists."""
+    _defaults = dict(applyForces=True, updatePhys="never", dist00=True, evalStress=False, reorderEvery=1000)
+
+    def __init__(self, cg2=None, cp2=None, law=None, **kw):
+        super().__init__(**kw)
+        self.geoFunctors = list(cg2 or [])
+        self.phyFunctors = list(cp2 or [])
+        self.lawFunctors = list(law or [])
+
+
+class DynDt(Engine):
+    """DynDt (src/dem/DynDt.hpp): not run by the GPU engine."""
+    _defaults = dict(stepPeriod=100)
+
+
+_UPDATE_PHYS = {"never": abi.UPDATE_PHYS_NEVER, "always": abi.UPDATE_PHYS_ALWAYS, "once": abi.UPDATE_PHYS_ONCE}
+
+
+class GpuDemEngine(Engine):
+    """One GPU engine replacing [Leapfrog, InsertionSortCollider, ContactLoop].
+
+    Constructed like ContactLoop from the three functor lists (src/dem/ContactLoop.cpp:52-66), plus
+    the Leapfrog (damping, reset) and collider (verletDist) attributes.  Runs libwdem.so on one CUDA
+    device; errors come back as RuntimeError."""
+    _defaults = dict(damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
+                     updatePhys="never", dist00=True, device=0, keepGeom=True)
+
+    def __init__(self, cg2=None, cp2=None, law=None, **kw):
+        super().__init__(**kw)
+        self.geoFunctors = list(cg2 or [Cg2_Sphere_Sphere_L6Geom(), Cg2_Wall_Sphere_L6Geom()])
+        self.phyFunctors = list(cp2 or [Cp2_FrictMat_FrictPhys()])
+        self.lawFunctors = list(law or [Law2_L6Geom_FrictPhys_IdealElPl()])
+        self._h = None
+        self._mats = None
+        self._params = None
+        self._field = None
+        self._cp2_kind = abi.CP2_FRICT
+
+    @classmethod
+    def fromEngines(cls, engines):
+        """Build from Woo's [Leapfrog, InsertionSortCollider, ContactLoop] (py/utils.py:122-129)."""
+        lf = next(e for e in engines if isinstance(e, Leapfrog))
+        col = next(e for e in engines if isinstance(e, InsertionSortCollider))
+        cl = next(e for e in engines if isinstance(e, ContactLoop))
+        g = cls(cl.geoFunctors, cl.phyFunctors, cl.lawFunctors, damping=lf.damping, reset=lf.reset,
+                kinSplit=lf.kinSplit, verletDist=col.verletDist, applyForces=cl.applyForces,
+                updatePhys=cl.updatePhys, dist00=cl.dist00)
+        g.label = cl.label or "gpu"
+        g._sources = dict(leapfrog=lf, collider=col, contactLoop=cl)
+        return g
+
+    # ------------------------------------------------------------------ functor selection
+    def _functor(self, lst, classes):
+        for f in lst:
+            if isinstance(f, classes):
+                return f
+        return None
+
+    def _build_params(self, scene, field):
+        geo = self._functor(self.geoFunctors, (Cg2_Sphere_Sphere_L6Geom, Cg2_Wall_Sphere_L6Geom)) or Cg2_Sphere_Sphere_L6Geom()
+        cp2 = self._functor(self.phyFunctors, (Cp2_HertzMat_HertzPhys,)) or self._functor(self.phyFunctors, (Cp2_FrictMat_FrictPhys,))
+        law = self._functor(self.lawFunctors, (Law2_L6Geom_HertzPhys_DMT,)) or self._functor(self.lawFunctors, (Law2_L6Geom_FrictPhys_IdealElPl,))
+        if cp2 is None or law is None:
+            raise RuntimeError("GpuDemEngine needs a Cp2 (FrictMat/HertzMat) and a Law2 (IdealElPl/HertzPhys_DMT) functor")
+        if getattr(cp2, "tanPhi", None) is not None:
+            raise RuntimeError("Cp2_FrictMat_FrictPhys.tanPhi MatchMaker is not supported")
+        mats = {}
+        for p in field.par:
+            mats.setdefault(id(p.material), p.material)
+        mlist = list(mats.values())
+        self._mat_index = {id(m): i for i, m in enumerate(mlist)}
+        arr = (abi.Material * len(mlist))()
+        for i, m in enumerate(mlist):
+            arr[i].kind = getattr(m, "_kind", abi.MAT_FRICT)
+            arr[i].density = m.density
+            arr[i].young = m.young
+            arr[i].ktDivKn = getattr(m, "ktDivKn", 0.2)
+            arr[i].tanPhi = getattr(m, "tanPhi", 0.5)
+            arr[i].surfEnergy = getattr(m, "surfEnergy", 0.0)
+            arr[i].alpha = getattr(m, "alpha", 0.0)
+        self._mats = arr
+        self._mlist = mlist
+        p = abi.Params()
+        p.dt = scene.dt
+        p.step = scene.step
+        for k in range(3):
+            p.gravity[k] = field.gravity[k]
+        p.distFactor = field.distFactor
+        p.loneMask = field.loneMask
+        p.trackEnergy = 1 if scene.trackEnergy else 0
+        p.damping = self.damping
+        p.reset = 1 if self.reset else 0
+        p.kinSplit = 1 if self.kinSplit else 0
+        p.verletDist = self.verletDist
+        p.noRatch = int(geo.noRatch); p.iniLensTouch = int(geo.iniLensTouch)
+        p.trsfRenorm = int(geo.trsfRenorm); p.approxMask = int(geo.approxMask)
+        p.updatePhys = _UPDATE_PHYS[self.updatePhys] if isinstance(self.updatePhys, str) else int(self.updatePhys)
+        p.applyForces = int(self.applyForces)
+        p.dist00 = int(self.dist00)
+        if isinstance(cp2, Cp2_HertzMat_HertzPhys):
+            p.cp2 = abi.CP2_HERTZ; p.poisson = cp2.poisson; p.en = cp2.en
+        else:
+            p.cp2 = abi.CP2_FRICT; p.poisson = 0.2; p.en = nan
+        self._cp2_kind = p.cp2
+        if isinstance(law, Law2_L6Geom_HertzPhys_DMT):
+            p.law = abi.LAW_HERTZ_DMT; p.noAttraction = int(law.noAttraction)
+        else:
+            p.law = abi.LAW_IDEALELPL
+            p.noSlip = int(law.noSlip); p.noBreak = int(law.noBreak); p.noFrict = int(law.noFrict)
+            p.iniEqlb = int(law.iniEqlb)
+            p.relRollStiff = law.relRollStiff; p.relTwistStiff = law.relTwistStiff; p.rollTanPhi = law.rollTanPhi
+            p.noAttraction = 1
+        p.nMaterials = len(mlist)
+        p.materials = arr
+        return p
+
+    def _pack(self, field):
+        n = len(field.par)
+        pa = abi.ParticleArrays(n)
+        for p in field.par:
+            i = p.id
+            sh = p.shape
+            if isinstance(sh, Sphere):
+                pa.shape[i] = abi.SHAPE_SPHERE; pa.radius[i] = sh.radius
+            elif isinstance(sh, Wall):
+                pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
+            else:
+                raise RuntimeError(f"GpuDemEngine: unsupported shape {type(sh).__name__}")
+            pa.material[i] = self._mat_index[id(p.material)]
+            pa.mask[i] = p.mask
+            node = sh.nodes[0]
+            for name in _FIELD_ARRAY_NAMES:
+                getattr(pa, name)[i] = node._local[name]
+        return pa
+
+    # ------------------------------------------------------------------ engine protocol
+    def critDt(self):
+        return math.inf
+
+    def _ensure(self, scene, field):
+        if self._h is not None:
+            return
+        params = self._build_params(scene, field)
+        pa = self._pack(field)
+        h = abi.Handle(max(pa.n, 1), device=self.device)
+        h.keep_geom(self.keepGeom)
+        h.set_params(params)
+        h.upload_particles(pa)
+        h.set_params(params)
+        self._h, self._params, self._field = h, params, field
+        field._bind(self, pa)
+
+    def _refresh_from_sources(self):
+        """Attributes set on Woo's trio after the engine was built (S.lab.contactLoop.updatePhys=...)."""
+        src = getattr(self, "_sources", None)
+        if not src:
+            return
+        self.damping = src["leapfrog"].damping
+        self.updatePhys = src["contactLoop"].updatePhys
+        self.dist00 = src["contactLoop"].dist00
+
+    def run(self, scene, nSteps):
+        field = scene.dem
+        self._refresh_from_sources()
+        self._ensure(scene, field)
+        if field._dirty:
+            self._upload_edits(field)
+        p = self._params
+        p.dt = scene.dt
+        p.step = scene.step
+        p.damping = self.damping
+        for k in range(3):
+            p.gravity[k] = field.gravity[k]
+        up = _UPDATE_PHYS[self.updatePhys] if isinstance(self.updatePhys, str) else int(self.updatePhys)
+        p.updatePhys = up
+        for i, m in enumerate(self._mlist):
+            self._mats[i].young = m.young
+            self._mats[i].density = m.density
+            self._mats[i].tanPhi = getattr(m, "tanPhi", 0.5)
+            self._mats[i].ktDivKn = getattr(m, "ktDivKn", 0.2)
+        self._h.set_params(p)
+        field._stale = True
+        field._con_cache = None
+        self._h.step(nSteps)
+        if up == abi.UPDATE_PHYS_ONCE:
+            self.updatePhys = "never"
+            if getattr(self, "_sources", None):
+                self._sources["contactLoop"].updatePhys = "never"
+
+    def _upload_edits(self, field):
+        pa = field._arrays
+        n = pa.n
+        kin = {"pos", "vel", "angVel", "ori"}
+        if field._dirty <= kin:
+            self._h.write_state(n, pa.pos.ctypes.data, pa.vel.ctypes.data, pa.angVel.ctypes.data, pa.ori.ctypes.data)
+        else:
+            # mass/inertia/flags/forces changed: full upload, keeping the contact history
+            con = self._download_contacts()
+            self._h.upload_particles(pa)
+            self._h.set_params(self._params)
+            self._h.upload_contacts(con)
+        field._dirty.clear()
+
+    def _download_particles(self, field):
+        self._h.download_particles(field._arrays)
+        field._stale = False
+
+    def _download_contacts(self):
+        return self._h.download_contacts()
+
+    def status(self):
+        return self._h.status() if self._h else None
+
+    def kernelTimes(self):
+        return self._h.kernel_times() if self._h else {}

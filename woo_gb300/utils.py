@@ -1,0 +1,63 @@
+"""woo.utils slice for the DEM hot path (py/utils.py): defaultEngines / DemField.minimalEngines,
+sphere/wall constructors, defaultMaterial."""
+import math
+
+from . import dem
+from .dem import defaultMaterial  # noqa: F401
+
+
+def defaultEngines(damping=0.0, gravity=None, verletDist=-0.05, kinSplit=False, dontCollect=False, noSlip=False,
+                   noBreak=False, cp2=None, law=None, model=None, collider="sap", grid=None, dynDtPeriod=100,
+                   cpKw={}, lawKw={}):
+    """py/utils.py:94-129: [Leapfrog(reset=True), InsertionSortCollider, ContactLoop(...)] (+ DynDt).
+    Pass dynDtPeriod=0 to leave DynDt out (the GPU engine does not run it)."""
+    if gravity:
+        raise ValueError("gravity MUST NOT be specified anymore, set DemField.gravity=... instead.")
+    if model is not None:
+        raise ValueError("model= is not supported; pass cp2= and law=")
+    cp2 = [cp2 if cp2 else dem.Cp2_FrictMat_FrictPhys()]
+    law = [law if law else dem.Law2_L6Geom_FrictPhys_IdealElPl(noSlip=noSlip, noBreak=noBreak, label="contactLaw")]
+    for k, v in cpKw.items():
+        setattr(cp2[0], k, v)
+    for k, v in lawKw.items():
+        setattr(law[0], k, v)
+    if collider != "sap":
+        raise ValueError("only the sweep-and-prune collider ('sap') is provided")
+    engines = [
+        dem.Leapfrog(damping=damping, reset=True, kinSplit=kinSplit, dontCollect=dontCollect, label="leapfrog"),
+        dem.InsertionSortCollider([dem.Bo1_Sphere_Aabb(), dem.Bo1_Wall_Aabb()], label="collider", verletDist=verletDist),
+        dem.ContactLoop([dem.Cg2_Sphere_Sphere_L6Geom(), dem.Cg2_Wall_Sphere_L6Geom()], cp2, law, applyForces=True,
+                        label="contactLoop"),
+    ]
+    if dynDtPeriod > 0:
+        engines.append(dem.DynDt(stepPeriod=dynDtPeriod, label="dynDt"))
+    return engines
+
+
+def sphere(center, radius, mat=None, fixed=False, wire=False, color=None, highlight=False,
+           mask=dem.DEFAULT_MOVABLE_MASK, vel=None):
+    """py/utils.py:153-199."""
+    return dem.Sphere.make(center, radius, mat=mat, fixed=fixed, mask=mask, vel=vel)
+
+
+def wall(position, axis, sense=0, glAB=None, fixed=True, mass=0, color=None, mat=None, visible=True,
+         mask=dem.DEFAULT_BOUNDARY_MASK):
+    """py/utils.py:245-267."""
+    return dem.Wall.make(position, axis, sense=sense, mat=mat, fixed=fixed, mass=mass, mask=mask)
+
+
+def wallBox(box, which=(1, 1, 1, 1, 1, 1), **kw):
+    """py/utils.py:269-: six walls of an axis-aligned box facing inwards."""
+    lo, hi = box
+    out = []
+    for ax in range(3):
+        if which[2 * ax]:
+            out.append(wall(lo[ax], ax, sense=1, **kw))
+        if which[2 * ax + 1]:
+            out.append(wall(hi[ax], ax, sense=-1, **kw))
+    return out
+
+
+def spherePWaveDt(radius, density, young):
+    """py/utils.py:77-: r / sqrt(E/rho)."""
+    return radius / math.sqrt(young / density)
