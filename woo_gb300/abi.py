@@ -332,6 +332,14 @@ class Handle:
     def read_state(self, n, pos=None, vel=None, angVel=None, ori=None):
         self.check(self.lib.wdem_read_state(self.h, int(n), pos, vel, angVel, ori))
 
+    def energy(self):
+        e = (C.c_double * 8)()
+        self.check(self.lib.wdem_get_energy(self.h, e, 8))
+        return dict(zip(ENERGY_NAMES, list(e)))
+
+    def reset_energy(self):
+        self.check(self.lib.wdem_reset_energy(self.h))
+
     def fp64_peak(self):
         v = C.c_double()
         self.check(self.lib.wdem_fp64_peak(self.h, C.byref(v)))

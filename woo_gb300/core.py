@@ -116,4 +116,16 @@ class Scene:
 
     @property
     def energy(self):
-        raise RuntimeError("energy tracking is not available in the GPU engine yet")
+        """EnergyTracker (src/core/EnergyTracker.hpp): the tracked energies by name.  Slots that were
+        never touched (zero) are absent, as Woo does not create them (ZeroDontCreate)."""
+        if not self.trackEnergy:
+            return EnergyTracker({})
+        eng = self._engine()
+        if eng._h is None:
+            return EnergyTracker({})
+        return EnergyTracker({k: v for k, v in eng._h.energy().items() if v != 0.0})
+
+
+class EnergyTracker(dict):
+    def total(self):
+        return sum(self.values())

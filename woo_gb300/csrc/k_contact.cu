@@ -212,9 +212,18 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
   bool keep = true;
   double tqx = 0, tqy = 0, tqz = 0;
   const double dt = P.dt;
+  double eEl = 0, ePl = 0, eVN = 0, eVT = 0, eBr = 0;
   if (LAW == WDEM_LAW_IDEALELPL) {
-    if (uN > 0 && !P.noBreak) keep = false;
-    else {
+    if (uN > 0 && !P.noBreak) {
+      keep = false;
+      if (P.noSlip && P.trackEnergy) {
+        // elastic potential lost when a contact breaks without slipping (IdealElPl.cpp:28-40)
+        const double Fn = kn * uN;
+        const double sc = dt * kt;
+        const double ft0 = fy + sc * gvel.y, ft1 = fz + sc * gvel.z;
+        eBr = .5 * (Fn * Fn / kn + (ft0 * ft0 + ft1 * ft1) / kt);
+      }
+    } else {
       fx = kn * uN;
       if (P.noFrict || tanPhi == 0.) { fy = 0; fz = 0; }
       else {
@@ -227,12 +236,17 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
           double FtNorm = sqrt(ftSq);
           double ratio = maxFt / FtNorm;
           if (FtNorm == 0.) ratio = 0.;
+          if (P.trackEnergy) ePl = (kt != 0. ? (maxFt) * (FtNorm - maxFt) / kt : 0.);
           fy *= ratio; fz *= ratio;
         }
         // Eigen maxCoeff = maxi(maxi(f0,f1),f2) with maxi(a,b) = a<b ? b : a
         double m01 = (fx < fy) ? fy : fx;
         double mm = (m01 < fz) ? fz : m01;
         if (isnan(mm)) { if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = a; }
+      }
+      if (P.trackEnergy) {
+        const double el = 0.5 * (fx * fx / kn + (kt != 0. ? (fy * fy + fz * fz) / kt : 0.));
+        eEl = isnan(el) ? 0. : el;
       }
       if (P.relRollStiff > 0. && P.rollTanPhi > 0.) {
         double charLen = fabs(r1) + fabs(r2);
@@ -271,6 +285,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
       const double alphaC = .5 * (c_mats[p.meta[a].y].alpha + c_mats[p.meta[b].y].alpha);
       if (alphaC == 0. && P.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
       fx = Fne + Fna + Fnv;
+      if (P.trackEnergy) eVN = Fnv * velN * dt;
       kt = hz[1] * sqrt(uN < 0 ? -uN : 0);
       double sc = dt * kt;
       fy = fy + sc * gvel.y;
@@ -280,14 +295,21 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
       if (ftSq > maxFt * maxFt) {
         double FtNorm = sqrt(ftSq);
         double ratio = maxFt / FtNorm;
+        if (P.trackEnergy) ePl = (.5 * (FtNorm - maxFt) + maxFt) * (FtNorm - maxFt) / kt;
         fy *= ratio; fz *= ratio;
       } else {
         fy = fy + eta * gvel.y;
         fz = fz + eta * gvel.z;
+        if (P.trackEnergy) eVT = eta * (gvel.y * gvel.y + gvel.z * gvel.z) * dt;
       }
+      if (P.trackEnergy && uN < 0) eEl = kn0 * (2 / 5.) * pown5(sqrt(-uN)) + 0.5 * (fy * fy + fz * fz) / kt;
     }
   }
 
+  if (P.trackEnergy) {
+    c.energy[EC_ELAST][i] = eEl; c.energy[EC_PLAST][i] = ePl; c.energy[EC_VISCN][i] = eVN;
+    c.energy[EC_VISCT][i] = eVT; c.energy[EC_BROKEN][i] = eBr;
+  }
   if (!keep) {
     // ContactContainer::requestRemoval: geom and phys dropped, collider decides in the next step
     c.state[i] = CS_PENDING | sb;

@@ -71,6 +71,28 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const double4_32a pr = p.posr[i];
   d3 pos = xyz(pr);
   const d3 inertia = xyz(p.inert[i]);
+  if (P.trackEnergy) {
+    // Leapfrog::doDampingDissipation and doGravityWork (Leapfrog.cpp:53-74), mid-step values
+    double eDamp = 0, eGrav = 0;
+    if (damp && !(flags & WDEM_ENERGY_SKIP)) {
+      const d3 av = mk(fabs(vel.x), fabs(vel.y), fabs(vel.z)), af = mk(fabs(F.x), fabs(F.y), fabs(F.z));
+      const d3 aw = mk(fabs(angVel.x), fabs(angVel.y), fabs(angVel.z)), at = mk(fabs(T.x), fabs(T.y), fabs(T.z));
+      eDamp = dot(av, af) * damping * dt + dot(aw, at) * damping * dt;
+    }
+    if (P.hasGravity && !(flags & WDEM_GRAVITY_SKIP)) {
+      const d3 g = mk(P.gravity[0], P.gravity[1], P.gravity[2]);
+      if (blockedNone) eGrav = -dot(g, vel) * mass * dt;
+      else {
+        if (!(flags & 1u)) eGrav = eGrav - g.x * vel.x * mass * dt;
+        if (!(flags & 2u)) eGrav = eGrav - g.y * vel.y * mass * dt;
+        if (!(flags & 4u)) eGrav = eGrav - g.z * vel.z * mass * dt;
+      }
+    }
+    p.energy[EP_DAMP][i] = eDamp;
+    p.energy[EP_GRAV][i] = eGrav;
+  }
+  const d3 vel0 = vel, angVel0 = angVel;
+  d3 linAccelE = mk(0, 0, 0), angAccelE = mk(0, 0, 0);
   if (!blockedAll) {
     d3 linAccel;
     if (blockedNone) linAccel = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
@@ -88,6 +110,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       linAccel.z = linAccel.z * (1 - damping * signum(F.z * (vel.z + hd * linAccel.z)));
     }
     vel = vel + dt * linAccel;
+    linAccelE = linAccel;
     // a zero torque adds zeros to angVel, which changes no bit unless angVel holds a -0 (then the
     // reference's addition may turn it into +0): skip only when that cannot happen
     const bool inertiaPositive = positiveBits(inertia.x) && positiveBits(inertia.y) && positiveBits(inertia.z);
@@ -107,7 +130,22 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
         angAccel.z = angAccel.z * (1 - damping * signum(T.z * (angVel.z + hd * angAccel.z)));
       }
       angVel = angVel + dt * angAccel;
+      angAccelE = angAccel;
     }
+  }
+  if (P.trackEnergy) {
+    // Leapfrog::doKineticEnergy, spherical (Leapfrog.cpp:76-98): on-step velocities
+    double ek = 0;
+    if (!(flags & WDEM_ENERGY_SKIP)) {
+      const d3 pv = blockedAll ? mk(0, 0, 0) : vel0, pw = blockedAll ? mk(0, 0, 0) : angVel0;
+      const d3 cfv = pv + .5 * dt * linAccelE, cfa = pw + .5 * dt * angAccelE;
+      const double Etrans = .5 * mass * sqnorm(cfv);
+      double Erot = 0.5 * dot(cfa, mk(inertia.x * cfa.x, inertia.y * cfa.y, inertia.z * cfa.z));
+      const double imax = dmax3(inertia);
+      if (isnan(Erot) || isinf(imax)) Erot = 0;
+      ek = Etrans + Erot;
+    }
+    p.energy[EP_KIN][i] = ek;
   }
   // leapfrogTranslate (:275-278)
   pos = pos + vel * dt;
@@ -244,4 +282,45 @@ __global__ void k_refresh_posf(Particles p, int n) {
 void launch_refresh_posf(cudaStream_t s, Particles p, int n) {
   if (n > 0) (k_refresh_posf<<<(n + 255) / 256, 256, 0, s>>>(p, n), ++::wdem::g_kernel_launches);
 }
+}  // namespace wdem
+
+namespace wdem {
+
+// Deterministic sum: each block reduces a fixed slice in a fixed shared-memory tree, then one block
+// sums the block partials the same way.  The result is independent of scheduling.
+static const int ER_T = 256;
+__global__ void k_esum(const double* x, long long n, double* partials) {
+  __shared__ double sh[ER_T];
+  long long base = (long long)blockIdx.x * ER_T * 8;
+  double acc = 0;
+  for (int k = 0; k < 8; k++) {
+    long long i = base + (long long)k * ER_T + threadIdx.x;
+    if (i < n) acc = acc + x[i];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = ER_T / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+__global__ void k_efinal(const double* partials, long long nb, double* acc, int reset) {
+  __shared__ double sh[ER_T];
+  double a = 0;
+  for (long long i = threadIdx.x; i < nb; i += ER_T) a = a + partials[i];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int off = ER_T / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *acc = reset ? sh[0] : *acc + sh[0];
+}
+void energy_accumulate(cudaStream_t s, const double* x, long long n, double* partials, double* acc, bool reset) {
+  long long nb = (n + ER_T * 8 - 1) / (ER_T * 8);
+  if (nb > 0) (k_esum<<<(unsigned)nb, ER_T, 0, s>>>(x, n, partials), ++::wdem::g_kernel_launches);
+  (k_efinal<<<1, ER_T, 0, s>>>(partials, nb, acc, reset ? 1 : 0), ++::wdem::g_kernel_launches);
+}
+
 }  // namespace wdem

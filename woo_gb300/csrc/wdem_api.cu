@@ -86,6 +86,9 @@ struct wdem_handle {
   std::string err;
   double* staging = nullptr;    // 13 n doubles for wdem_write_state / wdem_read_state
   long long stagingCap = 0;
+  double* dEnergy = nullptr;    // WDEM_E_COUNT accumulators
+  double* ePartials = nullptr;  // block partials of the energy sums
+  long long ePartialsCap = 0;
 };
 
 namespace {
@@ -115,6 +118,7 @@ void freeContacts(ContactBuf& b) {
   for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
   for (int k = 0; k < OUT_COUNT; k++) cudaFree(c.out[k]);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
+  for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   memset(&c, 0, sizeof(c));
   b.cap = 0;
 }
@@ -132,6 +136,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom) {
   for (int k = 0; k < nh; k++) if ((e = dalloc(c.hist[k], cap))) return e;
   for (int k = 0; k < OUT_COUNT; k++) if ((e = dalloc(c.out[k], cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
+  for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   b.cap = cap;
   b.hertz = hertz;
   b.geom = geom;
@@ -239,6 +244,15 @@ int ensureCsr(wdem_handle* h, long long nc) {
     long long cap = std::max<long long>(2 * nc + 1, h->csrCap * 3 / 2);
     CK(dalloc(h->csr.ent, cap));
     h->csrCap = cap;
+  }
+  return WDEM_OK;
+}
+
+int ensurePartials(wdem_handle* h, long long n) {
+  long long need = n / 2048 + 16;
+  if (need > h->ePartialsCap) {
+    CK(dalloc(h->ePartials, need));
+    h->ePartialsCap = need;
   }
   return WDEM_OK;
 }
@@ -367,6 +381,8 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.torque, N) == cudaSuccess;
   ok &= dalloc(d.meta, N) == cudaSuccess;
   ok &= dalloc(d.posf, N) == cudaSuccess;
+  for (int k = 0; k < 3; k++) ok &= dalloc(d.energy[k], N) == cudaSuccess;
+  ok &= dalloc(h->dEnergy, WDEM_E_COUNT) == cudaSuccess;
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
   ok &= dalloc(h->cs.large, N) == cudaSuccess;
   ok &= dalloc(h->cs.counts, (size_t)N + 2) == cudaSuccess;
@@ -384,6 +400,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= cudaMallocHost((void**)&h->hcounts, 4 * sizeof(unsigned)) == cudaSuccess;
   if (!ok) { wdem_destroy(h); return WDEM_ERR_CUDA; }
   cudaMemset(h->dst, 0, sizeof(DeviceStatus));
+  cudaMemset(h->dEnergy, 0, sizeof(double) * WDEM_E_COUNT);
   cudaMemset(h->csr.rowptr, 0, sizeof(int) * ((size_t)N + 1));
   memset(h->hst, 0, sizeof(DeviceStatus));
   // an empty contact buffer on the current side
@@ -400,6 +417,8 @@ int wdem_destroy(wdem_handle* h) {
   Particles& d = h->d;
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
   cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
+  for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
+  cudaFree(h->dEnergy); cudaFree(h->ePartials);
   cudaFree(h->dSmall);
   freeContacts(h->buf[0]); freeContacts(h->buf[1]);
   cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor);
@@ -594,6 +613,13 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
       PhaseTimer t(h, PH_LEAPFROG);
       launch_leapfrog(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
     }
+    if (h->P.trackEnergy) {
+      int rc0;
+      if ((rc0 = ensurePartials(h, std::max<long long>(h->n, h->nContacts)))) return rc0;
+      energy_accumulate(s, h->d.energy[EP_GRAV], h->n, h->ePartials, h->dEnergy + WDEM_E_GRAV, false);
+      energy_accumulate(s, h->d.energy[EP_DAMP], h->n, h->ePartials, h->dEnergy + WDEM_E_NONVISCDAMP, false);
+      energy_accumulate(s, h->d.energy[EP_KIN], h->n, h->ePartials, h->dEnergy + WDEM_E_KINETIC, true);
+    }
     h->forcesInArrays = false;
     CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -606,9 +632,24 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
       PhaseTimer t(h, PH_COLLIDER);
       if ((rc = rebuild(h))) return rc;
     }
+    if (h->P.trackEnergy && h->nContacts > 0) {
+      for (int k = 0; k < EC_COUNT; k++)
+        CK(cudaMemsetAsync(h->buf[h->cur].c.energy[k], 0, sizeof(double) * h->nContacts, s));
+    }
     {
       PhaseTimer t(h, PH_CONTACTS);
       launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst);
+    }
+    if (h->P.trackEnergy) {
+      int rc0;
+      if ((rc0 = ensurePartials(h, std::max<long long>(h->n, h->nContacts)))) return rc0;
+      const Contacts& cc = h->buf[h->cur].c;
+      const long long nc = h->nContacts;
+      energy_accumulate(s, cc.energy[EC_ELAST], nc, h->ePartials, h->dEnergy + WDEM_E_ELAST, true);
+      energy_accumulate(s, cc.energy[EC_PLAST], nc, h->ePartials, h->dEnergy + WDEM_E_PLAST, false);
+      energy_accumulate(s, cc.energy[EC_VISCN], nc, h->ePartials, h->dEnergy + WDEM_E_VISCN, false);
+      energy_accumulate(s, cc.energy[EC_VISCT], nc, h->ePartials, h->dEnergy + WDEM_E_VISCT, false);
+      energy_accumulate(s, cc.energy[EC_BROKEN], nc, h->ePartials, h->dEnergy + WDEM_E_BROKEN, false);
     }
     if (h->updatePhys == WDEM_UPDATE_PHYS_ONCE) { h->updatePhys = WDEM_UPDATE_PHYS_NEVER; h->raw.updatePhys = WDEM_UPDATE_PHYS_NEVER; }
     h->step++;
@@ -794,11 +835,20 @@ int wdem_crit_dt(wdem_handle* h, double* dt) {
 }
 
 int wdem_get_energy(wdem_handle* h, double* e, int32_t n) {
-  if (!h || !e) return WDEM_ERR_ARG;
-  for (int k = 0; k < n; k++) e[k] = 0;
-  return fail(h, WDEM_ERR_UNSUPPORTED, "energy tracking is not implemented on the GPU engine");
+  if (!h || !e || n < 0) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  double v[WDEM_E_COUNT];
+  CK(cudaMemcpyAsync(v, h->dEnergy, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < n; k++) e[k] = k < WDEM_E_COUNT ? v[k] : 0.0;
+  return WDEM_OK;
 }
-int wdem_reset_energy(wdem_handle* h) { return h ? WDEM_OK : WDEM_ERR_ARG; }
+int wdem_reset_energy(wdem_handle* h) {
+  if (!h) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaMemsetAsync(h->dEnergy, 0, sizeof(double) * WDEM_E_COUNT, h->stream));
+  return WDEM_OK;
+}
 
 int wdem_get_status(wdem_handle* h, wdem_status* st) {
   if (!h || !st) return WDEM_ERR_ARG;

@@ -75,7 +75,10 @@ struct Particles {
   double4_32a *posr, *velm, *angw, *inert, *ori, *lastPos, *bbmin, *bbmax, *force, *torque;
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
+  double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
 };
+enum { EP_GRAV = 0, EP_DAMP = 1, EP_KIN = 2 };
+enum { EC_ELAST = 0, EC_PLAST = 1, EC_VISCN = 2, EC_VISCT = 3, EC_BROKEN = 4, EC_COUNT = 5 };
 
 struct Contacts {
   int2* ids;
@@ -85,6 +88,7 @@ struct Contacts {
   double* tanPhi;
   double* out[OUT_COUNT];
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
+  double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
 };
 
 struct Csr {
@@ -121,6 +125,8 @@ void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, cons
 void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori);
 double fp64_probe(cudaStream_t s, double* scratch, int sms, float* msOut);
 void launch_refresh_posf(cudaStream_t s, Particles p, int n);
+// deterministic sum of x[0..n) added to *acc (or stored, when reset): fixed-order block trees
+void energy_accumulate(cudaStream_t s, const double* x, long long n, double* partials, double* acc, bool reset);
 // ---- launchers (k_contact.cu) ----
 void upload_materials(const DevMaterial* m, int n);
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st);

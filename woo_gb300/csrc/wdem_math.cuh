@@ -126,6 +126,12 @@ __device__ __forceinline__ qd qnormalized(qd q) {
   return q;
 }
 
+// Eigen maxCoeff of a 3-vector: maxi(maxi(a0,a1),a2), maxi(a,b) = a<b ? b : a
+__device__ __forceinline__ double dmax3(d3 a) {
+  double m = (a.x < a.y) ? a.y : a.x;
+  return (m < a.z) ? a.z : m;
+}
+
 __device__ __forceinline__ double signum(double f) { return f < 0 ? -1.0 : (f > 0 ? 1.0 : 0.0); }
 
 // x^n by squaring, n small and fixed (pown of Woo's Math.hpp)
