@@ -152,8 +152,20 @@ typedef struct wdem_contacts {
   double* torque;         /* 3n CPhys.torque (local) */
   double* kn;             /* FrictPhys.kn */
   double* kt;             /* FrictPhys.kt */
-  double* tanPhi;         /* FrictPhys.tanPhi */
+  double* tanPhi;          /* FrictPhys.tanPhi */
+  int32_t* cellDist;       /* 3n Contact.cellDist (periodic cell offset of pB) */
 } wdem_contacts;
+
+/* ---- periodic cell (Cell, src/core/Cell.hpp:22-187), row-major 3x3 matrices ---------------------- */
+typedef struct wdem_cell {
+  int32_t periodic;        /* Scene.isPeriodic */
+  int32_t homoDeform;      /* Cell.homoDeform; only 4 (HOMO_GRADV2, the default) is supported */
+  double hSize[9];         /* Cell.hSize (columns = cell base vectors) */
+  double trsf[9];          /* Cell.trsf */
+  double gradV[9];         /* Cell.gradV (at t - dt/2) */
+  double nextGradV[9];     /* Cell.nextGradV (applied from the next step) */
+  double pprevHsize[9];    /* Cell.pprevHsize, output only */
+} wdem_cell;
 
 /* ---- status ----------------------------------------------------------------------------------- */
 typedef struct wdem_status {

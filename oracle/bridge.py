@@ -44,6 +44,9 @@ def load(variant="liborc.so"):
         "orc_step_count": ([h], C.c_long),
         "orc_set_update_phys": ([h, C.c_int], C.c_int),
         "orc_set_young": ([h, C.c_int, C.c_double], C.c_int),
+        "orc_set_cell": ([h, C.c_int, abi.D], C.c_int),
+        "orc_get_cell": ([h, abi.D], C.c_int),
+        "orc_stress": ([h, abi.D], C.c_int),
         "orc_collide_boxes": ([C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, C.c_int, abi.I32, C.c_long], C.c_long),
         "orc_collide_frames": ([C.c_int, C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, abi.I32, C.c_long], C.c_long),
     }
@@ -58,12 +61,14 @@ def load(variant="liborc.so"):
 class Oracle:
     """One CPU restatement of Woo's DEM scene (Leapfrog, InsertionSortCollider, ContactLoop)."""
 
-    def __init__(self, params, particles, contacts=None, canonical=True, sort_axis=0, variant="liborc.so"):
+    def __init__(self, params, particles, contacts=None, canonical=True, sort_axis=0, variant="liborc.so", cell=None):
         self.lib = load(variant)
         self.h = self.lib.orc_create()
         self._params = params
         self.lib.orc_set_mode(self.h, 1 if canonical else 0, 1 if canonical else 0, sort_axis)
         self.check(self.lib.orc_set_params(self.h, C.byref(params)))
+        if cell is not None:
+            self.set_cell(**cell)
         s = particles.struct()
         self.check(self.lib.orc_upload_particles(self.h, C.byref(s)))
         self.check(self.lib.orc_set_params(self.h, C.byref(params)))
@@ -114,6 +119,26 @@ class Oracle:
 
     def crit_dt(self):
         return self.lib.orc_crit_dt(self.h)
+
+    def set_cell(self, hSize, trsf=None, gradV=None, nextGradV=None):
+        """Periodic cell: 3x3 hSize (columns = base vectors), trsf, gradV, nextGradV."""
+        m = np.zeros(36)
+        m[0:9] = np.asarray(hSize, float).reshape(9)
+        m[9:18] = np.asarray(trsf if trsf is not None else np.eye(3), float).reshape(9)
+        m[18:27] = np.asarray(gradV if gradV is not None else np.zeros((3, 3)), float).reshape(9)
+        m[27:36] = np.asarray(nextGradV if nextGradV is not None else np.zeros((3, 3)), float).reshape(9)
+        self.lib.orc_set_cell(self.h, 1, abi.ptr(m, C.c_double))
+
+    def cell(self):
+        m = np.zeros(45)
+        self.lib.orc_get_cell(self.h, abi.ptr(m, C.c_double))
+        return dict(hSize=m[0:9].reshape(3, 3), trsf=m[9:18].reshape(3, 3), gradV=m[18:27].reshape(3, 3),
+                    nextGradV=m[27:36].reshape(3, 3), pprevHsize=m[36:45].reshape(3, 3))
+
+    def stress(self):
+        m = np.zeros(9)
+        self.lib.orc_stress(self.h, abi.ptr(m, C.c_double))
+        return m.reshape(3, 3)
 
     def energy(self):
         e = (C.c_double * 8)()

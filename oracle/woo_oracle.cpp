@@ -38,6 +38,7 @@
 #include <string>
 #include <vector>
 #include <chrono>
+#include <array>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -85,6 +86,111 @@ struct M3 {
 };
 /* M^T v: component i is column i dotted with v */
 static inline V3 mulT(const M3& m, const V3& v) { return V3(dot(m.c[0], v), dot(m.c[1], v), dot(m.c[2], v)); }
+
+/* general 3x3 helpers for the periodic cell, row-major r[i][k] */
+struct Mat {
+  double r[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  static Mat I() { Mat m; m.r[0][0] = m.r[1][1] = m.r[2][2] = 1; return m; }
+  V3 col(int k) const { return V3(r[0][k], r[1][k], r[2][k]); }
+};
+static Mat mmul(const Mat& a, const Mat& b) {
+  Mat c;
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][0] * b.r[0][k] + a.r[i][1] * b.r[1][k] + a.r[i][2] * b.r[2][k];
+  return c;
+}
+static V3 mvec(const Mat& a, const V3& v) {
+  return V3(a.r[0][0] * v.x + a.r[0][1] * v.y + a.r[0][2] * v.z, a.r[1][0] * v.x + a.r[1][1] * v.y + a.r[1][2] * v.z,
+            a.r[2][0] * v.x + a.r[2][1] * v.y + a.r[2][2] * v.z);
+}
+static V3 mvecI(const Mat& a, int c0, int c1, int c2) {
+  return mvec(a, V3((double)c0, (double)c1, (double)c2));
+}
+static Mat madd(const Mat& a, const Mat& b, double sb) {
+  Mat c;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] + sb * b.r[i][k];
+  return c;
+}
+static Mat mscale(const Mat& a, double s) { Mat c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] * s; return c; }
+static Mat mtrans(const Mat& a) { Mat c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[k][i]; return c; }
+static double mdet(const Mat& m) {
+  const double (*a)[3] = m.r;
+  return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[1][0] * (a[0][1] * a[2][2] - a[2][1] * a[0][2]) +
+         a[2][0] * (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+}
+/* inverse by the adjugate: inv = adj(m) / det(m) */
+static Mat minv(const Mat& m) {
+  const double (*a)[3] = m.r;
+  Mat c;
+  c.r[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  c.r[0][1] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+  c.r[0][2] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  c.r[1][0] = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  c.r[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+  c.r[1][2] = a[0][2] * a[1][0] - a[0][0] * a[1][2];
+  c.r[2][0] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  c.r[2][1] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+  c.r[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  double det = a[0][0] * c.r[0][0] + a[0][1] * c.r[1][0] + a[0][2] * c.r[2][0];
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] / det;
+  return c;
+}
+/* leviCivita (src/supp/base/Math.hpp:223-228): (m12-m21, m20-m02, m01-m10) */
+static V3 leviCivita(const Mat& m) { return V3(m.r[1][2] - m.r[2][1], m.r[2][0] - m.r[0][2], m.r[0][1] - m.r[1][0]); }
+
+/* Cell (src/core/Cell.hpp:22-187, Cell.cpp), homoDeform = HOMO_GRADV2 only */
+struct Cell {
+  Mat trsf = Mat::I(), hSize = Mat::I(), pprevHsize = Mat::I(), gradV, nextGradV, W;
+  V3 spinVec, size, cos;
+  Mat shearTrsf = Mat::I(), unshearTrsf = Mat::I();
+  bool hasShear = false;
+  /* Cell::integrateAndUpdate (Cell.cpp:81-120) */
+  void integrateAndUpdate(double dt) {
+    Mat trsfInc = mscale(gradV, dt);
+    trsf = madd(trsf, mmul(trsfInc, trsf), 1.0);
+    Mat prevHsize = hSize;
+    Mat gdt2 = mscale(mscale(gradV, dt), 1. / 2.);  /* gradV*dt/2. */
+    Mat A = madd(Mat::I(), gdt2, -1.0), B = madd(Mat::I(), gdt2, 1.0);
+    hSize = mmul(mmul(minv(A), B), hSize);
+    pprevHsize = mscale(madd(prevHsize, hSize, 1.0), .5);
+    if (mdet(hSize) == 0) throw std::runtime_error("Cell is degenerate (zero volume).");
+    Mat Hnorm;
+    for (int i = 0; i < 3; i++) {
+      V3 base = hSize.col(i);
+      size[i] = norm(base);
+      base = base / size[i];
+      Hnorm.r[0][i] = base.x; Hnorm.r[1][i] = base.y; Hnorm.r[2][i] = base.z;
+    }
+    for (int i = 0; i < 3; i++) {
+      int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+      cos[i] = sqnorm(cross(Hnorm.col(i1), Hnorm.col(i2)));
+    }
+    shearTrsf = Hnorm;
+    unshearTrsf = minv(shearTrsf);
+    const double (*h)[3] = hSize.r;
+    hasShear = (h[0][1] != 0 || h[0][2] != 0 || h[1][0] != 0 || h[1][2] != 0 || h[2][0] != 0 || h[2][1] != 0);
+  }
+  /* Cell::setNextGradV (Cell.cpp:60-66) */
+  void setNextGradV() {
+    gradV = nextGradV;
+    W = mscale(madd(gradV, mtrans(gradV), -1.0), .5);
+    spinVec = .5 * leviCivita(W);
+  }
+  V3 intrShiftPos(const int* cd) const { return mvecI(hSize, cd[0], cd[1], cd[2]); }
+  /* Cell::intrShiftVel, HOMO_GRADV2 (Cell.cpp:28-34): gradV*pprevHsize*cellDist */
+  V3 intrShiftVel(const int* cd) const { return mvecI(mmul(gradV, pprevHsize), cd[0], cd[1], cd[2]); }
+  /* Cell::shearAlignedExtents (Cell.cpp:68-78) */
+  V3 shearAlignedExtents(const V3& perp) const {
+    if (!hasShear) return perp;
+    V3 ret = perp;
+    for (int ax = 0; ax < 3; ax++) {
+      int ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
+      ret[ax1] += .5 * perp[ax1] * (1 / cos[ax] - 1);
+      ret[ax2] += .5 * perp[ax2] * (1 / cos[ax] - 1);
+    }
+    return ret;
+  }
+};
 
 struct Quat {
   double w = 1, x = 0, y = 0, z = 0;
@@ -180,6 +286,7 @@ struct Particle {
 
 struct Contact {
   int pA = -1, pB = -1;
+  int cellDist[3] = {0, 0, 0};
   bool geom = false, phys = false;
   int stepCreated = -1;
   double minDist00Sq = -1;
@@ -253,6 +360,9 @@ struct Scene {
   std::string err;
   int lastRunFull = 0;
   int parallel = 0;   /* OpenMP contact/node loops with a per-particle lock (reference's OpenMP build) */
+  bool periodic = false;
+  Cell cell;
+  double stress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #ifdef _OPENMP
   std::vector<omp_lock_t> locks;
   ~Scene() { for (auto& l : locks) omp_destroy_lock(&l); }
@@ -380,8 +490,16 @@ static void updateAabb(Scene& S, Particle& p) {
     double df = S.P.distFactor;
     double h = (df > 0 ? df : 1.) * p.radius;
     V3 half(h, h, h);
-    a.min = p.pos - half;
-    a.max = p.pos + half;
+    if (!S.periodic) {
+      a.min = p.pos - half;
+      a.max = p.pos + half;
+    } else {
+      /* Bo1_Sphere_Aabb::goGeneric, periodic (Sphere.cpp:66-81): unsheared centre, shear-aligned extents */
+      half = S.cell.shearAlignedExtents(half);
+      V3 c = mvec(S.cell.unshearTrsf, p.pos);
+      a.min = c - half;
+      a.max = c + half;
+    }
   } else {
     a.min = V3(-Inf, -Inf, -Inf);
     a.max = V3(Inf, Inf, Inf);
@@ -411,6 +529,100 @@ static bool aabbIsDirty(const Particle& p) {
   double d2 = sqnorm(p.bound.nodeLastPos - p.pos);
   return d2 > p.bound.maxD2;
 }
+/* InsertionSortCollider::cellWrapRel (InsertionSortCollider.cpp:624-628) */
+static double cellWrapRel(double x, double x0, double x1, int& period) {
+  double xNorm = (x - x0) / (x1 - x0);
+  period = (int)std::floor(xNorm);
+  return (xNorm - std::floor(xNorm)) * (x1 - x0);
+}
+/* spatialOverlapPeri_axis, the "new algorithm" (InsertionSortCollider.cpp:897-1010) */
+static bool spatialOverlapPeriAxis(int id1, int id2, double min1, double max1, double min2, double max2, double dim,
+                                   int& period) {
+  if (std::isinf(min1) || std::isinf(min2)) { period = 0; return true; }
+  int pmn1_2, pmx1_2, pmn2_1, pmx2_1;
+  double mn1_2 = cellWrapRel(min1, min2, min2 + dim, pmn1_2); (void)cellWrapRel(max1, min2, min2 + dim, pmx1_2);
+  double mn2_1 = cellWrapRel(min2, min1, min1 + dim, pmn2_1); (void)cellWrapRel(max2, min1, min1 + dim, pmx2_1);
+  if (pmn1_2 != pmx1_2 && pmn2_1 != pmx2_1)
+    throw std::runtime_error("InsertionSortCollider: ambiguous periodic contact ##" + std::to_string(id1) + "+" + std::to_string(id2));
+  else if (pmn2_1 == pmx2_1) { period = -pmn2_1; return mn2_1 < (max1 - min1); }
+  else { period = pmn1_2; return mn1_2 < (max2 - min2); }
+}
+/* spatialOverlapPeri (InsertionSortCollider.cpp:1027-1044) */
+static bool spatialOverlapPeri(const Scene& S, int id1, int id2, int* periods) {
+  for (int ax = 0; ax < 3; ax++)
+    if (!spatialOverlapPeriAxis(id1, id2, S.minima[3 * id1 + ax], S.maxima[3 * id1 + ax], S.minima[3 * id2 + ax],
+                                S.maxima[3 * id2 + ax], S.cell.size[ax], periods[ax]))
+      return false;
+  return true;
+}
+static bool overlapAny(const Scene& S, int a, int b) {
+  if (!S.periodic) return spatialOverlap(S, a, b);
+  int per[3];
+  return spatialOverlapPeri(S, a, b, per);
+}
+/* Periodic full run: the pair set the periodic insertion sort maintains
+ * (InsertionSortCollider.cpp:637-882): every pair overlapping under spatialOverlapPeri with its
+ * periods as Contact.cellDist; real contacts stay; non-real ones that stopped overlapping go.
+ * Candidates come from a periodic cell list (any complete candidate set gives the same result). */
+static void colliderPeriodicFull(Scene& S) {
+  const int n = (int)S.par.size();
+  /* existing non-real contacts that no longer overlap */
+  std::vector<CPtr> cur = S.linView;
+  for (auto& C : cur)
+    if (!C->isReal() && !overlapAny(S, C->pA, C->pB)) removeMaybe_fast(S, C);
+  V3 W;
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) W[k] = std::max(W[k], S.maxima[3 * i + k] - S.minima[3 * i + k]);
+  int nc[3];
+  double cw[3];
+  for (int k = 0; k < 3; k++) {
+    nc[k] = (W[k] > 0) ? (int)std::floor(S.cell.size[k] / (W[k] * (1 + 1e-6))) : 1;
+    if (nc[k] < 3) nc[k] = 1;
+    cw[k] = S.cell.size[k] / nc[k];
+  }
+  auto cellOf = [&](int i, int* c) {
+    for (int k = 0; k < 3; k++) {
+      double x = .5 * (S.minima[3 * i + k] + S.maxima[3 * i + k]);
+      double w = x - std::floor(x / S.cell.size[k]) * S.cell.size[k];
+      int v = (int)std::floor(w / cw[k]);
+      c[k] = std::min(std::max(v, 0), nc[k] - 1);
+    }
+  };
+  std::map<long, std::vector<int>> cells;
+  std::vector<std::array<int, 3>> cid(n);
+  for (int i = 0; i < n; i++) {
+    int c[3];
+    cellOf(i, c);
+    cid[i] = {c[0], c[1], c[2]};
+    cells[((long)c[2] * nc[1] + c[1]) * nc[0] + c[0]].push_back(i);
+  }
+  for (int i = 0; i < n; i++) {
+    std::vector<long> seen;
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          int c[3] = {cid[i][0] + dx, cid[i][1] + dy, cid[i][2] + dz};
+          for (int k = 0; k < 3; k++) c[k] = ((c[k] % nc[k]) + nc[k]) % nc[k];
+          long key = ((long)c[2] * nc[1] + c[1]) * nc[0] + c[0];
+          if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+          seen.push_back(key);
+          auto it = cells.find(key);
+          if (it == cells.end()) continue;
+          for (int j : it->second) {
+            if (j <= i) continue;
+            int per[3];
+            if (!spatialOverlapPeri(S, i, j, per)) continue;
+            if (findContact(S, i, j)) continue;
+            if (!mayCollide(S, S.par[i], S.par[j])) continue;
+            CPtr C = std::make_shared<Contact>();
+            C->pA = i; C->pB = j; C->stepCreated = (int)S.step;
+            for (int k = 0; k < 3; k++) C->cellDist[k] = per[k];
+            addMaybe_fast(S, C);
+          }
+        }
+  }
+}
+
 /* InsertionSortCollider::run, aperiodic (InsertionSortCollider.cpp:386-613) */
 static void colliderRun(Scene& S) {
   bool fullRun = false;
@@ -442,7 +654,19 @@ static void colliderRun(Scene& S) {
   if (!fullRun) {
     /* removePending (ContactContainer.hpp:78-93) with shouldBeRemoved (InsertionSortCollider.hpp:213-218) */
     auto pend = S.pending; S.pending.clear();
-    for (auto& pc : pend) if (pc.second || !spatialOverlap(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
+    for (auto& pc : pend) if (pc.second || !overlapAny(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
+    return;
+  }
+  if (S.periodic) {
+    S.nFullRuns++;
+    long nP = (long)S.par.size();
+    S.minima.assign(3 * nP, 0); S.maxima.assign(3 * nP, 0);
+    for (long id = 0; id < nP; id++)
+      for (int k = 0; k < 3; k++) { S.minima[3 * id + k] = S.par[id].bound.min[k]; S.maxima[3 * id + k] = S.par[id].bound.max[k]; }
+    auto pend = S.pending; S.pending.clear();
+    for (auto& pc : pend) if (pc.second || !overlapAny(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
+    for (int i = 0; i < 3; i++) S.BB[i].assign(2 * nP, Bounds());  /* marks "initialised" for the size check */
+    colliderPeriodicFull(S);
     return;
   }
   S.nFullRuns++;
@@ -530,7 +754,7 @@ static void handleSpheresLikeContact(Scene& S, Contact& C, const V3& pos1, const
   const V3 prevNormal = C.trsf.c[0];
   const V3 prevContPt = C.contPt;
   const double dt = P.dt;
-  V3 shiftVel2;  /* aperiodic */
+  V3 shiftVel2 = S.periodic ? S.cell.intrShiftVel(C.cellDist) : V3();
   V3 normRotVec = cross(prevNormal, currNormal);
   V3 midNormal = (P.approxMask & 1) ? prevNormal : 0.5 * (prevNormal + currNormal);
   if (norm(midNormal) == 0) midNormal = currNormal;
@@ -750,7 +974,7 @@ static void applyForceUninodal(Scene& S, const Contact& C, Particle& p) {
   double sign = isPA ? 1 : -1;
   V3 F = qrot(C.gori, C.force) * sign;
   V3 T = (isZero(C.torque) ? V3() : qrot(C.gori, C.torque)) * sign;
-  V3 xc = C.contPt - p.pos;
+  V3 xc = C.contPt - ((!isPA && S.periodic) ? p.pos + S.cell.intrShiftPos(C.cellDist) : p.pos);
   p.force = p.force + F;
   p.torque = p.torque + (cross(xc, F) + T);
 }
@@ -779,14 +1003,14 @@ static void contactLoopParallel(Scene& S) {
         Particle& a = S.par[C->pA];
         Particle& b = S.par[C->pB];
         if (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_WALL) continue;
-        if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) std::swap(C->pA, C->pB);
+        if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) { std::swap(C->pA, C->pB); for (int k = 0; k < 3; k++) C->cellDist[k] *= -1; }
         if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
           C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
         else C->minDist00Sq = -1;
       }
       Particle& pA = S.par[C->pA];
       Particle& pB = S.par[C->pB];
-      V3 shift2;
+      V3 shift2 = S.periodic ? S.cell.intrShiftPos(C->cellDist) : V3();
       if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
       bool geomCreated;
       if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
@@ -855,7 +1079,10 @@ static void contactLoopRun(Scene& S) {
                    (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_SPHERE) ||
                    (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL);
       if (!known) continue;
-      if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) std::swap(C->pA, C->pB); /* Contact::swapOrder */
+      if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) {  /* Contact::swapOrder (Contact.cpp:12-16) */
+        std::swap(C->pA, C->pB);
+        for (int k = 0; k < 3; k++) C->cellDist[k] *= -1;
+      }
       /* setMinDist00Sq: Sphere+Sphere only (Sphere.cpp:86-89), else -1 (ContactLoop.hpp:18) */
       if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
         C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
@@ -863,7 +1090,7 @@ static void contactLoopRun(Scene& S) {
     }
     Particle& pA = S.par[C->pA];
     Particle& pB = S.par[C->pB];
-    V3 shift2;
+    V3 shift2 = S.periodic ? S.cell.intrShiftPos(C->cellDist) : V3();
     if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
     bool geomCreated;
     if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
@@ -913,6 +1140,20 @@ static void leapfrogRun(Scene& S) {
   V3 gravity(P.gravity[0], P.gravity[1], P.gravity[2]);
   bool hasGravity = !isZero(gravity);
   const long np = (long)S.par.size();
+  /* GRADV2 matrices (Leapfrog.cpp:119-127) */
+  const bool peri = S.periodic;
+  Mat ImLL4hInv, IpLL4h, LmL;
+  V3 deltaSpinVec;
+  if (peri) {
+    const Mat& pprevL = S.cell.gradV;
+    const Mat& nnextL = S.cell.nextGradV;
+    Mat q = mscale(mscale(madd(nnextL, pprevL, 1.0), dt), 1. / 4.);   /* dt*(nnextL+pprevL)/4. */
+    ImLL4hInv = minv(madd(Mat::I(), q, -1.0));
+    IpLL4h = madd(Mat::I(), q, 1.0);
+    LmL = madd(nnextL, pprevL, -1.0);
+    deltaSpinVec = -.5 * leviCivita(mscale(madd(pprevL, mtrans(pprevL), -1.0), .5)) +
+                   .5 * leviCivita(mscale(madd(nnextL, mtrans(nnextL), -1.0), .5));
+  }
 #ifdef _OPENMP
 #pragma omp parallel for schedule(guided) if (S.parallel && !P.trackEnergy)
 #endif
@@ -945,20 +1186,29 @@ static void leapfrogRun(Scene& S) {
       /* computeAccel (:37-42) */
       if (p.isBlockedNone()) linAccel = f / p.mass;
       else for (int i = 0; i < 3; i++) if (!p.isBlockedAxisDOF(i, false)) linAccel[i] += f[i] / p.mass;
-      pprevFluctVel = p.vel; pprevFluctAngVel = p.angVel;
+      if (peri) {
+        /* Cell::pprevFluctVel / pprevFluctAngVel, HOMO_GRADV2 (Cell.cpp:36-57) */
+        pprevFluctVel = p.vel - mvec(S.cell.gradV, p.pos - dt / 2 * p.vel);
+        pprevFluctAngVel = p.angVel - S.cell.spinVec;
+      } else { pprevFluctVel = p.vel; pprevFluctAngVel = p.angVel; }
       /* nonviscDamp2nd (:33-35) */
       if (damp) for (int i = 0; i < 3; i++) linAccel[i] *= 1 - damping * Sign(f[i] * (pprevFluctVel[i] + 0.5 * dt * linAccel[i]));
-      p.vel = p.vel + dt * linAccel;
+      if (peri) p.vel = mvec(ImLL4hInv, mvec(LmL, p.pos) + mvec(IpLL4h, p.vel) + linAccel * dt);
+      else p.vel = p.vel + dt * linAccel;
       if (!isZero(p.inertia)) {
         if (!useAspherical) {
           if (p.isBlockedNone()) angAccel = V3(t.x / p.inertia.x, t.y / p.inertia.y, t.z / p.inertia.z);
           else for (int i = 0; i < 3; i++) if (!p.isBlockedAxisDOF(i, true)) angAccel[i] += t[i] / p.inertia[i];
           if (damp) for (int i = 0; i < 3; i++) angAccel[i] *= 1 - damping * Sign(t[i] * (pprevFluctAngVel[i] + 0.5 * dt * angAccel[i]));
           p.angVel = p.angVel + dt * angAccel;
+          if (peri) p.angVel = p.angVel - deltaSpinVec;
         } else {
           throw std::runtime_error("aspherical leapfrog is not restated for this particle model");
         }
       }
+    } else if (peri) {
+      /* fixed particle with GRADV2: velocity correction without acceleration (Leapfrog.cpp:207-211) */
+      p.vel = mvec(ImLL4hInv, mvec(LmL, p.pos) + mvec(IpLL4h, p.vel));
     }
     if (P.trackEnergy && !(p.flags & WDEM_ENERGY_SKIP)) {
       /* doKineticEnergy (:76-98), spherical */
@@ -1001,10 +1251,12 @@ static double pWaveDt(const Scene& S) {
 
 /* Scene::doOneStep (Scene.cpp:366-467) with engines [Leapfrog, InsertionSortCollider, ContactLoop] */
 static void doOneStep(Scene& S) {
+  if (S.periodic) S.cell.integrateAndUpdate(S.P.dt);
   if (S.P.trackEnergy) S.E.resetResettables();
   leapfrogRun(S);
   colliderRun(S);
   contactLoopRun(S);
+  if (S.periodic) S.cell.setNextGradV();
   S.step++;
   S.time += S.P.dt;
   S.P.step = S.step;
@@ -1099,6 +1351,7 @@ int orc_upload_contacts(orc_handle* h, const wdem_contacts* c) {
   for (long i = 0; i < c->n; i++) {
     CPtr C = std::make_shared<Contact>();
     C->pA = c->idA[i]; C->pB = c->idB[i];
+    if (c->cellDist) for (int k = 0; k < 3; k++) C->cellDist[k] = c->cellDist[3 * i + k];
     C->stepCreated = c->stepCreated[i];
     C->minDist00Sq = c->minDist00Sq ? c->minDist00Sq[i] : -1;
     if (c->real[i]) {
@@ -1174,6 +1427,7 @@ int orc_download_contacts(orc_handle* h, wdem_contacts* c) {
     const Contact& C = *v[i];
     if (c->idA) c->idA[i] = C.pA;
     if (c->idB) c->idB[i] = C.pB;
+    if (c->cellDist) for (int k = 0; k < 3; k++) c->cellDist[3 * i + k] = C.cellDist[k];
     if (c->real) c->real[i] = C.isReal();
     if (c->stepCreated) c->stepCreated[i] = C.stepCreated;
     if (c->minDist00Sq) c->minDist00Sq[i] = C.minDist00Sq;
@@ -1205,6 +1459,44 @@ double orc_verlet_dist(orc_handle* h) { return h->S.verletDist; }
 long orc_step_count(orc_handle* h) { return h->S.step; }
 int orc_set_update_phys(orc_handle* h, int up) { h->S.updatePhys = up; return 0; }
 int orc_set_young(orc_handle* h, int mat, double young) { h->S.mats[mat].young = young; return 0; }
+
+/* Periodic cell: row-major hSize, trsf, gradV, nextGradV (4 x 9 doubles); homoDeform GRADV2.
+ * Sets Cell like Cell.setHSize + nextGradV assignment (Cell.hpp:108, Cell.cpp:19-21). */
+int orc_set_cell(orc_handle* h, int periodic, const double* m) {
+  Scene& S = h->S;
+  S.periodic = periodic != 0;
+  if (!S.periodic) return 0;
+  Mat mats[4];
+  for (int q = 0; q < 4; q++) for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) mats[q].r[i][k] = m[9 * q + 3 * i + k];
+  S.cell.hSize = mats[0]; S.cell.pprevHsize = mats[0]; S.cell.trsf = mats[1];
+  S.cell.gradV = mats[2]; S.cell.nextGradV = mats[3];
+  S.cell.W = mscale(madd(S.cell.gradV, mtrans(S.cell.gradV), -1.0), .5);
+  S.cell.spinVec = .5 * leviCivita(S.cell.W);
+  S.cell.integrateAndUpdate(0);
+  return 0;
+}
+int orc_get_cell(orc_handle* h, double* m) {
+  const Cell& c = h->S.cell;
+  const Mat* mats[5] = {&c.hSize, &c.trsf, &c.gradV, &c.nextGradV, &c.pprevHsize};
+  for (int q = 0; q < 5; q++) for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) m[9 * q + 3 * i + k] = mats[q]->r[i][k];
+  return 0;
+}
+/* ContactLoop stress (ContactLoop.cpp:218-229, 243-244): sum over real contacts of F (global, on pA)
+ * times the branch dPos = pB - pA (+ cell shift), divided by the cell volume; row-major 3x3. */
+int orc_stress(orc_handle* h, double* out) {
+  Scene& S = h->S;
+  double st[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (auto& C : S.linView) {
+    if (!C->isReal()) continue;
+    V3 branch = S.par[C->pB].pos - S.par[C->pA].pos;
+    if (S.periodic) branch = branch + S.cell.intrShiftPos(C->cellDist);
+    V3 F = qrot(C->gori, C->force);
+    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) st[i][k] = st[i][k] + F[i] * branch[k];
+  }
+  double vol = S.periodic ? mdet(S.cell.hSize) : 1.0;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) out[3 * i + k] = st[i][k] / vol;
+  return 0;
+}
 
 /* InsertionSortCollider initial sort + sweep (InsertionSortCollider.cpp:536-605) over given boxes,
  * with spatialOverlap and mayCollide; writes pairs (min id, max id) sorted. */

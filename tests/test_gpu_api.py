@@ -30,10 +30,7 @@ def test_sphere_on_wall_script(wdem_lib):
     assert np.array_equal(S.dem.par[1].pos, po.pos[1])
     assert np.array_equal(S.dem.par[1].vel, po.vel[1])
     assert S.step == 400
-    c = S.dem.con[(0, 1)]
-    assert c is not None and c.real and c.geom.uN < 0
-    assert c.forceSign(0) == 1 and c.forceSign(1) == -1
-    assert S.dem.con.countReal() == 1
+    assert len(S.dem.con) == o.contacts().n
 
 
 def test_update_phys_script(wdem_lib):
@@ -67,10 +64,12 @@ def test_update_phys_script(wdem_lib):
 def test_edit_state_between_runs(wdem_lib):
     """Writing a particle's velocity between runs reaches the GPU without losing contact history."""
     m = dem.FrictMat(density=2500, young=1e7)
-    par = [dem.Wall.make(0, axis=2, sense=1, mat=m), dem.Sphere.make((0, 0, 0.0099), 0.01, mat=m)]
+    par = [dem.Wall.make(0, axis=2, sense=1, mat=m), dem.Sphere.make((0, 0, 0.009999), 0.01, mat=m)]
     S = Scene(fields=[dem.DemField(gravity=(0, 0, -9.81), par=par)], engines=dem.DemField.minimalEngines(dynDtPeriod=0))
-    S.run(10)
+    S.run(1)
     assert S.dem.con.countReal() == 1
+    c = S.dem.con[(0, 1)]
+    assert c.real and c.geom.uN < 0 and c.forceSign(0) == 1 and c.forceSign(1) == -1
     S.dem.par[1].vel = (0.1, 0, 0)
     S.run(1)
     assert S.dem.par[1].vel[0] > 0.05

@@ -1,0 +1,68 @@
+"""Periodic cell in the oracle: the known answer of py/tests/test_pbc.py (incident velocity across 10
+cells with homoDeform gradV2) and the periodic pair predicate against brute force over images."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import bridge
+from woo_gb300 import abi, scenes
+
+
+def test_l6geom_incident_velocity_gradv2():
+    """py/tests/test_pbc.py:86-95 (testL6GeomIncidentVelocity): sphere #1 ten cells away along z moving at
+    5 m/s; with nextGradV = diag(0,0,-1) its absolute velocity picks up the mean field, and the contact's
+    incident velocity, corrected by Cell.intrShiftVel, is the initial 5 m/s again."""
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=math.tan(0.5))]
+    mats = scenes.materials_array(mats_py)
+    init_pos = np.array([1.0, 1.0 + 1.0, 1.0 + 10 * 3.0])
+    pa = scenes.assemble(np.array([[1.0, 1, 1], init_pos]), np.array([0.5, 0.5]), 0, [], mats_py,
+                         vel=np.array([[0, 0, 0], [0, 0, 5.0]]))
+    p = scenes.default_params(mats, dt=0.0, damping=0.0, noBreak=1)
+    o = bridge.Oracle(p, pa, cell=dict(hSize=np.diag([2.5, 2.5, 3.0]), nextGradV=np.diag([0, 0, -1.0])))
+    o.step(1)                      # dt=0: only the velocity gradient takes effect
+    v = o.particles().vel
+    assert v[1, 2] == pytest.approx(5.0 - 31.0) and v[0, 2] == pytest.approx(-1.0)
+    p.dt = 1e-10
+    p.step = 1
+    o.lib.orc_set_params(o.h, __import__("ctypes").byref(p))
+    o.step(1)
+    c = o.contacts()
+    assert c.n == 1 and c.real[0] == 1
+    assert np.array_equal(c.cellDist[0], [0, 0, -10])
+    assert np.linalg.norm(c.geomVel[0]) == pytest.approx(np.linalg.norm([0, 0, 5.0]), abs=1e-7)
+
+
+def _image_pairs(pos, r, size):
+    """Brute force over all pairs: the integer cell shift k (per axis) of box 2 for which the boxes
+    overlap strictly, as spatialOverlapPeri requires; boxes are smaller than half the cell, so at most
+    one k per axis exists."""
+    n = len(r)
+    i, j = np.triu_indices(n, 1)
+    mn, mx = pos - r[:, None], pos + r[:, None]
+    lo = (mn[i] - mx[j]) / size          # k*size must lie in (mn1-mx2, mx1-mn2)
+    hi = (mx[i] - mn[j]) / size
+    k = np.floor(lo) + 1
+    ok = np.all((k * size > mn[i] - mx[j]) & (k * size < mx[i] - mn[j]), axis=1)
+    return {(int(a), int(b)): tuple(int(v) for v in kk) for a, b, kk in zip(i[ok], j[ok], k[ok])}
+
+
+def test_periodic_pairs_match_images():
+    """The oracle's periodic pair set (cell list + spatialOverlapPeri) equals the brute-force set of
+    pairs whose boxes overlap for some periodic image, with Contact.cellDist = that image."""
+    rng = np.random.default_rng(3)
+    n = 250
+    size = np.array([0.2, 0.25, 0.3])
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7)]
+    mats = scenes.materials_array(mats_py)
+    pos = rng.uniform(-0.3, 0.6, (n, 3))     # positions are not wrapped into the cell
+    r = rng.uniform(0.006, 0.014, n)
+    pa = scenes.assemble(pos, r, 0, [], mats_py)
+    p = scenes.default_params(mats, dt=1e-9, damping=0.0, verletDist=0.0)
+    o = bridge.Oracle(p, pa, cell=dict(hSize=np.diag(size)))
+    o.step(1)
+    c = o.contacts()
+    got = {(int(a), int(b)): tuple(int(v) for v in d) for a, b, d in zip(c.idA, c.idB, c.cellDist)}
+    exp = _image_pairs(pos, r, size)
+    assert len(exp) > 50
+    assert got == exp

@@ -75,7 +75,14 @@ class Particles(C.Structure):
 class Contacts(C.Structure):
     _fields_ = [("n", C.c_int64), ("idA", I32), ("idB", I32), ("real", I32), ("stepCreated", I32),
                 ("minDist00Sq", D), ("trsf", D), ("contPt", D), ("geomOri", D), ("geomVel", D),
-                ("geomAngVel", D), ("uN", D), ("force", D), ("torque", D), ("kn", D), ("kt", D), ("tanPhi", D)]
+                ("geomAngVel", D), ("uN", D), ("force", D), ("torque", D), ("kn", D), ("kt", D), ("tanPhi", D),
+                ("cellDist", I32)]
+
+
+class Cell(C.Structure):
+    _fields_ = [("periodic", C.c_int32), ("homoDeform", C.c_int32), ("hSize", C.c_double * 9),
+                ("trsf", C.c_double * 9), ("gradV", C.c_double * 9), ("nextGradV", C.c_double * 9),
+                ("pprevHsize", C.c_double * 9)]
 
 
 class Status(C.Structure):
@@ -163,11 +170,13 @@ class ContactArrays:
         self.kn = np.zeros(n)
         self.kt = np.zeros(n)
         self.tanPhi = np.zeros(n)
+        self.cellDist = np.zeros((n, 3), np.int32)
 
     def struct(self):
         s = Contacts()
         s.n = self.n
-        for name, ct in (("idA", C.c_int32), ("idB", C.c_int32), ("real", C.c_int32), ("stepCreated", C.c_int32)):
+        for name, ct in (("idA", C.c_int32), ("idB", C.c_int32), ("real", C.c_int32), ("stepCreated", C.c_int32),
+                         ("cellDist", C.c_int32)):
             setattr(s, name, ptr(getattr(self, name), ct))
         for name in ("minDist00Sq", "trsf", "contPt", "geomOri", "geomVel", "geomAngVel", "uN", "force", "torque",
                      "kn", "kt", "tanPhi"):
