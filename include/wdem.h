@@ -258,6 +258,18 @@ int wdem_set_timing(wdem_handle* h, int32_t enable);
  * in the contact's CGeom object; storing them costs 56 bytes per contact per step). */
 int wdem_keep_geom(wdem_handle* h, int32_t enable);
 
+/* Periodic cell: Scene.isPeriodic + Cell.hSize/trsf/gradV/nextGradV (src/core/Cell.hpp:22-187), set
+ * like Cell.setHSize and Cell.nextGradV from Python; homoDeform gradV2 only.  Call after
+ * wdem_upload_particles and before wdem_upload_contacts.  The cell advances every step
+ * (Cell::integrateAndUpdate at the start, Cell::setNextGradV at the end, src/core/Scene.cpp:411,430). */
+int wdem_set_cell(wdem_handle* h, const wdem_cell* c);
+int wdem_get_cell(wdem_handle* h, wdem_cell* c);
+
+/* Stress tensor of the contact network, row-major 3x3: sum over real contacts of the global contact
+ * force times the branch vector (pB image - pA) divided by the cell volume (ContactLoop.evalStress,
+ * src/dem/ContactLoop.cpp:218-229, 243-244); volume 1 for aperiodic scenes. */
+int wdem_get_stress(wdem_handle* h, double* stress);
+
 /* The CUDA stream (cudaStream_t) every kernel of this handle is launched on, for callers that
  * record CUDA events around wdem_step. */
 int wdem_get_stream(wdem_handle* h, void** stream);

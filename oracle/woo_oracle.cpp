@@ -1154,15 +1154,19 @@ static void leapfrogRun(Scene& S) {
     deltaSpinVec = -.5 * leviCivita(mscale(madd(pprevL, mtrans(pprevL), -1.0), .5)) +
                    .5 * leviCivita(mscale(madd(nnextL, mtrans(nnextL), -1.0), .5));
   }
+  /* reallyTrackEnergy (:132): no energy in step 0 of a periodic scene unless gradV is the identity */
+  bool gradVI = true;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) gradVI &= (S.cell.gradV.r[i][k] == (i == k ? 1.0 : 0.0));
+  const bool eTrack = P.trackEnergy && (!peri || S.step > 0 || gradVI);
 #ifdef _OPENMP
-#pragma omp parallel for schedule(guided) if (S.parallel && !P.trackEnergy)
+#pragma omp parallel for schedule(guided) if (S.parallel && !eTrack)
 #endif
   for (long ip = 0; ip < np; ip++) {
     Particle& p = S.par[ip];
     bool damp = (damping != 0. && !(p.flags & WDEM_DAMPING_SKIP));
     V3& f = p.force;
     V3& t = p.torque;
-    if (P.trackEnergy) {
+    if (eTrack) {
       if (damp && !(p.flags & WDEM_ENERGY_SKIP)) {
         /* doDampingDissipation (:53-64) */
         V3 av(std::abs(p.vel.x), std::abs(p.vel.y), std::abs(p.vel.z));
@@ -1210,7 +1214,7 @@ static void leapfrogRun(Scene& S) {
       /* fixed particle with GRADV2: velocity correction without acceleration (Leapfrog.cpp:207-211) */
       p.vel = mvec(ImLL4hInv, mvec(LmL, p.pos) + mvec(IpLL4h, p.vel));
     }
-    if (P.trackEnergy && !(p.flags & WDEM_ENERGY_SKIP)) {
+    if (eTrack && !(p.flags & WDEM_ENERGY_SKIP)) {
       /* doKineticEnergy (:76-98), spherical */
       V3 cfv = pprevFluctVel + .5 * dt * linAccel, cfa = pprevFluctAngVel + .5 * dt * angAccel;
       double Etrans = .5 * p.mass * sqnorm(cfv);

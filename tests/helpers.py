@@ -10,6 +10,8 @@ def gpu_handle(spec, keep_geom=True, contacts=None):
     h.set_params(spec.params)
     h.upload_particles(spec.particles)
     h.set_params(spec.params)
+    if getattr(spec, "cell", None) is not None:
+        h.set_cell(**spec.cell)
     if contacts is not None:
         h.upload_contacts(contacts)
     return h

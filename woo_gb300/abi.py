@@ -96,7 +96,7 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_download_contacts", "wdem_crit_dt", "wdem_get_energy", "wdem_reset_energy", "wdem_get_status",
            "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
-           "wdem_fp64_peak"]
+           "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress"]
 
 
 def ptr(a, ctype):
@@ -236,6 +236,9 @@ def load(path=None):
         "wdem_read_state": ([h, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "wdem_launch_count": ([h, C.POINTER(C.c_int64)], C.c_int),
         "wdem_fp64_peak": ([h, C.POINTER(C.c_double)], C.c_int),
+        "wdem_set_cell": ([h, C.POINTER(Cell)], C.c_int),
+        "wdem_get_cell": ([h, C.POINTER(Cell)], C.c_int),
+        "wdem_get_stress": ([h, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -348,6 +351,28 @@ class Handle:
 
     def reset_energy(self):
         self.check(self.lib.wdem_reset_energy(self.h))
+
+    def set_cell(self, hSize, trsf=None, gradV=None, nextGradV=None):
+        c = Cell()
+        c.periodic = 1
+        c.homoDeform = 4
+        for name, v in (("hSize", hSize), ("trsf", trsf if trsf is not None else np.eye(3)),
+                        ("gradV", gradV if gradV is not None else np.zeros((3, 3))),
+                        ("nextGradV", nextGradV if nextGradV is not None else np.zeros((3, 3)))):
+            arr = getattr(c, name)
+            for k, x in enumerate(np.asarray(v, float).reshape(9)):
+                arr[k] = x
+        self.check(self.lib.wdem_set_cell(self.h, C.byref(c)))
+
+    def cell(self):
+        c = Cell()
+        self.check(self.lib.wdem_get_cell(self.h, C.byref(c)))
+        return {k: np.array(list(getattr(c, k))).reshape(3, 3) for k in ("hSize", "trsf", "gradV", "nextGradV", "pprevHsize")}
+
+    def stress(self):
+        m = np.zeros(9)
+        self.check(self.lib.wdem_get_stress(self.h, ptr(m, C.c_double)))
+        return m.reshape(3, 3)
 
     def fp64_peak(self):
         v = C.c_double()

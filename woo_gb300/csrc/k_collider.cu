@@ -16,6 +16,8 @@
 //   5. carries contact history over through an open-addressing hash table keyed by (min id, max id),
 //   6. builds the per-particle contact CSR with rows ordered by the partner id.
 #include "wdem_internal.h"
+#include "wdem_math.cuh"
+#include "wdem_peri.cuh"
 #include "../../include/wdem.h"
 #include <cstdio>
 
@@ -36,8 +38,25 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
   double4_32a mn, mx;
   if (sh == WDEM_SHAPE_SPHERE) {
     double h = P.bboxFactor * pr.w;
-    mn = make_double4_32a(pr.x - h, pr.y - h, pr.z - h, 0);
-    mx = make_double4_32a(pr.x + h, pr.y + h, pr.z + h, 0);
+    if (!P.periodic) {
+      mn = make_double4_32a(pr.x - h, pr.y - h, pr.z - h, 0);
+      mx = make_double4_32a(pr.x + h, pr.y + h, pr.z + h, 0);
+    } else {
+      // periodic (Sphere.cpp:66-81): unsheared centre, extents enlarged by Cell::shearAlignedExtents
+      double hx = h, hy = h, hz = h;
+      if (P.hasShear) {
+        double e[3] = {h, h, h};
+        for (int ax = 0; ax < 3; ax++) {
+          int ax1 = (ax + 1) % 3, ax2 = (ax + 2) % 3;
+          e[ax1] = e[ax1] + .5 * h * P.sae[ax];
+          e[ax2] = e[ax2] + .5 * h * P.sae[ax];
+        }
+        hx = e[0]; hy = e[1]; hz = e[2];
+      }
+      const d3 c = mvec(P.unsh, mk(pr.x, pr.y, pr.z));
+      mn = make_double4_32a(c.x - hx, c.y - hy, c.z - hz, 0);
+      mx = make_double4_32a(c.x + hx, c.y + hy, c.z + hz, 0);
+    }
   } else {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     int ax = (p.meta[i].x >> 4) & 3;
@@ -436,15 +455,28 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
 // ------------------------------------------------------------------------------------ retain
 // Real contacts whose new boxes no longer overlap stay in the container (the reference collider
 // removes only non-real contacts on separation, InsertionSortCollider.cpp:107-110).
-__global__ void k_retain_flag(Particles p, Contacts old, long long nOld, unsigned* flag) {
+__global__ void k_retain_flag(StepParams P, Particles p, Contacts old, long long nOld, unsigned* flag) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nOld) return;
   unsigned f = 0;
   if ((old.state[c] & CS_MASK) == CS_REAL) {
     int2 id = old.ids[c];
-    if (!overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y])) f = 1;
+    bool ov;
+    if (P.periodic) {
+      int4 per; bool amb = false;
+      ov = overlapPeri(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y], P.csize, per, amb);
+    } else ov = overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y]);
+    if (!ov) f = 1;
   }
   flag[c] = f;
+}
+__global__ void k_retain_write_dist(Contacts old, long long nOld, const unsigned* flagScan, int4* out, long long base, long long cap) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nOld) return;
+  if (flagScan[c + 1] != flagScan[c]) {
+    long long o = base + flagScan[c];
+    if (o < cap) out[o] = old.cdist[c];
+  }
 }
 __global__ void k_retain_write(Contacts old, long long nOld, const unsigned* flagScan, int2* out, long long base, long long cap) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -527,7 +559,8 @@ __global__ void k_carry(Particles p, Contacts neu, long long nNew, Contacts old,
     neu.step0[c] = (int)step;
     return;
   }
-  neu.ids[c] = old.ids[j];  // keep the stored orientation
+  neu.ids[c] = old.ids[j];  // keep the stored orientation (and, periodic, the stored cellDist)
+  if (neu.cdist && old.cdist) neu.cdist[c] = old.cdist[j];
   neu.state[c] = st | (old.state[j] & CS_SHAPES);
   neu.step0[c] = old.step0[j];
   if (st == CS_REAL) {
@@ -557,6 +590,145 @@ __global__ void k_csr_rows(const unsigned long long* keys, long long ne, int idB
   for (long long k = rp + 1; k <= r; k++) rowptr[k] = (int)e;
   if (e == ne - 1)
     for (long long k = r + 1; k <= n; k++) rowptr[k] = (int)ne;
+}
+
+// ------------------------------------------------------------------------------------ periodic grid
+// Cells of the periodic box (unsheared coordinates), at least as wide as the widest box per axis, so
+// overlapping periodic images of two boxes lie in neighbouring cells (with wrap-around).  Axes with
+// fewer than 3 cells get one cell.  Candidates are then decided by the exact spatialOverlapPeri.
+struct PeriGrid {
+  int nc[3];
+  double cw[3];
+  int ok;
+};
+
+__global__ void k_grid_peri(const unsigned long long* ext, StepParams P, int maxCells, PeriGrid* g) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  PeriGrid G;
+  long long tot = 1;
+  for (int k = 0; k < 3; k++) {
+    double W = ordVal(~ext[12 + k]);
+    int n = (W > 0 && W < 1e300) ? (int)floor(P.csize[k] / (W * (1 + 1e-6))) : 1;
+    if (n < 3) n = 1;
+    if (n > 1024) n = 1024;
+    G.nc[k] = n;
+    tot *= n;
+  }
+  while (tot > maxCells) {
+    int kmax = 0;
+    for (int k = 1; k < 3; k++) if (G.nc[k] > G.nc[kmax]) kmax = k;
+    G.nc[kmax] = G.nc[kmax] * 3 / 4;
+    if (G.nc[kmax] < 3) G.nc[kmax] = 1;
+    tot = (long long)G.nc[0] * G.nc[1] * G.nc[2];
+  }
+  for (int k = 0; k < 3; k++) G.cw[k] = P.csize[k] / G.nc[k];
+  G.ok = 1;
+  *g = G;
+}
+
+__device__ __forceinline__ void periCell(const double4_32a& mn, const double4_32a& mx, const StepParams& P,
+                                         const PeriGrid& G, int* c) {
+  const double ctr[3] = {.5 * (mn.x + mx.x), .5 * (mn.y + mx.y), .5 * (mn.z + mx.z)};
+  for (int k = 0; k < 3; k++) {
+    double w = ctr[k] - floor(ctr[k] / P.csize[k]) * P.csize[k];
+    double v = floor(w / G.cw[k]);
+    c[k] = (int)fmin(fmax(v, 0.0), (double)(G.nc[k] - 1));
+  }
+}
+
+__global__ void k_keys_peri(StepParams P, Particles p, const int* small, int nSmall, const PeriGrid* g,
+                            unsigned long long* keys, unsigned* vals) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nSmall) return;
+  const PeriGrid G = *g;
+  const int i = small[k];
+  int c[3];
+  periCell(p.bbmin[i], p.bbmax[i], P, G, c);
+  keys[k] = ((unsigned long long)c[2] * G.nc[1] + c[1]) * G.nc[0] + c[0];
+  vals[k] = (unsigned)i;
+}
+
+__global__ void k_cell_start_plain(const unsigned long long* keys, int nSmall, long long ncells, int* cellStart) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nSmall == 0) {
+    for (long long k = s; k <= ncells; k += (long long)gridDim.x * blockDim.x) cellStart[k] = 0;
+    return;
+  }
+  if (s >= nSmall) return;
+  long long c = (long long)keys[s];
+  long long cp = s > 0 ? (long long)keys[s - 1] : -1;
+  for (long long k = cp + 1; k <= c; k++) cellStart[k] = s;
+  if (s == nSmall - 1)
+    for (long long k = c + 1; k <= ncells; k++) cellStart[k] = nSmall;
+}
+
+template <bool WRITE>
+__global__ void k_pairs_peri(StepParams P, Particles p, const int* small, int nSmall, const PeriGrid* g,
+                             const unsigned* vals, const int* cellStart, unsigned* counts, int2* out, int4* outDist,
+                             long long cap, DeviceStatus* st) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > nSmall) return;
+  if (k == nSmall) { if (!WRITE) counts[k] = 0; return; }
+  const PeriGrid G = *g;
+  const int i = small[k];
+  const int4 mi = p.meta[i];
+  const double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+  int c[3];
+  periCell(mn, mx, P, G, c);
+  unsigned cnt = 0;
+  unsigned long long base = WRITE ? counts[k] : 0;
+  long long seen[27];
+  int nseen = 0;
+  for (int dz = -1; dz <= 1; dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        int cc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
+        for (int q = 0; q < 3; q++) cc[q] = ((cc[q] % G.nc[q]) + G.nc[q]) % G.nc[q];
+        const long long key = ((long long)cc[2] * G.nc[1] + cc[1]) * G.nc[0] + cc[0];
+        bool dup = false;
+        for (int q = 0; q < nseen; q++) dup |= (seen[q] == key);
+        if (dup) continue;
+        seen[nseen++] = key;
+        const int beg = cellStart[key], end = cellStart[key + 1];
+        for (int q = beg; q < end; q++) {
+          const int j = (int)vals[q];
+          if (j <= i) continue;
+          const int4 mj = p.meta[j];
+          int4 per;
+          bool amb = false;
+          const bool ov = overlapPeri(mn, mx, p.bbmin[j], p.bbmax[j], P.csize, per, amb);
+          if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = i; continue; }
+          if (!ov) continue;
+          if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, P.loneMask)) continue;
+          if (WRITE) {
+            unsigned long long o = base + cnt;
+            if (o < (unsigned long long)cap) { out[o] = make_int2(i, j); outDist[o] = per; }
+          }
+          cnt++;
+        }
+      }
+  if (!WRITE) counts[k] = cnt;
+}
+
+// ------------------------------------------------------------------------------------ stress
+// ContactLoop stress (ContactLoop.cpp:218-229): F (global, on pA) x branch (pB image - pA) per real
+// contact; the nine components are summed by the deterministic energy reduction.
+__global__ void k_stress_terms(StepParams P, Particles p, Contacts c, long long nc, double* terms) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if ((c.state[i] & CS_MASK) == CS_REAL) {
+    const int2 id = c.ids[i];
+    d3 branch = xyz(p.posr[id.y]) - xyz(p.posr[id.x]);
+    if (P.periodic) {
+      const int4 cd = c.cdist[i];
+      branch = branch + mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
+    }
+    const double F[3] = {c.out[OUT_FX][i], c.out[OUT_FY][i], c.out[OUT_FZ][i]};
+    const double b[3] = {branch.x, branch.y, branch.z};
+    for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) v[3 * r + q] = F[r] * b[q];
+  }
+  for (int q = 0; q < 9; q++) terms[(long long)q * nc + i] = v[q];
 }
 
 }  // namespace wdem
@@ -593,12 +765,41 @@ void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, Colli
   else (k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
 }
 
-void col_retain_flags(cudaStream_t s, Particles p, Contacts old, long long nOld, ColliderScratch& cs) {
-  if (nOld > 0) (k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(p, old, nOld, cs.retainFlag), ++::wdem::g_kernel_launches);
+void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int4* out, long long base,
+                           long long cap) {
+  if (nOld > 0) (k_retain_write_dist<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap), ++::wdem::g_kernel_launches);
+}
+
+void col_retain_flags(cudaStream_t s, const StepParams& P, Particles p, Contacts old, long long nOld, ColliderScratch& cs) {
+  if (nOld > 0) (k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(P, p, old, nOld, cs.retainFlag), ++::wdem::g_kernel_launches);
   exclusive_scan_u32(s, cs.retainFlag, nOld, cs);
 }
 void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base, long long cap) {
   if (nOld > 0) (k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap), ++::wdem::g_kernel_launches);
+}
+
+void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall, ColliderScratch& cs,
+                  int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st) {
+  PeriGrid* g = (PeriGrid*)((char*)cs.temp + 256);
+  if (!write) {
+    unsigned long long* ext = (unsigned long long*)cs.temp;
+    (k_extents_init<<<1, 32, 0, s>>>(ext), ++::wdem::g_kernel_launches);
+    if (nSmall > 0) (k_extents<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, ext), ++::wdem::g_kernel_launches);
+    (k_grid_peri<<<1, 1, 0, s>>>(ext, P, cs.maxCols, g), ++::wdem::g_kernel_launches);
+    if (nSmall > 0) (k_keys_peri<<<(nSmall + 255) / 256, 256, 0, s>>>(P, p, small, nSmall, g, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
+    radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bitsFor((unsigned long long)cs.maxCols + 1), cs);
+    int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
+    (k_cell_start_plain<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.maxCols, cs.cellStart), ++::wdem::g_kernel_launches);
+  }
+  const int threads = nSmall + 1;
+  if (write) (k_pairs_peri<true><<<(threads + 127) / 128, 128, 0, s>>>(P, p, small, nSmall, g, cs.vals, cs.cellStart, cs.counts, out, outDist, cap, st), ++::wdem::g_kernel_launches);
+  else (k_pairs_peri<false><<<(threads + 127) / 128, 128, 0, s>>>(P, p, small, nSmall, g, cs.vals, cs.cellStart, cs.counts, out, outDist, cap, st), ++::wdem::g_kernel_launches);
+}
+
+void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, double* scratch9,
+                   double* partials, double* out9) {
+  if (nc > 0) (k_stress_terms<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(P, p, c, nc, scratch9), ++::wdem::g_kernel_launches);
+  for (int q = 0; q < 9; q++) energy_accumulate(s, scratch9 + (long long)q * nc, nc, partials, out9 + q, true);
 }
 
 void col_carry(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,

@@ -14,6 +14,7 @@
 // per particle through the CSR in a fixed order.
 #include "wdem_internal.h"
 #include "wdem_math.cuh"
+#include "wdem_peri.cuh"
 #include "../../include/wdem.h"
 
 namespace wdem {
@@ -69,7 +70,7 @@ __device__ __forceinline__ void cp2(const StepParams& P, int matA, int matB, dou
   }
 }
 
-template <int LAW, int CP2>
+template <int LAW, int CP2, bool PERI>
 __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
@@ -84,26 +85,52 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
   if (s == CS_PENDING) {
     // removePending of this step's collider (no rebuild happened; a rebuild clears PENDING):
     // drop the broken contact when the boxes of the last rebuild do not overlap.
-    if (!overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b])) { c.state[i] = CS_DEAD | sb; return; }
+    bool ov;
+    if (PERI) {
+      int4 per;
+      bool amb = false;
+      ov = overlapPeri(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b], P.csize, per, amb);
+      if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = a; return; }
+    } else
+      ov = overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b]);
+    if (!ov) { c.state[i] = CS_DEAD | sb; return; }
     s = CS_POTENTIAL;
     c.state[i] = s | sb;
   }
   const bool real = (s == CS_REAL);
+  // periodic: pB is taken at its image hSize*cellDist (ContactLoop.cpp:156, Cell::intrShiftPos)
+  int4 cd = make_int4(0, 0, 0, 0);
+  if (PERI) cd = c.cdist[i];
   if (!real && !(sb & CS_WALL_A)) {
     // Conservative FP32 cull of sphere pairs that cannot touch.  The FP32 copies carry a relative
     // error <= 2^-24 per coordinate and radius; the margin below (1e-5 relative on the contact
     // distance plus 1e-6 x the sum of |coordinates|) exceeds the accumulated FP32 error, so every
     // pair rejected here also fails the exact FP64 test of Cg2_Sphere_Sphere_L6Geom.  Pairs close to
     // touching, NaN and overflow fall through to the FP64 test.
-    const float4 fa = p.posf[a], fb = p.posf[b];
+    const float4 fa = p.posf[a];
+    float4 fb = p.posf[b];
+    float Sh = 0.f;
+    if (PERI) {
+      // FP32 image shift; its rounding is bounded by 2^-23 x sum |h_ij cellDist_j|, added to the margin
+      const float c0 = (float)cd.x, c1 = (float)cd.y, c2 = (float)cd.z;
+      const float h[9] = {(float)P.hS[0], (float)P.hS[1], (float)P.hS[2], (float)P.hS[3], (float)P.hS[4],
+                          (float)P.hS[5], (float)P.hS[6], (float)P.hS[7], (float)P.hS[8]};
+      fb.x += h[0] * c0 + h[1] * c1 + h[2] * c2;
+      fb.y += h[3] * c0 + h[4] * c1 + h[5] * c2;
+      fb.z += h[6] * c0 + h[7] * c1 + h[8] * c2;
+      for (int q = 0; q < 9; q++) Sh += fabsf(h[q]) * fabsf(q % 3 == 0 ? c0 : (q % 3 == 1 ? c1 : c2));
+    }
     const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
     const float d2 = dx * dx + dy * dy + dz * dz;
-    const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z);
+    const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
     const float R = (float)fabs(P.distFactor) * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
     if (d2 > R * R) return;
   }
   const double4_32a A4 = p.posr[a], B4 = p.posr[b];
-  const d3 pos1 = xyz(A4), pos2 = xyz(B4);
+  const d3 pos1 = xyz(A4);
+  d3 shift2 = mk(0, 0, 0);
+  if (PERI) shift2 = mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
+  const d3 pos2 = PERI ? xyz(B4) + shift2 : xyz(B4);
   double r1, r2, uN;
   d3 normal, contPt;
   if (!(sb & CS_WALL_A)) {
@@ -188,15 +215,19 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
       cur1 = normalized(cur1);
     }
     d3 midContPt, midPos1, midPos2;
+    // periodic: velocity of the pB image, Cell::intrShiftVel = gradV * pprevHsize * cellDist
+    d3 shiftVel2 = mk(0, 0, 0);
+    if (PERI) shiftVel2 = mvec(P.shv, mk((double)cd.x, (double)cd.y, (double)cd.z));
     if (am & 8) { midContPt = contPt; midPos1 = pos1; midPos2 = pos2; }
     else {
       midContPt = 0.5 * (prevContPt + contPt);
       midPos1 = pos1 - (dt * 0.5) * vel1;
-      midPos2 = pos2 - (dt * 0.5) * vel2;
+      midPos2 = PERI ? pos2 - (dt * 0.5) * (vel2 + shiftVel2) : pos2 - (dt * 0.5) * vel2;
     }
     d3 c1x = (P.noRatch && r1 > 0) ? r1 * midNormal : midContPt - midPos1;
     d3 c2x = (P.noRatch && r2 > 0) ? (-r2) * midNormal : midContPt - midPos2;
-    d3 relVel = (vel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
+    d3 relVel = PERI ? (vel2 + shiftVel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x))
+                     : (vel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
     gvel = mk(dot(mid0, relVel), dot(mid1, relVel), dot(mid2, relVel));
     d3 dw = angVel2 - angVel1;
     gangVel = mk(dot(mid0, dw), dot(mid1, dw), dot(mid2, dw));
@@ -350,11 +381,15 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   if (nc <= 0) return;
   unsigned blocks = (unsigned)((nc + 127) / 128);
-  if (P.law == WDEM_LAW_IDEALELPL) {
-    if (P.cp2 == WDEM_CP2_FRICT) (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
-    else (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+  if (P.periodic) {
+    if (P.law == WDEM_LAW_IDEALELPL)
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    else
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+  } else if (P.law == WDEM_LAW_IDEALELPL) {
+    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   } else {
-    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   }
 }
 

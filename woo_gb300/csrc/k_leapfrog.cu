@@ -41,7 +41,7 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
   }
 }
 
-template <bool FROM_ARRAYS>
+template <bool FROM_ARRAYS, bool PERI>
 __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const double4_32a pr = p.posr[i];
   d3 pos = xyz(pr);
   const d3 inertia = xyz(p.inert[i]);
-  if (P.trackEnergy) {
+  if (P.lfEnergy) {
     // Leapfrog::doDampingDissipation and doGravityWork (Leapfrog.cpp:53-74), mid-step values
     double eDamp = 0, eGrav = 0;
     if (damp && !(flags & WDEM_ENERGY_SKIP)) {
@@ -91,7 +91,12 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     p.energy[EP_DAMP][i] = eDamp;
     p.energy[EP_GRAV][i] = eGrav;
   }
-  const d3 vel0 = vel, angVel0 = angVel;
+  // fluctuation velocities (Cell::pprevFluctVel / pprevFluctAngVel, HOMO_GRADV2; Cell.cpp:36-57)
+  d3 vel0 = vel, angVel0 = angVel;
+  if (PERI && !blockedAll) {
+    vel0 = vel - mvec(P.gradV, pos - P.dt / 2 * vel);
+    angVel0 = angVel - mk(P.spinVec[0], P.spinVec[1], P.spinVec[2]);
+  }
   d3 linAccelE = mk(0, 0, 0), angAccelE = mk(0, 0, 0);
   if (!blockedAll) {
     d3 linAccel;
@@ -105,16 +110,18 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     // nonviscDamp2nd (Leapfrog.cpp:33-35)
     if (damp) {
       const double hd = 0.5 * dt;
-      linAccel.x = linAccel.x * (1 - damping * signum(F.x * (vel.x + hd * linAccel.x)));
-      linAccel.y = linAccel.y * (1 - damping * signum(F.y * (vel.y + hd * linAccel.y)));
-      linAccel.z = linAccel.z * (1 - damping * signum(F.z * (vel.z + hd * linAccel.z)));
+      linAccel.x = linAccel.x * (1 - damping * signum(F.x * (vel0.x + hd * linAccel.x)));
+      linAccel.y = linAccel.y * (1 - damping * signum(F.y * (vel0.y + hd * linAccel.y)));
+      linAccel.z = linAccel.z * (1 - damping * signum(F.z * (vel0.z + hd * linAccel.z)));
     }
-    vel = vel + dt * linAccel;
+    // v(t+dt/2): plain, or the homothetic GRADV2 form (Leapfrog.cpp:189-190)
+    if (PERI) vel = mvec(P.ImLL4hInv, mvec(P.LmL, pos) + mvec(P.IpLL4h, vel) + linAccel * dt);
+    else vel = vel + dt * linAccel;
     linAccelE = linAccel;
     // a zero torque adds zeros to angVel, which changes no bit unless angVel holds a -0 (then the
     // reference's addition may turn it into +0): skip only when that cannot happen
     const bool inertiaPositive = positiveBits(inertia.x) && positiveBits(inertia.y) && positiveBits(inertia.z);
-    if (!isZeroBits(inertia) && !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel))) {
+    if (!isZeroBits(inertia) && (PERI || !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel)))) {
       d3 angAccel;
       if (blockedNone) angAccel = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
       else {
@@ -125,15 +132,19 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       }
       if (damp) {
         const double hd = 0.5 * dt;
-        angAccel.x = angAccel.x * (1 - damping * signum(T.x * (angVel.x + hd * angAccel.x)));
-        angAccel.y = angAccel.y * (1 - damping * signum(T.y * (angVel.y + hd * angAccel.y)));
-        angAccel.z = angAccel.z * (1 - damping * signum(T.z * (angVel.z + hd * angAccel.z)));
+        angAccel.x = angAccel.x * (1 - damping * signum(T.x * (angVel0.x + hd * angAccel.x)));
+        angAccel.y = angAccel.y * (1 - damping * signum(T.y * (angVel0.y + hd * angAccel.y)));
+        angAccel.z = angAccel.z * (1 - damping * signum(T.z * (angVel0.z + hd * angAccel.z)));
       }
       angVel = angVel + dt * angAccel;
+      if (PERI) angVel = angVel - mk(P.dSpin[0], P.dSpin[1], P.dSpin[2]);
       angAccelE = angAccel;
     }
+  } else if (PERI) {
+    // fixed node with GRADV2: velocity correction without acceleration (Leapfrog.cpp:207-211)
+    vel = mvec(P.ImLL4hInv, mvec(P.LmL, pos) + mvec(P.IpLL4h, vel));
   }
-  if (P.trackEnergy) {
+  if (P.lfEnergy) {
     // Leapfrog::doKineticEnergy, spherical (Leapfrog.cpp:76-98): on-step velocities
     double ek = 0;
     if (!(flags & WDEM_ENERGY_SKIP)) {
@@ -182,8 +193,13 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
-  if (fromArrays) (k_leapfrog<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
-  else (k_leapfrog<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  if (P.periodic) {
+    if (fromArrays) (k_leapfrog<true, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    else (k_leapfrog<false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  } else {
+    if (fromArrays) (k_leapfrog<true, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    else (k_leapfrog<false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  }
 }
 
 // DemData.force/torque as Woo holds them after ContactLoop (reset to m*g by Leapfrog, then contacts)

@@ -34,7 +34,94 @@ struct ContactBuf {
   long long cap = 0;
   bool hertz = false;
   bool geom = false;
+  bool peri = false;
 };
+
+// Periodic cell on the host (Cell, src/core/Cell.hpp / Cell.cpp), homoDeform GRADV2; row-major 3x3.
+struct M3 {
+  double r[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  static M3 I() { M3 m; m.r[0][0] = m.r[1][1] = m.r[2][2] = 1; return m; }
+};
+M3 mul(const M3& a, const M3& b) {
+  M3 c;
+  for (int i = 0; i < 3; i++)
+    for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][0] * b.r[0][k] + a.r[i][1] * b.r[1][k] + a.r[i][2] * b.r[2][k];
+  return c;
+}
+M3 addScaled(const M3& a, const M3& b, double sb) {
+  M3 c;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] + sb * b.r[i][k];
+  return c;
+}
+M3 scaled(const M3& a, double s) { M3 c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] * s; return c; }
+M3 transposed(const M3& a) { M3 c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[k][i]; return c; }
+double det3(const M3& m) {
+  const double (*a)[3] = m.r;
+  return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[1][0] * (a[0][1] * a[2][2] - a[2][1] * a[0][2]) +
+         a[2][0] * (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+}
+// inverse = adjugate / determinant
+M3 inv3(const M3& m) {
+  const double (*a)[3] = m.r;
+  M3 c;
+  c.r[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  c.r[0][1] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+  c.r[0][2] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  c.r[1][0] = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  c.r[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+  c.r[1][2] = a[0][2] * a[1][0] - a[0][0] * a[1][2];
+  c.r[2][0] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  c.r[2][1] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+  c.r[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  double d = a[0][0] * c.r[0][0] + a[0][1] * c.r[1][0] + a[0][2] * c.r[2][0];
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] / d;
+  return c;
+}
+void leviCivita(const M3& m, double* v) { v[0] = m.r[1][2] - m.r[2][1]; v[1] = m.r[2][0] - m.r[0][2]; v[2] = m.r[0][1] - m.r[1][0]; }
+
+struct HostCell {
+  M3 trsf = M3::I(), hSize = M3::I(), pprevHsize = M3::I(), gradV, nextGradV, W, shearTrsf = M3::I(), unshearTrsf = M3::I();
+  double spinVec[3] = {0, 0, 0}, size[3] = {1, 1, 1}, cos[3] = {1, 1, 1};
+  bool hasShear = false;
+  // Cell::integrateAndUpdate (Cell.cpp:81-120)
+  bool integrateAndUpdate(double dt) {
+    M3 trsfInc = scaled(gradV, dt);
+    trsf = addScaled(trsf, mul(trsfInc, trsf), 1.0);
+    M3 prev = hSize;
+    M3 g2 = scaled(scaled(gradV, dt), 1. / 2.);
+    hSize = mul(mul(inv3(addScaled(M3::I(), g2, -1.0)), addScaled(M3::I(), g2, 1.0)), hSize);
+    pprevHsize = scaled(addScaled(prev, hSize, 1.0), .5);
+    if (det3(hSize) == 0) return false;
+    M3 Hn;
+    for (int i = 0; i < 3; i++) {
+      double b[3] = {hSize.r[0][i], hSize.r[1][i], hSize.r[2][i]};
+      size[i] = std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+      for (int k = 0; k < 3; k++) Hn.r[k][i] = b[k] / size[i];
+    }
+    for (int i = 0; i < 3; i++) {
+      int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+      double a[3] = {Hn.r[0][i1], Hn.r[1][i1], Hn.r[2][i1]}, b[3] = {Hn.r[0][i2], Hn.r[1][i2], Hn.r[2][i2]};
+      double c0 = a[1] * b[2] - a[2] * b[1], c1 = a[2] * b[0] - a[0] * b[2], c2 = a[0] * b[1] - a[1] * b[0];
+      cos[i] = c0 * c0 + c1 * c1 + c2 * c2;
+    }
+    shearTrsf = Hn;
+    unshearTrsf = inv3(Hn);
+    const double (*h)[3] = hSize.r;
+    hasShear = (h[0][1] != 0 || h[0][2] != 0 || h[1][0] != 0 || h[1][2] != 0 || h[2][0] != 0 || h[2][1] != 0);
+    return true;
+  }
+  // Cell::setNextGradV (Cell.cpp:60-66)
+  void setNextGradV() {
+    gradV = nextGradV;
+    W = scaled(addScaled(gradV, transposed(gradV), -1.0), .5);
+    double v[3];
+    leviCivita(W, v);
+    for (int k = 0; k < 3; k++) spinVec[k] = .5 * v[k];
+  }
+};
+
+void put9(double* dst, const M3& m) { for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) dst[3 * i + k] = m.r[i][k]; }
+M3 get9(const double* src) { M3 m; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) m.r[i][k] = src[3 * i + k]; return m; }
 
 }  // namespace
 
@@ -86,6 +173,11 @@ struct wdem_handle {
   std::string err;
   double* staging = nullptr;    // 13 n doubles for wdem_write_state / wdem_read_state
   long long stagingCap = 0;
+  bool periodic = false;
+  HostCell cell;
+  double* dStress = nullptr;    // 9 stress components + scratch for the terms
+  double* stressTerms = nullptr;
+  long long stressCap = 0;
   double* dEnergy = nullptr;    // WDEM_E_COUNT accumulators
   double* ePartials = nullptr;  // block partials of the energy sums
   long long ePartialsCap = 0;
@@ -119,12 +211,13 @@ void freeContacts(ContactBuf& b) {
   for (int k = 0; k < OUT_COUNT; k++) cudaFree(c.out[k]);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
+  cudaFree(c.cdist);
   memset(&c, 0, sizeof(c));
   b.cap = 0;
 }
 
 // (Re)allocate one contact buffer for `cap` contacts, keeping nothing.
-cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom) {
+cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, bool peri) {
   freeContacts(b);
   Contacts& c = b.c;
   cudaError_t e;
@@ -137,7 +230,9 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom) {
   for (int k = 0; k < OUT_COUNT; k++) if ((e = dalloc(c.out[k], cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
+  if (peri && (e = dalloc(c.cdist, cap))) return e;
   b.cap = cap;
+  b.peri = peri;
   b.hertz = hertz;
   b.geom = geom;
   return cudaSuccess;
@@ -278,14 +373,18 @@ int rebuild(wdem_handle* h) {
   int rc;
   if ((rc = ensureScratch(h, h->nContacts))) return rc;
   launch_bboxes(s, h->P, h->d, n);
-  col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
-  col_sort(s, h->d, h->dSmall, nSmall, cs);
-  col_sweep(s, h->d, nSmall, h->P.loneMask, cs, nullptr, 0, false, h->dst);
+  if (h->periodic) {
+    col_periodic(s, h->P, h->d, h->dSmall, nSmall, cs, nullptr, nullptr, 0, false, h->dst);
+  } else {
+    col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
+    col_sort(s, h->d, h->dSmall, nSmall, cs);
+    col_sweep(s, h->d, nSmall, h->P.loneMask, cs, nullptr, 0, false, h->dst);
+  }
   exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
   ContactBuf& old = h->buf[h->cur];
   ContactBuf& neu = h->buf[1 - h->cur];
   const long long nOld = h->nContacts;
-  col_retain_flags(s, h->d, old.c, nOld, cs);
+  col_retain_flags(s, h->P, h->d, old.c, nOld, cs);
   CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&h->hcounts[1], cs.retainFlag + nOld, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -293,12 +392,14 @@ int rebuild(wdem_handle* h) {
   const long long retained = h->hcounts[1];
   const long long nNew = total + retained;
   const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
-  if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom) {
+  if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom || neu.peri != h->periodic) {
     long long cap = std::max<long long>(nNew + nNew / 4 + 1024, neu.cap);
-    CK(allocContacts(neu, cap, hertz, h->keepGeom));
+    CK(allocContacts(neu, cap, hertz, h->keepGeom, h->periodic));
   }
-  col_sweep(s, h->d, nSmall, h->P.loneMask, cs, neu.c.ids, neu.cap, true, h->dst);
+  if (h->periodic) col_periodic(s, h->P, h->d, h->dSmall, nSmall, cs, neu.c.ids, neu.c.cdist, neu.cap, true, h->dst);
+  else col_sweep(s, h->d, nSmall, h->P.loneMask, cs, neu.c.ids, neu.cap, true, h->dst);
   col_retain_write(s, old.c, nOld, cs, neu.c.ids, total, neu.cap);
+  if (h->periodic && old.c.cdist) col_retain_write_dist(s, old.c, nOld, cs, neu.c.cdist, total, neu.cap);
   const int side = 1 - h->cur;
   if ((rc = ensureHash(h, side, nNew))) return rc;
   launch_hash_build(s, neu.c.ids, nNew, h->hk[side], h->hv[side], h->hcap[side], h->dst);
@@ -338,7 +439,30 @@ void fillStepParams(wdem_handle* h) {
   double en = r.en;
   P.viscAlpha = (en > 0 && en < 1.) ? -std::sqrt(5) * std::log(en) / (std::sqrt(std::log(en) * std::log(en) + M_PI * M_PI)) : 0.;
   P.trackEnergy = r.trackEnergy;
+  P.lfEnergy = r.trackEnergy;
   P.nMaterials = (int)h->mats.size();
+  P.periodic = h->periodic ? 1 : 0;
+}
+
+// Cell-dependent parameters of one step: shifts, unshear, Leapfrog GRADV2 matrices (Leapfrog.cpp:119-127)
+void fillCellParams(wdem_handle* h) {
+  StepParams& P = h->P;
+  const HostCell& c = h->cell;
+  const double dt = P.dt;
+  put9(P.hS, c.hSize);
+  put9(P.shv, mul(c.gradV, c.pprevHsize));
+  put9(P.unsh, c.unshearTrsf);
+  for (int k = 0; k < 3; k++) { P.csize[k] = c.size[k]; P.sae[k] = 1 / c.cos[k] - 1; P.spinVec[k] = c.spinVec[k]; }
+  P.hasShear = c.hasShear ? 1 : 0;
+  put9(P.gradV, c.gradV);
+  M3 q = scaled(scaled(addScaled(c.nextGradV, c.gradV, 1.0), dt), 1. / 4.);
+  put9(P.ImLL4hInv, inv3(addScaled(M3::I(), q, -1.0)));
+  put9(P.IpLL4h, addScaled(M3::I(), q, 1.0));
+  put9(P.LmL, addScaled(c.nextGradV, c.gradV, -1.0));
+  double a[3], b[3];
+  leviCivita(scaled(addScaled(c.gradV, transposed(c.gradV), -1.0), .5), a);
+  leviCivita(scaled(addScaled(c.nextGradV, transposed(c.nextGradV), -1.0), .5), b);
+  for (int k = 0; k < 3; k++) P.dSpin[k] = -.5 * a[k] + .5 * b[k];
 }
 
 // AabbCollider::setVerletDist (Collision.cpp:164-184): negative -> |verletDist| * min sphere radius
@@ -404,7 +528,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   cudaMemset(h->csr.rowptr, 0, sizeof(int) * ((size_t)N + 1));
   memset(h->hst, 0, sizeof(DeviceStatus));
   // an empty contact buffer on the current side
-  if (allocContacts(h->buf[0], 1024, false, false) != cudaSuccess) { wdem_destroy(h); return WDEM_ERR_CUDA; }
+  if (allocContacts(h->buf[0], 1024, false, false, false) != cudaSuccess) { wdem_destroy(h); return WDEM_ERR_CUDA; }
   if (ensureScratch(h, 0)) { wdem_destroy(h); return WDEM_ERR_CUDA; }
   *out = h;
   return WDEM_OK;
@@ -418,7 +542,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
   cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
-  cudaFree(h->dEnergy); cudaFree(h->ePartials);
+  cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
   freeContacts(h->buf[0]); freeContacts(h->buf[1]);
   cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor);
@@ -498,6 +622,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   for (int i = 0; i < n; i++) {
     int sh = p->shape[i];
     if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL) return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (sh == WDEM_SHAPE_WALL && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
     if (p->material[i] < 0 || (h->paramsSet && p->material[i] >= (int)h->mats.size()))
       return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
     const double* in = p->inertia + 3 * i;
@@ -556,17 +681,24 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
   cudaStream_t s = h->stream;
   const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
   ContactBuf& b = h->buf[h->cur];
-  if (nc > b.cap || b.hertz != hertz || b.geom != h->keepGeom) CK(allocContacts(b, std::max<long long>(nc + 1024, 1024), hertz, h->keepGeom));
+  if (nc > b.cap || b.hertz != hertz || b.geom != h->keepGeom || b.peri != h->periodic)
+    CK(allocContacts(b, std::max<long long>(nc + 1024, 1024), hertz, h->keepGeom, h->periodic));
   std::vector<int2> ids(nc);
   std::vector<uint8_t> state(nc);
   std::vector<int> step0(nc);
   std::vector<double> hist[HIST_FRICT], tanPhi(nc, 0.0);
+  std::vector<int4> cdist(nc, make_int4(0, 0, 0, 0));
   for (int k = 0; k < HIST_FRICT; k++) hist[k].assign(nc, 0.0);
   for (long long i = 0; i < nc; i++) {
     int a = c->idA[i], bb = c->idB[i];
     if (a < 0 || a >= h->n || bb < 0 || bb >= h->n || a == bb) return fail(h, WDEM_ERR_ARG, "bad contact ids");
-    if (h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[bb] == WDEM_SHAPE_WALL) std::swap(a, bb);
+    bool swapped = false;
+    if (h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[bb] == WDEM_SHAPE_WALL) { std::swap(a, bb); swapped = true; }
     ids[i] = make_int2(a, bb);
+    if (c->cellDist) {
+      int sg = swapped ? -1 : 1;
+      cdist[i] = make_int4(sg * c->cellDist[3 * i], sg * c->cellDist[3 * i + 1], sg * c->cellDist[3 * i + 2], 0);
+    }
     bool real = c->real[i] != 0;
     state[i] = (uint8_t)((real ? CS_REAL : CS_POTENTIAL) | (h->shape[a] == WDEM_SHAPE_WALL ? CS_WALL_A : 0) |
                          (h->shape[bb] == WDEM_SHAPE_WALL ? CS_WALL_B : 0));
@@ -585,6 +717,7 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     CK(cudaMemcpyAsync(b.c.step0, step0.data(), nc * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.c.tanPhi, tanPhi.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
     for (int k = 0; k < HIST_FRICT; k++) CK(cudaMemcpyAsync(b.c.hist[k], hist[k].data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (b.c.cdist) CK(cudaMemcpyAsync(b.c.cdist, cdist.data(), nc * sizeof(int4), cudaMemcpyHostToDevice, s));
   }
   launch_init_uploaded(s, h->P, h->d, b.c, nc);
   int rc;
@@ -609,11 +742,24 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   for (int it = 0; it < nSteps; it++) {
     h->P.step = h->step;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
+    if (h->periodic) {
+      // Scene::doOneStep prologue: cell->integrateAndUpdate(dt) (Scene.cpp:411)
+      if (!h->cell.integrateAndUpdate(h->P.dt)) return fail(h, WDEM_ERR_STATE, "Cell is degenerate (zero volume).");
+      fillCellParams(h);
+      // Leapfrog's reallyTrackEnergy (Leapfrog.cpp:132): no energy in step 0 with a non-zero gradient
+      bool gradVI = true;
+      for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) gradVI &= (h->cell.gradV.r[i][k] == (i == k ? 1.0 : 0.0));
+      h->P.lfEnergy = h->raw.trackEnergy && (h->step > 0 || gradVI);
+    }
     {
       PhaseTimer t(h, PH_LEAPFROG);
       launch_leapfrog(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
     }
-    if (h->P.trackEnergy) {
+    if (h->P.trackEnergy && !h->P.lfEnergy) {
+      // kinetic is resettable (EnergyTracker::resetResettables at the start of the step)
+      CK(cudaMemsetAsync(h->dEnergy + WDEM_E_KINETIC, 0, sizeof(double), s));
+    }
+    if (h->P.lfEnergy) {
       int rc0;
       if ((rc0 = ensurePartials(h, std::max<long long>(h->n, h->nContacts)))) return rc0;
       energy_accumulate(s, h->d.energy[EP_GRAV], h->n, h->ePartials, h->dEnergy + WDEM_E_GRAV, false);
@@ -652,6 +798,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
       energy_accumulate(s, cc.energy[EC_BROKEN], nc, h->ePartials, h->dEnergy + WDEM_E_BROKEN, false);
     }
     if (h->updatePhys == WDEM_UPDATE_PHYS_ONCE) { h->updatePhys = WDEM_UPDATE_PHYS_NEVER; h->raw.updatePhys = WDEM_UPDATE_PHYS_NEVER; }
+    if (h->periodic) h->cell.setNextGradV();  // epilogue (Scene.cpp:430)
     h->step++;
     h->P.step = h->step;
     h->raw.step = h->step;
@@ -698,6 +845,7 @@ struct HostContacts {
   std::vector<uint8_t> state;
   std::vector<int> step0;
   std::vector<double> hist[HIST_COUNT], tanPhi, geom[7];
+  std::vector<int4> cdist;
 };
 int fetchContacts(wdem_handle* h, HostContacts& hc) {
   cudaStream_t s = h->stream;
@@ -713,6 +861,10 @@ int fetchContacts(wdem_handle* h, HostContacts& hc) {
     for (int k = 0; k < nh; k++) {
       hc.hist[k].resize(nc);
       CK(cudaMemcpyAsync(hc.hist[k].data(), b.c.hist[k], nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    if (b.c.cdist) {
+      hc.cdist.resize(nc);
+      CK(cudaMemcpyAsync(hc.cdist.data(), b.c.cdist, nc * sizeof(int4), cudaMemcpyDeviceToHost, s));
     }
     if (b.geom)
       for (int k = 0; k < 7; k++) {
@@ -785,6 +937,10 @@ int wdem_download_contacts(wdem_handle* h, wdem_contacts* c) {
     int a = hc.ids[i].x, b = hc.ids[i].y;
     if (c->idA) c->idA[o] = a;
     if (c->idB) c->idB[o] = b;
+    if (c->cellDist) {
+      int4 d = hc.cdist.empty() ? make_int4(0, 0, 0, 0) : hc.cdist[i];
+      c->cellDist[3 * o] = d.x; c->cellDist[3 * o + 1] = d.y; c->cellDist[3 * o + 2] = d.z;
+    }
     if (c->real) c->real[o] = real ? 1 : 0;
     if (c->stepCreated) c->stepCreated[o] = hc.step0[i];
     if (c->minDist00Sq) {
@@ -951,6 +1107,66 @@ int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* l
     if (launches) launches[k] = h->phaseLaunches[k];
   }
   *count = PH_COUNT;
+  return WDEM_OK;
+}
+
+int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
+  if (!h || !c) return WDEM_ERR_ARG;
+  if (!c->periodic) { h->periodic = false; h->P.periodic = 0; h->needRebuild = true; return WDEM_OK; }
+  if (c->homoDeform != 4) return fail(h, WDEM_ERR_UNSUPPORTED, "Cell.homoDeform other than gradV2 (4) is not supported");
+  for (int s : h->shape)
+    if (s != WDEM_SHAPE_SPHERE) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
+  if (h->nContacts > 0 && !h->periodic) return fail(h, WDEM_ERR_STATE, "set the cell before uploading contacts");
+  HostCell& hc = h->cell;
+  // Cell.setHSize / trsf / nextGradV (Cell.hpp:108-111) then postLoad -> integrateAndUpdate(0)
+  hc.hSize = get9(c->hSize);
+  hc.pprevHsize = hc.hSize;
+  hc.trsf = get9(c->trsf);
+  hc.gradV = get9(c->gradV);
+  hc.nextGradV = get9(c->nextGradV);
+  hc.W = scaled(addScaled(hc.gradV, transposed(hc.gradV), -1.0), .5);
+  double v[3];
+  leviCivita(hc.W, v);
+  for (int k = 0; k < 3; k++) hc.spinVec[k] = .5 * v[k];
+  if (!hc.integrateAndUpdate(0)) return fail(h, WDEM_ERR_ARG, "Cell is degenerate (zero volume).");
+  h->periodic = true;
+  h->P.periodic = 1;
+  fillCellParams(h);
+  h->needRebuild = true;
+  return WDEM_OK;
+}
+
+int wdem_get_cell(wdem_handle* h, wdem_cell* c) {
+  if (!h || !c) return WDEM_ERR_ARG;
+  c->periodic = h->periodic ? 1 : 0;
+  c->homoDeform = 4;
+  put9(c->hSize, h->cell.hSize);
+  put9(c->trsf, h->cell.trsf);
+  put9(c->gradV, h->cell.gradV);
+  put9(c->nextGradV, h->cell.nextGradV);
+  put9(c->pprevHsize, h->cell.pprevHsize);
+  return WDEM_OK;
+}
+
+int wdem_get_stress(wdem_handle* h, double* stress) {
+  if (!h || !stress) return WDEM_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStream_t s = h->stream;
+  const long long nc = h->nContacts;
+  if (9 * std::max<long long>(nc, 1) > h->stressCap) {
+    CK(dalloc(h->stressTerms, (size_t)(9 * std::max<long long>(nc, 1))));
+    h->stressCap = 9 * std::max<long long>(nc, 1);
+  }
+  if (!h->dStress) CK(dalloc(h->dStress, 9));
+  int rc;
+  if ((rc = ensurePartials(h, std::max<long long>(nc, 1)))) return rc;
+  if (h->periodic) fillCellParams(h);
+  launch_stress(s, h->P, h->d, h->buf[h->cur].c, nc, h->stressTerms, h->ePartials, h->dStress);
+  double v[9];
+  CK(cudaMemcpyAsync(v, h->dStress, sizeof(v), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const double vol = h->periodic ? det3(h->cell.hSize) : 1.0;
+  for (int k = 0; k < 9; k++) stress[k] = v[k] / vol;
   return WDEM_OK;
 }
 

@@ -68,7 +68,20 @@ struct StepParams {
   int noAttraction;
   double poisson, en, viscAlpha;  // viscAlpha from en, computed once on the host
   int trackEnergy;
+  int lfEnergy;       // Leapfrog's reallyTrackEnergy: trackEnergy, off in step 0 of a cell with gradV != I
   int nMaterials;
+  // periodic cell (Cell, homoDeform GRADV2), row-major 3x3
+  int periodic;
+  int hasShear;
+  double hS[9];        // Cell.hSize: Contact shift = hSize * cellDist
+  double shv[9];       // Cell.gradV * Cell.pprevHsize: shift velocity = shv * cellDist
+  double unsh[9];      // Cell unshear transformation (box centres)
+  double csize[3];     // cell lengths (periodic collider)
+  double sae[3];       // 1/cos[ax] - 1 of Cell::shearAlignedExtents
+  double gradV[9];     // Cell.gradV (pprevFluctVel)
+  double spinVec[3];
+  double ImLL4hInv[9], IpLL4h[9], LmL[9];  // Leapfrog GRADV2 matrices
+  double dSpin[3];     // Leapfrog.deltaSpinVec
 };
 
 struct Particles {
@@ -89,6 +102,7 @@ struct Contacts {
   double* out[OUT_COUNT];
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
+  int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
 };
 
 struct Csr {
@@ -156,7 +170,14 @@ void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSm
 void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
 void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out,
                long long cap, bool write, DeviceStatus* st);
-void col_retain_flags(cudaStream_t s, Particles p, Contacts old, long long nOld, ColliderScratch& cs);
+// periodic collider: 3-D cell grid + spatialOverlapPeri
+void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall, ColliderScratch& cs,
+                  int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st);
+void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int4* out, long long base,
+                           long long cap);
+void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, double* scratch9,
+                   double* partials, double* out9);
+void col_retain_flags(cudaStream_t s, const StepParams& P, Particles p, Contacts old, long long nOld, ColliderScratch& cs);
 void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base,
                       long long cap);
 void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,

@@ -64,6 +64,11 @@ __device__ __forceinline__ double qdiv(double x, double y) {
 __device__ __forceinline__ double comp(d3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 __device__ __forceinline__ void setComp(d3& a, int i, double v) { if (i == 0) a.x = v; else if (i == 1) a.y = v; else a.z = v; }
 
+// row-major 3x3 times vector, each row summed left to right
+__device__ __forceinline__ d3 mvec(const double* m, d3 v) {
+  return mk(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z, m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+
 struct qd { double w, x, y, z; };
 
 // Rotation matrix given by columns c0, c1, c2 -> unit quaternion (Shoemake: trace branch, else the

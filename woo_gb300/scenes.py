@@ -26,12 +26,13 @@ DEFAULT_LONE_MASK = 0b0010
 
 
 class SceneSpec:
-    def __init__(self, params, materials, particles, name="", info=None):
+    def __init__(self, params, materials, particles, name="", info=None, cell=None):
         self.params = params
         self.materials = materials      # ctypes array kept alive for params.materials
         self.particles = particles
         self.name = name
         self.info = info or {}
+        self.cell = cell                # periodic cell: dict(hSize=, trsf=, gradV=, nextGradV=) or None
 
     def set_dt(self, dt):
         self.params.dt = dt
@@ -218,3 +219,39 @@ def random_cloud(n, seed, box=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="fric
     g = np.asarray(gravity, np.float64)
     pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
     return SceneSpec(p, mats, pa, f"cloud{n}", dict(seed=seed, dt=dt))
+
+
+def periodic_cloud(n, seed, size=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="frict", shear=0.2, rate=2.0,
+                   vel_scale=0.5, angvel_scale=5.0, damping=0.0, dense=0.9, tuck=0.3, **kw):
+    """Sphere cloud filling a periodic cell (Scene.isPeriodic, homoDeform gradV2).  The cloud is packed in
+    the box [0, size), then positions and box are squeezed by `dense` (<1 creates overlaps) and the cell
+    is a further `tuck` x rmin shorter on each axis, so spheres at opposite faces overlap through the
+    boundary from the start.  hSize has an xz shear of `shear` x the z size and nextGradV a simple shear
+    `rate` (1/s) of x along z.  No gravity, as usual for a cell."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.zeros(3), np.asarray(size, np.float64)
+    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed)
+    centers = centers * dense
+    k = len(radii)
+    L = hi * dense - tuck * rmin
+    hSize = np.diag(L)
+    hSize[0, 2] = shear * L[2]
+    nextGradV = np.zeros((3, 3))
+    nextGradV[0, 2] = rate
+    if law == "frict":
+        mats_py = [dict(kind=abi.MAT_FRICT, density=2500.0, young=1e7, ktDivKn=0.2, tanPhi=0.5),
+                   dict(kind=abi.MAT_FRICT, density=2000.0, young=3e7, ktDivKn=0.3, tanPhi=0.3)]
+        extra = dict(cp2=abi.CP2_FRICT, law=abi.LAW_IDEALELPL)
+    else:
+        mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.3, surfEnergy=0.01),
+                   dict(kind=abi.MAT_HERTZ, density=1200.0, young=8e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.02)]
+        extra = dict(cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.8)
+    extra.update(kw)
+    mat_idx = rng.integers(0, 2, k).astype(np.int32)
+    mats = materials_array(mats_py)
+    pa = assemble(centers, radii, mat_idx, [], mats_py, vel=rng.normal(0, vel_scale, (k, 3)))
+    pa.angVel[:] = rng.normal(0, angvel_scale, (k, 3))
+    dt = 0.3 * pwave_dt(radii, mat_idx, mats_py)
+    p = default_params(mats, dt=dt, gravity=(0, 0, 0), damping=damping, **extra)
+    cell = dict(hSize=hSize, trsf=np.eye(3), gradV=np.zeros((3, 3)), nextGradV=nextGradV)
+    return SceneSpec(p, mats, pa, f"peri{n}", dict(seed=seed, dt=dt), cell=cell)
