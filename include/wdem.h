@@ -39,7 +39,7 @@ enum {
   WDEM_ERR_TOO_BIG = -7,       /* particle larger than half the periodic cell (Woo: InsertionSortCollider.cpp:286-290) */
   WDEM_ERR_TIMEOUT = -8,       /* a bounded device loop hit its iteration limit */
   WDEM_ERR_STATE = -9,         /* call out of order (e.g. step before particles were uploaded) */
-  WDEM_ERR_NO_ALLOC = -10      /* reserved */
+  WDEM_ERR_NO_ALLOC = -10      /* the input exceeds the fixed scratch of an allocation-free entry point */
 };
 
 /* ---- enums mirroring Woo class names -------------------------------------------------------- */
@@ -269,6 +269,22 @@ int wdem_get_cell(wdem_handle* h, wdem_cell* c);
  * force times the branch vector (pB image - pA) divided by the cell volume (ContactLoop.evalStress,
  * src/dem/ContactLoop.cpp:218-229, 243-244); volume 1 for aperiodic scenes. */
 int wdem_get_stress(wdem_handle* h, double* stress);
+
+/* wdem_get_stress without any device memory allocation.  No counterpart in the reference: it exists
+ * for callers that must not touch the CUDA allocator at the moment they ask for the stress, e.g. a
+ * controller running between steps of a serving loop whose memory is fully reserved up front, where
+ * cudaMalloc can fail, or where the implicit device-wide synchronisation of cudaFree would stall other
+ * streams.  wdem_get_stress grows per-handle buffers on demand; this call instead uses one fixed
+ * 295,424-byte array in device memory, shared by all handles of the library on a device.
+ * - at most 16,777,216 contacts (WDEM_ERR_NO_ALLOC beyond that; wdem_get_stress has no such limit);
+ * - the result equals wdem_get_stress up to the order of the additions (relative ~1e-15), and is
+ *   itself deterministic;
+ * - the first call on each device looks the array's address up (this may load the module): make that
+ *   first call before capturing any stream;
+ * - the array is shared: calls that overlap in time on one device (several host threads, or handles
+ *   on different streams) race on it and give undefined results; serialise them per device.
+ * Synchronises the handle's stream before returning. */
+int wdem_get_stress_noalloc(wdem_handle* h, double* stress);
 
 /* The CUDA stream (cudaStream_t) every kernel of this handle is launched on, for callers that
  * record CUDA events around wdem_step. */

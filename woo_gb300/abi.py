@@ -96,7 +96,8 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_download_contacts", "wdem_crit_dt", "wdem_get_energy", "wdem_reset_energy", "wdem_get_status",
            "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
-           "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress"]
+           "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
+           "wdem_get_stress_noalloc"]
 
 
 def ptr(a, ctype):
@@ -239,6 +240,7 @@ def load(path=None):
         "wdem_set_cell": ([h, C.POINTER(Cell)], C.c_int),
         "wdem_get_cell": ([h, C.POINTER(Cell)], C.c_int),
         "wdem_get_stress": ([h, D], C.c_int),
+        "wdem_get_stress_noalloc": ([h, D], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -372,6 +374,12 @@ class Handle:
     def stress(self):
         m = np.zeros(9)
         self.check(self.lib.wdem_get_stress(self.h, ptr(m, C.c_double)))
+        return m.reshape(3, 3)
+
+    def stress_noalloc(self):
+        """wdem_get_stress through the allocation-free entry point (fixed device scratch)."""
+        m = np.zeros(9)
+        self.check(self.lib.wdem_get_stress_noalloc(self.h, ptr(m, C.c_double)))
         return m.reshape(3, 3)
 
     def fp64_peak(self):

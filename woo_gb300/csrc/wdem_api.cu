@@ -1170,6 +1170,25 @@ int wdem_get_stress(wdem_handle* h, double* stress) {
   return WDEM_OK;
 }
 
+int wdem_get_stress_noalloc(wdem_handle* h, double* stress) {
+  if (!h || !stress) return WDEM_ERR_ARG;
+  const long long nc = h->nContacts;
+  if (nc > stress_noalloc_max_contacts())
+    return fail(h, WDEM_ERR_NO_ALLOC, "wdem_get_stress_noalloc: " + std::to_string(nc) +
+                " contacts exceed its fixed scratch (at most " + std::to_string(stress_noalloc_max_contacts()) +
+                " contacts); use wdem_get_stress");
+  CK(cudaSetDevice(h->device));
+  void* scratch = nullptr;
+  CK(noalloc_scratch(h->device, &scratch));
+  if (h->periodic) fillCellParams(h);
+  double v[9];
+  CK(launch_stress_noalloc(h->stream, h->P, h->d, h->buf[h->cur].c, nc, scratch, v));
+  CK(cudaStreamSynchronize(h->stream));
+  const double vol = h->periodic ? det3(h->cell.hSize) : 1.0;
+  for (int k = 0; k < 9; k++) stress[k] = v[k] / vol;
+  return WDEM_OK;
+}
+
 int wdem_get_stream(wdem_handle* h, void** stream) {
   if (!h || !stream) return WDEM_ERR_ARG;
   *stream = (void*)h->stream;

@@ -175,6 +175,11 @@ void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* s
                   int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st);
 void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int4* out, long long base,
                            long long cap);
+// k_noalloc.cu: the stress sum with its scratch in a fixed device array (no allocation)
+long long stress_noalloc_max_contacts();
+cudaError_t noalloc_scratch(int device, void** addr);
+cudaError_t launch_stress_noalloc(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc,
+                                  void* scratch, double* out9);
 void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, double* scratch9,
                    double* partials, double* out9);
 void col_retain_flags(cudaStream_t s, const StepParams& P, Particles p, Contacts old, long long nOld, ColliderScratch& cs);
