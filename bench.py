@@ -14,6 +14,7 @@ Multi-GPU: the path does not shard (contacts couple neighbours); N ranks run N i
 """
 import argparse
 import json
+import re
 import math
 import os
 import statistics
@@ -193,13 +194,12 @@ def run_gpu(args, rank, world, local):
         k_ms, k_n = kt.get(kname, (0.0, 0))
         avg = k_ms / max(k_n, 1)
         ach = abytes / (avg / 1e3) / 1e9 if avg > 0 else 0.0
-        prof = os.path.join(ROOT, "profiles", f"{kname}_{args.workload}.json")
+        prof = os.path.join(ROOT, "profiles", f"{PROFILE_KERNEL[kname]}_{args.workload}.md")
         traffic = dp_ops = None
         if os.path.exists(prof):
-            with open(prof) as f:
-                pj = json.load(f)
-            traffic = pj.get("dram_bytes_per_launch")
-            dp_ops = pj.get("fp64_flops_per_launch")
+            figs = read_profile_figures(prof)
+            traffic = figs.get("dram_bytes_per_launch")
+            dp_ops = figs.get("fp64_flops_per_launch")
         rl[kname] = {"kernel": label, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": ach / hbm_peak, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": abytes, "traffic": traffic, "ms_avg": avg,
@@ -275,6 +275,20 @@ def cpu_baseline(args, full_n):
     return {"value": n * steps / total, "unit": "particle-steps/s", "cores": o.threads(), "kind": "port",
             "sample": f"{args.workload} cut to {n} particles (same density, box scaled), {steps} steps after 2 untimed, "
                       f"OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, {o.threads()} threads"}
+
+
+PROFILE_KERNEL = {"leapfrog": "k_leapfrog", "contacts": "k_contacts"}
+
+
+def read_profile_figures(path):
+    """`- name: number` lines of an ncu summary under profiles/ (per-launch figures of one capture)."""
+    figs = {}
+    with open(path) as f:
+        for line in f:
+            m = re.match(r"^- (\w+): ([0-9.eE+-]+)\s*$", line)
+            if m:
+                figs[m.group(1)] = float(m.group(2))
+    return figs
 
 
 def main():
