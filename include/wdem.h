@@ -43,7 +43,13 @@ enum {
 };
 
 /* ---- enums mirroring Woo class names -------------------------------------------------------- */
-enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1 };
+enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2 };
+/* Cg2_Ellipsoid_Ellipsoid_L6Geom solver: brent=True (Ellipsoid.hpp:57-59) or Newton-Raphson on dS/dlambda = 0
+ * (the reference's brent=False branch, which it leaves unimplemented, Ellipsoid.cpp:311-322) */
+enum { WDEM_ELL_BRENT = 0, WDEM_ELL_NEWTON = 1 };
+/* initial lambda of the Newton solve: lambda0 = max(a)/(max(a)+max(b)) (the reference's draft guess,
+ * Ellipsoid.cpp:314), the learned warm start, or the converged lambda of the previous step */
+enum { WDEM_WARM_COLD = 0, WDEM_WARM_MLP = 1, WDEM_WARM_HISTORY = 2 };
 enum { WDEM_MAT_FRICT = 0, WDEM_MAT_HERTZ = 1 };                 /* FrictMat, HertzMat */
 enum { WDEM_CP2_FRICT = 0, WDEM_CP2_HERTZ = 1 };                 /* Cp2_FrictMat_FrictPhys, Cp2_HertzMat_HertzPhys */
 enum { WDEM_LAW_IDEALELPL = 0, WDEM_LAW_HERTZ_DMT = 1 };         /* Law2_L6Geom_FrictPhys_IdealElPl, Law2_L6Geom_HertzPhys_DMT */
@@ -111,6 +117,12 @@ typedef struct wdem_params {
   int32_t nMaterials;
   int32_t _pad2;
   const wdem_material* materials;
+  /* Cg2_Ellipsoid_Ellipsoid_L6Geom / Cg2_Sphere_Ellipsoid_L6Geom (Ellipsoid.hpp:52-60) */
+  int32_t ellSolver;      /* WDEM_ELL_* */
+  int32_t brentBits;      /* Cg2_Ellipsoid_Ellipsoid_L6Geom.brentBits (default 4*sizeof(Real) = 32) */
+  double newtonTol;       /* Newton: converged when |delta lambda| <= newtonTol */
+  int32_t warmStart;      /* WDEM_WARM_* */
+  int32_t fallbackIters;  /* MLP warm start: Newton iterations before falling back to the cold start */
 } wdem_params;
 
 /* ---- particle state, SoA; all arrays have n (or 3n / 4n) items --------------------------------- */
@@ -132,6 +144,8 @@ typedef struct wdem_particles {
   double* angVel;         /* 3n DemData.angVel */
   double* force;          /* 3n DemData.force */
   double* torque;         /* 3n DemData.torque */
+  double* semiAxes;       /* 3n Ellipsoid.semiAxes (NULL when there are no ellipsoids) */
+  double* angMom;         /* 3n DemData.angMom, NaN = not initialised (aspherical Leapfrog); may be NULL */
 } wdem_particles;
 
 /* ---- contact state, SoA; n contacts ---------------------------------------------------------- */

@@ -40,6 +40,7 @@ def load(variant="liborc.so"):
         "orc_get_energy": ([h, C.POINTER(C.c_double), C.c_int], C.c_int),
         "orc_reset_energy": ([h], C.c_int),
         "orc_nfullruns": ([h], C.c_long),
+        "orc_ell_stats": ([h, C.POINTER(C.c_long), C.POINTER(C.c_long)], C.c_int),
         "orc_verlet_dist": ([h], C.c_double),
         "orc_step_count": ([h], C.c_long),
         "orc_set_update_phys": ([h, C.c_int], C.c_int),
@@ -150,6 +151,12 @@ class Oracle:
 
     def n_full_runs(self):
         return self.lib.orc_nfullruns(self.h)
+
+    def ell_stats(self):
+        """(solves, contact-function evaluations) of the ellipsoid functors so far."""
+        a, b = C.c_long(), C.c_long()
+        self.lib.orc_ell_stats(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def verlet_dist(self):
         return self.lib.orc_verlet_dist(self.h)

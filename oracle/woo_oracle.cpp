@@ -113,12 +113,14 @@ static Mat madd(const Mat& a, const Mat& b, double sb) {
 }
 static Mat mscale(const Mat& a, double s) { Mat c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] * s; return c; }
 static Mat mtrans(const Mat& a) { Mat c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[k][i]; return c; }
+/* Eigen's 3x3 determinant: expansion along row 0, m00 (m11 m22 - m12 m21) - m01 (m10 m22 - m12 m20)
+ * + m02 (m10 m21 - m11 m20) */
 static double mdet(const Mat& m) {
   const double (*a)[3] = m.r;
-  return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[1][0] * (a[0][1] * a[2][2] - a[2][1] * a[0][2]) +
-         a[2][0] * (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+  return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
 }
-/* inverse by the adjugate: inv = adj(m) / det(m) */
+/* Eigen's 3x3 inverse: cofactors, det = cofactors of column 0 dotted with column 0, then adjugate x (1/det) */
 static Mat minv(const Mat& m) {
   const double (*a)[3] = m.r;
   Mat c;
@@ -131,8 +133,9 @@ static Mat minv(const Mat& m) {
   c.r[2][0] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
   c.r[2][1] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
   c.r[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
-  double det = a[0][0] * c.r[0][0] + a[0][1] * c.r[1][0] + a[0][2] * c.r[2][0];
-  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] / det;
+  double det = c.r[0][0] * a[0][0] + c.r[0][1] * a[1][0] + c.r[0][2] * a[2][0];
+  double invdet = 1.0 / det;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] * invdet;
   return c;
 }
 /* leviCivita (src/supp/base/Math.hpp:223-228): (m12-m21, m20-m02, m01-m10) */
@@ -245,6 +248,27 @@ static Quat quatFromMatrix(const M3& m) {
   return q;
 }
 static inline double pow2(double x) { return x * x; }
+
+/* Quaternion::toRotationMatrix, Eigen's formula with tx = 2x, twx = tx w, ... (row-major result) */
+static Mat quatToMat(const Quat& q) {
+  const double tx = 2 * q.x, ty = 2 * q.y, tz = 2 * q.z;
+  const double twx = tx * q.w, twy = ty * q.w, twz = tz * q.w;
+  const double txx = tx * q.x, txy = ty * q.x, txz = tz * q.x;
+  const double tyy = ty * q.y, tyz = tz * q.y, tzz = tz * q.z;
+  Mat m;
+  m.r[0][0] = 1 - (tyy + tzz); m.r[0][1] = txy - twz;       m.r[0][2] = txz + twy;
+  m.r[1][0] = txy + twz;       m.r[1][1] = 1 - (txx + tzz); m.r[1][2] = tyz - twx;
+  m.r[2][0] = txz - twy;       m.r[2][1] = tyz + twx;       m.r[2][2] = 1 - (txx + tyy);
+  return m;
+}
+/* AngleAxis(q).angle(): 2 atan2(|q.vec|, |q.w|), 0 for a zero vector part */
+static double quatAngle(const Quat& q) {
+  const double n = std::sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
+  if (n != 0) return 2 * std::atan2(n, std::abs(q.w));
+  return 0;
+}
+static inline double minCoeff(const V3& a) { double r = a.x; if (a.y < r) r = a.y; if (a.z < r) r = a.z; return r; }
+static inline double maxCoeff(const V3& a) { double r = a.x; if (a.y > r) r = a.y; if (a.z > r) r = a.z; return r; }
 /* Math::Sign (src/supp/base/Math.hpp:145) */
 static inline double Sign(double f) { if (f < 0) return -1; if (f > 0) return 1; return 0; }
 /* pown (src/supp/base/Math.hpp:166-175): x^n by squaring */
@@ -260,7 +284,9 @@ struct Aabb {
   bool has = false;
   V3 min, max;
   V3 nodeLastPos;
+  Quat nodeLastOri;
   double maxD2 = 0;
+  double maxRot = -1;   /* < 0: rotation ignored (Sphere, Wall); Bo1_Ellipsoid_Aabb starts it at 0 */
 };
 
 struct Particle {
@@ -275,6 +301,8 @@ struct Particle {
   V3 inertia;
   V3 pos, vel, angVel, force, torque;
   Quat ori;
+  V3 semiAxes;                        /* Ellipsoid.semiAxes */
+  V3 angMom = V3(NaN, NaN, NaN);      /* DemData.angMom (aspherical Leapfrog) */
   Aabb bound;
   std::map<int, std::shared_ptr<struct Contact>> contacts; /* Particle::contacts (Particle.hpp:36) */
   bool isBlockedNone() const { return (flags & 63u) == 0; }
@@ -363,6 +391,7 @@ struct Scene {
   bool periodic = false;
   Cell cell;
   double stress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  long ellEvals = 0, ellSolves = 0;   /* contact-function evaluations / solves of the ellipsoid functors */
 #ifdef _OPENMP
   std::vector<omp_lock_t> locks;
   ~Scene() { for (auto& l : locks) omp_destroy_lock(&l); }
@@ -483,9 +512,23 @@ static void insertionSort(Scene& S, std::vector<Bounds>& v, bool doCollide) {
 }
 /* Bo1_Sphere_Aabb::go (Sphere.cpp:52-64), Bo1_Wall_Aabb::go (Wall.cpp:25-38), then the verlet
  * enlargement of AabbCollider::updateAabb (Collision.cpp:125-162) */
+/* Ellipsoid::trsfFromUnitSphere (Ellipsoid.cpp:77-82): column i = ori * (semiAxes[i] e_i) */
+static M3 ellTrsf(const Particle& p) {
+  M3 m;
+  m.c[0] = qrot(p.ori, V3(p.semiAxes.x, 0, 0));
+  m.c[1] = qrot(p.ori, V3(0, p.semiAxes.y, 0));
+  m.c[2] = qrot(p.ori, V3(0, 0, p.semiAxes.z));
+  return m;
+}
+/* half-extents along the global axes: norms of the rows of trsfFromUnitSphere (Ellipsoid.cpp:87-90) */
+static V3 ellExtents(const Particle& p) {
+  M3 m = ellTrsf(p);
+  V3 d;
+  for (int i = 0; i < 3; i++) d[i] = std::sqrt(m.c[0][i] * m.c[0][i] + m.c[1][i] * m.c[1][i] + m.c[2][i] * m.c[2][i]);
+  return d;
+}
 static void updateAabb(Scene& S, Particle& p) {
   Aabb& a = p.bound;
-  a.has = true;
   if (p.shape == WDEM_SHAPE_SPHERE) {
     double df = S.P.distFactor;
     double h = (df > 0 ? df : 1.) * p.radius;
@@ -500,14 +543,31 @@ static void updateAabb(Scene& S, Particle& p) {
       a.min = c - half;
       a.max = c + half;
     }
+  } else if (p.shape == WDEM_SHAPE_ELLIPSOID) {
+    /* Bo1_Ellipsoid_Aabb::go (Ellipsoid.cpp:97-119), aperiodic or unsheared cell: half-extents are the
+     * row norms of trsfFromUnitSphere; a new bound starts with maxRot = 0 (rotation-aware verlet) */
+    if (S.periodic && S.cell.hasShear) throw std::runtime_error("ellipsoids in a sheared periodic cell are not restated");
+    if (!a.has) a.maxRot = 0.;
+    V3 delta = ellExtents(p);
+    V3 c = S.periodic ? mvec(S.cell.unshearTrsf, p.pos) : p.pos;
+    a.min = c - delta;
+    a.max = c + delta;
   } else {
     a.min = V3(-Inf, -Inf, -Inf);
     a.max = V3(Inf, Inf, Inf);
     a.min[p.axis] = a.max[p.axis] = p.pos[p.axis];
   }
+  a.has = true;
   a.nodeLastPos = p.pos;
+  a.nodeLastOri = p.ori;
   a.maxD2 = pow2(S.verletDist);
   if (S.verletDist > 0) {
+    /* AabbCollider::updateAabb (Collision.cpp:152-161): rotation limit from the largest half-extent */
+    if (a.maxRot >= 0) {
+      double maxArm = .5 * maxCoeff(a.max - a.min);
+      if (maxArm > 0.) a.maxRot = std::atan(S.verletDist / maxArm);
+      else a.maxRot = 0.;
+    }
     V3 vd(S.verletDist, S.verletDist, S.verletDist);
     a.max = a.max + vd;
     a.min = a.min - vd;
@@ -517,8 +577,13 @@ static void updateAabb(Scene& S, Particle& p) {
 static void setVerletDist(Scene& S) {
   if (S.verletDist >= 0) return;
   double minR = Inf;
-  for (const Particle& p : S.par)
-    if (p.shape == WDEM_SHAPE_SPHERE && !std::isnan(p.radius)) minR = std::min(p.radius, minR);
+  for (const Particle& p : S.par) {
+    /* Shape::equivRadius: Sphere.radius, Ellipsoid cbrt(abc) (Ellipsoid.cpp:25-28), NaN for walls */
+    double r = NaN;
+    if (p.shape == WDEM_SHAPE_SPHERE) r = p.radius;
+    else if (p.shape == WDEM_SHAPE_ELLIPSOID) r = std::cbrt(p.semiAxes.x * p.semiAxes.y * p.semiAxes.z);
+    if (!std::isnan(r)) minR = std::min(r, minR);
+  }
   if (!std::isinf(minR)) S.verletDist = std::abs(S.verletDist) * minR;
   else S.verletDist = 0.0;
 }
@@ -526,8 +591,15 @@ static void setVerletDist(Scene& S) {
 static bool aabbIsDirty(const Particle& p) {
   if (!p.bound.has) return true;
   if (std::isnan(absmax(p.bound.min)) || std::isnan(absmax(p.bound.max))) return true;
-  double d2 = sqnorm(p.bound.nodeLastPos - p.pos);
-  return d2 > p.bound.maxD2;
+  double moveDueToRot2 = 0.;
+  if (p.bound.maxRot >= 0.) {
+    /* rotation since the last update (Collision.cpp:94-110) */
+    double rot = std::max(0., std::abs(quatAngle(qmul(qconj(p.bound.nodeLastOri), p.ori))));
+    if (rot > p.bound.maxRot) return true;
+    moveDueToRot2 = pow2(.5 * maxCoeff(p.bound.max - p.bound.min) * rot);
+  }
+  double d2 = std::max(0., sqnorm(p.bound.nodeLastPos - p.pos));
+  return d2 + moveDueToRot2 > p.bound.maxD2;
 }
 /* InsertionSortCollider::cellWrapRel (InsertionSortCollider.cpp:624-628) */
 static double cellWrapRel(double x, double x0, double x1, int& period) {
@@ -821,6 +893,183 @@ static bool cg2WallSphere(Scene& S, Contact& C, Particle& W, Particle& Sp, const
   return true;
 }
 
+/* ------------------------------------------------------------------ ellipsoids */
+/* Brent's minimisation without derivatives (R. P. Brent, "Algorithms for Minimization without
+ * Derivatives", 1973, ch. 5) as boost::math::tools::brent_find_minima performs it (Boost.Math,
+ * header-only, not vendored; the reference CI builds against Ubuntu 20.04's libboost 1.71).  Called at
+ * Ellipsoid.cpp:309 on [0, 1]: the requested bits are capped at half the mantissa (26 for double),
+ * tolerance 2^(1-bits); start at the upper end; a parabolic step through the three best points when it
+ * stays inside the bracket and shrinks, else a golden-section step (0.3819660, a float constant);
+ * never step by less than the tolerance.  Returns the abscissa and value of the minimum. */
+template <class F>
+static std::pair<double, double> brentMin(F f, double lo, double hi, int bits, long* evals) {
+  bits = std::min(std::numeric_limits<double>::digits / 2, bits);
+  const double tol = std::ldexp(1.0, 1 - bits);
+  const double golden = (double)0.3819660f;
+  double x = hi, w = hi, v = hi;
+  double fx = f(x), fw = fx, fv = fx;
+  double step = 0, step2 = 0;
+  long n = 1;
+  for (;;) {
+    const double mid = (lo + hi) / 2;
+    const double t1 = tol * std::abs(x) + tol / 4;
+    const double t2 = 2 * t1;
+    if (std::abs(x - mid) <= (t2 - (hi - lo) / 2)) break;
+    bool golden_step = true;
+    if (std::abs(step2) > t1) {
+      double r = (x - w) * (fx - fv);
+      double q = (x - v) * (fx - fw);
+      double p = (x - v) * q - (x - w) * r;
+      q = 2 * (q - r);
+      if (q > 0) p = -p;
+      q = std::abs(q);
+      const double prev = step2;
+      step2 = step;
+      if (!((std::abs(p) >= std::abs(q * prev / 2)) || (p <= q * (lo - x)) || (p >= q * (hi - x)))) {
+        golden_step = false;
+        step = p / q;
+        const double u = x + step;
+        if (((u - lo) < t2) || ((hi - u) < t2)) step = (mid - x) < 0 ? -std::abs(t1) : std::abs(t1);
+      }
+    }
+    if (golden_step) {
+      step2 = (x >= mid) ? lo - x : hi - x;
+      step = golden * step2;
+    }
+    const double u = (std::abs(step) >= t1) ? x + step : (step > 0 ? x + std::abs(t1) : x - std::abs(t1));
+    const double fu = f(u);
+    n++;
+    if (fu <= fx) {
+      if (u >= x) lo = x; else hi = x;
+      v = w; w = x; x = u;
+      fv = fw; fw = fx; fx = fu;
+    } else {
+      if (u < x) lo = u; else hi = u;
+      if ((fu <= fw) || (w == x)) { v = w; w = u; fv = fw; fw = fu; }
+      else if ((fu <= fv) || (v == x) || (v == w)) { v = u; fv = fu; }
+    }
+  }
+  if (evals) *evals += n;
+  return std::make_pair(x, fx);
+}
+
+/* Perram-Wertheim contact function of two ellipsoids (Ellipsoid.cpp:270-351; Perram & Wertheim 1985,
+ * Donev et al. 2005): A = sum u_k u_k^T / a_k^2, S(l) = l (1-l) R^T G(l)^-1 R with G = (1-l) A^-1 + l B^-1. */
+struct PwPair {
+  Mat Ainv, Binv;
+  V3 R;
+};
+static PwPair pwSetup(const Quat& oa, const V3& a, const Quat& ob, const V3& b, const V3& R) {
+  PwPair P;
+  Mat A, B;
+  const V3 e[3] = {V3(1, 0, 0), V3(0, 1, 0), V3(0, 0, 1)};
+  for (int k = 0; k < 3; k++) {
+    const V3 u = qrot(oa, e[k]), v = qrot(ob, e[k]);
+    const double a2 = pow2(a[k]), b2 = pow2(b[k]);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        A.r[i][j] = A.r[i][j] + (u[i] * u[j]) / a2;
+        B.r[i][j] = B.r[i][j] + (v[i] * v[j]) / b2;
+      }
+  }
+  P.Ainv = minv(A);
+  P.Binv = minv(B);
+  P.R = R;
+  return P;
+}
+static Mat pwG(const PwPair& P, double l) {
+  Mat G;
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) G.r[i][j] = (1 - l) * P.Ainv.r[i][j] + l * P.Binv.r[i][j];
+  return G;
+}
+/* the lambda functor of Ellipsoid.cpp:293: -l (1-l) R^T G^-1 R, evaluated left to right */
+static double pwNegS(const PwPair& P, double l) {
+  const Mat Gi = minv(pwG(P, l));
+  const double sc = -l * (1 - l);
+  const V3 sR = sc * P.R;
+  V3 t;
+  for (int j = 0; j < 3; j++) t[j] = sR.x * Gi.r[0][j] + sR.y * Gi.r[1][j] + sR.z * Gi.r[2][j];
+  return t.x * P.R.x + t.y * P.R.y + t.z * P.R.z;
+}
+/* dS/dl = (1-2l) h + l (1-l) h' with h = R^T x, h' = -x^T (B^-1 - A^-1) x, x = G^-1 R */
+static double pwDS(const PwPair& P, double l) {
+  const Mat Gi = minv(pwG(P, l));
+  const V3 x = mvec(Gi, P.R);
+  const Mat D = madd(P.Binv, P.Ainv, -1.0);
+  const double h = dot(P.R, x);
+  const double hp = -dot(x, mvec(D, x));
+  return (1 - 2 * l) * h + l * (1 - l) * hp;
+}
+/* The maximiser of S on [0, 1].  WDEM_ELL_BRENT: Brent on -S as the reference does.  Otherwise (the
+ * oracle for the Newton solver): bisection on the sign of dS/dl, which is decreasing because S is
+ * concave, to the last representable lambda, so the converged Newton solution is checked against
+ * the exact maximiser rather than against Brent's 26-bit answer. */
+static void pwSolve(const Scene& S, const PwPair& P, double& L, double& Fab, long* evals) {
+  if (S.P.ellSolver == WDEM_ELL_BRENT) {
+    auto r = brentMin([&](double l) { return pwNegS(P, l); }, 0., 1., S.P.brentBits, evals);
+    L = r.first;
+    Fab = -r.second;
+    return;
+  }
+  double lo = 0, hi = 1;
+  for (int it = 0; it < 200; it++) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (pwDS(P, mid) > 0) lo = mid; else hi = mid;
+  }
+  L = 0.5 * (lo + hi);
+  Fab = -pwNegS(P, L);
+}
+/* Cg2_Ellipsoid_Ellipsoid_L6Geom::go_Ellipsoid_or_Sphere (Ellipsoid.cpp:270-351); a sphere enters with
+ * semi-axes (r, r, r) and its own orientation (Cg2_Sphere_Ellipsoid_L6Geom::go, :262) */
+static bool cg2EllipsoidOrSphere(Scene& S, Contact& C, Particle& A, const V3& a, Particle& B, const V3& b,
+                                 const V3& shift2, bool force) {
+  const V3 ra = A.pos, rb = B.pos + shift2;
+  const V3 R = rb - ra;
+  const PwPair P = pwSetup(A.ori, a, B.ori, b, R);
+  double L, Fab;
+  pwSolve(S, P, L, Fab, S.parallel ? nullptr : &S.ellEvals);
+  if (!S.parallel) S.ellSolves++;
+  if (Fab > 1 && !C.isReal() && !force) return false;
+  const Mat Gi = minv(pwG(P, L));
+  const V3 nUnnorm = mvec(Gi, P.R);
+  const V3 contPt = ra + mvec(mscale(P.Ainv, 1 - L), nUnnorm);
+  const double mu = std::sqrt(Fab);
+  const double Rnorm = norm(R);
+  V3 nUnit = nUnnorm;
+  normalize(nUnit);
+  const V3 rUnit = R / Rnorm;
+  const double uN = Rnorm * (1 - 1 / mu) * dot(rUnit, nUnit);
+  handleSpheresLikeContact(S, C, ra, A.vel, A.angVel, rb, B.vel, B.angVel, nUnit, contPt, uN, norm(contPt - ra),
+                           norm(contPt - rb));
+  return true;
+}
+/* Cg2_Wall_Ellipsoid_L6Geom::go (Ellipsoid.cpp:227-257) */
+static bool cg2WallEllipsoid(Scene& S, Contact& C, Particle& W, Particle& E, const V3& shift2, bool force) {
+  const int ax = W.axis, sense = W.sense;
+  const V3 wallPos = W.pos;
+  const V3 ellPos = E.pos + shift2;
+  const M3 M = ellTrsf(E);
+  const double extent = std::sqrt(M.c[0][ax] * M.c[0][ax] + M.c[1][ax] * M.c[1][ax] + M.c[2][ax] * M.c[2][ax]);
+  if (((wallPos[ax] < (ellPos[ax] - extent)) || (wallPos[ax] > (ellPos[ax] + extent))) && !C.isReal() && !force) return false;
+  const double dist = ellPos[ax] - wallPos[ax];
+  int normAxSgn;
+  if (sense == 0) normAxSgn = dist > 0 ? 1 : -1;
+  else normAxSgn = (sense == 1 ? 1 : -1);
+  const V3 normal = (double)normAxSgn * V3(ax == 0 ? 1. : 0., ax == 1 ? 1. : 0., ax == 2 ? 1. : 0.);
+  const double uN = normAxSgn * dist - extent;
+  /* Mprime = M^T with unit columns; contact point = centre - normAxSgn (M Mprime).col(ax) */
+  V3 mp(M.c[0][ax], M.c[1][ax], M.c[2][ax]);   /* column ax of M^T = row ax of M */
+  normalize(mp);
+  V3 col;
+  for (int i = 0; i < 3; i++) col[i] = M.c[0][i] * mp.x + M.c[1][i] * mp.y + M.c[2][i] * mp.z;
+  V3 contPt = ellPos + (double)(-normAxSgn) * col;
+  contPt[ax] = wallPos[ax];
+  const double contR = norm(contPt - ellPos);
+  handleSpheresLikeContact(S, C, wallPos, W.vel, W.angVel, ellPos, E.vel, E.angVel, normal, contPt, uN, -contR, contR);
+  return true;
+}
+
 /* ------------------------------------------------------------------ physics */
 /* Cp2_FrictMat_FrictPhys::updateFrictPhys (FrictMat.cpp:20-44), MatchMaker unset -> min tanPhi */
 static void cp2Frict(Scene& S, Contact& C, const wdem_material& m1, const wdem_material& m2) {
@@ -981,6 +1230,45 @@ static void applyForceUninodal(Scene& S, const Contact& C, Particle& p) {
 
 static bool isSphereLike(int shape) { return shape == WDEM_SHAPE_SPHERE; }
 
+/* The shape pairs with a Cg2 functor and the order each functor wants (FUNCTOR2D of Sphere.hpp,
+ * Wall.hpp, Ellipsoid.hpp): Sphere+Sphere, Wall+Sphere, Ellipsoid+Ellipsoid, Sphere+Ellipsoid,
+ * Wall+Ellipsoid.  On the first visit of a fresh potential contact the pair is swapped into that order
+ * (Contact::swapOrder, Contact.cpp:12-16) and minDist00Sq is set (ContactLoop.cpp:147-153). */
+static bool freshContactSetup(Scene& S, Contact& C) {
+  const int sa = S.par[C.pA].shape, sb = S.par[C.pB].shape;
+  const bool swap = (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) ||
+                    (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
+                    (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL);
+  const bool known = swap || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_SPHERE) ||
+                     (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_SPHERE) ||
+                     (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_ELLIPSOID) ||
+                     (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_ELLIPSOID) ||
+                     (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_ELLIPSOID);
+  if (!known) return false;
+  if (swap) { std::swap(C.pA, C.pB); for (int k = 0; k < 3; k++) C.cellDist[k] *= -1; }
+  const Particle& A = S.par[C.pA];
+  const Particle& B = S.par[C.pB];
+  if (A.shape == WDEM_SHAPE_SPHERE && B.shape == WDEM_SHAPE_SPHERE)
+    C.minDist00Sq = pow2(std::abs(S.P.distFactor * (A.radius + B.radius)));        /* Sphere.cpp:86-89 */
+  else if (A.shape == WDEM_SHAPE_ELLIPSOID && B.shape == WDEM_SHAPE_ELLIPSOID)
+    C.minDist00Sq = pow2(maxCoeff(A.semiAxes) + maxCoeff(B.semiAxes));            /* Ellipsoid.cpp:265 */
+  else if (A.shape == WDEM_SHAPE_SPHERE && B.shape == WDEM_SHAPE_ELLIPSOID)
+    C.minDist00Sq = pow2(A.radius + maxCoeff(B.semiAxes));                        /* Ellipsoid.cpp:259 */
+  else C.minDist00Sq = -1;
+  return true;
+}
+static bool callGeom(Scene& S, Contact& C, Particle& pA, Particle& pB, const V3& shift2) {
+  const int sa = pA.shape, sb = pB.shape;
+  if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_SPHERE) return cg2SphereSphere(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_SPHERE) return cg2WallSphere(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_ELLIPSOID)
+    return cg2EllipsoidOrSphere(S, C, pA, pA.semiAxes, pB, pB.semiAxes, shift2, false);
+  if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_ELLIPSOID)
+    return cg2EllipsoidOrSphere(S, C, pA, V3(pA.radius, pA.radius, pA.radius), pB, pB.semiAxes, shift2, false);
+  if (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_ELLIPSOID) return cg2WallEllipsoid(S, C, pA, pB, shift2, false);
+  return false;
+}
+
 #ifdef _OPENMP
 /* ContactLoop::run as the reference's OpenMP build runs it: guided parallel loop over the
  * contacts (ContactLoop.cpp:134-137), forces added under a per-node lock (DemData::addForceTorque,
@@ -999,24 +1287,12 @@ static void contactLoopParallel(Scene& S) {
       const CPtr C = S.linView[i];
       if (!C->isReal() && !C->isColliding()) { myRemoveAfter.push_back(C); continue; }
       bool fresh = (S.step == C->stepCreated);
-      if (!C->isReal() && fresh) {
-        Particle& a = S.par[C->pA];
-        Particle& b = S.par[C->pB];
-        if (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_WALL) continue;
-        if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) { std::swap(C->pA, C->pB); for (int k = 0; k < 3; k++) C->cellDist[k] *= -1; }
-        if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
-          C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
-        else C->minDist00Sq = -1;
-      }
+      if (!C->isReal() && fresh && !freshContactSetup(S, *C)) continue;
       Particle& pA = S.par[C->pA];
       Particle& pB = S.par[C->pB];
       V3 shift2 = S.periodic ? S.cell.intrShiftPos(C->cellDist) : V3();
       if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
-      bool geomCreated;
-      if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
-      else if (pA.shape == WDEM_SHAPE_WALL && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2WallSphere(S, *C, pA, pB, shift2, false);
-      else geomCreated = false;
-      if (!geomCreated) continue;
+      if (!callGeom(S, *C, pA, pB, shift2)) continue;
       if (!C->phys) C->stepCreated = (int)S.step;
       if (!C->phys || S.updatePhys > WDEM_UPDATE_PHYS_NEVER) {
         const wdem_material& m1 = S.mats[pA.mat];
@@ -1071,32 +1347,12 @@ static void contactLoopRun(Scene& S) {
     const CPtr C = S.linView[i];
     if (!C->isReal() && !C->isColliding()) { removeAfter.push_back(C); continue; }
     bool fresh = (S.step == C->stepCreated);
-    if (!C->isReal() && fresh) {
-      /* functor order: Cg2_Wall_Sphere_L6Geom wants (Wall, Sphere) (FUNCTOR2D(Wall,Sphere)) */
-      Particle& a = S.par[C->pA];
-      Particle& b = S.par[C->pB];
-      bool known = (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_SPHERE) ||
-                   (a.shape == WDEM_SHAPE_WALL && b.shape == WDEM_SHAPE_SPHERE) ||
-                   (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL);
-      if (!known) continue;
-      if (a.shape == WDEM_SHAPE_SPHERE && b.shape == WDEM_SHAPE_WALL) {  /* Contact::swapOrder (Contact.cpp:12-16) */
-        std::swap(C->pA, C->pB);
-        for (int k = 0; k < 3; k++) C->cellDist[k] *= -1;
-      }
-      /* setMinDist00Sq: Sphere+Sphere only (Sphere.cpp:86-89), else -1 (ContactLoop.hpp:18) */
-      if (S.par[C->pA].shape == WDEM_SHAPE_SPHERE && S.par[C->pB].shape == WDEM_SHAPE_SPHERE)
-        C->minDist00Sq = pow2(std::abs(P.distFactor * (S.par[C->pA].radius + S.par[C->pB].radius)));
-      else C->minDist00Sq = -1;
-    }
+    if (!C->isReal() && fresh && !freshContactSetup(S, *C)) continue;
     Particle& pA = S.par[C->pA];
     Particle& pB = S.par[C->pB];
     V3 shift2 = S.periodic ? S.cell.intrShiftPos(C->cellDist) : V3();
     if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
-    bool geomCreated;
-    if (pA.shape == WDEM_SHAPE_SPHERE && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2SphereSphere(S, *C, pA, pB, shift2, false);
-    else if (pA.shape == WDEM_SHAPE_WALL && pB.shape == WDEM_SHAPE_SPHERE) geomCreated = cg2WallSphere(S, *C, pA, pB, shift2, false);
-    else geomCreated = false;
-    if (!geomCreated) continue;
+    if (!callGeom(S, *C, pA, pB, shift2)) continue;
     if (!C->phys) C->stepCreated = (int)S.step;
     if (!C->phys || S.updatePhys > WDEM_UPDATE_PHYS_NEVER) {
       const wdem_material& m1 = S.mats[pA.mat];
@@ -1132,6 +1388,43 @@ static void contactLoopRun(Scene& S) {
 }
 
 /* ------------------------------------------------------------------ integrator */
+/* Leapfrog::DotQ (Leapfrog.cpp:325-331) */
+static Quat dotQ(const V3& w, const Quat& Q) {
+  Quat d;
+  d.w = (-Q.x * w.x - Q.y * w.y - Q.z * w.z) / 2;
+  d.x = (Q.w * w.x - Q.z * w.y + Q.y * w.z) / 2;
+  d.y = (Q.z * w.x + Q.w * w.y - Q.x * w.z) / 2;
+  d.z = (-Q.y * w.x + Q.x * w.y + Q.w * w.z) / 2;
+  return d;
+}
+/* coefficient-wise q1 + f q2 (Woo's quaternion operator+ and scalar operator*, Math.hpp:139-140) */
+static Quat qaxpy(const Quat& q1, double f, const Quat& q2) {
+  return Quat(q1.w + q2.w * f, q1.x + q2.x * f, q1.y + q2.y * f, q1.z + q2.z * f);
+}
+/* Leapfrog::leapfrogAsphericalRotate (Leapfrog.cpp:299-322) */
+static void leapfrogAsphericalRotate(Scene& S, Particle& p, const V3& M) {
+  const double dt = S.P.dt;
+  if (std::isnan(minCoeff(p.angMom))) {
+    /* inertia.asDiagonal() * ori.conjugate() * angVel: diag(I) R(ori*) applied to angVel */
+    const Mat R = quatToMat(qconj(p.ori));
+    Mat DR;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) DR.r[i][j] = p.inertia[i] * R.r[i][j];
+    p.angMom = mvec(DR, p.angVel);
+  }
+  const Mat A = quatToMat(qconj(p.ori));
+  const V3 l_n = p.angMom + (dt / 2) * M;
+  const V3 l_b_n = mvec(A, l_n);
+  const V3 angVel_b_n(l_b_n.x / p.inertia.x, l_b_n.y / p.inertia.y, l_b_n.z / p.inertia.z);
+  const Quat dotQ_n = dotQ(angVel_b_n, p.ori);
+  const Quat Q_half = qaxpy(p.ori, dt / 2, dotQ_n);
+  p.angMom = p.angMom + dt * M;
+  const V3 l_b_half = mvec(A, p.angMom);
+  const V3 angVel_b_half(l_b_half.x / p.inertia.x, l_b_half.y / p.inertia.y, l_b_half.z / p.inertia.z);
+  const Quat dotQ_half = dotQ(angVel_b_half, Q_half);
+  p.ori = qaxpy(p.ori, dt, dotQ_half);
+  p.angVel = qrot(p.ori, angVel_b_half);
+  qnormalize(p.ori);
+}
 /* Leapfrog::run, aperiodic (Leapfrog.cpp:104-255), ForceResetter folded in via reset=True */
 static void leapfrogRun(Scene& S) {
   const wdem_params& P = S.P;
@@ -1207,7 +1500,9 @@ static void leapfrogRun(Scene& S) {
           p.angVel = p.angVel + dt * angAccel;
           if (peri) p.angVel = p.angVel - deltaSpinVec;
         } else {
-          throw std::runtime_error("aspherical leapfrog is not restated for this particle model");
+          /* aspherical: blocked rotational DOFs zero the torque, then nonviscDamp1st on the torque (:176-179) */
+          for (int i = 0; i < 3; i++) if (p.isBlockedAxisDOF(i, true)) t[i] = 0;
+          if (damp) for (int i = 0; i < 3; i++) t[i] *= 1 - damping * Sign(t[i] * pprevFluctAngVel[i]);
         }
       }
     } else if (peri) {
@@ -1218,12 +1513,24 @@ static void leapfrogRun(Scene& S) {
       /* doKineticEnergy (:76-98), spherical */
       V3 cfv = pprevFluctVel + .5 * dt * linAccel, cfa = pprevFluctAngVel + .5 * dt * angAccel;
       double Etrans = .5 * p.mass * sqnorm(cfv);
-      double Erot = 0.5 * dot(cfa, V3(p.inertia.x * cfa.x, p.inertia.y * cfa.y, p.inertia.z * cfa.z));
+      double Erot;
+      if (p.isAspherical()) {
+        /* .5 w^T (T^T diag(I) T) w with T the rotation matrix of ori (:86-89) */
+        const Mat T = quatToMat(p.ori);
+        Mat mI;
+        mI.r[0][0] = p.inertia.x; mI.r[1][1] = p.inertia.y; mI.r[2][2] = p.inertia.z;
+        const Mat M = mmul(mmul(mtrans(T), mI), T);
+        Erot = .5 * dot(cfa, mvec(M, cfa));
+      } else Erot = 0.5 * dot(cfa, V3(p.inertia.x * cfa.x, p.inertia.y * cfa.y, p.inertia.z * cfa.z));
       if (std::isnan(Erot) || std::isinf(absmax(p.inertia))) Erot = 0;
       S.E.v[WDEM_E_KINETIC] += Etrans + Erot;
     }
     /* leapfrogTranslate (:275-278) */
     p.pos = p.pos + p.vel * dt;
+    if (useAspherical) {
+      if (isZero(p.inertia)) throw std::runtime_error("Leapfrog: zero inertia of a node using the aspherical integrator");
+      leapfrogAsphericalRotate(S, p, t);
+    } else {
     /* leapfrogSphericalRotate (:280-297) */
     V3 axis = p.angVel;
     if (!isZero(axis)) {
@@ -1235,6 +1542,7 @@ static void leapfrogRun(Scene& S) {
       p.ori = qmul(q, p.ori);
     }
     qnormalize(p.ori);
+    }
     if (P.reset) {
       p.force = (hasGravity && !(p.flags & WDEM_GRAVITY_SKIP)) ? p.mass * gravity : V3();
       p.torque = V3();
@@ -1246,9 +1554,12 @@ static void leapfrogRun(Scene& S) {
 static double pWaveDt(const Scene& S) {
   double dt = Inf;
   for (const Particle& p : S.par) {
-    if (p.shape != WDEM_SHAPE_SPHERE) continue;
+    double radius;
+    if (p.shape == WDEM_SHAPE_SPHERE) radius = p.radius;
+    else if (p.shape == WDEM_SHAPE_ELLIPSOID) radius = minCoeff(p.semiAxes);
+    else continue;
     const wdem_material& m = S.mats[p.mat];
-    dt = std::min(dt, p.radius / (1. * std::sqrt(m.young / m.density)));
+    dt = std::min(dt, radius / (1. * std::sqrt(m.young / m.density)));
   }
   return dt;
 }
@@ -1340,6 +1651,12 @@ int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
     q.angVel = V3(p->angVel[3 * i], p->angVel[3 * i + 1], p->angVel[3 * i + 2]);
     q.force = V3(p->force[3 * i], p->force[3 * i + 1], p->force[3 * i + 2]);
     q.torque = V3(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2]);
+    if (p->semiAxes) q.semiAxes = V3(p->semiAxes[3 * i], p->semiAxes[3 * i + 1], p->semiAxes[3 * i + 2]);
+    if (p->angMom) q.angMom = V3(p->angMom[3 * i], p->angMom[3 * i + 1], p->angMom[3 * i + 2]);
+    if (q.shape == WDEM_SHAPE_ELLIPSOID && !(minCoeff(q.semiAxes) > 0)) {
+      S.err = "Ellipsoid #" + std::to_string(i) + ": all semi-axes must be positive";
+      return WDEM_ERR_ARG;
+    }
   }
   S.linView.clear(); S.pending.clear();
   for (int i = 0; i < 3; i++) S.BB[i].clear();
@@ -1412,6 +1729,7 @@ int orc_download_particles(orc_handle* h, wdem_particles* p) {
     if (p->angVel) { p->angVel[3 * i] = q.angVel.x; p->angVel[3 * i + 1] = q.angVel.y; p->angVel[3 * i + 2] = q.angVel.z; }
     if (p->force) { p->force[3 * i] = q.force.x; p->force[3 * i + 1] = q.force.y; p->force[3 * i + 2] = q.force.z; }
     if (p->torque) { p->torque[3 * i] = q.torque.x; p->torque[3 * i + 1] = q.torque.y; p->torque[3 * i + 2] = q.torque.z; }
+    if (p->angMom) { p->angMom[3 * i] = q.angMom.x; p->angMom[3 * i + 1] = q.angMom.y; p->angMom[3 * i + 2] = q.angMom.z; }
   }
   return 0;
 }
@@ -1459,6 +1777,8 @@ int orc_get_energy(orc_handle* h, double* e, int n) {
 int orc_reset_energy(orc_handle* h) { for (int i = 0; i < WDEM_E_COUNT; i++) h->S.E.v[i] = 0; return 0; }
 
 long orc_nfullruns(orc_handle* h) { return h->S.nFullRuns; }
+/* ellipsoid functor statistics: solves and contact-function evaluations so far */
+int orc_ell_stats(orc_handle* h, long* solves, long* evals) { *solves = h->S.ellSolves; *evals = h->S.ellEvals; return 0; }
 double orc_verlet_dist(orc_handle* h) { return h->S.verletDist; }
 long orc_step_count(orc_handle* h) { return h->S.step; }
 int orc_set_update_phys(orc_handle* h, int up) { h->S.updatePhys = up; return 0; }

@@ -1,6 +1,7 @@
 """The C ABI library loads without a GPU and exports every function include/wdem.h declares; host-only
 entry points work on the CPU."""
 import ctypes
+import subprocess
 import os
 import re
 
@@ -28,11 +29,27 @@ def test_abi_version(wdem_lib):
     assert wdem_lib.wdem_abi_version() == abi.ABI_VERSION
 
 
-def test_struct_sizes_match_header():
-    # wdem_params: the offsets of the last fields catch any ordering drift
-    assert ctypes.sizeof(abi.Material) == 56
-    assert abi.Params.materials.offset == ctypes.sizeof(abi.Params) - 8
-    assert ctypes.sizeof(abi.Particles) == 8 + 15 * 8
+def test_struct_layouts_match_header(tmp_path):
+    """Every field offset and struct size of the ctypes mirrors equals what the C compiler makes of
+    include/wdem.h."""
+    structs = {"wdem_material": abi.Material, "wdem_params": abi.Params, "wdem_particles": abi.Particles,
+               "wdem_contacts": abi.Contacts, "wdem_cell": abi.Cell, "wdem_status": abi.Status}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/wdem.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("  return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, f"{cname}.{fname}"
 
 
 def test_make_cloud_is_seeded_and_non_overlapping(wdem_lib):

@@ -25,7 +25,9 @@ WDEM_ERR_TOO_BIG = -7
 WDEM_ERR_TIMEOUT = -8
 WDEM_ERR_STATE = -9
 
-SHAPE_SPHERE, SHAPE_WALL = 0, 1
+SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID = 0, 1, 2
+ELL_BRENT, ELL_NEWTON = 0, 1
+WARM_COLD, WARM_MLP, WARM_HISTORY = 0, 1, 2
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
 LAW_IDEALELPL, LAW_HERTZ_DMT = 0, 1
@@ -63,13 +65,16 @@ class Params(C.Structure):
                 ("relRollStiff", C.c_double), ("relTwistStiff", C.c_double), ("rollTanPhi", C.c_double),
                 ("noAttraction", C.c_int32), ("_pad", C.c_int32),
                 ("nMaterials", C.c_int32), ("_pad2", C.c_int32),
-                ("materials", C.POINTER(Material))]
+                ("materials", C.POINTER(Material)),
+                ("ellSolver", C.c_int32), ("brentBits", C.c_int32), ("newtonTol", C.c_double),
+                ("warmStart", C.c_int32), ("fallbackIters", C.c_int32)]
 
 
 class Particles(C.Structure):
     _fields_ = [("n", C.c_int32), ("_pad", C.c_int32), ("shape", I32), ("radius", D), ("wallAxis", I32),
                 ("wallSense", I32), ("material", I32), ("mask", U32), ("flags", U32), ("mass", D),
-                ("inertia", D), ("pos", D), ("ori", D), ("vel", D), ("angVel", D), ("force", D), ("torque", D)]
+                ("inertia", D), ("pos", D), ("ori", D), ("vel", D), ("angVel", D), ("force", D), ("torque", D),
+                ("semiAxes", D), ("angMom", D)]
 
 
 class Contacts(C.Structure):
@@ -128,6 +133,8 @@ class ParticleArrays:
         self.angVel = np.zeros((n, 3))
         self.force = np.zeros((n, 3))
         self.torque = np.zeros((n, 3))
+        self.semiAxes = np.full((n, 3), np.nan)
+        self.angMom = np.full((n, 3), np.nan)
 
     def copy(self):
         o = ParticleArrays(self.n)
@@ -147,6 +154,7 @@ class ParticleArrays:
         s.ori = ptr(self.ori, C.c_double); s.vel = ptr(self.vel, C.c_double)
         s.angVel = ptr(self.angVel, C.c_double); s.force = ptr(self.force, C.c_double)
         s.torque = ptr(self.torque, C.c_double)
+        s.semiAxes = ptr(self.semiAxes, C.c_double); s.angMom = ptr(self.angMom, C.c_double)
         return s
 
 

@@ -55,12 +55,13 @@ M3 addScaled(const M3& a, const M3& b, double sb) {
 }
 M3 scaled(const M3& a, double s) { M3 c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[i][k] * s; return c; }
 M3 transposed(const M3& a) { M3 c; for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = a.r[k][i]; return c; }
+// Eigen's 3x3 determinant: expansion along row 0
 double det3(const M3& m) {
   const double (*a)[3] = m.r;
-  return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[1][0] * (a[0][1] * a[2][2] - a[2][1] * a[0][2]) +
-         a[2][0] * (a[0][1] * a[1][2] - a[1][1] * a[0][2]);
+  return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
 }
-// inverse = adjugate / determinant
+// Eigen's 3x3 inverse: adjugate x (1 / det), det from the cofactors of column 0
 M3 inv3(const M3& m) {
   const double (*a)[3] = m.r;
   M3 c;
@@ -73,8 +74,9 @@ M3 inv3(const M3& m) {
   c.r[2][0] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
   c.r[2][1] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
   c.r[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
-  double d = a[0][0] * c.r[0][0] + a[0][1] * c.r[1][0] + a[0][2] * c.r[2][0];
-  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] / d;
+  const double d = c.r[0][0] * a[0][0] + c.r[0][1] * a[1][0] + c.r[0][2] * a[2][0];
+  const double invdet = 1.0 / d;
+  for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) c.r[i][k] = c.r[i][k] * invdet;
   return c;
 }
 void leviCivita(const M3& m, double* v) { v[0] = m.r[1][2] - m.r[2][1]; v[1] = m.r[2][0] - m.r[0][2]; v[2] = m.r[0][1] - m.r[1][0]; }

@@ -88,7 +88,24 @@ def default_params(materials, **kw):
     p.noAttraction = kw.get("noAttraction", 1)
     p.nMaterials = len(materials)
     p.materials = materials
+    p.ellSolver = kw.get("ellSolver", abi.ELL_BRENT)
+    p.brentBits = kw.get("brentBits", 32)
+    p.newtonTol = kw.get("newtonTol", 1e-10)
+    p.warmStart = kw.get("warmStart", abi.WARM_COLD)
+    p.fallbackIters = kw.get("fallbackIters", 4)
     return p
+
+
+def ellipsoid_mass_inertia(semi_axes, density):
+    """Ellipsoid::lumpMassInertia (Ellipsoid.cpp:37-44): m = (4/3) pi abc rho,
+    I = (1/5) m (b^2+c^2, c^2+a^2, a^2+b^2), same operation order."""
+    s = np.asarray(semi_axes, np.float64).reshape(-1, 3)
+    rho = np.asarray(density, np.float64)
+    a, b, c = s[:, 0], s[:, 1], s[:, 2]
+    m = ((4 / 3.0) * math.pi) * ((a * b) * c) * rho
+    f = (1 / 5.0) * m
+    inertia = np.stack([0.0 + f * (b * b + c * c), 0.0 + f * (c * c + a * a), 0.0 + f * (a * a + b * b)], axis=1)
+    return m, inertia
 
 
 def sphere_mass_inertia(radius, density):
@@ -255,3 +272,104 @@ def periodic_cloud(n, seed, size=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="f
     p = default_params(mats, dt=dt, gravity=(0, 0, 0), damping=damping, **extra)
     cell = dict(hSize=hSize, trsf=np.eye(3), gradV=np.zeros((3, 3)), nextGradV=nextGradV)
     return SceneSpec(p, mats, pa, f"peri{n}", dict(seed=seed, dt=dt), cell=cell)
+
+
+def quat_from_axis_angle(axis, angle):
+    """Quaternion(AngleAxis(angle, axis/|axis|)) as (w, x, y, z)."""
+    ax = np.asarray(axis, np.float64)
+    ax = ax / math.sqrt(float(ax @ ax))
+    h = 0.5 * angle
+    return np.array([math.cos(h), math.sin(h) * ax[0], math.sin(h) * ax[1], math.sin(h) * ax[2]])
+
+
+def quat_rotate(q, v):
+    """q * v for a (w, x, y, z) quaternion: v + w uv + q.vec x uv with uv = 2 q.vec x v."""
+    qv = np.asarray(q[1:], np.float64)
+    v = np.asarray(v, np.float64)
+    uv = np.cross(qv, v)
+    uv = uv + uv
+    return v + q[0] * uv + np.cross(qv, uv)
+
+
+def random_quaternions(n, rng):
+    """Uniformly distributed unit quaternions (Shoemake 1992, 'Uniform random rotations'), (w, x, y, z)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1 - u1), np.sqrt(u1)
+    q = np.stack([b * np.cos(2 * np.pi * u3), a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2),
+                  b * np.sin(2 * np.pi * u3)], axis=1)
+    return q / np.linalg.norm(q, axis=1)[:, None]
+
+
+def assemble_ellipsoids(centers, semi_axes, oris, mat, walls, mats_py, vel=None, spheres=None):
+    """ParticleArrays: walls first, then ellipsoids (Ellipsoid.semiAxes, Node.ori), then optional spheres
+    given as (centers, radii, material)."""
+    nw, ne = len(walls), len(semi_axes)
+    ns = 0 if spheres is None else len(spheres[1])
+    n = nw + ne + ns
+    pa = abi.ParticleArrays(n)
+    for i, (ax, sense, pos, mi) in enumerate(walls):
+        pa.shape[i] = abi.SHAPE_WALL
+        pa.wallAxis[i] = ax
+        pa.wallSense[i] = sense
+        pa.pos[i, ax] = pos
+        pa.material[i] = mi
+        pa.mask[i] = DEFAULT_BOUNDARY_MASK
+        pa.flags[i] = abi.DOF_ALL
+    e = slice(nw, nw + ne)
+    pa.shape[e] = abi.SHAPE_ELLIPSOID
+    pa.semiAxes[e] = semi_axes
+    pa.pos[e] = centers
+    pa.ori[e] = oris
+    em = np.broadcast_to(np.asarray(mat, np.int32), (ne,))
+    pa.material[e] = em
+    pa.mask[e] = DEFAULT_MOVABLE_MASK
+    dens = np.array([mats_py[k].get("density", 1000.0) for k in range(len(mats_py))])[em]
+    m, inert = ellipsoid_mass_inertia(semi_axes, dens)
+    pa.mass[e] = m
+    pa.inertia[e] = inert
+    if vel is not None:
+        pa.vel[e] = vel
+    if ns:
+        c, r, sm = spheres
+        s = slice(nw + ne, n)
+        pa.shape[s] = abi.SHAPE_SPHERE
+        pa.radius[s] = r
+        pa.pos[s] = c
+        smi = np.broadcast_to(np.asarray(sm, np.int32), (ns,))
+        pa.material[s] = smi
+        pa.mask[s] = DEFAULT_MOVABLE_MASK
+        d2 = np.array([mats_py[k].get("density", 1000.0) for k in range(len(mats_py))])[smi]
+        m2, i2 = sphere_mass_inertia(r, d2)
+        pa.mass[s] = m2
+        pa.inertia[s] = i2[:, None]
+    return pa
+
+
+def ellipsoid_cloud(n, seed, box=(0.1, 0.1, 0.1), amin=0.004, amax=0.006, ratios=(1.0, 0.7, 0.5), walls=True,
+                    vel_scale=0.5, angvel_scale=5.0, gravity=(0, 0, -9.81), damping=0.2, dense=1.0, young=1e7,
+                    tanPhi=0.4, density=1000.0, dt_safety=0.9, **kw):
+    """Ellipsoids with semi-axes a*ratios (a uniform in [amin, amax]) and uniformly random orientations,
+    placed by random sequential addition of their bounding spheres (radius a) in `box`, optionally
+    squeezed by `dense` (< 1 makes overlaps); FrictMat + IdealElPl; dt = dt_safety x pWaveDt."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.zeros(3), np.asarray(box, np.float64)
+    centers, a = abi.make_cloud(lo, hi, amin, amax, n, seed)
+    if dense != 1.0:
+        c = hi / 2
+        centers = c + (centers - c) * dense
+    k = len(a)
+    semi = a[:, None] * np.asarray(ratios, np.float64)[None, :]
+    oris = random_quaternions(k, rng)
+    mats_py = [dict(kind=abi.MAT_FRICT, density=density, young=young, ktDivKn=0.2, tanPhi=tanPhi)]
+    mats = materials_array(mats_py)
+    pa = assemble_ellipsoids(centers, semi, oris, 0, box_walls(lo, hi) if walls else [], mats_py,
+                             vel=rng.normal(0, vel_scale, (k, 3)))
+    nw = 6 if walls else 0
+    pa.angVel[nw:] = rng.normal(0, angvel_scale, (k, 3))
+    dt = dt_safety * float(np.min(semi.min(axis=1) / np.sqrt(young / density)))
+    extra = dict(cp2=abi.CP2_FRICT, law=abi.LAW_IDEALELPL)
+    extra.update(kw)
+    p = default_params(mats, dt=dt, gravity=gravity, damping=damping, **extra)
+    g = np.asarray(gravity, np.float64)
+    pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
+    return SceneSpec(p, mats, pa, f"ell{n}", dict(seed=seed, dt=dt))
