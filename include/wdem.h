@@ -192,6 +192,9 @@ typedef struct wdem_status {
   int64_t capacity;        /* current contact capacity */
   int32_t lastRunFull;     /* 1 if the last step rebuilt the collider */
   int32_t _pad;
+  int64_t ellSolves;       /* ellipsoid contact-function maximisations since creation */
+  int64_t ellIters;        /* their Newton iterations (Brent: function evaluations) */
+  int64_t ellFallbacks;    /* learned warm starts that fell back to the cold start */
 } wdem_status;
 
 typedef struct wdem_handle wdem_handle;

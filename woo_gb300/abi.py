@@ -93,7 +93,8 @@ class Cell(C.Structure):
 class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("detail", C.c_int32), ("step", C.c_int64), ("nContacts", C.c_int64),
                 ("nReal", C.c_int64), ("nFullRuns", C.c_int64), ("capacity", C.c_int64),
-                ("lastRunFull", C.c_int32), ("_pad", C.c_int32)]
+                ("lastRunFull", C.c_int32), ("_pad", C.c_int32), ("ellSolves", C.c_int64), ("ellIters", C.c_int64),
+                ("ellFallbacks", C.c_int64)]
 
 
 EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params", "wdem_upload_particles",

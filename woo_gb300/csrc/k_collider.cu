@@ -57,6 +57,17 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
       mn = make_double4_32a(c.x - hx, c.y - hy, c.z - hz, 0);
       mx = make_double4_32a(c.x + hx, c.y + hy, c.z + hz, 0);
     }
+  } else if (sh == WDEM_SHAPE_ELLIPSOID) {
+    // Bo1_Ellipsoid_Aabb::go (Ellipsoid.cpp:97-107): half-extents = row norms of trsfFromUnitSphere
+    const double4_32a sa = p.semi[i], o4 = p.ori[i];
+    qd q;
+    q.w = o4.x; q.x = o4.y; q.y = o4.z; q.z = o4.w;
+    const d3 c0 = qrot(q, mk(sa.x, 0, 0)), c1 = qrot(q, mk(0, sa.y, 0)), c2 = qrot(q, mk(0, 0, sa.z));
+    const double hx = sqrt(c0.x * c0.x + c1.x * c1.x + c2.x * c2.x);
+    const double hy = sqrt(c0.y * c0.y + c1.y * c1.y + c2.y * c2.y);
+    const double hz = sqrt(c0.z * c0.z + c1.z * c1.z + c2.z * c2.z);
+    mn = make_double4_32a(pr.x - hx, pr.y - hy, pr.z - hz, 0);
+    mx = make_double4_32a(pr.x + hx, pr.y + hy, pr.z + hz, 0);
   } else {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     int ax = (p.meta[i].x >> 4) & 3;
@@ -64,6 +75,20 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
     mx = make_double4_32a(inf, inf, inf, 0);
     double c = ax == 0 ? pr.x : (ax == 1 ? pr.y : pr.z);
     if (ax == 0) { mn.x = c; mx.x = c; } else if (ax == 1) { mn.y = c; mx.y = c; } else { mn.z = c; mx.z = c; }
+  }
+  if (p.maxRot) {
+    // Aabb.maxRot: -1 (ignored) for spheres and walls; ellipsoids start at 0 and get
+    // atan(verletDist / largest half-extent) when verletDist > 0 (Collision.cpp:152-158)
+    double mr = -1.;
+    if (sh == WDEM_SHAPE_ELLIPSOID) {
+      mr = 0.;
+      if (P.verletDist > 0) {
+        const double arm = .5 * dmax3(mk(mx.x - mn.x, mx.y - mn.y, mx.z - mn.z));
+        mr = (arm > 0.) ? atan(P.verletDist / arm) : 0.;
+      }
+    }
+    p.maxRot[i] = mr;
+    p.lastOri[i] = p.ori[i];
   }
   if (P.verletDist > 0) {
     double vd = P.verletDist;
@@ -364,11 +389,15 @@ __device__ __forceinline__ bool overlap3(const double4_32a& mn1, const double4_3
 __device__ __forceinline__ bool mayCollide(unsigned m1, unsigned m2, unsigned lone) {
   return (m1 & m2) != 0 && (m1 & m2 & lone) == 0;
 }
-// contact orientation: same shape -> (lower id, higher id); wall + sphere -> wall first
+// contact orientation: same shape -> (lower id, higher id); otherwise the order of the Cg2 functor
+// (Wall+Sphere, Sphere+Ellipsoid, Wall+Ellipsoid)
 __device__ __forceinline__ int2 orient(int i, int j, int shi, int shj) {
   int a = min(i, j), b = max(i, j);
   int sa = (a == i) ? shi : shj, sb = (a == i) ? shj : shi;
-  if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) { int t = a; a = b; b = t; }
+  if ((sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
+      (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL)) {
+    int t = a; a = b; b = t;
+  }
   return make_int2(a, b);
 }
 
@@ -553,12 +582,15 @@ __global__ void k_carry(Particles p, Contacts neu, long long nNew, Contacts old,
     else st = (os == CS_REAL) ? CS_REAL : CS_POTENTIAL;
   }
   if (j < 0) {
-    const uint8_t sb = (uint8_t)((((p.meta[id.x].x & 15) == WDEM_SHAPE_WALL) ? CS_WALL_A : 0) |
-                                 (((p.meta[id.y].x & 15) == WDEM_SHAPE_WALL) ? CS_WALL_B : 0));
+    const int sa = p.meta[id.x].x & 15, sbb = p.meta[id.y].x & 15;
+    const uint8_t sb = (uint8_t)((sa == WDEM_SHAPE_WALL ? CS_WALL_A : 0) | (sbb == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
+                                 (sa == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (sbb == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
     neu.state[c] = CS_POTENTIAL | sb;
     neu.step0[c] = (int)step;
+    if (neu.lam) neu.lam[c] = __longlong_as_double(0x7ff8000000000000ll);
     return;
   }
+  if (neu.lam && old.lam) neu.lam[c] = old.lam[j];
   neu.ids[c] = old.ids[j];  // keep the stored orientation (and, periodic, the stored cellDist)
   if (neu.cdist && old.cdist) neu.cdist[c] = old.cdist[j];
   neu.state[c] = st | (old.state[j] & CS_SHAPES);

@@ -15,6 +15,7 @@
 #include "wdem_internal.h"
 #include "wdem_math.cuh"
 #include "wdem_peri.cuh"
+#include "wdem_ell.cuh"
 #include "../../include/wdem.h"
 
 namespace wdem {
@@ -70,7 +71,145 @@ __device__ __forceinline__ void cp2(const StepParams& P, int matA, int matB, dou
   }
 }
 
-template <int LAW, int CP2, bool PERI>
+// warp-aggregated add of per-thread counters (one atomic per warp)
+__device__ __forceinline__ void warpAdd(unsigned long long* dst, unsigned v) {
+  const unsigned mask = __activemask();
+  unsigned long long sum = v;
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(mask, sum, o);
+  if ((threadIdx.x & 31) == (__ffs(mask) - 1) && sum) atomicAdd(dst, sum);
+}
+
+// Perram-Wertheim geometry of an ellipsoid (or sphere + ellipsoid) pair, Cg2_Ellipsoid_Ellipsoid_L6Geom::
+// go_Ellipsoid_or_Sphere (Ellipsoid.cpp:270-351).  Returns false when the pair does not touch
+// (F_ab > 1) and the contact is not real.
+__device__ __noinline__ bool ellPairGeometry(const StepParams& P, const Particles& p, const Contacts& c, long long i,
+                                             int a, int b, bool real, d3 pos1, d3 pos2, d3& normal, d3& contPt,
+                                             double& uN, double& r1, double& r2, DeviceStatus* st) {
+  const double4_32a SA = p.semi[a], SB = p.semi[b], OA = p.ori[a], OB = p.ori[b];
+  qd oa, ob;
+  oa.w = OA.x; oa.x = OA.y; oa.y = OA.z; oa.z = OA.w;
+  ob.w = OB.x; ob.x = OB.y; ob.y = OB.z; ob.z = OB.w;
+  const d3 semiA = xyz(SA), semiB = xyz(SB);
+  const d3 R = pos2 - pos1;
+  const s33 Ai = symInv(shapeMatrix(oa, semiA));
+  const s33 Bi = symInv(shapeMatrix(ob, semiB));
+  double L, Fab;
+  unsigned iters = 0, fallback = 0;
+  if (P.ellSolver == WDEM_ELL_BRENT) {
+    int ev = 0;
+    if (!brentMax(Ai, Bi, R, P.brentTol, 1000, L, Fab, ev)) {
+      if (atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT) == 0) st->detail = a;
+      return false;
+    }
+    iters = (unsigned)ev;
+  } else {
+    const double cold = maxc(semiA) / (maxc(semiA) + maxc(semiB));
+    double l0 = cold;
+    int budget = 60;
+    if (P.warmStart == WDEM_WARM_HISTORY && c.lam) {
+      const double lh = c.lam[i];
+      if (lh > 0 && lh < 1) l0 = lh;
+    } else if (P.warmStart == WDEM_WARM_MLP && c.lam0) {
+      const double lm = (double)c.lam0[i];
+      if (lm > 0 && lm < 1) { l0 = lm; budget = P.fallbackIters; }
+    }
+    int it = newtonMax(Ai, Bi, R, l0, P.newtonTol, budget, L);
+    if (it < 0 && budget < 60) {
+      // the warm start did not converge within k iterations: plain cold-start Newton
+      fallback = 1;
+      iters += (unsigned)budget;
+      it = newtonMax(Ai, Bi, R, cold, P.newtonTol, 60, L);
+    }
+    if (it < 0) {
+      if (atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT) == 0) st->detail = a;
+      return false;
+    }
+    iters += (unsigned)it;
+    Fab = -pwNegS(Ai, Bi, R, L);
+  }
+  warpAdd(&st->ellSolves, 1u);
+  warpAdd(&st->ellIters, iters);
+  if (fallback) warpAdd(&st->ellFallbacks, fallback);
+  if (c.lam) c.lam[i] = L;
+  const bool touch = !(Fab > 1);
+  if (!touch && !real) {
+    if (P.ellLog) {
+      const unsigned long long k = atomicAdd(P.ellLogCount, 1ull);
+      if (k < (unsigned long long)P.ellLogCap) {
+        float* rec = P.ellLog + k * ELL_RECORD;
+        ellFeatures(oa, semiA, ob, semiB, R, rec);
+        // contact point of the scaled ellipsoids, as in the touching case
+        const s33 Gi = symInv(symMix(Ai, Bi, L));
+        const d3 n = symMul(Gi, R);
+        const double w = 1 - L;
+        const d3 v = mk((w * Ai.a) * n.x + (w * Ai.b) * n.y + (w * Ai.c) * n.z,
+                        (w * Ai.b) * n.x + (w * Ai.d) * n.y + (w * Ai.e) * n.z,
+                        (w * Ai.c) * n.x + (w * Ai.e) * n.y + (w * Ai.f) * n.z);
+        const d3 vl = qrot(qconj(oa), v);
+        const double is = 1.0 / (maxc(semiA) + maxc(semiB));
+        rec[13] = (float)L; rec[14] = (float)(vl.x * is); rec[15] = (float)(vl.y * is); rec[16] = (float)(vl.z * is);
+      }
+    }
+    return false;
+  }
+  const s33 Gi = symInv(symMix(Ai, Bi, L));
+  const d3 nUnnorm = symMul(Gi, R);
+  const double w = 1 - L;
+  const d3 v = mk((w * Ai.a) * nUnnorm.x + (w * Ai.b) * nUnnorm.y + (w * Ai.c) * nUnnorm.z,
+                  (w * Ai.b) * nUnnorm.x + (w * Ai.d) * nUnnorm.y + (w * Ai.e) * nUnnorm.z,
+                  (w * Ai.c) * nUnnorm.x + (w * Ai.e) * nUnnorm.y + (w * Ai.f) * nUnnorm.z);
+  contPt = pos1 + v;
+  const double mu = sqrt(Fab);
+  const double Rnorm = sqrt(sqnorm(R));
+  const d3 nUnit = normalized(nUnnorm);
+  const d3 rUnit = R / Rnorm;
+  uN = Rnorm * (1 - 1 / mu) * dot(rUnit, nUnit);
+  normal = nUnit;
+  r1 = sqrt(sqnorm(contPt - pos1));
+  r2 = sqrt(sqnorm(contPt - pos2));
+  if (P.ellLog) {
+    const unsigned long long k = atomicAdd(P.ellLogCount, 1ull);
+    if (k < (unsigned long long)P.ellLogCap) {
+      float* rec = P.ellLog + k * ELL_RECORD;
+      ellFeatures(oa, semiA, ob, semiB, R, rec);
+      const d3 vl = qrot(qconj(oa), v);
+      const double is = 1.0 / (maxc(semiA) + maxc(semiB));
+      rec[13] = (float)L; rec[14] = (float)(vl.x * is); rec[15] = (float)(vl.y * is); rec[16] = (float)(vl.z * is);
+    }
+  }
+  return true;
+}
+
+// Cg2_Wall_Ellipsoid_L6Geom::go (Ellipsoid.cpp:227-257); pA is the wall
+__device__ __forceinline__ bool wallEllGeometry(const Particles& p, int a, int b, bool real, d3 pos1, d3 pos2,
+                                                d3& normal, d3& contPt, double& uN, double& r1, double& r2) {
+  const int wa = p.meta[a].x;
+  const int ax = (wa >> 4) & 3, sense = ((wa >> 8) & 3) - 1;
+  const double4_32a SB = p.semi[b], OB = p.ori[b];
+  qd ob;
+  ob.w = OB.x; ob.x = OB.y; ob.y = OB.z; ob.z = OB.w;
+  const d3 c0 = qrot(ob, mk(SB.x, 0, 0)), c1 = qrot(ob, mk(0, SB.y, 0)), c2 = qrot(ob, mk(0, 0, SB.z));
+  const double m0 = comp(c0, ax), m1 = comp(c1, ax), m2 = comp(c2, ax);
+  const double extent = sqrt(m0 * m0 + m1 * m1 + m2 * m2);
+  const double wp = comp(pos1, ax), ep = comp(pos2, ax);
+  if (((wp < (ep - extent)) || (wp > (ep + extent))) && !real) return false;
+  const double dist = ep - wp;
+  const int sgn = (sense == 0) ? (dist > 0 ? 1 : -1) : (sense == 1 ? 1 : -1);
+  const double ds = (double)sgn;
+  normal = mk(ds * (ax == 0 ? 1. : 0.), ds * (ax == 1 ? 1. : 0.), ds * (ax == 2 ? 1. : 0.));
+  uN = sgn * dist - extent;
+  const d3 mp = normalized(mk(m0, m1, m2));
+  const d3 col = mk(c0.x * mp.x + c1.x * mp.y + c2.x * mp.z, c0.y * mp.x + c1.y * mp.y + c2.y * mp.z,
+                    c0.z * mp.x + c1.z * mp.y + c2.z * mp.z);
+  contPt = pos2 + (double)(-sgn) * col;
+  setComp(contPt, ax, wp);
+  const double contR = sqrt(sqnorm(contPt - pos2));
+  r1 = -contR;
+  r2 = contR;
+  return true;
+}
+
+template <int LAW, int CP2, bool PERI, bool ELL>
 __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
@@ -123,7 +262,9 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
     const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
     const float d2 = dx * dx + dy * dy + dz * dz;
     const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
-    const float R = (float)fabs(P.distFactor) * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
+    // ellipsoid pairs: bounding spheres (posf.w = largest semi-axis); outside them F_ab > 1
+    const float df = (ELL && (sb & CS_ELL)) ? 1.f : (float)fabs(P.distFactor);
+    const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
     if (d2 > R * R) return;
   }
   const double4_32a A4 = p.posr[a], B4 = p.posr[b];
@@ -133,7 +274,11 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
   const d3 pos2 = PERI ? xyz(B4) + shift2 : xyz(B4);
   double r1, r2, uN;
   d3 normal, contPt;
-  if (!(sb & CS_WALL_A)) {
+  if (ELL && (sb & CS_ELL)) {
+    if (sb & CS_WALL_A) {
+      if (!wallEllGeometry(p, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
+    } else if (!ellPairGeometry(P, p, c, i, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2, st)) return;
+  } else if (!(sb & CS_WALL_A)) {
     // Cg2_Sphere_Sphere_L6Geom::go
     r1 = A4.w; r2 = B4.w;
     d3 relPos = pos2 - pos1;
@@ -381,15 +526,18 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   if (nc <= 0) return;
   unsigned blocks = (unsigned)((nc + 127) / 128);
-  if (P.periodic) {
+  if (P.hasEll) {
+    // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
+    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+  } else if (P.periodic) {
     if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
     else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   } else if (P.law == WDEM_LAW_IDEALELPL) {
-    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   } else {
-    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
   }
 }
 

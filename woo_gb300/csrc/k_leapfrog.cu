@@ -41,12 +41,83 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
   }
 }
 
-template <bool FROM_ARRAYS, bool PERI>
+// Quaternion::toRotationMatrix (Eigen's formula), row-major
+__device__ __forceinline__ void quatToMat(qd q, double* m) {
+  const double tx = 2 * q.x, ty = 2 * q.y, tz = 2 * q.z;
+  const double twx = tx * q.w, twy = ty * q.w, twz = tz * q.w;
+  const double txx = tx * q.x, txy = ty * q.x, txz = tz * q.x;
+  const double tyy = ty * q.y, tyz = tz * q.y, tzz = tz * q.z;
+  m[0] = 1 - (tyy + tzz); m[1] = txy - twz;       m[2] = txz + twy;
+  m[3] = txy + twz;       m[4] = 1 - (txx + tzz); m[5] = tyz - twx;
+  m[6] = txz - twy;       m[7] = tyz + twx;       m[8] = 1 - (txx + tyy);
+}
+__device__ __forceinline__ double minc(d3 v) { double r = v.x; if (v.y < r) r = v.y; if (v.z < r) r = v.z; return r; }
+// Leapfrog::DotQ (Leapfrog.cpp:325-331)
+__device__ __forceinline__ qd dotQ(d3 w, qd Q) {
+  qd d;
+  d.w = (-Q.x * w.x - Q.y * w.y - Q.z * w.z) / 2;
+  d.x = (Q.w * w.x - Q.z * w.y + Q.y * w.z) / 2;
+  d.y = (Q.z * w.x + Q.w * w.y - Q.x * w.z) / 2;
+  d.z = (-Q.y * w.x + Q.x * w.y + Q.w * w.z) / 2;
+  return d;
+}
+// coefficient-wise q1 + q2 f (Woo's quaternion operator+ and scalar operator*)
+__device__ __forceinline__ qd qaxpy(qd q1, double f, qd q2) {
+  qd r;
+  r.w = q1.w + q2.w * f; r.x = q1.x + q2.x * f; r.y = q1.y + q2.y * f; r.z = q1.z + q2.z * f;
+  return r;
+}
+// Leapfrog::leapfrogAsphericalRotate (Leapfrog.cpp:299-322): angular momentum leapfrog in the body frame
+__device__ __noinline__ void asphericalRotate(const StepParams& P, Particles p, int i, d3 M, d3 inertia, qd& ori,
+                                              d3& angVel) {
+  const double dt = P.dt;
+  d3 am = xyz(p.angMom[i]);
+  double A[9];
+  qd oc;
+  oc.w = ori.w; oc.x = -ori.x; oc.y = -ori.y; oc.z = -ori.z;
+  quatToMat(oc, A);
+  if (isnan(minc(am))) {
+    // inertia.asDiagonal() * ori.conjugate() * angVel
+    double DR[9];
+    for (int r = 0; r < 3; r++) {
+      const double Ir = r == 0 ? inertia.x : (r == 1 ? inertia.y : inertia.z);
+      for (int k = 0; k < 3; k++) DR[3 * r + k] = Ir * A[3 * r + k];
+    }
+    am = mvec(DR, angVel);
+  }
+  const d3 l_n = am + (dt / 2) * M;
+  const d3 l_b_n = mvec(A, l_n);
+  const d3 w_b_n = mk(l_b_n.x / inertia.x, l_b_n.y / inertia.y, l_b_n.z / inertia.z);
+  const qd dq_n = dotQ(w_b_n, ori);
+  const qd q_half = qaxpy(ori, dt / 2, dq_n);
+  am = am + dt * M;
+  const d3 l_b_h = mvec(A, am);
+  const d3 w_b_h = mk(l_b_h.x / inertia.x, l_b_h.y / inertia.y, l_b_h.z / inertia.z);
+  const qd dq_h = dotQ(w_b_h, q_half);
+  ori = qaxpy(ori, dt, dq_h);
+  angVel = qrot(ori, w_b_h);
+  ori = qnormalized(ori);
+  p.angMom[i] = make_double4_32a(am.x, am.y, am.z, 0);
+}
+// .5 w^T (T^T diag(I) T) w, T = rotation matrix of ori, all nine products kept as in the reference
+__device__ __noinline__ double asphericalErot(qd ori, d3 inertia, d3 w) {
+  double T[9], TI[9], M[9];
+  quatToMat(ori, T);
+  const double I[9] = {inertia.x, 0, 0, 0, inertia.y, 0, 0, 0, inertia.z};
+  for (int r = 0; r < 3; r++)
+    for (int k = 0; k < 3; k++) TI[3 * r + k] = T[0 * 3 + r] * I[0 * 3 + k] + T[1 * 3 + r] * I[1 * 3 + k] + T[2 * 3 + r] * I[2 * 3 + k];
+  for (int r = 0; r < 3; r++)
+    for (int k = 0; k < 3; k++) M[3 * r + k] = TI[3 * r + 0] * T[0 * 3 + k] + TI[3 * r + 1] * T[1 * 3 + k] + TI[3 * r + 2] * T[2 * 3 + k];
+  return .5 * dot(w, mvec(M, w));
+}
+
+template <bool FROM_ARRAYS, bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int4 meta = p.meta[i];
   const unsigned flags = (unsigned)meta.w;
+  const bool asph = ELL && (meta.x & META_ASPH);
   const double4_32a vm = p.velm[i];
   const double mass = vm.w;
   const bool blockedAll = (flags & 63u) == 63u;
@@ -121,7 +192,19 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     // a zero torque adds zeros to angVel, which changes no bit unless angVel holds a -0 (then the
     // reference's addition may turn it into +0): skip only when that cannot happen
     const bool inertiaPositive = positiveBits(inertia.x) && positiveBits(inertia.y) && positiveBits(inertia.z);
-    if (!isZeroBits(inertia) && (PERI || !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel)))) {
+    if (ELL && asph) {
+      if (!isZeroBits(inertia)) {
+        // aspherical: blocked rotational DOFs zero the torque, then nonviscDamp1st (Leapfrog.cpp:176-179, 29-31)
+        if (flags & 8u) T.x = 0;
+        if (flags & 16u) T.y = 0;
+        if (flags & 32u) T.z = 0;
+        if (damp) {
+          T.x = T.x * (1 - damping * signum(T.x * angVel0.x));
+          T.y = T.y * (1 - damping * signum(T.y * angVel0.y));
+          T.z = T.z * (1 - damping * signum(T.z * angVel0.z));
+        }
+      }
+    } else if (!isZeroBits(inertia) && (PERI || !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel)))) {
       d3 angAccel;
       if (blockedNone) angAccel = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
       else {
@@ -151,7 +234,14 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       const d3 pv = blockedAll ? mk(0, 0, 0) : vel0, pw = blockedAll ? mk(0, 0, 0) : angVel0;
       const d3 cfv = pv + .5 * dt * linAccelE, cfa = pw + .5 * dt * angAccelE;
       const double Etrans = .5 * mass * sqnorm(cfv);
-      double Erot = 0.5 * dot(cfa, mk(inertia.x * cfa.x, inertia.y * cfa.y, inertia.z * cfa.z));
+      double Erot;
+      const bool aspherical = !(inertia.x == inertia.y && inertia.y == inertia.z);
+      if (ELL && aspherical) {
+        qd o;
+        const double4_32a o4e = p.ori[i];
+        o.w = o4e.x; o.x = o4e.y; o.y = o4e.z; o.z = o4e.w;
+        Erot = asphericalErot(o, inertia, cfa);
+      } else Erot = 0.5 * dot(cfa, mk(inertia.x * cfa.x, inertia.y * cfa.y, inertia.z * cfa.z));
       const double imax = dmax3(inertia);
       if (isnan(Erot) || isinf(imax)) Erot = 0;
       ek = Etrans + Erot;
@@ -163,6 +253,10 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   // leapfrogSphericalRotate (:280-297): q = AngleAxis(|w| dt, w/|w|) * q, normalised
   double4_32a o4 = p.ori[i];
   qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+  if (ELL && asph) {
+    if (isZeroBits(inertia)) { if (atomicCAS(&st->code, 0, WDEM_ERR_STATE) == 0) st->detail = i; }
+    else asphericalRotate(P, p, i, T, inertia, ori, angVel);
+  } else {
   if (!isZeroBits(angVel)) {
     double angle = sqrt(sqnorm(angVel));
     d3 axis = angVel / angle;
@@ -173,6 +267,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     ori = qmul(q, ori);
   }
   ori = qnormalized(ori);
+  }
   p.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
   p.posf[i] = make_float4((float)pos.x, (float)pos.y, (float)pos.z, (float)pr.w);
   p.velm[i] = make_double4_32a(vel.x, vel.y, vel.z, mass);
@@ -186,19 +281,45 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   // aabbIsDirty, run by the collider right after Leapfrog: moved^2 > verletDist^2
   const double4_32a lp = p.lastPos[i];
   const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
-  if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+  if (!ELL) {
+    if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+  } else {
+    // rotation-aware trigger for bounds that track it (maxRot >= 0; Collision.cpp:94-121)
+    double moveDueToRot2 = 0.;
+    const double mr = p.maxRot[i];
+    bool dirty = false;
+    if (mr >= 0.) {
+      const double4_32a l4 = p.lastOri[i];
+      qd lc;
+      lc.w = l4.x; lc.x = -l4.y; lc.y = -l4.z; lc.z = -l4.w;
+      const qd dq = qmul(lc, ori);
+      const double nv = sqrt(dq.x * dq.x + dq.y * dq.y + dq.z * dq.z);
+      const double ang = (nv != 0) ? 2 * atan2(nv, fabs(dq.w)) : 0.;
+      const double rot = fmax(0., fabs(ang));
+      if (rot > mr) dirty = true;
+      const double4_32a bmn = p.bbmin[i], bmx = p.bbmax[i];
+      const double arm = dmax3(mk(bmx.x - bmn.x, bmx.y - bmn.y, bmx.z - bmn.z));
+      const double mv = .5 * arm * rot;
+      moveDueToRot2 = mv * mv;
+    }
+    const double d2 = sqnorm(dd);
+    if (dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2) st->dirty = 1;
+  }
 }
 
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays, Contacts c, Csr csr,
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
-  if (P.periodic) {
-    if (fromArrays) (k_leapfrog<true, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
-    else (k_leapfrog<false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  if (P.hasEll) {
+    if (fromArrays) (k_leapfrog<true, false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    else (k_leapfrog<false, false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+  } else if (P.periodic) {
+    if (fromArrays) (k_leapfrog<true, true, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    else (k_leapfrog<false, true, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
   } else {
-    if (fromArrays) (k_leapfrog<true, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
-    else (k_leapfrog<false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    if (fromArrays) (k_leapfrog<true, false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    else (k_leapfrog<false, false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
   }
 }
 

@@ -35,6 +35,7 @@ struct ContactBuf {
   bool hertz = false;
   bool geom = false;
   bool peri = false;
+  bool ell = false;
 };
 
 // Periodic cell on the host (Cell, src/core/Cell.hpp / Cell.cpp), homoDeform GRADV2; row-major 3x3.
@@ -176,6 +177,11 @@ struct wdem_handle {
   double* staging = nullptr;    // 13 n doubles for wdem_write_state / wdem_read_state
   long long stagingCap = 0;
   bool periodic = false;
+  bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
+  std::vector<double> semi;     // host copy of the semi-axes (3n; spheres r, r, r)
+  float* ellLog = nullptr;      // training records of the ellipsoid solves, when logging
+  unsigned long long* ellLogCount = nullptr;
+  long long ellLogCap = 0;
   HostCell cell;
   double* dStress = nullptr;    // 9 stress components + scratch for the terms
   double* stressTerms = nullptr;
@@ -214,12 +220,14 @@ void freeContacts(ContactBuf& b) {
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   cudaFree(c.cdist);
+  cudaFree(c.lam);
+  cudaFree(c.lam0);
   memset(&c, 0, sizeof(c));
   b.cap = 0;
 }
 
 // (Re)allocate one contact buffer for `cap` contacts, keeping nothing.
-cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, bool peri) {
+cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, bool peri, bool ell) {
   freeContacts(b);
   Contacts& c = b.c;
   cudaError_t e;
@@ -233,8 +241,10 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   if (peri && (e = dalloc(c.cdist, cap))) return e;
+  if (ell && ((e = dalloc(c.lam, cap)) || (e = dalloc(c.lam0, cap)))) return e;
   b.cap = cap;
   b.peri = peri;
+  b.ell = ell;
   b.hertz = hertz;
   b.geom = geom;
   return cudaSuccess;
@@ -394,9 +404,9 @@ int rebuild(wdem_handle* h) {
   const long long retained = h->hcounts[1];
   const long long nNew = total + retained;
   const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
-  if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom || neu.peri != h->periodic) {
+  if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom || neu.peri != h->periodic || neu.ell != h->hasEll) {
     long long cap = std::max<long long>(nNew + nNew / 4 + 1024, neu.cap);
-    CK(allocContacts(neu, cap, hertz, h->keepGeom, h->periodic));
+    CK(allocContacts(neu, cap, hertz, h->keepGeom, h->periodic, h->hasEll));
   }
   if (h->periodic) col_periodic(s, h->P, h->d, h->dSmall, nSmall, cs, neu.c.ids, neu.c.cdist, neu.cap, true, h->dst);
   else col_sweep(s, h->d, nSmall, h->P.loneMask, cs, neu.c.ids, neu.cap, true, h->dst);
@@ -444,6 +454,15 @@ void fillStepParams(wdem_handle* h) {
   P.lfEnergy = r.trackEnergy;
   P.nMaterials = (int)h->mats.size();
   P.periodic = h->periodic ? 1 : 0;
+  P.hasEll = h->hasEll ? 1 : 0;
+  P.ellSolver = r.ellSolver;
+  P.brentTol = std::ldexp(1.0, 1 - std::min(std::numeric_limits<double>::digits / 2, (int)r.brentBits));
+  P.newtonTol = r.newtonTol;
+  P.warmStart = r.warmStart;
+  P.fallbackIters = r.fallbackIters;
+  P.ellLog = h->ellLog;
+  P.ellLogCount = h->ellLogCount;
+  P.ellLogCap = h->ellLogCap;
 }
 
 // Cell-dependent parameters of one step: shifts, unshear, Leapfrog GRADV2 matrices (Leapfrog.cpp:119-127)
@@ -472,8 +491,13 @@ void resolveVerlet(wdem_handle* h) {
   double vd = h->raw.verletDist;
   if (vd >= 0) { h->verletDistResolved = vd; return; }
   double minR = std::numeric_limits<double>::infinity();
-  for (int i = 0; i < h->n; i++)
-    if (h->shape[i] == WDEM_SHAPE_SPHERE && !std::isnan(h->radius[i])) minR = std::min(h->radius[i], minR);
+  for (int i = 0; i < h->n; i++) {
+    // Shape::equivRadius: Sphere.radius, Ellipsoid cbrt(abc) (Ellipsoid.cpp:25-28)
+    double r = std::numeric_limits<double>::quiet_NaN();
+    if (h->shape[i] == WDEM_SHAPE_SPHERE) r = h->radius[i];
+    else if (h->shape[i] == WDEM_SHAPE_ELLIPSOID) r = std::cbrt(h->semi[3 * i] * h->semi[3 * i + 1] * h->semi[3 * i + 2]);
+    if (!std::isnan(r)) minR = std::min(r, minR);
+  }
   h->verletDistResolved = std::isinf(minR) ? 0.0 : std::abs(vd) * minR;
 }
 
@@ -530,7 +554,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   cudaMemset(h->csr.rowptr, 0, sizeof(int) * ((size_t)N + 1));
   memset(h->hst, 0, sizeof(DeviceStatus));
   // an empty contact buffer on the current side
-  if (allocContacts(h->buf[0], 1024, false, false, false) != cudaSuccess) { wdem_destroy(h); return WDEM_ERR_CUDA; }
+  if (allocContacts(h->buf[0], 1024, false, false, false, false) != cudaSuccess) { wdem_destroy(h); return WDEM_ERR_CUDA; }
   if (ensureScratch(h, 0)) { wdem_destroy(h); return WDEM_ERR_CUDA; }
   *out = h;
   return WDEM_OK;
@@ -541,6 +565,8 @@ int wdem_destroy(wdem_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   Particles& d = h->d;
+  cudaFree(d.semi); cudaFree(d.angMom); cudaFree(d.lastOri); cudaFree(d.maxRot);
+  cudaFree(h->ellLog); cudaFree(h->ellLogCount);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
   cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
@@ -621,20 +647,39 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   h->smallIds.clear(); h->largeIds.clear();
   std::vector<double4_32a> posr(n), velm(n), angw(n), inert(n), ori(n), force(n), torque(n);
   std::vector<int4> meta(n);
+  std::vector<double> semi(3 * (size_t)n, 0.0);
+  bool anyEll = false;
   for (int i = 0; i < n; i++) {
     int sh = p->shape[i];
-    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL) return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID)
+      return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (sh == WDEM_SHAPE_ELLIPSOID) {
+      if (!p->semiAxes) return fail(h, WDEM_ERR_ARG, "ellipsoids need wdem_particles.semiAxes");
+      const double* sa = p->semiAxes + 3 * i;
+      if (!(sa[0] > 0 && sa[1] > 0 && sa[2] > 0))
+        return fail(h, WDEM_ERR_ARG, "Ellipsoid #" + std::to_string(i) + ": all semi-axes must be positive");
+      if (h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "ellipsoids in a periodic cell are not supported");
+    }
     if (sh == WDEM_SHAPE_WALL && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
     if (p->material[i] < 0 || (h->paramsSet && p->material[i] >= (int)h->mats.size()))
       return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
     const double* in = p->inertia + 3 * i;
     unsigned fl = p->flags[i];
     if (fl & (WDEM_CLUMP_CLUMP | WDEM_CLUMP_CLUMPED)) return fail(h, WDEM_ERR_UNSUPPORTED, "clumps are not supported");
-    bool asph = !(in[0] == in[1] && in[1] == in[2]);
-    if (asph && (fl & 56u) != 56u) return fail(h, WDEM_ERR_UNSUPPORTED, "aspherical integration (unequal inertia) is not supported");
+    // DemData::useAsphericalLeapfrog: unequal inertia and a free rotational DOF (Particle.hpp:275-277)
+    const bool asph = !(in[0] == in[1] && in[1] == in[2]) && (fl & 56u) != 56u;
+    if (asph && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "aspherical nodes in a periodic cell are not supported");
     int ax = p->wallAxis ? p->wallAxis[i] : 0, sense = p->wallSense ? p->wallSense[i] : 0;
     if (sh == WDEM_SHAPE_WALL && (ax < 0 || ax > 2 || sense < -1 || sense > 1)) return fail(h, WDEM_ERR_ARG, "bad wall axis/sense");
     double r = sh == WDEM_SHAPE_SPHERE ? p->radius[i] : 0.0;
+    if (sh == WDEM_SHAPE_ELLIPSOID) {
+      // bounding radius: the largest semi-axis (FP32 cull and minDist00Sq of the ellipsoid functors)
+      const double* sa = p->semiAxes + 3 * i;
+      r = sa[0]; if (sa[1] > r) r = sa[1]; if (sa[2] > r) r = sa[2];
+    }
+    if (sh == WDEM_SHAPE_ELLIPSOID) { semi[3 * i] = p->semiAxes[3 * i]; semi[3 * i + 1] = p->semiAxes[3 * i + 1]; semi[3 * i + 2] = p->semiAxes[3 * i + 2]; }
+    else if (sh == WDEM_SHAPE_SPHERE) { semi[3 * i] = semi[3 * i + 1] = semi[3 * i + 2] = r; }
+    anyEll |= (sh == WDEM_SHAPE_ELLIPSOID) || asph;
     posr[i] = make_double4_32a(p->pos[3 * i], p->pos[3 * i + 1], p->pos[3 * i + 2], r);
     velm[i] = make_double4_32a(p->vel[3 * i], p->vel[3 * i + 1], p->vel[3 * i + 2], p->mass[i]);
     angw[i] = make_double4_32a(p->angVel[3 * i], p->angVel[3 * i + 1], p->angVel[3 * i + 2], 0);
@@ -642,9 +687,11 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     ori[i] = make_double4_32a(p->ori[4 * i], p->ori[4 * i + 1], p->ori[4 * i + 2], p->ori[4 * i + 3]);
     force[i] = make_double4_32a(p->force[3 * i], p->force[3 * i + 1], p->force[3 * i + 2], 0);
     torque[i] = make_double4_32a(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2], 0);
-    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8), p->material[i], (int)p->mask[i], (int)fl);
-    if (sh == WDEM_SHAPE_SPHERE) h->smallIds.push_back(i); else h->largeIds.push_back(i);
+    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0), p->material[i], (int)p->mask[i], (int)fl);
+    if (sh != WDEM_SHAPE_WALL) h->smallIds.push_back(i); else h->largeIds.push_back(i);
   }
+  h->semi = semi;
+  h->hasEll = anyEll;
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   if (n > 0) {
@@ -656,6 +703,24 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     CK(cudaMemcpyAsync(h->d.force, force.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->d.torque, torque.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->d.meta, meta.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s));
+  }
+  if (h->hasEll) {
+    // rotation state of ellipsoid / aspherical scenes
+    if (!h->d.semi) {
+      CK(dalloc(h->d.semi, h->N)); CK(dalloc(h->d.angMom, h->N)); CK(dalloc(h->d.lastOri, h->N)); CK(dalloc(h->d.maxRot, h->N));
+    }
+    std::vector<double4_32a> sv(n), am(n);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    for (int i = 0; i < n; i++) {
+      sv[i] = make_double4_32a(semi[3 * i], semi[3 * i + 1], semi[3 * i + 2], 0);
+      if (p->angMom) am[i] = make_double4_32a(p->angMom[3 * i], p->angMom[3 * i + 1], p->angMom[3 * i + 2], 0);
+      else am[i] = make_double4_32a(nan, nan, nan, 0);
+    }
+    if (n > 0) {
+      CK(cudaMemcpyAsync(h->d.semi, sv.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(h->d.angMom, am.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));  // host vectors go out of scope
   }
   if (!h->smallIds.empty())
     CK(cudaMemcpyAsync(h->dSmall, h->smallIds.data(), h->smallIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -683,8 +748,8 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
   cudaStream_t s = h->stream;
   const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
   ContactBuf& b = h->buf[h->cur];
-  if (nc > b.cap || b.hertz != hertz || b.geom != h->keepGeom || b.peri != h->periodic)
-    CK(allocContacts(b, std::max<long long>(nc + 1024, 1024), hertz, h->keepGeom, h->periodic));
+  if (nc > b.cap || b.hertz != hertz || b.geom != h->keepGeom || b.peri != h->periodic || b.ell != h->hasEll)
+    CK(allocContacts(b, std::max<long long>(nc + 1024, 1024), hertz, h->keepGeom, h->periodic, h->hasEll));
   std::vector<int2> ids(nc);
   std::vector<uint8_t> state(nc);
   std::vector<int> step0(nc);
@@ -695,7 +760,11 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     int a = c->idA[i], bb = c->idB[i];
     if (a < 0 || a >= h->n || bb < 0 || bb >= h->n || a == bb) return fail(h, WDEM_ERR_ARG, "bad contact ids");
     bool swapped = false;
-    if (h->shape[a] == WDEM_SHAPE_SPHERE && h->shape[bb] == WDEM_SHAPE_WALL) { std::swap(a, bb); swapped = true; }
+    {
+      const int sa = h->shape[a], sbb = h->shape[bb];
+      if ((sa == WDEM_SHAPE_SPHERE && sbb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sbb == WDEM_SHAPE_SPHERE) ||
+          (sa == WDEM_SHAPE_ELLIPSOID && sbb == WDEM_SHAPE_WALL)) { std::swap(a, bb); swapped = true; }
+    }
     ids[i] = make_int2(a, bb);
     if (c->cellDist) {
       int sg = swapped ? -1 : 1;
@@ -703,7 +772,8 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     }
     bool real = c->real[i] != 0;
     state[i] = (uint8_t)((real ? CS_REAL : CS_POTENTIAL) | (h->shape[a] == WDEM_SHAPE_WALL ? CS_WALL_A : 0) |
-                         (h->shape[bb] == WDEM_SHAPE_WALL ? CS_WALL_B : 0));
+                         (h->shape[bb] == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
+                         (h->shape[a] == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (h->shape[bb] == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
     step0[i] = c->stepCreated[i];
     if (real) {
       if (!c->trsf || !c->contPt || !c->force || !c->kn || !c->kt || !c->tanPhi) return fail(h, WDEM_ERR_ARG, "real contact without history arrays");
@@ -720,6 +790,9 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     CK(cudaMemcpyAsync(b.c.tanPhi, tanPhi.data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
     for (int k = 0; k < HIST_FRICT; k++) CK(cudaMemcpyAsync(b.c.hist[k], hist[k].data(), nc * sizeof(double), cudaMemcpyHostToDevice, s));
     if (b.c.cdist) CK(cudaMemcpyAsync(b.c.cdist, cdist.data(), nc * sizeof(int4), cudaMemcpyHostToDevice, s));
+    // no solver history in the container: all-ones bytes are NaN, i.e. "cold start"
+    if (b.c.lam) CK(cudaMemsetAsync(b.c.lam, 0xFF, nc * sizeof(double), s));
+    if (b.c.lam0) CK(cudaMemsetAsync(b.c.lam0, 0xFF, nc * sizeof(float), s));
   }
   launch_init_uploaded(s, h->P, h->d, b.c, nc);
   int rc;
@@ -737,6 +810,13 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   for (int i = 0; i < h->n; i++)
     if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size())
       return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
+  if (h->hasEll && (h->P.law != WDEM_LAW_IDEALELPL || h->P.cp2 != WDEM_CP2_FRICT))
+    return fail(h, WDEM_ERR_UNSUPPORTED,
+                "ellipsoids and aspherical nodes run with Cp2_FrictMat_FrictPhys + Law2_L6Geom_FrictPhys_IdealElPl only");
+  if (h->hasEll && h->P.ellSolver != WDEM_ELL_BRENT && h->P.ellSolver != WDEM_ELL_NEWTON)
+    return fail(h, WDEM_ERR_ARG, "unknown ellipsoid solver");
+  if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && !(h->P.newtonTol > 0))
+    return fail(h, WDEM_ERR_ARG, "newtonTol must be positive");
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   for (int k = 0; k < 3; k++) { h->phaseMs[k] = 0; h->phaseLaunches[k] = 0; }
@@ -829,8 +909,14 @@ int wdem_download_particles(wdem_handle* h, wdem_particles* p) {
     CK(cudaMemcpyAsync(force.data(), h->d.force, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(torque.data(), h->d.torque, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
   }
+  std::vector<double4_32a> am;
+  if (h->hasEll && p->angMom && n > 0) {
+    am.resize(n);
+    CK(cudaMemcpyAsync(am.data(), h->d.angMom, n * sizeof(double4_32a), cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < n; i++) {
+    if (!am.empty()) { p->angMom[3 * i] = am[i].x; p->angMom[3 * i + 1] = am[i].y; p->angMom[3 * i + 2] = am[i].z; }
     if (p->pos) { p->pos[3 * i] = posr[i].x; p->pos[3 * i + 1] = posr[i].y; p->pos[3 * i + 2] = posr[i].z; }
     if (p->vel) { p->vel[3 * i] = velm[i].x; p->vel[3 * i + 1] = velm[i].y; p->vel[3 * i + 2] = velm[i].z; }
     if (p->angVel) { p->angVel[3 * i] = angw[i].x; p->angVel[3 * i + 1] = angw[i].y; p->angVel[3 * i + 2] = angw[i].z; }
@@ -983,10 +1069,15 @@ int wdem_crit_dt(wdem_handle* h, double* dt) {
   if (!h || !dt) return WDEM_ERR_ARG;
   double r = std::numeric_limits<double>::infinity();
   for (int i = 0; i < h->n; i++) {
-    if (h->shape[i] != WDEM_SHAPE_SPHERE) continue;
+    double radius;
+    if (h->shape[i] == WDEM_SHAPE_SPHERE) radius = h->radius[i];
+    else if (h->shape[i] == WDEM_SHAPE_ELLIPSOID) {
+      const double* sa = &h->semi[3 * i];
+      radius = sa[0]; if (sa[1] < radius) radius = sa[1]; if (sa[2] < radius) radius = sa[2];
+    } else continue;
     if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size()) return fail(h, WDEM_ERR_STATE, "materials not set");
     const wdem_material& m = h->mats[h->mat[i]];
-    r = std::min(r, h->radius[i] / (1. * std::sqrt(m.young / m.density)));
+    r = std::min(r, radius / (1. * std::sqrt(m.young / m.density)));
   }
   *dt = r;
   return WDEM_OK;
@@ -1026,6 +1117,9 @@ int wdem_get_status(wdem_handle* h, wdem_status* st) {
   st->nFullRuns = h->nFullRuns;
   st->capacity = h->buf[h->cur].cap;
   st->lastRunFull = h->lastRunFull;
+  st->ellSolves = (int64_t)h->hst->ellSolves;
+  st->ellIters = (int64_t)h->hst->ellIters;
+  st->ellFallbacks = (int64_t)h->hst->ellFallbacks;
   return WDEM_OK;
 }
 

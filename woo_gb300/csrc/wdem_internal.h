@@ -34,7 +34,9 @@ extern long long g_kernel_launches;
 
 // contact state byte: bits 0-1 the lifecycle state, bit 2 "pA is a wall", bit 3 "pB is a wall"
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
-enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_SHAPES = 12 };
+enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_ELL_B = 32, CS_ELL = 48, CS_SHAPES = 60 };
+// meta.x: shape (bits 0-3), wall axis (4-5), wall sense + 1 (8-9), aspherical Leapfrog (bit 12)
+enum { META_ASPH = 1 << 12 };
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
@@ -82,10 +84,24 @@ struct StepParams {
   double spinVec[3];
   double ImLL4hInv[9], IpLL4h[9], LmL[9];  // Leapfrog GRADV2 matrices
   double dSpin[3];     // Leapfrog.deltaSpinVec
+  // ellipsoids: Cg2_Ellipsoid_Ellipsoid_L6Geom solver
+  int hasEll;
+  int ellSolver;       // WDEM_ELL_*
+  double brentTol;     // 2^(1 - min(brentBits, 26))
+  double newtonTol;
+  int warmStart;       // WDEM_WARM_*
+  int fallbackIters;
+  float* ellLog;                     // training records of solved pairs (17 floats each), or null
+  unsigned long long* ellLogCount;
+  long long ellLogCap;
 };
 
 struct Particles {
   double4_32a *posr, *velm, *angw, *inert, *ori, *lastPos, *bbmin, *bbmax, *force, *torque;
+  // scenes with ellipsoids (else null): semi-axes (a, b, c, 0; spheres r, r, r), DemData.angMom
+  // (NaN = not initialised), Aabb.nodeLastOri and Aabb.maxRot (< 0: rotation ignored)
+  double4_32a *semi, *angMom, *lastOri;
+  double* maxRot;
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
   double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
@@ -103,6 +119,8 @@ struct Contacts {
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
   int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
+  double* lam;      // ellipsoid pairs: maximiser lambda of the last solve (NaN = none); null otherwise
+  float* lam0;      // learned warm start of this step's solve (NaN = none); null unless used
 };
 
 struct Csr {
@@ -127,6 +145,7 @@ struct DeviceStatus {
   int dirty;          // set by the integrator when a particle left its verlet box
   int overflow;
   unsigned long long pairTotal;
+  unsigned long long ellSolves, ellIters, ellFallbacks;  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
 

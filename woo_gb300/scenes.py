@@ -347,26 +347,35 @@ def assemble_ellipsoids(centers, semi_axes, oris, mat, walls, mats_py, vel=None,
 
 def ellipsoid_cloud(n, seed, box=(0.1, 0.1, 0.1), amin=0.004, amax=0.006, ratios=(1.0, 0.7, 0.5), walls=True,
                     vel_scale=0.5, angvel_scale=5.0, gravity=(0, 0, -9.81), damping=0.2, dense=1.0, young=1e7,
-                    tanPhi=0.4, density=1000.0, dt_safety=0.9, **kw):
+                    tanPhi=0.4, density=1000.0, dt_safety=0.9, sphere_frac=0.0, **kw):
     """Ellipsoids with semi-axes a*ratios (a uniform in [amin, amax]) and uniformly random orientations,
     placed by random sequential addition of their bounding spheres (radius a) in `box`, optionally
-    squeezed by `dense` (< 1 makes overlaps); FrictMat + IdealElPl; dt = dt_safety x pWaveDt."""
+    squeezed by `dense` (< 1 makes overlaps); FrictMat + IdealElPl; dt = dt_safety x pWaveDt.  A fraction
+    `sphere_frac` of the bodies are spheres of radius a instead (sphere + ellipsoid contacts)."""
     rng = np.random.default_rng(seed)
     lo, hi = np.zeros(3), np.asarray(box, np.float64)
     centers, a = abi.make_cloud(lo, hi, amin, amax, n, seed)
     if dense != 1.0:
         c = hi / 2
         centers = c + (centers - c) * dense
-    k = len(a)
-    semi = a[:, None] * np.asarray(ratios, np.float64)[None, :]
+    sph = rng.random(len(a)) < sphere_frac
+    ce, ae = centers[~sph], a[~sph]
+    k = len(ae)
+    semi = ae[:, None] * np.asarray(ratios, np.float64)[None, :]
     oris = random_quaternions(k, rng)
     mats_py = [dict(kind=abi.MAT_FRICT, density=density, young=young, ktDivKn=0.2, tanPhi=tanPhi)]
     mats = materials_array(mats_py)
-    pa = assemble_ellipsoids(centers, semi, oris, 0, box_walls(lo, hi) if walls else [], mats_py,
-                             vel=rng.normal(0, vel_scale, (k, 3)))
+    spheres = (centers[sph], a[sph], 0) if sph.any() else None
+    pa = assemble_ellipsoids(ce, semi, oris, 0, box_walls(lo, hi) if walls else [], mats_py,
+                             vel=rng.normal(0, vel_scale, (k, 3)), spheres=spheres)
     nw = 6 if walls else 0
-    pa.angVel[nw:] = rng.normal(0, angvel_scale, (k, 3))
-    dt = dt_safety * float(np.min(semi.min(axis=1) / np.sqrt(young / density)))
+    nb = pa.n - nw
+    pa.vel[nw:] = rng.normal(0, vel_scale, (nb, 3))
+    pa.angVel[nw:] = rng.normal(0, angvel_scale, (nb, 3))
+    smin = semi.min(axis=1) if k else np.array([np.inf])
+    if sph.any():
+        smin = np.concatenate([smin, a[sph]])
+    dt = dt_safety * float(np.min(smin / np.sqrt(young / density)))
     extra = dict(cp2=abi.CP2_FRICT, law=abi.LAW_IDEALELPL)
     extra.update(kw)
     p = default_params(mats, dt=dt, gravity=gravity, damping=damping, **extra)
