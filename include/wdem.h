@@ -287,6 +287,38 @@ int wdem_get_cell(wdem_handle* h, wdem_cell* c);
  * src/dem/ContactLoop.cpp:218-229, 243-244); volume 1 for aperiodic scenes. */
 int wdem_get_stress(wdem_handle* h, double* stress);
 
+/* ---- learned warm start of the ellipsoid solve (no counterpart in the reference) -------------------
+ * A 13 -> 64 -> 64 -> 64 -> 4 ReLU network, BF16 on the tensor cores with FP32 accumulation, predicts
+ * the maximiser lambda of the Perram-Wertheim contact function (and the contact point) of an ellipsoid
+ * pair from WDEM_WARM_INPUTS features; with warmStart = WDEM_WARM_MLP its lambda starts the Newton solve,
+ * which falls back to the cold start after fallbackIters iterations.  A record is the features followed
+ * by the solver's converged lambda and contact point (WDEM_WARM_RECORD floats): features = centre offset
+ * of B in A's frame (3), orientation of B relative to A with w >= 0 (4), semi-axes of A (3) and of B (3),
+ * lengths divided by max(a) + max(b); targets = lambda, contact point in A's frame / (max(a) + max(b)).
+ * Weights (WDEM_WARM_NPARAM floats): W1 (13 x 64, row = input), b1 (64), W2 (64 x 64), b2, W3, b3,
+ * W4 (64 x 4), b4 (4). */
+#define WDEM_WARM_INPUTS 13
+#define WDEM_WARM_OUTPUTS 4
+#define WDEM_WARM_RECORD 17
+#define WDEM_WARM_NPARAM 9476
+int wdem_warm_init(wdem_handle* h, uint64_t seed);                     /* He-uniform weights, zero biases */
+int wdem_warm_set_weights(wdem_handle* h, const float* w, int64_t n);  /* n == WDEM_WARM_NPARAM */
+int wdem_warm_get_weights(wdem_handle* h, float* w, int64_t n);
+/* outputs (n x 4) of feature rows (n x 13) */
+int wdem_warm_predict(wdem_handle* h, const float* x, int64_t n, float* y);
+/* gradient (WDEM_WARM_NPARAM) and value of the mean weighted squared error over n records
+ * (output weights 1, 0.1, 0.1, 0.1) */
+int wdem_warm_grad(wdem_handle* h, const float* records, int64_t n, float* grad, float* loss);
+/* Adam training on n records: epochs over a seeded shuffle, mini-batches of `batch`, learning rate lr
+ * decayed along a half cosine to lr/100 over the run; lossPerEpoch (epochs floats, may be NULL)
+ * receives the mean training loss of each epoch. */
+int wdem_warm_train(wdem_handle* h, const float* records, int64_t n, int32_t epochs, int32_t batch, float lr,
+                    uint64_t seed, float* lossPerEpoch);
+/* Log a record for every ellipsoid pair solved in the following steps, up to capRecords (0 stops and
+ * frees the log); wdem_ell_log_read copies up to cap logged records out and sets *n. */
+int wdem_ell_log(wdem_handle* h, int64_t capRecords);
+int wdem_ell_log_read(wdem_handle* h, float* out, int64_t cap, int64_t* n);
+
 /* wdem_get_stress without any device memory allocation.  No counterpart in the reference: it exists
  * for callers that must not touch the CUDA allocator at the moment they ask for the stress, e.g. a
  * controller running between steps of a serving loop whose memory is fully reserved up front, where

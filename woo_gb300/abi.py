@@ -27,6 +27,7 @@ WDEM_ERR_STATE = -9
 
 SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID = 0, 1, 2
 ELL_BRENT, ELL_NEWTON = 0, 1
+WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
 WARM_COLD, WARM_MLP, WARM_HISTORY = 0, 1, 2
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
@@ -43,6 +44,7 @@ ENERGY_NAMES = ["kinetic", "grav", "nonviscDamp", "elast", "plast", "viscN", "vi
 D = C.POINTER(C.c_double)
 I32 = C.POINTER(C.c_int32)
 U32 = C.POINTER(C.c_uint32)
+F32 = C.POINTER(C.c_float)
 
 
 class Material(C.Structure):
@@ -103,7 +105,8 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
-           "wdem_get_stress_noalloc"]
+           "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
+           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read"]
 
 
 def ptr(a, ctype):
@@ -250,6 +253,14 @@ def load(path=None):
         "wdem_get_cell": ([h, C.POINTER(Cell)], C.c_int),
         "wdem_get_stress": ([h, D], C.c_int),
         "wdem_get_stress_noalloc": ([h, D], C.c_int),
+        "wdem_warm_init": ([h, C.c_uint64], C.c_int),
+        "wdem_warm_set_weights": ([h, F32, C.c_int64], C.c_int),
+        "wdem_warm_get_weights": ([h, F32, C.c_int64], C.c_int),
+        "wdem_warm_predict": ([h, F32, C.c_int64, F32], C.c_int),
+        "wdem_warm_grad": ([h, F32, C.c_int64, F32, F32], C.c_int),
+        "wdem_warm_train": ([h, F32, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, F32], C.c_int),
+        "wdem_ell_log": ([h, C.c_int64], C.c_int),
+        "wdem_ell_log_read": ([h, F32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -390,6 +401,48 @@ class Handle:
         m = np.zeros(9)
         self.check(self.lib.wdem_get_stress_noalloc(self.h, ptr(m, C.c_double)))
         return m.reshape(3, 3)
+
+    # ---- learned warm start of the ellipsoid solve
+    def warm_init(self, seed=0):
+        self.check(self.lib.wdem_warm_init(self.h, seed))
+
+    def warm_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        self.check(self.lib.wdem_warm_set_weights(self.h, ptr(w, C.c_float), w.size))
+
+    def warm_get_weights(self):
+        w = np.zeros(WARM_NPARAM, np.float32)
+        self.check(self.lib.wdem_warm_get_weights(self.h, ptr(w, C.c_float), w.size))
+        return w
+
+    def warm_predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((len(X), WARM_OUTPUTS), np.float32)
+        self.check(self.lib.wdem_warm_predict(self.h, ptr(X, C.c_float), len(X), ptr(Y, C.c_float)))
+        return Y
+
+    def warm_grad(self, R):
+        R = np.ascontiguousarray(R, np.float32)
+        g = np.zeros(WARM_NPARAM, np.float32)
+        loss = np.zeros(1, np.float32)
+        self.check(self.lib.wdem_warm_grad(self.h, ptr(R, C.c_float), len(R), ptr(g, C.c_float), ptr(loss, C.c_float)))
+        return g, float(loss[0])
+
+    def warm_train(self, R, epochs=5, batch=512, lr=1e-3, seed=0):
+        R = np.ascontiguousarray(R, np.float32)
+        losses = np.zeros(max(epochs, 1), np.float32)
+        self.check(self.lib.wdem_warm_train(self.h, ptr(R, C.c_float), len(R), epochs, batch, lr, seed,
+                                            ptr(losses, C.c_float)))
+        return losses[:epochs]
+
+    def ell_log(self, cap):
+        self.check(self.lib.wdem_ell_log(self.h, cap))
+
+    def ell_log_read(self, cap):
+        out = np.zeros((cap, WARM_RECORD), np.float32)
+        n = C.c_int64()
+        self.check(self.lib.wdem_ell_log_read(self.h, ptr(out, C.c_float), cap, C.byref(n)))
+        return out[:n.value]
 
     def fp64_peak(self):
         v = C.c_double()

@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwdem.so")
 
-SOURCES = ["k_contact.cu", "k_leapfrog.cu", "k_collider.cu", "wdem_api.cu", "wdem_pack.cu", "k_noalloc.cu"]
+SOURCES = ["k_contact.cu", "k_leapfrog.cu", "k_collider.cu", "wdem_api.cu", "wdem_pack.cu", "k_noalloc.cu", "k_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2", "-Xcompiler", "-Wno-deprecated-declarations"]

@@ -183,6 +183,11 @@ struct wdem_handle {
   unsigned long long* ellLogCount = nullptr;
   long long ellLogCap = 0;
   HostCell cell;
+  // learned warm start: FP32 master weights (padded layout), BF16 copy, Adam moments, gradient
+  float *mlpW = nullptr, *mlpM = nullptr, *mlpV = nullptr, *mlpGrad = nullptr, *mlpLoss = nullptr;
+  uint16_t* mlpWbf = nullptr;
+  bool mlpReady = false;
+  long long mlpT = 0;
   double* dStress = nullptr;    // 9 stress components + scratch for the terms
   double* stressTerms = nullptr;
   long long stressCap = 0;
@@ -567,6 +572,7 @@ int wdem_destroy(wdem_handle* h) {
   Particles& d = h->d;
   cudaFree(d.semi); cudaFree(d.angMom); cudaFree(d.lastOri); cudaFree(d.maxRot);
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
+  cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
   cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
@@ -817,6 +823,8 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     return fail(h, WDEM_ERR_ARG, "unknown ellipsoid solver");
   if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && !(h->P.newtonTol > 0))
     return fail(h, WDEM_ERR_ARG, "newtonTol must be positive");
+  if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP && !h->mlpReady)
+    return fail(h, WDEM_ERR_STATE, "warmStart=MLP needs a network (wdem_warm_init / wdem_warm_set_weights / wdem_warm_train)");
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   for (int k = 0; k < 3; k++) { h->phaseMs[k] = 0; h->phaseLaunches[k] = 0; }
@@ -866,6 +874,8 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     }
     {
       PhaseTimer t(h, PH_CONTACTS);
+      if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP)
+        mlp_launch_warm(s, h->d, h->buf[h->cur].c, h->nContacts, h->mlpWbf, h->mlpW);
       launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst);
     }
     if (h->P.trackEnergy) {
@@ -1282,6 +1292,192 @@ int wdem_get_stress_noalloc(wdem_handle* h, double* stress) {
   CK(cudaStreamSynchronize(h->stream));
   const double vol = h->periodic ? det3(h->cell.hSize) : 1.0;
   for (int k = 0; k < 9; k++) stress[k] = v[k] / vol;
+  return WDEM_OK;
+}
+
+namespace {
+int mlpEnsure(wdem_handle* h) {
+  if (h->mlpW) return WDEM_OK;
+  const int n = mlp_npad();
+  CK(mlp_prepare_kernels());
+  CK(dalloc(h->mlpW, n)); CK(dalloc(h->mlpM, n)); CK(dalloc(h->mlpV, n)); CK(dalloc(h->mlpGrad, n)); CK(dalloc(h->mlpLoss, 1));
+  CK(dalloc(h->mlpWbf, n));
+  CK(cudaMemsetAsync(h->mlpGrad, 0, n * sizeof(float), h->stream));
+  return WDEM_OK;
+}
+int mlpUpload(wdem_handle* h, const std::vector<float>& pad) {
+  const int n = mlp_npad();
+  CK(cudaMemcpyAsync(h->mlpW, pad.data(), n * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->mlpM, 0, n * sizeof(float), h->stream));
+  CK(cudaMemsetAsync(h->mlpV, 0, n * sizeof(float), h->stream));
+  mlp_to_bf16(h->stream, h->mlpW, h->mlpWbf);
+  CK(cudaStreamSynchronize(h->stream));
+  h->mlpT = 0;
+  h->mlpReady = true;
+  return WDEM_OK;
+}
+unsigned long long splitmix64(unsigned long long& x) {
+  unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double uniform01(unsigned long long& x) { return (double)(splitmix64(x) >> 11) * (1.0 / 9007199254740992.0); }
+}  // namespace
+
+int wdem_warm_init(wdem_handle* h, uint64_t seed) {
+  if (!h) return WDEM_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  int rc;
+  if ((rc = mlpEnsure(h))) return rc;
+  // He-uniform weights (fan-in), zero biases
+  std::vector<float> pub(WDEM_WARM_NPARAM, 0.f);
+  unsigned long long st = seed;
+  const int fin[4] = {13, 64, 64, 64}, fout[4] = {64, 64, 64, 4};
+  size_t q = 0;
+  for (int l = 0; l < 4; l++) {
+    const double lim = std::sqrt(6.0 / fin[l]);
+    for (int k = 0; k < fin[l] * fout[l]; k++) pub[q++] = (float)((2 * uniform01(st) - 1) * lim);
+    q += fout[l];
+  }
+  std::vector<float> pad(mlp_npad());
+  mlp_unpack(pub.data(), pad.data());
+  return mlpUpload(h, pad);
+}
+
+int wdem_warm_set_weights(wdem_handle* h, const float* w, int64_t n) {
+  if (!h || !w || n != WDEM_WARM_NPARAM) return WDEM_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  int rc;
+  if ((rc = mlpEnsure(h))) return rc;
+  std::vector<float> pad(mlp_npad());
+  mlp_unpack(w, pad.data());
+  return mlpUpload(h, pad);
+}
+
+int wdem_warm_get_weights(wdem_handle* h, float* w, int64_t n) {
+  if (!h || !w || n != WDEM_WARM_NPARAM) return WDEM_ERR_ARG;
+  if (!h->mlpReady) return fail(h, WDEM_ERR_STATE, "no warm-start network");
+  std::vector<float> pad(mlp_npad());
+  CK(cudaMemcpyAsync(pad.data(), h->mlpW, pad.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  mlp_pack(pad.data(), w);
+  return WDEM_OK;
+}
+
+int wdem_warm_predict(wdem_handle* h, const float* x, int64_t n, float* y) {
+  if (!h || (n > 0 && (!x || !y)) || n < 0) return WDEM_ERR_ARG;
+  if (!h->mlpReady) return fail(h, WDEM_ERR_STATE, "no warm-start network");
+  if (n == 0) return WDEM_OK;
+  CK(cudaSetDevice(h->device));
+  float *dx = nullptr, *dy = nullptr;
+  CK(dalloc(dx, (size_t)n * WDEM_WARM_INPUTS));
+  if (dalloc(dy, (size_t)n * WDEM_WARM_OUTPUTS) != cudaSuccess) { cudaFree(dx); return fail(h, WDEM_ERR_CUDA, "out of memory"); }
+  cudaMemcpyAsync(dx, x, (size_t)n * WDEM_WARM_INPUTS * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+  mlp_launch_predict(h->stream, dx, n, dy, h->mlpWbf, h->mlpW);
+  cudaMemcpyAsync(y, dy, (size_t)n * WDEM_WARM_OUTPUTS * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(dx); cudaFree(dy);
+  if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
+  return WDEM_OK;
+}
+
+int wdem_warm_grad(wdem_handle* h, const float* records, int64_t n, float* grad, float* loss) {
+  if (!h || !records || !grad || !loss || n <= 0) return WDEM_ERR_ARG;
+  if (!h->mlpReady) return fail(h, WDEM_ERR_STATE, "no warm-start network");
+  CK(cudaSetDevice(h->device));
+  float* dr = nullptr;
+  CK(dalloc(dr, (size_t)n * WDEM_WARM_RECORD));
+  cudaMemcpyAsync(dr, records, (size_t)n * WDEM_WARM_RECORD * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+  cudaMemsetAsync(h->mlpGrad, 0, mlp_npad() * sizeof(float), h->stream);
+  cudaMemsetAsync(h->mlpLoss, 0, sizeof(float), h->stream);
+  mlp_launch_grad(h->stream, dr, nullptr, n, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss);
+  std::vector<float> pad(mlp_npad());
+  cudaMemcpyAsync(pad.data(), h->mlpGrad, pad.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(loss, h->mlpLoss, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemsetAsync(h->mlpGrad, 0, mlp_npad() * sizeof(float), h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  cudaFree(dr);
+  if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
+  mlp_pack(pad.data(), grad);
+  return WDEM_OK;
+}
+
+int wdem_warm_train(wdem_handle* h, const float* records, int64_t n, int32_t epochs, int32_t batch, float lr,
+                    uint64_t seed, float* lossPerEpoch) {
+  if (!h || !records || n <= 0 || epochs < 0 || batch <= 0 || !(lr > 0)) return WDEM_ERR_ARG;
+  if (n > (int64_t)INT32_MAX) return fail(h, WDEM_ERR_ARG, "too many training records");
+  CK(cudaSetDevice(h->device));
+  int rc;
+  if (!h->mlpReady && (rc = wdem_warm_init(h, seed))) return rc;
+  cudaStream_t s = h->stream;
+  float* dr = nullptr;
+  int* didx = nullptr;
+  CK(dalloc(dr, (size_t)n * WDEM_WARM_RECORD));
+  if (dalloc(didx, (size_t)n) != cudaSuccess) { cudaFree(dr); return fail(h, WDEM_ERR_CUDA, "out of memory"); }
+  cudaMemcpyAsync(dr, records, (size_t)n * WDEM_WARM_RECORD * sizeof(float), cudaMemcpyHostToDevice, s);
+  std::vector<int> perm(n);
+  unsigned long long st = seed ^ 0x5DEECE66Dull;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const long long totalSteps = (long long)epochs * ((n + batch - 1) / batch);
+  long long step = 0;
+  cudaError_t e = cudaSuccess;
+  for (int ep = 0; ep < epochs && e == cudaSuccess; ep++) {
+    for (int64_t k = 0; k < n; k++) perm[k] = (int)k;
+    for (int64_t k = n - 1; k > 0; k--) std::swap(perm[k], perm[(int64_t)(splitmix64(st) % (unsigned long long)(k + 1))]);
+    cudaMemcpyAsync(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(h->mlpLoss, 0, sizeof(float), s);
+    long long nb = 0;
+    for (int64_t b0 = 0; b0 < n; b0 += batch, nb++, step++) {
+      const long long m = std::min<long long>(batch, n - b0);
+      mlp_launch_grad(s, dr, didx + b0, m, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss);
+      h->mlpT++;
+      const float c1 = 1.f - std::pow(b1, (float)h->mlpT), c2 = 1.f - std::pow(b2, (float)h->mlpT);
+      // half-cosine decay from lr to lr/100 over all steps of this call
+      const double frac = totalSteps > 1 ? (double)step / (double)(totalSteps - 1) : 0.0;
+      const float lrt = (float)(lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+      mlp_launch_adam(s, h->mlpW, h->mlpM, h->mlpV, h->mlpGrad, h->mlpWbf, lrt, b1, b2, c1, c2, eps);
+    }
+    float l = 0;
+    cudaMemcpyAsync(&l, h->mlpLoss, sizeof(float), cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    if (lossPerEpoch) lossPerEpoch[ep] = l / (float)nb;
+  }
+  cudaFree(dr); cudaFree(didx);
+  if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
+  return WDEM_OK;
+}
+
+int wdem_ell_log(wdem_handle* h, int64_t capRecords) {
+  if (!h || capRecords < 0) return WDEM_ERR_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  cudaFree(h->ellLog); cudaFree(h->ellLogCount);
+  h->ellLog = nullptr; h->ellLogCount = nullptr; h->ellLogCap = 0;
+  if (capRecords > 0) {
+    CK(dalloc(h->ellLog, (size_t)capRecords * WDEM_WARM_RECORD));
+    CK(dalloc(h->ellLogCount, 1));
+    CK(cudaMemsetAsync(h->ellLogCount, 0, sizeof(unsigned long long), h->stream));
+    h->ellLogCap = capRecords;
+  }
+  fillStepParams(h);
+  return WDEM_OK;
+}
+
+int wdem_ell_log_read(wdem_handle* h, float* out, int64_t cap, int64_t* n) {
+  if (!h || !n || cap < 0 || (cap > 0 && !out)) return WDEM_ERR_ARG;
+  *n = 0;
+  if (!h->ellLog) return WDEM_OK;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, h->ellLogCount, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  long long m = std::min<long long>((long long)cnt, h->ellLogCap);
+  m = std::min<long long>(m, cap);
+  if (m > 0) {
+    CK(cudaMemcpyAsync(out, h->ellLog, (size_t)m * WDEM_WARM_RECORD * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  *n = m;
   return WDEM_OK;
 }
 

@@ -130,7 +130,7 @@ __device__ __forceinline__ bool brentMax(const s33& Ai, const s33& Bi, d3 R, dou
 // of S' (S' decreasing).  S' = (1-2l) h + l(1-l) h', S'' = -2h + 2(1-2l) h' + l(1-l) h'' with
 // h = R^T x, h' = -x^T D x, h'' = 2 (D x)^T G^-1 D x, x = G^-1 R, D = B^-1 - A^-1.
 __device__ __forceinline__ double newtonStep(const s33& Ai, const s33& Bi, const s33& D, d3 R, double l, double& lo,
-                                             double& hi) {
+                                             double& hi, double tol, bool& conv) {
   const s33 Gi = symInv(symMix(Ai, Bi, l));
   const d3 x = symMul(Gi, R);
   const d3 Dx = symMul(D, x);
@@ -140,23 +140,31 @@ __device__ __forceinline__ double newtonStep(const s33& Ai, const s33& Bi, const
   const double S1 = s * h + w * h1;
   const double S2 = -2 * h + 2 * s * h1 + w * h2;
   if (S1 > 0) lo = l; else hi = l;
-  double ln = l - S1 / S2;
-  if (!(ln > lo && ln < hi)) ln = 0.5 * (lo + hi);  // outside the bracket (or NaN): bisect
+  const double dl = -S1 / S2;
+  // converged: the Newton correction itself is below the tolerance (it may sit on a bracket end)
+  if (fabs(dl) <= tol) { conv = true; return l + dl; }
+  double ln = l + dl;
+  if (!(ln >= lo && ln <= hi)) ln = 0.5 * (lo + hi);  // outside the bracket (or NaN): bisect
   return ln;
 }
 
 // Newton-Raphson maximiser of S from l0; returns the number of iterations, or -1 when it did not converge
-// within maxIter.
+// within maxIter.  Converged when the correction |dl| <= tol, or when the error left after applying the
+// correction, estimated from quadratic convergence as K dl^2 with K = |dl_k| / dl_{k-1}^2, is <= tol
+// (only once the corrections shrink and |dl| < 1e-3, i.e. inside the quadratic regime).
 __device__ __forceinline__ int newtonMax(const s33& Ai, const s33& Bi, d3 R, double l0, double tol, int maxIter,
                                          double& L) {
   s33 D;
   D.a = Bi.a - Ai.a; D.b = Bi.b - Ai.b; D.c = Bi.c - Ai.c; D.d = Bi.d - Ai.d; D.e = Bi.e - Ai.e; D.f = Bi.f - Ai.f;
-  double lo = 0., hi = 1., l = l0;
+  double lo = 0., hi = 1., l = l0, prev = 0.;
   for (int it = 1; it <= maxIter; it++) {
-    const double ln = newtonStep(Ai, Bi, D, R, l, lo, hi);
-    const double dl = ln - l;
+    bool conv = false;
+    const double ln = newtonStep(Ai, Bi, D, R, l, lo, hi, tol, conv);
+    if (conv) { L = ln; return it; }
+    const double dl = fabs(ln - l);
+    if (prev > 0. && dl < 1e-3 && dl <= prev && (dl / (prev * prev)) * (dl * dl) <= tol) { L = ln; return it; }
+    prev = dl;
     l = ln;
-    if (fabs(dl) <= tol) { L = l; return it; }
   }
   L = l;
   return -1;

@@ -194,6 +194,18 @@ void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* s
                   int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st);
 void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int4* out, long long base,
                            long long cap);
+// k_mlp.cu: learned warm start of the ellipsoid solve
+int mlp_npad();
+void mlp_unpack(const float* pub, float* pad);
+void mlp_pack(const float* pad, float* pub);
+cudaError_t mlp_prepare_kernels();
+void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf);
+void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const uint16_t* wbf, const float* wf);
+void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf);
+void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
+                     float* grad, float* loss);
+void mlp_launch_adam(cudaStream_t s, float* w, float* m, float* v, float* grad, uint16_t* wbf, float lr, float b1,
+                     float b2, float c1, float c2, float eps);
 // k_noalloc.cu: the stress sum with its scratch in a fixed device array (no allocation)
 long long stress_noalloc_max_contacts();
 cudaError_t noalloc_scratch(int device, void** addr);
