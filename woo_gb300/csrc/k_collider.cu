@@ -98,6 +98,7 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
   p.bbmin[i] = mn;
   p.bbmax[i] = mx;
   p.lastPos[i] = make_double4_32a(pr.x, pr.y, pr.z, 0);
+  if (p.lastPosf) p.lastPosf[i] = make_float4(truncF(pr.x), truncF(pr.y), truncF(pr.z), 0.f);
 }
 
 void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n) {

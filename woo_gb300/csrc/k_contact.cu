@@ -209,64 +209,20 @@ __device__ __forceinline__ bool wallEllGeometry(const Particles& p, int a, int b
   return true;
 }
 
+// One contact of the work list: geometry, physics and law (ContactLoop.cpp:134-197).  PENDING
+// contacts have been resolved and potential pairs that cannot touch culled by k_contacts_cull.
 template <int LAW, int CP2, bool PERI, bool ELL>
-__global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) return;
+__device__ __forceinline__ void contactBody(const StepParams& P, const Particles& p, const Contacts& c, long long i,
+                                            DeviceStatus* st) {
   const uint8_t s0 = c.state[i];
   const uint8_t sb = s0 & CS_SHAPES;
-  uint8_t s = s0 & CS_MASK;
-  if (s == CS_DEAD) return;
-  // no Cg2 functor for Wall+Wall: the pair stays a potential contact (ContactLoop.cpp:149-150)
-  if (sb == (CS_WALL_A | CS_WALL_B)) return;
+  const uint8_t s = s0 & CS_MASK;
   const int2 id = c.ids[i];
   const int a = id.x, b = id.y;
-  if (s == CS_PENDING) {
-    // removePending of this step's collider (no rebuild happened; a rebuild clears PENDING):
-    // drop the broken contact when the boxes of the last rebuild do not overlap.
-    bool ov;
-    if (PERI) {
-      int4 per;
-      bool amb = false;
-      ov = overlapPeri(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b], P.csize, per, amb);
-      if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = a; return; }
-    } else
-      ov = overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b]);
-    if (!ov) { c.state[i] = CS_DEAD | sb; return; }
-    s = CS_POTENTIAL;
-    c.state[i] = s | sb;
-  }
   const bool real = (s == CS_REAL);
   // periodic: pB is taken at its image hSize*cellDist (ContactLoop.cpp:156, Cell::intrShiftPos)
   int4 cd = make_int4(0, 0, 0, 0);
   if (PERI) cd = c.cdist[i];
-  if (!real && !(sb & CS_WALL_A)) {
-    // Conservative FP32 cull of sphere pairs that cannot touch.  The FP32 copies carry a relative
-    // error <= 2^-24 per coordinate and radius; the margin below (1e-5 relative on the contact
-    // distance plus 1e-6 x the sum of |coordinates|) exceeds the accumulated FP32 error, so every
-    // pair rejected here also fails the exact FP64 test of Cg2_Sphere_Sphere_L6Geom.  Pairs close to
-    // touching, NaN and overflow fall through to the FP64 test.
-    const float4 fa = p.posf[a];
-    float4 fb = p.posf[b];
-    float Sh = 0.f;
-    if (PERI) {
-      // FP32 image shift; its rounding is bounded by 2^-23 x sum |h_ij cellDist_j|, added to the margin
-      const float c0 = (float)cd.x, c1 = (float)cd.y, c2 = (float)cd.z;
-      const float h[9] = {(float)P.hS[0], (float)P.hS[1], (float)P.hS[2], (float)P.hS[3], (float)P.hS[4],
-                          (float)P.hS[5], (float)P.hS[6], (float)P.hS[7], (float)P.hS[8]};
-      fb.x += h[0] * c0 + h[1] * c1 + h[2] * c2;
-      fb.y += h[3] * c0 + h[4] * c1 + h[5] * c2;
-      fb.z += h[6] * c0 + h[7] * c1 + h[8] * c2;
-      for (int q = 0; q < 9; q++) Sh += fabsf(h[q]) * fabsf(q % 3 == 0 ? c0 : (q % 3 == 1 ? c1 : c2));
-    }
-    const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
-    // ellipsoid pairs: bounding spheres (posf.w = largest semi-axis); outside them F_ab > 1
-    const float df = (ELL && (sb & CS_ELL)) ? 1.f : (float)fabs(P.distFactor);
-    const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
-    if (d2 > R * R) return;
-  }
   const double4_32a A4 = p.posr[a], B4 = p.posr[b];
   const d3 pos1 = xyz(A4);
   d3 shift2 = mk(0, 0, 0);
@@ -493,6 +449,7 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
   }
   // persistent history
   c.state[i] = CS_REAL | sb;
+  if (p.touched) { p.touched[a] = 1; p.touched[b] = 1; }
   c.hist[HIST_T0X][i] = cur0.x; c.hist[HIST_T0Y][i] = cur0.y; c.hist[HIST_T0Z][i] = cur0.z;
   c.hist[HIST_T1X][i] = cur1.x; c.hist[HIST_T1Y][i] = cur1.y; c.hist[HIST_T1Z][i] = cur1.z;
   c.hist[HIST_CX][i] = contPt.x; c.hist[HIST_CY][i] = contPt.y; c.hist[HIST_CZ][i] = contPt.z;
@@ -523,21 +480,119 @@ __global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Con
   c.out[OUT_TBX][i] = TB.x; c.out[OUT_TBY][i] = TB.y; c.out[OUT_TBZ][i] = TB.z;
 }
 
+template <int LAW, int CP2, bool PERI, bool ELL>
+__global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
+                                                  const unsigned* count, DeviceStatus* st) {
+  const unsigned m = *count;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
+    contactBody<LAW, CP2, PERI, ELL>(P, p, c, (long long)work[k], st);
+}
+
+// First pass over all contacts: resolves PENDING contacts (removePending of the collider: the broken
+// contact dies when the boxes of the last rebuild no longer overlap, else it is potential again), skips
+// dead pairs and wall+wall pairs (no Cg2 functor, ContactLoop.cpp:149-150), and culls potential pairs that
+// cannot touch with FP32 tests whose margins exceed their rounding (the exact FP64 test would reject
+// them too).  Survivors (real contacts and potential pairs near touching) are appended to the work list;
+// the list order is irrelevant because each contact is processed independently.
+template <bool PERI, bool ELL>
+__global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
+                                                       unsigned* work, unsigned* count, DeviceStatus* st) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < nc) {
+    const uint8_t s0 = c.state[i];
+    const uint8_t sb = s0 & CS_SHAPES;
+    uint8_t s = s0 & CS_MASK;
+    if (s != CS_DEAD && sb != (CS_WALL_A | CS_WALL_B)) {
+      const int2 id = c.ids[i];
+      const int a = id.x, b = id.y;
+      bool alive = true;
+      if (s == CS_PENDING) {
+        bool ov;
+        if (PERI) {
+          int4 per;
+          bool amb = false;
+          ov = overlapPeri(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b], P.csize, per, amb);
+          if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = a; ov = true; alive = false; }
+        } else
+          ov = overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b]);
+        if (!ov) { c.state[i] = CS_DEAD | sb; alive = false; }
+        else if (alive) { s = CS_POTENTIAL; c.state[i] = s | sb; }
+      }
+      if (alive) {
+        if (s == CS_REAL) need = true;
+        else if (!(sb & CS_WALL_A)) {
+          // Sphere/ellipsoid pairs: the FP32 copies carry a relative error below 2^-23 per coordinate and
+          // radius; the margin (1e-5 relative on the contact distance plus 1e-6 x the sum of |coordinates|)
+          // exceeds the accumulated FP32 error, so a pair rejected here fails the exact FP64 test of
+          // Cg2_Sphere_Sphere_L6Geom (ellipsoids: it lies outside the bounding spheres, F_ab > 1).
+          // Pairs close to touching, NaN and overflow fall through to the FP64 test.
+          const float4 fa = p.posf[a];
+          float4 fb = p.posf[b];
+          float Sh = 0.f;
+          if (PERI) {
+            // FP32 image shift; its rounding is bounded by 2^-23 x sum |h_ij cellDist_j|, added to the margin
+            const int4 cd = c.cdist[i];
+            const float c0 = (float)cd.x, c1 = (float)cd.y, c2 = (float)cd.z;
+            const float h[9] = {(float)P.hS[0], (float)P.hS[1], (float)P.hS[2], (float)P.hS[3], (float)P.hS[4],
+                                (float)P.hS[5], (float)P.hS[6], (float)P.hS[7], (float)P.hS[8]};
+            fb.x += h[0] * c0 + h[1] * c1 + h[2] * c2;
+            fb.y += h[3] * c0 + h[4] * c1 + h[5] * c2;
+            fb.z += h[6] * c0 + h[7] * c1 + h[8] * c2;
+            for (int q = 0; q < 9; q++) Sh += fabsf(h[q]) * fabsf(q % 3 == 0 ? c0 : (q % 3 == 1 ? c1 : c2));
+          }
+          const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
+          const float d2 = dx * dx + dy * dy + dz * dz;
+          const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
+          const float df = (ELL && (sb & CS_ELL)) ? 1.f : (float)fabs(P.distFactor);
+          const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
+          need = !(d2 > R * R);
+        } else {
+          // wall + sphere/ellipsoid: the distance along the wall axis against the radius (ellipsoids: the
+          // largest semi-axis, an upper bound of the extent), with the same kind of margin
+          const int ax = (p.meta[a].x >> 4) & 3;
+          const float4 fa = p.posf[a], fb = p.posf[b];
+          const float ca = ax == 0 ? fa.x : (ax == 1 ? fa.y : fa.z), cb = ax == 0 ? fb.x : (ax == 1 ? fb.y : fb.z);
+          const float dist = fabsf(cb - ca);
+          need = !(dist > fb.w * 1.00001f + 1e-6f * (fabsf(ca) + fabsf(cb)));
+        }
+      }
+    }
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, need);
+  if (ballot) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) work[base + __popc(ballot & ((1u << lane) - 1))] = (unsigned)i;
+  }
+}
+
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
   if (nc <= 0) return;
-  unsigned blocks = (unsigned)((nc + 127) / 128);
+  unsigned* count = &st->workCount;
+  cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+  const unsigned cb = (unsigned)((nc + 255) / 256);
+  const long long hb0 = (nc + 127) / 128;
+  const unsigned hb = (unsigned)(hb0 < 152 * 16 ? hb0 : 152 * 16);
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
-    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    (k_contacts_cull<false, true><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
   } else if (P.periodic) {
+    (k_contacts_cull<true, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
     if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
     else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
-  } else if (P.law == WDEM_LAW_IDEALELPL) {
-    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
   } else {
-    (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<blocks, 128, 0, s>>>(P, p, c, nc, st), ++::wdem::g_kernel_launches);
+    (k_contacts_cull<false, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    if (P.law == WDEM_LAW_IDEALELPL)
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+    else
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
   }
 }
 

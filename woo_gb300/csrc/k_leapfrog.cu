@@ -307,10 +307,188 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   }
 }
 
+// The same step as k_leapfrog<false, false, false> without energy tracking, issuing fewer FP64
+// operations with bit-identical results:
+//  - the CSR gather runs only for particles that a real contact touched in the last contact pass
+//    (p.touched, set by the contact kernel, cleared here); the others get m g;
+//  - Sign(F (v + dt/2 a)) of the damping comes from the sign bits (signProd) and the factor
+//    1 - damping Sign(...) from two constants; zero accelerations and velocities skip their updates
+//    (addScaled: adding a zero changes only -0);
+//  - the verlet trigger is decided in FP32 with an error margin from the FP32 shadows of the new and
+//    the last-rebuild positions, and in FP64 only when the margin does not decide it;
+//  - an orientation that does not rotate and that the last normalisation left unchanged (meta bit
+//    META_ORI_FIXED) is neither normalised again nor rewritten;
+//  - the FP32 shadow is written by mantissa truncation on the integer pipe.
+__global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
+                                                        DeviceStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 meta = p.meta[i];
+  const unsigned flags = (unsigned)meta.w;
+  const double4_32a vm = p.velm[i];
+  const double mass = vm.w;
+  const bool blockedAll = (flags & 63u) == 63u;
+  const bool blockedNone = (flags & 63u) == 0u;
+  d3 F, T;
+  if (!blockedAll) {
+    const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
+    if (grav) {
+      const bool mf = finiteBits(mass);
+      F.x = (zeroBits(P.gravity[0]) && mf) ? signedZero(mass, P.gravity[0]) : mass * P.gravity[0];
+      F.y = (zeroBits(P.gravity[1]) && mf) ? signedZero(mass, P.gravity[1]) : mass * P.gravity[1];
+      F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
+    } else F = mk(0, 0, 0);
+    T = mk(0, 0, 0);
+    if (p.touched[i]) {
+      p.touched[i] = 0;
+      const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
+      for (int e = e0; e < e1; e++) {
+        const unsigned en = csr.ent[e];
+        const unsigned ci = en & 0x7fffffffu;
+        if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
+        const d3 f = mk(c.out[OUT_FX][ci], c.out[OUT_FY][ci], c.out[OUT_FZ][ci]);
+        if (en >> 31) {
+          F = F + f * -1.0;
+          T = T + mk(c.out[OUT_TBX][ci], c.out[OUT_TBY][ci], c.out[OUT_TBZ][ci]);
+        } else {
+          F = F + f;
+          T = T + mk(c.out[OUT_TAX][ci], c.out[OUT_TAY][ci], c.out[OUT_TAZ][ci]);
+        }
+      }
+    }
+  } else {
+    F = mk(0, 0, 0); T = mk(0, 0, 0);
+  }
+  const double dt = P.dt;
+  const double damping = P.damping;
+  const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
+  d3 vel = xyz(vm);
+  const double4_32a w4 = p.angw[i];
+  d3 angVel = xyz(w4);
+  bool angChanged = false;
+  const double4_32a pr = p.posr[i];
+  d3 pos = xyz(pr);
+  if (!blockedAll) {
+    d3 lin;
+    if (blockedNone) lin = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
+    else {
+      lin = mk(0, 0, 0);
+      if (!(flags & 1u)) lin.x = lin.x + qdiv(F.x, mass);
+      if (!(flags & 2u)) lin.y = lin.y + qdiv(F.y, mass);
+      if (!(flags & 4u)) lin.z = lin.z + qdiv(F.z, mass);
+    }
+    if (damp) {
+      // nonviscDamp2nd: a *= 1 - damping Sign(F (v + dt/2 a)); a zero F gives Sign 0 and factor 1
+      const double hd = 0.5 * dt;
+      if (!zeroBits(F.x)) { const int sg = signProd(F.x, vel.x + hd * lin.x); if (sg) lin.x = lin.x * (sg > 0 ? P.dampM : P.dampP); }
+      if (!zeroBits(F.y)) { const int sg = signProd(F.y, vel.y + hd * lin.y); if (sg) lin.y = lin.y * (sg > 0 ? P.dampM : P.dampP); }
+      if (!zeroBits(F.z)) { const int sg = signProd(F.z, vel.z + hd * lin.z); if (sg) lin.z = lin.z * (sg > 0 ? P.dampM : P.dampP); }
+    }
+    vel.x = addScaled(vel.x, dt, lin.x);
+    vel.y = addScaled(vel.y, dt, lin.y);
+    vel.z = addScaled(vel.z, dt, lin.z);
+    if (!isZeroBits(T)) {
+      WDEM_REAL_BRANCH();
+      const d3 inertia = xyz(p.inert[i]);
+      if (!isZeroBits(inertia)) {
+        d3 ang;
+        if (blockedNone) ang = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
+        else {
+          ang = mk(0, 0, 0);
+          if (!(flags & 8u)) ang.x = ang.x + qdiv(T.x, inertia.x);
+          if (!(flags & 16u)) ang.y = ang.y + qdiv(T.y, inertia.y);
+          if (!(flags & 32u)) ang.z = ang.z + qdiv(T.z, inertia.z);
+        }
+        if (damp) {
+          const double hd = 0.5 * dt;
+          if (!zeroBits(T.x)) { const int sg = signProd(T.x, angVel.x + hd * ang.x); if (sg) ang.x = ang.x * (sg > 0 ? P.dampM : P.dampP); }
+          if (!zeroBits(T.y)) { const int sg = signProd(T.y, angVel.y + hd * ang.y); if (sg) ang.y = ang.y * (sg > 0 ? P.dampM : P.dampP); }
+          if (!zeroBits(T.z)) { const int sg = signProd(T.z, angVel.z + hd * ang.z); if (sg) ang.z = ang.z * (sg > 0 ? P.dampM : P.dampP); }
+        }
+        angVel.x = addScaled(angVel.x, dt, ang.x);
+        angVel.y = addScaled(angVel.y, dt, ang.y);
+        angVel.z = addScaled(angVel.z, dt, ang.z);
+        angChanged = true;
+      }
+    } else {
+      // a zero torque still divides by the inertia and adds to angVel: that changes angVel only when an
+      // inertia component is not positive (0/0, 0/negative) or angVel holds a -0
+      if (!(meta.x & META_IPOS) || hasNegZero(angVel)) {
+        WDEM_REAL_BRANCH();
+        const d3 inertia = xyz(p.inert[i]);
+        if (!isZeroBits(inertia)) {
+          d3 ang;
+          if (blockedNone) ang = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
+          else {
+            ang = mk(0, 0, 0);
+            if (!(flags & 8u)) ang.x = ang.x + qdiv(T.x, inertia.x);
+            if (!(flags & 16u)) ang.y = ang.y + qdiv(T.y, inertia.y);
+            if (!(flags & 32u)) ang.z = ang.z + qdiv(T.z, inertia.z);
+          }
+          angVel = angVel + dt * ang;
+          angChanged = true;
+        }
+      }
+    }
+  }
+  pos.x = addScaledR(pos.x, vel.x, dt);
+  pos.y = addScaledR(pos.y, vel.y, dt);
+  pos.z = addScaledR(pos.z, vel.z, dt);
+  // leapfrogSphericalRotate; an unrotated, already-normalised orientation is left alone
+  int mx = meta.x;
+  if (!isZeroBits(angVel)) {
+    const double4_32a o4 = p.ori[i];
+    qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+    double angle = sqrt(sqnorm(angVel));
+    d3 axis = angVel / angle;
+    double ha = 0.5 * (angle * dt);
+    double sh, ch;
+    sincos(ha, &sh, &ch);
+    qd q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
+    ori = qnormalized(qmul(q, ori));
+    p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+    mx &= ~META_ORI_FIXED;
+  } else if (!(mx & META_ORI_FIXED)) {
+    const double4_32a o4 = p.ori[i];
+    qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+    const double z2 = ori.x * ori.x + ori.y * ori.y + ori.z * ori.z + ori.w * ori.w;
+    if (isOneBits(z2)) mx |= META_ORI_FIXED;  // normalisation is the identity from now on
+    else {
+      ori = qnormalized(ori);
+      p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+    }
+  }
+  if (mx != meta.x) reinterpret_cast<int*>(&p.meta[i])[0] = mx;
+  p.posr[i] = make_double4_32a(pos.x, pos.y, pos.z, pr.w);
+  const float4 pf = make_float4(truncF(pos.x), truncF(pos.y), truncF(pos.z), truncF(pr.w));
+  p.posf[i] = pf;
+  p.velm[i] = make_double4_32a(vel.x, vel.y, vel.z, mass);
+  if (angChanged) p.angw[i] = make_double4_32a(angVel.x, angVel.y, angVel.z, w4.w);
+  if (!finiteBits(pos.x) || !finiteBits(pos.y) || !finiteBits(pos.z)) {
+    if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = i;
+  }
+  // aabbIsDirty (moved^2 > verletDist^2): FP32 distance of the shadows with a bound on its error
+  // (truncation < 2^-23 relative per coordinate, FP32 arithmetic a few 2^-24 of the distance)
+  const float4 lf = p.lastPosf[i];
+  const float dx = pf.x - lf.x, dy = pf.y - lf.y, dz = pf.z - lf.z;
+  const float df = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float S = fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(lf.x) + fabsf(lf.y) + fabsf(lf.z);
+  const float err = 2.5e-7f * S + 1e-6f * df;
+  if (!(df + err < P.verletLoF)) {
+    const double4_32a lp = p.lastPos[i];
+    const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
+    if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+  }
+}
+
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays, Contacts c, Csr csr,
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
+  if (!fromArrays && !P.hasEll && !P.periodic && !P.lfEnergy && p.touched) {
+    (k_leapfrog_fast<<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    return;
+  }
   if (P.hasEll) {
     if (fromArrays) (k_leapfrog<true, false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     else (k_leapfrog<false, false, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
@@ -355,7 +533,10 @@ __global__ void k_state_in(Particles p, int n, const double* pos, const double* 
   }
   if (vel) { double4_32a v = p.velm[i]; v.x = vel[3 * i]; v.y = vel[3 * i + 1]; v.z = vel[3 * i + 2]; p.velm[i] = v; }
   if (angVel) { double4_32a v = p.angw[i]; v.x = angVel[3 * i]; v.y = angVel[3 * i + 1]; v.z = angVel[3 * i + 2]; p.angw[i] = v; }
-  if (ori) p.ori[i] = make_double4_32a(ori[4 * i], ori[4 * i + 1], ori[4 * i + 2], ori[4 * i + 3]);
+  if (ori) {
+    p.ori[i] = make_double4_32a(ori[4 * i], ori[4 * i + 1], ori[4 * i + 2], ori[4 * i + 3]);
+    reinterpret_cast<int*>(&p.meta[i])[0] &= ~META_ORI_FIXED;
+  }
 }
 __global__ void k_state_out(Particles p, int n, double* pos, double* vel, double* angVel, double* ori) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -225,6 +225,7 @@ void freeContacts(ContactBuf& b) {
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   cudaFree(c.cdist);
+  cudaFree(c.work);
   cudaFree(c.lam);
   cudaFree(c.lam0);
   memset(&c, 0, sizeof(c));
@@ -245,6 +246,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   for (int k = 0; k < OUT_COUNT; k++) if ((e = dalloc(c.out[k], cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
+  if ((e = dalloc(c.work, cap))) return e;
   if (peri && (e = dalloc(c.cdist, cap))) return e;
   if (ell && ((e = dalloc(c.lam, cap)) || (e = dalloc(c.lam0, cap)))) return e;
   b.cap = cap;
@@ -445,6 +447,9 @@ void fillStepParams(wdem_handle* h) {
   P.damping = r.damping;
   P.verletDist = h->verletDistResolved;
   P.maxD2 = h->verletDistResolved * h->verletDistResolved;
+  P.verletLoF = (float)(h->verletDistResolved * (1 - 1e-6));
+  P.dampM = 1.0 - r.damping * 1.0;
+  P.dampP = 1.0 - r.damping * -1.0;
   P.noRatch = r.noRatch; P.iniLensTouch = r.iniLensTouch; P.trsfRenorm = r.trsfRenorm; P.approxMask = r.approxMask;
   P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
   P.cp2 = r.cp2; P.law = r.law;
@@ -536,6 +541,8 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.torque, N) == cudaSuccess;
   ok &= dalloc(d.meta, N) == cudaSuccess;
   ok &= dalloc(d.posf, N) == cudaSuccess;
+  ok &= dalloc(d.lastPosf, N) == cudaSuccess;
+  ok &= dalloc(d.touched, N) == cudaSuccess;
   for (int k = 0; k < 3; k++) ok &= dalloc(d.energy[k], N) == cudaSuccess;
   ok &= dalloc(h->dEnergy, WDEM_E_COUNT) == cudaSuccess;
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
@@ -574,7 +581,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
-  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
   cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
@@ -693,7 +700,10 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     ori[i] = make_double4_32a(p->ori[4 * i], p->ori[4 * i + 1], p->ori[4 * i + 2], p->ori[4 * i + 3]);
     force[i] = make_double4_32a(p->force[3 * i], p->force[3 * i + 1], p->force[3 * i + 2], 0);
     torque[i] = make_double4_32a(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2], 0);
-    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0), p->material[i], (int)p->mask[i], (int)fl);
+    auto posInert = [](double x) { return x > 0; };
+    const bool ipos = posInert(in[0]) && posInert(in[1]) && posInert(in[2]);
+    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0) | (ipos ? META_IPOS : 0),
+                        p->material[i], (int)p->mask[i], (int)fl);
     if (sh != WDEM_SHAPE_WALL) h->smallIds.push_back(i); else h->largeIds.push_back(i);
   }
   h->semi = semi;
@@ -734,6 +744,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   h->cs.nLarge = (int)h->largeIds.size();
   launch_refresh_posf(s, h->d, n);
+  if (n > 0) CK(cudaMemsetAsync(h->d.touched, 0, n, s));
   CK(cudaStreamSynchronize(s));
   h->nContacts = 0;
   h->forcesInArrays = true;

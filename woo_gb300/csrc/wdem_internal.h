@@ -36,7 +36,9 @@ extern long long g_kernel_launches;
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
 enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_ELL_B = 32, CS_ELL = 48, CS_SHAPES = 60 };
 // meta.x: shape (bits 0-3), wall axis (4-5), wall sense + 1 (8-9), aspherical Leapfrog (bit 12)
-enum { META_ASPH = 1 << 12 };
+// META_ORI_FIXED: the orientation is not rotating and normalising it is the identity (set and cleared by the
+// integrator); META_IPOS: all inertia components are positive (set at upload)
+enum { META_ASPH = 1 << 12, META_ORI_FIXED = 1 << 13, META_IPOS = 1 << 14 };
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
@@ -62,6 +64,8 @@ struct StepParams {
   double damping;
   double verletDist;        // resolved, >= 0
   double maxD2;             // verletDist^2
+  float verletLoF;          // FP32 lower bound of verletDist (FP32 verlet trigger)
+  double dampM, dampP;      // 1 - damping * 1 and 1 - damping * (-1), the nonviscDamp2nd factors
   int noRatch, iniLensTouch, trsfRenorm, approxMask;
   int updatePhysNow;        // Cp2 runs on existing contacts this step (updatePhys always/once)
   int cp2, law;
@@ -102,6 +106,8 @@ struct Particles {
   // (NaN = not initialised), Aabb.nodeLastOri and Aabb.maxRot (< 0: rotation ignored)
   double4_32a *semi, *angMom, *lastOri;
   double* maxRot;
+  float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
+  uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
   double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
@@ -119,6 +125,7 @@ struct Contacts {
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
   int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
+  unsigned* work;   // indices of the contacts the heavy pass processes this step (capacity = contacts)
   double* lam;      // ellipsoid pairs: maximiser lambda of the last solve (NaN = none); null otherwise
   float* lam0;      // learned warm start of this step's solve (NaN = none); null unless used
 };
@@ -145,7 +152,8 @@ struct DeviceStatus {
   int dirty;          // set by the integrator when a particle left its verlet box
   int overflow;
   unsigned long long pairTotal;
-  unsigned long long ellSolves, ellIters, ellFallbacks;  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
+  unsigned long long ellSolves, ellIters, ellFallbacks;
+  unsigned workCount;  // length of the contact work list of this step  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
 

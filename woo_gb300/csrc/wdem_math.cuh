@@ -139,6 +139,51 @@ __device__ __forceinline__ double dmax3(d3 a) {
 
 __device__ __forceinline__ double signum(double f) { return f < 0 ? -1.0 : (f > 0 ? 1.0 : 0.0); }
 
+__device__ __forceinline__ int expBits(double x) { return (int)((bitsOf(x) >> 52) & 0x7ff); }
+
+// Mathr::Sign(F * u) (-1, 0, +1; 0 for NaN): the sign bits decide unless a factor is zero, not finite,
+// subnormal, or the product could underflow to zero, in which case the product is formed.
+__device__ __forceinline__ int signProd(double F, double u) {
+  if (zeroBits(F) || zeroBits(u)) return 0;
+  const int eF = expBits(F), eu = expBits(u);
+  if (eF != 0 && eF != 0x7ff && eu != 0 && eu != 0x7ff && eF + eu > 1100)
+    return ((bitsOf(F) ^ bitsOf(u)) >> 63) ? -1 : 1;
+  WDEM_REAL_BRANCH();
+  const double pr = F * u;
+  return pr < 0 ? -1 : (pr > 0 ? 1 : 0);
+}
+
+// v + s a for a == +-0 and finite s: s a is a zero of sign(s) ^ sign(a), and adding a zero changes v only
+// from -0 to +0 (round to nearest: -0 + +0 = +0); otherwise the operations are done.
+__device__ __forceinline__ double addScaled(double v, double s, double a) {
+  if (zeroBits(a) && finiteBits(s)) {
+    const bool addendNeg = ((bitsOf(s) ^ bitsOf(a)) >> 63) != 0;
+    return (negZero(v) && !addendNeg) ? 0.0 : v;
+  }
+  WDEM_REAL_BRANCH();
+  return v + s * a;
+}
+// v + a s (operands of the product in this order) for the position update pos + vel dt
+__device__ __forceinline__ double addScaledR(double v, double a, double s) {
+  if (zeroBits(a) && finiteBits(s)) {
+    const bool addendNeg = ((bitsOf(s) ^ bitsOf(a)) >> 63) != 0;
+    return (negZero(v) && !addendNeg) ? 0.0 : v;
+  }
+  WDEM_REAL_BRANCH();
+  return v + a * s;
+}
+
+// double -> float by truncating the mantissa (error below 2^-23 relative) for values in the float normal
+// range, on the integer pipe; zeros keep their sign; other values use the hardware conversion.
+__device__ __forceinline__ float truncF(double x) {
+  const unsigned long long b = bitsOf(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e >= 897 && e <= 1150)
+    return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull) | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffull));
+  if ((b << 1) == 0) return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull));
+  return (float)x;
+}
+
 // x^n by squaring, n small and fixed (pown of Woo's Math.hpp)
 __device__ __forceinline__ double pown3(double x) {
   // n=3: d=1, r=1 -> pown(x*x,1) * x ; pown(y,1): d=0,r=1 -> 1*y
