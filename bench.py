@@ -1,22 +1,34 @@
 """Benchmark of the GB300 DEM timestep (particle-steps/s), one JSON line on rank 0.
 
-Workload (default): hertz1M -- 1,000,000 polydisperse HertzMat spheres (r ~ U[2,6] mm, DMT, en=.8,
-surfEnergy .01, tanPhi .3/.6) as a loose seeded cloud (solid fraction ~0.3) falling into a
-1 x 1 x 2 m walled box, dt = 0.3 x p-wave dt, verletDist 0.1 x rmin, Leapfrog -> collider ->
-ContactLoop every step.  A step is one pass of the hot path over all particles; the timed region
-covers K consecutive steps of one simulation (state larger than L2 stays resident in HBM).
+Workloads (synthetic, seeded; no dataset is involved):
+  hertz1M (default) -- 1,000,000 polydisperse HertzMat spheres (r ~ U[2,6] mm, DMT, en=.8, surfEnergy
+      .01, tanPhi .3/.6) as a loose cloud (solid fraction ~0.3) falling into a 1 x 1 x 2 m walled box,
+      dt = 0.3 x p-wave dt, verletDist 0.1 x rmin.  By default the timed region is the whole 20,000-step
+      job, collider rebuilds included.
+  hertz1M_settled -- the same spheres after settling on the GPU (untimed: 10 g and damping 0.5 until
+      the column has fallen, then 1 g), a few contacts per sphere; then timed with the job's parameters.
+  ell200k -- 200,000 ellipsoids (a ~ U[3,6] mm, b = .7a, c = .5a, random orientations) agitated in a
+      0.6 x 0.6 x 1.2 m walled box under gravity, FrictMat E 1e7 tanPhi .4, dt 0.9 x p-wave dt.  The
+      learned warm start is trained first (untimed) on records logged by the plain Newton solver; the
+      line reports the learned-warm-start run and, under "variants", the reference's Brent solver, the
+      plain cold-start Newton and the previous-step warm start on the same initial state.
+  spheres10k -- 10,000 monodisperse FrictMat spheres r = 5 mm in a 0.5 x 0.5 x 1 m box (CPU-runnable).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--workload hertz1M|spheres10k]
+A step is one pass of the hot path (Leapfrog -> collider -> ContactLoop) over all particles; the timed
+region covers K consecutive steps of one simulation, state resident in HBM (larger than L2).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--workload ...]
 
 --impl reference times the reference algorithm on the host cores (the OpenMP build of the CPU
 restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop), on a bounded cut of the workload.
 Multi-GPU: the path does not shard (contacts couple neighbours); N ranks run N independent replicas.
 """
 import argparse
+import ctypes
 import json
-import re
 import math
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -28,18 +40,31 @@ sys.path.insert(0, ROOT)
 
 import numpy as np
 
+WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "spheres10k"]
+DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "spheres10k": 2000}
+METRIC = "particle-steps/s per GB300"
+DESCR = {"hertz1M": "plain DEM step, HertzDMT settling",
+         "hertz1M_settled": "plain DEM step, HertzDMT, settled packing",
+         "ell200k": "ellipsoid DEM step, learned warm start",
+         "spheres10k": "plain DEM step, FrictMat IdealElPl"}
+
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default: per workload)")
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="hertz1M", choices=["hertz1M", "spheres10k"])
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--workload", default="hertz1M", choices=WORKLOADS)
+    ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--n", type=int, default=None,
+                    help="particle count of a smaller cut of the workload (same density; for profiling runs)")
+    a = ap.parse_args()
+    if a.steps is None:
+        a.steps = DEFAULT_STEPS[a.workload]
+    return a
 
 
 def dist_env():
@@ -109,23 +134,118 @@ class ClockSampler:
 
 
 def build_scene(name, n=None):
-    from woo_gb300 import scenes
+    from woo_gb300 import abi, scenes
     if name == "hertz1M":
         return scenes.hertz1M(n=n or 1_000_000)
+    if name == "hertz1M_settled":
+        return scenes.hertz1M(n=n or 1_000_000, height=0.95)
+    if name == "ell200k":
+        k = n or 200_000
+        sc = (k / 200_000) ** (1.0 / 3.0)
+        return scenes.ellipsoid_cloud(k, 7, box=(0.6 * sc, 0.6 * sc, 1.2 * sc), amin=0.003, amax=0.006, dense=1.0,
+                                      vel_scale=0.5, angvel_scale=5.0, young=1e7, tanPhi=0.4, damping=0.2,
+                                      ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_MLP)
     return scenes.spheres10k(n=n or 10000)
 
 
-def contact_kernel_bytes(cg, shapes, hertz):
-    """Algorithmic bytes of one contact-kernel launch: 80 B per particle touched by a contact
-    (pos 24, vel 24, angVel 24, radius 8), 288 B per real contact (ids 8, history read 112, history
-    write 96, reduction outputs 72), 16 B per potential-only pair (ids 8 + the distance-test data 8);
-    Hertz adds 16 B r/w (kn, kt) + 8 B per real contact."""
+def copy_params(p):
+    from woo_gb300 import abi
+    q = abi.Params()
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(p))
+    return q
+
+
+def settle(h, spec):
+    """Untimed settling on the GPU: gravity x 10 and damping 0.5 for as long as a free fall of half the
+    cloud height takes, then 3000 steps at 1 g with damping 0.5; the parameters are then restored."""
+    p = copy_params(spec.params)
+    dt = spec.params.dt
+    height = spec.info.get("height", 1.0)
+    g = abs(spec.params.gravity[2])
+    fall = int(math.sqrt(2 * 0.5 * height / (10 * g)) / dt)
+    for mult, steps in ((10.0, fall), (1.0, 3000)):
+        p.gravity[2] = spec.params.gravity[2] * mult
+        p.damping = 0.5
+        p.step = h.status().step
+        h.set_params(p)
+        h.step(steps)
+    q = copy_params(spec.params)
+    q.step = h.status().step
+    h.set_params(q)
+    return fall + 3000
+
+
+def contact_kernel_bytes(cg, hertz):
+    """Algorithmic bytes of one contact pass: 80 B per particle touched by a contact (pos 24, vel 24,
+    angVel 24, radius 8), 288 B per real contact (ids 8, history read 112, history write 96, reduction
+    outputs 72), 16 B per potential-only pair (ids 8 + the distance-test data 8); Hertz adds 16 B r/w
+    (kn, kt) + 8 B per real contact."""
     live = cg.n
     real = int(cg.real.sum())
     pot = live - real
     touched = len(np.unique(np.concatenate([cg.idA, cg.idB]))) if live else 0
     per_real = 288 + (24 if hertz else 0)
     return 80 * touched + per_real * real + 16 * pot, dict(real=real, potential=pot, touched=touched)
+
+
+def timed_steps(h, stream, k, world, local, barrier):
+    import torch
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    h.step(k)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def new_handle(spec, local, params=None):
+    from woo_gb300 import abi
+    h = abi.Handle(spec.particles.n, device=local)
+    h.set_params(params or spec.params)
+    h.upload_particles(spec.particles)
+    h.set_params(params or spec.params)
+    return h
+
+
+def ell_variants(args, spec, local, world, barrier, w):
+    """The same initial state under each solver: Brent (the reference's), Newton from the cold start,
+    Newton from the previous step's lambda, Newton from the learned warm start (weights w)."""
+    import torch
+    from woo_gb300 import abi
+    out = {}
+    for name, solver, warm in (("brent", abi.ELL_BRENT, abi.WARM_COLD), ("newton_cold", abi.ELL_NEWTON, abi.WARM_COLD),
+                               ("newton_history", abi.ELL_NEWTON, abi.WARM_HISTORY),
+                               ("newton_mlp", abi.ELL_NEWTON, abi.WARM_MLP)):
+        p = copy_params(spec.params)
+        p.ellSolver, p.warmStart = solver, warm
+        h = new_handle(spec, local, p)
+        if warm == abi.WARM_MLP:
+            h.warm_set_weights(w)
+        stream = torch.cuda.ExternalStream(h.stream(), device=local)
+        h.step(max(args.warmup, 3))
+        s0 = h.status()
+        h.set_timing(True)
+        ms = timed_steps(h, stream, args.steps, world, local, barrier)
+        kt = h.kernel_times()
+        s1 = h.status()
+        h.set_timing(False)
+        solves = s1.ellSolves - s0.ellSolves
+        c_ms, c_n = kt.get("contacts", (0.0, 1))
+        out[name] = {"value": world * spec.particles.n * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                     "contacts_ms_per_step": c_ms / max(c_n, 1), "solves_per_step": solves / args.steps,
+                     "iterations_per_solve": (s1.ellIters - s0.ellIters) / max(solves, 1),
+                     "fallback_fraction": (s1.ellFallbacks - s0.ellFallbacks) / max(solves, 1)}
+        h.close()
+    return out
 
 
 def run_gpu(args, rank, world, local):
@@ -140,13 +260,39 @@ def run_gpu(args, rank, world, local):
             torch.distributed.barrier()
 
     wbuild.build()
-    spec = build_scene(args.workload)
+    spec = build_scene(args.workload, n=args.n)
     n = spec.particles.n
-    h = abi.Handle(n, device=local)
-    h.set_params(spec.params)
-    h.upload_particles(spec.particles)
-    h.set_params(spec.params)
+    extra = {}
+    if args.workload == "ell200k":
+        # train the learned warm start on records of the plain (cold-start) Newton solver, untimed
+        p = copy_params(spec.params)
+        p.warmStart = abi.WARM_COLD
+        hl = new_handle(spec, local, p)
+        cap = 5_000_000
+        hl.ell_log(cap)
+        steps = 0
+        while hl.status().ellSolves < cap and steps < 400:
+            hl.step(20)
+            steps += 20
+        R = hl.ell_log_read(cap)
+        t0 = time.time()
+        losses = hl.warm_train(R, epochs=6, batch=512, lr=3e-3, seed=1)
+        w = hl.warm_get_weights()
+        hl.close()
+        extra["training"] = {"records": int(len(R)), "logged_steps": steps, "epochs": 6, "batch": 512,
+                             "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
+                             "seconds": time.time() - t0}
+        extra["variants"] = ell_variants(args, spec, local, world, barrier, w)
+        v = extra["variants"]
+        extra["warm_start_speedup"] = {
+            "contact_pass_vs_newton_cold": v["newton_cold"]["contacts_ms_per_step"] / v["newton_mlp"]["contacts_ms_per_step"],
+            "iterations_vs_newton_cold": v["newton_cold"]["iterations_per_solve"] / v["newton_mlp"]["iterations_per_solve"]}
+        h = new_handle(spec, local)
+        h.warm_set_weights(w)
+    else:
+        h = new_handle(spec, local)
     stream = torch.cuda.ExternalStream(h.stream(), device=local)
+    settled_steps = settle(h, spec) if args.workload == "hertz1M_settled" else 0
 
     # warm-up (includes the first collider build)
     h.step(max(args.warmup, 3))
@@ -157,39 +303,23 @@ def run_gpu(args, rank, world, local):
     h.set_timing(True)
     clocks = ClockSampler(local)
     clocks.start()
-    barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    h.step(args.steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1)
+    ms_max = timed_steps(h, stream, args.steps, world, local, barrier)
     clk = clocks.stop()
     launches = h.launch_count() - l0
     kt = h.kernel_times()
     st1 = h.status()
     h.set_timing(False)
-
-    # max over ranks
-    t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
     value = world * n * args.steps / (ms_max / 1e3)
 
     # roofline of the dominant kernel: algorithmic bytes per launch (contact counts at the end of the
     # timed region) over the CUDA-event average launch duration inside the timed region
     cg = h.download_contacts()
     hertz = spec.params.cp2 == abi.CP2_HERTZ
-    cbytes, counts = contact_kernel_bytes(cg, spec.particles.shape, hertz)
+    cbytes, counts = contact_kernel_bytes(cg, hertz)
     lbytes = 256 * n + 80 * counts["real"]   # fused CSR reduction + Leapfrog: 300+52-96 B/particle, 80 B/real contact
     fp64_peak = h.fp64_peak()
     rl = {}
-    for kname, label, abytes in (("contacts", "k_contacts (fused Cg2+Cp2+Law2)", cbytes),
+    for kname, label, abytes in (("contacts", "contact pass (k_contacts_cull + k_contacts: Cg2+Cp2+Law2)", cbytes),
                                  ("leapfrog", "k_leapfrog (CSR force gather + Leapfrog + verlet check)", lbytes)):
         k_ms, k_n = kt.get(kname, (0.0, 0))
         avg = k_ms / max(k_n, 1)
@@ -209,42 +339,56 @@ def run_gpu(args, rank, world, local):
                               "frac": (dp_ops / (avg / 1e3) / 1e9 / fp64_peak) if (dp_ops and avg > 0) else None}}
     dominant = max(rl, key=lambda k: rl[k]["ms_avg"])
 
-    # end-to-end through the public C ABI with host buffers: per step, the kinematic state goes in from
-    # pinned host memory (wdem_write_state), one step runs, and the state comes back (wdem_read_state)
-    e2e = None
+    # End to end through the public C ABI with host buffers, as the engine plug-in runs inside Woo's
+    # step loop: the kinematic state goes in from pinned host memory (wdem_write_state), then one
+    # wdem_step call per step (each one returns the step's status word to the host: error code and
+    # collider trigger), then the state comes back to pinned host memory (wdem_read_state).
+    e2e, roundtrip = None, None
     ne = min(args.e2e_steps, args.steps)
     if ne > 0:
-        pin = {k: torch.empty((n, w), dtype=torch.float64, pin_memory=True) for k, w in
+        pin = {k: torch.empty((n, w_), dtype=torch.float64, pin_memory=True) for k, w_ in
                (("pos", 3), ("vel", 3), ("angVel", 3), ("ori", 4))}
-        h.read_state(n, pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
+        ptrs = (pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
+        h.read_state(n, *ptrs)
+        bytes_io = n * (3 + 3 + 3 + 4) * 8
+        status_bytes = 128
         barrier()
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        t0 = time.perf_counter()
+        h.write_state(n, *ptrs)
         for _ in range(ne):
-            h.write_state(n, pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
             h.step(1)
-            h.read_state(n, pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
-        e1.record(stream)
-        e1.synchronize()
-        ems = e0.elapsed_time(e1)
-        te = torch.tensor([ems], device=f"cuda:{local}", dtype=torch.float64)
+        h.read_state(n, *ptrs)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        tt = torch.tensor([te], device=f"cuda:{local}", dtype=torch.float64)
         if world > 1:
-            torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-        bytes_io = n * (3 + 3 + 3 + 4) * 8
-        e2e = {"value": world * n * ne / (float(te.item()) / 1e3), "unit": "particle-steps/s",
-               "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io, "steps": ne}
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e = {"value": world * n * ne / float(tt.item()), "unit": "particle-steps/s",
+               "h2d_bytes_per_step": bytes_io / ne + ctypes.sizeof(abi.Params),
+               "d2h_bytes_per_step": bytes_io / ne + status_bytes, "steps": ne,
+               "pattern": "state in from pinned host memory, one wdem_step(h, 1) call per step, state out"}
+        # the same with the full kinematic state copied in and out around every single step
+        nr = min(50, ne)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(nr):
+            h.write_state(n, *ptrs)
+            h.step(1)
+            h.read_state(n, *ptrs)
+        torch.cuda.synchronize()
+        tr = time.perf_counter() - t0
+        roundtrip = {"value": n * nr / tr, "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_io,
+                     "d2h_bytes_per_step": bytes_io, "steps": nr}
 
     out = {
-        "metric": "particle-steps/s per GB300 (plain DEM step, HertzDMT settling)" if args.workload == "hertz1M"
-        else "particle-steps/s per GB300 (plain DEM step, FrictMat IdealElPl)",
+        "metric": f"{METRIC} ({DESCR[args.workload]})",
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded random sequential addition cloud)",
+        "dtype": "f64", "data": "synthetic (seeded random sequential addition packing)",
         "config": {"workload": args.workload, "n_particles": n, "dt": spec.params.dt,
                    "parallelism": f"replicas x{world}", "l2": "state larger than L2 (no flush needed)",
-                   "steps_simulated_before_timing": int(max(args.warmup, 3))},
+                   "steps_simulated_before_timing": int(max(args.warmup, 3)) + settled_steps},
         "gpu_launches": int(launches),
         "kernels": {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / max(v[1], 1)} for k, v in kt.items()},
         "contacts": dict(counts, collider_rebuilds_timed=int(st1.nFullRuns - st0.nFullRuns)),
@@ -252,17 +396,34 @@ def run_gpu(args, rank, world, local):
         "roofline_other": {k: v for k, v in rl.items() if k != dominant},
         "clocks": clk,
         "e2e": e2e,
+        "e2e_state_roundtrip_every_step": roundtrip,
     }
+    out.update(extra)
     h.close()
     return out, spec
 
 
 def cpu_baseline(args, full_n):
-    """OpenMP CPU restatement of Woo's step on the host cores, on a bounded cut of the workload."""
+    """OpenMP CPU restatement of Woo's step on the host cores, on a bounded cut of the workload
+    (the settled workload: a cut settled on the GPU, its state and contacts handed to the CPU)."""
     from oracle import bridge
-    cut = 100_000 if args.workload == "hertz1M" else 10000
+    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "spheres10k": 10000}
+    cut = cuts[args.workload]
     spec = build_scene(args.workload, n=cut)
-    o = bridge.Oracle(spec.params, spec.particles, canonical=False, variant="liborc_omp.so")
+    contacts = None
+    if args.workload == "hertz1M_settled":
+        from woo_gb300 import abi
+        h = new_handle(spec, 0)
+        settle(h, spec)
+        pa = h.download_particles(abi.ParticleArrays(spec.particles.n))
+        contacts = h.download_contacts()
+        spec.params.step = h.status().step
+        h.close()
+        spec.particles = pa
+    if args.workload == "ell200k":
+        from woo_gb300 import abi
+        spec.params.ellSolver = abi.ELL_BRENT   # the reference's solver
+    o = bridge.Oracle(spec.params, spec.particles, contacts=contacts, canonical=False, variant="liborc_omp.so")
     o.set_parallel(True)
     o.step(2)  # initial sort + first contacts, not timed
     steps, total = 0, 0.0
@@ -298,8 +459,7 @@ def main():
         if rank != 0:
             return 0
         cb = cpu_baseline(args, None)
-        out = {"metric": "particle-steps/s per GB300 (plain DEM step, HertzDMT settling)" if args.workload == "hertz1M"
-               else "particle-steps/s per GB300 (plain DEM step, FrictMat IdealElPl)",
+        out = {"metric": f"{METRIC} ({DESCR[args.workload]})",
                "value": cb["value"], "unit": cb["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                "higher_is_better": True, "impl": "reference", "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic", "config": {"workload": args.workload},

@@ -570,7 +570,8 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
   }
 }
 
-void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st) {
+void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
+                     const uint16_t* warmBf, const float* warmF) {
   if (nc <= 0) return;
   unsigned* count = &st->workCount;
   cudaMemsetAsync(count, 0, sizeof(unsigned), s);
@@ -580,6 +581,7 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
     (k_contacts_cull<false, true><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF);
     (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
   } else if (P.periodic) {
     (k_contacts_cull<true, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);

@@ -41,6 +41,16 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
   }
 }
 
+// Raises the collider trigger.  All particles of a free-falling cloud cross the verlet distance in the
+// same step, and a million stores to one word serialise in the memory system: one store per warp, and
+// none once the flag is seen set.
+__device__ __forceinline__ void raiseDirty(DeviceStatus* st, bool dirty) {
+  const unsigned am = __activemask();
+  const unsigned b = __ballot_sync(am, dirty);
+  if (b && (threadIdx.x & 31) == (unsigned)(__ffs(b) - 1))
+    if (*(volatile int*)&st->dirty == 0) st->dirty = 1;
+}
+
 // Quaternion::toRotationMatrix (Eigen's formula), row-major
 __device__ __forceinline__ void quatToMat(qd q, double* m) {
   const double tx = 2 * q.x, ty = 2 * q.y, tz = 2 * q.z;
@@ -282,7 +292,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const double4_32a lp = p.lastPos[i];
   const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
   if (!ELL) {
-    if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+    raiseDirty(st, sqnorm(dd) > P.maxD2);
   } else {
     // rotation-aware trigger for bounds that track it (maxRot >= 0; Collision.cpp:94-121)
     double moveDueToRot2 = 0.;
@@ -303,7 +313,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       moveDueToRot2 = mv * mv;
     }
     const double d2 = sqnorm(dd);
-    if (dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2) st->dirty = 1;
+    raiseDirty(st, dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2);
   }
 }
 
@@ -436,17 +446,11 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   pos.z = addScaledR(pos.z, vel.z, dt);
   // leapfrogSphericalRotate; an unrotated, already-normalised orientation is left alone
   int mx = meta.x;
+  bool rotate = false;
   if (!isZeroBits(angVel)) {
-    const double4_32a o4 = p.ori[i];
-    qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
-    double angle = sqrt(sqnorm(angVel));
-    d3 axis = angVel / angle;
-    double ha = 0.5 * (angle * dt);
-    double sh, ch;
-    sincos(ha, &sh, &ch);
-    qd q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
-    ori = qnormalized(qmul(q, ori));
-    p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+    // rotated by k_rotate_list after this kernel: spinning spheres are scattered over most warps, and
+    // the rotation would make every such warp wait for its few spinning lanes
+    rotate = true;
     mx &= ~META_ORI_FIXED;
   } else if (!(mx & META_ORI_FIXED)) {
     const double4_32a o4 = p.ori[i];
@@ -467,6 +471,17 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   if (!finiteBits(pos.x) || !finiteBits(pos.y) || !finiteBits(pos.z)) {
     if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = i;
   }
+  {
+    const unsigned am = __activemask();
+    const unsigned b = __ballot_sync(am, rotate);
+    if (b) {
+      const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&st->rotCount, (unsigned)__popc(b));
+      base = __shfl_sync(am, base, leader);
+      if (rotate) p.rotList[base + __popc(b & ((1u << lane) - 1))] = (unsigned)i;
+    }
+  }
   // aabbIsDirty (moved^2 > verletDist^2): FP32 distance of the shadows with a bound on its error
   // (truncation < 2^-23 relative per coordinate, FP32 arithmetic a few 2^-24 of the distance)
   const float4 lf = p.lastPosf[i];
@@ -474,10 +489,49 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   const float df = sqrtf(dx * dx + dy * dy + dz * dz);
   const float S = fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(lf.x) + fabsf(lf.y) + fabsf(lf.z);
   const float err = 2.5e-7f * S + 1e-6f * df;
+  bool dirty = false;
   if (!(df + err < P.verletLoF)) {
     const double4_32a lp = p.lastPos[i];
     const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
-    if (sqnorm(dd) > P.maxD2) st->dirty = 1;
+    dirty = sqnorm(dd) > P.maxD2;
+  }
+  raiseDirty(st, dirty);
+}
+
+// leapfrogSphericalRotate of the spheres k_leapfrog_fast listed: q = AngleAxis(|w| dt, w/|w|) q, normalised.
+// A sphere's orientation feeds nothing else in the step (sphere contacts do not read it): it is
+// integrated to within a few ulp of the reference's operations at a fraction of their cost --
+// reciprocals instead of the divisions, and for the half angles of a DEM step (|x| < 1e-3) the Taylor
+// polynomials sin x = x (1 - x^2/6 (1 - x^2/20)), cos x = 1 - x^2/2 (1 - x^2/12), whose truncation
+// errors (x^7/5040, x^6/720) are far below an ulp.
+__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const unsigned* count) {
+  const unsigned m = *count;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const unsigned i = p.rotList[k];
+    const d3 angVel = xyz(p.angw[i]);
+    const double4_32a o4 = p.ori[i];
+    qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+    const double angle = sqrt(sqnorm(angVel));
+    const double inv = 1.0 / angle;
+    const d3 axis = angVel * inv;
+    const double ha = 0.5 * (angle * P.dt);
+    double sh, ch;
+    if (fabs(ha) < 1e-3) {
+      const double h2 = ha * ha;
+      sh = ha * (1.0 - h2 * (1.0 / 6.0) * (1.0 - h2 * 0.05));
+      ch = 1.0 - h2 * 0.5 * (1.0 - h2 * (1.0 / 12.0));
+    } else {
+      WDEM_REAL_BRANCH();
+      sincos(ha, &sh, &ch);
+    }
+    qd q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
+    ori = qmul(q, ori);
+    const double z2 = ori.x * ori.x + ori.y * ori.y + ori.z * ori.z + ori.w * ori.w;
+    if (z2 > 0 && !isOneBits(z2)) {
+      const double rn = 1.0 / sqrt(z2);
+      ori.x *= rn; ori.y *= rn; ori.z *= rn; ori.w *= rn;
+    }
+    p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
   }
 }
 
@@ -485,8 +539,11 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
-  if (!fromArrays && !P.hasEll && !P.periodic && !P.lfEnergy && p.touched) {
+  if (!fromArrays && !P.hasEll && !P.periodic && !P.lfEnergy && p.touched && p.rotList) {
+    cudaMemsetAsync(&st->rotCount, 0, sizeof(unsigned), s);
     (k_leapfrog_fast<<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    const unsigned rb = blocks < 152 * 4 ? blocks : 152 * 4;
+    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, &st->rotCount), ++::wdem::g_kernel_launches);
     return;
   }
   if (P.hasEll) {

@@ -44,10 +44,11 @@ struct WarpSmem {
   uint16_t dz4[16 * 16];
   float out[16 * 8];
 };
-// weights: BF16 copy of the padded parameter vector; biases FP32
+// weights: BF16 copy of the padded parameter vector; biases FP32 (b1 at 0, b2 at 64, b3 at 128, b4 at 192)
+constexpr int SB1 = 0, SB2 = 64, SB3 = 128, SB4 = 192, NB = 200;
 struct NetSmem {
   uint16_t w[NPAD];
-  float b[NPAD];  // only the bias ranges are used
+  float b[NB];
 };
 
 __device__ __forceinline__ uint16_t bf(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
@@ -119,35 +120,43 @@ __device__ __forceinline__ void layer(const uint16_t* In, const uint16_t* W, con
 }
 
 __device__ __forceinline__ void forward(const NetSmem& net, WarpSmem& ws, int g, int t) {
-  layer<16, H, true>(ws.x, net.w + OFF_W1, net.b + OFF_B1, ws.a[0], nullptr, g, t);
-  layer<H, H, true>(ws.a[0], net.w + OFF_W2, net.b + OFF_B2, ws.a[1], nullptr, g, t);
-  layer<H, H, true>(ws.a[1], net.w + OFF_W3, net.b + OFF_B3, ws.a[2], nullptr, g, t);
-  layer<H, 8, false>(ws.a[2], net.w + OFF_W4, net.b + OFF_B4, nullptr, ws.out, g, t);
+  layer<16, H, true>(ws.x, net.w + OFF_W1, net.b + SB1, ws.a[0], nullptr, g, t);
+  layer<H, H, true>(ws.a[0], net.w + OFF_W2, net.b + SB2, ws.a[1], nullptr, g, t);
+  layer<H, H, true>(ws.a[1], net.w + OFF_W3, net.b + SB3, ws.a[2], nullptr, g, t);
+  layer<H, 8, false>(ws.a[2], net.w + OFF_W4, net.b + SB4, nullptr, ws.out, g, t);
 }
 
 __device__ __forceinline__ void loadNet(NetSmem& net, const uint16_t* wbf, const float* wf) {
-  for (int k = threadIdx.x; k < NPAD; k += blockDim.x) { net.w[k] = wbf[k]; net.b[k] = wf[k]; }
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(wbf);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(net.w);
+  for (int k = threadIdx.x; k < NPAD / 2; k += blockDim.x) dst[k] = src[k];
+  for (int k = threadIdx.x; k < NB; k += blockDim.x) {
+    const int off = k < 64 ? OFF_B1 + k : (k < 128 ? OFF_B2 + k - 64 : (k < 192 ? OFF_B3 + k - 128 : OFF_B4 + k - 192));
+    net.b[k] = wf[off];
+  }
   __syncthreads();
 }
 
 // ------------------------------------------------------------------------------ inference
 // lam0 of every ellipsoid pair (sphere + ellipsoid included; walls excluded) that the contact kernel
 // may solve this step; other entries are NaN (cold start).
-__global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, long long nc, const uint16_t* wbf,
-                                                  const float* wf) {
+__global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const unsigned* work, const unsigned* count,
+                                                  const uint16_t* wbf, const float* wf) {
   extern __shared__ __align__(16) unsigned char smem[];
   NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
   WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
   loadNet(net, wbf, wf);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   WarpSmem& ws = wsAll[warp];
-  for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < nc; base += (long long)gridDim.x * SAMPLES) {
-    const long long i = base + (lane & 15);
+  const long long nw = *count;
+  for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < nw; base += (long long)gridDim.x * SAMPLES) {
+    const long long kw = base + (lane & 15);
+    const long long i = kw < nw ? (long long)work[kw] : -1;
     bool use = false;
     if (lane < 16) {
       float f[ELL_FEATURES];
       for (int k = 0; k < ELL_FEATURES; k++) f[k] = 0.f;
-      if (i < nc) {
+      if (i >= 0) {
         const uint8_t sb = c.state[i] & CS_SHAPES;
         if ((sb & CS_ELL) && !(sb & CS_WALL_A) && (c.state[i] & CS_MASK) != CS_DEAD) {
           const int2 id = c.ids[i];
@@ -164,7 +173,7 @@ __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, long 
     }
     __syncwarp();
     forward(net, ws, g, t);
-    if (lane < 16 && i < nc) {
+    if (lane < 16 && i >= 0) {
       float l = ws.out[(lane & 15) * 8 + 0];
       l = fminf(fmaxf(l, 1e-3f), 1.f - 1e-3f);
       c.lam0[i] = use ? l : __int_as_float(0x7fffffff);
@@ -368,11 +377,12 @@ void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf) {
   (k_to_bf16<<<(NPAD + 255) / 256, 256, 0, s>>>(w, wbf, NPAD), ++::wdem::g_kernel_launches);
 }
 
-void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const uint16_t* wbf, const float* wf) {
+void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
+                     const uint16_t* wbf, const float* wf) {
   if (nc <= 0) return;
   long long blocks = (nc + SAMPLES - 1) / SAMPLES;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, nc, wbf, wf), ++::wdem::g_kernel_launches);
+  if (blocks > 152 * 2) blocks = 152 * 2;  // persistent blocks: the weights are loaded once per block
+  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, wbf, wf), ++::wdem::g_kernel_launches);
 }
 
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf) {

@@ -178,6 +178,7 @@ struct wdem_handle {
   long long stagingCap = 0;
   bool periodic = false;
   bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
+  long long matsChecked = -1;   // material-table size the particle material indices were checked against
   std::vector<double> semi;     // host copy of the semi-axes (3n; spheres r, r, r)
   float* ellLog = nullptr;      // training records of the ellipsoid solves, when logging
   unsigned long long* ellLogCount = nullptr;
@@ -543,6 +544,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.posf, N) == cudaSuccess;
   ok &= dalloc(d.lastPosf, N) == cudaSuccess;
   ok &= dalloc(d.touched, N) == cudaSuccess;
+  ok &= dalloc(d.rotList, N) == cudaSuccess;
   for (int k = 0; k < 3; k++) ok &= dalloc(d.energy[k], N) == cudaSuccess;
   ok &= dalloc(h->dEnergy, WDEM_E_COUNT) == cudaSuccess;
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
@@ -581,7 +583,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
-  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rotList);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
   cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
@@ -708,6 +710,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   }
   h->semi = semi;
   h->hasEll = anyEll;
+  h->matsChecked = -1;
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   if (n > 0) {
@@ -824,9 +827,13 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
 int wdem_step(wdem_handle* h, int32_t nSteps) {
   if (!h || nSteps < 0) return WDEM_ERR_ARG;
   if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "wdem_step before particles and params were set");
-  for (int i = 0; i < h->n; i++)
-    if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size())
-      return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
+  if (h->matsChecked != (long long)h->mats.size()) {
+    // material indices against the current table (once per table size: uploads re-check their own)
+    for (int i = 0; i < h->n; i++)
+      if (h->mat[i] < 0 || h->mat[i] >= (int)h->mats.size())
+        return fail(h, WDEM_ERR_ARG, "material index out of range for particle #" + std::to_string(i));
+    h->matsChecked = (long long)h->mats.size();
+  }
   if (h->hasEll && (h->P.law != WDEM_LAW_IDEALELPL || h->P.cp2 != WDEM_CP2_FRICT))
     return fail(h, WDEM_ERR_UNSUPPORTED,
                 "ellipsoids and aspherical nodes run with Cp2_FrictMat_FrictPhys + Law2_L6Geom_FrictPhys_IdealElPl only");
@@ -885,9 +892,9 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     }
     {
       PhaseTimer t(h, PH_CONTACTS);
-      if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP)
-        mlp_launch_warm(s, h->d, h->buf[h->cur].c, h->nContacts, h->mlpWbf, h->mlpW);
-      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst);
+      const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
+      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+                      warm ? h->mlpW : nullptr);
     }
     if (h->P.trackEnergy) {
       int rc0;

@@ -108,6 +108,7 @@ struct Particles {
   double* maxRot;
   float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
   uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
+  unsigned* rotList;  // spheres whose orientation the rotation pass integrates this step
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
   double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
@@ -153,7 +154,8 @@ struct DeviceStatus {
   int overflow;
   unsigned long long pairTotal;
   unsigned long long ellSolves, ellIters, ellFallbacks;
-  unsigned workCount;  // length of the contact work list of this step  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
+  unsigned workCount;  // length of the contact work list of this step
+  unsigned rotCount;   // length of the rotation list of this step  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
 
@@ -170,7 +172,9 @@ void launch_refresh_posf(cudaStream_t s, Particles p, int n);
 void energy_accumulate(cudaStream_t s, const double* x, long long n, double* partials, double* acc, bool reset);
 // ---- launchers (k_contact.cu) ----
 void upload_materials(const DevMaterial* m, int n);
-void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st);
+// warm: BF16 and FP32 weights of the learned warm start, run between the cull and the FP64 pass (or null)
+void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
+                     const uint16_t* warmBf = nullptr, const float* warmF = nullptr);
 void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc);
 // ---- collider (k_collider.cu) ----
 struct ColliderScratch {
@@ -208,7 +212,8 @@ void mlp_unpack(const float* pub, float* pad);
 void mlp_pack(const float* pad, float* pub);
 cudaError_t mlp_prepare_kernels();
 void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf);
-void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const uint16_t* wbf, const float* wf);
+void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
+                     const uint16_t* wbf, const float* wf);
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf);
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
                      float* grad, float* loss);
