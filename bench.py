@@ -12,6 +12,10 @@ Workloads (synthetic, seeded; no dataset is involved):
       learned warm start is trained first (untimed) on records logged by the plain Newton solver; the
       line reports the learned-warm-start run and, under "variants", the reference's Brent solver, the
       plain cold-start Newton and the previous-step warm start on the same initial state.
+  batch512 -- 512 independent oedometric scenes (sphere counts log-uniform in [500, 20000], r ~ U[1,3] mm,
+      tanPhi ~ U[.1,.8], young log-uniform in [1e6,1e8] Pa, per-scene dt, top wall at 0.05 m/s) stepped
+      as one batch; "scene_by_scene" times a seeded sample of 32 of the scenes run one after another on
+      their own handles and scales it to all 512.
   spheres10k -- 10,000 monodisperse FrictMat spheres r = 5 mm in a 0.5 x 0.5 x 1 m box (CPU-runnable).
 
 A step is one pass of the hot path (Leapfrog -> collider -> ContactLoop) over all particles; the timed
@@ -40,12 +44,13 @@ sys.path.insert(0, ROOT)
 
 import numpy as np
 
-WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "spheres10k"]
-DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "spheres10k": 2000}
+WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "batch512", "spheres10k"]
+DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "batch512": 500, "spheres10k": 2000}
 METRIC = "particle-steps/s per GB300"
 DESCR = {"hertz1M": "plain DEM step, HertzDMT settling",
          "hertz1M_settled": "plain DEM step, HertzDMT, settled packing",
          "ell200k": "ellipsoid DEM step, learned warm start",
+         "batch512": "512 batched oedometric scenes",
          "spheres10k": "plain DEM step, FrictMat IdealElPl"}
 
 
@@ -139,6 +144,8 @@ def build_scene(name, n=None):
         return scenes.hertz1M(n=n or 1_000_000)
     if name == "hertz1M_settled":
         return scenes.hertz1M(n=n or 1_000_000, height=0.95)
+    if name == "batch512":
+        return scenes.batch_oedometric(n or 512, 4)
     if name == "ell200k":
         k = n or 200_000
         sc = (k / 200_000) ** (1.0 / 3.0)
@@ -289,6 +296,27 @@ def run_gpu(args, rank, world, local):
             "iterations_vs_newton_cold": v["newton_cold"]["iterations_per_solve"] / v["newton_mlp"]["iterations_per_solve"]}
         h = new_handle(spec, local)
         h.warm_set_weights(w)
+    elif args.workload == "batch512":
+        # the same scenes one at a time on their own handles (a seeded sample, scaled to all scenes)
+        from woo_gb300 import scenes
+        nsc = len(spec.info["ranges"])
+        rng = np.random.default_rng(11)
+        sample = sorted(rng.choice(nsc, min(32, nsc), replace=False).tolist())
+        t_total, n_sample = 0.0, 0
+        for k in sample:
+            single = scenes.single_from_batch(spec, k)
+            hs = new_handle(single, local)
+            ss = torch.cuda.ExternalStream(hs.stream(), device=local)
+            hs.step(max(args.warmup, 3))
+            t_total += timed_steps(hs, ss, args.steps, world, local, barrier) / 1e3
+            n_sample += single.particles.n
+            hs.close()
+        scale = nsc / len(sample)
+        n_all = spec.particles.n
+        extra["scene_by_scene"] = {"sampled_scenes": len(sample), "steps": args.steps,
+                                   "seconds_sample": t_total, "seconds_all_estimated": t_total * scale,
+                                   "value": n_all * args.steps / (t_total * scale), "unit": "particle-steps/s"}
+        h = new_handle(spec, local)
     else:
         h = new_handle(spec, local)
     stream = torch.cuda.ExternalStream(h.stream(), device=local)
@@ -398,6 +426,8 @@ def run_gpu(args, rank, world, local):
         "e2e": e2e,
         "e2e_state_roundtrip_every_step": roundtrip,
     }
+    if "scene_by_scene" in extra:
+        extra["batch_speedup_vs_scene_by_scene"] = value / extra["scene_by_scene"]["value"]
     out.update(extra)
     h.close()
     return out, spec
@@ -407,7 +437,7 @@ def cpu_baseline(args, full_n):
     """OpenMP CPU restatement of Woo's step on the host cores, on a bounded cut of the workload
     (the settled workload: a cut settled on the GPU, its state and contacts handed to the CPU)."""
     from oracle import bridge
-    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "spheres10k": 10000}
+    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "batch512": 16, "spheres10k": 10000}
     cut = cuts[args.workload]
     spec = build_scene(args.workload, n=cut)
     contacts = None

@@ -123,6 +123,9 @@ typedef struct wdem_params {
   double newtonTol;       /* Newton: converged when |delta lambda| <= newtonTol */
   int32_t warmStart;      /* WDEM_WARM_* */
   int32_t fallbackIters;  /* MLP warm start: Newton iterations before falling back to the cold start */
+  /* Batched scenes: Scene.dt of each material's scene (nMaterials values), used instead of dt for the
+   * particles and contacts of that material; NULL = every particle steps with dt */
+  const double* materialDt;
 } wdem_params;
 
 /* ---- particle state, SoA; all arrays have n (or 3n / 4n) items --------------------------------- */
@@ -146,6 +149,8 @@ typedef struct wdem_particles {
   double* torque;         /* 3n DemData.torque */
   double* semiAxes;       /* 3n Ellipsoid.semiAxes (NULL when there are no ellipsoids) */
   double* angMom;         /* 3n DemData.angMom, NaN = not initialised (aspherical Leapfrog); may be NULL */
+  int32_t* scene;         /* batched independent scenes: scene index of each particle (0..4095); particles of
+                             different scenes never interact; NULL = one scene */
 } wdem_particles;
 
 /* ---- contact state, SoA; n contacts ---------------------------------------------------------- */

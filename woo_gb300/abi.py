@@ -69,14 +69,14 @@ class Params(C.Structure):
                 ("nMaterials", C.c_int32), ("_pad2", C.c_int32),
                 ("materials", C.POINTER(Material)),
                 ("ellSolver", C.c_int32), ("brentBits", C.c_int32), ("newtonTol", C.c_double),
-                ("warmStart", C.c_int32), ("fallbackIters", C.c_int32)]
+                ("warmStart", C.c_int32), ("fallbackIters", C.c_int32), ("materialDt", C.POINTER(C.c_double))]
 
 
 class Particles(C.Structure):
     _fields_ = [("n", C.c_int32), ("_pad", C.c_int32), ("shape", I32), ("radius", D), ("wallAxis", I32),
                 ("wallSense", I32), ("material", I32), ("mask", U32), ("flags", U32), ("mass", D),
                 ("inertia", D), ("pos", D), ("ori", D), ("vel", D), ("angVel", D), ("force", D), ("torque", D),
-                ("semiAxes", D), ("angMom", D)]
+                ("semiAxes", D), ("angMom", D), ("scene", I32)]
 
 
 class Contacts(C.Structure):
@@ -139,6 +139,7 @@ class ParticleArrays:
         self.torque = np.zeros((n, 3))
         self.semiAxes = np.full((n, 3), np.nan)
         self.angMom = np.full((n, 3), np.nan)
+        self.scene = np.zeros(n, np.int32)
 
     def copy(self):
         o = ParticleArrays(self.n)
@@ -159,6 +160,7 @@ class ParticleArrays:
         s.angVel = ptr(self.angVel, C.c_double); s.force = ptr(self.force, C.c_double)
         s.torque = ptr(self.torque, C.c_double)
         s.semiAxes = ptr(self.semiAxes, C.c_double); s.angMom = ptr(self.angMom, C.c_double)
+        s.scene = ptr(self.scene, C.c_int32)
         return s
 
 

@@ -410,6 +410,7 @@ struct SweepArgs {
   int nLarge;
   int nSmall;
   unsigned loneMask;
+  const int* sceneWall;  // per-scene ranges of the large list (null: one scene)
 };
 
 template <bool WRITE>
@@ -420,11 +421,12 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
   unsigned cnt = 0;
   unsigned long long base = WRITE ? counts[s] : 0;
   if (s == A.nSmall) {
-    // large-large pairs
+    // large-large pairs (walls of the same scene; the large list is grouped by scene)
     for (int a = 0; a < A.nLarge; a++)
       for (int b = a + 1; b < A.nLarge; b++) {
         int i = A.large[a], j = A.large[b];
         int4 mi = p.meta[i], mj = p.meta[j];
+        if (sceneOf(mi.x) != sceneOf(mj.x)) break;
         if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
         if (!overlap3(p.bbmin[i], p.bbmax[i], p.bbmin[j], p.bbmax[j])) continue;
         if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
@@ -465,13 +467,16 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
         int j = (int)A.vals[q];
         int4 mj = p.meta[j];
         if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
+        if (sceneOf(mi.x) != sceneOf(mj.x)) continue;
         if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
         if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
         cnt++;
       }
     }
   }
-  for (int a = 0; a < A.nLarge; a++) {
+  const int sc = sceneOf(mi.x);
+  const int a0 = A.sceneWall ? A.sceneWall[sc] : 0, a1 = A.sceneWall ? A.sceneWall[sc + 1] : A.nLarge;
+  for (int a = a0; a < a1; a++) {
     int j = A.large[a];
     int4 mj = p.meta[j];
     if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
@@ -793,6 +798,7 @@ void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, Colli
   SweepArgs A;
   A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
   A.nSmall = nSmall; A.loneMask = loneMask;
+  A.sceneWall = cs.nScenes > 1 ? cs.sceneWall : nullptr;
   int threads = nSmall + 1;
   if (write) (k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
   else (k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);

@@ -219,6 +219,8 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   const uint8_t s = s0 & CS_MASK;
   const int2 id = c.ids[i];
   const int a = id.x, b = id.y;
+  // batched scenes: the scene's dt (the material of pA belongs to its scene; walls too)
+  const double dtC = P.matDt ? P.matDt[p.meta[a].y] : P.dt;
   const bool real = (s == CS_REAL);
   // periodic: pB is taken at its image hSize*cellDist (ContactLoop.cpp:156, Cell::intrShiftPos)
   int4 cd = make_int4(0, 0, 0, 0);
@@ -295,7 +297,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     const d3 prevNormal = mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
     const d3 prevT1 = mk(c.hist[HIST_T1X][i], c.hist[HIST_T1Y][i], c.hist[HIST_T1Z][i]);
     const d3 prevContPt = mk(c.hist[HIST_CX][i], c.hist[HIST_CY][i], c.hist[HIST_CZ][i]);
-    const double dt = P.dt;
+    const double dt = dtC;
     const int am = P.approxMask;
     const d3 currNormal = normal;
     d3 normRotVec = cross(prevNormal, currNormal);
@@ -343,7 +345,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   // ---- Law2
   bool keep = true;
   double tqx = 0, tqy = 0, tqz = 0;
-  const double dt = P.dt;
+  const double dt = dtC;
   double eEl = 0, ePl = 0, eVN = 0, eVT = 0, eBr = 0;
   if (LAW == WDEM_LAW_IDEALELPL) {
     if (uN > 0 && !P.noBreak) {

@@ -79,8 +79,7 @@ __device__ __forceinline__ qd qaxpy(qd q1, double f, qd q2) {
 }
 // Leapfrog::leapfrogAsphericalRotate (Leapfrog.cpp:299-322): angular momentum leapfrog in the body frame
 __device__ __noinline__ void asphericalRotate(const StepParams& P, Particles p, int i, d3 M, d3 inertia, qd& ori,
-                                              d3& angVel) {
-  const double dt = P.dt;
+                                              d3& angVel, double dt) {
   d3 am = xyz(p.angMom[i]);
   double A[9];
   qd oc;
@@ -143,7 +142,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     // when downloaded (k_reduce_forces)
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }
-  const double dt = P.dt;
+  const double dt = dtOf(P, meta.y);
   const double damping = P.damping;
   const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
   d3 vel = xyz(vm);
@@ -265,7 +264,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
   if (ELL && asph) {
     if (isZeroBits(inertia)) { if (atomicCAS(&st->code, 0, WDEM_ERR_STATE) == 0) st->detail = i; }
-    else asphericalRotate(P, p, i, T, inertia, ori, angVel);
+    else asphericalRotate(P, p, i, T, inertia, ori, angVel, dt);
   } else {
   if (!isZeroBits(angVel)) {
     double angle = sqrt(sqnorm(angVel));
@@ -369,7 +368,7 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   } else {
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }
-  const double dt = P.dt;
+  const double dt = dtOf(P, meta.y);
   const double damping = P.damping;
   const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
   d3 vel = xyz(vm);
@@ -514,7 +513,7 @@ __global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, 
     const double angle = sqrt(sqnorm(angVel));
     const double inv = 1.0 / angle;
     const d3 axis = angVel * inv;
-    const double ha = 0.5 * (angle * P.dt);
+    const double ha = 0.5 * (angle * dtOf(P, p.meta[i].y));
     double sh, ch;
     if (fabs(ha) < 1e-3) {
       const double h2 = ha * ha;

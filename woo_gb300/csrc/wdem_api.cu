@@ -179,6 +179,9 @@ struct wdem_handle {
   bool periodic = false;
   bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
   long long matsChecked = -1;   // material-table size the particle material indices were checked against
+  double* dMatDt = nullptr;     // batched scenes: dt per material
+  int matDtCap = 0;
+  bool useMatDt = false;
   std::vector<double> semi;     // host copy of the semi-axes (3n; spheres r, r, r)
   float* ellLog = nullptr;      // training records of the ellipsoid solves, when logging
   unsigned long long* ellLogCount = nullptr;
@@ -465,6 +468,7 @@ void fillStepParams(wdem_handle* h) {
   P.lfEnergy = r.trackEnergy;
   P.nMaterials = (int)h->mats.size();
   P.periodic = h->periodic ? 1 : 0;
+  P.matDt = h->useMatDt ? h->dMatDt : nullptr;
   P.hasEll = h->hasEll ? 1 : 0;
   P.ellSolver = r.ellSolver;
   P.brentTol = std::ldexp(1.0, 1 - std::min(std::numeric_limits<double>::digits / 2, (int)r.brentBits));
@@ -581,6 +585,7 @@ int wdem_destroy(wdem_handle* h) {
   Particles& d = h->d;
   cudaFree(d.semi); cudaFree(d.angMom); cudaFree(d.lastOri); cudaFree(d.maxRot);
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
+  cudaFree(h->dMatDt); cudaFree(h->cs.sceneWall);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
   cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rotList);
@@ -612,7 +617,7 @@ int wdem_set_params(wdem_handle* h, const wdem_params* p) {
   if (p->iniEqlb) return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl.iniEqlb is not supported");
   if (!p->iniLensTouch) return fail(h, WDEM_ERR_UNSUPPORTED, "Cg2_*_L6Geom.iniLensTouch=False is not supported");
   if (!p->applyForces) return fail(h, WDEM_ERR_UNSUPPORTED, "ContactLoop.applyForces=False is not supported");
-  if (p->nMaterials <= 0 || !p->materials || p->nMaterials > MAX_MATERIALS) return fail(h, WDEM_ERR_ARG, "materials table missing or larger than 64");
+  if (p->nMaterials <= 0 || !p->materials || p->nMaterials > MAX_MATERIALS) return fail(h, WDEM_ERR_ARG, "materials table missing or larger than 1024");
   if (p->law == WDEM_LAW_HERTZ_DMT && p->cp2 != WDEM_CP2_HERTZ)
     return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT needs Cp2_HertzMat_HertzPhys");
   if (p->law == WDEM_LAW_IDEALELPL && p->cp2 != WDEM_CP2_FRICT)
@@ -642,6 +647,18 @@ int wdem_set_params(wdem_handle* h, const wdem_params* p) {
   }
   cudaSetDevice(h->device);
   upload_materials(dm.data(), (int)dm.size());
+  if (p->materialDt) {
+    for (int k = 0; k < p->nMaterials; k++)
+      if (!(p->materialDt[k] >= 0)) return fail(h, WDEM_ERR_ARG, "materialDt must be non-negative");
+    if (h->matDtCap < p->nMaterials) {
+      cudaFree(h->dMatDt);
+      h->dMatDt = nullptr;
+      CK(dalloc(h->dMatDt, (size_t)p->nMaterials));
+      h->matDtCap = p->nMaterials;
+    }
+    CK(cudaMemcpy(h->dMatDt, p->materialDt, p->nMaterials * sizeof(double), cudaMemcpyHostToDevice));
+    h->useMatDt = true;
+  } else h->useMatDt = false;
   if (h->particlesSet) resolveVerlet(h);
   fillStepParams(h);
   h->paramsSet = true;
@@ -664,6 +681,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   std::vector<int4> meta(n);
   std::vector<double> semi(3 * (size_t)n, 0.0);
   bool anyEll = false;
+  int nScenes = 1;
   for (int i = 0; i < n; i++) {
     int sh = p->shape[i];
     if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID)
@@ -704,9 +722,22 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     torque[i] = make_double4_32a(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2], 0);
     auto posInert = [](double x) { return x > 0; };
     const bool ipos = posInert(in[0]) && posInert(in[1]) && posInert(in[2]);
-    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0) | (ipos ? META_IPOS : 0),
+    const int sc = p->scene ? p->scene[i] : 0;
+    if (sc < 0 || sc >= MAX_SCENES) return fail(h, WDEM_ERR_ARG, "scene index out of range for particle #" + std::to_string(i));
+    nScenes = std::max(nScenes, sc + 1);
+    meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0) | (ipos ? META_IPOS : 0) |
+                            (sc << META_SCENE_SHIFT),
                         p->material[i], (int)p->mask[i], (int)fl);
     if (sh != WDEM_SHAPE_WALL) h->smallIds.push_back(i); else h->largeIds.push_back(i);
+  }
+  if (nScenes > 1 && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "batched scenes in a periodic cell are not supported");
+  // walls grouped by scene (stable: ids ascending within a scene); per-scene ranges
+  std::vector<int> sceneWall(nScenes + 1, 0);
+  if (nScenes > 1) {
+    std::stable_sort(h->largeIds.begin(), h->largeIds.end(),
+                     [&](int x, int y) { return (p->scene ? p->scene[x] : 0) < (p->scene ? p->scene[y] : 0); });
+    for (int id : h->largeIds) sceneWall[(p->scene ? p->scene[id] : 0) + 1]++;
+    for (int k = 0; k < nScenes; k++) sceneWall[k + 1] += sceneWall[k];
   }
   h->semi = semi;
   h->hasEll = anyEll;
@@ -746,6 +777,14 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   if (!h->largeIds.empty())
     CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   h->cs.nLarge = (int)h->largeIds.size();
+  cudaFree(h->cs.sceneWall);
+  h->cs.sceneWall = nullptr;
+  h->cs.nScenes = nScenes;
+  if (nScenes > 1) {
+    CK(dalloc(h->cs.sceneWall, (size_t)nScenes + 1));
+    CK(cudaMemcpyAsync(h->cs.sceneWall, sceneWall.data(), (nScenes + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+  }
   launch_refresh_posf(s, h->d, n);
   if (n > 0) CK(cudaMemsetAsync(h->d.touched, 0, n, s));
   CK(cudaStreamSynchronize(s));
@@ -1182,6 +1221,7 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
   }
   if (!h->smallIds.empty()) CK(cudaMemcpyAsync(h->dSmall, h->smallIds.data(), h->smallIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   if (!h->largeIds.empty()) CK(cudaMemcpyAsync(h->cs.large, h->largeIds.data(), h->largeIds.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  h->cs.nScenes = 1;
   h->cs.nLarge = (int)h->largeIds.size();
   h->nContacts = 0;
   int rc;
@@ -1241,6 +1281,7 @@ int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
   for (int s : h->shape)
     if (s != WDEM_SHAPE_SPHERE) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
   if (h->nContacts > 0 && !h->periodic) return fail(h, WDEM_ERR_STATE, "set the cell before uploading contacts");
+  if (h->cs.nScenes > 1) return fail(h, WDEM_ERR_UNSUPPORTED, "batched scenes in a periodic cell are not supported");
   HostCell& hc = h->cell;
   // Cell.setHSize / trsf / nextGradV (Cell.hpp:108-111) then postLoad -> integrateAndUpdate(0)
   hc.hSize = get9(c->hSize);

@@ -39,13 +39,16 @@ enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_EL
 // META_ORI_FIXED: the orientation is not rotating and normalising it is the identity (set and cleared by the
 // integrator); META_IPOS: all inertia components are positive (set at upload)
 enum { META_ASPH = 1 << 12, META_ORI_FIXED = 1 << 13, META_IPOS = 1 << 14 };
+// meta.x bits 16..27: scene index of batched independent scenes
+enum { META_SCENE_SHIFT = 16, MAX_SCENES = 4096 };
+__host__ __device__ __forceinline__ int sceneOf(int metax) { return (metax >> META_SCENE_SHIFT) & (MAX_SCENES - 1); }
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
        HIST_COUNT };
 enum { HIST_FRICT = HIST_E0 };  // FrictPhys contacts carry the first 14 history arrays
 enum { OUT_FX = 0, OUT_FY, OUT_FZ, OUT_TAX, OUT_TAY, OUT_TAZ, OUT_TBX, OUT_TBY, OUT_TBZ, OUT_COUNT };
-enum { MAX_MATERIALS = 64 };
+enum { MAX_MATERIALS = 1024 };  // 1024 x 56 B fits the 64 KB constant bank
 
 struct DevMaterial {
   int kind;
@@ -95,10 +98,14 @@ struct StepParams {
   double newtonTol;
   int warmStart;       // WDEM_WARM_*
   int fallbackIters;
+  const double* matDt;               // batched scenes: dt per material (device), or null (all use dt)
   float* ellLog;                     // training records of solved pairs (17 floats each), or null
   unsigned long long* ellLogCount;
   long long ellLogCap;
 };
+
+// time step of a particle (batched scenes: its material's scene dt)
+__device__ __forceinline__ double dtOf(const StepParams& P, int material) { return P.matDt ? P.matDt[material] : P.dt; }
 
 struct Particles {
   double4_32a *posr, *velm, *angw, *inert, *ori, *lastPos, *bbmin, *bbmax, *force, *torque;
@@ -188,8 +195,10 @@ struct ColliderScratch {
   int* cellStart;                       // maxCols + 1
   int maxCols;
   unsigned* counts;                     // nSmall+2 pair counts per sorted particle, scanned in place
-  int* large;                           // ids of walls (unbounded boxes)
+  int* large;                           // ids of walls (unbounded boxes), grouped by scene
   int nLarge;
+  int* sceneWall;                       // scene s owns large[sceneWall[s] .. sceneWall[s+1])
+  int nScenes;
   GridParams* grid;
   unsigned* retainFlag;                 // old contacts retained (scanned in place)
   long long retainCap;

@@ -16,6 +16,7 @@ Masses and inertias follow Sphere::lumpMassInertia (src/dem/Sphere.cpp:26-33).
 import math
 
 import numpy as np
+from ctypes import c_double as C_double
 
 from . import abi
 
@@ -382,3 +383,96 @@ def ellipsoid_cloud(n, seed, box=(0.1, 0.1, 0.1), amin=0.004, amax=0.006, ratios
     g = np.asarray(gravity, np.float64)
     pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
     return SceneSpec(p, mats, pa, f"ell{n}", dict(seed=seed, dt=dt))
+
+
+def oedometric_scene(n, seed, young, tanPhi, rmin=0.001, rmax=0.003, density=2600.0, top_vel=0.05, dt_safety=0.9,
+                     dense=1.0):
+    """One oedometric compression scene (after examples/oedometric.py): spheres with r ~ U[rmin, rmax] packed
+    loosely (solid fraction ~0.3) in a box of base L x L and height 2L with 5 fixed walls, the top wall
+    just above the topmost sphere moving down at top_vel (all DOFs blocked); particle FrictMat(young,
+    ktDivKn .2, tanPhi), walls the same material without friction; gravity -10, damping 0.4.
+    Returns (centers, radii, walls, mats_py, dt) for batch assembly."""
+    vol = n * (4.0 / 3.0) * math.pi * ((rmax ** 4 - rmin ** 4) / (4 * (rmax - rmin))) / 0.3
+    L = (vol / 2.0) ** (1.0 / 3.0)
+    lo, hi = np.zeros(3), np.array([L, L, 2 * L])
+    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed, max_attempts=400)
+    if dense != 1.0:
+        # squeezed towards the box centre: overlaps from the start (dense < 1)
+        c = hi / 2
+        centers = c + (centers - c) * dense
+    ztop = float(np.max(centers[:, 2] + radii)) + 1e-4
+    walls = [(0, 1, 0.0, 1), (0, -1, L, 1), (1, 1, 0.0, 1), (1, -1, L, 1), (2, 1, 0.0, 1), (2, -1, ztop, 1)]
+    mats_py = [dict(kind=abi.MAT_FRICT, density=density, young=young, ktDivKn=0.2, tanPhi=tanPhi),
+               dict(kind=abi.MAT_FRICT, density=density, young=young, ktDivKn=0.2, tanPhi=0.0)]
+    dt = dt_safety * float(np.min(radii)) / math.sqrt(young / density)
+    return dict(centers=centers, radii=radii, walls=walls, mats=mats_py, dt=dt, box=hi, top_vel=top_vel)
+
+
+def batch_oedometric(n_scenes, seed, nmin=500, nmax=20000, spacing=None, verletDist=1e-4, dense=1.0):
+    """n_scenes independent oedometric scenes in one particle set (BASELINE config 4): sphere counts
+    log-uniform in [nmin, nmax], tanPhi ~ U[0.1, 0.8], young log-uniform in [1e6, 1e8] Pa, per-scene
+    dt = 0.9 x the scene's p-wave dt (wdem_params.materialDt).  Scene k is shifted along x by k x spacing
+    so the scenes stay apart; each particle carries its scene index.  Returns the SceneSpec (info holds
+    the per-scene particle ranges, counts and dt)."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(math.log(nmin), math.log(nmax), n_scenes)).astype(int)
+    tanphis = rng.uniform(0.1, 0.8, n_scenes)
+    youngs = np.exp(rng.uniform(math.log(1e6), math.log(1e8), n_scenes))
+    parts = [oedometric_scene(int(counts[k]), seed * 100003 + k, float(youngs[k]), float(tanphis[k]), dense=dense)
+             for k in range(n_scenes)]
+    if spacing is None:
+        spacing = 1.25 * max(float(pt["box"][0]) for pt in parts)
+    ntot = sum(6 + len(pt["radii"]) for pt in parts)
+    pa = abi.ParticleArrays(ntot)
+    mats_py, mat_dt, ranges = [], [], []
+    q = 0
+    for k, pt in enumerate(parts):
+        off = np.array([k * spacing, 0.0, 0.0])
+        m0 = len(mats_py)
+        mats_py += pt["mats"]
+        mat_dt += [pt["dt"], pt["dt"]]
+        ns = len(pt["radii"])
+        sub = assemble(pt["centers"] + off, pt["radii"], m0, [(ax, se, pos + off[ax], m0 + mi) for ax, se, pos, mi in pt["walls"]],
+                       mats_py)
+        sub.vel[5] = [0.0, 0.0, -pt["top_vel"]]   # the top wall
+        for name in ("shape", "radius", "wallAxis", "wallSense", "material", "mask", "flags", "mass", "inertia", "pos",
+                     "ori", "vel", "angVel", "force", "torque"):
+            getattr(pa, name)[q:q + 6 + ns] = getattr(sub, name)
+        pa.scene[q:q + 6 + ns] = k
+        ranges.append((q, q + 6 + ns))
+        q += 6 + ns
+    g = np.array([0.0, 0.0, -10.0])
+    mov = pa.shape == abi.SHAPE_SPHERE
+    pa.force[mov] = pa.mass[mov, None] * g[None, :]
+    mats = materials_array(mats_py)
+    dt_arr = (C_double * len(mat_dt))(*mat_dt)
+    p = default_params(mats, dt=float(min(mat_dt)), gravity=tuple(g), damping=0.4, verletDist=verletDist)
+    p.materialDt = dt_arr
+    spec = SceneSpec(p, mats, pa, f"batch{n_scenes}",
+                     dict(seed=seed, counts=[int(c) for c in counts], ranges=ranges, dt=mat_dt[::2], spacing=spacing,
+                          youngs=youngs.tolist(), tanphis=tanphis.tolist()))
+    spec.keep = dt_arr
+    spec.scene_parts = parts
+    return spec
+
+
+def single_from_batch(spec, k):
+    """Scene k of a batch as its own SceneSpec (its particles, its two materials, its dt), for checks."""
+    a, b = spec.info["ranges"][k]
+    n = b - a
+    pa = abi.ParticleArrays(n)
+    for name in ("shape", "radius", "wallAxis", "wallSense", "material", "mask", "flags", "mass", "inertia", "pos", "ori",
+                 "vel", "angVel", "force", "torque"):
+        getattr(pa, name)[:] = getattr(spec.particles, name)[a:b]
+    m0 = int(pa.material.min())
+    pa.material[:] -= m0
+    mats_src = spec.materials
+    mats_py = []
+    for mi in (m0, m0 + 1):
+        m = mats_src[mi]
+        mats_py.append(dict(kind=m.kind, density=m.density, young=m.young, ktDivKn=m.ktDivKn, tanPhi=m.tanPhi,
+                            surfEnergy=m.surfEnergy, alpha=m.alpha))
+    mats = materials_array(mats_py)
+    p = default_params(mats, dt=spec.info["dt"][k], gravity=tuple(spec.params.gravity), damping=spec.params.damping,
+                       verletDist=spec.params.verletDist)
+    return SceneSpec(p, mats, pa, f"scene{k}", dict(range=(a, b)))
