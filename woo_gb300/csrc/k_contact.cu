@@ -578,8 +578,10 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   unsigned* count = &st->workCount;
   cudaMemsetAsync(count, 0, sizeof(unsigned), s);
   const unsigned cb = (unsigned)((nc + 255) / 256);
+  // the FP64 pass loops over the work list (length known on the device only): 4 blocks per SM fill the
+  // GPU at its register count, and no more blocks are launched to find the list short
   const long long hb0 = (nc + 127) / 128;
-  const unsigned hb = (unsigned)(hb0 < 152 * 16 ? hb0 : 152 * 16);
+  const unsigned hb = (unsigned)(hb0 < 152 * 4 ? hb0 : 152 * 4);
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
     (k_contacts_cull<false, true><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);

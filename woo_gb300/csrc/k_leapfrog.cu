@@ -339,8 +339,9 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   const bool blockedAll = (flags & 63u) == 63u;
   const bool blockedNone = (flags & 63u) == 0u;
   d3 F, T;
+  bool touchedNow = false;
+  const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
   if (!blockedAll) {
-    const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
     if (grav) {
       const bool mf = finiteBits(mass);
       F.x = (zeroBits(P.gravity[0]) && mf) ? signedZero(mass, P.gravity[0]) : mass * P.gravity[0];
@@ -348,7 +349,8 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
       F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
-    if (p.touched[i]) {
+    touchedNow = p.touched[i] != 0;
+    if (touchedNow) {
       p.touched[i] = 0;
       const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
       for (int e = e0; e < e1; e++) {
@@ -373,13 +375,19 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
   d3 vel = xyz(vm);
   const double4_32a w4 = p.angw[i];
+  const double4_32a& w4c = w4;
   d3 angVel = xyz(w4);
   bool angChanged = false;
   const double4_32a pr = p.posr[i];
   d3 pos = xyz(pr);
   if (!blockedAll) {
     d3 lin;
-    if (blockedNone) lin = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
+    if (blockedNone && grav && !touchedNow && P.gravAxis >= 0) {
+      // F = m g exactly: the acceleration along the gravity axis is the cached qdiv(m g, m); the other
+      // components are qdiv of signed zeros, i.e. the zeros themselves
+      lin = F;
+      if (P.gravAxis == 0) lin.x = w4c.w; else if (P.gravAxis == 1) lin.y = w4c.w; else lin.z = w4c.w;
+    } else if (blockedNone) lin = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
     else {
       lin = mk(0, 0, 0);
       if (!(flags & 1u)) lin.x = lin.x + qdiv(F.x, mass);
@@ -655,6 +663,22 @@ __global__ void k_refresh_posf(Particles p, int n) {
 }
 void launch_refresh_posf(cudaStream_t s, Particles p, int n) {
   if (n > 0) (k_refresh_posf<<<(n + 255) / 256, 256, 0, s>>>(p, n), ++::wdem::g_kernel_launches);
+}
+
+// The acceleration of a particle that only gravity acts on, qdiv(m g, m) with the integrator's own
+// operations, cached in angw.w so that the integrator does not repeat the division every step.
+__global__ void k_grav_acc(StepParams P, Particles p, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4_32a w = p.angw[i];
+  if (P.gravAxis >= 0) {
+    const double m = p.velm[i].w;
+    w.w = qdiv(m * P.gravity[P.gravAxis], m);
+  } else w.w = 0.;
+  p.angw[i] = w;
+}
+void launch_grav_acc(cudaStream_t s, const StepParams& P, Particles p, int n) {
+  if (n > 0) (k_grav_acc<<<(n + 255) / 256, 256, 0, s>>>(P, p, n), ++::wdem::g_kernel_launches);
 }
 }  // namespace wdem
 

@@ -179,6 +179,7 @@ struct wdem_handle {
   bool periodic = false;
   bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
   long long matsChecked = -1;   // material-table size the particle material indices were checked against
+  bool gravAccDirty = true;     // angw.w (cached gravity acceleration) needs recomputing
   double* dMatDt = nullptr;     // batched scenes: dt per material
   int matDtCap = 0;
   bool useMatDt = false;
@@ -445,6 +446,12 @@ void fillStepParams(wdem_handle* h) {
   P.step = h->step;
   for (int k = 0; k < 3; k++) P.gravity[k] = r.gravity[k];
   P.hasGravity = !(r.gravity[0] == 0 && r.gravity[1] == 0 && r.gravity[2] == 0);
+  {
+    int nz = 0, ax = -1;
+    for (int k = 0; k < 3; k++) if (r.gravity[k] != 0) { nz++; ax = k; }
+    P.gravAxis = (nz == 1) ? ax : -1;
+    h->gravAccDirty = true;  // recomputed before the next step (parameters change rarely)
+  }
   P.distFactor = r.distFactor;
   P.bboxFactor = r.distFactor > 0 ? r.distFactor : 1.;
   P.loneMask = r.loneMask;
@@ -742,6 +749,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   h->semi = semi;
   h->hasEll = anyEll;
   h->matsChecked = -1;
+  h->gravAccDirty = true;
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   if (n > 0) {
@@ -886,6 +894,10 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   cudaStream_t s = h->stream;
   for (int k = 0; k < 3; k++) { h->phaseMs[k] = 0; h->phaseLaunches[k] = 0; }
   h->evMarks.clear(); h->evUsed = 0;
+  if (h->gravAccDirty) {
+    launch_grav_acc(s, h->P, h->d, h->n);
+    h->gravAccDirty = false;
+  }
   for (int it = 0; it < nSteps; it++) {
     h->P.step = h->step;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);

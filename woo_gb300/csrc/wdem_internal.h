@@ -69,6 +69,7 @@ struct StepParams {
   double maxD2;             // verletDist^2
   float verletLoF;          // FP32 lower bound of verletDist (FP32 verlet trigger)
   double dampM, dampP;      // 1 - damping * 1 and 1 - damping * (-1), the nonviscDamp2nd factors
+  int gravAxis;             // the only non-zero gravity component, or -1 (angw.w then holds RN(RN(m g)/m))
   int noRatch, iniLensTouch, trsfRenorm, approxMask;
   int updatePhysNow;        // Cp2 runs on existing contacts this step (updatePhys always/once)
   int cp2, law;
@@ -175,6 +176,8 @@ void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, cons
 void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori);
 double fp64_probe(cudaStream_t s, double* scratch, int sms, float* msOut);
 void launch_refresh_posf(cudaStream_t s, Particles p, int n);
+// angw.w = RN(RN(m g[gravAxis]) / m), the acceleration of a particle under gravity alone
+void launch_grav_acc(cudaStream_t s, const StepParams& P, Particles p, int n);
 // deterministic sum of x[0..n) added to *acc (or stored, when reset): fixed-order block trees
 void energy_accumulate(cudaStream_t s, const double* x, long long n, double* partials, double* acc, bool reset);
 // ---- launchers (k_contact.cu) ----
