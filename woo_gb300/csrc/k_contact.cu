@@ -500,6 +500,8 @@ template <bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
                                                        unsigned* work, unsigned* count, DeviceStatus* st) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // the integrator's rotation list of this step has been consumed: its counter starts the next step at 0
+  if (i == 0) st->rotCount = 0;
   bool need = false;
   if (i < nc) {
     const uint8_t s0 = c.state[i];
@@ -574,7 +576,10 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
 
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
                      const uint16_t* warmBf, const float* warmF) {
-  if (nc <= 0) return;
+  if (nc <= 0) {
+    cudaMemsetAsync(&st->rotCount, 0, sizeof(unsigned), s);  // otherwise cleared by the cull kernel
+    return;
+  }
   unsigned* count = &st->workCount;
   cudaMemsetAsync(count, 0, sizeof(unsigned), s);
   const unsigned cb = (unsigned)((nc + 255) / 256);

@@ -486,7 +486,8 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
       unsigned base = 0;
       if (lane == leader) base = atomicAdd(&st->rotCount, (unsigned)__popc(b));
       base = __shfl_sync(am, base, leader);
-      if (rotate) p.rotList[base + __popc(b & ((1u << lane) - 1))] = (unsigned)i;
+      const unsigned slot = base + __popc(b & ((1u << lane) - 1));
+      if (rotate && slot < (unsigned)n) p.rotList[slot] = (unsigned)i;
     }
   }
   // aabbIsDirty (moved^2 > verletDist^2): FP32 distance of the shadows with a bound on its error
@@ -511,8 +512,8 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
 // reciprocals instead of the divisions, and for the half angles of a DEM step (|x| < 1e-3) the Taylor
 // polynomials sin x = x (1 - x^2/6 (1 - x^2/20)), cos x = 1 - x^2/2 (1 - x^2/12), whose truncation
 // errors (x^7/5040, x^6/720) are far below an ulp.
-__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const unsigned* count) {
-  const unsigned m = *count;
+__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const unsigned* count, unsigned cap) {
+  const unsigned m = *count < cap ? *count : cap;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     const unsigned i = p.rotList[k];
     const d3 angVel = xyz(p.angw[i]);
@@ -547,10 +548,10 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
   if (!fromArrays && !P.hasEll && !P.periodic && !P.lfEnergy && p.touched && p.rotList) {
-    cudaMemsetAsync(&st->rotCount, 0, sizeof(unsigned), s);
+    // st->rotCount is zero here: k_contacts_cull clears it for the next step (and the handle starts at zero)
     (k_leapfrog_fast<<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     const unsigned rb = blocks < 152 * 4 ? blocks : 152 * 4;
-    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, &st->rotCount), ++::wdem::g_kernel_launches);
+    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, &st->rotCount, (unsigned)n), ++::wdem::g_kernel_launches);
     return;
   }
   if (P.hasEll) {

@@ -898,6 +898,9 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     launch_grav_acc(s, h->P, h->d, h->n);
     h->gravAccDirty = false;
   }
+  // the integrator's rotation-list counter starts every call at zero (within a call the contact pass
+  // clears it for the next step)
+  CK(cudaMemsetAsync(&h->dst->rotCount, 0, sizeof(unsigned), s));
   for (int it = 0; it < nSteps; it++) {
     h->P.step = h->step;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
