@@ -16,6 +16,10 @@ Workloads (synthetic, seeded; no dataset is involved):
       tanPhi ~ U[.1,.8], young log-uniform in [1e6,1e8] Pa, per-scene dt, top wall at 0.05 m/s) stepped
       as one batch; "scene_by_scene" times a seeded sample of 32 of the scenes run one after another on
       their own handles and scales it to all 512.
+  peri8M -- 8,000,000 spheres, lognormal radii (median 1 mm, sigma .25, clipped [.5,2] mm) in a periodic
+      cell under simple shear (gradV rate 1/s), FrictMat E 1e8 tanPhi .5, IdealElPl; packed by periodic
+      random sequential addition at solid fraction 0.3 (the configuration's 0.62 needs a compression
+      run, not done); the stress tensor at the end of the timed steps is reported.
   spheres10k -- 10,000 monodisperse FrictMat spheres r = 5 mm in a 0.5 x 0.5 x 1 m box (CPU-runnable).
 
 A step is one pass of the hot path (Leapfrog -> collider -> ContactLoop) over all particles; the timed
@@ -44,13 +48,15 @@ sys.path.insert(0, ROOT)
 
 import numpy as np
 
-WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "batch512", "spheres10k"]
-DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "batch512": 500, "spheres10k": 2000}
+WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "batch512", "peri8M", "spheres10k"]
+DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "batch512": 500, "peri8M": 500,
+                 "spheres10k": 2000}
 METRIC = "particle-steps/s per GB300"
 DESCR = {"hertz1M": "plain DEM step, HertzDMT settling",
          "hertz1M_settled": "plain DEM step, HertzDMT, settled packing",
          "ell200k": "ellipsoid DEM step, learned warm start",
          "batch512": "512 batched oedometric scenes",
+         "peri8M": "periodic simple shear, FrictMat IdealElPl",
          "spheres10k": "plain DEM step, FrictMat IdealElPl"}
 
 
@@ -144,6 +150,8 @@ def build_scene(name, n=None):
         return scenes.hertz1M(n=n or 1_000_000)
     if name == "hertz1M_settled":
         return scenes.hertz1M(n=n or 1_000_000, height=0.95)
+    if name == "peri8M":
+        return scenes.peri_shear(n=n or 8_000_000)
     if name == "batch512":
         return scenes.batch_oedometric(n or 512, 4)
     if name == "ell200k":
@@ -220,6 +228,8 @@ def new_handle(spec, local, params=None):
     h.set_params(params or spec.params)
     h.upload_particles(spec.particles)
     h.set_params(params or spec.params)
+    if getattr(spec, "cell", None) is not None:
+        h.set_cell(**spec.cell)
     return h
 
 
@@ -431,6 +441,9 @@ def run_gpu(args, rank, world, local):
         "e2e": e2e,
         "e2e_state_roundtrip_every_step": roundtrip,
     }
+    if getattr(spec, "cell", None) is not None:
+        extra["stress_end_Pa"] = h.stress().tolist()
+        extra["packing"] = {"solid_fraction": spec.info.get("phi")}
     if "scene_by_scene" in extra:
         extra["batch_speedup_vs_scene_by_scene"] = value / extra["scene_by_scene"]["value"]
     out.update(extra)
@@ -442,7 +455,8 @@ def cpu_baseline(args, full_n):
     """OpenMP CPU restatement of Woo's step on the host cores, on a bounded cut of the workload
     (the settled workload: a cut settled on the GPU, its state and contacts handed to the CPU)."""
     from oracle import bridge
-    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "batch512": 16, "spheres10k": 10000}
+    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "batch512": 16, "peri8M": 10_000,
+            "spheres10k": 10000}
     cut = cuts[args.workload]
     spec = build_scene(args.workload, n=cut)
     contacts = None
@@ -458,7 +472,8 @@ def cpu_baseline(args, full_n):
     if args.workload == "ell200k":
         from woo_gb300 import abi
         spec.params.ellSolver = abi.ELL_BRENT   # the reference's solver
-    o = bridge.Oracle(spec.params, spec.particles, contacts=contacts, canonical=False, variant="liborc_omp.so")
+    o = bridge.Oracle(spec.params, spec.particles, contacts=contacts, canonical=False, variant="liborc_omp.so",
+                      cell=getattr(spec, "cell", None))
     o.set_parallel(True)
     o.step(2)  # initial sort + first contacts, not timed
     steps, total = 0, 0.0

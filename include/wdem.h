@@ -364,6 +364,10 @@ int wdem_launch_count(wdem_handle* h, int64_t* count);
  * (<= n; largest radii first) or a negative WDEM_ERR_*. */
 int64_t wdem_make_cloud(const double* lo, const double* hi, double rMin, double rMax, int64_t n, uint64_t seed,
                         int32_t maxAttempts, double* centers, double* radii);
+/* The same for n caller-given radii rIn (placed largest first); periodic != 0 fills the periodic box
+ * [lo, hi) with no overlap across its faces either (nearest-image test). */
+int64_t wdem_make_cloud_radii(const double* lo, const double* hi, int32_t periodic, int64_t n, const double* rIn,
+                              uint64_t seed, int32_t maxAttempts, double* centers, double* radii);
 
 #ifdef __cplusplus
 }

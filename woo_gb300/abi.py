@@ -106,7 +106,7 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
-           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read"]
+           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii"]
 
 
 def ptr(a, ctype):
@@ -262,6 +262,7 @@ def load(path=None):
         "wdem_warm_grad": ([h, F32, C.c_int64, F32, F32], C.c_int),
         "wdem_warm_train": ([h, F32, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, F32], C.c_int),
         "wdem_ell_log": ([h, C.c_int64], C.c_int),
+        "wdem_make_cloud_radii": ([D, D, C.c_int32, C.c_int64, D, C.c_uint64, C.c_int32, D, D], C.c_int64),
         "wdem_ell_log_read": ([h, F32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -482,4 +483,20 @@ def make_cloud(lo, hi, rmin, rmax, n, seed, max_attempts=200):
                             int(max_attempts), ptr(centers, C.c_double), ptr(radii, C.c_double))
     if k < 0:
         raise WdemError(int(k), "wdem_make_cloud: bad arguments")
+    return centers[:k].copy(), radii[:k].copy()
+
+
+def make_cloud_radii(lo, hi, radii_in, seed, periodic=False, max_attempts=200):
+    """Seeded non-overlapping cloud for given radii (see wdem_make_cloud_radii); returns (centers, radii)."""
+    lib = load()
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    rin = np.ascontiguousarray(radii_in, np.float64)
+    n = len(rin)
+    centers = np.zeros((n, 3))
+    radii = np.zeros(n)
+    k = lib.wdem_make_cloud_radii(ptr(lo, C.c_double), ptr(hi, C.c_double), 1 if periodic else 0, n, ptr(rin, C.c_double),
+                                  int(seed), int(max_attempts), ptr(centers, C.c_double), ptr(radii, C.c_double))
+    if k < 0:
+        raise WdemError(int(k), "wdem_make_cloud_radii: bad arguments")
     return centers[:k].copy(), radii[:k].copy()
