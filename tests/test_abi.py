@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from woo_gb300 import abi
 
@@ -61,6 +62,28 @@ def test_make_cloud_is_seeded_and_non_overlapping(wdem_lib):
     assert (d >= r1[:, None] + r1[None]).all()
     assert (c1 - r1[:, None] >= 0).all() and (c1 + r1[:, None] <= 0.1).all()
     assert abs(np.sum(np.sort(r1)[::-1] - r1)) == 0  # largest first
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_make_cloud_radii_non_overlapping(wdem_lib, periodic):
+    """Random sequential addition of given radii: seeded, no overlap (under the minimum image when periodic),
+    inside the box (centres only, when periodic)."""
+    rng = np.random.default_rng(3)
+    rin = np.sort(rng.uniform(0.02, 0.05, 300))[::-1]
+    L = 1.0
+    c1, r1 = abi.make_cloud_radii([0, 0, 0], [L, L, L], rin, 9, periodic=periodic)
+    c2, r2 = abi.make_cloud_radii([0, 0, 0], [L, L, L], rin, 9, periodic=periodic)
+    assert np.array_equal(c1, c2) and np.array_equal(r1, r2)
+    assert len(r1) > 200
+    dv = c1[:, None] - c1[None]
+    if periodic:
+        dv -= L * np.round(dv / L)
+        assert (c1 >= 0).all() and (c1 < L).all()
+    else:
+        assert (c1 - r1[:, None] >= 0).all() and (c1 + r1[:, None] <= L).all()
+    d = np.linalg.norm(dv, axis=2)
+    np.fill_diagonal(d, np.inf)
+    assert (d >= r1[:, None] + r1[None]).all()
 
 
 def test_null_arguments_are_rejected(wdem_lib):

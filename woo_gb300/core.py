@@ -7,6 +7,8 @@ GpuDemEngine built from their attributes (the drop-in replacement); any other en
 """
 import math
 
+import numpy as np
+
 from . import dem
 
 
@@ -25,8 +27,79 @@ class Labels:
             self._d[k] = v
 
 
+class Cell:
+    """Cell (src/core/Cell.hpp:22-187), homoDeform gradV2: hSize (columns = cell vectors), trsf, gradV,
+    nextGradV (the velocity gradient applied from the next step).  Read back after every run."""
+
+    _HOMO = ("none", "pos", "vel", "vel2", "gradV2")
+
+    def __init__(self):
+        self._hSize = np.eye(3)
+        self._trsf = np.eye(3)
+        self._gradV = np.zeros((3, 3))
+        self._nextGradV = np.zeros((3, 3))
+        self._homoDeform = "gradV2"
+        self._edited = True
+
+    @property
+    def homoDeform(self):
+        return self._homoDeform
+
+    @homoDeform.setter
+    def homoDeform(self, v):
+        """Cell::homoDeform (Cell.hpp:135): only the default gradV2 integration is provided."""
+        v = self._HOMO[v] if isinstance(v, int) else str(v)
+        if v not in self._HOMO:
+            raise ValueError(f"Cell.homoDeform: unknown mode {v!r}")
+        if v != "gradV2":
+            raise RuntimeError(f"Cell.homoDeform={v!r} is not supported (only 'gradV2')")
+        self._homoDeform = v
+
+    def _prop(name):
+        def get(self):
+            return getattr(self, "_" + name).copy()
+
+        def set_(self, v):
+            m = np.asarray(v, np.float64).reshape(3, 3).copy()
+            if name == "hSize" and np.linalg.det(m) <= 0:
+                # Cell::setHSize / integrateAndUpdate: a degenerate (or inverted) cell is an error
+                raise RuntimeError("Cell.hSize: degenerate or inverted cell (det(hSize) <= 0)")
+            setattr(self, "_" + name, m)
+            self._edited = True
+        return property(get, set_)
+
+    hSize = _prop("hSize")
+    trsf = _prop("trsf")
+    gradV = _prop("gradV")
+    nextGradV = _prop("nextGradV")
+    del _prop
+
+    def setBox(self, *box):
+        """Cell.setBox: rectangular cell of the given size."""
+        size = box[0] if len(box) == 1 else box
+        self.hSize = np.diag(np.asarray(size, np.float64).reshape(3))
+
+    @property
+    def hSize0(self):
+        """Reference cell: trsf^-1 · hSize."""
+        return np.linalg.solve(self._trsf, self._hSize)
+
+    @property
+    def size(self):
+        return np.linalg.norm(self._hSize, axis=0)
+
+    @property
+    def volume(self):
+        return float(np.linalg.det(self._hSize))
+
+    def _sync(self, d):
+        self._hSize, self._trsf, self._gradV = d["hSize"], d["trsf"], d["gradV"]
+        self._nextGradV = d["nextGradV"]
+        self._edited = False
+
+
 class Scene:
-    """Scene (src/core/Scene.hpp:191-205 attributes dt, dtSafety, step, time, trackEnergy)."""
+    """Scene (src/core/Scene.hpp:191-205 attributes dt, dtSafety, step, time, trackEnergy, isPeriodic, cell)."""
 
     def __init__(self, fields=None, engines=None, dt=float("nan"), dtSafety=0.9, trackEnergy=False):
         self.fields = list(fields or [])
@@ -38,6 +111,8 @@ class Scene:
         self.trackEnergy = bool(trackEnergy)
         self.lab = Labels()
         self._gpu = None
+        self.periodic = False
+        self.cell = Cell()
         self.engines = list(engines or [])
         for f in self.fields:
             f.scene = self

@@ -89,6 +89,12 @@ class DemData:
     mass = property(lambda s: float(s._get("mass")), lambda s, v: s._set("mass", float(v)))
     inertia = property(lambda s: s._get("inertia"), lambda s, v: s._set("inertia", _vec3(v)))
     flags = property(lambda s: int(s._get("flags")), lambda s, v: s._set("flags", int(v)))
+    angMom = property(lambda s: s._get("angMom"), lambda s, v: s._set("angMom", _vec3(v)))
+
+    @property
+    def isAspherical(self):
+        i = self.inertia
+        return not (i[0] == i[1] and i[1] == i[2])
 
     @property
     def blocked(self):
@@ -120,7 +126,8 @@ class Node:
 
     def __init__(self, pos=(0, 0, 0), ori=(1, 0, 0, 0)):
         self._local = dict(pos=_vec3(pos), ori=_quat(ori), vel=np.zeros(3), angVel=np.zeros(3),
-                           force=np.zeros(3), torque=np.zeros(3), mass=0.0, inertia=np.zeros(3), flags=0)
+                           force=np.zeros(3), torque=np.zeros(3), mass=0.0, inertia=np.zeros(3), flags=0,
+                           angMom=np.full(3, nan))
         self._field = None
         self._idx = -1
         self.dem = DemData(self)
@@ -205,6 +212,42 @@ class Wall(Shape):
         n.dem.mass = float(mass)
         if fixed:
             n.dem.blocked = "xyzXYZ"
+        return p
+
+
+class Ellipsoid(Shape):
+    """Ellipsoid (src/dem/Ellipsoid.hpp:11-40): semiAxes; mass and inertia from
+    Ellipsoid::lumpMassInertia (Ellipsoid.cpp:37-44)."""
+    _shape = abi.SHAPE_ELLIPSOID
+
+    def __init__(self, semiAxes=(nan, nan, nan)):
+        super().__init__()
+        self.semiAxes = _vec3(semiAxes)
+
+    def equivRadius(self):
+        return float(np.cbrt(self.semiAxes[0] * self.semiAxes[1] * self.semiAxes[2]))
+
+    def volume(self):
+        return (4 / 3.0) * math.pi * float(self.semiAxes[0] * self.semiAxes[1] * self.semiAxes[2])
+
+    @staticmethod
+    def make(center, semiAxes, ori=(1, 0, 0, 0), mat=None, fixed=False, mask=DEFAULT_MOVABLE_MASK, vel=None):
+        """Ellipsoid.make (py/_monkey/... ; the reference's Shape::make + lumpMassInertia)."""
+        from . import scenes
+        mat = mat if mat is not None else defaultMaterial()
+        sh = Ellipsoid(semiAxes)
+        if not np.all(sh.semiAxes > 0):
+            raise RuntimeError("Ellipsoid: all semi-principal semiAxes must be positive")
+        n = Node(pos=center, ori=ori)
+        sh.nodes.append(n)
+        p = Particle(shape=sh, material=mat, mask=mask)
+        m, inertia = scenes.ellipsoid_mass_inertia(sh.semiAxes[None, :], mat.density)
+        n.dem.mass = float(m[0])
+        n.dem.inertia = inertia[0]
+        if fixed:
+            n.dem.blocked = "xyzXYZ"
+        if vel is not None:
+            n.dem.vel = vel
         return p
 
 
@@ -315,8 +358,15 @@ class Contact:
         self.minDist00Sq = float(ca.minDist00Sq[i])
         if self.real:
             pa, pb = field.par[self.id1], field.par[self.id2]
-            r1 = -pb.shape.radius if isinstance(pa.shape, Wall) else pa.shape.radius
-            r2 = pb.shape.radius
+            if isinstance(pa.shape, Sphere) and isinstance(pb.shape, Sphere) or \
+                    isinstance(pa.shape, Wall) and isinstance(pb.shape, Sphere):
+                r1 = -pb.shape.radius if isinstance(pa.shape, Wall) else pa.shape.radius
+                r2 = pb.shape.radius
+            else:
+                # ellipsoid functors: distances of the contact point from the centres (Ellipsoid.cpp:250, 349)
+                cp = ca.contPt[i]
+                r2 = float(np.linalg.norm(cp - pb.pos))
+                r1 = -r2 if isinstance(pa.shape, Wall) else float(np.linalg.norm(cp - pa.pos))
             lens = np.array([abs(r1), abs(r2)])
             rr = min(r1, r2) if (r1 > 0 and r2 > 0) else (r1 if r1 > 0 else r2)
             self.geom = L6Geom(float(ca.uN[i]), ca.geomVel[i].copy(), ca.geomAngVel[i].copy(), ca.trsf[i],
@@ -391,7 +441,7 @@ class ContactContainer:
 
 
 # ---------------------------------------------------------------------------------------- field
-_FIELD_ARRAY_NAMES = ("pos", "ori", "vel", "angVel", "force", "torque", "mass", "inertia", "flags")
+_FIELD_ARRAY_NAMES = ("pos", "ori", "vel", "angVel", "force", "torque", "mass", "inertia", "flags", "angMom")
 
 
 class DemField:
@@ -457,8 +507,15 @@ class DemField:
         """DemField::critDt -> DemFuncs::pWaveDt (src/dem/Particle.cpp:399-404, src/dem/Funcs.cpp:151-175)."""
         dt = math.inf
         for p in self.par:
-            if isinstance(p.shape, Sphere) and isinstance(p.material, ElastMat):
-                dt = min(dt, p.shape.radius / (1.0 * math.sqrt(p.material.young / p.material.density)))
+            if not isinstance(p.material, ElastMat):
+                continue
+            if isinstance(p.shape, Sphere):
+                r = p.shape.radius
+            elif isinstance(p.shape, Ellipsoid):
+                r = float(np.min(p.shape.semiAxes))
+            else:
+                continue
+            dt = min(dt, r / (1.0 * math.sqrt(p.material.young / p.material.density)))
         return dt
 
     @staticmethod
@@ -503,6 +560,27 @@ class Cg2_Sphere_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
 
 class Cg2_Wall_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
     """Cg2_Wall_Sphere_L6Geom (src/dem/Wall.cpp:50-84)."""
+
+
+class Bo1_Ellipsoid_Aabb(BoundFunctor):
+    """Bo1_Ellipsoid_Aabb (src/dem/Ellipsoid.hpp:44-51)."""
+
+
+class Cg2_Ellipsoid_Ellipsoid_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Ellipsoid_Ellipsoid_L6Geom (src/dem/Ellipsoid.hpp:52-62): brent, brentBits.  brent=False selects
+    the Newton solve (unimplemented in the reference), converged to newtonTol, started from warmStart
+    'cold' | 'history' | 'mlp' (warmStartWeights: the learned network's WDEM_WARM_NPARAM weights), falling
+    back to the cold start after fallbackIters iterations."""
+    _defaults = dict(brent=True, brentBits=32, newtonTol=1e-10, warmStart="cold", fallbackIters=4,
+                     warmStartWeights=None)
+
+
+class Cg2_Sphere_Ellipsoid_L6Geom(Cg2_Ellipsoid_Ellipsoid_L6Geom):
+    """Cg2_Sphere_Ellipsoid_L6Geom (src/dem/Ellipsoid.hpp:64-72)."""
+
+
+class Cg2_Wall_Ellipsoid_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Wall_Ellipsoid_L6Geom (src/dem/Ellipsoid.hpp:74-81)."""
 
 
 class CPhysFunctor(Functor):
@@ -616,7 +694,11 @@ class GpuDemEngine(Engine):
         return None
 
     def _build_params(self, scene, field):
-        geo = self._functor(self.geoFunctors, (Cg2_Sphere_Sphere_L6Geom, Cg2_Wall_Sphere_L6Geom)) or Cg2_Sphere_Sphere_L6Geom()
+        geo = self._functor(self.geoFunctors, (Cg2_Any_Any_L6Geom__Base,)) or Cg2_Sphere_Sphere_L6Geom()
+        if any(isinstance(p.shape, Ellipsoid) for p in field.par) and \
+                self._functor(self.geoFunctors, (Cg2_Ellipsoid_Ellipsoid_L6Geom,)) is None:
+            raise RuntimeError("ellipsoids in the scene need Cg2_Ellipsoid_Ellipsoid_L6Geom (or its sphere variant) "
+                               "in ContactLoop.geoFunctors")
         cp2 = self._functor(self.phyFunctors, (Cp2_HertzMat_HertzPhys,)) or self._functor(self.phyFunctors, (Cp2_FrictMat_FrictPhys,))
         law = self._functor(self.lawFunctors, (Law2_L6Geom_HertzPhys_DMT,)) or self._functor(self.lawFunctors, (Law2_L6Geom_FrictPhys_IdealElPl,))
         if cp2 is None or law is None:
@@ -671,6 +753,14 @@ class GpuDemEngine(Engine):
             p.noAttraction = 1
         p.nMaterials = len(mlist)
         p.materials = arr
+        ell = self._functor(self.geoFunctors, (Cg2_Ellipsoid_Ellipsoid_L6Geom,))
+        p.ellSolver = abi.ELL_BRENT if (ell is None or ell.brent) else abi.ELL_NEWTON
+        p.brentBits = int(ell.brentBits) if ell is not None else 32
+        p.newtonTol = float(ell.newtonTol) if ell is not None else 1e-10
+        p.warmStart = {"cold": abi.WARM_COLD, "history": abi.WARM_HISTORY, "mlp": abi.WARM_MLP}[
+            ell.warmStart if ell is not None else "cold"]
+        p.fallbackIters = int(ell.fallbackIters) if ell is not None else 4
+        self._ellFunctor = ell
         return p
 
     def _pack(self, field):
@@ -683,6 +773,8 @@ class GpuDemEngine(Engine):
                 pa.shape[i] = abi.SHAPE_SPHERE; pa.radius[i] = sh.radius
             elif isinstance(sh, Wall):
                 pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
+            elif isinstance(sh, Ellipsoid):
+                pa.shape[i] = abi.SHAPE_ELLIPSOID; pa.semiAxes[i] = sh.semiAxes
             else:
                 raise RuntimeError(f"GpuDemEngine: unsupported shape {type(sh).__name__}")
             pa.material[i] = self._mat_index[id(p.material)]
@@ -706,6 +798,14 @@ class GpuDemEngine(Engine):
         h.set_params(params)
         h.upload_particles(pa)
         h.set_params(params)
+        if getattr(scene, "periodic", False):
+            c = scene.cell
+            h.set_cell(c.hSize, c.trsf, c.gradV, c.nextGradV)
+        ell = getattr(self, "_ellFunctor", None)
+        if ell is not None and ell.warmStart == "mlp":
+            if ell.warmStartWeights is None:
+                raise RuntimeError("Cg2_Ellipsoid_Ellipsoid_L6Geom.warmStart='mlp' needs warmStartWeights")
+            h.warm_set_weights(ell.warmStartWeights)
         self._h, self._params, self._field = h, params, field
         field._bind(self, pa)
 
@@ -740,7 +840,15 @@ class GpuDemEngine(Engine):
         self._h.set_params(p)
         field._stale = True
         field._con_cache = None
+        if getattr(scene, "periodic", False):
+            c = scene.cell
+            if c._edited:
+                self._h.set_cell(c.hSize, c.trsf, c.gradV, c.nextGradV)
+                c._edited = False
         self._h.step(nSteps)
+        if getattr(scene, "periodic", False):
+            cc = self._h.cell()
+            scene.cell._sync(cc)
         if up == abi.UPDATE_PHYS_ONCE:
             self.updatePhys = "never"
             if getattr(self, "_sources", None):
