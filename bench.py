@@ -18,8 +18,9 @@ Workloads (synthetic, seeded; no dataset is involved):
       their own handles and scales it to all 512.
   peri8M -- 8,000,000 spheres, lognormal radii (median 1 mm, sigma .25, clipped [.5,2] mm) in a periodic
       cell under simple shear (gradV rate 1/s), FrictMat E 1e8 tanPhi .5, IdealElPl; packed by periodic
-      random sequential addition at solid fraction 0.3 (the configuration's 0.62 needs a compression
-      run, not done); the stress tensor at the end of the timed steps is reported.
+      random sequential addition at solid fraction 0.3, then densified to 0.62 on the GPU (radius growth
+      with damping, scaled back to the original radii; untimed); the stress tensor at the
+      end of the timed steps is reported.
   spheres10k -- 10,000 monodisperse FrictMat spheres r = 5 mm in a 0.5 x 0.5 x 1 m box (CPU-runnable).
 
 A step is one pass of the hot path (Leapfrog -> collider -> ContactLoop) over all particles; the timed
@@ -70,6 +71,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--queue-depth", type=int, default=None,
+                    help="steps queued before the host checks the collider trigger (engine default 32; 1 = every step)")
     ap.add_argument("--n", type=int, default=None,
                     help="particle count of a smaller cut of the workload (same density; for profiling runs)")
     a = ap.parse_args()
@@ -151,7 +154,7 @@ def build_scene(name, n=None):
     if name == "hertz1M_settled":
         return scenes.hertz1M(n=n or 1_000_000, height=0.95)
     if name == "peri8M":
-        return scenes.peri_shear(n=n or 8_000_000)
+        return scenes.densify_periodic(scenes.peri_shear(n=n or 8_000_000), phi_target=0.62)
     if name == "batch512":
         return scenes.batch_oedometric(n or 512, 4)
     if name == "ell200k":
@@ -222,9 +225,14 @@ def timed_steps(h, stream, k, world, local, barrier):
     return float(t.item())
 
 
+QUEUE_DEPTH = None
+
+
 def new_handle(spec, local, params=None):
     from woo_gb300 import abi
     h = abi.Handle(spec.particles.n, device=local)
+    if QUEUE_DEPTH is not None:
+        h.set_queue_depth(QUEUE_DEPTH)
     h.set_params(params or spec.params)
     h.upload_particles(spec.particles)
     h.set_params(params or spec.params)
@@ -347,9 +355,15 @@ def run_gpu(args, rank, world, local):
     value = world * n * args.steps / (ms_max / 1e3)
     # per-phase CUDA-event times (leapfrog, collider, contacts) from a following window of the same run;
     # kept out of the timed region above so that the extra events do not slow it
+    # (the window is also the cudaProfilerStart/Stop range: `ncu --profile-from-start off` captures
+    # these launches only, at the state the timed region ended in)
     kw = min(args.steps, 2000)
     h.set_timing(True)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
     h.step(kw)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     kt = h.kernel_times()
     h.set_timing(False)
 
@@ -430,7 +444,8 @@ def run_gpu(args, rank, world, local):
         "dtype": "f64", "data": "synthetic (seeded random sequential addition packing)",
         "config": {"workload": args.workload, "n_particles": n, "dt": spec.params.dt,
                    "parallelism": f"replicas x{world}", "l2": "state larger than L2 (no flush needed)",
-                   "steps_simulated_before_timing": int(max(args.warmup, 3)) + settled_steps},
+                   "steps_simulated_before_timing": int(max(args.warmup, 3)) + settled_steps,
+                   "queue_depth": 32 if args.queue_depth is None else args.queue_depth},
         "gpu_launches": int(launches),
         "kernels": {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / max(v[1], 1)} for k, v in kt.items()},
         "kernels_window_steps": kw,
@@ -503,7 +518,9 @@ def read_profile_figures(path):
 
 
 def main():
+    global QUEUE_DEPTH
     args = parse()
+    QUEUE_DEPTH = args.queue_depth
     rank, world, local = dist_env()
     if args.impl == "reference":
         if rank != 0:

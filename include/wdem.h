@@ -275,6 +275,14 @@ int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* l
 /* Enable/disable per-kernel CUDA-event timing inside wdem_step (off by default). */
 int wdem_set_timing(wdem_handle* h, int32_t enable);
 
+/* Steps that wdem_step may queue on the device before it checks the collider trigger on the host
+ * (default 32; 0 or 1 = check after every integrator pass).  Queued kernels guard themselves: once
+ * the integrator of a step raises the trigger, the rest of the queue does nothing, and the host
+ * rebuilds and finishes that step exactly as with one step per check, so results do not depend on
+ * the depth.  No counterpart in the reference, whose loop checks in every step
+ * (InsertionSortCollider::run, InsertionSortCollider.cpp:386-400). */
+int wdem_set_queue_depth(wdem_handle* h, int32_t depth);
+
 /* Keep L6Geom.uN, L6Geom.vel and L6Geom.angVel of every real contact so that
  * wdem_download_contacts can return them (off by default: they are per-step values that Woo keeps
  * in the contact's CGeom object; storing them costs 56 bytes per contact per step). */

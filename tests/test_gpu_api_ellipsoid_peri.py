@@ -85,8 +85,9 @@ def test_periodic_shear_script(wdem_lib, shear):
         assert np.array_equal(vel, po.vel), "velocities differ"
         oc = o.cell()
         assert np.array_equal(S.cell.hSize, oc["hSize"]) and np.array_equal(S.cell.trsf, oc["trsf"])
-    assert len(S.dem.con) == int(np.count_nonzero(o.contacts().real))
-    assert len(S.dem.con) > 0
+    oc = o.contacts()
+    assert len(S.dem.con) == oc.n
+    assert S.dem.con.countReal() == int(np.count_nonzero(oc.real)) > 0
     if shear:
         assert 0 < S.cell.hSize[0, 2] <= 200 * S.dt * shear * 4 * (1 + 1e-12)
         assert np.array_equal(S.cell.gradV, S.cell.nextGradV)

@@ -101,3 +101,40 @@ def test_periodic_rejects_walls(wdem_lib):
     h = gpu_handle(spec)
     with pytest.raises(abi.WdemError):
         h.set_cell(np.eye(3))
+
+
+@pytest.mark.parametrize("damping", [0.0, 0.3])
+def test_periodic_damped_changing_gradient(wdem_lib, damping):
+    """Damping on the fluctuation velocity and spin, and a velocity gradient that changes between
+    steps (L+ != L-, non-zero deltaSpinVec): bitwise against the oracle."""
+    spec = scenes.periodic_cloud(400, 11, law="frict", shear=0.1, rate=3.0, damping=damping)
+    n = spec.particles.n
+    h = gpu_handle(spec)
+    o = bridge.Oracle(spec.params, spec.particles, cell=spec.cell)
+    rng = np.random.default_rng(2)
+    for chunk in (1, 20, 40, 100):
+        h.step(chunk)
+        o.step(chunk)
+        _check_same(h, o, n)
+        g = rng.normal(0, 2.0, (3, 3))
+        c = o.cell()
+        h.set_cell(c["hSize"], c["trsf"], c["gradV"], g)
+        o.set_cell(c["hSize"], c["trsf"], c["gradV"], g)
+    assert np.array_equal(h.cell()["hSize"], o.cell()["hSize"])
+
+
+def test_densified_periodic_packing(wdem_lib):
+    """Radius-growth densification of a loose periodic packing on the GPU: the target solid fraction,
+    the original radii, real contacts, and then the sheared dense packing bitwise against the oracle."""
+    loose = scenes.peri_shear(n=3000, seed=3)
+    spec = scenes.densify_periodic(loose, phi_target=0.62, stages=8, steps_per_stage=100, relax=200)
+    assert spec.info["phi"] == pytest.approx(0.62, rel=1e-9)
+    assert np.array_equal(spec.particles.radius, loose.particles.radius)
+    n = spec.particles.n
+    h = gpu_handle(spec)
+    o = bridge.Oracle(spec.params, spec.particles, cell=spec.cell)
+    for chunk in (1, 30, 120):
+        h.step(chunk)
+        o.step(chunk)
+        cg = _check_same(h, o, n)
+    assert int(cg.real.sum()) > n

@@ -102,7 +102,7 @@ class Status(C.Structure):
 EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params", "wdem_upload_particles",
            "wdem_upload_contacts", "wdem_step", "wdem_download_particles", "wdem_contact_count",
            "wdem_download_contacts", "wdem_crit_dt", "wdem_get_energy", "wdem_reset_energy", "wdem_get_status",
-           "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_keep_geom",
+           "wdem_last_error", "wdem_collide_boxes", "wdem_kernel_times", "wdem_set_timing", "wdem_set_queue_depth", "wdem_keep_geom",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
@@ -244,6 +244,7 @@ def load(path=None):
         "wdem_collide_boxes": ([h, C.c_int32, D, D, U32, C.c_uint32, I32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "wdem_kernel_times": ([h, C.POINTER(C.c_char_p), D, I32, C.c_int32, I32], C.c_int),
         "wdem_set_timing": ([h, C.c_int32], C.c_int),
+        "wdem_set_queue_depth": ([h, C.c_int32], C.c_int),
         "wdem_keep_geom": ([h, C.c_int32], C.c_int),
         "wdem_make_cloud": ([D, D, C.c_double, C.c_double, C.c_int64, C.c_uint64, C.c_int32, D, D], C.c_int64),
         "wdem_get_stream": ([h, C.POINTER(C.c_void_p)], C.c_int),
@@ -345,6 +346,10 @@ class Handle:
 
     def set_timing(self, on):
         self.check(self.lib.wdem_set_timing(self.h, 1 if on else 0))
+
+    def set_queue_depth(self, depth):
+        """Steps queued before the host checks the collider trigger (1 = every step)."""
+        self.check(self.lib.wdem_set_queue_depth(self.h, int(depth)))
 
     def keep_geom(self, on):
         self.check(self.lib.wdem_keep_geom(self.h, 1 if on else 0))

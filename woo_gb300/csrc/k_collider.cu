@@ -498,8 +498,25 @@ __global__ void k_retain_flag(StepParams P, Particles p, Contacts old, long long
     int2 id = old.ids[c];
     bool ov;
     if (P.periodic) {
-      int4 per; bool amb = false;
-      ov = overlapPeri(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y], P.csize, per, amb);
+      const double4_32a mn1 = p.bbmin[id.x], mx1 = p.bbmax[id.x], mn2 = p.bbmin[id.y], mx2 = p.bbmax[id.y];
+      // boxes that overlap on every axis by more than the FP32 margin (and are narrow enough that no
+      // ambiguity exists) overlap in the exact test too
+      const double lo1[3] = {mn1.x, mn1.y, mn1.z}, hi1[3] = {mx1.x, mx1.y, mx1.z};
+      const double lo2[3] = {mn2.x, mn2.y, mn2.z}, hi2[3] = {mx2.x, mx2.y, mx2.z};
+      bool sure = true;
+      for (int k = 0; k < 3 && sure; k++) {
+        const double L = P.csize[k];
+        const double ca = .5 * (lo1[k] + hi1[k]), cb = .5 * (lo2[k] + hi2[k]);
+        const double ha = .5 * (hi1[k] - lo1[k]), hb = .5 * (hi2[k] - lo2[k]);
+        if (!(ha < .25 * L) || !(hb < .25 * L)) { sure = false; break; }
+        const float Lf = (float)L;
+        sure = periNear((float)(ca - floor(ca / L) * L), (float)ha, (float)(cb - floor(cb / L) * L), (float)hb, Lf, 1.f / Lf);
+      }
+      if (sure) ov = true;
+      else {
+        int4 per; bool amb = false;
+        ov = overlapPeri(mn1, mx1, mn2, mx2, P.csize, per, amb);
+      }
     } else ov = overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y]);
     if (!ov) f = 1;
   }
@@ -686,7 +703,9 @@ __global__ void k_keys_peri(StepParams P, Particles p, const int* small, int nSm
   vals[k] = (unsigned)i;
 }
 
-__global__ void k_cell_start_plain(const unsigned long long* keys, int nSmall, long long ncells, int* cellStart) {
+// cellStart[c] = first sorted position of cell c, for the grid's own cells (nc0 nc1 nc2 + 1 entries)
+__global__ void k_cell_start_plain(const unsigned long long* keys, int nSmall, const PeriGrid* g, int* cellStart) {
+  const long long ncells = (long long)g->nc[0] * g->nc[1] * g->nc[2];
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (nSmall == 0) {
     for (long long k = s; k <= ncells; k += (long long)gridDim.x * blockDim.x) cellStart[k] = 0;
@@ -700,52 +719,117 @@ __global__ void k_cell_start_plain(const unsigned long long* keys, int nSmall, l
     for (long long k = c + 1; k <= ncells; k++) cellStart[k] = nSmall;
 }
 
-template <bool WRITE>
-__global__ void k_pairs_peri(StepParams P, Particles p, const int* small, int nSmall, const PeriGrid* g,
-                             const unsigned* vals, const int* cellStart, unsigned* counts, int2* out, int4* outDist,
-                             long long cap, DeviceStatus* st) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k > nSmall) return;
-  if (k == nSmall) { if (!WRITE) counts[k] = 0; return; }
-  const PeriGrid G = *g;
-  const int i = small[k];
-  const int4 mi = p.meta[i];
+// FP32 copies, in cell order, of each box's centre wrapped into the cell and of its half-widths: the
+// candidate loop rejects with them the pairs whose minimum-image centre distance exceeds the sum of
+// the half-widths by more than the rounding of these copies on some axis.  Such boxes are disjoint on
+// that axis for every period shift, so spatialOverlapPeri rejects them too, and it is evaluated (in
+// FP64, as the reference does) only for the survivors.  Boxes wider than a quarter of the cell skip
+// the filter (there the exact test may find an ambiguous contact, which is an error to report).
+__global__ void k_peri_sorted(StepParams P, Particles p, const unsigned* vals, int nSmall, float4* pc, float4* ph) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nSmall) return;
+  const int i = (int)vals[q];
   const double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+  const double lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+  float c[3], h[3];
+  bool wide = false;
+  for (int k = 0; k < 3; k++) {
+    const double L = P.csize[k];
+    const double ctr = .5 * (lo[k] + hi[k]), half = .5 * (hi[k] - lo[k]);
+    const double w = ctr - floor(ctr / L) * L;
+    c[k] = (float)w;
+    h[k] = (float)half;
+    wide |= !(half < .25 * L);  // also catches infinite and NaN extents
+  }
+  pc[q] = make_float4(c[0], c[1], c[2], 0.f);
+  ph[q] = make_float4(h[0], h[1], h[2], wide ? 1.f : 0.f);
+}
+
+
+
+// Candidate pass: thread q takes the q-th box in cell order and runs the FP32 filter against the boxes
+// of the 27 neighbouring cells (wrapped, each cell once) with a larger particle id; it counts (WRITE
+// false) or writes (WRITE true, at its scanned offset) the survivors.  The exact FP64 test runs in a
+// separate dense pass (k_peri_exact): inside this loop the survivors of one warp's 32 boxes differ per
+// lane, and the FP64 test would run with a few lanes at a time.
+template <bool WRITE>
+__global__ void k_peri_cand(StepParams P, int nSmall, const PeriGrid* g, const unsigned long long* keys,
+                            const unsigned* vals, const float4* pc, const float4* ph, const int* cellStart,
+                            unsigned* counts, int2* cand, long long cap) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q > nSmall) return;
+  if (q == nSmall) { if (!WRITE) counts[q] = 0; return; }
+  const PeriGrid G = *g;
+  const int i = (int)vals[q];
+  const float4 c1 = pc[q], h1 = ph[q];
+  const float L0 = (float)P.csize[0], L1 = (float)P.csize[1], L2 = (float)P.csize[2];
+  const float iL0 = 1.f / L0, iL1 = 1.f / L1, iL2 = 1.f / L2;
+  const long long key0 = (long long)keys[q];
   int c[3];
-  periCell(mn, mx, P, G, c);
+  c[0] = (int)(key0 % G.nc[0]);
+  c[1] = (int)((key0 / G.nc[0]) % G.nc[1]);
+  c[2] = (int)(key0 / ((long long)G.nc[0] * G.nc[1]));
+  // neighbouring cells per axis, each index once (axes of one or two cells have fewer)
+  int nbr[3][3], nn[3];
+  for (int a = 0; a < 3; a++) {
+    nn[a] = 0;
+    for (int d = -1; d <= 1; d++) {
+      const int v = ((c[a] + d) % G.nc[a] + G.nc[a]) % G.nc[a];
+      bool dup = false;
+      for (int b = 0; b < nn[a]; b++) dup |= (nbr[a][b] == v);
+      if (!dup) nbr[a][nn[a]++] = v;
+    }
+  }
   unsigned cnt = 0;
-  unsigned long long base = WRITE ? counts[k] : 0;
-  long long seen[27];
-  int nseen = 0;
-  for (int dz = -1; dz <= 1; dz++)
-    for (int dy = -1; dy <= 1; dy++)
-      for (int dx = -1; dx <= 1; dx++) {
-        int cc[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
-        for (int q = 0; q < 3; q++) cc[q] = ((cc[q] % G.nc[q]) + G.nc[q]) % G.nc[q];
-        const long long key = ((long long)cc[2] * G.nc[1] + cc[1]) * G.nc[0] + cc[0];
-        bool dup = false;
-        for (int q = 0; q < nseen; q++) dup |= (seen[q] == key);
-        if (dup) continue;
-        seen[nseen++] = key;
+  const unsigned long long base = WRITE ? counts[q] : 0;
+  for (int az = 0; az < nn[2]; az++)
+    for (int ay = 0; ay < nn[1]; ay++)
+      for (int ax = 0; ax < nn[0]; ax++) {
+        const long long key = ((long long)nbr[2][az] * G.nc[1] + nbr[1][ay]) * G.nc[0] + nbr[0][ax];
         const int beg = cellStart[key], end = cellStart[key + 1];
-        for (int q = beg; q < end; q++) {
-          const int j = (int)vals[q];
+        for (int q2 = beg; q2 < end; q2++) {
+          const int j = (int)vals[q2];
           if (j <= i) continue;
-          const int4 mj = p.meta[j];
-          int4 per;
-          bool amb = false;
-          const bool ov = overlapPeri(mn, mx, p.bbmin[j], p.bbmax[j], P.csize, per, amb);
-          if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = i; continue; }
-          if (!ov) continue;
-          if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, P.loneMask)) continue;
+          const float4 h2 = ph[q2];
+          if (h1.w == 0.f && h2.w == 0.f) {
+            const float4 c2 = pc[q2];
+            if (periFar(c1.x, h1.x, c2.x, h2.x, L0, iL0) || periFar(c1.y, h1.y, c2.y, h2.y, L1, iL1) ||
+                periFar(c1.z, h1.z, c2.z, h2.z, L2, iL2))
+              continue;
+          }
           if (WRITE) {
-            unsigned long long o = base + cnt;
-            if (o < (unsigned long long)cap) { out[o] = make_int2(i, j); outDist[o] = per; }
+            const unsigned long long o = base + cnt;
+            if (o < (unsigned long long)cap) cand[o] = make_int2(i, j);
           }
           cnt++;
         }
       }
-  if (!WRITE) counts[k] = cnt;
+  if (!WRITE) counts[q] = cnt;
+}
+
+// Exact pass, one thread per candidate: spatialOverlapPeri (FP64, the reference's operations; an
+// ambiguous contact is an error) and Collider::mayCollide.
+__global__ void k_peri_exact(StepParams P, Particles p, const int2* cand, long long nc, unsigned* flag, int4* per,
+                             DeviceStatus* st) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc) return;
+  const int2 ij = cand[k];
+  int4 pr = make_int4(0, 0, 0, 0);
+  bool amb = false;
+  bool ok = overlapPeri(p.bbmin[ij.x], p.bbmax[ij.x], p.bbmin[ij.y], p.bbmax[ij.y], P.csize, pr, amb);
+  if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = ij.x; ok = false; }
+  if (ok) ok = mayCollide((unsigned)p.meta[ij.x].z, (unsigned)p.meta[ij.y].z, P.loneMask);
+  flag[k] = ok ? 1u : 0u;
+  per[k] = pr;
+}
+
+// the accepted candidates, in candidate order, with their cellDist
+__global__ void k_peri_emit(const int2* cand, const int4* per, const unsigned* flagScan, long long nc, int2* out,
+                            int4* outDist, long long cap) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nc || flagScan[k + 1] == flagScan[k]) return;
+  const long long o = flagScan[k];
+  if (o < cap) { out[o] = cand[k]; outDist[o] = per[k]; }
 }
 
 // ------------------------------------------------------------------------------------ stress
@@ -817,9 +901,12 @@ void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScra
   if (nOld > 0) (k_retain_write<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(old, nOld, cs.retainFlag, out, base, cap), ++::wdem::g_kernel_launches);
 }
 
-void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall, ColliderScratch& cs,
-                  int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st) {
+// periodic pair search, part 1: grid, cell sort, FP32 candidates counted (write false; counts
+// scanned, total at counts[nSmall + 1]) or written (write true)
+void col_periodic_cand(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall,
+                       ColliderScratch& cs, bool write) {
   PeriGrid* g = (PeriGrid*)((char*)cs.temp + 256);
+  const int threads = nSmall + 1;
   if (!write) {
     unsigned long long* ext = (unsigned long long*)cs.temp;
     (k_extents_init<<<1, 32, 0, s>>>(ext), ++::wdem::g_kernel_launches);
@@ -827,12 +914,26 @@ void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* s
     (k_grid_peri<<<1, 1, 0, s>>>(ext, P, cs.maxCols, g), ++::wdem::g_kernel_launches);
     if (nSmall > 0) (k_keys_peri<<<(nSmall + 255) / 256, 256, 0, s>>>(P, p, small, nSmall, g, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
     radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bitsFor((unsigned long long)cs.maxCols + 1), cs);
-    int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
-    (k_cell_start_plain<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.maxCols, cs.cellStart), ++::wdem::g_kernel_launches);
+    int t = nSmall > 0 ? nSmall : (cs.maxCols + 1);
+    (k_cell_start_plain<<<(t + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, g, cs.cellStart), ++::wdem::g_kernel_launches);
+    if (nSmall > 0) (k_peri_sorted<<<(nSmall + 255) / 256, 256, 0, s>>>(P, p, cs.vals, nSmall, cs.periC, cs.periH), ++::wdem::g_kernel_launches);
+    (k_peri_cand<false><<<(threads + 127) / 128, 128, 0, s>>>(P, nSmall, g, cs.keys, cs.vals, cs.periC, cs.periH, cs.cellStart, cs.counts, nullptr, 0), ++::wdem::g_kernel_launches);
+    exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
+  } else {
+    (k_peri_cand<true><<<(threads + 127) / 128, 128, 0, s>>>(P, nSmall, g, cs.keys, cs.vals, cs.periC, cs.periH, cs.cellStart, cs.counts, cs.cand, cs.candCap), ++::wdem::g_kernel_launches);
   }
-  const int threads = nSmall + 1;
-  if (write) (k_pairs_peri<true><<<(threads + 127) / 128, 128, 0, s>>>(P, p, small, nSmall, g, cs.vals, cs.cellStart, cs.counts, out, outDist, cap, st), ++::wdem::g_kernel_launches);
-  else (k_pairs_peri<false><<<(threads + 127) / 128, 128, 0, s>>>(P, p, small, nSmall, g, cs.vals, cs.cellStart, cs.counts, out, outDist, cap, st), ++::wdem::g_kernel_launches);
+}
+
+// part 2: the exact test of nCand candidates; flags scanned, accepted total at candFlag[nCand]
+void col_periodic_exact(cudaStream_t s, const StepParams& P, Particles p, ColliderScratch& cs, long long nCand,
+                        DeviceStatus* st) {
+  if (nCand > 0) (k_peri_exact<<<(unsigned)((nCand + 255) / 256), 256, 0, s>>>(P, p, cs.cand, nCand, cs.candFlag, cs.candPer, st), ++::wdem::g_kernel_launches);
+  exclusive_scan_u32(s, cs.candFlag, nCand, cs);
+}
+
+// part 3: accepted pairs and their cellDist into the new container
+void col_periodic_emit(cudaStream_t s, ColliderScratch& cs, long long nCand, int2* out, int4* outDist, long long cap) {
+  if (nCand > 0) (k_peri_emit<<<(unsigned)((nCand + 255) / 256), 256, 0, s>>>(cs.cand, cs.candPer, cs.candFlag, nCand, out, outDist, cap), ++::wdem::g_kernel_launches);
 }
 
 void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, double* scratch9,

@@ -482,8 +482,10 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   c.out[OUT_TBX][i] = TB.x; c.out[OUT_TBY][i] = TB.y; c.out[OUT_TBZ][i] = TB.z;
 }
 
+// 128 threads, 4 blocks per SM (<= 128 registers a thread, no spills): one wave of the 152 x 4 blocks
+// that launch_contacts starts
 template <int LAW, int CP2, bool PERI, bool ELL>
-__global__ void __launch_bounds__(128) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
+__global__ void __launch_bounds__(128, 4) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
                                                   const unsigned* count, DeviceStatus* st) {
   const unsigned m = *count;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
@@ -500,8 +502,10 @@ template <bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
                                                        unsigned* work, unsigned* count, DeviceStatus* st) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // a step queued behind a collider trigger: the work list stays empty, so the heavy pass is a no-op too
+  if (haltedContacts(st, P.step)) return;
   // the integrator's rotation list of this step has been consumed: its counter starts the next step at 0
-  if (i == 0) st->rotCount = 0;
+  if (i == 0) { st->rotCount = 0; st->touchCount = 0; }
   bool need = false;
   if (i < nc) {
     const uint8_t s0 = c.state[i];
@@ -577,7 +581,7 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
                      const uint16_t* warmBf, const float* warmF) {
   if (nc <= 0) {
-    cudaMemsetAsync(&st->rotCount, 0, sizeof(unsigned), s);  // otherwise cleared by the cull kernel
+    cudaMemsetAsync(&st->rotCount, 0, 2 * sizeof(unsigned), s);  // rotCount, touchCount; otherwise cleared by the cull kernel
     return;
   }
   unsigned* count = &st->workCount;

@@ -44,11 +44,14 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
 // Raises the collider trigger.  All particles of a free-falling cloud cross the verlet distance in the
 // same step, and a million stores to one word serialise in the memory system: one store per warp, and
 // none once the flag is seen set.
-__device__ __forceinline__ void raiseDirty(DeviceStatus* st, bool dirty) {
+__device__ __forceinline__ void raiseDirty(DeviceStatus* st, bool dirty, long long step) {
   const unsigned am = __activemask();
   const unsigned b = __ballot_sync(am, dirty);
   if (b && (threadIdx.x & 31) == (unsigned)(__ffs(b) - 1))
-    if (*(volatile int*)&st->dirty == 0) st->dirty = 1;
+    if (*(volatile int*)&st->dirty == 0) {
+      st->dirty = 1;
+      st->haltAt = step + 1;
+    }
 }
 
 // Quaternion::toRotationMatrix (Eigen's formula), row-major
@@ -123,7 +126,7 @@ __device__ __noinline__ double asphericalErot(qd ori, d3 inertia, d3 w) {
 template <bool FROM_ARRAYS, bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || haltedIntegrator(st, P.step)) return;
   const int4 meta = p.meta[i];
   const unsigned flags = (unsigned)meta.w;
   const bool asph = ELL && (meta.x & META_ASPH);
@@ -291,7 +294,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const double4_32a lp = p.lastPos[i];
   const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
   if (!ELL) {
-    raiseDirty(st, sqnorm(dd) > P.maxD2);
+    raiseDirty(st, sqnorm(dd) > P.maxD2, P.step);
   } else {
     // rotation-aware trigger for bounds that track it (maxRot >= 0; Collision.cpp:94-121)
     double moveDueToRot2 = 0.;
@@ -312,14 +315,14 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       moveDueToRot2 = mv * mv;
     }
     const double d2 = sqnorm(dd);
-    raiseDirty(st, dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2);
+    raiseDirty(st, dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2, P.step);
   }
 }
 
-// The same step as k_leapfrog<false, false, false> without energy tracking, issuing fewer FP64
-// operations with bit-identical results:
+// The same step as k_leapfrog<false, PERI, false> without energy tracking, for one particle, issuing
+// fewer FP64 operations with bit-identical results:
 //  - the CSR gather runs only for particles that a real contact touched in the last contact pass
-//    (p.touched, set by the contact kernel, cleared here); the others get m g;
+//    (p.touched, set by the contact kernel; those run in k_leapfrog_touched); the others get m g;
 //  - Sign(F (v + dt/2 a)) of the damping comes from the sign bits (signProd) and the factor
 //    1 - damping Sign(...) from two constants; zero accelerations and velocities skip their updates
 //    (addScaled: adding a zero changes only -0);
@@ -328,10 +331,9 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
 //  - an orientation that does not rotate and that the last normalisation left unchanged (meta bit
 //    META_ORI_FIXED) is neither normalised again nor rewritten;
 //  - the FP32 shadow is written by mantissa truncation on the integer pipe.
-__global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
-                                                        DeviceStatus* st) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+template <bool PERI>
+__device__ __forceinline__ void integrateFast(const StepParams& P, const Particles& p, const int i, const int n, const Contacts& c,
+                                              const Csr& csr, DeviceStatus* st, const bool touchedNow) {
   const int4 meta = p.meta[i];
   const unsigned flags = (unsigned)meta.w;
   const double4_32a vm = p.velm[i];
@@ -339,7 +341,6 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   const bool blockedAll = (flags & 63u) == 63u;
   const bool blockedNone = (flags & 63u) == 0u;
   d3 F, T;
-  bool touchedNow = false;
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
   if (!blockedAll) {
     if (grav) {
@@ -349,9 +350,7 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
       F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
-    touchedNow = p.touched[i] != 0;
     if (touchedNow) {
-      p.touched[i] = 0;
       const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
       for (int e = e0; e < e1; e++) {
         const unsigned en = csr.ent[e];
@@ -395,15 +394,33 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
       if (!(flags & 4u)) lin.z = lin.z + qdiv(F.z, mass);
     }
     if (damp) {
-      // nonviscDamp2nd: a *= 1 - damping Sign(F (v + dt/2 a)); a zero F gives Sign 0 and factor 1
+      // nonviscDamp2nd: a *= 1 - damping Sign(F (v + dt/2 a)); a zero F gives Sign 0 and factor 1.
+      // Periodic: v is the fluctuation velocity v - gradV (x - dt/2 v) (Cell::pprevFluctVel)
+      d3 v0 = vel;
+      if (PERI) {
+        const double hdt = P.dt / 2;
+        const d3 w = mk(addZ(pos.x, negD(mulZ(vel.x, hdt))), addZ(pos.y, negD(mulZ(vel.y, hdt))),
+                        addZ(pos.z, negD(mulZ(vel.z, hdt))));
+        const d3 g = mvecC(P.gradV, P.clsGradV, w);
+        v0 = mk(addZ(vel.x, negD(g.x)), addZ(vel.y, negD(g.y)), addZ(vel.z, negD(g.z)));
+      }
       const double hd = 0.5 * dt;
-      if (!zeroBits(F.x)) { const int sg = signProd(F.x, vel.x + hd * lin.x); if (sg) lin.x = lin.x * (sg > 0 ? P.dampM : P.dampP); }
-      if (!zeroBits(F.y)) { const int sg = signProd(F.y, vel.y + hd * lin.y); if (sg) lin.y = lin.y * (sg > 0 ? P.dampM : P.dampP); }
-      if (!zeroBits(F.z)) { const int sg = signProd(F.z, vel.z + hd * lin.z); if (sg) lin.z = lin.z * (sg > 0 ? P.dampM : P.dampP); }
+      if (!zeroBits(F.x)) { const int sg = signProd(F.x, v0.x + hd * lin.x); if (sg) lin.x = lin.x * (sg > 0 ? P.dampM : P.dampP); }
+      if (!zeroBits(F.y)) { const int sg = signProd(F.y, v0.y + hd * lin.y); if (sg) lin.y = lin.y * (sg > 0 ? P.dampM : P.dampP); }
+      if (!zeroBits(F.z)) { const int sg = signProd(F.z, v0.z + hd * lin.z); if (sg) lin.z = lin.z * (sg > 0 ? P.dampM : P.dampP); }
     }
-    vel.x = addScaled(vel.x, dt, lin.x);
-    vel.y = addScaled(vel.y, dt, lin.y);
-    vel.z = addScaled(vel.z, dt, lin.z);
+    if (PERI) {
+      // GRADV2 (Leapfrog.cpp:189-190): v = (I - dt(L+ + L-)/4)^-1 ((L+ - L-) x + (I + dt(L+ + L-)/4) v + a dt)
+      const d3 a = mvecC(P.LmL, P.clsLmL, pos);
+      const d3 b = mvecC(P.IpLL4h, P.clsIpLL4h, vel);
+      const d3 sum = mk(addZ(addZ(a.x, b.x), mulZ(lin.x, dt)), addZ(addZ(a.y, b.y), mulZ(lin.y, dt)),
+                        addZ(addZ(a.z, b.z), mulZ(lin.z, dt)));
+      vel = mvecC(P.ImLL4hInv, P.clsImLL4hInv, sum);
+    } else {
+      vel.x = addScaled(vel.x, dt, lin.x);
+      vel.y = addScaled(vel.y, dt, lin.y);
+      vel.z = addScaled(vel.z, dt, lin.z);
+    }
     if (!isZeroBits(T)) {
       WDEM_REAL_BRANCH();
       const d3 inertia = xyz(p.inert[i]);
@@ -418,9 +435,13 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
         }
         if (damp) {
           const double hd = 0.5 * dt;
-          if (!zeroBits(T.x)) { const int sg = signProd(T.x, angVel.x + hd * ang.x); if (sg) ang.x = ang.x * (sg > 0 ? P.dampM : P.dampP); }
-          if (!zeroBits(T.y)) { const int sg = signProd(T.y, angVel.y + hd * ang.y); if (sg) ang.y = ang.y * (sg > 0 ? P.dampM : P.dampP); }
-          if (!zeroBits(T.z)) { const int sg = signProd(T.z, angVel.z + hd * ang.z); if (sg) ang.z = ang.z * (sg > 0 ? P.dampM : P.dampP); }
+          // periodic: the fluctuation spin angVel - spinVec (Cell::pprevFluctAngVel)
+          const d3 w0 = PERI ? mk(addZ(angVel.x, negD(P.spinVec[0])), addZ(angVel.y, negD(P.spinVec[1])),
+                                  addZ(angVel.z, negD(P.spinVec[2])))
+                             : angVel;
+          if (!zeroBits(T.x)) { const int sg = signProd(T.x, w0.x + hd * ang.x); if (sg) ang.x = ang.x * (sg > 0 ? P.dampM : P.dampP); }
+          if (!zeroBits(T.y)) { const int sg = signProd(T.y, w0.y + hd * ang.y); if (sg) ang.y = ang.y * (sg > 0 ? P.dampM : P.dampP); }
+          if (!zeroBits(T.z)) { const int sg = signProd(T.z, w0.z + hd * ang.z); if (sg) ang.z = ang.z * (sg > 0 ? P.dampM : P.dampP); }
         }
         angVel.x = addScaled(angVel.x, dt, ang.x);
         angVel.y = addScaled(angVel.y, dt, ang.y);
@@ -447,6 +468,20 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
         }
       }
     }
+    // periodic spin correction angVel -= deltaSpinVec (Leapfrog.cpp:192-197), for nodes with inertia;
+    // subtracting +0 leaves every value unchanged
+    if (PERI && !P.dSpinZero) {
+      const double4_32a in4 = p.inert[i];
+      if (!isZeroBits(xyz(in4))) {
+        angVel = mk(addZ(angVel.x, negD(P.dSpin[0])), addZ(angVel.y, negD(P.dSpin[1])), addZ(angVel.z, negD(P.dSpin[2])));
+        angChanged = true;
+      }
+    }
+  } else if (PERI) {
+    // fixed node with GRADV2: velocity correction without acceleration (Leapfrog.cpp:207-211)
+    const d3 a = mvecC(P.LmL, P.clsLmL, pos);
+    const d3 b = mvecC(P.IpLL4h, P.clsIpLL4h, vel);
+    vel = mvecC(P.ImLL4hInv, P.clsImLL4hInv, mk(addZ(a.x, b.x), addZ(a.y, b.y), addZ(a.z, b.z)));
   }
   pos.x = addScaledR(pos.x, vel.x, dt);
   pos.y = addScaledR(pos.y, vel.y, dt);
@@ -503,7 +538,43 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
     const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
     dirty = sqnorm(dd) > P.maxD2;
   }
-  raiseDirty(st, dirty);
+  raiseDirty(st, dirty, P.step);
+}
+
+// First pass: particles without contact forces this step.  Those that a real contact touched are
+// compacted into touchList instead: their force gather and divisions would hold up the FP64 pipe
+// for whole warps of gravity-only neighbours.
+template <bool PERI>
+__global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
+                                                        DeviceStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || haltedIntegrator(st, P.step)) return;
+  const bool listed = ((unsigned)p.meta[i].w & 63u) != 63u && p.touched[i] != 0;
+  const unsigned am = __activemask();
+  const unsigned b = __ballot_sync(am, listed);
+  if (b) {
+    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(&st->touchCount, (unsigned)__popc(b));
+    base = __shfl_sync(am, base, leader);
+    const unsigned slot = base + __popc(b & ((1u << lane) - 1));
+    if (listed && slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
+  }
+  if (listed) return;
+  integrateFast<PERI>(P, p, i, n, c, csr, st, false);
+}
+
+// Second pass: the listed particles, with their CSR force gather.
+template <bool PERI>
+__global__ void __launch_bounds__(256) k_leapfrog_touched(StepParams P, Particles p, int n, Contacts c, Csr csr,
+                                                           DeviceStatus* st) {
+  if (haltedIntegrator(st, P.step)) return;
+  const unsigned m = st->touchCount < (unsigned)n ? st->touchCount : (unsigned)n;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    const int i = (int)p.touchList[k];
+    p.touched[i] = 0;
+    integrateFast<PERI>(P, p, i, n, c, csr, st, true);
+  }
 }
 
 // leapfrogSphericalRotate of the spheres k_leapfrog_fast listed: q = AngleAxis(|w| dt, w/|w|) q, normalised.
@@ -512,8 +583,9 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
 // reciprocals instead of the divisions, and for the half angles of a DEM step (|x| < 1e-3) the Taylor
 // polynomials sin x = x (1 - x^2/6 (1 - x^2/20)), cos x = 1 - x^2/2 (1 - x^2/12), whose truncation
 // errors (x^7/5040, x^6/720) are far below an ulp.
-__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const unsigned* count, unsigned cap) {
-  const unsigned m = *count < cap ? *count : cap;
+__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const DeviceStatus* st, unsigned cap) {
+  if (haltedIntegrator(st, P.step)) return;
+  const unsigned m = st->rotCount < cap ? st->rotCount : cap;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
     const unsigned i = p.rotList[k];
     const d3 angVel = xyz(p.angw[i]);
@@ -547,11 +619,17 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
                      DeviceStatus* st) {
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
-  if (!fromArrays && !P.hasEll && !P.periodic && !P.lfEnergy && p.touched && p.rotList) {
+  if (!fromArrays && !P.hasEll && !P.lfEnergy && p.touched && p.rotList) {
     // st->rotCount is zero here: k_contacts_cull clears it for the next step (and the handle starts at zero)
-    (k_leapfrog_fast<<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     const unsigned rb = blocks < 152 * 4 ? blocks : 152 * 4;
-    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, &st->rotCount, (unsigned)n), ++::wdem::g_kernel_launches);
+    if (P.periodic) {
+      (k_leapfrog_fast<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      (k_leapfrog_touched<true><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    } else {
+      (k_leapfrog_fast<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      (k_leapfrog_touched<false><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+    }
+    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, st, (unsigned)n), ++::wdem::g_kernel_launches);
     return;
   }
   if (P.hasEll) {

@@ -163,6 +163,11 @@ struct wdem_handle {
   long long step = 0;
   long long nFullRuns = 0;
   int lastRunFull = 0;
+  // queued steps (runQueued): depth limit (0 or 1: every step checked on the host), mean steps between
+  // rebuilds, steps since the last one
+  int maxAhead = 32;
+  double rebuildInterval = 16;
+  int sinceRebuild = 0;
   int updatePhys = 0;
   double verletDistResolved = 0;
   bool verletResolved = false;
@@ -331,6 +336,11 @@ int ensureScratch(wdem_handle* h, long long nc) {
     cs.histCap = 256 * tiles + 1;
     CK(dalloc(cs.hist, cs.histCap));
   }
+  if (h->periodic && (long long)h->smallIds.size() + 1 > cs.periCap) {
+    long long cap = (long long)h->smallIds.size() + 1;
+    CK(dalloc(cs.periC, cap)); CK(dalloc(cs.periH, cap));
+    cs.periCap = cap;
+  }
   long long needRetain = std::max<long long>(h->nContacts, nc) + 2;
   if (needRetain > cs.retainCap) {
     long long cap = std::max<long long>(needRetain, cs.retainCap * 3 / 2);
@@ -340,6 +350,23 @@ int ensureScratch(wdem_handle* h, long long nc) {
   // scan scratch: level sums of the longest scan (histograms, pair counts, retain flags)
   long long longest = std::max<long long>(std::max<long long>(cs.histCap, (long long)h->N + 2), cs.retainCap);
   long long needSums = 64 + 2 * (longest / 1024 + 64) + 4096;
+  if (needSums > cs.blockSumsCap) {
+    CK(dalloc(cs.blockSums, needSums));
+    cs.blockSumsCap = needSums;
+  }
+  return WDEM_OK;
+}
+
+// periodic candidate buffers for n candidates (flags scanned in place: n + 1 entries), and the scan
+// scratch for a scan of that length
+int ensureCand(wdem_handle* h, long long n) {
+  ColliderScratch& cs = h->cs;
+  if (n + 1 > cs.candCap) {
+    long long cap = std::max<long long>(n + n / 4 + 1024, cs.candCap);
+    CK(dalloc(cs.cand, cap)); CK(dalloc(cs.candPer, cap)); CK(dalloc(cs.candFlag, cap + 1));
+    cs.candCap = cap;
+  }
+  long long needSums = 64 + 2 * ((n + 1) / 1024 + 64) + 4096;
   if (needSums > cs.blockSumsCap) {
     CK(dalloc(cs.blockSums, needSums));
     cs.blockSumsCap = needSums;
@@ -397,19 +424,28 @@ int rebuild(wdem_handle* h) {
   int rc;
   if ((rc = ensureScratch(h, h->nContacts))) return rc;
   launch_bboxes(s, h->P, h->d, n);
+  const unsigned* totalSrc = cs.counts + nSmall + 1;
+  long long nCand = 0;
   if (h->periodic) {
-    col_periodic(s, h->P, h->d, h->dSmall, nSmall, cs, nullptr, nullptr, 0, false, h->dst);
+    col_periodic_cand(s, h->P, h->d, h->dSmall, nSmall, cs, false);
+    CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    nCand = h->hcounts[0];
+    if ((rc = ensureCand(h, nCand))) return rc;
+    col_periodic_cand(s, h->P, h->d, h->dSmall, nSmall, cs, true);
+    col_periodic_exact(s, h->P, h->d, cs, nCand, h->dst);
+    totalSrc = cs.candFlag + nCand;
   } else {
     col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
     col_sort(s, h->d, h->dSmall, nSmall, cs);
     col_sweep(s, h->d, nSmall, h->P.loneMask, cs, nullptr, 0, false, h->dst);
+    exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
   }
-  exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
   ContactBuf& old = h->buf[h->cur];
   ContactBuf& neu = h->buf[1 - h->cur];
   const long long nOld = h->nContacts;
   col_retain_flags(s, h->P, h->d, old.c, nOld, cs);
-  CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&h->hcounts[0], totalSrc, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&h->hcounts[1], cs.retainFlag + nOld, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const long long total = h->hcounts[0];
@@ -420,7 +456,7 @@ int rebuild(wdem_handle* h) {
     long long cap = std::max<long long>(nNew + nNew / 4 + 1024, neu.cap);
     CK(allocContacts(neu, cap, hertz, h->keepGeom, h->periodic, h->hasEll));
   }
-  if (h->periodic) col_periodic(s, h->P, h->d, h->dSmall, nSmall, cs, neu.c.ids, neu.c.cdist, neu.cap, true, h->dst);
+  if (h->periodic) col_periodic_emit(s, cs, nCand, neu.c.ids, neu.c.cdist, neu.cap);
   else col_sweep(s, h->d, nSmall, h->P.loneMask, cs, neu.c.ids, neu.cap, true, h->dst);
   col_retain_write(s, old.c, nOld, cs, neu.c.ids, total, neu.cap);
   if (h->periodic && old.c.cdist) col_retain_write_dist(s, old.c, nOld, cs, neu.c.cdist, total, neu.cap);
@@ -488,6 +524,21 @@ void fillStepParams(wdem_handle* h) {
 }
 
 // Cell-dependent parameters of one step: shifts, unshear, Leapfrog GRADV2 matrices (Leapfrog.cpp:119-127)
+// MCLS_* class of each entry of a row-major 3x3 matrix, 2 bits per entry
+int entryClasses(const double* m) {
+  int c = 0;
+  for (int k = 0; k < 9; k++) {
+    unsigned long long b;
+    std::memcpy(&b, &m[k], 8);
+    int e = MCLS_GEN;
+    if (b == 0) e = MCLS_PZERO;
+    else if (b == 0x8000000000000000ull) e = MCLS_NZERO;
+    else if (m[k] == 1.0) e = MCLS_ONE;
+    c |= e << (2 * k);
+  }
+  return c;
+}
+
 void fillCellParams(wdem_handle* h) {
   StepParams& P = h->P;
   const HostCell& c = h->cell;
@@ -506,6 +557,13 @@ void fillCellParams(wdem_handle* h) {
   leviCivita(scaled(addScaled(c.gradV, transposed(c.gradV), -1.0), .5), a);
   leviCivita(scaled(addScaled(c.nextGradV, transposed(c.nextGradV), -1.0), .5), b);
   for (int k = 0; k < 3; k++) P.dSpin[k] = -.5 * a[k] + .5 * b[k];
+  P.clsGradV = entryClasses(P.gradV);
+  P.clsImLL4hInv = entryClasses(P.ImLL4hInv);
+  P.clsIpLL4h = entryClasses(P.IpLL4h);
+  P.clsLmL = entryClasses(P.LmL);
+  unsigned long long sb[3];
+  std::memcpy(sb, P.dSpin, sizeof sb);
+  P.dSpinZero = (sb[0] | sb[1] | sb[2]) == 0 ? 1 : 0;
 }
 
 // AabbCollider::setVerletDist (Collision.cpp:164-184): negative -> |verletDist| * min sphere radius
@@ -556,6 +614,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.lastPosf, N) == cudaSuccess;
   ok &= dalloc(d.touched, N) == cudaSuccess;
   ok &= dalloc(d.rotList, N) == cudaSuccess;
+  ok &= dalloc(d.touchList, N) == cudaSuccess;
   for (int k = 0; k < 3; k++) ok &= dalloc(d.energy[k], N) == cudaSuccess;
   ok &= dalloc(h->dEnergy, WDEM_E_COUNT) == cudaSuccess;
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
@@ -595,7 +654,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(h->dMatDt); cudaFree(h->cs.sceneWall);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
-  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rotList);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rotList); cudaFree(d.touchList);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
   cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
@@ -605,7 +664,8 @@ int wdem_destroy(wdem_handle* h) {
   ColliderScratch& cs = h->cs;
   cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
   cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid);
-  cudaFree(cs.retainFlag); cudaFree(cs.temp);
+  cudaFree(cs.retainFlag); cudaFree(cs.temp); cudaFree(cs.periC); cudaFree(cs.periH);
+  cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag);
   cudaFree(h->dst);
   cudaFree(h->staging);
   if (h->hst) cudaFreeHost(h->hst);
@@ -871,6 +931,70 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
   return WDEM_OK;
 }
 
+// Steps queued without a host check in between.  Every step of Woo's loop ends its integrator with the
+// collider trigger (Collision.cpp:80-184), and the contact pass must not start before a triggered rebuild;
+// checking on the host costs a device round trip per step.  Instead `ahead` steps are queued at once and
+// their kernels guard themselves (haltedIntegrator / haltedContacts): when the integrator of step k raises
+// the trigger, the contact pass of k and all later queued kernels return at once.  The host then sees
+// haltAt, rebuilds and runs the contact pass of step k, exactly the sequence of the one-step path.  Only
+// the configurations whose host-side per-step work is none are queued: no periodic cell (integrated on
+// the host each step), no energy tracking (host-launched reductions), no updatePhys='once', no phase
+// timing.
+static int queueDepth(wdem_handle* h, int left) {
+  if (left < 2 || h->timing || h->periodic || h->P.trackEnergy || h->needRebuild || h->forcesInArrays ||
+      h->verletDistResolved == 0 || h->updatePhys == WDEM_UPDATE_PHYS_ONCE || h->maxAhead < 2)
+    return 1;
+  // expected steps between rebuilds r: a queue of sqrt(3 r) balances the wasted no-op launches behind a
+  // trigger against the round trips saved
+  int q = (int)std::lround(std::sqrt(3.0 * h->rebuildInterval));
+  q = std::max(2, std::min(q, h->maxAhead));
+  return std::min(q, left);
+}
+
+static int runQueued(wdem_handle* h, int ahead, int& done) {
+  cudaStream_t s = h->stream;
+  const long long s0 = h->step;
+  h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
+  const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
+  StepParams P = h->P;
+  for (int g = 0; g < ahead; g++) {
+    P.step = s0 + g;
+    launch_leapfrog(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
+    launch_contacts(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+                    warm ? h->mlpW : nullptr);
+  }
+  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int rc;
+  if ((rc = checkDeviceStatus(h))) return rc;
+  const long long halt = h->hst->haltAt;
+  if (halt == 0) {
+    h->sinceRebuild += ahead;
+    done = ahead;
+    h->lastRunFull = 0;
+  } else {
+    const long long k = halt - 1;  // steps s0 .. k-1 are complete, step k has been integrated
+    if (k < s0 || k >= s0 + ahead) return fail(h, WDEM_ERR_STATE, "queued steps: trigger outside the queue");
+    h->step = k;
+    h->P.step = k;
+    h->raw.step = k;
+    CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
+    if ((rc = rebuild(h))) return rc;
+    launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+                    warm ? h->mlpW : nullptr);
+    h->sinceRebuild += (int)(k - s0) + 1;
+    h->rebuildInterval = 0.75 * h->rebuildInterval + 0.25 * h->sinceRebuild;
+    h->sinceRebuild = 0;
+    done = (int)(k - s0) + 1;
+    h->lastRunFull = 1;
+  }
+  h->step = s0 + done;
+  h->P.step = h->step;
+  h->raw.step = h->step;
+  return WDEM_OK;
+}
+
 int wdem_step(wdem_handle* h, int32_t nSteps) {
   if (!h || nSteps < 0) return WDEM_ERR_ARG;
   if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "wdem_step before particles and params were set");
@@ -901,7 +1025,15 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   // the integrator's rotation-list counter starts every call at zero (within a call the contact pass
   // clears it for the next step)
   CK(cudaMemsetAsync(&h->dst->rotCount, 0, sizeof(unsigned), s));
+  CK(cudaMemsetAsync(&h->dst->touchCount, 0, sizeof(unsigned), s));
   for (int it = 0; it < nSteps; it++) {
+    const int ahead = queueDepth(h, nSteps - it);
+    if (ahead > 1) {
+      int done = 0, rc;
+      if ((rc = runQueued(h, ahead, done))) return rc;
+      it += done - 1;
+      continue;
+    }
     h->P.step = h->step;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
     if (h->periodic) {
@@ -935,8 +1067,14 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     if ((rc = checkDeviceStatus(h))) return rc;
     bool full = h->needRebuild || h->hst->dirty || h->verletDistResolved == 0;
     h->lastRunFull = full;
+    h->sinceRebuild++;
+    if (full) {
+      h->rebuildInterval = 0.75 * h->rebuildInterval + 0.25 * h->sinceRebuild;
+      h->sinceRebuild = 0;
+    }
     if (full) {
       CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
+      CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
       PhaseTimer t(h, PH_COLLIDER);
       if ((rc = rebuild(h))) return rc;
     }
@@ -1272,6 +1410,12 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
   return WDEM_OK;
 }
 
+int wdem_set_queue_depth(wdem_handle* h, int32_t depth) {
+  if (!h || depth < 0 || depth > 4096) return WDEM_ERR_ARG;
+  h->maxAhead = depth;
+  return WDEM_OK;
+}
+
 int wdem_set_timing(wdem_handle* h, int32_t enable) {
   if (!h) return WDEM_ERR_ARG;
   h->timing = enable != 0;
@@ -1291,7 +1435,13 @@ int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* l
 
 int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
   if (!h || !c) return WDEM_ERR_ARG;
-  if (!c->periodic) { h->periodic = false; h->P.periodic = 0; h->needRebuild = true; return WDEM_OK; }
+  // a full collider run follows only a change of periodicity (InsertionSortCollider::prologue_doFullRun,
+  // InsertionSortCollider.cpp:377-382); new cell matrices alone do not trigger one
+  if (!c->periodic) {
+    if (h->periodic) h->needRebuild = true;
+    h->periodic = false; h->P.periodic = 0;
+    return WDEM_OK;
+  }
   if (c->homoDeform != 4) return fail(h, WDEM_ERR_UNSUPPORTED, "Cell.homoDeform other than gradV2 (4) is not supported");
   for (int s : h->shape)
     if (s != WDEM_SHAPE_SPHERE) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
@@ -1309,10 +1459,10 @@ int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
   leviCivita(hc.W, v);
   for (int k = 0; k < 3; k++) hc.spinVec[k] = .5 * v[k];
   if (!hc.integrateAndUpdate(0)) return fail(h, WDEM_ERR_ARG, "Cell is degenerate (zero volume).");
+  if (!h->periodic) h->needRebuild = true;
   h->periodic = true;
   h->P.periodic = 1;
   fillCellParams(h);
-  h->needRebuild = true;
   return WDEM_OK;
 }
 

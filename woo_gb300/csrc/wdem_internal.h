@@ -55,6 +55,9 @@ struct DevMaterial {
   double density, young, ktDivKn, tanPhi, surfEnergy, alpha;
 };
 
+// classes of a matrix entry: +0, -0, exactly 1, anything else
+enum { MCLS_PZERO = 0, MCLS_NZERO = 1, MCLS_ONE = 2, MCLS_GEN = 3 };
+
 // Engine + functor attributes as the kernels see them.
 struct StepParams {
   double dt;
@@ -92,6 +95,10 @@ struct StepParams {
   double spinVec[3];
   double ImLL4hInv[9], IpLL4h[9], LmL[9];  // Leapfrog GRADV2 matrices
   double dSpin[3];     // Leapfrog.deltaSpinVec
+  // entry classes of gradV, ImLL4hInv, IpLL4h, LmL (2 bits per entry, row-major: MCLS_* below), for
+  // products that skip bit-exactly what a zero or a unit entry contributes
+  int clsGradV, clsImLL4hInv, clsIpLL4h, clsLmL;
+  int dSpinZero;       // every dSpin component is +0
   // ellipsoids: Cg2_Ellipsoid_Ellipsoid_L6Geom solver
   int hasEll;
   int ellSolver;       // WDEM_ELL_*
@@ -117,6 +124,7 @@ struct Particles {
   float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
   uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
   unsigned* rotList;  // spheres whose orientation the rotation pass integrates this step
+  unsigned* touchList;  // particles with contact forces this step (integrated by the second pass)
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
   double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
@@ -160,12 +168,32 @@ struct DeviceStatus {
   int detail;
   int dirty;          // set by the integrator when a particle left its verlet box
   int overflow;
+  long long haltAt;   // 0, or 1 + the step whose integrator raised the collider trigger (see haltedIntegrator)
   unsigned long long pairTotal;
-  unsigned long long ellSolves, ellIters, ellFallbacks;
+  unsigned long long ellSolves, ellIters, ellFallbacks;  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
   unsigned workCount;  // length of the contact work list of this step
-  unsigned rotCount;   // length of the rotation list of this step  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
+  unsigned rotCount;   // length of the rotation list of this step
+  unsigned touchCount; // length of the touched-particle list of this step
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
+
+#ifdef __CUDACC__
+// Steps queued ahead of the host's collider check.  The integrator of step s that raises the collider
+// trigger also stores haltAt = s + 1; from then on the contact pass of step s and every kernel of the
+// later steps return at once, until the host has rebuilt the pair set, cleared the trigger and run the
+// contact pass of step s itself.  With one step per check (haltAt cleared before the contact pass) the
+// guards never fire.  The word is read with a plain (L1-cached) load: the values that matter were
+// written by earlier kernels, and a store by the running integrator (step + 1) does not halt it; a
+// volatile load per warp would send every warp of the grid to the same L2 line.
+__device__ __forceinline__ bool haltedIntegrator(const DeviceStatus* st, long long step) {
+  const long long h = st->haltAt;
+  return h != 0 && h <= step;
+}
+__device__ __forceinline__ bool haltedContacts(const DeviceStatus* st, long long step) {
+  const long long h = st->haltAt;
+  return h != 0 && h <= step + 1;
+}
+#endif
 
 // ---- launchers (k_leapfrog.cu) ----
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays,
@@ -205,6 +233,12 @@ struct ColliderScratch {
   GridParams* grid;
   unsigned* retainFlag;                 // old contacts retained (scanned in place)
   long long retainCap;
+  float4 *periC, *periH;                // periodic: wrapped FP32 box centres / half-widths in cell order
+  long long periCap;
+  int2* cand;                           // periodic: FP32 candidate pairs, their exact-test flags
+  int4* candPer;                        //   (scanned in place) and cellDist
+  unsigned* candFlag;
+  long long candCap;
   void* temp;                           // small scratch (extent reduction)
   long long launches;                   // kernels launched by the collider (counted on the host)
 };
@@ -213,9 +247,12 @@ void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSm
 void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
 void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out,
                long long cap, bool write, DeviceStatus* st);
-// periodic collider: 3-D cell grid + spatialOverlapPeri
-void col_periodic(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall, ColliderScratch& cs,
-                  int2* out, int4* outDist, long long cap, bool write, DeviceStatus* st);
+// periodic collider: 3-D cell grid, FP32 candidates, exact spatialOverlapPeri, emission
+void col_periodic_cand(cudaStream_t s, const StepParams& P, Particles p, const int* small, int nSmall,
+                       ColliderScratch& cs, bool write);
+void col_periodic_exact(cudaStream_t s, const StepParams& P, Particles p, ColliderScratch& cs, long long nCand,
+                        DeviceStatus* st);
+void col_periodic_emit(cudaStream_t s, ColliderScratch& cs, long long nCand, int2* out, int4* outDist, long long cap);
 void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int4* out, long long base,
                            long long cap);
 // k_mlp.cu: learned warm start of the ellipsoid solve

@@ -163,6 +163,41 @@ __device__ __forceinline__ double addScaled(double v, double s, double a) {
   WDEM_REAL_BRANCH();
   return v + s * a;
 }
+// a * b with a of known class (0: +0, 1: -0, 2: exactly 1, 3: other; MCLS_* of the step parameters):
+// a zero or unit factor times a finite b is formed on the integer pipe (IEEE: +-0 * b is the zero with
+// the sign of the product, 1 * b is b)
+__device__ __forceinline__ double mulC(double a, int cls, double b) {
+  if (cls != 3 && finiteBits(b)) return cls == 2 ? b : signedZero(a, b);
+  WDEM_REAL_BRANCH();
+  return a * b;
+}
+// a * b where a zero a times a finite b is the signed zero
+__device__ __forceinline__ double mulZ(double a, double b) {
+  if (zeroBits(a) && finiteBits(b)) return signedZero(a, b);
+  WDEM_REAL_BRANCH();
+  return a * b;
+}
+// a + b; when an operand is a zero the sum is the other operand, except -0 + +0 = +0 (round to nearest)
+__device__ __forceinline__ double addZ(double a, double b) {
+  if (zeroBits(b)) return (negZero(a) && !negZero(b)) ? 0.0 : a;
+  if (zeroBits(a)) return b;
+  WDEM_REAL_BRANCH();
+  return a + b;
+}
+__device__ __forceinline__ double negD(double a) { return __longlong_as_double((long long)(bitsOf(a) ^ 0x8000000000000000ull)); }
+// row-major m (entry classes cls) times v, each row summed left to right: mvec with the zero and unit
+// entries' contributions formed exactly without FP64 operations
+__device__ __forceinline__ d3 mvecC(const double* m, int cls, d3 v) {
+  double r[3];
+  for (int i = 0; i < 3; i++) {
+    const double t0 = mulC(m[3 * i], (cls >> (6 * i)) & 3, v.x);
+    const double t1 = mulC(m[3 * i + 1], (cls >> (6 * i + 2)) & 3, v.y);
+    const double t2 = mulC(m[3 * i + 2], (cls >> (6 * i + 4)) & 3, v.z);
+    r[i] = addZ(addZ(t0, t1), t2);
+  }
+  return mk(r[0], r[1], r[2]);
+}
+
 // v + a s (operands of the product in this order) for the position update pos + vel dt
 __device__ __forceinline__ double addScaledR(double v, double a, double s) {
   if (zeroBits(a) && finiteBits(s)) {

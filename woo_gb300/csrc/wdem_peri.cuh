@@ -40,4 +40,21 @@ __device__ __forceinline__ bool overlapPeri(const double4_32a& mn1, const double
   return true;
 }
 
+// FP32 screens of spatialOverlapPeri on wrapped box centres and half-widths.
+// minimum-image centre distance on one axis (the image choice can differ from the exact one only where
+// both images are about L/2 away, beyond any half-width sum below L/2)
+__device__ __forceinline__ float periDist(float c1, float c2, float L, float invL) {
+  const float d = c2 - c1;
+  return fabsf(d - L * rintf(d * invL));
+}
+// the boxes are disjoint on this axis for every period shift: the rounding of the FP32 copies (centres
+// wrapped to [0, L), half-widths) and of this arithmetic is a few 2^-24 L, the margin 1e-5 L
+__device__ __forceinline__ bool periFar(float c1, float h1, float c2, float h2, float L, float invL) {
+  return periDist(c1, c2, L, invL) > h1 + h2 + 1e-5f * L;
+}
+// ... or overlapping on this axis for the nearest image, by more than the same margin
+__device__ __forceinline__ bool periNear(float c1, float h1, float c2, float h2, float L, float invL) {
+  return periDist(c1, c2, L, invL) < h1 + h2 - 1e-5f * L;
+}
+
 }  // namespace wdem

@@ -13,6 +13,7 @@ the particle arrays.  The benchmark scenes follow the configurations the engine 
 
 Masses and inertias follow Sphere::lumpMassInertia (src/dem/Sphere.cpp:26-33).
 """
+import ctypes
 import math
 
 import numpy as np
@@ -476,6 +477,76 @@ def single_from_batch(spec, k):
     p = default_params(mats, dt=spec.info["dt"][k], gravity=tuple(spec.params.gravity), damping=spec.params.damping,
                        verletDist=spec.params.verletDist)
     return SceneSpec(p, mats, pa, f"scene{k}", dict(range=(a, b)))
+
+
+def densify_periodic(spec, phi_target=0.62, stages=48, steps_per_stage=100, relax=600, damping=0.5, frictionless=False,
+                     device=0):
+    """Dense periodic packing from a loose one, on the GPU engine (the role of randomPeriPack's
+    compression, py/pack.py:572): the radii grow in `stages` geometric steps to the solid fraction
+    `phi_target`, each followed by `steps_per_stage` steps with non-viscous damping `damping` (and
+    the scene's friction, or none) and no cell motion, then `relax` more steps in three parts.  Every
+    stage and part starts from rest (velocities zeroed: the energy of the overlaps a growth step makes
+    is not carried on).  The result is scaled back to the original radii (positions and cell by 1/s),
+    so it is the same packing with the spec's radii in a smaller cell, and starts with the affine
+    velocity field of the scene's nextGradV.  Returns a new SceneSpec with the scene's own parameters
+    and cell gradients."""
+    pa0 = spec.particles
+    n = pa0.n
+    r0 = pa0.radius.copy()
+    L = float(spec.cell["hSize"][0][0])
+    vs = float(np.sum((4.0 / 3.0) * math.pi * r0 ** 3))
+    phi0 = vs / L ** 3
+    sfin = (phi_target / phi0) ** (1.0 / 3.0)
+    dens = np.array([spec.materials[int(k)].density for k in range(len(spec.materials))])[pa0.material]
+    p = abi.Params()
+    ctypes.memmove(ctypes.byref(p), ctypes.byref(spec.params), ctypes.sizeof(p))
+    p.damping = damping
+    # frictionless growth packs denser before it jams (fewer contacts at a given fraction); with the
+    # scene's friction the packing jams earlier and is compressed beyond that, contact-rich
+    grow_mats = (abi.Material * len(spec.materials))()
+    ctypes.memmove(grow_mats, spec.materials, ctypes.sizeof(grow_mats))
+    if frictionless:
+        for k in range(len(grow_mats)):
+            grow_mats[k].tanPhi = 0.0
+    p.materials = grow_mats
+    still = dict(hSize=np.diag([L, L, L]), trsf=np.eye(3), gradV=np.zeros((3, 3)), nextGradV=np.zeros((3, 3)))
+    pos, ori = pa0.pos.copy(), pa0.ori.copy()
+    runs = [(sfin ** (k / stages), steps_per_stage) for k in range(1, stages + 1)]
+    runs += [(sfin, relax // 3)] * 3
+    h = abi.Handle(n, device=device)
+    try:
+        for s, steps in runs:
+            up = pa0.copy()
+            up.pos, up.ori = pos, ori
+            up.vel[:] = 0
+            up.angVel[:] = 0
+            up.radius = r0 * s
+            m, inert = sphere_mass_inertia(up.radius, dens)
+            up.mass = m
+            up.inertia = np.repeat(inert[:, None], 3, axis=1)
+            h.set_params(p)
+            h.upload_particles(up)
+            h.set_params(p)
+            h.set_cell(**still)
+            h.step(steps)
+            st = h.download_particles(abi.ParticleArrays(n))
+            pos, ori = st.pos.copy(), st.ori.copy()
+    finally:
+        h.close()
+    out = pa0.copy()
+    out.pos = pos / sfin
+    out.ori = ori
+    out.vel = out.pos @ np.asarray(spec.cell["nextGradV"], np.float64).T
+    out.angVel[:] = 0
+    Ld = L / sfin
+    cell = dict(spec.cell)
+    cell["hSize"] = np.diag([Ld, Ld, Ld])
+    info = dict(spec.info)
+    info.update(L=Ld, phi=vs / Ld ** 3, densified=dict(stages=stages, steps_per_stage=steps_per_stage, relax=relax,
+                                                        damping=damping, phi_from=phi0))
+    q = abi.Params()
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(spec.params), ctypes.sizeof(q))
+    return SceneSpec(q, spec.materials, out, spec.name, info, cell=cell)
 
 
 def peri_shear(n=8_000_000, seed=5, phi=0.3, rate=1.0, young=1e8, tanPhi=0.5, density=1000.0, dt_safety=0.9):
