@@ -126,6 +126,15 @@ typedef struct wdem_params {
   /* Batched scenes: Scene.dt of each material's scene (nMaterials values), used instead of dt for the
    * particles and contacts of that material; NULL = every particle steps with dt */
   const double* materialDt;
+  /* DynDt (src/dem/DynDt.hpp:5-27) after ContactLoop in each step where it is activated as a
+   * PeriodicEngine with stepPeriod = dynDtPeriod (stepModulo, initRun; Engine.cpp:170-196); 0 = no DynDt.
+   * The critical step from the contact stiffnesses times dtSafety (Scene.dtSafety), capped by the
+   * growth dt (1 + dynDtMaxRelInc)^(steps since the previous run), becomes Scene.dt after the step
+   * (Scene.cpp:432).  Sphere and wall scenes with one dt (materialDt NULL). */
+  int32_t dynDtPeriod;
+  int32_t _pad3;
+  double dynDtMaxRelInc;  /* DynDt.maxRelInc (default 1e-4) */
+  double dtSafety;        /* Scene.dtSafety (default .9) */
 } wdem_params;
 
 /* ---- particle state, SoA; all arrays have n (or 3n / 4n) items --------------------------------- */
@@ -200,6 +209,9 @@ typedef struct wdem_status {
   int64_t ellSolves;       /* ellipsoid contact-function maximisations since creation */
   int64_t ellIters;        /* their Newton iterations (Brent: function evaluations) */
   int64_t ellFallbacks;    /* learned warm starts that fell back to the cold start */
+  double dt;               /* Scene.dt for the next step (DynDt may have changed it) */
+  double dynDtCrit;        /* critical step of DynDt's last run (DynDt::critDt_stiffness), NaN before */
+  double timeSum;          /* sum of dt over the steps run by this handle (Scene.time advances by it) */
 } wdem_status;
 
 typedef struct wdem_handle wdem_handle;

@@ -37,6 +37,8 @@ def load(variant="liborc.so"):
         "orc_contact_count": ([h], C.c_long),
         "orc_download_contacts": ([h, C.POINTER(abi.Contacts)], C.c_int),
         "orc_crit_dt": ([h], C.c_double),
+        "orc_get_dt": ([h], C.c_double),
+        "orc_dyndt_crit": ([h], C.c_double),
         "orc_get_energy": ([h, C.POINTER(C.c_double), C.c_int], C.c_int),
         "orc_reset_energy": ([h], C.c_int),
         "orc_nfullruns": ([h], C.c_long),
@@ -148,6 +150,12 @@ class Oracle:
 
     def reset_energy(self):
         self.lib.orc_reset_energy(self.h)
+
+    def dt(self):
+        return self.lib.orc_get_dt(self.h)
+
+    def dyndt_crit(self):
+        return self.lib.orc_dyndt_crit(self.h)
 
     def n_full_runs(self):
         return self.lib.orc_nfullruns(self.h)

@@ -392,6 +392,9 @@ struct Scene {
   Cell cell;
   double stress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   long ellEvals = 0, ellSolves = 0;   /* contact-function evaluations / solves of the ellipsoid functors */
+  /* DynDt as a PeriodicEngine (Engine.hpp:130-160): stepLast, stepPrev; Scene.nextDt; last critical step */
+  long dynStepLast = -1, dynStepPrev = -1;
+  double nextDt = NaN, dynDtCrit = NaN;
 #ifdef _OPENMP
   std::vector<omp_lock_t> locks;
   ~Scene() { for (auto& l : locks) omp_destroy_lock(&l); }
@@ -1565,16 +1568,64 @@ static double pWaveDt(const Scene& S) {
 }
 
 /* Scene::doOneStep (Scene.cpp:366-467) with engines [Leapfrog, InsertionSortCollider, ContactLoop] */
+/* DynDt::nodalCritDtSq (DynDt.cpp:46-63) with nodalStiffAdd (DynDt.cpp:16-38); the contact normal is
+ * the contact node's orientation applied to the x axis; Eigen's n.array().pow(2) is taken as n*n */
+static double nodalCritDtSq(const Scene& S, int i) {
+  const Particle& q = S.par[i];
+  if (q.isBlockedAll()) return Inf;
+  V3 ktrans(0, 0, 0), krot(0, 0, 0);
+  for (const auto& kv : q.contacts) {
+    const Contact& C = *kv.second;
+    if (!C.isReal()) continue;
+    const int ix = (C.pA == i) ? 0 : 1;
+    const V3 n = qrot(C.gori, V3(1, 0, 0));
+    const V3 n2(n.x * n.x, n.y * n.y, n.z * n.z);
+    const double knt = C.kn - C.kt;
+    ktrans = V3(ktrans.x + (n2.x * knt + C.kt), ktrans.y + (n2.y * knt + C.kt), ktrans.z + (n2.z * knt + C.kt));
+    const double sc = (C.lens[ix] * C.lens[ix]) * C.kt;  /* pow2(lens[ix]) * kt */
+    krot = V3(krot.x + sc * (n2.y + n2.z), krot.y + sc * (n2.z + n2.x), krot.z + sc * (n2.x + n2.y));
+  }
+  double ret = Inf;
+  const double kt[3] = {ktrans.x, ktrans.y, ktrans.z}, kr[3] = {krot.x, krot.y, krot.z};
+  const double in[3] = {q.inertia.x, q.inertia.y, q.inertia.z};
+  for (int k = 0; k < 3; k++) if (kt[k] != 0 && q.mass > 0. && !q.isBlockedAxisDOF(k, false)) ret = std::min(ret, q.mass / std::abs(kt[k]));
+  for (int k = 0; k < 3; k++) if (kr[k] != 0 && in[k] > 0. && !q.isBlockedAxisDOF(k, true)) ret = std::min(ret, in[k] / std::abs(kr[k]));
+  return 2 * ret;
+}
+
+/* DynDt::run (DynDt.cpp:86-113), when PeriodicEngine::isActivated (Engine.cpp:170-196: stepPeriod with
+ * stepModulo, initRun) says so; the new dt takes effect after the step (Scene.cpp:432) */
+static void dynDtRun(Scene& S) {
+  const long per = S.P.dynDtPeriod;
+  if (per <= 0) return;
+  const long s = S.step;
+  if (S.dynStepLast < 0) S.dynStepLast = s;
+  if (!((s - S.dynStepLast >= per) || (s % per == 0))) return;
+  S.dynStepPrev = S.dynStepLast;
+  S.dynStepLast = s;
+  double ret = Inf;  /* DynDt::critDt_stiffness */
+  for (size_t i = 0; i < S.par.size(); i++) ret = std::min(ret, nodalCritDtSq(S, (int)i));
+  const double crDt = std::sqrt(ret);
+  S.dynDtCrit = crDt;
+  if (std::isinf(crDt)) return;
+  const long nSteps = S.step - S.dynStepPrev;
+  const double maxNewDt = S.P.dt * pown(1. + S.P.dynDtMaxRelInc, (unsigned)nSteps);
+  const double nextDt = std::min(crDt * S.P.dtSafety, maxNewDt);
+  if (nextDt != S.P.dt) S.nextDt = nextDt;
+}
+
 static void doOneStep(Scene& S) {
   if (S.periodic) S.cell.integrateAndUpdate(S.P.dt);
   if (S.P.trackEnergy) S.E.resetResettables();
   leapfrogRun(S);
   colliderRun(S);
   contactLoopRun(S);
+  dynDtRun(S);
   if (S.periodic) S.cell.setNextGradV();
   S.step++;
   S.time += S.P.dt;
   S.P.step = S.step;
+  if (!std::isnan(S.nextDt)) { S.P.dt = S.nextDt; S.nextDt = NaN; }
 }
 
 }  // namespace orc
@@ -1735,6 +1786,10 @@ int orc_download_particles(orc_handle* h, wdem_particles* p) {
 }
 
 long orc_contact_count(orc_handle* h) { return (long)h->S.linView.size(); }
+
+/* Scene.dt for the next step and DynDt's last critical step */
+double orc_get_dt(orc_handle* h) { return h->S.P.dt; }
+double orc_dyndt_crit(orc_handle* h) { return h->S.dynDtCrit; }
 
 /* contacts sorted by (min id, max id) */
 int orc_download_contacts(orc_handle* h, wdem_contacts* c) {

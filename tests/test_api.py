@@ -69,10 +69,19 @@ def test_params_packing():
 
 
 def test_unsupported_engine_rejected():
+    class PyRunner(dem.Engine):
+        pass
+    S = small_scene()
+    S.engines = utils.defaultEngines(dynDtPeriod=0) + [PyRunner()]
+    with pytest.raises(RuntimeError, match="PyRunner"):
+        S.run(1)
+
+
+def test_dyndt_engine_is_taken_over():
     S = small_scene()
     S.engines = utils.defaultEngines(dynDtPeriod=100)
-    with pytest.raises(RuntimeError, match="DynDt"):
-        S.run(1)
+    g = S._engine()
+    assert isinstance(g._dynDt, dem.DynDt) and g._dynDt.stepPeriod == 100 and g._dynDt.maxRelInc == 1e-4
 
 
 def test_fails_loudly_without_gpu():

@@ -69,7 +69,9 @@ class Params(C.Structure):
                 ("nMaterials", C.c_int32), ("_pad2", C.c_int32),
                 ("materials", C.POINTER(Material)),
                 ("ellSolver", C.c_int32), ("brentBits", C.c_int32), ("newtonTol", C.c_double),
-                ("warmStart", C.c_int32), ("fallbackIters", C.c_int32), ("materialDt", C.POINTER(C.c_double))]
+                ("warmStart", C.c_int32), ("fallbackIters", C.c_int32), ("materialDt", C.POINTER(C.c_double)),
+                ("dynDtPeriod", C.c_int32), ("_pad3", C.c_int32), ("dynDtMaxRelInc", C.c_double),
+                ("dtSafety", C.c_double)]
 
 
 class Particles(C.Structure):
@@ -96,7 +98,7 @@ class Status(C.Structure):
     _fields_ = [("code", C.c_int32), ("detail", C.c_int32), ("step", C.c_int64), ("nContacts", C.c_int64),
                 ("nReal", C.c_int64), ("nFullRuns", C.c_int64), ("capacity", C.c_int64),
                 ("lastRunFull", C.c_int32), ("_pad", C.c_int32), ("ellSolves", C.c_int64), ("ellIters", C.c_int64),
-                ("ellFallbacks", C.c_int64)]
+                ("ellFallbacks", C.c_int64), ("dt", C.c_double), ("dynDtCrit", C.c_double), ("timeSum", C.c_double)]
 
 
 EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params", "wdem_upload_particles",

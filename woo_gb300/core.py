@@ -145,16 +145,20 @@ class Scene:
         ee = self._engines
         gpu = [e for e in ee if isinstance(e, dem.GpuDemEngine)]
         trio = (dem.Leapfrog, dem.InsertionSortCollider, dem.ContactLoop)
-        others = [e for e in ee if not isinstance(e, (dem.GpuDemEngine,) + trio)]
+        dyn = [e for e in ee if isinstance(e, dem.DynDt)]
+        others = [e for e in ee if not isinstance(e, (dem.GpuDemEngine, dem.DynDt) + trio)]
         if others:
             names = ", ".join(type(e).__name__ for e in others)
-            raise RuntimeError(f"engines not run by the GPU engine: {names} (DynDt: pass dynDtPeriod=0)")
+            raise RuntimeError(f"engines not run by the GPU engine: {names}")
+        if len(dyn) > 1:
+            raise RuntimeError("more than one DynDt engine")
         if gpu:
             self._gpu = gpu[0]
         elif all(any(isinstance(e, t) for e in ee) for t in trio):
             self._gpu = dem.GpuDemEngine.fromEngines(ee)
         else:
             raise RuntimeError("Scene.engines must hold GpuDemEngine or Leapfrog + InsertionSortCollider + ContactLoop")
+        self._gpu._dynDt = dyn[0] if dyn else None
         return self._gpu
 
     def critDt(self):
@@ -181,7 +185,7 @@ class Scene:
         eng = self._engine()
         eng.run(self, int(nSteps))
         self.step += int(nSteps)
-        self.time += self.dt * int(nSteps)
+        self.time += eng._ran_time
 
     def one(self):
         self.run(1)

@@ -490,7 +490,8 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
 // ------------------------------------------------------------------------------------ retain
 // Real contacts whose new boxes no longer overlap stay in the container (the reference collider
 // removes only non-real contacts on separation, InsertionSortCollider.cpp:107-110).
-__global__ void k_retain_flag(StepParams P, Particles p, Contacts old, long long nOld, unsigned* flag) {
+__global__ void k_retain_flag(StepParams P, Particles p, Contacts old, long long nOld, unsigned* flag,
+                              const float4* pci, const float4* phi) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nOld) return;
   unsigned f = 0;
@@ -498,24 +499,16 @@ __global__ void k_retain_flag(StepParams P, Particles p, Contacts old, long long
     int2 id = old.ids[c];
     bool ov;
     if (P.periodic) {
-      const double4_32a mn1 = p.bbmin[id.x], mx1 = p.bbmax[id.x], mn2 = p.bbmin[id.y], mx2 = p.bbmax[id.y];
-      // boxes that overlap on every axis by more than the FP32 margin (and are narrow enough that no
-      // ambiguity exists) overlap in the exact test too
-      const double lo1[3] = {mn1.x, mn1.y, mn1.z}, hi1[3] = {mx1.x, mx1.y, mx1.z};
-      const double lo2[3] = {mn2.x, mn2.y, mn2.z}, hi2[3] = {mx2.x, mx2.y, mx2.z};
-      bool sure = true;
-      for (int k = 0; k < 3 && sure; k++) {
-        const double L = P.csize[k];
-        const double ca = .5 * (lo1[k] + hi1[k]), cb = .5 * (lo2[k] + hi2[k]);
-        const double ha = .5 * (hi1[k] - lo1[k]), hb = .5 * (hi2[k] - lo2[k]);
-        if (!(ha < .25 * L) || !(hb < .25 * L)) { sure = false; break; }
-        const float Lf = (float)L;
-        sure = periNear((float)(ca - floor(ca / L) * L), (float)ha, (float)(cb - floor(cb / L) * L), (float)hb, Lf, 1.f / Lf);
-      }
-      if (sure) ov = true;
+      // boxes that overlap on every axis by more than the FP32 margin (both narrow: no ambiguity) overlap
+      // in the exact test too (the FP32 copies of this rebuild, k_peri_sorted)
+      const float4 c1 = pci[id.x], h1 = phi[id.x], c2 = pci[id.y], h2 = phi[id.y];
+      const float L0 = (float)P.csize[0], L1 = (float)P.csize[1], L2 = (float)P.csize[2];
+      if (h1.w == 0.f && h2.w == 0.f && periNear(c1.x, h1.x, c2.x, h2.x, L0, 1.f / L0) &&
+          periNear(c1.y, h1.y, c2.y, h2.y, L1, 1.f / L1) && periNear(c1.z, h1.z, c2.z, h2.z, L2, 1.f / L2))
+        ov = true;
       else {
         int4 per; bool amb = false;
-        ov = overlapPeri(mn1, mx1, mn2, mx2, P.csize, per, amb);
+        ov = overlapPeri(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y], P.csize, per, amb);
       }
     } else ov = overlap3(p.bbmin[id.x], p.bbmax[id.x], p.bbmin[id.y], p.bbmax[id.y]);
     if (!ov) f = 1;
@@ -725,7 +718,8 @@ __global__ void k_cell_start_plain(const unsigned long long* keys, int nSmall, c
 // that axis for every period shift, so spatialOverlapPeri rejects them too, and it is evaluated (in
 // FP64, as the reference does) only for the survivors.  Boxes wider than a quarter of the cell skip
 // the filter (there the exact test may find an ambiguous contact, which is an error to report).
-__global__ void k_peri_sorted(StepParams P, Particles p, const unsigned* vals, int nSmall, float4* pc, float4* ph) {
+__global__ void k_peri_sorted(StepParams P, Particles p, const unsigned* vals, int nSmall, float4* pc, float4* ph,
+                              float4* pci, float4* phi) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nSmall) return;
   const int i = (int)vals[q];
@@ -743,6 +737,8 @@ __global__ void k_peri_sorted(StepParams P, Particles p, const unsigned* vals, i
   }
   pc[q] = make_float4(c[0], c[1], c[2], 0.f);
   ph[q] = make_float4(h[0], h[1], h[2], wide ? 1.f : 0.f);
+  pci[i] = pc[q];
+  phi[i] = ph[q];
 }
 
 
@@ -894,7 +890,7 @@ void col_retain_write_dist(cudaStream_t s, Contacts old, long long nOld, Collide
 }
 
 void col_retain_flags(cudaStream_t s, const StepParams& P, Particles p, Contacts old, long long nOld, ColliderScratch& cs) {
-  if (nOld > 0) (k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(P, p, old, nOld, cs.retainFlag), ++::wdem::g_kernel_launches);
+  if (nOld > 0) (k_retain_flag<<<(unsigned)((nOld + 255) / 256), 256, 0, s>>>(P, p, old, nOld, cs.retainFlag, cs.periCi, cs.periHi), ++::wdem::g_kernel_launches);
   exclusive_scan_u32(s, cs.retainFlag, nOld, cs);
 }
 void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base, long long cap) {
@@ -916,7 +912,7 @@ void col_periodic_cand(cudaStream_t s, const StepParams& P, Particles p, const i
     radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bitsFor((unsigned long long)cs.maxCols + 1), cs);
     int t = nSmall > 0 ? nSmall : (cs.maxCols + 1);
     (k_cell_start_plain<<<(t + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, g, cs.cellStart), ++::wdem::g_kernel_launches);
-    if (nSmall > 0) (k_peri_sorted<<<(nSmall + 255) / 256, 256, 0, s>>>(P, p, cs.vals, nSmall, cs.periC, cs.periH), ++::wdem::g_kernel_launches);
+    if (nSmall > 0) (k_peri_sorted<<<(nSmall + 255) / 256, 256, 0, s>>>(P, p, cs.vals, nSmall, cs.periC, cs.periH, cs.periCi, cs.periHi), ++::wdem::g_kernel_launches);
     (k_peri_cand<false><<<(threads + 127) / 128, 128, 0, s>>>(P, nSmall, g, cs.keys, cs.vals, cs.periC, cs.periH, cs.cellStart, cs.counts, nullptr, 0), ++::wdem::g_kernel_launches);
     exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
   } else {

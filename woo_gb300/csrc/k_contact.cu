@@ -486,10 +486,10 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
 // that launch_contacts starts
 template <int LAW, int CP2, bool PERI, bool ELL>
 __global__ void __launch_bounds__(128, 4) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
-                                                  const unsigned* count, DeviceStatus* st) {
-  const unsigned m = *count;
+                                                  const unsigned* count, long long nc, DeviceStatus* st) {
+  const unsigned m = workLen(count);
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
-    contactBody<LAW, CP2, PERI, ELL>(P, p, c, (long long)work[k], st);
+    contactBody<LAW, CP2, PERI, ELL>(P, p, c, (long long)workItem(work, count, nc, k), st);
 }
 
 // First pass over all contacts: resolves PENDING contacts (removePending of the collider: the broken
@@ -502,16 +502,19 @@ template <bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
                                                        unsigned* work, unsigned* count, DeviceStatus* st) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // the contact's state is loaded before the guard (its load is issued first, not after the guard's)
+  const uint8_t s0 = i < nc ? c.state[i] : (uint8_t)CS_DEAD;
   // a step queued behind a collider trigger: the work list stays empty, so the heavy pass is a no-op too
   if (haltedContacts(st, P.step)) return;
-  // the integrator's rotation list of this step has been consumed: its counter starts the next step at 0
+  // the integrator's lists of this step have been consumed: their counters start the next step at 0
   if (i == 0) { st->rotCount = 0; st->touchCount = 0; }
-  bool need = false;
+  bool need = false, realNow = false;
   if (i < nc) {
-    const uint8_t s0 = c.state[i];
     const uint8_t sb = s0 & CS_SHAPES;
     uint8_t s = s0 & CS_MASK;
-    if (s != CS_DEAD && sb != (CS_WALL_A | CS_WALL_B)) {
+    if (s == CS_POTENTIAL && !PERI && (s0 & CS_FAR)) {
+      // cannot touch before the next rebuild: nothing to load
+    } else if (s != CS_DEAD && sb != (CS_WALL_A | CS_WALL_B)) {
       const int2 id = c.ids[i];
       const int a = id.x, b = id.y;
       bool alive = true;
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
         else if (alive) { s = CS_POTENTIAL; c.state[i] = s | sb; }
       }
       if (alive) {
-        if (s == CS_REAL) need = true;
+        if (s == CS_REAL) need = realNow = true;
         else if (!(sb & CS_WALL_A)) {
           // Sphere/ellipsoid pairs: the FP32 copies carry a relative error below 2^-23 per coordinate and
           // radius; the margin (1e-5 relative on the contact distance plus 1e-6 x the sum of |coordinates|)
@@ -555,6 +558,11 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
           const float df = (ELL && (sb & CS_ELL)) ? 1.f : (float)fabs(P.distFactor);
           const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
           need = !(d2 > R * R);
+          if (!PERI && !need) {
+            // far: the distance exceeds the (error-padded) contact distance by 4 verletDist (CS_FAR)
+            const float Rf = (R + 4.f * P.verletHiF) * 1.00001f;
+            if (d2 > Rf * Rf) c.state[i] = (uint8_t)(CS_POTENTIAL | CS_FAR | sb);
+          }
         } else {
           // wall + sphere/ellipsoid: the distance along the wall axis against the radius (ellipsoids: the
           // largest semi-axis, an upper bound of the extent), with the same kind of margin
@@ -567,14 +575,23 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
       }
     }
   }
-  const unsigned ballot = __ballot_sync(0xffffffffu, need);
-  if (ballot) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1;
+  const unsigned bReal = __ballot_sync(0xffffffffu, need && realNow);
+  const unsigned bPot = __ballot_sync(0xffffffffu, need && !realNow);
+  if (bReal) {
+    const int leader = __ffs(bReal) - 1;
     unsigned base = 0;
-    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(ballot));
+    if (lane == leader) base = atomicAdd(&count[0], (unsigned)__popc(bReal));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (need) work[base + __popc(ballot & ((1u << lane) - 1))] = (unsigned)i;
+    if (need && realNow) work[base + __popc(bReal & below)] = (unsigned)i;
+  }
+  if (bPot) {
+    const int leader = __ffs(bPot) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(&count[1], (unsigned)__popc(bPot));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need && !realNow) work[nc - 1 - (base + __popc(bPot & below))] = (unsigned)i;
   }
 }
 
@@ -584,8 +601,8 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
     cudaMemsetAsync(&st->rotCount, 0, 2 * sizeof(unsigned), s);  // rotCount, touchCount; otherwise cleared by the cull kernel
     return;
   }
-  unsigned* count = &st->workCount;
-  cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+  unsigned* count = &st->workCount;  // workCount, workPot
+  cudaMemsetAsync(count, 0, 2 * sizeof(unsigned), s);
   const unsigned cb = (unsigned)((nc + 255) / 256);
   // the FP64 pass loops over the work list (length known on the device only): 4 blocks per SM fill the
   // GPU at its register count, and no more blocks are launched to find the list short
@@ -595,19 +612,19 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
     (k_contacts_cull<false, true><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
     if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF);
-    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
   } else if (P.periodic) {
     (k_contacts_cull<true, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
     if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
     else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
   } else {
     (k_contacts_cull<false, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
     if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
     else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, st), ++::wdem::g_kernel_launches);
+      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
   }
 }
 

@@ -6,6 +6,8 @@
 // One thread per particle.  The force on a particle is m*g (reset at the end of the previous step)
 // plus the contributions of its real contacts, added in the order of the contacts' (min id, max id)
 // keys; that fixed order makes the sum deterministic and identical to the CPU oracle's.
+#include <algorithm>
+
 #include "wdem_internal.h"
 #include "wdem_math.cuh"
 #include "../../include/wdem.h"
@@ -319,10 +321,52 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   }
 }
 
+// leapfrogSphericalRotate of a sphere with angVel != 0: q = AngleAxis(|w| dt, w/|w|) q, normalised.
+// A sphere's orientation feeds nothing else in the step (sphere contacts do not read it): it is
+// integrated to within a few ulp of the reference's operations at a fraction of their cost.  For the
+// half angles of a DEM step (h = |w| dt/2 < 1e-3) the Taylor polynomials sin h = h (1 - h^2/6 (1 -
+// h^2/20)) and cos h = 1 - h^2/2 (1 - h^2/12) (truncation errors h^7/5040 and h^6/720, far below an
+// ulp) need neither |w| nor the axis: the vector part sin(h) w/|w| = w dt/2 (1 - h^2/6 (1 - h^2/20))
+// with h^2 = |w|^2 dt^2/4.  The normalisation 1/sqrt(z) of a product of unit quaternions (|z - 1| a
+// few ulp) is its Taylor polynomial 1 - e/2 + 3e^2/8, e = z - 1 (error 5e^3/16, far below an ulp).
+__device__ __forceinline__ void rotateSphere(const StepParams& P, const Particles& p, unsigned i, d3 angVel, int mat) {
+  const double4_32a o4 = p.ori[i];
+  qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
+  const double dt = dtOf(P, mat);
+  const double w2 = sqnorm(angVel);
+  const double h2 = 0.25 * (w2 * (dt * dt));
+  qd q;
+  if (h2 < 1e-6) {
+    const double f = (0.5 * dt) * (1.0 - h2 * (1.0 / 6.0) * (1.0 - h2 * 0.05));
+    q.w = 1.0 - h2 * 0.5 * (1.0 - h2 * (1.0 / 12.0));
+    q.x = angVel.x * f; q.y = angVel.y * f; q.z = angVel.z * f;
+  } else {
+    WDEM_REAL_BRANCH();
+    const double angle = sqrt(w2);
+    const double inv = 1.0 / angle;
+    double sh, ch;
+    sincos(0.5 * (angle * dt), &sh, &ch);
+    q.w = ch; q.x = sh * (angVel.x * inv); q.y = sh * (angVel.y * inv); q.z = sh * (angVel.z * inv);
+  }
+  ori = qmul(q, ori);
+  const double z2 = ori.x * ori.x + ori.y * ori.y + ori.z * ori.z + ori.w * ori.w;
+  if (!isOneBits(z2)) {
+    double rn;
+    const double e = z2 - 1.0;
+    if (fabs(e) < 1e-6) rn = 1.0 - e * (0.5 - 0.375 * e);
+    else {
+      WDEM_REAL_BRANCH();
+      rn = z2 > 0 ? 1.0 / sqrt(z2) : 1.0;
+    }
+    ori.x *= rn; ori.y *= rn; ori.z *= rn; ori.w *= rn;
+  }
+  p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+}
+
 // The same step as k_leapfrog<false, PERI, false> without energy tracking, for one particle, issuing
 // fewer FP64 operations with bit-identical results:
 //  - the CSR gather runs only for particles that a real contact touched in the last contact pass
-//    (p.touched, set by the contact kernel; those run in k_leapfrog_touched); the others get m g;
+//    (p.touched, set by the contact kernel; those run in k_leapfrog_lists); the others get m g;
 //  - Sign(F (v + dt/2 a)) of the damping comes from the sign bits (signProd) and the factor
 //    1 - damping Sign(...) from two constants; zero accelerations and velocities skip their updates
 //    (addScaled: adding a zero changes only -0);
@@ -490,8 +534,9 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   int mx = meta.x;
   bool rotate = false;
   if (!isZeroBits(angVel)) {
-    // rotated by k_rotate_list after this kernel: spinning spheres are scattered over most warps, and
-    // the rotation would make every such warp wait for its few spinning lanes
+    // untouched spheres: rotated from the rotation list in the second pass (spinning spheres are
+    // scattered over most warps, whose FP64 pipe would wait for their few spinning lanes); the second
+    // pass's own (touched) particles rotate here
     rotate = true;
     mx &= ~META_ORI_FIXED;
   } else if (!(mx & META_ORI_FIXED)) {
@@ -513,7 +558,9 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   if (!finiteBits(pos.x) || !finiteBits(pos.y) || !finiteBits(pos.z)) {
     if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = i;
   }
-  {
+  if (touchedNow) {
+    if (rotate) rotateSphere(P, p, (unsigned)i, angVel, meta.y);
+  } else {
     const unsigned am = __activemask();
     const unsigned b = __ballot_sync(am, rotate);
     if (b) {
@@ -534,6 +581,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   const float err = 2.5e-7f * S + 1e-6f * df;
   bool dirty = false;
   if (!(df + err < P.verletLoF)) {
+    WDEM_REAL_BRANCH();
     const double4_32a lp = p.lastPos[i];
     const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
     dirty = sqnorm(dd) > P.maxD2;
@@ -548,8 +596,12 @@ template <bool PERI>
 __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
                                                         DeviceStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || haltedIntegrator(st, P.step)) return;
-  const bool listed = ((unsigned)p.meta[i].w & 63u) != 63u && p.touched[i] != 0;
+  if (i >= n) return;
+  // the particle's first loads are issued before the guard's, not after it
+  const unsigned fl = (unsigned)p.meta[i].w;
+  const uint8_t tch = p.touched[i];
+  if (haltedIntegrator(st, P.step)) return;
+  const bool listed = (fl & 63u) != 63u && tch != 0;
   const unsigned am = __activemask();
   const unsigned b = __ballot_sync(am, listed);
   if (b) {
@@ -564,55 +616,38 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
   integrateFast<PERI>(P, p, i, n, c, csr, st, false);
 }
 
-// Second pass: the listed particles, with their CSR force gather.
+// Second pass, over two lists: the touched particles (CSR force gather, full integration, rotation
+// inline), then the rotation list of the first pass.
 template <bool PERI>
-__global__ void __launch_bounds__(256) k_leapfrog_touched(StepParams P, Particles p, int n, Contacts c, Csr csr,
-                                                           DeviceStatus* st) {
+__global__ void __launch_bounds__(256) k_leapfrog_lists(StepParams P, Particles p, int n, Contacts c, Csr csr,
+                                                         DeviceStatus* st) {
   if (haltedIntegrator(st, P.step)) return;
-  const unsigned m = st->touchCount < (unsigned)n ? st->touchCount : (unsigned)n;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
-    const int i = (int)p.touchList[k];
-    p.touched[i] = 0;
-    integrateFast<PERI>(P, p, i, n, c, csr, st, true);
+  const unsigned nt = st->touchCount < (unsigned)n ? st->touchCount : (unsigned)n;
+  const unsigned nr = st->rotCount < (unsigned)n ? st->rotCount : (unsigned)n;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nt + nr; k += gridDim.x * blockDim.x) {
+    if (k < nt) {
+      const int i = (int)p.touchList[k];
+      p.touched[i] = 0;
+      integrateFast<PERI>(P, p, i, n, c, csr, st, true);
+    } else {
+      const unsigned i = p.rotList[k - nt];
+      rotateSphere(P, p, i, xyz(p.angw[i]), p.meta[i].y);
+    }
   }
 }
 
-// leapfrogSphericalRotate of the spheres k_leapfrog_fast listed: q = AngleAxis(|w| dt, w/|w|) q, normalised.
-// A sphere's orientation feeds nothing else in the step (sphere contacts do not read it): it is
-// integrated to within a few ulp of the reference's operations at a fraction of their cost --
-// reciprocals instead of the divisions, and for the half angles of a DEM step (|x| < 1e-3) the Taylor
-// polynomials sin x = x (1 - x^2/6 (1 - x^2/20)), cos x = 1 - x^2/2 (1 - x^2/12), whose truncation
-// errors (x^7/5040, x^6/720) are far below an ulp.
-__global__ void __launch_bounds__(256) k_rotate_list(StepParams P, Particles p, const DeviceStatus* st, unsigned cap) {
-  if (haltedIntegrator(st, P.step)) return;
-  const unsigned m = st->rotCount < cap ? st->rotCount : cap;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
-    const unsigned i = p.rotList[k];
-    const d3 angVel = xyz(p.angw[i]);
-    const double4_32a o4 = p.ori[i];
-    qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
-    const double angle = sqrt(sqnorm(angVel));
-    const double inv = 1.0 / angle;
-    const d3 axis = angVel * inv;
-    const double ha = 0.5 * (angle * dtOf(P, p.meta[i].y));
-    double sh, ch;
-    if (fabs(ha) < 1e-3) {
-      const double h2 = ha * ha;
-      sh = ha * (1.0 - h2 * (1.0 / 6.0) * (1.0 - h2 * 0.05));
-      ch = 1.0 - h2 * 0.5 * (1.0 - h2 * (1.0 / 12.0));
-    } else {
-      WDEM_REAL_BRANCH();
-      sincos(ha, &sh, &ch);
-    }
-    qd q; q.w = ch; q.x = sh * axis.x; q.y = sh * axis.y; q.z = sh * axis.z;
-    ori = qmul(q, ori);
-    const double z2 = ori.x * ori.x + ori.y * ori.y + ori.z * ori.z + ori.w * ori.w;
-    if (z2 > 0 && !isOneBits(z2)) {
-      const double rn = 1.0 / sqrt(z2);
-      ori.x *= rn; ori.y *= rn; ori.z *= rn; ori.w *= rn;
-    }
-    p.ori[i] = make_double4_32a(ori.w, ori.x, ori.y, ori.z);
+// resident blocks of the list pass on the whole GPU (one wave; queried once per instantiation)
+template <bool PERI>
+static unsigned listGrid() {
+  static unsigned g = 0;
+  if (g == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_leapfrog_lists<PERI>, 256, 0);
+    g = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per);
   }
+  return g;
 }
 
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays, Contacts c, Csr csr,
@@ -620,16 +655,17 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
   if (n <= 0) return;
   unsigned blocks = (n + 255) / 256;
   if (!fromArrays && !P.hasEll && !P.lfEnergy && p.touched && p.rotList) {
-    // st->rotCount is zero here: k_contacts_cull clears it for the next step (and the handle starts at zero)
-    const unsigned rb = blocks < 152 * 4 ? blocks : 152 * 4;
+    // st->rotCount and st->touchCount are zero here: k_contacts_cull clears them for the next step (and
+    // the handle starts at zero)
     if (P.periodic) {
+      const unsigned rb = std::min(blocks, listGrid<true>());
       (k_leapfrog_fast<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
-      (k_leapfrog_touched<true><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      (k_leapfrog_lists<true><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     } else {
+      const unsigned rb = std::min(blocks, listGrid<false>());
       (k_leapfrog_fast<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
-      (k_leapfrog_touched<false><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      (k_leapfrog_lists<false><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     }
-    (k_rotate_list<<<rb, 256, 0, s>>>(P, p, st, (unsigned)n), ++::wdem::g_kernel_launches);
     return;
   }
   if (P.hasEll) {
@@ -642,6 +678,58 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
     if (fromArrays) (k_leapfrog<true, false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     else (k_leapfrog<false, false, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
   }
+}
+
+// DynDt::nodalCritDtSq (DynDt.cpp:46-63) with nodalStiffAdd (DynDt.cpp:16-38): the squared critical
+// step of a node from the stiffnesses of its real contacts, visited in the order of the partner ids
+// (Particle::contacts, a map by id); the contact normal is the contact node's orientation applied to
+// the x axis, Eigen's n.array().pow(2) is the squares n*n, L6Geom.lens of sphere contacts are the radii
+// (a wall's lens is the sphere's radius).  The minimum over nodes is exact in any order: positive
+// doubles order as their bit patterns (kept complemented, so that zero means none).
+__global__ void k_dyndt(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned flags = (unsigned)p.meta[i].w;
+  if ((flags & 63u) == 63u) return;  // completely blocked: always stable (Inf)
+  d3 kt3 = mk(0, 0, 0), kr3 = mk(0, 0, 0);
+  const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
+  for (int e = e0; e < e1; e++) {
+    const unsigned en = csr.ent[e];
+    const unsigned ci = en & 0x7fffffffu;
+    if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
+    const bool isB = (en >> 31) != 0;
+    const double kn = c.hist[HIST_KN][ci], kt = c.hist[HIST_KT][ci];
+    const d3 c0 = mk(c.hist[HIST_T0X][ci], c.hist[HIST_T0Y][ci], c.hist[HIST_T0Z][ci]);
+    const d3 c1 = mk(c.hist[HIST_T1X][ci], c.hist[HIST_T1Y][ci], c.hist[HIST_T1Z][ci]);
+    const qd ori = quatFromCols(c0, c1, cross(c0, c1));
+    const d3 nrm = qrot(ori, mk(1, 0, 0));
+    const d3 n2 = mk(nrm.x * nrm.x, nrm.y * nrm.y, nrm.z * nrm.z);
+    const double knt = kn - kt;
+    kt3 = mk(kt3.x + (n2.x * knt + kt), kt3.y + (n2.y * knt + kt), kt3.z + (n2.z * knt + kt));
+    // lens[ix]: the radius of this node's sphere; a wall takes the sphere's (|-r|)
+    const int2 id = c.ids[ci];
+    const int other = isB ? id.x : id.y;
+    const bool wallA = (c.state[ci] & CS_WALL_A) != 0;
+    const double len = (!isB && wallA) ? p.posr[other].w : p.posr[i].w;
+    const double sc = (len * len) * kt;
+    kr3 = mk(kr3.x + sc * (n2.y + n2.z), kr3.y + sc * (n2.z + n2.x), kr3.z + sc * (n2.x + n2.y));
+  }
+  const double mass = p.velm[i].w;
+  const d3 inertia = xyz(p.inert[i]);
+  double ret = __longlong_as_double(0x7ff0000000000000ll);
+  const double kt[3] = {kt3.x, kt3.y, kt3.z}, kr[3] = {kr3.x, kr3.y, kr3.z}, in[3] = {inertia.x, inertia.y, inertia.z};
+  for (int k = 0; k < 3; k++)
+    if (kt[k] != 0 && mass > 0. && !(flags & (1u << k))) { const double v = mass / fabs(kt[k]); ret = v < ret ? v : ret; }
+  for (int k = 0; k < 3; k++)
+    if (kr[k] != 0 && in[k] > 0. && !(flags & (8u << k))) { const double v = in[k] / fabs(kr[k]); ret = v < ret ? v : ret; }
+  ret = 2 * ret;
+  if (!(ret < __longlong_as_double(0x7ff0000000000000ll))) return;  // Inf (or NaN): no bound from this node
+  atomicMax(&st->dynNotMin, ~(unsigned long long)__double_as_longlong(ret));
+}
+
+void launch_dyndt(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
+  if (n <= 0) return;
+  (k_dyndt<<<(n + 127) / 128, 128, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
 }
 
 // DemData.force/torque as Woo holds them after ContactLoop (reset to m*g by Leapfrog, then contacts)

@@ -141,17 +141,17 @@ __device__ __forceinline__ void loadNet(NetSmem& net, const uint16_t* wbf, const
 // lam0 of every ellipsoid pair (sphere + ellipsoid included; walls excluded) that the contact kernel
 // may solve this step; other entries are NaN (cold start).
 __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const unsigned* work, const unsigned* count,
-                                                  const uint16_t* wbf, const float* wf) {
+                                                  long long ncon, const uint16_t* wbf, const float* wf) {
   extern __shared__ __align__(16) unsigned char smem[];
   NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
   WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
   loadNet(net, wbf, wf);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   WarpSmem& ws = wsAll[warp];
-  const long long nw = *count;
+  const long long nw = workLen(count);
   for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < nw; base += (long long)gridDim.x * SAMPLES) {
     const long long kw = base + (lane & 15);
-    const long long i = kw < nw ? (long long)work[kw] : -1;
+    const long long i = kw < nw ? (long long)workItem(work, count, ncon, (unsigned)kw) : -1;
     bool use = false;
     if (lane < 16) {
       float f[ELL_FEATURES];
@@ -382,7 +382,7 @@ void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, cons
   if (nc <= 0) return;
   long long blocks = (nc + SAMPLES - 1) / SAMPLES;
   if (blocks > 152 * 2) blocks = 152 * 2;  // persistent blocks: the weights are loaded once per block
-  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, wbf, wf), ++::wdem::g_kernel_launches);
+  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, nc, wbf, wf), ++::wdem::g_kernel_launches);
 }
 
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf) {

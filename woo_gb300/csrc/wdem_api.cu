@@ -168,6 +168,11 @@ struct wdem_handle {
   int maxAhead = 32;
   double rebuildInterval = 16;
   int sinceRebuild = 0;
+  // DynDt as a PeriodicEngine (Engine.hpp:130-160): stepLast / stepPrev, Scene.nextDt, last critical step
+  long long dynStepLast = -1, dynStepPrev = -1;
+  double nextDt = std::numeric_limits<double>::quiet_NaN();
+  double dynDtCrit = std::numeric_limits<double>::quiet_NaN();
+  double timeSum = 0;  // sum of dt over the steps run
   int updatePhys = 0;
   double verletDistResolved = 0;
   bool verletResolved = false;
@@ -339,6 +344,7 @@ int ensureScratch(wdem_handle* h, long long nc) {
   if (h->periodic && (long long)h->smallIds.size() + 1 > cs.periCap) {
     long long cap = (long long)h->smallIds.size() + 1;
     CK(dalloc(cs.periC, cap)); CK(dalloc(cs.periH, cap));
+    CK(dalloc(cs.periCi, (size_t)h->N + 1)); CK(dalloc(cs.periHi, (size_t)h->N + 1));
     cs.periCap = cap;
   }
   long long needRetain = std::max<long long>(h->nContacts, nc) + 2;
@@ -495,6 +501,7 @@ void fillStepParams(wdem_handle* h) {
   P.verletDist = h->verletDistResolved;
   P.maxD2 = h->verletDistResolved * h->verletDistResolved;
   P.verletLoF = (float)(h->verletDistResolved * (1 - 1e-6));
+  P.verletHiF = (float)(h->verletDistResolved * (1 + 1e-6));
   P.dampM = 1.0 - r.damping * 1.0;
   P.dampP = 1.0 - r.damping * -1.0;
   P.noRatch = r.noRatch; P.iniLensTouch = r.iniLensTouch; P.trsfRenorm = r.trsfRenorm; P.approxMask = r.approxMask;
@@ -664,7 +671,7 @@ int wdem_destroy(wdem_handle* h) {
   ColliderScratch& cs = h->cs;
   cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
   cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid);
-  cudaFree(cs.retainFlag); cudaFree(cs.temp); cudaFree(cs.periC); cudaFree(cs.periH);
+  cudaFree(cs.retainFlag); cudaFree(cs.temp); cudaFree(cs.periC); cudaFree(cs.periH); cudaFree(cs.periCi); cudaFree(cs.periHi);
   cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag);
   cudaFree(h->dst);
   cudaFree(h->staging);
@@ -940,6 +947,59 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
 // the configurations whose host-side per-step work is none are queued: no periodic cell (integrated on
 // the host each step), no energy tracking (host-launched reductions), no updatePhys='once', no phase
 // timing.
+// pown (src/supp/base/Math.hpp:166-175): x^n by squaring, x^n = (x^2)^(n/2) x^(n%2)
+static double powUint(double x, unsigned n) {
+  const unsigned d = n >> 1, r = n & 1;
+  const double x2d = d == 0 ? 1 : powUint(x * x, d);
+  const double xr = r == 0 ? 1 : x;
+  return x2d * xr;
+}
+
+// PeriodicEngine::isActivated for a step period with stepModulo (Engine.cpp:170-196), from the second
+// call on (the first call only records stepLast, see wdem_step)
+static bool dynDtDue(const wdem_handle* h, long long s) {
+  const long long per = h->raw.dynDtPeriod;
+  return per > 0 && ((s - h->dynStepLast >= per) || (s % per == 0));
+}
+// the first step >= s at which DynDt runs
+static long long dynDtNext(const wdem_handle* h, long long s) {
+  const long long per = h->raw.dynDtPeriod;
+  if (per <= 0) return std::numeric_limits<long long>::max();
+  const long long mult = (s + per - 1) / per * per;
+  return std::min(mult, std::max(s, h->dynStepLast + per));
+}
+// DynDt::run (DynDt.cpp:86-113) after the contact pass of step s, when due
+static int dynDtAfterContacts(wdem_handle* h, long long s) {
+  if (!dynDtDue(h, s)) return WDEM_OK;
+  h->dynStepPrev = h->dynStepLast;
+  h->dynStepLast = s;
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(&h->dst->dynNotMin, 0, sizeof(unsigned long long), st));
+  launch_dyndt(st, h->P, h->d, h->n, h->buf[h->cur].c, h->csr, h->dst);
+  unsigned long long v = 0;
+  CK(cudaMemcpyAsync(h->hcounts + 2, &h->dst->dynNotMin, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::memcpy(&v, h->hcounts + 2, sizeof v);
+  double sq = std::numeric_limits<double>::infinity();
+  if (v != 0) { const unsigned long long b = ~v; std::memcpy(&sq, &b, sizeof sq); }
+  const double crDt = std::sqrt(sq);  // DynDt::critDt_stiffness
+  h->dynDtCrit = crDt;
+  if (std::isinf(crDt)) return WDEM_OK;  // no timestep computed, keep the current one
+  const long long nSteps = s - h->dynStepPrev;
+  const double dt = h->raw.dt;
+  const double maxNewDt = dt * powUint(1. + h->raw.dynDtMaxRelInc, (unsigned)nSteps);
+  const double nextDt = std::min(crDt * h->raw.dtSafety, maxNewDt);
+  if (nextDt != dt) h->nextDt = nextDt;
+  return WDEM_OK;
+}
+// Scene::doOneStep epilogue (Scene.cpp:432): a new dt from DynDt takes effect for the next step
+static void applyNextDt(wdem_handle* h) {
+  if (std::isnan(h->nextDt)) return;
+  h->raw.dt = h->nextDt;
+  h->P.dt = h->nextDt;
+  h->nextDt = std::numeric_limits<double>::quiet_NaN();
+}
+
 static int queueDepth(wdem_handle* h, int left) {
   if (left < 2 || h->timing || h->periodic || h->P.trackEnergy || h->needRebuild || h->forcesInArrays ||
       h->verletDistResolved == 0 || h->updatePhys == WDEM_UPDATE_PHYS_ONCE || h->maxAhead < 2)
@@ -948,7 +1008,11 @@ static int queueDepth(wdem_handle* h, int left) {
   // trigger against the round trips saved
   int q = (int)std::lround(std::sqrt(3.0 * h->rebuildInterval));
   q = std::max(2, std::min(q, h->maxAhead));
-  return std::min(q, left);
+  q = std::min(q, left);
+  // DynDt runs on the host side of its step: the queue ends there
+  const long long toDyn = dynDtNext(h, h->step) - h->step + 1;
+  if (toDyn < q) q = (int)std::max<long long>(1, toDyn);
+  return q;
 }
 
 static int runQueued(wdem_handle* h, int ahead, int& done) {
@@ -989,9 +1053,13 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
     done = (int)(k - s0) + 1;
     h->lastRunFull = 1;
   }
+  // the queue ends at or before the next DynDt step: run it if the last completed step is due
+  if ((rc = dynDtAfterContacts(h, s0 + done - 1))) return rc;
   h->step = s0 + done;
   h->P.step = h->step;
   h->raw.step = h->step;
+  for (int k = 0; k < done; k++) h->timeSum += h->raw.dt;  // Scene.time += dt per step
+  applyNextDt(h);
   return WDEM_OK;
 }
 
@@ -1014,6 +1082,12 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     return fail(h, WDEM_ERR_ARG, "newtonTol must be positive");
   if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP && !h->mlpReady)
     return fail(h, WDEM_ERR_STATE, "warmStart=MLP needs a network (wdem_warm_init / wdem_warm_set_weights / wdem_warm_train)");
+  if (h->raw.dynDtPeriod > 0 && (h->hasEll || h->raw.materialDt))
+    return fail(h, WDEM_ERR_UNSUPPORTED, "DynDt runs with sphere and wall scenes of one dt only");
+  if (h->raw.dynDtPeriod > 0 && !(1. + h->raw.dynDtMaxRelInc != 1.))
+    return fail(h, WDEM_ERR_ARG, "DynDt: maxRelInc too small (1.0+maxRelInc==1.0)");
+  // PeriodicEngine::isActivated, first call: counting starts at this step
+  if (h->raw.dynDtPeriod > 0 && h->dynStepLast < 0) h->dynStepLast = h->step;
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
   for (int k = 0; k < 3; k++) { h->phaseMs[k] = 0; h->phaseLaunches[k] = 0; }
@@ -1100,10 +1174,13 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
       energy_accumulate(s, cc.energy[EC_BROKEN], nc, h->ePartials, h->dEnergy + WDEM_E_BROKEN, false);
     }
     if (h->updatePhys == WDEM_UPDATE_PHYS_ONCE) { h->updatePhys = WDEM_UPDATE_PHYS_NEVER; h->raw.updatePhys = WDEM_UPDATE_PHYS_NEVER; }
+    if ((rc = dynDtAfterContacts(h, h->step))) return rc;  // DynDt, the engine after ContactLoop
     if (h->periodic) h->cell.setNextGradV();  // epilogue (Scene.cpp:430)
     h->step++;
     h->P.step = h->step;
     h->raw.step = h->step;
+    h->timeSum += h->raw.dt;
+    applyNextDt(h);
   }
   CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -1340,6 +1417,9 @@ int wdem_get_status(wdem_handle* h, wdem_status* st) {
   st->ellSolves = (int64_t)h->hst->ellSolves;
   st->ellIters = (int64_t)h->hst->ellIters;
   st->ellFallbacks = (int64_t)h->hst->ellFallbacks;
+  st->dt = h->raw.dt;
+  st->dynDtCrit = h->dynDtCrit;
+  st->timeSum = h->timeSum;
   return WDEM_OK;
 }
 

@@ -35,6 +35,10 @@ extern long long g_kernel_launches;
 // contact state byte: bits 0-1 the lifecycle state, bit 2 "pA is a wall", bit 3 "pB is a wall"
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
 enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_ELL_B = 32, CS_ELL = 48, CS_SHAPES = 60 };
+// a potential pair that cannot touch before the next collider run (set by the contact cull, dropped by
+// the rebuild's carry): every particle stays within verletDist of its position at the last rebuild,
+// so two bounding spheres come closer by at most 4 verletDist between any two steps without a rebuild
+enum : uint8_t { CS_FAR = 64 };
 // meta.x: shape (bits 0-3), wall axis (4-5), wall sense + 1 (8-9), aspherical Leapfrog (bit 12)
 // META_ORI_FIXED: the orientation is not rotating and normalising it is the identity (set and cleared by the
 // integrator); META_IPOS: all inertia components are positive (set at upload)
@@ -71,6 +75,7 @@ struct StepParams {
   double verletDist;        // resolved, >= 0
   double maxD2;             // verletDist^2
   float verletLoF;          // FP32 lower bound of verletDist (FP32 verlet trigger)
+  float verletHiF;          // FP32 upper bound of verletDist (far-pair screen of the contact cull)
   double dampM, dampP;      // 1 - damping * 1 and 1 - damping * (-1), the nonviscDamp2nd factors
   int gravAxis;             // the only non-zero gravity component, or -1 (angw.w then holds RN(RN(m g)/m))
   int noRatch, iniLensTouch, trsfRenorm, approxMask;
@@ -171,13 +176,23 @@ struct DeviceStatus {
   long long haltAt;   // 0, or 1 + the step whose integrator raised the collider trigger (see haltedIntegrator)
   unsigned long long pairTotal;
   unsigned long long ellSolves, ellIters, ellFallbacks;  // ellipsoid solves / Newton iterations (Brent: evaluations) / MLP fallbacks
-  unsigned workCount;  // length of the contact work list of this step
+  unsigned workCount;  // contact work list of this step: real contacts at work[0 .. workCount)
+  unsigned workPot;    //   potential pairs near touching at work[nc - workPot .. nc), in reverse
   unsigned rotCount;   // length of the rotation list of this step
   unsigned touchCount; // length of the touched-particle list of this step
+  unsigned long long dynNotMin;  // DynDt: ~bits of the smallest nodal critical step^2 (0: none yet)
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
 
 #ifdef __CUDACC__
+// The work list: real contacts from the front, potential pairs from the back (so that the warps of the
+// FP64 pass run either the full geometry + law path or the short rejection, not both); wc points to
+// DeviceStatus.workCount (followed by workPot).
+__device__ __forceinline__ unsigned workLen(const unsigned* wc) { return wc[0] + wc[1]; }
+__device__ __forceinline__ unsigned workItem(const unsigned* work, const unsigned* wc, long long nc, unsigned k) {
+  return k < wc[0] ? work[k] : work[nc - 1 - (k - wc[0])];
+}
+
 // Steps queued ahead of the host's collider check.  The integrator of step s that raises the collider
 // trigger also stores haltAt = s + 1; from then on the contact pass of step s and every kernel of the
 // later steps return at once, until the host has rebuilt the pair set, cleared the trigger and run the
@@ -199,6 +214,8 @@ __device__ __forceinline__ bool haltedContacts(const DeviceStatus* st, long long
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays,
                      Contacts c, Csr csr, DeviceStatus* st);
 void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr);
+// DynDt: the smallest nodal critical step^2 into st->dynNotMin (as ~bits; cleared by the caller)
+void launch_dyndt(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st);
 void launch_state_in(cudaStream_t s, Particles p, int n, const double* pos, const double* vel, const double* angVel,
                      const double* ori);
 void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* vel, double* angVel, double* ori);
@@ -234,6 +251,7 @@ struct ColliderScratch {
   unsigned* retainFlag;                 // old contacts retained (scanned in place)
   long long retainCap;
   float4 *periC, *periH;                // periodic: wrapped FP32 box centres / half-widths in cell order
+  float4 *periCi, *periHi;              //   the same by particle id
   long long periCap;
   int2* cand;                           // periodic: FP32 candidate pairs, their exact-test flags
   int4* candPer;                        //   (scanned in place) and cellDist

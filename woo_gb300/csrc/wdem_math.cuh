@@ -216,6 +216,7 @@ __device__ __forceinline__ float truncF(double x) {
   if (e >= 897 && e <= 1150)
     return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull) | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffull));
   if ((b << 1) == 0) return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull));
+  WDEM_REAL_BRANCH();
   return (float)x;
 }
 

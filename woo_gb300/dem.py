@@ -646,8 +646,10 @@ class ContactLoop(Engine):
 
 
 class DynDt(Engine):
-    """DynDt (src/dem/DynDt.hpp): not run by the GPU engine."""
-    _defaults = dict(stepPeriod=100)
+    """DynDt (src/dem/DynDt.hpp:5-27): adjusts Scene.dt from the contact stiffnesses every stepPeriod
+    steps (a PeriodicEngine with stepModulo); run by the GPU engine after its contact pass (sphere and
+    wall scenes).  dryRun is not provided."""
+    _defaults = dict(stepPeriod=100, maxRelInc=1e-4, dryRun=False)
 
 
 _UPDATE_PHYS = {"never": abi.UPDATE_PHYS_NEVER, "always": abi.UPDATE_PHYS_ALWAYS, "once": abi.UPDATE_PHYS_ONCE}
@@ -845,7 +847,19 @@ class GpuDemEngine(Engine):
             if c._edited:
                 self._h.set_cell(c.hSize, c.trsf, c.gradV, c.nextGradV)
                 c._edited = False
+        dyn = getattr(self, "_dynDt", None)
+        if dyn is not None and dyn.dryRun:
+            raise RuntimeError("DynDt.dryRun is not supported by the GPU engine")
+        p.dynDtPeriod = int(dyn.stepPeriod) if dyn is not None else 0
+        p.dynDtMaxRelInc = float(dyn.maxRelInc) if dyn is not None else 1e-4
+        p.dtSafety = float(scene.dtSafety)
+        if dyn is not None:
+            self._h.set_params(p)
+        t0 = self._h.status().timeSum
         self._h.step(nSteps)
+        st = self._h.status()
+        self._ran_time = st.timeSum - t0
+        scene.dt = st.dt
         if getattr(scene, "periodic", False):
             cc = self._h.cell()
             scene.cell._sync(cc)

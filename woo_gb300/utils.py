@@ -10,7 +10,7 @@ def defaultEngines(damping=0.0, gravity=None, verletDist=-0.05, kinSplit=False, 
                    noBreak=False, cp2=None, law=None, model=None, collider="sap", grid=None, dynDtPeriod=100,
                    cpKw={}, lawKw={}):
     """py/utils.py:94-129: [Leapfrog(reset=True), InsertionSortCollider, ContactLoop(...)] (+ DynDt).
-    Pass dynDtPeriod=0 to leave DynDt out (the GPU engine does not run it)."""
+    dynDtPeriod=0 leaves DynDt out."""
     if gravity:
         raise ValueError("gravity MUST NOT be specified anymore, set DemField.gravity=... instead.")
     if model is not None:
