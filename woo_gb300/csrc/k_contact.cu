@@ -12,6 +12,8 @@
 // Instead of adding into particles under a mutex (DemData::addForceTorque, Particle.hpp:249) each
 // real contact writes its global force and the torques on both particles; the integrator sums them
 // per particle through the CSR in a fixed order.
+#include <algorithm>
+
 #include "wdem_internal.h"
 #include "wdem_math.cuh"
 #include "wdem_peri.cuh"
@@ -498,83 +500,84 @@ __global__ void __launch_bounds__(128, 4) k_contacts(StepParams P, Particles p, 
 // cannot touch with FP32 tests whose margins exceed their rounding (the exact FP64 test would reject
 // them too).  Survivors (real contacts and potential pairs near touching) are appended to the work list;
 // the list order is irrelevant because each contact is processed independently.
+// One contact of the cull (see k_contacts_cull): need = the FP64 pass must see it this step, real = it
+// is a real contact; returns false when the contact can be left out of the pass until the next
+// rebuild (dead, wall + wall, or far).
 template <bool PERI, bool ELL>
-__global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
-                                                       unsigned* work, unsigned* count, DeviceStatus* st) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  // the contact's state is loaded before the guard (its load is issued first, not after the guard's)
-  const uint8_t s0 = i < nc ? c.state[i] : (uint8_t)CS_DEAD;
-  // a step queued behind a collider trigger: the work list stays empty, so the heavy pass is a no-op too
-  if (haltedContacts(st, P.step)) return;
-  // the integrator's lists of this step have been consumed: their counters start the next step at 0
-  if (i == 0) { st->rotCount = 0; st->touchCount = 0; }
-  bool need = false, realNow = false;
-  if (i < nc) {
-    const uint8_t sb = s0 & CS_SHAPES;
-    uint8_t s = s0 & CS_MASK;
-    if (s == CS_POTENTIAL && !PERI && (s0 & CS_FAR)) {
-      // cannot touch before the next rebuild: nothing to load
-    } else if (s != CS_DEAD && sb != (CS_WALL_A | CS_WALL_B)) {
-      const int2 id = c.ids[i];
-      const int a = id.x, b = id.y;
-      bool alive = true;
-      if (s == CS_PENDING) {
-        bool ov;
+__device__ __forceinline__ bool cullOne(const StepParams& P, const Particles& p, const Contacts& c, long long nc,
+                                        long long i, uint8_t s0, DeviceStatus* st, bool& need, bool& realNow) {
+  const uint8_t sb = s0 & CS_SHAPES;
+  uint8_t s = s0 & CS_MASK;
+  if (s == CS_POTENTIAL && !PERI && (s0 & CS_FAR)) {
+    // cannot touch before the next rebuild: nothing to load
+  } else if (s != CS_DEAD && sb != (CS_WALL_A | CS_WALL_B)) {
+    const int2 id = c.ids[i];
+    const int a = id.x, b = id.y;
+    bool alive = true;
+    if (s == CS_PENDING) {
+      bool ov;
+      if (PERI) {
+        int4 per;
+        bool amb = false;
+        ov = overlapPeri(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b], P.csize, per, amb);
+        if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = a; ov = true; alive = false; }
+      } else
+        ov = overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b]);
+      if (!ov) { c.state[i] = CS_DEAD | sb; alive = false; }
+      else if (alive) { s = CS_POTENTIAL; c.state[i] = s | sb; }
+    }
+    if (alive) {
+      if (s == CS_REAL) need = realNow = true;
+      else if (!(sb & CS_WALL_A)) {
+        // Sphere/ellipsoid pairs: the FP32 copies carry a relative error below 2^-23 per coordinate and
+        // radius; the margin (1e-5 relative on the contact distance plus 1e-6 x the sum of |coordinates|)
+        // exceeds the accumulated FP32 error, so a pair rejected here fails the exact FP64 test of
+        // Cg2_Sphere_Sphere_L6Geom (ellipsoids: it lies outside the bounding spheres, F_ab > 1).
+        // Pairs close to touching, NaN and overflow fall through to the FP64 test.
+        const float4 fa = p.posf[a];
+        float4 fb = p.posf[b];
+        float Sh = 0.f;
         if (PERI) {
-          int4 per;
-          bool amb = false;
-          ov = overlapPeri(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b], P.csize, per, amb);
-          if (amb) { if (atomicCAS(&st->code, 0, WDEM_ERR_TOO_BIG) == 0) st->detail = a; ov = true; alive = false; }
-        } else
-          ov = overlapBoxes(p.bbmin[a], p.bbmax[a], p.bbmin[b], p.bbmax[b]);
-        if (!ov) { c.state[i] = CS_DEAD | sb; alive = false; }
-        else if (alive) { s = CS_POTENTIAL; c.state[i] = s | sb; }
-      }
-      if (alive) {
-        if (s == CS_REAL) need = realNow = true;
-        else if (!(sb & CS_WALL_A)) {
-          // Sphere/ellipsoid pairs: the FP32 copies carry a relative error below 2^-23 per coordinate and
-          // radius; the margin (1e-5 relative on the contact distance plus 1e-6 x the sum of |coordinates|)
-          // exceeds the accumulated FP32 error, so a pair rejected here fails the exact FP64 test of
-          // Cg2_Sphere_Sphere_L6Geom (ellipsoids: it lies outside the bounding spheres, F_ab > 1).
-          // Pairs close to touching, NaN and overflow fall through to the FP64 test.
-          const float4 fa = p.posf[a];
-          float4 fb = p.posf[b];
-          float Sh = 0.f;
-          if (PERI) {
-            // FP32 image shift; its rounding is bounded by 2^-23 x sum |h_ij cellDist_j|, added to the margin
-            const int4 cd = c.cdist[i];
-            const float c0 = (float)cd.x, c1 = (float)cd.y, c2 = (float)cd.z;
-            const float h[9] = {(float)P.hS[0], (float)P.hS[1], (float)P.hS[2], (float)P.hS[3], (float)P.hS[4],
-                                (float)P.hS[5], (float)P.hS[6], (float)P.hS[7], (float)P.hS[8]};
-            fb.x += h[0] * c0 + h[1] * c1 + h[2] * c2;
-            fb.y += h[3] * c0 + h[4] * c1 + h[5] * c2;
-            fb.z += h[6] * c0 + h[7] * c1 + h[8] * c2;
-            for (int q = 0; q < 9; q++) Sh += fabsf(h[q]) * fabsf(q % 3 == 0 ? c0 : (q % 3 == 1 ? c1 : c2));
-          }
-          const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
-          const float d2 = dx * dx + dy * dy + dz * dz;
-          const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
-          const float df = (ELL && (sb & CS_ELL)) ? 1.f : (float)fabs(P.distFactor);
-          const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
-          need = !(d2 > R * R);
-          if (!PERI && !need) {
-            // far: the distance exceeds the (error-padded) contact distance by 4 verletDist (CS_FAR)
-            const float Rf = (R + 4.f * P.verletHiF) * 1.00001f;
-            if (d2 > Rf * Rf) c.state[i] = (uint8_t)(CS_POTENTIAL | CS_FAR | sb);
-          }
-        } else {
-          // wall + sphere/ellipsoid: the distance along the wall axis against the radius (ellipsoids: the
-          // largest semi-axis, an upper bound of the extent), with the same kind of margin
-          const int ax = (p.meta[a].x >> 4) & 3;
-          const float4 fa = p.posf[a], fb = p.posf[b];
-          const float ca = ax == 0 ? fa.x : (ax == 1 ? fa.y : fa.z), cb = ax == 0 ? fb.x : (ax == 1 ? fb.y : fb.z);
-          const float dist = fabsf(cb - ca);
-          need = !(dist > fb.w * 1.00001f + 1e-6f * (fabsf(ca) + fabsf(cb)));
+          // FP32 image shift; its rounding is bounded by 2^-23 x sum |h_ij cellDist_j|, added to the margin
+          const int4 cd = c.cdist[i];
+          const float c0 = (float)cd.x, c1 = (float)cd.y, c2 = (float)cd.z;
+          const float h[9] = {(float)P.hS[0], (float)P.hS[1], (float)P.hS[2], (float)P.hS[3], (float)P.hS[4],
+                              (float)P.hS[5], (float)P.hS[6], (float)P.hS[7], (float)P.hS[8]};
+          fb.x += h[0] * c0 + h[1] * c1 + h[2] * c2;
+          fb.y += h[3] * c0 + h[4] * c1 + h[5] * c2;
+          fb.z += h[6] * c0 + h[7] * c1 + h[8] * c2;
+          for (int q = 0; q < 9; q++) Sh += fabsf(h[q]) * fabsf(q % 3 == 0 ? c0 : (q % 3 == 1 ? c1 : c2));
         }
+        const float dx = fb.x - fa.x, dy = fb.y - fa.y, dz = fb.z - fa.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float S = fabsf(fa.x) + fabsf(fa.y) + fabsf(fa.z) + fabsf(fb.x) + fabsf(fb.y) + fabsf(fb.z) + 2.f * Sh;
+        const float df = (ELL && (sb & CS_ELL)) ? 1.f : P.distFactorF;
+        const float R = df * (fa.w + fb.w) * 1.00001f + 1e-6f * S;
+        need = !(d2 > R * R);
+        if (!PERI && !need) {
+          // far: the distance exceeds the (error-padded) contact distance by 4 verletDist (CS_FAR)
+          const float Rf = (R + 4.f * P.verletHiF) * 1.00001f;
+          if (d2 > Rf * Rf) c.state[i] = (uint8_t)(CS_POTENTIAL | CS_FAR | sb);
+        }
+      } else {
+        // wall + sphere/ellipsoid: the distance along the wall axis against the radius (ellipsoids: the
+        // largest semi-axis, an upper bound of the extent), with the same kind of margin
+        const int ax = (p.meta[a].x >> 4) & 3;
+        const float4 fa = p.posf[a], fb = p.posf[b];
+        const float ca = ax == 0 ? fa.x : (ax == 1 ? fa.y : fa.z), cb = ax == 0 ? fb.x : (ax == 1 ? fb.y : fb.z);
+        const float dist = fabsf(cb - ca);
+        need = !(dist > fb.w * 1.00001f + 1e-6f * (fabsf(ca) + fabsf(cb)));
       }
     }
   }
+  const uint8_t s1 = c.state[i];
+  return (s1 & CS_MASK) != CS_DEAD && (s1 & CS_SHAPES) != (CS_WALL_A | CS_WALL_B) && !(s1 & CS_FAR);
+}
+
+// warp-aggregated appends: the work list (real contacts from the front, potential pairs from the back)
+// and, in the full pass, the active list
+__device__ __forceinline__ void cullAppend(unsigned* work, unsigned* count, long long nc, long long i, bool need,
+                                           bool realNow, unsigned* act, unsigned* actCount, bool active) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1;
   const unsigned bReal = __ballot_sync(0xffffffffu, need && realNow);
@@ -593,34 +596,73 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
     base = __shfl_sync(0xffffffffu, base, leader);
     if (need && !realNow) work[nc - 1 - (base + __popc(bPot & below))] = (unsigned)i;
   }
+  if (act) {
+    const unsigned bAct = __ballot_sync(0xffffffffu, active);
+    if (bAct) {
+      const int leader = __ffs(bAct) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(actCount, (unsigned)__popc(bAct));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (active) act[base + __popc(bAct & below)] = (unsigned)i;
+    }
+  }
+}
+
+// First pass over the contacts: resolves PENDING contacts (removePending of the collider: the broken
+// contact dies when the boxes of the last rebuild no longer overlap, else it is potential again), skips
+// dead pairs and wall+wall pairs (no Cg2 functor, ContactLoop.cpp:149-150), and culls potential pairs that
+// cannot touch with FP32 tests whose margins exceed their rounding (the exact FP64 test would reject
+// them too).  Survivors (real contacts and potential pairs near touching) are appended to the work list;
+// the list order is irrelevant because each contact is processed independently.  FULL: one thread per
+// contact of the container, and the contacts that may need the pass before the next rebuild are
+// listed (act); otherwise the grid walks that list only.
+template <bool PERI, bool ELL, bool FULL>
+__global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
+                                                       unsigned* work, unsigned* count, DeviceStatus* st) {
+  const long long first = (long long)blockIdx.x * blockDim.x;
+  const long long m = FULL ? nc : (long long)st->actCount;
+  // a step queued behind a collider trigger: the work list stays empty, so the heavy pass is a no-op too
+  if (haltedContacts(st, P.step)) return;
+  // the integrator's lists of this step have been consumed: their counters start the next step at 0
+  if (first + threadIdx.x == 0) { st->rotCount = 0; st->touchCount = 0; }
+  const long long stride = FULL ? m + 1 : (long long)gridDim.x * blockDim.x;
+  for (long long base = first; base < m; base += stride) {
+    const long long k = base + threadIdx.x;
+    const long long i = k < m ? (FULL ? k : (long long)c.act[k]) : -1;
+    bool need = false, realNow = false, active = false;
+    if (i >= 0) active = cullOne<PERI, ELL>(P, p, c, nc, i, c.state[i], st, need, realNow);
+    cullAppend(work, count, nc, i, need, realNow, FULL ? c.act : nullptr, &st->actCount, active && FULL);
+  }
 }
 
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
-                     const uint16_t* warmBf, const float* warmF) {
+                     bool full, const uint16_t* warmBf, const float* warmF) {
   if (nc <= 0) {
     cudaMemsetAsync(&st->rotCount, 0, 2 * sizeof(unsigned), s);  // rotCount, touchCount; otherwise cleared by the cull kernel
     return;
   }
   unsigned* count = &st->workCount;  // workCount, workPot
   cudaMemsetAsync(count, 0, 2 * sizeof(unsigned), s);
-  const unsigned cb = (unsigned)((nc + 255) / 256);
+  if (full) cudaMemsetAsync(&st->actCount, 0, sizeof(unsigned), s);
+  // full pass: a thread per contact; list pass: a grid-stride walk of the active list
+  const unsigned cb = full ? (unsigned)((nc + 255) / 256) : (unsigned)std::min<long long>((nc + 255) / 256, 152 * 8);
   // the FP64 pass loops over the work list (length known on the device only): 4 blocks per SM fill the
   // GPU at its register count, and no more blocks are launched to find the list short
   const long long hb0 = (nc + 127) / 128;
   const unsigned hb = (unsigned)(hb0 < 152 * 4 ? hb0 : 152 * 4);
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
-    (k_contacts_cull<false, true><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    (full ? k_contacts_cull<false, true, true> : k_contacts_cull<false, true, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
     if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF);
     (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
   } else if (P.periodic) {
-    (k_contacts_cull<true, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    (full ? k_contacts_cull<true, false, true> : k_contacts_cull<true, false, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
     if (P.law == WDEM_LAW_IDEALELPL)
       (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
     else
       (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
   } else {
-    (k_contacts_cull<false, false><<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches);
+    (full ? k_contacts_cull<false, false, true> : k_contacts_cull<false, false, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
     if (P.law == WDEM_LAW_IDEALELPL)
       (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
     else

@@ -375,6 +375,14 @@ __device__ __forceinline__ void rotateSphere(const StepParams& P, const Particle
 //  - an orientation that does not rotate and that the last normalisation left unchanged (meta bit
 //    META_ORI_FIXED) is neither normalised again nor rewritten;
 //  - the FP32 shadow is written by mantissa truncation on the integer pipe.
+// m g along one axis: the signed zero of a zero g, nothing when the value is not used, else the product
+__device__ __forceinline__ double gravForce(double mass, bool massFinite, double g, bool unused) {
+  if (zeroBits(g) && massFinite) return signedZero(mass, g);
+  if (unused) return 0.0;
+  WDEM_REAL_BRANCH();
+  return mass * g;
+}
+
 template <bool PERI>
 __device__ __forceinline__ void integrateFast(const StepParams& P, const Particles& p, const int i, const int n, const Contacts& c,
                                               const Csr& csr, DeviceStatus* st, const bool touchedNow) {
@@ -386,12 +394,15 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   const bool blockedNone = (flags & 63u) == 0u;
   d3 F, T;
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
+  const bool damp = (P.dampOn && !(flags & WDEM_DAMPING_SKIP));
+  // the gravity-only path takes its acceleration from the cache; without damping nothing reads m g
+  // along the gravity axis then
+  const int skipAxis = (blockedNone && grav && !touchedNow && P.gravAxis >= 0 && !damp) ? P.gravAxis : -1;
   if (!blockedAll) {
     if (grav) {
       const bool mf = finiteBits(mass);
-      F.x = (zeroBits(P.gravity[0]) && mf) ? signedZero(mass, P.gravity[0]) : mass * P.gravity[0];
-      F.y = (zeroBits(P.gravity[1]) && mf) ? signedZero(mass, P.gravity[1]) : mass * P.gravity[1];
-      F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
+      F = mk(gravForce(mass, mf, P.gravity[0], skipAxis == 0), gravForce(mass, mf, P.gravity[1], skipAxis == 1),
+             gravForce(mass, mf, P.gravity[2], skipAxis == 2));
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
     if (touchedNow) {
@@ -414,8 +425,6 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }
   const double dt = dtOf(P, meta.y);
-  const double damping = P.damping;
-  const bool damp = (damping != 0. && !(flags & WDEM_DAMPING_SKIP));
   d3 vel = xyz(vm);
   const double4_32a w4 = p.angw[i];
   const double4_32a& w4c = w4;

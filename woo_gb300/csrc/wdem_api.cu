@@ -165,6 +165,7 @@ struct wdem_handle {
   int lastRunFull = 0;
   // queued steps (runQueued): depth limit (0 or 1: every step checked on the host), mean steps between
   // rebuilds, steps since the last one
+  bool actValid = false;  // the cull's active list matches the container (a full cull ran since the rebuild)
   int maxAhead = 32;
   double rebuildInterval = 16;
   int sinceRebuild = 0;
@@ -234,7 +235,7 @@ cudaError_t dalloc(T*& p, size_t count) {
 
 void freeContacts(ContactBuf& b) {
   Contacts& c = b.c;
-  cudaFree(c.ids); cudaFree(c.state); cudaFree(c.step0); cudaFree(c.tanPhi);
+  cudaFree(c.ids); cudaFree(c.state); cudaFree(c.act); cudaFree(c.step0); cudaFree(c.tanPhi);
   for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
   for (int k = 0; k < OUT_COUNT; k++) cudaFree(c.out[k]);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
@@ -262,6 +263,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   if ((e = dalloc(c.work, cap))) return e;
+  if ((e = dalloc(c.act, cap))) return e;
   if (peri && (e = dalloc(c.cdist, cap))) return e;
   if (ell && ((e = dalloc(c.lam, cap)) || (e = dalloc(c.lam0, cap)))) return e;
   b.cap = cap;
@@ -478,6 +480,7 @@ int rebuild(wdem_handle* h) {
   h->nContacts = nNew;
   h->nFullRuns++;
   h->needRebuild = false;
+  h->actValid = false;
   return WDEM_OK;
 }
 
@@ -495,6 +498,7 @@ void fillStepParams(wdem_handle* h) {
     h->gravAccDirty = true;  // recomputed before the next step (parameters change rarely)
   }
   P.distFactor = r.distFactor;
+  P.distFactorF = (float)std::fabs(r.distFactor);
   P.bboxFactor = r.distFactor > 0 ? r.distFactor : 1.;
   P.loneMask = r.loneMask;
   P.damping = r.damping;
@@ -504,6 +508,7 @@ void fillStepParams(wdem_handle* h) {
   P.verletHiF = (float)(h->verletDistResolved * (1 + 1e-6));
   P.dampM = 1.0 - r.damping * 1.0;
   P.dampP = 1.0 - r.damping * -1.0;
+  P.dampOn = r.damping != 0. ? 1 : 0;
   P.noRatch = r.noRatch; P.iniLensTouch = r.iniLensTouch; P.trsfRenorm = r.trsfRenorm; P.approxMask = r.approxMask;
   P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
   P.cp2 = r.cp2; P.law = r.law;
@@ -686,6 +691,7 @@ int wdem_destroy(wdem_handle* h) {
 const char* wdem_last_error(wdem_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
 int wdem_set_params(wdem_handle* h, const wdem_params* p) {
+  if (h) h->actValid = false;  // the far-pair screen depends on verletDist and distFactor
   if (!h || !p) return WDEM_ERR_ARG;
   if (!p->reset) return fail(h, WDEM_ERR_UNSUPPORTED, "Leapfrog.reset=False is not supported (ForceResetter is folded into the GPU engine)");
   if (p->iniEqlb) return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl.iniEqlb is not supported");
@@ -1024,7 +1030,9 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   for (int g = 0; g < ahead; g++) {
     P.step = s0 + g;
     launch_leapfrog(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
-    launch_contacts(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+    const bool full = !h->actValid;
+    h->actValid = true;
+    launch_contacts(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, full, warm ? h->mlpWbf : nullptr,
                     warm ? h->mlpW : nullptr);
   }
   CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
@@ -1045,8 +1053,9 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
     CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
     if ((rc = rebuild(h))) return rc;
-    launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+    launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                     warm ? h->mlpW : nullptr);
+    h->actValid = true;
     h->sinceRebuild += (int)(k - s0) + 1;
     h->rebuildInterval = 0.75 * h->rebuildInterval + 0.25 * h->sinceRebuild;
     h->sinceRebuild = 0;
@@ -1159,8 +1168,9 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     {
       PhaseTimer t(h, PH_CONTACTS);
       const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
-      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, warm ? h->mlpWbf : nullptr,
+      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                       warm ? h->mlpW : nullptr);
+      h->actValid = true;
     }
     if (h->P.trackEnergy) {
       int rc0;

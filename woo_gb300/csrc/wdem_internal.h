@@ -77,6 +77,8 @@ struct StepParams {
   float verletLoF;          // FP32 lower bound of verletDist (FP32 verlet trigger)
   float verletHiF;          // FP32 upper bound of verletDist (far-pair screen of the contact cull)
   double dampM, dampP;      // 1 - damping * 1 and 1 - damping * (-1), the nonviscDamp2nd factors
+  int dampOn;               // damping != 0
+  float distFactorF;        // |distFactor| in FP32 (contact cull)
   int gravAxis;             // the only non-zero gravity component, or -1 (angw.w then holds RN(RN(m g)/m))
   int noRatch, iniLensTouch, trsfRenorm, approxMask;
   int updatePhysNow;        // Cp2 runs on existing contacts this step (updatePhys always/once)
@@ -148,6 +150,7 @@ struct Contacts {
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
   int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
   unsigned* work;   // indices of the contacts the heavy pass processes this step (capacity = contacts)
+  unsigned* act;    // contacts the cull walks until the next rebuild (not dead, not wall + wall, not far)
   double* lam;      // ellipsoid pairs: maximiser lambda of the last solve (NaN = none); null otherwise
   float* lam0;      // learned warm start of this step's solve (NaN = none); null unless used
 };
@@ -181,6 +184,7 @@ struct DeviceStatus {
   unsigned rotCount;   // length of the rotation list of this step
   unsigned touchCount; // length of the touched-particle list of this step
   unsigned long long dynNotMin;  // DynDt: ~bits of the smallest nodal critical step^2 (0: none yet)
+  unsigned actCount;   // length of the contact cull's active list
   double ext[12];     // box extents reduction scratch (as ordered ints)
 };
 
@@ -229,7 +233,7 @@ void energy_accumulate(cudaStream_t s, const double* x, long long n, double* par
 void upload_materials(const DevMaterial* m, int n);
 // warm: BF16 and FP32 weights of the learned warm start, run between the cull and the FP64 pass (or null)
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
-                     const uint16_t* warmBf = nullptr, const float* warmF = nullptr);
+                     bool full, const uint16_t* warmBf = nullptr, const float* warmF = nullptr);
 void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc);
 // ---- collider (k_collider.cu) ----
 struct ColliderScratch {
