@@ -30,23 +30,46 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
 __device__ __forceinline__ bool isZero(d3 a) { return a.x == 0 && a.y == 0 && a.z == 0; }
 
 // Predicates on the bit patterns, evaluated on the integer pipe instead of FP64 compares (the FP64
-// pipe is the binding unit of these kernels on GB300).  Each equals its FP64 counterpart exactly.
-__device__ __forceinline__ unsigned long long bitsOf(double x) { return (unsigned long long)__double_as_longlong(x); }
-__device__ __forceinline__ bool zeroBits(double x) { return (bitsOf(x) << 1) == 0; }                     // x == 0
-__device__ __forceinline__ bool isZeroBits(d3 a) { return ((bitsOf(a.x) | bitsOf(a.y) | bitsOf(a.z)) << 1) == 0; }
-__device__ __forceinline__ bool negZero(double x) { return bitsOf(x) == 0x8000000000000000ull; }
+// pipe is the binding unit of these kernels on GB300).  Each equals its FP64 counterpart exactly.  The
+// two 32-bit halves come out of an asm move, which the compiler cannot see through: a 64-bit bit test
+// such as (bits << 1) == 0 is recognised as x == 0 and turned back into an FP64 compare.
+struct Halves { unsigned lo, hi; };
+__device__ __forceinline__ Halves halvesOf(double x) {
+  Halves h;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(h.lo), "=r"(h.hi) : "d"(x));
+  return h;
+}
+__device__ __forceinline__ double fromHalves(unsigned lo, unsigned hi) {
+  double x;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lo), "r"(hi));
+  return x;
+}
+__device__ __forceinline__ unsigned long long bitsOf(double x) {
+  const Halves h = halvesOf(x);
+  return ((unsigned long long)h.hi << 32) | h.lo;
+}
+__device__ __forceinline__ bool zeroBits(double x) { const Halves h = halvesOf(x); return ((h.hi << 1) | h.lo) == 0; }  // x == 0
+__device__ __forceinline__ bool isZeroBits(d3 a) {
+  const Halves x = halvesOf(a.x), y = halvesOf(a.y), z = halvesOf(a.z);
+  return (((x.hi | y.hi | z.hi) << 1) | x.lo | y.lo | z.lo) == 0;
+}
+__device__ __forceinline__ bool negZero(double x) { const Halves h = halvesOf(x); return h.hi == 0x80000000u && h.lo == 0; }
 __device__ __forceinline__ bool hasNegZero(d3 a) { return negZero(a.x) || negZero(a.y) || negZero(a.z); }
 // y > 0 (positive, nonzero, not NaN; +inf included)
 __device__ __forceinline__ bool positiveBits(double y) {
-  long long b = __double_as_longlong(y);
-  return b > 0 && b <= 0x7ff0000000000000ll;
+  const Halves h = halvesOf(y);
+  const bool pos = !(h.hi & 0x80000000u) && (h.hi | h.lo) != 0;
+  const bool notNaN = h.hi < 0x7ff00000u || (h.hi == 0x7ff00000u && h.lo == 0);
+  return pos && notNaN;
 }
-__device__ __forceinline__ bool isOneBits(double x) { return bitsOf(x) == 0x3ff0000000000000ull; }       // x == 1.0
-__device__ __forceinline__ bool finiteBits(double x) { return ((bitsOf(x) >> 52) & 0x7ff) != 0x7ff; }
+__device__ __forceinline__ bool isOneBits(double x) { const Halves h = halvesOf(x); return h.hi == 0x3ff00000u && h.lo == 0; }  // x == 1.0
+__device__ __forceinline__ bool finiteBits(double x) { return (halvesOf(x).hi & 0x7ff00000u) != 0x7ff00000u; }
 // a * b for finite a and b == +-0: the zero with the product's sign
 __device__ __forceinline__ double signedZero(double a, double b) {
-  return __longlong_as_double((long long)((bitsOf(a) ^ bitsOf(b)) & 0x8000000000000000ull));
+  return fromHalves(0u, (halvesOf(a).hi ^ halvesOf(b).hi) & 0x80000000u);
 }
+// the sign bits of a and b differ
+__device__ __forceinline__ bool signsDiffer(double a, double b) { return ((halvesOf(a).hi ^ halvesOf(b).hi) >> 31) != 0; }
 // Eigen normalize().  When the squared norm is exactly 1, sqrt gives exactly 1 and the divisions
 // are identities: skipping them changes no bit and saves FP64 issue slots.
 __device__ __forceinline__ d3 normalized(d3 a) {
@@ -139,7 +162,7 @@ __device__ __forceinline__ double dmax3(d3 a) {
 
 __device__ __forceinline__ double signum(double f) { return f < 0 ? -1.0 : (f > 0 ? 1.0 : 0.0); }
 
-__device__ __forceinline__ int expBits(double x) { return (int)((bitsOf(x) >> 52) & 0x7ff); }
+__device__ __forceinline__ int expBits(double x) { return (int)((halvesOf(x).hi >> 20) & 0x7ff); }
 
 // Mathr::Sign(F * u) (-1, 0, +1; 0 for NaN): the sign bits decide unless a factor is zero, not finite,
 // subnormal, or the product could underflow to zero, in which case the product is formed.
@@ -147,7 +170,7 @@ __device__ __forceinline__ int signProd(double F, double u) {
   if (zeroBits(F) || zeroBits(u)) return 0;
   const int eF = expBits(F), eu = expBits(u);
   if (eF != 0 && eF != 0x7ff && eu != 0 && eu != 0x7ff && eF + eu > 1100)
-    return ((bitsOf(F) ^ bitsOf(u)) >> 63) ? -1 : 1;
+    return signsDiffer(F, u) ? -1 : 1;
   WDEM_REAL_BRANCH();
   const double pr = F * u;
   return pr < 0 ? -1 : (pr > 0 ? 1 : 0);
@@ -157,7 +180,7 @@ __device__ __forceinline__ int signProd(double F, double u) {
 // from -0 to +0 (round to nearest: -0 + +0 = +0); otherwise the operations are done.
 __device__ __forceinline__ double addScaled(double v, double s, double a) {
   if (zeroBits(a) && finiteBits(s)) {
-    const bool addendNeg = ((bitsOf(s) ^ bitsOf(a)) >> 63) != 0;
+    const bool addendNeg = signsDiffer(s, a);
     return (negZero(v) && !addendNeg) ? 0.0 : v;
   }
   WDEM_REAL_BRANCH();
@@ -184,7 +207,7 @@ __device__ __forceinline__ double addZ(double a, double b) {
   WDEM_REAL_BRANCH();
   return a + b;
 }
-__device__ __forceinline__ double negD(double a) { return __longlong_as_double((long long)(bitsOf(a) ^ 0x8000000000000000ull)); }
+__device__ __forceinline__ double negD(double a) { const Halves h = halvesOf(a); return fromHalves(h.lo, h.hi ^ 0x80000000u); }
 // row-major m (entry classes cls) times v, each row summed left to right: mvec with the zero and unit
 // entries' contributions formed exactly without FP64 operations
 __device__ __forceinline__ d3 mvecC(const double* m, int cls, d3 v) {
@@ -201,7 +224,7 @@ __device__ __forceinline__ d3 mvecC(const double* m, int cls, d3 v) {
 // v + a s (operands of the product in this order) for the position update pos + vel dt
 __device__ __forceinline__ double addScaledR(double v, double a, double s) {
   if (zeroBits(a) && finiteBits(s)) {
-    const bool addendNeg = ((bitsOf(s) ^ bitsOf(a)) >> 63) != 0;
+    const bool addendNeg = signsDiffer(s, a);
     return (negZero(v) && !addendNeg) ? 0.0 : v;
   }
   WDEM_REAL_BRANCH();
@@ -211,11 +234,12 @@ __device__ __forceinline__ double addScaledR(double v, double a, double s) {
 // double -> float by truncating the mantissa (error below 2^-23 relative) for values in the float normal
 // range, on the integer pipe; zeros keep their sign; other values use the hardware conversion.
 __device__ __forceinline__ float truncF(double x) {
-  const unsigned long long b = bitsOf(x);
-  const int e = (int)((b >> 52) & 0x7ff);
+  const Halves h = halvesOf(x);
+  const int e = (int)((h.hi >> 20) & 0x7ff);
+  // sign, rebased exponent, the top 23 of the 52 mantissa bits (20 in hi, 3 in lo)
   if (e >= 897 && e <= 1150)
-    return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull) | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffull));
-  if ((b << 1) == 0) return __uint_as_float((unsigned)((b >> 32) & 0x80000000ull));
+    return __uint_as_float((h.hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((h.hi & 0xfffffu) << 3) | (h.lo >> 29));
+  if (((h.hi << 1) | h.lo) == 0) return __uint_as_float(h.hi & 0x80000000u);
   WDEM_REAL_BRANCH();
   return (float)x;
 }
