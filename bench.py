@@ -487,6 +487,30 @@ def cpu_baseline(args, full_n):
     if args.workload == "ell200k":
         from woo_gb300 import abi
         spec.params.ellSolver = abi.ELL_BRENT   # the reference's solver
+    if args.workload == "batch512":
+        # the reference runs independent scenes one by one (a scene per process in its batch system): a
+        # seeded sample of the scenes, each on its own, time split evenly
+        from woo_gb300 import scenes
+        nsc = len(spec.info["ranges"])
+        sample = sorted(np.random.default_rng(13).choice(nsc, min(8, nsc), replace=False).tolist())
+        psteps, total, threads = 0, 0.0, 1
+        for k in sample:
+            single = scenes.single_from_batch(spec, k)
+            o = bridge.Oracle(single.params, single.particles, canonical=False, variant="liborc_omp.so")
+            o.set_parallel(True)
+            threads = o.threads()
+            o.step(2)
+            t, st, kk = 0.0, 0, 10
+            while t < args.cpu_seconds / len(sample) and st < 100000:
+                t += o.step_timed(kk)
+                st += kk
+                kk = min(kk * 2, 2000)
+            psteps += single.particles.n * st
+            total += t
+        return {"value": psteps / total, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                "sample": f"{len(sample)} of the scenes (seeded) run one after another, each for ~{args.cpu_seconds / len(sample):.1f} s "
+                          f"after 2 untimed steps, OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, "
+                          f"{threads} threads"}
     o = bridge.Oracle(spec.params, spec.particles, contacts=contacts, canonical=False, variant="liborc_omp.so",
                       cell=getattr(spec, "cell", None))
     o.set_parallel(True)

@@ -244,7 +244,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     d3 relPos = pos2 - pos1;
     double t = fabs(P.distFactor) * (r1 + r2);
     double unDistSq = sqnorm(relPos) - t * t;
-    if (unDistSq > 0 && !real) return;
+    if (positiveBits(unDistSq) && !real) return;
     double dist = sqrt(sqnorm(relPos));
     uN = dist - (r1 + r2);
     normal = relPos / dist;
@@ -304,7 +304,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     const d3 currNormal = normal;
     d3 normRotVec = cross(prevNormal, currNormal);
     d3 midNormal = (am & 1) ? prevNormal : 0.5 * (prevNormal + currNormal);
-    if (sqnorm(midNormal) == 0) midNormal = currNormal;
+    if (zeroBits(sqnorm(midNormal))) midNormal = currNormal;
     else if (!(am & 2) && !(am & 1)) midNormal = normalized(midNormal);
     d3 normTwistVec = midNormal * dt * 0.5 * dot(midNormal, angVel1 + angVel2);
     d3 rt = normRotVec + normTwistVec;
@@ -329,8 +329,8 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
       midPos1 = pos1 - (dt * 0.5) * vel1;
       midPos2 = PERI ? pos2 - (dt * 0.5) * (vel2 + shiftVel2) : pos2 - (dt * 0.5) * vel2;
     }
-    d3 c1x = (P.noRatch && r1 > 0) ? r1 * midNormal : midContPt - midPos1;
-    d3 c2x = (P.noRatch && r2 > 0) ? (-r2) * midNormal : midContPt - midPos2;
+    d3 c1x = (P.noRatch && positiveBits(r1)) ? r1 * midNormal : midContPt - midPos1;
+    d3 c2x = (P.noRatch && positiveBits(r2)) ? (-r2) * midNormal : midContPt - midPos2;
     d3 relVel = PERI ? (vel2 + shiftVel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x))
                      : (vel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
     gvel = mk(dot(mid0, relVel), dot(mid1, relVel), dot(mid2, relVel));
@@ -350,7 +350,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   const double dt = dtC;
   double eEl = 0, ePl = 0, eVN = 0, eVT = 0, eBr = 0;
   if (LAW == WDEM_LAW_IDEALELPL) {
-    if (uN > 0 && !P.noBreak) {
+    if (positiveBits(uN) && !P.noBreak) {
       keep = false;
       if (P.noSlip && P.trackEnergy) {
         // elastic potential lost when a contact breaks without slipping (IdealElPl.cpp:28-40)
@@ -361,7 +361,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
       }
     } else {
       fx = kn * uN;
-      if (P.noFrict || tanPhi == 0.) { fy = 0; fz = 0; }
+      if (P.noFrict || zeroBits(tanPhi)) { fy = 0; fz = 0; }
       else {
         double sc = dt * kt;
         fy = fy + sc * gvel.y;
@@ -371,14 +371,14 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
         if (ftSq > maxFt * maxFt && !P.noSlip) {
           double FtNorm = sqrt(ftSq);
           double ratio = maxFt / FtNorm;
-          if (FtNorm == 0.) ratio = 0.;
+          if (zeroBits(FtNorm)) ratio = 0.;
           if (P.trackEnergy) ePl = (kt != 0. ? (maxFt) * (FtNorm - maxFt) / kt : 0.);
           fy *= ratio; fz *= ratio;
         }
         // Eigen maxCoeff = maxi(maxi(f0,f1),f2) with maxi(a,b) = a<b ? b : a
         double m01 = (fx < fy) ? fy : fx;
         double mm = (m01 < fz) ? fz : m01;
-        if (isnan(mm)) { if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = a; }
+        if (nanBits(mm)) { if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = a; }
       }
       if (P.trackEnergy) {
         const double el = 0.5 * (fx * fx / kn + (kt != 0. ? (fy * fy + fz * fz) / kt : 0.));
@@ -411,18 +411,18 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     const double velN = gvel.x;
     const double kn0 = hz[0];
     kn = (3 / 2.) * kn0 * sqrt(-uN);
-    if (uN > 0) keep = false;
+    if (positiveBits(uN)) keep = false;
     else {
       double Fne = -kn0 * pown3(sqrt(-uN));
       double Fna = hz[3];
-      double eta = (hz[2] > 0 ? hz[2] * sqrt(sqrt(dmax(-uN, 0.))) : 0.);
+      double eta = (positiveBits(hz[2]) ? hz[2] * sqrt(sqrt(dmax(-uN, 0.))) : 0.);
       double Fnv = eta * velN;
       // HertzPhys.alpha = mean of the materials' alpha (Hertz.cpp:52); the clamp applies when it is 0
       const double alphaC = .5 * (c_mats[p.meta[a].y].alpha + c_mats[p.meta[b].y].alpha);
-      if (alphaC == 0. && P.noAttraction && Fne + Fnv > 0) Fnv = -Fne;
+      if (zeroBits(alphaC) && P.noAttraction && positiveBits(Fne + Fnv)) Fnv = -Fne;
       fx = Fne + Fna + Fnv;
       if (P.trackEnergy) eVN = Fnv * velN * dt;
-      kt = hz[1] * sqrt(uN < 0 ? -uN : 0);
+      kt = hz[1] * sqrt(negativeBits(uN) ? -uN : 0);
       double sc = dt * kt;
       fy = fy + sc * gvel.y;
       fz = fz + sc * gvel.z;
@@ -473,7 +473,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   const qd ori = quatFromCols(cur0, cur1, cur2);
   const d3 F = qrot(ori, mk(fx, fy, fz));
   const d3 tq = mk(tqx, tqy, tqz);
-  const d3 T = isZero(tq) ? mk(0, 0, 0) : qrot(ori, tq);
+  const d3 T = isZeroBits(tq) ? mk(0, 0, 0) : qrot(ori, tq);
   const d3 xcA = contPt - pos1;
   const d3 xcB = contPt - pos2;
   const d3 TA = cross(xcA, F) + T;

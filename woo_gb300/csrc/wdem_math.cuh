@@ -62,6 +62,17 @@ __device__ __forceinline__ bool positiveBits(double y) {
   const bool notNaN = h.hi < 0x7ff00000u || (h.hi == 0x7ff00000u && h.lo == 0);
   return pos && notNaN;
 }
+// y < 0 (negative, nonzero, not NaN; -inf included)
+__device__ __forceinline__ bool negativeBits(double y) {
+  const Halves h = halvesOf(y);
+  const unsigned m = h.hi & 0x7fffffffu;
+  return (h.hi & 0x80000000u) && (m | h.lo) != 0 && (m < 0x7ff00000u || (m == 0x7ff00000u && h.lo == 0));
+}
+__device__ __forceinline__ bool nanBits(double x) {
+  const Halves h = halvesOf(x);
+  const unsigned m = h.hi & 0x7fffffffu;
+  return m > 0x7ff00000u || (m == 0x7ff00000u && h.lo != 0);
+}
 __device__ __forceinline__ bool isOneBits(double x) { const Halves h = halvesOf(x); return h.hi == 0x3ff00000u && h.lo == 0; }  // x == 1.0
 __device__ __forceinline__ bool finiteBits(double x) { return (halvesOf(x).hi & 0x7ff00000u) != 0x7ff00000u; }
 // a * b for finite a and b == +-0: the zero with the product's sign
