@@ -383,12 +383,28 @@ __device__ __forceinline__ double gravForce(double mass, bool massFinite, double
   return mass * g;
 }
 
+// The particle's records (meta, velm, angw, posr, lastPosf) are loaded by the caller, all at once.
+struct FastRec {
+  int4 meta;
+  double4_32a vm, w4, pr;
+  float4 lf;
+};
+__device__ __forceinline__ FastRec loadFast(const Particles& p, int i) {
+  FastRec r;
+  r.meta = p.meta[i];
+  r.vm = p.velm[i];
+  r.w4 = p.angw[i];
+  r.pr = p.posr[i];
+  r.lf = p.lastPosf[i];
+  return r;
+}
+
 template <bool PERI>
 __device__ __forceinline__ void integrateFast(const StepParams& P, const Particles& p, const int i, const int n, const Contacts& c,
-                                              const Csr& csr, DeviceStatus* st, const bool touchedNow) {
-  const int4 meta = p.meta[i];
+                                              const Csr& csr, DeviceStatus* st, const bool touchedNow, const FastRec& rec) {
+  const int4 meta = rec.meta;
   const unsigned flags = (unsigned)meta.w;
-  const double4_32a vm = p.velm[i];
+  const double4_32a vm = rec.vm;
   const double mass = vm.w;
   const bool blockedAll = (flags & 63u) == 63u;
   const bool blockedNone = (flags & 63u) == 0u;
@@ -426,11 +442,11 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   }
   const double dt = dtOf(P, meta.y);
   d3 vel = xyz(vm);
-  const double4_32a w4 = p.angw[i];
+  const double4_32a w4 = rec.w4;
   const double4_32a& w4c = w4;
   d3 angVel = xyz(w4);
   bool angChanged = false;
-  const double4_32a pr = p.posr[i];
+  const double4_32a pr = rec.pr;
   d3 pos = xyz(pr);
   if (!blockedAll) {
     d3 lin;
@@ -583,7 +599,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
   }
   // aabbIsDirty (moved^2 > verletDist^2): FP32 distance of the shadows with a bound on its error
   // (truncation < 2^-23 relative per coordinate, FP32 arithmetic a few 2^-24 of the distance)
-  const float4 lf = p.lastPosf[i];
+  const float4 lf = rec.lf;
   const float dx = pf.x - lf.x, dy = pf.y - lf.y, dz = pf.z - lf.z;
   const float df = sqrtf(dx * dx + dy * dy + dz * dz);
   const float S = fabsf(pf.x) + fabsf(pf.y) + fabsf(pf.z) + fabsf(lf.x) + fabsf(lf.y) + fabsf(lf.z);
@@ -602,15 +618,15 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
 // compacted into touchList instead: their force gather and divisions would hold up the FP64 pipe
 // for whole warps of gravity-only neighbours.
 template <bool PERI>
-__global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
+__global__ void __launch_bounds__(256, 4) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
                                                         DeviceStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  // the particle's first loads are issued before the guard's, not after it
-  const unsigned fl = (unsigned)p.meta[i].w;
+  // all of the particle's loads are issued together, before the guard's and the list decision
+  const FastRec rec = loadFast(p, i);
   const uint8_t tch = p.touched[i];
   if (haltedIntegrator(st, P.step)) return;
-  const bool listed = (fl & 63u) != 63u && tch != 0;
+  const bool listed = ((unsigned)rec.meta.w & 63u) != 63u && tch != 0;
   const unsigned am = __activemask();
   const unsigned b = __ballot_sync(am, listed);
   if (b) {
@@ -622,7 +638,7 @@ __global__ void __launch_bounds__(256) k_leapfrog_fast(StepParams P, Particles p
     if (listed && slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
   }
   if (listed) return;
-  integrateFast<PERI>(P, p, i, n, c, csr, st, false);
+  integrateFast<PERI>(P, p, i, n, c, csr, st, false, rec);
 }
 
 // Second pass, over two lists: the touched particles (CSR force gather, full integration, rotation
@@ -637,7 +653,7 @@ __global__ void __launch_bounds__(256) k_leapfrog_lists(StepParams P, Particles 
     if (k < nt) {
       const int i = (int)p.touchList[k];
       p.touched[i] = 0;
-      integrateFast<PERI>(P, p, i, n, c, csr, st, true);
+      integrateFast<PERI>(P, p, i, n, c, csr, st, true, loadFast(p, i));
     } else {
       const unsigned i = p.rotList[k - nt];
       rotateSphere(P, p, i, xyz(p.angw[i]), p.meta[i].y);
