@@ -1,7 +1,7 @@
 """ctypes bridge to the CPU oracle (oracle/woo_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-leg, as the checker of the GPU engine.  It reuses the wdem.h struct layouts of woo_gb300.abi so that
+leg, to compare the GPU engine's results with.  It reuses the wdem.h struct layouts of woo_gb300.abi so that
 both sides receive byte-identical inputs.
 """
 import ctypes as C

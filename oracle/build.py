@@ -1,6 +1,7 @@
 """Build the CPU oracle (oracle/woo_oracle.cpp) into oracle/_build/liborc.so.
 
-TEST INFRASTRUCTURE: the oracle is the checker of the GPU engine, never part of it.  Compiled with
+TEST INFRASTRUCTURE: the oracle is what the GPU engine's results are compared with, never part of
+the engine.  Compiled with
 -ffp-contract=off so that a*b+c stays two IEEE operations on x86-64 and on aarch64 alike.
 An OpenMP build (liborc_omp.so) serves as the timed CPU baseline.
 """

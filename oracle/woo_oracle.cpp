@@ -2,8 +2,8 @@
  * woo_oracle.cpp -- CPU ORACLE for the GB300 DEM engine.  TEST INFRASTRUCTURE ONLY.
  *
  * A plain C++17 restatement of woodem/woo's DEM timestep (Leapfrog -> InsertionSortCollider ->
- * ContactLoop), written from the reference sources cited at each function.  It is the checker for
- * the CUDA engine: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
+ * ContactLoop), written from the reference sources cited at each function.  The CUDA engine's results
+ * are compared with it: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
  * The product library (libwdem.so) never links or calls it.
  *
  * Build: oracle/build.sh (g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared [-fopenmp]).

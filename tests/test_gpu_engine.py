@@ -26,7 +26,7 @@ def real_only(c):
 
 @pytest.mark.parametrize("law", ["frict", "hertz"])
 def test_one_step_from_identical_state_with_history(wdem_lib, law):
-    """Spec bar: per-contact forces within 1e-12 relative after one step from an identical state
+    """The parity bar: per-contact forces within 1e-12 relative after one step from an identical state
     (particles + contact history uploaded into both engines); here they are bit-identical."""
     spec = scenes.random_cloud(500, 21, dense=0.85, law=law)
     pre = bridge.Oracle(spec.params, spec.particles)

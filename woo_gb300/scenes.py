@@ -410,7 +410,7 @@ def oedometric_scene(n, seed, young, tanPhi, rmin=0.001, rmax=0.003, density=260
 
 
 def batch_oedometric(n_scenes, seed, nmin=500, nmax=20000, spacing=None, verletDist=1e-4, dense=1.0):
-    """n_scenes independent oedometric scenes in one particle set (BASELINE config 4): sphere counts
+    """n_scenes independent oedometric scenes in one particle set (the 512-scene batch workload): sphere counts
     log-uniform in [nmin, nmax], tanPhi ~ U[0.1, 0.8], young log-uniform in [1e6, 1e8] Pa, per-scene
     dt = 0.9 x the scene's p-wave dt (wdem_params.materialDt).  Scene k is shifted along x by k x spacing
     so the scenes stay apart; each particle carries its scene index.  Returns the SceneSpec (info holds
@@ -550,7 +550,7 @@ def densify_periodic(spec, phi_target=0.62, stages=48, steps_per_stage=100, rela
 
 
 def peri_shear(n=8_000_000, seed=5, phi=0.3, rate=1.0, young=1e8, tanPhi=0.5, density=1000.0, dt_safety=0.9):
-    """BASELINE config 5 geometry: spheres with lognormal radii (median 1 mm, sigma 0.25, clipped to
+    """The periodic simple-shear workload: spheres with lognormal radii (median 1 mm, sigma 0.25, clipped to
     [0.5, 2] mm) packed without overlap (periodic random sequential addition) in a cubic periodic cell
     sized for solid fraction `phi`, simple shear nextGradV[0][2] = rate (1/s), FrictMat E `young`,
     tanPhi .5, IdealElPl, no gravity, dt = dt_safety x p-wave dt.  Random sequential addition reaches
