@@ -1,5 +1,6 @@
-"""Periodic cell in the oracle: the known answer of py/tests/test_pbc.py (incident velocity across 10
-cells with homoDeform gradV2) and the periodic pair predicate against brute force over images."""
+"""Periodic cell in the oracle: the known answers of py/tests/test_pbc.py (incident velocity across 10
+cells with homoDeform gradV2, over-half-cell contacts, the double-contact error, cellDist of shifted
+spheres) and the periodic pair predicate against brute force over images."""
 import math
 
 import numpy as np
@@ -66,3 +67,41 @@ def test_periodic_pairs_match_images():
     exp = _image_pairs(pos, r, size)
     assert len(exp) > 50
     assert got == exp
+
+
+def _two_spheres(c0, r0, c1, r1):
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=0.5)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([c0, c1], float), np.array([r0, r1]), 0, [], mats_py)
+    p = scenes.default_params(mats, dt=1e-8, gravity=(0, 0, 0), damping=0.0)
+    return bridge.Oracle(p, pa, cell=dict(hSize=np.eye(3))), mats
+
+
+@pytest.mark.parametrize("shift", [(0, 0, 0), (13, 14, 15)])
+def test_over_half_cell_contact(shift):
+    """py/tests/test_pbc.py:130-144 (testOverHalfContact): a sphere spanning more than half the unit cell;
+    the pair's cellDist follows a shift of the first sphere by whole cells."""
+    o, _ = _two_spheres(np.array([.3, .5, .5]) + shift, .4, (.7, .9, .5), .1)
+    o.step(1)
+    c = o.contacts()
+    assert c.n == 1 and (c.idA[0], c.idB[0]) == (0, 1)
+    assert tuple(c.cellDist[0]) == shift
+
+
+def test_double_contact_is_an_error():
+    """py/tests/test_pbc.py:145-155 (testDoubleContact): boxes overlapping on both sides across the cell
+    are an error of the collider."""
+    o, _ = _two_spheres((.3, .5, .5), .4, (.8, .9, .5), .2)
+    with pytest.raises(RuntimeError, match="ambiguous periodic contact"):
+        o.step(1)
+
+
+@pytest.mark.parametrize("shift", [(0, 0, 0), (1, 2, 3), (6, 8, -4)])
+def test_normal_contact_cell_dist(shift):
+    """py/tests/test_pbc.py:156-169 (testNormalContact): a real contact whose second sphere is moved by
+    whole cells has cellDist = -shift."""
+    o, _ = _two_spheres((.5, .5, .5), .2, np.array([.8, .6, .5]) + shift, .2)
+    o.step(1)
+    c = o.contacts()
+    assert c.n == 1 and c.real[0] == 1
+    assert tuple(c.cellDist[0]) == tuple(-np.array(shift))
