@@ -91,3 +91,42 @@ def test_fails_loudly_without_gpu():
     S = small_scene()
     with pytest.raises(RuntimeError):
         S.run(1)
+
+
+def test_guess_moving():
+    """py/tests/test_demfield.py:11-22 (testGuessMoving)."""
+    def dd(blocked="", mass=0.0, vel=(0, 0, 0)):
+        n = dem.Node()
+        n.dem.blocked = blocked
+        n.dem.mass = mass
+        n.dem.vel = vel
+        return n.dem
+    assert not dd(mass=0).guessMoving()
+    assert not dd("xyz", mass=0).guessMoving()
+    assert dd("xyzXY", mass=1).guessMoving()
+    assert not dd("xyzXYZ", mass=1).guessMoving()
+    assert dd("xyzXYZ", mass=1, vel=(1, 1, 1)).guessMoving()
+
+
+def test_nodes_left_out_are_held_fixed():
+    """A particle whose node is not collected into DemField.nodes (nodes=False, or nodes=-1 and
+    guessMoving() false) is not integrated: the engine uploads it fully blocked and at rest, while the
+    Python side keeps its own attributes."""
+    m = dem.FrictMat()
+    S = small_scene()
+    ghost = dem.Sphere.make((0, 0, 0.5), 0.01, mat=m)
+    ghost.shape.nodes[0].dem.mass = 0.0
+    S.dem.par.add(ghost)
+    held = dem.Sphere.make((0, 0, 0.8), 0.01, mat=m)
+    S.dem.par.add(held, nodes=False)
+    held.vel = (1, 2, 3)
+    S._prepare_dt()
+    g = S._engine()
+    g._build_params(S, S.dem)
+    pa = g._pack(S.dem)
+    dv = g._device_view(S.dem, pa)
+    for p in (ghost, held):
+        assert dv.flags[p.id] & 63 == 63 and not dv.vel[p.id].any()
+    assert pa.flags[held.id] & 63 == 0 and tuple(pa.vel[held.id]) == (1, 2, 3)
+    others = [p.id for p in S.dem.par if p.id not in (ghost.id, held.id)]
+    assert np.array_equal(dv.flags[others], pa.flags[others])

@@ -120,6 +120,12 @@ class DemData:
     def isBlockedAll(self):
         return (self.flags & 63) == 63
 
+    def guessMoving(self):
+        """DemData::guessMoving (src/dem/Particle.cpp:638-640): whether the node needs motion integration
+        (it has mass and a free DOF, or a velocity)."""
+        return (self.mass != 0. and not self.isBlockedAll()) or bool(np.any(self.vel != 0)) or \
+            bool(np.any(self.angVel != 0))
+
 
 class Node:
     """Node (src/core/Field.hpp) with DemData; pos and ori (w, x, y, z)."""
@@ -299,11 +305,15 @@ class ParticleContainer:
         self._list = []
 
     def add(self, par, nodes=-1):
+        """ParticleContainer.add: nodes=True puts the particle's node into DemField.nodes (integrated by
+        Leapfrog), False leaves it out, -1 decides by DemData.guessMoving (DemField.collectNodes)."""
         if isinstance(par, (list, tuple)):
-            return [self.add(p) for p in par]
+            return [self.add(p, nodes=nodes) for p in par]
         if self._field._engine_bound():
             raise RuntimeError("adding particles after the GPU engine has started is not supported")
         par.id = len(self._list)
+        node = par.shape.nodes[0]
+        par._integrated = bool(nodes) if nodes != -1 else node.dem.guessMoving()
         self._list.append(par)
         return par.id
 
@@ -786,6 +796,18 @@ class GpuDemEngine(Engine):
                 getattr(pa, name)[i] = node._local[name]
         return pa
 
+    def _device_view(self, field, pa):
+        """The arrays as uploaded: a particle whose node is not in DemField.nodes is never moved by
+        Leapfrog, so the GPU engine holds it fixed (all DOFs blocked, no velocity)."""
+        idle = [p.id for p in field.par if not getattr(p, "_integrated", True)]
+        if not idle:
+            return pa
+        up = pa.copy()
+        up.flags[idle] |= 63
+        up.vel[idle] = 0
+        up.angVel[idle] = 0
+        return up
+
     # ------------------------------------------------------------------ engine protocol
     def critDt(self):
         return math.inf
@@ -798,7 +820,7 @@ class GpuDemEngine(Engine):
         h = abi.Handle(max(pa.n, 1), device=self.device)
         h.keep_geom(self.keepGeom)
         h.set_params(params)
-        h.upload_particles(pa)
+        h.upload_particles(self._device_view(field, pa))
         h.set_params(params)
         if getattr(scene, "periodic", False):
             c = scene.cell
@@ -872,12 +894,13 @@ class GpuDemEngine(Engine):
         pa = field._arrays
         n = pa.n
         kin = {"pos", "vel", "angVel", "ori"}
+        dv = self._device_view(field, pa)
         if field._dirty <= kin:
-            self._h.write_state(n, pa.pos.ctypes.data, pa.vel.ctypes.data, pa.angVel.ctypes.data, pa.ori.ctypes.data)
+            self._h.write_state(n, dv.pos.ctypes.data, dv.vel.ctypes.data, dv.angVel.ctypes.data, dv.ori.ctypes.data)
         else:
             # mass/inertia/flags/forces changed: full upload, keeping the contact history
             con = self._download_contacts()
-            self._h.upload_particles(pa)
+            self._h.upload_particles(dv)
             self._h.set_params(self._params)
             self._h.upload_contacts(con)
         field._dirty.clear()
