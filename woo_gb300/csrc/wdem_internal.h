@@ -130,8 +130,8 @@ struct Particles {
   double* maxRot;
   float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
   uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
-  unsigned* rotList;  // spheres whose orientation the rotation pass integrates this step
-  unsigned* touchList;  // particles with contact forces this step (integrated by the second pass)
+  unsigned* rotList;    // untouched spinning spheres, rotated by the integrator's list pass this step
+  unsigned* touchList;  // particles with contact forces this step (integrated by the list pass)
   int4* meta;
   float4* posf;  // FP32 shadow of posr (x, y, z, radius), refreshed whenever posr changes
   double* energy[3];  // per-particle energy terms of this step (grav, nonviscDamp, kinetic) when tracked
