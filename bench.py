@@ -206,6 +206,21 @@ def contact_kernel_bytes(cg, hertz):
     return 80 * touched + per_real * real + 16 * pot, dict(real=real, potential=pot, touched=touched)
 
 
+def max_over_ranks(x, world, device):
+    """The largest of the ranks' values (the slowest rank's time): all-reduce MAX when world > 1."""
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, n, steps, seconds):
+    """Whole-job particle-steps/s of `world` replicas of an n-particle scene stepped `steps` times, timed
+    by the slowest replica."""
+    return world * n * steps / seconds
+
+
 def timed_steps(h, stream, k, world, local, barrier):
     import torch
     barrier()
@@ -219,10 +234,7 @@ def timed_steps(h, stream, k, world, local, barrier):
     torch.cuda.synchronize()
     barrier()
     ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    return float(t.item())
+    return max_over_ranks(ms, world, f"cuda:{local}")
 
 
 QUEUE_DEPTH = None
@@ -352,7 +364,7 @@ def run_gpu(args, rank, world, local):
     clk = clocks.stop()
     launches = h.launch_count() - l0
     st1 = h.status()
-    value = world * n * args.steps / (ms_max / 1e3)
+    value = replica_throughput(world, n, args.steps, ms_max / 1e3)
     # per-phase CUDA-event times (leapfrog, collider, contacts) from a following window of the same run;
     # kept out of the timed region above so that the extra events do not slow it
     # (the window is also the cudaProfilerStart/Stop range: `ncu --profile-from-start off` captures
@@ -417,10 +429,8 @@ def run_gpu(args, rank, world, local):
         h.read_state(n, *ptrs)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
-        tt = torch.tensor([te], device=f"cuda:{local}", dtype=torch.float64)
-        if world > 1:
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e = {"value": world * n * ne / float(tt.item()), "unit": "particle-steps/s",
+        te_max = max_over_ranks(te, world, f"cuda:{local}")
+        e2e = {"value": replica_throughput(world, n, ne, te_max), "unit": "particle-steps/s",
                "h2d_bytes_per_step": bytes_io / ne + ctypes.sizeof(abi.Params),
                "d2h_bytes_per_step": bytes_io / ne + status_bytes, "steps": ne,
                "pattern": "state in from pinned host memory, one wdem_step(h, 1) call per step, state out"}
