@@ -216,7 +216,8 @@ typedef struct wdem_status {
 
 typedef struct wdem_handle wdem_handle;
 
-/* Library ABI version (WDEM_ABI_VERSION). */
+/* Library ABI version (WDEM_ABI_VERSION).  No counterpart in the reference, whose engines live in the
+ * same binary as the Python module; a binding checks it once after loading the library. */
 int wdem_abi_version(void);
 
 /* Create a handle for up to maxParticles particles on CUDA device `device`.
@@ -224,7 +225,8 @@ int wdem_abi_version(void);
  * Scene.engines (py/utils.py:122-129; engine base src/core/Engine.hpp:19-104). */
 int wdem_create(int device, int32_t maxParticles, wdem_handle** out);
 
-/* Release all device memory and the stream. */
+/* Release all device memory and the stream; replaces removing the three engines from Scene.engines
+ * (their destructors, src/core/Engine.hpp:19-104). */
 int wdem_destroy(wdem_handle* h);
 
 /* Set engine/functor attributes (Leapfrog, InsertionSortCollider, ContactLoop, Cg2/Cp2/Law2 attrs,
@@ -249,18 +251,22 @@ int wdem_step(wdem_handle* h, int32_t nSteps);
  * force/torque are DemData.force/torque as Woo has them after ContactLoop: m*g + contact forces. */
 int wdem_download_particles(wdem_handle* h, wdem_particles* p);
 
-/* Number of contacts in the container (real + potential), as len(S.dem.con). */
+/* Number of contacts in the container (real + potential), as len(S.dem.con)
+ * (ContactContainer.__len__, src/dem/ContactContainer.hpp:61,121). */
 int wdem_contact_count(wdem_handle* h, int64_t* n);
 
 /* Download the contact container; c->n must be >= wdem_contact_count.  Contacts come sorted by
- * (min id, max id).  Null arrays are skipped. */
+ * (min id, max id).  Null arrays are skipped.  Replaces iterating S.dem.con from Python
+ * (ContactContainer::pyIter / pyNth, src/dem/ContactContainer.cpp:219-233). */
 int wdem_download_contacts(wdem_handle* h, wdem_contacts* c);
 
 /* Critical timestep of the field, DemFuncs::pWaveDt (src/dem/Funcs.cpp:151-175), via DemField::critDt
  * (src/dem/Particle.cpp:399-404): min over spheres of r/sqrt(E/rho). */
 int wdem_crit_dt(wdem_handle* h, double* dt);
 
-/* Energies accumulated since the last reset, in WDEM_E_* order (EnergyTracker). */
+/* Energies accumulated since the last reset, in WDEM_E_* order: the entries ContactLoop and Leapfrog
+ * add to Scene.energy (EnergyTracker::add, src/core/EnergyTracker.hpp:29-61; Scene.energy
+ * src/core/Scene.hpp:223).  wdem_reset_energy is EnergyTracker.clear (EnergyTracker.hpp:60). */
 int wdem_get_energy(wdem_handle* h, double* e, int32_t n);
 int wdem_reset_energy(wdem_handle* h);
 
@@ -281,10 +287,13 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
                        int32_t* pairs, int64_t maxPairs, int64_t* nPairs);
 
 /* Per-kernel device time of the last wdem_step call, in milliseconds, summed over its steps.
+ * Counterpart of Engine.execTime / execCount under Master.timingEnabled (src/core/Engine.hpp:92-93),
+ * per kernel instead of per engine.
  * names[i] (static strings) and ms[i], up to n entries; *count gets the number of entries. */
 int wdem_kernel_times(wdem_handle* h, const char** names, double* ms, int32_t* launches, int32_t n, int32_t* count);
 
-/* Enable/disable per-kernel CUDA-event timing inside wdem_step (off by default). */
+/* Enable/disable per-kernel CUDA-event timing inside wdem_step (off by default), as
+ * Master.timingEnabled switches Engine.execTime accounting (src/core/Engine.hpp:92-94). */
 int wdem_set_timing(wdem_handle* h, int32_t enable);
 
 /* Steps that wdem_step may queue on the device before it checks the collider trigger on the host
@@ -297,7 +306,8 @@ int wdem_set_queue_depth(wdem_handle* h, int32_t depth);
 
 /* Keep L6Geom.uN, L6Geom.vel and L6Geom.angVel of every real contact so that
  * wdem_download_contacts can return them (off by default: they are per-step values that Woo keeps
- * in the contact's CGeom object; storing them costs 56 bytes per contact per step). */
+ * in the contact's CGeom object, L6Geom.vel/angVel/uN at src/dem/L6Geom.hpp:16-18; storing them
+ * costs 56 bytes per contact per step). */
 int wdem_keep_geom(wdem_handle* h, int32_t enable);
 
 /* Periodic cell: Scene.isPeriodic + Cell.hSize/trsf/gradV/nextGradV (src/core/Cell.hpp:22-187), set
@@ -361,21 +371,24 @@ int wdem_ell_log_read(wdem_handle* h, float* out, int64_t cap, int64_t* n);
 int wdem_get_stress_noalloc(wdem_handle* h, double* stress);
 
 /* The CUDA stream (cudaStream_t) every kernel of this handle is launched on, for callers that
- * record CUDA events around wdem_step. */
+ * record CUDA events around wdem_step.  No counterpart in the reference (CPU only). */
 int wdem_get_stream(wdem_handle* h, void** stream);
 
 /* Overwrite / read the kinematic state of the first n particles in place, without touching the
- * contact container (as editing S.dem.par[i].pos/vel between steps in Woo).  Caller host buffers
+ * contact container (as editing S.dem.par[i].pos/vel/angVel between steps in Woo: the Particle
+ * properties of src/dem/Particle.hpp:100-104).  Caller host buffers
  * (pinned memory gives full copy bandwidth); null arrays are skipped; pos/vel/angVel are 3n, ori 4n. */
 int wdem_write_state(wdem_handle* h, int32_t n, const double* pos, const double* vel, const double* angVel,
                      const double* ori);
 int wdem_read_state(wdem_handle* h, int32_t n, double* pos, double* vel, double* angVel, double* ori);
 
 /* Measured FP64 fused-multiply-add throughput of the device in GFLOP/s (2 flops per FMA): the
- * ceiling of the FP64-issue-bound kernels, reported beside the HBM roofline. */
+ * ceiling of the FP64-issue-bound kernels, reported beside the HBM roofline.  No counterpart in the
+ * reference. */
 int wdem_fp64_peak(wdem_handle* h, double* gflops);
 
-/* Number of CUDA kernels launched by the library in this process (every launch site counts). */
+/* Number of CUDA kernels launched by the library in this process (every launch site counts).  No
+ * counterpart in the reference. */
 int wdem_launch_count(wdem_handle* h, int64_t* count);
 
 /* Seeded random sequential addition of n non-overlapping spheres, radii uniform in [rMin, rMax],
