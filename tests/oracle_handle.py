@@ -1,0 +1,78 @@
+"""A stand-in for woo_gb300.abi.Handle that forwards the engine's handle calls to the oracle.
+
+Test infrastructure: with it, the host-side layers (Scene, DemField, GpuDemEngine's bookkeeping, the
+outlets) run unchanged on the CPU, and a GPU scene can be compared with the same script run on the
+oracle.  Only the calls GpuDemEngine makes are provided.
+"""
+import ctypes as C
+from types import SimpleNamespace
+
+from oracle import bridge
+from woo_gb300 import abi
+
+
+class OracleHandle:
+    def __init__(self, max_particles, device=0):
+        self.o = None
+        self.params = None
+        self.time_sum = 0.0
+        self.max_particles = max_particles
+
+    def _check(self, rc):
+        self.o.check(rc)
+
+    def keep_geom(self, on):
+        pass
+
+    def set_params(self, params):
+        self.params = params
+        if self.o is not None:
+            self._check(self.o.lib.orc_set_params(self.o.h, C.byref(params)))
+
+    def upload_particles(self, pa):
+        if pa.n > self.max_particles:
+            raise abi.WdemError(-1, "too many particles")
+        if self.o is None:
+            self.o = bridge.Oracle(self.params, pa)
+            return
+        s = pa.struct()
+        self._check(self.o.lib.orc_upload_particles(self.o.h, C.byref(s)))
+
+    def upload_contacts(self, ca):
+        s = ca.struct()
+        self._check(self.o.lib.orc_upload_contacts(self.o.h, C.byref(s)))
+
+    def set_cell(self, hSize, trsf=None, gradV=None, nextGradV=None):
+        self.o.set_cell(hSize, trsf, gradV, nextGradV)
+
+    def cell(self):
+        return self.o.cell()
+
+    def step(self, n=1):
+        for _ in range(int(n)):
+            self.time_sum += self.o.dt()
+            self.o.step(1)
+
+    def status(self):
+        return SimpleNamespace(code=0, timeSum=self.time_sum, dt=self.o.dt(), dynDtCrit=self.o.dyndt_crit())
+
+    def download_particles(self, pa):
+        s = pa.struct()
+        self.o.lib.orc_download_particles(self.o.h, C.byref(s))
+        return pa
+
+    def download_contacts(self):
+        return self.o.contacts()
+
+    def contact_count(self):
+        return self.o.lib.orc_contact_count(self.o.h)
+
+    def energy(self):
+        return self.o.energy()
+
+
+def run_on_oracle(monkeypatch, scene, n):
+    """scene.run(n) with the engine's handle created on the oracle (on the first run)."""
+    with monkeypatch.context() as m:
+        m.setattr(abi, "Handle", OracleHandle)
+        scene.run(n)

@@ -1,0 +1,244 @@
+"""Outlets (src/dem/Outlet.cpp) and particle removal through the Python surface, on the CPU: the
+PeriodicEngine schedule against a step-by-step isActivated loop, the container semantics of removed
+ids, and whole scripts (Scene + GpuDemEngine bookkeeping + outlet) run with the engine's handle on the
+oracle."""
+import copy
+import math
+
+import numpy as np
+import pytest
+
+from woo_gb300 import dem
+from woo_gb300.core import Scene
+
+from oracle_handle import run_on_oracle
+
+R = 0.01
+
+
+def funnel(n_side=3, layers=3, floor=False, seed=5, extra=None, engines=()):
+    """Spheres of radius 1 cm between four side walls (x, y = +-5 cm), falling with random velocities;
+    an optional floor at z = 0; `extra` = positions of more spheres appended after the column."""
+    rng = np.random.default_rng(seed)
+    m = dem.FrictMat(density=2500, young=1e7, ktDivKn=0.2, tanPhi=0.5)
+    par = [dem.Wall.make(-0.05, axis=0, sense=1, mat=m), dem.Wall.make(0.05, axis=0, sense=-1, mat=m),
+           dem.Wall.make(-0.05, axis=1, sense=1, mat=m), dem.Wall.make(0.05, axis=1, sense=-1, mat=m)]
+    if floor:
+        par.append(dem.Wall.make(0, axis=2, sense=1, mat=m))
+    for k in range(layers):
+        for i in range(n_side):
+            for j in range(n_side):
+                c = (-0.025 + 0.025 * i, -0.025 + 0.025 * j, 0.02 + 0.025 * k)
+                v = (rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2), rng.uniform(-1.0, 0.0))
+                par.append(dem.Sphere.make(c, R, mat=m, vel=v))
+    for c in (extra or []):
+        par.append(dem.Sphere.make(c, R, mat=m))
+    return Scene(fields=[dem.DemField(gravity=(0, 0, -9.81), par=par)],
+                 engines=dem.DemField.minimalEngines(damping=0.2, dynDtPeriod=0) + list(engines), dtSafety=0.9)
+
+
+# ------------------------------------------------------------------------------------------ schedule
+class _Rec(dem.PeriodicEngine):
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.fired = []
+
+    def run(self, scene):
+        self.fired.append((scene.step, scene.time))
+
+
+class _StubGpu:
+    """Counts the steps the scene asks the GPU for."""
+
+    def __init__(self, dt):
+        self.dt = dt
+        self.steps = 0
+        self._ran_time = 0.0
+
+    def run(self, scene, k):
+        assert k >= 1
+        self.steps += k
+        self._ran_time = k * self.dt
+
+
+def _naive(eng, s0, n, dt):
+    """Woo: isActivated evaluated in every step (Scene::doOneStep), time advancing by dt."""
+    e = copy.deepcopy(eng)
+    out = []
+    for s in range(s0, s0 + n):
+        if e._activate(s, s * dt):
+            out.append(s)
+    return out, e
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_schedule_matches_step_by_step_activation(seed):
+    rng = np.random.default_rng(seed)
+    kw = dict(stepPeriod=int(rng.integers(1, 8)), stepModulo=bool(rng.integers(2)), initRun=bool(rng.integers(2)),
+              nDo=int(rng.choice([-1, 0, 1, 2, 3])))
+    s0 = int(rng.integers(0, 20))
+    chunks = [int(x) for x in rng.integers(1, 15, size=int(rng.integers(1, 4)))]
+    dt = 0.5
+    eng = _Rec(**kw)
+    ref, ref_eng = _naive(eng, s0, sum(chunks), dt)
+    S = Scene(fields=[dem.DemField()])
+    S.dt, S.step, S.time = dt, s0, s0 * dt
+    S._gpu = _StubGpu(dt)
+    S._host = [eng]
+    for c in chunks:
+        S.run(c)
+    assert [s for s, _ in eng.fired] == ref
+    assert all(t == s * dt for s, t in eng.fired)
+    assert S.step == s0 + sum(chunks) and S._gpu.steps == sum(chunks)
+    assert (eng.nDone, eng.stepLast, eng.stepPrev) == (ref_eng.nDone, ref_eng.stepLast, ref_eng.stepPrev)
+
+
+def test_time_based_periods_rejected():
+    S = funnel(engines=[dem.BoxOutlet(box=((-1, -1, -1), (1, 1, 1)), virtPeriod=0.1)])
+    with pytest.raises(RuntimeError, match="virtPeriod"):
+        S._engine()
+
+
+# ------------------------------------------------------------------------------------------ container
+def test_container_removed_ids():
+    S = funnel()
+    par = S.dem.par
+    n = len(par)
+    assert par.remove(6) is True and par.remove(6) is False
+    assert not par.exists(6) and len(par) == n
+    with pytest.raises(IndexError, match="No such particle: #6"):
+        par[6]
+    assert [p.id for p in par] == [i for i in range(n) if i != 6]
+    assert par.remove([n - 1, n - 2, 3]) == [True, True, True]
+    assert len(par) == n - 2                                      # trailing empty ids are trimmed
+    assert par[-1].id == n - 3
+    p = dem.Sphere.make((0, 0, 0.5), R)
+    assert par.add(p) == 6                                        # findFreeId: the first freed id
+    assert par.add(dem.Sphere.make((0, 0, 0.6), R)) == 3
+    with pytest.raises(IndexError, match="already has id"):
+        par.add(p)
+
+
+def test_removed_id_is_a_dead_slot_on_the_device():
+    S = funnel()
+    S.dem.par.remove(7)
+    S._prepare_dt()
+    g = S._engine()
+    g._build_params(S, S.dem)
+    pa = g._pack(S.dem)
+    view = g._device_view(S.dem, pa)
+    assert view.mask[7] == 0 and view.flags[7] & 63 == 63
+    assert not view.vel[7].any() and not view.angVel[7].any()
+    assert (view.mask[[i for i in range(pa.n) if i != 7]] != 0).all()
+
+
+# ------------------------------------------------------------------------------------------ scripts
+def test_box_outlet_deletes_and_books(monkeypatch):
+    out = dem.BoxOutlet(box=((-1, -1, -0.05), (1, 1, 10)), stepPeriod=50, save=True)
+    S = funnel(engines=[out])
+    n0 = len(S.dem.par)
+    masses = {p.id: p.mass for p in S.dem.par}
+    run_on_oracle(monkeypatch, S, 1201)                   # the last step (1200) runs the outlet
+    gone = [i for i in range(n0) if not S.dem.par.exists(i)]
+    assert out.num == len(gone) > 5
+    assert out.nDone == 1201 // 50 + 1
+    assert out.mass == pytest.approx(sum(masses[i] for i in gone), rel=1e-14)
+    d, m, t = out.diamMassTime()
+    assert np.all(d == 2 * R) and m.sum() == pytest.approx(out.mass, rel=1e-14)
+    assert np.all(np.diff(t) >= 0) and out.massOfDiam(0.019, 0.021) == pytest.approx(out.mass, rel=1e-14)
+    assert out.locs == [-1] * out.num
+    # every remaining movable particle is inside the box after the outlet's last run
+    for p in S.dem.par:
+        if isinstance(p.shape, dem.Sphere):
+            assert p.pos[2] >= -0.05
+    # no contact of a removed particle is left
+    ca = S.dem._contacts()
+    assert not np.isin(ca.idA, gone).any() and not np.isin(ca.idB, gone).any()
+    assert math.isfinite(out.currRate)
+
+
+def test_removal_does_not_change_the_motion(monkeypatch):
+    """A sphere that never touches the others, removed when it has fallen out of the box (at the run of
+    step 2100, with ~70 real contacts in the column), leaves the rest of the scene exactly as in the scene
+    without it: the contact history of the other particles is kept across the removal and the collider
+    rebuild that follows it."""
+    out = dem.BoxOutlet(box=((-5, -5, -1), (5, 5, 10)), stepPeriod=300, initRun=False)
+    A = funnel(floor=True, layers=6, extra=[(3.0, 0, -0.70)], engines=[out])
+    B = funnel(floor=True, layers=6)
+    n = len(B.dem.par)
+    run_on_oracle(monkeypatch, A, 301)
+    assert out.nDone == 1 and out.stepPrev == 0           # step 0 only started the count (initRun=False)
+    run_on_oracle(monkeypatch, A, 1500)
+    assert out.nDone == 6 and out.num == 0 and A.dem.par.exists(n)
+    assert A.dem.con.countReal() > 20
+    run_on_oracle(monkeypatch, A, 600)
+    assert out.nDone == 8 and out.num == 1 and not A.dem.par.exists(n)
+    assert out.stepLast == 2400 and out.stepPrev == 2100
+    run_on_oracle(monkeypatch, A, 300)
+    run_on_oracle(monkeypatch, B, 2701)
+    assert A.step == B.step == 2701
+    ca, cb = A.dem._contacts(), B.dem._contacts()
+    ra, rb = ca.real.astype(bool), cb.real.astype(bool)
+    assert ra.sum() > 50
+    assert np.array_equal(ca.keys()[ra], cb.keys()[rb])
+    for name in ("force", "trsf", "contPt", "kn", "kt", "stepCreated"):
+        assert np.array_equal(getattr(ca, name)[ra], getattr(cb, name)[rb]), name
+    for i in range(n):
+        assert np.array_equal(A.dem.par[i].pos, B.dem.par[i].pos)
+        assert np.array_equal(A.dem.par[i].vel, B.dem.par[i].vel)
+        assert np.array_equal(A.dem.par[i].angVel, B.dem.par[i].angVel)
+
+
+def test_marking_mode(monkeypatch):
+    out = dem.BoxOutlet(box=((-1, -1, -0.05), (1, 1, 10)), stepPeriod=40, markMask=16)
+    S = funnel(engines=[out])
+    n0 = len(S.dem.par)
+    run_on_oracle(monkeypatch, S, 801)
+    marked = [p.id for p in S.dem.par if p.mask & 16]
+    assert len(S.dem.par) == n0 and all(S.dem.par.exists(i) for i in range(n0))
+    assert out.num == len(marked) > 3                     # each particle is marked once
+    assert all(S.dem.par[i].mask == (dem.DemField.defaultMovableMask | 16) for i in marked)
+    assert all(S.dem.par[i].pos[2] < -0.05 for i in marked)
+
+
+def test_crazy_and_stacked_outlets(monkeypatch):
+    crazy = dem.CrazyOutlet(limVelNorm=50.0, stepPeriod=10)
+    stacked = dem.StackedBoxOutlet(box=((-1, -1, -10), (1, 1, -0.05)), divs=(-0.3, -0.1), axis=2, loc0=10,
+                                   inside=True, stepPeriod=10, save=True)
+    S = funnel(engines=[crazy, stacked])
+    S.dem.par[8].vel = (0, 0, -60.0)
+    run_on_oracle(monkeypatch, S, 1)
+    assert crazy.num == 1 and not S.dem.par.exists(8)
+    run_on_oracle(monkeypatch, S, 1300)
+    assert stacked.num > 5
+    assert set(stacked.locs) <= {10, 11, 12} and 12 in stacked.locs
+    with pytest.raises(RuntimeError, match="increasing"):
+        dem.StackedBoxOutlet(divs=(0.2, 0.1))
+
+
+def test_kin_outlet_energy(monkeypatch):
+    """Scene.energy['kinOutlet'] sums DemData::getEk_any of the deleted particles at their removal."""
+
+    class Snap(dem.PeriodicEngine):
+        def run(self, scene):
+            f = scene.dem
+            if f._stale:
+                f._engine._download_particles(f)
+            self.states.append(f._arrays.copy())
+
+    snap = Snap(stepPeriod=50)
+    snap.states = []
+    out = dem.BoxOutlet(box=((-1, -1, -0.05), (1, 1, 10)), stepPeriod=50)
+    S = funnel(engines=[snap, out])
+    S.trackEnergy = True
+    alive = set(range(len(S.dem.par)))
+    run_on_oracle(monkeypatch, S, 1001)
+    expect = 0.0
+    for st in snap.states:
+        for i in sorted(alive):
+            if i >= 4 and st.pos[i][2] < -0.05:
+                v, w = st.vel[i], st.angVel[i]
+                expect += .5 * (st.mass[i] * float(v @ v)) + .5 * float(w @ (st.inertia[i] * w))
+                alive.discard(i)
+    assert out.num == len(set(range(len(snap.states[0].pos))) - alive)
+    assert S.energy["kinOutlet"] == pytest.approx(expect, rel=1e-12)

@@ -205,6 +205,25 @@ class ContactArrays:
         b = np.maximum(self.idA, self.idB).astype(np.int64)
         return (a << 32) | b
 
+    def take(self, index):
+        """The contacts selected by `index` (boolean mask or integer indices), in that order."""
+        index = np.asarray(index)
+        idx = np.nonzero(index)[0] if index.dtype == bool else index.astype(np.int64)
+        o = ContactArrays(len(idx))
+        for k, v in self.__dict__.items():
+            if isinstance(v, np.ndarray):
+                setattr(o, k, np.ascontiguousarray(v[idx]))
+        return o
+
+    def without_particles(self, ids):
+        """The container after removing every contact of the given particles, as DemField::removeParticle
+        does (src/dem/Particle.cpp:519-527); the other contacts keep their order and history."""
+        ids = np.asarray(list(ids), np.int32)
+        if len(ids) == 0 or self.n == 0:
+            return self
+        gone = np.isin(self.idA, ids) | np.isin(self.idB, ids)
+        return self.take(~gone)
+
 
 class WdemError(RuntimeError):
     """A wdem_* call failed; carries the negative WDEM_ERR_* code."""

@@ -3,7 +3,8 @@
 Scene.run/one follow Scene::doOneStep (src/core/Scene.cpp:366-467): when dt is NaN it becomes
 dtSafety x min(critDt of engines and fields); the engines run in order; step and time advance.
 An engine list holding Woo's [Leapfrog, InsertionSortCollider, ContactLoop] trio is run by one
-GpuDemEngine built from their attributes (the drop-in replacement); any other engine is rejected.
+GpuDemEngine built from their attributes (the drop-in replacement); DynDt runs inside it and
+periodic host engines (outlets) between its steps; any other engine is rejected.
 """
 import math
 
@@ -111,6 +112,8 @@ class Scene:
         self.trackEnergy = bool(trackEnergy)
         self.lab = Labels()
         self._gpu = None
+        self._host = []
+        self._host_energy = {}
         self.periodic = False
         self.cell = Cell()
         self.engines = list(engines or [])
@@ -132,6 +135,7 @@ class Scene:
     def engines(self, ee):
         self._engines = list(ee)
         self._gpu = None
+        self._host = []
         self.lab = Labels()
         for e in self._engines:
             self.lab._set(getattr(e, "label", ""), e)
@@ -146,7 +150,8 @@ class Scene:
         gpu = [e for e in ee if isinstance(e, dem.GpuDemEngine)]
         trio = (dem.Leapfrog, dem.InsertionSortCollider, dem.ContactLoop)
         dyn = [e for e in ee if isinstance(e, dem.DynDt)]
-        others = [e for e in ee if not isinstance(e, (dem.GpuDemEngine, dem.DynDt) + trio)]
+        host = [e for e in ee if isinstance(e, dem.PeriodicEngine) and type(e).run is not dem.PeriodicEngine.run]
+        others = [e for e in ee if not isinstance(e, (dem.GpuDemEngine, dem.DynDt) + trio) and e not in host]
         if others:
             names = ", ".join(type(e).__name__ for e in others)
             raise RuntimeError(f"engines not run by the GPU engine: {names}")
@@ -159,6 +164,9 @@ class Scene:
         else:
             raise RuntimeError("Scene.engines must hold GpuDemEngine or Leapfrog + InsertionSortCollider + ContactLoop")
         self._gpu._dynDt = dyn[0] if dyn else None
+        for e in host:
+            e._check()
+        self._host = host
         return self._gpu
 
     def critDt(self):
@@ -178,14 +186,49 @@ class Scene:
             self.dt = self.dtSafety * dt
 
     def run(self, nSteps=1, wait=True):
-        """Run nSteps steps (the GPU runs them back to back; wait is accepted for compatibility)."""
+        """Run nSteps steps (wait is accepted for compatibility).  The GPU runs the steps back to back,
+        stopping after the contact pass of each step at which a host engine (an outlet) is due: that
+        engine then runs with step, time, dt and cell.gradV as Scene::doOneStep has them while its
+        engines run (before the epilogue, src/core/Scene.cpp:428-432)."""
         if nSteps <= 0:
             return
         self._prepare_dt()
         eng = self._engine()
-        eng.run(self, int(nSteps))
-        self.step += int(nSteps)
+        end = self.step + int(nSteps)
+        while self.step < end:
+            due = [e._next_step(self.step, self.time) for e in self._host]
+            due = [t for t in due if t is not None and t < end]
+            if not due:
+                self._gpu_steps(eng, end - self.step)
+                break
+            t = min(due)
+            if t > self.step:
+                self._gpu_steps(eng, t - self.step)
+            dt, gradV, time = self.dt, self.cell.gradV, self.time
+            eng.run(self, 1)
+            new_dt, new_gradV = self.dt, self.cell._gradV
+            self.dt = dt
+            self.cell._gradV = gradV
+            try:
+                for e in self._host:
+                    if e._activate(self.step, time):
+                        e.run(self)
+            finally:
+                self.dt = new_dt
+                self.cell._gradV = new_gradV
+            self.step += 1
+            self.time += eng._ran_time
+
+    def _gpu_steps(self, eng, k):
+        eng.run(self, int(k))
+        self.step += int(k)
         self.time += eng._ran_time
+
+    def _energy_add(self, name, value):
+        """EnergyTracker::add with ZeroDontCreate|IsIncrement, for energies booked on the host."""
+        if value == 0.0 and name not in self._host_energy:
+            return
+        self._host_energy[name] = self._host_energy.get(name, 0.0) + value
 
     def one(self):
         self.run(1)
@@ -201,8 +244,10 @@ class Scene:
             return EnergyTracker({})
         eng = self._engine()
         if eng._h is None:
-            return EnergyTracker({})
-        return EnergyTracker({k: v for k, v in eng._h.energy().items() if v != 0.0})
+            return EnergyTracker(dict(self._host_energy))
+        d = {k: v for k, v in eng._h.energy().items() if v != 0.0}
+        d.update(self._host_energy)
+        return EnergyTracker(d)
 
 
 class EnergyTracker(dict):

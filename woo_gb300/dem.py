@@ -269,8 +269,26 @@ class Particle:
     def __init__(self, shape=None, material=None, mask=1):
         self.shape = shape
         self.material = material
-        self.mask = int(mask)
+        self._mask = int(mask)
         self.id = -1
+
+    def _bound(self):
+        if self.shape is None or not self.shape.nodes:
+            return None
+        return self.shape.nodes[0]._field
+
+    @property
+    def mask(self):
+        return self._mask
+
+    @mask.setter
+    def mask(self, v):
+        """Particle.mask; on a running field the new mask reaches the collider at the next run (contacts
+        already in the container stay, as in Woo)."""
+        self._mask = int(v)
+        f = self._bound()
+        if f is not None and f.par.exists(self.id) and f.par[self.id] is self:
+            f._set_mask(self.id, self._mask)
 
     def _node(self):
         if not self.shape or len(self.shape.nodes) != 1:
@@ -303,28 +321,84 @@ class ParticleContainer:
     def __init__(self, field):
         self._field = field
         self._list = []
+        self._free = []
 
     def add(self, par, nodes=-1):
-        """ParticleContainer.add: nodes=True puts the particle's node into DemField.nodes (integrated by
-        Leapfrog), False leaves it out, -1 decides by DemData.guessMoving (DemField.collectNodes)."""
+        """ParticleContainer.add (pyAppend, ParticleContainer.cpp:176-207): nodes=True puts the particle's
+        node into DemField.nodes (integrated by Leapfrog), False leaves it out, -1 decides by
+        DemData.guessMoving.  The particle takes the first free id (findFreeId, :23-36): an id left by
+        a removed particle, else the next one past the end."""
         if isinstance(par, (list, tuple)):
             return [self.add(p, nodes=nodes) for p in par]
+        if par is None:
+            raise ValueError("Particle to be added is None.")
+        if par.id >= 0:
+            raise IndexError(f"Particle already has id {par.id} set; appending such particle (for the second time) "
+                             "is not allowed.")
+        if nodes not in (-1, 0, 1):
+            raise ValueError(f"nodes must be in {{-1,0,1}} (not {nodes}).")
         if self._field._engine_bound():
             raise RuntimeError("adding particles after the GPU engine has started is not supported")
-        par.id = len(self._list)
+        id = len(self._list)
+        while self._free:
+            f = self._free.pop(0)
+            if f <= len(self._list):
+                id = f
+                break
         node = par.shape.nodes[0]
         par._integrated = bool(nodes) if nodes != -1 else node.dem.guessMoving()
-        self._list.append(par)
+        par.id = id
+        if id == len(self._list):
+            self._list.append(par)
+        else:
+            self._list[id] = par
         return par.id
 
     def __getitem__(self, i):
+        """ParticleContainer::pyGetItem (ParticleContainer.cpp:230-235): negative ids count from the end;
+        an id without a particle raises IndexError."""
+        n = len(self._list)
+        if -n <= i < 0:
+            i += n
+        if not self.exists(i):
+            raise IndexError(f"No such particle: #{i}.")
         return self._list[i]
 
     def __len__(self):
+        """Size of the id range (ids of removed particles included, trailing ones trimmed)."""
         return len(self._list)
 
     def __iter__(self):
-        return iter(self._list)
+        """Existing particles by increasing id (ParticleContainer::pyIterator::next skips removed ids)."""
+        return (p for p in self._list if p is not None)
+
+    def exists(self, id):
+        return 0 <= id < len(self._list) and self._list[id] is not None
+
+    def remove(self, ids):
+        """ParticleContainer.remove (pyRemove / pyRemoveList, ParticleContainer.cpp:107-117): remove one
+        particle (returns whether it existed) or a sequence of them (list of such flags), with all of
+        their contacts (DemField::removeParticle, Particle.cpp:483-530).  Ids of the other particles do
+        not change; a removed id is left empty."""
+        if isinstance(ids, (list, tuple, np.ndarray)):
+            ids = [int(i) for i in ids]
+            done = [self.exists(i) for i in ids]
+            gone = sorted({i for i, d in zip(ids, done) if d})
+        else:
+            ok = self.exists(int(ids))
+            gone = [int(ids)] if ok else []
+            done = ok
+        if gone:
+            self._field._remove_particles(gone)
+        return done
+
+    def _drop(self, ids):
+        for i in ids:
+            self._list[i] = None
+            self._free.append(i)
+        # removing the last particle shrinks the container (ParticleContainer::remove, :150-154)
+        while self._list and self._list[-1] is None:
+            self._list.pop()
 
 
 # ---------------------------------------------------------------------------------------- contacts
@@ -471,6 +545,7 @@ class DemField:
         self._arrays = None      # abi.ParticleArrays once bound to an engine
         self._stale = False      # device state newer than _arrays
         self._dirty = set()      # host edits not yet uploaded
+        self._dead = set()       # slots of removed particles on the device (never collide, never move)
         self._con_cache = None
         if par:
             self.par.add(list(par))
@@ -500,6 +575,17 @@ class DemField:
             self._engine._download_particles(self)
         getattr(self._arrays, name)[idx] = v
         self._dirty.add(name)
+
+    def _set_mask(self, idx, mask):
+        self._arrays.mask[idx] = mask
+        self._dirty.add("mask")
+
+    def _remove_particles(self, ids):
+        """DemField::removeParticle for each id (src/dem/Particle.cpp:483-530): its contacts go, the other
+        particles keep their ids and contact history."""
+        if self._engine is not None:
+            self._engine._remove_particles(self, ids)
+        self.par._drop(ids)
 
     def _contacts(self):
         if self._engine is None:
@@ -628,6 +714,70 @@ class Engine(_Attrs):
 
     def critDt(self):
         return math.inf
+
+
+class PeriodicEngine(Engine):
+    """PeriodicEngine (src/core/Engine.hpp:129-161) for engines that run on the host between GPU steps.
+    Activation follows PeriodicEngine::isActivated (src/core/Engine.cpp:170-195) with the step
+    criterion; virtPeriod and realPeriod (simulation and wall-clock time) are not supported, since the
+    GPU runs the steps between two activations without stopping."""
+    _defaults = dict(virtPeriod=0.0, realPeriod=0.0, stepPeriod=1, stepModulo=True, nDo=-1, nDone=0,
+                     initRun=True, virtLast=nan, realLast=nan, stepLast=-1, stepPrev=-1, virtPrev=-1.0,
+                     realPrev=-1.0)
+
+    def _check(self):
+        if self.virtPeriod > 0 or self.realPeriod > 0:
+            raise RuntimeError(f"{type(self).__name__}: virtPeriod/realPeriod are not supported on the GPU engine "
+                               "(use stepPeriod)")
+
+    def _exhausted(self):
+        return self.stepPeriod <= 0 or (self.nDo >= 0 and self.nDone >= self.nDo)
+
+    def _next_step(self, s, time):
+        """The first step >= s at which isActivated may fire (None: never), given that it is evaluated in
+        every step from s on (a dead engine is not evaluated).  The first evaluation starts the count
+        (Engine.cpp:175-178); where it does not fire, that is all it does, so it is done here."""
+        if self.dead:
+            return None
+        per = int(self.stepPeriod)
+        if self.stepLast < 0:
+            if not self._exhausted() and self.stepModulo and s % per == 0:
+                return s
+            self.stepLast = s
+            self.virtLast = time
+            self.realLast = _clock()
+        if self._exhausted():
+            return None
+        t = self.stepLast + per
+        if self.stepModulo:
+            t = min(t, -(-s // per) * per)
+        return max(t, s)
+
+    def _activate(self, s, time):
+        """PeriodicEngine::isActivated at step s (Engine.cpp:170-195), step criterion."""
+        now = _clock()
+        init = self.stepLast < 0
+        if init:
+            self.realLast, self.virtLast, self.stepLast = now, time, s
+        per = int(self.stepPeriod)
+        if (self.nDo < 0 or self.nDone < self.nDo) and per > 0 and \
+                ((s - self.stepLast >= per) or (self.stepModulo and s % per == 0)):
+            self.realPrev, self.realLast = self.realLast, now
+            self.virtPrev, self.virtLast = self.virtLast, time
+            self.stepPrev, self.stepLast = self.stepLast, s
+            if init and not self.initRun:
+                return False
+            self.nDone += 1
+            return True
+        return False
+
+    def run(self, scene):
+        raise NotImplementedError
+
+
+def _clock():
+    import time as _t
+    return _t.time()
 
 
 class Leapfrog(Engine):
@@ -778,35 +928,66 @@ class GpuDemEngine(Engine):
     def _pack(self, field):
         n = len(field.par)
         pa = abi.ParticleArrays(n)
-        for p in field.par:
-            i = p.id
-            sh = p.shape
-            if isinstance(sh, Sphere):
-                pa.shape[i] = abi.SHAPE_SPHERE; pa.radius[i] = sh.radius
-            elif isinstance(sh, Wall):
-                pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
-            elif isinstance(sh, Ellipsoid):
-                pa.shape[i] = abi.SHAPE_ELLIPSOID; pa.semiAxes[i] = sh.semiAxes
-            else:
-                raise RuntimeError(f"GpuDemEngine: unsupported shape {type(sh).__name__}")
-            pa.material[i] = self._mat_index[id(p.material)]
-            pa.mask[i] = p.mask
-            node = sh.nodes[0]
-            for name in _FIELD_ARRAY_NAMES:
-                getattr(pa, name)[i] = node._local[name]
+        live = [p for p in field.par]
+        if not live:
+            raise RuntimeError("GpuDemEngine: the field has no particles")
+        filler = next((p for p in live if isinstance(p.shape, Sphere)), live[0])
+        for i in range(n):
+            if not field.par.exists(i):
+                # an id left by a removed particle: a dead slot holding a copy of a live particle's data,
+                # which the device view keeps fixed and out of every contact
+                self._pack_one(pa, i, filler)
+                field._dead.add(i)
+        for p in live:
+            self._pack_one(pa, p.id, p)
         return pa
+
+    def _pack_one(self, pa, i, p):
+        sh = p.shape
+        if isinstance(sh, Sphere):
+            pa.shape[i] = abi.SHAPE_SPHERE; pa.radius[i] = sh.radius
+        elif isinstance(sh, Wall):
+            pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
+        elif isinstance(sh, Ellipsoid):
+            pa.shape[i] = abi.SHAPE_ELLIPSOID; pa.semiAxes[i] = sh.semiAxes
+        else:
+            raise RuntimeError(f"GpuDemEngine: unsupported shape {type(sh).__name__}")
+        pa.material[i] = self._mat_index[id(p.material)]
+        pa.mask[i] = p.mask
+        node = sh.nodes[0]
+        for name in _FIELD_ARRAY_NAMES:
+            getattr(pa, name)[i] = node._local[name]
 
     def _device_view(self, field, pa):
         """The arrays as uploaded: a particle whose node is not in DemField.nodes is never moved by
-        Leapfrog, so the GPU engine holds it fixed (all DOFs blocked, no velocity)."""
+        Leapfrog, so the GPU engine holds it fixed (all DOFs blocked, no velocity).  The slot of a
+        removed particle is held fixed as well and gets mask 0, so that Collider::mayCollide
+        (src/dem/Collision.cpp:21-43) never pairs it."""
         idle = [p.id for p in field.par if not getattr(p, "_integrated", True)]
-        if not idle:
+        dead = sorted(field._dead)
+        if not idle and not dead:
             return pa
         up = pa.copy()
-        up.flags[idle] |= 63
-        up.vel[idle] = 0
-        up.angVel[idle] = 0
+        for ids in (idle, dead):
+            up.flags[ids] |= 63
+            up.vel[ids] = 0
+            up.angVel[ids] = 0
+        up.mask[dead] = 0
         return up
+
+    def _remove_particles(self, field, ids):
+        """Remove particles from a running field: their contacts leave the container and their slots
+        become dead; the other contacts keep their history.  The collider rebuilds at the next step,
+        which does not change the motion (every pair that can touch before the next rebuild is found)."""
+        if field._stale:
+            self._download_particles(field)
+        con = self._download_contacts().without_particles(ids)
+        field._dead.update(int(i) for i in ids)
+        self._h.upload_particles(self._device_view(field, field._arrays))
+        self._h.set_params(self._params)
+        self._h.upload_contacts(con)
+        field._dirty.clear()
+        field._con_cache = None
 
     # ------------------------------------------------------------------ engine protocol
     def critDt(self):
@@ -917,3 +1098,6 @@ class GpuDemEngine(Engine):
 
     def kernelTimes(self):
         return self._h.kernel_times() if self._h else {}
+
+
+from .outlet import Outlet, BoxOutlet, StackedBoxOutlet, CrazyOutlet  # noqa: E402  (they derive from PeriodicEngine)
