@@ -24,6 +24,9 @@ class OracleHandle:
     def keep_geom(self, on):
         pass
 
+    def close(self):
+        self.o = None
+
     def set_params(self, params):
         self.params = params
         if self.o is not None:

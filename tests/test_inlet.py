@@ -1,0 +1,160 @@
+"""Inlets (src/dem/Inlet.cpp) through the Python surface on the CPU, with the engine's handle on the
+oracle: mass-rate bookkeeping, non-overlapping placement, the maxNum / maxMass / maxAttempts endings,
+reuse of removed ids, and growth of the engine past its capacity."""
+import math
+
+import numpy as np
+import pytest
+
+from woo_gb300 import dem
+from woo_gb300.core import Scene
+
+from oracle_handle import run_on_oracle
+
+
+def bin_scene(engines=(), gravity=(0, 0, -9.81), n_pre=0, **kw):
+    """A 10 x 10 cm walled bin with a floor; n_pre spheres of radius 6 mm already in it."""
+    m = dem.FrictMat(density=2500, young=1e7, ktDivKn=0.2, tanPhi=0.5)
+    par = [dem.Wall.make(-0.05, axis=0, sense=1, mat=m), dem.Wall.make(0.05, axis=0, sense=-1, mat=m),
+           dem.Wall.make(-0.05, axis=1, sense=1, mat=m), dem.Wall.make(0.05, axis=1, sense=-1, mat=m),
+           dem.Wall.make(0, axis=2, sense=1, mat=m)]
+    for k in range(n_pre):
+        par.append(dem.Sphere.make((-0.03 + 0.015 * (k % 5), -0.03 + 0.015 * (k // 5 % 5), 0.006 + 0.013 * (k // 25)),
+                                   0.006, mat=m))
+    S = Scene(fields=[dem.DemField(gravity=gravity, par=par)],
+              engines=dem.DemField.minimalEngines(damping=0.2, dynDtPeriod=0) + list(engines), dtSafety=0.9, **kw)
+    return S, m
+
+
+def inlet(mat, **kw):
+    kw.setdefault("box", ((-0.05, -0.05, 0.1), (0.05, 0.05, 0.2)))
+    kw.setdefault("stepPeriod", 100)
+    return dem.BoxInlet(materials=[mat], generator=dem.MinMaxSphereGenerator(dRange=(0.008, 0.012)), **kw)
+
+
+def _no_overlap(S, ids):
+    c = np.array([S.dem.par[i].pos for i in ids])
+    r = np.array([S.dem.par[i].shape.radius for i in ids])
+    d = np.sqrt(((c[:, None, :] - c[None, :, :]) ** 2).sum(-1))
+    np.fill_diagonal(d, np.inf)
+    return bool((d >= r[:, None] + r[None, :]).all())
+
+
+def test_mass_rate_bookkeeping(monkeypatch):
+    S, m = bin_scene(gravity=(0, 0, 0))
+    ii = inlet(m, massRate=0.2, seed=3)
+    S.engines = S.engines + [ii]
+    n0 = len(S.dem.par)
+    run_on_oracle(monkeypatch, S, 701)                    # runs at steps 0, 100, ..., 700
+    assert ii.nDone == 8
+    # the first run sees no elapsed steps (stepPrev is this step, Inlet.cpp:251-254): goal grows 7 times
+    goal = 0.2 * S.dt * 700
+    assert ii.stepGoalMass == pytest.approx(goal, rel=1e-12)
+    assert goal <= ii.mass < goal + 2500 * 4 / 3 * math.pi * 0.006 ** 3
+    new = list(range(n0, len(S.dem.par)))
+    assert ii.num == len(new) > 5
+    assert ii.mass == pytest.approx(sum(S.dem.par[i].mass for i in new), rel=1e-12)
+    assert all(S.dem.par[i].mask == dem.DemField.defaultInletMask for i in new)
+    # zero gravity and no velocity: placed without overlap, the spheres stay where they were put
+    assert _no_overlap(S, new)
+    lo, hi = np.array([-0.05, -0.05, 0.1]), np.array([0.05, 0.05, 0.2])
+    for i in new:
+        p, r = S.dem.par[i].pos, S.dem.par[i].shape.radius
+        assert np.all(p - r >= lo) and np.all(p + r <= hi)
+        assert 0.004 <= r <= 0.006
+    assert S.dem.con.countReal() == 0
+    d, mm = ii.generator.diamMass()
+    assert len(d) == ii.num and mm.sum() == pytest.approx(ii.mass, rel=1e-12)
+    assert math.isfinite(ii.currRate) and ii.currRate > 0
+
+
+def test_max_num_ends_and_particles_fall(monkeypatch):
+    S, m = bin_scene()
+    ii = inlet(m, massRate=5.0, maxNum=12, seed=1)
+    S.engines = S.engines + [ii]
+    n0 = len(S.dem.par)
+    run_on_oracle(monkeypatch, S, 2001)
+    assert ii.num == 12 and ii.dead and ii.currRate == 0.
+    assert len(S.dem.par) == n0 + 12
+    zs = [S.dem.par[i].pos[2] for i in range(n0, n0 + 12)]
+    assert max(zs) < 0.1                                  # fell out of the inlet box, bouncing on the floor
+    assert min(S.dem.par[i].pos[2] - S.dem.par[i].shape.radius for i in range(n0, n0 + 12)) > -0.002
+
+
+def test_fill_until_attempts_fail(monkeypatch):
+    """massRate=0: as many particles as fit (maxAttempts failures end the run, Inlet.cpp:306-311)."""
+    S, m = bin_scene(gravity=(0, 0, 0))
+    ii = inlet(m, massRate=0, maxAttempts=300, seed=2, box=((-0.02, -0.02, 0.1), (0.02, 0.02, 0.14)))
+    S.engines = S.engines + [ii]
+    run_on_oracle(monkeypatch, S, 1)
+    assert 15 <= ii.num <= 64
+    new = list(range(5, len(S.dem.par)))
+    assert _no_overlap(S, new)
+
+
+def test_max_attempts_error_and_dead(monkeypatch):
+    S, m = bin_scene(gravity=(0, 0, 0))
+    tiny = ((-0.003, -0.003, 0.1), (0.003, 0.003, 0.106))  # smaller than every generated sphere
+    ii = inlet(m, massRate=1.0, maxAttempts=50, box=tiny)
+    S.engines = S.engines + [ii]
+    with pytest.raises(RuntimeError, match="maxAttempts reached"):
+        run_on_oracle(monkeypatch, S, 101)
+    S2, m2 = bin_scene(gravity=(0, 0, 0))
+    ij = inlet(m2, massRate=1.0, maxAttempts=50, box=tiny, atMaxAttempts="dead")
+    S2.engines = S2.engines + [ij]
+    run_on_oracle(monkeypatch, S2, 201)
+    assert ij.dead and ij.num == 0
+
+
+def test_removed_ids_are_reused(monkeypatch):
+    S, m = bin_scene(n_pre=10, gravity=(0, 0, 0))
+    S.dem.par[7].pos = (0.0, 0.0, -0.5)                   # below the floor: the outlet takes them
+    S.dem.par[9].pos = (0.01, 0.0, -0.5)
+    out = dem.BoxOutlet(box=((-1, -1, -0.1), (1, 1, 1)), stepPeriod=50)
+    ii = inlet(m, massRate=0.5, maxNum=3, seed=4, stepPeriod=100)
+    S.engines = S.engines + [out, ii]
+    n0 = len(S.dem.par)
+    run_on_oracle(monkeypatch, S, 201)
+    assert out.num == 2 and ii.num == 3
+    # ParticleContainer::findFreeId: the freed ids first (in the order they were freed), then the end
+    assert len(S.dem.par) == n0 + 1
+    assert all(S.dem.par.exists(i) for i in range(n0 + 1))
+    assert S.dem.par[7].mask == S.dem.par[9].mask == S.dem.par[n0].mask == dem.DemField.defaultInletMask
+
+
+def test_growth_past_capacity_keeps_state(monkeypatch):
+    """More particles than the engine has room for: a new handle takes the state over; accumulated
+    energies continue, and the scene matches one run with room to spare from the start."""
+    runs = []
+    for cap in (0, 1):
+        S, m = bin_scene(n_pre=20, trackEnergy=True)
+        ii = inlet(m, massRate=1.0, maxNum=30, seed=6,
+                   shooter=dem.AlignedMinMaxShooter(dir=(0, 0, -1), vRange=(0.1, 0.5)))
+        S.engines = S.engines + [ii]
+        S._engine().capacity = (len(S.dem.par) + 1) if cap else 0
+        run_on_oracle(monkeypatch, S, 1501)
+        runs.append(S)
+    a, b = runs
+    assert a._gpu._cap >= len(a.dem.par) and len(b.dem.par) <= b._gpu._cap < 2 * len(b.dem.par)
+    assert b._gpu._cap > 26                               # the small-capacity run went through a new handle
+    assert len(a.dem.par) == len(b.dem.par)
+    for i in range(len(a.dem.par)):
+        assert np.array_equal(a.dem.par[i].pos, b.dem.par[i].pos)
+    ea, eb = a.energy, b.energy
+    assert ea["kinInlet"] < 0                             # -Ek of the shot particles (Inlet.cpp:484)
+    for k in ("grav", "nonviscDamp", "kinInlet"):
+        assert eb[k] == pytest.approx(ea[k], rel=1e-12), k
+    assert eb["kinetic"] == pytest.approx(ea["kinetic"], rel=1e-12)
+
+
+def test_inlet_crit_dt_and_rejections():
+    S, m = bin_scene()
+    ii = inlet(m, massRate=1.0)
+    # RandomInlet::critDt: generator.critDt(density, young) = spherePWaveDt(dRange[0], ...)
+    assert ii.critDt() == pytest.approx(0.008 / math.sqrt(1e7 / 2500))
+    S.engines = S.engines + [ii]
+    S._prepare_dt()
+    assert S.dt == pytest.approx(0.9 * 0.006 / math.sqrt(1e7 / 2500)) or S.dt <= 0.9 * ii.critDt()
+    with pytest.raises(RuntimeError, match="doneHook"):
+        S2, m2 = bin_scene(engines=[inlet(m, massRate=1.0, doneHook="print(1)")])
+        S2._engine()

@@ -245,7 +245,7 @@ class Scene:
         eng = self._engine()
         if eng._h is None:
             return EnergyTracker(dict(self._host_energy))
-        d = {k: v for k, v in eng._h.energy().items() if v != 0.0}
+        d = {k: v for k, v in eng.energy().items() if v != 0.0}
         d.update(self._host_energy)
         return EnergyTracker(d)
 

@@ -329,7 +329,14 @@ class ParticleContainer:
         DemData.guessMoving.  The particle takes the first free id (findFreeId, :23-36): an id left by
         a removed particle, else the next one past the end."""
         if isinstance(par, (list, tuple)):
-            return [self.add(p, nodes=nodes) for p in par]
+            ids = [self._add_one(p, nodes) for p in par]
+            self._field._particles_added([self._list[i] for i in ids])
+            return ids
+        i = self._add_one(par, nodes)
+        self._field._particles_added([par])
+        return i
+
+    def _add_one(self, par, nodes):
         if par is None:
             raise ValueError("Particle to be added is None.")
         if par.id >= 0:
@@ -337,8 +344,6 @@ class ParticleContainer:
                              "is not allowed.")
         if nodes not in (-1, 0, 1):
             raise ValueError(f"nodes must be in {{-1,0,1}} (not {nodes}).")
-        if self._field._engine_bound():
-            raise RuntimeError("adding particles after the GPU engine has started is not supported")
         id = len(self._list)
         while self._free:
             f = self._free.pop(0)
@@ -579,6 +584,12 @@ class DemField:
     def _set_mask(self, idx, mask):
         self._arrays.mask[idx] = mask
         self._dirty.add("mask")
+
+    def _particles_added(self, pars):
+        """Particles added to a running field reach the GPU at the next run (with the contact history
+        of the others), in the slots of their ids."""
+        if self._engine is not None:
+            self._engine._add_particles(self, pars)
 
     def _remove_particles(self, ids):
         """DemField::removeParticle for each id (src/dem/Particle.cpp:483-530): its contacts go, the other
@@ -821,7 +832,7 @@ class GpuDemEngine(Engine):
     Constructed like ContactLoop from the three functor lists (src/dem/ContactLoop.cpp:52-66), plus
     the Leapfrog (damping, reset) and collider (verletDist) attributes.  Runs libwdem.so on one CUDA
     device; errors come back as RuntimeError."""
-    _defaults = dict(damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
+    _defaults = dict(capacity=0, damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
                      updatePhys="never", dist00=True, device=0, keepGeom=True)
 
     def __init__(self, cg2=None, cp2=None, law=None, **kw):
@@ -998,7 +1009,15 @@ class GpuDemEngine(Engine):
             return
         params = self._build_params(scene, field)
         pa = self._pack(field)
-        h = abi.Handle(max(pa.n, 1), device=self.device)
+        cap = max(pa.n, 1, int(self.capacity))
+        inlets = [e for e in getattr(scene, "_host", []) if hasattr(e, "_reserve")]
+        if inlets and not self.capacity:
+            # room for the particles the inlets may add (their maxNum / maxMass), else twice the scene
+            res = [e._reserve() for e in inlets]
+            cap = max(cap, pa.n + (sum(res) if all(r is not None for r in res) else max(pa.n, 1024)))
+        self._cap = cap
+        self._energy_base = {}
+        h = abi.Handle(cap, device=self.device)
         h.keep_geom(self.keepGeom)
         h.set_params(params)
         h.upload_particles(self._device_view(field, pa))
@@ -1079,12 +1098,88 @@ class GpuDemEngine(Engine):
         if field._dirty <= kin:
             self._h.write_state(n, dv.pos.ctypes.data, dv.vel.ctypes.data, dv.angVel.ctypes.data, dv.ori.ctypes.data)
         else:
-            # mass/inertia/flags/forces changed: full upload, keeping the contact history
+            # mass/inertia/flags/masks changed or particles added: full upload, keeping the contact history
             con = self._download_contacts()
+            if n > self._cap:
+                self._regrow(field, max(n, 2 * self._cap))
+            self._h.set_params(self._params)   # materials of added particles first
             self._h.upload_particles(dv)
             self._h.set_params(self._params)
             self._h.upload_contacts(con)
         field._dirty.clear()
+
+    def _add_particles(self, field, pars):
+        """Particles added to the running field: packed into the slots of their ids (reused ids of removed
+        particles first, as ParticleContainer::findFreeId), uploaded at the next run."""
+        if field._stale:
+            self._download_particles(field)
+        pa = field._arrays
+        n = len(field.par)
+        if n > pa.n:
+            grown = abi.ParticleArrays(n)
+            for k, v in pa.__dict__.items():
+                if isinstance(v, np.ndarray):
+                    getattr(grown, k)[:pa.n] = v
+            pa = grown
+            field._arrays = pa
+        for p in pars:
+            m = p.material
+            if id(m) not in self._mat_index:
+                self._add_material(m)
+            self._pack_one(pa, p.id, p)
+            for nd in p.shape.nodes:
+                nd._field, nd._idx = field, p.id
+            field._dead.discard(p.id)
+        field._dirty.add("added")
+        field._con_cache = None
+
+    def _add_material(self, m):
+        self._mat_index[id(m)] = len(self._mlist)
+        self._mlist.append(m)
+        arr = (abi.Material * len(self._mlist))()
+        for i in range(len(self._mlist) - 1):
+            arr[i] = self._mats[i]
+        k = len(self._mlist) - 1
+        arr[k].kind = getattr(m, "_kind", abi.MAT_FRICT)
+        arr[k].density = m.density
+        arr[k].young = m.young
+        arr[k].ktDivKn = getattr(m, "ktDivKn", 0.2)
+        arr[k].tanPhi = getattr(m, "tanPhi", 0.5)
+        arr[k].surfEnergy = getattr(m, "surfEnergy", 0.0)
+        arr[k].alpha = getattr(m, "alpha", 0.0)
+        self._mats = arr
+        self._params.nMaterials = len(self._mlist)
+        self._params.materials = arr
+
+    def _regrow(self, field, cap):
+        """A new handle with room for `cap` particles, carrying the state over: particles (uploaded by the
+        caller), contacts, the periodic cell, and the energies booked so far (kept on the host)."""
+        if getattr(self, "_dynDt", None) is not None:
+            raise RuntimeError(f"GpuDemEngine: {len(field.par)} particles exceed the engine's capacity {self._cap} "
+                               "and DynDt keeps its schedule on the device; set GpuDemEngine.capacity")
+        if getattr(field.scene, "periodic", False):
+            raise RuntimeError("GpuDemEngine: particles added to a periodic scene beyond the engine's capacity; "
+                               "set GpuDemEngine.capacity")
+        e = self._h.energy()
+        for k, v in e.items():
+            # kinetic and elast are reset every step (EnergyTracker::resetResettables): the new handle's value
+            # is the current one; the others accumulate
+            if k not in ("kinetic", "elast"):
+                self._energy_base[k] = self._energy_base.get(k, 0.0) + v
+        self._h.close()
+        h = abi.Handle(cap, device=self.device)
+        h.keep_geom(self.keepGeom)
+        ell = getattr(self, "_ellFunctor", None)
+        if ell is not None and ell.warmStart == "mlp":
+            h.warm_set_weights(ell.warmStartWeights)
+        self._h, self._cap = h, cap
+
+    def energy(self):
+        """Energies of the run so far (the device's totals plus those of replaced handles)."""
+        d = dict(self._h.energy())
+        for k, v in getattr(self, "_energy_base", {}).items():
+            d[k] = d.get(k, 0.0) + v
+        return d
 
     def _download_particles(self, field):
         self._h.download_particles(field._arrays)
@@ -1101,3 +1196,5 @@ class GpuDemEngine(Engine):
 
 
 from .outlet import Outlet, BoxOutlet, StackedBoxOutlet, CrazyOutlet  # noqa: E402  (they derive from PeriodicEngine)
+from .inlet import (Inlet, RandomInlet, BoxInlet, ParticleGenerator, MinMaxSphereGenerator,  # noqa: E402
+                    AlignedMinMaxShooter)

@@ -1,0 +1,336 @@
+"""Inlets (woo.dem.Inlet, src/dem/Inlet.hpp / Inlet.cpp): periodic engines that insert new spheres
+into a running scene at a prescribed mass rate.
+
+They run on the host between GPU steps, scheduled like the outlets (PeriodicEngine::isActivated,
+src/core/Engine.cpp:170-195).  New particles take the ids that removed particles left (findFreeId)
+or are appended; the GPU engine uploads them, with the contact history of the others, before its
+next step.  The sphere generator, the placement test and the mass bookkeeping follow
+RandomInlet::run (Inlet.cpp:228-515) for a spheres-only generator:
+
+- the goal mass grows by massRate*dt*(steps since the previous run); particles are made until the
+  generated mass reaches it (or, for massRate <= 0, until maxAttempts placements fail);
+- a particle is placed at random positions inside the box shrunk by padDist until it overlaps none of
+  the spheres near the box (existing ones and the ones placed in this run), trying a new particle
+  every maxAttempts/attemptPar attempts; atMaxAttempts decides what a failure does;
+- maxMass / maxNum end the inlet (dead, currRate zeroed when zeroRateAtStop).
+
+Random numbers come from a numpy generator seeded by `seed` (Woo draws from the C library's rand(),
+so its placements cannot be reproduced anyway).  Not provided: clump generators, PsdSphereGenerator,
+spatial biases, periodic cells, doneHook strings.
+"""
+import math
+
+import numpy as np
+
+from . import dem
+
+nan = float("nan")
+
+MAXATT = {"error": 0, "dead": 1, "warn": 2, "silent": 3, "nothing": 3, "ignore": 3, "": 3, "doneHook": 4, "done": 4}
+
+
+class ParticleGenerator(dem._Attrs):
+    """ParticleGenerator (Inlet.hpp:53-86): genDiamMassTime of the generated particles (with save)."""
+    _defaults = dict(save=True)
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.genDiamMassTime = []
+
+    def revokeLast(self):
+        if self.save and self.genDiamMassTime:
+            self.genDiamMassTime.pop()
+
+    def clear(self):
+        self.genDiamMassTime = []
+
+    def diamMass(self, zipped=False):
+        if zipped:
+            return [(d, m) for d, m, _ in self.genDiamMassTime]
+        return (np.array([d for d, _, _ in self.genDiamMassTime]), np.array([m for _, m, _ in self.genDiamMassTime]))
+
+    def massOfDiam(self, min=0, max=math.inf):
+        return sum(m for d, m, _ in self.genDiamMassTime if min <= d <= max)
+
+
+class MinMaxSphereGenerator(ParticleGenerator):
+    """MinMaxSphereGenerator (Inlet.hpp:88-99, Inlet.cpp:189-200): spheres with diameter uniform in dRange."""
+    _defaults = dict(dRange=(nan, nan))
+
+    def isSpheresOnly(self):
+        return True
+
+    def padDist(self):
+        return min(self.dRange) / 2.
+
+    def minMaxDiam(self):
+        return tuple(self.dRange)
+
+    def critDt(self, density, young):
+        # DemFuncs::spherePWaveDt(dRange[0], density, young): the reference passes the smaller diameter
+        return self.dRange[0] / math.sqrt(young / density)
+
+    def __call__(self, mat, time, rng):
+        d0, d1 = (float(x) for x in self.dRange)
+        if math.isnan(d0) or math.isnan(d1) or d0 > d1:
+            raise RuntimeError("MinMaxSphereGenerator: dRange[0]>dRange[1], or they are NaN!")
+        r = .5 * (d0 + rng.random() * (d1 - d0))
+        p = dem.Sphere.make((0, 0, 0), r, mat=mat)
+        if self.save:
+            self.genDiamMassTime.append((2 * r, p.mass, time))
+        return 2 * r, [(p, (np.array([-r, -r, -r]), np.array([r, r, r])))]
+
+
+class AlignedMinMaxShooter(dem._Attrs):
+    """AlignedMinMaxShooter (Inlet.hpp:109-121): velocity dir * U(vRange), no rotation."""
+    _defaults = dict(dir=(1.0, 0.0, 0.0), vRange=(nan, nan))
+
+    def __call__(self, node, rng):
+        v0, v1 = (float(x) for x in self.vRange)
+        if math.isnan(max(v0, v1)):
+            raise RuntimeError("AlignedMinMaxShooter.vRange: must not contain NaN.")
+        d = np.asarray(self.dir, np.float64)
+        d = d / math.sqrt(float(d @ d))
+        node.dem.vel = d * (v0 + rng.random() * (v1 - v0))
+        node.dem.angVel = (0, 0, 0)
+
+
+class Inlet(dem.PeriodicEngine):
+    """Inlet (Inlet.hpp:15-51): mask of new particles, maxMass / maxNum limits, mass and num generated,
+    currRate smoothed by currRateSmooth."""
+    _defaults = dict(mask=dem.DemField.defaultInletMask, maxMass=-1.0, maxNum=-1, doneHook="", mass=0.0, num=0,
+                     currRate=nan, zeroRateAtStop=True, currRateSmooth=1.0, glColor=0.0)
+
+    def _check(self):
+        super()._check()
+        if self.doneHook:
+            raise RuntimeError(f"{type(self).__name__}.doneHook (a Python string run by Woo) is not supported")
+
+    def setCurrRate(self, rate):
+        if math.isnan(self.currRate) or self.stepPrev < 0:
+            self.currRate = rate
+        else:
+            self.currRate = (1 - self.currRateSmooth) * self.currRate + self.currRateSmooth * rate
+
+    def everythingDone(self):
+        """Inlet::everythingDone (Inlet.cpp:215-225)."""
+        if (self.maxMass > 0 and self.mass >= self.maxMass) or (self.maxNum > 0 and self.num >= self.maxNum):
+            self.dead = True
+            if self.zeroRateAtStop:
+                self.currRate = 0.
+            return True
+        return False
+
+
+def _box_contains_box(box, b):
+    (lo, hi), (blo, bhi) = box, b
+    return bool(np.all(lo <= blo) and np.all(bhi <= hi))
+
+
+def _sq_exterior_distance(box, p):
+    lo, hi = box
+    d = np.maximum(lo - p, 0.) + np.maximum(p - hi, 0.)
+    return float(d @ d)
+
+
+class RandomInlet(Inlet):
+    """RandomInlet (Inlet.hpp:196-241, RandomInlet::run Inlet.cpp:228-515), spheres-only generators."""
+    _defaults = dict(massRate=nan, materials=(), generator=None, shooter=None, spatialBias=None, maxAttempts=5000,
+                     attemptPar=5, atMaxAttempts="error", padDist=0.0, color=nan, stepGoalMass=0.0,
+                     collideExisting=True, seed=0)
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self._rng = np.random.default_rng(self.seed)
+        self._inserted = []
+
+    def _check(self):
+        super()._check()
+        if self.spatialBias is not None:
+            raise RuntimeError("RandomInlet.spatialBias is not supported")
+
+    def critDt(self):
+        """RandomInlet::critDt (Inlet.cpp:203-212)."""
+        if self.generator is None:
+            return math.inf
+        ret = math.inf
+        for m in self.materials:
+            if isinstance(m, dem.ElastMat):
+                ret = min(ret, self.generator.critDt(m.density, m.young))
+        return ret
+
+    def minMaxDiam(self):
+        return self.generator.minMaxDiam() if self.generator is not None else (nan, nan)
+
+    def clear(self):
+        if self.generator is not None:
+            self.generator.clear()
+        self.num = 0
+        self.mass = 0.
+        self.stepGoalMass = 0.
+
+    def randomPosition(self, diam, padDist):
+        raise RuntimeError("Calling RandomInlet.randomPosition (abstract method); use derived classes.")
+
+    def validateBox(self, b):
+        raise RuntimeError("Calling RandomInlet.validateBox (abstract method); use derived classes.")
+
+    def _reserve(self):
+        """How many particles this inlet may still add (None: no bound known)."""
+        if self.maxNum > 0:
+            return max(self.maxNum - self.num, 0)
+        if self.maxMass > 0 and self.generator is not None and self.materials:
+            dmin = float(self.generator.minMaxDiam()[0])
+            rho = min(m.density for m in self.materials)
+            mmin = (4 / 3.0) * math.pi * (dmin / 2) ** 3 * rho
+            if mmin > 0:
+                return int(math.ceil(max(self.maxMass - self.mass, 0) / mmin)) + 1
+        return None
+
+    def run(self, scene):
+        field = scene.dem
+        if getattr(scene, "periodic", False):
+            raise RuntimeError("RandomInlet in a periodic cell is not supported")
+        if self.generator is None:
+            raise RuntimeError("RandomInlet.generator==None!")
+        if not self.materials:
+            raise RuntimeError("RandomInlet.materials is empty!")
+        if math.isnan(self.massRate):
+            raise RuntimeError(f"RandomInlet.massRate must be given (is {self.massRate}); if you want to generate as "
+                               "many particles as possible, say massRate=0.")
+        if self.massRate <= 0 and self.maxAttempts == 0:
+            raise RuntimeError("RandomInlet.massFlowRate<=0 (no massFlowRate prescribed), but RandomInlet.maxAttempts==0. "
+                               "(unlimited number of attempts); this would cause infinite loop.")
+        if not self.generator.isSpheresOnly():
+            raise RuntimeError("RandomInlet: only spheres-only generators are supported")
+        atMax = MAXATT[self.atMaxAttempts] if isinstance(self.atMaxAttempts, str) else int(self.atMaxAttempts)
+        rng = self._rng
+        self.padDist = self.generator.padDist()
+        if math.isnan(self.padDist) or self.padDist < 0:
+            raise RuntimeError(f"generator.padDist(): returned invalid value {self.padDist}")
+        if self.stepPrev == -1 and self.stepPeriod > 0:
+            self.stepPrev = -self.stepPeriod
+        nSteps = scene.step - self.stepPrev
+        self.stepGoalMass += self.massRate * scene.dt * nSteps
+        step_mass = 0.
+        # spheres near the inlet: the existing ones, then those placed in this run (Inlet.cpp:259-284)
+        box = self._box_global()
+        pack_c, pack_r = [], []
+        arr = field._arrays
+        if arr is not None and field._stale:
+            field._engine._download_particles(field)
+        for p in field.par:
+            if not isinstance(p.shape, dem.Sphere):
+                continue
+            pos = arr.pos[p.id] if arr is not None else p.pos
+            r = p.shape.radius
+            if box is not None and _sq_exterior_distance(box, pos) > r * r:
+                continue
+            pack_c.append(np.array(pos, np.float64))
+            pack_r.append(r)
+        new = []
+        done = False
+        while True:
+            if self.everythingDone():
+                done = True
+                break
+            if self.massRate > 0 and self.mass >= self.stepGoalMass:
+                break
+            attempt = -1
+            placed = None
+            while True:
+                attempt += 1
+                if attempt >= self.maxAttempts:
+                    self.generator.revokeLast()
+                    if self.massRate <= 0:
+                        break
+                    if atMax == 0:
+                        raise RuntimeError(f"RandomInlet.maxAttempts reached ({self.maxAttempts})")
+                    if atMax == 1:
+                        self.dead = True
+                        done = True
+                    break
+                per = self.maxAttempts // self.attemptPar if self.attemptPar else 0
+                if attempt == 0 or (per > 0 and attempt % per == 0):
+                    if attempt > 0:
+                        self.generator.revokeLast()
+                    mi = 0
+                    if len(self.materials) > 1:
+                        # the reference picks max(size*U, size-1): always the last material
+                        mi = max(int(len(self.materials) * rng.random()), len(self.materials) - 1)
+                    mat = self.materials[mi]
+                    diam, pee = self.generator(mat, scene.time, rng)
+                pos = self.randomPosition(diam, self.padDist)
+                ok = True
+                for par, (elo, ehi) in pee:
+                    if not self.validateBox((elo + pos, ehi + pos)):
+                        ok = False
+                        break
+                    r = par.shape.radius
+                    sub = par.shape.nodes[0]._local["pos"]
+                    c = pos + sub
+                    for sc, sr in zip(pack_c, pack_r):
+                        d = sc - c
+                        if float(d @ d) < (sr + r) * (sr + r):
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if ok:
+                    for par, _ in pee:
+                        pack_c.append(pos + par.shape.nodes[0]._local["pos"])
+                        pack_r.append(par.shape.radius)
+                    placed = pee
+                    break
+            if placed is None:
+                break
+            self.num += 1
+            for par, _ in placed:
+                par.mask = self.mask
+                node = par.shape.nodes[0]
+                node.pos = node._local["pos"] + pos
+                if self.shooter is not None:
+                    self.shooter(node, rng)
+                if scene.trackEnergy:
+                    from .outlet import kinetic_energy
+                    ek = kinetic_energy(node.dem.mass, node.dem.inertia, node.pos, node.dem.vel, node.dem.angVel,
+                                        node.ori, scene.dt)
+                    scene._energy_add("kinInlet", -ek)
+                self.mass += node.dem.mass
+                step_mass += node.dem.mass
+                new.append(par)
+        if new:
+            field.par.add(new, nodes=1)
+            self._inserted.extend(p.id for p in new)
+        if not done:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                self.setCurrRate(float(np.float64(step_mass) / (np.float64(nSteps) * scene.dt)))
+
+    def _box_global(self):
+        return None
+
+
+class BoxInlet(RandomInlet):
+    """BoxInlet (Inlet.hpp:243-268, Inlet.cpp:518-525): random positions in the axis-aligned box shrunk by
+    padDist; a particle's box must lie in the box."""
+    _defaults = dict(box=((nan, nan, nan), (nan, nan, nan)), node=None)
+
+    def _check(self):
+        super()._check()
+        if self.node is not None:
+            raise RuntimeError("BoxInlet.node is not supported (give the box in global coordinates)")
+
+    def _lohi(self):
+        lo, hi = self.box
+        return np.asarray(lo, np.float64).reshape(3), np.asarray(hi, np.float64).reshape(3)
+
+    def _box_global(self):
+        return self._lohi()
+
+    def randomPosition(self, diam, padDist):
+        lo, hi = self._lohi()
+        lo2, hi2 = lo + padDist, hi - padDist
+        return np.array([lo2[k] + (hi2[k] - lo2[k]) * self._rng.random() for k in range(3)])
+
+    def validateBox(self, b):
+        return _box_contains_box(self._lohi(), b)
