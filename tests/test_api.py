@@ -130,3 +130,12 @@ def test_nodes_left_out_are_held_fixed():
     assert pa.flags[held.id] & 63 == 0 and tuple(pa.vel[held.id]) == (1, 2, 3)
     others = [p.id for p in S.dem.par if p.id not in (ghost.id, held.id)]
     assert np.array_equal(dv.flags[others], pa.flags[others])
+
+
+def test_impose_is_rejected_not_ignored():
+    """DemData.impose (prescribed motion inside Leapfrog) is not provided: setting one raises."""
+    p = dem.Sphere.make((0, 0, 0), 0.01)
+    assert p.impose is None
+    p.impose = None
+    with pytest.raises(RuntimeError, match="impose"):
+        p.impose = object()

@@ -158,3 +158,28 @@ def test_inlet_crit_dt_and_rejections():
     with pytest.raises(RuntimeError, match="doneHook"):
         S2, m2 = bin_scene(engines=[inlet(m, massRate=1.0, doneHook="print(1)")])
         S2._engine()
+
+
+def test_energy_random_inlet_then_outlet(monkeypatch):
+    """py/tests/test_energy.py:50-67: an inlet shoots one sphere into an empty field and an outlet
+    deletes it in the same step; kinInlet = -Ek, kinOutlet = Ek, and the energies sum to zero.  (The
+    reference's engine list is [InsertionSortCollider, BoxInlet, BoxOutlet]; here the GPU engine's trio
+    stands in for the collider.)"""
+    from woo_gb300 import utils
+    mat = utils.defaultMaterial()
+    vel, rad = 1., .1
+    m = mat.density * (4 / 3.) * math.pi * rad ** 3
+    Ek = .5 * m * vel ** 2
+    S = Scene(fields=[dem.DemField(gravity=(0, 0, 0))], trackEnergy=True)
+    S.engines = dem.DemField.minimalEngines(dynDtPeriod=0) + [
+        dem.BoxInlet(maxNum=1, materials=[mat], generator=dem.MinMaxSphereGenerator(dRange=(2 * rad, 2 * rad)),
+                     shooter=dem.AlignedMinMaxShooter(dir=(1, 0, 0), vRange=(vel, vel)),
+                     box=((-.5, -.5, -.5), (.5, .5, .5)), massRate=0),
+        dem.BoxOutlet(inside=True, box=((-1, -1, -1), (1, 1, 1))),
+    ]
+    S.dt = .05
+    run_on_oracle(monkeypatch, S, 1)
+    assert len(S.dem.par) == 0
+    assert S.energy["kinOutlet"] == Ek
+    assert S.energy["kinInlet"] == -Ek
+    assert S.energy.total() == 0.

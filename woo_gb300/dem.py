@@ -120,6 +120,17 @@ class DemData:
     def isBlockedAll(self):
         return (self.flags & 63) == 63
 
+    @property
+    def impose(self):
+        return None
+
+    @impose.setter
+    def impose(self, v):
+        """DemData.impose (prescribed motion applied inside Leapfrog::run, src/dem/Leapfrog.cpp:22,205,
+        238-248) is not provided by the GPU engine; setting one is an error rather than being ignored."""
+        if v is not None:
+            raise RuntimeError(f"DemData.impose ({type(v).__name__}) is not supported by the GPU engine")
+
     def guessMoving(self):
         """DemData::guessMoving (src/dem/Particle.cpp:638-640): whether the node needs motion integration
         (it has mass and a free DOF, or a velocity)."""
@@ -304,6 +315,7 @@ class Particle:
     mass = property(lambda s: s._node().dem.mass)
     inertia = property(lambda s: s._node().dem.inertia)
     blocked = property(lambda s: s._node().dem.blocked, lambda s, v: setattr(s._node().dem, "blocked", v))
+    impose = property(lambda s: s._node().dem.impose, lambda s, v: setattr(s._node().dem, "impose", v))
 
     @property
     def nodes(self):
@@ -1045,6 +1057,10 @@ class GpuDemEngine(Engine):
     def run(self, scene, nSteps):
         field = scene.dem
         self._refresh_from_sources()
+        if self._h is None and next(iter(field.par), None) is None:
+            # nothing to integrate yet (an inlet fills the field later): only time advances
+            self._ran_time = nSteps * scene.dt
+            return
         self._ensure(scene, field)
         if field._dirty:
             self._upload_edits(field)
