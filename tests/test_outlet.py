@@ -129,18 +129,22 @@ def test_removed_id_is_a_dead_slot_on_the_device():
     view = g._device_view(S.dem, pa)
     assert view.mask[7] == 0 and view.flags[7] & 63 == 63
     assert not view.vel[7].any() and not view.angVel[7].any()
+    assert np.array_equal(view.pos[7], pa.pos[4])          # parked on the first live sphere
     assert (view.mask[[i for i in range(pa.n) if i != 7]] != 0).all()
 
 
 # ------------------------------------------------------------------------------------------ scripts
 def test_box_outlet_deletes_and_books(monkeypatch):
-    out = dem.BoxOutlet(box=((-1, -1, -0.05), (1, 1, 10)), stepPeriod=50, save=True)
+    out = dem.BoxOutlet(box=((-1, -1, -0.05), (1, 1, 10)), stepPeriod=50, save=True, savePar=True)
     S = funnel(engines=[out])
     n0 = len(S.dem.par)
     masses = {p.id: p.mass for p in S.dem.par}
     run_on_oracle(monkeypatch, S, 1201)                   # the last step (1200) runs the outlet
     gone = [i for i in range(n0) if not S.dem.par.exists(i)]
     assert out.num == len(gone) > 5
+    # a removed particle keeps the state it had when the outlet took it (outside the box), detached
+    assert len(out.par) == out.num
+    assert all(p.pos[2] < -0.05 and p.shape.nodes[0]._field is None for p in out.par)
     assert out.nDone == 1201 // 50 + 1
     assert out.mass == pytest.approx(sum(masses[i] for i in gone), rel=1e-14)
     d, m, t = out.diamMassTime()

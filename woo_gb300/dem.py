@@ -608,6 +608,12 @@ class DemField:
         particles keep their ids and contact history."""
         if self._engine is not None:
             self._engine._remove_particles(self, ids)
+            # the removed particles keep their last state, detached from the field
+            for i in ids:
+                node = self.par._list[i].shape.nodes[0]
+                node._local = {k: (getattr(self._arrays, k)[i].copy() if isinstance(getattr(self._arrays, k)[i], np.ndarray)
+                                   else getattr(self._arrays, k)[i].item()) for k in _FIELD_ARRAY_NAMES}
+                node._field, node._idx = None, -1
         self.par._drop(ids)
 
     def _contacts(self):
@@ -995,7 +1001,13 @@ class GpuDemEngine(Engine):
             up.flags[ids] |= 63
             up.vel[ids] = 0
             up.angVel[ids] = 0
-        up.mask[dead] = 0
+        if dead:
+            up.mask[dead] = 0
+            # parked on a live particle, so that a particle removed far outside the domain does not
+            # stretch the collider's grid
+            anchor = next((p.id for p in field.par if isinstance(p.shape, Sphere)), None)
+            if anchor is not None:
+                up.pos[dead] = pa.pos[anchor]
         return up
 
     def _remove_particles(self, field, ids):
