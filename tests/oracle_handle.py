@@ -52,9 +52,20 @@ class OracleHandle:
         return self.o.cell()
 
     def step(self, n=1):
+        import time
+        t0 = time.perf_counter()
         for _ in range(int(n)):
             self.time_sum += self.o.dt()
             self.o.step(1)
+        self._last = (time.perf_counter() - t0) * 1e3, int(n)
+
+    def set_timing(self, on):
+        self.timing = bool(on)
+
+    def kernel_times(self):
+        """The oracle's wall time of the last step call, booked as the contact phase."""
+        ms, n = getattr(self, "_last", (0.0, 0))
+        return {"leapfrog": (0.0, n), "collider": (0.0, 0), "contacts": (ms, n)}
 
     def status(self):
         return SimpleNamespace(code=0, timeSum=self.time_sum, dt=self.o.dt(), dynDtCrit=self.o.dyndt_crit())

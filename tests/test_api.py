@@ -139,3 +139,21 @@ def test_impose_is_rejected_not_ignored():
     p.impose = None
     with pytest.raises(RuntimeError, match="impose"):
         p.impose = object()
+
+
+def test_exec_time_with_timing_enabled(monkeypatch):
+    """Master.timingEnabled: execTime/execCount on the engine and on Woo's trio it stands for."""
+    from oracle_handle import run_on_oracle
+    S = small_scene()
+    run_on_oracle(monkeypatch, S, 5)
+    assert S.lab.contactLoop.execCount == 0
+    woo.master.timingEnabled = True
+    try:
+        run_on_oracle(monkeypatch, S, 7)
+    finally:
+        woo.master.timingEnabled = False
+    run_on_oracle(monkeypatch, S, 3)
+    for e in (S.lab.leapfrog, S.lab.collider, S.lab.contactLoop):
+        assert e.execCount == 7
+    assert S.lab.contactLoop.execTime > 0 and S._gpu.execCount == 7
+    assert S._gpu.execTime >= S.lab.contactLoop.execTime

@@ -738,8 +738,21 @@ class Law2_L6Geom_HertzPhys_DMT(LawFunctor):
 
 
 # ---------------------------------------------------------------------------------------- engines
+class Master:
+    """woo.master: timingEnabled switches engine timing on (Master.timingEnabled, Engine.execTime and
+    Engine.execCount, src/core/Engine.hpp:92-94)."""
+
+    def __init__(self):
+        self.timingEnabled = False
+
+
+master = Master()
+
+
 class Engine(_Attrs):
-    _defaults = dict(dead=False)
+    """Engine (src/core/Engine.hpp:19-104): dead; execTime (ns) and execCount, accumulated while
+    master.timingEnabled is set."""
+    _defaults = dict(dead=False, execTime=0, execCount=0)
 
     def critDt(self):
         return math.inf
@@ -900,6 +913,13 @@ class GpuDemEngine(Engine):
         for p in field.par:
             mats.setdefault(id(p.material), p.material)
         mlist = list(mats.values())
+        if isinstance(cp2, Cp2_HertzMat_HertzPhys):
+            bad = sorted({type(m).__name__ for m in mlist if not isinstance(m, HertzMat)})
+            if bad:
+                # ContactLoop.cpp:181: a CPhysFunctor must exist for every contacting material pair, and
+                # Cp2_HertzMat_HertzPhys takes HertzMat only (Hertz.hpp:54)
+                raise RuntimeError(f"Cp2_HertzMat_HertzPhys needs HertzMat for every particle (found {', '.join(bad)}): "
+                                   "a CPhysFunctor must be available for every contacting material combination")
         self._mat_index = {id(m): i for i, m in enumerate(mlist)}
         arr = (abi.Material * len(mlist))()
         for i, m in enumerate(mlist):
@@ -1105,8 +1125,14 @@ class GpuDemEngine(Engine):
         p.dtSafety = float(scene.dtSafety)
         if dyn is not None:
             self._h.set_params(p)
+        timing = bool(master.timingEnabled)
+        if timing != getattr(self, "_timing_on", False):
+            self._h.set_timing(timing)
+            self._timing_on = timing
         t0 = self._h.status().timeSum
         self._h.step(nSteps)
+        if timing:
+            self._book_times(nSteps)
         st = self._h.status()
         self._ran_time = st.timeSum - t0
         scene.dt = st.dt
@@ -1117,6 +1143,19 @@ class GpuDemEngine(Engine):
             self.updatePhys = "never"
             if getattr(self, "_sources", None):
                 self._sources["contactLoop"].updatePhys = "never"
+
+    def _book_times(self, nSteps):
+        """Device time of the three phases (CUDA events around each kernel) as execTime/execCount of this
+        engine and of the Leapfrog, InsertionSortCollider and ContactLoop it stands for."""
+        kt = self._h.kernel_times()
+        self.execTime += int(round(sum(ms for ms, _ in kt.values()) * 1e6))
+        self.execCount += nSteps
+        src = getattr(self, "_sources", None)
+        if src:
+            for phase, key in (("leapfrog", "leapfrog"), ("collider", "collider"), ("contacts", "contactLoop")):
+                if phase in kt:
+                    src[key].execTime += int(round(kt[phase][0] * 1e6))
+                    src[key].execCount += nSteps
 
     def _upload_edits(self, field):
         pa = field._arrays

@@ -1,6 +1,7 @@
 """woo.utils slice for the DEM hot path (py/utils.py): defaultEngines / DemField.minimalEngines,
 sphere/wall constructors, defaultMaterial."""
 import math
+import warnings
 
 from . import dem
 from .dem import defaultMaterial  # noqa: F401
@@ -14,9 +15,22 @@ def defaultEngines(damping=0.0, gravity=None, verletDist=-0.05, kinSplit=False, 
     if gravity:
         raise ValueError("gravity MUST NOT be specified anymore, set DemField.gravity=... instead.")
     if model is not None:
-        raise ValueError("model= is not supported; pass cp2= and law=")
-    cp2 = [cp2 if cp2 else dem.Cp2_FrictMat_FrictPhys()]
-    law = [law if law else dem.Law2_L6Geom_FrictPhys_IdealElPl(noSlip=noSlip, noBreak=noBreak, label="contactLaw")]
+        # py/utils.py:100-108: the functors and the damping come from the ContactModelSelector
+        if cp2 or law:
+            warnings.warn("cp2 and law args are ignored when model is provided.")
+        if damping != 0.:
+            warnings.warn("damping is ignored when model is provided.")
+        cp2, law = model.getFunctors()
+        if len(law) == 1:
+            law[0].label = "contactLaw"
+        if len(cp2) == 1:
+            cp2[0].label = "cp2"
+        damping = model.getNonviscDamping()
+        if model.distFactor != 1.0:
+            raise ValueError("ContactModelSelector.distFactor is not copied into the engines; set DemField.distFactor")
+    else:
+        cp2 = [cp2 if cp2 else dem.Cp2_FrictMat_FrictPhys()]
+        law = [law if law else dem.Law2_L6Geom_FrictPhys_IdealElPl(noSlip=noSlip, noBreak=noBreak, label="contactLaw")]
     for k, v in cpKw.items():
         setattr(cp2[0], k, v)
     for k, v in lawKw.items():
