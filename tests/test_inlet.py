@@ -183,3 +183,30 @@ def test_energy_random_inlet_then_outlet(monkeypatch):
     assert S.energy["kinOutlet"] == Ek
     assert S.energy["kinInlet"] == -Ek
     assert S.energy.total() == 0.
+
+
+def test_sphere_pack_grid_matches_brute_force():
+    from woo_gb300.inlet import _SpherePack
+    rng = np.random.default_rng(7)
+    C = rng.uniform(-0.3, 0.2, (3000, 3))
+    R = rng.uniform(0.002, 0.01, 3000)
+    pk = _SpherePack(C, R, rmax=0.012)
+    allC, allR = list(C), list(R)
+    hits = 0
+    for k in range(3000):
+        c = rng.uniform(-0.32, 0.22, 3)
+        r = rng.uniform(0.002, 0.012)
+        if k % 3 == 0:                                    # near-touching: exactly at the sum of radii
+            j = rng.integers(len(allR))
+            u = rng.normal(size=3)
+            c = allC[j] + u / np.linalg.norm(u) * (allR[j] + r)
+        A, B = np.array(allC), np.array(allR)
+        d = A - c
+        brute = bool(np.any(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2] < (B + r) * (B + r)))
+        assert pk.overlaps(c, r) == brute
+        hits += brute
+        if not brute and k % 2:
+            pk.add(c, r)
+            allC.append(c)
+            allR.append(r)
+    assert 100 < hits < 2900

@@ -246,3 +246,28 @@ def test_kin_outlet_energy(monkeypatch):
                 alive.discard(i)
     assert out.num == len(set(range(len(snap.states[0].pos))) - alive)
     assert S.energy["kinOutlet"] == pytest.approx(expect, rel=1e-12)
+
+
+def test_row_tests_match_point_tests():
+    """The vectorized volume tests give what isInside gives point by point (rotated local frame,
+    stacked slabs, speed limit), and canonicalize_rows wraps into the sheared cell."""
+    from woo_gb300 import outlet as O
+    rng = np.random.default_rng(0)
+    P = rng.uniform(-1.5, 1.5, (400, 3))
+    V = rng.normal(0, 30, (400, 3))
+    node = dem.Node(pos=(0.1, -0.2, 0.3), ori=(np.cos(0.3), 0, np.sin(0.3), 0))
+    for o in (dem.BoxOutlet(box=((-1, -0.5, -1), (0.5, 1, 0.8))),
+              dem.BoxOutlet(box=((-1, -0.5, -1), (0.5, 1, 0.8)), node=node),
+              dem.StackedBoxOutlet(box=((-1, -1, -1), (1, 1, 1)), divs=(-0.2, 0.4), axis=1, loc0=3, node=node),
+              dem.CrazyOutlet(limVelNorm=40.0)):
+        ins, loc = o.inside_rows(P, V)
+        for i in range(len(P)):
+            assert (bool(ins[i]), int(loc[i])) == o.isInside(P[i], V[i])
+        assert 0 < ins.sum() < len(P)
+    cell = O.CellView(hSize=[[1.0, 0.3, 0.0], [0.0, 1.2, 0.0], [0.0, 0.0, 0.9]], gradV=np.zeros((3, 3)))
+    W = cell.canonicalize_rows(P * 3)
+    U = (np.linalg.inv(cell.shearTrsf) @ W.T).T
+    assert np.all(U >= -1e-12) and np.all(U <= cell.size[None, :] + 1e-12)
+    # the wrapped point is the original one shifted by whole cell vectors
+    k = np.linalg.solve(cell.hSize, (P * 3 - W).T).T
+    assert np.allclose(k, np.round(k), atol=1e-9)

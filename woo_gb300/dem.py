@@ -577,9 +577,12 @@ class DemField:
     def _bind(self, engine, arrays):
         self._engine = engine
         self._arrays = arrays
+        # slots of existing particles whose node is in DemField.nodes (what outlets look at)
+        self._moving = np.zeros(arrays.n, bool)
         for p in self.par:
             for n in p.shape.nodes:
                 n._field, n._idx = self, p.id
+            self._moving[p.id] = getattr(p, "_integrated", True)
 
     def _get(self, idx, name):
         if self._stale:
@@ -1038,6 +1041,7 @@ class GpuDemEngine(Engine):
             self._download_particles(field)
         con = self._download_contacts().without_particles(ids)
         field._dead.update(int(i) for i in ids)
+        field._moving[list(ids)] = False
         self._h.upload_particles(self._device_view(field, field._arrays))
         self._h.set_params(self._params)
         self._h.upload_contacts(con)
@@ -1189,6 +1193,7 @@ class GpuDemEngine(Engine):
                     getattr(grown, k)[:pa.n] = v
             pa = grown
             field._arrays = pa
+            field._moving = np.concatenate([field._moving, np.zeros(n - len(field._moving), bool)])
         for p in pars:
             m = p.material
             if id(m) not in self._mat_index:
@@ -1197,6 +1202,7 @@ class GpuDemEngine(Engine):
             for nd in p.shape.nodes:
                 nd._field, nd._idx = field, p.id
             field._dead.discard(p.id)
+            field._moving[p.id] = getattr(p, "_integrated", True)
         field._dirty.add("added")
         field._con_cache = None
 

@@ -122,6 +122,55 @@ class Inlet(dem.PeriodicEngine):
         return False
 
 
+class _SpherePack:
+    """The spheres a new particle must not overlap: |c - s.c|^2 < (s.r + r)^2 is an overlap
+    (Inlet.cpp:363-370).  A uniform grid of cell size 2*rmax (rmax bounds every radius, new ones
+    included) limits the test to the 27 cells around c, which hold every sphere that can overlap."""
+
+    def __init__(self, C, R, rmax):
+        n = len(R)
+        self.h = 2. * max(float(rmax), float(R.max()) if n else 0.)
+        if not self.h > 0:
+            self.h = 1.
+        self.C = np.empty((max(2 * n, 64), 3))
+        self.R = np.empty(len(self.C))
+        self.n = n
+        self.C[:n], self.R[:n] = C, R
+        self.cells = {}
+        if n:
+            K = np.floor(C / self.h).astype(np.int64)
+            order = np.lexsort((K[:, 2], K[:, 1], K[:, 0]))
+            Ks = K[order]
+            starts = np.nonzero(np.any(np.diff(Ks, axis=0) != 0, axis=1))[0] + 1
+            bounds = np.concatenate([[0], starts, [n]])
+            for a, b in zip(bounds[:-1], bounds[1:]):
+                self.cells[tuple(Ks[a].tolist())] = order[a:b].tolist()
+
+    def _key(self, c):
+        return tuple(int(math.floor(x / self.h)) for x in c)
+
+    def overlaps(self, c, r):
+        kx, ky, kz = self._key(c)
+        idx = []
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    idx.extend(self.cells.get((kx + dx, ky + dy, kz + dz), ()))
+        if not idx:
+            return False
+        d = self.C[idx] - c[None, :]
+        s = self.R[idx] + r
+        return bool(np.any(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2] < s * s))
+
+    def add(self, c, r):
+        if self.n == len(self.R):
+            self.C = np.concatenate([self.C, np.empty_like(self.C)])
+            self.R = np.concatenate([self.R, np.empty_like(self.R)])
+        self.C[self.n], self.R[self.n] = c, r
+        self.cells.setdefault(self._key(c), []).append(self.n)
+        self.n += 1
+
+
 def _box_contains_box(box, b):
     (lo, hi), (blo, bhi) = box, b
     return bool(np.all(lo <= blo) and np.all(bhi <= hi))
@@ -214,20 +263,7 @@ class RandomInlet(Inlet):
         self.stepGoalMass += self.massRate * scene.dt * nSteps
         step_mass = 0.
         # spheres near the inlet: the existing ones, then those placed in this run (Inlet.cpp:259-284)
-        box = self._box_global()
-        pack_c, pack_r = [], []
-        arr = field._arrays
-        if arr is not None and field._stale:
-            field._engine._download_particles(field)
-        for p in field.par:
-            if not isinstance(p.shape, dem.Sphere):
-                continue
-            pos = arr.pos[p.id] if arr is not None else p.pos
-            r = p.shape.radius
-            if box is not None and _sq_exterior_distance(box, pos) > r * r:
-                continue
-            pack_c.append(np.array(pos, np.float64))
-            pack_r.append(r)
+        pack = _SpherePack(*self._existing_spheres(field), rmax=float(self.generator.minMaxDiam()[1]) / 2.)
         new = []
         done = False
         while True:
@@ -266,20 +302,12 @@ class RandomInlet(Inlet):
                     if not self.validateBox((elo + pos, ehi + pos)):
                         ok = False
                         break
-                    r = par.shape.radius
-                    sub = par.shape.nodes[0]._local["pos"]
-                    c = pos + sub
-                    for sc, sr in zip(pack_c, pack_r):
-                        d = sc - c
-                        if float(d @ d) < (sr + r) * (sr + r):
-                            ok = False
-                            break
-                    if not ok:
+                    if pack.overlaps(pos + par.shape.nodes[0]._local["pos"], par.shape.radius):
+                        ok = False
                         break
                 if ok:
                     for par, _ in pee:
-                        pack_c.append(pos + par.shape.nodes[0]._local["pos"])
-                        pack_r.append(par.shape.radius)
+                        pack.add(pos + par.shape.nodes[0]._local["pos"], par.shape.radius)
                     placed = pee
                     break
             if placed is None:
@@ -308,6 +336,30 @@ class RandomInlet(Inlet):
 
     def _box_global(self):
         return None
+
+    def _existing_spheres(self, field):
+        """Centres and radii of the spheres in the field that reach into the inlet's box
+        (squaredExteriorDistance(pos) <= r^2); every sphere when the inlet has no box."""
+        arr = field._arrays
+        if arr is not None:
+            if field._stale:
+                field._engine._download_particles(field)
+            live = np.ones(arr.n, bool)
+            if field._dead:
+                live[list(field._dead)] = False
+            ids = np.nonzero(live & (arr.shape == dem.abi.SHAPE_SPHERE))[0]
+            C, R = arr.pos[ids].copy(), arr.radius[ids].copy()
+        else:
+            sph = [p for p in field.par if isinstance(p.shape, dem.Sphere)]
+            C = np.array([p.pos for p in sph], np.float64).reshape(-1, 3)
+            R = np.array([p.shape.radius for p in sph], np.float64)
+        box = self._box_global()
+        if box is not None and len(R):
+            lo, hi = box
+            d = np.maximum(lo[None, :] - C, 0.) + np.maximum(C - hi[None, :], 0.)
+            keep = ~(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2] > R * R)
+            C, R = C[keep], R[keep]
+        return C, R
 
 
 class BoxInlet(RandomInlet):

@@ -48,6 +48,20 @@ def glob2loc(node, p):
     return _rotate(qc, np.asarray(p, np.float64) - node.pos)
 
 
+def matvec_rows(M, P):
+    """M @ p for every row p of P (n x 3), each component summed left to right."""
+    return np.stack([M[i, 0] * P[:, 0] + M[i, 1] * P[:, 1] + M[i, 2] * P[:, 2] for i in range(3)], axis=1)
+
+
+def sqnorm_rows(V):
+    return V[:, 0] * V[:, 0] + V[:, 1] * V[:, 1] + V[:, 2] * V[:, 2]
+
+
+def glob2loc_rows(node, P):
+    q = np.asarray(node.ori, np.float64)
+    return matvec_rows(rotation_matrix([q[0], -q[1], -q[2], -q[3]]), P - np.asarray(node.pos, np.float64))
+
+
 class CellView:
     """What the outlets need of Cell (src/core/Cell.hpp:72-103, Cell.cpp:36-58, 81-120), homoDeform gradV2:
     canonicalizePt and the fluctuation velocities."""
@@ -64,12 +78,12 @@ class CellView:
 
     def canonicalizePt(self, p):
         """shearPt(wrapPt(unshearPt(p))), wrapNum(x, sz) = (x/sz - floor(x/sz))*sz (CompUtils.hpp:10)."""
-        u = self.unshearTrsf @ np.asarray(p, np.float64)
-        w = np.empty(3)
-        for i in range(3):
-            nrm = u[i] / self.size[i]
-            w[i] = (nrm - math.floor(nrm)) * self.size[i]
-        return self.shearTrsf @ w
+        return self.canonicalize_rows(np.asarray(p, np.float64).reshape(1, 3))[0]
+
+    def canonicalize_rows(self, P):
+        U = matvec_rows(self.unshearTrsf, P)
+        nrm = U / self.size[None, :]
+        return matvec_rows(self.shearTrsf, (nrm - np.floor(nrm)) * self.size[None, :])
 
     def pprevFluctVel(self, pos, vel, dt):
         """Cell::pprevFluctVel, HOMO_GRADV2: vel - gradV*(pos - dt/2*vel)."""
@@ -110,26 +124,36 @@ class Outlet(dem.PeriodicEngine):
         """(inside?, loc) of a point; loc is -1 unless the outlet subdivides its volume."""
         raise RuntimeError(f"{type(self).__name__} did not override Outlet::isInside.")
 
+    def inside_rows(self, P, V):
+        """isInside for every row of P (positions) and V (velocities): (bool array, loc array)."""
+        res = [self.isInside(P[i], V[i]) for i in range(len(P))]
+        return np.array([r[0] for r in res], bool), np.array([r[1] for r in res], np.int64)
+
     def _select(self, field, cell):
-        """Particles to delete/mark, by increasing id (the std::set of Outlet.cpp:18), with their loc."""
+        """Particles to delete/mark, by increasing id (the std::set of Outlet.cpp:18), with their loc;
+        only particles whose node is in DemField.nodes are looked at (Outlet.cpp:21)."""
         deleting = self.markMask == 0
         arr = field._arrays
-        picked = []
-        for p in field.par:
-            if not getattr(p, "_integrated", True):
-                continue  # the node is not in DemField.nodes (Outlet.cpp:21)
-            i = p.id
-            pos = arr.pos[i] if arr is not None else p.pos
-            vel = arr.vel[i] if arr is not None else p.vel
-            inside, loc = self.isInside(cell.canonicalizePt(pos) if cell is not None else pos, vel)
-            if self.inside != inside:
-                continue
-            if self.mask and not (self.mask & p.mask):
-                continue
-            if not deleting and (self.markMask & p.mask) == self.markMask:
-                continue
-            picked.append((i, loc))
-        return picked
+        if arr is not None:
+            ids = np.nonzero(field._moving)[0]
+            P, V, masks = arr.pos[ids], arr.vel[ids], arr.mask[ids].astype(np.int64)
+        else:
+            par = [p for p in field.par if getattr(p, "_integrated", True)]
+            ids = np.array([p.id for p in par], np.int64)
+            P = np.array([p.pos for p in par]).reshape(-1, 3)
+            V = np.array([p.vel for p in par]).reshape(-1, 3)
+            masks = np.array([p.mask for p in par], np.int64)
+        if len(ids) == 0:
+            return []
+        if cell is not None:
+            P = cell.canonicalize_rows(P)
+        inside, loc = self.inside_rows(P, V)
+        sel = inside == bool(self.inside)
+        if self.mask:
+            sel &= (masks & self.mask) != 0
+        if not deleting:
+            sel &= (masks & self.markMask) != self.markMask
+        return list(zip(ids[sel].tolist(), loc[sel].tolist()))
 
     def run(self, scene):
         field = scene.dem
@@ -234,6 +258,15 @@ class BoxOutlet(Outlet):
         p = glob2loc(self.node, pos) if self.node is not None else pos
         return _box_contains(self._box(), p), -1
 
+    def _contains_rows(self, P):
+        lo, hi = self._box()
+        L = glob2loc_rows(self.node, P) if self.node is not None else P
+        return np.all(lo[None, :] <= L, axis=1) & np.all(L <= hi[None, :], axis=1), L
+
+    def inside_rows(self, P, V):
+        inside, _ = self._contains_rows(P)
+        return inside, np.full(len(P), -1, np.int64)
+
 
 class StackedBoxOutlet(BoxOutlet):
     """StackedBoxOutlet (Outlet.hpp:77-90, Outlet.cpp:206-224): a BoxOutlet whose box is cut along axis at
@@ -256,6 +289,11 @@ class StackedBoxOutlet(BoxOutlet):
         loc = int(np.searchsorted(np.asarray(self.divs, np.float64), p[self.axis], side="right"))
         return True, loc + self.loc0
 
+    def inside_rows(self, P, V):
+        inside, L = self._contains_rows(P)
+        loc = np.searchsorted(np.asarray(self.divs, np.float64), L[:, self.axis], side="right") + self.loc0
+        return inside, np.where(inside, loc, -1).astype(np.int64)
+
 
 class CrazyOutlet(Outlet):
     """CrazyOutlet (Outlet.hpp:65-73, Outlet.cpp:253-259): a point is 'inside' while its node's speed is at
@@ -263,5 +301,8 @@ class CrazyOutlet(Outlet):
     _defaults = dict(limVelNorm=1000.0)
 
     def isInside(self, pos, vel):
-        v = np.asarray(vel, np.float64)
-        return bool(float(v @ v) <= self.limVelNorm * self.limVelNorm), -1
+        v = np.asarray(vel, np.float64).reshape(1, 3)
+        return bool(sqnorm_rows(v)[0] <= self.limVelNorm * self.limVelNorm), -1
+
+    def inside_rows(self, P, V):
+        return sqnorm_rows(V) <= self.limVelNorm * self.limVelNorm, np.full(len(P), -1, np.int64)
