@@ -114,6 +114,9 @@ class Scene:
         self._gpu = None
         self._host = []
         self._host_energy = {}
+        self.stopAtStep = 0
+        self.stopAtTime = float("nan")
+        self.stopAtHook = ""
         self.periodic = False
         self.cell = Cell()
         self.engines = list(engines or [])
@@ -185,14 +188,55 @@ class Scene:
                 raise RuntimeError("Failed to obtain meaningful dt from engines and fields automatically.")
             self.dt = self.dtSafety * dt
 
-    def run(self, nSteps=1, wait=True):
-        """Run nSteps steps (wait is accepted for compatibility).  The GPU runs the steps back to back,
-        stopping after the contact pass of each step at which a host engine (an outlet) is due: that
-        engine then runs with step, time, dt and cell.gradV as Scene::doOneStep has them while its
-        engines run (before the epilogue, src/core/Scene.cpp:428-432)."""
-        if nSteps <= 0:
+    def run(self, steps=-1, wait=True, time=float("nan"), nSteps=None):
+        """Scene.run(steps, wait, time) (src/core/Scene.cpp): `steps` > 0 sets stopAtStep = step + steps,
+        `time` sets stopAtTime = time + `time`; the run ends at stopAtStep, or after the first step that
+        brings Scene.time to stopAtTime.  The GPU engine runs synchronously, so `wait` changes nothing,
+        and a run without a stop condition is an error instead of a loop without end.  steps=0 returns
+        at once."""
+        if nSteps is not None:
+            steps = nSteps
+        if steps == 0:
             return
+        if steps is not None and steps > 0:
+            self.stopAtStep = self.step + int(steps)
+        if not math.isnan(time):
+            self.stopAtTime = self.time + time
+        if self.stopAtHook:
+            raise RuntimeError("Scene.stopAtHook (a Python string run by Woo) is not supported")
+        by_step = self.stopAtStep > self.step
+        by_time = not math.isnan(self.stopAtTime) and self.time < self.stopAtTime
+        if not by_step and not by_time:
+            raise RuntimeError("Scene.run: nothing to run until (give steps or time, or set stopAtStep / stopAtTime "
+                               "beyond the current step and time)")
         self._prepare_dt()
+        while True:
+            k = self.stopAtStep - self.step if by_step else None
+            if by_time:
+                est = int((self.stopAtTime - self.time) / self.dt) - 2
+                kt = max(est, 1)
+                dyn = [e for e in self._engines if isinstance(e, dem.DynDt) and e.stepPeriod > 0]
+                if dyn and est > 1:
+                    # a new dt takes effect after a DynDt step: keep it constant within the chunk
+                    per = int(dyn[0].stepPeriod)
+                    kt = min(kt, (-(-self.step // per) * per) - self.step + 1)
+                k = kt if k is None else min(k, kt)
+            self._run_steps(max(int(k), 1))
+            if by_step and self.step >= self.stopAtStep:
+                break
+            if by_time and self.time >= self.stopAtTime:
+                break
+
+    def _run_steps(self, nSteps):
+        """nSteps steps: the GPU runs them back to back, stopping after the contact pass of each step at
+        which a host engine (an outlet, an inlet) is due; that engine then runs with step, time, dt and
+        cell.gradV as Scene::doOneStep has them while its engines run (before the epilogue,
+        src/core/Scene.cpp:428-432).  Without engines only step and time advance."""
+        if not self._engines and self._gpu is None:
+            for _ in range(int(nSteps)):
+                self.step += 1
+                self.time += self.dt
+            return
         eng = self._engine()
         end = self.step + int(nSteps)
         while self.step < end:
