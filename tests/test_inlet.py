@@ -210,3 +210,16 @@ def test_sphere_pack_grid_matches_brute_force():
             allC.append(c)
             allR.append(r)
     assert 100 < hits < 2900
+
+
+def test_generator_psd(monkeypatch):
+    S, m = bin_scene(gravity=(0, 0, 0))
+    ii = inlet(m, massRate=0, maxAttempts=300, seed=2, box=((-0.02, -0.02, 0.1), (0.02, 0.02, 0.14)))
+    S.engines = S.engines + [ii]
+    run_on_oracle(monkeypatch, S, 1)
+    d, f = ii.generator.psd(num=10)
+    assert len(d) == 10 and f[-1] == pytest.approx(1.0) and all(a <= b for a, b in zip(f, f[1:]))
+    dm = ii.generator.diamMass()
+    assert min(d) == pytest.approx(min(dm[0])) and max(d) == pytest.approx(max(dm[0]))
+    _, cnt = ii.generator.psd(mass=False, normalize=False, cumulative=True, num=10)
+    assert cnt[-1] == ii.num

@@ -271,3 +271,36 @@ def test_row_tests_match_point_tests():
     # the wrapped point is the original one shifted by whole cell vectors
     k = np.linalg.solve(cell.hSize, (P * 3 - W).T).T
     assert np.allclose(k, np.round(k), atol=1e-9)
+
+
+def test_psd_known_answer():
+    """DemFuncs::psd on four diameters: bins 1 + int(3*(d-1)/3) -> 1, 2, 3, 3."""
+    from woo_gb300.outlet import psd
+    items = [(1., 1., 0.), (2., 1., 0.), (3., 1., 0.), (4., 1., 0.)]
+    rows = psd(items, True, True, 4, (math.nan, math.nan), lambda it, i: it[0], lambda it, i: it[1])
+    assert rows == [[1., 0.], [2., .25], [3., .5], [4., 1.]]
+    rows = psd(items, False, False, 4, (math.nan, math.nan), lambda it, i: it[0], lambda it, i: it[1])
+    assert [r[1] for r in rows] == [0., 1., 1., 2.]
+    # above the given range: counted in the total only
+    rows = psd(items, False, True, 3, (1., 3.), lambda it, i: it[0], lambda it, i: it[1])
+    assert [r[1] for r in rows] == [0., .25, .5]
+    with pytest.raises(RuntimeError, match="no spherical"):
+        psd([], True, True, 4, (math.nan, math.nan), lambda it, i: it[0], lambda it, i: it[1])
+    assert psd([], True, True, 4, (math.nan, math.nan), None, None, emptyOk=True) == [[0., 0.], [0., 0.]]
+
+
+def test_outlet_psd_filters(monkeypatch):
+    out = dem.StackedBoxOutlet(box=((-1, -1, -10), (1, 1, -0.05)), divs=(-0.3,), axis=2, inside=True,
+                               stepPeriod=10, save=True)
+    S = funnel(engines=[out])
+    run_on_oracle(monkeypatch, S, 1300)
+    d, f = out.psd()
+    assert len(d) == 80 and f[-1] == pytest.approx(1.0)
+    kw = dict(cumulative=False, normalize=False, dRange=(0.015, 0.025), num=5)
+    by_loc = [out.psd(locs=[k], **kw)[1] for k in (0, 1)]
+    total = out.psd(**kw)[1]
+    assert np.allclose(np.add(by_loc[0], by_loc[1]), total)
+    assert sum(total) == pytest.approx(out.mass) and set(out.locs) <= {0, 1}
+    assert out.psd(locs=[0], emptyOk=True, **kw)[1] == by_loc[0]
+    with pytest.raises(RuntimeError, match="save"):
+        dem.BoxOutlet().psd()

@@ -50,7 +50,20 @@ class ParticleGenerator(dem._Attrs):
         return (np.array([d for d, _, _ in self.genDiamMassTime]), np.array([m for _, m, _ in self.genDiamMassTime]))
 
     def massOfDiam(self, min=0, max=math.inf):
-        return sum(m for d, m, _ in self.genDiamMassTime if min <= d <= max)
+        ret = 0.
+        for d, m, _ in self.genDiamMassTime:
+            if d >= min and d <= max:
+                ret += m
+        return ret
+
+    def psd(self, mass=True, cumulative=True, normalize=True, dRange=(nan, nan), tRange=(nan, nan), num=80):
+        """ParticleGenerator.psd (Inlet.cpp:165-173): size distribution of the generated particles."""
+        from .outlet import psd, _seq_to_py, _t_ok
+        if not self.save:
+            raise RuntimeError("ParticleGenerator.save must be True for calling ParticleGenerator.psd()")
+        rows = psd(self.genDiamMassTime, cumulative, normalize, int(num), dRange,
+                   lambda dmt, i: dmt[0] if _t_ok(tRange, dmt[2]) else nan, lambda dmt, i: dmt[1] if mass else 1.)
+        return _seq_to_py(rows, False)
 
 
 class MinMaxSphereGenerator(ParticleGenerator):

@@ -8,7 +8,7 @@ Deleting a particle removes its contacts and leaves its id empty; the other part
 and their contact history (DemField::removeParticle, src/dem/Particle.cpp:483-530).
 
 Uninodal particles only (no clumps).  StackedBoxOutlet and CrazyOutlet are provided besides
-BoxOutlet; Outlet.psd is not.
+BoxOutlet.
 """
 import math
 
@@ -101,6 +101,61 @@ def kinetic_energy(mass, inertia, pos, vel, angVel, ori, dt, cell=None):
     fa = cell.pprevFluctAngVel(angVel) if cell is not None else np.asarray(angVel, np.float64)
     erot = .5 * float(fa @ ((T.T @ np.diag(inertia) @ T) @ fa))
     return etrans + erot
+
+
+def psd(items, cumulative, normalize, num, dRange, diameter, weight, emptyOk=False):
+    """DemFuncs::psd (src/dem/Funcs.hpp:61-102): `num` points (diameter, weight in the bins up to it).
+    Without a valid dRange it spans the diameters given.  Items with a NaN diameter or weight, or zero
+    weight, are left out; items above the range count in the total weight only.  An item goes to bin
+    1 + int((num-1)*(d-d0)/(d1-d0)), clamped to [0, num-1]."""
+    d0, d1 = (float(x) for x in dRange)
+    if math.isnan(d0) or math.isnan(d1) or d0 < 0 or d1 <= 0 or d0 >= d1:
+        d0, d1 = math.inf, -math.inf
+        for n, it in enumerate(items):
+            d = diameter(it, n)
+            if d < d0:
+                d0 = d
+            if d > d1:
+                d1 = d
+        if math.isinf(d0):
+            if not emptyOk:
+                raise RuntimeError("DemFuncs::psd: no spherical particles?")
+            return [[0., 0.], [0., 0.]]
+    ret = [[0., 0.] for _ in range(num)]
+    total = 0.
+    for n, it in enumerate(items):
+        d, w = diameter(it, n), weight(it, n)
+        if math.isnan(d) or math.isnan(w) or w == 0.:
+            continue
+        total += w
+        if d > d1:
+            continue
+        x = (num - 1) * _fdiv(d - d0, d1 - d0)
+        # all diameters equal: 0/0; the reference casts the NaN to int, which x86 turns into INT_MIN,
+        # so the item lands in bin 0
+        b = 0 if math.isnan(x) else max(0, min(num - 1, 1 + int(x)))
+        ret[b][1] += w
+    for i in range(num):
+        ret[i][0] = d0 + _fdiv(i * (d1 - d0), num - 1)
+    if normalize:
+        for i in range(num):
+            ret[i][1] = _fdiv(ret[i][1], total)
+    if cumulative:
+        for i in range(1, num):
+            ret[i][1] += ret[i - 1][1]
+    return ret
+
+
+def _seq_to_py(rows, zipped):
+    """DemFuncs::seqVectorToPy: a tuple of per-component lists, or a list of rows when zipped."""
+    if zipped:
+        return [tuple(r) for r in rows]
+    return tuple(list(c) for c in zip(*rows)) if rows else ()
+
+
+def _t_ok(tRange, t):
+    t0, t1 = (float(x) for x in tRange)
+    return math.isnan(t0) or math.isnan(t1) or (t0 <= t < t1)
 
 
 class Outlet(dem.PeriodicEngine):
@@ -229,6 +284,22 @@ class Outlet(dem.PeriodicEngine):
             if d >= min and d <= max:
                 ret += m
         return ret
+
+    def psd(self, mass=True, cumulative=True, normalize=True, num=80, dRange=(nan, nan), tRange=(nan, nan),
+            zip=False, emptyOk=False, locs=()):
+        """Outlet.psd (Outlet.cpp:132-148): size distribution of the deleted particles, by mass or count,
+        within the time range tRange and, when locs is given, from those locations only."""
+        if not self.save:
+            raise RuntimeError("Outlet.psd(): Outlet.save must be True.")
+        want = set(int(x) for x in locs)
+
+        def diameter(dmt, i):
+            ok = _t_ok(tRange, dmt[2]) and (not want or (i < len(self.locs) and self.locs[i] in want))
+            return dmt[0] if ok else nan
+
+        rows = psd(self._diamMassTime, cumulative, normalize, int(num), dRange, diameter,
+                   lambda dmt, i: dmt[1] if mass else 1., emptyOk=emptyOk)
+        return _seq_to_py(rows, zip)
 
 
 def _equiv_radius(shape):
