@@ -223,3 +223,74 @@ def test_generator_psd(monkeypatch):
     assert min(d) == pytest.approx(min(dm[0])) and max(d) == pytest.approx(max(dm[0]))
     _, cnt = ii.generator.psd(mass=False, normalize=False, cumulative=True, num=10)
     assert cnt[-1] == ii.num
+
+
+def test_angle_inside_cases():
+    from woo_gb300.outlet import angle_inside
+    assert angle_inside(0.1, 0., 1.) and not angle_inside(-0.1, 0., 1.)
+    assert angle_inside(0., 1.5 * math.pi, 0.5 * math.pi)      # interval across 0 (a > b)
+    assert not angle_inside(math.pi, 1.5 * math.pi, 0.5 * math.pi)
+    assert angle_inside(123., 0., 2 * math.pi)                   # the whole circle
+    assert angle_inside(0.3 + 2 * math.pi, 0., 1.)               # phi wraps
+
+
+def _node(pos, angle):
+    return dem.Node(pos=pos, ori=(math.cos(angle / 2), 0, 0, math.sin(angle / 2)))
+
+
+def test_cylinder_and_arc_inlets_place_inside(monkeypatch):
+    from woo_gb300.outlet import cart2cyl, glob2loc
+    m = dem.FrictMat(density=2500, young=1e7)
+    gen = lambda: dem.MinMaxSphereGenerator(dRange=(0.006, 0.01))
+    cyl = dem.CylinderInlet(node=_node((0.3, 0.1, 0.5), 0.7), height=0.1, radius=0.04, massRate=0, maxAttempts=200,
+                            materials=[m], generator=gen(), seed=1)
+    arc = dem.ArcInlet(node=_node((-0.3, 0.0, 0.5), 0.2), cylBox=((0.05, 0.3, 0.0), (0.12, 1.8, 0.05)), massRate=0,
+                       maxAttempts=200, materials=[m], generator=gen(), seed=2)
+    box2 = dem.BoxInlet2d(box=((-0.05, -0.05, 0.8), (0.05, 0.05, 0.805)), axis=2, massRate=0, maxAttempts=200,
+                          materials=[m], generator=gen(), seed=3)
+    S, _ = bin_scene(gravity=(0, 0, 0))
+    S.engines = S.engines + [cyl, arc, box2]
+    run_on_oracle(monkeypatch, S, 1)
+    assert cyl.num > 5 and arc.num > 5 and box2.num > 3
+    ids = {k: list(v._inserted) for k, v in (("cyl", cyl), ("arc", arc), ("box2", box2))}
+    for i in ids["cyl"]:
+        p, r = S.dem.par[i].pos, S.dem.par[i].shape.radius
+        for c in _box_corners(p, r):
+            q = glob2loc(cyl.node, c)
+            assert 0 <= q[0] <= 0.1 and q[1] ** 2 + q[2] ** 2 <= 0.04 ** 2
+    for i in ids["arc"]:
+        p, r = S.dem.par[i].pos, S.dem.par[i].shape.radius
+        for c in _box_corners(p, r):
+            q = cart2cyl(glob2loc(arc.node, c))
+            assert 0.05 <= q[0] <= 0.12 and 0.3 <= q[1] <= 1.8 and 0 <= q[2] <= 0.05
+    sticks_out = False
+    for i in ids["box2"]:
+        p, r = S.dem.par[i].pos, S.dem.par[i].shape.radius
+        assert -0.05 <= p[0] - r and p[0] + r <= 0.05 and -0.05 <= p[1] - r and p[1] + r <= 0.05
+        sticks_out |= p[2] + r > 0.805 or p[2] - r < 0.8
+    assert sticks_out                                             # along the axis the box is not enforced
+    allnew = ids["cyl"] + ids["arc"] + ids["box2"]
+    assert _no_overlap(S, allnew)
+
+
+def _box_corners(p, r):
+    return [p + r * np.array([sx, sy, sz]) for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]
+
+
+def test_arc_outlet(monkeypatch):
+    from woo_gb300.outlet import cart2cyl, glob2loc
+    node = _node((0.0, 0.0, 0.0), 0.0)
+    out = dem.ArcOutlet(node=node, cylBox=((0.0, -0.6, -1.0), (0.04, 0.6, 0.07)), inside=True, stepPeriod=1000)
+    S, m = bin_scene(n_pre=25, gravity=(0, 0, 0))
+    S.engines = S.engines + [out]
+    before = {p.id: p.pos for p in S.dem.par if isinstance(p.shape, dem.Sphere)}
+    run_on_oracle(monkeypatch, S, 1)
+    gone = {i for i in before if not S.dem.par.exists(i)}
+    expect = set()
+    for i, p in before.items():
+        q = cart2cyl(glob2loc(node, p))
+        if q[0] <= 0.04 and -0.6 <= q[1] <= 0.6 and -1 <= q[2] <= 0.07:
+            expect.add(i)
+    assert gone == expect and 0 < len(gone) < 25
+    with pytest.raises(RuntimeError, match="node"):
+        dem.ArcOutlet(cylBox=((0, 0, 0), (1, 1, 1)))

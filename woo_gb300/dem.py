@@ -1268,6 +1268,6 @@ class GpuDemEngine(Engine):
         return self._h.kernel_times() if self._h else {}
 
 
-from .outlet import Outlet, BoxOutlet, StackedBoxOutlet, CrazyOutlet  # noqa: E402  (they derive from PeriodicEngine)
-from .inlet import (Inlet, RandomInlet, BoxInlet, ParticleGenerator, MinMaxSphereGenerator,  # noqa: E402
-                    AlignedMinMaxShooter)
+from .outlet import Outlet, BoxOutlet, StackedBoxOutlet, ArcOutlet, CrazyOutlet  # noqa: E402
+from .inlet import (Inlet, RandomInlet, BoxInlet, BoxInlet2d, CylinderInlet, ArcInlet,  # noqa: E402
+                    ParticleGenerator, MinMaxSphereGenerator, AlignedMinMaxShooter)

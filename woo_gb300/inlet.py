@@ -14,9 +14,10 @@ RandomInlet::run (Inlet.cpp:228-515) for a spheres-only generator:
   every maxAttempts/attemptPar attempts; atMaxAttempts decides what a failure does;
 - maxMass / maxNum end the inlet (dead, currRate zeroed when zeroRateAtStop).
 
-Random numbers come from a numpy generator seeded by `seed` (Woo draws from the C library's rand(),
-so its placements cannot be reproduced anyway).  Not provided: clump generators, PsdSphereGenerator,
-spatial biases, periodic cells, doneHook strings.
+Inlet volumes: BoxInlet, BoxInlet2d, CylinderInlet, ArcInlet.  Random numbers come from a numpy
+generator seeded by `seed` (Woo draws from the C library's rand(), so its placements cannot be
+reproduced anyway).  Not provided: clump generators, PsdSphereGenerator, spatial biases, periodic
+cells, doneHook strings.
 """
 import math
 
@@ -399,3 +400,85 @@ class BoxInlet(RandomInlet):
 
     def validateBox(self, b):
         return _box_contains_box(self._lohi(), b)
+
+
+def _loc2glob(node, p):
+    from .outlet import rotation_matrix
+    return rotation_matrix(node.ori) @ np.asarray(p, np.float64) + np.asarray(node.pos, np.float64)
+
+
+def _corners(b):
+    lo, hi = b
+    return [np.array([(hi if i & 1 else lo)[0], (hi if i & 2 else lo)[1], (hi if i & 4 else lo)[2]]) for i in range(8)]
+
+
+class BoxInlet2d(BoxInlet):
+    """BoxInlet2d (Inlet.hpp:290-298): a particle's box must lie in the inlet's box in the plane normal
+    to `axis` only (it may stick out along the axis)."""
+    _defaults = dict(axis=2)
+
+    def validateBox(self, b):
+        a1, a2 = (self.axis + 1) % 3, (self.axis + 2) % 3
+        (lo, hi), (blo, bhi) = self._lohi(), b
+        return bool(lo[a1] <= blo[a1] and lo[a2] <= blo[a2] and bhi[a1] <= hi[a1] and bhi[a2] <= hi[a2])
+
+
+class CylinderInlet(RandomInlet):
+    """CylinderInlet (Inlet.hpp:271-288, Inlet.cpp:564-590): a cylinder of `radius` along the local x-axis
+    of node, x from 0 to `height`; positions uniform in it (shrunk by padDist), every corner of a
+    particle's box inside."""
+    _defaults = dict(node=None, height=nan, radius=nan)
+
+    def _check(self):
+        super()._check()
+        if self.node is None:
+            raise RuntimeError("CylinderInlet.node==None.")
+
+    def randomPosition(self, diam, padDist):
+        if padDist > self.radius:
+            raise RuntimeError(f"CylinderInlet.randomPosition: padDist={padDist} > radius={self.radius}")
+        r3 = [self._rng.random() for _ in range(3)]
+        t = 2 * math.pi * r3[0]
+        u = 2 * r3[1]
+        r = 2. - u if u > 1. else u
+        h = r3[2] * (self.height - 2 * padDist) + padDist
+        return _loc2glob(self.node, [h, (self.radius - padDist) * r * math.cos(t), (self.radius - padDist) * r * math.sin(t)])
+
+    def validateBox(self, b):
+        from .outlet import glob2loc
+        for c in _corners(b):
+            p = glob2loc(self.node, c)
+            if p[0] < 0. or p[0] > self.height:
+                return False
+            if p[1] * p[1] + p[2] * p[2] > self.radius * self.radius:
+                return False
+        return True
+
+
+class ArcInlet(RandomInlet):
+    """ArcInlet (Inlet.hpp:300-315, Inlet.cpp:593-612): positions uniform (in cartesian space) in a box
+    of cylindrical coordinates of node's frame, padded by padDist (padDist/rho0 in the angle); every
+    corner of a particle's box inside."""
+    _defaults = dict(node=None, cylBox=((0., 0., 0.), (0., 0., 0.)))
+
+    def _check(self):
+        super()._check()
+        if self.node is None:
+            raise RuntimeError("ArcInlet.node: must not be None.")
+        lo, hi = self.cylBox
+        if lo[0] < 0 or hi[0] < 0:
+            raise RuntimeError(f"ArcInlet.cylBox: radius bounds (x-component) must be non-negative (not {lo[0]}..{hi[0]}).")
+
+    def randomPosition(self, diam, padDist):
+        from .outlet import cyl2cart
+        lo, hi = (np.asarray(x, np.float64) for x in self.cylBox)
+        pad = np.array([padDist, padDist / lo[0], padDist])
+        lo, hi = lo + pad, hi - pad
+        rx, ry, rz = (self._rng.random() for _ in range(3))
+        # CompUtils::cylCoordBox_sample_cylindrical (CompUtils.cpp:134-143)
+        r = math.sqrt(lo[0] * lo[0] + rx * (hi[0] * hi[0] - lo[0] * lo[0]))
+        return _loc2glob(self.node, cyl2cart([r, lo[1] + ry * (hi[1] - lo[1]), lo[2] + rz * (hi[2] - lo[2])]))
+
+    def validateBox(self, b):
+        from .outlet import cyl_box_contains, glob2loc
+        return all(cyl_box_contains(self.cylBox, glob2loc(self.node, c)) for c in _corners(b))

@@ -7,8 +7,8 @@ with Scene.step, Scene.time, Scene.dt and Cell.gradV as the engines of that step
 Deleting a particle removes its contacts and leaves its id empty; the other particles keep their ids
 and their contact history (DemField::removeParticle, src/dem/Particle.cpp:483-530).
 
-Uninodal particles only (no clumps).  StackedBoxOutlet and CrazyOutlet are provided besides
-BoxOutlet.
+Uninodal particles only (no clumps).  BoxOutlet, StackedBoxOutlet, ArcOutlet and CrazyOutlet are
+provided.
 """
 import math
 
@@ -377,3 +377,50 @@ class CrazyOutlet(Outlet):
 
     def inside_rows(self, P, V):
         return sqnorm_rows(V) <= self.limVelNorm * self.limVelNorm, np.full(len(P), -1, np.int64)
+
+
+def cart2cyl(p):
+    """CompUtils::cart2cyl (src/supp/base/CompUtils.cpp:115-117): (rho, phi, z)."""
+    return np.array([math.sqrt(p[0] * p[0] + p[1] * p[1]), math.atan2(p[1], p[0]), p[2]])
+
+
+def cyl2cart(c):
+    """CompUtils::cyl2cart (CompUtils.cpp:120-122)."""
+    return np.array([c[0] * math.cos(c[1]), c[0] * math.sin(c[1]), c[2]])
+
+
+def angle_inside(phi, a, b):
+    """CompUtils::angleInside (CompUtils.cpp:124-132): phi within the angle interval (a, b)."""
+    if abs(a - b) >= 2 * math.pi:
+        return True
+    if a > b:
+        a -= 2 * math.pi
+    if a == b:
+        return math.fmod(a, 2 * math.pi) == math.fmod(phi, 2 * math.pi)
+    x = (phi - a) / (2 * math.pi)
+    pphi = (x - math.floor(x)) * (2 * math.pi)
+    return pphi < (b - a)
+
+
+def cyl_box_contains(box, pt):
+    """CompUtils::cylCoordBox_contains_cartesian (CompUtils.cpp:145-156): pt cartesian, box in
+    cylindrical coordinates ((rho0, phi0, z0), (rho1, phi1, z1))."""
+    (lo, hi), c = box, cart2cyl(pt)
+    return bool(lo[0] <= c[0] <= hi[0] and angle_inside(c[1], lo[1], hi[1]) and lo[2] <= c[2] <= hi[2])
+
+
+class ArcOutlet(Outlet):
+    """ArcOutlet (Outlet.hpp:92-106, Outlet.cpp:226-237): the volume is a prismatic arc, a box in the
+    cylindrical coordinates (rho, phi, z) of node's local frame."""
+    _defaults = dict(node=None, cylBox=((0., 0., 0.), (0., 0., 0.)), glSlices=32)
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        lo, hi = self.cylBox
+        if (lo[0] <= hi[0] and lo[1] <= hi[1] and lo[2] <= hi[2]) and (lo[0] < 0 or hi[0] < 0):
+            raise RuntimeError(f"ArcOutlet.cylBox: radius bounds (x-component) must be non-negative (not {lo[0]}..{hi[0]}).")
+        if self.node is None:
+            raise RuntimeError("ArcOutlet.node: must not be None.")
+
+    def isInside(self, pos, vel):
+        return cyl_box_contains(self.cylBox, glob2loc(self.node, pos)), -1
