@@ -294,3 +294,40 @@ def test_arc_outlet(monkeypatch):
     assert gone == expect and 0 < len(gone) < 25
     with pytest.raises(RuntimeError, match="node"):
         dem.ArcOutlet(cylBox=((0, 0, 0), (1, 1, 1)))
+
+
+def test_psd_generator_follows_the_curve():
+    """Discrete number PSD: the bin choice is deterministic and keeps every bin within one particle of
+    its share (Psd.cpp:58-114); sanitizePsd drops leading zeros and normalizes."""
+    g = dem.PsdSphereGenerator(psdPts=[(0.005, 0), (0.006, 0), (0.01, 20), (0.02, 100)], discrete=True, mass=False)
+    assert g.psdPts == [[0.006, 0.], [0.01, .2], [0.02, 1.]]
+    m = dem.FrictMat(density=2000)
+    rng = np.random.default_rng(0)
+    ds = [g(m, 0., rng)[0] for _ in range(200)]
+    assert ds[0] == pytest.approx(0.01)                  # the first bin with a positive passing value
+    assert set(np.round(ds, 6)) <= {0.01, 0.02}
+    n_small = sum(1 for d in ds if d < 0.015)
+    assert abs(n_small - 0.2 * 200) <= 1
+    # continuous mass PSD: diameters within the curve, mass shares close to it
+    g2 = dem.PsdSphereGenerator(psdPts=[(0.004, 0), (0.008, .5), (0.012, 1.)], mass=True)
+    ds = [g2(m, 0., rng)[0] for _ in range(400)]
+    assert min(ds) >= 0.004 - 1e-12 and max(ds) <= 0.012 + 1e-12
+    masses = np.array([d ** 3 for d in ds])
+    assert abs(masses[np.array(ds) <= 0.008].sum() / masses.sum() - 0.5) < 0.05
+    g2.revokeLast()
+    assert len(g2.genDiamMassTime) == 399
+    with pytest.raises(RuntimeError, match="increasing"):
+        dem.PsdSphereGenerator(psdPts=[(0.01, .5), (0.005, 1.)])
+
+
+def test_inlet_with_psd_generator(monkeypatch):
+    S, m = bin_scene(gravity=(0, 0, 0))
+    ii = dem.BoxInlet(box=((-0.05, -0.05, 0.1), (0.05, 0.05, 0.2)), stepPeriod=100, massRate=0, maxAttempts=500,
+                      materials=[m], generator=dem.PsdSphereGenerator(psdPts=[(0.006, 0), (0.012, 1.)]), seed=5)
+    S.engines = S.engines + [ii]
+    run_on_oracle(monkeypatch, S, 1)
+    assert ii.num > 20
+    new = list(range(5, len(S.dem.par)))
+    assert _no_overlap(S, new)
+    r = np.array([S.dem.par[i].shape.radius for i in new])
+    assert r.min() >= 0.003 - 1e-12 and r.max() <= 0.006 + 1e-12

@@ -1270,4 +1270,4 @@ class GpuDemEngine(Engine):
 
 from .outlet import Outlet, BoxOutlet, StackedBoxOutlet, ArcOutlet, CrazyOutlet  # noqa: E402
 from .inlet import (Inlet, RandomInlet, BoxInlet, BoxInlet2d, CylinderInlet, ArcInlet,  # noqa: E402
-                    ParticleGenerator, MinMaxSphereGenerator, AlignedMinMaxShooter)
+                    ParticleGenerator, MinMaxSphereGenerator, PsdSphereGenerator, AlignedMinMaxShooter)

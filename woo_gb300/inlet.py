@@ -16,8 +16,8 @@ RandomInlet::run (Inlet.cpp:228-515) for a spheres-only generator:
 
 Inlet volumes: BoxInlet, BoxInlet2d, CylinderInlet, ArcInlet.  Random numbers come from a numpy
 generator seeded by `seed` (Woo draws from the C library's rand(), so its placements cannot be
-reproduced anyway).  Not provided: clump generators, PsdSphereGenerator, spatial biases, periodic
-cells, doneHook strings.
+reproduced anyway).  Generators: MinMaxSphereGenerator, PsdSphereGenerator.  Not provided: clump
+generators, spatial biases, periodic cells, doneHook strings.
 """
 import math
 
@@ -90,6 +90,121 @@ class MinMaxSphereGenerator(ParticleGenerator):
             raise RuntimeError("MinMaxSphereGenerator: dRange[0]>dRange[1], or they are NaN!")
         r = .5 * (d0 + rng.random() * (d1 - d0))
         p = dem.Sphere.make((0, 0, 0), r, mat=mat)
+        if self.save:
+            self.genDiamMassTime.append((2 * r, p.mass, time))
+        return 2 * r, [(p, (np.array([-r, -r, -r]), np.array([r, r, r])))]
+
+
+def sanitize_psd(pts, src):
+    """PsdSphereGenerator::sanitizePsd (src/dem/Psd.cpp:23-44): checks, leading zero points and trailing
+    repeated maxima dropped, passing values normalized to end at 1."""
+    pts = [[float(d), float(f)] for d, f in pts]
+    if not pts:
+        return pts
+    for i in range(len(pts) - 1):
+        if pts[i][0] < 0 or pts[i][1] < 0:
+            raise RuntimeError(src + ": negative values not allowed.")
+        if pts[i][0] > pts[i + 1][0]:
+            raise RuntimeError(f"{src}: diameters (the x-component) must be increasing ({pts[i][0]}>={pts[i + 1][0]})")
+        if pts[i][1] > pts[i + 1][1]:
+            raise RuntimeError(f"{src}: passing values (the y-component) must be increasing ({pts[i][1]}>{pts[i + 1][1]})")
+    max_pass = pts[-1][1]
+    ii = 0
+    while ii < len(pts) and not pts[ii][1] > 0:
+        ii += 1
+    if ii > 1:
+        pts = pts[ii - 1:]
+    ii = len(pts) - 2
+    while ii >= 0 and not pts[ii][1] < max_pass:
+        ii -= 1
+    if ii < len(pts) - 2:
+        pts = pts[:ii + 2]
+    if not pts:
+        raise RuntimeError(src + ": empty after removing spurious values?")
+    if max_pass != 1.0:
+        for v in pts:
+            v[1] /= max_pass
+    return pts
+
+
+class PsdSphereGenerator(ParticleGenerator):
+    """PsdSphereGenerator (src/dem/Psd.hpp:6-36, Psd.cpp:23-175): spheres following the cumulative PSD
+    psdPts (diameter, passing fraction), by mass or by number.  Each new sphere goes to the PSD point
+    whose bin is furthest below its share; with `discrete` it takes that point's diameter, otherwise a
+    diameter between the previous point and it (inverse-square interpolation for mass PSDs, linear for
+    number PSDs)."""
+    _defaults = dict(discrete=False, psdPts=(), mass=True)
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.psdPts = sanitize_psd(self.psdPts, "PsdSphereGenerator.psdPts")
+        self.weightPerBin = [0.] * len(self.psdPts)
+        self.weightTotal = 0.
+        self._last = None
+
+    def isSpheresOnly(self):
+        return True
+
+    def padDist(self):
+        return self.psdPts[0][0] / 2. if self.psdPts else nan
+
+    def minMaxDiam(self):
+        return (self.psdPts[0][0], self.psdPts[-1][0]) if self.psdPts else (nan, nan)
+
+    def critDt(self, density, young):
+        if not self.psdPts:
+            return math.inf
+        return self.minMaxDiam()[0] / math.sqrt(young / density)
+
+    def clear(self):
+        super().clear()
+        self.weightTotal = 0.
+        self.weightPerBin = [0.] * len(self.psdPts)
+
+    def computeNextRadiusBin(self, rng):
+        """PsdSphereGenerator::computeNextRadiusBin (Psd.cpp:58-114)."""
+        pts = self.psdPts
+        if not pts:
+            raise RuntimeError("PsdSphereGenerator.psdPts is empty.")
+        max_diff, max_bin = -math.inf, -1
+        if self.weightTotal <= 0:
+            max_bin = 0
+            for i in range(len(pts) - 1):
+                if pts[i + 1][1] - pts[i][1] > 0 and pts[i][1] > 0:
+                    max_bin = i
+                    break
+        else:
+            for i in range(len(pts)):
+                desired = pts[i][1] - (pts[i - 1][1] if i > 0 else 0.)
+                diff = desired - self.weightPerBin[i] * 1. / self.weightTotal
+                if diff > max_diff and not (self.discrete and desired == 0.):
+                    max_diff, max_bin = diff, i
+        if self.discrete:
+            r = pts[max_bin][0] / 2.
+        elif max_bin == 0:
+            r = pts[0][0] / 2.
+        else:
+            a, b = pts[max_bin - 1][0] / 2., pts[max_bin][0] / 2.
+            u = rng.random()
+            r = math.sqrt(1 / (1 / (a * a) + u * (1 / (b * b) - 1 / (a * a)))) if self.mass else a + u * (b - a)
+        return r, max_bin
+
+    def revokeLast(self):
+        if self._last is not None:
+            b, w = self._last
+            self.weightPerBin[b] -= w
+            self.weightTotal -= w
+        super().revokeLast()
+
+    def __call__(self, mat, time, rng):
+        if self.mass and not mat.density > 0:
+            raise ValueError(f"PsdSphereGenerator: material density must be positive (not {mat.density})")
+        r, b = self.computeNextRadiusBin(rng)
+        p = dem.Sphere.make((0, 0, 0), r, mat=mat)
+        w = p.mass if self.mass else 1.
+        self.weightPerBin[b] += w
+        self.weightTotal += w
+        self._last = (b, w)
         if self.save:
             self.genDiamMassTime.append((2 * r, p.mass, time))
         return 2 * r, [(p, (np.array([-r, -r, -r]), np.array([r, r, r])))]
