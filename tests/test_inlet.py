@@ -331,3 +331,14 @@ def test_inlet_with_psd_generator(monkeypatch):
     assert _no_overlap(S, new)
     r = np.array([S.dem.par[i].shape.radius for i in new])
     assert r.min() >= 0.003 - 1e-12 and r.max() <= 0.006 + 1e-12
+
+
+def test_placed_particles_stay_when_attempts_run_out(monkeypatch):
+    """atMaxAttempts='error' raises, but what was placed before in that run stays (Inlet.cpp:313, 495)."""
+    S, m = bin_scene(gravity=(0, 0, 0))
+    ii = inlet(m, massRate=50.0, maxAttempts=40, seed=2, box=((-0.02, -0.02, 0.1), (0.02, 0.02, 0.13)))
+    S.engines = S.engines + [ii]
+    n0 = len(S.dem.par)
+    with pytest.raises(RuntimeError, match="maxAttempts reached"):
+        run_on_oracle(monkeypatch, S, 101)
+    assert ii.num > 0 and len(S.dem.par) == n0 + ii.num

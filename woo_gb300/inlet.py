@@ -410,6 +410,10 @@ class RandomInlet(Inlet):
                     if self.massRate <= 0:
                         break
                     if atMax == 0:
+                        # the particles placed before are in the scene already (Woo inserts each at once)
+                        if new:
+                            field.par.add(new, nodes=1)
+                            self._inserted.extend(p.id for p in new)
                         raise RuntimeError(f"RandomInlet.maxAttempts reached ({self.maxAttempts})")
                     if atMax == 1:
                         self.dead = True
