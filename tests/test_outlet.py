@@ -304,3 +304,52 @@ def test_outlet_psd_filters(monkeypatch):
     assert out.psd(locs=[0], emptyOk=True, **kw)[1] == by_loc[0]
     with pytest.raises(RuntimeError, match="save"):
         dem.BoxOutlet().psd()
+
+
+def test_periodic_outlet_canonical_positions_and_fluctuation_energy(monkeypatch):
+    """A sheared periodic cell: the outlet tests canonicalized positions (Outlet.cpp:20-24) and books
+    kinOutlet from the fluctuation velocities with the step's own gradV (Particle.cpp:247-265)."""
+    from woo_gb300 import utils
+
+    class Snap(dem.PeriodicEngine):
+        def run(self, scene):
+            f = scene.dem
+            if f._stale:
+                f._engine._download_particles(f)
+            self.states.append((scene.step, f._arrays.copy(), scene.cell.hSize, scene.cell.gradV, scene.dt,
+                                [p.id for p in f.par]))
+
+    rng = np.random.default_rng(5)
+    m = dem.FrictMat(density=1e3, young=1e6, ktDivKn=.2, tanPhi=.4)
+    snap = Snap(stepPeriod=25)
+    snap.states = []
+    out = dem.BoxOutlet(box=((-10, -10, 0.0), (10, 10, 1.2)), inside=True, stepPeriod=25)
+    S = Scene(fields=[dem.DemField(gravity=(0, 0, 0))],
+              engines=utils.defaultEngines(damping=.2, dynDtPeriod=0) + [snap, out], dtSafety=.5, trackEnergy=True)
+    S.periodic = True
+    S.cell.setBox(4, 4, 4)
+    S.cell.nextGradV = np.array([[0, 0, 0.2], [0, 0, 0], [0, 0, 0]])
+    for ix in range(4):
+        for iy in range(4):
+            for iz in range(4):
+                c = np.array([ix, iy, iz]) + .5 + rng.uniform(-.05, .05, 3)
+                S.dem.par.add(utils.sphere(c, .45, mat=m, vel=rng.normal(0, .3, 3)))
+    run_on_oracle(monkeypatch, S, 101)
+    assert out.nDone == 5 and out.num > 10
+    expect_gone, expect_ek = [], 0.0
+    alive = set(range(64))
+    for step, st, hsize, gradv, dt, live in snap.states:
+        for i in sorted(set(live) & alive):
+            frac = np.linalg.solve(hsize, st.pos[i])
+            z = (hsize @ (frac - np.floor(frac)))[2]
+            if 0.0 <= z <= 1.2:
+                expect_gone.append(i)
+                alive.discard(i)
+                v = st.vel[i] - gradv @ (st.pos[i] - dt / 2 * st.vel[i])
+                W = .5 * (gradv - gradv.T)
+                spin = .5 * np.array([W[1, 2] - W[2, 1], W[2, 0] - W[0, 2], W[0, 1] - W[1, 0]])
+                w = st.angVel[i] - spin
+                expect_ek += .5 * st.mass[i] * float(v @ v) + .5 * float(w @ (st.inertia[i] * w))
+    assert sorted(expect_gone) == sorted(i for i in range(64) if not S.dem.par.exists(i))
+    assert S.energy["kinOutlet"] == pytest.approx(expect_ek, rel=1e-10)
+    assert any(np.any(g != 0) for _, _, _, g, _, _ in snap.states)   # the shear was on while the outlet ran
