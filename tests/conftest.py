@@ -10,6 +10,7 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libwdem.so")
+    config.addinivalue_line("markers", "host_engines: scripts with outlets/inlets (host engines between GPU steps)")
 
 
 def _has_gpu():
@@ -23,7 +24,17 @@ def _has_gpu():
 HAS_GPU = _has_gpu()
 
 
+def _order(item):
+    # the kernel parity tests first, then the scripts with host engines (outlets, inlets), so that a
+    # failure there under -x does not hide the kernel results; test_zz_* stay last
+    mod = getattr(item, "module", None)
+    if mod is not None and mod.__name__.startswith("test_zz"):
+        return 2
+    return 1 if "host_engines" in item.keywords else 0
+
+
 def pytest_collection_modifyitems(config, items):
+    items.sort(key=_order)
     if HAS_GPU:
         return
     skip = pytest.mark.skip(reason="no CUDA device")

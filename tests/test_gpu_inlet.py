@@ -10,7 +10,7 @@ from oracle_handle import run_on_oracle
 from test_gpu_outlet import _compare
 from test_inlet import bin_scene, inlet
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.host_engines]
 
 
 def _pair(**kw):

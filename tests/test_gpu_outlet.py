@@ -8,7 +8,7 @@ from woo_gb300 import dem
 from oracle_handle import run_on_oracle
 from test_outlet import funnel
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.host_engines]
 
 
 def _compare(Sg, So, n0):
