@@ -86,3 +86,12 @@ def test_cell_only_gradv2():
             c.homoDeform = mode
     with pytest.raises(ValueError):
         c.homoDeform = "bogus"
+
+
+def test_utils_ellipsoid():
+    """woo.utils.ellipsoid (py/utils.py:201-211) gives the same particle as Ellipsoid.make."""
+    from woo_gb300 import utils as U
+    a = U.ellipsoid((1, 2, 3), (0.1, 0.2, 0.3), ori=(0, 1, 0, 0), angVel=(0, 0, 2))
+    b = dem.Ellipsoid.make((1, 2, 3), (0.1, 0.2, 0.3), ori=(0, 1, 0, 0))
+    assert a.mass == b.mass and np.array_equal(a.inertia, b.inertia) and np.array_equal(a.ori, b.ori)
+    assert np.array_equal(a.angVel, [0, 0, 2]) and a.mask == dem.DemField.defaultMovableMask

@@ -54,6 +54,16 @@ def sphere(center, radius, mat=None, fixed=False, wire=False, color=None, highli
     return dem.Sphere.make(center, radius, mat=mat, fixed=fixed, mask=mask, vel=vel)
 
 
+def ellipsoid(center, semiAxes, ori=(1, 0, 0, 0), angVel=None, color=None, mat=None, fixed=False, wire=False,
+              visible=True, mask=dem.DEFAULT_MOVABLE_MASK, **kw):
+    """py/utils.py:201-211: an Ellipsoid particle (ori as (w, x, y, z)); angVel sets the node's angular
+    velocity."""
+    p = dem.Ellipsoid.make(center, semiAxes, ori=ori, mat=mat, fixed=fixed, mask=mask)
+    if angVel is not None:
+        p.angVel = angVel
+    return p
+
+
 def wall(position, axis, sense=0, glAB=None, fixed=True, mass=0, color=None, mat=None, visible=True,
          mask=dem.DEFAULT_BOUNDARY_MASK):
     """py/utils.py:245-267."""
