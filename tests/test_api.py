@@ -157,3 +157,26 @@ def test_exec_time_with_timing_enabled(monkeypatch):
         assert e.execCount == 7
     assert S.lab.contactLoop.execTime > 0 and S._gpu.execCount == 7
     assert S._gpu.execTime >= S.lab.contactLoop.execTime
+
+
+def test_unbalanced_force_and_energy(monkeypatch):
+    """DemFuncs::unbalancedForce and utils.unbalancedEnergy on a settling column (on the oracle): the
+    ratio falls as the column comes to rest, and matches the definition recomputed here."""
+    from oracle_handle import run_on_oracle
+    S = small_scene(trackEnergy=True)
+    run_on_oracle(monkeypatch, S, 50)
+    assert math.isnan(S.dem.unbalancedForce())            # no contact yet: 0/0, as in the reference
+    run_on_oracle(monkeypatch, S, 500)
+    u0 = S.dem.unbalancedForce()
+    assert math.isfinite(u0)
+    run_on_oracle(monkeypatch, S, 4000)
+    u1 = S.dem.unbalancedForce()
+    assert u1 < u0
+    F = [np.linalg.norm(p.f) for p in S.dem.par if p.blocked == ""]
+    C = [np.linalg.norm(c.phys.force) for c in S.dem.con]
+    assert u1 == pytest.approx(np.mean(F) / np.mean(C), rel=1e-12)
+    assert S.dem.unbalancedForce(useMaxForce=True) == pytest.approx(max(F) / np.mean(C), rel=1e-12)
+    assert utils.unbalancedForce(S) == u1
+    ue = utils.unbalancedEnergy(S)
+    e = S.energy
+    assert ue == e["kinetic"] / e["elast"]

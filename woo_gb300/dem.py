@@ -631,6 +631,36 @@ class DemField:
     def nodes(self):
         return [p.shape.nodes[0] for p in self.par]
 
+    def unbalancedForce(self, useMaxForce=False):
+        """DemFuncs::unbalancedForce (src/dem/Funcs.cpp:231-258): the mean (or maximum) force norm on the
+        moving nodes with no blocked DOF, over the mean force norm of the contacts.  The reference reads
+        Contact.phys of every contact in the container; here the mean is over the real contacts (the
+        potential ones have no phys)."""
+        if self._engine is not None and self._stale:
+            self._engine._download_particles(self)
+        sumF, maxF, nb = 0., 0., 0
+        for p in self.par:
+            if not getattr(p, "_integrated", True):
+                continue
+            d = p.shape.nodes[0].dem
+            if d.flags & 63 or d.flags & DemData.CLUMP_CLUMPED:
+                continue
+            f = d.force
+            cur = math.sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2])
+            maxF = max(cur, maxF)
+            sumF += cur
+            nb += 1
+        meanF = float(np.float64(sumF) / np.float64(nb)) if nb else float("nan")
+        ca = self._contacts()
+        sumC, nc = 0., 0
+        for i in np.nonzero(ca.real)[0]:
+            f = ca.force[i]
+            sumC += math.sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2])
+            nc += 1
+        with np.errstate(divide="ignore", invalid="ignore"):
+            meanC = np.float64(sumC) / np.float64(nc)
+            return float(np.float64(maxF if useMaxForce else meanF) / meanC)
+
     def critDt(self):
         """DemField::critDt -> DemFuncs::pWaveDt (src/dem/Particle.cpp:399-404, src/dem/Funcs.cpp:151-175)."""
         dt = math.inf

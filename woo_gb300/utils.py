@@ -85,3 +85,18 @@ def wallBox(box, which=(1, 1, 1, 1, 1, 1), **kw):
 def spherePWaveDt(radius, density, young):
     """py/utils.py:77-: r / sqrt(E/rho)."""
     return radius / math.sqrt(young / density)
+
+
+def unbalancedEnergy(S):
+    """py/utils.py:757-763: kinetic over elastic energy (NaN when either is missing or elast is 0)."""
+    if not S.trackEnergy:
+        raise RuntimeError("Scene.trackEnergy==False")
+    e = S.energy
+    if "elast" not in e or "kinetic" not in e or e["elast"] == 0:
+        return float("nan")
+    return e["kinetic"] / e["elast"]
+
+
+def unbalancedForce(S=None, useMaxForce=False, field=None):
+    """DemFuncs::unbalancedForce of the scene's DemField (see DemField.unbalancedForce)."""
+    return (field if field is not None else S.dem).unbalancedForce(useMaxForce)
