@@ -1272,6 +1272,7 @@ class GpuDemEngine(Engine):
         self._h.close()
         h = abi.Handle(cap, device=self.device)
         h.keep_geom(self.keepGeom)
+        self._timing_on = False   # a new handle starts untimed; run() switches it on again if wanted
         ell = getattr(self, "_ellFunctor", None)
         if ell is not None and ell.warmStart == "mlp":
             h.warm_set_weights(ell.warmStartWeights)
