@@ -353,3 +353,16 @@ def test_periodic_outlet_canonical_positions_and_fluctuation_energy(monkeypatch)
     assert sorted(expect_gone) == sorted(i for i in range(64) if not S.dem.par.exists(i))
     assert S.energy["kinOutlet"] == pytest.approx(expect_ek, rel=1e-10)
     assert any(np.any(g != 0) for _, _, _, g, _, _ in snap.states)   # the shear was on while the outlet ran
+
+
+def test_dead_slots_spread_over_live_spheres():
+    S = funnel()
+    S.dem.par.remove(list(range(4, 20)))
+    S._prepare_dt()
+    g = S._engine()
+    g._build_params(S, S.dem)
+    pa = g._pack(S.dem)
+    view = g._device_view(S.dem, pa)
+    parked = {tuple(view.pos[i]) for i in range(4, 20)}
+    live = {tuple(pa.pos[i]) for i in range(20, 31)}
+    assert parked <= live and len(parked) == 11              # 16 dead slots over the 11 live spheres

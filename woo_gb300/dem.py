@@ -1056,11 +1056,11 @@ class GpuDemEngine(Engine):
             up.angVel[ids] = 0
         if dead:
             up.mask[dead] = 0
-            # parked on a live particle, so that a particle removed far outside the domain does not
-            # stretch the collider's grid
-            anchor = next((p.id for p in field.par if isinstance(p.shape, Sphere)), None)
-            if anchor is not None:
-                up.pos[dead] = pa.pos[anchor]
+            # parked on live spheres (spread over them, so that many removed particles do not crowd one
+            # grid cell), so that a particle removed far outside the domain does not stretch the grid
+            anchors = [p.id for p in field.par if isinstance(p.shape, Sphere)]
+            if anchors:
+                up.pos[dead] = pa.pos[np.asarray(anchors)[np.arange(len(dead)) % len(anchors)]]
         return up
 
     def _remove_particles(self, field, ids):
