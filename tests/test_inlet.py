@@ -342,3 +342,39 @@ def test_placed_particles_stay_when_attempts_run_out(monkeypatch):
     with pytest.raises(RuntimeError, match="maxAttempts reached"):
         run_on_oracle(monkeypatch, S, 101)
     assert ii.num > 0 and len(S.dem.par) == n0 + ii.num
+
+
+def test_scene_save_load_continues(monkeypatch, tmp_path):
+    """Scene.save / Scene.load mid-run (with an inlet and an outlet): the loaded scene continues exactly
+    like the original (particles, real contacts with history, host-engine counters, energies)."""
+    def make():
+        S, m = bin_scene(n_pre=20, trackEnergy=True)
+        ii = inlet(m, massRate=1.0, maxNum=25, seed=9, shooter=dem.AlignedMinMaxShooter(dir=(0, 0, -1), vRange=(0.1, 0.3)))
+        out = dem.BoxOutlet(box=((0.03, -1, -1), (1, 1, 1)), inside=True, stepPeriod=70)
+        S.engines = S.engines + [ii, out]
+        return S
+    A = make()
+    run_on_oracle(monkeypatch, A, 801)
+    path = tmp_path / "scene.pkl"
+    A.save(str(path))
+    B = Scene.load(str(path))
+    assert B.step == A.step and B.time == A.time and B._gpu._h is None
+    run_on_oracle(monkeypatch, A, 700)
+    run_on_oracle(monkeypatch, B, 700)
+    assert A.step == B.step == 1501 and A.time == B.time
+    ia, oa = A.engines[-2], A.engines[-1]
+    ib, ob = B.engines[-2], B.engines[-1]
+    assert (ia.num, ia.mass, oa.num, oa.mass) == (ib.num, ib.mass, ob.num, ob.mass)
+    assert ia.num > 0 and oa.num > 0
+    assert [p.id for p in A.dem.par] == [p.id for p in B.dem.par]
+    for p in A.dem.par:
+        q = B.dem.par[p.id]
+        assert np.array_equal(p.pos, q.pos) and np.array_equal(p.vel, q.vel) and np.array_equal(p.angVel, q.angVel)
+    ca, cb = A.dem._contacts(), B.dem._contacts()
+    ra, rb = ca.real.astype(bool), cb.real.astype(bool)
+    assert ra.sum() > 5 and np.array_equal(ca.keys()[ra], cb.keys()[rb])
+    for name in ("force", "trsf", "contPt", "kn", "kt"):
+        assert np.array_equal(getattr(ca, name)[ra], getattr(cb, name)[rb]), name
+    ea, eb = A.energy, B.energy
+    for k in ("grav", "nonviscDamp", "kinInlet"):
+        assert eb[k] == pytest.approx(ea[k], rel=1e-12), k

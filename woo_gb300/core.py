@@ -261,18 +261,49 @@ class Scene:
                 self.dt = new_dt
                 self.cell._gradV = new_gradV
             self.step += 1
-            self.time += eng._ran_time
+            self._advance_time(eng)
 
     def _gpu_steps(self, eng, k):
         eng.run(self, int(k))
         self.step += int(k)
-        self.time += eng._ran_time
+        self._advance_time(eng)
+
+    def _advance_time(self, eng):
+        t = getattr(eng, "_time_after", None)
+        self.time = t if t is not None else self.time + eng._ran_time
 
     def _energy_add(self, name, value):
         """EnergyTracker::add with ZeroDontCreate|IsIncrement, for energies booked on the host."""
         if value == 0.0 and name not in self._host_energy:
             return
         self._host_energy[name] = self._host_energy.get(name, 0.0) + value
+
+    def save(self, path):
+        """Scene.save: the scene as a pickle (format of this package, not Woo's archives): particles with
+        their current state, the contact container with its history, engines and host engines with
+        their counters, the periodic cell, step, time, dt and the energies booked so far.  Loading
+        it (Scene.load) and running continues the motion; the first step runs the collider in full.
+        Not kept: DynDt's device-side schedule (it restarts with its next period) and the cell's
+        previous-step size."""
+        import pickle
+        with open(path, "wb") as f:
+            pickle.dump(self, f, protocol=pickle.HIGHEST_PROTOCOL)
+
+    @staticmethod
+    def load(path):
+        import pickle
+        with open(path, "rb") as f:
+            S = pickle.load(f)
+        if not isinstance(S, Scene):
+            raise TypeError("Loaded object of type " + type(S).__name__ + " is not a Scene")
+        return S
+
+    def __getstate__(self):
+        d = dict(self.__dict__)
+        for fld in self.fields:
+            if getattr(fld, "_engine", None) is not None and fld._stale:
+                fld._engine._download_particles(fld)
+        return d
 
     def one(self):
         self.run(1)

@@ -163,6 +163,17 @@ class Node:
     pos = property(lambda s: s._get("pos"), lambda s, v: s._set("pos", _vec3(v)))
     ori = property(lambda s: s._get("ori"), lambda s, v: s._set("ori", _quat(v)))
 
+    def __getstate__(self):
+        """Pickled with its current state and unbound (a loaded scene uploads it again)."""
+        d = dict(self.__dict__)
+        f = self._field
+        if f is not None and f._arrays is not None and 0 <= self._idx < f._arrays.n:
+            d["_local"] = {k: (getattr(f._arrays, k)[self._idx].copy()
+                               if isinstance(getattr(f._arrays, k)[self._idx], np.ndarray)
+                               else getattr(f._arrays, k)[self._idx].item()) for k in _FIELD_ARRAY_NAMES}
+        d["_field"], d["_idx"] = None, -1
+        return d
+
 
 # ---------------------------------------------------------------------------------------- shapes
 DEFAULT_MOVABLE_MASK = 0b0101
@@ -595,6 +606,19 @@ class DemField:
             self._engine._download_particles(self)
         getattr(self._arrays, name)[idx] = v
         self._dirty.add(name)
+
+    def __getstate__(self):
+        d = dict(self.__dict__)
+        if self._engine is not None:
+            d["_saved_contacts"] = self._engine._download_contacts()
+        for k in ("_engine", "_arrays", "_moving"):
+            d.pop(k, None)
+        d["_stale"], d["_dirty"], d["_dead"], d["_con_cache"] = False, set(), set(), None
+        return d
+
+    def __setstate__(self, d):
+        self.__dict__.update(d)
+        self._engine, self._arrays = None, None
 
     def _set_mask(self, idx, mask):
         self._arrays.mask[idx] = mask
@@ -1094,7 +1118,8 @@ class GpuDemEngine(Engine):
             res = [e._reserve() for e in inlets]
             cap = max(cap, pa.n + (sum(res) if all(r is not None for r in res) else max(pa.n, 1024)))
         self._cap = cap
-        self._energy_base = {}
+        if not hasattr(self, "_energy_base"):
+            self._energy_base = {}
         h = abi.Handle(cap, device=self.device)
         h.keep_geom(self.keepGeom)
         h.set_params(params)
@@ -1108,6 +1133,11 @@ class GpuDemEngine(Engine):
             if ell.warmStartWeights is None:
                 raise RuntimeError("Cg2_Ellipsoid_Ellipsoid_L6Geom.warmStart='mlp' needs warmStartWeights")
             h.warm_set_weights(ell.warmStartWeights)
+        saved = getattr(field, "_saved_contacts", None)
+        if saved is not None:
+            # a loaded scene: its contact container, with the history (the collider then runs in full)
+            h.upload_contacts(saved)
+            field._saved_contacts = None
         self._h, self._params, self._field = h, params, field
         field._bind(self, pa)
 
@@ -1125,7 +1155,11 @@ class GpuDemEngine(Engine):
         self._refresh_from_sources()
         if self._h is None and next(iter(field.par), None) is None:
             # nothing to integrate yet (an inlet fills the field later): only time advances
-            self._ran_time = nSteps * scene.dt
+            t = scene.time
+            for _ in range(int(nSteps)):
+                t += scene.dt
+            self._time_after = t
+            self._ran_time = t - scene.time
             return
         self._ensure(scene, field)
         if field._dirty:
@@ -1168,7 +1202,15 @@ class GpuDemEngine(Engine):
         if timing:
             self._book_times(nSteps)
         st = self._h.status()
-        self._ran_time = st.timeSum - t0
+        if dyn is None:
+            # dt was constant: Scene.time advances by dt per step, as Scene::doOneStep adds it
+            t = scene.time
+            for _ in range(int(nSteps)):
+                t += p.dt
+            self._time_after = t
+        else:
+            self._time_after = scene.time + (st.timeSum - t0)
+        self._ran_time = self._time_after - scene.time
         scene.dt = st.dt
         if getattr(scene, "periodic", False):
             cc = self._h.cell()
@@ -1177,6 +1219,19 @@ class GpuDemEngine(Engine):
             self.updatePhys = "never"
             if getattr(self, "_sources", None):
                 self._sources["contactLoop"].updatePhys = "never"
+
+    def __getstate__(self):
+        d = dict(self.__dict__)
+        if self._h is not None:
+            base = dict(getattr(self, "_energy_base", {}))
+            for k, v in self._h.energy().items():
+                if k not in ("kinetic", "elast"):
+                    base[k] = base.get(k, 0.0) + v
+            d["_energy_base"] = base
+        for k in ("_h", "_params", "_mats", "_mlist", "_mat_index", "_field", "_timing_on", "_ellFunctor"):
+            d.pop(k, None)
+        d["_h"] = None
+        return d
 
     def _book_times(self, nSteps):
         """Device time of the three phases (CUDA events around each kernel) as execTime/execCount of this
