@@ -366,3 +366,23 @@ def test_dead_slots_spread_over_live_spheres():
     parked = {tuple(view.pos[i]) for i in range(4, 20)}
     live = {tuple(pa.pos[i]) for i in range(20, 31)}
     assert parked <= live and len(parked) == 11              # 16 dead slots over the 11 live spheres
+
+
+def test_disappear_and_reappear(monkeypatch):
+    """ParticleContainer.disappear / reappear (ParticleContainer.cpp:239-273): a resting sphere loses its
+    contacts with the new mask and falls through the floor; reappearing restores its mask."""
+    S = funnel(floor=True, layers=1, n_side=1)
+    run_on_oracle(monkeypatch, S, 3000)
+    sid = 5
+    assert S.dem.con.existsReal(4, sid)                   # resting on the floor
+    S.dem.par.disappear([sid], mask=0b1000)
+    assert not S.dem.con.exists(4, sid)
+    assert S.dem.par[sid].mask == 0b1000 and S.dem.par[sid].shape.visible is False
+    run_on_oracle(monkeypatch, S, 400)
+    assert S.dem.par[sid].pos[2] < 0                      # no contact with the floor any more
+    S.dem.par.reappear([sid], mask=dem.DemField.defaultMovableMask)
+    assert S.dem.par[sid].mask == dem.DemField.defaultMovableMask and S.dem.par[sid].shape.visible is True
+    with pytest.raises(RuntimeError, match="removeOverlapping"):
+        S.dem.par.reappear([sid], mask=5, removeOverlapping=True)
+    with pytest.raises(IndexError):
+        S.dem.par.disappear([999], mask=0)

@@ -420,6 +420,31 @@ class ParticleContainer:
             self._field._remove_particles(gone)
         return done
 
+    def remask(self, ids, mask, visible=True, removeContacts=False, removeOverlapping=False):
+        """ParticleContainer.remask (ParticleContainer.cpp:239-273): new mask (and visibility) for the
+        particles; with removeContacts, their contacts that may no longer collide (Collider::mayCollide
+        under the new masks) are removed.  removeOverlapping tests the collider's bounding boxes, which
+        live on the GPU, and is not provided."""
+        if removeOverlapping:
+            raise RuntimeError("ParticleContainer.remask(removeOverlapping=True) is not supported")
+        ids = [int(i) for i in ids]
+        for i in ids:
+            if not self.exists(i):
+                raise IndexError(f"No such particle: #{i}.")
+        for i in ids:
+            self._list[i].mask = int(mask)
+            self._list[i].shape.visible = bool(visible)
+        if removeContacts:
+            self._field._remove_uncollidable_contacts(ids)
+
+    def disappear(self, ids, mask):
+        """remask(ids, mask, visible=False, removeContacts=True)."""
+        self.remask(ids, mask, visible=False, removeContacts=True, removeOverlapping=False)
+
+    def reappear(self, ids, mask, removeOverlapping=False):
+        """remask(ids, mask, visible=True, removeContacts=False, removeOverlapping)."""
+        self.remask(ids, mask, visible=True, removeContacts=False, removeOverlapping=removeOverlapping)
+
     def _drop(self, ids):
         for i in ids:
             self._list[i] = None
@@ -629,6 +654,17 @@ class DemField:
         of the others), in the slots of their ids."""
         if self._engine is not None:
             self._engine._add_particles(self, pars)
+
+    def _remove_uncollidable_contacts(self, ids):
+        """Remove the contacts of the given particles whose pair may no longer collide (mask & mask == 0,
+        or a common loneMask bit; Collider::mayCollide, src/dem/Collision.cpp:21-43)."""
+        if self._engine is None:
+            return
+        self._engine._remove_contacts_where(self, ids, self._may_collide)
+
+    def _may_collide(self, a, b):
+        ma, mb = self.par[a].mask, self.par[b].mask
+        return (ma & mb) != 0 and (ma & mb & self.loneMask) == 0
 
     def _remove_particles(self, ids):
         """DemField::removeParticle for each id (src/dem/Particle.cpp:483-530): its contacts go, the other
@@ -1263,6 +1299,24 @@ class GpuDemEngine(Engine):
             self._h.set_params(self._params)
             self._h.upload_contacts(con)
         field._dirty.clear()
+
+    def _remove_contacts_where(self, field, ids, may_collide):
+        """Drop the contacts of `ids` for which may_collide(idA, idB) is false; the others keep their
+        history.  The particle arrays (with the new masks) and the contacts are uploaded again."""
+        if field._stale:
+            self._download_particles(field)
+        con = self._download_contacts()
+        sel = np.isin(con.idA, ids) | np.isin(con.idB, ids)
+        drop = np.zeros(con.n, bool)
+        for k in np.nonzero(sel)[0]:
+            drop[k] = not may_collide(int(con.idA[k]), int(con.idB[k]))
+        if drop.any() or field._dirty:
+            self._h.set_params(self._params)
+            self._h.upload_particles(self._device_view(field, field._arrays))
+            self._h.set_params(self._params)
+            self._h.upload_contacts(con.take(~drop))
+            field._dirty.clear()
+        field._con_cache = None
 
     def _add_particles(self, field, pars):
         """Particles added to the running field: packed into the slots of their ids (reused ids of removed
