@@ -180,3 +180,9 @@ def test_unbalanced_force_and_energy(monkeypatch):
     ue = utils.unbalancedEnergy(S)
     e = S.energy
     assert ue == e["kinetic"] / e["elast"]
+
+
+def test_demfield_nodes_are_the_integrated_ones():
+    S = small_scene()
+    ids = [n._local["pos"][2] for n in S.dem.nodes]
+    assert len(S.dem.nodes) == 5 and min(ids) > 0         # the wall (fixed, massless) is not collected

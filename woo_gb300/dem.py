@@ -689,7 +689,9 @@ class DemField:
     # --- Woo API
     @property
     def nodes(self):
-        return [p.shape.nodes[0] for p in self.par]
+        """DemField.nodes: the nodes Leapfrog integrates, those added with nodes=True or guessed moving
+        (ParticleContainer.add, DemData.guessMoving); fixed particles' nodes are not in it."""
+        return [p.shape.nodes[0] for p in self.par if getattr(p, "_integrated", True)]
 
     def unbalancedForce(self, useMaxForce=False):
         """DemFuncs::unbalancedForce (src/dem/Funcs.cpp:231-258): the mean (or maximum) force norm on the
