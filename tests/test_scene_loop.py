@@ -65,3 +65,18 @@ def test_zero_steps_and_hooks():
     S.stopAtHook = "S.lab.a+=1"
     with pytest.raises(RuntimeError, match="stopAtHook"):
         S.run(5)
+
+
+def test_save_tmp_load_tmp(monkeypatch):
+    """Scene.saveTmp / loadTmp (py/tests/test_io.py:105-111): a copy from memory continues like the original."""
+    S = funnel(floor=True)
+    run_on_oracle(monkeypatch, S, 200)
+    S.saveTmp("a")
+    T = Scene.loadTmp("a")
+    run_on_oracle(monkeypatch, S, 300)
+    run_on_oracle(monkeypatch, T, 300)
+    assert T.step == S.step == 500 and T.time == S.time
+    for p in S.dem.par:
+        assert (p.pos == T.dem.par[p.id].pos).all() and (p.vel == T.dem.par[p.id].vel).all()
+    with pytest.raises(ValueError):
+        Scene.loadTmp("missing")

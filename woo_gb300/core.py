@@ -99,6 +99,9 @@ class Cell:
         self._edited = False
 
 
+_TMP = {}   # scenes kept in memory by Scene.saveTmp
+
+
 class Scene:
     """Scene (src/core/Scene.hpp:191-205 attributes dt, dtSafety, step, time, trackEnergy, isPeriodic, cell)."""
 
@@ -297,6 +300,19 @@ class Scene:
         if not isinstance(S, Scene):
             raise TypeError("Loaded object of type " + type(S).__name__ + " is not a Scene")
         return S
+
+    def saveTmp(self, name="", quiet=False):
+        """Scene.saveTmp: the scene kept in memory under `name` (as Scene.save writes it)."""
+        import pickle
+        _TMP[name] = pickle.dumps(self, protocol=pickle.HIGHEST_PROTOCOL)
+
+    @staticmethod
+    def loadTmp(name=""):
+        """Scene.loadTmp: a new scene from the state saved by saveTmp under `name`."""
+        import pickle
+        if name not in _TMP:
+            raise ValueError(f"No memory-saved scene named {name!r}")
+        return pickle.loads(_TMP[name])
 
     def __getstate__(self):
         d = dict(self.__dict__)
