@@ -80,3 +80,13 @@ def test_save_tmp_load_tmp(monkeypatch):
         assert (p.pos == T.dem.par[p.id].pos).all() and (p.vel == T.dem.par[p.id].vel).all()
     with pytest.raises(ValueError):
         Scene.loadTmp("missing")
+
+
+def test_synchronous_loop_controls():
+    S = Scene(dt=1.)
+    with S.paused():
+        assert not S.running
+    S.run(3)
+    S.stop()
+    S.wait()
+    assert S.step == 3 and not S.running

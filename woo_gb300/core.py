@@ -321,6 +321,21 @@ class Scene:
                 fld._engine._download_particles(fld)
         return d
 
+    @property
+    def running(self):
+        """Scene.running: a run returns only when its steps are done, so no run is in progress between
+        calls."""
+        return False
+
+    def stop(self):
+        """Scene.stop: nothing runs in the background, so there is nothing to stop."""
+        return None
+
+    def paused(self):
+        """Scene.paused(): a context manager; with synchronous runs it only brackets the block."""
+        import contextlib
+        return contextlib.nullcontext(self)
+
     def one(self):
         self.run(1)
 
