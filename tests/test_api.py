@@ -186,3 +186,11 @@ def test_demfield_nodes_are_the_integrated_ones():
     S = small_scene()
     ids = [n._local["pos"][2] for n in S.dem.nodes]
     assert len(S.dem.nodes) == 5 and min(ids) > 0         # the wall (fixed, massless) is not collected
+
+
+def test_particle_kinetic_energies():
+    p = dem.Sphere.make((0, 0, 0), 0.01, vel=(1, 2, 2))
+    p.angVel = (0, 0, 3)
+    assert p.Ekt == pytest.approx(0.5 * p.mass * 9)
+    assert p.Ekr == pytest.approx(0.5 * p.inertia[2] * 9)
+    assert p.Ek == pytest.approx(p.Ekt + p.Ekr)

@@ -337,6 +337,17 @@ class Particle:
         v = self.vel
         return 0.5 * self.mass * float(v @ v)
 
+    @property
+    def Ekr(self):
+        """Rotational kinetic energy, DemData::getEk_any(rot) (src/dem/Particle.cpp:257-263), without
+        the periodic cell's spin."""
+        from .outlet import kinetic_energy
+        return kinetic_energy(0.0, self.inertia, self.pos, self.vel, self.angVel, self.ori, 0.0)
+
+    @property
+    def Ek(self):
+        return self.Ekt + self.Ekr
+
 
 class ParticleContainer:
     """S.dem.par (src/dem/ParticleContainer.hpp)."""
