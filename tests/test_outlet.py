@@ -386,3 +386,14 @@ def test_disappear_and_reappear(monkeypatch):
         S.dem.par.reappear([sid], mask=5, removeOverlapping=True)
     with pytest.raises(IndexError):
         S.dem.par.disappear([999], mask=0)
+
+
+def test_contact_container_clear(monkeypatch):
+    S = funnel(floor=True, layers=2)
+    run_on_oracle(monkeypatch, S, 2500)
+    assert S.dem.con.countReal() > 3
+    S.dem.con.clear()
+    assert len(S.dem.con) == 0
+    run_on_oracle(monkeypatch, S, 1)
+    assert S.dem.con.countReal() > 3                      # found again, with fresh history
+    assert all(c.stepCreated == 2500 for c in S.dem.con)

@@ -576,6 +576,13 @@ class ContactContainer:
     def countReal(self):
         return int(self._arrays().real.sum())
 
+    def clear(self):
+        """ContactContainer.clear: every contact (real or potential) is removed, history included; the
+        collider then runs in full at the next step."""
+        f = self._field
+        if f._engine is not None:
+            f._engine._remove_contacts_where(f, [p.id for p in f.par], lambda a, b: False)
+
     def realRatio(self):
         n = len(self)
         return self.countReal() / n if n else float("nan")
