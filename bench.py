@@ -3,10 +3,12 @@
 Workloads (synthetic, seeded; no dataset is involved):
   hertz1M (default) -- 1,000,000 polydisperse HertzMat spheres (r ~ U[2,6] mm, DMT, en=.8, surfEnergy
       .01, tanPhi .3/.6) as a loose cloud (solid fraction ~0.3) falling into a 1 x 1 x 2 m walled box,
-      dt = 0.3 x p-wave dt, verletDist 0.1 x rmin.  By default the timed region is the whole 20,000-step
-      job, collider rebuilds included.
-  hertz1M_settled -- the same spheres after settling on the GPU (untimed: 10 g and damping 0.5 until
-      the column has fallen, then 1 g), a few contacts per sphere; then timed with the job's parameters.
+      dt = 0.3 x p-wave dt, verletDist 0.1 x rmin.  The timed region is K steps after W warm-up steps of
+      that job, the same steps that the CPU arm (--impl reference) times.  The line also carries
+      "settled": the same spheres settled on the GPU first (untimed: 10 g and damping 0.5 while the cloud
+      falls, then 3000 steps at 1 g), then W + K steps with the job's parameters, about one real contact
+      per sphere, with the CPU port timed on that same settled state in the same process.
+  hertz1M_settled -- the settled state alone as the headline.
   ell200k -- 200,000 ellipsoids (a ~ U[3,6] mm, b = .7a, c = .5a, random orientations) agitated in a
       0.6 x 0.6 x 1.2 m walled box under gravity, FrictMat E 1e7 tanPhi .4, dt 0.9 x p-wave dt.  The
       learned warm start is trained first (untimed) on records logged by the plain Newton solver; the
@@ -28,8 +30,9 @@ region covers K consecutive steps of one simulation, state resident in HBM (larg
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference] [--workload ...]
 
---impl reference times the reference algorithm on the host cores (the OpenMP build of the CPU
-restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop), on a bounded cut of the workload.
+--impl reference times the reference algorithm on the host cores: the OpenMP build of the CPU
+restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, on the same scene (built by the
+oracle's copy of the packing generator, so the engine library is never loaded) and the same W + K steps.
 Multi-GPU: the path does not shard (contacts couple neighbours); N ranks run N independent replicas.
 """
 import argparse
@@ -50,7 +53,7 @@ sys.path.insert(0, ROOT)
 import numpy as np
 
 WORKLOADS = ["hertz1M", "hertz1M_settled", "ell200k", "batch512", "peri8M", "spheres10k"]
-DEFAULT_STEPS = {"hertz1M": 20000, "hertz1M_settled": 2000, "ell200k": 500, "batch512": 500, "peri8M": 500,
+DEFAULT_STEPS = {"hertz1M": 20, "hertz1M_settled": 20, "ell200k": 500, "batch512": 500, "peri8M": 500,
                  "spheres10k": 2000}
 METRIC = "particle-steps/s per GB300"
 DESCR = {"hertz1M": "plain DEM step, HertzDMT settling",
@@ -65,7 +68,7 @@ def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None, help="timed steps (default: per workload)")
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="hertz1M", choices=WORKLOADS)
     ap.add_argument("--e2e-steps", type=int, default=2000)
@@ -75,6 +78,9 @@ def parse():
                     help="steps queued before the host checks the collider trigger (engine default 32; 1 = every step)")
     ap.add_argument("--n", type=int, default=None,
                     help="particle count of a smaller cut of the workload (same density; for profiling runs)")
+    ap.add_argument("--no-settled", action="store_true", help="hertz1M: leave out the settled-state object")
+    ap.add_argument("--profile-region", default="main", choices=["main", "settled", "none"],
+                    help="timed region bracketed by cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     a = ap.parse_args()
     if a.steps is None:
         a.steps = DEFAULT_STEPS[a.workload]
@@ -147,63 +153,57 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_scene(name, n=None):
+def build_scene(name, n=None, packer="engine"):
+    """The workload's seeded scene.  packer="oracle" builds the same packing with the oracle's restatement
+    of the generator (the CPU arm, which must not load the engine library)."""
     from woo_gb300 import abi, scenes
-    if name == "hertz1M":
-        return scenes.hertz1M(n=n or 1_000_000)
-    if name == "hertz1M_settled":
-        return scenes.hertz1M(n=n or 1_000_000, height=0.95)
-    if name == "peri8M":
-        return scenes.densify_periodic(scenes.peri_shear(n=n or 8_000_000), phi_target=0.62)
-    if name == "batch512":
-        return scenes.batch_oedometric(n or 512, 4)
-    if name == "ell200k":
-        k = n or 200_000
-        sc = (k / 200_000) ** (1.0 / 3.0)
-        return scenes.ellipsoid_cloud(k, 7, box=(0.6 * sc, 0.6 * sc, 1.2 * sc), amin=0.003, amax=0.006, dense=1.0,
-                                      vel_scale=0.5, angvel_scale=5.0, young=1e7, tanPhi=0.4, damping=0.2,
-                                      ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_MLP)
-    return scenes.spheres10k(n=n or 10000)
+    if packer == "oracle":
+        from oracle import bridge
+        scenes.set_packer(bridge.make_cloud, bridge.make_cloud_radii)
+    try:
+        if name == "hertz1M":
+            return scenes.hertz1M(n=n or 1_000_000)
+        if name == "hertz1M_settled":
+            return scenes.hertz1M(n=n or 1_000_000, height=0.95)
+        if name == "peri8M":
+            return scenes.densify_periodic(scenes.peri_shear(n=n or 8_000_000), phi_target=0.62)
+        if name == "batch512":
+            return scenes.batch_oedometric(n or 512, 4)
+        if name == "ell200k":
+            k = n or 200_000
+            sc = (k / 200_000) ** (1.0 / 3.0)
+            return scenes.ellipsoid_cloud(k, 7, box=(0.6 * sc, 0.6 * sc, 1.2 * sc), amin=0.003, amax=0.006, dense=1.0,
+                                          vel_scale=0.5, angvel_scale=5.0, young=1e7, tanPhi=0.4, damping=0.2,
+                                          ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_MLP)
+        return scenes.spheres10k(n=n or 10000)
+    finally:
+        scenes.set_packer()
 
 
 def copy_params(p):
-    from woo_gb300 import abi
-    q = abi.Params()
-    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(p))
-    return q
+    from woo_gb300 import scenes
+    return scenes.copy_params(p)
 
 
 def settle(h, spec):
-    """Untimed settling on the GPU: gravity x 10 and damping 0.5 for as long as a free fall of half the
-    cloud height takes, then 3000 steps at 1 g with damping 0.5; the parameters are then restored."""
-    p = copy_params(spec.params)
-    dt = spec.params.dt
-    height = spec.info.get("height", 1.0)
-    g = abs(spec.params.gravity[2])
-    fall = int(math.sqrt(2 * 0.5 * height / (10 * g)) / dt)
-    for mult, steps in ((10.0, fall), (1.0, 3000)):
-        p.gravity[2] = spec.params.gravity[2] * mult
-        p.damping = 0.5
-        p.step = h.status().step
-        h.set_params(p)
-        h.step(steps)
-    q = copy_params(spec.params)
-    q.step = h.status().step
-    h.set_params(q)
-    return fall + 3000
+    """Untimed settling on the GPU (scenes.settle): 10 g and damping 0.5 while the cloud falls half its
+    height, then 3000 steps at 1 g; the job's parameters are restored."""
+    from woo_gb300 import scenes
+    return scenes.settle(h, spec)
 
 
 def contact_kernel_bytes(cg, hertz):
-    """Algorithmic bytes of one contact pass: 80 B per particle touched by a contact (pos 24, vel 24,
-    angVel 24, radius 8), 288 B per real contact (ids 8, history read 112, history write 96, reduction
-    outputs 72), 16 B per potential-only pair (ids 8 + the distance-test data 8); Hertz adds 16 B r/w
-    (kn, kt) + 8 B per real contact."""
+    """Algorithmic bytes of one contact pass (fixed per-unit figures): 80 B per particle touched by a real
+    contact (pos 24, vel 24, angVel 24, radius 8), 288 B per real contact (ids 8, history read 112, history
+    write 96, reduction outputs 72; Hertz adds 16 B r/w of kn, kt and 8 B contRad), 16 B per live
+    potential-only pair (ids 8 + the distance-test data 8)."""
     live = cg.n
-    real = int(cg.real.sum())
+    r = cg.real == 1
+    real = int(r.sum())
     pot = live - real
-    touched = len(np.unique(np.concatenate([cg.idA, cg.idB]))) if live else 0
+    touched = len(np.unique(np.concatenate([cg.idA[r], cg.idB[r]]))) if real else 0
     per_real = 288 + (24 if hertz else 0)
-    return 80 * touched + per_real * real + 16 * pot, dict(real=real, potential=pot, touched=touched)
+    return 80 * touched + per_real * real + 16 * pot, dict(real=real, potential=pot, touched_by_real=touched)
 
 
 def max_over_ranks(x, world, device):
@@ -221,17 +221,23 @@ def replica_throughput(world, n, steps, seconds):
     return world * n * steps / seconds
 
 
-def timed_steps(h, stream, k, world, local, barrier):
+def timed_steps(h, stream, k, world, local, barrier, profile=False):
+    """K steps timed with CUDA events on the engine's stream (barrier and synchronize on both sides); with
+    profile, the region is bracketed by cudaProfilerStart/Stop for ncu --profile-from-start off."""
     import torch
     barrier()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    if profile:
+        torch.cuda.profiler.start()
     ev0.record(stream)
     h.step(k)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
+    if profile:
+        torch.cuda.profiler.stop()
     barrier()
     ms = ev0.elapsed_time(ev1)
     return max_over_ranks(ms, world, f"cuda:{local}")
@@ -283,6 +289,151 @@ def ell_variants(args, spec, local, world, barrier, w):
                      "fallback_fraction": (s1.ellFallbacks - s0.ellFallbacks) / max(solves, 1)}
         h.close()
     return out
+
+
+def state_tag(args, region, n):
+    """Descriptor of the state a timed region starts from; an ncu summary under profiles/ is used for this
+    region's traffic only when it records the same descriptor (a capture of the same deterministic run)."""
+    return f"{args.workload}/{region}/n={n}/warmup={max(args.warmup, 3)}/steps={args.steps}"
+
+
+def read_profile_figures(tag):
+    """`- name: number` figures of the ncu summary under profiles/ that records `- state: <tag>`."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return {}
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".md"):
+            continue
+        figs, st = {}, None
+        with open(os.path.join(d, fn)) as f:
+            for line in f:
+                m = re.match(r"^- state: (\S+)\s*$", line)
+                if m:
+                    st = m.group(1)
+                m = re.match(r"^- ([\w.]+): ([0-9.eE+-]+)\s*$", line)
+                if m:
+                    figs[m.group(1)] = float(m.group(2))
+        if st == tag:
+            return figs
+    return {}
+
+
+PHASE_KERNELS = {"contacts": ("k_contacts_cull", "k_contacts"), "leapfrog": ("k_leapfrog_fast", "k_leapfrog_lists")}
+PHASE_LABEL = {"contacts": "contact pass (k_contacts_cull + k_contacts: Cg2+Cp2+Law2)",
+               "leapfrog": "integrator (k_leapfrog_fast + k_leapfrog_lists: CSR force gather + Leapfrog + verlet check)"}
+
+
+def measure_region(h, spec, args, world, local, barrier, region, clocks=None):
+    """W warm-up steps, K timed steps (CUDA events), then a window of steps with per-phase CUDA events for
+    the roofline objects and the collider figures.  Returns the region's figures."""
+    import torch
+    from woo_gb300 import abi
+    n = spec.particles.n
+    stream = torch.cuda.ExternalStream(h.stream(), device=local)
+    h.step(max(args.warmup, 3))
+    st0 = h.status()
+    l0 = h.launch_count()
+    ms = timed_steps(h, stream, args.steps, world, local, barrier, profile=(args.profile_region == region))
+    launches = h.launch_count() - l0
+    st1 = h.status()
+    cg = h.download_contacts()   # the state at the end of the timed region
+    hertz = spec.params.cp2 == abi.CP2_HERTZ
+    cbytes, counts = contact_kernel_bytes(cg, hertz)
+    lbytes = 256 * n + 80 * counts["real"]   # Leapfrog 300 + CSR 52 - 96 fused B/particle, 80 B/real contact
+    # per-phase CUDA events over a following window (the timed region runs without them)
+    kw = max(args.steps, 200)
+    s0 = h.status()
+    h.set_timing(True)
+    torch.cuda.synchronize()
+    h.step(kw)
+    torch.cuda.synchronize()
+    kt = h.kernel_times()
+    h.set_timing(False)
+    s1 = h.status()
+    hbm_peak, peak_kind = load_peaks()
+    fp64_peak = h.fp64_peak()
+    figs = read_profile_figures(state_tag(args, region, n))
+    rl = {}
+    for ph, abytes in (("contacts", cbytes), ("leapfrog", lbytes)):
+        k_ms, k_n = kt.get(ph, (0.0, 0))
+        avg = k_ms / max(k_n, 1)
+        ach = abytes / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+        names = PHASE_KERNELS[ph]
+        tr = [figs.get(f"{k}.dram_bytes_per_launch") for k in names]
+        traffic = sum(tr) if all(t is not None for t in tr) else None
+        dp = [figs.get(f"{k}.fp64_ops_per_launch") for k in names]
+        dp_ops = sum(dp) if all(t is not None for t in dp) else None
+        rl[ph] = {"kernel": PHASE_LABEL[ph], "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": ach / hbm_peak, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                  "algorithmic_bytes_per_launch": abytes, "traffic": traffic,
+                  "traffic_source": "ncu capture of this region's launches (same seeded run)" if traffic else None,
+                  "ms_avg": avg, "launches_in_window": k_n,
+                  "fp64": {"peak_gflops_measured": fp64_peak, "ops_per_launch_ncu": dp_ops,
+                           "achieved_gflops": (dp_ops / (avg / 1e3) / 1e9) if (dp_ops and avg > 0) else None,
+                           "frac": (dp_ops / (avg / 1e3) / 1e9 / fp64_peak) if (dp_ops and avg > 0) else None}}
+    c_ms, c_n = kt.get("collider", (0.0, 0))
+    rebuilds = int(s1.nFullRuns - s0.nFullRuns)
+    return {
+        "value": replica_throughput(world, n, args.steps, ms / 1e3), "ms_per_step": ms / args.steps,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "gpu_launches": int(launches),
+        "contacts": dict(counts, collider_rebuilds_timed=int(st1.nFullRuns - st0.nFullRuns)),
+        "collider": {"window_steps": kw, "rebuilds_in_window": rebuilds,
+                     "collider_ms_per_rebuild": (c_ms / c_n) if c_n else None,
+                     "steps_per_rebuild": (kw / rebuilds) if rebuilds else None},
+        "kernels": {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / max(v[1], 1)} for k, v in kt.items()},
+        "kernels_window_steps": kw, "rooflines": rl, "state": state_tag(args, region, n),
+    }
+
+
+def e2e_measure(h, n, ne, world, local, barrier):
+    """End to end through the public C ABI with host buffers, as the engine plug-in runs inside Woo's step
+    loop: the kinematic state goes in from pinned host memory once per job (wdem_write_state), then one
+    wdem_step call per step (each returns the step's status word to the host: error code and collider
+    trigger), then the state comes back to pinned host memory (wdem_read_state).  Beside it, the same with
+    the whole kinematic state copied in and out around every single step."""
+    import torch
+    from woo_gb300 import abi
+    pin = {k: torch.empty((n, w_), dtype=torch.float64, pin_memory=True) for k, w_ in
+           (("pos", 3), ("vel", 3), ("angVel", 3), ("ori", 4))}
+    ptrs = (pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
+    h.read_state(n, *ptrs)
+    bytes_io = n * (3 + 3 + 3 + 4) * 8
+    status_bytes = 128
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h.write_state(n, *ptrs)
+    for _ in range(ne):
+        h.step(1)
+    h.read_state(n, *ptrs)
+    torch.cuda.synchronize()
+    te = max_over_ranks(time.perf_counter() - t0, world, f"cuda:{local}")
+    e2e = {"value": replica_throughput(world, n, ne, te), "unit": "particle-steps/s",
+           "h2d_bytes_per_step": bytes_io / ne + ctypes.sizeof(abi.Params),
+           "d2h_bytes_per_step": bytes_io / ne + status_bytes, "steps": ne,
+           "pattern": "state copied in once and out once per job of `steps` steps (the engine keeps the state "
+                      "resident between wdem_step calls), one wdem_step(h, 1) call per step returning its status"}
+    nr = min(50, ne)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(nr):
+        h.write_state(n, *ptrs)
+        h.step(1)
+        h.read_state(n, *ptrs)
+    torch.cuda.synchronize()
+    tr = time.perf_counter() - t0
+    roundtrip = {"value": n * nr / tr, "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_io,
+                 "d2h_bytes_per_step": bytes_io, "steps": nr,
+                 "pattern": "whole kinematic state copied host->device and back around every step"}
+    return e2e, roundtrip
+
+
+def common_config(args, spec):
+    """The config object both arms print (the driver compares them)."""
+    return {"workload": args.workload, "n_particles": int(spec.particles.n), "dt": float(spec.params.dt),
+            "steps_simulated_before_timing": int(max(args.warmup, 3)), "timed_steps": int(args.steps),
+            "l2": "state larger than L2 (no flush needed)"}
 
 
 def run_gpu(args, rank, world, local):
@@ -349,141 +500,109 @@ def run_gpu(args, rank, world, local):
         h = new_handle(spec, local)
     else:
         h = new_handle(spec, local)
-    stream = torch.cuda.ExternalStream(h.stream(), device=local)
     settled_steps = settle(h, spec) if args.workload == "hertz1M_settled" else 0
-
-    # warm-up (includes the first collider build)
-    h.step(max(args.warmup, 3))
-    st0 = h.status()
-    l0 = h.launch_count()
-    hbm_peak, peak_kind = load_peaks()
 
     clocks = ClockSampler(local)
     clocks.start()
-    ms_max = timed_steps(h, stream, args.steps, world, local, barrier)
-    clk = clocks.stop()
-    launches = h.launch_count() - l0
-    st1 = h.status()
-    value = replica_throughput(world, n, args.steps, ms_max / 1e3)
-    # per-phase CUDA-event times (leapfrog, collider, contacts) from a following window of the same run;
-    # kept out of the timed region above so that the extra events do not slow it
-    # (the window is also the cudaProfilerStart/Stop range: `ncu --profile-from-start off` captures
-    # these launches only, at the state the timed region ended in)
-    kw = min(args.steps, 2000)
-    h.set_timing(True)
-    torch.cuda.synchronize()
-    torch.cuda.profiler.start()
-    h.step(kw)
-    torch.cuda.synchronize()
-    torch.cuda.profiler.stop()
-    kt = h.kernel_times()
-    h.set_timing(False)
-
-    # roofline of the dominant kernel: algorithmic bytes per launch (contact counts at the end of the
-    # timed region) over the CUDA-event average launch duration inside the timed region
-    cg = h.download_contacts()
-    hertz = spec.params.cp2 == abi.CP2_HERTZ
-    cbytes, counts = contact_kernel_bytes(cg, hertz)
-    lbytes = 256 * n + 80 * counts["real"]   # fused CSR reduction + Leapfrog: 300+52-96 B/particle, 80 B/real contact
-    fp64_peak = h.fp64_peak()
-    rl = {}
-    for kname, label, abytes in (("contacts", "contact pass (k_contacts_cull + k_contacts: Cg2+Cp2+Law2)", cbytes),
-                                 ("leapfrog", "k_leapfrog (CSR force gather + Leapfrog + verlet check)", lbytes)):
-        k_ms, k_n = kt.get(kname, (0.0, 0))
-        avg = k_ms / max(k_n, 1)
-        ach = abytes / (avg / 1e3) / 1e9 if avg > 0 else 0.0
-        prof = os.path.join(ROOT, "profiles", f"{PROFILE_KERNEL[kname]}_{args.workload}.md")
-        traffic = dp_ops = None
-        if os.path.exists(prof):
-            figs = read_profile_figures(prof)
-            traffic = figs.get("dram_bytes_per_launch")
-            dp_ops = figs.get("fp64_flops_per_launch")
-        rl[kname] = {"kernel": label, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach / hbm_peak, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_launch": abytes, "traffic": traffic, "ms_avg": avg,
-                     "fp64": {"peak_gflops_measured": fp64_peak,
-                              "flops_per_launch_ncu": dp_ops,
-                              "achieved_gflops": (dp_ops / (avg / 1e3) / 1e9) if (dp_ops and avg > 0) else None,
-                              "frac": (dp_ops / (avg / 1e3) / 1e9 / fp64_peak) if (dp_ops and avg > 0) else None}}
-    dominant = max(rl, key=lambda k: rl[k]["ms_avg"])
-
-    # End to end through the public C ABI with host buffers, as the engine plug-in runs inside Woo's
-    # step loop: the kinematic state goes in from pinned host memory (wdem_write_state), then one
-    # wdem_step call per step (each one returns the step's status word to the host: error code and
-    # collider trigger), then the state comes back to pinned host memory (wdem_read_state).
-    e2e, roundtrip = None, None
+    main = measure_region(h, spec, args, world, local, barrier, "main")
+    e2e, roundtrip = (None, None)
     ne = min(args.e2e_steps, args.steps)
     if ne > 0:
-        pin = {k: torch.empty((n, w_), dtype=torch.float64, pin_memory=True) for k, w_ in
-               (("pos", 3), ("vel", 3), ("angVel", 3), ("ori", 4))}
-        ptrs = (pin["pos"].data_ptr(), pin["vel"].data_ptr(), pin["angVel"].data_ptr(), pin["ori"].data_ptr())
-        h.read_state(n, *ptrs)
-        bytes_io = n * (3 + 3 + 3 + 4) * 8
-        status_bytes = 128
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        h.write_state(n, *ptrs)
-        for _ in range(ne):
-            h.step(1)
-        h.read_state(n, *ptrs)
-        torch.cuda.synchronize()
-        te = time.perf_counter() - t0
-        te_max = max_over_ranks(te, world, f"cuda:{local}")
-        e2e = {"value": replica_throughput(world, n, ne, te_max), "unit": "particle-steps/s",
-               "h2d_bytes_per_step": bytes_io / ne + ctypes.sizeof(abi.Params),
-               "d2h_bytes_per_step": bytes_io / ne + status_bytes, "steps": ne,
-               "pattern": "state in from pinned host memory, one wdem_step(h, 1) call per step, state out"}
-        # the same with the full kinematic state copied in and out around every single step
-        nr = min(50, ne)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(nr):
-            h.write_state(n, *ptrs)
-            h.step(1)
-            h.read_state(n, *ptrs)
-        torch.cuda.synchronize()
-        tr = time.perf_counter() - t0
-        roundtrip = {"value": n * nr / tr, "unit": "particle-steps/s", "h2d_bytes_per_step": bytes_io,
-                     "d2h_bytes_per_step": bytes_io, "steps": nr}
-
-    out = {
-        "metric": f"{METRIC} ({DESCR[args.workload]})",
-        "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded random sequential addition packing)",
-        "config": {"workload": args.workload, "n_particles": n, "dt": spec.params.dt,
-                   "parallelism": f"replicas x{world}", "l2": "state larger than L2 (no flush needed)",
-                   "steps_simulated_before_timing": int(max(args.warmup, 3)) + settled_steps,
-                   "queue_depth": 32 if args.queue_depth is None else args.queue_depth},
-        "gpu_launches": int(launches),
-        "kernels": {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / max(v[1], 1)} for k, v in kt.items()},
-        "kernels_window_steps": kw,
-        "contacts": dict(counts, collider_rebuilds_timed=int(st1.nFullRuns - st0.nFullRuns)),
-        "roofline": rl[dominant],
-        "roofline_other": {k: v for k, v in rl.items() if k != dominant},
-        "clocks": clk,
-        "e2e": e2e,
-        "e2e_state_roundtrip_every_step": roundtrip,
-    }
+        e2e, roundtrip = e2e_measure(h, n, ne, world, local, barrier)
     if getattr(spec, "cell", None) is not None:
         extra["stress_end_Pa"] = h.stress().tolist()
         extra["packing"] = {"solid_fraction": spec.info.get("phi")}
-    if "scene_by_scene" in extra:
-        extra["batch_speedup_vs_scene_by_scene"] = value / extra["scene_by_scene"]["value"]
-    out.update(extra)
     h.close()
+
+    settled = None
+    if args.workload == "hertz1M" and not args.no_settled:
+        # the same spheres settled on the GPU (untimed), then W + K steps with the job's parameters
+        hs = new_handle(spec, local)
+        t0 = time.time()
+        nsettle = settle(hs, spec)
+        settle_s = time.time() - t0
+        settled = measure_region(hs, spec, args, world, local, barrier, "settled")
+        settled["settling"] = {"steps": nsettle, "seconds": settle_s,
+                               "how": "10 g and damping 0.5 while the cloud falls half its height, then 3000 steps at 1 g"}
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            # the CPU port on this same settled state: particles and contacts (with history) handed over
+            pa = hs.download_particles(abi.ParticleArrays(n))
+            ca = hs.download_contacts()
+            sp = copy_params(spec.params)
+            sp.step = hs.status().step
+            settled["cpu_baseline"] = cpu_timed(args, sp, pa, ca, None,
+                                                f"the same settled {n}-particle state at step {sp.step} "
+                                                f"(particles and contacts with history from the GPU), {{steps}} steps after 2 untimed")
+            settled["vs_cpu_baseline"] = settled["value"] / settled["cpu_baseline"]["value"]
+        hs.close()
+    clk = clocks.stop()
+    clk["interval"] = "sampled over the GPU run: warm-up, timed regions, windows, e2e and settling"
+
+    dominant = max(main["rooflines"], key=lambda k: main["rooflines"][k]["ms_avg"])
+    out = {
+        "metric": f"{METRIC} ({DESCR[args.workload]})",
+        "value": main["value"], "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random sequential addition packing)",
+        "config": common_config(args, spec),
+        "engine": {"parallelism": f"replicas x{world}",
+                   "queue_depth": 32 if args.queue_depth is None else args.queue_depth,
+                   "steps_simulated_before_warmup": settled_steps},
+        "gpu_launches": main["gpu_launches"],
+        "contacts": main["contacts"], "collider": main["collider"],
+        "kernels": main["kernels"], "kernels_window_steps": main["kernels_window_steps"],
+        "roofline": main["rooflines"][dominant],
+        "roofline_other": {k: v for k, v in main["rooflines"].items() if k != dominant},
+        "clocks": clk, "e2e": e2e, "e2e_state_roundtrip_every_step": roundtrip,
+    }
+    if settled is not None:
+        out["settled"] = settled
+    if "scene_by_scene" in extra:
+        extra["batch_speedup_vs_scene_by_scene"] = out["value"] / extra["scene_by_scene"]["value"]
+    out.update(extra)
     return out, spec
 
 
-def cpu_baseline(args, full_n):
-    """OpenMP CPU restatement of Woo's step on the host cores, on a bounded cut of the workload
-    (the settled workload: a cut settled on the GPU, its state and contacts handed to the CPU)."""
+def cpu_timed(args, params, particles, contacts, cell, sample, max_steps=None):
+    """The OpenMP port on the host cores: 2 untimed steps (the initial sort), then timed steps until K steps
+    or about --cpu-seconds have run (steady_clock, in the library)."""
     from oracle import bridge
-    cuts = {"hertz1M": 100_000, "hertz1M_settled": 100_000, "ell200k": 10_000, "batch512": 16, "peri8M": 10_000,
-            "spheres10k": 10000}
+    o = bridge.Oracle(params, particles, contacts=contacts, canonical=False, variant="liborc_omp.so", cell=cell)
+    o.set_parallel(True)
+    o.step(2)
+    steps, total, k = 0, 0.0, 1
+    cap = max_steps or args.steps
+    while steps < cap and (total < args.cpu_seconds or steps == 0):
+        kk = min(k, cap - steps)
+        total += o.step_timed(kk)
+        steps += kk
+        k = min(k * 2, 2000)
+    n = particles.n
+    return {"value": n * steps / total, "unit": "particle-steps/s", "cores": o.threads(), "kind": "port",
+            "steps": steps, "seconds": total,
+            "sample": sample.format(steps=steps) + f", OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/"
+                                                    f"ContactLoop, {o.threads()} threads"}
+
+
+def cpu_baseline(args):
+    """OpenMP CPU restatement of Woo's step on the host cores.  hertz1M: the same 1M scene and the same
+    W warm-up + K timed steps as the GPU arm.  The other workloads: a bounded cut (settled: a cut settled
+    on the GPU, its state and contacts handed to the CPU)."""
+    from oracle import bridge
+    if args.workload == "hertz1M":
+        spec = build_scene(args.workload, n=args.n, packer="oracle")
+        o = bridge.Oracle(spec.params, spec.particles, canonical=False, variant="liborc_omp.so")
+        o.set_parallel(True)
+        o.step(max(args.warmup, 3))
+        total = o.step_timed(args.steps)
+        n = spec.particles.n
+        return {"value": n * args.steps / total, "unit": "particle-steps/s", "cores": o.threads(), "kind": "port",
+                "steps": args.steps, "seconds": total,
+                "sample": f"the same {n}-particle scene and steps: {max(args.warmup, 3)} untimed + {args.steps} timed, "
+                          f"OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, {o.threads()} threads"}, spec
+    cuts = {"hertz1M_settled": 100_000, "ell200k": 10_000, "batch512": 16, "peri8M": 10_000, "spheres10k": 10000}
     cut = cuts[args.workload]
-    spec = build_scene(args.workload, n=cut)
+    spec = build_scene(args.workload, n=cut, packer="oracle")
     contacts = None
     if args.workload == "hertz1M_settled":
         from woo_gb300 import abi
@@ -520,35 +639,11 @@ def cpu_baseline(args, full_n):
         return {"value": psteps / total, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                 "sample": f"{len(sample)} of the scenes (seeded) run one after another, each for ~{args.cpu_seconds / len(sample):.1f} s "
                           f"after 2 untimed steps, OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, "
-                          f"{threads} threads"}
-    o = bridge.Oracle(spec.params, spec.particles, contacts=contacts, canonical=False, variant="liborc_omp.so",
-                      cell=getattr(spec, "cell", None))
-    o.set_parallel(True)
-    o.step(2)  # initial sort + first contacts, not timed
-    steps, total = 0, 0.0
-    k = 10
-    while total < args.cpu_seconds and steps < 100000:
-        total += o.step_timed(k)
-        steps += k
-        k = min(k * 2, 2000)
-    n = spec.particles.n
-    return {"value": n * steps / total, "unit": "particle-steps/s", "cores": o.threads(), "kind": "port",
-            "sample": f"{args.workload} cut to {n} particles (same density, box scaled), {steps} steps after 2 untimed, "
-                      f"OpenMP restatement of Woo's Leapfrog/InsertionSortCollider/ContactLoop, {o.threads()} threads"}
-
-
-PROFILE_KERNEL = {"leapfrog": "k_leapfrog", "contacts": "k_contacts"}
-
-
-def read_profile_figures(path):
-    """`- name: number` lines of an ncu summary under profiles/ (per-launch figures of one capture)."""
-    figs = {}
-    with open(path) as f:
-        for line in f:
-            m = re.match(r"^- (\w+): ([0-9.eE+-]+)\s*$", line)
-            if m:
-                figs[m.group(1)] = float(m.group(2))
-    return figs
+                          f"{threads} threads"}, spec
+    cb = cpu_timed(args, spec.params, spec.particles, contacts, getattr(spec, "cell", None),
+                   f"{args.workload} cut to {spec.particles.n} particles (same density, box scaled), {{steps}} steps after 2 untimed",
+                   max_steps=100000)
+    return cb, spec
 
 
 def main():
@@ -559,11 +654,13 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        cb = cpu_baseline(args, None)
+        cb, spec = cpu_baseline(args)
         out = {"metric": f"{METRIC} ({DESCR[args.workload]})",
                "value": cb["value"], "unit": cb["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                "higher_is_better": True, "impl": "reference", "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-               "data": "synthetic", "config": {"workload": args.workload},
+               "data": "synthetic (seeded random sequential addition packing)",
+               "config": common_config(args, spec) if args.workload == "hertz1M" else {"workload": args.workload,
+                                                                                      "n_particles": int(spec.particles.n)},
                "cpu_baseline": cb,
                "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
@@ -571,7 +668,7 @@ def main():
     out, spec = run_gpu(args, rank, world, local)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(args, spec.particles.n)
+            out["cpu_baseline"], _ = cpu_baseline(args)
         print(json.dumps(out))
     return 0
 

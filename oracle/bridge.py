@@ -28,6 +28,7 @@ def load(variant="liborc.so"):
         "orc_set_params": ([h, C.POINTER(abi.Params)], C.c_int),
         "orc_set_mode": ([h, C.c_int, C.c_int, C.c_int], C.c_int),
         "orc_set_parallel": ([h, C.c_int], C.c_int),
+        "orc_set_det_parallel": ([h, C.c_int], C.c_int),
         "orc_threads": ([], C.c_int),
         "orc_upload_particles": ([h, C.POINTER(abi.Particles)], C.c_int),
         "orc_upload_contacts": ([h, C.POINTER(abi.Contacts)], C.c_int),
@@ -52,6 +53,11 @@ def load(variant="liborc.so"):
         "orc_stress": ([h, abi.D], C.c_int),
         "orc_collide_boxes": ([C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, C.c_int, abi.I32, C.c_long], C.c_long),
         "orc_collide_frames": ([C.c_int, C.c_int, abi.D, abi.D, abi.U32, C.c_uint32, abi.I32, C.c_long], C.c_long),
+        "orc_make_cloud": ([abi.D, abi.D, C.c_double, C.c_double, C.c_int64, C.c_uint64, C.c_int32, abi.D, abi.D],
+                           C.c_int64),
+        "orc_make_cloud_radii": ([abi.D, abi.D, C.c_int32, C.c_int64, abi.D, C.c_uint64, C.c_int32, abi.D, abi.D],
+                                 C.c_int64),
+        "orc_sort_passes": ([h], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -64,7 +70,12 @@ def load(variant="liborc.so"):
 class Oracle:
     """One CPU restatement of Woo's DEM scene (Leapfrog, InsertionSortCollider, ContactLoop)."""
 
-    def __init__(self, params, particles, contacts=None, canonical=True, sort_axis=0, variant="liborc.so", cell=None):
+    def __init__(self, params, particles, contacts=None, canonical=True, sort_axis=0, variant="liborc.so", cell=None,
+                 threads=False):
+        """threads=True: the OpenMP build with loops that give the serial results bit for bit (canonical
+        runs only), for the long parity runs."""
+        if threads:
+            variant = "liborc_omp.so"
         self.lib = load(variant)
         self.h = self.lib.orc_create()
         self._params = params
@@ -79,6 +90,10 @@ class Oracle:
             cs = contacts.struct()
             self.check(self.lib.orc_upload_contacts(self.h, C.byref(cs)))
         self.n = particles.n
+        if threads:
+            if not canonical:
+                raise ValueError("threads=True reproduces the canonical serial oracle only")
+            self.check(self.lib.orc_set_det_parallel(self.h, 1))
 
     def check(self, rc):
         if rc != 0:
@@ -98,6 +113,10 @@ class Oracle:
 
     def threads(self):
         return self.lib.orc_threads()
+
+    def sort_passes(self):
+        """Passes of the last parallel insertion sort (OpenMP build)."""
+        return self.lib.orc_sort_passes(self.h)
 
     def step(self, n=1):
         self.check(self.lib.orc_step(self.h, int(n)))
@@ -204,3 +223,35 @@ def collide_frames(mins, maxs, mask, lone_mask):
     lib.orc_collide_frames(n, nf, abi.ptr(mins, C.c_double), abi.ptr(maxs, C.c_double), abi.ptr(mask, C.c_uint32),
                            lone_mask, abi.ptr(pairs, C.c_int32), cnt)
     return pairs[:cnt]
+
+
+def make_cloud(lo, hi, rmin, rmax, n, seed, max_attempts=200, variant="liborc.so"):
+    """The benchmark's seeded sphere cloud built by the oracle's restatement of the engine's generator
+    (identical arrays to woo_gb300.abi.make_cloud); returns (centers (k,3), radii (k,))."""
+    lib = load(variant)
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    centers = np.zeros((n, 3))
+    radii = np.zeros(n)
+    k = lib.orc_make_cloud(abi.ptr(lo, C.c_double), abi.ptr(hi, C.c_double), float(rmin), float(rmax), int(n),
+                           int(seed), int(max_attempts), abi.ptr(centers, C.c_double), abi.ptr(radii, C.c_double))
+    if k < 0:
+        raise RuntimeError("orc_make_cloud: bad arguments")
+    return centers[:k].copy(), radii[:k].copy()
+
+
+def make_cloud_radii(lo, hi, radii_in, seed, periodic=False, max_attempts=200, variant="liborc.so"):
+    """The oracle's restatement of woo_gb300.abi.make_cloud_radii (identical arrays)."""
+    lib = load(variant)
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    rin = np.ascontiguousarray(radii_in, np.float64)
+    n = len(rin)
+    centers = np.zeros((n, 3))
+    radii = np.zeros(n)
+    k = lib.orc_make_cloud_radii(abi.ptr(lo, C.c_double), abi.ptr(hi, C.c_double), 1 if periodic else 0, n,
+                                 abi.ptr(rin, C.c_double), int(seed), int(max_attempts), abi.ptr(centers, C.c_double),
+                                 abi.ptr(radii, C.c_double))
+    if k < 0:
+        raise RuntimeError("orc_make_cloud_radii: bad arguments")
+    return centers[:k].copy(), radii[:k].copy()

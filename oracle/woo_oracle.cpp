@@ -41,6 +41,7 @@
 #include <array>
 #ifdef _OPENMP
 #include <omp.h>
+#include <parallel/algorithm>
 #endif
 
 #include "../include/wdem.h"
@@ -377,6 +378,10 @@ struct Scene {
   std::vector<Bounds> BB[3];
   std::vector<double> minima, maxima;
   std::vector<CPtr> makeContacts, removeContacts;
+  /* OpenMP build: per-thread queues of the parallel insertion sort (mmakeContacts / rremoveContacts,
+   * InsertionSortCollider.hpp:95-113) */
+  std::vector<std::vector<CPtr>> makeT, removeT;
+  long sortPasses = 0;        /* passes of the last parallel insertion sort (diagnostics) */
   double verletDist = -0.05;  /* resolved on first run */
   long nFullRuns = 0;
   int sortAxis = 0;
@@ -388,6 +393,8 @@ struct Scene {
   std::string err;
   int lastRunFull = 0;
   int parallel = 0;   /* OpenMP contact/node loops with a per-particle lock (reference's OpenMP build) */
+  int detParallel = 0; /* OpenMP threads that reproduce the serial results bit for bit (long parity runs) */
+  bool anyEll = false; /* an ellipsoid among the particles */
   bool periodic = false;
   Cell cell;
   double stress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -476,14 +483,16 @@ static bool spatialOverlap(const Scene& S, int id1, int id2) {
          (mn[3 * id1 + 2] <= mx[3 * id2 + 2]) && (mx[3 * id1 + 2] >= mn[3 * id2 + 2]);
 }
 /* makeContactLater (InsertionSortCollider.hpp:106-113) */
-static void makeContactLater(Scene& S, int a, int b) {
+/* tid >= 0: the queue of that OpenMP thread (parallel insertion sort); -1: the serial queue */
+static void makeContactLater(Scene& S, int a, int b, int tid = -1) {
   CPtr C = std::make_shared<Contact>();
   if (S.canonicalOrient && S.par[a].shape == S.par[b].shape && a > b) std::swap(a, b);
   C->pA = a; C->pB = b; C->stepCreated = (int)S.step;
-  S.makeContacts.push_back(C);
+  (tid < 0 ? S.makeContacts : S.makeT[tid]).push_back(C);
 }
-/* handleBoundInversion (InsertionSortCollider.cpp:78-113) */
-static void handleBoundInversion(Scene& S, int id1, int id2, bool separating) {
+/* handleBoundInversion (InsertionSortCollider.cpp:78-113); the container is only read here (additions
+ * and removals are queued), so the OpenMP threads of the parallel sort may call it concurrently */
+static void handleBoundInversion(Scene& S, int id1, int id2, bool separating, int tid = -1) {
   bool overlap = separating ? false : spatialOverlap(S, id1, id2);
   CPtr C = findContact(S, id1, id2);
   bool hasCon = (bool)C;
@@ -491,10 +500,10 @@ static void handleBoundInversion(Scene& S, int id1, int id2, bool separating) {
   if (overlap && hasCon) return;
   if (overlap) {
     if (!mayCollide(S, S.par[id1], S.par[id2])) return;
-    makeContactLater(S, id1, id2);
+    makeContactLater(S, id1, id2, tid);
     return;
   }
-  if (!C->isReal()) S.removeContacts.push_back(C);
+  if (!C->isReal()) (tid < 0 ? S.removeContacts : S.removeT[tid]).push_back(C);
 }
 /* insertionSort_part, serial form (InsertionSortCollider.cpp:189-223) */
 static void insertionSort(Scene& S, std::vector<Bounds>& v, bool doCollide) {
@@ -513,6 +522,66 @@ static void insertionSort(Scene& S, std::vector<Bounds>& v, bool doCollide) {
     v[j + 1] = viInit;
   }
 }
+#ifdef _OPENMP
+/* insertionSort_part (InsertionSortCollider.cpp:189-223): sort v[iBegin, iEnd) starting at iStart; when
+ * iStart > iBegin (a later pass) it stops at the first ordered couple */
+static void insertionSortPart(Scene& S, std::vector<Bounds>& v, bool doCollide, long iBegin, long iEnd, long iStart,
+                              int tid) {
+  const bool earlyStop = (iBegin != iStart);
+  for (long i = std::max(iStart, iBegin + 1); i < iEnd; i++) {
+    if (!(v[i - 1] > v[i])) {
+      if (earlyStop) return;
+      continue;
+    }
+    const Bounds viInit = v[i];
+    long j = i - 1;
+    const bool viInitBB = viInit.hasBB, viInitIsMin = viInit.isMin;
+    while (j >= iBegin && v[j] > viInit) {
+      v[j + 1] = v[j];
+      if (viInitIsMin != v[j].isMin && doCollide && viInitBB && v[j].hasBB && viInit.id != v[j].id)
+        handleBoundInversion(S, viInit.id, v[j].id, !viInitIsMin, tid);
+      j--;
+    }
+    v[j + 1] = viInit;
+  }
+}
+/* InsertionSortCollider::insertionSort, OpenMP form (InsertionSortCollider.cpp:124-186) with the default
+ * ompTuneSort = (1, 1000, 0) and maxSortPass = -100 (InsertionSortCollider.hpp:291,295): the bounds are cut
+ * into one chunk per thread (at least 2000 bounds each, rounded to a multiple of the thread count); the
+ * chunks are sorted in parallel, alternately between the split points and between the mid-chunk points,
+ * until every split point is ordered.  Inversions go to per-thread queues. */
+static void insertionSortParallel(Scene& S, std::vector<Bounds>& v, bool doCollide) {
+  const long size = (long)v.size();
+  if (size == 0) return;
+  const int TH = omp_get_max_threads();
+  const long minPerCore = 2 * 1000;
+  long chunks = TH;
+  if (size / chunks < minPerCore) chunks = TH * (long)std::ceil(std::max(1L, size / minPerCore) * 1. / TH);
+  const long chunkSize = size / chunks;
+  if (chunks == 1 || chunkSize < 100) { insertionSort(S, v, doCollide); return; }
+  std::vector<long> splits0(chunks + 1), splits1(chunks);
+  for (long i = 0; i < chunks; i++) { splits0[i] = i * chunkSize; splits1[i] = i * chunkSize + chunkSize / 2; }
+  splits0[chunks] = size;
+  const long maxPass = 100L * TH;
+  bool isOk = false;
+  long pass;
+  for (pass = 0; !isOk; pass++) {
+    if (pass == maxPass) throw std::runtime_error("InsertionSortCollider: sort not done after the maximum number of partial sort passes");
+    const bool even = (pass % 2) == 0;
+    const std::vector<long>& sp = even ? splits0 : splits1;
+    const long nch = even ? chunks : chunks - 1;
+#pragma omp parallel for schedule(static)
+    for (long chunk = 0; chunk < nch; chunk++) {
+      const long start = pass == 0 ? sp[chunk] : (even ? splits1[chunk] : splits0[chunk + 1]);
+      insertionSortPart(S, v, doCollide, sp[chunk], sp[chunk + 1], start, omp_get_thread_num());
+    }
+    isOk = true;
+    for (long chunk = even ? 1 : 0; chunk < chunks; chunk++)
+      if (v[sp[chunk] - 1] > v[sp[chunk]]) { isOk = false; break; }
+  }
+  S.sortPasses = pass;
+}
+#endif
 /* Bo1_Sphere_Aabb::go (Sphere.cpp:52-64), Bo1_Wall_Aabb::go (Wall.cpp:25-38), then the verlet
  * enlargement of AabbCollider::updateAabb (Collision.cpp:125-162) */
 /* Ellipsoid::trsfFromUnitSphere (Ellipsoid.cpp:77-82): column i = ori * (semiAxes[i] e_i) */
@@ -671,32 +740,150 @@ static void colliderPeriodicFull(Scene& S) {
     cid[i] = {c[0], c[1], c[2]};
     cells[((long)c[2] * nc[1] + c[1]) * nc[0] + c[0]].push_back(i);
   }
-  for (int i = 0; i < n; i++) {
-    std::vector<long> seen;
+  /* candidate search (read-only), then the new contacts are added in the order of the serial loop: by i,
+   * then by neighbour cell; OpenMP threads take contiguous ranges of i (each pair is met once, from its
+   * lower id, so additions made during the loop never change a later test) */
+  struct NewPair { int i, j, per[3]; };
+  auto search = [&](int i0, int i1, std::vector<NewPair>& out) {
+    for (int i = i0; i < i1; i++) {
+      std::vector<long> seen;
+      for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            int c[3] = {cid[i][0] + dx, cid[i][1] + dy, cid[i][2] + dz};
+            for (int k = 0; k < 3; k++) c[k] = ((c[k] % nc[k]) + nc[k]) % nc[k];
+            long key = ((long)c[2] * nc[1] + c[1]) * nc[0] + c[0];
+            if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+            seen.push_back(key);
+            auto it = cells.find(key);
+            if (it == cells.end()) continue;
+            for (int j : it->second) {
+              if (j <= i) continue;
+              NewPair q;
+              q.i = i; q.j = j;
+              if (!spatialOverlapPeri(S, i, j, q.per)) continue;
+              if (findContact(S, i, j)) continue;
+              if (!mayCollide(S, S.par[i], S.par[j])) continue;
+              out.push_back(q);
+            }
+          }
+    }
+  };
+  std::vector<std::vector<NewPair>> found;
+#ifdef _OPENMP
+  if (S.parallel || S.detParallel) {
+    const int T = omp_get_max_threads();
+    found.assign(T, std::vector<NewPair>());
+#pragma omp parallel num_threads(T)
+    {
+      const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+      search((int)((long)n * t / nt), (int)((long)n * (t + 1) / nt), found[t]);
+    }
+  } else
+#endif
+  {
+    found.assign(1, std::vector<NewPair>());
+    search(0, n, found[0]);
+  }
+  for (auto& part : found)
+    for (const NewPair& q : part) {
+      CPtr C = std::make_shared<Contact>();
+      C->pA = q.i; C->pB = q.j; C->stepCreated = (int)S.step;
+      for (int k = 0; k < 3; k++) C->cellDist[k] = q.per[k];
+      addMaybe_fast(S, C);
+    }
+}
+
+#ifdef _OPENMP
+/* The pairs of the initial sort's sweep (InsertionSortCollider.cpp:572-587), found through a cell grid by
+ * OpenMP threads: the timing build's replacement of the serial sweep along sortAxis, which visits every
+ * bound between a box's minimum and maximum (about 4 minutes for a million spheres on one core; it runs
+ * once, before any timed step).  The same predicate decides (handleBoundInversion: spatialOverlap,
+ * mayCollide, existing contact); a new contact's pA is the particle whose minimum along sortAxis comes
+ * first, as in the sweep.  Existing non-real contacts of boxes that meet along sortAxis but do not overlap
+ * are removed, as the sweep does. */
+static void initialPairsGrid(Scene& S) {
+  const long nP = (long)S.par.size();
+  const int ax = S.sortAxis;
+  const int TH = omp_get_max_threads();
+  S.makeT.assign(TH, std::vector<CPtr>());
+  S.removeT.assign(TH, std::vector<CPtr>());
+  const double* mn = S.minima.data();
+  const double* mx = S.maxima.data();
+  /* boxes with finite extents go into the grid; the others (walls) are tested against every box */
+  double lo[3] = {Inf, Inf, Inf}, hi[3] = {-Inf, -Inf, -Inf}, w = 0;
+  std::vector<int> grid, large;
+  std::vector<char> inGrid(nP, 0);
+  for (long i = 0; i < nP; i++) {
+    if (!S.par[i].bound.has) continue;
+    bool fin = true;
+    for (int k = 0; k < 3; k++) fin = fin && std::isfinite(mn[3 * i + k]) && std::isfinite(mx[3 * i + k]);
+    if (!fin) { large.push_back((int)i); continue; }
+    inGrid[i] = 1;
+    grid.push_back((int)i);
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], mn[3 * i + k]); hi[k] = std::max(hi[k], mx[3 * i + k]);
+      w = std::max(w, mx[3 * i + k] - mn[3 * i + k]);
+    }
+  }
+  int nc[3] = {1, 1, 1};
+  if (!grid.empty() && w > 0)
+    for (int k = 0; k < 3; k++) nc[k] = (int)std::max(1.0, std::min(1024.0, std::floor((hi[k] - lo[k]) / w)));
+  auto cellOf = [&](long i, int k) {
+    const double c = 0.5 * (mn[3 * i + k] + mx[3 * i + k]);
+    int v = (int)std::floor((c - lo[k]) / (hi[k] - lo[k]) * nc[k]);
+    return std::min(std::max(v, 0), nc[k] - 1);
+  };
+  const long ncell = (long)nc[0] * nc[1] * nc[2];
+  std::vector<long> start(ncell + 1, 0);
+  std::vector<int> cellIx(nP, -1);
+  for (int i : grid) { long c = cellOf(i, 0) + nc[0] * (cellOf(i, 1) + (long)nc[1] * cellOf(i, 2)); cellIx[i] = (int)c; start[c + 1]++; }
+  for (long c = 0; c < ncell; c++) start[c + 1] += start[c];
+  std::vector<int> members(grid.size());
+  {
+    std::vector<long> fill(start.begin(), start.end() - 1);
+    for (int i : grid) members[fill[cellIx[i]]++] = i;
+  }
+  /* the sweep's order along sortAxis: the bound with the smaller coordinate first (ties by id) */
+  auto firstOf = [&](int a, int b) { return (mn[3 * a + ax] < mn[3 * b + ax] || (mn[3 * a + ax] == mn[3 * b + ax] && a < b)); };
+  auto consider = [&](int a, int b, int tid) {
+    if (!spatialOverlap(S, a, b)) return;
+    if (findContact(S, a, b)) return;
+    if (!mayCollide(S, S.par[a], S.par[b])) return;
+    if (firstOf(a, b)) makeContactLater(S, a, b, tid); else makeContactLater(S, b, a, tid);
+  };
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (long q = 0; q < (long)grid.size(); q++) {
+    const int tid = omp_get_thread_num();
+    const int i = grid[q];
+    const int ci[3] = {cellOf(i, 0), cellOf(i, 1), cellOf(i, 2)};
     for (int dz = -1; dz <= 1; dz++)
       for (int dy = -1; dy <= 1; dy++)
         for (int dx = -1; dx <= 1; dx++) {
-          int c[3] = {cid[i][0] + dx, cid[i][1] + dy, cid[i][2] + dz};
-          for (int k = 0; k < 3; k++) c[k] = ((c[k] % nc[k]) + nc[k]) % nc[k];
-          long key = ((long)c[2] * nc[1] + c[1]) * nc[0] + c[0];
-          if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
-          seen.push_back(key);
-          auto it = cells.find(key);
-          if (it == cells.end()) continue;
-          for (int j : it->second) {
-            if (j <= i) continue;
-            int per[3];
-            if (!spatialOverlapPeri(S, i, j, per)) continue;
-            if (findContact(S, i, j)) continue;
-            if (!mayCollide(S, S.par[i], S.par[j])) continue;
-            CPtr C = std::make_shared<Contact>();
-            C->pA = i; C->pB = j; C->stepCreated = (int)S.step;
-            for (int k = 0; k < 3; k++) C->cellDist[k] = per[k];
-            addMaybe_fast(S, C);
-          }
+          const int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
+          if (cx < 0 || cy < 0 || cz < 0 || cx >= nc[0] || cy >= nc[1] || cz >= nc[2]) continue;
+          const long c = cx + nc[0] * (cy + (long)nc[1] * cz);
+          for (long m = start[c]; m < start[c + 1]; m++) if (members[m] > i) consider(i, members[m], tid);
         }
   }
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (long i = 0; i < nP; i++) {
+    if (!S.par[i].bound.has) continue;
+    for (int L : large)
+      if (L != (int)i && (inGrid[i] || L < (int)i)) consider(std::min((int)i, L), std::max((int)i, L), omp_get_thread_num());
+  }
+  /* existing non-real contacts met along sortAxis whose boxes no longer overlap */
+  const long nl = (long)S.linView.size();
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < nl; k++) {
+    const CPtr& C = S.linView[k];
+    if (C->isReal()) continue;
+    const int a = C->pA, b = C->pB;
+    const bool meet = !(mx[3 * a + ax] < mn[3 * b + ax] || mx[3 * b + ax] < mn[3 * a + ax]);
+    if (meet && !spatialOverlap(S, a, b)) S.removeT[omp_get_thread_num()].push_back(C);
+  }
 }
+#endif
 
 /* InsertionSortCollider::run, aperiodic (InsertionSortCollider.cpp:386-613) */
 static void colliderRun(Scene& S) {
@@ -712,7 +899,7 @@ static void colliderRun(Scene& S) {
     const long np = (long)S.par.size();
     int dirtyAny = 0;
 #ifdef _OPENMP
-#pragma omp parallel for reduction(| : dirtyAny) if (S.parallel)
+#pragma omp parallel for reduction(| : dirtyAny) if (S.parallel || S.detParallel)
 #endif
     for (long i = 0; i < np; i++) if (aabbIsDirty(S.par[i])) dirtyAny |= 1;
     recompute = dirtyAny != 0;
@@ -720,7 +907,7 @@ static void colliderRun(Scene& S) {
   if (recompute) {
     const long np = (long)S.par.size();
 #ifdef _OPENMP
-#pragma omp parallel for if (S.parallel)
+#pragma omp parallel for if (S.parallel || S.detParallel)
 #endif
     for (long i = 0; i < np; i++) updateAabb(S, S.par[i]);
   }
@@ -756,13 +943,20 @@ static void colliderRun(Scene& S) {
       }
   }
   S.minima.assign(3 * nPar, 0); S.maxima.assign(3 * nPar, 0);
-  /* copy bounds (:457-494) */
-  for (int j = 0; j < 3; j++)
-    for (Bounds& b : S.BB[j]) {
-      const Aabb& bv = S.par[b.id].bound;
-      b.hasBB = bv.has;
-      b.coord = b.hasBB ? (b.isMin ? bv.min[j] : bv.max[j]) : S.par[b.id].pos[j];
-    }
+  /* copy bounds (:457-494; an OpenMP loop over the bound index in the reference) */
+  {
+    const long nb = 2 * nPar;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) if (S.parallel)
+#endif
+    for (long i = 0; i < nb; i++)
+      for (int j = 0; j < 3; j++) {
+        Bounds& b = S.BB[j][i];
+        const Aabb& bv = S.par[b.id].bound;
+        b.hasBB = bv.has;
+        b.coord = b.hasBB ? (b.isMin ? bv.min[j] : bv.max[j]) : S.par[b.id].pos[j];
+      }
+  }
   /* minima/maxima (:498-506) */
   for (long id = 0; id < nPar; id++)
     for (int k = 0; k < 3; k++) {
@@ -775,9 +969,26 @@ static void colliderRun(Scene& S) {
     for (auto& pc : pend) if (pc.second || !spatialOverlap(S, pc.first->pA, pc.first->pB)) removeContact(S, pc.first);
   }
   if (!doInitSort) {
+#ifdef _OPENMP
+    if (S.parallel) {
+      const int TH = omp_get_max_threads();
+      S.makeT.assign(TH, std::vector<CPtr>());
+      S.removeT.assign(TH, std::vector<CPtr>());
+      for (int i = 0; i < 3; i++) insertionSortParallel(S, S.BB[i], true);
+    } else
+#endif
     for (int i = 0; i < 3; i++) insertionSort(S, S.BB[i], true);
   } else {
+    /* std::sort(std::execution::par, ...) or __gnu_parallel::sort in the reference's OpenMP build (:540-553) */
+#ifdef _OPENMP
+    if (S.parallel) for (int i = 0; i < 3; i++) __gnu_parallel::sort(S.BB[i].begin(), S.BB[i].end());
+    else
+#endif
     for (int i = 0; i < 3; i++) std::sort(S.BB[i].begin(), S.BB[i].end());
+#ifdef _OPENMP
+    if (S.parallel) { initialPairsGrid(S); goto process; }
+#endif
+    {
     std::vector<Bounds>& V = S.BB[S.sortAxis];
     long n2 = 2 * nPar;
     for (long i = 0; i < n2; i++) {
@@ -788,12 +999,19 @@ static void colliderRun(Scene& S) {
         handleBoundInversion(S, iid, V[j].id, false);
       }
     }
+    }
   }
-  /* makeRemoveContactLater_process (:35-63): removals first, then additions */
+#ifdef _OPENMP
+process:
+#endif
+  /* makeRemoveContactLater_process (:35-63): removals first, then additions (per-thread queues in
+   * thread order in the OpenMP build) */
   for (auto& C : S.removeContacts) removeMaybe_fast(S, C);
   S.removeContacts.clear();
+  for (auto& q : S.removeT) { for (auto& C : q) removeMaybe_fast(S, C); q.clear(); }
   for (auto& C : S.makeContacts) addMaybe_fast(S, C);
   S.makeContacts.clear();
+  for (auto& q : S.makeT) { for (auto& C : q) addMaybe_fast(S, C); q.clear(); }
 }
 
 /* ------------------------------------------------------------------ geometry */
@@ -1333,6 +1551,72 @@ static void contactLoopParallel(Scene& S) {
 }
 #endif
 
+#ifdef _OPENMP
+/* The serial loop below computed by OpenMP threads, with its results bit for bit (the long canonical
+ * parity runs): a contact's geometry, physics and law read the particles (unchanged during the loop) and
+ * write that contact only, so the contacts run in parallel and their outcomes (dropped when not colliding,
+ * removal requested by the law) are applied afterwards in container order, as the serial loop applies
+ * them; forces are then added in key order.  Not used with energy tracking (the laws add to shared
+ * accumulators) or ellipsoids (solver counters). */
+static void contactLoopDet(Scene& S) {
+  const wdem_params& P = S.P;
+  const long size = (long)S.linView.size();
+  std::vector<char> outcome(size, 0);  /* 1: removeAfter, 2: requestRemoval */
+  long errIdx = -1;
+  std::string errMsg;
+#pragma omp parallel for schedule(guided)
+  for (long i = 0; i < size; i++) {
+    const CPtr& C = S.linView[i];
+    if (!C->isReal() && !C->isColliding()) { outcome[i] = 1; continue; }
+    bool fresh = (S.step == C->stepCreated);
+    if (!C->isReal() && fresh && !freshContactSetup(S, *C)) continue;
+    Particle& pA = S.par[C->pA];
+    Particle& pB = S.par[C->pB];
+    V3 shift2 = S.periodic ? S.cell.intrShiftPos(C->cellDist) : V3();
+    if (P.dist00 && !C->isReal() && !fresh && C->minDist00Sq > 0 && sqnorm(pA.pos - (pB.pos + shift2)) > C->minDist00Sq) continue;
+    bool keep = true;
+    try {
+      if (!callGeom(S, *C, pA, pB, shift2)) continue;
+      if (!C->phys) C->stepCreated = (int)S.step;
+      if (!C->phys || S.updatePhys > WDEM_UPDATE_PHYS_NEVER) {
+        const wdem_material& m1 = S.mats[pA.mat];
+        const wdem_material& m2 = S.mats[pB.mat];
+        if (P.cp2 == WDEM_CP2_FRICT) cp2Frict(S, *C, m1, m2);
+        else {
+          if (m1.kind != WDEM_MAT_HERTZ || m2.kind != WDEM_MAT_HERTZ)
+            throw std::runtime_error("ContactLoop: ##" + std::to_string(pA.id) + "+" + std::to_string(pB.id) + ": no Contact.phys created from materials");
+          cp2Hertz(S, *C, m1, m2);
+        }
+      }
+      keep = (P.law == WDEM_LAW_IDEALELPL) ? lawIdealElPl(S, *C) : lawHertzDMT(S, *C);
+    } catch (std::exception& e) {
+#pragma omp critical
+      if (errIdx < 0 || i < errIdx) { errIdx = i; errMsg = e.what(); }
+      continue;
+    }
+    if (!keep) outcome[i] = 2;
+  }
+  if (errIdx >= 0) { S.err = errMsg; throw std::runtime_error(errMsg); }
+  std::vector<CPtr> removeAfter;
+  for (long i = 0; i < size; i++) {
+    if (outcome[i] == 1) removeAfter.push_back(S.linView[i]);
+    else if (outcome[i] == 2) requestRemoval(S, S.linView[i]);
+  }
+  for (auto& c : removeAfter) removeContact(S, c);
+  if (P.applyForces) {
+    std::vector<CPtr> real;
+    for (auto& c : S.linView) if (c->isReal()) real.push_back(c);
+    std::sort(real.begin(), real.end(), [](const CPtr& a, const CPtr& b) {
+      long ka = ((long)std::min(a->pA, a->pB) << 32) | std::max(a->pA, a->pB);
+      long kb = ((long)std::min(b->pA, b->pB) << 32) | std::max(b->pA, b->pB);
+      return ka < kb;
+    });
+    for (auto& c : real) { applyForceUninodal(S, *c, S.par[c->pA]); applyForceUninodal(S, *c, S.par[c->pB]); }
+  }
+  if (S.updatePhys == WDEM_UPDATE_PHYS_ONCE) S.updatePhys = WDEM_UPDATE_PHYS_NEVER;
+}
+#endif
+
 /* ContactLoop::run (ContactLoop.cpp:93-268), aperiodic, no hook, no stress */
 static void contactLoopRun(Scene& S) {
   const wdem_params& P = S.P;
@@ -1345,6 +1629,7 @@ static void contactLoopRun(Scene& S) {
   size_t size = S.linView.size();
 #ifdef _OPENMP
   if (S.parallel && S.applyOrder == 0) { contactLoopParallel(S); return; }
+  if (S.detParallel && S.applyOrder == 1 && !P.trackEnergy && !S.anyEll) { contactLoopDet(S); return; }
 #endif
   for (size_t i = 0; i < size; i++) {
     const CPtr C = S.linView[i];
@@ -1455,7 +1740,7 @@ static void leapfrogRun(Scene& S) {
   for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) gradVI &= (S.cell.gradV.r[i][k] == (i == k ? 1.0 : 0.0));
   const bool eTrack = P.trackEnergy && (!peri || S.step > 0 || gradVI);
 #ifdef _OPENMP
-#pragma omp parallel for schedule(guided) if (S.parallel && !eTrack)
+#pragma omp parallel for schedule(guided) if ((S.parallel || S.detParallel) && !eTrack)
 #endif
   for (long ip = 0; ip < np; ip++) {
     Particle& p = S.par[ip];
@@ -1633,6 +1918,131 @@ static void doOneStep(Scene& S) {
 /* ====================================================================== C ABI for tests */
 using namespace orc;
 
+/* ------------------------------------------------------------------ scene generator
+ * The seeded random sequential addition that builds the benchmark packings (the engine library's
+ * wdem_make_cloud / wdem_make_cloud_radii), restated so that the CPU arm of the benchmark builds the same
+ * packing without loading the engine library; tests/test_oracle_pack.py checks that both give identical
+ * arrays.  Radii (given, or drawn uniformly in [rMin, rMax] from a SplitMix64 stream) are placed largest
+ * first, each at the first of maxAttempts uniformly random centres that overlaps no placed sphere
+ * (nearest periodic image in a periodic box); candidates are found in a grid of cells at least 2 rMax wide. */
+static uint64_t packNext(uint64_t& s) {
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+static double packUniform(uint64_t& s) { return (double)(packNext(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* wdem_make_cloud: uniform radii, aperiodic box, cells of exactly 2 rMax from lo */
+static int64_t packCloud(const double* lo, const double* hi, double rMin, double rMax, int64_t n, uint64_t seed,
+                         int32_t maxAttempts, double* centers, double* radii) {
+  uint64_t rs = seed;
+  std::vector<double> r(n);
+  for (int64_t i = 0; i < n; i++) r[i] = (rMax > rMin) ? rMin + (rMax - rMin) * packUniform(rs) : rMin;
+  std::sort(r.begin(), r.end(), [](double a, double b) { return a > b; });
+  const double cell = 2 * rMax;
+  int nc[3];
+  for (int k = 0; k < 3; k++) nc[k] = std::max(1, (int)std::ceil((hi[k] - lo[k]) / cell));
+  std::vector<int64_t> head((size_t)nc[0] * nc[1] * nc[2], -1), next;
+  std::vector<double> c, rr;
+  auto cellIdx = [&](const double* x) {
+    int64_t idx[3];
+    for (int k = 0; k < 3; k++) idx[k] = std::min(std::max((int)std::floor((x[k] - lo[k]) / cell), 0), nc[k] - 1);
+    return idx[0] + nc[0] * (idx[1] + (int64_t)nc[1] * idx[2]);
+  };
+  for (int64_t i = 0; i < n; i++) {
+    const double ri = r[i];
+    double x[3];
+    bool ok = false;
+    for (int a = 0; a < maxAttempts && !ok; a++) {
+      for (int k = 0; k < 3; k++) x[k] = lo[k] + ri + (hi[k] - lo[k] - 2 * ri) * packUniform(rs);
+      int ci[3];
+      for (int k = 0; k < 3; k++) ci[k] = std::min(std::max((int)std::floor((x[k] - lo[k]) / cell), 0), nc[k] - 1);
+      ok = true;
+      for (int dz = -1; dz <= 1 && ok; dz++)
+        for (int dy = -1; dy <= 1 && ok; dy++)
+          for (int dx = -1; dx <= 1 && ok; dx++) {
+            const int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
+            if (cx < 0 || cy < 0 || cz < 0 || cx >= nc[0] || cy >= nc[1] || cz >= nc[2]) continue;
+            for (int64_t j = head[cx + nc[0] * (cy + (int64_t)nc[1] * cz)]; j >= 0; j = next[j]) {
+              const double d0 = x[0] - c[3 * j], d1 = x[1] - c[3 * j + 1], d2 = x[2] - c[3 * j + 2];
+              const double sr = ri + rr[j];
+              if (d0 * d0 + d1 * d1 + d2 * d2 < sr * sr) { ok = false; break; }
+            }
+          }
+    }
+    if (!ok) continue;
+    const int64_t ci = cellIdx(x);
+    next.push_back(head[ci]);
+    head[ci] = (int64_t)rr.size();
+    c.insert(c.end(), x, x + 3);
+    rr.push_back(ri);
+  }
+  std::copy(c.begin(), c.end(), centers);
+  std::copy(rr.begin(), rr.end(), radii);
+  return (int64_t)rr.size();
+}
+
+/* wdem_make_cloud_radii: given radii, optionally periodic; cells L/floor(L / 2 rMax) wide */
+static int64_t packCloudRadii(const double* lo, const double* hi, int periodic, int64_t n, const double* rIn,
+                              uint64_t seed, int32_t maxAttempts, double* centers, double* radii) {
+  std::vector<double> r(rIn, rIn + n);
+  for (double v : r) if (!(v > 0)) return WDEM_ERR_ARG;
+  std::sort(r.begin(), r.end(), [](double a, double b) { return a > b; });
+  uint64_t rs = seed;
+  const double cell = 2 * (n > 0 ? r[0] : 1.0);
+  double L[3];
+  int nc[3];
+  for (int k = 0; k < 3; k++) { L[k] = hi[k] - lo[k]; nc[k] = std::max(1, (int)std::floor(L[k] / cell)); }
+  std::vector<int64_t> head((size_t)nc[0] * nc[1] * nc[2], -1), next;
+  std::vector<double> c, rr;
+  auto cellOf = [&](const double* x, int* ci) {
+    for (int k = 0; k < 3; k++) ci[k] = std::min(std::max((int)std::floor((x[k] - lo[k]) / L[k] * nc[k]), 0), nc[k] - 1);
+  };
+  for (int64_t i = 0; i < n; i++) {
+    const double ri = r[i];
+    double x[3];
+    bool ok = false;
+    for (int a = 0; a < maxAttempts && !ok; a++) {
+      for (int k = 0; k < 3; k++)
+        x[k] = periodic ? lo[k] + L[k] * packUniform(rs) : lo[k] + ri + (L[k] - 2 * ri) * packUniform(rs);
+      int ci[3];
+      cellOf(x, ci);
+      ok = true;
+      int span[3];
+      for (int k = 0; k < 3; k++) span[k] = nc[k] >= 2 ? 1 : 0;
+      for (int dz = -span[2]; dz <= span[2] && ok; dz++)
+        for (int dy = -span[1]; dy <= span[1] && ok; dy++)
+          for (int dx = -span[0]; dx <= span[0] && ok; dx++) {
+            if (periodic && ((nc[0] == 2 && dx == 1) || (nc[1] == 2 && dy == 1) || (nc[2] == 2 && dz == 1))) continue;
+            int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
+            if (periodic) { cx = (cx + nc[0]) % nc[0]; cy = (cy + nc[1]) % nc[1]; cz = (cz + nc[2]) % nc[2]; }
+            else if (cx < 0 || cy < 0 || cz < 0 || cx >= nc[0] || cy >= nc[1] || cz >= nc[2]) continue;
+            for (int64_t j = head[cx + nc[0] * (cy + (int64_t)nc[1] * cz)]; j >= 0; j = next[j]) {
+              double d[3];
+              for (int k = 0; k < 3; k++) {
+                d[k] = x[k] - c[3 * j + k];
+                if (periodic) d[k] -= L[k] * std::nearbyint(d[k] / L[k]);
+              }
+              const double sr = ri + rr[j];
+              if (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] < sr * sr) { ok = false; break; }
+            }
+          }
+    }
+    if (!ok) continue;
+    int ci[3];
+    cellOf(x, ci);
+    const int64_t cidx = ci[0] + nc[0] * (ci[1] + (int64_t)nc[1] * ci[2]);
+    next.push_back(head[cidx]);
+    head[cidx] = (int64_t)rr.size();
+    c.insert(c.end(), x, x + 3);
+    rr.push_back(ri);
+  }
+  std::copy(c.begin(), c.end(), centers);
+  std::copy(rr.begin(), rr.end(), radii);
+  return (int64_t)rr.size();
+}
+
 struct orc_handle { Scene S; };
 
 extern "C" {
@@ -1661,6 +2071,17 @@ int orc_set_parallel(orc_handle* h, int on) {
   for (auto& l : S.locks) omp_init_lock(&l);
   S.parallel = on;
   if (on) S.applyOrder = 0;
+  return 0;
+#else
+  (void)h; (void)on;
+  return -1;
+#endif
+}
+
+/* Deterministic OpenMP loops (liborc_omp.so only): the serial oracle's results bit for bit, canonical mode. */
+int orc_set_det_parallel(orc_handle* h, int on) {
+#ifdef _OPENMP
+  h->S.detParallel = on;
   return 0;
 #else
   (void)h; (void)on;
@@ -1713,6 +2134,8 @@ int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
   for (int i = 0; i < 3; i++) S.BB[i].clear();
   S.dirty = true;
   S.verletDist = S.P.verletDist;
+  S.anyEll = false;
+  for (const Particle& q : S.par) if (q.shape == WDEM_SHAPE_ELLIPSOID) S.anyEll = true;
   return 0;
 }
 
@@ -1832,6 +2255,19 @@ int orc_get_energy(orc_handle* h, double* e, int n) {
 int orc_reset_energy(orc_handle* h) { for (int i = 0; i < WDEM_E_COUNT; i++) h->S.E.v[i] = 0; return 0; }
 
 long orc_nfullruns(orc_handle* h) { return h->S.nFullRuns; }
+int64_t orc_make_cloud(const double* lo, const double* hi, double rMin, double rMax, int64_t n, uint64_t seed,
+                       int32_t maxAttempts, double* centers, double* radii) {
+  if (!lo || !hi || !centers || !radii || n < 0 || rMin <= 0 || rMax < rMin) return WDEM_ERR_ARG;
+  return packCloud(lo, hi, rMin, rMax, n, seed, maxAttempts, centers, radii);
+}
+int64_t orc_make_cloud_radii(const double* lo, const double* hi, int32_t periodic, int64_t n, const double* rIn,
+                             uint64_t seed, int32_t maxAttempts, double* centers, double* radii) {
+  if (!lo || !hi || !rIn || !centers || !radii || n < 0) return WDEM_ERR_ARG;
+  return packCloudRadii(lo, hi, periodic, n, rIn, seed, maxAttempts, centers, radii);
+}
+
+int orc_sort_passes(orc_handle* h) { return (int)h->S.sortPasses; }
+
 /* ellipsoid functor statistics: solves and contact-function evaluations so far */
 int orc_ell_stats(orc_handle* h, long* solves, long* evals) { *solves = h->S.ellSolves; *evals = h->S.ellEvals; return 0; }
 double orc_verlet_dist(orc_handle* h) { return h->S.verletDist; }

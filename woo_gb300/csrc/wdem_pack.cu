@@ -110,8 +110,7 @@ extern "C" int64_t wdem_make_cloud_radii(const double* lo, const double* hi, int
   int nc[3];
   for (int k = 0; k < 3; k++) {
     L[k] = hi[k] - lo[k];
-    nc[k] = std::max(1, (int)std::floor(L[k] / cell));  // periodic: cells at least 2 rMax wide
-    if (!periodic) nc[k] = std::max(1, (int)std::ceil(L[k] / cell));
+    nc[k] = std::max(1, (int)std::floor(L[k] / cell));  // cells at least 2 rMax wide
   }
   const int64_t ncells = (int64_t)nc[0] * nc[1] * nc[2];
   std::vector<int64_t> head(ncells, -1), next;
@@ -141,9 +140,10 @@ extern "C" int64_t wdem_make_cloud_radii(const double* lo, const double* hi, int
       for (int dz = -span[2]; dz <= span[2] && ok; dz++)
         for (int dy = -span[1]; dy <= span[1] && ok; dy++)
           for (int dx = -span[0]; dx <= span[0] && ok; dx++) {
-            if (nc[0] == 2 && dx == 1) continue;  // two cells: -1 and +1 are the same neighbour
-            if (nc[1] == 2 && dy == 1) continue;
-            if (nc[2] == 2 && dz == 1) continue;
+            // periodic with two cells: -1 and +1 are the same neighbour
+            if (periodic && nc[0] == 2 && dx == 1) continue;
+            if (periodic && nc[1] == 2 && dy == 1) continue;
+            if (periodic && nc[2] == 2 && dz == 1) continue;
             int cx = ci[0] + dx, cy = ci[1] + dy, cz = ci[2] + dz;
             if (periodic) {
               cx = (cx + nc[0]) % nc[0]; cy = (cy + nc[1]) % nc[1]; cz = (cz + nc[2]) % nc[2];

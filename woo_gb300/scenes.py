@@ -21,6 +21,26 @@ from ctypes import c_double as C_double
 
 from . import abi
 
+# The seeded packing generator the builders call: the engine library's (wdem_make_cloud,
+# wdem_make_cloud_radii) unless set_packer installs another implementation of the same algorithm.
+_PACKER = {"cloud": None, "cloud_radii": None}
+
+
+def set_packer(cloud=None, cloud_radii=None):
+    """Install the functions that build the seeded packings (same signatures as abi.make_cloud and
+    abi.make_cloud_radii); None restores the engine library's."""
+    _PACKER["cloud"] = cloud
+    _PACKER["cloud_radii"] = cloud_radii
+
+
+def make_cloud(*a, **kw):
+    return (_PACKER["cloud"] or abi.make_cloud)(*a, **kw)
+
+
+def make_cloud_radii(*a, **kw):
+    return (_PACKER["cloud_radii"] or abi.make_cloud_radii)(*a, **kw)
+
+
 # DemField defaults (src/dem/Particle.hpp:334-361)
 DEFAULT_MOVABLE_MASK = 0b0101
 DEFAULT_BOUNDARY_MASK = 0b0011
@@ -172,7 +192,7 @@ def spheres10k(n=10000, seed=1):
     """10k monodisperse FrictMat spheres in a walled 0.5 x 0.5 x 1.0 m box (IdealElPl)."""
     mats_py = [dict(kind=abi.MAT_FRICT, density=3000.0, young=1e7, ktDivKn=0.2, tanPhi=0.5)]
     lo, hi = np.array([0.0, 0.0, 0.0]), np.array([0.5, 0.5, 1.0])
-    centers, radii = abi.make_cloud(lo, hi, 0.005, 0.005, n, seed)
+    centers, radii = make_cloud(lo, hi, 0.005, 0.005, n, seed)
     mats = materials_array(mats_py)
     pa = assemble(centers, radii, 0, box_walls(lo, hi), mats_py)
     dt = 0.4 * pwave_dt(radii, np.zeros(len(radii), int), mats_py)
@@ -191,7 +211,7 @@ def hertz1M(n=1_000_000, seed=2, height=1.12, prefall=0.0):
                dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.01)]
     sc = (n / 1e6) ** (1.0 / 3.0)
     lo, hi = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 2.0]) * sc
-    centers, radii = abi.make_cloud(lo, np.array([1.0, 1.0, height]) * sc, 0.002, 0.006, n, seed, max_attempts=400)
+    centers, radii = make_cloud(lo, np.array([1.0, 1.0, height]) * sc, 0.002, 0.006, n, seed, max_attempts=400)
     k = len(radii)
     mat_idx = (np.arange(k) % 2).astype(np.int32)
     mats = materials_array(mats_py)
@@ -212,7 +232,7 @@ def random_cloud(n, seed, box=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="fric
     velocities, optional box walls, FrictMat/IdealElPl or HertzMat/DMT."""
     rng = np.random.default_rng(seed)
     lo, hi = np.zeros(3), np.asarray(box, np.float64)
-    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed)
+    centers, radii = make_cloud(lo, hi, rmin, rmax, n, seed)
     if dense != 1.0:
         c = hi / 2
         centers = c + (centers - c) * dense
@@ -249,7 +269,7 @@ def periodic_cloud(n, seed, size=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="f
     `rate` (1/s) of x along z.  No gravity, as usual for a cell."""
     rng = np.random.default_rng(seed)
     lo, hi = np.zeros(3), np.asarray(size, np.float64)
-    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed)
+    centers, radii = make_cloud(lo, hi, rmin, rmax, n, seed)
     centers = centers * dense
     k = len(radii)
     L = hi * dense - tuck * rmin
@@ -356,7 +376,7 @@ def ellipsoid_cloud(n, seed, box=(0.1, 0.1, 0.1), amin=0.004, amax=0.006, ratios
     `sphere_frac` of the bodies are spheres of radius a instead (sphere + ellipsoid contacts)."""
     rng = np.random.default_rng(seed)
     lo, hi = np.zeros(3), np.asarray(box, np.float64)
-    centers, a = abi.make_cloud(lo, hi, amin, amax, n, seed)
+    centers, a = make_cloud(lo, hi, amin, amax, n, seed)
     if dense != 1.0:
         c = hi / 2
         centers = c + (centers - c) * dense
@@ -396,7 +416,7 @@ def oedometric_scene(n, seed, young, tanPhi, rmin=0.001, rmax=0.003, density=260
     vol = n * (4.0 / 3.0) * math.pi * ((rmax ** 4 - rmin ** 4) / (4 * (rmax - rmin))) / 0.3
     L = (vol / 2.0) ** (1.0 / 3.0)
     lo, hi = np.zeros(3), np.array([L, L, 2 * L])
-    centers, radii = abi.make_cloud(lo, hi, rmin, rmax, n, seed, max_attempts=400)
+    centers, radii = make_cloud(lo, hi, rmin, rmax, n, seed, max_attempts=400)
     if dense != 1.0:
         # squeezed towards the box centre: overlaps from the start (dense < 1)
         c = hi / 2
@@ -455,6 +475,35 @@ def batch_oedometric(n_scenes, seed, nmin=500, nmax=20000, spacing=None, verletD
     spec.keep = dt_arr
     spec.scene_parts = parts
     return spec
+
+
+def copy_params(p):
+    """An independent copy of an abi.Params."""
+    q = abi.Params()
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(p))
+    return q
+
+
+def settle(h, spec, tail_steps=3000):
+    """Settle a falling cloud on the GPU handle h (untimed preparation of a packed state): gravity x 10 and
+    non-viscous damping 0.5 for as long as a free fall of half the cloud height takes, then `tail_steps`
+    steps at 1 g with damping 0.5; the scene's parameters are restored afterwards (Scene.step kept).
+    Returns the number of steps run."""
+    p = copy_params(spec.params)
+    dt = spec.params.dt
+    height = spec.info.get("height", 1.0)
+    g = abs(spec.params.gravity[2])
+    fall = int(math.sqrt(2 * 0.5 * height / (10 * g)) / dt)
+    for mult, steps in ((10.0, fall), (1.0, tail_steps)):
+        p.gravity[2] = spec.params.gravity[2] * mult
+        p.damping = 0.5
+        p.step = h.status().step
+        h.set_params(p)
+        h.step(steps)
+    q = copy_params(spec.params)
+    q.step = h.status().step
+    h.set_params(q)
+    return fall + tail_steps
 
 
 def single_from_batch(spec, k):
@@ -559,7 +608,7 @@ def peri_shear(n=8_000_000, seed=5, phi=0.3, rate=1.0, young=1e8, tanPhi=0.5, de
     r = np.clip(np.exp(rng.normal(math.log(1e-3), 0.25, n)), 0.5e-3, 2e-3)
     vol = float(np.sum((4.0 / 3.0) * math.pi * r ** 3)) / phi
     L = vol ** (1.0 / 3.0)
-    centers, radii = abi.make_cloud_radii(np.zeros(3), np.array([L, L, L]), r, seed, periodic=True, max_attempts=100)
+    centers, radii = make_cloud_radii(np.zeros(3), np.array([L, L, L]), r, seed, periodic=True, max_attempts=100)
     k = len(radii)
     mats_py = [dict(kind=abi.MAT_FRICT, density=density, young=young, ktDivKn=0.2, tanPhi=tanPhi)]
     mats = materials_array(mats_py)
