@@ -526,7 +526,7 @@ def run_gpu(args, rank, world, local):
                                "how": "10 g and damping 0.5 while the cloud falls half its height, then 3000 steps at 1 g"}
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             # the CPU port on this same settled state: particles and contacts (with history) handed over
-            pa = hs.download_particles(abi.ParticleArrays(n))
+            pa = hs.download_particles(spec.particles.copy())   # dynamic state over the static arrays
             ca = hs.download_contacts()
             sp = copy_params(spec.params)
             sp.step = hs.status().step
@@ -608,7 +608,7 @@ def cpu_baseline(args):
         from woo_gb300 import abi
         h = new_handle(spec, 0)
         settle(h, spec)
-        pa = h.download_particles(abi.ParticleArrays(spec.particles.n))
+        pa = h.download_particles(spec.particles.copy())
         contacts = h.download_contacts()
         spec.params.step = h.status().step
         h.close()
