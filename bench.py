@@ -79,6 +79,9 @@ def parse():
     ap.add_argument("--n", type=int, default=None,
                     help="particle count of a smaller cut of the workload (same density; for profiling runs)")
     ap.add_argument("--no-settled", action="store_true", help="hertz1M: leave out the settled-state object")
+    ap.add_argument("--arith", default="fma", choices=["fma", "exact"],
+                    help="arithmetic of the contact and integrator kernels (wdem_params.arith): FP64 with FMA "
+                         "contraction, or the reference's IEEE operations bit for bit")
     ap.add_argument("--profile-region", default="main", choices=["main", "settled", "none"],
                     help="timed region bracketed by cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     a = ap.parse_args()
@@ -449,6 +452,7 @@ def run_gpu(args, rank, world, local):
 
     wbuild.build()
     spec = build_scene(args.workload, n=args.n)
+    spec.params.arith = abi.ARITH_FMA if args.arith == "fma" else abi.ARITH_EXACT
     n = spec.particles.n
     extra = {}
     if args.workload == "ell200k":
@@ -524,6 +528,17 @@ def run_gpu(args, rank, world, local):
         settled = measure_region(hs, spec, args, world, local, barrier, "settled")
         settled["settling"] = {"steps": nsettle, "seconds": settle_s,
                                "how": "10 g and damping 0.5 while the cloud falls half its height, then 3000 steps at 1 g"}
+        if args.arith == "fma":
+            # the same settled run continued with the exact variant (the reference's operations bit for bit)
+            pe = copy_params(spec.params)
+            pe.arith = abi.ARITH_EXACT
+            pe.step = hs.status().step
+            hs.set_params(pe)
+            ex = measure_region(hs, spec, args, world, local, barrier, "settled_exact")
+            settled["exact_arith"] = {k: ex[k] for k in ("value", "ms_per_step", "contacts", "kernels")}
+            pf = copy_params(spec.params)
+            pf.step = hs.status().step
+            hs.set_params(pf)
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             # the CPU port on this same settled state: particles and contacts (with history) handed over
             pa = hs.download_particles(spec.particles.copy())   # dynamic state over the static arrays
@@ -545,7 +560,7 @@ def run_gpu(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random sequential addition packing)",
         "config": common_config(args, spec),
-        "engine": {"parallelism": f"replicas x{world}",
+        "engine": {"parallelism": f"replicas x{world}", "arith": args.arith,
                    "queue_depth": 32 if args.queue_depth is None else args.queue_depth,
                    "steps_simulated_before_warmup": settled_steps},
         "gpu_launches": main["gpu_launches"],

@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libwdem.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # error codes
 WDEM_OK = 0
@@ -31,6 +31,7 @@ WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
 WARM_COLD, WARM_MLP, WARM_HISTORY = 0, 1, 2
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
+ARITH_EXACT, ARITH_FMA = 0, 1
 LAW_IDEALELPL, LAW_HERTZ_DMT = 0, 1
 UPDATE_PHYS_NEVER, UPDATE_PHYS_ALWAYS, UPDATE_PHYS_ONCE = 0, 1, 2
 
@@ -71,7 +72,7 @@ class Params(C.Structure):
                 ("ellSolver", C.c_int32), ("brentBits", C.c_int32), ("newtonTol", C.c_double),
                 ("warmStart", C.c_int32), ("fallbackIters", C.c_int32), ("materialDt", C.POINTER(C.c_double)),
                 ("dynDtPeriod", C.c_int32), ("_pad3", C.c_int32), ("dynDtMaxRelInc", C.c_double),
-                ("dtSafety", C.c_double)]
+                ("dtSafety", C.c_double), ("arith", C.c_int32), ("_pad4", C.c_int32)]
 
 
 class Particles(C.Structure):

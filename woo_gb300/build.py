@@ -3,6 +3,8 @@
 The library holds the CUDA kernels and the C++ host runtime behind the C ABI of include/wdem.h.
 Each translation unit compiles in parallel; FP64 arithmetic is kept IEEE-exact (no FMA contraction
 on the device or the host) so that per-contact results reproduce the CPU restatement bit for bit.
+The contact and integrator kernels are compiled a second time with WDEM_FMA and FMA contraction (the
+contracted variant, selected per handle by wdem_params.arith).
 """
 import os
 import shutil
@@ -17,6 +19,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwdem.so")
 
 SOURCES = ["k_contact.cu", "k_leapfrog.cu", "k_collider.cu", "wdem_api.cu", "wdem_pack.cu", "k_noalloc.cu", "k_mlp.cu"]
+# (source, object name, extra flags): the contracted variant of the step kernels
+VARIANTS = [("k_contact.cu", "k_contact_fma", ["-DWDEM_FMA", "--fmad=true"]),
+            ("k_leapfrog.cu", "k_leapfrog_fma", ["-DWDEM_FMA", "--fmad=true"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2", "-Xcompiler", "-Wno-deprecated-declarations"]
@@ -29,9 +34,11 @@ def nvcc():
     return exe
 
 
-def _compile(src, verbose):
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *FLAGS, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(unit, verbose):
+    src, name, extra = unit
+    obj = os.path.join(BUILD, name + ".o")
+    flags = [f for f in FLAGS if not (extra and f == "--fmad=false")]
+    cmd = [nvcc(), *ARCH, *flags, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -53,8 +60,9 @@ def build(force=False, verbose=False):
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    units = [(s, os.path.splitext(s)[0], []) for s in SOURCES] + VARIANTS
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        results = list(ex.map(lambda u: _compile(u, verbose), units))
     if verbose:
         for _, log in results:
             sys.stderr.write(log)

@@ -585,35 +585,59 @@ void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned lo
 // created in this step (InsertionSortCollider.hpp:106-113 stepCreated=scene->step).  A contact that
 // the law broke in the previous step (pending) becomes potential: removePending in a full run keeps
 // it only when its new boxes overlap, which holds for every pair the sweep emitted.
-__global__ void k_carry(Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
-                        const unsigned* hv, unsigned long long cap, long long step, int nHist) {
+// Compaction: the pairs that were real contacts before the rebuild go to the front of the new container,
+// in emission order (the role of ContactLoop's reorderContacts, ContactLoop.cpp:75-91), so that the real
+// contacts the contact pass and the force gather touch every step are dense in every per-contact array.
+// Pass 1 finds each new pair's old index (or none) and flags the real ones; after a scan of the flags,
+// pass 2 writes each contact at its place: real ones at their rank, the others after them in order.
+__global__ void k_part_flag(Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
+                            unsigned long long cap, unsigned long long* tmpIds, unsigned* tmpJ, unsigned* flag,
+                            int4* tmpDist) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nNew) return;
-  int2 id = neu.ids[c];
-  long long j = hashFind(hk, hv, cap, pairKey(id.x, id.y));
-  uint8_t st = CS_POTENTIAL;
+  const int2 id = neu.ids[c];
+  tmpIds[c] = ((unsigned long long)(unsigned)id.y << 32) | (unsigned)id.x;
+  if (tmpDist) tmpDist[c] = neu.cdist[c];
+  const long long j = hashFind(hk, hv, cap, pairKey(id.x, id.y));
+  unsigned jj = 0xffffffffu, f = 0;
   if (j >= 0) {
-    uint8_t os = old.state[j] & CS_MASK;
-    if (os == CS_DEAD) j = -1;
-    else st = (os == CS_REAL) ? CS_REAL : CS_POTENTIAL;
+    const uint8_t os = old.state[j] & CS_MASK;
+    if (os != CS_DEAD) { jj = (unsigned)j; f = (os == CS_REAL) ? 1u : 0u; }
   }
-  if (j < 0) {
+  tmpJ[c] = jj;
+  flag[c] = f;
+}
+__global__ void k_carry_compact(Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* tmpIds,
+                                const unsigned* tmpJ, const unsigned* scan, const int4* tmpDist, long long step, int nHist) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nNew) return;
+  const unsigned before = scan[c];
+  const bool wasReal = scan[c + 1] != before;
+  const long long d = wasReal ? (long long)before : (long long)scan[nNew] + (c - (long long)before);
+  const unsigned long long t = tmpIds[c];
+  const int2 id = make_int2((int)(unsigned)(t & 0xffffffffu), (int)(unsigned)(t >> 32));
+  const unsigned jj = tmpJ[c];
+  if (jj == 0xffffffffu) {
     const int sa = p.meta[id.x].x & 15, sbb = p.meta[id.y].x & 15;
     const uint8_t sb = (uint8_t)((sa == WDEM_SHAPE_WALL ? CS_WALL_A : 0) | (sbb == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
                                  (sa == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (sbb == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
-    neu.state[c] = CS_POTENTIAL | sb;
-    neu.step0[c] = (int)step;
-    if (neu.lam) neu.lam[c] = __longlong_as_double(0x7ff8000000000000ll);
+    neu.ids[d] = id;
+    if (neu.cdist) neu.cdist[d] = tmpDist[c];
+    neu.state[d] = CS_POTENTIAL | sb;
+    neu.step0[d] = (int)step;
+    if (neu.lam) neu.lam[d] = __longlong_as_double(0x7ff8000000000000ll);
     return;
   }
-  if (neu.lam && old.lam) neu.lam[c] = old.lam[j];
-  neu.ids[c] = old.ids[j];  // keep the stored orientation (and, periodic, the stored cellDist)
-  if (neu.cdist && old.cdist) neu.cdist[c] = old.cdist[j];
-  neu.state[c] = st | (old.state[j] & CS_SHAPES);
-  neu.step0[c] = old.step0[j];
-  if (st == CS_REAL) {
-    for (int h = 0; h < nHist; h++) neu.hist[h][c] = old.hist[h][j];
-    neu.tanPhi[c] = old.tanPhi[j];
+  const long long j = jj;
+  if (neu.lam && old.lam) neu.lam[d] = old.lam[j];
+  else if (neu.lam) neu.lam[d] = __longlong_as_double(0x7ff8000000000000ll);
+  neu.ids[d] = old.ids[j];  // keep the stored orientation (and, periodic, the stored cellDist)
+  if (neu.cdist) neu.cdist[d] = old.cdist ? old.cdist[j] : tmpDist[c];
+  neu.state[d] = (wasReal ? CS_REAL : CS_POTENTIAL) | (old.state[j] & CS_SHAPES);
+  neu.step0[d] = old.step0[j];
+  if (wasReal) {
+    for (int h = 0; h < nHist; h++) neu.hist[h][d] = old.hist[h][j];
+    neu.tanPhi[d] = old.tanPhi[j];
   }
 }
 
@@ -938,9 +962,19 @@ void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c,
   for (int q = 0; q < 9; q++) energy_accumulate(s, scratch9 + (long long)q * nc, nc, partials, out9 + q, true);
 }
 
-void col_carry(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
-               const unsigned* hv, unsigned long long cap, long long step, int nHist) {
-  if (nNew > 0) (k_carry<<<(unsigned)((nNew + 255) / 256), 256, 0, s>>>(p, neu, nNew, old, hk, hv, cap, step, nHist), ++::wdem::g_kernel_launches);
+long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old,
+                            const unsigned long long* hk, const unsigned* hv, unsigned long long cap, long long step,
+                            int nHist, ColliderScratch& cs) {
+  if (nNew <= 0) return 0;
+  unsigned long long* tmpIds = cs.keys;
+  unsigned* tmpJ = cs.vals;
+  unsigned* flag = cs.valsAlt;
+  int4* tmpDist = neu.cdist ? reinterpret_cast<int4*>(cs.keysAlt) : nullptr;
+  const unsigned blocks = (unsigned)((nNew + 255) / 256);
+  (k_part_flag<<<blocks, 256, 0, s>>>(neu, nNew, old, hk, hv, cap, tmpIds, tmpJ, flag, tmpDist), ++::wdem::g_kernel_launches);
+  exclusive_scan_u32(s, flag, nNew, cs);
+  (k_carry_compact<<<blocks, 256, 0, s>>>(p, neu, nNew, old, tmpIds, tmpJ, flag, tmpDist, step, nHist), ++::wdem::g_kernel_launches);
+  return nNew;
 }
 
 void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs) {

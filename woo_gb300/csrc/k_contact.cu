@@ -15,12 +15,14 @@
 #include <algorithm>
 
 #include "wdem_internal.h"
+#include "wdem_variant.h"
 #include "wdem_math.cuh"
 #include "wdem_peri.cuh"
 #include "wdem_ell.cuh"
 #include "../../include/wdem.h"
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 __constant__ DevMaterial c_mats[MAX_MATERIALS];
 
@@ -243,9 +245,10 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     r1 = A4.w; r2 = B4.w;
     d3 relPos = pos2 - pos1;
     double t = fabs(P.distFactor) * (r1 + r2);
-    double unDistSq = sqnorm(relPos) - t * t;
+    const double relSq = sqnormExact(relPos);
+    double unDistSq = __dsub_rn(relSq, __dmul_rn(t, t));
     if (positiveBits(unDistSq) && !real) return;
-    double dist = sqrt(sqnorm(relPos));
+    double dist = sqrt(relSq);
     uN = dist - (r1 + r2);
     normal = relPos / dist;
     contPt = pos1 + (r1 + 0.5 * uN) * normal;
@@ -670,9 +673,11 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   }
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // HertzPhys constants (kn0, kt0, alpha_sqrtMK, adhesion) of uploaded real contacts: Woo stores them
 // in HertzPhys (Hertz.hpp:16-31); they are pure functions of the materials, radii and masses.
@@ -693,4 +698,5 @@ void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Cont
   (k_init_uploaded<<<(unsigned)((nc + 127) / 128), 128, 0, s>>>(P, p, c, nc), ++::wdem::g_kernel_launches);
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem

@@ -9,10 +9,12 @@
 #include <algorithm>
 
 #include "wdem_internal.h"
+#include "wdem_variant.h"
 #include "wdem_math.cuh"
 #include "../../include/wdem.h"
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // F = m g (unless gravitySkip) + sum of contact forces; T = sum of contact torques
 __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double mass, unsigned flags, const Contacts& c,
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   d3 linAccelE = mk(0, 0, 0), angAccelE = mk(0, 0, 0);
   if (!blockedAll) {
     d3 linAccel;
-    if (blockedNone) linAccel = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
+    if (blockedNone) linAccel = divBy(F, mass);
     else {
       linAccel = mk(0, 0, 0);
       if (!(flags & 1u)) linAccel.x = linAccel.x + qdiv(F.x, mass);
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       }
     } else if (!isZeroBits(inertia) && (PERI || !(isZeroBits(T) && inertiaPositive && !hasNegZero(angVel)))) {
       d3 angAccel;
-      if (blockedNone) angAccel = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
+      if (blockedNone) angAccel = divByEach(T, inertia);
       else {
         angAccel = mk(0, 0, 0);
         if (!(flags & 8u)) angAccel.x = angAccel.x + qdiv(T.x, inertia.x);
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     p.energy[EP_KIN][i] = ek;
   }
   // leapfrogTranslate (:275-278)
-  pos = pos + vel * dt;
+  pos = mk(addMulExact(pos.x, vel.x, dt), addMulExact(pos.y, vel.y, dt), addMulExact(pos.z, vel.z, dt));
   // leapfrogSphericalRotate (:280-297): q = AngleAxis(|w| dt, w/|w|) * q, normalised
   double4_32a o4 = p.ori[i];
   qd ori; ori.w = o4.x; ori.x = o4.y; ori.y = o4.z; ori.z = o4.w;
@@ -455,7 +457,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
       // components are qdiv of signed zeros, i.e. the zeros themselves
       lin = F;
       if (P.gravAxis == 0) lin.x = w4c.w; else if (P.gravAxis == 1) lin.y = w4c.w; else lin.z = w4c.w;
-    } else if (blockedNone) lin = mk(qdiv(F.x, mass), qdiv(F.y, mass), qdiv(F.z, mass));
+    } else if (blockedNone) lin = divBy(F, mass);
     else {
       lin = mk(0, 0, 0);
       if (!(flags & 1u)) lin.x = lin.x + qdiv(F.x, mass);
@@ -495,7 +497,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
       const d3 inertia = xyz(p.inert[i]);
       if (!isZeroBits(inertia)) {
         d3 ang;
-        if (blockedNone) ang = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
+        if (blockedNone) ang = divByEach(T, inertia);
         else {
           ang = mk(0, 0, 0);
           if (!(flags & 8u)) ang.x = ang.x + qdiv(T.x, inertia.x);
@@ -525,7 +527,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
         const d3 inertia = xyz(p.inert[i]);
         if (!isZeroBits(inertia)) {
           d3 ang;
-          if (blockedNone) ang = mk(qdiv(T.x, inertia.x), qdiv(T.y, inertia.y), qdiv(T.z, inertia.z));
+          if (blockedNone) ang = divByEach(T, inertia);
           else {
             ang = mk(0, 0, 0);
             if (!(flags & 8u)) ang.x = ang.x + qdiv(T.x, inertia.x);
@@ -773,9 +775,11 @@ void launch_reduce_forces(cudaStream_t s, const StepParams& P, Particles p, int 
   (k_reduce_forces<<<(n + 127) / 128, 128, 0, s>>>(P, p, n, c, csr), ++::wdem::g_kernel_launches);
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // Kinematic state exchange with caller buffers (xyz-interleaved / wxyz) through a device staging
 // area: scatter into the double4 records, or gather out of them.
@@ -810,9 +814,11 @@ void launch_state_out(cudaStream_t s, Particles p, int n, double* pos, double* v
   if (n > 0) (k_state_out<<<(n + 255) / 256, 256, 0, s>>>(p, n, pos, vel, angVel, ori), ++::wdem::g_kernel_launches);
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // FP64 issue-rate probe: independent chains of fused multiply-adds (explicit __fma_rn, so the
 // no-contraction build flag does not split them).  2 flops per FMA.
@@ -844,9 +850,11 @@ double fp64_probe(cudaStream_t s, double* scratch, int sms, float* msOut) {
   return ms > 0 ? flops / (ms * 1e-3) / 1e9 : 0.0;
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 __global__ void k_refresh_posf(Particles p, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -872,9 +880,11 @@ __global__ void k_grav_acc(StepParams P, Particles p, int n) {
 void launch_grav_acc(cudaStream_t s, const StepParams& P, Particles p, int n) {
   if (n > 0) (k_grav_acc<<<(n + 255) / 256, 256, 0, s>>>(P, p, n), ++::wdem::g_kernel_launches);
 }
+WDEM_VARIANT_END
 }  // namespace wdem
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // Deterministic sum: each block reduces a fixed slice in a fixed shared-memory tree, then one block
 // sums the block partials the same way.  The result is independent of scheduling.
@@ -913,4 +923,5 @@ void energy_accumulate(cudaStream_t s, const double* x, long long n, double* par
   (k_efinal<<<1, ER_T, 0, s>>>(partials, nb, acc, reset ? 1 : 0), ++::wdem::g_kernel_launches);
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem

@@ -207,12 +207,23 @@ struct wdem_handle {
   double* dStress = nullptr;    // 9 stress components + scratch for the terms
   double* stressTerms = nullptr;
   long long stressCap = 0;
+  std::vector<DevMaterial> devMats;  // the materials table in the kernels' layout
   double* dEnergy = nullptr;    // WDEM_E_COUNT accumulators
   double* ePartials = nullptr;  // block partials of the energy sums
   long long ePartialsCap = 0;
 };
 
 namespace {
+
+// The materials table lives in constant memory, one per device and kernel variant, shared by the handles
+// of the process: the handle that last uploaded it is recorded, and a step of another handle uploads its
+// own table first.
+const wdem_handle* g_matsOwner[64] = {nullptr};
+void uploadMaterials(wdem_handle* h) {
+  upload_materials(h->devMats.data(), (int)h->devMats.size());
+  contracted::upload_materials(h->devMats.data(), (int)h->devMats.size());
+  if (h->device >= 0 && h->device < 64) g_matsOwner[h->device] = h;
+}
 
 int fail(wdem_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -469,11 +480,13 @@ int rebuild(wdem_handle* h) {
   col_retain_write(s, old.c, nOld, cs, neu.c.ids, total, neu.cap);
   if (h->periodic && old.c.cdist) col_retain_write_dist(s, old.c, nOld, cs, neu.c.cdist, total, neu.cap);
   const int side = 1 - h->cur;
+  // history carried over, contacts real before the rebuild compacted to the front (the sort scratch,
+  // sized for 2 nNew entries, holds the temporaries); then the new table is hashed in that final order
+  if ((rc = ensureScratch(h, nNew))) return rc;
+  col_carry_compact(s, h->d, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
+                    (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT, cs);
   if ((rc = ensureHash(h, side, nNew))) return rc;
   launch_hash_build(s, neu.c.ids, nNew, h->hk[side], h->hv[side], h->hcap[side], h->dst);
-  col_carry(s, h->d, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
-            (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT);
-  if ((rc = ensureScratch(h, nNew))) return rc;
   if ((rc = ensureCsr(h, nNew))) return rc;
   col_csr(s, neu.c, nNew, n, h->csr, cs);
   h->cur = side;
@@ -660,6 +673,7 @@ int wdem_destroy(wdem_handle* h) {
   if (!h) return WDEM_ERR_ARG;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->device >= 0 && h->device < 64 && g_matsOwner[h->device] == h) g_matsOwner[h->device] = nullptr;
   Particles& d = h->d;
   cudaFree(d.semi); cudaFree(d.angMom); cudaFree(d.lastOri); cudaFree(d.maxRot);
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
@@ -697,6 +711,7 @@ int wdem_set_params(wdem_handle* h, const wdem_params* p) {
   if (p->iniEqlb) return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl.iniEqlb is not supported");
   if (!p->iniLensTouch) return fail(h, WDEM_ERR_UNSUPPORTED, "Cg2_*_L6Geom.iniLensTouch=False is not supported");
   if (!p->applyForces) return fail(h, WDEM_ERR_UNSUPPORTED, "ContactLoop.applyForces=False is not supported");
+  if (p->arith != WDEM_ARITH_EXACT && p->arith != WDEM_ARITH_FMA) return fail(h, WDEM_ERR_ARG, "arith must be WDEM_ARITH_EXACT or WDEM_ARITH_FMA");
   if (p->nMaterials <= 0 || !p->materials || p->nMaterials > MAX_MATERIALS) return fail(h, WDEM_ERR_ARG, "materials table missing or larger than 1024");
   if (p->law == WDEM_LAW_HERTZ_DMT && p->cp2 != WDEM_CP2_HERTZ)
     return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT needs Cp2_HertzMat_HertzPhys");
@@ -719,14 +734,15 @@ int wdem_set_params(wdem_handle* h, const wdem_params* p) {
   h->mats.assign(p->materials, p->materials + p->nMaterials);
   h->step = p->step;
   if (updatePhysChanged) h->updatePhys = p->updatePhys;
-  std::vector<DevMaterial> dm(h->mats.size());
+  std::vector<DevMaterial> dm(h->mats.size());  // the table of both kernel variants (constant memory)
   for (size_t k = 0; k < h->mats.size(); k++) {
     const wdem_material& m = h->mats[k];
     dm[k].kind = m.kind; dm[k].density = m.density; dm[k].young = m.young; dm[k].ktDivKn = m.ktDivKn;
     dm[k].tanPhi = m.tanPhi; dm[k].surfEnergy = m.surfEnergy; dm[k].alpha = m.alpha;
   }
   cudaSetDevice(h->device);
-  upload_materials(dm.data(), (int)dm.size());
+  h->devMats = dm;
+  uploadMaterials(h);
   if (p->materialDt) {
     for (int k = 0; k < p->nMaterials; k++)
       if (!(p->materialDt[k] >= 0)) return fail(h, WDEM_ERR_ARG, "materialDt must be non-negative");
@@ -934,7 +950,7 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     if (b.c.lam) CK(cudaMemsetAsync(b.c.lam, 0xFF, nc * sizeof(double), s));
     if (b.c.lam0) CK(cudaMemsetAsync(b.c.lam0, 0xFF, nc * sizeof(float), s));
   }
-  launch_init_uploaded(s, h->P, h->d, b.c, nc);
+  (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_init_uploaded : launch_init_uploaded)(s, h->P, h->d, b.c, nc);
   int rc;
   if ((rc = ensureHash(h, h->cur, nc))) return rc;
   launch_hash_build(s, b.c.ids, nc, h->hk[h->cur], h->hv[h->cur], h->hcap[h->cur], h->dst);
@@ -1029,10 +1045,10 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   StepParams P = h->P;
   for (int g = 0; g < ahead; g++) {
     P.step = s0 + g;
-    launch_leapfrog(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
+    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
     const bool full = !h->actValid;
     h->actValid = true;
-    launch_contacts(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, full, warm ? h->mlpWbf : nullptr,
+    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, full, warm ? h->mlpWbf : nullptr,
                     warm ? h->mlpW : nullptr);
   }
   CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
@@ -1053,7 +1069,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
     CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
     if ((rc = rebuild(h))) return rc;
-    launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
+    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                     warm ? h->mlpW : nullptr);
     h->actValid = true;
     h->sinceRebuild += (int)(k - s0) + 1;
@@ -1085,6 +1101,10 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   if (h->hasEll && (h->P.law != WDEM_LAW_IDEALELPL || h->P.cp2 != WDEM_CP2_FRICT))
     return fail(h, WDEM_ERR_UNSUPPORTED,
                 "ellipsoids and aspherical nodes run with Cp2_FrictMat_FrictPhys + Law2_L6Geom_FrictPhys_IdealElPl only");
+  if (h->device >= 0 && h->device < 64 && g_matsOwner[h->device] != h) {
+    cudaSetDevice(h->device);
+    uploadMaterials(h);  // another handle of this process uploaded its table since
+  }
   if (h->hasEll && h->P.ellSolver != WDEM_ELL_BRENT && h->P.ellSolver != WDEM_ELL_NEWTON)
     return fail(h, WDEM_ERR_ARG, "unknown ellipsoid solver");
   if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && !(h->P.newtonTol > 0))
@@ -1130,7 +1150,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     }
     {
       PhaseTimer t(h, PH_LEAPFROG);
-      launch_leapfrog(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
+      (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
     }
     if (h->P.trackEnergy && !h->P.lfEnergy) {
       // kinetic is resettable (EnergyTracker::resetResettables at the start of the step)
@@ -1168,7 +1188,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     {
       PhaseTimer t(h, PH_CONTACTS);
       const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
-      launch_contacts(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
+      (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                       warm ? h->mlpW : nullptr);
       h->actValid = true;
     }

@@ -15,8 +15,10 @@
 // the general one.
 #pragma once
 #include "wdem_math.cuh"
+#include "wdem_variant.h"
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 struct s33 { double a, b, c, d, e, f; };  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
 
@@ -191,4 +193,5 @@ __device__ __forceinline__ void ellFeatures(qd oa, d3 semiA, qd ob, d3 semiB, d3
   f[10] = (float)(semiB.x * is); f[11] = (float)(semiB.y * is); f[12] = (float)(semiB.z * is);
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem

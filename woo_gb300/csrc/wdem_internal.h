@@ -229,6 +229,16 @@ void launch_refresh_posf(cudaStream_t s, Particles p, int n);
 void launch_grav_acc(cudaStream_t s, const StepParams& P, Particles p, int n);
 // deterministic sum of x[0..n) added to *acc (or stored, when reset): fixed-order block trees
 void energy_accumulate(cudaStream_t s, const double* x, long long n, double* partials, double* acc, bool reset);
+// ---- the contracted variant of k_leapfrog.cu and k_contact.cu (compiled with WDEM_FMA, wdem_variant.h):
+// the same launchers, FP64 multiply-adds contracted, one reciprocal per vector division
+namespace contracted {
+void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays,
+                     Contacts c, Csr csr, DeviceStatus* st);
+void upload_materials(const DevMaterial* m, int n);
+void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
+                     bool full, const uint16_t* warmBf = nullptr, const float* warmF = nullptr);
+void launch_init_uploaded(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc);
+}  // namespace contracted
 // ---- launchers (k_contact.cu) ----
 void upload_materials(const DevMaterial* m, int n);
 // warm: BF16 and FP32 weights of the learned warm start, run between the cull and the FP64 pass (or null)
@@ -302,9 +312,12 @@ void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScra
                       long long cap);
 void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
                        unsigned long long cap, DeviceStatus* st);
-void col_carry(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, const unsigned long long* hk,
-               const unsigned* hv, unsigned long long cap, long long step, int nHist);
 void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs);
+// history carry-over with compaction: contacts that were real before the rebuild first (in emission order),
+// then the others; uses the sort scratch (sized for 2 nNew) as temporary storage
+long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old,
+                            const unsigned long long* hk, const unsigned* hv, unsigned long long cap, long long step,
+                            int nHist, ColliderScratch& cs);
 // exclusive scan of a[0..n) in place; a[n] receives the total (the array holds n+1 entries)
 void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs);
 int sort_passes_for(int nSmallBits);

@@ -2,15 +2,19 @@
 //
 // Every helper performs the IEEE operations in the same order as Woo's Eigen expressions
 // (left-to-right; dot = (a0 b0 + a1 b1) + a2 b2), and the kernels are compiled with
-// --fmad=false, so per-contact results reproduce the CPU restatement bit for bit.
+// --fmad=false, so per-contact results reproduce the CPU restatement bit for bit.  In the contracted
+// variant (WDEM_FMA, wdem_variant.h) multiply-adds become FMAs and the helpers marked below divide by a
+// scalar through one reciprocal (normalisations through one reciprocal square root).
 #pragma once
 #include <cuda_runtime.h>
+#include "wdem_variant.h"
 
 // Keeps the compiler from if-converting a skipped branch (which would issue the FP64 division
 // sequence anyway under a predicate): the empty volatile asm marks the block as having effects.
 #define WDEM_REAL_BRANCH() asm volatile("")
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 struct d3 { double x, y, z; };
 
@@ -21,9 +25,21 @@ __device__ __forceinline__ d3 operator-(d3 a, d3 b) { return mk(a.x - b.x, a.y -
 __device__ __forceinline__ d3 operator-(d3 a) { return mk(-a.x, -a.y, -a.z); }
 __device__ __forceinline__ d3 operator*(d3 a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
 __device__ __forceinline__ d3 operator*(double s, d3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+#ifdef WDEM_FMA
+__device__ __forceinline__ d3 operator/(d3 a, double s) { const double r = 1.0 / s; return mk(a.x * r, a.y * r, a.z * r); }
+#else
 __device__ __forceinline__ d3 operator/(d3 a, double s) { return mk(a.x / s, a.y / s, a.z / s); }
+#endif
 __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ double sqnorm(d3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+// sqnorm with every operation rounded on its own in both variants (never contracted): the contracted
+// variant keeps the sphere distance, the near-cancelling overlap |d| - r1 - r2 and the position update
+// identical to the exact variant, so that contact forces agree to rounding after a step from one state
+__device__ __forceinline__ double sqnormExact(d3 a) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y)), __dmul_rn(a.z, a.z));
+}
+// v + a s, never contracted (the position update pos + vel dt)
+__device__ __forceinline__ double addMulExact(double v, double a, double s) { return __dadd_rn(v, __dmul_rn(a, s)); }
 __device__ __forceinline__ d3 cross(d3 a, d3 b) {
   return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
@@ -85,7 +101,11 @@ __device__ __forceinline__ bool signsDiffer(double a, double b) { return ((halve
 // are identities: skipping them changes no bit and saves FP64 issue slots.
 __device__ __forceinline__ d3 normalized(d3 a) {
   double z = sqnorm(a);
+#ifdef WDEM_FMA
+  if (z > 0 && z != 1.0) { WDEM_REAL_BRANCH(); const double r = rsqrt(z); a.x *= r; a.y *= r; a.z *= r; }
+#else
   if (z > 0 && z != 1.0) { WDEM_REAL_BRANCH(); double n = sqrt(z); a.x /= n; a.y /= n; a.z /= n; }
+#endif
   return a;
 }
 // x / y for y > 0 finite or +inf: a zero numerator is its own quotient (keeping the sign of zero),
@@ -94,6 +114,25 @@ __device__ __forceinline__ double qdiv(double x, double y) {
   double r = x;
   if (!(zeroBits(x) && positiveBits(y))) { WDEM_REAL_BRANCH(); r = x / y; }
   return r;
+}
+// v / s per component (v / m, the acceleration of a node): three qdiv; contracted variant: one reciprocal
+__device__ __forceinline__ d3 divBy(d3 v, double s) {
+#ifdef WDEM_FMA
+  const double r = 1.0 / s;
+  return mk(v.x * r, v.y * r, v.z * r);
+#else
+  return mk(qdiv(v.x, s), qdiv(v.y, s), qdiv(v.z, s));
+#endif
+}
+// v / d per component (torque / inertia): three qdiv; contracted variant: one reciprocal when the three
+// divisors are equal (spheres), else three
+__device__ __forceinline__ d3 divByEach(d3 v, d3 d) {
+#ifdef WDEM_FMA
+  if (d.x == d.y && d.y == d.z) { const double r = 1.0 / d.x; return mk(v.x * r, v.y * r, v.z * r); }
+  return mk(v.x / d.x, v.y / d.y, v.z / d.z);
+#else
+  return mk(qdiv(v.x, d.x), qdiv(v.y, d.y), qdiv(v.z, d.z));
+#endif
 }
 __device__ __forceinline__ double comp(d3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 __device__ __forceinline__ void setComp(d3& a, int i, double v) { if (i == 0) a.x = v; else if (i == 1) a.y = v; else a.z = v; }
@@ -161,7 +200,11 @@ __device__ __forceinline__ qd qmul(qd a, qd b) {
 
 __device__ __forceinline__ qd qnormalized(qd q) {
   double z2 = q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w;
+#ifdef WDEM_FMA
+  if (!isOneBits(z2) && z2 > 0) { WDEM_REAL_BRANCH(); const double r = rsqrt(z2); q.x *= r; q.y *= r; q.z *= r; q.w *= r; }
+#else
   if (!isOneBits(z2) && z2 > 0) { WDEM_REAL_BRANCH(); double n = sqrt(z2); q.x /= n; q.y /= n; q.z /= n; q.w /= n; }
+#endif
   return q;
 }
 
@@ -239,7 +282,7 @@ __device__ __forceinline__ double addScaledR(double v, double a, double s) {
     return (negZero(v) && !addendNeg) ? 0.0 : v;
   }
   WDEM_REAL_BRANCH();
-  return v + a * s;
+  return addMulExact(v, a, s);
 }
 
 // double -> float by truncating the mantissa (error below 2^-23 relative) for values in the float normal
@@ -270,4 +313,5 @@ __device__ __forceinline__ double pown5(double x) {
   return p2 * x;
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem

@@ -4,8 +4,10 @@
 // number of cells by which pB is shifted to overlap pA.  Same IEEE operations as the reference.
 #pragma once
 #include <cuda_runtime.h>
+#include "wdem_variant.h"
 
 namespace wdem {
+WDEM_VARIANT_BEGIN
 
 // InsertionSortCollider::cellWrapRel (InsertionSortCollider.cpp:624-628)
 __device__ __forceinline__ double cellWrapRel(double x, double x0, double x1, int& period) {
@@ -57,4 +59,5 @@ __device__ __forceinline__ bool periNear(float c1, float h1, float c2, float h2,
   return periDist(c1, c2, L, invL) < h1 + h2 - 1e-5f * L;
 }
 
+WDEM_VARIANT_END
 }  // namespace wdem

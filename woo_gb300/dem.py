@@ -975,9 +975,10 @@ class GpuDemEngine(Engine):
 
     Constructed like ContactLoop from the three functor lists (src/dem/ContactLoop.cpp:52-66), plus
     the Leapfrog (damping, reset) and collider (verletDist) attributes.  Runs libwdem.so on one CUDA
-    device; errors come back as RuntimeError."""
+    device; errors come back as RuntimeError.  arith: "exact" (the reference's IEEE operations, bit for
+    bit) or "fma" (FP64 multiply-adds contracted, one reciprocal per vector division)."""
     _defaults = dict(capacity=0, damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
-                     updatePhys="never", dist00=True, device=0, keepGeom=True)
+                     updatePhys="never", dist00=True, device=0, keepGeom=True, arith="exact")
 
     def __init__(self, cg2=None, cp2=None, law=None, **kw):
         super().__init__(**kw)
@@ -1084,6 +1085,9 @@ class GpuDemEngine(Engine):
         p.warmStart = {"cold": abi.WARM_COLD, "history": abi.WARM_HISTORY, "mlp": abi.WARM_MLP}[
             ell.warmStart if ell is not None else "cold"]
         p.fallbackIters = int(ell.fallbackIters) if ell is not None else 4
+        if self.arith not in ("exact", "fma"):
+            raise ValueError("GpuDemEngine.arith must be 'exact' or 'fma'")
+        p.arith = abi.ARITH_FMA if self.arith == "fma" else abi.ARITH_EXACT
         self._ellFunctor = ell
         return p
 

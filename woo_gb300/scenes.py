@@ -115,6 +115,7 @@ def default_params(materials, **kw):
     p.newtonTol = kw.get("newtonTol", 1e-10)
     p.warmStart = kw.get("warmStart", abi.WARM_COLD)
     p.fallbackIters = kw.get("fallbackIters", 4)
+    p.arith = kw.get("arith", abi.ARITH_EXACT)
     return p
 
 
