@@ -5,8 +5,8 @@ Workloads (synthetic, seeded; no dataset is involved):
       .01, tanPhi .3/.6) as a loose cloud (solid fraction ~0.3) falling into a 1 x 1 x 2 m walled box,
       dt = 0.3 x p-wave dt, verletDist 0.1 x rmin.  The timed region is K steps after W warm-up steps of
       that job, the same steps that the CPU arm (--impl reference) times.  The line also carries
-      "settled": the same spheres settled on the GPU first (untimed: 10 g and damping 0.5 while the cloud
-      falls, then 3000 steps at 1 g), then W + K steps with the job's parameters, about one real contact
+      "settled": the same spheres settled on the GPU first (untimed, damping 0.5: 10 g while the cloud
+      falls, then 1 g; scenes.settle), then W + K steps with the job's parameters, about one real contact
       per sphere, with the CPU port timed on that same settled state in the same process.
   hertz1M_settled -- the settled state alone as the headline.
   ell200k -- 200,000 ellipsoids (a ~ U[3,6] mm, b = .7a, c = .5a, random orientations) agitated in a
@@ -189,8 +189,8 @@ def copy_params(p):
 
 
 def settle(h, spec):
-    """Untimed settling on the GPU (scenes.settle): 10 g and damping 0.5 while the cloud falls half its
-    height, then 3000 steps at 1 g; the job's parameters are restored."""
+    """Untimed settling on the GPU (scenes.settle): damping 0.5, 10 g while the cloud falls, then 1 g; the
+    job's parameters are restored."""
     from woo_gb300 import scenes
     return scenes.settle(h, spec)
 
@@ -527,7 +527,8 @@ def run_gpu(args, rank, world, local):
         settle_s = time.time() - t0
         settled = measure_region(hs, spec, args, world, local, barrier, "settled")
         settled["settling"] = {"steps": nsettle, "seconds": settle_s,
-                               "how": "10 g and damping 0.5 while the cloud falls half its height, then 3000 steps at 1 g"}
+                               "how": "damping 0.5: 10 g and 2.5 dt while the cloud falls, 8000 steps at 1 g and 2.5 dt, "
+                                      "2000 steps at 1 g and dt"}
         if args.arith == "fma":
             # the same settled run continued with the exact variant (the reference's operations bit for bit)
             pe = copy_params(spec.params)

@@ -23,7 +23,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _state(law, seed):
-    spec = scenes.random_cloud(3000, seed, box=(0.2, 0.2, 0.2), rmin=0.003, rmax=0.005, dense=0.82, law=law)
+    spec = scenes.random_cloud(4000, seed, box=(0.2, 0.2, 0.2), rmin=0.003, rmax=0.005, dense=0.7, law=law,
+                               vel_scale=0.05, angvel_scale=1.0)
     h = gpu_handle(spec, keep_geom=False)
     h.step(120)
     pa = h.download_particles(spec.particles.copy())

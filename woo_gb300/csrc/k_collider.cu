@@ -402,7 +402,25 @@ __device__ __forceinline__ int2 orient(int i, int j, int shi, int shj) {
   return make_int2(a, b);
 }
 
+// Sweep records, two float4 per particle in sort order: the box in FP32 with the minimum rounded down and
+// the maximum rounded up (every pair of FP64 boxes that overlap overlaps in FP32 too, so a pair the FP32
+// test rejects needs no FP64 test), the mask (lo.w) and meta.x with shape and scene (hi.w).  The sweep
+// walks these contiguous records instead of gathering meta, bbmin and bbmax by particle id.
+__global__ void k_sweep_records(Particles p, const unsigned* vals, int nSmall, float4* rec) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nSmall) return;
+  const int i = (int)vals[s];
+  const double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+  const int4 m = p.meta[i];
+  rec[2 * s] = make_float4(__double2float_rd(mn.x), __double2float_rd(mn.y), __double2float_rd(mn.z), __uint_as_float((unsigned)m.z));
+  rec[2 * s + 1] = make_float4(__double2float_ru(mx.x), __double2float_ru(mx.y), __double2float_ru(mx.z), __int_as_float(m.x));
+}
+__device__ __forceinline__ bool overlapF(const float4& mn1, const float4& mx1, const float4& mn2, const float4& mx2) {
+  return (mn1.x <= mx2.x) && (mx1.x >= mn2.x) && (mn1.y <= mx2.y) && (mx1.y >= mn2.y) && (mn1.z <= mx2.z) && (mx1.z >= mn2.z);
+}
+
 struct SweepArgs {
+  const float4* rec;
   const unsigned long long* keys;
   const unsigned* vals;
   const int* cellStart;
@@ -440,6 +458,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
   int i = (int)A.vals[s];
   int4 mi = p.meta[i];
   double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
+  const float4 fmn = A.rec[2 * s], fmx = A.rec[2 * s + 1];
   unsigned qi = (unsigned)(key & QMAX);
   unsigned qmax = quant(cmp3(mx, G.sweepAxis), G);
   long long col = (long long)(key >> QBITS);
@@ -464,12 +483,15 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
       for (; q < end; q++) {
         unsigned long long kq = A.keys[q];
         if ((unsigned)(kq & QMAX) > qmax) break;
+        const float4 gmn = A.rec[2 * q], gmx = A.rec[2 * q + 1];
+        const unsigned maskj = __float_as_uint(gmn.w);
+        const int metaxj = __float_as_int(gmx.w);
+        if (!mayCollide((unsigned)mi.z, maskj, A.loneMask)) continue;
+        if (sceneOf(mi.x) != sceneOf(metaxj)) continue;
+        if (!overlapF(fmn, fmx, gmn, gmx)) continue;
         int j = (int)A.vals[q];
-        int4 mj = p.meta[j];
-        if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
-        if (sceneOf(mi.x) != sceneOf(mj.x)) continue;
         if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
-        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
+        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, metaxj & 15); }
         cnt++;
       }
     }
@@ -866,7 +888,8 @@ __global__ void k_stress_terms(StepParams P, Particles p, Contacts c, long long 
       const int4 cd = c.cdist[i];
       branch = branch + mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
     }
-    const double F[3] = {c.out[OUT_FX][i], c.out[OUT_FY][i], c.out[OUT_FZ][i]};
+    const double4_32a f4 = c.out[OUT_RECORDS * i + OUT_F];
+    const double F[3] = {f4.x, f4.y, f4.z};
     const double b[3] = {branch.x, branch.y, branch.z};
     for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) v[3 * r + q] = F[r] * b[q];
   }
@@ -895,11 +918,13 @@ void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, Collide
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bits, cs);
   int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
   (k_cell_start<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.grid, cs.cellStart), ++::wdem::g_kernel_launches);
+  if (nSmall > 0) (k_sweep_records<<<(nSmall + 255) / 256, 256, 0, s>>>(p, cs.vals, nSmall, cs.srec), ++::wdem::g_kernel_launches);
 }
 
 void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out, long long cap,
                bool write, DeviceStatus* st) {
   SweepArgs A;
+  A.rec = cs.srec;
   A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
   A.nSmall = nSmall; A.loneMask = loneMask;
   A.sceneWall = cs.nScenes > 1 ? cs.sceneWall : nullptr;

@@ -413,19 +413,35 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   } else {
     const double velN = gvel.x;
     const double kn0 = hz[0];
+#ifdef WDEM_FMA
+    // one square root of the overlap for kn, Fne and kt, and its square root for the viscous coefficient
+    const double sq = sqrt(dmax(-uN, 0.));
+    kn = (3 / 2.) * kn0 * sq;
+#else
     kn = (3 / 2.) * kn0 * sqrt(-uN);
+#endif
     if (positiveBits(uN)) keep = false;
     else {
+#ifdef WDEM_FMA
+      double Fne = -kn0 * pown3(sq);
+      double Fna = hz[3];
+      double eta = (positiveBits(hz[2]) ? hz[2] * sqrt(sq) : 0.);
+#else
       double Fne = -kn0 * pown3(sqrt(-uN));
       double Fna = hz[3];
       double eta = (positiveBits(hz[2]) ? hz[2] * sqrt(sqrt(dmax(-uN, 0.))) : 0.);
+#endif
       double Fnv = eta * velN;
       // HertzPhys.alpha = mean of the materials' alpha (Hertz.cpp:52); the clamp applies when it is 0
       const double alphaC = .5 * (c_mats[p.meta[a].y].alpha + c_mats[p.meta[b].y].alpha);
       if (zeroBits(alphaC) && P.noAttraction && positiveBits(Fne + Fnv)) Fnv = -Fne;
       fx = Fne + Fna + Fnv;
       if (P.trackEnergy) eVN = Fnv * velN * dt;
+#ifdef WDEM_FMA
+      kt = hz[1] * sq;
+#else
       kt = hz[1] * sqrt(negativeBits(uN) ? -uN : 0);
+#endif
       double sc = dt * kt;
       fy = fy + sc * gvel.y;
       fz = fz + sc * gvel.z;
@@ -482,9 +498,10 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   const d3 TA = cross(xcA, F) + T;
   const d3 FB = F * -1.0;
   const d3 TB = cross(xcB, FB) + T * -1.0;
-  c.out[OUT_FX][i] = F.x; c.out[OUT_FY][i] = F.y; c.out[OUT_FZ][i] = F.z;
-  c.out[OUT_TAX][i] = TA.x; c.out[OUT_TAY][i] = TA.y; c.out[OUT_TAZ][i] = TA.z;
-  c.out[OUT_TBX][i] = TB.x; c.out[OUT_TBY][i] = TB.y; c.out[OUT_TBZ][i] = TB.z;
+  double4_32a* o = c.out + OUT_RECORDS * i;
+  o[OUT_F] = make_double4_32a(F.x, F.y, F.z, 0.0);
+  o[OUT_TA] = make_double4_32a(TA.x, TA.y, TA.z, 0.0);
+  o[OUT_TB] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
 }
 
 // 128 threads, 4 blocks per SM (<= 128 registers a thread, no spills): one wave of the 152 x 4 blocks

@@ -34,13 +34,14 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
     const unsigned en = csr.ent[e];
     const unsigned ci = en & 0x7fffffffu;
     if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
-    const d3 f = mk(c.out[OUT_FX][ci], c.out[OUT_FY][ci], c.out[OUT_FZ][ci]);
+    const double4_32a* o = c.out + OUT_RECORDS * (long long)ci;
+    const d3 f = xyz(o[OUT_F]);
     if (en >> 31) {
       F = F + f * -1.0;
-      T = T + mk(c.out[OUT_TBX][ci], c.out[OUT_TBY][ci], c.out[OUT_TBZ][ci]);
+      T = T + xyz(o[OUT_TB]);
     } else {
       F = F + f;
-      T = T + mk(c.out[OUT_TAX][ci], c.out[OUT_TAY][ci], c.out[OUT_TAZ][ci]);
+      T = T + xyz(o[OUT_TA]);
     }
   }
 }
@@ -429,13 +430,14 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
         const unsigned en = csr.ent[e];
         const unsigned ci = en & 0x7fffffffu;
         if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
-        const d3 f = mk(c.out[OUT_FX][ci], c.out[OUT_FY][ci], c.out[OUT_FZ][ci]);
+        const double4_32a* o = c.out + OUT_RECORDS * (long long)ci;
+        const d3 f = xyz(o[OUT_F]);
         if (en >> 31) {
           F = F + f * -1.0;
-          T = T + mk(c.out[OUT_TBX][ci], c.out[OUT_TBY][ci], c.out[OUT_TBZ][ci]);
+          T = T + xyz(o[OUT_TB]);
         } else {
           F = F + f;
-          T = T + mk(c.out[OUT_TAX][ci], c.out[OUT_TAY][ci], c.out[OUT_TAZ][ci]);
+          T = T + xyz(o[OUT_TA]);
         }
       }
     }

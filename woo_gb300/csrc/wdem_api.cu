@@ -248,7 +248,7 @@ void freeContacts(ContactBuf& b) {
   Contacts& c = b.c;
   cudaFree(c.ids); cudaFree(c.state); cudaFree(c.act); cudaFree(c.step0); cudaFree(c.tanPhi);
   for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
-  for (int k = 0; k < OUT_COUNT; k++) cudaFree(c.out[k]);
+  cudaFree(c.out);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   cudaFree(c.cdist);
@@ -270,7 +270,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if ((e = dalloc(c.tanPhi, cap))) return e;
   int nh = hertz ? HIST_COUNT : HIST_FRICT;
   for (int k = 0; k < nh; k++) if ((e = dalloc(c.hist[k], cap))) return e;
-  for (int k = 0; k < OUT_COUNT; k++) if ((e = dalloc(c.out[k], cap))) return e;
+  if ((e = dalloc(c.out, (size_t)OUT_RECORDS * cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   if ((e = dalloc(c.work, cap))) return e;
@@ -294,7 +294,7 @@ void copyContacts(cudaStream_t s, ContactBuf& dst, const ContactBuf& src, long l
   cudaMemcpyAsync(dst.c.tanPhi, src.c.tanPhi, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   for (int k = 0; k < HIST_COUNT; k++)
     if (dst.c.hist[k] && src.c.hist[k]) cudaMemcpyAsync(dst.c.hist[k], src.c.hist[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  for (int k = 0; k < OUT_COUNT; k++) cudaMemcpyAsync(dst.c.out[k], src.c.out[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(dst.c.out, src.c.out, (size_t)OUT_RECORDS * n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, s);
 }
 
 unsigned long long nextPow2(unsigned long long v) {
@@ -645,6 +645,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(h->dSmall, N) == cudaSuccess;
   ok &= dalloc(h->cs.large, N) == cudaSuccess;
   ok &= dalloc(h->cs.counts, (size_t)N + 2) == cudaSuccess;
+  ok &= dalloc(h->cs.srec, 2 * (size_t)N + 2) == cudaSuccess;
   ok &= dalloc(h->cs.grid, 1) == cudaSuccess;
   ok &= dalloc(h->csr.rowptr, (size_t)N + 1) == cudaSuccess;
   ok &= dalloc(h->csr.cursor, (size_t)N) == cudaSuccess;
@@ -689,7 +690,7 @@ int wdem_destroy(wdem_handle* h) {
   for (int k = 0; k < 2; k++) { cudaFree(h->hk[k]); cudaFree(h->hv[k]); }
   ColliderScratch& cs = h->cs;
   cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
-  cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid);
+  cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid); cudaFree(cs.srec);
   cudaFree(cs.retainFlag); cudaFree(cs.temp); cudaFree(cs.periC); cudaFree(cs.periH); cudaFree(cs.periCi); cudaFree(cs.periHi);
   cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag);
   cudaFree(h->dst);

@@ -20,7 +20,8 @@
 //     hist    double x 14 SoA: trsf col0 (3), trsf col1 (3), contPt (3), force (3, local), kn, kt
 //             (+4 for HertzPhys: kn0, kt0, alpha_sqrtMK, adhesion force)
 //     tanPhi  double
-//     out     double x 9 SoA: global force on pA (3), torque on pA (3), torque on pB (3)
+//     out     3 double4_32a records per contact (one 32-byte sector each): global force on pA, torque on
+//             pA, torque on pB (x, y, z, unused); the integrator's gather reads two whole sectors per entry
 //   CSR over particles: rowptr[N+1], entries[2C] = contact index | (isB << 31), rows sorted
 //   by the partner's id key so that sums run in the order of the sorted contact keys.
 #pragma once
@@ -51,7 +52,7 @@ enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, 
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
        HIST_COUNT };
 enum { HIST_FRICT = HIST_E0 };  // FrictPhys contacts carry the first 14 history arrays
-enum { OUT_FX = 0, OUT_FY, OUT_FZ, OUT_TAX, OUT_TAY, OUT_TAZ, OUT_TBX, OUT_TBY, OUT_TBZ, OUT_COUNT };
+enum { OUT_F = 0, OUT_TA = 1, OUT_TB = 2, OUT_RECORDS = 3 };  // records of one contact in Contacts.out
 enum { MAX_MATERIALS = 1024 };  // 1024 x 56 B fits the 64 KB constant bank
 
 struct DevMaterial {
@@ -145,7 +146,7 @@ struct Contacts {
   int* step0;
   double* hist[HIST_COUNT];
   double* tanPhi;
-  double* out[OUT_COUNT];
+  double4_32a* out;  // OUT_RECORDS records per contact: out[OUT_RECORDS * i + OUT_F / OUT_TA / OUT_TB]
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
   int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
@@ -255,6 +256,7 @@ struct ColliderScratch {
   unsigned* blockSums;                  // scan scratch
   long long blockSumsCap;
   int* cellStart;                       // maxCols + 1
+  float4* srec;                         // sweep records in sort order: 2 per particle (N capacity)
   int maxCols;
   unsigned* counts;                     // nSmall+2 pair counts per sorted particle, scanned in place
   int* large;                           // ids of walls (unbounded boxes), grouped by scene

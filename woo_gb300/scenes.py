@@ -485,26 +485,32 @@ def copy_params(p):
     return q
 
 
-def settle(h, spec, tail_steps=3000):
-    """Settle a falling cloud on the GPU handle h (untimed preparation of a packed state): gravity x 10 and
-    non-viscous damping 0.5 for as long as a free fall of half the cloud height takes, then `tail_steps`
-    steps at 1 g with damping 0.5; the scene's parameters are restored afterwards (Scene.step kept).
+def settle(h, spec, tail_steps=8000, dt_factor=2.5, relax_steps=2000):
+    """Settle a falling cloud on the GPU handle h (untimed preparation of a packed state), with
+    non-viscous damping 0.5 throughout: gravity x 10 at dt_factor x dt while the whole cloud falls (the fall
+    time of its height at the damped 5 g), `tail_steps` more at 1 g and dt_factor x dt, then `relax_steps`
+    at 1 g and the scene's dt.  The scene's parameters are restored afterwards (Scene.step kept).
     Returns the number of steps run."""
     p = copy_params(spec.params)
     dt = spec.params.dt
     height = spec.info.get("height", 1.0)
     g = abs(spec.params.gravity[2])
-    fall = int(math.sqrt(2 * 0.5 * height / (10 * g)) / dt)
-    for mult, steps in ((10.0, fall), (1.0, tail_steps)):
+    fall = int(math.sqrt(2 * height / (5 * g)) / (dt_factor * dt))
+    total = 0
+    for mult, steps, f in ((10.0, fall, dt_factor), (1.0, tail_steps, dt_factor), (1.0, relax_steps, 1.0)):
+        if steps <= 0:
+            continue
         p.gravity[2] = spec.params.gravity[2] * mult
         p.damping = 0.5
+        p.dt = dt * f
         p.step = h.status().step
         h.set_params(p)
         h.step(steps)
+        total += steps
     q = copy_params(spec.params)
     q.step = h.status().step
     h.set_params(q)
-    return fall + tail_steps
+    return total
 
 
 def single_from_batch(spec, k):
