@@ -53,6 +53,26 @@ def test_noalloc_stress_many_blocks(wdem_lib):
     _compare(h)
 
 
+def test_noalloc_stress_allocates_nothing(wdem_lib):
+    """On a fresh handle, before any call of the allocating wdem_get_stress: the first call looks up the
+    scratch array's address (and may load the module), the second call must leave the device's free
+    memory exactly as it was."""
+    torch = pytest.importorskip("torch")
+    spec = scenes.random_cloud(1500, 6, dense=0.85)
+    h = gpu_handle(spec)
+    h.step(40)
+    a = h.stress_noalloc()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    b = h.stress_noalloc()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    assert np.array_equal(a, b)
+    ref = h.stress()
+    assert np.allclose(a, ref, rtol=0, atol=TOL * np.abs(ref).max())
+
+
 def test_noalloc_stress_no_contacts(wdem_lib):
     spec = scenes.random_cloud(20, 1, box=(1.0, 1.0, 1.0), walls=False, gravity=(0, 0, 0))
     h = gpu_handle(spec)

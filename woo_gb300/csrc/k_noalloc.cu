@@ -87,7 +87,8 @@ long long stress_noalloc_max_contacts() { return NA_CHUNK * NA_MAX_BLOCKS; }
 
 // Device address of the scratch array, looked up once per device (cudaGetSymbolAddress may load the
 // module on first use under lazy loading, so the first call on a device belongs outside any stream
-// capture).
+// capture).  The address is kept for the life of the process: a cudaDeviceReset, which also invalidates
+// every handle on that device, invalidates it too, and the library must not be used on that device again.
 cudaError_t noalloc_scratch(int device, void** addr) {
   if (device < 0 || device >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_na_mutex);
