@@ -379,6 +379,14 @@ int wdem_ell_log_read(wdem_handle* h, float* out, int64_t cap, int64_t* n);
  * Synchronises the handle's stream before returning. */
 int wdem_get_stress_noalloc(wdem_handle* h, double* stress);
 
+/* Upper bound on the contact container (real and potential pairs) for callers that budget device memory;
+ * 0 (the default) = grow as needed.  No counterpart in the reference, whose container grows without
+ * bound.  A collider run or a contact upload that needs more than maxContacts stops with
+ * WDEM_ERR_OVERFLOW before it allocates or changes the container; the step that hit the limit is left
+ * half done (its integrator ran), so the caller re-uploads the state (or raises the limit and restarts
+ * from its own copy) before stepping on. */
+int wdem_set_contact_limit(wdem_handle* h, int64_t maxContacts);
+
 /* The CUDA stream (cudaStream_t) every kernel of this handle is launched on, for callers that
  * record CUDA events around wdem_step.  No counterpart in the reference (CPU only). */
 int wdem_get_stream(wdem_handle* h, void** stream);

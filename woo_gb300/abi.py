@@ -109,7 +109,7 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
-           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii"]
+           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii", "wdem_set_contact_limit"]
 
 
 def ptr(a, ctype):
@@ -286,6 +286,7 @@ def load(path=None):
         "wdem_warm_train": ([h, F32, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64, F32], C.c_int),
         "wdem_ell_log": ([h, C.c_int64], C.c_int),
         "wdem_make_cloud_radii": ([D, D, C.c_int32, C.c_int64, D, C.c_uint64, C.c_int32, D, D], C.c_int64),
+        "wdem_set_contact_limit": ([h, C.c_int64], C.c_int),
         "wdem_ell_log_read": ([h, F32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -368,6 +369,10 @@ class Handle:
 
     def set_timing(self, on):
         self.check(self.lib.wdem_set_timing(self.h, 1 if on else 0))
+
+    def set_contact_limit(self, max_contacts):
+        """Upper bound on the contact container (0 = none): beyond it a step fails with WDEM_ERR_OVERFLOW."""
+        self.check(self.lib.wdem_set_contact_limit(self.h, int(max_contacts)))
 
     def set_queue_depth(self, depth):
         """Steps queued before the host checks the collider trigger (1 = every step)."""

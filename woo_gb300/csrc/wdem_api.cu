@@ -208,6 +208,7 @@ struct wdem_handle {
   double* stressTerms = nullptr;
   long long stressCap = 0;
   std::vector<DevMaterial> devMats;  // the materials table in the kernels' layout
+  long long contactLimit = 0;        // wdem_set_contact_limit (0: none)
   double* dEnergy = nullptr;    // WDEM_E_COUNT accumulators
   double* ePartials = nullptr;  // block partials of the energy sums
   long long ePartialsCap = 0;
@@ -428,6 +429,11 @@ int checkDeviceStatus(wdem_handle* h) {
     std::string m;
     if (code == WDEM_ERR_NAN) m = "NaN in the state or in a contact force (particle #" + std::to_string(h->hst->detail) + ")";
     else if (code == WDEM_ERR_OVERFLOW) m = "contact hash table overflow";
+    else if (code == WDEM_ERR_TOO_BIG)
+      m = "ambiguous periodic contact of particle #" + std::to_string(h->hst->detail) +
+          ": the boxes overlap across more than one period (a particle larger than half of the cell)";
+    else if (code == WDEM_ERR_TIMEOUT)
+      m = "a bounded device loop hit its iteration limit (contact solver, particle #" + std::to_string(h->hst->detail) + ")";
     else m = "device error " + std::to_string(code);
     return fail(h, code, m);
   }
@@ -470,6 +476,9 @@ int rebuild(wdem_handle* h) {
   const long long total = h->hcounts[0];
   const long long retained = h->hcounts[1];
   const long long nNew = total + retained;
+  if (h->contactLimit > 0 && nNew > h->contactLimit)
+    return fail(h, WDEM_ERR_OVERFLOW, "collider: " + std::to_string(nNew) + " contacts exceed the limit of " +
+                                          std::to_string(h->contactLimit) + " (wdem_set_contact_limit)");
   const bool hertz = (h->P.cp2 == WDEM_CP2_HERTZ);
   if (nNew > neu.cap || neu.hertz != hertz || neu.geom != h->keepGeom || neu.peri != h->periodic || neu.ell != h->hasEll) {
     long long cap = std::max<long long>(nNew + nNew / 4 + 1024, neu.cap);
@@ -900,6 +909,9 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
   if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "upload particles and params before contacts");
   const long long nc = c->n;
   if (nc < 0) return WDEM_ERR_ARG;
+  if (h->contactLimit > 0 && nc > h->contactLimit)
+    return fail(h, WDEM_ERR_OVERFLOW, "upload: " + std::to_string(nc) + " contacts exceed the limit of " +
+                                          std::to_string(h->contactLimit) + " (wdem_set_contact_limit)");
   if (nc > 0 && (!c->idA || !c->idB || !c->real || !c->stepCreated)) return fail(h, WDEM_ERR_ARG, "null contact id/state array");
   cudaSetDevice(h->device);
   cudaStream_t s = h->stream;
@@ -1518,6 +1530,12 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
   }
   *nPairs = total;
   h->particlesSet = false;  // the particle arrays no longer hold a scene
+  return WDEM_OK;
+}
+
+int wdem_set_contact_limit(wdem_handle* h, int64_t maxContacts) {
+  if (!h || maxContacts < 0) return WDEM_ERR_ARG;
+  h->contactLimit = maxContacts;
   return WDEM_OK;
 }
 
