@@ -379,6 +379,23 @@ int wdem_ell_log_read(wdem_handle* h, float* out, int64_t cap, int64_t* n);
  * Synchronises the handle's stream before returning. */
 int wdem_get_stress_noalloc(wdem_handle* h, double* stress);
 
+/* Remove particles between steps, on the device (DemField::removeParticle, src/dem/Particle.cpp:483-530,
+ * as Outlet::run calls it, src/dem/Outlet.cpp:15-116): the m slots `ids` become inert (mask 0, so that
+ * Collider::mayCollide never pairs them; all DOFs blocked; zero velocity) and are parked at park[3k..3k+2]
+ * when park is not NULL; every contact of a removed particle dies with its history.  The forces of the step
+ * just run (removed contacts included, as the reference applied them before the outlet ran) are kept for the
+ * next integration; the collider runs in full at the next step.  Only the ids, the park positions and the
+ * contact states are touched: nothing is copied back to the host. */
+int wdem_remove_particles(wdem_handle* h, int32_t m, const int32_t* ids, const double* park);
+
+/* Insert particles between steps, on the device (particles added by RandomInlet::run,
+ * src/dem/Inlet.cpp:228-515): the p->n particles of p go to the slots ids[0 .. p->n) -- slots of removed
+ * particles (below the current count) or new slots that extend the particle count contiguously, up to the
+ * handle's capacity.  Spheres and ellipsoids (the latter when the handle already holds ellipsoids); walls
+ * go through wdem_upload_particles.  The other particles and the contact container stay on the device; the
+ * collider runs in full at the next step. */
+int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* ids);
+
 /* Upper bound on the contact container (real and potential pairs) for callers that budget device memory;
  * 0 (the default) = grow as needed.  No counterpart in the reference, whose container grows without
  * bound.  A collider run or a contact upload that needs more than maxContacts stops with

@@ -7,6 +7,8 @@ oracle.  Only the calls GpuDemEngine makes are provided.
 import ctypes as C
 from types import SimpleNamespace
 
+import numpy as np
+
 from oracle import bridge
 from woo_gb300 import abi
 
@@ -35,6 +37,7 @@ class OracleHandle:
     def upload_particles(self, pa):
         if pa.n > self.max_particles:
             raise abi.WdemError(-1, "too many particles")
+        self._pa = pa.copy()
         if self.o is None:
             self.o = bridge.Oracle(self.params, pa)
             return
@@ -83,6 +86,45 @@ class OracleHandle:
 
     def energy(self):
         return self.o.energy()
+
+    # removal and insertion between steps, restated on the host: download, edit, upload (the semantics of
+    # wdem_remove_particles / wdem_add_particles: removed slots inert and parked, their contacts gone, the
+    # forces of the step just run kept for the next integration)
+    def _state(self):
+        pa = self._pa.copy()
+        self.download_particles(pa)
+        return pa
+
+    def remove_particles(self, ids, park=None):
+        pa = self._state()
+        con = self.download_contacts().without_particles(ids)
+        ids = list(ids)
+        pa.mask[ids] = 0
+        pa.flags[ids] |= 63
+        pa.vel[ids] = 0
+        pa.angVel[ids] = 0
+        if park is not None:
+            pa.pos[ids] = park
+        self.upload_particles(pa)
+        self.set_params(self.params)
+        self.upload_contacts(con)
+
+    def add_particles(self, particles, ids):
+        pa = self._state()
+        con = self.download_contacts()
+        n = max(pa.n, max(ids) + 1)
+        if n > pa.n:
+            grown = abi.ParticleArrays(n)
+            for k, v in pa.__dict__.items():
+                if isinstance(v, np.ndarray):
+                    getattr(grown, k)[:pa.n] = v
+            pa = grown
+        for k, v in particles.__dict__.items():
+            if isinstance(v, np.ndarray):
+                getattr(pa, k)[list(ids)] = v
+        self.upload_particles(pa)
+        self.set_params(self.params)
+        self.upload_contacts(con)
 
 
 def run_on_oracle(monkeypatch, scene, n):

@@ -109,7 +109,8 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_make_cloud", "wdem_get_stream", "wdem_write_state", "wdem_read_state", "wdem_launch_count",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
-           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii", "wdem_set_contact_limit"]
+           "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii", "wdem_set_contact_limit",
+           "wdem_remove_particles", "wdem_add_particles"]
 
 
 def ptr(a, ctype):
@@ -149,6 +150,15 @@ class ParticleArrays:
         for k, v in self.__dict__.items():
             if isinstance(v, np.ndarray):
                 setattr(o, k, v.copy())
+        return o
+
+    def take(self, index):
+        """The particles selected by `index` (integer indices), in that order."""
+        idx = np.asarray(index, np.int64)
+        o = ParticleArrays(len(idx))
+        for k, v in self.__dict__.items():
+            if isinstance(v, np.ndarray):
+                setattr(o, k, np.ascontiguousarray(v[idx]))
         return o
 
     def struct(self):
@@ -287,6 +297,8 @@ def load(path=None):
         "wdem_ell_log": ([h, C.c_int64], C.c_int),
         "wdem_make_cloud_radii": ([D, D, C.c_int32, C.c_int64, D, C.c_uint64, C.c_int32, D, D], C.c_int64),
         "wdem_set_contact_limit": ([h, C.c_int64], C.c_int),
+        "wdem_remove_particles": ([h, C.c_int32, I32, D], C.c_int),
+        "wdem_add_particles": ([h, C.POINTER(Particles), I32], C.c_int),
         "wdem_ell_log_read": ([h, F32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -369,6 +381,22 @@ class Handle:
 
     def set_timing(self, on):
         self.check(self.lib.wdem_set_timing(self.h, 1 if on else 0))
+
+    def remove_particles(self, ids, park=None):
+        """Remove particles on the device (wdem_remove_particles): their slots become inert, their contacts
+        die; `park` (k x 3) gives the positions the slots are parked at."""
+        ids = np.ascontiguousarray(ids, np.int32)
+        pk = None if park is None else np.ascontiguousarray(park, np.float64).reshape(len(ids), 3)
+        self.check(self.lib.wdem_remove_particles(self.h, len(ids), ptr(ids, C.c_int32),
+                                                  None if pk is None else ptr(pk, C.c_double)))
+
+    def add_particles(self, particles, ids):
+        """Insert particles on the device (wdem_add_particles) into the slots `ids`."""
+        ids = np.ascontiguousarray(ids, np.int32)
+        if len(ids) != particles.n:
+            raise ValueError("one slot per added particle")
+        s = particles.struct()
+        self.check(self.lib.wdem_add_particles(self.h, C.byref(s), ptr(ids, C.c_int32)))
 
     def set_contact_limit(self, max_contacts):
         """Upper bound on the contact container (0 = none): beyond it a step fails with WDEM_ERR_OVERFLOW."""

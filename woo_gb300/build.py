@@ -18,7 +18,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwdem.so")
 
-SOURCES = ["k_contact.cu", "k_leapfrog.cu", "k_collider.cu", "wdem_api.cu", "wdem_pack.cu", "k_noalloc.cu", "k_mlp.cu"]
+SOURCES = ["k_contact.cu", "k_leapfrog.cu", "k_collider.cu", "wdem_api.cu", "wdem_pack.cu", "k_noalloc.cu", "k_mlp.cu",
+           "k_edit.cu"]
 # (source, object name, extra flags): the contracted variant of the step kernels
 VARIANTS = [("k_contact.cu", "k_contact_fma", ["-DWDEM_FMA", "--fmad=true"]),
             ("k_leapfrog.cu", "k_leapfrog_fma", ["-DWDEM_FMA", "--fmad=true"])]

@@ -209,6 +209,14 @@ struct wdem_handle {
   long long stressCap = 0;
   std::vector<DevMaterial> devMats;  // the materials table in the kernels' layout
   long long contactLimit = 0;        // wdem_set_contact_limit (0: none)
+  // particle removal / insertion (wdem_remove_particles, wdem_add_particles): per-particle flags, id list,
+  // park positions and the packed records of inserted particles
+  uint8_t* editGone = nullptr;
+  int* editIds = nullptr;
+  double* editPark = nullptr;
+  double4_32a* editRec = nullptr;
+  int4* editMeta = nullptr;
+  long long editCap = 0;
   double* dEnergy = nullptr;    // WDEM_E_COUNT accumulators
   double* ePartials = nullptr;  // block partials of the energy sums
   long long ePartialsCap = 0;
@@ -704,6 +712,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag);
   cudaFree(h->dst);
   cudaFree(h->staging);
+  cudaFree(h->editGone); cudaFree(h->editIds); cudaFree(h->editPark); cudaFree(h->editRec); cudaFree(h->editMeta);
   if (h->hst) cudaFreeHost(h->hst);
   if (h->hcounts) cudaFreeHost(h->hcounts);
   for (auto e : h->evPool) cudaEventDestroy(e);
@@ -1530,6 +1539,155 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
   }
   *nPairs = total;
   h->particlesSet = false;  // the particle arrays no longer hold a scene
+  return WDEM_OK;
+}
+
+namespace {
+// device buffers for an edit of m particles (the per-particle flags cover the capacity)
+int ensureEdit(wdem_handle* h, long long m) {
+  if (!h->editGone) {
+    CK(dalloc(h->editGone, (size_t)h->N));
+    CK(cudaMemset(h->editGone, 0, (size_t)h->N));
+  }
+  if (m > h->editCap) {
+    const long long cap = std::max<long long>(m, 1024);
+    CK(dalloc(h->editIds, cap)); CK(dalloc(h->editPark, 3 * cap));
+    CK(dalloc(h->editRec, (size_t)EDIT_RECORDS * cap)); CK(dalloc(h->editMeta, cap));
+    h->editCap = cap;
+  }
+  return WDEM_OK;
+}
+// the forces of the step just run into the particle arrays, for the next integration: the contact
+// container changes before it, but those forces were applied in the step that ran (ContactLoop, then the
+// host engines)
+void materialiseForces(wdem_handle* h) {
+  if (!h->forcesInArrays) {
+    launch_reduce_forces(h->stream, h->P, h->d, h->n, h->buf[h->cur].c, h->csr);
+    h->forcesInArrays = true;
+  }
+}
+}  // namespace
+
+int wdem_remove_particles(wdem_handle* h, int32_t m, const int32_t* ids, const double* park) {
+  if (!h || m < 0 || (m > 0 && !ids)) return WDEM_ERR_ARG;
+  if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "remove particles after particles and params were set");
+  std::vector<char> seen(h->n, 0);
+  for (int k = 0; k < m; k++) {
+    if (ids[k] < 0 || ids[k] >= h->n) return fail(h, WDEM_ERR_ARG, "particle id " + std::to_string(ids[k]) + " out of range");
+    if (seen[ids[k]]) return fail(h, WDEM_ERR_ARG, "particle id " + std::to_string(ids[k]) + " given twice");
+    seen[ids[k]] = 1;
+  }
+  if (m == 0) return WDEM_OK;
+  cudaSetDevice(h->device);
+  int rc;
+  if ((rc = ensureEdit(h, m))) return rc;
+  cudaStream_t s = h->stream;
+  materialiseForces(h);
+  CK(cudaMemcpyAsync(h->editIds, ids, m * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (park) CK(cudaMemcpyAsync(h->editPark, park, 3 * (size_t)m * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_kill(s, h->d, h->n, h->editIds, m, park ? h->editPark : nullptr, h->editGone, h->buf[h->cur].c, h->nContacts);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  h->needRebuild = true;
+  h->actValid = false;
+  return WDEM_OK;
+}
+
+int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* ids) {
+  if (!h || !p || p->n < 0 || (p->n > 0 && !ids)) return WDEM_ERR_ARG;
+  if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "add particles after particles and params were set");
+  const int m = p->n;
+  if (m == 0) return WDEM_OK;
+  if (!p->shape || !p->radius || !p->material || !p->mask || !p->flags || !p->mass || !p->inertia || !p->pos || !p->ori ||
+      !p->vel || !p->angVel || !p->force || !p->torque)
+    return fail(h, WDEM_ERR_ARG, "null particle array");
+  int newN = h->n;
+  for (int k = 0; k < m; k++) {
+    if (ids[k] < 0 || ids[k] >= h->N) return fail(h, WDEM_ERR_ARG, "slot " + std::to_string(ids[k]) + " outside the handle capacity");
+    newN = std::max(newN, ids[k] + 1);
+  }
+  std::vector<char> seen(newN, 0);
+  for (int k = 0; k < m; k++) {
+    if (seen[ids[k]]) return fail(h, WDEM_ERR_ARG, "slot " + std::to_string(ids[k]) + " given twice");
+    seen[ids[k]] = 1;
+  }
+  for (int i = h->n; i < newN; i++)
+    if (!seen[i]) return fail(h, WDEM_ERR_ARG, "new slots must extend the particle count contiguously (slot " + std::to_string(i) + " missing)");
+  std::vector<double4_32a> rec((size_t)EDIT_RECORDS * m);
+  std::vector<int4> meta(m);
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (int k = 0; k < m; k++) {
+    const int sh = p->shape[k];
+    if (sh == WDEM_SHAPE_WALL) return fail(h, WDEM_ERR_UNSUPPORTED, "walls are added through wdem_upload_particles");
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_ELLIPSOID) return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape");
+    if (p->material[k] < 0 || p->material[k] >= (int)h->mats.size())
+      return fail(h, WDEM_ERR_ARG, "material index out of range for an added particle");
+    const unsigned fl = p->flags[k];
+    if (fl & (WDEM_CLUMP_CLUMP | WDEM_CLUMP_CLUMPED)) return fail(h, WDEM_ERR_UNSUPPORTED, "clumps are not supported");
+    const double* in = p->inertia + 3 * k;
+    const bool asph = !(in[0] == in[1] && in[1] == in[2]) && (fl & 56u) != 56u;
+    if ((sh == WDEM_SHAPE_ELLIPSOID || asph) && !h->hasEll)
+      return fail(h, WDEM_ERR_UNSUPPORTED, "ellipsoids or aspherical nodes in a handle without them: use wdem_upload_particles");
+    if ((sh == WDEM_SHAPE_ELLIPSOID || asph) && h->periodic)
+      return fail(h, WDEM_ERR_UNSUPPORTED, "ellipsoids and aspherical nodes in a periodic cell are not supported");
+    const int sc = p->scene ? p->scene[k] : 0;
+    if (sc < 0 || sc >= std::max(1, h->cs.nScenes)) return fail(h, WDEM_ERR_ARG, "scene index out of range for an added particle");
+    double r = p->radius[k];
+    double sa[3] = {r, r, r};
+    if (sh == WDEM_SHAPE_ELLIPSOID) {
+      if (!p->semiAxes) return fail(h, WDEM_ERR_ARG, "ellipsoids need wdem_particles.semiAxes");
+      for (int q = 0; q < 3; q++) sa[q] = p->semiAxes[3 * k + q];
+      if (!(sa[0] > 0 && sa[1] > 0 && sa[2] > 0)) return fail(h, WDEM_ERR_ARG, "ellipsoid semi-axes must be positive");
+      r = std::max(sa[0], std::max(sa[1], sa[2]));
+    }
+    double4_32a* q = rec.data() + (size_t)EDIT_RECORDS * k;
+    q[0] = make_double4_32a(p->pos[3 * k], p->pos[3 * k + 1], p->pos[3 * k + 2], r);
+    q[1] = make_double4_32a(p->vel[3 * k], p->vel[3 * k + 1], p->vel[3 * k + 2], p->mass[k]);
+    q[2] = make_double4_32a(p->angVel[3 * k], p->angVel[3 * k + 1], p->angVel[3 * k + 2], 0);
+    q[3] = make_double4_32a(in[0], in[1], in[2], 0);
+    q[4] = make_double4_32a(p->ori[4 * k], p->ori[4 * k + 1], p->ori[4 * k + 2], p->ori[4 * k + 3]);
+    q[5] = make_double4_32a(p->force[3 * k], p->force[3 * k + 1], p->force[3 * k + 2], 0);
+    q[6] = make_double4_32a(p->torque[3 * k], p->torque[3 * k + 1], p->torque[3 * k + 2], 0);
+    q[7] = make_double4_32a(sa[0], sa[1], sa[2], 0);
+    q[8] = p->angMom ? make_double4_32a(p->angMom[3 * k], p->angMom[3 * k + 1], p->angMom[3 * k + 2], 0)
+                     : make_double4_32a(nan, nan, nan, 0);
+    const bool ipos = in[0] > 0 && in[1] > 0 && in[2] > 0;
+    meta[k] = make_int4(sh | (1 << 8) | (asph ? META_ASPH : 0) | (ipos ? META_IPOS : 0) | (sc << META_SCENE_SHIFT),
+                        p->material[k], (int)p->mask[k], (int)fl);
+  }
+  cudaSetDevice(h->device);
+  int rc;
+  if ((rc = ensureEdit(h, m))) return rc;
+  cudaStream_t s = h->stream;
+  materialiseForces(h);
+  CK(cudaMemcpyAsync(h->editIds, ids, m * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(h->editRec, rec.data(), rec.size() * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(h->editMeta, meta.data(), m * sizeof(int4), cudaMemcpyHostToDevice, s));
+  launch_put(s, h->d, h->editIds, m, h->editRec, h->editMeta, h->hasEll);
+  CK(cudaGetLastError());
+  // host copies of the static data; the new slots join the collider's sorted set
+  const int oldN = h->n;
+  h->shape.resize(newN); h->mat.resize(newN); h->radius.resize(newN); h->semi.resize(3 * (size_t)newN);
+  for (int k = 0; k < m; k++) {
+    const int i = ids[k];
+    h->shape[i] = p->shape[k]; h->mat[i] = p->material[k]; h->radius[i] = p->radius[k];
+    const double4_32a sv = rec[(size_t)EDIT_RECORDS * k + 7];
+    h->semi[3 * i] = sv.x; h->semi[3 * i + 1] = sv.y; h->semi[3 * i + 2] = sv.z;
+  }
+  if (newN > oldN) {
+    const size_t first = h->smallIds.size();
+    for (int i = oldN; i < newN; i++) h->smallIds.push_back(i);
+    CK(cudaMemcpyAsync(h->dSmall + first, h->smallIds.data() + first, (h->smallIds.size() - first) * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  h->n = newN;
+  h->matsChecked = -1;
+  h->gravAccDirty = true;
+  h->needRebuild = true;
+  h->actValid = false;
+  resolveVerlet(h);
+  fillStepParams(h);
   return WDEM_OK;
 }
 

@@ -302,6 +302,11 @@ void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long
                      float* grad, float* loss);
 void mlp_launch_adam(cudaStream_t s, float* w, float* m, float* v, float* grad, uint16_t* wbf, float lr, float b1,
                      float b2, float c1, float c2, float eps);
+// k_edit.cu: particle removal and insertion between steps
+enum { EDIT_RECORDS = 9 };  // double4 records per inserted particle (posr .. torque, semi, angMom)
+void launch_kill(cudaStream_t s, Particles p, int n, const int* ids, int m, const double* park, uint8_t* gone,
+                 Contacts c, long long nc);
+void launch_put(cudaStream_t s, Particles p, const int* ids, int m, const double4_32a* rec, const int4* meta, bool withRot);
 // k_noalloc.cu: the stress sum with its scratch in a fixed device array (no allocation)
 long long stress_noalloc_max_contacts();
 cudaError_t noalloc_scratch(int device, void** addr);

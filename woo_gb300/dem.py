@@ -1140,26 +1140,36 @@ class GpuDemEngine(Engine):
             up.angVel[ids] = 0
         if dead:
             up.mask[dead] = 0
-            # parked on live spheres (spread over them, so that many removed particles do not crowd one
-            # grid cell), so that a particle removed far outside the domain does not stretch the grid
-            anchors = [p.id for p in field.par if isinstance(p.shape, Sphere)]
-            if anchors:
-                up.pos[dead] = pa.pos[np.asarray(anchors)[np.arange(len(dead)) % len(anchors)]]
+            park = self._park_positions(field, pa, dead)
+            if park is not None:
+                up.pos[dead] = park
         return up
 
+    def _park_positions(self, field, pa, dead):
+        """Where the slots `dead` (sorted) are parked: on live spheres, spread over them so that many removed
+        particles do not crowd one grid cell, and so that a particle removed far outside the domain does not
+        stretch the collider's grid."""
+        anchors = [p.id for p in field.par if isinstance(p.shape, Sphere)]
+        if not anchors:
+            return None
+        return pa.pos[np.asarray(anchors)[np.arange(len(dead)) % len(anchors)]]
+
     def _remove_particles(self, field, ids):
-        """Remove particles from a running field: their contacts leave the container and their slots
-        become dead; the other contacts keep their history.  The collider rebuilds at the next step,
-        which does not change the motion (every pair that can touch before the next rebuild is found)."""
+        """Remove particles from a running field, on the device (wdem_remove_particles): their contacts
+        leave the container and their slots become dead; the other contacts keep their history and nothing
+        but the ids and park positions crosses to the device.  The collider rebuilds at the next step, which
+        does not change the motion (every pair that can touch before the next rebuild is found)."""
         if field._stale:
             self._download_particles(field)
-        con = self._download_contacts().without_particles(ids)
-        field._dead.update(int(i) for i in ids)
-        field._moving[list(ids)] = False
-        self._h.upload_particles(self._device_view(field, field._arrays))
-        self._h.set_params(self._params)
-        self._h.upload_contacts(con)
-        field._dirty.clear()
+        ids = sorted(int(i) for i in ids)
+        field._dead.update(ids)
+        field._moving[ids] = False
+        dead = sorted(field._dead)
+        park = self._park_positions(field, field._arrays, dead)
+        if park is not None:
+            where = {d: k for k, d in enumerate(dead)}
+            park = park[[where[i] for i in ids]]
+        self._h.remove_particles(ids, park)
         field._con_cache = None
 
     # ------------------------------------------------------------------ engine protocol
@@ -1311,7 +1321,15 @@ class GpuDemEngine(Engine):
         n = pa.n
         kin = {"pos", "vel", "angVel", "ori"}
         dv = self._device_view(field, pa)
-        if field._dirty <= kin:
+        added = sorted(getattr(field, "_added", ()))
+        if added and field._dirty <= kin | {"added"} and n <= self._cap:
+            # particles from inlets go into their slots on the device (wdem_add_particles); the rest of
+            # the particle and contact state stays there
+            self._h.set_params(self._params)   # materials of added particles first
+            self._h.add_particles(dv.take(added), added)
+            if field._dirty & kin:
+                self._h.write_state(n, dv.pos.ctypes.data, dv.vel.ctypes.data, dv.angVel.ctypes.data, dv.ori.ctypes.data)
+        elif field._dirty <= kin:
             self._h.write_state(n, dv.pos.ctypes.data, dv.vel.ctypes.data, dv.angVel.ctypes.data, dv.ori.ctypes.data)
         else:
             # mass/inertia/flags/masks changed or particles added: full upload, keeping the contact history
@@ -1323,6 +1341,7 @@ class GpuDemEngine(Engine):
             self._h.set_params(self._params)
             self._h.upload_contacts(con)
         field._dirty.clear()
+        field._added = set()
 
     def _remove_contacts_where(self, field, ids, may_collide):
         """Drop the contacts of `ids` for which may_collide(idA, idB) is false; the others keep their
@@ -1367,6 +1386,9 @@ class GpuDemEngine(Engine):
             field._dead.discard(p.id)
             field._moving[p.id] = getattr(p, "_integrated", True)
         field._dirty.add("added")
+        if not hasattr(field, "_added"):
+            field._added = set()
+        field._added.update(p.id for p in pars)
         field._con_cache = None
 
     def _add_material(self, m):
