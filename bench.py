@@ -432,6 +432,44 @@ def e2e_measure(h, n, ne, world, local, barrier):
     return e2e, roundtrip
 
 
+def edit_event_cost(h, spec, k=1000):
+    """Cost of an outlet / inlet event at the handle's size: k spheres removed on the device
+    (wdem_remove_particles) and put back into their slots (wdem_add_particles), against the whole-state
+    host round trip that such an event needs without those calls (particles and contacts down, filtered on
+    the host, up again).  Wall times of the calls, which synchronise."""
+    import torch
+    from woo_gb300 import abi
+    n = spec.particles.n
+    rng = np.random.default_rng(5)
+    ids = np.sort(rng.choice(np.arange(6, n), k, replace=False)).astype(np.int32)
+    before = h.download_particles(spec.particles.copy())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h.remove_particles(ids)
+    t_rm = time.perf_counter() - t0
+    back = before.take(ids)
+    back.vel[:] = 0
+    back.angVel[:] = 0
+    t0 = time.perf_counter()
+    h.add_particles(back, ids)
+    t_add = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pa = h.download_particles(spec.particles.copy())
+    ca = h.download_contacts()
+    keep = ~(np.isin(ca.idA, ids) | np.isin(ca.idB, ids))
+    ca = ca.take(keep)
+    h.upload_particles(pa)
+    p = copy_params(spec.params)
+    p.step = h.status().step
+    h.set_params(p)
+    h.upload_contacts(ca)
+    t_host = time.perf_counter() - t0
+    return {"particles": int(k), "remove_ms": t_rm * 1e3, "add_ms": t_add * 1e3, "host_roundtrip_ms": t_host * 1e3,
+            "contacts_in_container": int(ca.n),
+            "what": "k spheres removed on the device and re-inserted into their slots, against the host round trip "
+                    "of the whole particle and contact state that the same event costs without those calls"}
+
+
 def common_config(args, spec):
     """The config object both arms print (the driver compares them)."""
     return {"workload": args.workload, "n_particles": int(spec.particles.n), "dt": float(spec.params.dt),
@@ -550,6 +588,7 @@ def run_gpu(args, rank, world, local):
                                                 f"the same settled {n}-particle state at step {sp.step} "
                                                 f"(particles and contacts with history from the GPU), {{steps}} steps after 2 untimed")
             settled["vs_cpu_baseline"] = settled["value"] / settled["cpu_baseline"]["value"]
+        settled["edit_events"] = edit_event_cost(hs, spec)
         hs.close()
     clk = clocks.stop()
     clk["interval"] = "sampled over the GPU run: warm-up, timed regions, windows, e2e and settling"
