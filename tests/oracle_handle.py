@@ -10,7 +10,7 @@ from types import SimpleNamespace
 import numpy as np
 
 from oracle import bridge
-from woo_gb300 import abi
+from woo_gb300 import abi, scenes
 
 
 class OracleHandle:
@@ -95,6 +95,14 @@ class OracleHandle:
         self.download_particles(pa)
         return pa
 
+    def _reupload(self, pa, con):
+        # the oracle takes Scene.step from the parameters: keep the current one
+        q = scenes.copy_params(self.params)
+        q.step = self.o.lib.orc_step_count(self.o.h)
+        self.upload_particles(pa)
+        self.set_params(q)
+        self.upload_contacts(con)
+
     def remove_particles(self, ids, park=None):
         pa = self._state()
         con = self.download_contacts().without_particles(ids)
@@ -105,9 +113,7 @@ class OracleHandle:
         pa.angVel[ids] = 0
         if park is not None:
             pa.pos[ids] = park
-        self.upload_particles(pa)
-        self.set_params(self.params)
-        self.upload_contacts(con)
+        self._reupload(pa, con)
 
     def add_particles(self, particles, ids):
         pa = self._state()
@@ -122,9 +128,7 @@ class OracleHandle:
         for k, v in particles.__dict__.items():
             if isinstance(v, np.ndarray):
                 getattr(pa, k)[list(ids)] = v
-        self.upload_particles(pa)
-        self.set_params(self.params)
-        self.upload_contacts(con)
+        self._reupload(pa, con)
 
 
 def run_on_oracle(monkeypatch, scene, n):
