@@ -82,6 +82,8 @@ def parse():
     ap.add_argument("--arith", default="fma", choices=["fma", "exact"],
                     help="arithmetic of the contact and integrator kernels (wdem_params.arith): FP64 with FMA "
                          "contraction, or the reference's IEEE operations bit for bit")
+    ap.add_argument("--autotune", default="auto", choices=["auto", "on", "off"],
+                    help="tune the kernels' launch shape (wdem_autotune) before the timed region; auto: batch512 only")
     ap.add_argument("--profile-region", default="main", choices=["main", "settled", "none"],
                     help="timed region bracketed by cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     a = ap.parse_args()
@@ -543,6 +545,21 @@ def run_gpu(args, rank, world, local):
     else:
         h = new_handle(spec, local)
     settled_steps = settle(h, spec) if args.workload == "hertz1M_settled" else 0
+    if args.autotune == "on" or (args.autotune == "auto" and args.workload == "batch512"):
+        # the fixed default launch shape first, then the autotuner's pick (both untimed for the line;
+        # the timed region below runs with the tuned shape)
+        st = torch.cuda.ExternalStream(h.stream(), device=local)
+        h.step(max(args.warmup, 3))
+        ms_fixed = timed_steps(h, st, args.steps, world, local, barrier)
+        default_shape = h.launch_shape()
+        t0 = time.time()
+        tune = h.autotune(5)
+        extra["autotune"] = {"default_shape": default_shape, "tuned_shape": tune["shape"],
+                             "tuner_ms_per_step_start": tune["ms_start"], "tuner_ms_per_step_best": tune["ms"],
+                             "tuning_seconds": time.time() - t0,
+                             "fixed_shape_value": replica_throughput(world, n, args.steps, ms_fixed / 1e3),
+                             "how": "coordinate descent over block sizes and blocks per SM of the contact pass, the "
+                                    "cull and the integrator, 5 timed steps per candidate (wdem_autotune)"}
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -614,6 +631,8 @@ def run_gpu(args, rank, world, local):
         out["settled"] = settled
     if "scene_by_scene" in extra:
         extra["batch_speedup_vs_scene_by_scene"] = out["value"] / extra["scene_by_scene"]["value"]
+    if "autotune" in extra:
+        extra["autotune"]["gain_over_fixed_shape"] = out["value"] / extra["autotune"]["fixed_shape_value"]
     out.update(extra)
     return out, spec
 

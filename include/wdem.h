@@ -396,6 +396,29 @@ int wdem_remove_particles(wdem_handle* h, int32_t m, const int32_t* ids, const d
  * collider runs in full at the next step. */
 int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* ids);
 
+/* Launch shape of the step kernels (no counterpart in the reference, which has none): threads per block of
+ * the contact pass's FP64 kernel (64, 128, 256), its resident blocks per SM (0 = as many as fit), threads
+ * per block of the contact cull (128, 256, 512) and of the integrator's first pass (128, 256, 512), blocks
+ * per SM of the integrator's list pass (0 = as many as fit).  Results do not depend on the shape (every
+ * contact and particle is computed alone; sums run in fixed orders): only the speed does. */
+typedef struct wdem_launch_shape {
+  int32_t contactsBlock;
+  int32_t contactsPerSM;
+  int32_t cullBlock;
+  int32_t integratorBlock;
+  int32_t listsPerSM;
+  int32_t _pad;
+} wdem_launch_shape;
+int wdem_set_launch_shape(wdem_handle* h, const wdem_launch_shape* shape);
+int wdem_get_launch_shape(wdem_handle* h, wdem_launch_shape* shape);
+
+/* Autotuner of the launch shape (no counterpart in the reference): runs the simulation forward, each
+ * candidate shape for stepsPerCandidate steps (after 2 untimed ones) with the per-phase CUDA-event times of
+ * the integrator and the contact pass as its cost, by coordinate descent over the five knobs starting from
+ * the current shape; keeps and returns the fastest shape and its cost and that of the starting shape (ms per
+ * step).  The run advances by the steps it takes (results are those of the same steps run untuned). */
+int wdem_autotune(wdem_handle* h, int32_t stepsPerCandidate, wdem_launch_shape* best, double* msBest, double* msStart);
+
 /* Upper bound on the contact container (real and potential pairs) for callers that budget device memory;
  * 0 (the default) = grow as needed.  No counterpart in the reference, whose container grows without
  * bound.  A collider run or a contact upload that needs more than maxContacts stops with

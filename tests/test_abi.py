@@ -34,7 +34,8 @@ def test_struct_layouts_match_header(tmp_path):
     """Every field offset and struct size of the ctypes mirrors equals what the C compiler makes of
     include/wdem.h."""
     structs = {"wdem_material": abi.Material, "wdem_params": abi.Params, "wdem_particles": abi.Particles,
-               "wdem_contacts": abi.Contacts, "wdem_cell": abi.Cell, "wdem_status": abi.Status}
+               "wdem_contacts": abi.Contacts, "wdem_cell": abi.Cell, "wdem_status": abi.Status,
+               "wdem_launch_shape": abi.LaunchShape}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/wdem.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -89,6 +89,14 @@ class Contacts(C.Structure):
                 ("cellDist", I32)]
 
 
+class LaunchShape(C.Structure):
+    _fields_ = [("contactsBlock", C.c_int32), ("contactsPerSM", C.c_int32), ("cullBlock", C.c_int32),
+                ("integratorBlock", C.c_int32), ("listsPerSM", C.c_int32), ("_pad", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
+
+
 class Cell(C.Structure):
     _fields_ = [("periodic", C.c_int32), ("homoDeform", C.c_int32), ("hSize", C.c_double * 9),
                 ("trsf", C.c_double * 9), ("gradV", C.c_double * 9), ("nextGradV", C.c_double * 9),
@@ -110,7 +118,8 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_fp64_peak", "wdem_set_cell", "wdem_get_cell", "wdem_get_stress",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
            "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii", "wdem_set_contact_limit",
-           "wdem_remove_particles", "wdem_add_particles"]
+           "wdem_remove_particles", "wdem_add_particles", "wdem_set_launch_shape", "wdem_get_launch_shape",
+           "wdem_autotune"]
 
 
 def ptr(a, ctype):
@@ -298,6 +307,9 @@ def load(path=None):
         "wdem_make_cloud_radii": ([D, D, C.c_int32, C.c_int64, D, C.c_uint64, C.c_int32, D, D], C.c_int64),
         "wdem_set_contact_limit": ([h, C.c_int64], C.c_int),
         "wdem_remove_particles": ([h, C.c_int32, I32, D], C.c_int),
+        "wdem_set_launch_shape": ([h, C.POINTER(LaunchShape)], C.c_int),
+        "wdem_get_launch_shape": ([h, C.POINTER(LaunchShape)], C.c_int),
+        "wdem_autotune": ([h, C.c_int32, C.POINTER(LaunchShape), C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "wdem_add_particles": ([h, C.POINTER(Particles), I32], C.c_int),
         "wdem_ell_log_read": ([h, F32, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
     }
@@ -397,6 +409,25 @@ class Handle:
             raise ValueError("one slot per added particle")
         s = particles.struct()
         self.check(self.lib.wdem_add_particles(self.h, C.byref(s), ptr(ids, C.c_int32)))
+
+    def launch_shape(self):
+        s = LaunchShape()
+        self.check(self.lib.wdem_get_launch_shape(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def set_launch_shape(self, **shape):
+        s = LaunchShape()
+        self.check(self.lib.wdem_get_launch_shape(self.h, C.byref(s)))
+        for k, v in shape.items():
+            setattr(s, k, int(v))
+        self.check(self.lib.wdem_set_launch_shape(self.h, C.byref(s)))
+
+    def autotune(self, steps_per_candidate=10):
+        """Pick the fastest launch shape on the running simulation (wdem_autotune); returns
+        dict(shape=..., ms=..., ms_start=...)."""
+        s, a, b = LaunchShape(), C.c_double(), C.c_double()
+        self.check(self.lib.wdem_autotune(self.h, int(steps_per_candidate), C.byref(s), C.byref(a), C.byref(b)))
+        return {"shape": s.as_dict(), "ms": a.value, "ms_start": b.value}
 
     def set_contact_limit(self, max_contacts):
         """Upper bound on the contact container (0 = none): beyond it a step fails with WDEM_ERR_OVERFLOW."""

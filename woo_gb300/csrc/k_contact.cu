@@ -504,11 +504,12 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   o[OUT_TB] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
 }
 
-// 128 threads, 4 blocks per SM (<= 128 registers a thread, no spills): one wave of the 152 x 4 blocks
-// that launch_contacts starts
-template <int LAW, int CP2, bool PERI, bool ELL>
-__global__ void __launch_bounds__(128, 4) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
-                                                  const unsigned* count, long long nc, DeviceStatus* st) {
+// BS threads a block and 512 threads an SM (<= 128 registers a thread, no spills); the grid (blocks per
+// SM) and BS are the launch shape of the step parameters, chosen by the autotuner or the defaults (128
+// threads, 4 blocks per SM: one wave)
+template <int LAW, int CP2, bool PERI, bool ELL, int BS>
+__global__ void __launch_bounds__(BS, 512 / BS) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
+                                                        const unsigned* count, long long nc, DeviceStatus* st) {
   const unsigned m = workLen(count);
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
     contactBody<LAW, CP2, PERI, ELL>(P, p, c, (long long)workItem(work, count, nc, k), st);
@@ -636,8 +637,8 @@ __device__ __forceinline__ void cullAppend(unsigned* work, unsigned* count, long
 // the list order is irrelevant because each contact is processed independently.  FULL: one thread per
 // contact of the container, and the contacts that may need the pass before the next rebuild are
 // listed (act); otherwise the grid walks that list only.
-template <bool PERI, bool ELL, bool FULL>
-__global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
+template <bool PERI, bool ELL, bool FULL, int BS>
+__global__ void __launch_bounds__(BS) k_contacts_cull(StepParams P, Particles p, Contacts c, long long nc,
                                                        unsigned* work, unsigned* count, DeviceStatus* st) {
   const long long first = (long long)blockIdx.x * blockDim.x;
   const long long m = FULL ? nc : (long long)st->actCount;
@@ -655,6 +656,38 @@ __global__ void __launch_bounds__(256) k_contacts_cull(StepParams P, Particles p
   }
 }
 
+// the cull with the block size of the launch shape
+template <bool PERI, bool ELL>
+static void launchCull(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, unsigned* count,
+                       DeviceStatus* st, bool full) {
+  const int bs = P.shCullBlock == 128 || P.shCullBlock == 512 ? P.shCullBlock : 256;
+  const long long sms = P.numSMs > 0 ? P.numSMs : 152;
+  // full pass: a thread per contact; list pass: a grid-stride walk of the active list (2048 threads an SM)
+  const unsigned cb = full ? (unsigned)((nc + bs - 1) / bs) : (unsigned)std::min<long long>((nc + bs - 1) / bs, sms * (2048 / bs));
+#define WDEM_CULL(BS_)                                                                                              \
+  (full ? k_contacts_cull<PERI, ELL, true, BS_> : k_contacts_cull<PERI, ELL, false, BS_>)<<<cb, BS_, 0, s>>>(      \
+      P, p, c, nc, c.work, count, st)
+  if (bs == 128) WDEM_CULL(128);
+  else if (bs == 512) WDEM_CULL(512);
+  else WDEM_CULL(256);
+#undef WDEM_CULL
+  ++::wdem::g_kernel_launches;
+}
+// the FP64 pass with the block size and blocks per SM of the launch shape
+template <int LAW, int CP2, bool PERI, bool ELL>
+static void launchHeavy(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, unsigned* count,
+                        DeviceStatus* st) {
+  const int bs = P.shContactsBlock == 64 || P.shContactsBlock == 256 ? P.shContactsBlock : 128;
+  const long long sms = P.numSMs > 0 ? P.numSMs : 152;
+  const long long perSM = P.shContactsPerSM > 0 ? P.shContactsPerSM : 512 / bs;
+  const long long need = (nc + bs - 1) / bs;
+  const unsigned hb = (unsigned)std::max<long long>(1, std::min(need, sms * perSM));
+  if (bs == 64) k_contacts<LAW, CP2, PERI, ELL, 64><<<hb, 64, 0, s>>>(P, p, c, c.work, count, nc, st);
+  else if (bs == 256) k_contacts<LAW, CP2, PERI, ELL, 256><<<hb, 256, 0, s>>>(P, p, c, c.work, count, nc, st);
+  else k_contacts<LAW, CP2, PERI, ELL, 128><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st);
+  ++::wdem::g_kernel_launches;
+}
+
 void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, DeviceStatus* st,
                      bool full, const uint16_t* warmBf, const float* warmF) {
   if (nc <= 0) {
@@ -664,29 +697,21 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   unsigned* count = &st->workCount;  // workCount, workPot
   cudaMemsetAsync(count, 0, 2 * sizeof(unsigned), s);
   if (full) cudaMemsetAsync(&st->actCount, 0, sizeof(unsigned), s);
-  // full pass: a thread per contact; list pass: a grid-stride walk of the active list
-  const unsigned cb = full ? (unsigned)((nc + 255) / 256) : (unsigned)std::min<long long>((nc + 255) / 256, 152 * 8);
-  // the FP64 pass loops over the work list (length known on the device only): 4 blocks per SM fill the
-  // GPU at its register count, and no more blocks are launched to find the list short
-  const long long hb0 = (nc + 127) / 128;
-  const unsigned hb = (unsigned)(hb0 < 152 * 4 ? hb0 : 152 * 4);
+  // the FP64 pass loops over the work list (length known on the device only): by default 4 blocks of 128
+  // per SM fill the GPU at its register count, and no more blocks are launched to find the list short
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
-    (full ? k_contacts_cull<false, true, true> : k_contacts_cull<false, true, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
+    launchCull<false, true>(s, P, p, c, nc, count, st, full);
     if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF);
-    (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
+    launchHeavy<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true>(s, P, p, c, nc, count, st);
   } else if (P.periodic) {
-    (full ? k_contacts_cull<true, false, true> : k_contacts_cull<true, false, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
-    if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
-    else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
+    launchCull<true, false>(s, P, p, c, nc, count, st, full);
+    if (P.law == WDEM_LAW_IDEALELPL) launchHeavy<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, true, false>(s, P, p, c, nc, count, st);
+    else launchHeavy<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, true, false>(s, P, p, c, nc, count, st);
   } else {
-    (full ? k_contacts_cull<false, false, true> : k_contacts_cull<false, false, false>)<<<cb, 256, 0, s>>>(P, p, c, nc, c.work, count, st), ++::wdem::g_kernel_launches;
-    if (P.law == WDEM_LAW_IDEALELPL)
-      (k_contacts<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
-    else
-      (k_contacts<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st), ++::wdem::g_kernel_launches);
+    launchCull<false, false>(s, P, p, c, nc, count, st, full);
+    if (P.law == WDEM_LAW_IDEALELPL) launchHeavy<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, false>(s, P, p, c, nc, count, st);
+    else launchHeavy<WDEM_LAW_HERTZ_DMT, WDEM_CP2_HERTZ, false, false>(s, P, p, c, nc, count, st);
   }
 }
 

@@ -621,9 +621,9 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
 // First pass: particles without contact forces this step.  Those that a real contact touched are
 // compacted into touchList instead: their force gather and divisions would hold up the FP64 pipe
 // for whole warps of gravity-only neighbours.
-template <bool PERI>
-__global__ void __launch_bounds__(256, 4) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
-                                                        DeviceStatus* st) {
+template <bool PERI, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
+                                                               DeviceStatus* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // all of the particle's loads are issued together, before the guard's and the list decision
@@ -665,18 +665,28 @@ __global__ void __launch_bounds__(256) k_leapfrog_lists(StepParams P, Particles 
   }
 }
 
-// resident blocks of the list pass on the whole GPU (one wave; queried once per instantiation)
+// resident blocks of the list pass on the whole GPU (one wave; queried once per instantiation), or the
+// launch shape's blocks per SM
 template <bool PERI>
-static unsigned listGrid() {
-  static unsigned g = 0;
-  if (g == 0) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+static unsigned listGrid(const StepParams& P) {
+  static int per = 0;
+  if (per == 0) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_leapfrog_lists<PERI>, 256, 0);
-    g = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per);
+    per = std::max(1, per);
   }
-  return g;
+  const int sms = P.numSMs > 0 ? P.numSMs : 152;
+  const int want = P.shListsPerSM > 0 ? std::min(P.shListsPerSM, per) : per;
+  return (unsigned)sms * (unsigned)want;
+}
+// the first pass with the block size of the launch shape
+template <bool PERI>
+static void launchFast(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
+  const int bs = P.shLeapBlock == 128 || P.shLeapBlock == 512 ? P.shLeapBlock : 256;
+  const unsigned blocks = (unsigned)((n + bs - 1) / bs);
+  if (bs == 128) k_leapfrog_fast<PERI, 128><<<blocks, 128, 0, s>>>(P, p, n, c, csr, st);
+  else if (bs == 512) k_leapfrog_fast<PERI, 512><<<blocks, 512, 0, s>>>(P, p, n, c, csr, st);
+  else k_leapfrog_fast<PERI, 256><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  ++::wdem::g_kernel_launches;
 }
 
 void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, int fromArrays, Contacts c, Csr csr,
@@ -687,12 +697,12 @@ void launch_leapfrog(cudaStream_t s, const StepParams& P, Particles p, int n, in
     // st->rotCount and st->touchCount are zero here: k_contacts_cull clears them for the next step (and
     // the handle starts at zero)
     if (P.periodic) {
-      const unsigned rb = std::min(blocks, listGrid<true>());
-      (k_leapfrog_fast<true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      const unsigned rb = std::min(blocks, listGrid<true>(P));
+      launchFast<true>(s, P, p, n, c, csr, st);
       (k_leapfrog_lists<true><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     } else {
-      const unsigned rb = std::min(blocks, listGrid<false>());
-      (k_leapfrog_fast<false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
+      const unsigned rb = std::min(blocks, listGrid<false>(P));
+      launchFast<false>(s, P, p, n, c, csr, st);
       (k_leapfrog_lists<false><<<rb, 256, 0, s>>>(P, p, n, c, csr, st), ++::wdem::g_kernel_launches);
     }
     return;

@@ -209,6 +209,8 @@ struct wdem_handle {
   long long stressCap = 0;
   std::vector<DevMaterial> devMats;  // the materials table in the kernels' layout
   long long contactLimit = 0;        // wdem_set_contact_limit (0: none)
+  wdem_launch_shape launchShape{128, 0, 256, 256, 0, 0};  // launch shape of the step kernels
+  int numSMs = 152;
   // particle removal / insertion (wdem_remove_particles, wdem_add_particles): per-particle flags, id list,
   // park positions and the packed records of inserted particles
   uint8_t* editGone = nullptr;
@@ -519,6 +521,9 @@ void fillStepParams(wdem_handle* h) {
   StepParams& P = h->P;
   P.dt = r.dt;
   P.step = h->step;
+  P.shContactsBlock = h->launchShape.contactsBlock; P.shContactsPerSM = h->launchShape.contactsPerSM;
+  P.shCullBlock = h->launchShape.cullBlock; P.shLeapBlock = h->launchShape.integratorBlock; P.shListsPerSM = h->launchShape.listsPerSM;
+  P.numSMs = h->numSMs;
   for (int k = 0; k < 3; k++) P.gravity[k] = r.gravity[k];
   P.hasGravity = !(r.gravity[0] == 0 && r.gravity[1] == 0 && r.gravity[2] == 0);
   {
@@ -638,6 +643,12 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) { delete h; return WDEM_ERR_CUDA; }
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { delete h; return WDEM_ERR_CUDA; }
+  {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0) h->numSMs = sms;
+    h->P.numSMs = h->numSMs;
+    h->P.shContactsBlock = 128; h->P.shCullBlock = 256; h->P.shLeapBlock = 256;
+  }
   int N = maxParticles;
   Particles& d = h->d;
   bool ok = true;
@@ -1688,6 +1699,77 @@ int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* i
   h->actValid = false;
   resolveVerlet(h);
   fillStepParams(h);
+  return WDEM_OK;
+}
+
+namespace {
+bool shapeValid(const wdem_launch_shape& s) {
+  auto in = [](int v, std::initializer_list<int> ok) { for (int o : ok) if (v == o) return true; return false; };
+  return in(s.contactsBlock, {64, 128, 256}) && s.contactsPerSM >= 0 && s.contactsPerSM <= 64 &&
+         in(s.cullBlock, {128, 256, 512}) && in(s.integratorBlock, {128, 256, 512}) && s.listsPerSM >= 0 &&
+         s.listsPerSM <= 64;
+}
+}  // namespace
+
+int wdem_set_launch_shape(wdem_handle* h, const wdem_launch_shape* shape) {
+  if (!h || !shape) return WDEM_ERR_ARG;
+  if (!shapeValid(*shape)) return fail(h, WDEM_ERR_ARG, "launch shape: block sizes 64/128/256 (contacts), 128/256/512 (cull, integrator); blocks per SM 0..64");
+  h->launchShape = *shape;
+  h->launchShape._pad = 0;
+  fillStepParams(h);
+  return WDEM_OK;
+}
+
+int wdem_get_launch_shape(wdem_handle* h, wdem_launch_shape* shape) {
+  if (!h || !shape) return WDEM_ERR_ARG;
+  *shape = h->launchShape;
+  return WDEM_OK;
+}
+
+int wdem_autotune(wdem_handle* h, int32_t stepsPerCandidate, wdem_launch_shape* best, double* msBest, double* msStart) {
+  if (!h || stepsPerCandidate <= 0) return WDEM_ERR_ARG;
+  if (!h->particlesSet || !h->paramsSet) return fail(h, WDEM_ERR_STATE, "autotune after particles and params were set");
+  const bool timingWas = h->timing;
+  h->timing = true;
+  // cost of a shape: per-phase device time of the integrator and the contact pass per step
+  auto cost = [&](const wdem_launch_shape& s, double& ms) -> int {
+    h->launchShape = s;
+    fillStepParams(h);
+    int rc = wdem_step(h, 2);
+    if (rc) return rc;
+    if ((rc = wdem_step(h, stepsPerCandidate))) return rc;
+    ms = (h->phaseMs[PH_LEAPFROG] + h->phaseMs[PH_CONTACTS]) / stepsPerCandidate;
+    return WDEM_OK;
+  };
+  wdem_launch_shape cur = h->launchShape;
+  double curMs = 0;
+  int rc = cost(cur, curMs);
+  const double startMs = curMs;
+  const std::vector<std::pair<int wdem_launch_shape::*, std::vector<int>>> knobs = {
+      {&wdem_launch_shape::contactsBlock, {64, 128, 256}},
+      {&wdem_launch_shape::contactsPerSM, {0, 1, 2, 4, 8, 16}},
+      {&wdem_launch_shape::cullBlock, {128, 256, 512}},
+      {&wdem_launch_shape::integratorBlock, {128, 256, 512}},
+      {&wdem_launch_shape::listsPerSM, {0, 1, 2, 4}}};
+  for (const auto& kv : knobs) {
+    if (rc) break;
+    for (int v : kv.second) {
+      if (cur.*(kv.first) == v) continue;
+      wdem_launch_shape c = cur;
+      c.*(kv.first) = v;
+      if (!shapeValid(c)) continue;
+      double ms = 0;
+      if ((rc = cost(c, ms))) break;
+      if (ms < curMs) { cur = c; curMs = ms; }
+    }
+  }
+  h->timing = timingWas;
+  h->launchShape = cur;
+  fillStepParams(h);
+  if (rc) return rc;
+  if (best) *best = cur;
+  if (msBest) *msBest = curMs;
+  if (msStart) *msStart = startMs;
   return WDEM_OK;
 }
 

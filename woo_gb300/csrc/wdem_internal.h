@@ -118,6 +118,11 @@ struct StepParams {
   float* ellLog;                     // training records of solved pairs (17 floats each), or null
   unsigned long long* ellLogCount;
   long long ellLogCap;
+  // launch shape (host-side choices carried with the parameters; the kernels do not read them): block
+  // sizes of the contact FP64 pass, the contact cull and the integrator's first pass; resident blocks per
+  // SM of the contact FP64 pass and of the integrator's list pass (0: as many as fit); SMs of the device
+  int shContactsBlock, shContactsPerSM, shCullBlock, shLeapBlock, shListsPerSM;
+  int numSMs;
 };
 
 // time step of a particle (batched scenes: its material's scene dt)

@@ -976,9 +976,10 @@ class GpuDemEngine(Engine):
     Constructed like ContactLoop from the three functor lists (src/dem/ContactLoop.cpp:52-66), plus
     the Leapfrog (damping, reset) and collider (verletDist) attributes.  Runs libwdem.so on one CUDA
     device; errors come back as RuntimeError.  arith: "exact" (the reference's IEEE operations, bit for
-    bit) or "fma" (FP64 multiply-adds contracted, one reciprocal per vector division)."""
+    bit) or "fma" (FP64 multiply-adds contracted, one reciprocal per vector division).  autotune: pick the
+    kernels' launch shape on the first run (woo_gb300.tuning: cached per GPU and workload)."""
     _defaults = dict(capacity=0, damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
-                     updatePhys="never", dist00=True, device=0, keepGeom=True, arith="exact")
+                     updatePhys="never", dist00=True, device=0, keepGeom=True, arith="exact", autotune=False)
 
     def __init__(self, cg2=None, cp2=None, law=None, **kw):
         super().__init__(**kw)
@@ -1234,6 +1235,29 @@ class GpuDemEngine(Engine):
         self._ensure(scene, field)
         if field._dirty:
             self._upload_edits(field)
+        if self.autotune and not getattr(self, "_tuned", None):
+            from . import tuning
+            key = tuning.workload_key(len(field.par), self._params.law, getattr(scene, "periodic", False),
+                                      any(isinstance(p.shape, Ellipsoid) for p in field.par))
+            self._h.set_params(self._params)
+
+            def probe():
+                # a handle with a copy of the state to tune on, so that the run itself does not advance
+                if field._stale:
+                    self._download_particles(field)
+                t = abi.Handle(self._cap, device=self.device)
+                t.keep_geom(False)
+                t.set_params(self._params)
+                t.upload_particles(self._device_view(field, field._arrays))
+                t.set_params(self._params)
+                if getattr(scene, "periodic", False):
+                    c = scene.cell
+                    t.set_cell(c.hSize, c.trsf, c.gradV, c.nextGradV)
+                con = self._download_contacts()
+                if con.n:
+                    t.upload_contacts(con)
+                return t
+            self._tuned = tuning.tuned(self._h, self.device, key, probe=probe)
         p = self._params
         p.dt = scene.dt
         p.step = scene.step
