@@ -179,7 +179,7 @@ def build_scene(name, n=None, packer="engine"):
             sc = (k / 200_000) ** (1.0 / 3.0)
             return scenes.ellipsoid_cloud(k, 7, box=(0.6 * sc, 0.6 * sc, 1.2 * sc), amin=0.003, amax=0.006, dense=1.0,
                                           vel_scale=0.5, angvel_scale=5.0, young=1e7, tanPhi=0.4, damping=0.2,
-                                          ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_MLP)
+                                          ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_HISTORY_MLP)
         return scenes.spheres10k(n=n or 10000)
     finally:
         scenes.set_packer()
@@ -266,17 +266,19 @@ def new_handle(spec, local, params=None):
 
 def ell_variants(args, spec, local, world, barrier, w):
     """The same initial state under each solver: Brent (the reference's), Newton from the cold start,
-    Newton from the previous step's lambda, Newton from the learned warm start (weights w)."""
+    Newton from the previous step's lambda, Newton from the learned warm start (weights w), and Newton
+    from the previous step's lambda with the learned warm start for pairs solved for the first time."""
     import torch
     from woo_gb300 import abi
     out = {}
     for name, solver, warm in (("brent", abi.ELL_BRENT, abi.WARM_COLD), ("newton_cold", abi.ELL_NEWTON, abi.WARM_COLD),
                                ("newton_history", abi.ELL_NEWTON, abi.WARM_HISTORY),
-                               ("newton_mlp", abi.ELL_NEWTON, abi.WARM_MLP)):
+                               ("newton_mlp", abi.ELL_NEWTON, abi.WARM_MLP),
+                               ("newton_history_mlp", abi.ELL_NEWTON, abi.WARM_HISTORY_MLP)):
         p = copy_params(spec.params)
         p.ellSolver, p.warmStart = solver, warm
         h = new_handle(spec, local, p)
-        if warm == abi.WARM_MLP:
+        if warm in (abi.WARM_MLP, abi.WARM_HISTORY_MLP):
             h.warm_set_weights(w)
         stream = torch.cuda.ExternalStream(h.stream(), device=local)
         h.step(max(args.warmup, 3))
@@ -518,7 +520,13 @@ def run_gpu(args, rank, world, local):
         v = extra["variants"]
         extra["warm_start_speedup"] = {
             "contact_pass_vs_newton_cold": v["newton_cold"]["contacts_ms_per_step"] / v["newton_mlp"]["contacts_ms_per_step"],
-            "iterations_vs_newton_cold": v["newton_cold"]["iterations_per_solve"] / v["newton_mlp"]["iterations_per_solve"]}
+            "iterations_vs_newton_cold": v["newton_cold"]["iterations_per_solve"] / v["newton_mlp"]["iterations_per_solve"],
+            "history_mlp_contact_pass_vs_newton_cold":
+                v["newton_cold"]["contacts_ms_per_step"] / v["newton_history_mlp"]["contacts_ms_per_step"],
+            "history_mlp_iterations_vs_newton_cold":
+                v["newton_cold"]["iterations_per_solve"] / v["newton_history_mlp"]["iterations_per_solve"],
+            "history_contact_pass_vs_newton_cold":
+                v["newton_cold"]["contacts_ms_per_step"] / v["newton_history"]["contacts_ms_per_step"]}
         h = new_handle(spec, local)
         h.warm_set_weights(w)
     elif args.workload == "batch512":

@@ -48,8 +48,9 @@ enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2 };
  * (the reference's brent=False branch, which it leaves unimplemented, Ellipsoid.cpp:311-322) */
 enum { WDEM_ELL_BRENT = 0, WDEM_ELL_NEWTON = 1 };
 /* initial lambda of the Newton solve: lambda0 = max(a)/(max(a)+max(b)) (the reference's draft guess,
- * Ellipsoid.cpp:314), the learned warm start, or the converged lambda of the previous step */
-enum { WDEM_WARM_COLD = 0, WDEM_WARM_MLP = 1, WDEM_WARM_HISTORY = 2 };
+ * Ellipsoid.cpp:314), the learned warm start, the converged lambda of the previous step, or the previous
+ * step's lambda where the pair has one and the learned warm start for pairs solved for the first time */
+enum { WDEM_WARM_COLD = 0, WDEM_WARM_MLP = 1, WDEM_WARM_HISTORY = 2, WDEM_WARM_HISTORY_MLP = 3 };
 enum { WDEM_MAT_FRICT = 0, WDEM_MAT_HERTZ = 1 };                 /* FrictMat, HertzMat */
 enum { WDEM_CP2_FRICT = 0, WDEM_CP2_HERTZ = 1 };                 /* Cp2_FrictMat_FrictPhys, Cp2_HertzMat_HertzPhys */
 enum { WDEM_LAW_IDEALELPL = 0, WDEM_LAW_HERTZ_DMT = 1 };         /* Law2_L6Geom_FrictPhys_IdealElPl, Law2_L6Geom_HertzPhys_DMT */

@@ -98,3 +98,14 @@ def test_training_gain(wdem_lib):
     assert fb < 0.05
     pc, pm = gpu_particles(hc, cold.particles.n), gpu_particles(hm, mlp.particles.n)
     assert np.allclose(pc.pos, pm.pos, rtol=0, atol=1e-9 * np.abs(pc.pos).max())
+    # the previous step's lambda where a pair has one, the network for pairs solved for the first time:
+    # fewer iterations than the history warm start alone on the same run, the same trajectory
+    hist = scenes.ellipsoid_cloud(1500, 12, dense=0.75, ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_HISTORY)
+    both = scenes.ellipsoid_cloud(1500, 12, dense=0.75, ellSolver=abi.ELL_NEWTON, warmStart=abi.WARM_HISTORY_MLP)
+    hh, ih, _ = _iters(hist)
+    hb, ib, fbb = _iters(both, w)
+    print(f"history {ih:.3f}, history + learned {ib:.3f} Newton iterations per solve (fallbacks {fbb:.4f})")
+    assert ib <= ih and ib < ic
+    pb = gpu_particles(hb, both.particles.n)
+    assert np.allclose(pc.pos, pb.pos, rtol=0, atol=1e-9 * np.abs(pc.pos).max())
+

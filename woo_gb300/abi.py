@@ -28,7 +28,7 @@ WDEM_ERR_STATE = -9
 SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID = 0, 1, 2
 ELL_BRENT, ELL_NEWTON = 0, 1
 WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
-WARM_COLD, WARM_MLP, WARM_HISTORY = 0, 1, 2
+WARM_COLD, WARM_MLP, WARM_HISTORY, WARM_HISTORY_MLP = 0, 1, 2, 3
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
 ARITH_EXACT, ARITH_FMA = 0, 1

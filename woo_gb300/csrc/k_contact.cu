@@ -110,10 +110,13 @@ __device__ __noinline__ bool ellPairGeometry(const StepParams& P, const Particle
     const double cold = maxc(semiA) / (maxc(semiA) + maxc(semiB));
     double l0 = cold;
     int budget = 60;
-    if (P.warmStart == WDEM_WARM_HISTORY && c.lam) {
-      const double lh = c.lam[i];
-      if (lh > 0 && lh < 1) l0 = lh;
-    } else if (P.warmStart == WDEM_WARM_MLP && c.lam0) {
+    const double lh = c.lam ? c.lam[i] : -1.0;
+    const bool hist = lh > 0 && lh < 1;
+    if ((P.warmStart == WDEM_WARM_HISTORY || P.warmStart == WDEM_WARM_HISTORY_MLP) && hist) {
+      l0 = lh;
+    } else if ((P.warmStart == WDEM_WARM_MLP || P.warmStart == WDEM_WARM_HISTORY_MLP) && c.lam0) {
+      // the learned guess (for WDEM_WARM_HISTORY_MLP only where the pair has no previous maximiser),
+      // judged by the plain solve: cold start after fallbackIters iterations without convergence
       const double lm = (double)c.lam0[i];
       if (lm > 0 && lm < 1) { l0 = lm; budget = P.fallbackIters; }
     }
@@ -702,7 +705,7 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
     launchCull<false, true>(s, P, p, c, nc, count, st, full);
-    if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF);
+    if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF, P.warmStart == WDEM_WARM_HISTORY_MLP);
     launchHeavy<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true>(s, P, p, c, nc, count, st);
   } else if (P.periodic) {
     launchCull<true, false>(s, P, p, c, nc, count, st, full);

@@ -139,9 +139,11 @@ __device__ __forceinline__ void loadNet(NetSmem& net, const uint16_t* wbf, const
 
 // ------------------------------------------------------------------------------ inference
 // lam0 of every ellipsoid pair (sphere + ellipsoid included; walls excluded) that the contact kernel
-// may solve this step; other entries are NaN (cold start).
+// may solve this step; other entries are NaN (cold start).  onlyFresh: pairs that carry the previous
+// step's maximiser (c.lam in (0, 1)) get NaN as well (the solve starts from that), and a warp whose 16
+// pairs all carry one skips the network.
 __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const unsigned* work, const unsigned* count,
-                                                  long long ncon, const uint16_t* wbf, const float* wf) {
+                                                  long long ncon, const uint16_t* wbf, const float* wf, int onlyFresh) {
   extern __shared__ __align__(16) unsigned char smem[];
   NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
   WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
@@ -158,7 +160,8 @@ __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const
       for (int k = 0; k < ELL_FEATURES; k++) f[k] = 0.f;
       if (i >= 0) {
         const uint8_t sb = c.state[i] & CS_SHAPES;
-        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && (c.state[i] & CS_MASK) != CS_DEAD) {
+        const bool hasLam = onlyFresh && c.lam && c.lam[i] > 0 && c.lam[i] < 1;
+        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && (c.state[i] & CS_MASK) != CS_DEAD && !hasLam) {
           const int2 id = c.ids[i];
           const double4_32a OA = p.ori[id.x], OB = p.ori[id.y];
           qd oa, ob;
@@ -172,6 +175,12 @@ __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const
       for (int k = 0; k < 16; k++) ws.x[(lane & 15) * 16 + k] = bf(k < ELL_FEATURES ? f[k] : 0.f);
     }
     __syncwarp();
+    if (__ballot_sync(0xffffffffu, use) == 0) {
+      // no pair of this warp needs the network
+      if (lane < 16 && i >= 0) c.lam0[i] = __int_as_float(0x7fffffff);
+      __syncwarp();
+      continue;
+    }
     forward(net, ws, g, t);
     if (lane < 16 && i >= 0) {
       float l = ws.out[(lane & 15) * 8 + 0];
@@ -378,11 +387,12 @@ void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf) {
 }
 
 void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
-                     const uint16_t* wbf, const float* wf) {
+                     const uint16_t* wbf, const float* wf, bool onlyFresh) {
   if (nc <= 0) return;
   long long blocks = (nc + SAMPLES - 1) / SAMPLES;
   if (blocks > 152 * 2) blocks = 152 * 2;  // persistent blocks: the weights are loaded once per block
-  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, nc, wbf, wf), ++::wdem::g_kernel_launches);
+  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, nc, wbf, wf, onlyFresh ? 1 : 0),
+   ++::wdem::g_kernel_launches);
 }
 
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf) {

@@ -1074,7 +1074,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   cudaStream_t s = h->stream;
   const long long s0 = h->step;
   h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
-  const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
+  const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
   StepParams P = h->P;
   for (int g = 0; g < ahead; g++) {
     P.step = s0 + g;
@@ -1142,7 +1142,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     return fail(h, WDEM_ERR_ARG, "unknown ellipsoid solver");
   if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && !(h->P.newtonTol > 0))
     return fail(h, WDEM_ERR_ARG, "newtonTol must be positive");
-  if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP && !h->mlpReady)
+  if (h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP) && !h->mlpReady)
     return fail(h, WDEM_ERR_STATE, "warmStart=MLP needs a network (wdem_warm_init / wdem_warm_set_weights / wdem_warm_train)");
   if (h->raw.dynDtPeriod > 0 && (h->hasEll || h->raw.materialDt))
     return fail(h, WDEM_ERR_UNSUPPORTED, "DynDt runs with sphere and wall scenes of one dt only");
@@ -1220,7 +1220,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     }
     {
       PhaseTimer t(h, PH_CONTACTS);
-      const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && h->P.warmStart == WDEM_WARM_MLP;
+      const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
       (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                       warm ? h->mlpW : nullptr);
       h->actValid = true;

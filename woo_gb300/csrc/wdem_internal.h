@@ -301,7 +301,7 @@ void mlp_pack(const float* pad, float* pub);
 cudaError_t mlp_prepare_kernels();
 void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf);
 void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
-                     const uint16_t* wbf, const float* wf);
+                     const uint16_t* wbf, const float* wf, bool onlyFresh);
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf);
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
                      float* grad, float* loss);

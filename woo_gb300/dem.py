@@ -1083,7 +1083,8 @@ class GpuDemEngine(Engine):
         p.ellSolver = abi.ELL_BRENT if (ell is None or ell.brent) else abi.ELL_NEWTON
         p.brentBits = int(ell.brentBits) if ell is not None else 32
         p.newtonTol = float(ell.newtonTol) if ell is not None else 1e-10
-        p.warmStart = {"cold": abi.WARM_COLD, "history": abi.WARM_HISTORY, "mlp": abi.WARM_MLP}[
+        p.warmStart = {"cold": abi.WARM_COLD, "history": abi.WARM_HISTORY, "mlp": abi.WARM_MLP,
+                       "history+mlp": abi.WARM_HISTORY_MLP}[
             ell.warmStart if ell is not None else "cold"]
         p.fallbackIters = int(ell.fallbackIters) if ell is not None else 4
         if self.arith not in ("exact", "fma"):
@@ -1200,7 +1201,7 @@ class GpuDemEngine(Engine):
             c = scene.cell
             h.set_cell(c.hSize, c.trsf, c.gradV, c.nextGradV)
         ell = getattr(self, "_ellFunctor", None)
-        if ell is not None and ell.warmStart == "mlp":
+        if ell is not None and ell.warmStart in ("mlp", "history+mlp"):
             if ell.warmStartWeights is None:
                 raise RuntimeError("Cg2_Ellipsoid_Ellipsoid_L6Geom.warmStart='mlp' needs warmStartWeights")
             h.warm_set_weights(ell.warmStartWeights)
@@ -1453,7 +1454,7 @@ class GpuDemEngine(Engine):
         h.keep_geom(self.keepGeom)
         self._timing_on = False   # a new handle starts untimed; run() switches it on again if wanted
         ell = getattr(self, "_ellFunctor", None)
-        if ell is not None and ell.warmStart == "mlp":
+        if ell is not None and ell.warmStart in ("mlp", "history+mlp"):
             h.warm_set_weights(ell.warmStartWeights)
         self._h, self._cap = h, cap
 
