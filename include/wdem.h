@@ -43,7 +43,11 @@ enum {
 };
 
 /* ---- enums mirroring Woo class names -------------------------------------------------------- */
-enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2 };
+/* Facet (src/dem/Facet.hpp): a triangle of three nodes; node 0 is the particle's pos, nodes 1 and 2 come in
+ * wdem_particles.facetVerts; radius holds Facet.halfThick.  Facets are fixed (all DOFs blocked, no
+ * velocity), contact spheres through Cg2_Facet_Sphere_L6Geom and receive no contact force from the
+ * contact loop (ContactLoop::applyForceUninodal skips shapes with more than one node). */
+enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2, WDEM_SHAPE_FACET = 3 };
 /* Cg2_Ellipsoid_Ellipsoid_L6Geom solver: brent=True (Ellipsoid.hpp:57-59) or Newton-Raphson on dS/dlambda = 0
  * (the reference's brent=False branch, which it leaves unimplemented, Ellipsoid.cpp:311-322) */
 enum { WDEM_ELL_BRENT = 0, WDEM_ELL_NEWTON = 1 };
@@ -170,6 +174,7 @@ typedef struct wdem_particles {
   double* angMom;         /* 3n DemData.angMom, NaN = not initialised (aspherical Leapfrog); may be NULL */
   int32_t* scene;         /* batched independent scenes: scene index of each particle (0..4095); particles of
                              different scenes never interact; NULL = one scene */
+  double* facetVerts;     /* 9n: Facet node positions 0, 1, 2 (node 0 equal to pos); NULL when there are no facets */
 } wdem_particles;
 
 /* ---- contact state, SoA; n contacts ---------------------------------------------------------- */

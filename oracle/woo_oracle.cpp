@@ -303,6 +303,7 @@ struct Particle {
   V3 pos, vel, angVel, force, torque;
   Quat ori;
   V3 semiAxes;                        /* Ellipsoid.semiAxes */
+  V3 fv1, fv2;                        /* Facet nodes 1 and 2 (node 0 is pos; radius holds halfThick) */
   V3 angMom = V3(NaN, NaN, NaN);      /* DemData.angMom (aspherical Leapfrog) */
   Aabb bound;
   std::map<int, std::shared_ptr<struct Contact>> contacts; /* Particle::contacts (Particle.hpp:36) */
@@ -624,6 +625,19 @@ static void updateAabb(Scene& S, Particle& p) {
     V3 c = S.periodic ? mvec(S.cell.unshearTrsf, p.pos) : p.pos;
     a.min = c - delta;
     a.max = c + delta;
+  } else if (p.shape == WDEM_SHAPE_FACET) {
+    /* Bo1_Facet_Aabb::go (Facet.cpp:275-298), aperiodic: the nodes +- halfThick, coefficient-wise min/max */
+    if (S.periodic) throw std::runtime_error("facets in a periodic cell are not restated");
+    const V3 ht(p.radius, p.radius, p.radius);
+    a.min = p.pos - ht;
+    a.max = p.pos + ht;
+    for (const V3* v : {&p.fv1, &p.fv2}) {
+      const V3 lo = *v - ht, hi = *v + ht;
+      for (int k = 0; k < 3; k++) {
+        a.min[k] = std::min(a.min[k], lo[k]);
+        a.max[k] = std::max(a.max[k], hi[k]);
+      }
+    }
   } else {
     a.min = V3(-Inf, -Inf, -Inf);
     a.max = V3(Inf, Inf, Inf);
@@ -1114,6 +1128,70 @@ static bool cg2WallSphere(Scene& S, Contact& C, Particle& W, Particle& Sp, const
   return true;
 }
 
+/* ------------------------------------------------------------------ facets */
+/* CompUtils::closestSegmentPt (CompUtils.cpp:59-65) */
+static V3 closestSegmentPt(const V3& P, const V3& A, const V3& B) {
+  const V3 BA = B - A;
+  if (sqnorm(BA) == 0.) return A;
+  const double u = (dot(P, BA) - dot(A, BA)) / sqnorm(BA);
+  return A + std::min(1., std::max(0., u)) * BA;
+}
+/* CompUtils::triangleBarycentrics (CompUtils.cpp:94-112): the 2x2 system by Eigen's closed-form inverse
+ * (1/det times the adjugate, det = m00 m11 - m10 m01) */
+static V3 triangleBarycentrics(const V3& x, const V3& A, const V3& B, const V3& C) {
+  const V3 vB = B - A, vC = C - A, vX = x - A;
+  const double m00 = dot(vB, vB), m01 = dot(vC, vB), m10 = dot(vB, vC), m11 = dot(vC, vC);
+  const double invdet = 1. / (m00 * m11 - m10 * m01);
+  const double i00 = m11 * invdet, i10 = -m10 * invdet, i01 = -m01 * invdet, i11 = m00 * invdet;
+  const double b0 = dot(vX, vB), b1 = dot(vX, vC);
+  const double u = i00 * b0 + i01 * b1, v = i10 * b0 + i11 * b1;
+  return V3(1 - u - v, u, v);
+}
+/* Cg2_Facet_Sphere_L6Geom::go (Facet.cpp:333-390) for a facet without neighbour angles (n21lim NaN: no
+ * boundary adjustment) and without fakeVel; Facet::getNormal, getOuterVectors (Facet.cpp:76-79, 110-116),
+ * interpolatePtLinAngVel (Facet.cpp:162-179). */
+static bool cg2FacetSphere(Scene& S, Contact& C, Particle& F, Particle& Sp, const V3& shift2, bool force) {
+  const V3 n0 = F.pos, n1 = F.fv1, n2 = F.fv2;
+  const double ht = F.radius, r = Sp.radius;
+  const V3 sC = Sp.pos + shift2;
+  V3 fNormal = cross(n1 - n0, n2 - n0);
+  normalize(fNormal);
+  const double planeDist = dot(sC - n0, fNormal);
+  if (std::abs(planeDist) > (r + ht) && !C.isReal() && !force) return false;
+  const V3 fC = sC - planeDist * fNormal;
+  const V3 nn = cross(n1 - n0, n2 - n0);
+  const V3 outVec[3] = {cross(n1 - n0, nn), cross(n2 - n1, nn), cross(n0 - n2, nn)};
+  const V3 nodes[3] = {n0, n1, n2};
+  double ll[3];
+  for (int i = 0; i < 3; i++) ll[i] = dot(outVec[i], fC - nodes[i]);
+  const int w = (ll[0] > 0 ? 1 : 0) + (ll[1] > 0 ? 2 : 0) + (ll[2] > 0 ? 4 : 0);
+  V3 contPt;
+  switch (w) {
+    case 0: contPt = fC; break;
+    case 1: contPt = closestSegmentPt(fC, n0, n1); break;
+    case 2: contPt = closestSegmentPt(fC, n1, n2); break;
+    case 4: contPt = closestSegmentPt(fC, n2, n0); break;
+    case 3: contPt = n1; break;
+    case 5: contPt = n0; break;
+    case 6: contPt = n2; break;
+    default: throw std::logic_error("Cg2_Facet_Sphere_L6Geom: impossible sphere-facet intersection");
+  }
+  V3 normal = sC - contPt;
+  if (sqnorm(normal) > pow2(r + ht) && !C.isReal() && !force) return false;
+  const double dist = norm(normal);
+  if (dist != 0) normal = normal / dist;
+  else normal = C.geom ? qrot(C.gori, V3(1, 0, 0)) : V3(1, 0, 0);
+  if (ht > 0) contPt = contPt + normal * ht;
+  const double uN = dist - r - ht;
+  /* velocity of the facet at contPt: barycentric interpolation of the nodes' velocities (zero: fixed) */
+  const V3 a = triangleBarycentrics(contPt, n0, n1, n2);
+  const V3 vv[3] = {F.vel, V3(), V3()};
+  const V3 linVel = a[0] * vv[0] + a[1] * vv[1] + a[2] * vv[2];
+  const V3 angVel = cross(n0 - contPt, vv[0]) + cross(n1 - contPt, vv[1]) + cross(n2 - contPt, vv[2]);
+  handleSpheresLikeContact(S, C, contPt, linVel, angVel, sC, Sp.vel, Sp.angVel, normal, contPt, uN, std::max(ht, r), r);
+  return true;
+}
+
 /* ------------------------------------------------------------------ ellipsoids */
 /* Brent's minimisation without derivatives (R. P. Brent, "Algorithms for Minimization without
  * Derivatives", 1973, ch. 5) as boost::math::tools::brent_find_minima performs it (Boost.Math,
@@ -1440,6 +1518,7 @@ static bool lawHertzDMT(Scene& S, Contact& C) {
 
 /* Contact::getForceTorqueBranch (Contact.cpp:24-34) + DemData::addForceTorque (Particle.hpp:249) */
 static void applyForceUninodal(Scene& S, const Contact& C, Particle& p) {
+  if (p.shape == WDEM_SHAPE_FACET) return;  /* sh->nodes.size() != 1 (ContactLoop.cpp:272) */
   bool isPA = (C.pA == p.id);
   double sign = isPA ? 1 : -1;
   V3 F = qrot(C.gori, C.force) * sign;
@@ -1459,8 +1538,10 @@ static bool freshContactSetup(Scene& S, Contact& C) {
   const int sa = S.par[C.pA].shape, sb = S.par[C.pB].shape;
   const bool swap = (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) ||
                     (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
-                    (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL);
+                    (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL) ||
+                    (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET);
   const bool known = swap || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_SPHERE) ||
+                     (sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) ||
                      (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_SPHERE) ||
                      (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_ELLIPSOID) ||
                      (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_ELLIPSOID) ||
@@ -1487,6 +1568,7 @@ static bool callGeom(Scene& S, Contact& C, Particle& pA, Particle& pB, const V3&
   if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_ELLIPSOID)
     return cg2EllipsoidOrSphere(S, C, pA, V3(pA.radius, pA.radius, pA.radius), pB, pB.semiAxes, shift2, false);
   if (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_ELLIPSOID) return cg2WallEllipsoid(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) return cg2FacetSphere(S, C, pA, pB, shift2, false);
   return false;
 }
 
@@ -2125,6 +2207,11 @@ int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
     q.torque = V3(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2]);
     if (p->semiAxes) q.semiAxes = V3(p->semiAxes[3 * i], p->semiAxes[3 * i + 1], p->semiAxes[3 * i + 2]);
     if (p->angMom) q.angMom = V3(p->angMom[3 * i], p->angMom[3 * i + 1], p->angMom[3 * i + 2]);
+    if (q.shape == WDEM_SHAPE_FACET) {
+      if (!p->facetVerts) { S.err = "facets need wdem_particles.facetVerts"; return WDEM_ERR_ARG; }
+      q.fv1 = V3(p->facetVerts[9 * i + 3], p->facetVerts[9 * i + 4], p->facetVerts[9 * i + 5]);
+      q.fv2 = V3(p->facetVerts[9 * i + 6], p->facetVerts[9 * i + 7], p->facetVerts[9 * i + 8]);
+    }
     if (q.shape == WDEM_SHAPE_ELLIPSOID && !(minCoeff(q.semiAxes) > 0)) {
       S.err = "Ellipsoid #" + std::to_string(i) + ": all semi-axes must be positive";
       return WDEM_ERR_ARG;
@@ -2160,7 +2247,9 @@ int orc_upload_contacts(orc_handle* h, const wdem_contacts* c) {
       /* lens/contA for iniLensTouch=true; Hertz constants recomputed from the materials */
       const Particle& a = S.par[C->pA];
       const Particle& b = S.par[C->pB];
-      double r1 = a.shape == WDEM_SHAPE_WALL ? -b.radius : a.radius, r2 = b.radius;
+      /* the radii handleSpheresLikeContact got: -r for walls, max(halfThick, r) for facets */
+      double r1 = a.shape == WDEM_SHAPE_WALL ? -b.radius : a.shape == WDEM_SHAPE_FACET ? std::max(a.radius, b.radius) : a.radius;
+      double r2 = b.radius;
       C->lens[0] = std::abs(r1); C->lens[1] = std::abs(r2);
       C->contA = M_PI * pow2((r1 > 0 && r2 > 0) ? std::min(r1, r2) : (r1 > 0 ? r1 : r2));
       if (S.P.cp2 == WDEM_CP2_HERTZ) {

@@ -25,7 +25,7 @@ WDEM_ERR_TOO_BIG = -7
 WDEM_ERR_TIMEOUT = -8
 WDEM_ERR_STATE = -9
 
-SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID = 0, 1, 2
+SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID, SHAPE_FACET = 0, 1, 2, 3
 ELL_BRENT, ELL_NEWTON = 0, 1
 WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
 WARM_COLD, WARM_MLP, WARM_HISTORY, WARM_HISTORY_MLP = 0, 1, 2, 3
@@ -79,7 +79,7 @@ class Particles(C.Structure):
     _fields_ = [("n", C.c_int32), ("_pad", C.c_int32), ("shape", I32), ("radius", D), ("wallAxis", I32),
                 ("wallSense", I32), ("material", I32), ("mask", U32), ("flags", U32), ("mass", D),
                 ("inertia", D), ("pos", D), ("ori", D), ("vel", D), ("angVel", D), ("force", D), ("torque", D),
-                ("semiAxes", D), ("angMom", D), ("scene", I32)]
+                ("semiAxes", D), ("angMom", D), ("scene", I32), ("facetVerts", D)]
 
 
 class Contacts(C.Structure):
@@ -153,6 +153,7 @@ class ParticleArrays:
         self.semiAxes = np.full((n, 3), np.nan)
         self.angMom = np.full((n, 3), np.nan)
         self.scene = np.zeros(n, np.int32)
+        self.facetVerts = np.full((n, 9), np.nan)
 
     def copy(self):
         o = ParticleArrays(self.n)
@@ -183,6 +184,7 @@ class ParticleArrays:
         s.torque = ptr(self.torque, C.c_double)
         s.semiAxes = ptr(self.semiAxes, C.c_double); s.angMom = ptr(self.angMom, C.c_double)
         s.scene = ptr(self.scene, C.c_int32)
+        s.facetVerts = ptr(self.facetVerts, C.c_double)
         return s
 
 

@@ -68,6 +68,19 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
     const double hz = sqrt(c0.z * c0.z + c1.z * c1.z + c2.z * c2.z);
     mn = make_double4_32a(pr.x - hx, pr.y - hy, pr.z - hz, 0);
     mx = make_double4_32a(pr.x + hx, pr.y + hy, pr.z + hz, 0);
+  } else if (sh == WDEM_SHAPE_FACET) {
+    // Bo1_Facet_Aabb::go (Facet.cpp:275-298), aperiodic: the three nodes +- halfThick (posr.w), coefficient-wise
+    // min/max in the order of Eigen's array().min()/max() (std::min/std::max semantics)
+    const double ht = pr.w;
+    mn = make_double4_32a(pr.x - ht, pr.y - ht, pr.z - ht, 0);
+    mx = make_double4_32a(pr.x + ht, pr.y + ht, pr.z + ht, 0);
+    const double4_32a v[2] = {p.fv1[i], p.fv2[i]};
+    for (int k = 0; k < 2; k++) {
+      const double lx = v[k].x - ht, ly = v[k].y - ht, lz = v[k].z - ht;
+      const double ux = v[k].x + ht, uy = v[k].y + ht, uz = v[k].z + ht;
+      mn.x = (lx < mn.x) ? lx : mn.x; mn.y = (ly < mn.y) ? ly : mn.y; mn.z = (lz < mn.z) ? lz : mn.z;
+      mx.x = (mx.x < ux) ? ux : mx.x; mx.y = (mx.y < uy) ? uy : mx.y; mx.z = (mx.z < uz) ? uz : mx.z;
+    }
   } else {
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
     int ax = (p.meta[i].x >> 4) & 3;
@@ -391,12 +404,11 @@ __device__ __forceinline__ bool mayCollide(unsigned m1, unsigned m2, unsigned lo
   return (m1 & m2) != 0 && (m1 & m2 & lone) == 0;
 }
 // contact orientation: same shape -> (lower id, higher id); otherwise the order of the Cg2 functor
-// (Wall+Sphere, Sphere+Ellipsoid, Wall+Ellipsoid)
+// (Wall+Sphere, Facet+Sphere, Sphere+Ellipsoid, Wall+Ellipsoid)
 __device__ __forceinline__ int2 orient(int i, int j, int shi, int shj) {
   int a = min(i, j), b = max(i, j);
   int sa = (a == i) ? shi : shj, sb = (a == i) ? shj : shi;
-  if ((sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
-      (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL)) {
+  if (pairSwaps(sa, sb)) {
     int t = a; a = b; b = t;
   }
   return make_int2(a, b);
@@ -640,9 +652,7 @@ __global__ void k_carry_compact(Particles p, Contacts neu, long long nNew, Conta
   const int2 id = make_int2((int)(unsigned)(t & 0xffffffffu), (int)(unsigned)(t >> 32));
   const unsigned jj = tmpJ[c];
   if (jj == 0xffffffffu) {
-    const int sa = p.meta[id.x].x & 15, sbb = p.meta[id.y].x & 15;
-    const uint8_t sb = (uint8_t)((sa == WDEM_SHAPE_WALL ? CS_WALL_A : 0) | (sbb == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
-                                 (sa == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (sbb == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
+    const uint8_t sb = pairShapeBits(p.meta[id.x].x & 15, p.meta[id.y].x & 15);
     neu.ids[d] = id;
     if (neu.cdist) neu.cdist[d] = tmpDist[c];
     neu.state[d] = CS_POTENTIAL | sb;

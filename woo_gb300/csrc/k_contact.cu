@@ -216,6 +216,82 @@ __device__ __forceinline__ bool wallEllGeometry(const Particles& p, int a, int b
   return true;
 }
 
+// CompUtils::closestSegmentPt (CompUtils.cpp:59-65)
+__device__ __forceinline__ d3 closestSegmentPt(d3 P, d3 A, d3 B) {
+  const d3 BA = B - A;
+  const double bb = sqnorm(BA);
+  if (bb == 0.) return A;
+  const double u = (dot(P, BA) - dot(A, BA)) / bb;
+  const double lo = (0. < u) ? u : 0.;        // std::max(0., u)
+  const double t = (lo < 1.) ? lo : 1.;       // std::min(1., .)
+  return A + t * BA;
+}
+
+// Cg2_Facet_Sphere_L6Geom::go (Facet.cpp:333-390) for facets without neighbour angles (Facet.n21lim NaN: no
+// boundary adjustment) and without fakeVel.  pA is the facet: node 0 at n0, nodes 1 and 2 in fv1/fv2,
+// half-thickness ht; pB the sphere at sC.  The projected centre is classified against the outer vectors of
+// the three edges (Facet::getOuterVectors, Facet.cpp:113-117) and snapped to the triangle, an edge or a node.
+__device__ __forceinline__ bool facetSphereGeometry(const Particles& p, const Contacts& c, long long i, int a, bool real,
+                                                    d3 n0, double ht, d3 sC, double r, d3& normal, d3& contPt,
+                                                    double& uN, double& r1, double& r2, DeviceStatus* st) {
+  const d3 n1 = xyz(p.fv1[a]), n2 = xyz(p.fv2[a]);
+  const d3 nn = cross(n1 - n0, n2 - n0);
+  const d3 fNormal = normalized(nn);
+  const double planeDist = dot(sC - n0, fNormal);
+  const double rh = r + ht;
+  if (fabs(planeDist) > rh && !real) return false;
+  const d3 fC = sC - planeDist * fNormal;
+  const double l0 = dot(cross(n1 - n0, nn), fC - n0);
+  const double l1 = dot(cross(n2 - n1, nn), fC - n1);
+  const double l2 = dot(cross(n0 - n2, nn), fC - n2);
+  const int w = (l0 > 0 ? 1 : 0) + (l1 > 0 ? 2 : 0) + (l2 > 0 ? 4 : 0);
+  switch (w) {
+    case 0: contPt = fC; break;
+    case 1: contPt = closestSegmentPt(fC, n0, n1); break;
+    case 2: contPt = closestSegmentPt(fC, n1, n2); break;
+    case 4: contPt = closestSegmentPt(fC, n2, n0); break;
+    case 3: contPt = n1; break;
+    case 5: contPt = n0; break;
+    case 6: contPt = n2; break;
+    default:
+      // outside all three edges: the reference throws logic_error
+      if (atomicCAS(&st->code, 0, WDEM_ERR_UNSUPPORTED) == 0) st->detail = a;
+      return false;
+  }
+  normal = sC - contPt;
+  if (sqnorm(normal) > rh * rh && !real) return false;
+  const double dist = sqrt(sqnorm(normal));
+  if (dist != 0) normal = normal / dist;
+  else if (real) {
+    // the sphere's centre on the facet: the previous normal, L6Geom.node.ori * UnitX
+    const d3 c0 = mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
+    const d3 c1 = mk(c.hist[HIST_T1X][i], c.hist[HIST_T1Y][i], c.hist[HIST_T1Z][i]);
+    normal = qrot(quatFromCols(c0, c1, cross(c0, c1)), mk(1, 0, 0));
+  } else normal = mk(1, 0, 0);
+  if (ht > 0) contPt = contPt + normal * ht;
+  uN = dist - r - ht;
+  r1 = (ht < r) ? r : ht;  // std::max(halfThick, radius)
+  r2 = r;
+  return true;
+}
+
+// Facet::interpolatePtLinAngVel (Facet.cpp:161-179) at x without fakeVel: barycentric weights of x
+// (CompUtils::triangleBarycentrics, CompUtils.cpp:94-112: the 2x2 system solved by Eigen's closed-form
+// inverse) applied to the node velocities; node 0 moves with the particle, nodes 1 and 2 are at rest
+__device__ __forceinline__ void facetPointVel(const Particles& p, int a, d3 n0, d3 x, d3& vel, d3& angVel) {
+  const d3 n1 = xyz(p.fv1[a]), n2 = xyz(p.fv2[a]);
+  const d3 vB = n1 - n0, vC = n2 - n0, vX = x - n0;
+  const double m00 = dot(vB, vB), m01 = dot(vC, vB), m10 = dot(vB, vC), m11 = dot(vC, vC);
+  const double invdet = 1. / (m00 * m11 - m10 * m01);
+  const double i00 = m11 * invdet, i10 = -m10 * invdet, i01 = -m01 * invdet, i11 = m00 * invdet;
+  const double b0 = dot(vX, vB), b1 = dot(vX, vC);
+  const double u = i00 * b0 + i01 * b1, v = i10 * b0 + i11 * b1;
+  const double a0 = 1 - u - v;
+  const d3 v0 = vel, z = mk(0, 0, 0);
+  vel = a0 * v0 + u * z + v * z;
+  angVel = cross(n0 - x, v0) + cross(n1 - x, z) + cross(n2 - x, z);
+}
+
 // One contact of the work list: geometry, physics and law (ContactLoop.cpp:134-197).  PENDING
 // contacts have been resolved and potential pairs that cannot touch culled by k_contacts_cull.
 template <int LAW, int CP2, bool PERI, bool ELL>
@@ -233,7 +309,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   int4 cd = make_int4(0, 0, 0, 0);
   if (PERI) cd = c.cdist[i];
   const double4_32a A4 = p.posr[a], B4 = p.posr[b];
-  const d3 pos1 = xyz(A4);
+  d3 pos1 = xyz(A4);
   d3 shift2 = mk(0, 0, 0);
   if (PERI) shift2 = mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
   const d3 pos2 = PERI ? xyz(B4) + shift2 : xyz(B4);
@@ -243,6 +319,8 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     if (sb & CS_WALL_A) {
       if (!wallEllGeometry(p, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
     } else if (!ellPairGeometry(P, p, c, i, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2, st)) return;
+  } else if (!PERI && (sb & CS_FACET)) {  // facets are aperiodic only
+    if (!facetSphereGeometry(p, c, i, a, real, pos1, A4.w, pos2, B4.w, normal, contPt, uN, r1, r2, st)) return;
   } else if (!(sb & CS_WALL_A)) {
     // Cg2_Sphere_Sphere_L6Geom::go
     r1 = A4.w; r2 = B4.w;
@@ -286,7 +364,13 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   d3 cur0, cur1, gvel, gangVel;
   const double4_32a V1 = p.velm[a], V2 = p.velm[b];
   const double4_32a W1 = p.angw[a], W2 = p.angw[b];
-  const d3 vel1 = xyz(V1), vel2 = xyz(V2), angVel1 = xyz(W1), angVel2 = xyz(W2);
+  d3 vel1 = xyz(V1), angVel1 = xyz(W1);
+  const d3 vel2 = xyz(V2), angVel2 = xyz(W2);
+  if (!PERI && (sb & CS_FACET)) {
+    // handleSpheresLikeContact gets the facet as a point at contPt moving with the interpolated velocities
+    facetPointVel(p, a, pos1, contPt, vel1, angVel1);
+    pos1 = contPt;
+  }
   if (!real) {
     // new L6Geom: setInitialLocalCoords (L6Geom.cpp:25-36), node.pos = contPt
     d3 locX = normal;
@@ -552,6 +636,7 @@ __device__ __forceinline__ bool cullOne(const StepParams& P, const Particles& p,
     }
     if (alive) {
       if (s == CS_REAL) need = realNow = true;
+      else if (sb & CS_FACET) need = true;  // facet + sphere: the FP64 functor decides every step
       else if (!(sb & CS_WALL_A)) {
         // Sphere/ellipsoid pairs: the FP32 copies carry a relative error below 2^-23 per coordinate and
         // radius; the margin (1e-5 relative on the contact distance plus 1e-6 x the sum of |coordinates|)
@@ -732,7 +817,9 @@ __global__ void k_init_uploaded(StepParams P, Particles p, Contacts c, long long
   const int2 id = c.ids[i];
   const int4 ma = p.meta[id.x], mb = p.meta[id.y];
   const double rb = p.posr[id.y].w;
-  const double r1 = ((ma.x & 15) == WDEM_SHAPE_WALL) ? -rb : p.posr[id.x].w, r2 = rb;
+  const double ra = p.posr[id.x].w;
+  const double r1 = ((ma.x & 15) == WDEM_SHAPE_WALL) ? -rb : ((ma.x & 15) == WDEM_SHAPE_FACET ? ((ra < rb) ? rb : ra) : ra);
+  const double r2 = rb;
   double kn, kt, tanPhi, hz[4];
   cp2<WDEM_CP2_HERTZ>(P, ma.y, mb.y, r1, r2, p.velm[id.x].w, p.velm[id.y].w, kn, kt, tanPhi, hz);
   c.hist[HIST_E0][i] = hz[0]; c.hist[HIST_E1][i] = hz[1]; c.hist[HIST_E2][i] = hz[2]; c.hist[HIST_E3][i] = hz[3];

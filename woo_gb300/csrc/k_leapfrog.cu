@@ -33,7 +33,11 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
   for (int e = e0; e < e1; e++) {
     const unsigned en = csr.ent[e];
     const unsigned ci = en & 0x7fffffffu;
-    if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
+    const uint8_t s = c.state[ci];
+    if ((s & CS_MASK) != CS_REAL) continue;
+    // a facet (pA) gets no force from its contacts: ContactLoop::applyForceUninodal skips shapes with
+    // more than one node (ContactLoop.cpp:270-276)
+    if ((s & CS_FACET) && !(en >> 31)) continue;
     const double4_32a* o = c.out + OUT_RECORDS * (long long)ci;
     const d3 f = xyz(o[OUT_F]);
     if (en >> 31) {

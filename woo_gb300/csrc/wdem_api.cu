@@ -189,6 +189,10 @@ struct wdem_handle {
   long long stagingCap = 0;
   bool periodic = false;
   bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
+  // facet + wall / facet + facet pairs of one scene whose masks share bits (facet, other, mask & mask); none may
+  // survive loneMask at a step
+  std::vector<int4> facetPairs;
+  unsigned facetsChecked = ~0u;  // loneMask the pairs were last checked against (~0: not yet)
   long long matsChecked = -1;   // material-table size the particle material indices were checked against
   bool gravAccDirty = true;     // angw.w (cached gravity acceleration) needs recomputing
   double* dMatDt = nullptr;     // batched scenes: dt per material
@@ -442,6 +446,9 @@ int checkDeviceStatus(wdem_handle* h) {
     else if (code == WDEM_ERR_TOO_BIG)
       m = "ambiguous periodic contact of particle #" + std::to_string(h->hst->detail) +
           ": the boxes overlap across more than one period (a particle larger than half of the cell)";
+    else if (code == WDEM_ERR_UNSUPPORTED)
+      m = "sphere-facet contact with the projected centre outside all three edges of Facet #" +
+          std::to_string(h->hst->detail) + " (degenerate facet)";
     else if (code == WDEM_ERR_TIMEOUT)
       m = "a bounded device loop hit its iteration limit (contact solver, particle #" + std::to_string(h->hst->detail) + ")";
     else m = "device error " + std::to_string(code);
@@ -705,6 +712,7 @@ int wdem_destroy(wdem_handle* h) {
   if (h->device >= 0 && h->device < 64 && g_matsOwner[h->device] == h) g_matsOwner[h->device] = nullptr;
   Particles& d = h->d;
   cudaFree(d.semi); cudaFree(d.angMom); cudaFree(d.lastOri); cudaFree(d.maxRot);
+  cudaFree(d.fv1); cudaFree(d.fv2);
   cudaFree(h->ellLog); cudaFree(h->ellLogCount);
   cudaFree(h->dMatDt); cudaFree(h->cs.sceneWall);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
@@ -808,10 +816,31 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   std::vector<double> semi(3 * (size_t)n, 0.0);
   bool anyEll = false;
   int nScenes = 1;
+  std::vector<double4_32a> fv1, fv2;
+  std::vector<int> facetIds;
+  std::vector<int4> facetPairs;
   for (int i = 0; i < n; i++) {
     int sh = p->shape[i];
-    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID)
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID && sh != WDEM_SHAPE_FACET)
       return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (sh == WDEM_SHAPE_FACET) {
+      // fixed facets: nodes 1 and 2 are not integrated, so node 0 may not move either
+      const std::string fid = "Facet #" + std::to_string(i);
+      if (!p->facetVerts) return fail(h, WDEM_ERR_ARG, "facets need wdem_particles.facetVerts");
+      if (h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "facets in a periodic cell are not supported");
+      if ((p->flags[i] & 63u) != 63u) return fail(h, WDEM_ERR_UNSUPPORTED, fid + ": facets must have all DOFs blocked");
+      for (int k = 0; k < 3; k++)
+        if (p->vel[3 * i + k] != 0 || p->angVel[3 * i + k] != 0)
+          return fail(h, WDEM_ERR_UNSUPPORTED, fid + ": moving facets are not supported (velocity must be zero)");
+      if (!(p->radius[i] >= 0) || !std::isfinite(p->radius[i])) return fail(h, WDEM_ERR_ARG, fid + ": bad halfThick");
+      const double* v = p->facetVerts + 9 * (size_t)i;
+      for (int k = 0; k < 9; k++)
+        if (!std::isfinite(v[k])) return fail(h, WDEM_ERR_ARG, fid + ": non-finite node position");
+      if (fv1.empty()) { fv1.assign(n, make_double4_32a(0, 0, 0, 0)); fv2.assign(n, make_double4_32a(0, 0, 0, 0)); }
+      fv1[i] = make_double4_32a(v[3], v[4], v[5], 0);
+      fv2[i] = make_double4_32a(v[6], v[7], v[8], 0);
+      facetIds.push_back(i);
+    }
     if (sh == WDEM_SHAPE_ELLIPSOID) {
       if (!p->semiAxes) return fail(h, WDEM_ERR_ARG, "ellipsoids need wdem_particles.semiAxes");
       const double* sa = p->semiAxes + 3 * i;
@@ -830,7 +859,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     if (asph && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "aspherical nodes in a periodic cell are not supported");
     int ax = p->wallAxis ? p->wallAxis[i] : 0, sense = p->wallSense ? p->wallSense[i] : 0;
     if (sh == WDEM_SHAPE_WALL && (ax < 0 || ax > 2 || sense < -1 || sense > 1)) return fail(h, WDEM_ERR_ARG, "bad wall axis/sense");
-    double r = sh == WDEM_SHAPE_SPHERE ? p->radius[i] : 0.0;
+    double r = (sh == WDEM_SHAPE_SPHERE || sh == WDEM_SHAPE_FACET) ? p->radius[i] : 0.0;  // facets: halfThick
     if (sh == WDEM_SHAPE_ELLIPSOID) {
       // bounding radius: the largest semi-axis (FP32 cull and minDist00Sq of the ellipsoid functors)
       const double* sa = p->semiAxes + 3 * i;
@@ -854,7 +883,8 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     meta[i] = make_int4(sh | (ax << 4) | ((sense + 1) << 8) | (asph ? META_ASPH : 0) | (ipos ? META_IPOS : 0) |
                             (sc << META_SCENE_SHIFT),
                         p->material[i], (int)p->mask[i], (int)fl);
-    if (sh != WDEM_SHAPE_WALL) h->smallIds.push_back(i); else h->largeIds.push_back(i);
+    // walls and facets go to the collider's list of large bodies, tested against every box of their scene
+    if (sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_FACET) h->smallIds.push_back(i); else h->largeIds.push_back(i);
   }
   if (nScenes > 1 && h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "batched scenes in a periodic cell are not supported");
   // walls grouped by scene (stable: ids ascending within a scene); per-scene ranges
@@ -867,6 +897,13 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   }
   h->semi = semi;
   h->hasEll = anyEll;
+  for (int f : facetIds)
+    for (int j : h->largeIds) {
+      const unsigned mm = p->mask[f] & p->mask[j];
+      if (j != f && mm != 0 && (p->scene ? p->scene[f] == p->scene[j] : true)) facetPairs.push_back(make_int4(f, j, (int)mm, 0));
+    }
+  h->facetPairs = facetPairs;
+  h->facetsChecked = ~0u;
   h->matsChecked = -1;
   h->gravAccDirty = true;
   cudaSetDevice(h->device);
@@ -897,6 +934,12 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
       CK(cudaMemcpyAsync(h->d.semi, sv.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(h->d.angMom, am.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
     }
+    CK(cudaStreamSynchronize(s));  // host vectors go out of scope
+  }
+  if (!facetIds.empty()) {
+    if (!h->d.fv1) { CK(dalloc(h->d.fv1, h->N)); CK(dalloc(h->d.fv2, h->N)); }
+    CK(cudaMemcpyAsync(h->d.fv1, fv1.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d.fv2, fv2.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));  // host vectors go out of scope
   }
   if (!h->smallIds.empty())
@@ -949,20 +992,14 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     int a = c->idA[i], bb = c->idB[i];
     if (a < 0 || a >= h->n || bb < 0 || bb >= h->n || a == bb) return fail(h, WDEM_ERR_ARG, "bad contact ids");
     bool swapped = false;
-    {
-      const int sa = h->shape[a], sbb = h->shape[bb];
-      if ((sa == WDEM_SHAPE_SPHERE && sbb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sbb == WDEM_SHAPE_SPHERE) ||
-          (sa == WDEM_SHAPE_ELLIPSOID && sbb == WDEM_SHAPE_WALL)) { std::swap(a, bb); swapped = true; }
-    }
+    if (pairSwaps(h->shape[a], h->shape[bb])) { std::swap(a, bb); swapped = true; }
     ids[i] = make_int2(a, bb);
     if (c->cellDist) {
       int sg = swapped ? -1 : 1;
       cdist[i] = make_int4(sg * c->cellDist[3 * i], sg * c->cellDist[3 * i + 1], sg * c->cellDist[3 * i + 2], 0);
     }
     bool real = c->real[i] != 0;
-    state[i] = (uint8_t)((real ? CS_REAL : CS_POTENTIAL) | (h->shape[a] == WDEM_SHAPE_WALL ? CS_WALL_A : 0) |
-                         (h->shape[bb] == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
-                         (h->shape[a] == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (h->shape[bb] == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
+    state[i] = (uint8_t)((real ? CS_REAL : CS_POTENTIAL) | pairShapeBits(h->shape[a], h->shape[bb]));
     step0[i] = c->stepCreated[i];
     if (real) {
       if (!c->trsf || !c->contPt || !c->force || !c->kn || !c->kt || !c->tanPhi) return fail(h, WDEM_ERR_ARG, "real contact without history arrays");
@@ -1134,6 +1171,17 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   if (h->hasEll && (h->P.law != WDEM_LAW_IDEALELPL || h->P.cp2 != WDEM_CP2_FRICT))
     return fail(h, WDEM_ERR_UNSUPPORTED,
                 "ellipsoids and aspherical nodes run with Cp2_FrictMat_FrictPhys + Law2_L6Geom_FrictPhys_IdealElPl only");
+  if (!h->facetPairs.empty() && h->facetsChecked != h->P.loneMask) {
+    // Cg2_Facet_Facet_L6Geom and Cg2_Wall_Facet_L6Geom are not implemented: such pairs must be excluded by
+    // the masks (Collider::mayCollide), as DemField.defaultBoundaryMask with DemField.loneMask does
+    for (const int4& q : h->facetPairs)
+      if (((unsigned)q.z & h->P.loneMask) == 0)
+        return fail(h, WDEM_ERR_UNSUPPORTED, "Facet #" + std::to_string(q.x) + " may collide with " +
+                                                 (h->shape[q.y] == WDEM_SHAPE_WALL ? "Wall #" : "Facet #") + std::to_string(q.y) +
+                                                 ": facet-facet and wall-facet contacts are not implemented (give the "
+                                                 "boundaries a common loneMask bit)");
+    h->facetsChecked = h->P.loneMask;
+  }
   if (h->device >= 0 && h->device < 64 && g_matsOwner[h->device] != h) {
     cudaSetDevice(h->device);
     uploadMaterials(h);  // another handle of this process uploaded its table since
@@ -1601,6 +1649,10 @@ int wdem_remove_particles(wdem_handle* h, int32_t m, const int32_t* ids, const d
   CK(cudaStreamSynchronize(s));
   h->needRebuild = true;
   h->actValid = false;
+  // a removed facet (mask 0) no longer pairs with the other boundaries
+  h->facetPairs.erase(std::remove_if(h->facetPairs.begin(), h->facetPairs.end(),
+                                     [&](const int4& q) { return seen[q.x] || seen[q.y]; }),
+                      h->facetPairs.end());
   return WDEM_OK;
 }
 
@@ -1624,6 +1676,9 @@ int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* i
   }
   for (int i = h->n; i < newN; i++)
     if (!seen[i]) return fail(h, WDEM_ERR_ARG, "new slots must extend the particle count contiguously (slot " + std::to_string(i) + " missing)");
+  for (int k = 0; k < m; k++)
+    if (ids[k] < h->n && (h->shape[ids[k]] == WDEM_SHAPE_WALL || h->shape[ids[k]] == WDEM_SHAPE_FACET))
+      return fail(h, WDEM_ERR_ARG, "slot " + std::to_string(ids[k]) + " belongs to a wall or facet and is not reused");
   std::vector<double4_32a> rec((size_t)EDIT_RECORDS * m);
   std::vector<int4> meta(m);
   const double nan = std::numeric_limits<double>::quiet_NaN();
@@ -1813,7 +1868,9 @@ int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
   }
   if (c->homoDeform != 4) return fail(h, WDEM_ERR_UNSUPPORTED, "Cell.homoDeform other than gradV2 (4) is not supported");
   for (int s : h->shape)
-    if (s != WDEM_SHAPE_SPHERE) return fail(h, WDEM_ERR_UNSUPPORTED, "walls in a periodic cell are not supported");
+    if (s != WDEM_SHAPE_SPHERE)
+      return fail(h, WDEM_ERR_UNSUPPORTED, std::string(s == WDEM_SHAPE_FACET ? "facets" : s == WDEM_SHAPE_WALL ? "walls" : "ellipsoids") +
+                                               " in a periodic cell are not supported");
   if (h->nContacts > 0 && !h->periodic) return fail(h, WDEM_ERR_STATE, "set the cell before uploading contacts");
   if (h->cs.nScenes > 1) return fail(h, WDEM_ERR_UNSUPPORTED, "batched scenes in a periodic cell are not supported");
   HostCell& hc = h->cell;

@@ -27,15 +27,19 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "../../include/wdem.h"
 
 namespace wdem {
 
 // kernels launched by the library in this process (incremented at every launch site)
 extern long long g_kernel_launches;
 
-// contact state byte: bits 0-1 the lifecycle state, bit 2 "pA is a wall", bit 3 "pB is a wall"
+// contact state byte: bits 0-1 the lifecycle state, bit 2 "pA is a wall", bit 3 "pB is a wall", bits 4-5
+// "pA / pB is an ellipsoid", bit 7 "pA is a facet" (pB then is a sphere).  A pair without a geometry
+// functor (wall + wall, facet + ellipsoid) carries both wall bits and is never evaluated.
 enum ContactState : uint8_t { CS_POTENTIAL = 0, CS_REAL = 1, CS_PENDING = 2, CS_DEAD = 3 };
-enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_ELL_B = 32, CS_ELL = 48, CS_SHAPES = 60 };
+enum : uint8_t { CS_MASK = 3, CS_WALL_A = 4, CS_WALL_B = 8, CS_ELL_A = 16, CS_ELL_B = 32, CS_ELL = 48, CS_FACET = 128,
+                 CS_SHAPES = 188 };
 // a potential pair that cannot touch before the next collider run (set by the contact cull, dropped by
 // the rebuild's carry): every particle stays within verletDist of its position at the last rebuild,
 // so two bounding spheres come closer by at most 4 verletDist between any two steps without a rebuild
@@ -47,6 +51,21 @@ enum { META_ASPH = 1 << 12, META_ORI_FIXED = 1 << 13, META_IPOS = 1 << 14 };
 // meta.x bits 16..27: scene index of batched independent scenes
 enum { META_SCENE_SHIFT = 16, MAX_SCENES = 4096 };
 __host__ __device__ __forceinline__ int sceneOf(int metax) { return (metax >> META_SCENE_SHIFT) & (MAX_SCENES - 1); }
+// Pair orientation as the geometry functors take it (GeomDispatcher::getFunctor2D swaps a fresh contact,
+// ContactLoop.cpp:144-150): the pair (lower id, higher id) is swapped when its shapes come in the order
+// Sphere+Wall, Ellipsoid+Sphere, Ellipsoid+Wall or Sphere+Facet.
+__host__ __device__ __forceinline__ bool pairSwaps(int sa, int sb) {
+  return (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
+         (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET);
+}
+// shape bits of the state byte of an oriented pair; pairs with no functor (wall + wall, facet + anything but
+// a sphere) get both wall bits and are skipped
+__host__ __device__ __forceinline__ uint8_t pairShapeBits(int sa, int sb) {
+  if (sa == WDEM_SHAPE_FACET || sb == WDEM_SHAPE_FACET)
+    return (uint8_t)((sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) ? CS_FACET : (CS_WALL_A | CS_WALL_B));
+  return (uint8_t)((sa == WDEM_SHAPE_WALL ? CS_WALL_A : 0) | (sb == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
+                   (sa == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (sb == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
+}
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
@@ -135,6 +154,7 @@ struct Particles {
   double4_32a *semi, *angMom, *lastOri;
   double* maxRot;
   float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
+  double4_32a *fv1, *fv2;  // facets: nodes 1 and 2 (node 0 is posr); null when the scene has no facets
   uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
   unsigned* rotList;    // untouched spinning spheres, rotated by the integrator's list pass this step
   unsigned* touchList;  // particles with contact forces this step (integrated by the list pass)

@@ -279,6 +279,57 @@ class Ellipsoid(Shape):
         return p
 
 
+class Facet(Shape):
+    """Facet (src/dem/Facet.hpp:8-57): a triangle of three nodes with halfThick.  The GPU engine takes fixed
+    facets (all DOFs blocked, at rest) without fakeVel and without neighbour angles (n21lim NaN); it contacts
+    spheres through Cg2_Facet_Sphere_L6Geom.  The engine binds node 0 to the particle's slot; nodes 1 and 2
+    keep their positions."""
+    _shape = abi.SHAPE_FACET
+
+    def __init__(self, halfThick=0.0):
+        super().__init__()
+        self.halfThick = float(halfThick)
+        self.fakeVel = np.zeros(3)
+
+    def _verts(self):
+        return [nd.pos if k == 0 else nd._local["pos"] for k, nd in enumerate(self.nodes)]
+
+    def getNormal(self):
+        """Facet::getNormal (Facet.cpp:74-77): (n1 - n0) x (n2 - n0), normalised."""
+        a, b, c = self._verts()
+        v = np.cross(b - a, c - a)
+        return v / np.linalg.norm(v)
+
+    def getArea(self):
+        a, b, c = self._verts()
+        return 0.5 * float(np.linalg.norm(np.cross(b - a, c - a)))
+
+    def getCentroid(self):
+        a, b, c = self._verts()
+        return (a + b + c) / 3.0
+
+    def equivRadius(self):
+        return nan
+
+    @staticmethod
+    def make(vertices, halfThick=0.0, mat=None, fixed=True, mask=DEFAULT_BOUNDARY_MASK, fakeVel=None, wire=True,
+             color=None):
+        """woo.utils.facet / Facet.make (py/utils.py:315-341): three new nodes (masses and inertia 0,
+        all DOFs blocked when fixed), DemField.defaultBoundaryMask."""
+        if fakeVel is not None and np.any(np.asarray(fakeVel, float) != 0):
+            raise RuntimeError("Facet.fakeVel is not supported by the GPU engine")
+        mat = mat if mat is not None else defaultMaterial()
+        sh = Facet(halfThick)
+        for v in vertices:
+            n = Node(pos=v)
+            if fixed:
+                n.dem.blocked = "xyzXYZ"
+            sh.nodes.append(n)
+        if len(sh.nodes) != 3:
+            raise ValueError("Facet.make needs three vertices")
+        return Particle(shape=sh, material=mat, mask=mask)
+
+
 def defaultMaterial():
     """woo.utils.defaultMaterial (py/utils.py:86-92)."""
     return FrictMat(density=1e3, young=1e7, ktDivKn=0.2, tanPhi=math.tan(0.5))
@@ -510,6 +561,9 @@ class Contact:
                     isinstance(pa.shape, Wall) and isinstance(pb.shape, Sphere):
                 r1 = -pb.shape.radius if isinstance(pa.shape, Wall) else pa.shape.radius
                 r2 = pb.shape.radius
+            elif isinstance(pa.shape, Facet):
+                # Cg2_Facet_Sphere_L6Geom: max(halfThick, radius) and radius (Facet.cpp:389)
+                r1, r2 = max(pa.shape.halfThick, pb.shape.radius), pb.shape.radius
             else:
                 # ellipsoid functors: distances of the contact point from the centres (Ellipsoid.cpp:250, 349)
                 cp = ca.contPt[i]
@@ -599,6 +653,14 @@ class ContactContainer:
 _FIELD_ARRAY_NAMES = ("pos", "ori", "vel", "angVel", "force", "torque", "mass", "inertia", "flags", "angMom")
 
 
+def _bind_nodes(p, field):
+    """The particle's node state lives in the field's arrays at its id; a facet binds node 0 only (nodes 1
+    and 2 are fixed positions carried in ParticleArrays.facetVerts)."""
+    nodes = p.shape.nodes[:1] if isinstance(p.shape, Facet) else p.shape.nodes
+    for n in nodes:
+        n._field, n._idx = field, p.id
+
+
 class DemField:
     """DemField (src/dem/Particle.hpp:310-391)."""
     defaultMovableBit, defaultBoundaryBit, defaultOutletBit, defaultStaticBit = 1, 2, 4, 8
@@ -634,8 +696,7 @@ class DemField:
         # slots of existing particles whose node is in DemField.nodes (what outlets look at)
         self._moving = np.zeros(arrays.n, bool)
         for p in self.par:
-            for n in p.shape.nodes:
-                n._field, n._idx = self, p.id
+            _bind_nodes(p, self)
             self._moving[p.id] = getattr(p, "_integrated", True)
 
     def _get(self, idx, name):
@@ -798,6 +859,14 @@ class Cg2_Sphere_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
 
 class Cg2_Wall_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
     """Cg2_Wall_Sphere_L6Geom (src/dem/Wall.cpp:50-84)."""
+
+
+class Bo1_Facet_Aabb(BoundFunctor):
+    """Bo1_Facet_Aabb (src/dem/Facet.hpp:58-64)."""
+
+
+class Cg2_Facet_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Facet_Sphere_L6Geom (src/dem/Facet.cpp:333-390)."""
 
 
 class Bo1_Ellipsoid_Aabb(BoundFunctor):
@@ -983,7 +1052,7 @@ class GpuDemEngine(Engine):
 
     def __init__(self, cg2=None, cp2=None, law=None, **kw):
         super().__init__(**kw)
-        self.geoFunctors = list(cg2 or [Cg2_Sphere_Sphere_L6Geom(), Cg2_Wall_Sphere_L6Geom()])
+        self.geoFunctors = list(cg2 or [Cg2_Sphere_Sphere_L6Geom(), Cg2_Facet_Sphere_L6Geom(), Cg2_Wall_Sphere_L6Geom()])
         self.phyFunctors = list(cp2 or [Cp2_FrictMat_FrictPhys()])
         self.lawFunctors = list(law or [Law2_L6Geom_FrictPhys_IdealElPl()])
         self._h = None
@@ -1018,6 +1087,9 @@ class GpuDemEngine(Engine):
                 self._functor(self.geoFunctors, (Cg2_Ellipsoid_Ellipsoid_L6Geom,)) is None:
             raise RuntimeError("ellipsoids in the scene need Cg2_Ellipsoid_Ellipsoid_L6Geom (or its sphere variant) "
                                "in ContactLoop.geoFunctors")
+        if any(isinstance(p.shape, Facet) for p in field.par) and \
+                self._functor(self.geoFunctors, (Cg2_Facet_Sphere_L6Geom,)) is None:
+            raise RuntimeError("facets in the scene need Cg2_Facet_Sphere_L6Geom in ContactLoop.geoFunctors")
         cp2 = self._functor(self.phyFunctors, (Cp2_HertzMat_HertzPhys,)) or self._functor(self.phyFunctors, (Cp2_FrictMat_FrictPhys,))
         law = self._functor(self.lawFunctors, (Law2_L6Geom_HertzPhys_DMT,)) or self._functor(self.lawFunctors, (Law2_L6Geom_FrictPhys_IdealElPl,))
         if cp2 is None or law is None:
@@ -1118,6 +1190,9 @@ class GpuDemEngine(Engine):
             pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
         elif isinstance(sh, Ellipsoid):
             pa.shape[i] = abi.SHAPE_ELLIPSOID; pa.semiAxes[i] = sh.semiAxes
+        elif isinstance(sh, Facet):
+            pa.shape[i] = abi.SHAPE_FACET; pa.radius[i] = sh.halfThick
+            pa.facetVerts[i] = np.concatenate(sh._verts())
         else:
             raise RuntimeError(f"GpuDemEngine: unsupported shape {type(sh).__name__}")
         pa.material[i] = self._mat_index[id(p.material)]
@@ -1347,7 +1422,9 @@ class GpuDemEngine(Engine):
         kin = {"pos", "vel", "angVel", "ori"}
         dv = self._device_view(field, pa)
         added = sorted(getattr(field, "_added", ()))
-        if added and field._dirty <= kin | {"added"} and n <= self._cap:
+        # facets (multi-node) are not inserted in place: a full upload takes them
+        inplace = not any(isinstance(field.par[i].shape, Facet) for i in added if field.par.exists(i))
+        if added and inplace and field._dirty <= kin | {"added"} and n <= self._cap:
             # particles from inlets go into their slots on the device (wdem_add_particles); the rest of
             # the particle and contact state stays there
             self._h.set_params(self._params)   # materials of added particles first
@@ -1406,8 +1483,7 @@ class GpuDemEngine(Engine):
             if id(m) not in self._mat_index:
                 self._add_material(m)
             self._pack_one(pa, p.id, p)
-            for nd in p.shape.nodes:
-                nd._field, nd._idx = field, p.id
+            _bind_nodes(p, field)
             field._dead.discard(p.id)
             field._moving[p.id] = getattr(p, "_integrated", True)
         field._dirty.add("added")

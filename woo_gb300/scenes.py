@@ -297,6 +297,83 @@ def periodic_cloud(n, seed, size=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="f
     return SceneSpec(p, mats, pa, f"peri{n}", dict(seed=seed, dt=dt), cell=cell)
 
 
+def add_facets(pa, triangles, halfThick=0.0, mat=0):
+    """ParticleArrays with fixed facets appended after the particles of pa: Facet.make defaults
+    (py/utils.py:315-341) -- DemField.defaultBoundaryMask, all DOFs blocked, node masses and inertia 0;
+    node 0 is the particle's position and the radius slot holds halfThick."""
+    tri = np.asarray(triangles, np.float64).reshape(-1, 3, 3)
+    n0, nf = pa.n, len(tri)
+    out = abi.ParticleArrays(n0 + nf)
+    for k, v in pa.__dict__.items():
+        if isinstance(v, np.ndarray):
+            getattr(out, k)[:n0] = v
+    f = slice(n0, n0 + nf)
+    out.shape[f] = abi.SHAPE_FACET
+    out.pos[f] = tri[:, 0]
+    out.facetVerts[f] = tri.reshape(nf, 9)
+    out.radius[f] = halfThick
+    out.material[f] = mat
+    out.mask[f] = DEFAULT_BOUNDARY_MASK
+    out.flags[f] = abi.DOF_ALL
+    out.mass[f] = 0.0
+    out.inertia[f] = 0.0
+    return out
+
+
+def valley_facets(lo, hi, nx, ny, depth):
+    """A floor over the box's x/y extent made of nx x ny rectangles split into two triangles each, folded
+    into a V along x (height depth * |x - xc| / (xc - x0) above lo[2]); vertex order gives upward normals."""
+    xs = np.linspace(lo[0], hi[0], nx + 1)
+    ys = np.linspace(lo[1], hi[1], ny + 1)
+    xc = 0.5 * (lo[0] + hi[0])
+    z = lambda x: lo[2] + depth * abs(x - xc) / (xc - lo[0])
+    tris = []
+    for i in range(nx):
+        for j in range(ny):
+            a = (xs[i], ys[j], z(xs[i]))
+            b = (xs[i + 1], ys[j], z(xs[i + 1]))
+            c = (xs[i + 1], ys[j + 1], z(xs[i + 1]))
+            d = (xs[i], ys[j + 1], z(xs[i]))
+            tris.append((a, b, c))
+            tris.append((a, c, d))
+    return np.array(tris)
+
+
+def facet_valley(n, seed, box=(0.1, 0.1, 0.1), nx=6, ny=5, depth=0.02, halfThick=0.0, law="frict", vel_scale=0.3,
+                 dense=1.0, gravity=(0, 0, -9.81), damping=0.2, **kw):
+    """Spheres falling into a V-shaped valley triangulated into facets (2 nx ny Facets, halfThick), with four
+    side walls: exercises facet interiors, edges and vertices."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.zeros(3), np.asarray(box, np.float64)
+    cloud_lo = lo + np.array([0, 0, depth + 0.001])
+    centers, radii = make_cloud(cloud_lo, hi, 0.004, 0.006, n, seed)
+    if dense != 1.0:
+        c = 0.5 * (cloud_lo + hi)
+        centers = c + (centers - c) * dense
+    k = len(radii)
+    if law == "frict":
+        mats_py = [dict(kind=abi.MAT_FRICT, density=2500.0, young=1e7, ktDivKn=0.2, tanPhi=0.5),
+                   dict(kind=abi.MAT_FRICT, density=2000.0, young=3e7, ktDivKn=0.3, tanPhi=0.3)]
+        extra = dict(cp2=abi.CP2_FRICT, law=abi.LAW_IDEALELPL)
+    else:
+        mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=5e7, ktDivKn=0.2, tanPhi=0.3, surfEnergy=0.01),
+                   dict(kind=abi.MAT_HERTZ, density=1200.0, young=8e7, ktDivKn=0.2, tanPhi=0.6, surfEnergy=0.02)]
+        extra = dict(cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.8)
+    extra.update(kw)
+    mat_idx = rng.integers(0, 2, k).astype(np.int32)
+    mats = materials_array(mats_py)
+    walls = [w for w in box_walls(lo, hi) if w[0] != 2]
+    pa = assemble(centers, radii, mat_idx, walls, mats_py, vel=rng.normal(0, vel_scale, (k, 3)))
+    nw = len(walls)
+    pa.angVel[nw:] = rng.normal(0, 5.0, (k, 3))
+    g = np.asarray(gravity, np.float64)
+    pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
+    pa = add_facets(pa, valley_facets(lo, hi, nx, ny, depth), halfThick=halfThick, mat=1)
+    dt = 0.3 * pwave_dt(radii, mat_idx, mats_py)
+    p = default_params(mats, dt=dt, gravity=gravity, damping=damping, **extra)
+    return SceneSpec(p, mats, pa, f"valley{n}", dict(seed=seed, dt=dt, n_spheres=k, n_facets=2 * nx * ny))
+
+
 def quat_from_axis_angle(axis, angle):
     """Quaternion(AngleAxis(angle, axis/|axis|)) as (w, x, y, z)."""
     ax = np.asarray(axis, np.float64)

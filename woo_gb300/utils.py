@@ -1,5 +1,5 @@
 """woo.utils slice for the DEM hot path (py/utils.py): defaultEngines / DemField.minimalEngines,
-sphere/wall constructors, defaultMaterial."""
+sphere/ellipsoid/facet/wall constructors, defaultMaterial."""
 import math
 import warnings
 
@@ -39,9 +39,10 @@ def defaultEngines(damping=0.0, gravity=None, verletDist=-0.05, kinSplit=False, 
         raise ValueError("only the sweep-and-prune collider ('sap') is provided")
     engines = [
         dem.Leapfrog(damping=damping, reset=True, kinSplit=kinSplit, dontCollect=dontCollect, label="leapfrog"),
-        dem.InsertionSortCollider([dem.Bo1_Sphere_Aabb(), dem.Bo1_Wall_Aabb()], label="collider", verletDist=verletDist),
-        dem.ContactLoop([dem.Cg2_Sphere_Sphere_L6Geom(), dem.Cg2_Wall_Sphere_L6Geom()], cp2, law, applyForces=True,
-                        label="contactLoop"),
+        dem.InsertionSortCollider([dem.Bo1_Sphere_Aabb(), dem.Bo1_Facet_Aabb(), dem.Bo1_Wall_Aabb()], label="collider",
+                                  verletDist=verletDist),
+        dem.ContactLoop([dem.Cg2_Sphere_Sphere_L6Geom(), dem.Cg2_Facet_Sphere_L6Geom(), dem.Cg2_Wall_Sphere_L6Geom()],
+                        cp2, law, applyForces=True, label="contactLoop"),
     ]
     if dynDtPeriod > 0:
         engines.append(dem.DynDt(stepPeriod=dynDtPeriod, label="dynDt"))
@@ -62,6 +63,12 @@ def ellipsoid(center, semiAxes, ori=(1, 0, 0, 0), angVel=None, color=None, mat=N
     if angVel is not None:
         p.angVel = angVel
     return p
+
+
+def facet(vertices, fakeVel=None, halfThick=0.0, fixed=True, wire=True, color=None, highlight=False, mat=None,
+          visible=True, mask=dem.DEFAULT_BOUNDARY_MASK):
+    """py/utils.py:315-341: a Facet of three new nodes."""
+    return dem.Facet.make(vertices, halfThick=halfThick, mat=mat, fixed=fixed, mask=mask, fakeVel=fakeVel)
 
 
 def wall(position, axis, sense=0, glAB=None, fixed=True, mass=0, color=None, mat=None, visible=True,
