@@ -70,3 +70,32 @@ def test_resume_continues_exactly(tmp_path, law):
     assert np.array_equal(np.sort(ca.keys()[ra]), np.sort(cb.keys()[rb]))
     oa, ob = np.argsort(ca.keys()[ra]), np.argsort(cb.keys()[rb])
     assert np.array_equal(ca.force[ra][oa], cb.force[rb][ob])
+
+
+
+def test_resume_sheared_periodic(tmp_path):
+    """A sheared periodic cell under simple shear, saved halfway and resumed, continues bit for bit.  The
+    archive holds hSize, trsf, gradV and nextGradV but not Cell.pprevHsize: every step starts with
+    Cell::integrateAndUpdate (src/core/Scene.cpp:411), which sets pprevHsize = (previous + new hSize) / 2
+    before the contact loop reads it (Cell::intrShiftVel, src/core/Cell.cpp:31), so the value a resumed
+    handle starts with (hSize, as after the reference's Scene.load) is never used."""
+    spec = scenes.periodic_cloud(300, 4, dense=0.85)
+    whole = bridge.Oracle(spec.params, spec.particles, cell=spec.cell)
+    whole.step(150)
+    first = bridge.Oracle(spec.params, spec.particles, cell=spec.cell)
+    first.step(70)
+    cell = first.cell()
+    assert not np.array_equal(cell["pprevHsize"], cell["hSize"])
+    c = first.contacts()
+    assert np.any(c.cellDist[c.real == 1] != 0)
+    path = tmp_path / "half.npz"
+    checkpoint.save_state(path, _state(first, spec.particles), c, 70, spec.params.dt, cell)
+    s = checkpoint.load_state(path)
+    p = scenes.copy_params(spec.params)
+    p.step, p.dt = s["step"], s["dt"]
+    second = bridge.Oracle(p, s["particles"], contacts=s["contacts"], cell=s["cell"])
+    second.step(80)
+    a, b = whole.particles(), second.particles()
+    for k in ("pos", "vel", "angVel", "force", "torque"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert np.array_equal(whole.cell()["hSize"], second.cell()["hSize"])

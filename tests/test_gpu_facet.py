@@ -118,4 +118,4 @@ def test_scene_api(wdem_lib):
     for p in S.dem.par:
         if isinstance(p.shape, dem.Sphere):
             assert np.array_equal(p.pos, po.pos[p.id]) and np.array_equal(p.vel, po.vel[p.id])
-    assert len(S.dem.con) == int(o.contacts().real.sum())
+    assert len(S.dem.con) == o.contacts().n

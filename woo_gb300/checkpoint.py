@@ -7,7 +7,10 @@ InsertionSortCollider.hpp:225).  This format holds what the GPU engine needs to 
 wdem_particles and wdem_contacts arrays of woo_gb300.abi, the cell matrices, Scene.step and Scene.dt.
 After `resume` the first step runs the collider in full, as the reference does after a load, so real
 contacts, their history and the particle trajectories continue exactly; potential (not touching)
-pairs are found anew.  The ellipsoid solver's last maximiser (a warm start only) is not saved.
+pairs are found anew.  The ellipsoid solver's last maximiser (a warm start only) is not saved, nor is
+Cell.pprevHsize: every step starts with Cell::integrateAndUpdate (src/core/Scene.cpp:411), which sets it
+from the previous and new hSize before the contact loop reads it, so a sheared periodic run resumes bit
+for bit without it.
 """
 import numpy as np
 

@@ -635,7 +635,7 @@ class ContactContainer:
         collider then runs in full at the next step."""
         f = self._field
         if f._engine is not None:
-            f._engine._remove_contacts_where(f, [p.id for p in f.par], lambda a, b: False)
+            f._engine._clear_contacts(f)
 
     def realRatio(self):
         n = len(self)
@@ -1461,6 +1461,19 @@ class GpuDemEngine(Engine):
             self._h.set_params(self._params)
             self._h.upload_contacts(con.take(~drop))
             field._dirty.clear()
+        field._con_cache = None
+
+    def _clear_contacts(self, field):
+        """An empty contact container replaces the device's (nothing is downloaded).  The particle arrays
+        go up with it: they carry the forces of the last contact pass, which the next integration uses as
+        Woo's DemData.force outlives the cleared contacts."""
+        if field._stale:
+            self._download_particles(field)
+        self._h.set_params(self._params)
+        self._h.upload_particles(self._device_view(field, field._arrays))
+        self._h.set_params(self._params)
+        self._h.upload_contacts(abi.ContactArrays(0))
+        field._dirty.clear()
         field._con_cache = None
 
     def _add_particles(self, field, pars):
