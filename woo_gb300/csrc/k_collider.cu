@@ -683,6 +683,16 @@ __global__ void k_csr_entries(Contacts c, long long nc, int idBits, unsigned lon
   keys[2 * e + 1] = ((unsigned long long)(unsigned)id.y << idBits) | (unsigned)id.x;
   vals[2 * e + 1] = (unsigned)e | 0x80000000u;
 }
+// the sorted entries, and each contact's two entry positions (where the contact pass writes its shares)
+__global__ void k_csr_ent_slots(const unsigned* vals, long long ne, unsigned* ent, int2* slot) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const unsigned v = vals[e];
+  ent[e] = v;
+  const unsigned ci = v & 0x7fffffffu;
+  if (v >> 31) slot[ci].y = (int)e;
+  else slot[ci].x = (int)e;
+}
 __global__ void k_csr_rows(const unsigned long long* keys, long long ne, int idBits, int n, int* rowptr) {
   long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) {
@@ -898,7 +908,7 @@ __global__ void k_stress_terms(StepParams P, Particles p, Contacts c, long long 
       const int4 cd = c.cdist[i];
       branch = branch + mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
     }
-    const double4_32a f4 = c.out[OUT_RECORDS * i + OUT_F];
+    const double4_32a f4 = c.out[OUT_RECORDS * (long long)c.slot[i].x + OUT_F];  // pA's entry: the force on pA
     const double F[3] = {f4.x, f4.y, f4.z};
     const double b[3] = {branch.x, branch.y, branch.z};
     for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) v[3 * r + q] = F[r] * b[q];
@@ -1019,7 +1029,7 @@ void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderS
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, ne, 2 * idBits, cs);
   long long threads = ne > 0 ? ne : (long long)n + 1;
   (k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr), ++::wdem::g_kernel_launches);
-  if (ne > 0) cudaMemcpyAsync(csr.ent, cs.vals, ne * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
+  if (ne > 0) (k_csr_ent_slots<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(cs.vals, ne, csr.ent, c.slot), ++::wdem::g_kernel_launches);
 }
 
 }  // namespace wdem

@@ -585,10 +585,18 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   const d3 TA = cross(xcA, F) + T;
   const d3 FB = F * -1.0;
   const d3 TB = cross(xcB, FB) + T * -1.0;
-  double4_32a* o = c.out + OUT_RECORDS * i;
-  o[OUT_F] = make_double4_32a(F.x, F.y, F.z, 0.0);
-  o[OUT_TA] = make_double4_32a(TA.x, TA.y, TA.z, 0.0);
-  o[OUT_TB] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
+  // each particle's share at its CSR entry, stamped with this pass; a facet (pA) takes none
+  // (ContactLoop::applyForceUninodal skips shapes with more than one node, ContactLoop.cpp:270-276)
+  const int2 sl = c.slot[i];
+  const double stamp = __longlong_as_double(P.seq);
+  if (PERI || !(sb & CS_FACET)) {
+    double4_32a* oa = c.out + OUT_RECORDS * (long long)sl.x;
+    oa[OUT_F] = make_double4_32a(F.x, F.y, F.z, stamp);
+    oa[OUT_T] = make_double4_32a(TA.x, TA.y, TA.z, 0.0);
+  }
+  double4_32a* ob = c.out + OUT_RECORDS * (long long)sl.y;
+  ob[OUT_F] = make_double4_32a(FB.x, FB.y, FB.z, stamp);
+  ob[OUT_T] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
 }
 
 // BS threads a block and 512 threads an SM (<= 128 registers a thread, no spills); the grid (blocks per

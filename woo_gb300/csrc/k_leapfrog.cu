@@ -17,6 +17,20 @@ namespace wdem {
 WDEM_VARIANT_BEGIN
 
 // F = m g (unless gravitySkip) + sum of contact forces; T = sum of contact torques
+// Contact forces and torques of particle i from the previous contact pass: its CSR row's records, in the
+// row's order (the partner ids'), those stamped by that pass only (contacts real after it).
+__device__ __forceinline__ void gatherRow(const StepParams& P, int i, const Contacts& c, const Csr& csr, d3& F, d3& T) {
+  const long long want = P.seq - 1;
+  const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
+  for (int e = e0; e < e1; e++) {
+    const double4_32a* o = c.out + OUT_RECORDS * (long long)e;
+    const double4_32a f4 = o[OUT_F];
+    if (__double_as_longlong(f4.w) != want) continue;
+    F = F + xyz(f4);
+    T = T + xyz(o[OUT_T]);
+  }
+}
+
 __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double mass, unsigned flags, const Contacts& c,
                                             const Csr& csr, d3& F, d3& T) {
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
@@ -29,25 +43,7 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
     F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
   } else F = mk(0, 0, 0);
   T = mk(0, 0, 0);
-  const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
-  for (int e = e0; e < e1; e++) {
-    const unsigned en = csr.ent[e];
-    const unsigned ci = en & 0x7fffffffu;
-    const uint8_t s = c.state[ci];
-    if ((s & CS_MASK) != CS_REAL) continue;
-    // a facet (pA) gets no force from its contacts: ContactLoop::applyForceUninodal skips shapes with
-    // more than one node (ContactLoop.cpp:270-276)
-    if ((s & CS_FACET) && !(en >> 31)) continue;
-    const double4_32a* o = c.out + OUT_RECORDS * (long long)ci;
-    const d3 f = xyz(o[OUT_F]);
-    if (en >> 31) {
-      F = F + f * -1.0;
-      T = T + xyz(o[OUT_TB]);
-    } else {
-      F = F + f;
-      T = T + xyz(o[OUT_TA]);
-    }
-  }
+  gatherRow(P, i, c, csr, F, T);
 }
 
 // Raises the collider trigger.  All particles of a free-falling cloud cross the verlet distance in the
@@ -428,23 +424,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
              gravForce(mass, mf, P.gravity[2], skipAxis == 2));
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
-    if (touchedNow) {
-      const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
-      for (int e = e0; e < e1; e++) {
-        const unsigned en = csr.ent[e];
-        const unsigned ci = en & 0x7fffffffu;
-        if ((c.state[ci] & CS_MASK) != CS_REAL) continue;
-        const double4_32a* o = c.out + OUT_RECORDS * (long long)ci;
-        const d3 f = xyz(o[OUT_F]);
-        if (en >> 31) {
-          F = F + f * -1.0;
-          T = T + xyz(o[OUT_TB]);
-        } else {
-          F = F + f;
-          T = T + xyz(o[OUT_TA]);
-        }
-      }
-    }
+    if (touchedNow) gatherRow(P, i, c, csr, F, T);
   } else {
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }

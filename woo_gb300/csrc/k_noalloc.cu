@@ -54,7 +54,7 @@ k_stress_noalloc(StepParams P, Particles p, Contacts c, long long nc, unsigned c
       const int4 cd = c.cdist[i];
       branch = branch + mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
     }
-    const double4_32a f4 = c.out[OUT_RECORDS * i + OUT_F];
+    const double4_32a f4 = c.out[OUT_RECORDS * (long long)c.slot[i].x + OUT_F];  // pA's entry: the force on pA
     const double F[3] = {f4.x, f4.y, f4.z};
     const double b[3] = {branch.x, branch.y, branch.z};
     for (int r = 0; r < 3; r++)

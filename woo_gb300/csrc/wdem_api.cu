@@ -161,6 +161,7 @@ struct wdem_handle {
   bool needRebuild = true;
   bool keepGeom = false;
   long long step = 0;
+  long long seq = 0;            // contact passes run so far (stamps of the force records; never reset)
   long long nFullRuns = 0;
   int lastRunFull = 0;
   // queued steps (runQueued): depth limit (0 or 1: every step checked on the host), mean steps between
@@ -263,7 +264,7 @@ void freeContacts(ContactBuf& b) {
   Contacts& c = b.c;
   cudaFree(c.ids); cudaFree(c.state); cudaFree(c.act); cudaFree(c.step0); cudaFree(c.tanPhi);
   for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
-  cudaFree(c.out);
+  cudaFree(c.out); cudaFree(c.slot);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   cudaFree(c.cdist);
@@ -285,7 +286,10 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if ((e = dalloc(c.tanPhi, cap))) return e;
   int nh = hertz ? HIST_COUNT : HIST_FRICT;
   for (int k = 0; k < nh; k++) if ((e = dalloc(c.hist[k], cap))) return e;
-  if ((e = dalloc(c.out, (size_t)OUT_RECORDS * cap))) return e;
+  // two CSR entries per contact; stamps start at -1 (no pass has written them)
+  if ((e = dalloc(c.out, (size_t)OUT_RECORDS * 2 * cap))) return e;
+  if ((e = cudaMemset(c.out, 0xff, (size_t)OUT_RECORDS * 2 * cap * sizeof(double4_32a)))) return e;
+  if ((e = dalloc(c.slot, cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   if ((e = dalloc(c.work, cap))) return e;
@@ -309,7 +313,6 @@ void copyContacts(cudaStream_t s, ContactBuf& dst, const ContactBuf& src, long l
   cudaMemcpyAsync(dst.c.tanPhi, src.c.tanPhi, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
   for (int k = 0; k < HIST_COUNT; k++)
     if (dst.c.hist[k] && src.c.hist[k]) cudaMemcpyAsync(dst.c.hist[k], src.c.hist[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(dst.c.out, src.c.out, (size_t)OUT_RECORDS * n * sizeof(double4_32a), cudaMemcpyDeviceToDevice, s);
 }
 
 unsigned long long nextPow2(unsigned long long v) {
@@ -1113,8 +1116,10 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
   const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
   StepParams P = h->P;
+  const long long q0 = h->seq;
   for (int g = 0; g < ahead; g++) {
     P.step = s0 + g;
+    P.seq = q0 + 1 + g;
     (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
     const bool full = !h->actValid;
     h->actValid = true;
@@ -1135,6 +1140,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
     if (k < s0 || k >= s0 + ahead) return fail(h, WDEM_ERR_STATE, "queued steps: trigger outside the queue");
     h->step = k;
     h->P.step = k;
+    h->P.seq = q0 + 1 + (k - s0);
     h->raw.step = k;
     CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
@@ -1150,6 +1156,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   }
   // the queue ends at or before the next DynDt step: run it if the last completed step is due
   if ((rc = dynDtAfterContacts(h, s0 + done - 1))) return rc;
+  h->seq = q0 + done;
   h->step = s0 + done;
   h->P.step = h->step;
   h->raw.step = h->step;
@@ -1219,6 +1226,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
       continue;
     }
     h->P.step = h->step;
+    h->P.seq = ++h->seq;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
     if (h->periodic) {
       // Scene::doOneStep prologue: cell->integrateAndUpdate(dt) (Scene.cpp:411)
@@ -1306,7 +1314,9 @@ int wdem_download_particles(wdem_handle* h, wdem_particles* p) {
   cudaStream_t s = h->stream;
   const int n = std::min(h->n, p->n);
   if (!h->forcesInArrays) {
-    launch_reduce_forces(s, h->P, h->d, h->n, h->buf[h->cur].c, h->csr);
+    StepParams P = h->P;
+    P.seq = h->seq + 1;  // the records of the last contact pass
+    launch_reduce_forces(s, P, h->d, h->n, h->buf[h->cur].c, h->csr);
   }
   std::vector<double4_32a> posr(n), velm(n), angw(n), ori(n), force(n), torque(n);
   if (n > 0) {
@@ -1621,7 +1631,9 @@ int ensureEdit(wdem_handle* h, long long m) {
 // host engines)
 void materialiseForces(wdem_handle* h) {
   if (!h->forcesInArrays) {
-    launch_reduce_forces(h->stream, h->P, h->d, h->n, h->buf[h->cur].c, h->csr);
+    StepParams P = h->P;
+    P.seq = h->seq + 1;  // the records of the last contact pass
+    launch_reduce_forces(h->stream, P, h->d, h->n, h->buf[h->cur].c, h->csr);
     h->forcesInArrays = true;
   }
 }

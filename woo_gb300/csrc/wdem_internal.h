@@ -20,8 +20,10 @@
 //     hist    double x 14 SoA: trsf col0 (3), trsf col1 (3), contPt (3), force (3, local), kn, kt
 //             (+4 for HertzPhys: kn0, kt0, alpha_sqrtMK, adhesion force)
 //     tanPhi  double
-//     out     3 double4_32a records per contact (one 32-byte sector each): global force on pA, torque on
-//             pA, torque on pB (x, y, z, unused); the integrator's gather reads two whole sectors per entry
+//     slot    int2     the contact's two entries in the CSR (pA's, pB's)
+//     out     2 double4_32a records per CSR entry (one 32-byte sector each), written by the contact pass at
+//             the entry's position: (force on the entry's particle, pass stamp), (torque, unused); a particle's
+//             records are contiguous, so the integrator's gather reads its CSR row as one run
 //   CSR over particles: rowptr[N+1], entries[2C] = contact index | (isB << 31), rows sorted
 //   by the partner's id key so that sums run in the order of the sorted contact keys.
 #pragma once
@@ -71,7 +73,9 @@ enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, 
        HIST_E0, HIST_E1, HIST_E2, HIST_E3,   // HertzPhys constants: kn0, kt0, alpha_sqrtMK, DMT adhesion force
        HIST_COUNT };
 enum { HIST_FRICT = HIST_E0 };  // FrictPhys contacts carry the first 14 history arrays
-enum { OUT_F = 0, OUT_TA = 1, OUT_TB = 2, OUT_RECORDS = 3 };  // records of one contact in Contacts.out
+// records of one CSR entry in Contacts.out: the force with the stamp of the contact pass that wrote it in w
+// (its StepParams.seq; a record whose stamp is not the previous pass's is stale and skipped), the torque
+enum { OUT_F = 0, OUT_T = 1, OUT_RECORDS = 2 };
 enum { MAX_MATERIALS = 1024 };  // 1024 x 56 B fits the 64 KB constant bank
 
 struct DevMaterial {
@@ -86,6 +90,7 @@ enum { MCLS_PZERO = 0, MCLS_NZERO = 1, MCLS_ONE = 2, MCLS_GEN = 3 };
 struct StepParams {
   double dt;
   long long step;
+  long long seq;            // number of this step's contact pass (never reset); stamps the pass's force records
   double gravity[3];
   int hasGravity;
   double distFactor;        // DemField.distFactor
@@ -171,7 +176,8 @@ struct Contacts {
   int* step0;
   double* hist[HIST_COUNT];
   double* tanPhi;
-  double4_32a* out;  // OUT_RECORDS records per contact: out[OUT_RECORDS * i + OUT_F / OUT_TA / OUT_TB]
+  int2* slot;        // CSR entries of the contact: (pA's, pB's)
+  double4_32a* out;  // OUT_RECORDS records per CSR entry e: out[OUT_RECORDS * e + OUT_F / OUT_T] (capacity 2C entries)
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
   int4* cdist;      // periodic: Contact.cellDist (x, y, z, unused); null otherwise
