@@ -47,7 +47,12 @@ enum {
  * wdem_particles.facetVerts; radius holds Facet.halfThick.  Facets are fixed (all DOFs blocked, no
  * velocity), contact spheres through Cg2_Facet_Sphere_L6Geom and receive no contact force from the
  * contact loop (ContactLoop::applyForceUninodal skips shapes with more than one node). */
-enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2, WDEM_SHAPE_FACET = 3 };
+/* Capsule (src/dem/Capsule.hpp:8-35): a cylinder of length shaft along the node's local x axis with
+ * hemispherical caps; radius in wdem_particles.radius, the shaft in wdem_particles.shaft.  Capsules are
+ * aspherical (they take the ellipsoids' rotation state and their laws: FrictMat + IdealElPl) and contact
+ * spheres, walls and other capsules (Cg2_Sphere_Capsule_L6Geom, Cg2_Wall_Capsule_L6Geom,
+ * Cg2_Capsule_Capsule_L6Geom). */
+enum { WDEM_SHAPE_SPHERE = 0, WDEM_SHAPE_WALL = 1, WDEM_SHAPE_ELLIPSOID = 2, WDEM_SHAPE_FACET = 3, WDEM_SHAPE_CAPSULE = 4 };
 /* Cg2_Ellipsoid_Ellipsoid_L6Geom solver: brent=True (Ellipsoid.hpp:57-59) or Newton-Raphson on dS/dlambda = 0
  * (the reference's brent=False branch, which it leaves unimplemented, Ellipsoid.cpp:311-322) */
 enum { WDEM_ELL_BRENT = 0, WDEM_ELL_NEWTON = 1 };
@@ -175,6 +180,7 @@ typedef struct wdem_particles {
   int32_t* scene;         /* batched independent scenes: scene index of each particle (0..4095); particles of
                              different scenes never interact; NULL = one scene */
   double* facetVerts;     /* 9n: Facet node positions 0, 1, 2 (node 0 equal to pos); NULL when there are no facets */
+  double* shaft;          /* n: Capsule.shaft; NULL when there are no capsules */
 } wdem_particles;
 
 /* ---- contact state, SoA; n contacts ---------------------------------------------------------- */

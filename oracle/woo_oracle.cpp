@@ -304,6 +304,7 @@ struct Particle {
   Quat ori;
   V3 semiAxes;                        /* Ellipsoid.semiAxes */
   V3 fv1, fv2;                        /* Facet nodes 1 and 2 (node 0 is pos; radius holds halfThick) */
+  double shaft = NaN;                 /* Capsule.shaft (radius holds Capsule.radius) */
   V3 angMom = V3(NaN, NaN, NaN);      /* DemData.angMom (aspherical Leapfrog) */
   Aabb bound;
   std::map<int, std::shared_ptr<struct Contact>> contacts; /* Particle::contacts (Particle.hpp:36) */
@@ -625,6 +626,24 @@ static void updateAabb(Scene& S, Particle& p) {
     V3 c = S.periodic ? mvec(S.cell.unshearTrsf, p.pos) : p.pos;
     a.min = c - delta;
     a.max = c + delta;
+  } else if (p.shape == WDEM_SHAPE_CAPSULE) {
+    /* Bo1_Capsule_Aabb::go (Capsule.cpp:97-114) with Capsule::alignedBox (:67-73), aperiodic: the box of the
+     * four points pos +- dShaft +- radius (1,1,1), dShaft = ori (shaft/2, 0, 0); a new bound starts with
+     * maxRot = 0 (rotation-aware verlet) */
+    if (S.periodic) throw std::runtime_error("capsules in a periodic cell are not restated");
+    if (!a.has) a.maxRot = 0.;
+    const V3 dShaft = qrot(p.ori, V3(.5 * p.shaft, 0, 0));
+    a.min = V3(Inf, Inf, Inf);
+    a.max = V3(-Inf, -Inf, -Inf);
+    for (double sa : {-1., 1.})
+      for (double sb : {-1., 1.}) {
+        const double br = sb * p.radius;
+        const V3 q = (p.pos + sa * dShaft) + V3(br, br, br);
+        for (int k = 0; k < 3; k++) {
+          a.min[k] = std::min(a.min[k], q[k]);
+          a.max[k] = std::max(a.max[k], q[k]);
+        }
+      }
   } else if (p.shape == WDEM_SHAPE_FACET) {
     /* Bo1_Facet_Aabb::go (Facet.cpp:275-298), aperiodic: the nodes +- halfThick, coefficient-wise min/max */
     if (S.periodic) throw std::runtime_error("facets in a periodic cell are not restated");
@@ -659,6 +678,12 @@ static void updateAabb(Scene& S, Particle& p) {
     a.min = a.min - vd;
   }
 }
+/* Capsule::volume, Capsule::equivRadius (Capsule.cpp:25-31) */
+static double capsuleEquivRadius(const Particle& p) {
+  const double r = p.radius;
+  const double vol = (4 / 3.) * M_PI * (r * r * r) + M_PI * (r * r) * p.shaft;
+  return std::cbrt(vol * 3 / (4 * M_PI));
+}
 /* AabbCollider::setVerletDist (Collision.cpp:164-184) */
 static void setVerletDist(Scene& S) {
   if (S.verletDist >= 0) return;
@@ -668,6 +693,7 @@ static void setVerletDist(Scene& S) {
     double r = NaN;
     if (p.shape == WDEM_SHAPE_SPHERE) r = p.radius;
     else if (p.shape == WDEM_SHAPE_ELLIPSOID) r = std::cbrt(p.semiAxes.x * p.semiAxes.y * p.semiAxes.z);
+    else if (p.shape == WDEM_SHAPE_CAPSULE) r = capsuleEquivRadius(p);
     if (!std::isnan(r)) minR = std::min(r, minR);
   }
   if (!std::isinf(minR)) S.verletDist = std::abs(S.verletDist) * minR;
@@ -1192,6 +1218,237 @@ static bool cg2FacetSphere(Scene& S, Contact& C, Particle& F, Particle& Sp, cons
   return true;
 }
 
+/* ------------------------------------------------------------------ capsules */
+/* Cg2_Sphere_Capsule_L6Geom::go (Capsule.cpp:198-216): the closest point of the capsule's axis segment */
+static bool cg2SphereCapsule(Scene& S, Contact& C, Particle& Sp, Particle& Cap, const V3& shift2, bool force) {
+  const V3 spherePos = Sp.pos;
+  const V3 capPos = Cap.pos + shift2;
+  const double rSum = Sp.radius + Cap.radius;
+  const V3 half = qrot(Cap.ori, V3(Cap.shaft / 2., 0, 0));
+  const V3 A = capPos - half, B = capPos + half;
+  const V3 pt = closestSegmentPt(spherePos, A, B);
+  const double distSq = sqnorm(pt - spherePos);
+  if (!C.isReal() && distSq > pow2(rSum) && !force) return false;
+  const double dist = std::sqrt(distSq);
+  const V3 normal = (pt - spherePos) / dist;
+  const double uN = dist - rSum;
+  const V3 contPt = spherePos + normal * (Sp.radius + .5 * uN);
+  handleSpheresLikeContact(S, C, spherePos, Sp.vel, Sp.angVel, capPos, Cap.vel, Cap.angVel, normal, contPt, uN, Sp.radius, Cap.radius);
+  return true;
+}
+
+/* Cg2_Wall_Capsule_L6Geom::go (Capsule.cpp:116-164): the overlaps of the two end caps with the wall place
+ * the contact point (weighted by the overlaps) and give uN */
+static bool cg2WallCapsule(Scene& S, Contact& C, Particle& W, Particle& Cap, const V3& shift2, bool force) {
+  const V3 wallPos = W.pos;
+  const V3 capPos = Cap.pos + shift2;
+  const int ax = W.axis, sense = W.sense;
+  const V3 half = qrot(Cap.ori, V3(Cap.shaft / 2., 0, 0));
+  const V3 AB[2] = {capPos - half, capPos + half};
+  const double d0 = AB[0][ax] - wallPos[ax], d1 = AB[1][ax] - wallPos[ax];
+  if (!C.isReal() && (std::abs(d0) > Cap.radius && std::abs(d1) > Cap.radius) && !force) return false;
+  const double cDist = capPos[ax] - wallPos[ax];
+  V3 normal(0, 0, 0);
+  if (sense == 0) normal[ax] = C.geom ? C.trsf.c[0][ax] : (cDist > 0 ? 1. : -1.);
+  else normal[ax] = (sense == 1 ? 1. : -1);
+  const double u0 = d0 * normal[ax] - Cap.radius, u1 = d1 * normal[ax] - Cap.radius;
+  V3 contPt;
+  double uN;
+  if (u0 * u1 < 0) {
+    /* the ends on opposite sides: the overlapping one takes all */
+    const int q = (u0 < 0 ? 0 : 1);
+    contPt = AB[q];
+    uN = q == 0 ? u0 : u1;
+  } else if (u0 + u1 != 0.) {
+    const double sum = u0 + u1;
+    double w0 = u0 / sum, w1 = u1 / sum;
+    if (u0 > 0) std::swap(w0, w1);  /* no overlap: the end closer to the wall weighs more */
+    contPt = w0 * AB[0] + w1 * AB[1];
+    uN = w0 * u0 + w1 * u1;
+  } else {
+    contPt = .5 * (AB[0] + AB[1]);
+    uN = 0.;
+  }
+  contPt[ax] = wallPos[ax];
+  handleSpheresLikeContact(S, C, wallPos, W.vel, W.angVel, capPos, Cap.vel, Cap.angVel, normal, contPt, uN, -Cap.radius, Cap.radius);
+  return true;
+}
+
+/* CompUtils::distSq_SegmentSegment (CompUtils.cpp:260-592): squared distance of two segments given by centre,
+ * unit direction and half-length, with the parameters (s0, s1) of the closest points -- D. Eberly's method
+ * ("Distance Between Two Line Segments in 3D", Geometric Tools) as the reference has it: the minimum of the
+ * quadratic in (s0, s1) is classified into the nine regions of the parameter rectangle; on a side one
+ * parameter sits at its bound and the other is minimised and clamped, a corner tries one side and, when the
+ * clamp ends on the far bound, the other; nearly parallel segments (|1 - (d0.d1)^2| < 1e-8) take the
+ * symmetric average of the two one-sided solutions.  Every region keeps the reference's order of
+ * comparisons and of the additions in the distance formulas. */
+struct SegSeg {
+  double a01, b0, b1, c, e0, e1;
+  /* s1 = f, s0 = the clamped minimiser t = -(a01 f + b0); lowFirst: tested as t < -e0, t <= e0, else;
+   * otherwise as t > e0, t >= -e0, else.  far: the last branch was taken. */
+  double withS1(double f, bool lowFirst, double& s0, double& s1, bool& far) const {
+    s1 = f;
+    const double t = -(a01 * s1 + b0);
+    bool inner = false;
+    far = false;
+    if (lowFirst) {
+      if (t < -e0) s0 = -e0;
+      else if (t <= e0) { s0 = t; inner = true; }
+      else { s0 = e0; far = true; }
+    } else {
+      if (t > e0) s0 = e0;
+      else if (t >= -e0) { s0 = t; inner = true; }
+      else { s0 = -e0; far = true; }
+    }
+    const double x = inner ? -s0 * s0 : s0 * (s0 - 2. * t);
+    return x + s1 * (s1 + 2. * b1) + c;
+  }
+  /* s0 = f, s1 = the clamped minimiser t = -(a01 f + b1) */
+  double withS0(double f, bool lowFirst, double& s0, double& s1) const {
+    s0 = f;
+    const double t = -(a01 * s0 + b1);
+    bool inner = false;
+    if (lowFirst) {
+      if (t < -e1) s1 = -e1;
+      else if (t <= e1) { s1 = t; inner = true; }
+      else s1 = e1;
+    } else {
+      if (t > e1) s1 = e1;
+      else if (t >= -e1) { s1 = t; inner = true; }
+      else s1 = -e1;
+    }
+    const double x = inner ? -s1 * s1 : s1 * (s1 - 2. * t);
+    return x + s0 * (s0 + 2. * b0) + c;
+  }
+};
+static double distSqSegSeg(const V3& c0, const V3& d0, double e0, const V3& c1, const V3& d1, double e1, double& s0, double& s1) {
+  const V3 diff = c0 - c1;
+  SegSeg g;
+  g.a01 = -dot(d0, d1);
+  g.b0 = dot(diff, d0);
+  g.b1 = -dot(diff, d1);
+  g.c = sqnorm(diff);
+  g.e0 = e0;
+  g.e1 = e1;
+  const double a01 = g.a01, b0 = g.b0, b1 = g.b1, c = g.c;
+  const double det = std::abs(1. - a01 * a01);
+  double d;
+  bool far;
+  if (det >= 1e-8) {
+    s0 = a01 * b1 - b0;
+    s1 = a01 * b0 - b1;
+    const double ed0 = e0 * det, ed1 = e1 * det;
+    if (s0 >= -ed0) {
+      if (s0 <= ed0) {
+        if (s1 >= -ed1) {
+          if (s1 <= ed1) {                                    /* interior */
+            const double inv = 1. / det;
+            s0 *= inv;
+            s1 *= inv;
+            d = s0 * (s0 + a01 * s1 + 2. * b0) + s1 * (a01 * s0 + s1 + 2. * b1) + c;
+          } else d = g.withS1(e1, true, s0, s1, far);        /* side s1 = e1 */
+        } else d = g.withS1(-e1, true, s0, s1, far);         /* side s1 = -e1 */
+      } else {
+        if (s1 >= -ed1) {
+          if (s1 <= ed1) d = g.withS0(e0, true, s0, s1);     /* side s0 = e0 */
+          else {                                             /* corner (e0, e1) */
+            d = g.withS1(e1, true, s0, s1, far);
+            if (far) d = g.withS0(e0, true, s0, s1);
+          }
+        } else {                                             /* corner (e0, -e1) */
+          d = g.withS1(-e1, true, s0, s1, far);
+          if (far) d = g.withS0(e0, false, s0, s1);
+        }
+      }
+    } else {
+      if (s1 >= -ed1) {
+        if (s1 <= ed1) d = g.withS0(-e0, true, s0, s1);      /* side s0 = -e0 */
+        else {                                               /* corner (-e0, e1) */
+          d = g.withS1(e1, false, s0, s1, far);
+          if (far) d = g.withS0(-e0, true, s0, s1);
+        }
+      } else {                                               /* corner (-e0, -e1) */
+        d = g.withS1(-e1, false, s0, s1, far);
+        if (far) d = g.withS0(-e0, true, s0, s1);
+      }
+    }
+  } else {
+    /* parallel: the averaged b0 makes the distance symmetric in the two segments */
+    const double e0pe1 = e0 + e1;
+    const double sign = (a01 > 0. ? -1. : 1.);
+    const double b0Avr = .5 * (b0 - sign * b1);
+    double lambda = -b0Avr;
+    if (lambda < -e0pe1) lambda = -e0pe1;
+    else if (lambda > e0pe1) lambda = e0pe1;
+    s1 = -sign * lambda * e1 / e0pe1;
+    s0 = lambda + sign * s1;
+    d = lambda * (lambda + 2. * b0Avr) + c;
+  }
+  if (d < 0.) d = 0.;
+  return d;
+}
+
+/* Cg2_Capsule_Capsule_L6Geom::go (Capsule.cpp:223-323): uN and the normal from the closest points of the two
+ * axis segments; the contact point from the closest points unless two or more end caps overlap the other
+ * capsule's axis, in which case the overlapping ends' points (each moved towards its capsule's end by the
+ * other's radius share) are averaged with weights rSum - distance */
+static bool cg2CapsuleCapsule(Scene& S, Contact& C, Particle& P1, Particle& P2, const V3& shift2, bool force) {
+  const V3 pos1 = P1.pos, pos2 = P2.pos + shift2;
+  const V3 dir1 = qrot(P1.ori, V3(1, 0, 0)), dir2 = qrot(P2.ori, V3(1, 0, 0));
+  const double rSum = P1.radius + P2.radius;
+  double u, v;
+  const double distSq = distSqSegSeg(pos1, dir1, .5 * P1.shaft, pos2, dir2, .5 * P2.shaft, u, v);
+  if (!C.isReal() && distSq > pow2(rSum) && !force) return false;
+  const V3 close0 = pos1 + dir1 * u, close1 = pos2 + dir2 * v;
+  const V3 ends[2][2] = {{pos1 - .5 * P1.shaft * dir1, pos1 + .5 * P1.shaft * dir1},
+                         {pos2 - .5 * P2.shaft * dir2, pos2 + .5 * P2.shaft * dir2}};
+  const double dist = std::sqrt(distSq);
+  const double uN = dist - (P1.radius + P2.radius);
+  const V3 normal = (close1 - close0) / dist;
+  int bits = 0, nOver = 0;
+  V3 eClose[2][2];
+  double eDistSq[2][2];
+  for (int a = 0; a < 2; a++) {
+    const int b = 1 - a;
+    for (int e = 0; e < 2; e++) {
+      eClose[a][e] = closestSegmentPt(ends[a][e], ends[b][0], ends[b][1]);
+      eDistSq[a][e] = sqnorm(eClose[a][e] - ends[a][e]);
+      if (eDistSq[a][e] < pow2(rSum)) { bits |= 1 << (2 * a + e); nOver++; }
+    }
+  }
+  const double r1r = P1.radius / rSum, r2r = P2.radius / rSum;
+  /* the overlapping end moved from its closest point on the other axis towards itself by the other's share */
+  auto endPoint = [&](int a, int e) { return eClose[a][e] + (ends[a][e] - eClose[a][e]) * (a == 0 ? r2r : r1r); };
+  auto endWeight = [&](int a, int e) { return rSum - std::sqrt(eDistSq[a][e]); };
+  V3 contPt;
+  if (nOver < 2) contPt = close0 + (P1.radius + 0.5 * uN) * normal;
+  else if (nOver == 4) {
+    V3 pp(0, 0, 0);
+    double ww = 0.;
+    for (int a = 0; a < 2; a++)
+      for (int e = 0; e < 2; e++) {
+        const double w = endWeight(a, e);
+        pp = pp + w * endPoint(a, e);
+        ww += w;
+      }
+    contPt = pp / ww;
+  } else {
+    /* two or three overlapping ends (bit 2a+e for end e of capsule a): the two that place the contact; with
+     * three, the two ends of the capsule whose both ends overlap (the reference's lookup table) */
+    static const int pick[16][2][2] = {
+        {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{0, 0}, {0, 0}}, {{0, 0}, {0, 1}},
+        {{0, 0}, {0, 0}}, {{0, 0}, {1, 0}}, {{0, 1}, {1, 0}}, {{0, 0}, {0, 1}},
+        {{0, 0}, {0, 0}}, {{0, 0}, {1, 1}}, {{0, 1}, {1, 1}}, {{0, 0}, {0, 1}},
+        {{1, 0}, {1, 1}}, {{1, 0}, {1, 1}}, {{1, 0}, {1, 1}}, {{0, 0}, {0, 0}}};
+    const int (&ix)[2][2] = pick[bits];
+    const V3 p0 = endPoint(ix[0][0], ix[0][1]), p1 = endPoint(ix[1][0], ix[1][1]);
+    const double w0 = endWeight(ix[0][0], ix[0][1]), w1 = endWeight(ix[1][0], ix[1][1]);
+    contPt = (w0 * p0 + w1 * p1) / (w0 + w1);
+  }
+  handleSpheresLikeContact(S, C, pos1, P1.vel, P1.angVel, pos2, P2.vel, P2.angVel, normal, contPt, uN, P1.radius, P2.radius);
+  return true;
+}
+
 /* ------------------------------------------------------------------ ellipsoids */
 /* Brent's minimisation without derivatives (R. P. Brent, "Algorithms for Minimization without
  * Derivatives", 1973, ch. 5) as boost::math::tools::brent_find_minima performs it (Boost.Math,
@@ -1539,9 +1796,14 @@ static bool freshContactSetup(Scene& S, Contact& C) {
   const bool swap = (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) ||
                     (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
                     (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL) ||
-                    (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET);
+                    (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET) ||
+                    (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_SPHERE) ||
+                    (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_WALL);
   const bool known = swap || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_SPHERE) ||
                      (sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) ||
+                     (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_CAPSULE) ||
+                     (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_CAPSULE) ||
+                     (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_CAPSULE) ||
                      (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_SPHERE) ||
                      (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_ELLIPSOID) ||
                      (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_ELLIPSOID) ||
@@ -1556,6 +1818,10 @@ static bool freshContactSetup(Scene& S, Contact& C) {
     C.minDist00Sq = pow2(maxCoeff(A.semiAxes) + maxCoeff(B.semiAxes));            /* Ellipsoid.cpp:265 */
   else if (A.shape == WDEM_SHAPE_SPHERE && B.shape == WDEM_SHAPE_ELLIPSOID)
     C.minDist00Sq = pow2(A.radius + maxCoeff(B.semiAxes));                        /* Ellipsoid.cpp:259 */
+  else if (A.shape == WDEM_SHAPE_SPHERE && B.shape == WDEM_SHAPE_CAPSULE)
+    C.minDist00Sq = pow2(A.radius + B.radius + .5 * B.shaft);                     /* Capsule.cpp:193-196 */
+  else if (A.shape == WDEM_SHAPE_CAPSULE && B.shape == WDEM_SHAPE_CAPSULE)
+    C.minDist00Sq = pow2(A.radius + .5 * A.shaft + B.radius + .5 * B.shaft);      /* Capsule.cpp:218-221 */
   else C.minDist00Sq = -1;
   return true;
 }
@@ -1569,6 +1835,9 @@ static bool callGeom(Scene& S, Contact& C, Particle& pA, Particle& pB, const V3&
     return cg2EllipsoidOrSphere(S, C, pA, V3(pA.radius, pA.radius, pA.radius), pB, pB.semiAxes, shift2, false);
   if (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_ELLIPSOID) return cg2WallEllipsoid(S, C, pA, pB, shift2, false);
   if (sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) return cg2FacetSphere(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_CAPSULE) return cg2SphereCapsule(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_WALL && sb == WDEM_SHAPE_CAPSULE) return cg2WallCapsule(S, C, pA, pB, shift2, false);
+  if (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_CAPSULE) return cg2CapsuleCapsule(S, C, pA, pB, shift2, false);
   return false;
 }
 
@@ -1927,6 +2196,7 @@ static double pWaveDt(const Scene& S) {
     double radius;
     if (p.shape == WDEM_SHAPE_SPHERE) radius = p.radius;
     else if (p.shape == WDEM_SHAPE_ELLIPSOID) radius = minCoeff(p.semiAxes);
+    else if (p.shape == WDEM_SHAPE_CAPSULE) radius = p.radius;
     else continue;
     const wdem_material& m = S.mats[p.mat];
     dt = std::min(dt, radius / (1. * std::sqrt(m.young / m.density)));
@@ -2207,6 +2477,12 @@ int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
     q.torque = V3(p->torque[3 * i], p->torque[3 * i + 1], p->torque[3 * i + 2]);
     if (p->semiAxes) q.semiAxes = V3(p->semiAxes[3 * i], p->semiAxes[3 * i + 1], p->semiAxes[3 * i + 2]);
     if (p->angMom) q.angMom = V3(p->angMom[3 * i], p->angMom[3 * i + 1], p->angMom[3 * i + 2]);
+    if (q.shape == WDEM_SHAPE_CAPSULE) {
+      if (!p->shaft) { S.err = "capsules need wdem_particles.shaft"; return WDEM_ERR_ARG; }
+      q.shaft = p->shaft[i];
+      /* Capsule::selfTest (Capsule.cpp:19-23) */
+      if (!(q.radius > 0.) || !(q.shaft >= 0.)) { S.err = "Capsule: radius must be positive and shaft non-negative"; return WDEM_ERR_ARG; }
+    }
     if (q.shape == WDEM_SHAPE_FACET) {
       if (!p->facetVerts) { S.err = "facets need wdem_particles.facetVerts"; return WDEM_ERR_ARG; }
       q.fv1 = V3(p->facetVerts[9 * i + 3], p->facetVerts[9 * i + 4], p->facetVerts[9 * i + 5]);
@@ -2222,7 +2498,7 @@ int orc_upload_particles(orc_handle* h, const wdem_particles* p) {
   S.dirty = true;
   S.verletDist = S.P.verletDist;
   S.anyEll = false;
-  for (const Particle& q : S.par) if (q.shape == WDEM_SHAPE_ELLIPSOID) S.anyEll = true;
+  for (const Particle& q : S.par) if (q.shape == WDEM_SHAPE_ELLIPSOID || q.shape == WDEM_SHAPE_CAPSULE) S.anyEll = true;
   return 0;
 }
 

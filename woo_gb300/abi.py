@@ -25,7 +25,7 @@ WDEM_ERR_TOO_BIG = -7
 WDEM_ERR_TIMEOUT = -8
 WDEM_ERR_STATE = -9
 
-SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID, SHAPE_FACET = 0, 1, 2, 3
+SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID, SHAPE_FACET, SHAPE_CAPSULE = 0, 1, 2, 3, 4
 ELL_BRENT, ELL_NEWTON = 0, 1
 WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
 WARM_COLD, WARM_MLP, WARM_HISTORY, WARM_HISTORY_MLP = 0, 1, 2, 3
@@ -79,7 +79,7 @@ class Particles(C.Structure):
     _fields_ = [("n", C.c_int32), ("_pad", C.c_int32), ("shape", I32), ("radius", D), ("wallAxis", I32),
                 ("wallSense", I32), ("material", I32), ("mask", U32), ("flags", U32), ("mass", D),
                 ("inertia", D), ("pos", D), ("ori", D), ("vel", D), ("angVel", D), ("force", D), ("torque", D),
-                ("semiAxes", D), ("angMom", D), ("scene", I32), ("facetVerts", D)]
+                ("semiAxes", D), ("angMom", D), ("scene", I32), ("facetVerts", D), ("shaft", D)]
 
 
 class Contacts(C.Structure):
@@ -154,6 +154,7 @@ class ParticleArrays:
         self.angMom = np.full((n, 3), np.nan)
         self.scene = np.zeros(n, np.int32)
         self.facetVerts = np.full((n, 9), np.nan)
+        self.shaft = np.full(n, np.nan)
 
     def copy(self):
         o = ParticleArrays(self.n)
@@ -185,6 +186,7 @@ class ParticleArrays:
         s.semiAxes = ptr(self.semiAxes, C.c_double); s.angMom = ptr(self.angMom, C.c_double)
         s.scene = ptr(self.scene, C.c_int32)
         s.facetVerts = ptr(self.facetVerts, C.c_double)
+        s.shaft = ptr(self.shaft, C.c_double)
         return s
 
 

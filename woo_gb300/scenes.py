@@ -297,6 +297,92 @@ def periodic_cloud(n, seed, size=(0.1, 0.1, 0.1), rmin=0.004, rmax=0.006, law="f
     return SceneSpec(p, mats, pa, f"peri{n}", dict(seed=seed, dt=dt), cell=cell)
 
 
+def capsule_mass_inertia(radius, shaft, density):
+    """Capsule::lumpMassInertia (src/dem/Capsule.cpp:44-57): mass and the principal inertia (Ix along the
+    axis, Iy = Iz) of a cylinder of length shaft with hemispherical caps, in the node's frame."""
+    r = np.asarray(radius, np.float64)
+    s = np.asarray(shaft, np.float64)
+    rho = np.asarray(density, np.float64)
+    r2, r3 = r * r, r * r * r
+    mCaps = (4 / 3.0) * math.pi * r3 * rho
+    mShaft = math.pi * r2 * s * rho
+    distCap = .5 * s + (3 / 8.0) * r
+    Ix = 2 * mCaps * r2 / 5.0 + .5 * mShaft * r2
+    Iy = (83 / 320.0) * mCaps * r2 + mCaps * (distCap * distCap) + (1 / 12.0) * mShaft * (3 * r2 + s * s)
+    m = mCaps + mShaft
+    return m, np.stack([Ix, Iy, Iy], axis=-1)
+
+
+def add_capsules(pa, centers, radii, shafts, oris, mat, mats_py, vel=None, mask=None):
+    """ParticleArrays with capsules appended after the particles of pa (woo.utils.capsule, py/utils.py:213-221):
+    DemField.defaultMovableMask, mass and inertia from Capsule::lumpMassInertia."""
+    centers = np.asarray(centers, np.float64).reshape(-1, 3)
+    n0, nc = pa.n, len(centers)
+    out = abi.ParticleArrays(n0 + nc)
+    for k, v in pa.__dict__.items():
+        if isinstance(v, np.ndarray):
+            getattr(out, k)[:n0] = v
+    c = slice(n0, n0 + nc)
+    out.shape[c] = abi.SHAPE_CAPSULE
+    out.pos[c] = centers
+    out.radius[c] = radii
+    out.shaft[c] = shafts
+    out.ori[c] = oris
+    cm = np.broadcast_to(np.asarray(mat, np.int32), (nc,))
+    out.material[c] = cm
+    out.mask[c] = DEFAULT_MOVABLE_MASK if mask is None else mask
+    dens = np.array([mats_py[k].get("density", 1000.0) for k in range(len(mats_py))])[cm]
+    m, inert = capsule_mass_inertia(np.broadcast_to(radii, (nc,)), np.broadcast_to(shafts, (nc,)), dens)
+    out.mass[c] = m
+    out.inertia[c] = inert
+    if vel is not None:
+        out.vel[c] = vel
+    return out
+
+
+def capsule_cloud(n_caps, n_spheres, seed, box=(0.12, 0.12, 0.12), rmin=0.003, rmax=0.005, smin=0.0, smax=0.012,
+                  dense=0.85, vel_scale=0.3, gravity=(0, 0, -9.81), damping=0.2, walls=True, **kw):
+    """Capsules (radius ~ U[rmin, rmax], shaft ~ U[smin, smax], random orientations) and spheres in a walled
+    box, FrictMat + IdealElPl: sphere-capsule, capsule-capsule and wall-capsule contacts.  Positions come
+    from a sphere packing of the capsules' bounding radii, squeezed by `dense` (<1 creates overlaps)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.zeros(3), np.asarray(box, np.float64)
+    rc = rng.uniform(rmin, rmax, n_caps)
+    sc = rng.uniform(smin, smax, n_caps)
+    rs = rng.uniform(rmin, rmax, n_spheres)
+    rin = np.concatenate([rc + .5 * sc, rs])
+    centers, radii = make_cloud_radii(lo, hi, rin, seed)
+    if dense != 1.0:
+        mid = hi / 2
+        centers = mid + (centers - mid) * dense
+    # the packer returns the radii it placed (reordered, some dropped): find each one's source
+    where = {}
+    for j, v in enumerate(rin):
+        where.setdefault(float(v), []).append(j)
+    src = np.array([where[float(v)].pop(0) for v in radii], int)
+    isCap = src < n_caps
+    capIdx = src[isCap]
+    mats_py = [dict(kind=abi.MAT_FRICT, density=2500.0, young=1e7, ktDivKn=0.2, tanPhi=0.5),
+               dict(kind=abi.MAT_FRICT, density=2000.0, young=3e7, ktDivKn=0.3, tanPhi=0.3)]
+    mats = materials_array(mats_py)
+    sph = ~isCap
+    ns = int(sph.sum())
+    mat_s = rng.integers(0, 2, ns).astype(np.int32)
+    pa = assemble(centers[sph], radii[sph], mat_s, box_walls(lo, hi) if walls else [], mats_py,
+                  vel=rng.normal(0, vel_scale, (ns, 3)))
+    ci = capIdx
+    ncap = len(ci)
+    pa = add_capsules(pa, centers[isCap], rc[ci], sc[ci], random_quaternions(ncap, rng), rng.integers(0, 2, ncap),
+                      mats_py, vel=rng.normal(0, vel_scale, (ncap, 3)))
+    nw = 6 if walls else 0
+    pa.angVel[nw:] = rng.normal(0, 5.0, (pa.n - nw, 3))
+    g = np.asarray(gravity, np.float64)
+    pa.force[nw:] = pa.mass[nw:, None] * g[None, :]
+    dt = 0.3 * pwave_dt(np.concatenate([radii[sph], rc[ci]]), np.concatenate([mat_s, np.zeros(ncap, int)]), mats_py)
+    p = default_params(mats, dt=dt, gravity=gravity, damping=damping, **kw)
+    return SceneSpec(p, mats, pa, f"capsules{ncap}", dict(seed=seed, dt=dt, n_capsules=ncap, n_spheres=ns))
+
+
 def add_facets(pa, triangles, halfThick=0.0, mat=0):
     """ParticleArrays with fixed facets appended after the particles of pa: Facet.make defaults
     (py/utils.py:315-341) -- DemField.defaultBoundaryMask, all DOFs blocked, node masses and inertia 0;
