@@ -68,6 +68,24 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
     const double hz = sqrt(c0.z * c0.z + c1.z * c1.z + c2.z * c2.z);
     mn = make_double4_32a(pr.x - hx, pr.y - hy, pr.z - hz, 0);
     mx = make_double4_32a(pr.x + hx, pr.y + hy, pr.z + hz, 0);
+  } else if (sh == WDEM_SHAPE_CAPSULE) {
+    // Bo1_Capsule_Aabb::go (Capsule.cpp:97-114) with Capsule::alignedBox (:67-73): the box of the four points
+    // pos +- dShaft +- radius (1,1,1), dShaft = ori (shaft/2, 0, 0), min/max as Eigen's AlignedBox::extend
+    const double4_32a cs = p.semi[i], o4 = p.ori[i];
+    qd q;
+    q.w = o4.x; q.x = o4.y; q.y = o4.z; q.z = o4.w;
+    const d3 ds = qrot(q, mk(.5 * cs.y, 0, 0));
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    mn = make_double4_32a(inf, inf, inf, 0);
+    mx = make_double4_32a(-inf, -inf, -inf, 0);
+    for (int sa = -1; sa <= 1; sa += 2)
+      for (int sb = -1; sb <= 1; sb += 2) {
+        const double br = (double)sb * cs.x;
+        const d3 e = mk(pr.x, pr.y, pr.z) + (double)sa * ds;
+        const double x = e.x + br, y = e.y + br, z = e.z + br;
+        mn.x = (x < mn.x) ? x : mn.x; mn.y = (y < mn.y) ? y : mn.y; mn.z = (z < mn.z) ? z : mn.z;
+        mx.x = (mx.x < x) ? x : mx.x; mx.y = (mx.y < y) ? y : mx.y; mx.z = (mx.z < z) ? z : mx.z;
+      }
   } else if (sh == WDEM_SHAPE_FACET) {
     // Bo1_Facet_Aabb::go (Facet.cpp:275-298), aperiodic: the three nodes +- halfThick (posr.w), coefficient-wise
     // min/max in the order of Eigen's array().min()/max() (std::min/std::max semantics)
@@ -93,7 +111,7 @@ __global__ void k_bboxes(StepParams P, Particles p, int n) {
     // Aabb.maxRot: -1 (ignored) for spheres and walls; ellipsoids start at 0 and get
     // atan(verletDist / largest half-extent) when verletDist > 0 (Collision.cpp:152-158)
     double mr = -1.;
-    if (sh == WDEM_SHAPE_ELLIPSOID) {
+    if (sh == WDEM_SHAPE_ELLIPSOID || sh == WDEM_SHAPE_CAPSULE) {
       mr = 0.;
       if (P.verletDist > 0) {
         const double arm = .5 * dmax3(mk(mx.x - mn.x, mx.y - mn.y, mx.z - mn.z));

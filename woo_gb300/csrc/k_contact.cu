@@ -292,6 +292,252 @@ __device__ __forceinline__ void facetPointVel(const Particles& p, int a, d3 n0, 
   angVel = cross(n0 - x, v0) + cross(n1 - x, z) + cross(n2 - x, z);
 }
 
+// ------------------------------------------------------------------------------------ capsules
+// Capsules keep (radius, shaft, 0) in Particles.semi and their bounding radius radius + shaft/2 in posr.w.
+__device__ __forceinline__ qd oriOf(const Particles& p, int i) {
+  const double4_32a o = p.ori[i];
+  qd q;
+  q.w = o.x; q.x = o.y; q.y = o.z; q.z = o.w;
+  return q;
+}
+
+// Cg2_Sphere_Capsule_L6Geom::go (Capsule.cpp:198-216); pA is the sphere, pB the capsule
+__device__ __noinline__ bool sphereCapsuleGeometry(const Particles& p, int a, int b, bool real, d3 spherePos, d3 capPos,
+                                                   d3& normal, d3& contPt, double& uN, double& r1, double& r2) {
+  const double rs = p.posr[a].w;
+  const double4_32a cs = p.semi[b];
+  const double rc = cs.x;
+  const double rSum = rs + rc;
+  const d3 half = qrot(oriOf(p, b), mk(cs.y / 2., 0, 0));
+  const d3 pt = closestSegmentPt(spherePos, capPos - half, capPos + half);
+  const double distSq = sqnorm(pt - spherePos);
+  if (!real && distSq > rSum * rSum) return false;
+  const double dist = sqrt(distSq);
+  normal = (pt - spherePos) / dist;
+  uN = dist - rSum;
+  contPt = spherePos + normal * (rs + .5 * uN);
+  r1 = rs;
+  r2 = rc;
+  return true;
+}
+
+// Cg2_Wall_Capsule_L6Geom::go (Capsule.cpp:116-164); pA is the wall.  The overlaps of the two end caps with
+// the wall weight the contact point and give uN.
+__device__ __noinline__ bool wallCapsuleGeometry(const Particles& p, const Contacts& c, long long i, int a, int b,
+                                                 bool real, d3 wallPos, d3 capPos, d3& normal, d3& contPt,
+                                                 double& uN, double& r1, double& r2) {
+  const int wa = p.meta[a].x;
+  const int ax = (wa >> 4) & 3, sense = ((wa >> 8) & 3) - 1;
+  const double4_32a cs = p.semi[b];
+  const double rc = cs.x;
+  const d3 half = qrot(oriOf(p, b), mk(cs.y / 2., 0, 0));
+  const d3 A = capPos - half, B = capPos + half;
+  const double wp = comp(wallPos, ax);
+  const double d0 = comp(A, ax) - wp, d1 = comp(B, ax) - wp;
+  if (!real && (fabs(d0) > rc && fabs(d1) > rc)) return false;
+  const double cDist = comp(capPos, ax) - wp;
+  double nax;
+  if (sense == 0) nax = real ? comp(mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]), ax) : (cDist > 0 ? 1. : -1.);
+  else nax = (sense == 1 ? 1. : -1);
+  normal = mk(0, 0, 0);
+  setComp(normal, ax, nax);
+  const double u0 = d0 * nax - rc, u1 = d1 * nax - rc;
+  if (u0 * u1 < 0) {
+    // the ends on opposite sides of the wall: the overlapping one takes all
+    contPt = u0 < 0 ? A : B;
+    uN = u0 < 0 ? u0 : u1;
+  } else if (u0 + u1 != 0.) {
+    const double sum = u0 + u1;
+    double w0 = u0 / sum, w1 = u1 / sum;
+    if (u0 > 0) { const double t = w0; w0 = w1; w1 = t; }  // no overlap: the end closer to the wall weighs more
+    contPt = w0 * A + w1 * B;
+    uN = w0 * u0 + w1 * u1;
+  } else {
+    contPt = .5 * (A + B);
+    uN = 0.;
+  }
+  setComp(contPt, ax, wp);
+  r1 = -rc;
+  r2 = rc;
+  return true;
+}
+
+// CompUtils::distSq_SegmentSegment (CompUtils.cpp:260-592): D. Eberly's segment distance ("Distance Between
+// Two Line Segments in 3D", Geometric Tools) as the reference has it -- the minimum of the quadratic in the
+// segment parameters (s0, s1) classified into the nine regions of the parameter rectangle; on a side one
+// parameter sits at its bound and the other is minimised and clamped, a corner tries one side and, when the
+// clamp ends on the far bound, the other; nearly parallel segments take the symmetric average.  The
+// comparisons and the additions of the distance formulas keep the reference's order in every region.
+struct SegSeg {
+  double a01, b0, b1, c, e0, e1;
+  // s1 = f, s0 the clamped minimiser t = -(a01 f + b0); lowFirst: tested t < -e0, t <= e0, else, otherwise
+  // t > e0, t >= -e0, else; far: the last branch was taken
+  __device__ __forceinline__ double withS1(double f, bool lowFirst, double& s0, double& s1, bool& far) const {
+    s1 = f;
+    const double t = -(a01 * s1 + b0);
+    bool inner = false;
+    far = false;
+    if (lowFirst) {
+      if (t < -e0) s0 = -e0;
+      else if (t <= e0) { s0 = t; inner = true; }
+      else { s0 = e0; far = true; }
+    } else {
+      if (t > e0) s0 = e0;
+      else if (t >= -e0) { s0 = t; inner = true; }
+      else { s0 = -e0; far = true; }
+    }
+    const double x = inner ? -s0 * s0 : s0 * (s0 - 2. * t);
+    return x + s1 * (s1 + 2. * b1) + c;
+  }
+  // s0 = f, s1 the clamped minimiser t = -(a01 f + b1)
+  __device__ __forceinline__ double withS0(double f, bool lowFirst, double& s0, double& s1) const {
+    s0 = f;
+    const double t = -(a01 * s0 + b1);
+    bool inner = false;
+    if (lowFirst) {
+      if (t < -e1) s1 = -e1;
+      else if (t <= e1) { s1 = t; inner = true; }
+      else s1 = e1;
+    } else {
+      if (t > e1) s1 = e1;
+      else if (t >= -e1) { s1 = t; inner = true; }
+      else s1 = -e1;
+    }
+    const double x = inner ? -s1 * s1 : s1 * (s1 - 2. * t);
+    return x + s0 * (s0 + 2. * b0) + c;
+  }
+};
+__device__ __forceinline__ double distSqSegSeg(d3 c0, d3 d0, double e0, d3 c1, d3 d1, double e1, double& s0, double& s1) {
+  const d3 diff = c0 - c1;
+  SegSeg g;
+  g.a01 = -dot(d0, d1);
+  g.b0 = dot(diff, d0);
+  g.b1 = -dot(diff, d1);
+  g.c = sqnorm(diff);
+  g.e0 = e0;
+  g.e1 = e1;
+  const double a01 = g.a01, b0 = g.b0, b1 = g.b1, c = g.c;
+  const double det = fabs(1. - a01 * a01);
+  double d;
+  bool far;
+  if (det >= 1e-8) {
+    s0 = a01 * b1 - b0;
+    s1 = a01 * b0 - b1;
+    const double ed0 = e0 * det, ed1 = e1 * det;
+    if (s0 >= -ed0) {
+      if (s0 <= ed0) {
+        if (s1 >= -ed1) {
+          if (s1 <= ed1) {  // interior
+            const double inv = 1. / det;
+            s0 *= inv;
+            s1 *= inv;
+            d = s0 * (s0 + a01 * s1 + 2. * b0) + s1 * (a01 * s0 + s1 + 2. * b1) + c;
+          } else d = g.withS1(e1, true, s0, s1, far);
+        } else d = g.withS1(-e1, true, s0, s1, far);
+      } else {
+        if (s1 >= -ed1) {
+          if (s1 <= ed1) d = g.withS0(e0, true, s0, s1);
+          else {
+            d = g.withS1(e1, true, s0, s1, far);
+            if (far) d = g.withS0(e0, true, s0, s1);
+          }
+        } else {
+          d = g.withS1(-e1, true, s0, s1, far);
+          if (far) d = g.withS0(e0, false, s0, s1);
+        }
+      }
+    } else {
+      if (s1 >= -ed1) {
+        if (s1 <= ed1) d = g.withS0(-e0, true, s0, s1);
+        else {
+          d = g.withS1(e1, false, s0, s1, far);
+          if (far) d = g.withS0(-e0, true, s0, s1);
+        }
+      } else {
+        d = g.withS1(-e1, false, s0, s1, far);
+        if (far) d = g.withS0(-e0, true, s0, s1);
+      }
+    }
+  } else {
+    // parallel: the averaged b0 makes the distance symmetric in the two segments
+    const double e0pe1 = e0 + e1;
+    const double sign = (a01 > 0. ? -1. : 1.);
+    const double b0Avr = .5 * (b0 - sign * b1);
+    double lambda = -b0Avr;
+    if (lambda < -e0pe1) lambda = -e0pe1;
+    else if (lambda > e0pe1) lambda = e0pe1;
+    s1 = -sign * lambda * e1 / e0pe1;
+    s0 = lambda + sign * s1;
+    d = lambda * (lambda + 2. * b0Avr) + c;
+  }
+  if (d < 0.) d = 0.;
+  return d;
+}
+
+// Cg2_Capsule_Capsule_L6Geom::go (Capsule.cpp:223-323): uN and the normal from the closest points of the axis
+// segments; the contact point from those unless two or more end caps overlap the other capsule's axis, in
+// which case the overlapping ends' points (moved from their closest point on the other axis towards the end
+// by the other radius' share of rSum) are averaged with weights rSum - distance
+__device__ __noinline__ bool capsuleCapsuleGeometry(const Particles& p, int a, int b, bool real, d3 pos1, d3 pos2,
+                                                    d3& normal, d3& contPt, double& uN, double& r1, double& r2) {
+  const double4_32a c1 = p.semi[a], c2 = p.semi[b];
+  const d3 dir1 = qrot(oriOf(p, a), mk(1, 0, 0)), dir2 = qrot(oriOf(p, b), mk(1, 0, 0));
+  const double rSum = c1.x + c2.x;
+  double u, v;
+  const double distSq = distSqSegSeg(pos1, dir1, .5 * c1.y, pos2, dir2, .5 * c2.y, u, v);
+  if (!real && distSq > rSum * rSum) return false;
+  const d3 close0 = pos1 + dir1 * u, close1 = pos2 + dir2 * v;
+  const d3 h1 = .5 * c1.y * dir1, h2 = .5 * c2.y * dir2;
+  const d3 ends[2][2] = {{pos1 - h1, pos1 + h1}, {pos2 - h2, pos2 + h2}};
+  const double dist = sqrt(distSq);
+  uN = dist - (c1.x + c2.x);
+  normal = (close1 - close0) / dist;
+  int bits = 0, nOver = 0;
+  d3 eClose[2][2];
+  double eDistSq[2][2];
+  for (int s = 0; s < 2; s++) {
+    const int t = 1 - s;
+    for (int e = 0; e < 2; e++) {
+      eClose[s][e] = closestSegmentPt(ends[s][e], ends[t][0], ends[t][1]);
+      eDistSq[s][e] = sqnorm(eClose[s][e] - ends[s][e]);
+      if (eDistSq[s][e] < rSum * rSum) { bits |= 1 << (2 * s + e); nOver++; }
+    }
+  }
+  const double r1r = c1.x / rSum, r2r = c2.x / rSum;
+  if (nOver < 2) contPt = close0 + (c1.x + 0.5 * uN) * normal;
+  else if (nOver == 4) {
+    d3 pp = mk(0, 0, 0);
+    double ww = 0.;
+    for (int s = 0; s < 2; s++)
+      for (int e = 0; e < 2; e++) {
+        const double w = rSum - sqrt(eDistSq[s][e]);
+        pp = pp + w * (eClose[s][e] + (ends[s][e] - eClose[s][e]) * (s == 0 ? r2r : r1r));
+        ww += w;
+      }
+    contPt = pp / ww;
+  } else {
+    // two or three overlapping ends (bit 2s+e for end e of capsule s): the two that place the contact; with
+    // three, the two ends of the capsule whose both ends overlap (the reference's lookup table)
+    int q0s = 0, q0e = 0, q1s = 0, q1e = 0;
+    switch (bits) {
+      case 3: case 7: case 11: q1e = 1; break;           // ends of capsule 0
+      case 5: q1s = 1; break;                             // (0,0), (1,0)
+      case 6: q0e = 1; q1s = 1; break;                    // (0,1), (1,0)
+      case 9: q1s = 1; q1e = 1; break;                    // (0,0), (1,1)
+      case 10: q0e = 1; q1s = 1; q1e = 1; break;          // (0,1), (1,1)
+      case 12: case 13: case 14: q0s = 1; q1s = 1; q1e = 1; break;  // ends of capsule 1
+      default: break;
+    }
+    const d3 p0 = eClose[q0s][q0e] + (ends[q0s][q0e] - eClose[q0s][q0e]) * (q0s == 0 ? r2r : r1r);
+    const d3 p1 = eClose[q1s][q1e] + (ends[q1s][q1e] - eClose[q1s][q1e]) * (q1s == 0 ? r2r : r1r);
+    const double w0 = rSum - sqrt(eDistSq[q0s][q0e]), w1 = rSum - sqrt(eDistSq[q1s][q1e]);
+    contPt = (w0 * p0 + w1 * p1) / (w0 + w1);
+  }
+  r1 = c1.x;
+  r2 = c2.x;
+  return true;
+}
+
 // One contact of the work list: geometry, physics and law (ContactLoop.cpp:134-197).  PENDING
 // contacts have been resolved and potential pairs that cannot touch culled by k_contacts_cull.
 template <int LAW, int CP2, bool PERI, bool ELL>
@@ -316,7 +562,14 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   double r1, r2, uN;
   d3 normal, contPt;
   if (ELL && (sb & CS_ELL)) {
-    if (sb & CS_WALL_A) {
+    // aspherical shapes: ellipsoids and capsules (pB is the capsule of a sphere or wall pair)
+    if ((p.meta[b].x & 15) == WDEM_SHAPE_CAPSULE) {
+      if (sb & CS_WALL_A) {
+        if (!wallCapsuleGeometry(p, c, i, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
+      } else if ((p.meta[a].x & 15) == WDEM_SHAPE_SPHERE) {
+        if (!sphereCapsuleGeometry(p, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
+      } else if (!capsuleCapsuleGeometry(p, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
+    } else if (sb & CS_WALL_A) {
       if (!wallEllGeometry(p, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2)) return;
     } else if (!ellPairGeometry(P, p, c, i, a, b, real, pos1, pos2, normal, contPt, uN, r1, r2, st)) return;
   } else if (!PERI && (sb & CS_FACET)) {  // facets are aperiodic only

@@ -161,8 +161,9 @@ __global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const
       if (i >= 0) {
         const uint8_t sb = c.state[i] & CS_SHAPES;
         const bool hasLam = onlyFresh && c.lam && c.lam[i] > 0 && c.lam[i] < 1;
-        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && (c.state[i] & CS_MASK) != CS_DEAD && !hasLam) {
-          const int2 id = c.ids[i];
+        const int2 id = c.ids[i];
+        const bool ellPair = (p.meta[id.x].x & 15) != WDEM_SHAPE_CAPSULE && (p.meta[id.y].x & 15) != WDEM_SHAPE_CAPSULE;
+        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && ellPair && (c.state[i] & CS_MASK) != CS_DEAD && !hasLam) {
           const double4_32a OA = p.ori[id.x], OB = p.ori[id.y];
           qd oa, ob;
           oa.w = OA.x; oa.x = OA.y; oa.y = OA.z; oa.z = OA.w;

@@ -629,10 +629,15 @@ void resolveVerlet(wdem_handle* h) {
   if (vd >= 0) { h->verletDistResolved = vd; return; }
   double minR = std::numeric_limits<double>::infinity();
   for (int i = 0; i < h->n; i++) {
-    // Shape::equivRadius: Sphere.radius, Ellipsoid cbrt(abc) (Ellipsoid.cpp:25-28)
+    // Shape::equivRadius: Sphere.radius, Ellipsoid cbrt(abc) (Ellipsoid.cpp:25-28), Capsule the radius of the
+    // sphere of its volume (Capsule.cpp:25-31); NaN for walls and facets
     double r = std::numeric_limits<double>::quiet_NaN();
     if (h->shape[i] == WDEM_SHAPE_SPHERE) r = h->radius[i];
     else if (h->shape[i] == WDEM_SHAPE_ELLIPSOID) r = std::cbrt(h->semi[3 * i] * h->semi[3 * i + 1] * h->semi[3 * i + 2]);
+    else if (h->shape[i] == WDEM_SHAPE_CAPSULE) {
+      const double rc = h->radius[i], vol = (4 / 3.) * M_PI * (rc * rc * rc) + M_PI * (rc * rc) * h->semi[3 * i + 1];
+      r = std::cbrt(vol * 3 / (4 * M_PI));
+    }
     if (!std::isnan(r)) minR = std::min(r, minR);
   }
   h->verletDistResolved = std::isinf(minR) ? 0.0 : std::abs(vd) * minR;
@@ -822,10 +827,20 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   std::vector<double4_32a> fv1, fv2;
   std::vector<int> facetIds;
   std::vector<int4> facetPairs;
+  std::vector<int2> capMasks;  // (mask, scene) of every capsule
   for (int i = 0; i < n; i++) {
     int sh = p->shape[i];
-    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID && sh != WDEM_SHAPE_FACET)
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_WALL && sh != WDEM_SHAPE_ELLIPSOID && sh != WDEM_SHAPE_FACET &&
+        sh != WDEM_SHAPE_CAPSULE)
       return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape of particle #" + std::to_string(i));
+    if (sh == WDEM_SHAPE_CAPSULE) {
+      if (!p->shaft) return fail(h, WDEM_ERR_ARG, "capsules need wdem_particles.shaft");
+      // Capsule::selfTest (Capsule.cpp:19-23)
+      if (!(p->radius[i] > 0.) || !(p->shaft[i] >= 0.))
+        return fail(h, WDEM_ERR_ARG, "Capsule #" + std::to_string(i) + ": radius must be positive and shaft non-negative");
+      if (h->periodic) return fail(h, WDEM_ERR_UNSUPPORTED, "capsules in a periodic cell are not supported");
+      capMasks.push_back(make_int2((int)p->mask[i], p->scene ? p->scene[i] : 0));
+    }
     if (sh == WDEM_SHAPE_FACET) {
       // fixed facets: nodes 1 and 2 are not integrated, so node 0 may not move either
       const std::string fid = "Facet #" + std::to_string(i);
@@ -863,6 +878,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     int ax = p->wallAxis ? p->wallAxis[i] : 0, sense = p->wallSense ? p->wallSense[i] : 0;
     if (sh == WDEM_SHAPE_WALL && (ax < 0 || ax > 2 || sense < -1 || sense > 1)) return fail(h, WDEM_ERR_ARG, "bad wall axis/sense");
     double r = (sh == WDEM_SHAPE_SPHERE || sh == WDEM_SHAPE_FACET) ? p->radius[i] : 0.0;  // facets: halfThick
+    if (sh == WDEM_SHAPE_CAPSULE) r = p->radius[i] + .5 * p->shaft[i];                    // bounding radius
     if (sh == WDEM_SHAPE_ELLIPSOID) {
       // bounding radius: the largest semi-axis (FP32 cull and minDist00Sq of the ellipsoid functors)
       const double* sa = p->semiAxes + 3 * i;
@@ -870,7 +886,8 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
     }
     if (sh == WDEM_SHAPE_ELLIPSOID) { semi[3 * i] = p->semiAxes[3 * i]; semi[3 * i + 1] = p->semiAxes[3 * i + 1]; semi[3 * i + 2] = p->semiAxes[3 * i + 2]; }
     else if (sh == WDEM_SHAPE_SPHERE) { semi[3 * i] = semi[3 * i + 1] = semi[3 * i + 2] = r; }
-    anyEll |= (sh == WDEM_SHAPE_ELLIPSOID) || asph;
+    else if (sh == WDEM_SHAPE_CAPSULE) { semi[3 * i] = p->radius[i]; semi[3 * i + 1] = p->shaft[i]; semi[3 * i + 2] = 0; }
+    anyEll |= (sh == WDEM_SHAPE_ELLIPSOID) || (sh == WDEM_SHAPE_CAPSULE) || asph;
     posr[i] = make_double4_32a(p->pos[3 * i], p->pos[3 * i + 1], p->pos[3 * i + 2], r);
     velm[i] = make_double4_32a(p->vel[3 * i], p->vel[3 * i + 1], p->vel[3 * i + 2], p->mass[i]);
     angw[i] = make_double4_32a(p->angVel[3 * i], p->angVel[3 * i + 1], p->angVel[3 * i + 2], 0);
@@ -905,6 +922,17 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
       const unsigned mm = p->mask[f] & p->mask[j];
       if (j != f && mm != 0 && (p->scene ? p->scene[f] == p->scene[j] : true)) facetPairs.push_back(make_int4(f, j, (int)mm, 0));
     }
+  // facet + capsule pairs (no Cg2_Facet_Capsule_L6Geom here) are refused like facet + wall: y = -1
+  if (!facetIds.empty() && !capMasks.empty()) {
+    std::sort(capMasks.begin(), capMasks.end(), [](int2 x, int2 y) { return x.x != y.x ? x.x < y.x : x.y < y.y; });
+    capMasks.erase(std::unique(capMasks.begin(), capMasks.end(), [](int2 x, int2 y) { return x.x == y.x && x.y == y.y; }),
+                   capMasks.end());
+    for (int f : facetIds)
+      for (const int2& cm : capMasks) {
+        const unsigned mm = p->mask[f] & (unsigned)cm.x;
+        if (mm != 0 && (p->scene ? p->scene[f] : 0) == cm.y) facetPairs.push_back(make_int4(f, -1, (int)mm, 0));
+      }
+  }
   h->facetPairs = facetPairs;
   h->facetsChecked = ~0u;
   h->matsChecked = -1;
@@ -1182,11 +1210,15 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     // Cg2_Facet_Facet_L6Geom and Cg2_Wall_Facet_L6Geom are not implemented: such pairs must be excluded by
     // the masks (Collider::mayCollide), as DemField.defaultBoundaryMask with DemField.loneMask does
     for (const int4& q : h->facetPairs)
-      if (((unsigned)q.z & h->P.loneMask) == 0)
+      if (((unsigned)q.z & h->P.loneMask) == 0) {
+        if (q.y < 0)
+          return fail(h, WDEM_ERR_UNSUPPORTED, "Facet #" + std::to_string(q.x) +
+                                                   " may collide with capsules: facet-capsule contacts are not implemented");
         return fail(h, WDEM_ERR_UNSUPPORTED, "Facet #" + std::to_string(q.x) + " may collide with " +
                                                  (h->shape[q.y] == WDEM_SHAPE_WALL ? "Wall #" : "Facet #") + std::to_string(q.y) +
                                                  ": facet-facet and wall-facet contacts are not implemented (give the "
                                                  "boundaries a common loneMask bit)");
+      }
     h->facetsChecked = h->P.loneMask;
   }
   if (h->device >= 0 && h->device < 64 && g_matsOwner[h->device] != h) {
@@ -1488,7 +1520,7 @@ int wdem_crit_dt(wdem_handle* h, double* dt) {
   double r = std::numeric_limits<double>::infinity();
   for (int i = 0; i < h->n; i++) {
     double radius;
-    if (h->shape[i] == WDEM_SHAPE_SPHERE) radius = h->radius[i];
+    if (h->shape[i] == WDEM_SHAPE_SPHERE || h->shape[i] == WDEM_SHAPE_CAPSULE) radius = h->radius[i];
     else if (h->shape[i] == WDEM_SHAPE_ELLIPSOID) {
       const double* sa = &h->semi[3 * i];
       radius = sa[0]; if (sa[1] < radius) radius = sa[1]; if (sa[2] < radius) radius = sa[2];
@@ -1697,16 +1729,19 @@ int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* i
   for (int k = 0; k < m; k++) {
     const int sh = p->shape[k];
     if (sh == WDEM_SHAPE_WALL) return fail(h, WDEM_ERR_UNSUPPORTED, "walls are added through wdem_upload_particles");
-    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_ELLIPSOID) return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape");
+    if (sh != WDEM_SHAPE_SPHERE && sh != WDEM_SHAPE_ELLIPSOID && sh != WDEM_SHAPE_CAPSULE)
+      return fail(h, WDEM_ERR_UNSUPPORTED, "unsupported shape");
+    if (sh == WDEM_SHAPE_CAPSULE && (!p->shaft || !(p->radius[k] > 0.) || !(p->shaft[k] >= 0.)))
+      return fail(h, WDEM_ERR_ARG, "capsules need a positive radius and a non-negative wdem_particles.shaft");
     if (p->material[k] < 0 || p->material[k] >= (int)h->mats.size())
       return fail(h, WDEM_ERR_ARG, "material index out of range for an added particle");
     const unsigned fl = p->flags[k];
     if (fl & (WDEM_CLUMP_CLUMP | WDEM_CLUMP_CLUMPED)) return fail(h, WDEM_ERR_UNSUPPORTED, "clumps are not supported");
     const double* in = p->inertia + 3 * k;
     const bool asph = !(in[0] == in[1] && in[1] == in[2]) && (fl & 56u) != 56u;
-    if ((sh == WDEM_SHAPE_ELLIPSOID || asph) && !h->hasEll)
+    if ((sh == WDEM_SHAPE_ELLIPSOID || sh == WDEM_SHAPE_CAPSULE || asph) && !h->hasEll)
       return fail(h, WDEM_ERR_UNSUPPORTED, "ellipsoids or aspherical nodes in a handle without them: use wdem_upload_particles");
-    if ((sh == WDEM_SHAPE_ELLIPSOID || asph) && h->periodic)
+    if ((sh == WDEM_SHAPE_ELLIPSOID || sh == WDEM_SHAPE_CAPSULE || asph) && h->periodic)
       return fail(h, WDEM_ERR_UNSUPPORTED, "ellipsoids and aspherical nodes in a periodic cell are not supported");
     const int sc = p->scene ? p->scene[k] : 0;
     if (sc < 0 || sc >= std::max(1, h->cs.nScenes)) return fail(h, WDEM_ERR_ARG, "scene index out of range for an added particle");
@@ -1718,6 +1753,7 @@ int wdem_add_particles(wdem_handle* h, const wdem_particles* p, const int32_t* i
       if (!(sa[0] > 0 && sa[1] > 0 && sa[2] > 0)) return fail(h, WDEM_ERR_ARG, "ellipsoid semi-axes must be positive");
       r = std::max(sa[0], std::max(sa[1], sa[2]));
     }
+    if (sh == WDEM_SHAPE_CAPSULE) { sa[0] = p->radius[k]; sa[1] = p->shaft[k]; sa[2] = 0; r = p->radius[k] + .5 * p->shaft[k]; }
     double4_32a* q = rec.data() + (size_t)EDIT_RECORDS * k;
     q[0] = make_double4_32a(p->pos[3 * k], p->pos[3 * k + 1], p->pos[3 * k + 2], r);
     q[1] = make_double4_32a(p->vel[3 * k], p->vel[3 * k + 1], p->vel[3 * k + 2], p->mass[k]);
@@ -1881,7 +1917,8 @@ int wdem_set_cell(wdem_handle* h, const wdem_cell* c) {
   if (c->homoDeform != 4) return fail(h, WDEM_ERR_UNSUPPORTED, "Cell.homoDeform other than gradV2 (4) is not supported");
   for (int s : h->shape)
     if (s != WDEM_SHAPE_SPHERE)
-      return fail(h, WDEM_ERR_UNSUPPORTED, std::string(s == WDEM_SHAPE_FACET ? "facets" : s == WDEM_SHAPE_WALL ? "walls" : "ellipsoids") +
+      return fail(h, WDEM_ERR_UNSUPPORTED, std::string(s == WDEM_SHAPE_FACET ? "facets" : s == WDEM_SHAPE_WALL ? "walls" :
+                                                       s == WDEM_SHAPE_CAPSULE ? "capsules" : "ellipsoids") +
                                                " in a periodic cell are not supported");
   if (h->nContacts > 0 && !h->periodic) return fail(h, WDEM_ERR_STATE, "set the cell before uploading contacts");
   if (h->cs.nScenes > 1) return fail(h, WDEM_ERR_UNSUPPORTED, "batched scenes in a periodic cell are not supported");

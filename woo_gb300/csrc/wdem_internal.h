@@ -58,15 +58,21 @@ __host__ __device__ __forceinline__ int sceneOf(int metax) { return (metax >> ME
 // Sphere+Wall, Ellipsoid+Sphere, Ellipsoid+Wall or Sphere+Facet.
 __host__ __device__ __forceinline__ bool pairSwaps(int sa, int sb) {
   return (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_SPHERE) ||
-         (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET);
+         (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_WALL) || (sa == WDEM_SHAPE_SPHERE && sb == WDEM_SHAPE_FACET) ||
+         (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_SPHERE) || (sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_WALL);
 }
-// shape bits of the state byte of an oriented pair; pairs with no functor (wall + wall, facet + anything but
-// a sphere) get both wall bits and are skipped
+// shape bits of the state byte of an oriented pair: capsules count as aspherical (the ellipsoid bits, the
+// contact kernel tells them apart by the shapes); pairs with no functor (wall + wall, facet + anything but a
+// sphere, capsule + ellipsoid) get both wall bits and are skipped
 __host__ __device__ __forceinline__ uint8_t pairShapeBits(int sa, int sb) {
   if (sa == WDEM_SHAPE_FACET || sb == WDEM_SHAPE_FACET)
     return (uint8_t)((sa == WDEM_SHAPE_FACET && sb == WDEM_SHAPE_SPHERE) ? CS_FACET : (CS_WALL_A | CS_WALL_B));
+  if ((sa == WDEM_SHAPE_CAPSULE && sb == WDEM_SHAPE_ELLIPSOID) || (sa == WDEM_SHAPE_ELLIPSOID && sb == WDEM_SHAPE_CAPSULE))
+    return (uint8_t)(CS_WALL_A | CS_WALL_B);
+  const bool aspA = sa == WDEM_SHAPE_ELLIPSOID || sa == WDEM_SHAPE_CAPSULE;
+  const bool aspB = sb == WDEM_SHAPE_ELLIPSOID || sb == WDEM_SHAPE_CAPSULE;
   return (uint8_t)((sa == WDEM_SHAPE_WALL ? CS_WALL_A : 0) | (sb == WDEM_SHAPE_WALL ? CS_WALL_B : 0) |
-                   (sa == WDEM_SHAPE_ELLIPSOID ? CS_ELL_A : 0) | (sb == WDEM_SHAPE_ELLIPSOID ? CS_ELL_B : 0));
+                   (aspA ? CS_ELL_A : 0) | (aspB ? CS_ELL_B : 0));
 }
 enum { HIST_T0X = 0, HIST_T0Y, HIST_T0Z, HIST_T1X, HIST_T1Y, HIST_T1Z, HIST_CX, HIST_CY, HIST_CZ,
        HIST_FX, HIST_FY, HIST_FZ, HIST_KN, HIST_KT,

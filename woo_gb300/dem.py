@@ -279,6 +279,51 @@ class Ellipsoid(Shape):
         return p
 
 
+class Capsule(Shape):
+    """Capsule (src/dem/Capsule.hpp:8-35): a cylinder of length shaft along the node's local x axis with
+    hemispherical caps of radius; mass and inertia from Capsule::lumpMassInertia (Capsule.cpp:44-57).  On
+    the GPU it is an aspherical shape (FrictMat + IdealElPl) contacting spheres, walls and capsules."""
+    _shape = abi.SHAPE_CAPSULE
+
+    def __init__(self, radius=nan, shaft=nan):
+        super().__init__()
+        self.radius = float(radius)
+        self.shaft = float(shaft)
+
+    def volume(self):
+        """Capsule::volume (Capsule.cpp:25-27)."""
+        r = self.radius
+        return (4 / 3.0) * math.pi * (r * r * r) + math.pi * (r * r) * self.shaft
+
+    def equivRadius(self):
+        return float(np.cbrt(self.volume() * 3 / (4 * math.pi)))
+
+    def endPt(self, i):
+        """Capsule::endPt (Capsule.hpp:24): end 0 at local -shaft/2 x, end 1 at +shaft/2 x."""
+        from . import scenes
+        n = self.nodes[0]
+        return n.pos + scenes.quat_rotate(n.ori, ((-.5 if i == 0 else .5) * self.shaft, 0, 0))
+
+    @staticmethod
+    def make(center, radius, shaft, ori=(1, 0, 0, 0), mat=None, fixed=False, mask=DEFAULT_MOVABLE_MASK, wire=False,
+             color=None):
+        """woo.utils.capsule / Capsule.make (py/utils.py:213-221)."""
+        from . import scenes
+        if not (radius > 0) or not (shaft >= 0):
+            raise RuntimeError("Capsule: radius must be positive and shaft non-negative")
+        mat = mat if mat is not None else defaultMaterial()
+        sh = Capsule(radius, shaft)
+        n = Node(pos=center, ori=ori)
+        sh.nodes.append(n)
+        p = Particle(shape=sh, material=mat, mask=mask)
+        m, inertia = scenes.capsule_mass_inertia(radius, shaft, mat.density)
+        n.dem.mass = float(m)
+        n.dem.inertia = np.asarray(inertia, float)
+        if fixed:
+            n.dem.blocked = "xyzXYZ"
+        return p
+
+
 class Facet(Shape):
     """Facet (src/dem/Facet.hpp:8-57): a triangle of three nodes with halfThick.  The GPU engine takes fixed
     facets (all DOFs blocked, at rest) without fakeVel and without neighbour angles (n21lim NaN); it contacts
@@ -564,6 +609,10 @@ class Contact:
             elif isinstance(pa.shape, Facet):
                 # Cg2_Facet_Sphere_L6Geom: max(halfThick, radius) and radius (Facet.cpp:389)
                 r1, r2 = max(pa.shape.halfThick, pb.shape.radius), pb.shape.radius
+            elif isinstance(pb.shape, Capsule):
+                # the capsule functors pass the radii (a wall's as -radius, Capsule.cpp:163, 215, 322)
+                r2 = pb.shape.radius
+                r1 = -r2 if isinstance(pa.shape, Wall) else pa.shape.radius
             else:
                 # ellipsoid functors: distances of the contact point from the centres (Ellipsoid.cpp:250, 349)
                 cp = ca.contPt[i]
@@ -808,7 +857,7 @@ class DemField:
         for p in self.par:
             if not isinstance(p.material, ElastMat):
                 continue
-            if isinstance(p.shape, Sphere):
+            if isinstance(p.shape, (Sphere, Capsule)):
                 r = p.shape.radius
             elif isinstance(p.shape, Ellipsoid):
                 r = float(np.min(p.shape.semiAxes))
@@ -859,6 +908,22 @@ class Cg2_Sphere_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
 
 class Cg2_Wall_Sphere_L6Geom(Cg2_Any_Any_L6Geom__Base):
     """Cg2_Wall_Sphere_L6Geom (src/dem/Wall.cpp:50-84)."""
+
+
+class Bo1_Capsule_Aabb(BoundFunctor):
+    """Bo1_Capsule_Aabb (src/dem/Capsule.hpp:36-46)."""
+
+
+class Cg2_Sphere_Capsule_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Sphere_Capsule_L6Geom (src/dem/Capsule.cpp:198-216)."""
+
+
+class Cg2_Wall_Capsule_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Wall_Capsule_L6Geom (src/dem/Capsule.cpp:116-164)."""
+
+
+class Cg2_Capsule_Capsule_L6Geom(Cg2_Any_Any_L6Geom__Base):
+    """Cg2_Capsule_Capsule_L6Geom (src/dem/Capsule.cpp:223-323)."""
 
 
 class Bo1_Facet_Aabb(BoundFunctor):
@@ -1052,7 +1117,9 @@ class GpuDemEngine(Engine):
 
     def __init__(self, cg2=None, cp2=None, law=None, **kw):
         super().__init__(**kw)
-        self.geoFunctors = list(cg2 or [Cg2_Sphere_Sphere_L6Geom(), Cg2_Facet_Sphere_L6Geom(), Cg2_Wall_Sphere_L6Geom()])
+        self.geoFunctors = list(cg2 or [Cg2_Sphere_Sphere_L6Geom(), Cg2_Facet_Sphere_L6Geom(), Cg2_Wall_Sphere_L6Geom(),
+                                        Cg2_Wall_Capsule_L6Geom(), Cg2_Capsule_Capsule_L6Geom(),
+                                        Cg2_Sphere_Capsule_L6Geom()])
         self.phyFunctors = list(cp2 or [Cp2_FrictMat_FrictPhys()])
         self.lawFunctors = list(law or [Law2_L6Geom_FrictPhys_IdealElPl()])
         self._h = None
@@ -1090,6 +1157,11 @@ class GpuDemEngine(Engine):
         if any(isinstance(p.shape, Facet) for p in field.par) and \
                 self._functor(self.geoFunctors, (Cg2_Facet_Sphere_L6Geom,)) is None:
             raise RuntimeError("facets in the scene need Cg2_Facet_Sphere_L6Geom in ContactLoop.geoFunctors")
+        if any(isinstance(p.shape, Capsule) for p in field.par):
+            missing = [c.__name__ for c in (Cg2_Sphere_Capsule_L6Geom, Cg2_Wall_Capsule_L6Geom, Cg2_Capsule_Capsule_L6Geom)
+                       if self._functor(self.geoFunctors, (c,)) is None]
+            if missing:
+                raise RuntimeError("capsules in the scene need " + ", ".join(missing) + " in ContactLoop.geoFunctors")
         cp2 = self._functor(self.phyFunctors, (Cp2_HertzMat_HertzPhys,)) or self._functor(self.phyFunctors, (Cp2_FrictMat_FrictPhys,))
         law = self._functor(self.lawFunctors, (Law2_L6Geom_HertzPhys_DMT,)) or self._functor(self.lawFunctors, (Law2_L6Geom_FrictPhys_IdealElPl,))
         if cp2 is None or law is None:
@@ -1190,6 +1262,8 @@ class GpuDemEngine(Engine):
             pa.shape[i] = abi.SHAPE_WALL; pa.wallAxis[i] = sh.axis; pa.wallSense[i] = sh.sense
         elif isinstance(sh, Ellipsoid):
             pa.shape[i] = abi.SHAPE_ELLIPSOID; pa.semiAxes[i] = sh.semiAxes
+        elif isinstance(sh, Capsule):
+            pa.shape[i] = abi.SHAPE_CAPSULE; pa.radius[i] = sh.radius; pa.shaft[i] = sh.shaft
         elif isinstance(sh, Facet):
             pa.shape[i] = abi.SHAPE_FACET; pa.radius[i] = sh.halfThick
             pa.facetVerts[i] = np.concatenate(sh._verts())
@@ -1314,7 +1388,7 @@ class GpuDemEngine(Engine):
         if self.autotune and not getattr(self, "_tuned", None):
             from . import tuning
             key = tuning.workload_key(len(field.par), self._params.law, getattr(scene, "periodic", False),
-                                      any(isinstance(p.shape, Ellipsoid) for p in field.par))
+                                      any(isinstance(p.shape, (Ellipsoid, Capsule)) for p in field.par))
             self._h.set_params(self._params)
 
             def probe():

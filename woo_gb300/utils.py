@@ -39,9 +39,11 @@ def defaultEngines(damping=0.0, gravity=None, verletDist=-0.05, kinSplit=False, 
         raise ValueError("only the sweep-and-prune collider ('sap') is provided")
     engines = [
         dem.Leapfrog(damping=damping, reset=True, kinSplit=kinSplit, dontCollect=dontCollect, label="leapfrog"),
-        dem.InsertionSortCollider([dem.Bo1_Sphere_Aabb(), dem.Bo1_Facet_Aabb(), dem.Bo1_Wall_Aabb()], label="collider",
-                                  verletDist=verletDist),
-        dem.ContactLoop([dem.Cg2_Sphere_Sphere_L6Geom(), dem.Cg2_Facet_Sphere_L6Geom(), dem.Cg2_Wall_Sphere_L6Geom()],
+        dem.InsertionSortCollider([dem.Bo1_Sphere_Aabb(), dem.Bo1_Facet_Aabb(), dem.Bo1_Wall_Aabb(), dem.Bo1_Capsule_Aabb()],
+                                  label="collider", verletDist=verletDist),
+        dem.ContactLoop([dem.Cg2_Sphere_Sphere_L6Geom(), dem.Cg2_Facet_Sphere_L6Geom(), dem.Cg2_Wall_Sphere_L6Geom(),
+                         dem.Cg2_Wall_Capsule_L6Geom(), dem.Cg2_Capsule_Capsule_L6Geom(),
+                         dem.Cg2_Sphere_Capsule_L6Geom()],
                         cp2, law, applyForces=True, label="contactLoop"),
     ]
     if dynDtPeriod > 0:
@@ -63,6 +65,12 @@ def ellipsoid(center, semiAxes, ori=(1, 0, 0, 0), angVel=None, color=None, mat=N
     if angVel is not None:
         p.angVel = angVel
     return p
+
+
+def capsule(center, radius, shaft, ori=(1, 0, 0, 0), fixed=False, color=None, wire=False, mat=None,
+            mask=dem.DEFAULT_MOVABLE_MASK):
+    """py/utils.py:213-221: a Capsule on a new node with orientation ori (w, x, y, z)."""
+    return dem.Capsule.make(center, radius, shaft, ori=ori, mat=mat, fixed=fixed, mask=mask)
 
 
 def facet(vertices, fakeVel=None, halfThick=0.0, fixed=True, wire=True, color=None, highlight=False, mat=None,
