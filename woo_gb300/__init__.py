@@ -6,8 +6,8 @@ include/wdem.h); there is no CPU fallback.
 """
 __version__ = "0.1.0"
 
-from . import abi, core, dem, models, scenes, utils  # noqa: E402,F401
+from . import abi, core, dem, models, pack, scenes, utils  # noqa: E402,F401
 from .core import Scene  # noqa: E402,F401
 from .dem import master  # noqa: E402,F401
-from .dem import (DemField, FrictMat, HertzMat, Sphere, Wall, GpuDemEngine, Leapfrog,  # noqa: E402,F401
-                  InsertionSortCollider, ContactLoop)
+from .dem import (DemField, FrictMat, HertzMat, Sphere, Wall, Ellipsoid, Capsule, Facet, GpuDemEngine,  # noqa: E402,F401
+                  Leapfrog, InsertionSortCollider, ContactLoop)
