@@ -7,11 +7,11 @@
 // on all three axes (spatialOverlap, InsertionSortCollider.cpp:67-73) and that mayCollide
 // (Collision.cpp:21-43), plus every real contact carried over from before (the reference never
 // removes real contacts in the collider).  Instead of an incremental insertion sort, the rebuild
-//   1. sorts small particles by (grid column in the two short axes, quantised box minimum along the
-//      longest axis) with an LSD radix sort written here,
-//   2. sweeps each particle forward along the long axis in its own and the 8 neighbouring columns,
+//   1. sorts small particles by (grid column in the two long axes, quantised box minimum along the
+//      shortest axis) with an LSD radix sort written here,
+//   2. sweeps each particle forward along the sweep axis in its own and the 8 neighbouring columns,
 //      testing the exact FP64 closed-interval overlap (grid cell >= widest box, so no pair is missed),
-//   3. tests walls and other unbounded boxes against every particle,
+//   3. tests walls, facets and other large boxes against every particle of their scene,
 //   4. writes the pairs in a deterministic order (count pass, exclusive scan, write pass),
 //   5. carries contact history over through an open-addressing hash table keyed by (min id, max id),
 //   6. builds the per-particle contact CSR with rows ordered by the partner id.
@@ -194,8 +194,11 @@ __global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxC
     bmax[a] = ordVal(~ext[9 + a]);
     w[a] = ordVal(~ext[12 + a]);
   }
+  // the sweep runs along the shortest extent of the box centres and the columns tile the two longest: the
+  // most columns for the cap, so the fewest boxes per column and the shortest binary searches into them
+  // (a row of batched scenes along one axis would otherwise put all scenes into the same few long columns)
   int ax = 0;
-  for (int a = 1; a < 3; a++) if (cmax[a] - cmin[a] > cmax[ax] - cmin[ax]) ax = a;
+  for (int a = 1; a < 3; a++) if (cmax[a] - cmin[a] < cmax[ax] - cmin[ax]) ax = a;
   int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;
   double W = fmax(w[a1], w[a2]);
   double cell = W * (1.0 + 1e-6) + 1e-300;
