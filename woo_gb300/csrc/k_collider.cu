@@ -468,21 +468,27 @@ template <bool WRITE>
 __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned* counts, int2* out, long long cap,
                         DeviceStatus* st) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s > A.nSmall) return;
+  if (s >= sweepThreads(A.nSmall, A.nLarge)) return;
   unsigned cnt = 0;
   unsigned long long base = WRITE ? counts[s] : 0;
-  if (s == A.nSmall) {
-    // large-large pairs (walls of the same scene; the large list is grouped by scene)
-    for (int a = 0; a < A.nLarge; a++)
+  if (s >= A.nSmall) {
+    // large-large pairs, one thread per large body a: the bodies after it in the large list up to the
+    // first one of another scene (the list is grouped by scene)
+    const int a = s - A.nSmall;
+    if (a < A.nLarge) {
+      const int i = A.large[a];
+      const int4 mi = p.meta[i];
+      const double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
       for (int b = a + 1; b < A.nLarge; b++) {
-        int i = A.large[a], j = A.large[b];
-        int4 mi = p.meta[i], mj = p.meta[j];
+        const int j = A.large[b];
+        const int4 mj = p.meta[j];
         if (sceneOf(mi.x) != sceneOf(mj.x)) break;
         if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
-        if (!overlap3(p.bbmin[i], p.bbmax[i], p.bbmin[j], p.bbmax[j])) continue;
+        if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
         if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
         cnt++;
       }
+    }
     if (!WRITE) counts[s] = cnt;
     return;
   }
@@ -969,7 +975,7 @@ void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, Colli
   A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
   A.nSmall = nSmall; A.loneMask = loneMask;
   A.sceneWall = cs.nScenes > 1 ? cs.sceneWall : nullptr;
-  int threads = nSmall + 1;
+  const int threads = sweepThreads(nSmall, cs.nLarge);
   if (write) (k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
   else (k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
 }

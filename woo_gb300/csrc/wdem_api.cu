@@ -469,7 +469,8 @@ int rebuild(wdem_handle* h) {
   int rc;
   if ((rc = ensureScratch(h, h->nContacts))) return rc;
   launch_bboxes(s, h->P, h->d, n);
-  const unsigned* totalSrc = cs.counts + nSmall + 1;
+  const int nSweep = sweepThreads(nSmall, cs.nLarge);
+  const unsigned* totalSrc = cs.counts + nSweep;
   long long nCand = 0;
   if (h->periodic) {
     col_periodic_cand(s, h->P, h->d, h->dSmall, nSmall, cs, false);
@@ -484,7 +485,7 @@ int rebuild(wdem_handle* h) {
     col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
     col_sort(s, h->d, h->dSmall, nSmall, cs);
     col_sweep(s, h->d, nSmall, h->P.loneMask, cs, nullptr, 0, false, h->dst);
-    exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
+    exclusive_scan_u32(s, cs.counts, nSweep, cs);
   }
   ContactBuf& old = h->buf[h->cur];
   ContactBuf& neu = h->buf[1 - h->cur];
@@ -1617,8 +1618,9 @@ int wdem_collide_boxes(wdem_handle* h, int32_t n, const double* mins, const doub
   col_extents_and_grid(s, h->d, h->dSmall, nSmall, cs);
   col_sort(s, h->d, h->dSmall, nSmall, cs);
   col_sweep(s, h->d, nSmall, loneMask, cs, nullptr, 0, false, h->dst);
-  exclusive_scan_u32(s, cs.counts, nSmall + 1, cs);
-  CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSmall + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  const int nSweep = sweepThreads(nSmall, cs.nLarge);
+  exclusive_scan_u32(s, cs.counts, nSweep, cs);
+  CK(cudaMemcpyAsync(&h->hcounts[0], cs.counts + nSweep, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   long long total = h->hcounts[0];
   int2* dpairs = nullptr;

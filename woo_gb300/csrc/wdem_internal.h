@@ -53,6 +53,9 @@ enum { META_ASPH = 1 << 12, META_ORI_FIXED = 1 << 13, META_IPOS = 1 << 14 };
 // meta.x bits 16..27: scene index of batched independent scenes
 enum { META_SCENE_SHIFT = 16, MAX_SCENES = 4096 };
 __host__ __device__ __forceinline__ int sceneOf(int metax) { return (metax >> META_SCENE_SHIFT) & (MAX_SCENES - 1); }
+// threads (and pair-count entries) of the collider's sweep: one per small box, one per large body (at least
+// one); the exclusive scan of the counts leaves the pair total at counts[sweepThreads]
+__host__ __device__ __forceinline__ int sweepThreads(int nSmall, int nLarge) { return nSmall + (nLarge > 0 ? nLarge : 1); }
 // Pair orientation as the geometry functors take it (GeomDispatcher::getFunctor2D swaps a fresh contact,
 // ContactLoop.cpp:144-150): the pair (lower id, higher id) is swapped when its shapes come in the order
 // Sphere+Wall, Ellipsoid+Sphere, Ellipsoid+Wall or Sphere+Facet.
