@@ -84,6 +84,8 @@ def parse():
                          "contraction, or the reference's IEEE operations bit for bit")
     ap.add_argument("--autotune", default="auto", choices=["auto", "on", "off"],
                     help="tune the kernels' launch shape (wdem_autotune) before the timed region; auto: batch512 only")
+    ap.add_argument("--graphs", default="off", choices=["auto", "on", "off"],
+                    help="queued steps launched as CUDA graphs (wdem_set_step_graphs): off (default), auto, on")
     ap.add_argument("--profile-region", default="main", choices=["main", "settled", "none"],
                     help="timed region bracketed by cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     a = ap.parse_args()
@@ -249,6 +251,7 @@ def timed_steps(h, stream, k, world, local, barrier, profile=False):
 
 
 QUEUE_DEPTH = None
+GRAPHS = "off"
 
 
 def new_handle(spec, local, params=None):
@@ -256,6 +259,7 @@ def new_handle(spec, local, params=None):
     h = abi.Handle(spec.particles.n, device=local)
     if QUEUE_DEPTH is not None:
         h.set_queue_depth(QUEUE_DEPTH)
+    h.set_step_graphs({"auto": abi.GRAPHS_AUTO, "on": abi.GRAPHS_ON, "off": abi.GRAPHS_OFF}[GRAPHS])
     h.set_params(params or spec.params)
     h.upload_particles(spec.particles)
     h.set_params(params or spec.params)
@@ -341,8 +345,10 @@ def measure_region(h, spec, args, world, local, barrier, region, clocks=None):
     h.step(max(args.warmup, 3))
     st0 = h.status()
     l0 = h.launch_count()
+    g0 = h.graph_stats()
     ms = timed_steps(h, stream, args.steps, world, local, barrier, profile=(args.profile_region == region))
     launches = h.launch_count() - l0
+    g1 = h.graph_stats()
     st1 = h.status()
     cg = h.download_contacts()   # the state at the end of the timed region
     hertz = spec.params.cp2 == abi.CP2_HERTZ
@@ -384,6 +390,7 @@ def measure_region(h, spec, args, world, local, barrier, region, clocks=None):
     return {
         "value": replica_throughput(world, n, args.steps, ms / 1e3), "ms_per_step": ms / args.steps,
         "steps": args.steps, "warmup": max(args.warmup, 3), "gpu_launches": int(launches),
+        "step_graphs": {"mode": GRAPHS, "captures": int(g1[0] - g0[0]), "replays": int(g1[1] - g0[1])},
         "contacts": dict(counts, collider_rebuilds_timed=int(st1.nFullRuns - st0.nFullRuns)),
         "collider": {"window_steps": kw, "rebuilds_in_window": rebuilds,
                      "collider_ms_per_rebuild": (c_ms / c_n) if c_n else None,
@@ -630,6 +637,7 @@ def run_gpu(args, rank, world, local):
         "config": common_config(args, spec),
         "engine": {"parallelism": f"replicas x{world}", "arith": args.arith,
                    "queue_depth": 32 if args.queue_depth is None else args.queue_depth,
+                   "step_graphs": main["step_graphs"],
                    "steps_simulated_before_warmup": settled_steps},
         "gpu_launches": main["gpu_launches"],
         "contacts": main["contacts"], "collider": main["collider"],
@@ -730,9 +738,10 @@ def cpu_baseline(args):
 
 
 def main():
-    global QUEUE_DEPTH
+    global QUEUE_DEPTH, GRAPHS
     args = parse()
     QUEUE_DEPTH = args.queue_depth
+    GRAPHS = args.graphs
     rank, world, local = dist_env()
     if args.impl == "reference":
         if rank != 0:

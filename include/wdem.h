@@ -325,6 +325,19 @@ int wdem_set_timing(wdem_handle* h, int32_t enable);
  * (InsertionSortCollider::run, InsertionSortCollider.cpp:386-400). */
 int wdem_set_queue_depth(wdem_handle* h, int32_t depth);
 
+/* How the queued steps reach the GPU: WDEM_GRAPHS_OFF (default) launches every kernel of the queue
+ * from the host; WDEM_GRAPHS_ON captures the queue's kernels once as a CUDA graph and launches that
+ * graph for every later queue with the same launch arguments (same parameters, arrays and contact
+ * count; a rebuild or an upload captures again); WDEM_GRAPHS_AUTO captures only when at least eight
+ * replays are expected before the next collider rebuild.  Results do not depend on the mode.  No
+ * counterpart in the reference, whose Scene::doOneStep calls each engine's run() in turn
+ * (src/core/Scene.cpp:420-426). */
+enum { WDEM_GRAPHS_OFF = 0, WDEM_GRAPHS_AUTO = 1, WDEM_GRAPHS_ON = 2 };
+int wdem_set_step_graphs(wdem_handle* h, int32_t mode);
+
+/* Graph captures and graph launches of queued steps since the handle was created. */
+int wdem_graph_stats(wdem_handle* h, int64_t* captures, int64_t* replays);
+
 /* Keep L6Geom.uN, L6Geom.vel and L6Geom.angVel of every real contact so that
  * wdem_download_contacts can return them (off by default: they are per-step values that Woo keeps
  * in the contact's CGeom object, L6Geom.vel/angVel/uN at src/dem/L6Geom.hpp:16-18; storing them

@@ -37,9 +37,11 @@ def test_forward_matches_reference(wdem_lib):
     X = _features(np.random.default_rng(0), 1000)
     Yg = h.warm_predict(X)
     Yr, _ = M.forward(w, X)
-    # BF16 re-rounding of intermediate activations may differ by one BF16 ulp between accumulation orders
-    assert np.abs(Yg - Yr).max() <= 1e-2 * np.abs(Yr).max()
-    assert np.corrcoef(Yg.ravel(), Yr.ravel())[0, 1] > 0.9999
+    # the tcgen05 kernel accumulates in FP32 like the reference's float64 sums rounded at the same BF16
+    # points; a BF16 re-rounding of an activation that lands on a rounding boundary could move an output by
+    # one BF16 ulp of that activation's contribution, which the 1e-3 bound would still cover
+    assert np.abs(Yg - Yr).max() <= 1e-3 * np.abs(Yr).max()
+    assert np.corrcoef(Yg.ravel(), Yr.ravel())[0, 1] > 0.999999
 
 
 def test_gradient_matches_reference(wdem_lib):

@@ -29,6 +29,7 @@ SHAPE_SPHERE, SHAPE_WALL, SHAPE_ELLIPSOID, SHAPE_FACET, SHAPE_CAPSULE = 0, 1, 2,
 ELL_BRENT, ELL_NEWTON = 0, 1
 WARM_INPUTS, WARM_OUTPUTS, WARM_RECORD, WARM_NPARAM = 13, 4, 17, 9476
 WARM_COLD, WARM_MLP, WARM_HISTORY, WARM_HISTORY_MLP = 0, 1, 2, 3
+GRAPHS_OFF, GRAPHS_AUTO, GRAPHS_ON = 0, 1, 2
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
 ARITH_EXACT, ARITH_FMA = 0, 1
@@ -119,7 +120,7 @@ EXPORTS = ["wdem_abi_version", "wdem_create", "wdem_destroy", "wdem_set_params",
            "wdem_get_stress_noalloc", "wdem_warm_init", "wdem_warm_set_weights", "wdem_warm_get_weights",
            "wdem_warm_predict", "wdem_warm_grad", "wdem_warm_train", "wdem_ell_log", "wdem_ell_log_read", "wdem_make_cloud_radii", "wdem_set_contact_limit",
            "wdem_remove_particles", "wdem_add_particles", "wdem_set_launch_shape", "wdem_get_launch_shape",
-           "wdem_autotune"]
+           "wdem_autotune", "wdem_set_step_graphs", "wdem_graph_stats"]
 
 
 def ptr(a, ctype):
@@ -290,6 +291,8 @@ def load(path=None):
         "wdem_kernel_times": ([h, C.POINTER(C.c_char_p), D, I32, C.c_int32, I32], C.c_int),
         "wdem_set_timing": ([h, C.c_int32], C.c_int),
         "wdem_set_queue_depth": ([h, C.c_int32], C.c_int),
+        "wdem_set_step_graphs": ([h, C.c_int32], C.c_int),
+        "wdem_graph_stats": ([h, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
         "wdem_keep_geom": ([h, C.c_int32], C.c_int),
         "wdem_make_cloud": ([D, D, C.c_double, C.c_double, C.c_int64, C.c_uint64, C.c_int32, D, D], C.c_int64),
         "wdem_get_stream": ([h, C.POINTER(C.c_void_p)], C.c_int),
@@ -440,6 +443,17 @@ class Handle:
     def set_queue_depth(self, depth):
         """Steps queued before the host checks the collider trigger (1 = every step)."""
         self.check(self.lib.wdem_set_queue_depth(self.h, int(depth)))
+
+    def set_step_graphs(self, mode):
+        """How queued steps are launched: GRAPHS_OFF (kernel by kernel), GRAPHS_AUTO or GRAPHS_ON (one CUDA
+        graph launch per queue, captured again when the launch arguments change)."""
+        self.check(self.lib.wdem_set_step_graphs(self.h, int(mode)))
+
+    def graph_stats(self):
+        """(captures, replays) of queued-step graphs on this handle."""
+        c, r = C.c_int64(), C.c_int64()
+        self.check(self.lib.wdem_graph_stats(self.h, C.byref(c), C.byref(r)))
+        return c.value, r.value
 
     def keep_geom(self, on):
         self.check(self.lib.wdem_keep_geom(self.h, 1 if on else 0))

@@ -24,8 +24,8 @@
 namespace wdem {
 
 static const unsigned long long HASH_EMPTY = ~0ull;
-static const int QBITS = 24;
-static const unsigned QMAX = (1u << QBITS) - 1;
+// columns of the sweep grid at most (keys of 20 column bits and 12 or more quantisation bits: 4 radix passes)
+static const int SWEEP_MAX_COLS = (1 << 20) - 2;
 
 // ------------------------------------------------------------------------------------------ boxes
 // Bo1_Sphere_Aabb::go / Bo1_Wall_Aabb::go + AabbCollider::updateAabb: pos +- bboxFactor*r,
@@ -162,6 +162,9 @@ __global__ void k_extents(Particles p, const int* small, int nSmall, unsigned lo
   if (threadIdx.x < 15) sh[threadIdx.x] = ~0ull;
   __syncthreads();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
+  // the 15 minima of the warp first (shuffles), then one shared atomic per warp and value
+  unsigned long long v[15];
+  for (int q = 0; q < 15; q++) v[q] = ~0ull;
   if (k < nSmall) {
     int i = small[k];
     double4_32a pr = p.posr[i];
@@ -170,22 +173,31 @@ __global__ void k_extents(Particles p, const int* small, int nSmall, unsigned lo
     double lo[3] = {mn.x, mn.y, mn.z};
     double hi[3] = {mx.x, mx.y, mx.z};
     for (int a = 0; a < 3; a++) {
-      atomicMin(&sh[a], ordKey(c[a]));
-      atomicMin(&sh[3 + a], ~ordKey(c[a]));
-      atomicMin(&sh[6 + a], ordKey(lo[a]));
-      atomicMin(&sh[9 + a], ~ordKey(hi[a]));
-      atomicMin(&sh[12 + a], ~ordKey(hi[a] - lo[a]));
+      v[a] = ordKey(c[a]);
+      v[3 + a] = ~ordKey(c[a]);
+      v[6 + a] = ordKey(lo[a]);
+      v[9 + a] = ~ordKey(hi[a]);
+      v[12 + a] = ~ordKey(hi[a] - lo[a]);
     }
   }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < 15; q++) {
+      const unsigned long long w = __shfl_xor_sync(0xffffffffu, v[q], o);
+      v[q] = w < v[q] ? w : v[q];
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int q = 0; q < 15; q++) atomicMin(&sh[q], v[q]);
   __syncthreads();
   if (threadIdx.x < 15) atomicMin(&ext[threadIdx.x], sh[threadIdx.x]);
 }
 
-__global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxCols, GridParams* g) {
+__global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxCols, int qbits, GridParams* g) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   GridParams G;
   G.nSmall = nSmall;
-  if (nSmall == 0) { G.ok = 0; G.sweepAxis = 0; G.ax1 = 1; G.ax2 = 2; G.ncx = G.ncy = 1; G.lo1 = G.lo2 = 0; G.cell = 1; G.loS = 0; G.invQ = 0; *g = G; return; }
+  G.qbits = qbits;
+  G.qmax = (1u << qbits) - 1;
+  if (nSmall == 0) { G.ok = 0; G.sweepAxis = 0; G.ax1 = 1; G.ax2 = 2; G.ncx = G.ncy = 1; G.lo1 = G.lo2 = 0; G.cell = 1; G.invCell = 1; G.loS = 0; G.invQ = 0; *g = G; return; }
   double cmin[3], cmax[3], bmin[3], bmax[3], w[3];
   for (int a = 0; a < 3; a++) {
     cmin[a] = ordVal(ext[a]);
@@ -217,12 +229,13 @@ __global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxC
   }
   G.sweepAxis = ax; G.ax1 = a1; G.ax2 = a2;
   G.cell = cell;
+  G.invCell = 1.0 / cell;
   G.lo1 = cmin[a1]; G.lo2 = cmin[a2];
   G.ncx = (int)(floor(e1 / cell) + 1);
   G.ncy = (int)(floor(e2 / cell) + 1);
   G.loS = bmin[ax];
   double span = bmax[ax] - bmin[ax];
-  G.invQ = (span > 0 && span < 1e300) ? (double)(QMAX - 1) / span : 0.0;
+  G.invQ = (span > 0 && span < 1e300) ? (double)(G.qmax - 1) / span : 0.0;
   if (!(G.invQ == G.invQ)) G.invQ = 0.0;
   if (!(G.loS == G.loS)) G.loS = 0.0;
   G.ok = 1;
@@ -231,17 +244,20 @@ __global__ void k_grid_setup(const unsigned long long* ext, int nSmall, int maxC
 
 __device__ __forceinline__ double cmp3(const double4_32a& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 
-// monotone non-decreasing quantisation along the sweep axis
+// monotone non-decreasing quantisation along the sweep axis (any such map gives the same pair set: ties
+// are ordered by particle id; coarser steps only lengthen the walks a little)
 __device__ __forceinline__ unsigned quant(double x, const GridParams& G) {
   double t = (x - G.loS) * G.invQ;
   if (!(t > 0)) return 0;                 // also NaN
-  if (t >= (double)QMAX) return QMAX;
+  if (t >= (double)G.qmax) return G.qmax;
   return (unsigned)t;                      // truncation == floor for t >= 0
 }
 
 __device__ __forceinline__ void columnOf(const double4_32a& pr, const GridParams& G, int& cx, int& cy) {
-  double t1 = floor((cmp3(pr, G.ax1) - G.lo1) / G.cell);
-  double t2 = floor((cmp3(pr, G.ax2) - G.lo2) / G.cell);
+  // multiplying by the rounded reciprocal moves a centre at most a few ulp across a column edge: two centres
+  // closer than the widest box (cell = widest box x (1 + 1e-6)) still fall into the same or adjacent columns
+  double t1 = floor((cmp3(pr, G.ax1) - G.lo1) * G.invCell);
+  double t2 = floor((cmp3(pr, G.ax2) - G.lo2) * G.invCell);
   cx = (int)fmin(fmax(t1, 0.0), (double)(G.ncx - 1));
   cy = (int)fmin(fmax(t2, 0.0), (double)(G.ncy - 1));
 }
@@ -256,7 +272,7 @@ __global__ void k_make_keys(Particles p, const int* small, int nSmall, const Gri
   columnOf(p.posr[i], G, cx, cy);
   unsigned long long col = (unsigned long long)cx + (unsigned long long)G.ncx * cy;
   unsigned q = quant(cmp3(p.bbmin[i], G.sweepAxis), G);
-  keys[k] = (col << QBITS) | q;
+  keys[k] = (col << G.qbits) | q;
   vals[k] = (unsigned)i;
 }
 
@@ -409,8 +425,9 @@ __global__ void k_cell_start(const unsigned long long* keys, int nSmall, const G
     return;
   }
   if (s >= nSmall) return;
-  long long c = (long long)(keys[s] >> QBITS);
-  long long cp = s > 0 ? (long long)(keys[s - 1] >> QBITS) : -1;
+  const int qb = g->qbits;
+  long long c = (long long)(keys[s] >> qb);
+  long long cp = s > 0 ? (long long)(keys[s - 1] >> qb) : -1;
   for (long long k = cp + 1; k <= c; k++) cellStart[k] = s;
   if (s == nSmall - 1)
     for (long long k = c + 1; k <= ncols; k++) cellStart[k] = nSmall;
@@ -462,8 +479,12 @@ struct SweepArgs {
   int nSmall;
   unsigned loneMask;
   const int* sceneWall;  // per-scene ranges of the large list (null: one scene)
+  int2* buf;             // SWEEP_BUF pairs per thread, written by the counting pass (null: none kept)
 };
 
+// The sweep runs twice: counting (WRITE false) and writing at the scanned offsets (WRITE true).  With a
+// buffer, the counting pass keeps each thread's first SWEEP_BUF pairs in walk order and the writing pass
+// copies them, walking again only for threads that found more: the output is the same, in the same order.
 template <bool WRITE>
 __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned* counts, int2* out, long long cap,
                         DeviceStatus* st) {
@@ -471,6 +492,24 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
   if (s >= sweepThreads(A.nSmall, A.nLarge)) return;
   unsigned cnt = 0;
   unsigned long long base = WRITE ? counts[s] : 0;
+  if (WRITE && A.buf) {
+    const unsigned found = counts[s + 1] - counts[s];
+    if (found <= (unsigned)SWEEP_BUF) {
+      const int2* b = A.buf + (long long)s * SWEEP_BUF;
+      for (unsigned k = 0; k < found; k++)
+        if (base + k < (unsigned long long)cap) out[base + k] = b[k];
+      return;
+    }
+  }
+  auto emit = [&](int2 pr) {
+    if (WRITE) {
+      const unsigned long long o = base + cnt;
+      if (o < (unsigned long long)cap) out[o] = pr;
+    } else if (A.buf && cnt < (unsigned)SWEEP_BUF) {
+      A.buf[(long long)s * SWEEP_BUF + cnt] = pr;
+    }
+    cnt++;
+  };
   if (s >= A.nSmall) {
     // large-large pairs, one thread per large body a: the bodies after it in the large list up to the
     // first one of another scene (the list is grouped by scene)
@@ -485,8 +524,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
         if (sceneOf(mi.x) != sceneOf(mj.x)) break;
         if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
         if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
-        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
-        cnt++;
+        emit(orient(i, j, mi.x & 15, mj.x & 15));
       }
     }
     if (!WRITE) counts[s] = cnt;
@@ -498,9 +536,9 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
   int4 mi = p.meta[i];
   double4_32a mn = p.bbmin[i], mx = p.bbmax[i];
   const float4 fmn = A.rec[2 * s], fmx = A.rec[2 * s + 1];
-  unsigned qi = (unsigned)(key & QMAX);
+  unsigned qi = (unsigned)(key & G.qmax);
   unsigned qmax = quant(cmp3(mx, G.sweepAxis), G);
-  long long col = (long long)(key >> QBITS);
+  long long col = (long long)(key >> G.qbits);
   int cx = (int)(col % G.ncx), cy = (int)(col / G.ncx);
   for (int dy = -1; dy <= 1; dy++) {
     int y = cy + dy;
@@ -513,7 +551,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
       int q;
       if (c2 == col) q = s + 1;
       else {
-        unsigned long long target = ((unsigned long long)c2 << QBITS) | qi;
+        unsigned long long target = ((unsigned long long)c2 << G.qbits) | qi;
         int lo = beg, hi = end;
         while (lo < hi) { int mid = (lo + hi) >> 1; if (A.keys[mid] < target) lo = mid + 1; else hi = mid; }
         q = lo;
@@ -521,7 +559,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
       }
       for (; q < end; q++) {
         unsigned long long kq = A.keys[q];
-        if ((unsigned)(kq & QMAX) > qmax) break;
+        if ((unsigned)(kq & G.qmax) > qmax) break;
         const float4 gmn = A.rec[2 * q], gmx = A.rec[2 * q + 1];
         const unsigned maskj = __float_as_uint(gmn.w);
         const int metaxj = __float_as_int(gmx.w);
@@ -530,8 +568,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
         if (!overlapF(fmn, fmx, gmn, gmx)) continue;
         int j = (int)A.vals[q];
         if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
-        if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, metaxj & 15); }
-        cnt++;
+        emit(orient(i, j, mi.x & 15, metaxj & 15));
       }
     }
   }
@@ -542,8 +579,7 @@ __global__ void k_sweep(Particles p, SweepArgs A, const GridParams* g, unsigned*
     int4 mj = p.meta[j];
     if (!mayCollide((unsigned)mi.z, (unsigned)mj.z, A.loneMask)) continue;
     if (!overlap3(mn, mx, p.bbmin[j], p.bbmax[j])) continue;
-    if (WRITE) { unsigned long long o = base + cnt; if (o < (unsigned long long)cap) out[o] = orient(i, j, mi.x & 15, mj.x & 15); }
-    cnt++;
+    emit(orient(i, j, mi.x & 15, mj.x & 15));
   }
   if (!WRITE) counts[s] = cnt;
 }
@@ -950,18 +986,27 @@ namespace wdem {
 
 
 static int bitsFor(unsigned long long v) { int b = 0; while ((1ull << b) < v) b++; return b < 1 ? 1 : b; }
+// the sweep grid's column cap and the quantisation bits of its keys: column bits + qbits fill 32, 40 or 48
+// bits (4, 5 or 6 radix passes), with at least 12 quantisation bits and at most 24
+static int sweepCols(const ColliderScratch& cs) { return std::min(cs.maxCols, SWEEP_MAX_COLS); }
+static int sweepQbits(const ColliderScratch& cs) {
+  const int cb = bitsFor((unsigned long long)sweepCols(cs) + 1);
+  int total = 32;
+  while (total - cb < 12) total += 8;
+  return std::min(24, total - cb);
+}
 
 // The collider sub-steps are called from wdem_api.cu through these thin wrappers.
 void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
   unsigned long long* ext = (unsigned long long*)cs.temp;
   (k_extents_init<<<1, 32, 0, s>>>(ext), ++::wdem::g_kernel_launches);
   if (nSmall > 0) (k_extents<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, ext), ++::wdem::g_kernel_launches);
-  (k_grid_setup<<<1, 1, 0, s>>>(ext, nSmall, cs.maxCols, cs.grid), ++::wdem::g_kernel_launches);
+  (k_grid_setup<<<1, 1, 0, s>>>(ext, nSmall, sweepCols(cs), sweepQbits(cs), cs.grid), ++::wdem::g_kernel_launches);
 }
 
 void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs) {
   if (nSmall > 0) (k_make_keys<<<(nSmall + 255) / 256, 256, 0, s>>>(p, small, nSmall, cs.grid, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
-  int bits = QBITS + bitsFor((unsigned long long)cs.maxCols + 1);
+  int bits = sweepQbits(cs) + bitsFor((unsigned long long)sweepCols(cs) + 1);
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, nSmall, bits, cs);
   int threads = nSmall > 0 ? nSmall : (cs.maxCols + 1);
   (k_cell_start<<<(threads + 255) / 256, 256, 0, s>>>(cs.keys, nSmall, cs.grid, cs.cellStart), ++::wdem::g_kernel_launches);
@@ -975,6 +1020,7 @@ void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, Colli
   A.keys = cs.keys; A.vals = cs.vals; A.cellStart = cs.cellStart; A.large = cs.large; A.nLarge = cs.nLarge;
   A.nSmall = nSmall; A.loneMask = loneMask;
   A.sceneWall = cs.nScenes > 1 ? cs.sceneWall : nullptr;
+  A.buf = cs.sweepBufCap >= sweepThreads(nSmall, cs.nLarge) ? cs.sweepBuf : nullptr;
   const int threads = sweepThreads(nSmall, cs.nLarge);
   if (write) (k_sweep<true><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);
   else (k_sweep<false><<<(threads + 127) / 128, 128, 0, s>>>(p, A, cs.grid, cs.counts, out, cap, st), ++::wdem::g_kernel_launches);

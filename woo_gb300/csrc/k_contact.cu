@@ -636,7 +636,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     // new CPhys (ContactLoop.cpp:179-180)
     cp2<CP2>(P, matA, matB, r1, r2, V1.w, V2.w, kn, kt, tanPhi, hz);
     fx = 0; fy = 0; fz = 0;
-    c.step0[i] = (int)P.step;
+    c.step0[i] = (int)stepOf(P, st);
   } else {
     // update (L6Geom.cpp:79-216)
     const d3 prevNormal = mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
@@ -657,7 +657,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     d3 mid2 = cross(mid0, mid1);
     cur0 = currNormal;
     cur1 = prevT1 - cross(mid1, rt);
-    if (P.trsfRenorm > 0 && (P.step % P.trsfRenorm) == 0) {
+    if (P.trsfRenorm > 0 && (stepOf(P, st) % P.trsfRenorm) == 0) {
       cur0 = normalized(cur0);
       cur1 = cur1 - cur0 * dot(cur1, cur0);
       cur1 = normalized(cur1);
@@ -841,7 +841,7 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   // each particle's share at its CSR entry, stamped with this pass; a facet (pA) takes none
   // (ContactLoop::applyForceUninodal skips shapes with more than one node, ContactLoop.cpp:270-276)
   const int2 sl = c.slot[i];
-  const double stamp = __longlong_as_double(P.seq);
+  const double stamp = __longlong_as_double(seqOf(P, st));
   if (PERI || !(sb & CS_FACET)) {
     double4_32a* oa = c.out + OUT_RECORDS * (long long)sl.x;
     oa[OUT_F] = make_double4_32a(F.x, F.y, F.z, stamp);
@@ -992,7 +992,7 @@ __global__ void __launch_bounds__(BS) k_contacts_cull(StepParams P, Particles p,
   const long long first = (long long)blockIdx.x * blockDim.x;
   const long long m = FULL ? nc : (long long)st->actCount;
   // a step queued behind a collider trigger: the work list stays empty, so the heavy pass is a no-op too
-  if (haltedContacts(st, P.step)) return;
+  if (haltedContacts(st, stepOf(P, st))) return;
   // the integrator's lists of this step have been consumed: their counters start the next step at 0
   if (first + threadIdx.x == 0) { st->rotCount = 0; st->touchCount = 0; }
   const long long stride = FULL ? m + 1 : (long long)gridDim.x * blockDim.x;
@@ -1051,7 +1051,7 @@ void launch_contacts(cudaStream_t s, const StepParams& P, Particles p, Contacts 
   if (P.hasEll) {
     // ellipsoid scenes: aperiodic, FrictMat + IdealElPl (checked on the host)
     launchCull<false, true>(s, P, p, c, nc, count, st, full);
-    if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF, P.warmStart == WDEM_WARM_HISTORY_MLP);
+    if (warmBf) mlp_launch_warm(s, p, c, nc, c.work, count, warmBf, warmF, P.warmStart == WDEM_WARM_HISTORY_MLP, st, P.numSMs);
     launchHeavy<WDEM_LAW_IDEALELPL, WDEM_CP2_FRICT, false, true>(s, P, p, c, nc, count, st);
   } else if (P.periodic) {
     launchCull<true, false>(s, P, p, c, nc, count, st, full);

@@ -19,8 +19,7 @@ WDEM_VARIANT_BEGIN
 // F = m g (unless gravitySkip) + sum of contact forces; T = sum of contact torques
 // Contact forces and torques of particle i from the previous contact pass: its CSR row's records, in the
 // row's order (the partner ids'), those stamped by that pass only (contacts real after it).
-__device__ __forceinline__ void gatherRow(const StepParams& P, int i, const Contacts& c, const Csr& csr, d3& F, d3& T) {
-  const long long want = P.seq - 1;
+__device__ __forceinline__ void gatherRow(long long want, int i, const Contacts& c, const Csr& csr, d3& F, d3& T) {
   const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
   for (int e = e0; e < e1; e++) {
     const double4_32a* o = c.out + OUT_RECORDS * (long long)e;
@@ -31,8 +30,8 @@ __device__ __forceinline__ void gatherRow(const StepParams& P, int i, const Cont
   }
 }
 
-__device__ __forceinline__ void gatherForce(const StepParams& P, int i, double mass, unsigned flags, const Contacts& c,
-                                            const Csr& csr, d3& F, d3& T) {
+__device__ __forceinline__ void gatherForce(const StepParams& P, long long want, int i, double mass, unsigned flags,
+                                            const Contacts& c, const Csr& csr, d3& F, d3& T) {
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
   if (grav) {
     // mass * g; a component of g that is exactly zero gives a zero of the sign of the (finite) mass,
@@ -43,7 +42,7 @@ __device__ __forceinline__ void gatherForce(const StepParams& P, int i, double m
     F.z = (zeroBits(P.gravity[2]) && mf) ? signedZero(mass, P.gravity[2]) : mass * P.gravity[2];
   } else F = mk(0, 0, 0);
   T = mk(0, 0, 0);
-  gatherRow(P, i, c, csr, F, T);
+  gatherRow(want, i, c, csr, F, T);
 }
 
 // Raises the collider trigger.  All particles of a free-falling cloud cross the verlet distance in the
@@ -131,7 +130,8 @@ __device__ __noinline__ double asphericalErot(qd ori, d3 inertia, d3 w) {
 template <bool FROM_ARRAYS, bool PERI, bool ELL>
 __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || haltedIntegrator(st, P.step)) return;
+  const long long step = stepOf(P, st);
+  if (i >= n || haltedIntegrator(st, step)) return;
   const int4 meta = p.meta[i];
   const unsigned flags = (unsigned)meta.w;
   const bool asph = ELL && (meta.x & META_ASPH);
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
     F = xyz(p.force[i]);
     T = xyz(p.torque[i]);
   } else if (!blockedAll) {
-    gatherForce(P, i, mass, flags, c, csr, F, T);
+    gatherForce(P, seqOf(P, st) - 1, i, mass, flags, c, csr, F, T);
   } else {
     // the force on a fully blocked node changes nothing in its motion; it is materialised only
     // when downloaded (k_reduce_forces)
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   const double4_32a lp = p.lastPos[i];
   const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
   if (!ELL) {
-    raiseDirty(st, sqnorm(dd) > P.maxD2, P.step);
+    raiseDirty(st, sqnorm(dd) > P.maxD2, step);
   } else {
     // rotation-aware trigger for bounds that track it (maxRot >= 0; Collision.cpp:94-121)
     double moveDueToRot2 = 0.;
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
       moveDueToRot2 = mv * mv;
     }
     const double d2 = sqnorm(dd);
-    raiseDirty(st, dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2, P.step);
+    raiseDirty(st, dirty || (d2 > 0. ? d2 : 0.) + moveDueToRot2 > P.maxD2, step);
   }
 }
 
@@ -424,7 +424,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
              gravForce(mass, mf, P.gravity[2], skipAxis == 2));
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
-    if (touchedNow) gatherRow(P, i, c, csr, F, T);
+    if (touchedNow) gatherRow(seqOf(P, st) - 1, i, c, csr, F, T);
   } else {
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }
@@ -599,7 +599,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
     const d3 dd = mk(lp.x, lp.y, lp.z) - pos;
     dirty = sqnorm(dd) > P.maxD2;
   }
-  raiseDirty(st, dirty, P.step);
+  raiseDirty(st, dirty, stepOf(P, st));
 }
 
 // First pass: particles without contact forces this step.  Those that a real contact touched are
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_leapfrog_fast(StepParams P, P
   // all of the particle's loads are issued together, before the guard's and the list decision
   const FastRec rec = loadFast(p, i);
   const uint8_t tch = p.touched[i];
-  if (haltedIntegrator(st, P.step)) return;
+  if (haltedIntegrator(st, stepOf(P, st))) return;
   const bool listed = ((unsigned)rec.meta.w & 63u) != 63u && tch != 0;
   const unsigned am = __activemask();
   const unsigned b = __ballot_sync(am, listed);
@@ -634,7 +634,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_leapfrog_fast(StepParams P, P
 template <bool PERI>
 __global__ void __launch_bounds__(256) k_leapfrog_lists(StepParams P, Particles p, int n, Contacts c, Csr csr,
                                                          DeviceStatus* st) {
-  if (haltedIntegrator(st, P.step)) return;
+  if (haltedIntegrator(st, stepOf(P, st))) return;
   const unsigned nt = st->touchCount < (unsigned)n ? st->touchCount : (unsigned)n;
   const unsigned nr = st->rotCount < (unsigned)n ? st->rotCount : (unsigned)n;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nt + nr; k += gridDim.x * blockDim.x) {
@@ -761,7 +761,7 @@ __global__ void k_reduce_forces(StepParams P, Particles p, int n, Contacts c, Cs
   if (i >= n) return;
   const int4 meta = p.meta[i];
   d3 F, T;
-  gatherForce(P, i, p.velm[i].w, (unsigned)meta.w, c, csr, F, T);
+  gatherForce(P, P.seq - 1, i, p.velm[i].w, (unsigned)meta.w, c, csr, F, T);
   p.force[i] = make_double4_32a(F.x, F.y, F.z, 0);
   p.torque[i] = make_double4_32a(T.x, T.y, T.z, 0);
 }

@@ -6,12 +6,13 @@
 // contact point in A's frame.  Its lambda starts the Newton solve (WDEM_WARM_MLP); the solve falls
 // back to the cold start when it has not converged after fallbackIters iterations.
 //
-// Arithmetic: BF16 operands, FP32 accumulation, on the tensor cores through mma.sync.m16n8k16 (one
-// warp = 16 samples; activations stay in shared memory between layers).  Rounding points, which the
-// CPU reference of the network follows: inputs, weights and post-ReLU activations are rounded to BF16;
-// biases, pre-activations and outputs stay FP32.  Training runs the backward pass with the same
-// fragments (BF16 operands: activations, dZ, weights; FP32 accumulation), sums the gradient of a
-// mini-batch per block in shared memory, and applies Adam (Kingma & Ba 2015) to FP32 master weights.
+// Arithmetic: BF16 operands, FP32 accumulation, on the tensor cores.  Rounding points, which the CPU
+// reference of the network follows: inputs, weights and post-ReLU activations are rounded to BF16;
+// biases, pre-activations and outputs stay FP32.  Inference (the warm start of the contact pass and
+// wdem_warm_predict) runs on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
+// memory, k_mlp_tc).  Training runs forward and backward with warp-level mma.sync.m16n8k16 (one warp =
+// 16 samples, activations in shared memory; BF16 operands: activations, dZ, weights), sums the gradient
+// of a mini-batch per block in shared memory, and applies Adam (Kingma & Ba 2015) to FP32 master weights.
 //
 // Parameter layout on the device (padded): W1[16][64] (input rows 13..15 zero), b1[64], W2[64][64],
 // b2[64], W3[64][64], b3[64], W4[64][8] (output columns 4..7 zero), b4[8]; W[l][in][out] row-major.
@@ -135,82 +136,6 @@ __device__ __forceinline__ void loadNet(NetSmem& net, const uint16_t* wbf, const
     net.b[k] = wf[off];
   }
   __syncthreads();
-}
-
-// ------------------------------------------------------------------------------ inference
-// lam0 of every ellipsoid pair (sphere + ellipsoid included; walls excluded) that the contact kernel
-// may solve this step; other entries are NaN (cold start).  onlyFresh: pairs that carry the previous
-// step's maximiser (c.lam in (0, 1)) get NaN as well (the solve starts from that), and a warp whose 16
-// pairs all carry one skips the network.
-__global__ void __launch_bounds__(128) k_mlp_warm(Particles p, Contacts c, const unsigned* work, const unsigned* count,
-                                                  long long ncon, const uint16_t* wbf, const float* wf, int onlyFresh) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
-  WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
-  loadNet(net, wbf, wf);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  WarpSmem& ws = wsAll[warp];
-  const long long nw = workLen(count);
-  for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < nw; base += (long long)gridDim.x * SAMPLES) {
-    const long long kw = base + (lane & 15);
-    const long long i = kw < nw ? (long long)workItem(work, count, ncon, (unsigned)kw) : -1;
-    bool use = false;
-    if (lane < 16) {
-      float f[ELL_FEATURES];
-      for (int k = 0; k < ELL_FEATURES; k++) f[k] = 0.f;
-      if (i >= 0) {
-        const uint8_t sb = c.state[i] & CS_SHAPES;
-        const bool hasLam = onlyFresh && c.lam && c.lam[i] > 0 && c.lam[i] < 1;
-        const int2 id = c.ids[i];
-        const bool ellPair = (p.meta[id.x].x & 15) != WDEM_SHAPE_CAPSULE && (p.meta[id.y].x & 15) != WDEM_SHAPE_CAPSULE;
-        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && ellPair && (c.state[i] & CS_MASK) != CS_DEAD && !hasLam) {
-          const double4_32a OA = p.ori[id.x], OB = p.ori[id.y];
-          qd oa, ob;
-          oa.w = OA.x; oa.x = OA.y; oa.y = OA.z; oa.z = OA.w;
-          ob.w = OB.x; ob.x = OB.y; ob.y = OB.z; ob.z = OB.w;
-          const d3 R = xyz(p.posr[id.y]) - xyz(p.posr[id.x]);
-          ellFeatures(oa, xyz(p.semi[id.x]), ob, xyz(p.semi[id.y]), R, f);
-          use = true;
-        }
-      }
-      for (int k = 0; k < 16; k++) ws.x[(lane & 15) * 16 + k] = bf(k < ELL_FEATURES ? f[k] : 0.f);
-    }
-    __syncwarp();
-    if (__ballot_sync(0xffffffffu, use) == 0) {
-      // no pair of this warp needs the network
-      if (lane < 16 && i >= 0) c.lam0[i] = __int_as_float(0x7fffffff);
-      __syncwarp();
-      continue;
-    }
-    forward(net, ws, g, t);
-    if (lane < 16 && i >= 0) {
-      float l = ws.out[(lane & 15) * 8 + 0];
-      l = fminf(fmaxf(l, 1e-3f), 1.f - 1e-3f);
-      c.lam0[i] = use ? l : __int_as_float(0x7fffffff);
-    }
-    __syncwarp();
-  }
-}
-
-// Arbitrary feature rows (n x 13) -> outputs (n x 4), for tests and tools.
-__global__ void __launch_bounds__(128) k_mlp_predict(const float* X, long long n, float* Y, const uint16_t* wbf,
-                                                     const float* wf) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
-  WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
-  loadNet(net, wbf, wf);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  WarpSmem& ws = wsAll[warp];
-  for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < n; base += (long long)gridDim.x * SAMPLES) {
-    const long long i = base + (lane & 15);
-    if (lane < 16)
-      for (int k = 0; k < 16; k++) ws.x[lane * 16 + k] = bf((i < n && k < ELL_FEATURES) ? X[i * ELL_FEATURES + k] : 0.f);
-    __syncwarp();
-    forward(net, ws, g, t);
-    if (lane < 16 && i < n)
-      for (int k = 0; k < ELL_TARGETS; k++) Y[i * ELL_TARGETS + k] = ws.out[lane * 8 + k];
-    __syncwarp();
-  }
 }
 
 // ------------------------------------------------------------------------------ training
@@ -343,6 +268,238 @@ __global__ void k_to_bf16(const float* w, uint16_t* wbf, int n) {
   if (k < n) wbf[k] = bf(w[k]);
 }
 
+// ------------------------------------------------------------------------------ inference on tcgen05
+// The same network for tiles of 128 samples on the 5th-generation tensor cores: one CTA of 4 warps per
+// tile (thread t owns sample t), BF16 operands in shared memory, FP32 accumulators in tensor memory (TMEM),
+// one elected thread issuing tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) and committing to
+// an mbarrier; the epilogue of each layer (bias, ReLU, BF16 rounding) reads the accumulator rows back with
+// tcgen05.ld and writes the next layer's A operand.  Rounding points as in the mma.sync path; only the
+// order of the FP32 additions inside the tensor core may differ.
+//
+// Operand layout: the canonical K-major layout without swizzling, 8 x 16-byte core matrices; element
+// (r, k) of an R x K operand at (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2 bytes, with
+// LBO = 128 (core matrices adjacent along K) and SBO = K / 8 * 128 (the next 8 rows).  A holds the
+// samples (rows) x inputs, B the outputs (rows) x inputs, i.e. W transposed.
+constexpr int TC_M = 128;            // samples per tile
+constexpr int TC_N4 = 16;            // output layer padded to the smallest N for M = 128
+constexpr int TC_W1 = 0;                          // B of layer 1: 64 x 16
+constexpr int TC_W2 = TC_W1 + H * 16 * 2;         // B of layer 2: 64 x 64
+constexpr int TC_W3 = TC_W2 + H * H * 2;          // B of layer 3
+constexpr int TC_W4 = TC_W3 + H * H * 2;          // B of layer 4: 16 x 64
+constexpr int TC_X = TC_W4 + TC_N4 * H * 2;       // A of layer 1: 128 x 16
+constexpr int TC_H = TC_X + TC_M * 16 * 2;        // A of layers 2-4: 128 x 64
+constexpr int TC_B = TC_H + TC_M * H * 2;         // biases, FP32: b1, b2, b3 (64 each), b4 (16)
+constexpr int TC_BAR = TC_B + (3 * H + TC_N4) * 4;  // mbarrier (8 bytes)
+constexpr int TC_TMEM = TC_BAR + 8;               // TMEM base address written by tcgen05.alloc
+constexpr size_t SMEM_TC = TC_TMEM + 8 + 1024;    // + alignment slack of the dynamic base
+constexpr unsigned TC_COLS = 64;                  // TMEM columns: one 128 x 64 FP32 accumulator
+constexpr long long TC_SPIN = 1ll << 26;          // bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t kmajorOff(int r, int k, int K) {
+  return (uint32_t)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+// tcgen05 shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
+// the fixed 0b001 at bits 46-48, base offset 0, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t tcDesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9 and 10-12 = 1), both
+// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+__host__ __device__ constexpr uint32_t tcIdesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tcMma(uint32_t dTmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dTmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tcCommit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// waits for the mbarrier phase `parity` to complete; false after TC_SPIN polls
+__device__ __forceinline__ bool tcWait(uint32_t bar, unsigned parity) {
+  for (long long it = 0; it < TC_SPIN; it++) {
+    unsigned done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tcFenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tcFenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxyFence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive accumulator columns of this thread's row (warp w reads TMEM lanes 32 w .. 32 w + 31)
+__device__ __forceinline__ void tcLoad16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
+}
+
+// one layer: D = A (128 x K, at aOff) x B^T (N x K, at bOff), issued by thread 0, waited for by all;
+// false when the wait gave up
+template <int K, int N>
+__device__ __forceinline__ bool tcLayer(unsigned char* sm, int aOff, int bOff, uint32_t dTmem, uint32_t bar,
+                                        unsigned& phase) {
+  proxyFence();  // this thread's st.shared of the operands, visible to the tensor core
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (threadIdx.x == 0) {
+    const uint32_t a0 = smemAddr(sm + aOff), b0 = smemAddr(sm + bOff);
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ks++)
+      tcMma(dTmem, tcDesc(a0 + 256 * ks, 128, K / 8 * 128), tcDesc(b0 + 256 * ks, 128, K / 8 * 128), tcIdesc(TC_M, N),
+            ks > 0 ? 1 : 0);
+    tcCommit(smemAddr(sm + TC_BAR));
+  }
+  const bool ok = tcWait(bar, phase);
+  phase ^= 1u;
+  tcFenceAfter();
+  return __syncthreads_and(ok) != 0;  // the same answer in every thread: all leave the tile loop together
+}
+
+// hidden-layer epilogue: this thread's accumulator row + bias, ReLU, BF16, into row t of the 128 x 64 A tile
+__device__ __forceinline__ void tcHidden(unsigned char* sm, uint32_t tRow, const float* bias, int t) {
+#pragma unroll
+  for (int c = 0; c < H; c += 16) {
+    float v[16];
+    tcLoad16(tRow + c, v);
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      w[k] = pk(bf(fmaxf(v[2 * k] + bias[c + 2 * k], 0.f)), bf(fmaxf(v[2 * k + 1] + bias[c + 2 * k + 1], 0.f)));
+    *reinterpret_cast<uint4*>(sm + TC_H + kmajorOff(t, c, H)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(sm + TC_H + kmajorOff(t, c + 8, H)) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
+// The network over tiles of 128 samples.  WORK: the samples are the contact work list (features from the
+// particle state, as k_mlp_warm; lam0 written); otherwise feature rows X -> output rows Y.
+template <bool WORK>
+__global__ void __launch_bounds__(128, 1) k_mlp_tc(Particles p, Contacts c, const unsigned* work, const unsigned* count,
+                                                   long long ncon, const float* X, long long nx, float* Y,
+                                                   const uint16_t* wbf, const float* wf, int onlyFresh,
+                                                   DeviceStatus* st) {
+  extern __shared__ unsigned char smRaw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smRaw) + 1023) & ~uintptr_t(1023));
+  const int t = threadIdx.x, warp = t >> 5;
+  // weights as B operands (W transposed: output rows, input columns), biases
+  for (int e = t; e < H * 16; e += blockDim.x) {
+    const int n = e / 16, k = e % 16;
+    *reinterpret_cast<uint16_t*>(sm + TC_W1 + kmajorOff(n, k, 16)) = wbf[OFF_W1 + k * H + n];
+  }
+  for (int e = t; e < H * H; e += blockDim.x) {
+    const int n = e / H, k = e % H;
+    *reinterpret_cast<uint16_t*>(sm + TC_W2 + kmajorOff(n, k, H)) = wbf[OFF_W2 + k * H + n];
+    *reinterpret_cast<uint16_t*>(sm + TC_W3 + kmajorOff(n, k, H)) = wbf[OFF_W3 + k * H + n];
+  }
+  for (int e = t; e < TC_N4 * H; e += blockDim.x) {
+    const int n = e / H, k = e % H;
+    *reinterpret_cast<uint16_t*>(sm + TC_W4 + kmajorOff(n, k, H)) = n < 8 ? wbf[OFF_W4 + k * 8 + n] : (uint16_t)0;
+  }
+  float* bias = reinterpret_cast<float*>(sm + TC_B);
+  for (int e = t; e < 3 * H + TC_N4; e += blockDim.x) {
+    const int l = e / H, j = e % H;
+    bias[e] = l == 0 ? wf[OFF_B1 + j] : (l == 1 ? wf[OFF_B2 + j] : (l == 2 ? wf[OFF_B3 + j] : (j < 8 ? wf[OFF_B4 + j] : 0.f)));
+  }
+  const uint32_t bar = smemAddr(sm + TC_BAR);
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(sm + TC_TMEM)),
+                 "r"(TC_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + TC_TMEM);
+  const uint32_t tRow = tmem + ((uint32_t)(32 * warp) << 16);  // this thread's accumulator row (lane 32 w + lane)
+  unsigned phase = 0;
+  bool ok = true;
+  const long long n = WORK ? (long long)workLen(count) : nx;
+  for (long long base = (long long)blockIdx.x * TC_M; base < n && ok; base += (long long)gridDim.x * TC_M) {
+    const long long s = base + t;
+    long long i = -1;
+    bool use = false;
+    float f[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) f[k] = 0.f;
+    if (WORK) {
+      i = s < n ? (long long)workItem(work, count, ncon, (unsigned)s) : -1;
+      if (i >= 0) {
+        const uint8_t sb = c.state[i] & CS_SHAPES;
+        const bool hasLam = onlyFresh && c.lam && c.lam[i] > 0 && c.lam[i] < 1;
+        const int2 id = c.ids[i];
+        const bool ellPair = (p.meta[id.x].x & 15) != WDEM_SHAPE_CAPSULE && (p.meta[id.y].x & 15) != WDEM_SHAPE_CAPSULE;
+        if ((sb & CS_ELL) && !(sb & CS_WALL_A) && ellPair && (c.state[i] & CS_MASK) != CS_DEAD && !hasLam) {
+          const double4_32a OA = p.ori[id.x], OB = p.ori[id.y];
+          qd oa, ob;
+          oa.w = OA.x; oa.x = OA.y; oa.y = OA.z; oa.z = OA.w;
+          ob.w = OB.x; ob.x = OB.y; ob.y = OB.z; ob.z = OB.w;
+          const d3 R = xyz(p.posr[id.y]) - xyz(p.posr[id.x]);
+          ellFeatures(oa, xyz(p.semi[id.x]), ob, xyz(p.semi[id.y]), R, f);
+          use = true;
+        }
+      }
+    } else if (s < n) {
+      for (int k = 0; k < ELL_FEATURES; k++) f[k] = X[s * ELL_FEATURES + k];
+      use = true;
+    }
+    // a tile none of whose pairs needs the network: cold starts only
+    if (!__syncthreads_or(use)) {
+      if (WORK && i >= 0) c.lam0[i] = __int_as_float(0x7fffffff);
+      continue;
+    }
+    uint32_t xw[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) xw[k] = pk(bf(f[2 * k]), bf(f[2 * k + 1]));
+    *reinterpret_cast<uint4*>(sm + TC_X + kmajorOff(t, 0, 16)) = make_uint4(xw[0], xw[1], xw[2], xw[3]);
+    *reinterpret_cast<uint4*>(sm + TC_X + kmajorOff(t, 8, 16)) = make_uint4(xw[4], xw[5], xw[6], xw[7]);
+    if (!(ok = tcLayer<16, H>(sm, TC_X, TC_W1, tmem, bar, phase))) break;
+    tcHidden(sm, tRow, bias, t);
+    if (!(ok = tcLayer<H, H>(sm, TC_H, TC_W2, tmem, bar, phase))) break;
+    tcHidden(sm, tRow, bias + H, t);
+    if (!(ok = tcLayer<H, H>(sm, TC_H, TC_W3, tmem, bar, phase))) break;
+    tcHidden(sm, tRow, bias + 2 * H, t);
+    if (!(ok = tcLayer<H, TC_N4>(sm, TC_H, TC_W4, tmem, bar, phase))) break;
+    float o[16];
+    tcLoad16(tRow, o);
+    if (WORK) {
+      if (i >= 0) {
+        const float l = fminf(fmaxf(o[0] + bias[3 * H], 1e-3f), 1.f - 1e-3f);
+        c.lam0[i] = use ? l : __int_as_float(0x7fffffff);
+      }
+    } else if (s < n) {
+      for (int k = 0; k < ELL_TARGETS; k++) Y[s * ELL_TARGETS + k] = o[k] + bias[3 * H + k];
+    }
+    tcFenceBefore();  // the accumulator reads are done before the next tile's first MMA overwrites it
+  }
+  if (!ok && t == 0) {
+    atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT);
+    st->detail = -1;
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
+}
+
 constexpr size_t SMEM_INFER = sizeof(NetSmem) + WARPS * sizeof(WarpSmem);
 constexpr size_t SMEM_TRAIN = SMEM_INFER + NPAD * sizeof(float);
 
@@ -378,8 +535,8 @@ void mlp_pack(const float* pad, float* pub) {
 
 cudaError_t mlp_prepare_kernels() {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_mlp_warm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_INFER))) return e;
-  if ((e = cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_INFER))) return e;
+  if ((e = cudaFuncSetAttribute(k_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC))) return e;
+  if ((e = cudaFuncSetAttribute(k_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC))) return e;
   return cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TRAIN);
 }
 
@@ -388,19 +545,24 @@ void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf) {
 }
 
 void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
-                     const uint16_t* wbf, const float* wf, bool onlyFresh) {
+                     const uint16_t* wbf, const float* wf, bool onlyFresh, DeviceStatus* st, int numSMs) {
   if (nc <= 0) return;
-  long long blocks = (nc + SAMPLES - 1) / SAMPLES;
-  if (blocks > 152 * 2) blocks = 152 * 2;  // persistent blocks: the weights are loaded once per block
-  (k_mlp_warm<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(p, c, work, count, nc, wbf, wf, onlyFresh ? 1 : 0),
+  long long blocks = (nc + TC_M - 1) / TC_M;
+  const long long cap = 2ll * (numSMs > 0 ? numSMs : 152);  // persistent blocks: weights staged once per block
+  if (blocks > cap) blocks = cap;
+  (k_mlp_tc<true><<<(unsigned)blocks, 128, SMEM_TC, s>>>(p, c, work, count, nc, nullptr, 0, nullptr, wbf, wf,
+                                                          onlyFresh ? 1 : 0, st),
    ++::wdem::g_kernel_launches);
 }
 
-void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf) {
+void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf,
+                        DeviceStatus* st) {
   if (n <= 0) return;
-  long long blocks = (n + SAMPLES - 1) / SAMPLES;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  (k_mlp_predict<<<(unsigned)blocks, 128, SMEM_INFER, s>>>(X, n, Y, wbf, wf), ++::wdem::g_kernel_launches);
+  long long blocks = (n + TC_M - 1) / TC_M;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  (k_mlp_tc<false><<<(unsigned)blocks, 128, SMEM_TC, s>>>(Particles{}, Contacts{}, nullptr, nullptr, 0, X, n, Y, wbf, wf,
+                                                           0, st),
+   ++::wdem::g_kernel_launches);
 }
 
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,

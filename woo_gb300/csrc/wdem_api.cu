@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -170,6 +171,17 @@ struct wdem_handle {
   int maxAhead = 32;
   double rebuildInterval = 16;
   int sinceRebuild = 0;
+  // queued steps replayed from CUDA graphs: one executable graph per (queue length, first cull full or
+  // not), valid while the launch arguments it was captured with (sig) are unchanged; the steps' numbers
+  // come from DeviceStatus.stepBase/seqBase, written before each replay
+  struct StepGraph {
+    std::vector<unsigned char> sig;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;  // kernel nodes of the graph
+  };
+  std::map<int, StepGraph> graphs;
+  int graphMode = WDEM_GRAPHS_OFF;
+  long long graphCaptures = 0, graphReplays = 0;
   // DynDt as a PeriodicEngine (Engine.hpp:130-160): stepLast / stepPrev, Scene.nextDt, last critical step
   long long dynStepLast = -1, dynStepPrev = -1;
   double nextDt = std::numeric_limits<double>::quiet_NaN();
@@ -378,6 +390,13 @@ int ensureScratch(wdem_handle* h, long long nc) {
     CK(dalloc(cs.periCi, (size_t)h->N + 1)); CK(dalloc(cs.periHi, (size_t)h->N + 1));
     cs.periCap = cap;
   }
+  // the counting sweep's pair buffer (not used by the periodic collider)
+  const long long nSweepT = sweepThreads((int)h->smallIds.size(), cs.nLarge);
+  if (!h->periodic && nSweepT > cs.sweepBufCap) {
+    const long long cap = std::max<long long>(nSweepT, cs.sweepBufCap * 5 / 4);
+    CK(dalloc(cs.sweepBuf, (size_t)cap * SWEEP_BUF));
+    cs.sweepBufCap = cap;
+  }
   long long needRetain = std::max<long long>(h->nContacts, nc) + 2;
   if (needRetain > cs.retainCap) {
     long long cap = std::max<long long>(needRetain, cs.retainCap * 3 / 2);
@@ -452,6 +471,8 @@ int checkDeviceStatus(wdem_handle* h) {
     else if (code == WDEM_ERR_UNSUPPORTED)
       m = "sphere-facet contact with the projected centre outside all three edges of Facet #" +
           std::to_string(h->hst->detail) + " (degenerate facet)";
+    else if (code == WDEM_ERR_TIMEOUT && h->hst->detail == -1)
+      m = "the tensor-core warm-start network did not complete within its wait limit";
     else if (code == WDEM_ERR_TIMEOUT)
       m = "a bounded device loop hit its iteration limit (contact solver, particle #" + std::to_string(h->hst->detail) + ")";
     else m = "device error " + std::to_string(code);
@@ -737,13 +758,15 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
   cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid); cudaFree(cs.srec);
   cudaFree(cs.retainFlag); cudaFree(cs.temp); cudaFree(cs.periC); cudaFree(cs.periH); cudaFree(cs.periCi); cudaFree(cs.periHi);
-  cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag);
+  cudaFree(cs.cand); cudaFree(cs.candPer); cudaFree(cs.candFlag); cudaFree(cs.sweepBuf);
   cudaFree(h->dst);
   cudaFree(h->staging);
   cudaFree(h->editGone); cudaFree(h->editIds); cudaFree(h->editPark); cudaFree(h->editRec); cudaFree(h->editMeta);
   if (h->hst) cudaFreeHost(h->hst);
   if (h->hcounts) cudaFreeHost(h->hcounts);
   for (auto e : h->evPool) cudaEventDestroy(e);
+  for (auto& g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return WDEM_OK;
@@ -1139,22 +1162,106 @@ static int queueDepth(wdem_handle* h, int left) {
   return q;
 }
 
+// The kernels of `ahead` queued steps (integrator, then contact pass), with the step numbers of P.step and
+// P.seq (absolute, or offsets when P.stepDev); the first contact pass culls the whole container if full.
+static void launchQueue(wdem_handle* h, StepParams P, int ahead, bool full, bool warm) {
+  cudaStream_t s = h->stream;
+  const long long step0 = P.step, seq0 = P.seq;
+  for (int g = 0; g < ahead; g++) {
+    P.step = step0 + g;
+    P.seq = seq0 + 1 + g;
+    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
+    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, g == 0 && full,
+                    warm ? h->mlpWbf : nullptr, warm ? h->mlpW : nullptr);
+  }
+}
+
+// The queue as one CUDA graph launch.  The graph is captured with P.stepDev (steps numbered from the
+// replay's bases) and kept with the bytes of every launch argument it holds: parameters, particle, contact
+// and CSR arrays, counts, status word and network weights.  A replay whose arguments differ (after a
+// rebuild, an upload, new parameters or a regrown array) captures again; with graphMode AUTO a capture is
+// made only when at least eight replays are expected before the next rebuild (a capture and instantiation
+// cost several times the host time of the launches it replaces).  Returns 1 if the queue was
+// launched, 0 if the caller launches it kernel by kernel, or a negative error code.
+static int replayQueue(wdem_handle* h, int ahead, bool full, bool warm) {
+  if (h->graphMode == WDEM_GRAPHS_OFF) return 0;
+  cudaStream_t s = h->stream;
+  StepParams P = h->P;
+  P.stepDev = 1;
+  P.step = 0;
+  P.seq = 0;
+  std::vector<unsigned char> sig;
+  auto put = [&sig](const void* x, size_t nb) {
+    const unsigned char* b = (const unsigned char*)x;
+    sig.insert(sig.end(), b, b + nb);
+  };
+  const int n = h->n, arith = h->raw.arith;
+  const void* wp[2] = {warm ? (const void*)h->mlpWbf : nullptr, warm ? (const void*)h->mlpW : nullptr};
+  put(&P, sizeof P); put(&h->d, sizeof h->d); put(&h->buf[h->cur].c, sizeof(Contacts)); put(&h->csr, sizeof h->csr);
+  put(&h->nContacts, sizeof h->nContacts); put(&n, sizeof n); put(&arith, sizeof arith); put(&h->dst, sizeof h->dst);
+  put(wp, sizeof wp);
+  const int key = 2 * ahead + (full ? 1 : 0);
+  auto it = h->graphs.find(key);
+  const bool valid = it != h->graphs.end() && it->second.exec && it->second.sig == sig;
+  if (!valid && h->graphMode == WDEM_GRAPHS_AUTO && h->rebuildInterval < 8.0 * ahead) return 0;
+  wdem_handle::StepGraph& g = h->graphs[key];
+  if (!valid) {
+    const long long k0 = ::wdem::g_kernel_launches;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launchQueue(h, P, ahead, full, warm);
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    const long long kernels = ::wdem::g_kernel_launches - k0;
+    ::wdem::g_kernel_launches = k0;  // captured, not launched
+    if (e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(h, WDEM_ERR_CUDA, std::string("capturing the queued steps: ") + cudaGetErrorString(e));
+    }
+    if (g.exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(g.exec, graph, &info) != cudaSuccess) {
+        cudaGetLastError();  // a topology change: instantiate anew
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+      }
+    }
+    cudaError_t ie = cudaSuccess;
+    if (!g.exec) ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      g.exec = nullptr;
+      return fail(h, WDEM_ERR_CUDA, std::string("instantiating the queued steps: ") + cudaGetErrorString(ie));
+    }
+    g.sig.swap(sig);
+    g.kernels = kernels;
+    h->graphCaptures++;
+  }
+  // the replay's step numbers: stepBase + g and seqBase + 1 + g for its g-th step
+  h->hst->stepBase = h->step;
+  h->hst->seqBase = h->seq;
+  CK(cudaMemcpyAsync(&h->dst->stepBase, &h->hst->stepBase, 2 * sizeof(long long), cudaMemcpyHostToDevice, s));
+  CK(cudaGraphLaunch(g.exec, s));
+  ::wdem::g_kernel_launches += g.kernels;
+  h->graphReplays++;
+  return 1;
+}
+
 static int runQueued(wdem_handle* h, int ahead, int& done) {
   cudaStream_t s = h->stream;
   const long long s0 = h->step;
   h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
   const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
-  StepParams P = h->P;
   const long long q0 = h->seq;
-  for (int g = 0; g < ahead; g++) {
-    P.step = s0 + g;
-    P.seq = q0 + 1 + g;
-    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
-    const bool full = !h->actValid;
-    h->actValid = true;
-    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, full, warm ? h->mlpWbf : nullptr,
-                    warm ? h->mlpW : nullptr);
+  const bool full = !h->actValid;
+  const int viaGraph = replayQueue(h, ahead, full, warm);
+  if (viaGraph < 0) return viaGraph;
+  if (viaGraph == 0) {
+    StepParams P = h->P;
+    P.step = s0;
+    P.seq = q0;
+    launchQueue(h, P, ahead, full, warm);
   }
+  h->actValid = true;
   CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   int rc;
@@ -1890,6 +1997,19 @@ int wdem_set_queue_depth(wdem_handle* h, int32_t depth) {
   return WDEM_OK;
 }
 
+int wdem_set_step_graphs(wdem_handle* h, int32_t mode) {
+  if (!h || mode < WDEM_GRAPHS_OFF || mode > WDEM_GRAPHS_ON) return WDEM_ERR_ARG;
+  h->graphMode = mode;
+  return WDEM_OK;
+}
+
+int wdem_graph_stats(wdem_handle* h, int64_t* captures, int64_t* replays) {
+  if (!h || !captures || !replays) return WDEM_ERR_ARG;
+  *captures = h->graphCaptures;
+  *replays = h->graphReplays;
+  return WDEM_OK;
+}
+
 int wdem_set_timing(wdem_handle* h, int32_t enable) {
   if (!h) return WDEM_ERR_ARG;
   h->timing = enable != 0;
@@ -2075,11 +2195,14 @@ int wdem_warm_predict(wdem_handle* h, const float* x, int64_t n, float* y) {
   CK(dalloc(dx, (size_t)n * WDEM_WARM_INPUTS));
   if (dalloc(dy, (size_t)n * WDEM_WARM_OUTPUTS) != cudaSuccess) { cudaFree(dx); return fail(h, WDEM_ERR_CUDA, "out of memory"); }
   cudaMemcpyAsync(dx, x, (size_t)n * WDEM_WARM_INPUTS * sizeof(float), cudaMemcpyHostToDevice, h->stream);
-  mlp_launch_predict(h->stream, dx, n, dy, h->mlpWbf, h->mlpW);
+  mlp_launch_predict(h->stream, dx, n, dy, h->mlpWbf, h->mlpW, h->dst);
   cudaMemcpyAsync(y, dy, (size_t)n * WDEM_WARM_OUTPUTS * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
   cudaFree(dx); cudaFree(dy);
   if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
+  int rc;
+  if ((rc = checkDeviceStatus(h))) return rc;
   return WDEM_OK;
 }
 

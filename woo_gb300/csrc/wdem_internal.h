@@ -56,6 +56,8 @@ __host__ __device__ __forceinline__ int sceneOf(int metax) { return (metax >> ME
 // threads (and pair-count entries) of the collider's sweep: one per small box, one per large body (at least
 // one); the exclusive scan of the counts leaves the pair total at counts[sweepThreads]
 __host__ __device__ __forceinline__ int sweepThreads(int nSmall, int nLarge) { return nSmall + (nLarge > 0 ? nLarge : 1); }
+// pairs of one sweep thread kept by the counting pass for the writing pass (a thread with more walks again)
+constexpr int SWEEP_BUF = 8;
 // Pair orientation as the geometry functors take it (GeomDispatcher::getFunctor2D swaps a fresh contact,
 // ContactLoop.cpp:144-150): the pair (lower id, higher id) is swapped when its shapes come in the order
 // Sphere+Wall, Ellipsoid+Sphere, Ellipsoid+Wall or Sphere+Facet.
@@ -100,6 +102,8 @@ struct StepParams {
   double dt;
   long long step;
   long long seq;            // number of this step's contact pass (never reset); stamps the pass's force records
+  int stepDev;              // 1: step and seq are offsets from DeviceStatus.stepBase/seqBase (steps replayed
+                            // from a CUDA graph, whose kernel arguments are fixed at capture)
   double gravity[3];
   int hasGravity;
   double distFactor;        // DemField.distFactor
@@ -208,6 +212,9 @@ struct GridParams {
   int ncx, ncy;
   double lo1, lo2, cell;
   double loS, invQ;  // quantisation along the sweep axis
+  double invCell;    // 1 / cell (column binning)
+  int qbits;         // sweep key: column << qbits | quantised lower bound (qbits chosen by the host so that the
+  unsigned qmax;     //   whole key fits the fewest 8-bit radix passes), qmax = 2^qbits - 1
   int nSmall;        // spheres in the sort
   int ok;
 };
@@ -227,6 +234,8 @@ struct DeviceStatus {
   unsigned long long dynNotMin;  // DynDt: ~bits of the smallest nodal critical step^2 (0: none yet)
   unsigned actCount;   // length of the contact cull's active list
   double ext[12];     // box extents reduction scratch (as ordered ints)
+  long long stepBase;  // graph replays: Scene.step of the replay's first step
+  long long seqBase;   //   and the contact-pass number before it
 };
 
 #ifdef __CUDACC__
@@ -245,6 +254,13 @@ __device__ __forceinline__ unsigned workItem(const unsigned* work, const unsigne
 // guards never fire.  The word is read with a plain (L1-cached) load: the values that matter were
 // written by earlier kernels, and a store by the running integrator (step + 1) does not halt it; a
 // volatile load per warp would send every warp of the grid to the same L2 line.
+// the step number and contact-pass number of the running kernel (StepParams.stepDev)
+__device__ __forceinline__ long long stepOf(const StepParams& P, const DeviceStatus* st) {
+  return P.stepDev ? st->stepBase + P.step : P.step;
+}
+__device__ __forceinline__ long long seqOf(const StepParams& P, const DeviceStatus* st) {
+  return P.stepDev ? st->seqBase + P.seq : P.seq;
+}
 __device__ __forceinline__ bool haltedIntegrator(const DeviceStatus* st, long long step) {
   const long long h = st->haltAt;
   return h != 0 && h <= step;
@@ -297,6 +313,8 @@ struct ColliderScratch {
   long long blockSumsCap;
   int* cellStart;                       // maxCols + 1
   float4* srec;                         // sweep records in sort order: 2 per particle (N capacity)
+  int2* sweepBuf;                       // the counting sweep's first SWEEP_BUF pairs of each thread
+  long long sweepBufCap;                //   (threads)
   int maxCols;
   unsigned* counts;                     // nSmall+2 pair counts per sorted particle, scanned in place
   int* large;                           // ids of walls (unbounded boxes), grouped by scene
@@ -336,8 +354,9 @@ void mlp_pack(const float* pad, float* pub);
 cudaError_t mlp_prepare_kernels();
 void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf);
 void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, const unsigned* work, const unsigned* count,
-                     const uint16_t* wbf, const float* wf, bool onlyFresh);
-void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf);
+                     const uint16_t* wbf, const float* wf, bool onlyFresh, DeviceStatus* st, int numSMs);
+void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf,
+                        DeviceStatus* st);
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
                      float* grad, float* loss);
 void mlp_launch_adam(cudaStream_t s, float* w, float* m, float* v, float* grad, uint16_t* wbf, float lr, float b1,
