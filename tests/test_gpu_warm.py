@@ -111,3 +111,18 @@ def test_training_gain(wdem_lib):
     pb = gpu_particles(hb, both.particles.n)
     assert np.allclose(pc.pos, pb.pos, rtol=0, atol=1e-9 * np.abs(pc.pos).max())
 
+
+
+def test_forward_large_batch(wdem_lib):
+    """2^20 rows through the tensor-core kernel (8192 tiles of 128 over the persistent CTAs): a seeded
+    sample of 4096 rows against the reference, every output finite."""
+    h = _handle()
+    h.warm_init(3)
+    w = h.warm_get_weights().astype(np.float64)
+    rng = np.random.default_rng(7)
+    X = _features(rng, 1 << 20)
+    Yg = h.warm_predict(X)
+    assert np.isfinite(Yg).all()
+    pick = rng.choice(len(X), 4096, replace=False)
+    Yr, _ = M.forward(w, X[pick])
+    assert np.abs(Yg[pick] - Yr).max() <= 1e-3 * np.abs(Yr).max()

@@ -162,9 +162,6 @@ __global__ void k_extents(Particles p, const int* small, int nSmall, unsigned lo
   if (threadIdx.x < 15) sh[threadIdx.x] = ~0ull;
   __syncthreads();
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  // the 15 minima of the warp first (shuffles), then one shared atomic per warp and value
-  unsigned long long v[15];
-  for (int q = 0; q < 15; q++) v[q] = ~0ull;
   if (k < nSmall) {
     int i = small[k];
     double4_32a pr = p.posr[i];
@@ -173,20 +170,13 @@ __global__ void k_extents(Particles p, const int* small, int nSmall, unsigned lo
     double lo[3] = {mn.x, mn.y, mn.z};
     double hi[3] = {mx.x, mx.y, mx.z};
     for (int a = 0; a < 3; a++) {
-      v[a] = ordKey(c[a]);
-      v[3 + a] = ~ordKey(c[a]);
-      v[6 + a] = ordKey(lo[a]);
-      v[9 + a] = ~ordKey(hi[a]);
-      v[12 + a] = ~ordKey(hi[a] - lo[a]);
+      atomicMin(&sh[a], ordKey(c[a]));
+      atomicMin(&sh[3 + a], ~ordKey(c[a]));
+      atomicMin(&sh[6 + a], ordKey(lo[a]));
+      atomicMin(&sh[9 + a], ~ordKey(hi[a]));
+      atomicMin(&sh[12 + a], ~ordKey(hi[a] - lo[a]));
     }
   }
-  for (int o = 16; o > 0; o >>= 1)
-    for (int q = 0; q < 15; q++) {
-      const unsigned long long w = __shfl_xor_sync(0xffffffffu, v[q], o);
-      v[q] = w < v[q] ? w : v[q];
-    }
-  if ((threadIdx.x & 31) == 0)
-    for (int q = 0; q < 15; q++) atomicMin(&sh[q], v[q]);
   __syncthreads();
   if (threadIdx.x < 15) atomicMin(&ext[threadIdx.x], sh[threadIdx.x]);
 }
@@ -308,112 +298,215 @@ __global__ void k_scan_tiles(unsigned* a, long long n, unsigned* sums) {
   if (threadIdx.x == SCAN_T - 1) sums[blockIdx.x] = s[SCAN_T - 1];
 }
 
-__global__ void k_scan_add(unsigned* a, long long n, const unsigned* sums) {
+
+
+// Exclusive scan of a[0..n) in place with the total written to a[n]: tile scans, the tile sums scanned by
+// the same routine (which leaves their total at sums[nb]), then the sums added back; with one tile the
+// tile kernel writes the total itself.
+__global__ void k_scan_add(unsigned* a, long long n, const unsigned* sums, long long nb) {
   long long base = (long long)blockIdx.x * SCAN_TILE;
   unsigned add = sums[blockIdx.x];
   for (int k = 0; k < SCAN_I; k++) {
     long long idx = base + threadIdx.x * SCAN_I + k;
     if (idx < n) a[idx] += add;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a[n] = sums[nb];
 }
-
 
 static void scan_rec(cudaStream_t s, unsigned* a, long long n, unsigned* scratch) {
   long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  if (nb == 0) return;
+  if (nb == 0) {
+    cudaMemsetAsync(a, 0, sizeof(unsigned), s);  // empty: total 0
+    return;
+  }
   unsigned* sums = scratch;  // nb + 1 entries
-  (k_scan_tiles<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums), ++::wdem::g_kernel_launches);
+  (k_scan_tiles<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, nb == 1 ? a + n : sums), ++::wdem::g_kernel_launches);
   if (nb > 1) {
     scan_rec(s, sums, nb, scratch + ((nb + 1 + 63) & ~63ll));
-    (k_scan_add<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums), ++::wdem::g_kernel_launches);
-  } else {
-    // single tile: sums[0] holds the total; scan of one element is 0
+    (k_scan_add<<<(unsigned)nb, SCAN_T, 0, s>>>(a, n, sums, nb), ++::wdem::g_kernel_launches);
   }
-}
-
-
-__global__ void k_save_last(const unsigned* a, long long n, unsigned* dst) { *dst = n > 0 ? a[n - 1] : 0; }
-__global__ void k_finish_total(unsigned* a, long long n, const unsigned* lastInput) {
-  a[n] = (n > 0 ? a[n - 1] : 0) + *lastInput;
 }
 
 void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs) {
-  unsigned* last = cs.blockSums;        // 1 entry
-  unsigned* scratch = cs.blockSums + 64;
-  (k_save_last<<<1, 1, 0, s>>>(a, n, last), ++::wdem::g_kernel_launches);
-  scan_rec(s, a, n, scratch);
-  (k_finish_total<<<1, 1, 0, s>>>(a, n, last), ++::wdem::g_kernel_launches);
+  scan_rec(s, a, n, cs.blockSums + 64);
 }
 
 // ------------------------------------------------------------------------------------ radix sort
-// LSD radix sort, 8-bit digits, keys u64 with u32 payload; stable within each pass, so the whole
-// sort is stable.  Per pass: tile histograms -> exclusive scan (digit-major) -> ranked scatter.
+// LSD radix sort, 8-bit digits, keys u64 with u32 payload, one kernel per digit (Merrill & Garland's
+// single-pass prefix scan with decoupled look-back, applied per digit as in "Onesweep", Adinets & Merrill
+// 2022).  Before the passes, one kernel counts the digits of every pass over the whole input (the global
+// digit starts do not depend on the order) and one block scans them.  A pass kernel takes its tile in
+// acquisition order (atomic counter, so every earlier tile is running or done), counts the tile's digits,
+// publishes them (aggregate), looks back over earlier tiles for the digit's exclusive prefix (stopping at
+// the first inclusive prefix), publishes its own inclusive prefix, ranks the tile's keys stably (round,
+// warp, lane order) into shared memory and writes each digit's run contiguously.  Every look-back wait is
+// bounded; a wait that gives up sets WDEM_ERR_TIMEOUT.
 static const int RS_T = 256, RS_R = 8, RS_TILE = RS_T * RS_R;
+static const int RS_MAX_PASSES = 8;
+static const unsigned RS_AGG = 1u << 30, RS_PRE = 2u << 30, RS_VAL = (1u << 30) - 1;
+static const long long RS_SPIN = 1ll << 22;
 
-__global__ void k_rs_hist(const unsigned long long* keys, long long n, int shift, unsigned* hist, long long nTiles) {
-  __shared__ unsigned h[256];
-  h[threadIdx.x] = 0;
+// global digit counts of all passes: gcount[p][d]
+__global__ void __launch_bounds__(RS_T) k_rs_count(const unsigned long long* keys, long long n, int passes, unsigned* gcount) {
+  __shared__ unsigned h[RS_MAX_PASSES][256];
+  for (int p = 0; p < passes; p++) h[p][threadIdx.x] = 0;
   __syncthreads();
-  long long base = (long long)blockIdx.x * RS_TILE;
-  for (int r = 0; r < RS_R; r++) {
-    long long idx = base + r * RS_T + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255], 1u);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long k = keys[i];
+    for (int p = 0; p < passes; p++) atomicAdd(&h[p][(k >> (8 * p)) & 255], 1u);
   }
   __syncthreads();
-  hist[(long long)threadIdx.x * nTiles + blockIdx.x] = h[threadIdx.x];
+  for (int p = 0; p < passes; p++)
+    if (h[p][threadIdx.x]) atomicAdd(&gcount[p * 256 + threadIdx.x], h[p][threadIdx.x]);
+}
+// exclusive scan of each pass's 256 counts (one block, thread = digit)
+__global__ void __launch_bounds__(RS_T) k_rs_starts(unsigned* gcount, int passes) {
+  __shared__ unsigned s[256];
+  for (int p = 0; p < passes; p++) {
+    const unsigned c = gcount[p * 256 + threadIdx.x];
+    s[threadIdx.x] = c;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+      const unsigned t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    gcount[p * 256 + threadIdx.x] = s[threadIdx.x] - c;
+    __syncthreads();
+  }
 }
 
-__global__ void k_rs_scatter(const unsigned long long* kin, const unsigned* vin, unsigned long long* kout,
-                             unsigned* vout, long long n, int shift, const unsigned* hist, long long nTiles) {
-  __shared__ unsigned wc[RS_T / 32][256];
+__global__ void __launch_bounds__(RS_T) k_rs_pass(const unsigned long long* kin, const unsigned* vin, unsigned long long* kout,
+                                                  unsigned* vout, long long n, int shift, const unsigned* digitStart,
+                                                  unsigned* status, unsigned* tileCounter, DeviceStatus* st) {
+  __shared__ unsigned tileS;
+  __shared__ unsigned cnt[256];      // the tile's digit counts
+  __shared__ unsigned lstart[256];   // exclusive prefix of cnt: the digit's run in the tile's staging
+  __shared__ unsigned goff[256];     // the digit's first position in the output
   __shared__ unsigned runBase[256];
-  __shared__ unsigned gOff[256];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  gOff[threadIdx.x] = hist[(long long)threadIdx.x * nTiles + blockIdx.x];
-  runBase[threadIdx.x] = 0;
-  long long base = (long long)blockIdx.x * RS_TILE;
+  __shared__ unsigned wc[RS_T / 32][256];
+  __shared__ unsigned long long skey[RS_TILE];
+  __shared__ unsigned sval[RS_TILE];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  if (t == 0) tileS = atomicAdd(tileCounter, 1u);
+  cnt[t] = 0;
+  runBase[t] = 0;
+  __syncthreads();
+  const long long tile = tileS;
+  const long long base = tile * RS_TILE;
+  unsigned long long k[RS_R];
+  unsigned v[RS_R];
+#pragma unroll
   for (int r = 0; r < RS_R; r++) {
-    for (int w = 0; w < RS_T / 32; w++) wc[w][threadIdx.x] = 0;
-    __syncthreads();
-    long long idx = base + r * RS_T + threadIdx.x;
-    bool valid = idx < n;
-    unsigned long long k = valid ? kin[idx] : 0;
-    unsigned v = valid ? vin[idx] : 0;
-    unsigned d = valid ? (unsigned)((k >> shift) & 255) : 256u + lane;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    unsigned rankInWarp = __popc(peers & ((1u << lane) - 1));
-    int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) wc[warp][d] = __popc(peers);
-    __syncthreads();
-    // per digit: exclusive prefix over warps, then advance the running base
-    {
-      unsigned dsum = 0;
-      for (int w = 0; w < RS_T / 32; w++) { unsigned c = wc[w][threadIdx.x]; wc[w][threadIdx.x] = dsum; dsum += c; }
-      // store the round total temporarily in runBase after use below
-      __syncthreads();
-      if (valid) {
-        unsigned pos = gOff[d] + runBase[d] + wc[warp][d] + rankInWarp;
-        kout[pos] = k;
-        vout[pos] = v;
+    const long long idx = base + r * RS_T + t;
+    k[r] = idx < n ? kin[idx] : 0;
+    v[r] = idx < n ? vin[idx] : 0;
+    if (idx < n) atomicAdd(&cnt[(k[r] >> shift) & 255], 1u);
+  }
+  __syncthreads();
+  // thread t: digit t.  Aggregate first, then the look-back, then the inclusive prefix.
+  const unsigned c = cnt[t];
+  volatile unsigned* mine = status + tile * 256;
+  unsigned excl = 0;
+  if (tile == 0) {
+    mine[t] = RS_PRE | c;
+  } else {
+    mine[t] = RS_AGG | c;
+    for (long long j = tile - 1; j >= 0; j--) {
+      volatile unsigned* pr = status + j * 256;
+      unsigned w = pr[t];
+      long long it = 0;
+      while ((w & ~RS_VAL) == 0) {
+        if (++it > RS_SPIN) {
+          atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT);
+          w = RS_PRE;
+          break;
+        }
+        __nanosleep(32);
+        w = pr[t];
       }
+      excl += w & RS_VAL;
+      if ((w & ~RS_VAL) == RS_PRE) break;
+    }
+    mine[t] = RS_PRE | (excl + c);
+  }
+  goff[t] = digitStart[t] + excl;
+  // exclusive scan of the tile's counts: where each digit's run starts in the staging arrays
+  {
+    unsigned* sc = &wc[0][0];  // free until the ranking rounds
+    sc[t] = c;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+      const unsigned u = t >= off ? sc[t - off] : 0;
       __syncthreads();
-      runBase[threadIdx.x] += dsum;
+      sc[t] += u;
+      __syncthreads();
+    }
+    lstart[t] = sc[t] - c;
+    __syncthreads();
+  }
+  // stable ranking into the staging arrays: round r, then warp, then lane
+  for (int r = 0; r < RS_R; r++) {
+    for (int w = 0; w < RS_T / 32; w++) wc[w][t] = 0;
+    __syncthreads();
+    const long long idx = base + r * RS_T + t;
+    const bool valid = idx < n;
+    const unsigned d = valid ? (unsigned)((k[r] >> shift) & 255) : 256u + lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned rankInWarp = __popc(peers & ((1u << lane) - 1));
+    if (valid && lane == __ffs(peers) - 1) wc[warp][d] = __popc(peers);
+    __syncthreads();
+    unsigned dsum = 0;
+    for (int w = 0; w < RS_T / 32; w++) { const unsigned cc = wc[w][t]; wc[w][t] = dsum; dsum += cc; }
+    __syncthreads();
+    if (valid) {
+      const unsigned pos = lstart[d] + runBase[d] + wc[warp][d] + rankInWarp;
+      skey[pos] = k[r];
+      sval[pos] = v[r];
     }
     __syncthreads();
+    runBase[t] += dsum;
+  }
+  __syncthreads();
+  // each digit's run written contiguously
+  const long long m = n - base < RS_TILE ? n - base : RS_TILE;
+  for (int j = t; j < m; j += RS_T) {
+    const unsigned long long kk = skey[j];
+    const unsigned d = (unsigned)((kk >> shift) & 255);
+    const unsigned pos = goff[d] + (unsigned)j - lstart[d];
+    kout[pos] = kk;
+    vout[pos] = sval[j];
   }
 }
 
+// scratch of one sort: status words of every pass (passes x tiles x 256), then the per-pass tile counters
+// and global digit starts (passes x 256), cleared by one memset
 static void radix_sort(cudaStream_t s, unsigned long long*& keys, unsigned*& vals, unsigned long long*& keysAlt,
                        unsigned*& valsAlt, long long n, int bits, ColliderScratch& cs) {
+  DeviceStatus* st = cs.st;
   if (n <= 1) return;
-  long long nTiles = (n + RS_TILE - 1) / RS_TILE;
-  for (int shift = 0; shift < bits; shift += 8) {
-    (k_rs_hist<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, n, shift, cs.hist, nTiles), ++::wdem::g_kernel_launches);
-    exclusive_scan_u32(s, cs.hist, 256 * nTiles, cs);
-    (k_rs_scatter<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, vals, keysAlt, valsAlt, n, shift, cs.hist, nTiles), ++::wdem::g_kernel_launches);
+  const long long nTiles = (n + RS_TILE - 1) / RS_TILE;
+  const int passes = (bits + 7) / 8;
+  unsigned* status = cs.hist;
+  unsigned* starts = status + (size_t)passes * nTiles * 256;
+  unsigned* counters = starts + passes * 256;
+  cudaMemsetAsync(status, 0, ((size_t)passes * nTiles * 256 + passes * 256 + passes) * sizeof(unsigned), s);
+  const unsigned cb = (unsigned)std::min<long long>((n + RS_T - 1) / RS_T, 152 * 8);
+  (k_rs_count<<<cb, RS_T, 0, s>>>(keys, n, passes, starts), ++::wdem::g_kernel_launches);
+  (k_rs_starts<<<1, RS_T, 0, s>>>(starts, passes), ++::wdem::g_kernel_launches);
+  for (int p = 0; p < passes; p++) {
+    (k_rs_pass<<<(unsigned)nTiles, RS_T, 0, s>>>(keys, vals, keysAlt, valsAlt, n, 8 * p, starts + p * 256,
+                                                  status + (size_t)p * nTiles * 256, counters + p, st),
+     ++::wdem::g_kernel_launches);
     unsigned long long* tk = keys; keys = keysAlt; keysAlt = tk;
     unsigned* tv = vals; vals = valsAlt; valsAlt = tv;
   }
+}
+// words of radix-sort scratch for n keys
+long long radix_scratch_words(long long n) {
+  const long long nTiles = (n + RS_TILE - 1) / RS_TILE;
+  return (long long)RS_MAX_PASSES * nTiles * 256 + RS_MAX_PASSES * 257 + 64;
 }
 
 // ------------------------------------------------------------------------------------ sort small

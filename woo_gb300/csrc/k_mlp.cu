@@ -6,13 +6,13 @@
 // contact point in A's frame.  Its lambda starts the Newton solve (WDEM_WARM_MLP); the solve falls
 // back to the cold start when it has not converged after fallbackIters iterations.
 //
-// Arithmetic: BF16 operands, FP32 accumulation, on the tensor cores.  Rounding points, which the CPU
-// reference of the network follows: inputs, weights and post-ReLU activations are rounded to BF16;
-// biases, pre-activations and outputs stay FP32.  Inference (the warm start of the contact pass and
-// wdem_warm_predict) runs on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
-// memory, k_mlp_tc).  Training runs forward and backward with warp-level mma.sync.m16n8k16 (one warp =
-// 16 samples, activations in shared memory; BF16 operands: activations, dZ, weights), sums the gradient
-// of a mini-batch per block in shared memory, and applies Adam (Kingma & Ba 2015) to FP32 master weights.
+// Arithmetic: BF16 operands, FP32 accumulation, on the 5th-generation tensor cores (tcgen05.mma with the
+// accumulators in tensor memory).  Rounding points, which the CPU reference of the network follows:
+// inputs, weights and post-ReLU activations are rounded to BF16, and so are the dZ operands of the
+// backward products; biases, pre-activations, outputs and bias gradients stay FP32.  Inference (the warm
+// start of the contact pass and wdem_warm_predict) is k_mlp_tc; training (k_mlp_grad_tc) runs forward,
+// backward and the weight-gradient products of tiles of 128 records, and Adam (Kingma & Ba 2015) updates
+// FP32 master weights (k_adam).
 //
 // Parameter layout on the device (padded): W1[16][64] (input rows 13..15 zero), b1[64], W2[64][64],
 // b2[64], W3[64][64], b3[64], W4[64][8] (output columns 4..7 zero), b4[8]; W[l][in][out] row-major.
@@ -32,219 +32,12 @@ namespace {
 constexpr int H = 64;
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + 16 * H, OFF_W2 = OFF_B1 + H, OFF_B2 = OFF_W2 + H * H, OFF_W3 = OFF_B2 + H,
               OFF_B3 = OFF_W3 + H * H, OFF_W4 = OFF_B3 + H, OFF_B4 = OFF_W4 + H * 8, NPAD = OFF_B4 + 8;
-constexpr int WARPS = 4;             // warps per block, 16 samples each
-constexpr int SAMPLES = 16 * WARPS;  // samples per block
 // loss weights of the four outputs: lambda, contact point x, y, z
 __constant__ float c_lossW[4] = {1.0f, 0.1f, 0.1f, 0.1f};
-
-// per-warp shared buffers (BF16 bits as uint16): x[16][16], a1..a3[16][64], dz[16][64]; out[16][8] fp32
-struct WarpSmem {
-  uint16_t x[16 * 16];
-  uint16_t a[3][16 * H];
-  uint16_t dz[16 * H];
-  uint16_t dz4[16 * 16];
-  float out[16 * 8];
-};
-// weights: BF16 copy of the padded parameter vector; biases FP32 (b1 at 0, b2 at 64, b3 at 128, b4 at 192)
-constexpr int SB1 = 0, SB2 = 64, SB3 = 128, SB4 = 192, NB = 200;
-struct NetSmem {
-  uint16_t w[NPAD];
-  float b[NB];
-};
 
 __device__ __forceinline__ uint16_t bf(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 __device__ __forceinline__ float fbf(uint16_t u) { return __bfloat162float(__ushort_as_bfloat16(u)); }
 __device__ __forceinline__ uint32_t pk(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
-
-__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// Fragment loaders for m16n8k16 (row.col): lane = 4 * g + t.  A (16 x 16): rows g, g+8; columns 2t, 2t+1
-// and 2t+8, 2t+9.  B (16 x 8): rows (k) 2t, 2t+1 and 2t+8, 2t+9; column (n) g.  C: rows g, g+8; columns
-// 2t, 2t+1.
-// A from a row-major tile T[16][ld] at column k0
-__device__ __forceinline__ void fragA(const uint16_t* T, int ld, int k0, int g, int t, uint32_t* a) {
-  a[0] = pk(T[g * ld + k0 + 2 * t], T[g * ld + k0 + 2 * t + 1]);
-  a[1] = pk(T[(g + 8) * ld + k0 + 2 * t], T[(g + 8) * ld + k0 + 2 * t + 1]);
-  a[2] = pk(T[g * ld + k0 + 2 * t + 8], T[g * ld + k0 + 2 * t + 9]);
-  a[3] = pk(T[(g + 8) * ld + k0 + 2 * t + 8], T[(g + 8) * ld + k0 + 2 * t + 9]);
-}
-// A = S^T for S row-major [16 samples][ld]: A[m][k] = S[k][m0 + m]
-__device__ __forceinline__ void fragAT(const uint16_t* S, int ld, int m0, int g, int t, uint32_t* a) {
-  a[0] = pk(S[(2 * t) * ld + m0 + g], S[(2 * t + 1) * ld + m0 + g]);
-  a[1] = pk(S[(2 * t) * ld + m0 + g + 8], S[(2 * t + 1) * ld + m0 + g + 8]);
-  a[2] = pk(S[(2 * t + 8) * ld + m0 + g], S[(2 * t + 9) * ld + m0 + g]);
-  a[3] = pk(S[(2 * t + 8) * ld + m0 + g + 8], S[(2 * t + 9) * ld + m0 + g + 8]);
-}
-// B from W row-major [K][ld]: B[k][n] = W[k0 + k][n0 + n]
-__device__ __forceinline__ void fragB(const uint16_t* W, int ld, int k0, int n0, int g, int t, uint32_t* b) {
-  b[0] = pk(W[(k0 + 2 * t) * ld + n0 + g], W[(k0 + 2 * t + 1) * ld + n0 + g]);
-  b[1] = pk(W[(k0 + 2 * t + 8) * ld + n0 + g], W[(k0 + 2 * t + 9) * ld + n0 + g]);
-}
-// B = W^T for W row-major [N][ld] with only kmax valid k: B[k][n] = W[n0 + n][k0 + k] (0 for k >= kmax)
-__device__ __forceinline__ void fragBT(const uint16_t* W, int ld, int k0, int n0, int kmax, int g, int t, uint32_t* b) {
-  const uint16_t* r = W + (n0 + g) * ld;
-  const int k = k0 + 2 * t;
-  b[0] = pk(k < kmax ? r[k] : 0, k + 1 < kmax ? r[k + 1] : 0);
-  b[1] = pk(k + 8 < kmax ? r[k + 8] : 0, k + 9 < kmax ? r[k + 9] : 0);
-}
-
-// One dense layer of the warp's 16 samples: Out = act(In[16][K] W[K][N] + b)
-template <int K, int N, bool RELU>
-__device__ __forceinline__ void layer(const uint16_t* In, const uint16_t* W, const float* b, uint16_t* OutBf,
-                                      float* OutF, int g, int t) {
-#pragma unroll
-  for (int nt = 0; nt < N / 8; nt++) {
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int ks = 0; ks < K / 16; ks++) {
-      uint32_t a[4], bb[2];
-      fragA(In, K, ks * 16, g, t, a);
-      fragB(W, N, ks * 16, nt * 8, g, t, bb);
-      mma16816(acc, a, bb);
-    }
-    const int col = nt * 8 + 2 * t;
-    const float z00 = acc[0] + b[col], z01 = acc[1] + b[col + 1], z10 = acc[2] + b[col], z11 = acc[3] + b[col + 1];
-    if (RELU) {
-      OutBf[g * N + col] = bf(fmaxf(z00, 0.f)); OutBf[g * N + col + 1] = bf(fmaxf(z01, 0.f));
-      OutBf[(g + 8) * N + col] = bf(fmaxf(z10, 0.f)); OutBf[(g + 8) * N + col + 1] = bf(fmaxf(z11, 0.f));
-    } else {
-      OutF[g * N + col] = z00; OutF[g * N + col + 1] = z01;
-      OutF[(g + 8) * N + col] = z10; OutF[(g + 8) * N + col + 1] = z11;
-    }
-  }
-  __syncwarp();
-}
-
-__device__ __forceinline__ void forward(const NetSmem& net, WarpSmem& ws, int g, int t) {
-  layer<16, H, true>(ws.x, net.w + OFF_W1, net.b + SB1, ws.a[0], nullptr, g, t);
-  layer<H, H, true>(ws.a[0], net.w + OFF_W2, net.b + SB2, ws.a[1], nullptr, g, t);
-  layer<H, H, true>(ws.a[1], net.w + OFF_W3, net.b + SB3, ws.a[2], nullptr, g, t);
-  layer<H, 8, false>(ws.a[2], net.w + OFF_W4, net.b + SB4, nullptr, ws.out, g, t);
-}
-
-__device__ __forceinline__ void loadNet(NetSmem& net, const uint16_t* wbf, const float* wf) {
-  const uint32_t* src = reinterpret_cast<const uint32_t*>(wbf);
-  uint32_t* dst = reinterpret_cast<uint32_t*>(net.w);
-  for (int k = threadIdx.x; k < NPAD / 2; k += blockDim.x) dst[k] = src[k];
-  for (int k = threadIdx.x; k < NB; k += blockDim.x) {
-    const int off = k < 64 ? OFF_B1 + k : (k < 128 ? OFF_B2 + k - 64 : (k < 192 ? OFF_B3 + k - 128 : OFF_B4 + k - 192));
-    net.b[k] = wf[off];
-  }
-  __syncthreads();
-}
-
-// ------------------------------------------------------------------------------ training
-// dW[in][out] += S^T dZ over the warp's 16 samples (S: [16][ldS] BF16 activations, dZ: [16][ldZ]),
-// accumulated into the block's shared gradient with shared-memory atomics.
-template <int M, int N>
-__device__ __forceinline__ void gradW(const uint16_t* S, int ldS, const uint16_t* dZ, int ldZ, float* gW, int g, int t) {
-#pragma unroll
-  for (int mt = 0; mt < M / 16; mt++)
-#pragma unroll
-    for (int nt = 0; nt < N / 8; nt++) {
-      uint32_t a[4], b[2];
-      fragAT(S, ldS, mt * 16, g, t, a);
-      // B[k = sample][n] = dZ[sample][nt*8 + n]
-      b[0] = pk(dZ[(2 * t) * ldZ + nt * 8 + g], dZ[(2 * t + 1) * ldZ + nt * 8 + g]);
-      b[1] = pk(dZ[(2 * t + 8) * ldZ + nt * 8 + g], dZ[(2 * t + 9) * ldZ + nt * 8 + g]);
-      float d[4] = {0.f, 0.f, 0.f, 0.f};
-      mma16816(d, a, b);
-      const int r0 = mt * 16 + g, col = nt * 8 + 2 * t;
-      atomicAdd(&gW[r0 * N + col], d[0]); atomicAdd(&gW[r0 * N + col + 1], d[1]);
-      atomicAdd(&gW[(r0 + 8) * N + col], d[2]); atomicAdd(&gW[(r0 + 8) * N + col + 1], d[3]);
-    }
-}
-
-// dA[16][K] = dZ[16][N] W^T (W: [K][N]) then dZ_prev = dA * (A > 0), stored as BF16; bias grad of the
-// previous layer from the FP32 values.
-template <int K, int N>
-__device__ __forceinline__ void backLayer(const uint16_t* dZ, const uint16_t* W, const uint16_t* A, uint16_t* dZprev,
-                                          float* gb, int g, int t) {
-#pragma unroll
-  for (int nt = 0; nt < K / 8; nt++) {
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    constexpr int KS = (N + 15) / 16;
-#pragma unroll
-    for (int ks = 0; ks < KS; ks++) {
-      uint32_t a[4], b[2];
-      // A[s][j] = dZ[s][ks*16 + j]  (dZ rows have stride max(N,16); padded columns are zero)
-      constexpr int ldz = N < 16 ? 16 : N;
-      fragA(dZ, ldz, ks * 16, g, t, a);
-      // B[j][k] = W[nt*8 + k][ks*16 + j]
-      fragBT(W, N, ks * 16, nt * 8, N, g, t, b);
-      mma16816(acc, a, b);
-    }
-    const int col = nt * 8 + 2 * t;
-    float z[4];
-    z[0] = fbf(A[g * K + col]) > 0.f ? acc[0] : 0.f;
-    z[1] = fbf(A[g * K + col + 1]) > 0.f ? acc[1] : 0.f;
-    z[2] = fbf(A[(g + 8) * K + col]) > 0.f ? acc[2] : 0.f;
-    z[3] = fbf(A[(g + 8) * K + col + 1]) > 0.f ? acc[3] : 0.f;
-    dZprev[g * K + col] = bf(z[0]); dZprev[g * K + col + 1] = bf(z[1]);
-    dZprev[(g + 8) * K + col] = bf(z[2]); dZprev[(g + 8) * K + col + 1] = bf(z[3]);
-    atomicAdd(&gb[col], z[0] + z[2]);
-    atomicAdd(&gb[col + 1], z[1] + z[3]);
-  }
-  __syncwarp();
-}
-
-// Gradient of the mean weighted squared error over the records idx[0..n) (or 0..n when idx is null),
-// summed into grad (padded layout, FP32) and loss (sum over the batch / n).
-__global__ void __launch_bounds__(128) k_mlp_grad(const float* rec, const int* idx, long long n, float invN,
-                                                  const uint16_t* wbf, const float* wf, float* grad, float* loss) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  NetSmem& net = *reinterpret_cast<NetSmem*>(smem);
-  WarpSmem* wsAll = reinterpret_cast<WarpSmem*>(smem + sizeof(NetSmem));
-  float* gsum = reinterpret_cast<float*>(smem + sizeof(NetSmem) + WARPS * sizeof(WarpSmem));
-  for (int k = threadIdx.x; k < NPAD; k += blockDim.x) gsum[k] = 0.f;
-  loadNet(net, wbf, wf);  // includes __syncthreads
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  WarpSmem& ws = wsAll[warp];
-  float myLoss = 0.f;
-  for (long long base = (long long)blockIdx.x * SAMPLES + warp * 16; base < n; base += (long long)gridDim.x * SAMPLES) {
-    const long long s = base + (lane & 15);
-    const bool valid = s < n;
-    const float* r = valid ? rec + (long long)(idx ? idx[s] : s) * ELL_RECORD : nullptr;
-    if (lane < 16)
-      for (int k = 0; k < 16; k++) ws.x[lane * 16 + k] = bf((valid && k < ELL_FEATURES) ? r[k] : 0.f);
-    __syncwarp();
-    forward(net, ws, g, t);
-    // dZ4 = 2 w (o - y) / n, padded to 16 columns of zeros
-    if (lane < 16) {
-      for (int k = 0; k < 16; k++) {
-        float d = 0.f;
-        if (valid && k < ELL_TARGETS) {
-          const float e = ws.out[lane * 8 + k] - r[ELL_FEATURES + k];
-          myLoss += c_lossW[k] * e * e * invN;
-          d = 2.f * c_lossW[k] * e * invN;
-          atomicAdd(&gsum[OFF_B4 + k], d);
-        }
-        ws.dz4[lane * 16 + k] = bf(d);
-      }
-    }
-    __syncwarp();
-    gradW<H, 8>(ws.a[2], H, ws.dz4, 16, gsum + OFF_W4, g, t);
-    backLayer<H, 8>(ws.dz4, net.w + OFF_W4, ws.a[2], ws.dz, gsum + OFF_B3, g, t);
-    gradW<H, H>(ws.a[1], H, ws.dz, H, gsum + OFF_W3, g, t);
-    // dz is both input and output of the next back step: route through dz4-sized staging? use a[2] as
-    // scratch for the new dZ (a3 is no longer needed)
-    backLayer<H, H>(ws.dz, net.w + OFF_W3, ws.a[1], ws.a[2], gsum + OFF_B2, g, t);
-    gradW<H, H>(ws.a[0], H, ws.a[2], H, gsum + OFF_W2, g, t);
-    backLayer<H, H>(ws.a[2], net.w + OFF_W2, ws.a[0], ws.dz, gsum + OFF_B1, g, t);
-    gradW<16, H>(ws.x, 16, ws.dz, H, gsum + OFF_W1, g, t);
-    __syncwarp();
-  }
-  for (int o = 16; o > 0; o >>= 1) myLoss += __shfl_xor_sync(0xffffffffu, myLoss, o);
-  if (lane == 0) atomicAdd(loss, myLoss);
-  __syncthreads();
-  for (int k = threadIdx.x; k < NPAD; k += blockDim.x)
-    if (gsum[k] != 0.f) atomicAdd(&grad[k], gsum[k]);
-}
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights; refreshes the BF16 copy and clears the gradient.
 __global__ void k_adam(float* w, float* m, float* v, float* grad, uint16_t* wbf, int n, float lr, float b1, float b2,
@@ -273,8 +66,7 @@ __global__ void k_to_bf16(const float* w, uint16_t* wbf, int n) {
 // tile (thread t owns sample t), BF16 operands in shared memory, FP32 accumulators in tensor memory (TMEM),
 // one elected thread issuing tcgen05.mma (M = 128, N = 64 or 16, K = 16 per instruction) and committing to
 // an mbarrier; the epilogue of each layer (bias, ReLU, BF16 rounding) reads the accumulator rows back with
-// tcgen05.ld and writes the next layer's A operand.  Rounding points as in the mma.sync path; only the
-// order of the FP32 additions inside the tensor core may differ.
+// tcgen05.ld and writes the next layer's A operand.  Rounding points as listed at the top of this file.
 //
 // Operand layout: the canonical K-major layout without swizzling, 8 x 16-byte core matrices; element
 // (r, k) of an R x K operand at (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2 bytes, with
@@ -371,7 +163,8 @@ __device__ __forceinline__ bool tcLayer(unsigned char* sm, int aOff, int bOff, u
 }
 
 // hidden-layer epilogue: this thread's accumulator row + bias, ReLU, BF16, into row t of the 128 x 64 A tile
-__device__ __forceinline__ void tcHidden(unsigned char* sm, uint32_t tRow, const float* bias, int t) {
+// at dst (default: the inference kernel's activation tile)
+__device__ __forceinline__ void tcHidden(unsigned char* sm, uint32_t tRow, const float* bias, int t, int dst = TC_H) {
 #pragma unroll
   for (int c = 0; c < H; c += 16) {
     float v[16];
@@ -380,13 +173,15 @@ __device__ __forceinline__ void tcHidden(unsigned char* sm, uint32_t tRow, const
 #pragma unroll
     for (int k = 0; k < 8; k++)
       w[k] = pk(bf(fmaxf(v[2 * k] + bias[c + 2 * k], 0.f)), bf(fmaxf(v[2 * k + 1] + bias[c + 2 * k + 1], 0.f)));
-    *reinterpret_cast<uint4*>(sm + TC_H + kmajorOff(t, c, H)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4*>(sm + TC_H + kmajorOff(t, c + 8, H)) = make_uint4(w[4], w[5], w[6], w[7]);
+    *reinterpret_cast<uint4*>(sm + dst + kmajorOff(t, c, H)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(sm + dst + kmajorOff(t, c + 8, H)) = make_uint4(w[4], w[5], w[6], w[7]);
   }
 }
 
 // The network over tiles of 128 samples.  WORK: the samples are the contact work list (features from the
-// particle state, as k_mlp_warm; lam0 written); otherwise feature rows X -> output rows Y.
+// particle state of each ellipsoid pair that the contact pass may solve; lam0 written, NaN = cold start;
+// with onlyFresh, pairs that carry the previous step's maximiser get NaN too, and a tile whose 128 pairs all
+// carry one skips the network); otherwise feature rows X -> output rows Y.
 template <bool WORK>
 __global__ void __launch_bounds__(128, 1) k_mlp_tc(Particles p, Contacts c, const unsigned* work, const unsigned* count,
                                                    long long ncon, const float* X, long long nx, float* Y,
@@ -500,8 +295,290 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(Particles p, Contacts c, cons
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
 }
 
-constexpr size_t SMEM_INFER = sizeof(NetSmem) + WARPS * sizeof(WarpSmem);
-constexpr size_t SMEM_TRAIN = SMEM_INFER + NPAD * sizeof(float);
+// ------------------------------------------------------------------------------ training on tcgen05
+// Forward, backward and weight gradients of tiles of 128 records on the tensor cores.  Per tile: the four
+// forward layers as in k_mlp_tc (activations H1..H3 kept in shared memory), the output error dZ4, then per
+// layer l = 4..1: dW_l += H_{l-1}^T dZ_l (M = inputs padded to 128, N = outputs, K = the 128 samples; the
+// accumulators stay in TMEM across all tiles of the CTA) and dA_{l-1} = dZ_l W_l^T (M = 128 samples, N = 64
+// inputs, K = outputs), whose epilogue masks by ReLU' (H_{l-1} > 0) and rounds to BF16 the next dZ.  The
+// transposed operands (H^T, dZ^T: samples along K) are written by each thread into its sample's column.
+// Bias gradients and the loss are summed from the FP32 values (warp shuffles, then shared atomics), as in
+// the warp-level kernel; the CTA adds everything to the global gradient once, at the end.
+constexpr int TT_FW1 = 0;                          // forward B operands (W^T: outputs x inputs)
+constexpr int TT_FW2 = TT_FW1 + H * 16 * 2;
+constexpr int TT_FW3 = TT_FW2 + H * H * 2;
+constexpr int TT_FW4 = TT_FW3 + H * H * 2;         // 16 x 64
+constexpr int TT_BW4 = TT_FW4 + TC_N4 * H * 2;     // backward B operands (W: inputs x outputs): 64 x 16
+constexpr int TT_BW3 = TT_BW4 + H * TC_N4 * 2;     // 64 x 64
+constexpr int TT_BW2 = TT_BW3 + H * H * 2;
+constexpr int TT_X = TT_BW2 + H * H * 2;           // 128 x 16
+constexpr int TT_H1 = TT_X + TC_M * 16 * 2;        // 128 x 64 each
+constexpr int TT_H2 = TT_H1 + TC_M * H * 2;
+constexpr int TT_H3 = TT_H2 + TC_M * H * 2;
+constexpr int TT_DZ = TT_H3 + TC_M * H * 2;        // dZ as the A operand of dA (128 x 64, or x 16 for dZ4)
+constexpr int TT_AT = TT_DZ + TC_M * H * 2;        // H^T or X^T: 128 (inputs, zero-padded) x 128 samples
+constexpr int TT_DZT = TT_AT + TC_M * TC_M * 2;    // dZ^T: 64 (outputs) x 128 samples
+constexpr int TT_BIAS = TT_DZT + H * TC_M * 2;     // b1, b2, b3, b4 (FP32)
+constexpr int TT_GB = TT_BIAS + (3 * H + TC_N4) * 4;  // bias-gradient sums of the CTA
+constexpr int TT_LOSS = TT_GB + (3 * H + TC_N4) * 4;
+constexpr int TT_BAR = TT_LOSS + 8;
+constexpr int TT_TMEM = TT_BAR + 8;
+constexpr size_t SMEM_TC_TRAIN = TT_TMEM + 8 + 1024;
+constexpr unsigned TT_COLS = 512;                  // TMEM: scratch 0..63, dW4 64..79, dW3 128.., dW2 192.., dW1 256..
+constexpr uint32_t TT_DW4 = 64, TT_DW3 = 128, TT_DW2 = 192, TT_DW1 = 256;
+
+// all threads: operands visible, one barrier; thread 0 runs `issue` (its MMAs) and commits; all wait.  The
+// same answer in every thread (false: the wait gave up).
+template <class F>
+__device__ __forceinline__ bool tcRound(unsigned char* sm, uint32_t bar, unsigned& phase, F issue) {
+  proxyFence();
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (threadIdx.x == 0) {
+    issue();
+    tcCommit(bar);
+  }
+  const bool ok = tcWait(bar, phase);
+  phase ^= 1u;
+  tcFenceAfter();
+  return __syncthreads_and(ok) != 0;
+}
+// D (TMEM) (+)= A (128 x K at aOff) x B^T (N x K at bOff), K-major operands
+template <int K, int N>
+__device__ __forceinline__ void tcIssue(unsigned char* sm, int aOff, int bOff, uint32_t d, bool accumulate) {
+  const uint32_t a0 = smemAddr(sm + aOff), b0 = smemAddr(sm + bOff);
+#pragma unroll
+  for (int ks = 0; ks < K / 16; ks++)
+    tcMma(d, tcDesc(a0 + 256 * ks, 128, K / 8 * 128), tcDesc(b0 + 256 * ks, 128, K / 8 * 128), tcIdesc(TC_M, N),
+          (ks > 0 || accumulate) ? 1 : 0);
+}
+// column sums of the warp (FP32, shuffles) added to the CTA's sums
+__device__ __forceinline__ void warpColumnAdd(float* dst, const float* v, int cols) {
+  for (int c = 0; c < cols; c++) {
+    float x = v[c];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&dst[c], x);
+  }
+}
+// the sample's column of a transposed operand: element (r, t) of an R x 128 K-major tile, r = 0 .. cols-1
+__device__ __forceinline__ void putColumn(unsigned char* sm, int off, int t, const uint16_t* v, int cols) {
+  for (int r = 0; r < cols; r++) *reinterpret_cast<uint16_t*>(sm + off + kmajorOff(r, t, TC_M)) = v[r];
+}
+// this thread's row of a 128 x 64 activation tile
+__device__ __forceinline__ void getRow64(const unsigned char* sm, int off, int t, uint16_t* v) {
+  for (int c = 0; c < H; c += 8) {
+    const uint4 q = *reinterpret_cast<const uint4*>(sm + off + kmajorOff(t, c, H));
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+    for (int k = 0; k < 4; k++) { v[c + 2 * k] = (uint16_t)(w[k] & 0xffff); v[c + 2 * k + 1] = (uint16_t)(w[k] >> 16); }
+  }
+}
+// dZ_prev = dA (this thread's accumulator row) masked by ReLU' of the activation row hv; bias-gradient sums;
+// dZ_prev as the next A operand (row t) and as the transposed B operand (column t)
+__device__ __forceinline__ void backEpilogue(unsigned char* sm, uint32_t tRow, const uint16_t* hv, float* gb, int t) {
+  float z[H];
+#pragma unroll
+  for (int c = 0; c < H; c += 16) tcLoad16(tRow + c, z + c);
+  uint16_t zb[H];
+#pragma unroll
+  for (int c = 0; c < H; c++) {
+    z[c] = fbf(hv[c]) > 0.f ? z[c] : 0.f;
+    zb[c] = bf(z[c]);
+  }
+  warpColumnAdd(gb, z, H);
+  for (int c = 0; c < H; c += 8) {
+    uint32_t w[4];
+    for (int k = 0; k < 4; k++) w[k] = pk(zb[c + 2 * k], zb[c + 2 * k + 1]);
+    *reinterpret_cast<uint4*>(sm + TT_DZ + kmajorOff(t, c, H)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  putColumn(sm, TT_DZT, t, zb, H);
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* rec, const int* idx, long long n, float invN,
+                                                        const uint16_t* wbf, const float* wf, float* grad, float* loss,
+                                                        DeviceStatus* st) {
+  extern __shared__ unsigned char smRaw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smRaw) + 1023) & ~uintptr_t(1023));
+  const int t = threadIdx.x, warp = t >> 5;
+  // weights: forward B (W^T) and backward B (W), biases; the padded rows of H^T stay zero
+  for (int e = t; e < H * 16; e += blockDim.x) {
+    const int nn = e / 16, k = e % 16;
+    *reinterpret_cast<uint16_t*>(sm + TT_FW1 + kmajorOff(nn, k, 16)) = wbf[OFF_W1 + k * H + nn];
+  }
+  for (int e = t; e < H * H; e += blockDim.x) {
+    const int a = e / H, b = e % H;
+    *reinterpret_cast<uint16_t*>(sm + TT_FW2 + kmajorOff(a, b, H)) = wbf[OFF_W2 + b * H + a];
+    *reinterpret_cast<uint16_t*>(sm + TT_FW3 + kmajorOff(a, b, H)) = wbf[OFF_W3 + b * H + a];
+    *reinterpret_cast<uint16_t*>(sm + TT_BW3 + kmajorOff(a, b, H)) = wbf[OFF_W3 + a * H + b];
+    *reinterpret_cast<uint16_t*>(sm + TT_BW2 + kmajorOff(a, b, H)) = wbf[OFF_W2 + a * H + b];
+  }
+  for (int e = t; e < TC_N4 * H; e += blockDim.x) {
+    const int a = e / H, b = e % H;  // forward: output a, input b
+    *reinterpret_cast<uint16_t*>(sm + TT_FW4 + kmajorOff(a, b, H)) = a < 8 ? wbf[OFF_W4 + b * 8 + a] : (uint16_t)0;
+    const int i = e / TC_N4, o = e % TC_N4;  // backward: input i, output o
+    *reinterpret_cast<uint16_t*>(sm + TT_BW4 + kmajorOff(i, o, TC_N4)) = o < 8 ? wbf[OFF_W4 + i * 8 + o] : (uint16_t)0;
+  }
+  for (int e = t; e < TC_M * TC_M / 8; e += blockDim.x) reinterpret_cast<uint4*>(sm + TT_AT)[e] = make_uint4(0, 0, 0, 0);
+  float* bias = reinterpret_cast<float*>(sm + TT_BIAS);
+  float* gb = reinterpret_cast<float*>(sm + TT_GB);
+  for (int e = t; e < 3 * H + TC_N4; e += blockDim.x) {
+    const int l = e / H, j = e % H;
+    bias[e] = l == 0 ? wf[OFF_B1 + j] : (l == 1 ? wf[OFF_B2 + j] : (l == 2 ? wf[OFF_B3 + j] : (j < 8 ? wf[OFF_B4 + j] : 0.f)));
+    gb[e] = 0.f;
+  }
+  if (t == 0) *reinterpret_cast<float*>(sm + TT_LOSS) = 0.f;
+  const uint32_t bar = smemAddr(sm + TT_BAR);
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(sm + TT_TMEM)),
+                 "r"(TT_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + TT_TMEM);
+  const uint32_t lane0 = (uint32_t)(32 * warp) << 16;
+  const uint32_t tRow = tmem + lane0;
+  unsigned phase = 0;
+  bool ok = true, first = true;
+  float myLoss = 0.f;
+  for (long long base = (long long)blockIdx.x * TC_M; base < n && ok; base += (long long)gridDim.x * TC_M) {
+    const long long s = base + t;
+    const bool valid = s < n;
+    const float* r = valid ? rec + (long long)(idx ? idx[s] : s) * ELL_RECORD : nullptr;
+    float f[16];
+    for (int k = 0; k < 16; k++) f[k] = (valid && k < ELL_FEATURES) ? r[k] : 0.f;
+    uint16_t xb[16];
+    for (int k = 0; k < 16; k++) xb[k] = bf(f[k]);
+    {
+      uint32_t xw[8];
+      for (int k = 0; k < 8; k++) xw[k] = pk(xb[2 * k], xb[2 * k + 1]);
+      *reinterpret_cast<uint4*>(sm + TT_X + kmajorOff(t, 0, 16)) = make_uint4(xw[0], xw[1], xw[2], xw[3]);
+      *reinterpret_cast<uint4*>(sm + TT_X + kmajorOff(t, 8, 16)) = make_uint4(xw[4], xw[5], xw[6], xw[7]);
+    }
+    // forward
+    if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<16, H>(sm, TT_X, TT_FW1, tmem, false); }))) break;
+    tcHidden(sm, tRow, bias, t, TT_H1);
+    if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<H, H>(sm, TT_H1, TT_FW2, tmem, false); }))) break;
+    tcHidden(sm, tRow, bias + H, t, TT_H2);
+    if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<H, H>(sm, TT_H2, TT_FW3, tmem, false); }))) break;
+    tcHidden(sm, tRow, bias + 2 * H, t, TT_H3);
+    if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<H, TC_N4>(sm, TT_H3, TT_FW4, tmem, false); }))) break;
+    // output error: dZ4 = 2 w (o - y) / n (zero for padded samples), its bias gradient, the loss
+    {
+      float o[16], d[16];
+      tcLoad16(tRow, o);
+      for (int k = 0; k < 16; k++) d[k] = 0.f;
+      if (valid)
+        for (int k = 0; k < ELL_TARGETS; k++) {
+          const float e = o[k] + bias[3 * H + k] - r[ELL_FEATURES + k];
+          myLoss += c_lossW[k] * e * e * invN;
+          d[k] = 2.f * c_lossW[k] * e * invN;
+        }
+      warpColumnAdd(gb + 3 * H, d, ELL_TARGETS);
+      uint16_t db[16];
+      for (int k = 0; k < 16; k++) db[k] = bf(d[k]);
+      uint32_t w[8];
+      for (int k = 0; k < 8; k++) w[k] = pk(db[2 * k], db[2 * k + 1]);
+      *reinterpret_cast<uint4*>(sm + TT_DZ + kmajorOff(t, 0, TC_N4)) = make_uint4(w[0], w[1], w[2], w[3]);
+      *reinterpret_cast<uint4*>(sm + TT_DZ + kmajorOff(t, 8, TC_N4)) = make_uint4(w[4], w[5], w[6], w[7]);
+      putColumn(sm, TT_DZT, t, db, TC_N4);
+      uint16_t hv[H];
+      getRow64(sm, TT_H3, t, hv);
+      putColumn(sm, TT_AT, t, hv, H);
+    }
+    const bool acc = !first;
+    // layer 4: dW4, dA3
+    if (!(ok = tcRound(sm, bar, phase, [&] {
+          tcIssue<TC_M, TC_N4>(sm, TT_AT, TT_DZT, tmem + TT_DW4, acc);
+          tcIssue<TC_N4, H>(sm, TT_DZ, TT_BW4, tmem, false);
+        })))
+      break;
+    {
+      uint16_t hv[H];
+      getRow64(sm, TT_H3, t, hv);
+      backEpilogue(sm, tRow, hv, gb + 2 * H, t);
+      getRow64(sm, TT_H2, t, hv);
+      putColumn(sm, TT_AT, t, hv, H);
+    }
+    // layer 3: dW3, dA2
+    if (!(ok = tcRound(sm, bar, phase, [&] {
+          tcIssue<TC_M, H>(sm, TT_AT, TT_DZT, tmem + TT_DW3, acc);
+          tcIssue<H, H>(sm, TT_DZ, TT_BW3, tmem, false);
+        })))
+      break;
+    {
+      uint16_t hv[H];
+      getRow64(sm, TT_H2, t, hv);
+      backEpilogue(sm, tRow, hv, gb + H, t);
+      getRow64(sm, TT_H1, t, hv);
+      putColumn(sm, TT_AT, t, hv, H);
+    }
+    // layer 2: dW2, dA1
+    if (!(ok = tcRound(sm, bar, phase, [&] {
+          tcIssue<TC_M, H>(sm, TT_AT, TT_DZT, tmem + TT_DW2, acc);
+          tcIssue<H, H>(sm, TT_DZ, TT_BW2, tmem, false);
+        })))
+      break;
+    {
+      uint16_t hv[H];
+      getRow64(sm, TT_H1, t, hv);
+      backEpilogue(sm, tRow, hv, gb, t);
+      // X^T in rows 0..15 of the transposed operand, zeros over the rows of H1^T above them
+      uint16_t xv[H];
+      for (int k = 0; k < H; k++) xv[k] = k < 16 ? xb[k] : (uint16_t)0;
+      putColumn(sm, TT_AT, t, xv, H);
+    }
+    // layer 1: dW1
+    if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<TC_M, H>(sm, TT_AT, TT_DZT, tmem + TT_DW1, acc); }))) break;
+    first = false;
+  }
+  if (!ok && t == 0) {
+    atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT);
+    st->detail = -1;
+  }
+  // the CTA's sums into the global gradient: weight rows are TMEM lanes (inputs), columns the outputs
+  if (ok && !first) {
+    const int m = 32 * warp + (t & 31);  // this thread's input row
+    for (int c = 0; c < TC_N4; c += 16) {
+      float v[16];
+      tcLoad16(tmem + lane0 + TT_DW4 + c, v);
+      if (m < H)
+        for (int k = 0; k < 8; k++) if (v[k] != 0.f) atomicAdd(&grad[OFF_W4 + m * 8 + k], v[k]);
+    }
+    for (int c = 0; c < H; c += 16) {
+      float v3[16], v2[16], v1[16];
+      tcLoad16(tmem + lane0 + TT_DW3 + c, v3);
+      tcLoad16(tmem + lane0 + TT_DW2 + c, v2);
+      tcLoad16(tmem + lane0 + TT_DW1 + c, v1);
+      for (int k = 0; k < 16; k++) {
+        if (m < H && v3[k] != 0.f) atomicAdd(&grad[OFF_W3 + m * H + c + k], v3[k]);
+        if (m < H && v2[k] != 0.f) atomicAdd(&grad[OFF_W2 + m * H + c + k], v2[k]);
+        if (m < 16 && v1[k] != 0.f) atomicAdd(&grad[OFF_W1 + m * H + c + k], v1[k]);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) myLoss += __shfl_xor_sync(0xffffffffu, myLoss, o);
+  if ((t & 31) == 0) atomicAdd(reinterpret_cast<float*>(sm + TT_LOSS), myLoss);
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  if (ok && !first) {
+    for (int e = t; e < 3 * H + ELL_TARGETS; e += blockDim.x) {
+      const int l = e / H, j = e % H;
+      const int off = l == 0 ? OFF_B1 + j : (l == 1 ? OFF_B2 + j : (l == 2 ? OFF_B3 + j : OFF_B4 + j));
+      if (gb[e] != 0.f) atomicAdd(&grad[off], gb[e]);
+    }
+    if (t == 0) atomicAdd(loss, *reinterpret_cast<float*>(sm + TT_LOSS));
+  }
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TT_COLS) : "memory");
+}
+
 
 }  // namespace
 
@@ -537,7 +614,8 @@ cudaError_t mlp_prepare_kernels() {
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(k_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC))) return e;
   if ((e = cudaFuncSetAttribute(k_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC))) return e;
-  return cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TRAIN);
+  if ((e = cudaFuncSetAttribute(k_mlp_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC_TRAIN))) return e;
+  return cudaSuccess;
 }
 
 void mlp_to_bf16(cudaStream_t s, const float* w, uint16_t* wbf) {
@@ -566,11 +644,12 @@ void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, c
 }
 
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
-                     float* grad, float* loss) {
+                     float* grad, float* loss, DeviceStatus* st, int numSMs) {
   if (n <= 0) return;
-  long long blocks = (n + SAMPLES - 1) / SAMPLES;
-  if (blocks > 152 * 2) blocks = 152 * 2;
-  (k_mlp_grad<<<(unsigned)blocks, 128, SMEM_TRAIN, s>>>(rec, idx, n, 1.0f / (float)n, wbf, wf, grad, loss),
+  long long blocks = (n + TC_M - 1) / TC_M;
+  const long long sms = numSMs > 0 ? numSMs : 152;  // one CTA per SM: it holds 512 TMEM columns
+  if (blocks > sms) blocks = sms;
+  (k_mlp_grad_tc<<<(unsigned)blocks, 128, SMEM_TC_TRAIN, s>>>(rec, idx, n, 1.0f / (float)n, wbf, wf, grad, loss, st),
    ++::wdem::g_kernel_launches);
 }
 

@@ -380,8 +380,7 @@ int ensureScratch(wdem_handle* h, long long nc) {
     CK(dalloc(cs.keys, cap)); CK(dalloc(cs.keysAlt, cap));
     CK(dalloc(cs.vals, cap)); CK(dalloc(cs.valsAlt, cap));
     cs.sortCap = cap;
-    long long tiles = (cap + 2047) / 2048;
-    cs.histCap = 256 * tiles + 1;
+    cs.histCap = radix_scratch_words(cap);
     CK(dalloc(cs.hist, cs.histCap));
   }
   if (h->periodic && (long long)h->smallIds.size() + 1 > cs.periCap) {
@@ -721,6 +720,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   h->cs.maxCols = std::max(1024, std::min(1 << 24, 2 * N));
   ok &= dalloc(h->cs.cellStart, (size_t)h->cs.maxCols + 2) == cudaSuccess;
   ok &= dalloc(h->dst, 1) == cudaSuccess;
+  h->cs.st = h->dst;
   ok &= cudaMallocHost((void**)&h->hst, sizeof(DeviceStatus)) == cudaSuccess;
   ok &= cudaMallocHost((void**)&h->hcounts, 4 * sizeof(unsigned)) == cudaSuccess;
   if (!ok) { wdem_destroy(h); return WDEM_ERR_CUDA; }
@@ -2215,14 +2215,17 @@ int wdem_warm_grad(wdem_handle* h, const float* records, int64_t n, float* grad,
   cudaMemcpyAsync(dr, records, (size_t)n * WDEM_WARM_RECORD * sizeof(float), cudaMemcpyHostToDevice, h->stream);
   cudaMemsetAsync(h->mlpGrad, 0, mlp_npad() * sizeof(float), h->stream);
   cudaMemsetAsync(h->mlpLoss, 0, sizeof(float), h->stream);
-  mlp_launch_grad(h->stream, dr, nullptr, n, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss);
+  mlp_launch_grad(h->stream, dr, nullptr, n, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss, h->dst, h->numSMs);
   std::vector<float> pad(mlp_npad());
   cudaMemcpyAsync(pad.data(), h->mlpGrad, pad.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
   cudaMemcpyAsync(loss, h->mlpLoss, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
   cudaMemsetAsync(h->mlpGrad, 0, mlp_npad() * sizeof(float), h->stream);
+  cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
   cudaFree(dr);
   if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
+  int rc;
+  if ((rc = checkDeviceStatus(h))) return rc;
   mlp_pack(pad.data(), grad);
   return WDEM_OK;
 }
@@ -2254,7 +2257,7 @@ int wdem_warm_train(wdem_handle* h, const float* records, int64_t n, int32_t epo
     long long nb = 0;
     for (int64_t b0 = 0; b0 < n; b0 += batch, nb++, step++) {
       const long long m = std::min<long long>(batch, n - b0);
-      mlp_launch_grad(s, dr, didx + b0, m, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss);
+      mlp_launch_grad(s, dr, didx + b0, m, h->mlpWbf, h->mlpW, h->mlpGrad, h->mlpLoss, h->dst, h->numSMs);
       h->mlpT++;
       const float c1 = 1.f - std::pow(b1, (float)h->mlpT), c2 = 1.f - std::pow(b2, (float)h->mlpT);
       // half-cosine decay from lr to lr/100 over all steps of this call
@@ -2269,7 +2272,9 @@ int wdem_warm_train(wdem_handle* h, const float* records, int64_t n, int32_t epo
   }
   cudaFree(dr); cudaFree(didx);
   if (e != cudaSuccess) return fail(h, WDEM_ERR_CUDA, cudaGetErrorString(e));
-  return WDEM_OK;
+  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return checkDeviceStatus(h);
 }
 
 int wdem_ell_log(wdem_handle* h, int64_t capRecords) {

@@ -332,11 +332,13 @@ struct ColliderScratch {
   unsigned* candFlag;
   long long candCap;
   void* temp;                           // small scratch (extent reduction)
+  DeviceStatus* st;                     // the handle's status word (bounded waits report there)
   long long launches;                   // kernels launched by the collider (counted on the host)
 };
 void launch_bboxes(cudaStream_t s, const StepParams& P, Particles p, int n);
 void col_extents_and_grid(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
 void col_sort(cudaStream_t s, Particles p, const int* small, int nSmall, ColliderScratch& cs);
+long long radix_scratch_words(long long n);  // radix-sort scratch (cs.hist) for n keys
 void col_sweep(cudaStream_t s, Particles p, int nSmall, unsigned loneMask, ColliderScratch& cs, int2* out,
                long long cap, bool write, DeviceStatus* st);
 // periodic collider: 3-D cell grid, FP32 candidates, exact spatialOverlapPeri, emission
@@ -358,7 +360,7 @@ void mlp_launch_warm(cudaStream_t s, Particles p, Contacts c, long long nc, cons
 void mlp_launch_predict(cudaStream_t s, const float* X, long long n, float* Y, const uint16_t* wbf, const float* wf,
                         DeviceStatus* st);
 void mlp_launch_grad(cudaStream_t s, const float* rec, const int* idx, long long n, const uint16_t* wbf, const float* wf,
-                     float* grad, float* loss);
+                     float* grad, float* loss, DeviceStatus* st, int numSMs);
 void mlp_launch_adam(cudaStream_t s, float* w, float* m, float* v, float* grad, uint16_t* wbf, float lr, float b1,
                      float b2, float c1, float c2, float eps);
 // k_edit.cu: particle removal and insertion between steps
