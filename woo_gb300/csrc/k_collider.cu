@@ -840,14 +840,18 @@ __global__ void k_csr_entries(Contacts c, long long nc, int idBits, unsigned lon
   vals[2 * e + 1] = (unsigned)e | 0x80000000u;
 }
 // the sorted entries, and each contact's two entry positions (where the contact pass writes its shares)
-__global__ void k_csr_ent_slots(const unsigned* vals, long long ne, unsigned* ent, int2* slot) {
+// with their positions in the rows (which bit of the row's mask the contact pass sets)
+__global__ void k_csr_ent_slots(const unsigned* vals, const unsigned long long* keys, int idBits, const int* rowptr,
+                                long long ne, unsigned* ent, int2* slot, uchar2* rowBit) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
   const unsigned v = vals[e];
   ent[e] = v;
   const unsigned ci = v & 0x7fffffffu;
-  if (v >> 31) slot[ci].y = (int)e;
-  else slot[ci].x = (int)e;
+  const long long k = e - rowptr[keys[e] >> idBits];
+  const unsigned char bit = (unsigned char)(k < 31 ? k : 31);
+  if (v >> 31) { slot[ci].y = (int)e; rowBit[ci].y = bit; }
+  else { slot[ci].x = (int)e; rowBit[ci].x = bit; }
 }
 __global__ void k_csr_rows(const unsigned long long* keys, long long ne, int idBits, int n, int* rowptr) {
   long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1195,7 +1199,9 @@ void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderS
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, ne, 2 * idBits, cs);
   long long threads = ne > 0 ? ne : (long long)n + 1;
   (k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr), ++::wdem::g_kernel_launches);
-  if (ne > 0) (k_csr_ent_slots<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(cs.vals, ne, csr.ent, c.slot), ++::wdem::g_kernel_launches);
+  if (ne > 0)
+    (k_csr_ent_slots<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(cs.vals, cs.keys, idBits, csr.rowptr, ne, csr.ent, c.slot, c.rowBit),
+     ++::wdem::g_kernel_launches);
 }
 
 }  // namespace wdem

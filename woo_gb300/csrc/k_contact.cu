@@ -677,8 +677,13 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
     d3 relVel = PERI ? (vel2 + shiftVel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x))
                      : (vel2 + cross(angVel2, c2x)) - (vel1 + cross(angVel1, c1x));
     gvel = mk(dot(mid0, relVel), dot(mid1, relVel), dot(mid2, relVel));
-    d3 dw = angVel2 - angVel1;
-    gangVel = mk(dot(mid0, dw), dot(mid1, dw), dot(mid2, dw));
+    // L6Geom.angVel feeds only the rolling/twisting resistance of IdealElPl and the downloaded geometry
+    if (c.geom[0] || (LAW == WDEM_LAW_IDEALELPL && P.relRollStiff > 0. && P.rollTanPhi > 0.)) {
+      const d3 dw = angVel2 - angVel1;
+      gangVel = mk(dot(mid0, dw), dot(mid1, dw), dot(mid2, dw));
+    } else {
+      gangVel = mk(0, 0, 0);
+    }
     fx = c.hist[HIST_FX][i]; fy = c.hist[HIST_FY][i]; fz = c.hist[HIST_FZ][i];
     kn = c.hist[HIST_KN][i]; kt = c.hist[HIST_KT][i];
     tanPhi = c.tanPhi[i];
@@ -829,6 +834,8 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   }
   // Contact::getForceTorqueBranch: F = ori*force, T = ori*torque (zero if torque is zero),
   // branch xc = contPt - node pos; the particle receives F and xc x F + T (sign -1 for pB)
+  // (the quaternion of the frame, not the frame's columns: the frame update is first order and drifts from
+  // orthonormality between renormalisations, which Quaternion(Matrix3) absorbs)
   const qd ori = quatFromCols(cur0, cur1, cur2);
   const d3 F = qrot(ori, mk(fx, fy, fz));
   const d3 tq = mk(tqx, tqy, tqz);
@@ -850,6 +857,12 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   double4_32a* ob = c.out + OUT_RECORDS * (long long)sl.y;
   ob[OUT_F] = make_double4_32a(FB.x, FB.y, FB.z, stamp);
   ob[OUT_T] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
+  // the row positions this pass stamped, for the integrator's gather
+  if (p.rowMask) {
+    const uchar2 rb = c.rowBit[i];
+    if (PERI || !(sb & CS_FACET)) atomicOr(&p.rowMask[a], 1u << rb.x);
+    atomicOr(&p.rowMask[b], 1u << rb.y);
+  }
 }
 
 // BS threads a block and 512 threads an SM (<= 128 registers a thread, no spills); the grid (blocks per

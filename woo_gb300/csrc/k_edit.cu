@@ -38,6 +38,7 @@ __global__ void k_kill_slots(Particles p, const int* ids, int m, const double* p
   p.force[i] = make_double4_32a(0, 0, 0, 0);
   p.torque[i] = make_double4_32a(0, 0, 0, 0);
   p.touched[i] = 0;
+  p.rowMask[i] = 0;
 }
 
 __global__ void k_kill_contacts(Contacts c, long long nc, const uint8_t* gone) {
@@ -73,6 +74,7 @@ __global__ void k_put_slots(Particles p, const int* ids, int m, const double4_32
   p.lastPos[i] = make_double4_32a(r[0].x, r[0].y, r[0].z, 0);
   p.posf[i] = make_float4((float)r[0].x, (float)r[0].y, (float)r[0].z, (float)r[0].w);
   p.touched[i] = 0;
+  p.rowMask[i] = 0;
   if (withRot) {
     p.semi[i] = r[7];
     p.angMom[i] = r[8];

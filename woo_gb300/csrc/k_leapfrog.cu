@@ -30,6 +30,34 @@ __device__ __forceinline__ void gatherRow(long long want, int i, const Contacts&
   }
 }
 
+// The same sum over the entries of the row that the contact pass marked in the particle's row mask, in the
+// row's order: an entry outside the mask was not stamped by that pass; a stale bit (from a pass before a
+// rebuild) fails the stamp test as in gatherRow.
+__device__ __forceinline__ void gatherRowMasked(long long want, int i, unsigned mask, const Contacts& c, const Csr& csr,
+                                                d3& F, d3& T) {
+  const int e0 = csr.rowptr[i], e1 = csr.rowptr[i + 1];
+  unsigned lo = mask & 0x7fffffffu;
+  while (lo) {
+    const int e = e0 + __ffs(lo) - 1;
+    lo &= lo - 1;
+    if (e >= e1) break;
+    const double4_32a* o = c.out + OUT_RECORDS * (long long)e;
+    const double4_32a f4 = o[OUT_F];
+    if (__double_as_longlong(f4.w) != want) continue;
+    F = F + xyz(f4);
+    T = T + xyz(o[OUT_T]);
+  }
+  if (mask & 0x80000000u) {
+    for (int e = e0 + 31; e < e1; e++) {
+      const double4_32a* o = c.out + OUT_RECORDS * (long long)e;
+      const double4_32a f4 = o[OUT_F];
+      if (__double_as_longlong(f4.w) != want) continue;
+      F = F + xyz(f4);
+      T = T + xyz(o[OUT_T]);
+    }
+  }
+}
+
 __device__ __forceinline__ void gatherForce(const StepParams& P, long long want, int i, double mass, unsigned flags,
                                             const Contacts& c, const Csr& csr, d3& F, d3& T) {
   const bool grav = P.hasGravity && !(flags & WDEM_GRAVITY_SKIP);
@@ -132,6 +160,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(StepParams P, Particles p, int
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   const long long step = stepOf(P, st);
   if (i >= n || haltedIntegrator(st, step)) return;
+  if (p.rowMask) p.rowMask[i] = 0;  // this path gathers whole rows; the marks of the last pass are consumed
   const int4 meta = p.meta[i];
   const unsigned flags = (unsigned)meta.w;
   const bool asph = ELL && (meta.x & META_ASPH);
@@ -404,7 +433,8 @@ __device__ __forceinline__ FastRec loadFast(const Particles& p, int i) {
 
 template <bool PERI>
 __device__ __forceinline__ void integrateFast(const StepParams& P, const Particles& p, const int i, const int n, const Contacts& c,
-                                              const Csr& csr, DeviceStatus* st, const bool touchedNow, const FastRec& rec) {
+                                              const Csr& csr, DeviceStatus* st, const bool touchedNow, const FastRec& rec,
+                                              const unsigned rowMask) {
   const int4 meta = rec.meta;
   const unsigned flags = (unsigned)meta.w;
   const double4_32a vm = rec.vm;
@@ -424,7 +454,7 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
              gravForce(mass, mf, P.gravity[2], skipAxis == 2));
     } else F = mk(0, 0, 0);
     T = mk(0, 0, 0);
-    if (touchedNow) gatherRow(seqOf(P, st) - 1, i, c, csr, F, T);
+    if (touchedNow) gatherRowMasked(seqOf(P, st) - 1, i, rowMask, c, csr, F, T);
   } else {
     F = mk(0, 0, 0); T = mk(0, 0, 0);
   }
@@ -626,7 +656,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS) k_leapfrog_fast(StepParams P, P
     if (listed && slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
   }
   if (listed) return;
-  integrateFast<PERI>(P, p, i, n, c, csr, st, false, rec);
+  integrateFast<PERI>(P, p, i, n, c, csr, st, false, rec, 0u);
 }
 
 // Second pass, over two lists: the touched particles (CSR force gather, full integration, rotation
@@ -641,7 +671,9 @@ __global__ void __launch_bounds__(256) k_leapfrog_lists(StepParams P, Particles 
     if (k < nt) {
       const int i = (int)p.touchList[k];
       p.touched[i] = 0;
-      integrateFast<PERI>(P, p, i, n, c, csr, st, true, loadFast(p, i));
+      const unsigned m = p.rowMask[i];
+      p.rowMask[i] = 0;
+      integrateFast<PERI>(P, p, i, n, c, csr, st, true, loadFast(p, i), m);
     } else {
       const unsigned i = p.rotList[k - nt];
       rotateSphere(P, p, i, xyz(p.angw[i]), p.meta[i].y);

@@ -276,7 +276,7 @@ void freeContacts(ContactBuf& b) {
   Contacts& c = b.c;
   cudaFree(c.ids); cudaFree(c.state); cudaFree(c.act); cudaFree(c.step0); cudaFree(c.tanPhi);
   for (int k = 0; k < HIST_COUNT; k++) cudaFree(c.hist[k]);
-  cudaFree(c.out); cudaFree(c.slot);
+  cudaFree(c.out); cudaFree(c.slot); cudaFree(c.rowBit);
   for (int k = 0; k < 7; k++) cudaFree(c.geom[k]);
   for (int k = 0; k < EC_COUNT; k++) cudaFree(c.energy[k]);
   cudaFree(c.cdist);
@@ -302,6 +302,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if ((e = dalloc(c.out, (size_t)OUT_RECORDS * 2 * cap))) return e;
   if ((e = cudaMemset(c.out, 0xff, (size_t)OUT_RECORDS * 2 * cap * sizeof(double4_32a)))) return e;
   if ((e = dalloc(c.slot, cap))) return e;
+  if ((e = dalloc(c.rowBit, cap))) return e;
   if (geom) for (int k = 0; k < 7; k++) if ((e = dalloc(c.geom[k], cap))) return e;
   for (int k = 0; k < EC_COUNT; k++) if ((e = dalloc(c.energy[k], cap))) return e;
   if ((e = dalloc(c.work, cap))) return e;
@@ -702,6 +703,7 @@ int wdem_create(int device, int32_t maxParticles, wdem_handle** out) {
   ok &= dalloc(d.posf, N) == cudaSuccess;
   ok &= dalloc(d.lastPosf, N) == cudaSuccess;
   ok &= dalloc(d.touched, N) == cudaSuccess;
+  ok &= dalloc(d.rowMask, N) == cudaSuccess;
   ok &= dalloc(d.rotList, N) == cudaSuccess;
   ok &= dalloc(d.touchList, N) == cudaSuccess;
   for (int k = 0; k < 3; k++) ok &= dalloc(d.energy[k], N) == cudaSuccess;
@@ -747,7 +749,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(h->dMatDt); cudaFree(h->cs.sceneWall);
   cudaFree(h->mlpW); cudaFree(h->mlpM); cudaFree(h->mlpV); cudaFree(h->mlpGrad); cudaFree(h->mlpLoss); cudaFree(h->mlpWbf);
   cudaFree(d.posr); cudaFree(d.velm); cudaFree(d.angw); cudaFree(d.inert); cudaFree(d.ori);
-  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rotList); cudaFree(d.touchList);
+  cudaFree(d.lastPos); cudaFree(d.bbmin); cudaFree(d.bbmax); cudaFree(d.force); cudaFree(d.torque); cudaFree(d.meta); cudaFree(d.posf); cudaFree(d.lastPosf); cudaFree(d.touched); cudaFree(d.rowMask); cudaFree(d.rotList); cudaFree(d.touchList);
   for (int k = 0; k < 3; k++) cudaFree(d.energy[k]);
   cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
@@ -1012,6 +1014,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   }
   launch_refresh_posf(s, h->d, n);
   if (n > 0) CK(cudaMemsetAsync(h->d.touched, 0, n, s));
+  if (n > 0) CK(cudaMemsetAsync(h->d.rowMask, 0, n * sizeof(unsigned), s));
   CK(cudaStreamSynchronize(s));
   h->nContacts = 0;
   h->forcesInArrays = true;

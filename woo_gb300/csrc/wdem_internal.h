@@ -174,6 +174,8 @@ struct Particles {
   float4* lastPosf;   // FP32 shadow of lastPos (truncated), for the verlet trigger
   double4_32a *fv1, *fv2;  // facets: nodes 1 and 2 (node 0 is posr); null when the scene has no facets
   uint8_t* touched;   // 1 when a real contact of the last contact pass involves the particle
+  unsigned* rowMask;  // positions in the particle's CSR row that the last contact pass stamped: bit k for
+                      // entry rowptr + k (k < 31), bit 31 for any entry from rowptr + 31 on
   unsigned* rotList;    // untouched spinning spheres, rotated by the integrator's list pass this step
   unsigned* touchList;  // particles with contact forces this step (integrated by the list pass)
   int4* meta;
@@ -190,6 +192,7 @@ struct Contacts {
   double* hist[HIST_COUNT];
   double* tanPhi;
   int2* slot;        // CSR entries of the contact: (pA's, pB's)
+  uchar2* rowBit;    // the same entries as positions in their rows, min(position, 31)
   double4_32a* out;  // OUT_RECORDS records per CSR entry e: out[OUT_RECORDS * e + OUT_F / OUT_T] (capacity 2C entries)
   double* geom[7];  // optional (download): L6Geom.uN, vel (3), angVel (3); null when not kept
   double* energy[EC_COUNT];  // per-contact energy terms of this step when tracked (else null)
