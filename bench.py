@@ -79,9 +79,10 @@ def parse():
     ap.add_argument("--n", type=int, default=None,
                     help="particle count of a smaller cut of the workload (same density; for profiling runs)")
     ap.add_argument("--no-settled", action="store_true", help="hertz1M: leave out the settled-state object")
-    ap.add_argument("--arith", default="fma", choices=["fma", "exact"],
+    ap.add_argument("--arith", default="fma", choices=["fma", "dw", "exact"],
                     help="arithmetic of the contact and integrator kernels (wdem_params.arith): FP64 with FMA "
-                         "contraction, or the reference's IEEE operations bit for bit")
+                         "contraction, that with the contact law in double-word FP32, or the reference's IEEE "
+                         "operations bit for bit")
     ap.add_argument("--autotune", default="auto", choices=["auto", "on", "off"],
                     help="tune the kernels' launch shape (wdem_autotune) before the timed region; auto: batch512 only")
     ap.add_argument("--graphs", default="off", choices=["auto", "on", "off"],
@@ -501,7 +502,7 @@ def run_gpu(args, rank, world, local):
 
     wbuild.build()
     spec = build_scene(args.workload, n=args.n)
-    spec.params.arith = abi.ARITH_FMA if args.arith == "fma" else abi.ARITH_EXACT
+    spec.params.arith = {"fma": abi.ARITH_FMA, "dw": abi.ARITH_DW, "exact": abi.ARITH_EXACT}[args.arith]
     n = spec.particles.n
     extra = {}
     if args.workload == "ell200k":
@@ -610,6 +611,13 @@ def run_gpu(args, rank, world, local):
             hs.set_params(pe)
             ex = measure_region(hs, spec, args, world, local, barrier, "settled_exact")
             settled["exact_arith"] = {k: ex[k] for k in ("value", "ms_per_step", "contacts", "kernels")}
+            # and with the contact law in double-word FP32 (the same 1e-12 bar as the contracted variant)
+            pd = copy_params(spec.params)
+            pd.arith = abi.ARITH_DW
+            pd.step = hs.status().step
+            hs.set_params(pd)
+            dw = measure_region(hs, spec, args, world, local, barrier, "settled_dw")
+            settled["dw_arith"] = {k: dw[k] for k in ("value", "ms_per_step", "contacts", "kernels", "rooflines")}
             pf = copy_params(spec.params)
             pf.step = hs.status().step
             hs.set_params(pf)

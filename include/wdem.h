@@ -65,7 +65,7 @@ enum { WDEM_CP2_FRICT = 0, WDEM_CP2_HERTZ = 1 };                 /* Cp2_FrictMat
 enum { WDEM_LAW_IDEALELPL = 0, WDEM_LAW_HERTZ_DMT = 1 };         /* Law2_L6Geom_FrictPhys_IdealElPl, Law2_L6Geom_HertzPhys_DMT */
 enum { WDEM_UPDATE_PHYS_NEVER = 0, WDEM_UPDATE_PHYS_ALWAYS = 1, WDEM_UPDATE_PHYS_ONCE = 2 };
 /* wdem_params.arith: the arithmetic of the contact and integrator kernels (no counterpart in the reference) */
-enum { WDEM_ARITH_EXACT = 0, WDEM_ARITH_FMA = 1 };
+enum { WDEM_ARITH_EXACT = 0, WDEM_ARITH_FMA = 1, WDEM_ARITH_DW = 2 };
 
 /* DemData.flags bits (src/dem/Particle.hpp:197-200) */
 enum {
@@ -151,7 +151,10 @@ typedef struct wdem_params {
    * WDEM_ARITH_EXACT (0) = the reference's IEEE FP64 operations in its order, results equal to the CPU
    * restatement bit for bit; WDEM_ARITH_FMA (1) = FP64 multiply-adds contracted into FMAs and one
    * reciprocal per division of a vector by a scalar (per-contact forces within 1e-12 relative of the exact
-   * ones after one step from the same state; the collider's pair set is unchanged for the same boxes). */
+   * ones after one step from the same state; the collider's pair set is unchanged for the same boxes);
+   * WDEM_ARITH_DW (2) = as FMA, and the update of real sphere and wall contacts (frame, law, force
+   * rotation, branch torques) in double-word FP32 arithmetic of 48 significant bits, positions, overlaps,
+   * contact points and the differences they cancel in kept in FP64 (the same 1e-12 bar). */
   int32_t arith;
   int32_t _pad4;
 } wdem_params;

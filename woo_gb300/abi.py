@@ -32,7 +32,7 @@ WARM_COLD, WARM_MLP, WARM_HISTORY, WARM_HISTORY_MLP = 0, 1, 2, 3
 GRAPHS_OFF, GRAPHS_AUTO, GRAPHS_ON = 0, 1, 2
 MAT_FRICT, MAT_HERTZ = 0, 1
 CP2_FRICT, CP2_HERTZ = 0, 1
-ARITH_EXACT, ARITH_FMA = 0, 1
+ARITH_EXACT, ARITH_FMA, ARITH_DW = 0, 1, 2
 LAW_IDEALELPL, LAW_HERTZ_DMT = 0, 1
 UPDATE_PHYS_NEVER, UPDATE_PHYS_ALWAYS, UPDATE_PHYS_ONCE = 0, 1, 2
 

@@ -19,6 +19,7 @@
 #include "wdem_math.cuh"
 #include "wdem_peri.cuh"
 #include "wdem_ell.cuh"
+#include "wdem_dw.cuh"
 #include "../../include/wdem.h"
 
 namespace wdem {
@@ -865,15 +866,279 @@ __device__ __forceinline__ void contactBody(const StepParams& P, const Particles
   }
 }
 
+#ifdef WDEM_FMA
+// ---------------------------------------------------------------------------- double-word contact law
+// The update of a real sphere-sphere or wall-sphere contact (L6Geom.cpp:79-216 with IdealElPl.cpp:15-92 or
+// Hertz.cpp:85-114,170-210) with the frame, the law and the force rotation in double-word FP32 arithmetic
+// (wdem_dw.cuh, 48 significant bits), selected by wdem_params.arith = WDEM_ARITH_DW.  FP64 stays where a
+// difference cancels: the positions, the centre distance and the overlap uN = |d| - r1 - r2 (square root of
+// the exactly rounded squared distance), the contact point, and the differences of positions and of
+// velocities that the branch vectors and the relative velocity start from.  Everything else (the frame
+// update, the local velocities, the Hertz or ideal-plastic law, the Coulomb cap, the quaternion of the frame
+// and the rotation of the force, the branch torques) runs on the FP32 pipes.  New contacts, facets, rolling
+// resistance, energy tracking, updatePhys and approxMask keep the FP64 law for the whole pass (the host
+// decides, dwEligible); the double-word kernel takes the real contacts at the front of the work list and
+// the FP64 kernel the potential pairs behind them, so that neither kernel carries both bodies.
+__device__ __forceinline__ double fToD(float f) {  // exact, on the integer pipe (subnormals as zero)
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sgn);
+  if (e == 0xffu) return (double)f;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ double dwToD(dwf x) { return fToD(x.h) + fToD(x.l); }
+__device__ __forceinline__ dw3 dw3Of(d3 v) { return dw3From(v.x, v.y, v.z); }
+__device__ __forceinline__ d3 dw3ToD(dw3 v) { return mk(dwToD(v.x), dwToD(v.y), dwToD(v.z)); }
+__device__ __forceinline__ dw3 dw3Scale(dw3 a, float p2) { return {dwScale(a.x, p2), dwScale(a.y, p2), dwScale(a.z, p2)}; }
+__device__ __forceinline__ dw3 dw3Normalized(dw3 a) { return dw3Mul(a, dwRecip(dwSqrt(dw3Sq(a)))); }
+struct dwq {
+  dwf w, x, y, z;
+};
+// Quaternion(Matrix3) of the frame with columns c0, c1, c2 (the branches of quatFromCols)
+__device__ __forceinline__ dwq dwQuatFromCols(dw3 c0, dw3 c1, dw3 c2) {
+  const dwf m00 = c0.x, m10 = c0.y, m20 = c0.z, m01 = c1.x, m11 = c1.y, m21 = c1.z, m02 = c2.x, m12 = c2.y, m22 = c2.z;
+  dwq q;
+  const dwf tr = dwAdd(dwAdd(m00, m11), m22);
+  if (dwPos(tr)) {
+    dwf t = dwSqrt(dwAddF(tr, 1.f));
+    q.w = dwScale(t, 0.5f);
+    t = dwScale(dwRecip(t), 0.5f);
+    q.x = dwMul(dwSub(m21, m12), t);
+    q.y = dwMul(dwSub(m02, m20), t);
+    q.z = dwMul(dwSub(m10, m01), t);
+  } else {
+    int i = 0;
+    if (dwGt(m11, m00)) i = 1;
+    if (dwGt(m22, i == 0 ? m00 : m11)) i = 2;
+    if (i == 0) {
+      dwf t = dwSqrt(dwAddF(dwSub(dwSub(m00, m11), m22), 1.f));
+      q.x = dwScale(t, 0.5f); t = dwScale(dwRecip(t), 0.5f);
+      q.w = dwMul(dwSub(m21, m12), t); q.y = dwMul(dwAdd(m10, m01), t); q.z = dwMul(dwAdd(m20, m02), t);
+    } else if (i == 1) {
+      dwf t = dwSqrt(dwAddF(dwSub(dwSub(m11, m22), m00), 1.f));
+      q.y = dwScale(t, 0.5f); t = dwScale(dwRecip(t), 0.5f);
+      q.w = dwMul(dwSub(m02, m20), t); q.z = dwMul(dwAdd(m21, m12), t); q.x = dwMul(dwAdd(m01, m10), t);
+    } else {
+      dwf t = dwSqrt(dwAddF(dwSub(dwSub(m22, m00), m11), 1.f));
+      q.z = dwScale(t, 0.5f); t = dwScale(dwRecip(t), 0.5f);
+      q.w = dwMul(dwSub(m10, m01), t); q.x = dwMul(dwAdd(m02, m20), t); q.y = dwMul(dwAdd(m12, m21), t);
+    }
+  }
+  return q;
+}
+// v rotated by q: uv = q.vec x v, uv += uv, v + w uv + q.vec x uv (as qrot)
+__device__ __forceinline__ dw3 dwQrot(dwq q, dw3 v) {
+  const dw3 qv = {q.x, q.y, q.z};
+  const dw3 uv = dw3Scale(dw3Cross(qv, v), 2.f);
+  return dw3Add(dw3Add(v, dw3Mul(uv, q.w)), dw3Cross(qv, uv));
+}
+
+template <int LAW, int CP2, bool PERI>
+__device__ __forceinline__ void contactBodyDW(const StepParams& P, const Particles& p, const Contacts& c, long long i,
+                                              DeviceStatus* st) {
+  const uint8_t s0 = c.state[i];
+  const uint8_t sb = s0 & CS_SHAPES;
+  if ((s0 & CS_MASK) != CS_REAL) return;  // the front of the work list holds real contacts only
+  const int2 id = c.ids[i];
+  const int a = id.x, b = id.y;
+  const double dtC = P.matDt ? P.matDt[p.meta[a].y] : P.dt;
+  int4 cd = make_int4(0, 0, 0, 0);
+  if (PERI) cd = c.cdist[i];
+  const double4_32a A4 = p.posr[a], B4 = p.posr[b];
+  const d3 pos1 = xyz(A4);
+  d3 shift2 = mk(0, 0, 0);
+  if (PERI) shift2 = mvec(P.hS, mk((double)cd.x, (double)cd.y, (double)cd.z));
+  const d3 pos2 = PERI ? xyz(B4) + shift2 : xyz(B4);
+  double r1, r2, uN;
+  dw3 normal, d1, d2;  // d1, d2: the contact point's offsets from pA's and pB's node (the branch vectors)
+  d3 contPt;
+  if (!(sb & CS_WALL_A)) {
+    // Cg2_Sphere_Sphere_L6Geom::go of a real contact: uN in FP64, the normal and the contact point's offset
+    // from pA in double words
+    r1 = A4.w; r2 = B4.w;
+    const d3 relPos = pos2 - pos1;
+    const double dist = sqrt(sqnormExact(relPos));
+    uN = dist - (r1 + r2);
+    const dw3 relPosW = dw3Of(relPos);
+    normal = dw3Mul(relPosW, dwRecip(dwFrom(dist)));
+    d1 = dw3Mul(normal, dwFrom(r1 + 0.5 * uN));
+    d2 = dw3Sub(d1, relPosW);
+    contPt = pos1 + dw3ToD(d1);
+  } else {
+    // Cg2_Wall_Sphere_L6Geom::go (pA is the wall)
+    const int wa = p.meta[a].x;
+    const int ax = (wa >> 4) & 3, sense = ((wa >> 8) & 3) - 1;
+    const double radius = B4.w;
+    const double dist = comp(pos2, ax) - comp(pos1, ax);
+    contPt = pos2;
+    setComp(contPt, ax, comp(pos1, ax));
+    const double nax = sense == 0 ? comp(mk(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]), ax)
+                                  : (sense == 1 ? 1. : -1.);
+    normal = {dwF(0.f), dwF(0.f), dwF(0.f)};
+    if (ax == 0) normal.x = dwF((float)nax); else if (ax == 1) normal.y = dwF((float)nax); else normal.z = dwF((float)nax);
+    uN = nax * dist - radius;
+    r1 = -radius; r2 = radius;
+    d1 = dw3Of(contPt - pos1);
+    d2 = dw3Of(contPt - pos2);
+  }
+  // L6Geom update (L6Geom.cpp:79-216), approxMask 0
+  const dw3 prevNormal = dw3From(c.hist[HIST_T0X][i], c.hist[HIST_T0Y][i], c.hist[HIST_T0Z][i]);
+  const dw3 prevT1 = dw3From(c.hist[HIST_T1X][i], c.hist[HIST_T1Y][i], c.hist[HIST_T1Z][i]);
+  const d3 prevContPt = mk(c.hist[HIST_CX][i], c.hist[HIST_CY][i], c.hist[HIST_CZ][i]);
+  const dwf dt = dwFrom(dtC);
+  const dwf dtHalf = dwScale(dt, 0.5f);
+  const double4_32a V1 = p.velm[a], V2 = p.velm[b];
+  const double4_32a W1 = p.angw[a], W2 = p.angw[b];
+  const dw3 angVel1 = dw3From(W1.x, W1.y, W1.z), angVel2 = dw3From(W2.x, W2.y, W2.z);
+  const dw3 currNormal = normal;
+  const dw3 normRotVec = dw3Cross(prevNormal, currNormal);
+  dw3 midNormal = dw3Scale(dw3Add(prevNormal, currNormal), 0.5f);
+  if (dwIsZero(dw3Sq(midNormal))) midNormal = currNormal;
+  else midNormal = dw3Normalized(midNormal);
+  const dw3 normTwistVec = dw3Mul(midNormal, dwMul(dtHalf, dw3Dot(midNormal, dw3Add(angVel1, angVel2))));
+  const dw3 rt = dw3Add(normRotVec, normTwistVec);
+  const dw3 mid0 = midNormal;
+  const dw3 mid1 = dw3Sub(prevT1, dw3Scale(dw3Cross(prevT1, rt), 0.5f));
+  const dw3 mid2 = dw3Cross(mid0, mid1);
+  dw3 cur0 = currNormal;
+  dw3 cur1 = dw3Sub(prevT1, dw3Cross(mid1, rt));
+  if (P.trsfRenorm > 0 && (stepOf(P, st) % P.trsfRenorm) == 0) {
+    cur0 = dw3Normalized(cur0);
+    cur1 = dw3Sub(cur1, dw3Mul(cur0, dw3Dot(cur1, cur0)));
+    cur1 = dw3Normalized(cur1);
+  }
+  // branch vectors midContPt - midPos = (contPt - pos) + (prevContPt - contPt) / 2 + dt/2 vel: the offsets
+  // d1, d2 and the FP64 difference of the two contact points, which are close together
+  d3 shiftVel2 = mk(0, 0, 0);
+  if (PERI) shiftVel2 = mvec(P.shv, mk((double)cd.x, (double)cd.y, (double)cd.z));
+  const d3 vel1d = xyz(V1), vel2d = PERI ? xyz(V2) + shiftVel2 : xyz(V2);
+  const dw3 halfPrev = dw3Scale(dw3Of(prevContPt - contPt), 0.5f);
+  const dw3 c1x = (P.noRatch && positiveBits(r1)) ? dw3Mul(midNormal, dwFrom(r1))
+                                                   : dw3Add(dw3Add(d1, halfPrev), dw3Mul(dw3Of(vel1d), dtHalf));
+  const dw3 c2x = (P.noRatch && positiveBits(r2)) ? dw3Mul(midNormal, dwFrom(-r2))
+                                                   : dw3Add(dw3Add(d2, halfPrev), dw3Mul(dw3Of(vel2d), dtHalf));
+  const dw3 relVel = dw3Add(dw3Of(vel2d - vel1d), dw3Sub(dw3Cross(angVel2, c2x), dw3Cross(angVel1, c1x)));
+  const dw3 gvel = {dw3Dot(mid0, relVel), dw3Dot(mid1, relVel), dw3Dot(mid2, relVel)};
+  dwf fx = dwFrom(c.hist[HIST_FX][i]), fy = dwFrom(c.hist[HIST_FY][i]), fz = dwFrom(c.hist[HIST_FZ][i]);
+  double knD = c.hist[HIST_KN][i], ktD = c.hist[HIST_KT][i];
+  const dwf tanPhi = dwFrom(c.tanPhi[i]);
+  const dw3 cur2 = dw3Cross(cur0, cur1);
+  // ---- Law2
+  bool keep = true;
+  if (LAW == WDEM_LAW_IDEALELPL) {
+    if (positiveBits(uN) && !P.noBreak) keep = false;
+    else {
+      fx = dwFrom(knD * uN);  // FP64: the normal force carries the relative error of uN only
+      if (P.noFrict || zeroBits(c.tanPhi[i])) { fy = dwF(0.f); fz = dwF(0.f); }
+      else {
+        const dwf sc = dwFrom(dtC * ktD);
+        fy = dwAdd(fy, dwMul(sc, gvel.y));
+        fz = dwAdd(fz, dwMul(sc, gvel.z));
+        const dwf maxFt = dwMul(dwAbs(fx), tanPhi);
+        const dwf ftSq = dwAdd(dwMul(fy, fy), dwMul(fz, fz));
+        if (dwGt(ftSq, dwMul(maxFt, maxFt)) && !P.noSlip) {
+          const dwf FtNorm = dwSqrt(ftSq);
+          const dwf ratio = dwIsZero(FtNorm) ? dwF(0.f) : dwDiv(maxFt, FtNorm);
+          fy = dwMul(fy, ratio); fz = dwMul(fz, ratio);
+        }
+        if (isnan(fx.h) || isnan(fy.h) || isnan(fz.h)) { if (atomicCAS(&st->code, 0, WDEM_ERR_NAN) == 0) st->detail = a; }
+      }
+    }
+  } else {
+    const double kn0 = c.hist[HIST_E0][i];
+    if (positiveBits(uN)) keep = false;
+    else {
+      // the normal force in FP64 as in the contracted FP64 body: near equilibrium the elastic and adhesive
+      // terms cancel, and the sum must carry no more than the overlap's relative error
+      const double velN = dwToD(gvel.x);
+      const double sq = sqrt(dmax(-uN, 0.));
+      knD = (3 / 2.) * kn0 * sq;
+      const double Fne = -kn0 * pown3(sq);
+      const double Fna = c.hist[HIST_E3][i];
+      const double hz2 = c.hist[HIST_E2][i];
+      const double etaD = positiveBits(hz2) ? hz2 * sqrt(sq) : 0.;
+      double Fnv = etaD * velN;
+      const double alphaC = .5 * (c_mats[p.meta[a].y].alpha + c_mats[p.meta[b].y].alpha);
+      if (zeroBits(alphaC) && P.noAttraction && positiveBits(Fne + Fnv)) Fnv = -Fne;
+      fx = dwFrom(Fne + Fna + Fnv);
+      const dwf eta = dwFrom(etaD);
+      ktD = c.hist[HIST_E1][i] * sq;
+      const dwf sc = dwFrom(dtC * ktD);
+      fy = dwAdd(fy, dwMul(sc, gvel.y));
+      fz = dwAdd(fz, dwMul(sc, gvel.z));
+      const dwf maxFt = dwMul(dwAbs(dwMin(dwF(0.f), fx)), tanPhi);
+      const dwf ftSq = dwAdd(dwMul(fy, fy), dwMul(fz, fz));
+      if (dwGt(ftSq, dwMul(maxFt, maxFt))) {
+        const dwf ratio = dwDiv(maxFt, dwSqrt(ftSq));
+        fy = dwMul(fy, ratio); fz = dwMul(fz, ratio);
+      } else {
+        fy = dwAdd(fy, dwMul(eta, gvel.y));
+        fz = dwAdd(fz, dwMul(eta, gvel.z));
+      }
+    }
+  }
+  if (!keep) {
+    c.state[i] = CS_PENDING | sb;
+    return;
+  }
+  c.state[i] = CS_REAL | sb;
+  if (p.touched) { p.touched[a] = 1; p.touched[b] = 1; }
+  const d3 c0d = dw3ToD(cur0), c1d = dw3ToD(cur1);
+  c.hist[HIST_T0X][i] = c0d.x; c.hist[HIST_T0Y][i] = c0d.y; c.hist[HIST_T0Z][i] = c0d.z;
+  c.hist[HIST_T1X][i] = c1d.x; c.hist[HIST_T1Y][i] = c1d.y; c.hist[HIST_T1Z][i] = c1d.z;
+  c.hist[HIST_CX][i] = contPt.x; c.hist[HIST_CY][i] = contPt.y; c.hist[HIST_CZ][i] = contPt.z;
+  c.hist[HIST_FX][i] = dwToD(fx); c.hist[HIST_FY][i] = dwToD(fy); c.hist[HIST_FZ][i] = dwToD(fz);
+  c.hist[HIST_KN][i] = knD; c.hist[HIST_KT][i] = ktD;
+  if (c.geom[0]) {
+    const dw3 dw_ = dw3Sub(angVel2, angVel1);
+    c.geom[0][i] = uN;
+    c.geom[1][i] = dwToD(gvel.x); c.geom[2][i] = dwToD(gvel.y); c.geom[3][i] = dwToD(gvel.z);
+    c.geom[4][i] = dwToD(dw3Dot(mid0, dw_)); c.geom[5][i] = dwToD(dw3Dot(mid1, dw_)); c.geom[6][i] = dwToD(dw3Dot(mid2, dw_));
+  }
+  // Contact::getForceTorqueBranch: F = ori * force, branch torques xc x F (no CPhys torque on this path)
+  const dw3 F = dwQrot(dwQuatFromCols(cur0, cur1, cur2), dw3{fx, fy, fz});
+  const d3 Fd = dw3ToD(F);
+  const d3 TA = dw3ToD(dw3Cross(d1, F));
+  const d3 TB = dw3ToD(dw3Cross(d2, dw3Scale(F, -1.f)));
+  const int2 sl = c.slot[i];
+  const double stamp = __longlong_as_double(seqOf(P, st));
+  if (PERI || !(sb & CS_FACET)) {
+    double4_32a* oa = c.out + OUT_RECORDS * (long long)sl.x;
+    oa[OUT_F] = make_double4_32a(Fd.x, Fd.y, Fd.z, stamp);
+    oa[OUT_T] = make_double4_32a(TA.x, TA.y, TA.z, 0.0);
+  }
+  double4_32a* ob = c.out + OUT_RECORDS * (long long)sl.y;
+  ob[OUT_F] = make_double4_32a(-Fd.x, -Fd.y, -Fd.z, stamp);
+  ob[OUT_T] = make_double4_32a(TB.x, TB.y, TB.z, 0.0);
+  if (p.rowMask) {
+    const uchar2 rb = c.rowBit[i];
+    if (PERI || !(sb & CS_FACET)) atomicOr(&p.rowMask[a], 1u << rb.x);
+    atomicOr(&p.rowMask[b], 1u << rb.y);
+  }
+}
+#endif
+
 // BS threads a block and 512 threads an SM (<= 128 registers a thread, no spills); the grid (blocks per
 // SM) and BS are the launch shape of the step parameters, chosen by the autotuner or the defaults (128
 // threads, 4 blocks per SM: one wave)
-template <int LAW, int CP2, bool PERI, bool ELL, int BS>
+template <int LAW, int CP2, bool PERI, bool ELL, int BS, bool DW = false>
 __global__ void __launch_bounds__(BS, 512 / BS) k_contacts(StepParams P, Particles p, Contacts c, const unsigned* work,
-                                                        const unsigned* count, long long nc, DeviceStatus* st) {
-  const unsigned m = workLen(count);
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
+                                                        const unsigned* count, long long nc, DeviceStatus* st,
+                                                        int part) {
+  // part 0: the whole work list; 1: the real contacts at its front; 2: the potential pairs behind them
+  const unsigned k0 = part == 2 ? count[0] : 0u;
+  const unsigned m = part == 1 ? count[0] : workLen(count);
+  for (unsigned k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+#ifdef WDEM_FMA
+    if (DW) {
+      contactBodyDW<LAW, CP2, PERI>(P, p, c, (long long)workItem(work, count, nc, k), st);
+      continue;
+    }
+#endif
     contactBody<LAW, CP2, PERI, ELL>(P, p, c, (long long)workItem(work, count, nc, k), st);
+  }
 }
 
 // First pass over all contacts: resolves PENDING contacts (removePending of the collider: the broken
@@ -1035,6 +1300,15 @@ static void launchCull(cudaStream_t s, const StepParams& P, Particles p, Contact
 #undef WDEM_CULL
   ++::wdem::g_kernel_launches;
 }
+#ifdef WDEM_FMA
+// the double-word law applies to the whole pass: no facets, no energy tracking, no updatePhys, no approxMask,
+// no rolling resistance
+template <int LAW>
+static bool dwEligible(const StepParams& P) {
+  return P.dw && !P.hasFacets && !P.trackEnergy && !P.updatePhysNow && P.approxMask == 0 &&
+         !(LAW == WDEM_LAW_IDEALELPL && P.relRollStiff > 0. && P.rollTanPhi > 0.);
+}
+#endif
 // the FP64 pass with the block size and blocks per SM of the launch shape
 template <int LAW, int CP2, bool PERI, bool ELL>
 static void launchHeavy(cudaStream_t s, const StepParams& P, Particles p, Contacts c, long long nc, unsigned* count,
@@ -1044,9 +1318,20 @@ static void launchHeavy(cudaStream_t s, const StepParams& P, Particles p, Contac
   const long long perSM = P.shContactsPerSM > 0 ? P.shContactsPerSM : 512 / bs;
   const long long need = (nc + bs - 1) / bs;
   const unsigned hb = (unsigned)std::max<long long>(1, std::min(need, sms * perSM));
-  if (bs == 64) k_contacts<LAW, CP2, PERI, ELL, 64><<<hb, 64, 0, s>>>(P, p, c, c.work, count, nc, st);
-  else if (bs == 256) k_contacts<LAW, CP2, PERI, ELL, 256><<<hb, 256, 0, s>>>(P, p, c, c.work, count, nc, st);
-  else k_contacts<LAW, CP2, PERI, ELL, 128><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st);
+  int part = 0;
+#ifdef WDEM_FMA
+  if (!ELL && dwEligible<LAW>(P)) {
+    // the double-word law for the real contacts, then the FP64 kernel for the potential pairs
+    if (bs == 64) k_contacts<LAW, CP2, PERI, false, 64, true><<<hb, 64, 0, s>>>(P, p, c, c.work, count, nc, st, 1);
+    else if (bs == 256) k_contacts<LAW, CP2, PERI, false, 256, true><<<hb, 256, 0, s>>>(P, p, c, c.work, count, nc, st, 1);
+    else k_contacts<LAW, CP2, PERI, false, 128, true><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st, 1);
+    ++::wdem::g_kernel_launches;
+    part = 2;
+  }
+#endif
+  if (bs == 64) k_contacts<LAW, CP2, PERI, ELL, 64><<<hb, 64, 0, s>>>(P, p, c, c.work, count, nc, st, part);
+  else if (bs == 256) k_contacts<LAW, CP2, PERI, ELL, 256><<<hb, 256, 0, s>>>(P, p, c, c.work, count, nc, st, part);
+  else k_contacts<LAW, CP2, PERI, ELL, 128><<<hb, 128, 0, s>>>(P, p, c, c.work, count, nc, st, part);
   ++::wdem::g_kernel_launches;
 }
 

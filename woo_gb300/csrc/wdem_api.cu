@@ -202,6 +202,7 @@ struct wdem_handle {
   long long stagingCap = 0;
   bool periodic = false;
   bool hasEll = false;          // ellipsoids or aspherical nodes: per-particle rotation state allocated
+  bool hasFacets = false;       // facets among the particles (their contacts take the FP64 law)
   // facet + wall / facet + facet pairs of one scene whose masks share bits (facet, other, mask & mask); none may
   // survive loneMask at a step
   std::vector<int4> facetPairs;
@@ -579,6 +580,7 @@ void fillStepParams(wdem_handle* h) {
   P.noRatch = r.noRatch; P.iniLensTouch = r.iniLensTouch; P.trsfRenorm = r.trsfRenorm; P.approxMask = r.approxMask;
   P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
   P.cp2 = r.cp2; P.law = r.law;
+  P.dw = r.arith == WDEM_ARITH_DW ? 1 : 0;
   P.noSlip = r.noSlip; P.noBreak = r.noBreak; P.noFrict = r.noFrict;
   P.relRollStiff = r.relRollStiff; P.relTwistStiff = r.relTwistStiff; P.rollTanPhi = r.rollTanPhi;
   P.noAttraction = r.noAttraction;
@@ -592,6 +594,7 @@ void fillStepParams(wdem_handle* h) {
   P.periodic = h->periodic ? 1 : 0;
   P.matDt = h->useMatDt ? h->dMatDt : nullptr;
   P.hasEll = h->hasEll ? 1 : 0;
+  P.hasFacets = h->hasFacets ? 1 : 0;
   P.ellSolver = r.ellSolver;
   P.brentTol = std::ldexp(1.0, 1 - std::min(std::numeric_limits<double>::digits / 2, (int)r.brentBits));
   P.newtonTol = r.newtonTol;
@@ -783,7 +786,8 @@ int wdem_set_params(wdem_handle* h, const wdem_params* p) {
   if (p->iniEqlb) return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_FrictPhys_IdealElPl.iniEqlb is not supported");
   if (!p->iniLensTouch) return fail(h, WDEM_ERR_UNSUPPORTED, "Cg2_*_L6Geom.iniLensTouch=False is not supported");
   if (!p->applyForces) return fail(h, WDEM_ERR_UNSUPPORTED, "ContactLoop.applyForces=False is not supported");
-  if (p->arith != WDEM_ARITH_EXACT && p->arith != WDEM_ARITH_FMA) return fail(h, WDEM_ERR_ARG, "arith must be WDEM_ARITH_EXACT or WDEM_ARITH_FMA");
+  if (p->arith != WDEM_ARITH_EXACT && p->arith != WDEM_ARITH_FMA && p->arith != WDEM_ARITH_DW)
+    return fail(h, WDEM_ERR_ARG, "arith must be WDEM_ARITH_EXACT, WDEM_ARITH_FMA or WDEM_ARITH_DW");
   if (p->nMaterials <= 0 || !p->materials || p->nMaterials > MAX_MATERIALS) return fail(h, WDEM_ERR_ARG, "materials table missing or larger than 1024");
   if (p->law == WDEM_LAW_HERTZ_DMT && p->cp2 != WDEM_CP2_HERTZ)
     return fail(h, WDEM_ERR_UNSUPPORTED, "Law2_L6Geom_HertzPhys_DMT needs Cp2_HertzMat_HertzPhys");
@@ -943,6 +947,7 @@ int wdem_upload_particles(wdem_handle* h, const wdem_particles* p) {
   }
   h->semi = semi;
   h->hasEll = anyEll;
+  h->hasFacets = !facetIds.empty();
   for (int f : facetIds)
     for (int j : h->largeIds) {
       const unsigned mm = p->mask[f] & p->mask[j];
@@ -1078,7 +1083,7 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
     if (b.c.lam) CK(cudaMemsetAsync(b.c.lam, 0xFF, nc * sizeof(double), s));
     if (b.c.lam0) CK(cudaMemsetAsync(b.c.lam0, 0xFF, nc * sizeof(float), s));
   }
-  (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_init_uploaded : launch_init_uploaded)(s, h->P, h->d, b.c, nc);
+  (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_init_uploaded : launch_init_uploaded)(s, h->P, h->d, b.c, nc);
   int rc;
   if ((rc = ensureHash(h, h->cur, nc))) return rc;
   launch_hash_build(s, b.c.ids, nc, h->hk[h->cur], h->hv[h->cur], h->hcap[h->cur], h->dst);
@@ -1173,8 +1178,8 @@ static void launchQueue(wdem_handle* h, StepParams P, int ahead, bool full, bool
   for (int g = 0; g < ahead; g++) {
     P.step = step0 + g;
     P.seq = seq0 + 1 + g;
-    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
-    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, g == 0 && full,
+    (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_leapfrog : launch_leapfrog)(s, P, h->d, h->n, 0, h->buf[h->cur].c, h->csr, h->dst);
+    (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_contacts : launch_contacts)(s, P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, g == 0 && full,
                     warm ? h->mlpWbf : nullptr, warm ? h->mlpW : nullptr);
   }
 }
@@ -1284,7 +1289,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
     CK(cudaMemsetAsync(&h->dst->dirty, 0, sizeof(int), s));
     CK(cudaMemsetAsync(&h->dst->haltAt, 0, sizeof(long long), s));
     if ((rc = rebuild(h))) return rc;
-    (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
+    (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                     warm ? h->mlpW : nullptr);
     h->actValid = true;
     h->sinceRebuild += (int)(k - s0) + 1;
@@ -1382,7 +1387,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     }
     {
       PhaseTimer t(h, PH_LEAPFROG);
-      (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_leapfrog : launch_leapfrog)(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
+      (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_leapfrog : launch_leapfrog)(s, h->P, h->d, h->n, h->forcesInArrays ? 1 : 0, h->buf[h->cur].c, h->csr, h->dst);
     }
     if (h->P.trackEnergy && !h->P.lfEnergy) {
       // kinetic is resettable (EnergyTracker::resetResettables at the start of the step)
@@ -1420,7 +1425,7 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     {
       PhaseTimer t(h, PH_CONTACTS);
       const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
-      (h->raw.arith == WDEM_ARITH_FMA ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
+      (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_contacts : launch_contacts)(s, h->P, h->d, h->buf[h->cur].c, h->nContacts, h->dst, !h->actValid, warm ? h->mlpWbf : nullptr,
                       warm ? h->mlpW : nullptr);
       h->actValid = true;
     }

@@ -102,6 +102,8 @@ struct StepParams {
   double dt;
   long long step;
   long long seq;            // number of this step's contact pass (never reset); stamps the pass's force records
+  int dw;                   // the contact law of real sphere/wall contacts in double-word FP32 (WDEM_ARITH_DW)
+  int hasFacets;            // the scene has facets
   int stepDev;              // 1: step and seq are offsets from DeviceStatus.stepBase/seqBase (steps replayed
                             // from a CUDA graph, whose kernel arguments are fixed at capture)
   double gravity[3];

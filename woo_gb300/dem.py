@@ -1110,7 +1110,8 @@ class GpuDemEngine(Engine):
     Constructed like ContactLoop from the three functor lists (src/dem/ContactLoop.cpp:52-66), plus
     the Leapfrog (damping, reset) and collider (verletDist) attributes.  Runs libwdem.so on one CUDA
     device; errors come back as RuntimeError.  arith: "exact" (the reference's IEEE operations, bit for
-    bit) or "fma" (FP64 multiply-adds contracted, one reciprocal per vector division).  autotune: pick the
+    bit), "fma" (FP64 multiply-adds contracted, one reciprocal per vector division) or "dw" (as "fma", with
+    the contact law of real sphere and wall contacts in double-word FP32).  autotune: pick the
     kernels' launch shape on the first run (woo_gb300.tuning: cached per GPU and workload)."""
     _defaults = dict(capacity=0, damping=0.2, reset=True, kinSplit=False, verletDist=-0.05, applyForces=True,
                      updatePhys="never", dist00=True, device=0, keepGeom=True, arith="exact", autotune=False)
@@ -1231,9 +1232,9 @@ class GpuDemEngine(Engine):
                        "history+mlp": abi.WARM_HISTORY_MLP}[
             ell.warmStart if ell is not None else "cold"]
         p.fallbackIters = int(ell.fallbackIters) if ell is not None else 4
-        if self.arith not in ("exact", "fma"):
-            raise ValueError("GpuDemEngine.arith must be 'exact' or 'fma'")
-        p.arith = abi.ARITH_FMA if self.arith == "fma" else abi.ARITH_EXACT
+        if self.arith not in ("exact", "fma", "dw"):
+            raise ValueError("GpuDemEngine.arith must be 'exact', 'fma' or 'dw'")
+        p.arith = {"exact": abi.ARITH_EXACT, "fma": abi.ARITH_FMA, "dw": abi.ARITH_DW}[self.arith]
         self._ellFunctor = ell
         return p
 
