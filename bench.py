@@ -306,7 +306,8 @@ def ell_variants(args, spec, local, world, barrier, w):
 def state_tag(args, region, n):
     """Descriptor of the state a timed region starts from; an ncu summary under profiles/ is used for this
     region's traffic only when it records the same descriptor (a capture of the same deterministic run)."""
-    return f"{args.workload}/{region}/n={n}/warmup={max(args.warmup, 3)}/steps={args.steps}"
+    tag = f"{args.workload}/{region}/n={n}/warmup={max(args.warmup, 3)}/steps={args.steps}"
+    return tag if args.arith == "fma" else f"{tag}/arith={args.arith}"
 
 
 def read_profile_figures(tag):
