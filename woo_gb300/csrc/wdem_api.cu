@@ -1155,10 +1155,14 @@ static void applyNextDt(wdem_handle* h) {
   h->nextDt = std::numeric_limits<double>::quiet_NaN();
 }
 
+// steps may run queued (no host-side per-step work, queue depth not set to 1)
+static bool queueEligible(const wdem_handle* h) {
+  return !(h->timing || h->periodic || h->P.trackEnergy || h->needRebuild || h->forcesInArrays ||
+           h->verletDistResolved == 0 || h->updatePhys == WDEM_UPDATE_PHYS_ONCE || h->maxAhead < 2);
+}
+
 static int queueDepth(wdem_handle* h, int left) {
-  if (left < 2 || h->timing || h->periodic || h->P.trackEnergy || h->needRebuild || h->forcesInArrays ||
-      h->verletDistResolved == 0 || h->updatePhys == WDEM_UPDATE_PHYS_ONCE || h->maxAhead < 2)
-    return 1;
+  if (left < 2 || !queueEligible(h)) return 1;
   // expected steps between rebuilds r: a queue of sqrt(3 r) balances the wasted no-op launches behind a
   // trigger against the round trips saved
   int q = (int)std::lround(std::sqrt(3.0 * h->rebuildInterval));
@@ -1254,7 +1258,9 @@ static int replayQueue(wdem_handle* h, int ahead, bool full, bool warm) {
   return 1;
 }
 
-static int runQueued(wdem_handle* h, int ahead, int& done) {
+// Runs up to `ahead` queued steps; `statusCurrent` tells whether the host's status word is still the
+// device's (no kernel that may raise an error ran after it was read back).
+static int runQueued(wdem_handle* h, int ahead, int& done, bool& statusCurrent) {
   cudaStream_t s = h->stream;
   const long long s0 = h->step;
   h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
@@ -1275,6 +1281,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done) {
   int rc;
   if ((rc = checkDeviceStatus(h))) return rc;
   const long long halt = h->hst->haltAt;
+  statusCurrent = (halt == 0);
   if (halt == 0) {
     h->sinceRebuild += ahead;
     done = ahead;
@@ -1365,14 +1372,20 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
   // clears it for the next step)
   CK(cudaMemsetAsync(&h->dst->rotCount, 0, sizeof(unsigned), s));
   CK(cudaMemsetAsync(&h->dst->touchCount, 0, sizeof(unsigned), s));
+  // true while the status word on the host is the one the last queue read back (nothing launched since)
+  bool statusRead = false;
   for (int it = 0; it < nSteps; it++) {
     const int ahead = queueDepth(h, nSteps - it);
-    if (ahead > 1) {
+    if (queueEligible(h)) {
+      // also a single step: the integrator and the guarded contact pass go out together and the host reads
+      // the status once (a trigger halts the contact pass on the device; the host then rebuilds and runs it),
+      // one round trip per call instead of a check between the two kernels and another at the end
       int done = 0, rc;
-      if ((rc = runQueued(h, ahead, done))) return rc;
+      if ((rc = runQueued(h, ahead, done, statusRead))) return rc;
       it += done - 1;
       continue;
     }
+    statusRead = false;
     h->P.step = h->step;
     h->P.seq = ++h->seq;
     h->P.updatePhysNow = (h->updatePhys != WDEM_UPDATE_PHYS_NEVER);
@@ -1449,8 +1462,10 @@ int wdem_step(wdem_handle* h, int32_t nSteps) {
     h->timeSum += h->raw.dt;
     applyNextDt(h);
   }
-  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  if (!statusRead) {
+    CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
   collectTimes(h);
   CK(cudaGetLastError());
   return checkDeviceStatus(h);
