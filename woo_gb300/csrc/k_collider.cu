@@ -23,7 +23,6 @@
 
 namespace wdem {
 
-static const unsigned long long HASH_EMPTY = ~0ull;
 // columns of the sweep grid at most (keys of 20 column bits and 12 or more quantisation bits: 4 radix passes)
 static const int SWEEP_MAX_COLS = (1 << 20) - 2;
 
@@ -722,52 +721,20 @@ __global__ void k_retain_write(Contacts old, long long nOld, const unsigned* fla
   }
 }
 
-// ------------------------------------------------------------------------------------ hash table
-__device__ __forceinline__ unsigned long long pairKey(int a, int b) {
-  unsigned lo = (unsigned)min(a, b), hi = (unsigned)max(a, b);
-  return ((unsigned long long)lo << 32) | hi;
-}
-// 64-bit finaliser of MurmurHash3 (Appleby), a published bit mixer
-__device__ __forceinline__ unsigned long long hmix(unsigned long long k) {
-  k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
-  return k;
-}
-__global__ void k_hash_clear(unsigned long long* hk, unsigned long long cap) {
-  unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < cap) hk[i] = HASH_EMPTY;
-}
-__global__ void k_hash_insert(const int2* ids, long long n, unsigned long long* hk, unsigned* hv, unsigned long long cap,
-                              DeviceStatus* st) {
-  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  int2 id = ids[c];
-  unsigned long long key = pairKey(id.x, id.y);
-  unsigned long long pos = hmix(key) & (cap - 1);
-  for (unsigned long long probe = 0; probe < cap; probe++) {
-    unsigned long long prev = atomicCAS(&hk[pos], HASH_EMPTY, key);
-    if (prev == HASH_EMPTY || prev == key) { hv[pos] = (unsigned)c; return; }
-    pos = (pos + 1) & (cap - 1);
+// ------------------------------------------------------------------------------------ old-contact lookup
+// The contact of the pair (a, b) in the container whose CSR is `csr` (built at the last rebuild or upload):
+// binary search of the partner in the row of the lower id, whose keys are sorted by partner; -1 if none.
+__device__ __forceinline__ long long csrFind(const Csr& csr, int a, int b) {
+  const int lo = min(a, b), hi = max(a, b);
+  if (lo < 0 || hi >= csr.n) return -1;  // ids the rows do not cover (appended since) had no contact
+  const unsigned long long key = ((unsigned long long)(unsigned)lo << csr.idBits) | (unsigned)hi;
+  int l = csr.rowptr[lo], r = csr.rowptr[lo + 1];
+  while (l < r) {
+    const int m = (l + r) >> 1;
+    if (csr.keys[m] < key) l = m + 1; else r = m;
   }
-  atomicCAS(&st->code, 0, WDEM_ERR_OVERFLOW);
-}
-__device__ __forceinline__ long long hashFind(const unsigned long long* hk, const unsigned* hv, unsigned long long cap,
-                                              unsigned long long key) {
-  if (cap == 0) return -1;
-  unsigned long long pos = hmix(key) & (cap - 1);
-  for (unsigned long long probe = 0; probe < cap; probe++) {
-    unsigned long long k = hk[pos];
-    if (k == key) return (long long)hv[pos];
-    if (k == HASH_EMPTY) return -1;
-    pos = (pos + 1) & (cap - 1);
-  }
+  if (l < csr.rowptr[lo + 1] && csr.keys[l] == key) return (long long)(csr.ent[l] & 0x7fffffffu);
   return -1;
-}
-
-void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
-                       unsigned long long cap, DeviceStatus* st) {
-  if (cap == 0) return;
-  (k_hash_clear<<<(unsigned)((cap + 255) / 256), 256, 0, s>>>(hk, cap), ++::wdem::g_kernel_launches);
-  if (n > 0) (k_hash_insert<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ids, n, hk, hv, cap, st), ++::wdem::g_kernel_launches);
 }
 
 // ------------------------------------------------------------------------------------ carry-over
@@ -780,15 +747,14 @@ void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned lo
 // contacts the contact pass and the force gather touch every step are dense in every per-contact array.
 // Pass 1 finds each new pair's old index (or none) and flags the real ones; after a scan of the flags,
 // pass 2 writes each contact at its place: real ones at their rank, the others after them in order.
-__global__ void k_part_flag(Contacts neu, long long nNew, Contacts old, const unsigned long long* hk, const unsigned* hv,
-                            unsigned long long cap, unsigned long long* tmpIds, unsigned* tmpJ, unsigned* flag,
-                            int4* tmpDist) {
+__global__ void k_part_flag(Contacts neu, long long nNew, Contacts old, Csr oldCsr, unsigned long long* tmpIds,
+                            unsigned* tmpJ, unsigned* flag, int4* tmpDist) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nNew) return;
   const int2 id = neu.ids[c];
   tmpIds[c] = ((unsigned long long)(unsigned)id.y << 32) | (unsigned)id.x;
   if (tmpDist) tmpDist[c] = neu.cdist[c];
-  const long long j = hashFind(hk, hv, cap, pairKey(id.x, id.y));
+  const long long j = csrFind(oldCsr, id.x, id.y);
   unsigned jj = 0xffffffffu, f = 0;
   if (j >= 0) {
     const uint8_t os = old.state[j] & CS_MASK;
@@ -1177,26 +1143,29 @@ void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c,
   for (int q = 0; q < 9; q++) energy_accumulate(s, scratch9 + (long long)q * nc, nc, partials, out9 + q, true);
 }
 
-long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old,
-                            const unsigned long long* hk, const unsigned* hv, unsigned long long cap, long long step,
-                            int nHist, ColliderScratch& cs) {
+long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, Csr oldCsr,
+                            long long step, int nHist, ColliderScratch& cs) {
   if (nNew <= 0) return 0;
   unsigned long long* tmpIds = cs.keys;
   unsigned* tmpJ = cs.vals;
   unsigned* flag = cs.valsAlt;
   int4* tmpDist = neu.cdist ? reinterpret_cast<int4*>(cs.keysAlt) : nullptr;
   const unsigned blocks = (unsigned)((nNew + 255) / 256);
-  (k_part_flag<<<blocks, 256, 0, s>>>(neu, nNew, old, hk, hv, cap, tmpIds, tmpJ, flag, tmpDist), ++::wdem::g_kernel_launches);
+  (k_part_flag<<<blocks, 256, 0, s>>>(neu, nNew, old, oldCsr, tmpIds, tmpJ, flag, tmpDist), ++::wdem::g_kernel_launches);
   exclusive_scan_u32(s, flag, nNew, cs);
   (k_carry_compact<<<blocks, 256, 0, s>>>(p, neu, nNew, old, tmpIds, tmpJ, flag, tmpDist, step, nHist), ++::wdem::g_kernel_launches);
   return nNew;
 }
 
-void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs) {
+void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr& csr, ColliderScratch& cs) {
   int idBits = bitsFor((unsigned long long)n + 1);
   long long ne = 2 * nc;
   if (nc > 0) (k_csr_entries<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(c, nc, idBits, cs.keys, cs.vals), ++::wdem::g_kernel_launches);
   radix_sort(s, cs.keys, cs.vals, cs.keysAlt, cs.valsAlt, ne, 2 * idBits, cs);
+  // the sorted keys stay with the CSR for the next rebuild's carry (cs.keys is the sort's scratch)
+  if (ne > 0) cudaMemcpyAsync(csr.keys, cs.keys, (size_t)ne * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s);
+  csr.idBits = idBits;
+  csr.n = n;
   long long threads = ne > 0 ? ne : (long long)n + 1;
   (k_csr_rows<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(cs.keys, ne, idBits, n, csr.rowptr), ++::wdem::g_kernel_launches);
   if (ne > 0)

@@ -145,10 +145,6 @@ struct wdem_handle {
   long long nContacts = 0;
   Csr csr{};
   long long csrCap = 0;
-  unsigned long long* hk[2] = {nullptr, nullptr};
-  unsigned* hv[2] = {nullptr, nullptr};
-  unsigned long long hcap[2] = {0, 0};
-  unsigned long long hallo[2] = {0, 0};
   ColliderScratch cs{};
   DeviceStatus* dst = nullptr;
   DeviceStatus* hst = nullptr;  // pinned
@@ -319,21 +315,6 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
 }
 
 // Copy the first n contacts of src into dst (both device), used when a buffer grows in place.
-void copyContacts(cudaStream_t s, ContactBuf& dst, const ContactBuf& src, long long n) {
-  if (n <= 0) return;
-  cudaMemcpyAsync(dst.c.ids, src.c.ids, n * sizeof(int2), cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(dst.c.state, src.c.state, n, cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(dst.c.step0, src.c.step0, n * sizeof(int), cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(dst.c.tanPhi, src.c.tanPhi, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-  for (int k = 0; k < HIST_COUNT; k++)
-    if (dst.c.hist[k] && src.c.hist[k]) cudaMemcpyAsync(dst.c.hist[k], src.c.hist[k], n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-}
-
-unsigned long long nextPow2(unsigned long long v) {
-  unsigned long long p = 1;
-  while (p < v) p <<= 1;
-  return p;
-}
 
 size_t evNext(wdem_handle* h) {
   if (h->evUsed >= h->evPool.size()) {
@@ -431,21 +412,11 @@ int ensureCand(wdem_handle* h, long long n) {
   return WDEM_OK;
 }
 
-int ensureHash(wdem_handle* h, int side, long long n) {
-  unsigned long long cap = nextPow2(std::max<unsigned long long>(1024, 2ull * (unsigned long long)n));
-  if (cap > h->hallo[side]) {
-    CK(dalloc(h->hk[side], cap));
-    CK(dalloc(h->hv[side], cap));
-    h->hallo[side] = cap;
-  }
-  h->hcap[side] = cap;
-  return WDEM_OK;
-}
-
 int ensureCsr(wdem_handle* h, long long nc) {
   if (2 * nc + 1 > h->csrCap) {
     long long cap = std::max<long long>(2 * nc + 1, h->csrCap * 3 / 2);
     CK(dalloc(h->csr.ent, cap));
+    CK(dalloc(h->csr.keys, cap));
     h->csrCap = cap;
   }
   return WDEM_OK;
@@ -532,13 +503,13 @@ int rebuild(wdem_handle* h) {
   col_retain_write(s, old.c, nOld, cs, neu.c.ids, total, neu.cap);
   if (h->periodic && old.c.cdist) col_retain_write_dist(s, old.c, nOld, cs, neu.c.cdist, total, neu.cap);
   const int side = 1 - h->cur;
-  // history carried over, contacts real before the rebuild compacted to the front (the sort scratch,
-  // sized for 2 nNew entries, holds the temporaries); then the new table is hashed in that final order
+  // history carried over (each new pair found in the old container through the old CSR's sorted keys),
+  // contacts real before the rebuild compacted to the front (the sort scratch, sized for 2 nNew entries,
+  // holds the temporaries); then the new container's CSR
   if ((rc = ensureScratch(h, nNew))) return rc;
-  col_carry_compact(s, h->d, neu.c, nNew, old.c, h->hk[h->cur], h->hv[h->cur], nOld > 0 ? h->hcap[h->cur] : 0, h->step,
-                    (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT, cs);
-  if ((rc = ensureHash(h, side, nNew))) return rc;
-  launch_hash_build(s, neu.c.ids, nNew, h->hk[side], h->hv[side], h->hcap[side], h->dst);
+  Csr oldCsr = h->csr;
+  if (nOld <= 0) oldCsr.n = 0;
+  col_carry_compact(s, h->d, neu.c, nNew, old.c, oldCsr, h->step, (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT, cs);
   if ((rc = ensureCsr(h, nNew))) return rc;
   col_csr(s, neu.c, nNew, n, h->csr, cs);
   h->cur = side;
@@ -757,8 +728,7 @@ int wdem_destroy(wdem_handle* h) {
   cudaFree(h->dEnergy); cudaFree(h->ePartials); cudaFree(h->dStress); cudaFree(h->stressTerms);
   cudaFree(h->dSmall);
   freeContacts(h->buf[0]); freeContacts(h->buf[1]);
-  cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor);
-  for (int k = 0; k < 2; k++) { cudaFree(h->hk[k]); cudaFree(h->hv[k]); }
+  cudaFree(h->csr.rowptr); cudaFree(h->csr.ent); cudaFree(h->csr.cursor); cudaFree(h->csr.keys);
   ColliderScratch& cs = h->cs;
   cudaFree(cs.keys); cudaFree(cs.keysAlt); cudaFree(cs.vals); cudaFree(cs.valsAlt); cudaFree(cs.hist);
   cudaFree(cs.blockSums); cudaFree(cs.cellStart); cudaFree(cs.counts); cudaFree(cs.large); cudaFree(cs.grid); cudaFree(cs.srec);
@@ -1085,8 +1055,10 @@ int wdem_upload_contacts(wdem_handle* h, const wdem_contacts* c) {
   }
   (h->raw.arith != WDEM_ARITH_EXACT ? contracted::launch_init_uploaded : launch_init_uploaded)(s, h->P, h->d, b.c, nc);
   int rc;
-  if ((rc = ensureHash(h, h->cur, nc))) return rc;
-  launch_hash_build(s, b.c.ids, nc, h->hk[h->cur], h->hv[h->cur], h->hcap[h->cur], h->dst);
+  // the uploaded container's CSR: the next rebuild carries the history of its contacts through it
+  if ((rc = ensureScratch(h, nc))) return rc;
+  if ((rc = ensureCsr(h, nc))) return rc;
+  col_csr(s, b.c, nc, h->n, h->csr, h->cs);
   CK(cudaStreamSynchronize(s));
   h->nContacts = nc;
   h->needRebuild = true;

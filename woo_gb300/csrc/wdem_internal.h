@@ -209,6 +209,10 @@ struct Csr {
   int* rowptr;    // N+1
   unsigned* ent;  // 2C
   int* cursor;    // N (scratch for filling)
+  unsigned long long* keys;  // 2C: the entries' sort keys, row << idBits | partner (the next rebuild's carry
+                             // finds each old contact in them)
+  int idBits;     // bits of a particle id in keys
+  int n;          // particles the rows cover (0: no rows)
 };
 
 // Uniform-grid / sweep parameters computed on the device at each rebuild.
@@ -383,14 +387,11 @@ void launch_stress(cudaStream_t s, const StepParams& P, Particles p, Contacts c,
 void col_retain_flags(cudaStream_t s, const StepParams& P, Particles p, Contacts old, long long nOld, ColliderScratch& cs);
 void col_retain_write(cudaStream_t s, Contacts old, long long nOld, ColliderScratch& cs, int2* out, long long base,
                       long long cap);
-void launch_hash_build(cudaStream_t s, const int2* ids, long long n, unsigned long long* hk, unsigned* hv,
-                       unsigned long long cap, DeviceStatus* st);
-void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr csr, ColliderScratch& cs);
+void col_csr(cudaStream_t s, Contacts c, long long nc, int n, Csr& csr, ColliderScratch& cs);
 // history carry-over with compaction: contacts that were real before the rebuild first (in emission order),
 // then the others; uses the sort scratch (sized for 2 nNew) as temporary storage
-long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old,
-                            const unsigned long long* hk, const unsigned* hv, unsigned long long cap, long long step,
-                            int nHist, ColliderScratch& cs);
+long long col_carry_compact(cudaStream_t s, Particles p, Contacts neu, long long nNew, Contacts old, Csr oldCsr,
+                            long long step, int nHist, ColliderScratch& cs);
 // exclusive scan of a[0..n) in place; a[n] receives the total (the array holds n+1 entries)
 void exclusive_scan_u32(cudaStream_t s, unsigned* a, long long n, ColliderScratch& cs);
 int sort_passes_for(int nSmallBits);
