@@ -8,12 +8,14 @@
 // (Collision.cpp:21-43), plus every real contact carried over from before (the reference never
 // removes real contacts in the collider).  Instead of an incremental insertion sort, the rebuild
 //   1. sorts small particles by (grid column in the two long axes, quantised box minimum along the
-//      shortest axis) with an LSD radix sort written here,
+//      shortest axis) with an LSD radix sort written here (one kernel per digit, decoupled look-back),
 //   2. sweeps each particle forward along the sweep axis in its own and the 8 neighbouring columns,
 //      testing the exact FP64 closed-interval overlap (grid cell >= widest box, so no pair is missed),
 //   3. tests walls, facets and other large boxes against every particle of their scene,
-//   4. writes the pairs in a deterministic order (count pass, exclusive scan, write pass),
-//   5. carries contact history over through an open-addressing hash table keyed by (min id, max id),
+//   4. writes the pairs in a deterministic order (count pass with each particle's first pairs buffered,
+//      exclusive scan, write pass),
+//   5. carries contact history over, finding each pair's old contact by a binary search in the old
+//      CSR's sorted keys (row of the lower id, keyed by the partner),
 //   6. builds the per-particle contact CSR with rows ordered by the partner id.
 #include "wdem_internal.h"
 #include "wdem_math.cuh"

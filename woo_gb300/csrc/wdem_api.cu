@@ -436,7 +436,7 @@ int checkDeviceStatus(wdem_handle* h) {
     int code = h->hst->code;
     std::string m;
     if (code == WDEM_ERR_NAN) m = "NaN in the state or in a contact force (particle #" + std::to_string(h->hst->detail) + ")";
-    else if (code == WDEM_ERR_OVERFLOW) m = "contact hash table overflow";
+    else if (code == WDEM_ERR_OVERFLOW) m = "a device table ran out of capacity";
     else if (code == WDEM_ERR_TOO_BIG)
       m = "ambiguous periodic contact of particle #" + std::to_string(h->hst->detail) +
           ": the boxes overlap across more than one period (a particle larger than half of the cell)";
