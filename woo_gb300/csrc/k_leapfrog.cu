@@ -634,29 +634,85 @@ __device__ __forceinline__ void integrateFast(const StepParams& P, const Particl
 
 // First pass: particles without contact forces this step.  Those that a real contact touched are
 // compacted into touchList instead: their force gather and divisions would hold up the FP64 pipe
-// for whole warps of gravity-only neighbours.
-template <bool PERI, int BS>
+// for whole warps of gravity-only neighbours.  DENSE (many real contacts): a block that has touched
+// particles also compacts its other particles to its first threads, so that their FP64 work issues in
+// full warps, and appends its touched ones with one atomic.
+template <bool PERI, int BS, bool DENSE>
 __global__ void __launch_bounds__(BS, 1024 / BS) k_leapfrog_fast(StepParams P, Particles p, int n, Contacts c, Csr csr,
                                                                DeviceStatus* st) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  // all of the particle's loads are issued together, before the guard's and the list decision
-  const FastRec rec = loadFast(p, i);
-  const uint8_t tch = p.touched[i];
-  if (haltedIntegrator(st, stepOf(P, st))) return;
-  const bool listed = ((unsigned)rec.meta.w & 63u) != 63u && tch != 0;
-  const unsigned am = __activemask();
-  const unsigned b = __ballot_sync(am, listed);
-  if (b) {
-    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(&st->touchCount, (unsigned)__popc(b));
-    base = __shfl_sync(am, base, leader);
-    const unsigned slot = base + __popc(b & ((1u << lane) - 1));
-    if (listed && slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
+  if constexpr (!DENSE) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // all of the particle's loads are issued together, before the guard's and the list decision
+    const FastRec rec = loadFast(p, i);
+    const uint8_t tch = p.touched[i];
+    if (haltedIntegrator(st, stepOf(P, st))) return;
+    const bool listed = ((unsigned)rec.meta.w & 63u) != 63u && tch != 0;
+    const unsigned am = __activemask();
+    const unsigned b = __ballot_sync(am, listed);
+    if (b) {
+      const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(&st->touchCount, (unsigned)__popc(b));
+      base = __shfl_sync(am, base, leader);
+      const unsigned slot = base + __popc(b & ((1u << lane) - 1));
+      if (listed && slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
+    }
+    if (listed) return;
+    integrateFast<PERI>(P, p, i, n, c, csr, st, false, rec, 0u);
+  } else {
+    constexpr int NW = BS / 32;
+    __shared__ unsigned sCnt[2][NW];
+    __shared__ int sIdx[BS];
+    __shared__ unsigned sBase;
+    const int i = blockIdx.x * BS + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool live = i < n;
+    FastRec rec;
+    uint8_t tch = 0;
+    if (live) {
+      rec = loadFast(p, i);
+      tch = p.touched[i];
+    }
+    const bool run = live && !haltedIntegrator(st, stepOf(P, st));
+    const bool listed = run && ((unsigned)rec.meta.w & 63u) != 63u && tch != 0;
+    const bool own = run && !listed;
+    // every thread of the block reaches the barriers: none returns before them
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned bl = __ballot_sync(0xffffffffu, listed), bo = __ballot_sync(0xffffffffu, own);
+    if (lane == 0) {
+      sCnt[0][w] = (unsigned)__popc(bl);
+      sCnt[1][w] = (unsigned)__popc(bo);
+    }
+    __syncthreads();
+    unsigned preL = 0, preO = 0, nL = 0, nO = 0;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) {
+      const unsigned a = sCnt[0][k], b = sCnt[1][k];
+      if (k < w) {
+        preL += a;
+        preO += b;
+      }
+      nL += a;
+      nO += b;
+    }
+    bool mine = own;
+    int j = i;
+    if (nL != 0) {  // the same for every thread of the block
+      if (threadIdx.x == 0) sBase = atomicAdd(&st->touchCount, nL);
+      if (own) sIdx[preO + (unsigned)__popc(bo & lt)] = i;
+      __syncthreads();
+      if (listed) {
+        const unsigned slot = sBase + preL + (unsigned)__popc(bl & lt);
+        if (slot < (unsigned)n) p.touchList[slot] = (unsigned)i;
+      }
+      mine = threadIdx.x < nO;
+      j = mine ? sIdx[threadIdx.x] : i;
+      if (mine && j != i) rec = loadFast(p, j);  // the block loaded it a moment ago
+    }
+    if (!mine) return;
+    integrateFast<PERI>(P, p, j, n, c, csr, st, false, rec, 0u);
   }
-  if (listed) return;
-  integrateFast<PERI>(P, p, i, n, c, csr, st, false, rec, 0u);
 }
 
 // Second pass, over two lists: the touched particles (CSR force gather, full integration, rotation
@@ -694,14 +750,21 @@ static unsigned listGrid(const StepParams& P) {
   const int want = P.shListsPerSM > 0 ? std::min(P.shListsPerSM, per) : per;
   return (unsigned)sms * (unsigned)want;
 }
-// the first pass with the block size of the launch shape
+// the first pass with the block size of the launch shape; the block-compacting one when the last step the
+// host saw had many real contacts (either is exact: they differ only in which thread integrates a particle)
 template <bool PERI>
 static void launchFast(cudaStream_t s, const StepParams& P, Particles p, int n, Contacts c, Csr csr, DeviceStatus* st) {
   const int bs = P.shLeapBlock == 128 || P.shLeapBlock == 512 ? P.shLeapBlock : 256;
   const unsigned blocks = (unsigned)((n + bs - 1) / bs);
-  if (bs == 128) k_leapfrog_fast<PERI, 128><<<blocks, 128, 0, s>>>(P, p, n, c, csr, st);
-  else if (bs == 512) k_leapfrog_fast<PERI, 512><<<blocks, 512, 0, s>>>(P, p, n, c, csr, st);
-  else k_leapfrog_fast<PERI, 256><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  if (P.denseTouch) {
+    if (bs == 128) k_leapfrog_fast<PERI, 128, true><<<blocks, 128, 0, s>>>(P, p, n, c, csr, st);
+    else if (bs == 512) k_leapfrog_fast<PERI, 512, true><<<blocks, 512, 0, s>>>(P, p, n, c, csr, st);
+    else k_leapfrog_fast<PERI, 256, true><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  } else {
+    if (bs == 128) k_leapfrog_fast<PERI, 128, false><<<blocks, 128, 0, s>>>(P, p, n, c, csr, st);
+    else if (bs == 512) k_leapfrog_fast<PERI, 512, false><<<blocks, 512, 0, s>>>(P, p, n, c, csr, st);
+    else k_leapfrog_fast<PERI, 256, false><<<blocks, 256, 0, s>>>(P, p, n, c, csr, st);
+  }
   ++::wdem::g_kernel_launches;
 }
 

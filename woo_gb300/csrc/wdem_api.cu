@@ -164,6 +164,7 @@ struct wdem_handle {
   // queued steps (runQueued): depth limit (0 or 1: every step checked on the host), mean steps between
   // rebuilds, steps since the last one
   bool actValid = false;  // the cull's active list matches the container (a full cull ran since the rebuild)
+  bool denseTouch = false;  // real contacts were at least n/8 at the end of the last queue that ran through
   int maxAhead = 32;
   double rebuildInterval = 16;
   int sinceRebuild = 0;
@@ -1239,6 +1240,7 @@ static int runQueued(wdem_handle* h, int ahead, int& done, bool& statusCurrent) 
   const bool warm = h->hasEll && h->P.ellSolver == WDEM_ELL_NEWTON && (h->P.warmStart == WDEM_WARM_MLP || h->P.warmStart == WDEM_WARM_HISTORY_MLP);
   const long long q0 = h->seq;
   const bool full = !h->actValid;
+  h->P.denseTouch = h->denseTouch ? 1 : 0;
   const int viaGraph = replayQueue(h, ahead, full, warm);
   if (viaGraph < 0) return viaGraph;
   if (viaGraph == 0) {
@@ -1255,6 +1257,8 @@ static int runQueued(wdem_handle* h, int ahead, int& done, bool& statusCurrent) 
   const long long halt = h->hst->haltAt;
   statusCurrent = (halt == 0);
   if (halt == 0) {
+    // a halted queue's last contact pass did not run (its count is zero): the choice stays
+    h->denseTouch = 8ull * h->hst->workCount >= (unsigned long long)h->n;
     h->sinceRebuild += ahead;
     done = ahead;
     h->lastRunFull = 0;

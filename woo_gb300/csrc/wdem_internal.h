@@ -106,6 +106,8 @@ struct StepParams {
   int hasFacets;            // the scene has facets
   int stepDev;              // 1: step and seq are offsets from DeviceStatus.stepBase/seqBase (steps replayed
                             // from a CUDA graph, whose kernel arguments are fixed at capture)
+  int denseTouch;           // 1: real contacts were at least n/8 in the last step the host saw; the
+                            // integrator's first pass then compacts each block's untouched particles
   double gravity[3];
   int hasGravity;
   double distFactor;        // DemField.distFactor
