@@ -484,7 +484,7 @@ def edit_event_cost(h, spec, k=1000):
 
 
 def common_config(args, spec):
-    """The config object both arms print (the driver compares them)."""
+    """The config object both arms print, identical for the same workload so their lines can be compared."""
     return {"workload": args.workload, "n_particles": int(spec.particles.n), "dt": float(spec.params.dt),
             "steps_simulated_before_timing": int(max(args.warmup, 3)), "timed_steps": int(args.steps),
             "l2": "state larger than L2 (no flush needed)"}
