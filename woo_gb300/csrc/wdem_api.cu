@@ -5,7 +5,8 @@
 // (src/core/Scene.cpp:420-427):
 //   1. k_leapfrog      forces gathered through the contact CSR, integration, verlet trigger
 //   2. collider        only when a particle left its verlet box (or after an upload): boxes, grid,
-//                      radix sort, sweep, hash-table carry-over of contact history, CSR
+//                      radix sort, sweep, contact history carried over through the old CSR's
+//                      sorted keys, real contacts compacted to the front, CSR
 //   3. k_contacts      fused Cg2 + Cp2 + Law2 over the contact list
 #include "wdem_internal.h"
 #include "../../include/wdem.h"
