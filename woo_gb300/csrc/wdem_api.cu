@@ -295,7 +295,7 @@ cudaError_t allocContacts(ContactBuf& b, long long cap, bool hertz, bool geom, b
   if ((e = dalloc(c.state, cap))) return e;
   if ((e = dalloc(c.step0, cap))) return e;
   if ((e = dalloc(c.tanPhi, cap))) return e;
-  int nh = hertz ? HIST_COUNT : HIST_FRICT;
+  int nh = hertz ? (int)HIST_COUNT : (int)HIST_FRICT;
   for (int k = 0; k < nh; k++) if ((e = dalloc(c.hist[k], cap))) return e;
   // two CSR entries per contact; stamps start at -1 (no pass has written them)
   if ((e = dalloc(c.out, (size_t)OUT_RECORDS * 2 * cap))) return e;
@@ -511,7 +511,7 @@ int rebuild(wdem_handle* h) {
   if ((rc = ensureScratch(h, nNew))) return rc;
   Csr oldCsr = h->csr;
   if (nOld <= 0) oldCsr.n = 0;
-  col_carry_compact(s, h->d, neu.c, nNew, old.c, oldCsr, h->step, (hertz && old.hertz) ? HIST_COUNT : HIST_FRICT, cs);
+  col_carry_compact(s, h->d, neu.c, nNew, old.c, oldCsr, h->step, (hertz && old.hertz) ? (int)HIST_COUNT : (int)HIST_FRICT, cs);
   if ((rc = ensureCsr(h, nNew))) return rc;
   col_csr(s, neu.c, nNew, n, h->csr, cs);
   h->cur = side;
@@ -1503,7 +1503,7 @@ int fetchContacts(wdem_handle* h, HostContacts& hc) {
     CK(cudaMemcpyAsync(hc.state.data(), b.c.state, nc, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(hc.step0.data(), b.c.step0, nc * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(hc.tanPhi.data(), b.c.tanPhi, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
-    int nh = b.hertz ? HIST_COUNT : HIST_FRICT;
+    int nh = b.hertz ? (int)HIST_COUNT : (int)HIST_FRICT;
     for (int k = 0; k < nh; k++) {
       hc.hist[k].resize(nc);
       CK(cudaMemcpyAsync(hc.hist[k].data(), b.c.hist[k], nc * sizeof(double), cudaMemcpyDeviceToHost, s));
