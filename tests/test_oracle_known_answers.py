@@ -153,3 +153,50 @@ def test_canonical_orientation_is_immaterial():
     # amplify velocity differences): about 1e-11 m after 30 steps at these sizes
     a.step(30); b.step(30)
     assert np.allclose(a.particles().pos, b.particles().pos, rtol=0, atol=1e-9)
+
+
+def test_sliding_block_coulomb_limit():
+    """Analytic: a sphere with its rotations blocked (DemData.blocked 'XYZ'), settled on a wall, slides
+    like a block once given a horizontal velocity v0.  Law2_L6Geom_FrictPhys_IdealElPl caps the tangential
+    force at tanPhi times the normal force (src/dem/IdealElPl.cpp:60-75), so while the block slides
+    |Ft| = tanPhi |Fn| (to rounding), its velocity falls linearly, v = v0 - tanPhi g t, and it stops after
+    sliding v0^2 / (2 tanPhi g)."""
+    g, r, mu, v0 = 9.81, 0.01, 0.4, 0.3
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
+    pa.flags[1] = abi.DOF_RX | abi.DOF_RY | abi.DOF_RZ
+    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
+    n_settle = 4000
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5), pa)
+    o.step(n_settle)
+    c = o.contacts()
+    m = pa.mass[1]
+    assert c.n == 1 and c.real[0] == 1
+    assert abs(c.force[0, 0]) == pytest.approx(m * g, rel=1e-9)       # settled: Fn = m g
+    # the settled state (dynamic fields and contact history) with the block pushed along x, no damping
+    d = o.particles()
+    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
+        getattr(pa, name)[:] = getattr(d, name)
+    pa.vel[1] = (v0, 0.0, 0.0)
+    x0 = pa.pos[1, 0]
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle), pa,
+                      contacts=c)
+    t_stop = v0 / (mu * g)
+    k_stop = int(t_stop / dt)
+    k = 0
+    for chunk in (1, 99, 400, 500, 500):
+        o.step(chunk)
+        k += chunk
+        assert k < k_stop
+        c = o.contacts()
+        fn, ft = abs(c.force[0, 0]), math.hypot(c.force[0, 1], c.force[0, 2])
+        assert ft == pytest.approx(mu * fn, rel=1e-12), f"step {k}: not on the Coulomb cone"
+        # the first step integrates the settled forces (no friction yet); friction acts from the second
+        v = o.particles().vel[1]
+        assert v[0] == pytest.approx(v0 - mu * g * (k - 1) * dt, rel=1e-10)
+        assert abs(v[1]) < 1e-12 * v0
+    o.step(k_stop // 2 + k_stop - k)
+    p = o.particles()
+    assert abs(p.vel[1, 0]) < 0.01 * v0                                 # stopped (tangential spring only)
+    assert p.pos[1, 0] - x0 == pytest.approx(v0 * v0 / (2 * mu * g), rel=2e-3)

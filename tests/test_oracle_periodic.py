@@ -1,6 +1,7 @@
 """Periodic cell in the oracle: the known answers of py/tests/test_pbc.py (incident velocity across 10
-cells with homoDeform gradV2, over-half-cell contacts, the double-contact error, cellDist of shifted
-spheres) and the periodic pair predicate against brute force over images."""
+cells with homoDeform gradV2, the cell's trsf/hSize recursion, over-half-cell contacts, the
+double-contact error, cellDist of shifted spheres) and the periodic pair predicate against brute force
+over images."""
 import math
 
 import numpy as np
@@ -33,6 +34,38 @@ def test_l6geom_incident_velocity_gradv2():
     assert np.array_equal(c.cellDist[0], [0, 0, -10])
     assert np.linalg.norm(c.geomVel[0]) == pytest.approx(np.linalg.norm([0, 0, 5.0]), abs=1e-7)
 
+
+
+def test_cell_integration_gradv2():
+    """py/tests/test_pbc.py:35-50 (testVelGrad) in the homoDeform mode restated here (gradV2): each step,
+    Cell::integrateAndUpdate (src/core/Cell.cpp:81-100) accumulates trsf += dt gradV trsf, the recursion
+    the reference's test checks, and advances hSize by the midpoint rule
+    hSize = (I - gradV dt/2)^-1 (I + gradV dt/2) hSize (the gradV2 branch; the test's own
+    hSize += dt gradV hSize is the other modes' first-order rule), with pprevHsize the mean of the old
+    and the new hSize.  A simple shear with a compression, over 10 steps."""
+    G = np.array([[0.0, 0.4, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, -1.0]])
+    dt = 1e-3
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([[1.0, 1.0, 1.0]]), np.array([0.1]), 0, [], mats_py)
+    p = scenes.default_params(mats, dt=dt, damping=0.0)
+    h0 = np.diag([2.5, 2.5, 3.0])
+    o = bridge.Oracle(p, pa, cell=dict(hSize=h0, gradV=G, nextGradV=G))
+    eye = np.eye(3)
+    hs, tr, first = h0.copy(), eye.copy(), h0.copy()
+    for _ in range(10):
+        prev = hs
+        tr = tr + dt * G @ tr
+        hs = np.linalg.solve(eye - G * dt / 2, (eye + G * dt / 2) @ hs)
+        first = first + dt * G @ first
+        o.step(1)
+        c = o.cell()
+        np.testing.assert_allclose(c["trsf"], tr, rtol=0, atol=1e-14)
+        np.testing.assert_allclose(c["hSize"], hs, rtol=0, atol=3e-14)
+        np.testing.assert_allclose(c["pprevHsize"], (prev + hs) / 2, rtol=0, atol=3e-14)
+    # the midpoint rule and the first-order one part at O(dt^2) per step: the two modes are distinct
+    assert abs(c["hSize"][2, 2] - first[2, 2]) > 1e-6
+    assert c["hSize"][2, 2] == pytest.approx(3.0 * ((1 - dt / 2) / (1 + dt / 2)) ** 10, rel=1e-14)
 
 def _image_pairs(pos, r, size):
     """Brute force over all pairs: the integer cell shift k (per axis) of box 2 for which the boxes
