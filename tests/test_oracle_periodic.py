@@ -1,6 +1,6 @@
 """Periodic cell in the oracle: the known answers of py/tests/test_pbc.py (incident velocity across 10
 cells with homoDeform gradV2, the cell's trsf/hSize recursion, over-half-cell contacts, the
-double-contact error, cellDist of shifted spheres) and the periodic pair predicate against brute force
+double-contact error, cellDist of shifted spheres, a pair formed across the boundary) and the periodic pair predicate against brute force
 over images."""
 import math
 
@@ -138,3 +138,26 @@ def test_normal_contact_cell_dist(shift):
     c = o.contacts()
     assert c.n == 1 and c.real[0] == 1
     assert tuple(c.cellDist[0]) == tuple(-np.array(shift))
+
+
+def test_cross_boundary_pair():
+    """py/tests/test_pbc.py:174-203 (testCrossBoundarySort) in its observable form: with verletDist 0 the
+    collider runs every step; a sphere that crosses the cell's x boundary in its second step, from the
+    incrementally sorted state of the first, is paired with the sphere near x = 0 through the next
+    period (cellDist -1 on x, the pair set of the brute-force image search), and not before."""
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=0.5)]
+    mats = scenes.materials_array(mats_py)
+    r = 0.02
+    pos = np.array([[0.02, 0.5, 0.5], [0.52, 0.5, 0.5], [0.8, 0.2, 0.2]])
+    pa = scenes.assemble(pos, np.full(3, r), 0, [], mats_py, vel=np.array([[0, 0, 0], [0.265, 0, 0], [0, 0, 0]]))
+    p = scenes.default_params(mats, dt=1.0, damping=0.0, verletDist=0.0)
+    o = bridge.Oracle(p, pa, cell=dict(hSize=np.eye(3)))
+    o.step(1)                                   # sphere 1 at x = 0.785: no pair
+    assert o.contacts().n == 0
+    o.step(1)                                   # x = 1.05, i.e. 0.05 in the next period: overlaps sphere 0
+    x = o.particles().pos
+    assert x[1, 0] == pytest.approx(1.05)
+    c = o.contacts()
+    got = {(int(a), int(b)): tuple(int(v) for v in d) for a, b, d in zip(c.idA, c.idB, c.cellDist)}
+    assert got == {(0, 1): (-1, 0, 0)} == _image_pairs(x, np.full(3, r), np.ones(3))
+    assert c.real[0] == 1
