@@ -200,3 +200,31 @@ def test_sliding_block_coulomb_limit():
     p = o.particles()
     assert abs(p.vel[1, 0]) < 0.01 * v0                                 # stopped (tangential spring only)
     assert p.pos[1, 0] - x0 == pytest.approx(v0 * v0 / (2 * mu * g), rel=2e-3)
+
+
+def test_dmt_adhesion_equilibrium():
+    """Analytic: two equal HertzMat spheres with surface energy, exactly touching and at rest, are pulled
+    together by the DMT adhesion 4 pi R gamma (src/dem/Hertz.cpp:105) against the Hertz elastic force
+    kn0 (-uN)^(3/2), kn0 = K sqrt(R), K = (4/3) / sum((1 - nu^2) / E) (Cp2_HertzMat_HertzPhys,
+    src/dem/Hertz.cpp:44-47); the viscous term (en < 1) damps the oscillation, so the pair comes to rest
+    at uN = -(4 pi gamma sqrt(R) / K)^(2/3), with R = r/2 (contact lengths = radii at touching)."""
+    r, E, nu, gamma = 0.01, 1e7, 0.2, 1.0
+    mats_py = [dict(kind=abi.MAT_HERTZ, density=1000.0, young=E, tanPhi=0.5, surfEnergy=gamma, alpha=0.0)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([[0.0, 0.0, 0.0], [0.0, 2 * r, 0.0]]), np.array([r, r]), 0, [], mats_py)
+    dt = 0.3 * scenes.pwave_dt(np.array([r, r]), np.zeros(2, int), mats_py)
+    p = scenes.default_params(mats, dt=dt, damping=0.0, cp2=abi.CP2_HERTZ, law=abi.LAW_HERTZ_DMT, en=0.5,
+                              poisson=nu)
+    o = bridge.Oracle(p, pa)
+    o.step(1)
+    c = o.contacts()
+    assert c.n == 1 and c.real[0] == 1 and c.uN[0] == 0.0
+    o.step(6000)
+    c = o.contacts()
+    K = (4 / 3) / (2 * (1 - nu * nu) / E)
+    R = r / 2
+    un_eq = -((4 * math.pi * gamma * math.sqrt(R) / K) ** (2 / 3))
+    assert c.uN[0] == pytest.approx(un_eq, rel=1e-12)
+    assert abs(c.force[0, 0]) < 1e-12 * 4 * math.pi * R * gamma       # elastic and adhesive forces balance
+    v = o.particles().vel
+    assert np.abs(v).max() < 1e-12
