@@ -284,6 +284,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(Particles p, Contacts c, cons
     }
     tcFenceBefore();  // the accumulator reads are done before the next tile's first MMA overwrites it
   }
+  // a round that timed out may still have MMAs running: wait for its commit once more (bounded) before the
+  // accumulator columns and the barrier's shared memory are given up
+  if (!ok) tcWait(bar, phase ^ 1u);
   if (!ok && t == 0) {
     atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT);
     st->detail = -1;
@@ -537,6 +540,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_grad_tc(const float* rec, const 
     if (!(ok = tcRound(sm, bar, phase, [&] { tcIssue<TC_M, H>(sm, TT_AT, TT_DZT, tmem + TT_DW1, acc); }))) break;
     first = false;
   }
+  if (!ok) tcWait(bar, phase ^ 1u);  // as in k_mlp_tc: the timed-out round's MMAs, before TMEM is freed
   if (!ok && t == 0) {
     atomicCAS(&st->code, 0, WDEM_ERR_TIMEOUT);
     st->detail = -1;
