@@ -158,7 +158,7 @@ def test_canonical_orientation_is_immaterial():
 def test_sliding_block_coulomb_limit():
     """Analytic: a sphere with its rotations blocked (DemData.blocked 'XYZ'), settled on a wall, slides
     like a block once given a horizontal velocity v0.  Law2_L6Geom_FrictPhys_IdealElPl caps the tangential
-    force at tanPhi times the normal force (src/dem/IdealElPl.cpp:60-75), so while the block slides
+    force at tanPhi times the normal force (src/dem/IdealElPl.cpp:55-77), so while the block slides
     |Ft| = tanPhi |Fn| (to rounding), its velocity falls linearly, v = v0 - tanPhi g t, and it stops after
     sliding v0^2 / (2 tanPhi g)."""
     g, r, mu, v0 = 9.81, 0.01, 0.4, 0.3
@@ -204,8 +204,8 @@ def test_sliding_block_coulomb_limit():
 
 def test_dmt_adhesion_equilibrium():
     """Analytic: two equal HertzMat spheres with surface energy, exactly touching and at rest, are pulled
-    together by the DMT adhesion 4 pi R gamma (src/dem/Hertz.cpp:105) against the Hertz elastic force
-    kn0 (-uN)^(3/2), kn0 = K sqrt(R), K = (4/3) / sum((1 - nu^2) / E) (Cp2_HertzMat_HertzPhys,
+    together by the DMT adhesion 4 pi R gamma (src/dem/Hertz.cpp:114) against the Hertz elastic force
+    kn0 (-uN)^(3/2) (:108), kn0 = K sqrt(R), K = (4/3) / sum((1 - nu^2) / E) (Cp2_HertzMat_HertzPhys,
     src/dem/Hertz.cpp:44-47); the viscous term (en < 1) damps the oscillation, so the pair comes to rest
     at uN = -(4 pi gamma sqrt(R) / K)^(2/3), with R = r/2 (contact lengths = radii at touching)."""
     r, E, nu, gamma = 0.01, 1e7, 0.2, 1.0
@@ -228,3 +228,46 @@ def test_dmt_adhesion_equilibrium():
     assert abs(c.force[0, 0]) < 1e-12 * 4 * math.pi * R * gamma       # elastic and adhesive forces balance
     v = o.particles().vel
     assert np.abs(v).max() < 1e-12
+
+
+def test_rolling_resistance_deceleration():
+    """Analytic: a sphere settled on a wall and set rolling (v0 along x, angVel = v0 / r about y) with
+    IdealElPl rolling resistance (relRollStiff > 0, rollTanPhi; src/dem/IdealElPl.cpp:93-118): the rolling
+    moment sits on its cap |Fn| rollTanPhi charLen, charLen = lens sum = 2 r (Cg2_Wall_Sphere_L6Geom
+    passes the radius for both lengths, iniLensTouch; src/dem/Wall.cpp:82, L6Geom.cpp:61), the friction
+    force stays inside the Coulomb cone, so the sphere rolls without sliding and decelerates at
+    a = -M / (r (m + I / r^2)) = -(10/7) rollTanPhi g for a solid sphere.  The tangential spring makes
+    the rolling constraint elastic (velocity ripple of ~1e-3 v0); the displacement averages it out."""
+    g, r, mu, v0, rtp = 9.81, 0.01, 0.5, 0.3, 0.1
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
+    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
+    kw = dict(relRollStiff=1.0, rollTanPhi=rtp)
+    n_settle = 4000
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5, **kw), pa)
+    o.step(n_settle)
+    c = o.contacts()
+    d = o.particles()
+    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
+        getattr(pa, name)[:] = getattr(d, name)
+    pa.vel[1] = (v0, 0.0, 0.0)
+    pa.angVel[1] = (0.0, v0 / r, 0.0)
+    x0 = pa.pos[1, 0]
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle, **kw), pa,
+                      contacts=c)
+    a = -(10 / 7) * rtp * g
+    k = 0
+    for chunk in (1, 99, 400, 500, 500):
+        o.step(chunk)
+        k += chunk
+        c = o.contacts()
+        p = o.particles()
+        fn = abs(c.force[0, 0])
+        tr, ft = math.hypot(c.torque[0, 1], c.torque[0, 2]), math.hypot(c.force[0, 1], c.force[0, 2])
+        assert tr == pytest.approx(fn * rtp * 2 * r, rel=1e-12), f"step {k}: rolling moment not at its cap"
+        assert ft < mu * fn, f"step {k}: sliding"
+        assert abs(p.vel[1, 0] - p.angVel[1, 1] * r) < 5e-3 * v0             # rolling, up to the spring
+        assert abs(p.vel[1, 0] - (v0 + a * (k - 1) * dt)) < 5e-3 * v0
+    T = k * dt
+    assert p.pos[1, 0] - x0 - v0 * T == pytest.approx(a * T * T / 2, rel=2e-3)
