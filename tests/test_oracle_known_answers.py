@@ -271,3 +271,38 @@ def test_rolling_resistance_deceleration():
         assert abs(p.vel[1, 0] - (v0 + a * (k - 1) * dt)) < 5e-3 * v0
     T = k * dt
     assert p.pos[1, 0] - x0 - v0 * T == pytest.approx(a * T * T / 2, rel=2e-3)
+
+
+def test_twisting_resistance_spin_down():
+    """Analytic: a sphere settled on a wall and spun about the wall normal (angVel = w0 along z), with
+    IdealElPl twisting resistance (relTwistStiff > 0; src/dem/IdealElPl.cpp:98-106): the twisting moment
+    sits on its cap |Fn| rollTanPhi charLen (charLen = 2 r), the contact point does not slide (the spin
+    axis is the normal), so the spin falls linearly, I dw/dt = -M, dw/dt = -5 rollTanPhi g / r for a solid
+    sphere, until it stops."""
+    g, r, mu, w0, rtp = 9.81, 0.01, 0.5, 20.0, 0.1
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
+    mats = scenes.materials_array(mats_py)
+    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
+    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
+    kw = dict(relRollStiff=1.0, relTwistStiff=1.0, rollTanPhi=rtp)
+    n_settle = 4000
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5, **kw), pa)
+    o.step(n_settle)
+    c = o.contacts()
+    d = o.particles()
+    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
+        getattr(pa, name)[:] = getattr(d, name)
+    pa.angVel[1] = (0.0, 0.0, w0)
+    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle, **kw), pa,
+                      contacts=c)
+    alpha = -5 * rtp * g / r
+    k = 0
+    for chunk in (1, 99, 200, 300, 400):
+        o.step(chunk)
+        k += chunk
+        assert k * dt < w0 / -alpha
+        c = o.contacts()
+        w = o.particles().angVel[1]
+        assert abs(c.torque[0, 0]) == pytest.approx(abs(c.force[0, 0]) * rtp * 2 * r, rel=1e-12)
+        assert w[2] == pytest.approx(w0 + alpha * (k - 1) * dt, rel=1e-6)
+        assert math.hypot(w[0], w[1]) < 1e-3 * w0
