@@ -306,3 +306,31 @@ def test_twisting_resistance_spin_down():
         assert abs(c.torque[0, 0]) == pytest.approx(abs(c.force[0, 0]) * rtp * 2 * r, rel=1e-12)
         assert w[2] == pytest.approx(w0 + alpha * (k - 1) * dt, rel=1e-6)
         assert math.hypot(w[0], w[1]) < 1e-3 * w0
+
+
+@pytest.mark.parametrize("en", [0.8, 0.5])
+def test_hertz_restitution_independent_of_impact_velocity(en):
+    """Analytic property of the damped Hertz law (Law2_L6Geom_HertzPhys_DMT without adhesion,
+    src/dem/Hertz.cpp:85-210; damping coefficient alpha sqrt(m kn0) from en, Hertz.cpp:63-75): with an
+    elastic force kn0 d^(3/2) and a viscous force alpha sqrt(m kn0) d^(1/4) d', the equation of motion
+    scales with the impact velocity, so the coefficient of restitution of a binary collision does not
+    depend on it (the reference's alpha(en) relation makes it close to en, not equal: about 0.81 for
+    en = 0.8 here)."""
+    mats_py = [dict(kind=abi.MAT_HERTZ, density=1e3, young=1e8, ktDivKn=0.2, tanPhi=0.5, surfEnergy=0.0, alpha=0.0)]
+    es = []
+    for v0 in (1.0, 1e-1, 1e-2):
+        spec = two_spheres(0.05, 1e-5, v0, mats_py, "hertz", 0.1, en=en)
+        o = bridge.Oracle(spec.params, spec.particles)
+        started = False
+        for _ in range(2000):
+            o.step(10)
+            c = o.contacts()
+            real = bool(c.n and c.real[0])
+            started = started or real
+            if started and not real:
+                break
+        assert started and not real
+        v = o.particles().vel
+        es.append((v[1, 1] - v[0, 1]) / v0)
+    assert 0 < es[0] < 1
+    assert max(es) - min(es) < 1e-3 * es[0]
