@@ -334,3 +334,36 @@ def test_hertz_restitution_independent_of_impact_velocity(en):
         es.append((v[1, 1] - v[0, 1]) / v0)
     assert 0 < es[0] < 1
     assert max(es) - min(es) < 1e-3 * es[0]
+
+
+def test_hertz_viscous_energy_balance():
+    """Energy bookkeeping of the damped Hertz law: over a head-on collision the kinetic energy lost equals
+    the viscous dissipation booked as viscN (Fnv velN dt per step, src/dem/Hertz.cpp:181) up to that
+    rectangle rule's first-order error in dt, and the tracker's kinetic slot is 1/2 m v^2 of the state."""
+    mats_py = [dict(kind=abi.MAT_HERTZ, density=1e3, young=1e8, ktDivKn=0.2, tanPhi=0.5, surfEnergy=0.0, alpha=0.0)]
+
+    def balance(dt_safety):
+        spec = two_spheres(0.05, 1e-5, 1.0, mats_py, "hertz", dt_safety, en=0.5)
+        spec.params.trackEnergy = 1
+        m, v = spec.particles.mass, spec.particles.vel
+        ke0 = 0.5 * (m[:, None] * v * v).sum()
+        o = bridge.Oracle(spec.params, spec.particles)
+        started = False
+        for _ in range(4000):
+            o.step(10)
+            c = o.contacts()
+            real = bool(c.n and c.real[0])
+            started = started or real
+            if started and not real:
+                break
+        assert started and not real
+        v = o.particles().vel
+        ke1 = 0.5 * (m[:, None] * v * v).sum()
+        e = o.energy()
+        assert e["kinetic"] == pytest.approx(ke1, rel=1e-12)
+        assert e["elast"] == 0.0                      # separated: no stored elastic energy
+        return abs(e["viscN"] / (ke0 - ke1) - 1)
+
+    err1, err2 = balance(0.1), balance(0.05)
+    assert err1 < 5e-3
+    assert err2 < 0.6 * err1                          # first order in dt
