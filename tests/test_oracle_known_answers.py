@@ -155,35 +155,52 @@ def test_canonical_orientation_is_immaterial():
     assert np.allclose(a.particles().pos, b.particles().pos, rtol=0, atol=1e-9)
 
 
+class SettledOnWall:
+    """One FrictMat sphere (r = 1 cm) settled on a floor wall under gravity (4000 steps with Leapfrog
+    damping 0.5); `restart` continues from that state, particles and contact history, without damping and
+    with a new velocity and angular velocity of the sphere."""
+    g, r, n_settle = 9.81, 0.01, 4000
+
+    def __init__(self, mu, flags=0, **kw):
+        self.mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
+        self.mats = scenes.materials_array(self.mats_py)
+        self.kw = kw
+        pa = scenes.assemble(np.array([[0, 0, self.r]]), np.array([self.r]), 0, [(2, 1, 0.0, 0)], self.mats_py)
+        pa.flags[1] |= flags
+        self.dt = 0.3 * scenes.pwave_dt(np.array([self.r]), np.zeros(1, int), self.mats_py)
+        o = bridge.Oracle(scenes.default_params(self.mats, dt=self.dt, gravity=(0, 0, -self.g), damping=0.5, **kw), pa)
+        o.step(self.n_settle)
+        self.contacts = o.contacts()
+        d = o.particles()
+        for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
+            getattr(pa, name)[:] = getattr(d, name)
+        self.particles = pa
+        self.mass = pa.mass[1]
+        self.x0 = pa.pos[1, 0]
+
+    def restart(self, vel=(0.0, 0.0, 0.0), angVel=(0.0, 0.0, 0.0), **kw):
+        pa = self.particles.copy()
+        pa.vel[1] = vel
+        pa.angVel[1] = angVel
+        p = scenes.default_params(self.mats, dt=self.dt, gravity=(0, 0, -self.g), damping=0.0, step=self.n_settle,
+                                  **self.kw, **kw)
+        return bridge.Oracle(p, pa, contacts=self.contacts)
+
+
 def test_sliding_block_coulomb_limit():
     """Analytic: a sphere with its rotations blocked (DemData.blocked 'XYZ'), settled on a wall, slides
     like a block once given a horizontal velocity v0.  Law2_L6Geom_FrictPhys_IdealElPl caps the tangential
     force at tanPhi times the normal force (src/dem/IdealElPl.cpp:55-77), so while the block slides
     |Ft| = tanPhi |Fn| (to rounding), its velocity falls linearly, v = v0 - tanPhi g t, and it stops after
     sliding v0^2 / (2 tanPhi g)."""
-    g, r, mu, v0 = 9.81, 0.01, 0.4, 0.3
-    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
-    mats = scenes.materials_array(mats_py)
-    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
-    pa.flags[1] = abi.DOF_RX | abi.DOF_RY | abi.DOF_RZ
-    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
-    n_settle = 4000
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5), pa)
-    o.step(n_settle)
-    c = o.contacts()
-    m = pa.mass[1]
+    mu, v0 = 0.4, 0.3
+    w = SettledOnWall(mu, flags=abi.DOF_RX | abi.DOF_RY | abi.DOF_RZ)
+    g, dt = w.g, w.dt
+    c = w.contacts
     assert c.n == 1 and c.real[0] == 1
-    assert abs(c.force[0, 0]) == pytest.approx(m * g, rel=1e-9)       # settled: Fn = m g
-    # the settled state (dynamic fields and contact history) with the block pushed along x, no damping
-    d = o.particles()
-    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
-        getattr(pa, name)[:] = getattr(d, name)
-    pa.vel[1] = (v0, 0.0, 0.0)
-    x0 = pa.pos[1, 0]
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle), pa,
-                      contacts=c)
-    t_stop = v0 / (mu * g)
-    k_stop = int(t_stop / dt)
+    assert abs(c.force[0, 0]) == pytest.approx(w.mass * g, rel=1e-9)   # settled: Fn = m g
+    o = w.restart(vel=(v0, 0.0, 0.0))
+    k_stop = int(v0 / (mu * g) / dt)
     k = 0
     for chunk in (1, 99, 400, 500, 500):
         o.step(chunk)
@@ -199,7 +216,29 @@ def test_sliding_block_coulomb_limit():
     o.step(k_stop // 2 + k_stop - k)
     p = o.particles()
     assert abs(p.vel[1, 0]) < 0.01 * v0                                 # stopped (tangential spring only)
-    assert p.pos[1, 0] - x0 == pytest.approx(v0 * v0 / (2 * mu * g), rel=2e-3)
+    assert p.pos[1, 0] - w.x0 == pytest.approx(v0 * v0 / (2 * mu * g), rel=2e-3)
+
+
+def test_sliding_block_plastic_dissipation():
+    """Energy bookkeeping of IdealElPl's Coulomb slip (the plast entry, maxFt (|Ft trial| - maxFt) / kt per
+    step, src/dem/IdealElPl.cpp:57-74): while the block of the previous case slides, and after it stopped,
+    the kinetic energy lost equals the plastic dissipation plus the change of the stored elastic energy."""
+    mu, v0 = 0.4, 0.3
+    w = SettledOnWall(mu, flags=abi.DOF_RX | abi.DOF_RY | abi.DOF_RZ)
+    o = w.restart(vel=(v0, 0.0, 0.0), trackEnergy=1)
+
+    def state():
+        e = o.energy()
+        return 0.5 * w.mass * float((o.particles().vel[1] ** 2).sum()), e["plast"], e["elast"], e["grav"]
+
+    o.step(1)
+    ke0, pl0, el0, gr0 = state()
+    for steps in (499, 1000, 1500):
+        o.step(steps)
+        ke, pl, el, gr = state()
+        lost = ke0 - ke
+        assert lost > 0
+        assert (pl - pl0) + (el - el0) + (gr - gr0) == pytest.approx(lost, rel=1e-3)
 
 
 def test_dmt_adhesion_equilibrium():
@@ -238,25 +277,11 @@ def test_rolling_resistance_deceleration():
     force stays inside the Coulomb cone, so the sphere rolls without sliding and decelerates at
     a = -M / (r (m + I / r^2)) = -(10/7) rollTanPhi g for a solid sphere.  The tangential spring makes
     the rolling constraint elastic (velocity ripple of ~1e-3 v0); the displacement averages it out."""
-    g, r, mu, v0, rtp = 9.81, 0.01, 0.5, 0.3, 0.1
-    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
-    mats = scenes.materials_array(mats_py)
-    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
-    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
-    kw = dict(relRollStiff=1.0, rollTanPhi=rtp)
-    n_settle = 4000
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5, **kw), pa)
-    o.step(n_settle)
-    c = o.contacts()
-    d = o.particles()
-    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
-        getattr(pa, name)[:] = getattr(d, name)
-    pa.vel[1] = (v0, 0.0, 0.0)
-    pa.angVel[1] = (0.0, v0 / r, 0.0)
-    x0 = pa.pos[1, 0]
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle, **kw), pa,
-                      contacts=c)
-    a = -(10 / 7) * rtp * g
+    mu, v0, rtp = 0.5, 0.3, 0.1
+    w = SettledOnWall(mu, relRollStiff=1.0, rollTanPhi=rtp)
+    r, dt = w.r, w.dt
+    o = w.restart(vel=(v0, 0.0, 0.0), angVel=(0.0, v0 / r, 0.0))
+    a = -(10 / 7) * rtp * w.g
     k = 0
     for chunk in (1, 99, 400, 500, 500):
         o.step(chunk)
@@ -270,7 +295,7 @@ def test_rolling_resistance_deceleration():
         assert abs(p.vel[1, 0] - p.angVel[1, 1] * r) < 5e-3 * v0             # rolling, up to the spring
         assert abs(p.vel[1, 0] - (v0 + a * (k - 1) * dt)) < 5e-3 * v0
     T = k * dt
-    assert p.pos[1, 0] - x0 - v0 * T == pytest.approx(a * T * T / 2, rel=2e-3)
+    assert p.pos[1, 0] - w.x0 - v0 * T == pytest.approx(a * T * T / 2, rel=2e-3)
 
 
 def test_twisting_resistance_spin_down():
@@ -279,33 +304,21 @@ def test_twisting_resistance_spin_down():
     sits on its cap |Fn| rollTanPhi charLen (charLen = 2 r), the contact point does not slide (the spin
     axis is the normal), so the spin falls linearly, I dw/dt = -M, dw/dt = -5 rollTanPhi g / r for a solid
     sphere, until it stops."""
-    g, r, mu, w0, rtp = 9.81, 0.01, 0.5, 20.0, 0.1
-    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=1e7, ktDivKn=0.2, tanPhi=mu)]
-    mats = scenes.materials_array(mats_py)
-    pa = scenes.assemble(np.array([[0, 0, r]]), np.array([r]), 0, [(2, 1, 0.0, 0)], mats_py)
-    dt = 0.3 * scenes.pwave_dt(np.array([r]), np.zeros(1, int), mats_py)
-    kw = dict(relRollStiff=1.0, relTwistStiff=1.0, rollTanPhi=rtp)
-    n_settle = 4000
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.5, **kw), pa)
-    o.step(n_settle)
-    c = o.contacts()
-    d = o.particles()
-    for name in ("pos", "ori", "vel", "angVel", "force", "torque"):
-        getattr(pa, name)[:] = getattr(d, name)
-    pa.angVel[1] = (0.0, 0.0, w0)
-    o = bridge.Oracle(scenes.default_params(mats, dt=dt, gravity=(0, 0, -g), damping=0.0, step=n_settle, **kw), pa,
-                      contacts=c)
-    alpha = -5 * rtp * g / r
+    mu, w0, rtp = 0.5, 20.0, 0.1
+    w = SettledOnWall(mu, relRollStiff=1.0, relTwistStiff=1.0, rollTanPhi=rtp)
+    r, dt = w.r, w.dt
+    o = w.restart(angVel=(0.0, 0.0, w0))
+    alpha = -5 * rtp * w.g / r
     k = 0
     for chunk in (1, 99, 200, 300, 400):
         o.step(chunk)
         k += chunk
         assert k * dt < w0 / -alpha
         c = o.contacts()
-        w = o.particles().angVel[1]
+        wv = o.particles().angVel[1]
         assert abs(c.torque[0, 0]) == pytest.approx(abs(c.force[0, 0]) * rtp * 2 * r, rel=1e-12)
-        assert w[2] == pytest.approx(w0 + alpha * (k - 1) * dt, rel=1e-6)
-        assert math.hypot(w[0], w[1]) < 1e-3 * w0
+        assert wv[2] == pytest.approx(w0 + alpha * (k - 1) * dt, rel=1e-6)
+        assert math.hypot(wv[0], wv[1]) < 1e-3 * w0
 
 
 @pytest.mark.parametrize("en", [0.8, 0.5])
