@@ -221,7 +221,7 @@ def test_sliding_block_coulomb_limit():
 
 def test_sliding_block_plastic_dissipation():
     """Energy bookkeeping of IdealElPl's Coulomb slip (the plast entry, maxFt (|Ft trial| - maxFt) / kt per
-    step, src/dem/IdealElPl.cpp:57-74): while the block of the previous case slides, and after it stopped,
+    step, src/dem/IdealElPl.cpp:58-77): while the block of the previous case slides, and after it stopped,
     the kinetic energy lost equals the plastic dissipation plus the change of the stored elastic energy."""
     mu, v0 = 0.4, 0.3
     w = SettledOnWall(mu, flags=abi.DOF_RX | abi.DOF_RY | abi.DOF_RZ)
