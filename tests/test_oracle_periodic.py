@@ -161,3 +161,31 @@ def test_cross_boundary_pair():
     got = {(int(a), int(b)): tuple(int(v) for v in d) for a, b, d in zip(c.idA, c.idB, c.cellDist)}
     assert got == {(0, 1): (-1, 0, 0)} == _image_pairs(x, np.full(3, r), np.ones(3))
     assert c.real[0] == 1
+
+
+def test_stress_of_one_contact_across_the_boundary():
+    """ContactLoop's stress (src/dem/ContactLoop.cpp:217-227, 244): the sum over real contacts of the global
+    contact force times the branch vector (from A to B through the contact's period), over the cell
+    volume.  One FrictPhys pair of equal spheres meeting across the x boundary of a 1 x 1 x 1 cell, at
+    rest, with overlap d: kn = E A / (l0 + l1) with A = pi r^2 and l0 = l1 = r (Cp2_FrictMat_FrictPhys,
+    src/dem/FrictMat.cpp:39), the normal force kn uN along the normal from A to B, so
+    stress_xx = kn uN |branch| / V (negative: compression), every other component zero."""
+    r, E = 0.05, 1e7
+    mats_py = [dict(kind=abi.MAT_FRICT, density=1000.0, young=E, ktDivKn=0.2, tanPhi=0.5)]
+    mats = scenes.materials_array(mats_py)
+    pos = np.array([[0.05, 0.5, 0.5], [0.96, 0.5, 0.5]])   # B's image at x = -0.04: centre distance 0.09
+    pa = scenes.assemble(pos, np.array([r, r]), 0, [], mats_py)
+    p = scenes.default_params(mats, dt=1e-9, damping=0.0)
+    o = bridge.Oracle(p, pa, cell=dict(hSize=np.eye(3)))
+    o.step(1)
+    c = o.contacts()
+    assert c.n == 1 and c.real[0] == 1 and tuple(c.cellDist[0]) == (-1, 0, 0)
+    un = c.uN[0]
+    assert un == pytest.approx(-0.01, rel=1e-12)
+    kn = E * math.pi * r * r / (2 * r)
+    assert c.kn[0] == pytest.approx(kn, rel=1e-14)
+    s = o.stress()
+    assert s[0, 0] == pytest.approx(kn * un * 0.09, rel=1e-12)
+    off = s.copy()
+    off[0, 0] = 0.0
+    assert np.all(off == 0.0)
