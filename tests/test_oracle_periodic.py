@@ -164,7 +164,7 @@ def test_cross_boundary_pair():
 
 
 def test_stress_of_one_contact_across_the_boundary():
-X: the sum over real contacts of the global
+    """ContactLoop's stress (src/dem/ContactLoop.cpp:218-229, 244): the sum over real contacts of the global
     contact force times the branch vector (from A to B through the contact's period), over the cell
     volume.  One FrictPhys pair of equal spheres meeting across the x boundary of a 1 x 1 x 1 cell, at
     rest, with overlap d: kn = E A / (l0 + l1) with A = pi r^2 and l0 = l1 = r (Cp2_FrictMat_FrictPhys,
